@@ -1,0 +1,151 @@
+"""ctypes mirror of include/graniitti_gb300.h and the loader of the CUDA library.
+
+The library is built in-tree (graniitti_gb300/_build/libgrn.so) by
+graniitti_gb300.build.build_library(). Loading never falls back to anything:
+a missing or unloadable library raises.
+"""
+import ctypes
+import os
+
+_HERE = os.path.dirname(os.path.abspath(__file__))
+LIB_PATH = os.path.join(_HERE, "_build", "libgrn.so")
+
+c_double = ctypes.c_double
+c_int32 = ctypes.c_int32
+c_int64 = ctypes.c_int64
+c_uint32 = ctypes.c_uint32
+c_uint64 = ctypes.c_uint64
+c_void_p = ctypes.c_void_p
+
+# Status codes
+GRN_OK = 0
+GRN_ERR_INVALID = 1
+GRN_ERR_CUDA = 2
+GRN_ERR_UNSUPPORTED = 3
+GRN_ERR_NAN = 4
+GRN_ERR_STATE = 5
+GRN_ERR_NO_DEVICE = 6
+
+GRN_FLAG_KINEMATICS_OK = 1
+GRN_FLAG_FIDCUTS_OK = 2
+GRN_FLAG_VETOCUTS_OK = 4
+GRN_FLAG_AMPLITUDE_OK = 8
+
+GRN_PROC_REGGE_CON = 1
+GRN_PS_CONTINUUM = 1
+GRN_PREC_FP64 = 0
+GRN_PREC_MIXED = 1
+
+
+class SoftParams(ctypes.Structure):
+    _fields_ = [(n, c_double) for n in
+                ("delta_P", "alpha_P", "gN_P", "gN_O", "g3P", "gamma", "fc1", "fc2", "fc3")] + \
+               [("odderon_on", c_int32), ("_pad", c_int32)]
+
+
+class ReggeParams(ctypes.Structure):
+    _fields_ = [("a0", c_double * 3), ("ap", c_double * 3), ("sgn", c_double * 3),
+                ("s0", c_double), ("active", c_int32 * 3), ("offshellFF", c_int32),
+                ("c", c_double * 3), ("b_EXP", c_double), ("a_OREAR", c_double),
+                ("b_OREAR", c_double), ("b_POW", c_double)]
+
+
+class GenCuts(ctypes.Structure):
+    _fields_ = [(n, c_double) for n in
+                ("rap_min", "rap_max", "kt_min", "kt_max", "fpt_min", "fpt_max")]
+
+
+class FidCuts(ctypes.Structure):
+    _fields_ = [("active", c_int32), ("_pad", c_int32)] + [(n, c_double) for n in (
+        "eta_min", "eta_max", "rap_min", "rap_max", "pt_min", "pt_max", "Et_min", "Et_max",
+        "M_min", "M_max", "Y_min", "Y_max", "Pt_min", "Pt_max",
+        "ft_min", "ft_max", "fM_min", "fM_max")]
+
+
+class LoopNumerics(ctypes.Structure):
+    _fields_ = [("n_kt", c_int32), ("n_phi", c_int32), ("kt_min", c_double), ("kt_max", c_double),
+                ("n_bt", c_int32), ("n_kt2", c_int32)]
+
+
+class ProcessParams(ctypes.Structure):
+    _fields_ = [("process", c_int32), ("phase_space", c_int32), ("n_central", c_int32),
+                ("screening", c_int32), ("sqrt_s", c_double), ("m_beam", c_double),
+                ("m_central", c_double * 8), ("s_factor", c_double),
+                ("gcuts", GenCuts), ("fcuts", FidCuts), ("soft", SoftParams),
+                ("regge", ReggeParams), ("loop", LoopNumerics)]
+
+
+class VegasParams(ctypes.Structure):
+    _fields_ = [("bins", c_int32), ("iter", c_int32), ("ncall", c_int64), ("lambda_", c_double),
+                ("chi2max", c_double), ("precision", c_double), ("burnin_iter", c_int32),
+                ("prec", c_int32), ("seed", c_uint64)]
+
+
+class VegasResult(ctypes.Structure):
+    _fields_ = [(n, c_double) for n in (
+        "sigma", "sigma_err", "chi2", "I_this", "I2_this", "maxf", "maxW", "evaluations",
+        "amplitude_ok", "kinematics_ok", "fidcuts_ok", "vetocuts_ok")] + \
+               [("iterations", c_int64), ("nan_count", c_int64)]
+
+
+# Every exported entry point with its ctypes signature (restype, argtypes).
+SIGNATURES = {
+    "grn_default_params": (None, [c_void_p]),
+    "grn_create": (c_int32, [c_void_p, c_int32, c_void_p]),
+    "grn_destroy": (c_int32, [c_void_p]),
+    "grn_engine_stream": (c_void_p, [c_void_p]),
+    "grn_dim": (c_int32, [c_void_p]),
+    "grn_last_error": (ctypes.c_char_p, []),
+    "grn_version": (ctypes.c_char_p, []),
+    "grn_eikonal_build": (c_int32, [c_void_p, c_int32, c_int32]),
+    "grn_eikonal_xs": (c_int32, [c_void_p, c_void_p, c_void_p, c_void_p]),
+    "grn_eikonal_get": (c_int32, [c_void_p, c_void_p, c_void_p]),
+    "grn_eikonal_set": (c_int32, [c_void_p, c_int32, c_void_p, c_int32, c_void_p]),
+    "grn_event_weights": (c_int32, [c_void_p, c_void_p, c_int64, c_int32, c_void_p, c_void_p,
+                                    c_int32]),
+    "grn_event_kinematics": (c_int32, [c_void_p, c_void_p, c_int64, c_int32, c_void_p, c_void_p,
+                                       c_void_p]),
+    "grn_uniforms": (c_int32, [c_void_p, c_uint64, c_uint32, c_int64, c_int64, c_int32,
+                               c_void_p]),
+    "grn_vegas_init": (c_int32, [c_void_p, c_void_p]),
+    "grn_vegas_iteration": (c_int32, [c_void_p, c_int32, c_int32, c_uint32, c_void_p]),
+    "grn_vegas_integrate": (c_int32, [c_void_p, c_void_p, c_void_p]),
+    "grn_vegas_get_grid": (c_int32, [c_void_p, c_void_p]),
+    "grn_vegas_set_grid": (c_int32, [c_void_p, c_void_p]),
+    "grn_vegas_clear": (c_int32, [c_void_p]),
+    "grn_unweight": (c_int32, [c_void_p, c_double, c_uint64, c_void_p, c_void_p, c_void_p,
+                               c_int64]),
+    "grn_vegas_points": (c_int32, [c_void_p, c_void_p, c_int64, c_void_p]),
+}
+
+_lib = None
+
+
+def load_library(path=LIB_PATH):
+    """Load libgrn.so and attach the signatures. Raises when it is missing."""
+    global _lib
+    if _lib is not None:
+        return _lib
+    if not os.path.exists(path):
+        raise RuntimeError(
+            "graniitti_gb300: CUDA library %s is missing; build it with "
+            "graniitti_gb300.build.build_library()" % path)
+    lib = ctypes.CDLL(path)
+    for name, (res, args) in SIGNATURES.items():
+        fn = getattr(lib, name)
+        fn.restype = res
+        fn.argtypes = args
+    _lib = lib
+    return lib
+
+
+class GrnError(RuntimeError):
+    def __init__(self, status, msg):
+        super().__init__("grn status %d: %s" % (status, msg))
+        self.status = status
+
+
+def check(status):
+    if status != GRN_OK:
+        msg = _lib.grn_last_error().decode() if _lib is not None else "?"
+        raise GrnError(status, msg)

@@ -1,0 +1,204 @@
+"""Steering-card reader: the generator's JSON5 cards -> engine parameters.
+
+Mirrors what MGraniitti::ReadInput and MProcess::post_Constructor derive from a
+card (src/MGraniitti.cc:318-963, src/MContinuum.cc:64-89), for the process family
+the engine implements. The card layout (GENERALPARAM, PROCESSPARAM,
+INTEGRALPARAM, GENCUTS, FIDCUTS, VETOCUTS blocks) is the generator's own so that
+existing cards run unchanged.
+"""
+import json
+import math
+import re
+
+from . import _abi
+from .modeldata import PARTICLES, TUNES
+
+_PROC_RE = re.compile(r"^\s*([A-Za-z]+)\[([A-Z+]+)\]<([A-Z])>\s*$")
+
+
+def strip_json5(text):
+    """Remove // and /* */ comments and trailing commas (MAux.cc:309-340)."""
+    out = []
+    i, n = 0, len(text)
+    in_str = False
+    while i < n:
+        ch = text[i]
+        if in_str:
+            out.append(ch)
+            if ch == "\\" and i + 1 < n:
+                out.append(text[i + 1])
+                i += 2
+                continue
+            if ch == '"':
+                in_str = False
+            i += 1
+            continue
+        if ch == '"':
+            in_str = True
+            out.append(ch)
+            i += 1
+        elif text.startswith("//", i):
+            j = text.find("\n", i)
+            i = n if j < 0 else j
+        elif text.startswith("/*", i):
+            j = text.find("*/", i + 2)
+            i = n if j < 0 else j + 2
+        else:
+            out.append(ch)
+            i += 1
+    s = "".join(out)
+    return re.sub(r",(\s*[}\]])", r"\1", s)
+
+
+def read_card(path):
+    with open(path) as f:
+        return json.loads(strip_json5(f.read()))
+
+
+def parse_process(proc):
+    """'PP[CON]<C> -> pi+ pi-' -> (istate, channel, class, [final states], options)."""
+    opts = {}
+    if "@" in proc:
+        head, tail = proc.split("@", 1)
+        for tok in ("@" + tail).split("@")[1:]:
+            tok = tok.strip()
+            if ":" in tok:
+                k, v = tok.split(":", 1)
+                opts[k.strip()] = v.strip()
+        proc = head
+    if "->" not in proc:
+        raise ValueError("process string needs '->': %r" % proc)
+    left, right = proc.split("->", 1)
+    m = _PROC_RE.match(left)
+    if not m:
+        raise ValueError("cannot parse process %r" % left)
+    finals = right.split()
+    return m.group(1), m.group(2), m.group(3), finals, opts
+
+
+class UnsupportedProcess(ValueError):
+    pass
+
+
+def build_params(card, process=None, tune=None):
+    """Engine ProcessParams from a parsed card (dict) and an optional process override."""
+    P = _abi.ProcessParams()
+    gp = card["GENERALPARAM"]
+    pp = card["PROCESSPARAM"]
+    tune = tune or gp.get("MODELPARAM", "TUNE0")
+    if tune not in TUNES:
+        raise UnsupportedProcess("model tune %s is not bundled" % tune)
+    T = TUNES[tune]
+    proc = process or pp["PROCESS"]
+    istate, channel, cls, finals, _ = parse_process(proc)
+    if not (istate == "PP" and channel == "CON" and cls == "C" and len(finals) == 2):
+        raise UnsupportedProcess("engine implements PP[CON]<C> -> 2-body, got %r" % proc)
+    if int(pp.get("NSTARS", 0)) != 0:
+        raise UnsupportedProcess("forward excitation (NSTARS > 0) is not implemented")
+    if pp["BEAM"] != ["p+", "p+"]:
+        raise UnsupportedProcess("beams other than p+ p+ are not implemented")
+    E1, E2 = float(pp["ENERGY"][0]), float(pp["ENERGY"][1])
+    if E1 != E2:
+        raise UnsupportedProcess("asymmetric beams are not implemented")
+    mb = PARTICLES["p+"][1]
+    E1 = max(E1, 1.001 * mb)
+    # s = (pbeam1 + pbeam2)^2 with equal energies (MProcess.cc:309-324)
+    P.sqrt_s = 2.0 * E1
+    P.m_beam = mb
+    P.process = _abi.GRN_PROC_REGGE_CON
+    P.phase_space = _abi.GRN_PS_CONTINUUM
+    P.n_central = 2
+    P.screening = 1 if pp.get("POMLOOP", False) else 0
+    for k, name in enumerate(finals):
+        if name not in PARTICLES:
+            raise UnsupportedProcess("unknown final state %s" % name)
+        P.m_central[k] = PARTICLES[name][1]
+    # identical-particle factor (MProcess.cc:449-468)
+    P.s_factor = float(math.factorial(2) if finals[0] == finals[1] else 1)
+
+    # Generation cuts with post_Constructor defaults (MContinuum.cc:64-89,
+    # MProcess.cc:1369-1386).
+    g = card.get("GENCUTS", {}).get("<C>", {})
+    rap = g.get("Rap", [-9.0, 9.0])
+    P.gcuts.rap_min, P.gcuts.rap_max = rap
+    kt = g.get("Kt", [0.0, 10.0 / 2])
+    P.gcuts.kt_min, P.gcuts.kt_max = kt
+    pt = g.get("Pt", [0.0, 2.5])
+    P.gcuts.fpt_min, P.gcuts.fpt_max = pt
+
+    # Fiducial cuts (FIDCUT defaults, MKinematics.h:1579-1611).
+    f = card.get("FIDCUTS", {})
+    fc = P.fcuts
+    fc.active = 1 if f.get("active", False) else 0
+    defaults = dict(eta=(-30.0, 30.0), rap=(-30.0, 30.0), pt=(0.0, 1e6), Et=(0.0, 1e6),
+                    M=(0.0, 1e6), Y=(-30.0, 30.0), Pt=(0.0, 1e6), ft=(0.0, 1e6), fM=(0.0, 1e6))
+    part = f.get("PARTICLE", {})
+    sysb = f.get("SYSTEM", {})
+    fwd = f.get("FORWARD", {})
+    vals = dict(defaults)
+    if "Eta" in part: vals["eta"] = part["Eta"]
+    if "Rap" in part: vals["rap"] = part["Rap"]
+    if "Pt" in part: vals["pt"] = part["Pt"]
+    if "Et" in part: vals["Et"] = part["Et"]
+    if "M" in sysb: vals["M"] = sysb["M"]
+    if "Rap" in sysb: vals["Y"] = sysb["Rap"]
+    if "Pt" in sysb: vals["Pt"] = sysb["Pt"]
+    if "t" in fwd: vals["ft"] = fwd["t"]
+    if "M" in fwd: vals["fM"] = fwd["M"]
+    for key, (lo, hi) in vals.items():
+        setattr(fc, key + "_min", float(lo))
+        setattr(fc, key + "_max", float(hi))
+    if card.get("VETOCUTS", {}).get("active", False):
+        raise UnsupportedProcess("veto cuts are not implemented")
+
+    # Model parameters.
+    s = T["PARAM_SOFT"]
+    P.soft.delta_P = s["DELTA_P"]
+    P.soft.alpha_P = s["ALPHA_P"]
+    P.soft.gN_P = s["gN_P"]
+    P.soft.gN_O = s["gN_O"]
+    P.soft.g3P = s["g3P"] * s["gN_P"]  # stored in the reference's convention (MForm.cc:132)
+    P.soft.gamma = s["gamma"]
+    P.soft.fc1, P.soft.fc2, P.soft.fc3 = s["fc1"], s["fc2"], s["fc3"]
+    P.soft.odderon_on = 1 if s["ODDERON_ON"] else 0
+    r = T["PARAM_REGGE"]
+    for k in range(3):
+        P.regge.a0[k] = r["a0"][k]
+        P.regge.ap[k] = r["ap"][k]
+        P.regge.sgn[k] = r["sgn"][k]
+    P.regge.s0 = r["s0"]
+    P.regge.offshellFF = r["offshellFF"]
+    P.regge.b_EXP, P.regge.a_OREAR, P.regge.b_OREAR, P.regge.b_POW = (
+        r["b_EXP"], r["a_OREAR"], r["b_OREAR"], r["b_POW"])
+    cpl = T["COUPLINGS"][PARTICLES[finals[0]][3]]
+    for k in range(3):
+        P.regge.c[k] = cpl["c"][k]
+        P.regge.active[k] = 1 if cpl["n"][k] else 0
+
+    # Loop numerics: defaults 15 x 12 moved by 3*ND (MEikonal.h:40-57), tables
+    # 10000 intervals (modeldata/NUMERICS.json).
+    nd = int(card.get("INTEGRALPARAM", {}).get("POMLOOP", {}).get("ND", 0))
+    P.loop.n_kt = max(3, 3 * nd + 15)
+    P.loop.n_phi = max(3, 3 * nd + 12)
+    P.loop.kt_min = 1e-4
+    P.loop.kt_max = 1.75
+    P.loop.n_bt = 10000
+    P.loop.n_kt2 = 10000
+    return P
+
+
+def vegas_params(card, prec=_abi.GRN_PREC_FP64, seed=1):
+    v = card.get("INTEGRALPARAM", {}).get("VEGAS", {})
+    vp = _abi.VegasParams()
+    vp.bins = int(v.get("BINS", 128))
+    if vp.bins % 2:
+        raise ValueError("VEGAS::BINS must be even")
+    vp.iter = int(v.get("ITER", 15))
+    vp.ncall = int(v.get("NCALL", 20000))
+    vp.lambda_ = float(v.get("LAMBDA", 1.5))
+    vp.chi2max = float(v.get("CHI2MAX", 10.0))
+    vp.precision = float(v.get("PRECISION", 0.01))
+    vp.burnin_iter = 3
+    vp.prec = prec
+    vp.seed = seed
+    return vp

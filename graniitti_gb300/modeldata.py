@@ -1,0 +1,40 @@
+"""Model and particle data the engine needs, bundled with the package.
+
+Values are those of the generator's TUNE0 parameter set
+(modeldata/TUNE0/GENERAL.json: PARAM_SOFT 9-29, PARAM_REGGE 90-129, PARAM_PI 146-149)
+and of its PDG 2018 mass/width table (modeldata/mass_width_2018.mcd). Only the
+entries the engine's processes use are carried; the layout is this package's own.
+"""
+
+TUNES = {
+    "TUNE0": {
+        "PARAM_SOFT": {
+            "DELTA_P": 0.098, "ALPHA_P": 0.065, "gN_P": 8.20, "gN_O": 0.10, "g3P": 0.15,
+            "gamma": 0.45, "fc1": 0.34, "fc2": 5.0, "fc3": 10.0, "ODDERON_ON": False,
+        },
+        "PARAM_REGGE": {
+            "a0": [1.088, 0.55, 0.55], "ap": [0.20, 0.93, 0.93], "sgn": [1, -1, 1], "s0": 1.0,
+            "offshellFF": 2, "b_EXP": 0.944, "a_OREAR": 0.638, "b_OREAR": 1.886, "b_POW": 0.500,
+        },
+        # Final-state Reggeon couplings c and on/off flags n, by coupling class.
+        "COUPLINGS": {
+            "PARAM_PI": {"c": [35.00184, 81.63672, 10.86264], "n": [True, False, False]},
+            "PARAM_K": {"c": [30.35376, 44.31084, 23.38164], "n": [True, False, False]},
+            "PARAM_P": {"c": [27.0, 0.0, 0.0], "n": [True, False, False]},
+            "PARAM_RHO": {"c": [25.0, 0.0, 0.0], "n": [True, False, False]},
+            "PARAM_PHI": {"c": [18.0, 0.0, 0.0], "n": [True, False, False]},
+            "PARAM_X": {"c": [15.0, 0.0, 0.0], "n": [True, False, False]},
+        },
+    }
+}
+
+# name -> (pdg, mass GeV, width GeV, coupling class)
+PARTICLES = {
+    "p+": (2212, 9.38272081e-01, 0.0, "PARAM_P"),
+    "p-": (-2212, 9.38272081e-01, 0.0, "PARAM_P"),
+    "pi+": (211, 1.3957061e-01, 2.5284e-17, "PARAM_PI"),
+    "pi-": (-211, 1.3957061e-01, 2.5284e-17, "PARAM_PI"),
+    "pi0": (111, 1.349770e-01, 7.73e-09, "PARAM_PI"),
+    "K+": (321, 4.93677e-01, 5.317e-17, "PARAM_K"),
+    "K-": (-321, 4.93677e-01, 5.317e-17, "PARAM_K"),
+}

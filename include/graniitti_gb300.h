@@ -1,0 +1,262 @@
+/*
+ * graniitti_gb300.h — C ABI of the GB300 event-weight engine.
+ *
+ * The engine replaces one data-parallel path of the GRANIITTI generator:
+ *   unit-hypercube point u  ->  phase-space map  ->  |M|^2  ->  (eikonal kt-loop
+ *   screening)  ->  event weight  ->  VEGAS accumulate / refine  ->  unweighting.
+ * Every entry point below names the reference interface it stands in for
+ * (paths relative to the GRANIITTI source tree).
+ *
+ * Conventions
+ *   - Plain C types only; no exceptions cross this boundary. Every call returns a
+ *     grn_status; grn_last_error() gives a message for the calling thread.
+ *   - Array arguments may be host or device pointers unless stated otherwise;
+ *     host arrays are staged through engine-owned device buffers (the copies are
+ *     part of the call). Device arrays are used in place.
+ *   - All work is ordered on the engine's CUDA stream (grn_engine_stream).
+ *   - One engine per host thread. An engine is not re-entrant.
+ *   - Units: GeV, GeV^2, weights in barn (the reference's convention).
+ */
+#ifndef GRANIITTI_GB300_H
+#define GRANIITTI_GB300_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* ------------------------------------------------------------------------ */
+/* Status codes                                                               */
+/* ------------------------------------------------------------------------ */
+typedef int32_t grn_status;
+enum {
+  GRN_OK              = 0,
+  GRN_ERR_INVALID     = 1, /* bad argument or configuration                 */
+  GRN_ERR_CUDA        = 2, /* CUDA runtime error (message has the detail)    */
+  GRN_ERR_UNSUPPORTED = 3, /* process / option not implemented by the engine */
+  GRN_ERR_NAN         = 4, /* more than 50 NaN/Inf weights (MProcess.h:317) */
+  GRN_ERR_STATE       = 5, /* call order violated (e.g. tables not built)   */
+  GRN_ERR_NO_DEVICE   = 6  /* no CUDA device visible                         */
+};
+
+/* Per-point flag bits: the four AuxIntData booleans (MProcess.h:37-52). */
+enum {
+  GRN_FLAG_KINEMATICS_OK = 1,
+  GRN_FLAG_FIDCUTS_OK    = 2,
+  GRN_FLAG_VETOCUTS_OK   = 4,
+  GRN_FLAG_AMPLITUDE_OK  = 8
+};
+
+/* Process kinds: the PROC_k wrappers of MSubProc.h the engine implements. */
+enum {
+  GRN_PROC_REGGE_CON = 1 /* "PP[CON]<C> -> a b", 2-body, MRegge::ME4 (MSubProc.h:361-380) */
+};
+
+/* Phase-space classes (MProcess subclasses). */
+enum {
+  GRN_PS_CONTINUUM = 1 /* <C>: MContinuum (src/MContinuum.cc) */
+};
+
+/* Arithmetic of the kt-loop (the tree-level kinematics is always FP64). */
+enum {
+  GRN_PREC_FP64  = 0, /* everything FP64: parity path against the reference */
+  GRN_PREC_MIXED = 1  /* FP64 kinematics, FP32 loop amplitudes with compensated sums */
+};
+
+/* ------------------------------------------------------------------------ */
+/* Configuration: what MGraniitti::ReadInput + MProcess::post_Constructor     */
+/* derive from a steering card (src/MGraniitti.cc:318-963).                   */
+/* ------------------------------------------------------------------------ */
+typedef struct grn_soft_params { /* PARAM_SOFT, src/MForm.cc:71-151 */
+  double delta_P, alpha_P, gN_P, gN_O, g3P, gamma, fc1, fc2, fc3;
+  int32_t odderon_on;
+  int32_t _pad;
+} grn_soft_params;
+
+typedef struct grn_regge_params { /* PARAM_REGGE, src/MRegge.cc:950-1039 */
+  double  a0[3], ap[3], sgn[3];
+  double  s0;
+  int32_t active[3]; /* trajectory on/off ("n") for the final state */
+  int32_t offshellFF; /* 0 exponential, 1 Orear, 2 power law */
+  double  c[3];       /* final-state couplings ("c") */
+  double  b_EXP, a_OREAR, b_OREAR, b_POW;
+} grn_regge_params;
+
+typedef struct grn_gencuts { /* GENCUT, include/Graniitti/MKinematics.h:1554-1576 */
+  double rap_min, rap_max;       /* <C> final-state rapidity window */
+  double kt_min, kt_max;         /* <C> intermediate kt (post_Constructor default 10/Kf) */
+  double fpt_min, fpt_max;       /* forward-leg pT (SetTechnicalBoundaries default 0, 2.5) */
+} grn_gencuts;
+
+typedef struct grn_fidcuts { /* FIDCUT, include/Graniitti/MKinematics.h:1579-1611 */
+  int32_t active;
+  int32_t _pad;
+  double  eta_min, eta_max, rap_min, rap_max, pt_min, pt_max, Et_min, Et_max;
+  double  M_min, M_max, Y_min, Y_max, Pt_min, Pt_max;
+  double  ft_min, ft_max, fM_min, fM_max;
+} grn_fidcuts;
+
+typedef struct grn_loop_numerics { /* MEikonalNumerics, include/Graniitti/MEikonal.h:26-95 */
+  int32_t n_kt;      /* NumberLoopKT: kt intervals (multiple of 3) */
+  int32_t n_phi;     /* NumberLoopPHI: phi intervals (multiple of 3) */
+  double  kt_min;    /* MinLoopKT */
+  double  kt_max;    /* MaxLoopKT */
+  int32_t n_bt;      /* NumberBT: density-table intervals (even) */
+  int32_t n_kt2;     /* NumberKT2: screening-table intervals (even) */
+} grn_loop_numerics;
+
+typedef struct grn_process_params {
+  int32_t process;        /* GRN_PROC_* */
+  int32_t phase_space;    /* GRN_PS_* */
+  int32_t n_central;      /* first-level central final states (2 supported) */
+  int32_t screening;      /* POMLOOP */
+  double  sqrt_s;         /* from the beam energies (symmetric beams) */
+  double  m_beam;         /* beam (and elastic forward) mass */
+  double  m_central[8];   /* central final-state masses */
+  double  s_factor;       /* identical-particle symmetry factor (MProcess.cc:449) */
+  grn_gencuts       gcuts;
+  grn_fidcuts       fcuts;
+  grn_soft_params   soft;
+  grn_regge_params  regge;
+  grn_loop_numerics loop;
+} grn_process_params;
+
+/* Fill every field with the reference defaults for "PP[CON]<C> -> pi+ pi-" at
+ * sqrt(s) = 13 TeV, TUNE0 (modeldata/TUNE0/GENERAL.json), cuts as documented. */
+void grn_default_params(grn_process_params *p);
+
+/* ------------------------------------------------------------------------ */
+/* Engine lifetime                                                            */
+/* ------------------------------------------------------------------------ */
+typedef struct grn_engine grn_engine;
+
+/* Replaces process construction + MProcess::post_Constructor
+ * (src/MGraniitti.cc:245-276, src/MContinuum.cc:64-89). */
+grn_status grn_create(const grn_process_params *p, int32_t device, grn_engine **out);
+grn_status grn_destroy(grn_engine *e);
+/* CUDA stream (cudaStream_t) of the engine, as an opaque pointer. */
+void *grn_engine_stream(grn_engine *e);
+/* Phase-space dimension (MProcess::GetdLIPSDim, include/Graniitti/MProcess.h:160). */
+int32_t grn_dim(const grn_engine *e);
+/* Message of the last failing call on this thread (never NULL). */
+const char *grn_last_error(void);
+/* Library version string. */
+const char *grn_version(void);
+
+/* ------------------------------------------------------------------------ */
+/* Eikonal tables                                                             */
+/* ------------------------------------------------------------------------ */
+/* Builds the impact-parameter density table (MBT) and the kt^2 screening
+ * amplitude table (MSA) on the device and the eikonal cross sections.
+ * Replaces MEikonal::S3Constructor (src/MEikonal.cc:46-132) including
+ * S3Density (177-216), S3Screening (222-245) and S3CalcXS (254-376, single
+ * channel). n_bt / n_kt2 <= 0 take the values in the process parameters. */
+grn_status grn_eikonal_build(grn_engine *e, int32_t n_bt, int32_t n_kt2);
+/* sigma_tot, sigma_el, sigma_inel in barn (MEikonal::GetTotXS, MEikonal.cc:39-43). */
+grn_status grn_eikonal_xs(grn_engine *e, double *tot, double *el, double *inel);
+/* Copy tables out: rows of (x, Re, Im); mbt has n_bt+1 rows, msa n_kt2+1 rows
+ * (IArray1D::F, include/Graniitti/MEikonal.h:149). Host pointers. */
+grn_status grn_eikonal_get(grn_engine *e, double *mbt, double *msa);
+/* Inject precomputed tables (MGraniitti::Initialize(const MEikonal&),
+ * src/MGraniitti.cc:1045-1054; IArray1D::ReadArray, MEikonal.cc:436-482). */
+grn_status grn_eikonal_set(grn_engine *e, int32_t n_bt, const double *mbt, int32_t n_kt2,
+                           const double *msa);
+
+/* ------------------------------------------------------------------------ */
+/* Event weights: the per-point boundary                                      */
+/* ------------------------------------------------------------------------ */
+/* Batch form of MProcess::EventWeight(randvec, aux)
+ * (include/Graniitti/MProcess.h:84; src/MContinuum.cc:164-193).
+ *   u      : n points x dim, point-major (randvec of each point contiguous)
+ *   w_out  : n weights [barn], 0 when a cut or the kinematics fails
+ *   flags  : n bytes of GRN_FLAG_* (may be NULL)
+ *   prec   : GRN_PREC_FP64 or GRN_PREC_MIXED (loop arithmetic)
+ * The call is synchronous with respect to the host when any pointer is a host
+ * pointer; with device pointers it is stream-ordered. */
+grn_status grn_event_weights(grn_engine *e, const double *u, int64_t n, int32_t dim,
+                             double *w_out, uint8_t *flags, int32_t prec);
+
+/* Kinematics of the same points without the amplitude, for record building and
+ * tests: per point 16 doubles = (px,py,pz,E) of the two forward legs and the two
+ * central particles (LORENTZSCALAR::pfinal[1..4]), plus t1, t2 into ts (2 per
+ * point, may be NULL). Replaces BNRandomKin+BNBuildKin (MContinuum.cc:276-435). */
+grn_status grn_event_kinematics(grn_engine *e, const double *u, int64_t n, int32_t dim,
+                                double *p4_out, double *ts_out, uint8_t *flags);
+
+/* ------------------------------------------------------------------------ */
+/* Counter-based uniforms (Philox4x32-10, Salmon et al., SC'11)               */
+/* ------------------------------------------------------------------------ */
+/* out[i*dim + d] = uniform double in [0,1) of point (first + i), dimension d,
+ * key = seed, stream = stream id. The reference draws from std::ranlux48
+ * (include/Graniitti/MRandom.h:62); the engine's draws are counter-based so that
+ * any point can be regenerated. */
+grn_status grn_uniforms(grn_engine *e, uint64_t seed, uint32_t stream, int64_t first, int64_t n,
+                        int32_t dim, double *out);
+
+/* ------------------------------------------------------------------------ */
+/* VEGAS                                                                      */
+/* ------------------------------------------------------------------------ */
+typedef struct grn_vegas_params { /* VEGASPARAM, include/Graniitti/MVEGAS.h:18-32 */
+  int32_t bins;       /* BINS (even) */
+  int32_t iter;       /* ITER */
+  int64_t ncall;      /* NCALL per iteration */
+  double  lambda;     /* LAMBDA */
+  double  chi2max;    /* CHI2MAX */
+  double  precision;  /* PRECISION (relative) */
+  int32_t burnin_iter;/* BURN-IN iterations (SampleVegas default 3) */
+  int32_t prec;       /* GRN_PREC_* of the weights */
+  uint64_t seed;      /* Philox key */
+} grn_vegas_params;
+
+typedef struct grn_vegas_result {
+  double  sigma, sigma_err, chi2;  /* global estimates [barn] (MGraniitti.cc:1222-1251) */
+  double  I_this, I2_this;         /* this iteration's integral and error^2 */
+  double  maxf, maxW;              /* max VEGAS-weighted f and raw W (init > 0 only) */
+  double  evaluations;             /* Stats::evaluations */
+  double  amplitude_ok, kinematics_ok, fidcuts_ok, vetocuts_ok; /* pass counts */
+  int64_t iterations;              /* iterations run in this call */
+  int64_t nan_count;               /* NaN/Inf weights zeroed */
+} grn_vegas_result;
+
+/* VEGASData::Init (MVEGAS.h:38-56) with init = 0 (fresh uniform grid). */
+grn_status grn_vegas_init(grn_engine *e, const grn_vegas_params *vp);
+/* One VEGAS iteration: draw ncall points, map through the grid, weigh them and
+ * accumulate f, f^2 histograms and the global estimates; then, if refine != 0,
+ * VEGASData::OptimizeGrid (MVEGAS.h:107-142). mode: 0 = burn-in (init 0, maxf not
+ * tracked), 1 = integration (init 1). Replaces one pass of the iteration loop of
+ * MGraniitti::VEGAS + VEGASMultiThread (MGraniitti.cc:1146-1443).
+ * The weighted values f of the last iteration stay on the device for
+ * grn_unweight. */
+grn_status grn_vegas_iteration(grn_engine *e, int32_t mode, int32_t refine, uint32_t iter_id,
+                               grn_vegas_result *out);
+/* Full integration as MGraniitti::SampleVegas with GMODE = 0
+ * (src/MGraniitti.cc:1074-1126): burn-in iterations, then integration
+ * iterations until PRECISION and CHI2MAX are met (chi2 > 50 restarts with 10x
+ * calls). */
+grn_status grn_vegas_integrate(grn_engine *e, const grn_vegas_params *vp, grn_vegas_result *out);
+/* Grid access: xmat as bins x dim doubles, bin-major (VEGASData::xmat). Host. */
+grn_status grn_vegas_get_grid(grn_engine *e, double *xmat);
+grn_status grn_vegas_set_grid(grn_engine *e, const double *xmat);
+/* Clear the global (sumdata, sumchi2, sweight) estimates: VEGASData::ClearIntegral. */
+grn_status grn_vegas_clear(grn_engine *e);
+
+/* ------------------------------------------------------------------------ */
+/* Unweighting                                                                */
+/* ------------------------------------------------------------------------ */
+/* Hit-or-miss over the last iteration's points: accept point i when
+ * U_i < f_i / fmax, count f_i > fmax as overflow (rejected).
+ * Replaces the acceptance test of MGraniitti::SaveEvent (MGraniitti.cc:1651-1664).
+ * idx_out (capacity cap, host or device, may be NULL) receives the accepted
+ * point indices in increasing order. */
+grn_status grn_unweight(grn_engine *e, double fmax, uint64_t seed, int64_t *n_accepted,
+                        int64_t *n_overflow, int64_t *idx_out, int64_t cap);
+/* The u vectors of points of the last iteration (n x dim, host), for record
+ * building (MProcess::EventRecord on the host). */
+grn_status grn_vegas_points(grn_engine *e, const int64_t *idx, int64_t n, double *u_out);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* GRANIITTI_GB300_H */

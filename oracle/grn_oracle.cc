@@ -1,0 +1,734 @@
+// grn_oracle.cc — CPU ORACLE for the GB300 event-weight engine.
+//
+// TEST INFRASTRUCTURE ONLY. This file restates, in plain FP64 C++, the reference
+// generator's algorithm for the engine's hot path so that the tests and the
+// benchmark's CPU baseline have an independent checker. The product (the CUDA
+// library under graniitti_gb300/) never links, loads or calls it. Only tests/,
+// __graft_entry__.smoke() and bench.py's CPU legs use it.
+//
+// Parity pin: the restatement is checked against golden vectors produced by the
+// UNMODIFIED reference sources (oracle/refbuild + tests/golden/make_golden.py).
+//
+// The restatement follows the reference's own formulation (4-vectors, the
+// two-body longitudinal solution, Lorentz scalars from 4-vector sums); the GPU
+// kernels use a light-cone formulation of the same physics, so agreement between
+// the two is a check of both. File:line citations refer to the GRANIITTI tree.
+
+#include <algorithm>
+#include <cmath>
+#include <complex>
+#include <cstdint>
+#include <cstring>
+#include <thread>
+#include <vector>
+
+#include "graniitti_gb300.h"
+
+namespace orc {
+
+using cplx = std::complex<double>;
+
+constexpr double PI       = 3.14159265358979323846264338327950288;
+constexpr double ZERO_EPS = 1e-12;  // MProcess.h: ZERO_EPS used as log(0 + ZERO_EPS)
+// Unit conversions (include/Graniitti/MPDG.h:63-78).
+constexpr double HBAR     = 6.582119514E-25;
+constexpr double C_LIGHT  = 2.99792458E8;
+constexpr double GEV2M    = HBAR * C_LIGHT;
+constexpr double GEV2FM   = GEV2M * 1E15;
+constexpr double GEV2BARN = (GEV2M * GEV2M) / 1E-28;
+constexpr double MPI_SOFT = 0.13957018;  // PDG::mpi used by S3PomAlpha (MPDG.h:56)
+
+// Eikonal numerics constants (include/Graniitti/MEikonal.h:27-40).
+constexpr double MIN_KT2 = 1E-6, MAX_KT2 = 25.0;
+constexpr double MIN_BT = 1E-6;
+constexpr double MAX_BT = 10.0 / GEV2FM;
+constexpr double FB_MIN_KT = 1E-9, FB_MAX_KT = 30.0;
+constexpr int    FB_N = 10000;
+
+inline double sq(double x) { return x * x; }
+inline double msqrt(double x) { return std::sqrt(std::max(0.0, x)); }
+
+// ---------------------------------------------------------------------------
+// Minimal 4-vector (px, py, pz, E), metric (+,-,-,-).
+struct V4 {
+  double x = 0, y = 0, z = 0, e = 0;
+  V4() {}
+  V4(double x_, double y_, double z_, double e_) : x(x_), y(y_), z(z_), e(e_) {}
+  V4     operator+(const V4 &o) const { return V4(x + o.x, y + o.y, z + o.z, e + o.e); }
+  V4     operator-(const V4 &o) const { return V4(x - o.x, y - o.y, z - o.z, e - o.e); }
+  double m2() const { return e * e - (x * x + y * y + z * z); }
+  double m() const { const double v = m2(); return v > 0 ? std::sqrt(v) : -std::sqrt(-v); }
+  double pt2() const { return x * x + y * y; }
+  double pt() const { return msqrt(pt2()); }
+  double p3() const { return msqrt(x * x + y * y + z * z); }
+  double rap() const { return 0.5 * std::log((e + z) / (e - z)); }
+  double eta() const { const double p = p3(); return 0.5 * std::log((p + z) / (p - z)); }
+  double mt() const { return msqrt(m2() + pt2()); }
+};
+
+// ---------------------------------------------------------------------------
+// Bessel J0: rational approximation for |x| < 8 and the asymptotic modulus/phase
+// form for |x| >= 8, as published in Abramowitz & Stegun (1965) 9.4 and used by
+// the reference's BESSJ0 (libs/extmath.hpp:12-46). The coefficient tables are the
+// published ones; they must be identical for table parity.
+double bessel_j0(double x) {
+  if (x == 0.0) return 1.0;
+  const double ax = std::fabs(x);
+  if (ax < 8.0) {
+    const double y   = x * x;
+    const double num = 57568490574.0 +
+                       y * (-13362590354.0 + y * (651619640.7 + y * (-11214424.18 +
+                       y * (77392.33017 + y * (-184.9052456)))));
+    const double den = 57568490411.0 +
+                       y * (1029532985.0 + y * (9494680.718 + y * (59272.64853 +
+                       y * (267.8532712 + y * 1.0))));
+    return num / den;
+  }
+  const double z  = 8.0 / ax;
+  const double y  = z * z;
+  const double xx = ax - 0.785398164;
+  const double p  = 1.0 + y * (-0.1098628627E-2 + y * (0.2734510407E-4 +
+                    y * (-0.2073370639E-5 + y * 0.2093887211E-6)));
+  const double q  = -0.1562499995E-1 + y * (0.1430488765E-3 + y * (-0.6911147651E-5 +
+                    y * (0.7621095161E-6 + y * (-0.9349451520E-7))));
+  return std::sqrt(0.636619772 / ax) * (p * std::cos(xx) - z * q * std::sin(xx));
+}
+
+// Composite Simpson 1/3 rule over N+1 equidistant samples, N even
+// (include/Graniitti/MMath.h:378-394).
+template <typename T>
+T simpson13(const std::vector<T> &f, double h) {
+  const std::size_t N = f.size() - 1;
+  T even = 0.0, odd = 0.0;
+  for (std::size_t j = 1; j + 1 <= N / 2; ++j) even += f[2 * j];
+  for (std::size_t j = 1; j <= N / 2; ++j) odd += f[2 * j - 1];
+  return h * (f[0] + 2.0 * even + 4.0 * odd + f[N]) / 3.0;
+}
+
+// Simpson 3/8 weights 1,3,3,2,3,3,2,...,3,3,1 over N+1 points, N % 3 == 0
+// (include/Graniitti/MMath.h:502-516).
+std::vector<double> simpson38_weights(int N) {
+  std::vector<double> w(N + 1, 3.0);
+  w[0] = w[N] = 1.0;
+  for (int i = 3; i < N; i += 3) w[i] = 2.0;
+  return w;
+}
+
+// ---------------------------------------------------------------------------
+// Model functions.
+
+// Regge signature factor (src/MForm.cc:382-385).
+cplx regge_eta(double alpha, double sigma) {
+  const cplx i(0, 1);
+  return -(1.0 + sigma * std::exp(-i * PI * alpha)) / std::sin(PI * alpha);
+}
+// Linear-trajectory signature factor (src/MForm.cc:394-396).
+cplx regge_eta_linear(double t, double a0, double ap, double sigma) {
+  const cplx i(0, 1);
+  return regge_eta(a0, sigma) * std::exp(-i * PI / 2.0 * ap * t);
+}
+// Proton form factor, double pole (src/MForm.cc:433-435).
+double proton_ff(const grn_soft_params &sp, double t) {
+  return (1.0 / (1.0 - t / sp.fc1)) * (1.0 / (1.0 - t / sp.fc2));
+}
+// Pion-loop insert of the non-linear pomeron trajectory (src/MForm.cc:418-427).
+double pion_loop(const grn_soft_params &sp, double tau, double t) {
+  const double sqt = std::sqrt(1.0 + tau);
+  const double fpi = 1.0 / (1.0 - t / sp.fc3);
+  return (4.0 / tau) * fpi * fpi *
+         (2.0 * tau - std::pow(1.0 + tau, 1.5) * std::log((sqt + 1.0) / (sqt - 1.0)) +
+          std::log(1.0 / (MPI_SOFT * MPI_SOFT)));
+}
+// Non-linear pomeron trajectory (src/MForm.cc:402-413).
+double pomeron_alpha(const grn_soft_params &sp, double t) {
+  const double beta_pi = (2.0 / 3.0) * sp.gN_P;
+  const double pic     = (beta_pi * beta_pi * MPI_SOFT * MPI_SOFT) / (32.0 * PI * PI * PI);
+  const double h       = pic * pion_loop(sp, 4.0 * MPI_SOFT * MPI_SOFT / std::fabs(t), t);
+  return 1.0 + sp.delta_P + sp.alpha_P * t - h;
+}
+// Single pomeron elastic amplitude (src/MEikonal.cc:139-162), C-even only.
+cplx elastic_amp(const grn_soft_params &sp, double s, double t) {
+  const double F = proton_ff(sp, t);
+  const double a = pomeron_alpha(sp, t);
+  cplx A = sp.gN_P * sp.gN_P * F * F * regge_eta(a, 1.0) * std::pow(s, a);
+  if (sp.odderon_on) A += sp.gN_O * sp.gN_O * F * F * regge_eta(a, -1.0) * std::pow(s, a);
+  return A;
+}
+
+// Regge propagator sum (s/s0)^alpha(t) with signature factors (src/MRegge.cc:888-906).
+cplx regge_prop(const grn_regge_params &rp, double s, double t) {
+  cplx M(0, 0);
+  for (int k = 0; k < 3; ++k) {
+    if (!rp.active[k]) continue;
+    const double alpha = rp.a0[k] + rp.ap[k] * t;
+    M += regge_eta_linear(t, rp.a0[k], rp.ap[k], rp.sgn[k]) * std::pow(s / rp.s0, alpha);
+  }
+  return M;
+}
+// Off-shell meson form factor (src/MRegge.cc:1155-1174).
+double meson_ff(const grn_regge_params &rp, double that, double M2) {
+  const double tp = that - M2;
+  switch (rp.offshellFF) {
+    case 0: return std::exp(-rp.b_EXP * std::fabs(tp));
+    case 1: return std::exp(-rp.b_OREAR * msqrt(std::fabs(tp) + sq(rp.a_OREAR)) +
+                            rp.a_OREAR * rp.b_OREAR);
+    default: return 1.0 / (1.0 - tp / rp.b_POW);
+  }
+}
+
+// ---------------------------------------------------------------------------
+// Kinematics state of one event (the part of LORENTZSCALAR the path uses).
+struct Event {
+  V4     pb1, pb2;         // beams
+  V4     pf[5];            // pfinal[0..4]: central system, forward 1, forward 2, central a, b
+  V4     q;                // intermediate difference momentum (pkt_[0])
+  double t1 = 0, t2 = 0, that = 0, uhat = 0, m2 = 0, Y = 0, Pt = 0;
+  double ss[5][5] = {};
+};
+
+struct Setup {
+  grn_process_params p;
+  double             s = 0, sqrt_s = 0;
+  V4                 pb1, pb2;
+  const double      *msa = nullptr;  // (x, re, im) rows
+  int                n_kt2 = 0;
+};
+
+// Longitudinal momentum of leg 3 in p1 p2 -> p3 {p5} p4 (CM frame): the two
+// forward legs carry transverse masses a = m3^2+pt3^2, b = m4^2+pt4^2 and share the
+// energy-momentum (E_R, pz_R) = (sqrt(s) - E5, -pz5); the forward-going root of the
+// two-body problem. Same quantity as kinematics::SolvePz (MKinematics.h:220-229).
+double solve_pz(double m3, double m4, double pt3, double pt4, double pz5, double E5, double s) {
+  const double ER  = std::sqrt(s) - E5;
+  const double pzR = -pz5;
+  const double MR2 = ER * ER - pzR * pzR;
+  const double a   = m3 * m3 + pt3 * pt3;
+  const double b   = m4 * m4 + pt4 * pt4;
+  const double lam = sq(MR2 - a - b) - 4.0 * a * b;
+  return (pzR * (MR2 + a - b) + ER * std::sqrt(lam)) / (2.0 * MR2);
+}
+
+// Energy-momentum conservation check with 1e-6 tolerance (MMath.h:191-198).
+bool check_emc(const V4 &d) {
+  const double eps = 1e-6;
+  return !(std::fabs(d.x) > eps || std::fabs(d.y) > eps || std::fabs(d.z) > eps || d.e > eps);
+}
+
+// Lorentz scalars of a 2 -> 4 event (MProcess.cc:1499-1584, Nf = 4).
+bool lorentz_scalars(const Setup &S, Event &ev) {
+  for (int i = 0; i <= 4; ++i)
+    for (int j = i + 1; j <= 4; ++j) {
+      ev.ss[i][j] = (ev.pf[i] + ev.pf[j]).m2();
+      ev.ss[j][i] = ev.ss[i][j];
+      if (ev.ss[i][j] < 0) return false;
+    }
+  if (ev.ss[1][0] < 0 || ev.ss[2][0] < 0) return false;
+  const V4 q1 = S.pb1 - ev.pf[1];
+  const V4 q2 = S.pb2 - ev.pf[2];
+  ev.t1 = q1.m2();
+  ev.t2 = q2.m2();
+  if (ev.t1 > 0 || ev.t2 > 0) return false;
+  ev.that = (q1 - ev.pf[3]).m2();
+  ev.uhat = (q1 - ev.pf[4]).m2();
+  ev.m2   = ev.pf[0].m2();
+  ev.Y    = ev.pf[0].rap();
+  ev.Pt   = ev.pf[0].pt();
+  return true;
+}
+
+// Central particles from the 2x2 linear system (MContinuum.cc:438-550, Kf = 2):
+// 2 p_a = q - w, 2 p_b = -q - w with w = p1T + p2T, then (pz, E) from rapidity.
+void central_pair(const V4 &q, const V4 &p1, const V4 &p2, const double m[2], const double y[2],
+                  V4 out[2]) {
+  const double wx = p1.x + p2.x, wy = p1.y + p2.y;
+  const double px[2] = {0.5 * (q.x - wx), 0.5 * (-q.x - wx)};
+  const double py[2] = {0.5 * (q.y - wy), 0.5 * (-q.y - wy)};
+  for (int i = 0; i < 2; ++i) {
+    const double mt = msqrt(m[i] * m[i] + px[i] * px[i] + py[i] * py[i]);
+    out[i]          = V4(px[i], py[i], mt * std::sinh(y[i]), mt * std::cosh(y[i]));
+  }
+}
+
+// Forward legs from the central system (MContinuum.cc:372-384); false when the
+// event fails the crude energy check or the forward-direction check.
+bool forward_legs(const Setup &S, double pt1, double phi1x, double phi1y, double pt2,
+                  double phi2x, double phi2y, const V4 &sumP, V4 &p1, V4 &p2) {
+  (void)phi1x;
+  const double m1 = S.p.m_beam, m2 = S.p.m_beam;
+  const double p1z = solve_pz(m1, m2, pt1, pt2, sumP.z, sumP.e, S.s);
+  const double p2z = -(sumP.z + p1z);
+  if (p1z < 0 || p2z > 0) return false;
+  p1 = V4(phi1x, phi1y, p1z, msqrt(m1 * m1 + pt1 * pt1 + p1z * p1z));
+  p2 = V4(phi2x, phi2y, p2z, msqrt(m2 * m2 + pt2 * pt2 + p2z * p2z));
+  return true;
+}
+
+// BNRandomKin + BNBuildKin for Kf = 2 (MContinuum.cc:276-435).
+bool build_kinematics(const Setup &S, const double *u, Event &ev) {
+  const grn_gencuts &g = S.p.gcuts;
+  const double lo  = std::log(g.fpt_min + ZERO_EPS);
+  const double hi  = std::log(g.fpt_max);
+  const double pt1 = std::exp(lo + (hi - lo) * u[0]);
+  const double pt2 = std::exp(lo + (hi - lo) * u[1]);
+  const double phi1 = 2.0 * PI * u[2];
+  const double phi2 = 2.0 * PI * u[3];
+  const double kt   = g.kt_min + (g.kt_max - g.kt_min) * u[4];
+  const double phik = 2.0 * PI * u[5];
+  const double y[2] = {g.rap_min + (g.rap_max - g.rap_min) * u[6],
+                       g.rap_min + (g.rap_max - g.rap_min) * u[7]};
+
+  V4 p1(pt1 * std::cos(phi1), pt1 * std::sin(phi1), 0, 0);
+  V4 p2(pt2 * std::cos(phi2), pt2 * std::sin(phi2), 0, 0);
+  ev.q = V4(kt * std::cos(phik), kt * std::sin(phik), 0, 0);
+
+  V4 c[2];
+  central_pair(ev.q, p1, p2, S.p.m_central, y, c);
+  const V4 sumP = c[0] + c[1];
+  if (sumP.e > S.sqrt_s) return false;
+  if (!forward_legs(S, pt1, p1.x, p1.y, pt2, p2.x, p2.y, sumP, p1, p2)) return false;
+
+  ev.pf[0] = sumP;
+  ev.pf[1] = p1;
+  ev.pf[2] = p2;
+  ev.pf[3] = c[0];
+  ev.pf[4] = c[1];
+  if (sumP.m() < c[0].m() + c[1].m()) return false;
+  if (!check_emc((S.pb1 + S.pb2) - (p1 + p2 + sumP))) return false;
+  return lorentz_scalars(S, ev);
+}
+
+// LoopKinematics for Kf = 2 (MContinuum.cc:94-161): new forward transverse momenta,
+// central pair re-solved with the tree-level difference momentum, rapidities and
+// masses of the tree-level central particles.
+bool loop_kinematics(const Setup &S, const Event &born, double p1x, double p1y, double p2x,
+                     double p2y, Event &ev) {
+  const V4 p1T(p1x, p1y, 0, 0), p2T(p2x, p2y, 0, 0);
+  const double m[2] = {born.pf[3].m(), born.pf[4].m()};
+  const double y[2] = {born.pf[3].rap(), born.pf[4].rap()};
+  V4 c[2];
+  central_pair(born.q, p1T, p2T, m, y, c);
+  const V4 sumP = c[0] + c[1];
+  const double pt1 = p1T.pt(), pt2 = p2T.pt();
+  V4 p1, p2;
+  if (!forward_legs(S, pt1, p1x, p1y, pt2, p2x, p2y, sumP, p1, p2)) return false;
+  ev.q     = born.q;
+  ev.pf[0] = sumP;
+  ev.pf[1] = p1;
+  ev.pf[2] = p2;
+  ev.pf[3] = c[0];
+  ev.pf[4] = c[1];
+  if (!check_emc((S.pb1 + S.pb2) - (p1 + p2 + sumP))) return false;
+  return lorentz_scalars(S, ev);
+}
+
+// Regge continuum amplitude for a 2-body central state, sign +1
+// (MRegge::ME4, src/MRegge.cc:394-438; PomPomProtonVertex 637-644).
+cplx regge_me4(const Setup &S, const Event &ev) {
+  const grn_regge_params &rp = S.p.regge;
+  const double M2  = sq(S.p.m_central[0]);
+  const double FFA = S.p.soft.gN_P * proton_ff(S.p.soft, ev.t1);
+  const double FFB = S.p.soft.gN_P * proton_ff(S.p.soft, ev.t2);
+  const double g   = rp.c[0] / S.p.soft.gN_P;
+  const cplx At = regge_prop(rp, ev.ss[1][3], ev.t1) * FFA * meson_ff(rp, ev.that, M2) * g *
+                  (1.0 / (ev.that - M2)) * meson_ff(rp, ev.that, M2) * g *
+                  regge_prop(rp, ev.ss[2][4], ev.t2) * FFB;
+  const cplx Au = regge_prop(rp, ev.ss[1][4], ev.t1) * FFA * meson_ff(rp, ev.uhat, M2) * g *
+                  (1.0 / (ev.uhat - M2)) * meson_ff(rp, ev.uhat, M2) * g *
+                  regge_prop(rp, ev.ss[2][3], ev.t2) * FFB;
+  return At + Au;
+}
+
+// Linear interpolation on the kt^2 screening table (IArray1D::Interpolate1D,
+// src/MEikonal.cc:489-512).
+cplx msa_interp(const Setup &S, double a) {
+  const int    N    = S.n_kt2;
+  const double step = (MAX_KT2 - MIN_KT2) / N;
+  if (a < MIN_KT2) a = MIN_KT2;
+  int i = static_cast<int>(std::floor((a - MIN_KT2) / step));
+  if (i < 0) i = 0;
+  if (i >= N) i = N - 1;
+  const double *r0 = S.msa + 3 * i, *r1 = S.msa + 3 * (i + 1);
+  const cplx    y0(r0[1], r0[2]), y1(r1[1], r1[2]);
+  return y0 + (a - r0[0]) * ((y1 - y0) / (r1[0] - r0[0]));
+}
+
+// Eikonal kt-loop screened |M|^2 (MProcess::S3ScreenedAmp2, src/MProcess.cc:157-288).
+double screened_amp2(const Setup &S, const Event &born, const cplx &A0) {
+  const grn_loop_numerics &L = S.p.loop;
+  const double stepKT  = (L.kt_max - L.kt_min) / L.n_kt;
+  const double stepPhi = 2.0 * PI / L.n_phi;
+  const std::vector<double> U = simpson38_weights(L.n_phi);
+  const std::vector<double> V = simpson38_weights(L.n_kt);
+  cplx sum(0, 0);
+  Event lev;
+  for (int i = 0; i <= L.n_phi; ++i) {
+    const double phi = i * stepPhi;
+    for (int j = 0; j <= L.n_kt; ++j) {
+      const double kt   = L.kt_min + j * stepKT;
+      const cplx   Aeik = msa_interp(S, kt * kt);
+      const double kx = kt * std::cos(phi), ky = kt * std::sin(phi);
+      if (!loop_kinematics(S, born, born.pf[1].x - kx, born.pf[1].y - ky, born.pf[2].x + kx,
+                           born.pf[2].y + ky, lev))
+        continue;
+      const cplx A = regge_me4(S, lev);
+      sum += (U[i] * V[j]) * (Aeik * A * kt);
+    }
+  }
+  const cplx norm = cplx(0, 1) / (8.0 * PI * PI * S.s);
+  const cplx Aloop = norm * sum * (9.0 * stepPhi * stepKT / 64.0);
+  return std::norm(A0 + Aloop);
+}
+
+// Phase-space weight and integration volume (MContinuum.cc:619-656; ForwardVolume
+// MProcess.cc:1390-1415), elastic forward legs, Kf = 2.
+double ps_factor(const Setup &S, const Event &ev) {
+  const grn_gencuts &g = S.p.gcuts;
+  const double J = 1.0 / std::fabs(ev.pf[1].z / ev.pf[1].e - ev.pf[2].z / ev.pf[2].e);
+  const int Nf = 4;
+  const double psw = (1.0 / std::pow(2.0, 2 * (Nf - 2))) * (1.0 / std::pow(2.0 * PI, 3 * Nf - 4)) *
+                     (ev.pf[1].pt() / (2.0 * ev.pf[1].e)) * (ev.pf[2].pt() / (2.0 * ev.pf[2].e)) *
+                     J * ev.q.pt();
+  const double fwd = sq(2.0 * PI) * ev.pf[1].pt() * ev.pf[2].pt() *
+                     sq(std::log(g.fpt_max) - std::log(g.fpt_min + ZERO_EPS));
+  const double vol = (g.kt_max - g.kt_min) * (2.0 * PI) * sq(g.rap_max - g.rap_min) * fwd;
+  return psw * vol;
+}
+
+// Fiducial cuts (MProcess::CommonCuts + FindDecayCuts, MProcess.cc:1085-1154).
+bool fiducial(const Setup &S, const Event &ev) {
+  const grn_fidcuts &f = S.p.fcuts;
+  if (!f.active) return true;
+  const double at1 = std::fabs(ev.t1), at2 = std::fabs(ev.t2);
+  if (!(at1 >= f.ft_min && at1 <= f.ft_max && at2 >= f.ft_min && at2 <= f.ft_max)) return false;
+  const double M = msqrt(ev.m2);
+  if (!(M >= f.M_min && M <= f.M_max && ev.Y >= f.Y_min && ev.Y <= f.Y_max && ev.Pt >= f.Pt_min &&
+        ev.Pt <= f.Pt_max))
+    return false;
+  bool ok = true;
+  for (int k = 3; k <= 4; ++k) {
+    const V4 &p = ev.pf[k];
+    const double pt = p.pt(), et = p.mt(), eta = p.eta(), rap = p.rap();
+    if (!(pt >= f.pt_min && pt <= f.pt_max && et >= f.Et_min && et <= f.Et_max &&
+          eta >= f.eta_min && eta <= f.eta_max && rap >= f.rap_min && rap <= f.rap_max))
+      ok = false;
+  }
+  return ok;
+}
+
+// One event weight (MContinuum::EventWeight, src/MContinuum.cc:164-193).
+double event_weight(const Setup &S, const double *u, uint8_t &flags, Event &ev) {
+  double W = 0.0;
+  const bool kin = build_kinematics(S, u, ev);
+  const bool fid = kin && fiducial(S, ev);
+  const bool veto = true;
+  if (kin && fid && veto) {
+    const cplx A0 = regge_me4(S, ev);
+    const double amp2 = S.p.screening ? screened_amp2(S, ev, A0) : std::norm(A0);
+    W = (1.0 / S.p.s_factor) * ps_factor(S, ev) * amp2 * GEV2BARN / (2.0 * S.s);
+  }
+  bool amp_ok = true;
+  if (std::isnan(W) || std::isinf(W)) {
+    W      = 0.0;
+    amp_ok = false;
+  }
+  flags = (kin ? GRN_FLAG_KINEMATICS_OK : 0) | (fid ? GRN_FLAG_FIDCUTS_OK : 0) |
+          (veto ? GRN_FLAG_VETOCUTS_OK : 0) | (amp_ok ? GRN_FLAG_AMPLITUDE_OK : 0);
+  return W;
+}
+
+Setup make_setup(const grn_process_params *p, const double *msa, int n_kt2) {
+  Setup S;
+  S.p      = *p;
+  S.sqrt_s = p->sqrt_s;
+  S.s      = p->sqrt_s * p->sqrt_s;
+  const double E  = p->sqrt_s / 2.0;
+  const double pz = msqrt(E * E - sq(p->m_beam));
+  S.pb1 = V4(0, 0, pz, E);
+  S.pb2 = V4(0, 0, -pz, E);
+  S.msa   = msa;
+  S.n_kt2 = n_kt2;
+  return S;
+}
+
+template <typename F>
+void parallel_for(int64_t n, int nthreads, F &&fn) {
+  if (nthreads <= 1 || n < 64) {
+    fn(0, n);
+    return;
+  }
+  std::vector<std::thread> th;
+  const int64_t chunk = (n + nthreads - 1) / nthreads;
+  for (int t = 0; t < nthreads; ++t) {
+    const int64_t a = t * chunk, b = std::min<int64_t>(n, a + chunk);
+    if (a >= b) break;
+    th.emplace_back([&fn, a, b] { fn(a, b); });
+  }
+  for (auto &t : th) t.join();
+}
+
+// ---------------------------------------------------------------------------
+// Eikonal tables.
+
+// Linear interpolation of the density table (IArray1D::Interpolate1D).
+cplx table_interp(const double *tab, int N, double xmin, double xmax, double a) {
+  const double step = (xmax - xmin) / N;
+  if (a < xmin) a = xmin;
+  int i = static_cast<int>(std::floor((a - xmin) / step));
+  if (i < 0) i = 0;
+  if (i >= N) i = N - 1;
+  const double *r0 = tab + 3 * i, *r1 = tab + 3 * (i + 1);
+  const cplx y0(r0[1], r0[2]), y1(r1[1], r1[2]);
+  return y0 + (a - r0[0]) * ((y1 - y0) / (r1[0] - r0[0]));
+}
+
+}  // namespace orc
+
+// ===========================================================================
+// C interface used by the tests (ctypes) and by the benchmark's CPU legs.
+extern "C" {
+
+// Weights for n points (u point-major, dim = 8). msa may be NULL when the
+// process has no screening. rec (may be NULL) receives per point
+// t1, t2, m2 and the 4-vectors pfinal[1..4] (19 doubles).
+int orc_weights(const grn_process_params *p, const double *u, int64_t n, int32_t dim, double *w,
+                uint8_t *flags, double *rec, const double *msa, int32_t n_kt2, int32_t nthreads) {
+  if (!p || !u || !w || dim != 8 || p->n_central != 2) return GRN_ERR_INVALID;
+  if (p->screening && (!msa || n_kt2 < 2)) return GRN_ERR_STATE;
+  const orc::Setup S = orc::make_setup(p, msa, n_kt2);
+  orc::parallel_for(n, nthreads, [&](int64_t a, int64_t b) {
+    orc::Event ev;
+    for (int64_t i = a; i < b; ++i) {
+      uint8_t f = 0;
+      ev        = orc::Event();
+      w[i]      = orc::event_weight(S, u + i * dim, f, ev);
+      if (flags) flags[i] = f;
+      if (rec) {
+        double *r = rec + i * 19;
+        r[0] = ev.t1;
+        r[1] = ev.t2;
+        r[2] = ev.m2;
+        for (int k = 0; k < 4; ++k) {
+          const orc::V4 &v = ev.pf[k + 1];
+          r[3 + 4 * k + 0] = v.x;
+          r[3 + 4 * k + 1] = v.y;
+          r[3 + 4 * k + 2] = v.z;
+          r[3 + 4 * k + 3] = v.e;
+        }
+      }
+    }
+  });
+  return GRN_OK;
+}
+
+// Eikonal tables and cross sections (MEikonal::S3Constructor, S3Density,
+// S3Screening, S3CalcXS; src/MEikonal.cc:46-376). mbt: (n_bt+1) x 3,
+// msa: (n_kt2+1) x 3 rows of (x, Re, Im); xs: sigma_tot, sigma_el, sigma_inel [barn].
+int orc_eikonal(const grn_process_params *p, int32_t n_bt, int32_t n_kt2, double *mbt, double *msa,
+                double *xs, int32_t nthreads) {
+  using namespace orc;
+  if (!p || n_bt < 2 || n_kt2 < 2 || !mbt) return GRN_ERR_INVALID;
+  const double s = p->sqrt_s * p->sqrt_s;
+
+  // Density: (1 / 2 pi s) * int dkt A(s, -kt^2) J0(b kt) kt.
+  std::vector<cplx> amp(FB_N + 1);
+  const double kstep = (FB_MAX_KT - FB_MIN_KT) / FB_N;
+  for (int k = 0; k <= FB_N; ++k) {
+    const double kt = FB_MIN_KT + k * kstep;
+    amp[k]          = elastic_amp(p->soft, s, -kt * kt) * kt;
+  }
+  const double bstep = (MAX_BT - MIN_BT) / n_bt;
+  parallel_for(n_bt + 1, nthreads, [&](int64_t a, int64_t b) {
+    std::vector<cplx> f(FB_N + 1);
+    for (int64_t i = a; i < b; ++i) {
+      const double bt = MIN_BT + i * bstep;
+      for (int k = 0; k <= FB_N; ++k) f[k] = amp[k] * bessel_j0(bt * (FB_MIN_KT + k * kstep));
+      const cplx v = simpson13(f, kstep) * (1.0 / (2.0 * PI * s));
+      mbt[3 * i + 0] = bt;
+      mbt[3 * i + 1] = v.real();
+      mbt[3 * i + 2] = v.imag();
+    }
+  });
+
+  // Cross sections, single channel (S3CalcXS).
+  if (xs) {
+    const int    N    = 6000;
+    const double step = (MAX_BT - MIN_BT) / N;
+    std::vector<double> ft(N + 1), fe(N + 1), fi(N + 1);
+    for (int i = 0; i <= N; ++i) {
+      const double bt = MIN_BT + i * step;
+      const cplx   Om = table_interp(mbt, n_bt, MIN_BT, MAX_BT, bt);
+      const cplx   Ael = cplx(0, 1) * (1.0 - std::exp(cplx(0, 1) * Om / 2.0));
+      ft[i] = 2.0 * Ael.imag() * bt;
+      fe[i] = std::norm(Ael) * bt;
+      fi[i] = (2.0 * Ael.imag() - std::norm(Ael)) * bt;
+    }
+    xs[0] = 2.0 * PI * simpson13(ft, step) * GEV2BARN;
+    xs[1] = 2.0 * PI * simpson13(fe, step) * GEV2BARN;
+    xs[2] = 2.0 * PI * simpson13(fi, step) * GEV2BARN;
+  }
+
+  // Screening amplitude: 2s * 2pi * int db i(1 - exp(i Omega/2)) J0(b kt) b.
+  if (msa) {
+    const double step = (MAX_BT - MIN_BT) / FB_N;
+    std::vector<cplx> g(FB_N + 1);
+    for (int k = 0; k <= FB_N; ++k) {
+      const double bt = MIN_BT + k * step;
+      const cplx   Om = table_interp(mbt, n_bt, MIN_BT, MAX_BT, bt);
+      g[k] = cplx(0, 1) * (1.0 - std::exp(cplx(0, 1) * Om / 2.0)) * bt;
+    }
+    const double kstep2 = (MAX_KT2 - MIN_KT2) / n_kt2;
+    parallel_for(n_kt2 + 1, nthreads, [&](int64_t a, int64_t b) {
+      std::vector<cplx> f(FB_N + 1);
+      for (int64_t i = a; i < b; ++i) {
+        const double kt2 = MIN_KT2 + i * kstep2;
+        const double kt  = msqrt(kt2);
+        for (int k = 0; k <= FB_N; ++k) f[k] = g[k] * bessel_j0((MIN_BT + k * step) * kt);
+        const cplx v = (2.0 * s) * (2.0 * PI) * simpson13(f, step);
+        msa[3 * i + 0] = kt2;
+        msa[3 * i + 1] = v.real();
+        msa[3 * i + 2] = v.imag();
+      }
+    });
+  }
+  return GRN_OK;
+}
+
+// Bessel J0 as used by the tables (for unit tests).
+double orc_bessel_j0(double x) { return orc::bessel_j0(x); }
+
+// ---------------------------------------------------------------------------
+// VEGAS (include/Graniitti/MVEGAS.h:87-142; MGraniitti.cc:1357-1375).
+
+// Rebin: redistribute the bin edges of dimension j so that each new bin holds an
+// equal share ac of the importance r (MVEGAS.h:87-104).
+static void vegas_rebin(int bins, int dim, int j, double ac, const double *r, double *xmat) {
+  std::vector<double> xnew(bins);
+  int    k  = 0;
+  double dr = 0.0, zn = 0.0, zo = 0.0;
+  for (int i = 0; i < bins - 1; ++i) {
+    while (ac > dr) dr += r[(++k) - 1];
+    if (k > 1) zo = xmat[(k - 2) * dim + j];
+    zn = xmat[(k - 1) * dim + j];
+    dr -= ac;
+    xnew[i] = zn - (zn - zo) * dr / r[k - 1];
+  }
+  for (int i = 0; i < bins - 1; ++i) xmat[i * dim + j] = xnew[i];
+  xmat[(bins - 1) * dim + j] = 1.0;
+}
+
+// Fresh uniform grid: xmat[0][j] = 1 then a rebin from one bin
+// (VEGASData::ClearAll + InitGridDependent, MVEGAS.h:72-84, 163-187).
+void orc_vegas_grid_init(int32_t bins, int32_t dim, double *xmat) {
+  std::vector<double> r(bins, 1.0);
+  for (int i = 0; i < bins * dim; ++i) xmat[i] = 0.0;
+  for (int j = 0; j < dim; ++j) xmat[j] = 1.0;
+  for (int j = 0; j < dim; ++j) vegas_rebin(bins, dim, j, 1.0 / bins, r.data(), xmat);
+}
+
+// Smooth the f^2 histogram and rebin (VEGASData::OptimizeGrid, MVEGAS.h:107-142).
+// f2mat is bins x dim and is modified in place as in the reference.
+void orc_vegas_refine(int32_t bins, int32_t dim, double lambda, double *xmat, double *f2mat) {
+  const double EPS = 1.0e-30;
+  std::vector<double> d(dim), r(bins);
+  for (int j = 0; j < dim; ++j) {
+    double zo = f2mat[0 * dim + j], zn = f2mat[1 * dim + j];
+    f2mat[0 * dim + j] = (zo + zn) / 2.0;
+    d[j]               = f2mat[0 * dim + j];
+    for (int i = 2; i < bins; ++i) {
+      const double ac          = zo + zn;
+      zo                       = zn;
+      zn                       = f2mat[i * dim + j];
+      f2mat[(i - 1) * dim + j] = (ac + zn) / 3.0;
+      d[j] += f2mat[(i - 1) * dim + j];
+    }
+    f2mat[(bins - 1) * dim + j] = (zo + zn) / 2.0;
+    d[j] += f2mat[(bins - 1) * dim + j];
+  }
+  for (int j = 0; j < dim; ++j) {
+    double ac = 0.0;
+    for (int i = 0; i < bins; ++i) {
+      double &v = f2mat[i * dim + j];
+      if (v < EPS) v = EPS;
+      r[i] = std::pow((1.0 - v / d[j]) / (std::log(d[j]) - std::log(v) + EPS), lambda);
+      if (std::isnan(r[i]) || std::isinf(r[i])) r[i] = EPS;
+      ac += r[i];
+    }
+    vegas_rebin(bins, dim, j, ac / bins, r.data(), xmat);
+  }
+}
+
+// Map uniforms r (n x dim) through the grid: x, VEGAS weight and 1-based bins
+// (MGraniitti.cc:1357-1375).
+void orc_vegas_map(int32_t bins, int32_t dim, const double *xmat, const double *r, int64_t n,
+                   double *x, double *vw, int32_t *bin) {
+  for (int64_t k = 0; k < n; ++k) {
+    double w = 1.0;
+    for (int j = 0; j < dim; ++j) {
+      const double zn = r[k * dim + j] * bins + 1.0;
+      int          ind = static_cast<int>(static_cast<unsigned>(zn));
+      ind = std::max(1, std::min(ind, bins));
+      double zo, ac;
+      if (ind > 1) {
+        zo = xmat[(ind - 1) * dim + j] - xmat[(ind - 2) * dim + j];
+        ac = xmat[(ind - 2) * dim + j] + (zn - ind) * zo;
+      } else {
+        zo = xmat[(ind - 1) * dim + j];
+        ac = (zn - ind) * zo;
+      }
+      x[k * dim + j] = ac;
+      w *= zo * bins;
+      if (bin) bin[k * dim + j] = ind;
+    }
+    vw[k] = w;
+  }
+}
+
+// ---------------------------------------------------------------------------
+// Philox4x32-10 (Salmon, Moraes, Dror, Shaw, SC'11), written from the paper.
+static inline void philox_round(uint32_t c[4], const uint32_t k[2]) {
+  const uint64_t p0 = static_cast<uint64_t>(0xD2511F53u) * c[0];
+  const uint64_t p1 = static_cast<uint64_t>(0xCD9E8D57u) * c[2];
+  const uint32_t hi0 = static_cast<uint32_t>(p0 >> 32), lo0 = static_cast<uint32_t>(p0);
+  const uint32_t hi1 = static_cast<uint32_t>(p1 >> 32), lo1 = static_cast<uint32_t>(p1);
+  const uint32_t n0 = hi1 ^ c[1] ^ k[0];
+  const uint32_t n2 = hi0 ^ c[3] ^ k[1];
+  c[0] = n0;
+  c[1] = lo1;
+  c[2] = n2;
+  c[3] = lo0;
+}
+
+void orc_philox4x32_10(const uint32_t ctr[4], const uint32_t key[2], uint32_t out[4]) {
+  uint32_t c[4] = {ctr[0], ctr[1], ctr[2], ctr[3]};
+  uint32_t k[2] = {key[0], key[1]};
+  for (int r = 0; r < 10; ++r) {
+    philox_round(c, k);
+    if (r < 9) {
+      k[0] += 0x9E3779B9u;
+      k[1] += 0xBB67AE85u;
+    }
+  }
+  for (int i = 0; i < 4; ++i) out[i] = c[i];
+}
+
+// Uniforms of points first..first+n-1: counter = (index lo, index hi, dimension
+// block, stream), key = seed; each block gives two doubles (53-bit, [0,1)).
+void orc_uniforms(uint64_t seed, uint32_t stream, int64_t first, int64_t n, int32_t dim,
+                  double *out) {
+  const uint32_t key[2] = {static_cast<uint32_t>(seed), static_cast<uint32_t>(seed >> 32)};
+  for (int64_t i = 0; i < n; ++i) {
+    const uint64_t idx = static_cast<uint64_t>(first + i);
+    for (int blk = 0; 2 * blk < dim; ++blk) {
+      const uint32_t ctr[4] = {static_cast<uint32_t>(idx), static_cast<uint32_t>(idx >> 32),
+                               static_cast<uint32_t>(blk), stream};
+      uint32_t o[4];
+      orc_philox4x32_10(ctr, key, o);
+      const uint64_t a = (static_cast<uint64_t>(o[1]) << 32) | o[0];
+      const uint64_t b = (static_cast<uint64_t>(o[3]) << 32) | o[2];
+      out[i * dim + 2 * blk] = static_cast<double>(a >> 11) * 0x1.0p-53;
+      if (2 * blk + 1 < dim) out[i * dim + 2 * blk + 1] = static_cast<double>(b >> 11) * 0x1.0p-53;
+    }
+  }
+}
+
+}  // extern "C"

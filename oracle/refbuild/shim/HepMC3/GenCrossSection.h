@@ -1,0 +1,1 @@
+#include "HepMC3/StandIn.h"

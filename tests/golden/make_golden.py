@@ -1,0 +1,125 @@
+"""Generate the golden fixtures under tests/golden/ from the UNMODIFIED reference.
+
+Runs here (x86 container with the reference sources); the fixtures travel, the
+reference does not. Steps:
+  1. build the reference driver: make -C oracle/refbuild (oracle/_ref/bin/grn_ref)
+  2. draw Philox4x32-10 points (tests/philox_np.py), feed them to the reference's
+     MProcess::EventWeight, store points + weights + flags + kinematics
+  3. build the eikonal tables with the reference's MEikonal::S3Constructor
+  4. run the reference VEGAS integration for the cross section
+
+Usage: python tests/golden/make_golden.py [--ref /root/reference]
+"""
+import argparse
+import json
+import os
+import subprocess
+import sys
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+REPO = os.path.abspath(os.path.join(HERE, "..", ".."))
+sys.path.insert(0, os.path.join(REPO, "tests"))
+import philox_np  # noqa: E402
+
+REF_BIN = os.path.join(REPO, "oracle", "_ref", "bin", "grn_ref")
+CARD = os.path.join(HERE, "cards", "pp_con_pipi.json")
+CARD_SCR = os.path.join(HERE, "cards", "pp_con_pipi_screened.json")
+PROC = "PP[CON]<C> -> pi+ pi-"
+TMP = os.path.join(REPO, "_work", "golden_tmp")
+
+
+def run_weights(card, u, extra=()):
+    os.makedirs(TMP, exist_ok=True)
+    uf = os.path.join(TMP, "u.bin")
+    wf = os.path.join(TMP, "w.bin")
+    u.astype(np.float64).tofile(uf)
+    cmd = [REF_BIN, "weights", card, PROC, uf, str(u.shape[1]), wf] + list(extra)
+    subprocess.run(cmd, check=True, capture_output=True)
+    r = np.fromfile(wf).reshape(-1, 24)
+    return dict(w=r[:, 0], kin=r[:, 1].astype(np.uint8), fid=r[:, 2].astype(np.uint8),
+                veto=r[:, 3].astype(np.uint8), amp=r[:, 4].astype(np.uint8), t1=r[:, 5],
+                t2=r[:, 6], m2=r[:, 7], p4=r[:, 8:24].reshape(-1, 4, 4))
+
+
+def save(name, **arrays):
+    np.savez_compressed(os.path.join(HERE, name), **arrays)
+    print("wrote", name)
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--ref", default="/root/reference")
+    a = ap.parse_args()
+    subprocess.check_call(["make", "-s", "-C", os.path.join(REPO, "oracle", "refbuild"), "-j8",
+                           "REF=" + a.ref])
+
+    # c1: tree-level weights, TUNE0 (power-law off-shell form factor) and the
+    # exponential form-factor variant.
+    u = philox_np.uniforms(1, 4096, 8)
+    r = run_weights(CARD, u)
+    save("c1_tune0_weights.npz", seed=1, u=u, **r)
+    u = philox_np.uniforms(2, 1024, 8)
+    r = run_weights(CARD, u, ["--offshellff", "0"])
+    save("c1_expff_weights.npz", seed=2, u=u, **r)
+    u = philox_np.uniforms(3, 512, 8)
+    r = run_weights(CARD, u, ["--offshellff", "1"])
+    save("c1_orearff_weights.npz", seed=3, u=u, **r)
+
+    # Edge points: hypercube corners and faces (u = 0 exactly and u -> 1).
+    edge = []
+    for v in (0.0, 1.0 - 2.0**-53, 0.5):
+        edge.append(np.full(8, v))
+    rng = np.random.default_rng(5)
+    for _ in range(61):
+        x = rng.random(8)
+        k = rng.integers(0, 8, size=2)
+        x[k[0]] = 0.0
+        x[k[1]] = 1.0 - 2.0**-53
+        edge.append(x)
+    u = np.array(edge)
+    r = run_weights(CARD, u)
+    save("c1_edge_weights.npz", u=u, **r)
+
+    # Eikonal tables: 1024 impact-parameter intervals, 10000 kt^2 intervals.
+    os.makedirs(TMP, exist_ok=True)
+    tf = os.path.join(TMP, "eik.bin")
+    subprocess.run([REF_BIN, "eikonal", CARD_SCR, PROC, tf, "--nbt", "1024", "--nkt2", "10000"],
+                   check=True, capture_output=True)
+    e = np.fromfile(tf)
+    xs = e[:3]
+    mbt = e[3:3 + 1025 * 3].reshape(-1, 3)
+    msa = e[3 + 1025 * 3:].reshape(-1, 3)
+    save("eikonal_nbt1024_nkt10000.npz", xs=xs, mbt=mbt, msa=msa)
+    # Default numerics (10000 x 10000): cross sections only.
+    subprocess.run([REF_BIN, "eikonal", CARD_SCR, PROC, tf], check=True, capture_output=True)
+    e = np.fromfile(tf)
+    save("eikonal_default_xs.npz", xs=e[:3], mbt_rows=np.array(10001), msa_rows=np.array(10001))
+
+    # c2: screened weights. Loop grid 63 kt x 33 phi intervals (64 x 34 points),
+    # kt <= 3 GeV; and the reference default grid (15 x 12, kt <= 1.75 GeV).
+    u = philox_np.uniforms(11, 96, 8)
+    r = run_weights(CARD_SCR, u, ["--nbt", "1024", "--nkt2", "10000", "--loopkt", "63",
+                                  "--loopphi", "33", "--maxloopkt", "3.0"])
+    save("c2_screened_63x33_weights.npz", seed=11, u=u, n_bt=1024, n_kt2=10000, loop_kt=63,
+         loop_phi=33, loop_ktmax=3.0, **r)
+    u = philox_np.uniforms(12, 96, 8)
+    r = run_weights(CARD_SCR, u, ["--nbt", "1024", "--nkt2", "10000"])
+    save("c2_screened_15x12_weights.npz", seed=12, u=u, n_bt=1024, n_kt2=10000, loop_kt=15,
+         loop_phi=12, loop_ktmax=1.75, **r)
+
+    # VEGAS integration of c1 (reference ranlux48 points, 8 threads).
+    out = subprocess.run([REF_BIN, "vegas", CARD, PROC, "--cores", "8"], check=True,
+                         capture_output=True, text=True).stdout
+    line = [l for l in out.splitlines() if l.startswith("RESULT")][-1]
+    sigma, err = map(float, line.split()[1:3])
+    with open(os.path.join(HERE, "c1_vegas_sigma.json"), "w") as f:
+        json.dump({"process": PROC, "card": "cards/pp_con_pipi.json", "sigma_barn": sigma,
+                   "sigma_err_barn": err, "ncall": 100000, "iter": 5, "precision": 0.001}, f,
+                  indent=1)
+    print("c1 VEGAS sigma", sigma, "+-", err)
+
+
+if __name__ == "__main__":
+    main()
