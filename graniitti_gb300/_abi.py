@@ -116,6 +116,8 @@ SIGNATURES = {
     "grn_unweight": (c_int32, [c_void_p, c_double, c_uint64, c_void_p, c_void_p, c_void_p,
                                c_int64]),
     "grn_vegas_points": (c_int32, [c_void_p, c_void_p, c_int64, c_void_p]),
+    "grn_kernel_timing": (c_int32, [c_void_p, c_int32, c_void_p, c_void_p]),
+    "grn_fp32_peak": (c_int32, [c_int32, c_void_p]),
 }
 
 _lib = None

@@ -1,0 +1,832 @@
+// grn_api.cu — C ABI of the engine (include/graniitti_gb300.h): engine state,
+// device buffers, parameter derivation, eikonal table management and the VEGAS
+// driver (the host part of MGraniitti::SampleVegas / VEGAS).
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <cmath>
+#include <complex>
+#include <cstdio>
+#include <cstring>
+#include <string>
+#include <vector>
+
+#include "grn_internal.cuh"
+
+using grn::KArgs;
+
+namespace {
+
+thread_local std::string g_last_error = "ok";
+
+grn_status fail(grn_status st, const std::string &msg) {
+  g_last_error = msg;
+  return st;
+}
+
+#define GRN_CUDA(call)                                                                    \
+  do {                                                                                    \
+    const cudaError_t e_ = (call);                                                        \
+    if (e_ != cudaSuccess)                                                                \
+      return fail(GRN_ERR_CUDA, std::string(#call) + ": " + cudaGetErrorString(e_));      \
+  } while (0)
+
+// Grow-only device buffer.
+struct DevBuf {
+  void  *p   = nullptr;
+  size_t cap = 0;
+  cudaError_t ensure(size_t bytes) {
+    if (bytes <= cap) return cudaSuccess;
+    if (p) cudaFree(p);
+    p   = nullptr;
+    cap = 0;
+    const cudaError_t e = cudaMalloc(&p, bytes);
+    if (e == cudaSuccess) cap = bytes;
+    return e;
+  }
+  void release() {
+    if (p) cudaFree(p);
+    p   = nullptr;
+    cap = 0;
+  }
+  template <typename T>
+  T *as() const {
+    return static_cast<T *>(p);
+  }
+};
+
+bool is_device_ptr(const void *ptr) {
+  if (!ptr) return false;
+  cudaPointerAttributes a;
+  if (cudaPointerGetAttributes(&a, ptr) != cudaSuccess) {
+    cudaGetLastError();
+    return false;
+  }
+  return a.type == cudaMemoryTypeDevice || a.type == cudaMemoryTypeManaged;
+}
+
+std::vector<double> simpson38_weights(int N) {
+  std::vector<double> w(N + 1, 3.0);
+  w[0] = w[N] = 1.0;
+  for (int i = 3; i < N; i += 3) w[i] = 2.0;
+  return w;
+}
+
+}  // namespace
+
+struct grn_engine {
+  int                device = 0;
+  cudaStream_t       stream = nullptr;
+  grn_process_params P{};
+  grn::Consts        K{};
+  int                dim = 8;
+
+  // eikonal
+  int                 n_bt = 0, n_kt2 = 0;
+  bool                eik_ready = false;
+  DevBuf              d_mbt, d_msa, d_eik_nodes, d_xs;
+  std::vector<double> h_mbt, h_msa;
+  double              xs[3] = {0, 0, 0};
+  DevBuf              d_lc_kt, d_lc_phi;
+  int                 n_kt_nodes = 0, n_phi_nodes = 0;
+  double              loop_norm_im = 0.0;
+
+  // staging for host arrays
+  DevBuf d_u, d_w, d_flags, d_aux;
+
+  // VEGAS
+  int         bins = 0;
+  double      lambda = 1.5;
+  int64_t     ncall = 0;
+  uint64_t    seed = 1;
+  int         nblocks = 0;
+  DevBuf      d_xmat, d_xmat_prev, d_f2mat, d_f, d_part_hist, d_part_sc, d_sc;
+  double     *h_sc = nullptr;  // pinned
+  double      sumdata = 0, sumchi2 = 0, sweight = 0;
+  double      maxf = 0, maxW = 0;
+  double      evaluations = 0, amp_ok = 0, kin_ok = 0, fid_ok = 0, veto_ok = 0;
+  int64_t     nan_total = 0;
+  uint32_t    next_stream = 1;
+  int         prec = GRN_PREC_FP64;
+  int64_t     iters_since_clear = 0;
+  uint32_t    last_stream = 0;
+  int64_t     last_ncall = 0;
+  bool        vegas_ready = false;
+  bool        have_last = false;
+  // unweighting
+  DevBuf      d_uw_counts, d_uw_misc, d_uw_idx;
+  // timing of the sampling kernel
+  cudaEvent_t ev0 = nullptr, ev1 = nullptr;
+  double      sample_ms = 0.0;
+  int64_t     sample_launches = 0;
+
+  KArgs args() const {
+    KArgs a{};
+    a.P            = P;
+    a.K            = K;
+    a.lc_kt        = d_lc_kt.as<double>();
+    a.lc_phi       = d_lc_phi.as<double>();
+    a.n_kt_nodes   = n_kt_nodes;
+    a.n_phi_nodes  = n_phi_nodes;
+    a.loop_norm_re = 0.0;
+    a.loop_norm_im = loop_norm_im;
+    return a;
+  }
+};
+
+namespace {
+
+grn_status derive_consts(const grn_process_params &P, grn::Consts &K) {
+  using namespace grn;
+  if (P.process != GRN_PROC_REGGE_CON || P.phase_space != GRN_PS_CONTINUUM)
+    return fail(GRN_ERR_UNSUPPORTED, "only PP[CON]<C> (Regge continuum, <C> class) is implemented");
+  if (P.n_central != 2) return fail(GRN_ERR_UNSUPPORTED, "only 2-body central states");
+  if (!(P.sqrt_s > 2 * P.m_beam)) return fail(GRN_ERR_INVALID, "sqrt_s below threshold");
+  if (!(P.gcuts.fpt_max > 0) || !(P.gcuts.kt_max > P.gcuts.kt_min) ||
+      !(P.gcuts.rap_max > P.gcuts.rap_min))
+    return fail(GRN_ERR_INVALID, "invalid generation cuts");
+  if (!(P.s_factor >= 1.0)) return fail(GRN_ERR_INVALID, "s_factor must be >= 1");
+  K.sqrt_s = P.sqrt_s;
+  K.s      = P.sqrt_s * P.sqrt_s;
+  const double E  = 0.5 * P.sqrt_s;
+  const double pz = std::sqrt(std::max(0.0, E * E - P.m_beam * P.m_beam));
+  K.L       = E + pz;
+  K.eps     = P.m_beam * P.m_beam / K.L;
+  K.mp2     = P.m_beam * P.m_beam;
+  K.m3      = P.m_central[0];
+  K.m4      = P.m_central[1];
+  K.m3sq    = K.m3 * K.m3;
+  K.m4sq    = K.m4 * K.m4;
+  K.lnpt_lo = std::log(P.gcuts.fpt_min + kZeroEps);
+  K.lnpt_hi = std::log(P.gcuts.fpt_max);
+  const int    Nf = 4;
+  const double fwd_log = K.lnpt_hi - K.lnpt_lo;
+  const double vol = (P.gcuts.kt_max - P.gcuts.kt_min) * (2.0 * kPi) *
+                     std::pow(P.gcuts.rap_max - P.gcuts.rap_min, 2) * std::pow(2.0 * kPi, 2) *
+                     fwd_log * fwd_log;
+  K.w_const = (1.0 / P.s_factor) * (1.0 / std::pow(2.0, 2 * (Nf - 2))) *
+              (1.0 / std::pow(2.0 * kPi, 3 * Nf - 4)) * vol * kGeV2barn / (2.0 * K.s);
+  K.M2prop = K.m3sq;
+  K.g2     = std::pow(P.regge.c[0] / P.soft.gN_P, 2);
+  K.gN2    = P.soft.gN_P * P.soft.gN_P;
+  K.lns0   = std::log(P.regge.s0);
+  K.n_active = 0;
+  for (int k = 0; k < 3; ++k) {
+    K.active[k] = P.regge.active[k] ? 1 : 0;
+    K.n_active += K.active[k];
+    // ReggeEta(alpha, sigma) = -(1 + sigma e^{-i pi alpha}) / sin(pi alpha) (MForm.cc:382)
+    const std::complex<double> e =
+        -(1.0 + P.regge.sgn[k] * std::exp(std::complex<double>(0, -kPi * P.regge.a0[k]))) /
+        std::sin(kPi * P.regge.a0[k]);
+    K.eta0_re[k] = e.real();
+    K.eta0_im[k] = e.imag();
+  }
+  if (K.n_active == 0) return fail(GRN_ERR_INVALID, "no active Regge trajectory");
+  if (P.regge.offshellFF < 0 || P.regge.offshellFF > 2)
+    return fail(GRN_ERR_INVALID, "offshellFF must be 0, 1 or 2");
+  return GRN_OK;
+}
+
+// Host linear interpolation of the screening table (IArray1D::Interpolate1D).
+std::complex<double> msa_interp(const std::vector<double> &msa, int N, double a) {
+  const double step = (grn::kMaxKT2 - grn::kMinKT2) / N;
+  if (a < grn::kMinKT2) a = grn::kMinKT2;
+  int i = static_cast<int>(std::floor((a - grn::kMinKT2) / step));
+  i     = std::max(0, std::min(i, N - 1));
+  const double *r0 = &msa[3 * i], *r1 = &msa[3 * (i + 1)];
+  const std::complex<double> y0(r0[1], r0[2]), y1(r1[1], r1[2]);
+  return y0 + (a - r0[0]) * ((y1 - y0) / (r1[0] - r0[0]));
+}
+
+// kt-loop node tables from the screening table and the loop numerics.
+grn_status build_loop_nodes(grn_engine *e) {
+  const grn_loop_numerics &L = e->P.loop;
+  if (L.n_kt < 3 || L.n_phi < 3 || L.n_kt % 3 || L.n_phi % 3)
+    return fail(GRN_ERR_INVALID, "loop interval counts must be multiples of 3 (Simpson 3/8)");
+  if (L.n_kt + 1 > grn::kMaxLoopNodes || L.n_phi + 1 > grn::kMaxLoopNodes)
+    return fail(GRN_ERR_INVALID, "too many loop nodes");
+  if (!(L.kt_max > L.kt_min) || !(L.kt_max * L.kt_max <= grn::kMaxKT2 * (1 + 1e-5)))
+    return fail(GRN_ERR_INVALID, "loop kt range outside the screening table");
+  const double stepKT  = (L.kt_max - L.kt_min) / L.n_kt;
+  const double stepPhi = 2.0 * grn::kPi / L.n_phi;
+  const std::vector<double> U = simpson38_weights(L.n_phi), V = simpson38_weights(L.n_kt);
+  std::vector<double> kt(3 * (L.n_kt + 1)), ph(3 * (L.n_phi + 1));
+  for (int j = 0; j <= L.n_kt; ++j) {
+    const double k = L.kt_min + j * stepKT;
+    const std::complex<double> c = V[j] * k * msa_interp(e->h_msa, e->n_kt2, k * k);
+    kt[3 * j]     = k;
+    kt[3 * j + 1] = c.real();
+    kt[3 * j + 2] = c.imag();
+  }
+  for (int i = 0; i <= L.n_phi; ++i) {
+    const double phi = i * stepPhi;
+    ph[3 * i]     = std::cos(phi);
+    ph[3 * i + 1] = std::sin(phi);
+    ph[3 * i + 2] = U[i];
+  }
+  GRN_CUDA(e->d_lc_kt.ensure(kt.size() * sizeof(double)));
+  GRN_CUDA(e->d_lc_phi.ensure(ph.size() * sizeof(double)));
+  GRN_CUDA(cudaMemcpyAsync(e->d_lc_kt.p, kt.data(), kt.size() * sizeof(double),
+                           cudaMemcpyHostToDevice, e->stream));
+  GRN_CUDA(cudaMemcpyAsync(e->d_lc_phi.p, ph.data(), ph.size() * sizeof(double),
+                           cudaMemcpyHostToDevice, e->stream));
+  GRN_CUDA(cudaStreamSynchronize(e->stream));
+  e->n_kt_nodes   = L.n_kt + 1;
+  e->n_phi_nodes  = L.n_phi + 1;
+  // i / (8 pi^2 s) * 9 h_phi h_kt / 64 (MProcess.cc:254-261, MMath.h:470)
+  e->loop_norm_im = (9.0 * stepPhi * stepKT / 64.0) / (8.0 * grn::kPi * grn::kPi * e->K.s);
+  return GRN_OK;
+}
+
+grn_status require_screening_ready(grn_engine *e) {
+  if (e->P.screening && !e->eik_ready)
+    return fail(GRN_ERR_STATE, "screening is on: build or set the eikonal tables first");
+  return GRN_OK;
+}
+
+}  // namespace
+
+extern "C" {
+
+void grn_default_params(grn_process_params *p) {
+  if (!p) return;
+  std::memset(p, 0, sizeof(*p));
+  p->process     = GRN_PROC_REGGE_CON;
+  p->phase_space = GRN_PS_CONTINUUM;
+  p->n_central   = 2;
+  p->screening   = 0;
+  p->sqrt_s      = 13000.0;
+  p->m_beam      = 9.38272081e-01;  // proton (modeldata/mass_width_2018.mcd)
+  p->m_central[0] = p->m_central[1] = 1.3957061e-01;  // pi+-
+  p->s_factor    = 1.0;
+  p->gcuts = {-0.9, 0.9, 0.0, 5.0, 0.0, 2.5};
+  p->fcuts.active = 1;
+  p->fcuts.eta_min = -0.9;  p->fcuts.eta_max = 0.9;
+  p->fcuts.rap_min = -10.0; p->fcuts.rap_max = 10.0;
+  p->fcuts.pt_min = 0.1;    p->fcuts.pt_max = 1e5;
+  p->fcuts.Et_min = 0.0;    p->fcuts.Et_max = 1e5;
+  p->fcuts.M_min = 0.0;     p->fcuts.M_max = 1e5;
+  p->fcuts.Y_min = -10.0;   p->fcuts.Y_max = 10.0;
+  p->fcuts.Pt_min = 0.0;    p->fcuts.Pt_max = 1e5;
+  p->fcuts.ft_min = 0.0;    p->fcuts.ft_max = 1e5;
+  p->fcuts.fM_min = 0.0;    p->fcuts.fM_max = 1e5;
+  // TUNE0 PARAM_SOFT (modeldata/TUNE0/GENERAL.json:9-29)
+  p->soft = {0.098, 0.065, 8.20, 0.10, 0.15 * 8.20, 0.45, 0.34, 5.0, 10.0, 0, 0};
+  // TUNE0 PARAM_REGGE + PARAM_PI (GENERAL.json:90-149)
+  grn_regge_params &r = p->regge;
+  const double a0[3] = {1.088, 0.55, 0.55}, ap[3] = {0.20, 0.93, 0.93}, sg[3] = {1, -1, 1};
+  const double c[3] = {35.00184, 81.63672, 10.86264};
+  for (int k = 0; k < 3; ++k) {
+    r.a0[k] = a0[k]; r.ap[k] = ap[k]; r.sgn[k] = sg[k]; r.c[k] = c[k];
+    r.active[k] = (k == 0);
+  }
+  r.s0 = 1.0;
+  r.offshellFF = 2;
+  r.b_EXP = 0.944; r.a_OREAR = 0.638; r.b_OREAR = 1.886; r.b_POW = 0.5;
+  // Loop numerics: 15 x 12 intervals, kt in [1e-4, 1.75]; tables 10000 intervals
+  p->loop = {15, 12, 1e-4, 1.75, 10000, 10000};
+}
+
+const char *grn_last_error(void) { return g_last_error.c_str(); }
+const char *grn_version(void) { return "graniitti_gb300 0.1 (sm_103a)"; }
+
+grn_status grn_create(const grn_process_params *p, int32_t device, grn_engine **out) {
+  if (!p || !out) return fail(GRN_ERR_INVALID, "null argument");
+  *out = nullptr;
+  int ndev = 0;
+  if (cudaGetDeviceCount(&ndev) != cudaSuccess || ndev == 0) {
+    cudaGetLastError();
+    return fail(GRN_ERR_NO_DEVICE, "no CUDA device visible");
+  }
+  if (device < 0 || device >= ndev) return fail(GRN_ERR_INVALID, "bad device index");
+  grn::Consts K{};
+  const grn_status st = derive_consts(*p, K);
+  if (st != GRN_OK) return st;
+  GRN_CUDA(cudaSetDevice(device));
+  grn_engine *e = new grn_engine();
+  e->device     = device;
+  e->P          = *p;
+  e->K          = K;
+  cudaError_t ce = cudaStreamCreateWithFlags(&e->stream, cudaStreamNonBlocking);
+  if (ce == cudaSuccess) ce = cudaMallocHost(&e->h_sc, grn::VS_COUNT * sizeof(double));
+  if (ce == cudaSuccess) ce = cudaEventCreate(&e->ev0);
+  if (ce == cudaSuccess) ce = cudaEventCreate(&e->ev1);
+  if (ce != cudaSuccess) {
+    grn_destroy(e);
+    return fail(GRN_ERR_CUDA, std::string("engine setup: ") + cudaGetErrorString(ce));
+  }
+  *out = e;
+  return GRN_OK;
+}
+
+grn_status grn_destroy(grn_engine *e) {
+  if (!e) return GRN_OK;
+  cudaSetDevice(e->device);
+  if (e->stream) cudaStreamSynchronize(e->stream);
+  DevBuf *bufs[] = {&e->d_mbt, &e->d_msa, &e->d_eik_nodes, &e->d_xs, &e->d_lc_kt, &e->d_lc_phi,
+                    &e->d_u, &e->d_w, &e->d_flags, &e->d_aux, &e->d_xmat, &e->d_xmat_prev,
+                    &e->d_f2mat, &e->d_f, &e->d_part_hist, &e->d_part_sc, &e->d_sc,
+                    &e->d_uw_counts, &e->d_uw_misc, &e->d_uw_idx};
+  for (DevBuf *b : bufs) b->release();
+  if (e->h_sc) cudaFreeHost(e->h_sc);
+  if (e->ev0) cudaEventDestroy(e->ev0);
+  if (e->ev1) cudaEventDestroy(e->ev1);
+  if (e->stream) cudaStreamDestroy(e->stream);
+  delete e;
+  return GRN_OK;
+}
+
+void   *grn_engine_stream(grn_engine *e) { return e ? static_cast<void *>(e->stream) : nullptr; }
+int32_t grn_dim(const grn_engine *e) { return e ? e->dim : 0; }
+
+// ---------------------------------------------------------------------------
+// Eikonal tables
+
+grn_status grn_eikonal_build(grn_engine *e, int32_t n_bt, int32_t n_kt2) {
+  if (!e) return fail(GRN_ERR_INVALID, "null engine");
+  if (n_bt <= 0) n_bt = e->P.loop.n_bt;
+  if (n_kt2 <= 0) n_kt2 = e->P.loop.n_kt2;
+  if (n_bt < 2 || n_kt2 < 2 || n_bt % 2 || n_kt2 % 2)
+    return fail(GRN_ERR_INVALID, "table interval counts must be even and >= 2");
+  GRN_CUDA(cudaSetDevice(e->device));
+  GRN_CUDA(e->d_mbt.ensure(3 * (n_bt + 1) * sizeof(double)));
+  GRN_CUDA(e->d_msa.ensure(3 * (n_kt2 + 1) * sizeof(double)));
+  GRN_CUDA(e->d_eik_nodes.ensure((grn::kFBN + 1) * sizeof(double2)));
+  GRN_CUDA(e->d_xs.ensure(3 * sizeof(double)));
+  GRN_CUDA(grn::launch_eikonal_density(e->P.soft, e->K.s, n_bt, e->d_eik_nodes.as<double2>(),
+                                       e->d_mbt.as<double>(), e->stream));
+  GRN_CUDA(grn::launch_eikonal_screening(e->K.s, n_bt, e->d_mbt.as<double>(), n_kt2,
+                                         e->d_eik_nodes.as<double2>(), e->d_msa.as<double>(),
+                                         e->d_xs.as<double>(), e->stream));
+  e->h_mbt.assign(3 * (n_bt + 1), 0.0);
+  e->h_msa.assign(3 * (n_kt2 + 1), 0.0);
+  GRN_CUDA(cudaMemcpyAsync(e->h_mbt.data(), e->d_mbt.p, e->h_mbt.size() * sizeof(double),
+                           cudaMemcpyDeviceToHost, e->stream));
+  GRN_CUDA(cudaMemcpyAsync(e->h_msa.data(), e->d_msa.p, e->h_msa.size() * sizeof(double),
+                           cudaMemcpyDeviceToHost, e->stream));
+  GRN_CUDA(cudaMemcpyAsync(e->xs, e->d_xs.p, 3 * sizeof(double), cudaMemcpyDeviceToHost,
+                           e->stream));
+  GRN_CUDA(cudaStreamSynchronize(e->stream));
+  e->n_bt  = n_bt;
+  e->n_kt2 = n_kt2;
+  const grn_status st = build_loop_nodes(e);
+  if (st != GRN_OK) return st;
+  e->eik_ready = true;
+  return GRN_OK;
+}
+
+grn_status grn_eikonal_xs(grn_engine *e, double *tot, double *el, double *inel) {
+  if (!e || !e->eik_ready) return fail(GRN_ERR_STATE, "eikonal tables not built");
+  if (tot) *tot = e->xs[0];
+  if (el) *el = e->xs[1];
+  if (inel) *inel = e->xs[2];
+  return GRN_OK;
+}
+
+grn_status grn_eikonal_get(grn_engine *e, double *mbt, double *msa) {
+  if (!e || !e->eik_ready) return fail(GRN_ERR_STATE, "eikonal tables not built");
+  if (mbt) std::memcpy(mbt, e->h_mbt.data(), e->h_mbt.size() * sizeof(double));
+  if (msa) std::memcpy(msa, e->h_msa.data(), e->h_msa.size() * sizeof(double));
+  return GRN_OK;
+}
+
+grn_status grn_eikonal_set(grn_engine *e, int32_t n_bt, const double *mbt, int32_t n_kt2,
+                           const double *msa) {
+  if (!e || !mbt || !msa || n_bt < 2 || n_kt2 < 2) return fail(GRN_ERR_INVALID, "bad tables");
+  GRN_CUDA(cudaSetDevice(e->device));
+  e->h_mbt.assign(mbt, mbt + 3 * (n_bt + 1));
+  e->h_msa.assign(msa, msa + 3 * (n_kt2 + 1));
+  GRN_CUDA(e->d_mbt.ensure(e->h_mbt.size() * sizeof(double)));
+  GRN_CUDA(e->d_msa.ensure(e->h_msa.size() * sizeof(double)));
+  GRN_CUDA(e->d_xs.ensure(3 * sizeof(double)));
+  GRN_CUDA(cudaMemcpyAsync(e->d_mbt.p, e->h_mbt.data(), e->h_mbt.size() * sizeof(double),
+                           cudaMemcpyHostToDevice, e->stream));
+  GRN_CUDA(cudaMemcpyAsync(e->d_msa.p, e->h_msa.data(), e->h_msa.size() * sizeof(double),
+                           cudaMemcpyHostToDevice, e->stream));
+  GRN_CUDA(e->d_eik_nodes.ensure((grn::kFBN + 1) * sizeof(double2)));
+  // cross sections from the injected density (S3CalcXS)
+  GRN_CUDA(grn::launch_eikonal_xs(e->d_mbt.as<double>(), n_bt, e->d_xs.as<double>(), e->stream));
+  GRN_CUDA(cudaMemcpyAsync(e->xs, e->d_xs.p, 3 * sizeof(double), cudaMemcpyDeviceToHost,
+                           e->stream));
+  GRN_CUDA(cudaStreamSynchronize(e->stream));
+  e->n_bt  = n_bt;
+  e->n_kt2 = n_kt2;
+  const grn_status st = build_loop_nodes(e);
+  if (st != GRN_OK) return st;
+  e->eik_ready = true;
+  return GRN_OK;
+}
+
+// ---------------------------------------------------------------------------
+// Event weights
+
+grn_status grn_event_weights(grn_engine *e, const double *u, int64_t n, int32_t dim,
+                             double *w_out, uint8_t *flags, int32_t prec) {
+  if (!e || !u || !w_out || n < 0) return fail(GRN_ERR_INVALID, "null argument");
+  if (dim != e->dim) return fail(GRN_ERR_INVALID, "dim must equal grn_dim() = 8");
+  if (prec != GRN_PREC_FP64 && prec != GRN_PREC_MIXED) return fail(GRN_ERR_INVALID, "bad prec");
+  grn_status st = require_screening_ready(e);
+  if (st != GRN_OK) return st;
+  if (n == 0) return GRN_OK;
+  GRN_CUDA(cudaSetDevice(e->device));
+  const bool dev_u = is_device_ptr(u), dev_w = is_device_ptr(w_out);
+  const bool dev_f = flags ? is_device_ptr(flags) : true;
+  const double *du = u;
+  double       *dw = w_out;
+  uint8_t      *df = flags;
+  if (!dev_u) {
+    GRN_CUDA(e->d_u.ensure(n * dim * sizeof(double)));
+    GRN_CUDA(cudaMemcpyAsync(e->d_u.p, u, n * dim * sizeof(double), cudaMemcpyHostToDevice,
+                             e->stream));
+    du = e->d_u.as<double>();
+  }
+  if (!dev_w) {
+    GRN_CUDA(e->d_w.ensure(n * sizeof(double)));
+    dw = e->d_w.as<double>();
+  }
+  if (flags && !dev_f) {
+    GRN_CUDA(e->d_flags.ensure(n));
+    df = e->d_flags.as<uint8_t>();
+  }
+  GRN_CUDA(grn::launch_event_weights(e->args(), prec, du, n, dim, dw, df, e->stream));
+  if (!dev_w)
+    GRN_CUDA(cudaMemcpyAsync(w_out, dw, n * sizeof(double), cudaMemcpyDeviceToHost, e->stream));
+  if (flags && !dev_f)
+    GRN_CUDA(cudaMemcpyAsync(flags, df, n, cudaMemcpyDeviceToHost, e->stream));
+  if (!dev_u || !dev_w || (flags && !dev_f)) GRN_CUDA(cudaStreamSynchronize(e->stream));
+  return GRN_OK;
+}
+
+grn_status grn_event_kinematics(grn_engine *e, const double *u, int64_t n, int32_t dim,
+                                double *p4_out, double *ts_out, uint8_t *flags) {
+  if (!e || !u || n < 0) return fail(GRN_ERR_INVALID, "null argument");
+  if (dim != e->dim) return fail(GRN_ERR_INVALID, "dim must equal grn_dim() = 8");
+  if (n == 0) return GRN_OK;
+  GRN_CUDA(cudaSetDevice(e->device));
+  // Host-staged path only (diagnostics / record building).
+  GRN_CUDA(e->d_u.ensure(n * dim * sizeof(double)));
+  GRN_CUDA(e->d_aux.ensure(n * 18 * sizeof(double)));
+  GRN_CUDA(e->d_flags.ensure(n));
+  double *dp4 = e->d_aux.as<double>(), *dts = dp4 + n * 16;
+  GRN_CUDA(cudaMemcpyAsync(e->d_u.p, u, n * dim * sizeof(double),
+                           is_device_ptr(u) ? cudaMemcpyDeviceToDevice : cudaMemcpyHostToDevice,
+                           e->stream));
+  GRN_CUDA(grn::launch_event_kinematics(e->args(), e->d_u.as<double>(), n, dim, dp4, dts,
+                                        e->d_flags.as<uint8_t>(), e->stream));
+  if (p4_out)
+    GRN_CUDA(cudaMemcpyAsync(p4_out, dp4, n * 16 * sizeof(double), cudaMemcpyDefault, e->stream));
+  if (ts_out)
+    GRN_CUDA(cudaMemcpyAsync(ts_out, dts, n * 2 * sizeof(double), cudaMemcpyDefault, e->stream));
+  if (flags) GRN_CUDA(cudaMemcpyAsync(flags, e->d_flags.p, n, cudaMemcpyDefault, e->stream));
+  GRN_CUDA(cudaStreamSynchronize(e->stream));
+  return GRN_OK;
+}
+
+grn_status grn_uniforms(grn_engine *e, uint64_t seed, uint32_t stream, int64_t first, int64_t n,
+                        int32_t dim, double *out) {
+  if (!e || !out || n < 0 || dim < 1 || dim > 16) return fail(GRN_ERR_INVALID, "bad argument");
+  if (n == 0) return GRN_OK;
+  GRN_CUDA(cudaSetDevice(e->device));
+  const bool dev = is_device_ptr(out);
+  double    *d   = out;
+  if (!dev) {
+    GRN_CUDA(e->d_aux.ensure(n * dim * sizeof(double)));
+    d = e->d_aux.as<double>();
+  }
+  GRN_CUDA(grn::launch_uniforms(seed, stream, first, n, dim, d, e->stream));
+  if (!dev) {
+    GRN_CUDA(cudaMemcpyAsync(out, d, n * dim * sizeof(double), cudaMemcpyDeviceToHost, e->stream));
+    GRN_CUDA(cudaStreamSynchronize(e->stream));
+  }
+  return GRN_OK;
+}
+
+// ---------------------------------------------------------------------------
+// VEGAS
+
+static grn_status vegas_alloc(grn_engine *e) {
+  const int nh = e->bins * e->dim;
+  GRN_CUDA(e->d_xmat.ensure(nh * sizeof(double)));
+  GRN_CUDA(e->d_xmat_prev.ensure(nh * sizeof(double)));
+  GRN_CUDA(e->d_f2mat.ensure(nh * sizeof(double)));
+  GRN_CUDA(e->d_sc.ensure(grn::VS_COUNT * sizeof(double)));
+  if (e->nblocks == 0) e->nblocks = grn::vegas_grid_blocks(e->device);
+  GRN_CUDA(e->d_part_hist.ensure(static_cast<size_t>(e->nblocks) * nh * sizeof(double)));
+  GRN_CUDA(e->d_part_sc.ensure(static_cast<size_t>(e->nblocks) * grn::VS_COUNT * sizeof(double)));
+  GRN_CUDA(e->d_f.ensure(static_cast<size_t>(std::max<int64_t>(e->ncall, 1)) * sizeof(double)));
+  return GRN_OK;
+}
+
+grn_status grn_vegas_init(grn_engine *e, const grn_vegas_params *vp) {
+  if (!e || !vp) return fail(GRN_ERR_INVALID, "null argument");
+  if (vp->bins < 2 || vp->bins % 2 || vp->bins > 256)
+    return fail(GRN_ERR_INVALID, "VEGAS::BINS must be even and in [2, 256]");
+  if (vp->ncall < 1) return fail(GRN_ERR_INVALID, "VEGAS::NCALL must be positive");
+  if (!(vp->lambda >= 1.0 && vp->lambda <= 10.0))
+    return fail(GRN_ERR_INVALID, "VEGAS::LAMBDA out of [1, 10]");
+  GRN_CUDA(cudaSetDevice(e->device));
+  e->bins   = vp->bins;
+  e->lambda = vp->lambda;
+  e->ncall  = vp->ncall;
+  e->seed   = vp->seed;
+  e->prec   = vp->prec;
+  grn_status st = vegas_alloc(e);
+  if (st != GRN_OK) return st;
+  GRN_CUDA(grn::launch_vegas_grid_init(e->d_xmat.as<double>(), e->bins, e->dim, e->stream));
+  GRN_CUDA(cudaStreamSynchronize(e->stream));
+  e->sumdata = e->sumchi2 = e->sweight = 0.0;
+  e->iters_since_clear = 0;
+  e->vegas_ready = true;
+  e->have_last   = false;
+  return GRN_OK;
+}
+
+grn_status grn_vegas_clear(grn_engine *e) {
+  if (!e) return fail(GRN_ERR_INVALID, "null engine");
+  e->sumdata = e->sumchi2 = e->sweight = 0.0;
+  e->iters_since_clear = 0;
+  return GRN_OK;
+}
+
+// One iteration with `prec` arithmetic; updates the global estimates as the
+// reference does after joining its threads (MGraniitti.cc:1222-1251).
+static grn_status vegas_iteration_impl(grn_engine *e, int prec, int mode, int refine,
+                                       uint32_t stream_id, int64_t iter_index,
+                                       grn_vegas_result *out) {
+  const int nh = e->bins * e->dim;
+  GRN_CUDA(cudaMemcpyAsync(e->d_xmat_prev.p, e->d_xmat.p, nh * sizeof(double),
+                           cudaMemcpyDeviceToDevice, e->stream));
+  GRN_CUDA(cudaEventRecord(e->ev0, e->stream));
+  GRN_CUDA(grn::launch_vegas_sample(e->args(), prec, e->d_xmat.as<double>(), e->bins, e->dim,
+                                    e->ncall, e->seed, stream_id, mode != 0, e->d_f.as<double>(),
+                                    e->d_part_hist.as<double>(), e->d_part_sc.as<double>(),
+                                    e->nblocks, e->stream));
+  GRN_CUDA(cudaEventRecord(e->ev1, e->stream));
+  GRN_CUDA(grn::launch_vegas_reduce(e->d_part_hist.as<double>(), e->d_part_sc.as<double>(),
+                                    e->nblocks, nh, e->d_f2mat.as<double>(), e->d_sc.as<double>(),
+                                    e->stream));
+  GRN_CUDA(cudaMemcpyAsync(e->h_sc, e->d_sc.p, grn::VS_COUNT * sizeof(double),
+                           cudaMemcpyDeviceToHost, e->stream));
+  if (refine)
+    GRN_CUDA(grn::launch_vegas_refine(e->d_xmat.as<double>(), e->d_f2mat.as<double>(), e->bins,
+                                      e->dim, e->lambda, e->stream));
+  GRN_CUDA(cudaStreamSynchronize(e->stream));
+  {
+    float ms = 0.f;
+    GRN_CUDA(cudaEventElapsedTime(&ms, e->ev0, e->ev1));
+    e->sample_ms += ms;
+    e->sample_launches += 1;
+  }
+  e->last_stream = stream_id;
+  e->last_ncall  = e->ncall;
+  e->have_last   = true;
+
+  const double *sc    = e->h_sc;
+  const double  calls = static_cast<double>(e->ncall);
+  double fsum  = sc[grn::VS_FSUM] / calls;
+  double f2sum = sc[grn::VS_F2SUM] * (1.0 / calls) * (1.0 / calls);
+  const double I_this = fsum;
+  f2sum = std::sqrt(f2sum * calls);
+  f2sum = (f2sum - fsum) * (f2sum + fsum);
+  if (f2sum <= 0.0) f2sum = 1.0e-30;
+  const double I2_this = f2sum / calls;
+  const double alpha   = 1.0 / I2_this;
+  e->sumdata += alpha * I_this;
+  e->sumchi2 += alpha * I_this * I_this;
+  e->sweight += alpha;
+  if (mode != 0) {
+    e->maxf = std::max(e->maxf, sc[grn::VS_MAXF]);
+    e->maxW = std::max(e->maxW, sc[grn::VS_MAXW]);
+  }
+  e->evaluations += sc[grn::VS_EVAL];
+  e->amp_ok += sc[grn::VS_AMP_OK];
+  e->kin_ok += sc[grn::VS_KIN_OK];
+  e->fid_ok += sc[grn::VS_FID_OK];
+  e->veto_ok += sc[grn::VS_VETO_OK];
+  e->nan_total += static_cast<int64_t>(sc[grn::VS_NAN]);
+  if (out) {
+    out->sigma       = e->sumdata / e->sweight;
+    out->sigma_err   = std::sqrt(1.0 / e->sweight);
+    double chi2      = (e->sumchi2 - e->sumdata * e->sumdata / e->sweight) / (iter_index + 1e-5);
+    out->chi2        = chi2 < 0 ? 0.0 : chi2;
+    out->I_this      = I_this;
+    out->I2_this     = I2_this;
+    out->maxf        = e->maxf;
+    out->maxW        = e->maxW;
+    out->evaluations = e->evaluations;
+    out->amplitude_ok  = e->amp_ok;
+    out->kinematics_ok = e->kin_ok;
+    out->fidcuts_ok    = e->fid_ok;
+    out->vetocuts_ok   = e->veto_ok;
+    out->iterations    = 1;
+    out->nan_count     = e->nan_total;
+  }
+  if (e->nan_total > 50)
+    return fail(GRN_ERR_NAN, "more than 50 NaN/Inf weights: check model parameters and cuts");
+  return GRN_OK;
+}
+
+grn_status grn_vegas_iteration(grn_engine *e, int32_t mode, int32_t refine, uint32_t iter_id,
+                               grn_vegas_result *out) {
+  if (!e || !e->vegas_ready) return fail(GRN_ERR_STATE, "grn_vegas_init first");
+  grn_status st = require_screening_ready(e);
+  if (st != GRN_OK) return st;
+  GRN_CUDA(cudaSetDevice(e->device));
+  grn_vegas_result r{};
+  st = vegas_iteration_impl(e, e->prec, mode, refine, iter_id, e->iters_since_clear++, &r);
+  if (out) *out = r;
+  return st;
+}
+
+// The reference's VEGAS(init, calls, itermin) (MGraniitti.cc:1146-1338); returns the
+// call multiplier (1 = done, 10 = chi2 restart) through *factor.
+static grn_status vegas_run(grn_engine *e, const grn_vegas_params *vp, int init, int64_t calls,
+                            int itermin, int *factor, grn_vegas_result *out) {
+  *factor = 1;
+  if (calls != e->ncall) {
+    e->ncall = calls;
+    GRN_CUDA(e->d_f.ensure(static_cast<size_t>(calls) * sizeof(double)));
+  }
+  if (init == 0) {
+    GRN_CUDA(grn::launch_vegas_grid_init(e->d_xmat.as<double>(), e->bins, e->dim, e->stream));
+    e->sumdata = e->sumchi2 = e->sweight = 0.0;
+  } else if (init == 1) {
+    e->sumdata = e->sumchi2 = e->sweight = 0.0;
+  }
+  for (int64_t iter = 0; iter < itermin; ++iter) {
+    grn_vegas_result r{};
+    grn_status st = vegas_iteration_impl(e, vp->prec, init, 1, e->next_stream++, iter, &r);
+    if (st != GRN_OK) return st;
+    if (out) {
+      const int64_t its = out->iterations;
+      *out              = r;
+      out->iterations   = its + 1;
+    }
+    if (iter > 0) {
+      if (std::isnan(r.sigma) || std::isinf(r.sigma))
+        return fail(GRN_ERR_NAN, "VEGAS integral inf/nan: cuts or parameters need fixing");
+      if (r.sigma < 1e-60)
+        return fail(GRN_ERR_INVALID, "VEGAS integral < 1e-60: check cuts and decay mode");
+      if (r.chi2 > 50) {
+        *factor = 10;
+        return GRN_OK;
+      }
+    }
+    if (init > 0 && iter == itermin - 1 &&
+        (r.chi2 > vp->chi2max || r.sigma_err / r.sigma > vp->precision))
+      ++itermin;
+  }
+  return GRN_OK;
+}
+
+grn_status grn_vegas_integrate(grn_engine *e, const grn_vegas_params *vp, grn_vegas_result *out) {
+  if (!e || !vp) return fail(GRN_ERR_INVALID, "null argument");
+  grn_status st = require_screening_ready(e);
+  if (st != GRN_OK) return st;
+  st = grn_vegas_init(e, vp);
+  if (st != GRN_OK) return st;
+  grn_vegas_result r{};
+  int     burnin = std::max(1, vp->burnin_iter);
+  int64_t ncall  = vp->ncall;
+  // SampleVegas, GMODE = 0 (MGraniitti.cc:1086-1126), without the wall-clock
+  // based NCALL increase.
+  while (true) {
+    int factor = 1;
+    while (true) {
+      st = vegas_run(e, vp, 0, ncall, burnin, &factor, &r);
+      if (st != GRN_OK) return st;
+      ncall *= factor;
+      if (factor == 1) break;
+    }
+    r.iterations = 0;
+    st = vegas_run(e, vp, 1, ncall, vp->iter, &factor, &r);
+    if (st != GRN_OK) return st;
+    if (factor == 1) break;
+    ncall *= factor;
+    burnin *= 2;
+  }
+  if (out) *out = r;
+  return GRN_OK;
+}
+
+grn_status grn_vegas_get_grid(grn_engine *e, double *xmat) {
+  if (!e || !e->vegas_ready || !xmat) return fail(GRN_ERR_STATE, "VEGAS not initialised");
+  GRN_CUDA(cudaMemcpyAsync(xmat, e->d_xmat.p, e->bins * e->dim * sizeof(double),
+                           cudaMemcpyDefault, e->stream));
+  GRN_CUDA(cudaStreamSynchronize(e->stream));
+  return GRN_OK;
+}
+
+grn_status grn_vegas_set_grid(grn_engine *e, const double *xmat) {
+  if (!e || !e->vegas_ready || !xmat) return fail(GRN_ERR_STATE, "VEGAS not initialised");
+  GRN_CUDA(cudaMemcpyAsync(e->d_xmat.p, xmat, e->bins * e->dim * sizeof(double),
+                           cudaMemcpyDefault, e->stream));
+  GRN_CUDA(cudaStreamSynchronize(e->stream));
+  return GRN_OK;
+}
+
+// ---------------------------------------------------------------------------
+// Unweighting
+
+grn_status grn_unweight(grn_engine *e, double fmax, uint64_t seed, int64_t *n_accepted,
+                        int64_t *n_overflow, int64_t *idx_out, int64_t cap) {
+  if (!e || !e->have_last) return fail(GRN_ERR_STATE, "no VEGAS iteration to unweight");
+  if (!(fmax > 0)) return fail(GRN_ERR_INVALID, "fmax must be positive");
+  GRN_CUDA(cudaSetDevice(e->device));
+  const int64_t n   = e->last_ncall;
+  const int     nb  = grn::unweight_blocks(n);
+  const size_t  cnt = ((nb * sizeof(int) + 255) / 256) * 256 + nb * sizeof(int64_t);
+  GRN_CUDA(e->d_uw_counts.ensure(cnt));
+  GRN_CUDA(e->d_uw_misc.ensure(2 * sizeof(int64_t)));
+  GRN_CUDA(cudaMemsetAsync(e->d_uw_misc.p, 0, 2 * sizeof(int64_t), e->stream));
+  int64_t *didx     = nullptr;
+  const bool dev_ix = idx_out && is_device_ptr(idx_out);
+  if (idx_out && cap > 0) {
+    if (dev_ix) {
+      didx = idx_out;
+    } else {
+      GRN_CUDA(e->d_uw_idx.ensure(cap * sizeof(int64_t)));
+      didx = e->d_uw_idx.as<int64_t>();
+    }
+  }
+  int64_t *misc = e->d_uw_misc.as<int64_t>();
+  GRN_CUDA(grn::launch_unweight(e->d_f.as<double>(), n, fmax, seed, 0x80000000u | e->last_stream,
+                                e->d_uw_counts.as<int>(),
+                                reinterpret_cast<unsigned long long *>(misc + 1), didx, cap, misc,
+                                nb, e->stream));
+  int64_t h[2] = {0, 0};
+  GRN_CUDA(cudaMemcpyAsync(h, misc, 2 * sizeof(int64_t), cudaMemcpyDeviceToHost, e->stream));
+  GRN_CUDA(cudaStreamSynchronize(e->stream));
+  if (n_accepted) *n_accepted = h[0];
+  if (n_overflow) *n_overflow = h[1];
+  if (didx && !dev_ix) {
+    const int64_t m = std::min(h[0], cap);
+    GRN_CUDA(cudaMemcpy(idx_out, didx, m * sizeof(int64_t), cudaMemcpyDeviceToHost));
+  }
+  return GRN_OK;
+}
+
+grn_status grn_vegas_points(grn_engine *e, const int64_t *idx, int64_t n, double *u_out) {
+  if (!e || !e->have_last || !idx || !u_out) return fail(GRN_ERR_STATE, "no VEGAS iteration");
+  if (n == 0) return GRN_OK;
+  GRN_CUDA(cudaSetDevice(e->device));
+  GRN_CUDA(e->d_uw_idx.ensure(n * sizeof(int64_t)));
+  GRN_CUDA(e->d_aux.ensure(n * e->dim * sizeof(double)));
+  GRN_CUDA(cudaMemcpyAsync(e->d_uw_idx.p, idx, n * sizeof(int64_t), cudaMemcpyDefault, e->stream));
+  GRN_CUDA(grn::launch_vegas_points(e->d_xmat_prev.as<double>(), e->bins, e->dim, e->seed,
+                                    e->last_stream, e->d_uw_idx.as<int64_t>(), n,
+                                    e->d_aux.as<double>(), e->stream));
+  GRN_CUDA(cudaMemcpyAsync(u_out, e->d_aux.p, n * e->dim * sizeof(double), cudaMemcpyDefault,
+                           e->stream));
+  GRN_CUDA(cudaStreamSynchronize(e->stream));
+  return GRN_OK;
+}
+
+grn_status grn_kernel_timing(grn_engine *e, int32_t reset, double *total_ms, int64_t *launches) {
+  if (!e) return fail(GRN_ERR_INVALID, "null engine");
+  if (total_ms) *total_ms = e->sample_ms;
+  if (launches) *launches = e->sample_launches;
+  if (reset) {
+    e->sample_ms       = 0.0;
+    e->sample_launches = 0;
+  }
+  return GRN_OK;
+}
+
+grn_status grn_fp32_peak(int32_t device, double *tflops) {
+  if (!tflops) return fail(GRN_ERR_INVALID, "null argument");
+  int ndev = 0;
+  if (cudaGetDeviceCount(&ndev) != cudaSuccess || device < 0 || device >= ndev) {
+    cudaGetLastError();
+    return fail(GRN_ERR_NO_DEVICE, "no such CUDA device");
+  }
+  GRN_CUDA(cudaSetDevice(device));
+  int sms = 0;
+  GRN_CUDA(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, device));
+  const int blocks = sms * 8, threads = 256, iters = 1 << 14;
+  float    *sink = nullptr;
+  GRN_CUDA(cudaMalloc(&sink, sizeof(float)));
+  cudaEvent_t a, b;
+  cudaEventCreate(&a);
+  cudaEventCreate(&b);
+  double best = 0.0;
+  for (int rep = 0; rep < 4; ++rep) {
+    cudaEventRecord(a, nullptr);
+    grn::launch_fma_probe(blocks, threads, iters, sink, nullptr);
+    cudaEventRecord(b, nullptr);
+    cudaEventSynchronize(b);
+    float ms = 0.f;
+    cudaEventElapsedTime(&ms, a, b);
+    if (rep > 0 && ms > 0) best = std::max(best, grn::fma_probe_flops(blocks, threads, iters) /
+                                                   (ms * 1e-3) / 1e12);
+  }
+  cudaEventDestroy(a);
+  cudaEventDestroy(b);
+  cudaFree(sink);
+  const cudaError_t ce = cudaGetLastError();
+  if (ce != cudaSuccess) return fail(GRN_ERR_CUDA, cudaGetErrorString(ce));
+  *tflops = best;
+  return GRN_OK;
+}
+
+}  // extern "C"

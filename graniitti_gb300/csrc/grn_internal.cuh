@@ -1,0 +1,83 @@
+// grn_internal.cuh — kernel launch interface shared by grn_kernels.cu and grn_api.cu.
+#pragma once
+
+#include <cuda_runtime.h>
+
+#include <cstdint>
+
+#include "grn_physics.cuh"
+
+namespace grn {
+
+// Everything a weight kernel needs, passed by value (kernel parameter space).
+struct KArgs {
+  grn_process_params P;
+  Consts             K;
+  // kt-loop node tables (device): per kt node j (kt_j, Re c_j, Im c_j) with
+  // c_j = V_j * kt_j * A_eik(kt_j^2); per phi node i (cos phi_i, sin phi_i, U_i).
+  const double *lc_kt;
+  const double *lc_phi;
+  int           n_kt_nodes;
+  int           n_phi_nodes;
+  double        loop_norm_re, loop_norm_im;  // i/(8 pi^2 s) * 9 h_phi h_kt / 64
+};
+
+constexpr int kMaxLoopNodes = 256;  // per axis
+
+// Scalars accumulated per block by the VEGAS sampling kernel.
+enum VegasScalar {
+  VS_FSUM = 0,
+  VS_F2SUM,
+  VS_MAXF,
+  VS_MAXW,
+  VS_EVAL,
+  VS_AMP_OK,
+  VS_KIN_OK,
+  VS_FID_OK,
+  VS_VETO_OK,
+  VS_NAN,
+  VS_COUNT
+};
+
+// Launchers (all stream-ordered, return cudaGetLastError of the launch).
+cudaError_t launch_event_weights(const KArgs &a, int prec, const double *u, int64_t n, int dim,
+                                 double *w, uint8_t *flags, cudaStream_t st);
+cudaError_t launch_event_kinematics(const KArgs &a, const double *u, int64_t n, int dim,
+                                    double *p4, double *ts, uint8_t *flags, cudaStream_t st);
+cudaError_t launch_uniforms(uint64_t seed, uint32_t stream, int64_t first, int64_t n, int dim,
+                            double *out, cudaStream_t st);
+
+cudaError_t launch_eikonal_density(const grn_soft_params &sp, double s, int n_bt, double2 *amp,
+                                   double *mbt, cudaStream_t st);
+cudaError_t launch_eikonal_screening(double s, int n_bt, const double *mbt, int n_kt2, double2 *g,
+                                     double *msa, double *xs, cudaStream_t st);
+
+cudaError_t launch_eikonal_xs(const double *mbt, int n_bt, double *xs, cudaStream_t st);
+
+// VEGAS
+int         vegas_grid_blocks(int device);
+cudaError_t launch_vegas_grid_init(double *xmat, int bins, int dim, cudaStream_t st);
+cudaError_t launch_vegas_sample(const KArgs &a, int prec, const double *xmat, int bins, int dim,
+                                int64_t ncall, uint64_t seed, uint32_t stream, int track_max,
+                                double *f_out, double *part_hist, double *part_sc, int nblocks,
+                                cudaStream_t st);
+cudaError_t launch_vegas_reduce(const double *part_hist, const double *part_sc, int nblocks,
+                                int nhist, double *f2mat, double *sc, cudaStream_t st);
+cudaError_t launch_vegas_refine(double *xmat, double *f2mat, int bins, int dim, double lambda,
+                                cudaStream_t st);
+cudaError_t launch_vegas_points(const double *xmat, int bins, int dim, uint64_t seed,
+                                uint32_t stream, const int64_t *idx, int64_t n, double *u_out,
+                                cudaStream_t st);
+
+// Unweighting
+cudaError_t launch_unweight(const double *f, int64_t n, double fmax, uint64_t seed,
+                            uint32_t stream, int *blk_counts, unsigned long long *overflow,
+                            int64_t *idx_out, int64_t cap, int64_t *n_acc_dev, int nblocks,
+                            cudaStream_t st);
+int unweight_blocks(int64_t n);
+
+// FP32 FMA throughput probe: returns flops executed by one launch.
+double      fma_probe_flops(int blocks, int threads, int iters);
+cudaError_t launch_fma_probe(int blocks, int threads, int iters, float *sink, cudaStream_t st);
+
+}  // namespace grn

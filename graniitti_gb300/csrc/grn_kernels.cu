@@ -1,0 +1,819 @@
+// grn_kernels.cu — sm_103a kernels of the event-weight engine.
+//
+//   k_event_weights     one thread per event: FP64 light-cone kinematics, cuts,
+//                       Regge |M|^2 and (optionally) the eikonal kt-loop with the
+//                       node tables staged in shared memory (FP64 or FP32+Kahan).
+//   k_vegas_sample      persistent VEGAS pass: Philox points -> grid map ->
+//                       weight -> f, f^2 histograms in shared memory -> per-block
+//                       partials (reduced in fixed block order by k_vegas_reduce).
+//   k_vegas_refine      grid smoothing + rebinning, one thread per dimension.
+//   k_eik_*             eikonal density / screening tables (Fourier-Bessel sums).
+//   k_unweight_*        hit-or-miss acceptance + order-preserving compaction.
+#include <cuda_runtime.h>
+
+#include <cstdint>
+
+#include "grn_internal.cuh"
+
+namespace grn {
+
+// ---------------------------------------------------------------------------
+// Philox4x32-10 (Salmon et al., SC'11). counter = (index lo, index hi, block,
+// stream), key = seed. Each block gives two 53-bit doubles in [0, 1).
+__device__ __forceinline__ void philox_block(uint64_t seed, uint32_t stream, uint64_t idx,
+                                             uint32_t blk, double &r0, double &r1) {
+  uint32_t c0 = static_cast<uint32_t>(idx), c1 = static_cast<uint32_t>(idx >> 32), c2 = blk,
+           c3 = stream;
+  uint32_t k0 = static_cast<uint32_t>(seed), k1 = static_cast<uint32_t>(seed >> 32);
+#pragma unroll
+  for (int r = 0; r < 10; ++r) {
+    const uint32_t hi0 = __umulhi(0xD2511F53u, c0), lo0 = 0xD2511F53u * c0;
+    const uint32_t hi1 = __umulhi(0xCD9E8D57u, c2), lo1 = 0xCD9E8D57u * c2;
+    const uint32_t n0 = hi1 ^ c1 ^ k0;
+    const uint32_t n2 = hi0 ^ c3 ^ k1;
+    c0 = n0;
+    c1 = lo1;
+    c2 = n2;
+    c3 = lo0;
+    k0 += 0x9E3779B9u;
+    k1 += 0xBB67AE85u;
+  }
+  const uint64_t a = (static_cast<uint64_t>(c1) << 32) | c0;
+  const uint64_t b = (static_cast<uint64_t>(c3) << 32) | c2;
+  r0 = static_cast<double>(a >> 11) * 0x1.0p-53;
+  r1 = static_cast<double>(b >> 11) * 0x1.0p-53;
+}
+
+__device__ __forceinline__ void philox_point(uint64_t seed, uint32_t stream, uint64_t idx,
+                                             int dim, double *u) {
+  for (int blk = 0; 2 * blk < dim; ++blk) {
+    double r0, r1;
+    philox_block(seed, stream, idx, blk, r0, r1);
+    u[2 * blk] = r0;
+    if (2 * blk + 1 < dim) u[2 * blk + 1] = r1;
+  }
+}
+
+// ---------------------------------------------------------------------------
+// Bessel J0: Abramowitz & Stegun 9.4 rational / asymptotic approximation, the
+// same published coefficients as the reference's BESSJ0 (libs/extmath.hpp:12).
+__device__ double bessel_j0(double x) {
+  if (x == 0.0) return 1.0;
+  const double ax = fabs(x);
+  if (ax < 8.0) {
+    const double y = x * x;
+    const double num = 57568490574.0 +
+                       y * (-13362590354.0 + y * (651619640.7 + y * (-11214424.18 +
+                       y * (77392.33017 + y * (-184.9052456)))));
+    const double den = 57568490411.0 +
+                       y * (1029532985.0 + y * (9494680.718 + y * (59272.64853 +
+                       y * (267.8532712 + y * 1.0))));
+    return num / den;
+  }
+  const double z  = 8.0 / ax;
+  const double y  = z * z;
+  const double xx = ax - 0.785398164;
+  const double p  = 1.0 + y * (-0.1098628627E-2 + y * (0.2734510407E-4 +
+                    y * (-0.2073370639E-5 + y * 0.2093887211E-6)));
+  const double q  = -0.1562499995E-1 + y * (0.1430488765E-3 + y * (-0.6911147651E-5 +
+                    y * (0.7621095161E-6 + y * (-0.9349451520E-7))));
+  double sn, cs;
+  sincos(xx, &sn, &cs);
+  return sqrt(0.636619772 / ax) * (p * cs - z * q * sn);
+}
+
+// ---------------------------------------------------------------------------
+// kt-loop integral.
+
+template <typename T>
+struct KtNode {
+  T kt, cre, cim;
+};
+template <typename T>
+struct PhiNode {
+  T c, s, u;
+};
+
+template <typename T>
+__device__ __forceinline__ void kahan_add(T &sum, T &comp, T x) {
+  const T y = x - comp;
+  const T t = sum + y;
+  comp      = (t - sum) - y;
+  sum       = t;
+}
+
+// A_loop = i/(8 pi^2 s) * (9 h_phi h_kt / 64) * sum_ij U_i V_j A_eik(kt_j^2) kt_j A(i, j)
+// (MProcess::S3ScreenedAmp2, src/MProcess.cc:157-261; Simpson38Integral2D,
+// include/Graniitti/MMath.h:457-472). The kt-node factor c_j = V_j kt_j A_eik(kt_j^2)
+// is shared by all events and precomputed.
+template <typename T>
+__device__ cx<double> loop_integral(const KArgs &A, const Born &b, const KtNode<T> *skt,
+                                    const PhiNode<T> *sphi) {
+  LoopEvent<T> e;
+  make_loop_event<T>(A.K, b, e);
+  T ar = T(0), ai = T(0), cr = T(0), ci = T(0);
+  for (int j = 0; j < A.n_kt_nodes; ++j) {
+    const KtNode<T> nj = skt[j];
+    T ir = T(0), ii = T(0), dr = T(0), di = T(0);
+    for (int i = 0; i < A.n_phi_nodes; ++i) {
+      const PhiNode<T> ni = sphi[i];
+      cx<T> a;
+      if (loop_point_amp<T>(A.P, A.K, e, nj.kt * ni.c, nj.kt * ni.s, a)) {
+        kahan_add(ir, dr, ni.u * a.re);
+        kahan_add(ii, di, ni.u * a.im);
+      }
+    }
+    kahan_add(ar, cr, nj.cre * ir - nj.cim * ii);
+    kahan_add(ai, ci, nj.cre * ii + nj.cim * ir);
+  }
+  const double sr = double(ar), si = double(ai);
+  return {A.loop_norm_re * sr - A.loop_norm_im * si, A.loop_norm_re * si + A.loop_norm_im * sr};
+}
+
+// One event weight (MContinuum::EventWeight, src/MContinuum.cc:164-193).
+template <typename T>
+__device__ double event_weight(const KArgs &A, const double *u, uint8_t &flags,
+                               const KtNode<T> *skt, const PhiNode<T> *sphi) {
+  Born       b;
+  const bool kin = born_kinematics(A.P, A.K, u, b);
+  const bool fid = kin && fiducial_cuts(A.P, A.K, b);
+  double     W   = 0.0;
+  if (kin && fid) {
+    const cx<double> A0 = regge_me4<double>(A.P, A.K, b.t1, b.t2, log(b.s13), log(b.s14),
+                                            log(b.s23), log(b.s24), b.that, b.uhat);
+    double amp2;
+    if (A.P.screening) {
+      const cx<double> Al = loop_integral<T>(A, b, skt, sphi);
+      const double     re = A0.re + Al.re, im = A0.im + Al.im;
+      amp2                = re * re + im * im;
+    } else {
+      amp2 = A0.re * A0.re + A0.im * A0.im;
+    }
+    W = weight_jacobian(A.K, b) * amp2;
+  }
+  bool amp_ok = true;
+  if (!isfinite(W)) {
+    W      = 0.0;
+    amp_ok = false;
+  }
+  flags = (kin ? GRN_FLAG_KINEMATICS_OK : 0) | (fid ? GRN_FLAG_FIDCUTS_OK : 0) |
+          GRN_FLAG_VETOCUTS_OK | (amp_ok ? GRN_FLAG_AMPLITUDE_OK : 0);
+  return W;
+}
+
+// Stage the loop node tables into shared memory (converted to T).
+template <typename T>
+__device__ void stage_nodes(const KArgs &A, KtNode<T> *skt, PhiNode<T> *sphi) {
+  if (!A.P.screening) return;
+  for (int j = threadIdx.x; j < A.n_kt_nodes; j += blockDim.x)
+    skt[j] = {T(A.lc_kt[3 * j]), T(A.lc_kt[3 * j + 1]), T(A.lc_kt[3 * j + 2])};
+  for (int i = threadIdx.x; i < A.n_phi_nodes; i += blockDim.x)
+    sphi[i] = {T(A.lc_phi[3 * i]), T(A.lc_phi[3 * i + 1]), T(A.lc_phi[3 * i + 2])};
+}
+
+constexpr int kWeightThreads = 128;
+
+template <typename T>
+__global__ void __launch_bounds__(kWeightThreads)
+    k_event_weights(const KArgs A, const double *__restrict__ u, int64_t n, int dim,
+                    double *__restrict__ w, uint8_t *__restrict__ flags) {
+  __shared__ KtNode<T>  skt[kMaxLoopNodes];
+  __shared__ PhiNode<T> sphi[kMaxLoopNodes];
+  stage_nodes<T>(A, skt, sphi);
+  __syncthreads();
+  const int64_t i = static_cast<int64_t>(blockIdx.x) * blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  double x[8];
+#pragma unroll
+  for (int d = 0; d < 8; ++d) x[d] = u[i * dim + d];
+  uint8_t    f;
+  const double W = event_weight<T>(A, x, f, skt, sphi);
+  w[i]           = W;
+  if (flags) flags[i] = f;
+}
+
+cudaError_t launch_event_weights(const KArgs &a, int prec, const double *u, int64_t n, int dim,
+                                 double *w, uint8_t *flags, cudaStream_t st) {
+  if (n <= 0) return cudaSuccess;
+  const unsigned blocks = static_cast<unsigned>((n + kWeightThreads - 1) / kWeightThreads);
+  if (prec == GRN_PREC_MIXED)
+    k_event_weights<float><<<blocks, kWeightThreads, 0, st>>>(a, u, n, dim, w, flags);
+  else
+    k_event_weights<double><<<blocks, kWeightThreads, 0, st>>>(a, u, n, dim, w, flags);
+  return cudaGetLastError();
+}
+
+// Kinematics only: pfinal[1..4] as (px, py, pz, E), and t1, t2.
+__global__ void k_event_kinematics(const KArgs A, const double *__restrict__ u, int64_t n,
+                                   int dim, double *__restrict__ p4, double *__restrict__ ts,
+                                   uint8_t *__restrict__ flags) {
+  const int64_t i = static_cast<int64_t>(blockIdx.x) * blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  double x[8];
+#pragma unroll
+  for (int d = 0; d < 8; ++d) x[d] = u[i * dim + d];
+  Born       b;
+  const bool kin = born_kinematics(A.P, A.K, x, b);
+  const bool fid = kin && fiducial_cuts(A.P, A.K, b);
+  if (p4) {
+    double *o = p4 + i * 16;
+    o[0] = b.p1x; o[1] = b.p1y; o[2] = 0.5 * (b.p1p - b.p1m); o[3] = 0.5 * (b.p1p + b.p1m);
+    o[4] = b.p2x; o[5] = b.p2y; o[6] = 0.5 * (b.p2p - b.p2m); o[7] = 0.5 * (b.p2p + b.p2m);
+    o[8] = b.p3x; o[9] = b.p3y; o[10] = b.mt3 * sinh(b.y3); o[11] = b.mt3 * cosh(b.y3);
+    o[12] = b.p4x; o[13] = b.p4y; o[14] = b.mt4 * sinh(b.y4); o[15] = b.mt4 * cosh(b.y4);
+  }
+  if (ts) {
+    ts[2 * i]     = b.t1;
+    ts[2 * i + 1] = b.t2;
+  }
+  if (flags)
+    flags[i] = (kin ? GRN_FLAG_KINEMATICS_OK : 0) | (fid ? GRN_FLAG_FIDCUTS_OK : 0) |
+               GRN_FLAG_VETOCUTS_OK | GRN_FLAG_AMPLITUDE_OK;
+}
+
+cudaError_t launch_event_kinematics(const KArgs &a, const double *u, int64_t n, int dim,
+                                    double *p4, double *ts, uint8_t *flags, cudaStream_t st) {
+  if (n <= 0) return cudaSuccess;
+  const unsigned blocks = static_cast<unsigned>((n + 127) / 128);
+  k_event_kinematics<<<blocks, 128, 0, st>>>(a, u, n, dim, p4, ts, flags);
+  return cudaGetLastError();
+}
+
+__global__ void k_uniforms(uint64_t seed, uint32_t stream, int64_t first, int64_t n, int dim,
+                           double *out) {
+  const int64_t i = static_cast<int64_t>(blockIdx.x) * blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  double u[16];
+  philox_point(seed, stream, static_cast<uint64_t>(first + i), dim, u);
+  for (int d = 0; d < dim; ++d) out[i * dim + d] = u[d];
+}
+
+cudaError_t launch_uniforms(uint64_t seed, uint32_t stream, int64_t first, int64_t n, int dim,
+                            double *out, cudaStream_t st) {
+  if (n <= 0) return cudaSuccess;
+  k_uniforms<<<static_cast<unsigned>((n + 255) / 256), 256, 0, st>>>(seed, stream, first, n, dim,
+                                                                     out);
+  return cudaGetLastError();
+}
+
+// ---------------------------------------------------------------------------
+// Eikonal tables (MEikonal::S3Density / S3Screening / S3CalcXS,
+// src/MEikonal.cc:177-376). Simpson 1/3 weights are folded into the per-node
+// factors so that each table row is a plain dot product with J0.
+
+__device__ __forceinline__ double simpson13_w(int k, int N, double h) {
+  const double c = (k == 0 || k == N) ? 1.0 : ((k & 1) ? 4.0 : 2.0);
+  return c * h / 3.0;
+}
+
+// Pomeron trajectory with the pion-loop insert (src/MForm.cc:402-427).
+__device__ double pomeron_alpha(const grn_soft_params &sp, double t) {
+  const double beta_pi = (2.0 / 3.0) * sp.gN_P;
+  const double pic     = (beta_pi * beta_pi * kMpiSoft * kMpiSoft) / (32.0 * kPi * kPi * kPi);
+  const double tau     = 4.0 * kMpiSoft * kMpiSoft / fabs(t);
+  const double sqt     = sqrt(1.0 + tau);
+  const double fpi     = 1.0 / (1.0 - t / sp.fc3);
+  const double h       = (4.0 / tau) * fpi * fpi *
+                   (2.0 * tau - pow(1.0 + tau, 1.5) * log((sqt + 1.0) / (sqt - 1.0)) +
+                    log(1.0 / (kMpiSoft * kMpiSoft)));
+  return 1.0 + sp.delta_P + sp.alpha_P * t - pic * h;
+}
+
+// ReggeEta(alpha, sigma) = -(1 + sigma e^{-i pi alpha}) / sin(pi alpha) (MForm.cc:382-385).
+__device__ cx<double> regge_eta_dev(double alpha, double sigma) {
+  double sn, cs;
+  sincospi(alpha, &sn, &cs);
+  return {-(1.0 + sigma * cs) / sn, -(sigma * -sn) / sn};
+}
+
+// Node factors of the density transform: A(s, -kt^2) kt w_k / (2 pi s).
+__global__ void k_eik_amp(const grn_soft_params sp, double s, double2 *amp) {
+  const int k = blockIdx.x * blockDim.x + threadIdx.x;
+  if (k > kFBN) return;
+  const double h  = (kFBMaxKT - kFBMinKT) / kFBN;
+  const double kt = kFBMinKT + k * h;
+  const double t  = -kt * kt;
+  const double F  = 1.0 / ((1.0 - t / sp.fc1) * (1.0 - t / sp.fc2));
+  const double a  = pomeron_alpha(sp, t);
+  const double sa = exp(a * log(s));
+  cx<double> e    = regge_eta_dev(a, 1.0);
+  double     mag  = sp.gN_P * sp.gN_P * F * F * sa;
+  cx<double> A{mag * e.re, mag * e.im};
+  if (sp.odderon_on) {
+    const cx<double> eo  = regge_eta_dev(a, -1.0);
+    const double     mo  = sp.gN_O * sp.gN_O * F * F * sa;
+    A.re += mo * eo.re;
+    A.im += mo * eo.im;
+  }
+  const double f = kt * simpson13_w(k, kFBN, h) / (2.0 * kPi * s);
+  amp[k]         = make_double2(A.re * f, A.im * f);
+}
+
+constexpr int kEikThreads = 256;
+
+// Deterministic block reduction of a complex FP64 value (fixed tree order).
+__device__ double2 block_sum2(double2 v) {
+  __shared__ double sr[kEikThreads], si[kEikThreads];
+  sr[threadIdx.x] = v.x;
+  si[threadIdx.x] = v.y;
+  __syncthreads();
+  for (int o = kEikThreads / 2; o > 0; o >>= 1) {
+    if (threadIdx.x < o) {
+      sr[threadIdx.x] += sr[threadIdx.x + o];
+      si[threadIdx.x] += si[threadIdx.x + o];
+    }
+    __syncthreads();
+  }
+  return make_double2(sr[0], si[0]);
+}
+
+// One row per block: sum_k node[k] * J0(x_row * xnode_k); rows of (x, Re, Im).
+__global__ void __launch_bounds__(kEikThreads)
+    k_eik_rows(const double2 *__restrict__ node, double node_x0, double node_h, int nrows,
+               double row_x0, double row_h, int row_sqrt, double scale, double *out) {
+  const int r = blockIdx.x;
+  if (r > nrows) return;
+  const double xr  = row_x0 + r * row_h;
+  const double arg = row_sqrt ? sqrt(fmax(0.0, xr)) : xr;
+  double2 acc = make_double2(0.0, 0.0);
+  for (int k = threadIdx.x; k <= kFBN; k += kEikThreads) {
+    const double  j0 = bessel_j0(arg * (node_x0 + k * node_h));
+    const double2 v  = node[k];
+    acc.x += v.x * j0;
+    acc.y += v.y * j0;
+  }
+  const double2 s = block_sum2(acc);
+  if (threadIdx.x == 0) {
+    out[3 * r + 0] = xr;
+    out[3 * r + 1] = s.x * scale;
+    out[3 * r + 2] = s.y * scale;
+  }
+}
+
+// Linear interpolation in a (x, Re, Im) table (IArray1D::Interpolate1D,
+// src/MEikonal.cc:489-512).
+__device__ cx<double> table_interp(const double *tab, int N, double xmin, double xmax, double a) {
+  const double step = (xmax - xmin) / N;
+  if (a < xmin) a = xmin;
+  int i = static_cast<int>(floor((a - xmin) / step));
+  if (i < 0) i = 0;
+  if (i >= N) i = N - 1;
+  const double *r0 = tab + 3 * i, *r1 = tab + 3 * (i + 1);
+  const double  fr = (a - r0[0]) / (r1[0] - r0[0]);
+  return {r0[1] + fr * (r1[1] - r0[1]), r0[2] + fr * (r1[2] - r0[2])};
+}
+
+// Node factors of the screening transform: i (1 - exp(i Omega(b)/2)) b w_k.
+__global__ void k_eik_g(const double *mbt, int n_bt, double2 *g) {
+  const int k = blockIdx.x * blockDim.x + threadIdx.x;
+  if (k > kFBN) return;
+  const double h  = (kMaxBT - kMinBT) / kFBN;
+  const double bt = kMinBT + k * h;
+  const cx<double> Om = table_interp(mbt, n_bt, kMinBT, kMaxBT, bt);
+  // exp(i Om / 2) = exp(-Im/2) (cos(Re/2) + i sin(Re/2))
+  double sn, cs;
+  sincos(0.5 * Om.re, &sn, &cs);
+  const double m  = exp(-0.5 * Om.im);
+  const double er = 1.0 - m * cs, ei = -m * sn;  // 1 - exp(i Om/2)
+  const double f  = bt * simpson13_w(k, kFBN, h);
+  g[k]            = make_double2(-ei * f, er * f);  // i * (er + i ei)
+}
+
+// Single-channel eikonal cross sections (S3CalcXS, src/MEikonal.cc:254-376).
+__global__ void __launch_bounds__(kEikThreads) k_eik_xs(const double *mbt, int n_bt, double *xs) {
+  const int    N = 6000;
+  const double h = (kMaxBT - kMinBT) / N;
+  double2 a = make_double2(0.0, 0.0);
+  double  el = 0.0;
+  for (int k = threadIdx.x; k <= N; k += kEikThreads) {
+    const double bt = kMinBT + k * h;
+    const cx<double> Om = table_interp(mbt, n_bt, kMinBT, kMaxBT, bt);
+    double sn, cs;
+    sincos(0.5 * Om.re, &sn, &cs);
+    const double m  = exp(-0.5 * Om.im);
+    const double er = 1.0 - m * cs, ei = -m * sn;
+    // A_el = i (er + i ei) = -ei + i er
+    const double Are = -ei, Aim = er;
+    const double w   = simpson13_w(k, N, h) * bt;
+    a.x += 2.0 * Aim * w;
+    el += (Are * Are + Aim * Aim) * w;
+  }
+  const double2 tot = block_sum2(a);
+  __syncthreads();
+  const double2 elv = block_sum2(make_double2(el, 0.0));
+  if (threadIdx.x == 0) {
+    const double c = 2.0 * kPi * kGeV2barn;
+    xs[0]          = c * tot.x;
+    xs[1]          = c * elv.x;
+    xs[2]          = c * (tot.x - elv.x);
+  }
+}
+
+cudaError_t launch_eikonal_density(const grn_soft_params &sp, double s, int n_bt, double2 *amp,
+                                   double *mbt, cudaStream_t st) {
+  k_eik_amp<<<(kFBN + 1 + 255) / 256, 256, 0, st>>>(sp, s, amp);
+  const double h = (kFBMaxKT - kFBMinKT) / kFBN;
+  k_eik_rows<<<n_bt + 1, kEikThreads, 0, st>>>(amp, kFBMinKT, h, n_bt, kMinBT,
+                                               (kMaxBT - kMinBT) / n_bt, 0, 1.0, mbt);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_eikonal_screening(double s, int n_bt, const double *mbt, int n_kt2, double2 *g,
+                                     double *msa, double *xs, cudaStream_t st) {
+  k_eik_xs<<<1, kEikThreads, 0, st>>>(mbt, n_bt, xs);
+  k_eik_g<<<(kFBN + 1 + 255) / 256, 256, 0, st>>>(mbt, n_bt, g);
+  const double h = (kMaxBT - kMinBT) / kFBN;
+  k_eik_rows<<<n_kt2 + 1, kEikThreads, 0, st>>>(g, kMinBT, h, n_kt2, kMinKT2,
+                                                (kMaxKT2 - kMinKT2) / n_kt2, 1,
+                                                2.0 * s * 2.0 * kPi, msa);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_eikonal_xs(const double *mbt, int n_bt, double *xs, cudaStream_t st) {
+  k_eik_xs<<<1, kEikThreads, 0, st>>>(mbt, n_bt, xs);
+  return cudaGetLastError();
+}
+
+// ---------------------------------------------------------------------------
+// VEGAS (MGraniitti::VEGASMultiThread, src/MGraniitti.cc:1341-1443;
+// VEGASData, include/Graniitti/MVEGAS.h).
+
+constexpr int kVegasThreads = 128;
+constexpr int kMaxBins      = 256;
+constexpr int kMaxDim       = 8;
+
+template <typename T>
+__global__ void __launch_bounds__(kVegasThreads)
+    k_vegas_sample(const KArgs A, const double *__restrict__ xmat, int bins, int dim,
+                   int64_t ncall, uint64_t seed, uint32_t stream, int track_max,
+                   double *__restrict__ f_out, double *__restrict__ part_hist,
+                   double *__restrict__ part_sc) {
+  extern __shared__ double dsm[];
+  double *sx  = dsm;                   // bins * dim grid
+  double *sf2 = dsm + bins * dim;      // bins * dim f^2 histogram
+  __shared__ KtNode<T>  skt[kMaxLoopNodes];
+  __shared__ PhiNode<T> sphi[kMaxLoopNodes];
+  __shared__ double     ssc[VS_COUNT];
+  stage_nodes<T>(A, skt, sphi);
+  for (int i = threadIdx.x; i < bins * dim; i += blockDim.x) {
+    sx[i]  = xmat[i];
+    sf2[i] = 0.0;
+  }
+  if (threadIdx.x < VS_COUNT) ssc[threadIdx.x] = 0.0;
+  __syncthreads();
+
+  double fsum = 0.0, f2sum = 0.0, maxf = 0.0, maxW = 0.0;
+  double ev = 0.0, amp_ok = 0.0, kin_ok = 0.0, fid_ok = 0.0, veto_ok = 0.0, nan = 0.0;
+  const double dbins = static_cast<double>(bins);
+  const int64_t stride = static_cast<int64_t>(gridDim.x) * blockDim.x;
+  for (int64_t e = static_cast<int64_t>(blockIdx.x) * blockDim.x + threadIdx.x; e < ncall;
+       e += stride) {
+    double u[kMaxDim], x[kMaxDim];
+    int    ind[kMaxDim];
+    philox_point(seed, stream, static_cast<uint64_t>(e), dim, u);
+    double vw = 1.0;
+    for (int j = 0; j < dim; ++j) {
+      const double zn = u[j] * dbins + 1.0;
+      int          k  = static_cast<int>(zn);
+      k               = max(1, min(k, bins));
+      double zo, ac;
+      if (k > 1) {
+        zo = sx[(k - 1) * dim + j] - sx[(k - 2) * dim + j];
+        ac = sx[(k - 2) * dim + j] + (zn - k) * zo;
+      } else {
+        zo = sx[(k - 1) * dim + j];
+        ac = (zn - k) * zo;
+      }
+      x[j]   = ac;
+      ind[j] = k - 1;
+      vw *= zo * dbins;
+    }
+    uint8_t      fl;
+    const double W = event_weight<T>(A, x, fl, skt, sphi);
+    const double f = W * vw;
+    f_out[e]       = f;
+    const double f2 = f * f;
+    fsum += f;
+    f2sum += f2;
+    for (int j = 0; j < dim; ++j) atomicAdd(&sf2[ind[j] * dim + j], f2);
+    if (track_max) {
+      maxW = fmax(maxW, W);
+      maxf = fmax(maxf, f);
+    }
+    ev += 1.0;
+    amp_ok += (fl & GRN_FLAG_AMPLITUDE_OK) ? 1.0 : 0.0;
+    kin_ok += (fl & GRN_FLAG_KINEMATICS_OK) ? 1.0 : 0.0;
+    fid_ok += (fl & GRN_FLAG_FIDCUTS_OK) ? 1.0 : 0.0;
+    veto_ok += (fl & GRN_FLAG_VETOCUTS_OK) ? 1.0 : 0.0;
+    nan += (fl & GRN_FLAG_AMPLITUDE_OK) ? 0.0 : 1.0;
+  }
+  // Warp reductions (fixed shuffle order), then one lane per warp into shared.
+  for (int o = 16; o > 0; o >>= 1) {
+    fsum += __shfl_down_sync(0xffffffffu, fsum, o);
+    f2sum += __shfl_down_sync(0xffffffffu, f2sum, o);
+    maxf = fmax(maxf, __shfl_down_sync(0xffffffffu, maxf, o));
+    maxW = fmax(maxW, __shfl_down_sync(0xffffffffu, maxW, o));
+    ev += __shfl_down_sync(0xffffffffu, ev, o);
+    amp_ok += __shfl_down_sync(0xffffffffu, amp_ok, o);
+    kin_ok += __shfl_down_sync(0xffffffffu, kin_ok, o);
+    fid_ok += __shfl_down_sync(0xffffffffu, fid_ok, o);
+    veto_ok += __shfl_down_sync(0xffffffffu, veto_ok, o);
+    nan += __shfl_down_sync(0xffffffffu, nan, o);
+  }
+  __shared__ double wsc[kVegasThreads / 32][VS_COUNT];
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  if (lane == 0) {
+    wsc[warp][VS_FSUM]    = fsum;
+    wsc[warp][VS_F2SUM]   = f2sum;
+    wsc[warp][VS_MAXF]    = maxf;
+    wsc[warp][VS_MAXW]    = maxW;
+    wsc[warp][VS_EVAL]    = ev;
+    wsc[warp][VS_AMP_OK]  = amp_ok;
+    wsc[warp][VS_KIN_OK]  = kin_ok;
+    wsc[warp][VS_FID_OK]  = fid_ok;
+    wsc[warp][VS_VETO_OK] = veto_ok;
+    wsc[warp][VS_NAN]     = nan;
+  }
+  __syncthreads();
+  if (threadIdx.x < VS_COUNT) {
+    const int c = threadIdx.x;
+    double    v = wsc[0][c];
+    for (int w = 1; w < kVegasThreads / 32; ++w)
+      v = (c == VS_MAXF || c == VS_MAXW) ? fmax(v, wsc[w][c]) : v + wsc[w][c];
+    part_sc[static_cast<int64_t>(blockIdx.x) * VS_COUNT + c] = v;
+  }
+  double *ph = part_hist + static_cast<int64_t>(blockIdx.x) * bins * dim;
+  for (int i = threadIdx.x; i < bins * dim; i += blockDim.x) ph[i] = sf2[i];
+}
+
+int vegas_grid_blocks(int device) {
+  int sms = 0;
+  cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, device);
+  int per = 0;
+  cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, k_vegas_sample<float>, kVegasThreads,
+                                                2 * kMaxBins * kMaxDim * sizeof(double));
+  if (per < 1) per = 1;
+  return sms * per;
+}
+
+cudaError_t launch_vegas_sample(const KArgs &a, int prec, const double *xmat, int bins, int dim,
+                                int64_t ncall, uint64_t seed, uint32_t stream, int track_max,
+                                double *f_out, double *part_hist, double *part_sc, int nblocks,
+                                cudaStream_t st) {
+  const size_t sm = 2 * static_cast<size_t>(bins) * dim * sizeof(double);
+  if (prec == GRN_PREC_MIXED)
+    k_vegas_sample<float><<<nblocks, kVegasThreads, sm, st>>>(
+        a, xmat, bins, dim, ncall, seed, stream, track_max, f_out, part_hist, part_sc);
+  else
+    k_vegas_sample<double><<<nblocks, kVegasThreads, sm, st>>>(
+        a, xmat, bins, dim, ncall, seed, stream, track_max, f_out, part_hist, part_sc);
+  return cudaGetLastError();
+}
+
+// Sum the per-block partials in block order (deterministic for a fixed grid).
+__global__ void k_vegas_reduce(const double *__restrict__ part_hist,
+                               const double *__restrict__ part_sc, int nblocks, int nhist,
+                               double *__restrict__ f2mat, double *__restrict__ sc) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i < nhist) {
+    double v = 0.0;
+    for (int b = 0; b < nblocks; ++b) v += part_hist[static_cast<int64_t>(b) * nhist + i];
+    f2mat[i] = v;
+  } else if (i < nhist + VS_COUNT) {
+    const int c = i - nhist;
+    double    v = part_sc[c];
+    for (int b = 1; b < nblocks; ++b) {
+      const double x = part_sc[static_cast<int64_t>(b) * VS_COUNT + c];
+      v = (c == VS_MAXF || c == VS_MAXW) ? fmax(v, x) : v + x;
+    }
+    sc[c] = v;
+  }
+}
+
+cudaError_t launch_vegas_reduce(const double *part_hist, const double *part_sc, int nblocks,
+                                int nhist, double *f2mat, double *sc, cudaStream_t st) {
+  const int n = nhist + VS_COUNT;
+  k_vegas_reduce<<<(n + 255) / 256, 256, 0, st>>>(part_hist, part_sc, nblocks, nhist, f2mat, sc);
+  return cudaGetLastError();
+}
+
+// Rebin one dimension so that each new bin carries an equal share ac of the
+// importance r (VEGASData::Rebin, include/Graniitti/MVEGAS.h:87-104).
+__device__ void rebin_dim(int bins, int dim, int j, double ac, const double *r, double *xnew,
+                          double *xmat) {
+  int    k  = 0;
+  double dr = 0.0, zn = 0.0, zo = 0.0;
+  for (int i = 0; i < bins - 1; ++i) {
+    while (ac > dr && k < bins) dr += r[(++k) - 1];
+    if (k < 1) k = 1;
+    if (k > 1) zo = xmat[(k - 2) * dim + j];
+    zn = xmat[(k - 1) * dim + j];
+    dr -= ac;
+    xnew[i] = zn - (zn - zo) * dr / r[k - 1];
+  }
+  for (int i = 0; i < bins - 1; ++i) xmat[i * dim + j] = xnew[i];
+  xmat[(bins - 1) * dim + j] = 1.0;
+}
+
+// Fresh grid: all edges of bin 0 at 1, rebinned from one bin to `bins`
+// (VEGASData::ClearAll + InitGridDependent, MVEGAS.h:72-84, 163-187).
+__global__ void k_vegas_grid_init(double *xmat, int bins, int dim) {
+  extern __shared__ double sm[];
+  const int j = threadIdx.x;
+  if (j >= dim) return;
+  double *r = sm + j * 2 * bins, *xnew = r + bins;
+  for (int i = 0; i < bins; ++i) {
+    r[i]              = 1.0;
+    xmat[i * dim + j] = (i == 0) ? 1.0 : 0.0;
+  }
+  rebin_dim(bins, dim, j, 1.0 / bins, r, xnew, xmat);
+}
+
+cudaError_t launch_vegas_grid_init(double *xmat, int bins, int dim, cudaStream_t st) {
+  k_vegas_grid_init<<<1, dim, 2 * bins * dim * sizeof(double), st>>>(xmat, bins, dim);
+  return cudaGetLastError();
+}
+
+// Smoothing of the f^2 histogram and damped rebinning
+// (VEGASData::OptimizeGrid, include/Graniitti/MVEGAS.h:107-142).
+__global__ void k_vegas_refine(double *xmat, double *f2mat, int bins, int dim, double lambda) {
+  extern __shared__ double sm[];
+  const int j = threadIdx.x;
+  if (j >= dim) return;
+  double *r = sm + j * 2 * bins, *xnew = r + bins;
+  const double EPS = 1.0e-30;
+  double zo = f2mat[0 * dim + j], zn = f2mat[1 * dim + j];
+  f2mat[j]  = (zo + zn) / 2.0;
+  double d  = f2mat[j];
+  for (int i = 2; i < bins; ++i) {
+    const double ac          = zo + zn;
+    zo                       = zn;
+    zn                       = f2mat[i * dim + j];
+    f2mat[(i - 1) * dim + j] = (ac + zn) / 3.0;
+    d += f2mat[(i - 1) * dim + j];
+  }
+  f2mat[(bins - 1) * dim + j] = (zo + zn) / 2.0;
+  d += f2mat[(bins - 1) * dim + j];
+  double ac = 0.0;
+  for (int i = 0; i < bins; ++i) {
+    double v = f2mat[i * dim + j];
+    if (v < EPS) v = EPS;
+    f2mat[i * dim + j] = v;
+    double ri = pow((1.0 - v / d) / (log(d) - log(v) + EPS), lambda);
+    if (isnan(ri) || isinf(ri)) ri = EPS;
+    r[i] = ri;
+    ac += ri;
+  }
+  rebin_dim(bins, dim, j, ac / bins, r, xnew, xmat);
+}
+
+cudaError_t launch_vegas_refine(double *xmat, double *f2mat, int bins, int dim, double lambda,
+                                cudaStream_t st) {
+  k_vegas_refine<<<1, dim, 2 * bins * dim * sizeof(double), st>>>(xmat, f2mat, bins, dim, lambda);
+  return cudaGetLastError();
+}
+
+// Regenerate the hypercube points of given indices of an iteration.
+__global__ void k_vegas_points(const double *xmat, int bins, int dim, uint64_t seed,
+                               uint32_t stream, const int64_t *idx, int64_t n, double *out) {
+  const int64_t i = static_cast<int64_t>(blockIdx.x) * blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  double u[kMaxDim];
+  philox_point(seed, stream, static_cast<uint64_t>(idx[i]), dim, u);
+  for (int j = 0; j < dim; ++j) {
+    const double zn = u[j] * bins + 1.0;
+    int          k  = max(1, min(static_cast<int>(zn), bins));
+    double       zo, ac;
+    if (k > 1) {
+      zo = xmat[(k - 1) * dim + j] - xmat[(k - 2) * dim + j];
+      ac = xmat[(k - 2) * dim + j] + (zn - k) * zo;
+    } else {
+      zo = xmat[(k - 1) * dim + j];
+      ac = (zn - k) * zo;
+    }
+    out[i * dim + j] = ac;
+  }
+}
+
+cudaError_t launch_vegas_points(const double *xmat, int bins, int dim, uint64_t seed,
+                                uint32_t stream, const int64_t *idx, int64_t n, double *u_out,
+                                cudaStream_t st) {
+  if (n <= 0) return cudaSuccess;
+  k_vegas_points<<<static_cast<unsigned>((n + 127) / 128), 128, 0, st>>>(xmat, bins, dim, seed,
+                                                                        stream, idx, n, u_out);
+  return cudaGetLastError();
+}
+
+// ---------------------------------------------------------------------------
+// Unweighting (MGraniitti::SaveEvent hit-or-miss, src/MGraniitti.cc:1651-1664).
+
+constexpr int kUwThreads = 256;
+
+int unweight_blocks(int64_t n) { return static_cast<int>((n + kUwThreads - 1) / kUwThreads); }
+
+__device__ __forceinline__ bool uw_hit(const double *f, int64_t i, double fmax, uint64_t seed,
+                                       uint32_t stream, bool &overflow) {
+  double r0, r1;
+  philox_block(seed, stream, static_cast<uint64_t>(i), 0, r0, r1);
+  const double fi = f[i];
+  overflow        = fi > fmax;
+  return !overflow && (r0 < fi / fmax);
+}
+
+__global__ void __launch_bounds__(kUwThreads)
+    k_uw_count(const double *f, int64_t n, double fmax, uint64_t seed, uint32_t stream,
+               int *blk_counts, unsigned long long *overflow) {
+  const int64_t i   = static_cast<int64_t>(blockIdx.x) * kUwThreads + threadIdx.x;
+  bool          ovf = false;
+  const bool    hit = (i < n) && uw_hit(f, i, fmax, seed, stream, ovf);
+  const int     c   = __syncthreads_count(hit);
+  const int     o   = __syncthreads_count(i < n && ovf);
+  if (threadIdx.x == 0) {
+    blk_counts[blockIdx.x] = c;
+    if (o) atomicAdd(overflow, static_cast<unsigned long long>(o));
+  }
+}
+
+// Exclusive scan of the block counts, single block (counts fit in int64).
+__global__ void k_uw_scan(int *blk_counts, int nblocks, int64_t *offsets, int64_t *total) {
+  __shared__ int64_t carry;
+  if (threadIdx.x == 0) carry = 0;
+  __syncthreads();
+  for (int base = 0; base < nblocks; base += blockDim.x) {
+    const int i = base + threadIdx.x;
+    __shared__ int64_t buf[1024];
+    buf[threadIdx.x] = (i < nblocks) ? blk_counts[i] : 0;
+    __syncthreads();
+    for (int o = 1; o < static_cast<int>(blockDim.x); o <<= 1) {
+      const int64_t v = (static_cast<int>(threadIdx.x) >= o) ? buf[threadIdx.x - o] : 0;
+      __syncthreads();
+      buf[threadIdx.x] += v;
+      __syncthreads();
+    }
+    if (i < nblocks) offsets[i] = carry + buf[threadIdx.x] - ((i < nblocks) ? blk_counts[i] : 0);
+    __syncthreads();
+    if (threadIdx.x == blockDim.x - 1) carry += buf[threadIdx.x];
+    __syncthreads();
+  }
+  if (threadIdx.x == 0) *total = carry;
+}
+
+__global__ void __launch_bounds__(kUwThreads)
+    k_uw_scatter(const double *f, int64_t n, double fmax, uint64_t seed, uint32_t stream,
+                 const int64_t *offsets, int64_t *idx_out, int64_t cap) {
+  __shared__ int warp_counts[kUwThreads / 32];
+  const int64_t i   = static_cast<int64_t>(blockIdx.x) * kUwThreads + threadIdx.x;
+  bool          ovf = false;
+  const bool    hit = (i < n) && uw_hit(f, i, fmax, seed, stream, ovf);
+  const unsigned m  = __ballot_sync(0xffffffffu, hit);
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  if (lane == 0) warp_counts[warp] = __popc(m);
+  __syncthreads();
+  int before = 0;
+  for (int w = 0; w < warp; ++w) before += warp_counts[w];
+  const int64_t pos = offsets[blockIdx.x] + before + __popc(m & ((1u << lane) - 1u));
+  if (hit && pos < cap) idx_out[pos] = i;
+}
+
+cudaError_t launch_unweight(const double *f, int64_t n, double fmax, uint64_t seed,
+                            uint32_t stream, int *blk_counts, unsigned long long *overflow,
+                            int64_t *idx_out, int64_t cap, int64_t *n_acc_dev, int nblocks,
+                            cudaStream_t st) {
+  // offsets live right after the counts' int64 area: caller sizes blk_counts for
+  // nblocks ints + nblocks int64 (aligned).
+  int64_t *offsets = reinterpret_cast<int64_t *>(
+      reinterpret_cast<char *>(blk_counts) + ((nblocks * sizeof(int) + 255) / 256) * 256);
+  k_uw_count<<<nblocks, kUwThreads, 0, st>>>(f, n, fmax, seed, stream, blk_counts, overflow);
+  k_uw_scan<<<1, 1024, 0, st>>>(blk_counts, nblocks, offsets, n_acc_dev);
+  if (idx_out)
+    k_uw_scatter<<<nblocks, kUwThreads, 0, st>>>(f, n, fmax, seed, stream, offsets, idx_out, cap);
+  return cudaGetLastError();
+}
+
+// ---------------------------------------------------------------------------
+// FP32 FMA-chain probe: 8 independent chains per thread, register resident.
+__global__ void k_fma_probe(int iters, float *sink) {
+  float a[8];
+  const float x = 1.0f + 1e-7f * threadIdx.x, y = 0.999999f;
+#pragma unroll
+  for (int k = 0; k < 8; ++k) a[k] = x + k;
+  for (int i = 0; i < iters; ++i) {
+#pragma unroll
+    for (int k = 0; k < 8; ++k) a[k] = fmaf(a[k], y, x);
+  }
+  float t = 0.f;
+#pragma unroll
+  for (int k = 0; k < 8; ++k) t += a[k];
+  if (t == 12345.678f) sink[0] = t;  // keeps the chains live
+}
+
+double fma_probe_flops(int blocks, int threads, int iters) {
+  return 2.0 * 8.0 * static_cast<double>(iters) * blocks * threads;
+}
+
+cudaError_t launch_fma_probe(int blocks, int threads, int iters, float *sink, cudaStream_t st) {
+  k_fma_probe<<<blocks, threads, 0, st>>>(iters, sink);
+  return cudaGetLastError();
+}
+
+}  // namespace grn

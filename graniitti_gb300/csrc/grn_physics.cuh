@@ -1,0 +1,378 @@
+// grn_physics.cuh — device physics of the event-weight path.
+//
+// Formulation: light-cone components p+- = E +- pz throughout. For the elastic
+// forward legs the momentum-fraction losses x1, x2 follow from longitudinal
+// momentum conservation as a rapidly convergent fixed point, and every invariant
+// (t1, t2, s13 ..., t_hat, u_hat) is a sum of same-sign terms. No quantity of order
+// sqrt(s) is subtracted from another, which is what lets the kt-loop run in FP32.
+// Reference quantities are the ones of the GRANIITTI generator: file:line cited
+// per function.
+#pragma once
+
+#include <cstdint>
+#include <cmath>
+
+#include "graniitti_gb300.h"
+
+#ifdef __CUDACC__
+#define GRN_HD __host__ __device__ __forceinline__
+#else
+#define GRN_HD inline
+#endif
+
+namespace grn {
+
+constexpr double kPi = 3.14159265358979323846264338327950288;
+
+// hbar*c in GeV m; GeV^-2 -> barn (include/Graniitti/MPDG.h:63-78).
+constexpr double kHbar     = 6.582119514E-25;
+constexpr double kCLight   = 2.99792458E8;
+constexpr double kGeV2m    = kHbar * kCLight;
+constexpr double kGeV2fm   = kGeV2m * 1E15;
+constexpr double kGeV2barn = (kGeV2m * kGeV2m) / 1E-28;
+constexpr double kMpiSoft  = 0.13957018;  // pion mass of the pomeron pion loop (MPDG.h:56)
+constexpr double kZeroEps  = 1e-12;       // log(pt_min + ZERO_EPS) (MProcess.h)
+
+// Eikonal numerics (include/Graniitti/MEikonal.h:27-40).
+constexpr double kMinKT2  = 1E-6;
+constexpr double kMaxKT2  = 25.0;
+constexpr double kMinBT   = 1E-6;
+constexpr double kMaxBT   = 10.0 / kGeV2fm;
+constexpr double kFBMinKT = 1E-9;
+constexpr double kFBMaxKT = 30.0;
+constexpr int    kFBN     = 10000;
+
+template <typename T>
+struct cx {
+  T re, im;
+};
+template <typename T>
+GRN_HD cx<T> cmul(cx<T> a, cx<T> b) {
+  return {a.re * b.re - a.im * b.im, a.re * b.im + a.im * b.re};
+}
+template <typename T>
+GRN_HD cx<T> cscale(cx<T> a, T s) {
+  return {a.re * s, a.im * s};
+}
+template <typename T>
+GRN_HD cx<T> cadd(cx<T> a, cx<T> b) {
+  return {a.re + b.re, a.im + b.im};
+}
+
+// Per-engine constants derived once on the host from grn_process_params.
+struct Consts {
+  double s, sqrt_s;
+  double L, eps;            // beam light-cone: pb1+ = pb2- = L, pb1- = pb2+ = eps = m^2/L
+  double mp2;               // forward-leg mass^2 (elastic)
+  double m3, m4, m3sq, m4sq;
+  double lnpt_lo, lnpt_hi;  // log(fpt_min + ZERO_EPS), log(fpt_max)
+  double w_const;           // every u-independent factor of the weight
+  double M2prop;            // off-shell propagator nominal mass^2 (ME4: first central mass)
+  double g2;                // (c0 / gN_P)^2
+  double gN2;               // gN_P^2
+  double eta0_re[3], eta0_im[3];  // ReggeEta(a0_k, sgn_k)
+  double lns0;              // log(s0)
+  int    n_active;          // number of active trajectories
+  int    active[3];
+};
+
+// sin(pi x), cos(pi x) without rounding pi x first.
+GRN_HD void sincos_pi(double x, double &s, double &c) {
+#ifdef __CUDA_ARCH__
+  sincospi(x, &s, &c);
+#else
+  s = std::sin(kPi * x);
+  c = std::cos(kPi * x);
+#endif
+}
+GRN_HD void sincos_pi(float x, float &s, float &c) {
+#ifdef __CUDA_ARCH__
+  sincospif(x, &s, &c);
+#else
+  s = std::sin(float(kPi) * x);
+  c = std::cos(float(kPi) * x);
+#endif
+}
+
+// ---------------------------------------------------------------------------
+// Model functions, arithmetic type T.
+
+// Double-pole proton form factor (src/MForm.cc:433-435).
+template <typename T>
+GRN_HD T proton_ff(T fc1, T fc2, T t) {
+  return T(1) / ((T(1) - t / fc1) * (T(1) - t / fc2));
+}
+
+// Off-shell meson form factor (src/MRegge.cc:1155-1174).
+template <typename T>
+GRN_HD T meson_ff(const grn_regge_params &rp, T that, T M2) {
+  const T tp = that - M2;
+  if (rp.offshellFF == 0) return exp(-T(rp.b_EXP) * fabs(tp));
+  if (rp.offshellFF == 1)
+    return exp(-T(rp.b_OREAR) * sqrt(fabs(tp) + T(rp.a_OREAR) * T(rp.a_OREAR)) +
+               T(rp.a_OREAR) * T(rp.b_OREAR));
+  return T(1) / (T(1) - tp / T(rp.b_POW));
+}
+
+// Regge propagator sum over active trajectories:
+//   sum_k ReggeEta(a0_k,sgn_k) exp(-i pi/2 ap_k t) (s/s0)^(a0_k + ap_k t)
+// (src/MRegge.cc:888-906 with src/MForm.cc:382-396), from ln s.
+template <typename T>
+GRN_HD cx<T> regge_prop(const Consts &K, const grn_regge_params &rp, T lns, T t) {
+  cx<T> M{T(0), T(0)};
+#pragma unroll
+  for (int k = 0; k < 3; ++k) {
+    if (!K.active[k]) continue;
+    const T mag = exp((T(rp.a0[k]) + T(rp.ap[k]) * t) * (lns - T(K.lns0)));
+    T sn, cs;
+    sincos_pi(-T(0.5) * T(rp.ap[k]) * t, sn, cs);
+    const cx<T> ph{cs * mag, sn * mag};
+    M = cadd(M, cmul(cx<T>{T(K.eta0_re[k]), T(K.eta0_im[k])}, ph));
+  }
+  return M;
+}
+
+// ---------------------------------------------------------------------------
+// Born (tree-level) kinematics of p p -> p (a b) p in the <C> class, FP64.
+struct Born {
+  // forward legs
+  double p1x, p1y, p2x, p2y;   // transverse momenta
+  double pt1sq, pt2sq;
+  double x1, x2;               // light-cone momentum-fraction losses
+  double p1p, p1m, p2p, p2m;   // light-cone components (+, -)
+  // central pair
+  double p3x, p3y, p4x, p4y;
+  double p3p, p3m, p4p, p4m;
+  double mt3, mt4, y3, y4;
+  double kt;                   // |q| of the difference momentum
+  // invariants
+  double t1, t2, s13, s14, s23, s24, that, uhat, m2;
+};
+
+// Forward-leg light-cone solution given the central pair's P+, P- and the two
+// forward transverse masses^2 (elastic legs): longitudinal conservation
+//   x1 = (P+ - eps)/L + mT2^2/((1-x2) L^2),  x2 = (P- - eps)/L + mT1^2/((1-x1) L^2).
+// Same physical root as kinematics::SolvePz (include/Graniitti/MKinematics.h:220)
+// picks (forward-going legs, MContinuum.cc:375-380).
+template <typename T>
+GRN_HD bool solve_x(T a1, T a2, T c1, T c2, T &x1, T &x2) {
+  x1 = a1;
+  x2 = a2;
+#pragma unroll
+  for (int it = 0; it < 3; ++it) {
+    const T n1 = a1 + c2 / (T(1) - x2);
+    const T n2 = a2 + c1 / (T(1) - x1);
+    x1         = n1;
+    x2         = n2;
+  }
+  return (x1 > T(0)) && (x2 > T(0)) && (x1 < T(1)) && (x2 < T(1));
+}
+
+// BNRandomKin + BNBuildKin + GetLorentzScalars for Kf = 2
+// (src/MContinuum.cc:276-435, src/MProcess.cc:1499-1584).
+GRN_HD bool born_kinematics(const grn_process_params &P, const Consts &K, const double *u,
+                            Born &b) {
+  const grn_gencuts &g = P.gcuts;
+  const double pt1 = exp(K.lnpt_lo + (K.lnpt_hi - K.lnpt_lo) * u[0]);
+  const double pt2 = exp(K.lnpt_lo + (K.lnpt_hi - K.lnpt_lo) * u[1]);
+  double s1, c1, s2, c2, sk, ck;
+  sincos_pi(2.0 * u[2], s1, c1);
+  sincos_pi(2.0 * u[3], s2, c2);
+  const double kt = g.kt_min + (g.kt_max - g.kt_min) * u[4];
+  sincos_pi(2.0 * u[5], sk, ck);
+  b.y3 = g.rap_min + (g.rap_max - g.rap_min) * u[6];
+  b.y4 = g.rap_min + (g.rap_max - g.rap_min) * u[7];
+  b.kt = kt;
+
+  b.p1x = pt1 * c1;
+  b.p1y = pt1 * s1;
+  b.p2x = pt2 * c2;
+  b.p2y = pt2 * s2;
+  b.pt1sq = b.p1x * b.p1x + b.p1y * b.p1y;
+  b.pt2sq = b.p2x * b.p2x + b.p2y * b.p2y;
+  // Central pair transverse momenta from the linear system (MContinuum.cc:438-550).
+  const double wx = b.p1x + b.p2x, wy = b.p1y + b.p2y;
+  const double qx = kt * ck, qy = kt * sk;
+  b.p3x = 0.5 * (qx - wx);
+  b.p3y = 0.5 * (qy - wy);
+  b.p4x = 0.5 * (-qx - wx);
+  b.p4y = 0.5 * (-qy - wy);
+  b.mt3 = sqrt(K.m3sq + b.p3x * b.p3x + b.p3y * b.p3y);
+  b.mt4 = sqrt(K.m4sq + b.p4x * b.p4x + b.p4y * b.p4y);
+  const double e3 = exp(b.y3), e4 = exp(b.y4);
+  b.p3p = b.mt3 * e3;
+  b.p3m = b.mt3 / e3;
+  b.p4p = b.mt4 * e4;
+  b.p4m = b.mt4 / e4;
+  const double Pp = b.p3p + b.p4p, Pm = b.p3m + b.p4m;
+  if (0.5 * (Pp + Pm) > K.sqrt_s) return false;  // crude energy check (MContinuum.cc:373)
+
+  const double mT1sq = K.mp2 + b.pt1sq, mT2sq = K.mp2 + b.pt2sq;
+  const double L2    = K.L * K.L;
+  if (!solve_x((Pp - K.eps) / K.L, (Pm - K.eps) / K.L, mT1sq / L2, mT2sq / L2, b.x1, b.x2))
+    return false;
+  b.p1p = (1.0 - b.x1) * K.L;
+  b.p1m = mT1sq / b.p1p;
+  b.p2m = (1.0 - b.x2) * K.L;
+  b.p2p = mT2sq / b.p2m;
+
+  // Invariants: (pa + pb)^2 = ma^2 + mb^2 + pa+ pb- + pa- pb+ - 2 paT.pbT
+  b.t1  = -(b.pt1sq + b.x1 * b.x1 * K.mp2) / (1.0 - b.x1);
+  b.t2  = -(b.pt2sq + b.x2 * b.x2 * K.mp2) / (1.0 - b.x2);
+  b.s13 = K.mp2 + K.m3sq + b.p1p * b.p3m + b.p1m * b.p3p - 2.0 * (b.p1x * b.p3x + b.p1y * b.p3y);
+  b.s14 = K.mp2 + K.m4sq + b.p1p * b.p4m + b.p1m * b.p4p - 2.0 * (b.p1x * b.p4x + b.p1y * b.p4y);
+  b.s23 = K.mp2 + K.m3sq + b.p2p * b.p3m + b.p2m * b.p3p - 2.0 * (b.p2x * b.p3x + b.p2y * b.p3y);
+  b.s24 = K.mp2 + K.m4sq + b.p2p * b.p4m + b.p2m * b.p4p - 2.0 * (b.p2x * b.p4x + b.p2y * b.p4y);
+  b.m2  = K.m3sq + K.m4sq + b.p3p * b.p4m + b.p3m * b.p4p - 2.0 * (b.p3x * b.p4x + b.p3y * b.p4y);
+  // t_hat = (q1 - p3)^2 with q1 = pb1 - p1: (q1+ - p3+) = p4+ - eps + p2+ by conservation.
+  {
+    const double dp = b.p4p - K.eps + b.p2p;
+    const double dm = K.eps - b.p1m - b.p3m;
+    const double tx = b.p1x + b.p3x, ty = b.p1y + b.p3y;
+    b.that = dp * dm - (tx * tx + ty * ty);
+  }
+  {
+    const double dp = b.p3p - K.eps + b.p2p;
+    const double dm = K.eps - b.p1m - b.p4m;
+    const double tx = b.p1x + b.p4x, ty = b.p1y + b.p4y;
+    b.uhat = dp * dm - (tx * tx + ty * ty);
+  }
+  return true;
+}
+
+// Fiducial cuts (MProcess::CommonCuts + FindDecayCuts, src/MProcess.cc:1085-1154).
+GRN_HD bool fiducial_cuts(const grn_process_params &P, const Consts &K, const Born &b) {
+  const grn_fidcuts &f = P.fcuts;
+  if (!f.active) return true;
+  const double at1 = fabs(b.t1), at2 = fabs(b.t2);
+  if (!(at1 >= f.ft_min && at1 <= f.ft_max && at2 >= f.ft_min && at2 <= f.ft_max)) return false;
+  const double M  = sqrt(fmax(b.m2, 0.0));
+  const double Y  = 0.5 * log((b.p3p + b.p4p) / (b.p3m + b.p4m));
+  const double sx = b.p3x + b.p4x, sy = b.p3y + b.p4y;
+  const double Pt = sqrt(sx * sx + sy * sy);
+  if (!(M >= f.M_min && M <= f.M_max && Y >= f.Y_min && Y <= f.Y_max && Pt >= f.Pt_min &&
+        Pt <= f.Pt_max))
+    return false;
+  bool ok = true;
+  const double px[2] = {b.p3x, b.p4x}, py[2] = {b.p3y, b.p4y};
+  const double mt[2] = {b.mt3, b.mt4}, y[2] = {b.y3, b.y4};
+#pragma unroll
+  for (int k = 0; k < 2; ++k) {
+    const double pt  = sqrt(px[k] * px[k] + py[k] * py[k]);
+    const double pz  = mt[k] * sinh(y[k]);
+    const double eta = asinh(pz / pt);
+    if (!(pt >= f.pt_min && pt <= f.pt_max && mt[k] >= f.Et_min && mt[k] <= f.Et_max &&
+          eta >= f.eta_min && eta <= f.eta_max && y[k] >= f.rap_min && y[k] <= f.rap_max))
+      ok = false;
+  }
+  return ok;
+}
+
+// Regge continuum amplitude of a 2-body central state, sign +1
+// (MRegge::ME4, src/MRegge.cc:394-438; PomPomProtonVertex 637-644), from the
+// invariants. Used for the FP64 Born amplitude and, with T = float, per loop point.
+template <typename T>
+GRN_HD cx<T> regge_me4(const grn_process_params &P, const Consts &K, T t1, T t2, T lns13, T lns14,
+                       T lns23, T lns24, T that, T uhat) {
+  const grn_regge_params &rp = P.regge;
+  const T M2  = T(K.M2prop);
+  const T ffa = meson_ff<T>(rp, that, M2);
+  const T ffb = meson_ff<T>(rp, uhat, M2);
+  const T Xt  = ffa * ffa / (that - M2);
+  const T Xu  = ffb * ffb / (uhat - M2);
+  const T vtx = T(K.gN2) * proton_ff<T>(T(P.soft.fc1), T(P.soft.fc2), t1) *
+                proton_ff<T>(T(P.soft.fc1), T(P.soft.fc2), t2) * T(K.g2);
+  if (K.n_active == 1) {
+    // One trajectory: both channels share the phase exp(-i pi ap (t1+t2)/2).
+    const int k  = K.active[0] ? 0 : (K.active[1] ? 1 : 2);
+    const T   a1 = T(rp.a0[k]) + T(rp.ap[k]) * t1;
+    const T   a2 = T(rp.a0[k]) + T(rp.ap[k]) * t2;
+    const T   l0 = T(K.lns0);
+    const T   mt = exp(a1 * (lns13 - l0) + a2 * (lns24 - l0)) * Xt +
+                 exp(a1 * (lns14 - l0) + a2 * (lns23 - l0)) * Xu;
+    T sn, cs;
+    sincos_pi(-T(0.5) * T(rp.ap[k]) * (t1 + t2), sn, cs);
+    const cx<T> e0{T(K.eta0_re[k]), T(K.eta0_im[k])};
+    const cx<T> e2 = cmul(e0, e0);
+    return cscale(cmul(e2, cx<T>{cs, sn}), vtx * mt);
+  }
+  const cx<T> At = cscale(cmul(regge_prop<T>(K, rp, lns13, t1), regge_prop<T>(K, rp, lns24, t2)),
+                          Xt);
+  const cx<T> Au = cscale(cmul(regge_prop<T>(K, rp, lns14, t1), regge_prop<T>(K, rp, lns23, t2)),
+                          Xu);
+  return cscale(cadd(At, Au), vtx);
+}
+
+// Bare amplitude at one kt-loop point: forward legs p1T - k, p2T + k with the
+// tree-level central pair (for Kf = 2 the pair is unchanged because p1T + p2T is
+// loop invariant; MContinuum::LoopKinematics, src/MContinuum.cc:94-161).
+// Returns false when the point is kinematically invalid (the reference skips it).
+template <typename T>
+struct LoopEvent {
+  T p1x, p1y, p2x, p2y;     // tree-level forward transverse momenta
+  T p3x, p3y, p4x, p4y;
+  T p3p, p3m, p4p, p4m;
+  T a1, a2;                 // (P+ - eps)/L, (P- - eps)/L
+  T invL, invL2, L, eps, mp2, m3sq, m4sq;
+};
+
+template <typename T>
+GRN_HD bool loop_point_amp(const grn_process_params &P, const Consts &K, const LoopEvent<T> &e,
+                           T kx, T ky, cx<T> &A) {
+  const T q1x = e.p1x - kx, q1y = e.p1y - ky;
+  const T q2x = e.p2x + kx, q2y = e.p2y + ky;
+  const T pt1sq = q1x * q1x + q1y * q1y;
+  const T pt2sq = q2x * q2x + q2y * q2y;
+  const T mT1sq = e.mp2 + pt1sq, mT2sq = e.mp2 + pt2sq;
+  T x1, x2;
+  if (!solve_x<T>(e.a1, e.a2, mT1sq * e.invL2, mT2sq * e.invL2, x1, x2)) return false;
+  const T p1p = (T(1) - x1) * e.L;
+  const T p1m = mT1sq / p1p;
+  const T p2m = (T(1) - x2) * e.L;
+  const T p2p = mT2sq / p2m;
+  const T t1  = -(pt1sq + x1 * x1 * e.mp2) / (T(1) - x1);
+  const T t2  = -(pt2sq + x2 * x2 * e.mp2) / (T(1) - x2);
+  const T s13 = e.mp2 + e.m3sq + p1p * e.p3m + p1m * e.p3p - T(2) * (q1x * e.p3x + q1y * e.p3y);
+  const T s14 = e.mp2 + e.m4sq + p1p * e.p4m + p1m * e.p4p - T(2) * (q1x * e.p4x + q1y * e.p4y);
+  const T s23 = e.mp2 + e.m3sq + p2p * e.p3m + p2m * e.p3p - T(2) * (q2x * e.p3x + q2y * e.p3y);
+  const T s24 = e.mp2 + e.m4sq + p2p * e.p4m + p2m * e.p4p - T(2) * (q2x * e.p4x + q2y * e.p4y);
+  T that, uhat;
+  {
+    const T dp = e.p4p - e.eps + p2p;
+    const T dm = e.eps - p1m - e.p3m;
+    const T tx = q1x + e.p3x, ty = q1y + e.p3y;
+    that       = dp * dm - (tx * tx + ty * ty);
+  }
+  {
+    const T dp = e.p3p - e.eps + p2p;
+    const T dm = e.eps - p1m - e.p4m;
+    const T tx = q1x + e.p4x, ty = q1y + e.p4y;
+    uhat       = dp * dm - (tx * tx + ty * ty);
+  }
+  A = regge_me4<T>(P, K, t1, t2, log(s13), log(s14), log(s23), log(s24), that, uhat);
+  return true;
+}
+
+template <typename T>
+GRN_HD void make_loop_event(const Consts &K, const Born &b, LoopEvent<T> &e) {
+  e.p1x = T(b.p1x); e.p1y = T(b.p1y); e.p2x = T(b.p2x); e.p2y = T(b.p2y);
+  e.p3x = T(b.p3x); e.p3y = T(b.p3y); e.p4x = T(b.p4x); e.p4y = T(b.p4y);
+  e.p3p = T(b.p3p); e.p3m = T(b.p3m); e.p4p = T(b.p4p); e.p4m = T(b.p4m);
+  e.a1 = T((b.p3p + b.p4p - K.eps) / K.L);
+  e.a2 = T((b.p3m + b.p4m - K.eps) / K.L);
+  e.L = T(K.L); e.invL2 = T(1.0 / (K.L * K.L)); e.invL = T(1.0 / K.L);
+  e.eps = T(K.eps); e.mp2 = T(K.mp2); e.m3sq = T(K.m3sq); e.m4sq = T(K.m4sq);
+}
+
+// u-independent part of the weight and the u-dependent Jacobians
+// (MContinuum::EventWeight, BNPhaseSpaceWeight, BNIntegralVolume and
+// ForwardVolume; src/MContinuum.cc:164-193, 619-656; src/MProcess.cc:1390-1415).
+GRN_HD double weight_jacobian(const Consts &K, const Born &b) {
+  const double E1 = 0.5 * (b.p1p + b.p1m), pz1 = 0.5 * (b.p1p - b.p1m);
+  const double E2 = 0.5 * (b.p2p + b.p2m), pz2 = 0.5 * (b.p2p - b.p2m);
+  const double J  = 1.0 / fabs(pz1 / E1 - pz2 / E2);
+  const double pt1 = sqrt(b.pt1sq), pt2 = sqrt(b.pt2sq);
+  return K.w_const * (pt1 / (2.0 * E1)) * (pt2 / (2.0 * E2)) * J * b.kt * pt1 * pt2;
+}
+
+}  // namespace grn

@@ -1,0 +1,222 @@
+"""Host-side mirror of the generator's process / driver interface over the C ABI.
+
+Engine      one process on one GPU: event weights (MProcess::EventWeight in batch),
+            eikonal tables (MEikonal), VEGAS primitives and unweighting.
+Graniitti   the MGraniitti flow: ReadInput(card, process) -> Initialize() (eikonal
+            tables when screening is on, VEGAS integration) -> GetXS() ->
+            Generate(n) unweighted events.
+
+Arrays are numpy (host) or anything exposing data_ptr() with a CUDA device
+(torch tensors); host arrays are staged by the library.
+"""
+import ctypes
+
+import numpy as np
+
+from . import _abi
+from . import card as _card
+
+FP64 = _abi.GRN_PREC_FP64
+MIXED = _abi.GRN_PREC_MIXED
+
+
+def _ptr(a):
+    if a is None:
+        return None
+    if hasattr(a, "data_ptr"):
+        return ctypes.c_void_p(a.data_ptr())
+    if not a.flags["C_CONTIGUOUS"]:
+        raise ValueError("array must be C-contiguous")
+    return a.ctypes.data_as(ctypes.c_void_p)
+
+
+class Engine:
+    def __init__(self, params, device=0):
+        self.lib = _abi.load_library()
+        self.params = params
+        h = ctypes.c_void_p()
+        _abi.check(self.lib.grn_create(ctypes.byref(params), device, ctypes.byref(h)))
+        self.h = h
+        self.dim = self.lib.grn_dim(h)
+
+    def close(self):
+        if getattr(self, "h", None):
+            self.lib.grn_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    @property
+    def stream(self):
+        return self.lib.grn_engine_stream(self.h)
+
+    # -- event weights ------------------------------------------------------
+    def event_weights(self, u, prec=FP64, w=None, flags=None):
+        if hasattr(u, "data_ptr"):
+            n = u.shape[0]
+            _abi.check(self.lib.grn_event_weights(self.h, _ptr(u), n, self.dim, _ptr(w),
+                                                  _ptr(flags), prec))
+            return w, flags
+        u = np.ascontiguousarray(u, dtype=np.float64)
+        n = u.shape[0]
+        if u.shape[1] != self.dim:
+            raise ValueError("u must have %d columns" % self.dim)
+        w = np.zeros(n) if w is None else w
+        flags = np.zeros(n, dtype=np.uint8) if flags is None else flags
+        _abi.check(self.lib.grn_event_weights(self.h, _ptr(u), n, self.dim, _ptr(w), _ptr(flags),
+                                              prec))
+        return w, flags
+
+    def event_kinematics(self, u):
+        u = np.ascontiguousarray(u, dtype=np.float64)
+        n = u.shape[0]
+        p4 = np.zeros((n, 4, 4))
+        ts = np.zeros((n, 2))
+        fl = np.zeros(n, dtype=np.uint8)
+        _abi.check(self.lib.grn_event_kinematics(self.h, _ptr(u), n, self.dim, _ptr(p4), _ptr(ts),
+                                                 _ptr(fl)))
+        return p4, ts, fl
+
+    def uniforms(self, seed, n, dim=None, first=0, stream=0):
+        dim = dim or self.dim
+        out = np.zeros((n, dim))
+        _abi.check(self.lib.grn_uniforms(self.h, seed, stream, first, n, dim, _ptr(out)))
+        return out
+
+    # -- eikonal ------------------------------------------------------------
+    def eikonal_build(self, n_bt=0, n_kt2=0):
+        _abi.check(self.lib.grn_eikonal_build(self.h, n_bt, n_kt2))
+
+    def eikonal_xs(self):
+        t, e, i = ctypes.c_double(), ctypes.c_double(), ctypes.c_double()
+        _abi.check(self.lib.grn_eikonal_xs(self.h, ctypes.byref(t), ctypes.byref(e),
+                                           ctypes.byref(i)))
+        return t.value, e.value, i.value
+
+    def eikonal_tables(self, n_bt, n_kt2):
+        mbt = np.zeros((n_bt + 1, 3))
+        msa = np.zeros((n_kt2 + 1, 3))
+        _abi.check(self.lib.grn_eikonal_get(self.h, _ptr(mbt), _ptr(msa)))
+        return mbt, msa
+
+    def eikonal_set(self, mbt, msa):
+        mbt = np.ascontiguousarray(mbt, dtype=np.float64)
+        msa = np.ascontiguousarray(msa, dtype=np.float64)
+        _abi.check(self.lib.grn_eikonal_set(self.h, mbt.shape[0] - 1, _ptr(mbt), msa.shape[0] - 1,
+                                            _ptr(msa)))
+
+    # -- VEGAS --------------------------------------------------------------
+    def vegas_init(self, vp):
+        self.vp = vp
+        _abi.check(self.lib.grn_vegas_init(self.h, ctypes.byref(vp)))
+
+    def vegas_iteration(self, mode=1, refine=True, iter_id=1):
+        r = _abi.VegasResult()
+        _abi.check(self.lib.grn_vegas_iteration(self.h, mode, 1 if refine else 0, iter_id,
+                                                ctypes.byref(r)))
+        return r
+
+    def vegas_integrate(self, vp):
+        self.vp = vp
+        r = _abi.VegasResult()
+        _abi.check(self.lib.grn_vegas_integrate(self.h, ctypes.byref(vp), ctypes.byref(r)))
+        return r
+
+    def vegas_clear(self):
+        _abi.check(self.lib.grn_vegas_clear(self.h))
+
+    def vegas_grid(self):
+        x = np.zeros((self.vp.bins, self.dim))
+        _abi.check(self.lib.grn_vegas_get_grid(self.h, _ptr(x)))
+        return x
+
+    def vegas_set_grid(self, xmat):
+        xmat = np.ascontiguousarray(xmat, dtype=np.float64)
+        _abi.check(self.lib.grn_vegas_set_grid(self.h, _ptr(xmat)))
+
+    def unweight(self, fmax, seed=7, cap=0):
+        na, no = ctypes.c_int64(), ctypes.c_int64()
+        idx = np.zeros(max(cap, 1), dtype=np.int64)
+        _abi.check(self.lib.grn_unweight(self.h, fmax, seed, ctypes.byref(na), ctypes.byref(no),
+                                         _ptr(idx) if cap > 0 else None, cap))
+        return na.value, no.value, idx[:min(na.value, cap)]
+
+    def vegas_points(self, idx):
+        idx = np.ascontiguousarray(idx, dtype=np.int64)
+        out = np.zeros((idx.shape[0], self.dim))
+        _abi.check(self.lib.grn_vegas_points(self.h, _ptr(idx), idx.shape[0], _ptr(out)))
+        return out
+
+
+class Graniitti:
+    """MGraniitti-style driver (src/MGraniitti.cc) over the GPU engine."""
+
+    def __init__(self, device=0):
+        self.device = device
+        self.engine = None
+        self.card = None
+        self.vp = None
+        self.result = None
+        self.prec = FP64
+
+    def ReadInput(self, inputfile, cmd_PROCESS=None):
+        self.card = _card.read_card(inputfile)
+        self.params = _card.build_params(self.card, cmd_PROCESS)
+        self.vp = _card.vegas_params(self.card, prec=self.prec)
+        self.engine = Engine(self.params, self.device)
+
+    def SetVegasParam(self, **kw):
+        for k, v in kw.items():
+            setattr(self.vp, "lambda_" if k == "LAMBDA" else k.lower(), v)
+
+    def SetPrecision(self, prec):
+        self.prec = prec
+        if self.vp is not None:
+            self.vp.prec = prec
+
+    def Initialize(self):
+        if self.params.screening:
+            self.engine.eikonal_build()
+        self.result = self.engine.vegas_integrate(self.vp)
+        return self.result
+
+    def GetXS(self):
+        return self.result.sigma, self.result.sigma_err
+
+    def Generate(self, nevents, seed=11, max_iter=1000):
+        """Unweighted events: generation-mode VEGAS passes (frozen grid) with
+        hit-or-miss against the integration's max weight (MGraniitti.cc:1131-1134,
+        1651-1664). Returns (points, n_trials, n_overflow)."""
+        fmax = self.result.maxf
+        pts, trials, ovf = [], 0, 0
+        it = 0
+        while sum(len(p) for p in pts) < nevents and it < max_iter:
+            self.engine.vegas_iteration(mode=2, refine=False, iter_id=0x40000000 + it)
+            cap = int(self.vp.ncall)
+            na, no, idx = self.engine.unweight(fmax, seed=seed + it, cap=cap)
+            need = nevents - sum(len(p) for p in pts)
+            idx = idx[:need]
+            pts.append(self.engine.vegas_points(idx))
+            trials += int(self.vp.ncall) if need >= na else int(idx[-1]) + 1
+            ovf += no
+            it += 1
+        return np.concatenate(pts) if pts else np.zeros((0, 8)), trials, ovf
+
+
+def kernel_timing(engine, reset=True):
+    """(total ms, launches) of the VEGAS sampling kernel since the last reset."""
+    ms, n = ctypes.c_double(), ctypes.c_int64()
+    _abi.check(engine.lib.grn_kernel_timing(engine.h, 1 if reset else 0, ctypes.byref(ms),
+                                            ctypes.byref(n)))
+    return ms.value, n.value
+
+
+def fp32_peak(device=0):
+    lib = _abi.load_library()
+    t = ctypes.c_double()
+    _abi.check(lib.grn_fp32_peak(device, ctypes.byref(t)))
+    return t.value

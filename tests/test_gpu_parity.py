@@ -1,0 +1,140 @@
+"""GPU parity through the C ABI: the CUDA path against the reference's golden
+vectors and against the CPU oracle on the same seeded inputs."""
+import os
+
+import numpy as np
+import pytest
+
+import philox_np
+from conftest import GOLDEN
+from oracle import oracle_api as orc
+
+pytestmark = pytest.mark.gpu
+
+# FP64 path: the GPU's light-cone formulation vs the reference's 4-vector one.
+TOL_FP64_REF = 5e-10
+TOL_FP64_ORC = 5e-10
+# FP32 kt-loop with compensated sums vs FP64 (spec bound 1e-5 relative).
+TOL_MIXED = 1e-5
+
+
+def _load(name):
+    return np.load(os.path.join(GOLDEN, name))
+
+
+def _engine(P):
+    import graniitti_gb300 as g
+    return g.Engine(P, 0)
+
+
+def _rel(w, wr):
+    nz = wr > 0
+    assert np.array_equal(w > 0, nz)
+    return np.abs(w[nz] - wr[nz]) / wr[nz]
+
+
+def test_uniforms_bit_exact(gpu, params):
+    e = _engine(params)
+    a = e.uniforms(seed=0xDEADBEEF12345, n=100000, first=(1 << 40) + 3, stream=77)
+    b = philox_np.uniforms(0xDEADBEEF12345, 100000, 8, first=(1 << 40) + 3, stream=77)
+    assert np.array_equal(a, b)
+
+
+@pytest.mark.parametrize("name,ff", [("c1_tune0_weights.npz", 2), ("c1_expff_weights.npz", 0),
+                                     ("c1_orearff_weights.npz", 1), ("c1_edge_weights.npz", 2)])
+def test_tree_weights_vs_reference(gpu, params, name, ff):
+    import graniitti_gb300 as g
+    gl = _load(name)
+    params.regge.offshellFF = ff
+    try:
+        e = _engine(params)
+        w, fl = e.event_weights(gl["u"], prec=g.FP64)
+        wo, flo = orc.weights(params, gl["u"])
+    finally:
+        params.regge.offshellFF = 2
+    assert np.array_equal(fl & 1, gl["kin"])
+    kin = gl["kin"] == 1
+    assert np.array_equal(((fl >> 1) & 1)[kin], gl["fid"][kin])
+    assert np.array_equal(fl, flo)
+    assert _rel(w, gl["w"]).max() < TOL_FP64_REF
+    assert _rel(w, wo).max() < TOL_FP64_ORC
+
+
+def test_tree_weights_vs_oracle_large(gpu, params):
+    """2^18 fresh points, weights and flags against the oracle."""
+    import graniitti_gb300 as g
+    e = _engine(params)
+    u = e.uniforms(seed=99, n=1 << 18)
+    w, fl = e.event_weights(u, prec=g.FP64)
+    wo, flo = orc.weights(params, u, nthreads=16)
+    assert np.array_equal(fl, flo)
+    assert _rel(w, wo).max() < TOL_FP64_ORC
+    # mixed precision does not change the tree level (FP64 Born)
+    wm, _ = e.event_weights(u, prec=g.MIXED)
+    assert np.array_equal(wm, w)
+
+
+def test_kinematics_vs_reference(gpu, params):
+    gl = _load("c1_tune0_weights.npz")
+    e = _engine(params)
+    p4, ts, fl = e.event_kinematics(gl["u"])
+    kin = gl["kin"] == 1
+    scale = np.abs(gl["p4"]).max(axis=2, keepdims=True)
+    assert (np.abs(p4 - gl["p4"])[kin] / scale[kin]).max() < 1e-12
+    big = kin & (np.abs(gl["t1"]) > 1e-2)
+    assert np.max(np.abs(ts[big, 0] - gl["t1"][big]) / np.abs(gl["t1"][big])) < 1e-8
+
+
+def test_eikonal_tables_vs_reference(gpu, params_screened):
+    g = _load("eikonal_nbt1024_nkt10000.npz")
+    e = _engine(params_screened)
+    e.eikonal_build(1024, 10000)
+    xs = np.array(e.eikonal_xs())
+    assert np.max(np.abs(xs / g["xs"] - 1)) < 1e-12
+    mbt, msa = e.eikonal_tables(1024, 10000)
+    for mine, ref in ((mbt, g["mbt"]), (msa, g["msa"])):
+        assert np.max(np.abs(mine[:, 0] - ref[:, 0]) / np.maximum(1, np.abs(ref[:, 0]))) < 1e-13
+        z, zr = mine[:, 1] + 1j * mine[:, 2], ref[:, 1] + 1j * ref[:, 2]
+        assert np.max(np.abs(z - zr)) / np.max(np.abs(zr)) < 1e-12
+
+
+@pytest.mark.parametrize("name", ["c2_screened_63x33_weights.npz", "c2_screened_15x12_weights.npz"])
+def test_screened_weights_vs_reference(gpu, params_screened, name):
+    import graniitti_gb300 as g
+    gl = _load(name)
+    t = _load("eikonal_nbt1024_nkt10000.npz")
+    P = params_screened
+    P.loop.n_kt, P.loop.n_phi = int(gl["loop_kt"]), int(gl["loop_phi"])
+    P.loop.kt_max = float(gl["loop_ktmax"])
+    e = _engine(P)
+    e.eikonal_set(t["mbt"], t["msa"])  # the reference's own tables
+    w, fl = e.event_weights(gl["u"], prec=g.FP64)
+    assert np.array_equal(fl & 1, gl["kin"])
+    assert _rel(w, gl["w"]).max() < 1e-9
+    wm, _ = e.event_weights(gl["u"], prec=g.MIXED)
+    assert _rel(wm, w).max() < TOL_MIXED
+    # GPU-built tables give the same weights
+    e2 = _engine(P)
+    e2.eikonal_build(1024, 10000)
+    w2, _ = e2.event_weights(gl["u"], prec=g.FP64)
+    assert _rel(w2, gl["w"]).max() < 1e-9
+
+
+def test_screened_mixed_vs_oracle_c2_grid(gpu, params_screened):
+    """Configuration of the benchmark: 63 x 33 loop intervals, kt <= 3 GeV,
+    1024 b-points; FP32 compensated loop against the FP64 oracle."""
+    import graniitti_gb300 as g
+    P = params_screened
+    P.loop.n_kt, P.loop.n_phi, P.loop.kt_max = 63, 33, 3.0
+    e = _engine(P)
+    e.eikonal_build(1024, 10000)
+    _, msa = e.eikonal_tables(1024, 10000)
+    u = e.uniforms(seed=5, n=2048)
+    wm, fm = e.event_weights(u, prec=g.MIXED)
+    w64, f64 = e.event_weights(u, prec=g.FP64)
+    wo, fo = orc.weights(P, u, msa=msa, nthreads=16)
+    assert np.array_equal(fm, fo) and np.array_equal(f64, fo)
+    assert _rel(w64, wo).max() < 1e-9
+    r = _rel(wm, wo)
+    print("mixed-precision screened weights: max rel %.3e, median %.3e" % (r.max(), np.median(r)))
+    assert r.max() < TOL_MIXED

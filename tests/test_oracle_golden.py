@@ -1,0 +1,104 @@
+"""The CPU oracle against golden vectors produced by the unmodified reference.
+
+These pins are what make the oracle trustworthy as the checker of the GPU path.
+"""
+import json
+import os
+
+import numpy as np
+import pytest
+
+from conftest import GOLDEN
+from oracle import oracle_api as orc
+
+# Reference and oracle solve the forward-leg kinematics with different (equivalent)
+# formulas; the reference's own rounding noise reaches ~1e-10 on weights.
+W_TOL = 5e-10
+
+
+def _load(name):
+    return np.load(os.path.join(GOLDEN, name))
+
+
+def _check_weights(w, fl, g, tol=W_TOL):
+    assert np.array_equal(fl & 1, g["kin"]), "kinematics flags differ"
+    kin = g["kin"] == 1
+    assert np.array_equal(((fl >> 1) & 1)[kin], g["fid"][kin]), "fiducial flags differ"
+    wr = g["w"]
+    assert np.array_equal(w > 0, wr > 0)
+    nz = wr > 0
+    rel = np.abs(w[nz] - wr[nz]) / wr[nz]
+    assert rel.max() < tol, rel.max()
+    return rel
+
+
+@pytest.mark.parametrize("name,ff", [("c1_tune0_weights.npz", 2), ("c1_expff_weights.npz", 0),
+                                     ("c1_orearff_weights.npz", 1), ("c1_edge_weights.npz", 2)])
+def test_tree_weights(params, name, ff):
+    g = _load(name)
+    params.regge.offshellFF = ff
+    try:
+        w, fl, rec = orc.weights(params, g["u"], with_rec=True)
+    finally:
+        params.regge.offshellFF = 2
+    _check_weights(w, fl, g)
+    kin = g["kin"] == 1
+    # forward legs and central particles (px, py, pz, E)
+    p4 = rec[:, 3:].reshape(-1, 4, 4)
+    scale = np.abs(g["p4"]).max(axis=2, keepdims=True)
+    assert (np.abs(p4 - g["p4"])[kin] / scale[kin]).max() < 1e-12
+    # invariants: m2 everywhere, t1/t2 where |t| is not cancellation-limited in the reference
+    assert np.max(np.abs(rec[kin, 2] - g["m2"][kin]) / g["m2"][kin]) < 1e-10
+    big = kin & (np.abs(g["t1"]) > 1e-2)
+    assert np.max(np.abs(rec[big, 0] - g["t1"][big]) / np.abs(g["t1"][big])) < 1e-8
+
+
+def test_eikonal_tables_and_xs(params_screened):
+    g = _load("eikonal_nbt1024_nkt10000.npz")
+    mbt, msa, xs = orc.eikonal(params_screened, 1024, 10000, nthreads=8)
+    assert np.max(np.abs(xs / g["xs"] - 1)) < 1e-12
+    for mine, ref in ((mbt, g["mbt"]), (msa, g["msa"])):
+        assert np.max(np.abs(mine[:, 0] - ref[:, 0]) / np.maximum(1, np.abs(ref[:, 0]))) < 1e-13
+        z, zr = mine[:, 1] + 1j * mine[:, 2], ref[:, 1] + 1j * ref[:, 2]
+        assert np.max(np.abs(z - zr)) / np.max(np.abs(zr)) < 1e-12
+
+
+def test_eikonal_xs_default_numerics(params_screened):
+    """Total / elastic / inelastic cross sections at 13 TeV, TUNE0, 10000 x 10000."""
+    g = _load("eikonal_default_xs.npz")
+    _, _, xs = orc.eikonal(params_screened, 10000, 10000, nthreads=8, with_msa=False)
+    assert np.max(np.abs(xs / g["xs"] - 1)) < 1e-12
+    # published-style values in mb
+    assert abs(xs[0] * 1e3 - 105.08) < 0.01 and abs(xs[1] * 1e3 - 27.00) < 0.01
+
+
+@pytest.mark.parametrize("name", ["c2_screened_63x33_weights.npz", "c2_screened_15x12_weights.npz"])
+def test_screened_weights(params_screened, name):
+    g = _load(name)
+    t = _load("eikonal_nbt1024_nkt10000.npz")
+    P = params_screened
+    P.loop.n_kt, P.loop.n_phi = int(g["loop_kt"]), int(g["loop_phi"])
+    P.loop.kt_max = float(g["loop_ktmax"])
+    w, fl = orc.weights(P, g["u"], msa=t["msa"], nthreads=4)
+    _check_weights(w, fl, g, tol=1e-9)
+
+
+def test_bessel_j0_published_values():
+    # A&S Table 9.1 values of J0 (accuracy of the published approximation ~1e-8)
+    for x, v in ((0.0, 1.0), (1.0, 0.7651976866), (2.0, 0.2238907791), (5.0, -0.1775967713),
+                 (10.0, -0.2459357645), (20.0, 0.1670246643)):
+        assert abs(orc.bessel_j0(x) - v) < 2e-8
+
+
+def test_vegas_grid_uniform_and_refine():
+    x = orc.vegas_grid_init(128, 8)
+    assert np.allclose(x, (np.arange(1, 129) / 128.0)[:, None], rtol=0, atol=1e-15)
+    # a flat f^2 histogram leaves the uniform grid unchanged
+    x2 = orc.vegas_refine(x, np.ones((128, 8)))
+    assert np.allclose(x2, x, atol=1e-12)
+    # a peaked histogram concentrates bins where f^2 is large
+    f2 = np.ones((128, 8))
+    f2[:16, 0] = 1e4
+    x3 = orc.vegas_refine(x, f2)
+    assert x3[63, 0] < x[63, 0] and np.all(np.diff(x3[:, 0]) > 0)
+    assert np.allclose(x3[:, 1:], x[:, 1:], atol=1e-12)
