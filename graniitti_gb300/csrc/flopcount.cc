@@ -21,6 +21,7 @@ struct CF {
   float v;
   CF() : v(0) {}
   CF(double x) : v(static_cast<float>(x)) {}
+  explicit operator double() const { return v; }
 };
 inline CF operator+(CF a, CF b) { g_cnt.add++; return CF(a.v + b.v); }
 inline CF operator-(CF a, CF b) { g_cnt.add++; return CF(a.v - b.v); }
@@ -33,6 +34,7 @@ inline CF exp(CF a) { g_cnt.exp++; return CF(std::exp(a.v)); }
 inline CF log(CF a) { g_cnt.log++; return CF(std::log(a.v)); }
 inline CF sqrt(CF a) { g_cnt.sqrt++; return CF(std::sqrt(a.v)); }
 inline CF fabs(CF a) { return CF(std::fabs(a.v)); }
+inline CF fmadd(CF a, CF b, CF c) { g_cnt.mul++; g_cnt.add++; return CF(std::fma(a.v, b.v, c.v)); }
 inline void sincos_pi(CF x, CF &s, CF &c) {
   g_cnt.sincos++;
   s = CF(std::sin(grn::kPi * x.v));
@@ -69,13 +71,13 @@ int main() {
     for (double &x : u) x = rnd();
     grn::Born b;
     if (!grn::born_kinematics(P, K, u, b)) continue;
-    grn::LoopEvent<CF> le;
-    grn::make_loop_event<CF>(K, b, le);
+    grn::LoopEventF<CF> le;
+    grn::make_loop_event_fast<CF>(P, K, b, le);
     for (int j = 0; j < n_kt; ++j)
       for (int i = 0; i < n_phi; ++i) {
         const double kt = 1e-4 + j * (3.0 - 1e-4) / (n_kt - 1), ph = 2 * grn::kPi * i / (n_phi - 1);
         grn::cx<CF> A;
-        grn::loop_point_amp<CF>(P, K, le, CF(kt * std::cos(ph)), CF(kt * std::sin(ph)), A);
+        grn::loop_point_amp_fast<CF>(le, CF(kt * std::cos(ph)), CF(kt * std::sin(ph)), A);
         points += 1;
       }
   }

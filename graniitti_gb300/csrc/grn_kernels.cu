@@ -130,6 +130,39 @@ __device__ cx<double> loop_integral(const KArgs &A, const Born &b, const KtNode<
   return {A.loop_norm_re * sr - A.loop_norm_im * si, A.loop_norm_re * si + A.loop_norm_im * sr};
 }
 
+// FP32 loop with the one-division point evaluation (single active trajectory).
+__device__ cx<double> loop_integral_fast(const KArgs &A, const Born &b, const KtNode<float> *skt,
+                                         const PhiNode<float> *sphi) {
+  LoopEventF<float> e;
+  make_loop_event_fast<float>(A.P, A.K, b, e);
+  float ar = 0.f, ai = 0.f, cr = 0.f, ci = 0.f;
+  for (int j = 0; j < A.n_kt_nodes; ++j) {
+    const KtNode<float> nj = skt[j];
+    float ir = 0.f, ii = 0.f, dr = 0.f, di = 0.f;
+    for (int i = 0; i < A.n_phi_nodes; ++i) {
+      const PhiNode<float> ni = sphi[i];
+      cx<float> a;
+      if (loop_point_amp_fast<float>(e, nj.kt * ni.c, nj.kt * ni.s, a)) {
+        kahan_add(ir, dr, ni.u * a.re);
+        kahan_add(ii, di, ni.u * a.im);
+      }
+    }
+    kahan_add(ar, cr, nj.cre * ir - nj.cim * ii);
+    kahan_add(ai, ci, nj.cre * ii + nj.cim * ir);
+  }
+  const double sr = double(ar) * e.escale, si = double(ai) * e.escale;
+  return {A.loop_norm_re * sr - A.loop_norm_im * si, A.loop_norm_re * si + A.loop_norm_im * sr};
+}
+
+template <typename T>
+__device__ __forceinline__ cx<double> loop_dispatch(const KArgs &A, const Born &b,
+                                                    const KtNode<T> *skt, const PhiNode<T> *sphi) {
+  if constexpr (sizeof(T) == sizeof(float)) {
+    if (A.K.n_active == 1) return loop_integral_fast(A, b, skt, sphi);
+  }
+  return loop_integral<T>(A, b, skt, sphi);
+}
+
 // One event weight (MContinuum::EventWeight, src/MContinuum.cc:164-193).
 template <typename T>
 __device__ double event_weight(const KArgs &A, const double *u, uint8_t &flags,
@@ -143,7 +176,7 @@ __device__ double event_weight(const KArgs &A, const double *u, uint8_t &flags,
                                             log(b.s23), log(b.s24), b.that, b.uhat);
     double amp2;
     if (A.P.screening) {
-      const cx<double> Al = loop_integral<T>(A, b, skt, sphi);
+      const cx<double> Al = loop_dispatch<T>(A, b, skt, sphi);
       const double     re = A0.re + Al.re, im = A0.im + Al.im;
       amp2                = re * re + im * im;
     } else {

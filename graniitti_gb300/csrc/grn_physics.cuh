@@ -353,6 +353,187 @@ GRN_HD bool loop_point_amp(const grn_process_params &P, const Consts &K, const L
   return true;
 }
 
+// ---------------------------------------------------------------------------
+// Fast FP32 kt-loop point (one division per point).
+//
+// Per event: a_i = (P+- - eps)/L and ia_i = 1/(1 - a_i). Because
+// c_i = mT^2/L^2 ~ 1e-8, the fixed point above closes after one step,
+//   x1 = a1 + c2 ia2,  x2 = a2 + c1 ia1,  1/(1 - x1) = ia1 (1 + c2 ia2 ia1),
+// with a relative truncation error ~ (c ia)^2 ~ 1e-16, below FP32 resolution.
+// The Regge exponent E = a1 ln s13 + a2 ln s24 (~20) is accumulated in
+// double-float (error-free two-sum / two-product) so that the FP32 rounding of
+// the intercept and of the sum of logarithms is not amplified by exp(); the
+// off-shell form factors of the exponential kinds are folded into E and the
+// rational factors share one division.
+
+GRN_HD float fmadd(float a, float b, float c) { return fmaf(a, b, c); }
+GRN_HD double fmadd(double a, double b, double c) { return fma(a, b, c); }
+
+// s + e = a + b exactly (Knuth two-sum).
+template <typename T>
+GRN_HD void two_sum(T a, T b, T &s, T &e) {
+  s        = a + b;
+  const T v = s - a;
+  e        = (a - (s - v)) + (b - v);
+}
+
+// exp(ah + al) for a double-float argument, as exp(ah) (1 + al).
+template <typename T>
+GRN_HD T exp_df(T ah, T al) {
+  return exp(ah) * (T(1) + al);
+}
+
+template <typename T>
+struct LoopEventF {
+  T p1x, p1y, p2x, p2y;
+  T p3x, p3y, p4x, p4y;
+  T p3p, p3m, p4p, p4m;
+  T a1, a2, ia1, ia2;
+  T L, invL, invL2, eps, mp2, m3sq, m4sq, M2;
+  T a0h, a0l, ap, ifc1, ifc2;
+  T ff_b;      // b_POW (power law), b_EXP (exponential) or b_OREAR (Orear)
+  T ff_a2;     // a_OREAR^2
+  T ff_ab;     // a_OREAR * b_OREAR
+  T is0;       // 1 / s0
+  T eshift;    // per-event exponent offset: loop exponents are taken relative to it
+  double escale;  // exp(eshift), applied in FP64 after the loop sum
+  T pre_re, pre_im;  // ReggeEta(a0)^2 gN_P^2 (c0/gN_P)^2 [x b_POW^2 for the power law]
+  int ffmode;
+};
+
+template <typename T>
+GRN_HD void make_loop_event_fast(const grn_process_params &P, const Consts &K, const Born &b,
+                                 LoopEventF<T> &e) {
+  e.p1x = T(b.p1x); e.p1y = T(b.p1y); e.p2x = T(b.p2x); e.p2y = T(b.p2y);
+  e.p3x = T(b.p3x); e.p3y = T(b.p3y); e.p4x = T(b.p4x); e.p4y = T(b.p4y);
+  e.p3p = T(b.p3p); e.p3m = T(b.p3m); e.p4p = T(b.p4p); e.p4m = T(b.p4m);
+  const double a1 = (b.p3p + b.p4p - K.eps) / K.L, a2 = (b.p3m + b.p4m - K.eps) / K.L;
+  e.a1 = T(a1); e.a2 = T(a2);
+  e.ia1 = T(1.0 / (1.0 - a1)); e.ia2 = T(1.0 / (1.0 - a2));
+  e.L = T(K.L); e.invL = T(1.0 / K.L); e.invL2 = T(1.0 / (K.L * K.L));
+  e.eps = T(K.eps); e.mp2 = T(K.mp2); e.m3sq = T(K.m3sq); e.m4sq = T(K.m4sq); e.M2 = T(K.M2prop);
+  const int k = K.active[0] ? 0 : (K.active[1] ? 1 : 2);
+  const double a0 = P.regge.a0[k];
+  e.a0h = T(a0);
+  e.a0l = T(a0 - double(T(a0)));
+  e.ap  = T(P.regge.ap[k]);
+  e.ifc1 = T(1.0 / P.soft.fc1);
+  e.ifc2 = T(1.0 / P.soft.fc2);
+  e.ffmode = P.regge.offshellFF;
+  e.is0 = T(1.0 / P.regge.s0);
+  e.ff_a2 = T(P.regge.a_OREAR * P.regge.a_OREAR);
+  e.ff_ab = T(P.regge.a_OREAR * P.regge.b_OREAR);
+  double pre = K.gN2 * K.g2;
+  if (e.ffmode == 2) {
+    e.ff_b = T(P.regge.b_POW);
+    pre *= P.regge.b_POW * P.regge.b_POW;
+  } else if (e.ffmode == 0) {
+    e.ff_b = T(P.regge.b_EXP);
+  } else {
+    e.ff_b = T(P.regge.b_OREAR);
+  }
+  const double er = K.eta0_re[k], ei = K.eta0_im[k];
+  e.pre_re = T(pre * (er * er - ei * ei));
+  e.pre_im = T(pre * (2.0 * er * ei));
+  // Born t-channel exponent (FP64) as the offset that keeps exp() in FP32 range.
+  const double l0 = log(P.regge.s0);
+  const double L13 = log(b.s13) - l0, L24 = log(b.s24) - l0;
+  double Eb = (a0 + P.regge.ap[k] * b.t1) * L13 + (a0 + P.regge.ap[k] * b.t2) * L24;
+  const double ta = b.that - K.M2prop;
+  if (e.ffmode == 0) Eb += -2.0 * P.regge.b_EXP * fabs(ta);
+  if (e.ffmode == 1)
+    Eb += 2.0 * (P.regge.a_OREAR * P.regge.b_OREAR -
+                 P.regge.b_OREAR * sqrt(fabs(ta) + P.regge.a_OREAR * P.regge.a_OREAR));
+  e.eshift = T(Eb);
+  e.escale = exp(double(e.eshift));
+}
+
+// Bare Regge amplitude at one kt-loop point, single active trajectory with
+// s0 = 1. Same quantity as loop_point_amp (src/MContinuum.cc:94-161 kinematics,
+// src/MRegge.cc:394-438 amplitude).
+template <typename T>
+GRN_HD bool loop_point_amp_fast(const LoopEventF<T> &e, T kx, T ky, cx<T> &A) {
+  const T q1x = e.p1x - kx, q1y = e.p1y - ky;
+  const T q2x = e.p2x + kx, q2y = e.p2y + ky;
+  const T pt1sq = q1x * q1x + q1y * q1y;
+  const T pt2sq = q2x * q2x + q2y * q2y;
+  const T mT1sq = e.mp2 + pt1sq, mT2sq = e.mp2 + pt2sq;
+  const T c1 = mT1sq * e.invL2, c2 = mT2sq * e.invL2;
+  const T x1 = e.a1 + c2 * e.ia2;
+  const T x2 = e.a2 + c1 * e.ia1;
+  const T r1 = e.ia1 + e.ia1 * e.ia1 * e.ia2 * c2;  // 1/(1 - x1)
+  const T r2 = e.ia2 + e.ia2 * e.ia2 * e.ia1 * c1;  // 1/(1 - x2)
+  const T p1p = (T(1) - x1) * e.L;
+  const T p1m = mT1sq * e.invL * r1;
+  const T p2m = (T(1) - x2) * e.L;
+  const T p2p = mT2sq * e.invL * r2;
+  const T t1  = -(pt1sq + x1 * x1 * e.mp2) * r1;
+  const T t2  = -(pt2sq + x2 * x2 * e.mp2) * r2;
+  const T s13 = e.mp2 + e.m3sq + p1p * e.p3m + p1m * e.p3p - T(2) * (q1x * e.p3x + q1y * e.p3y);
+  const T s14 = e.mp2 + e.m4sq + p1p * e.p4m + p1m * e.p4p - T(2) * (q1x * e.p4x + q1y * e.p4y);
+  const T s23 = e.mp2 + e.m3sq + p2p * e.p3m + p2m * e.p3p - T(2) * (q2x * e.p3x + q2y * e.p3y);
+  const T s24 = e.mp2 + e.m4sq + p2p * e.p4m + p2m * e.p4p - T(2) * (q2x * e.p4x + q2y * e.p4y);
+  T ta, tb;  // t_hat - M2, u_hat - M2
+  {
+    const T dp = e.p4p - e.eps + p2p;
+    const T dm = e.eps - p1m - e.p3m;
+    const T tx = q1x + e.p3x, ty = q1y + e.p3y;
+    ta         = dp * dm - (tx * tx + ty * ty) - e.M2;
+  }
+  {
+    const T dp = e.p3p - e.eps + p2p;
+    const T dm = e.eps - p1m - e.p4m;
+    const T tx = q1x + e.p4x, ty = q1y + e.p4y;
+    tb         = dp * dm - (tx * tx + ty * ty) - e.M2;
+  }
+  const T L13 = log(s13 * e.is0), L14 = log(s14 * e.is0), L23 = log(s23 * e.is0),
+          L24 = log(s24 * e.is0);
+  // Exponents E_t = a0 (L13 + L24) + ap (t1 L13 + t2 L24) (+ form factors), E_u likewise.
+  T St, St_l, Su, Su_l;
+  two_sum(L13, L24, St, St_l);
+  two_sum(L14, L23, Su, Su_l);
+  const T Pt_h = e.a0h * St, Pu_h = e.a0h * Su;
+  const T Et_l = fmadd(e.a0h, St, -Pt_h) + e.a0h * St_l + e.a0l * St;
+  const T Eu_l = fmadd(e.a0h, Su, -Pu_h) + e.a0h * Su_l + e.a0l * Su;
+  const T Et_h = Pt_h - e.eshift, Eu_h = Pu_h - e.eshift;  // exact: both near eshift
+  T Qt = e.ap * (t1 * L13 + t2 * L24);
+  T Qu = e.ap * (t1 * L14 + t2 * L23);
+  T num, den;
+  const T Pd = (T(1) - t1 * e.ifc1) * (T(1) - t1 * e.ifc2) * (T(1) - t2 * e.ifc1) *
+               (T(1) - t2 * e.ifc2);
+  if (e.ffmode == 2) {
+    const T Da = e.ff_b - ta, Db = e.ff_b - tb;
+    T h, l;
+    two_sum(Et_h, Qt, h, l);
+    const T Xt = exp_df(h, Et_l + l);
+    two_sum(Eu_h, Qu, h, l);
+    const T Xu = exp_df(h, Eu_l + l);
+    num = Xt * (Db * Db) * tb + Xu * (Da * Da) * ta;
+    den = Pd * (Da * Da) * (Db * Db) * ta * tb;
+  } else {
+    T fa, fb;  // 2 ln ff(t_hat), 2 ln ff(u_hat)
+    if (e.ffmode == 0) {
+      fa = T(-2) * e.ff_b * fabs(ta);
+      fb = T(-2) * e.ff_b * fabs(tb);
+    } else {
+      fa = T(2) * (e.ff_ab - e.ff_b * sqrt(fabs(ta) + e.ff_a2));
+      fb = T(2) * (e.ff_ab - e.ff_b * sqrt(fabs(tb) + e.ff_a2));
+    }
+    T h, l;
+    two_sum(Et_h, Qt + fa, h, l);
+    const T Xt = exp_df(h, Et_l + l);
+    two_sum(Eu_h, Qu + fb, h, l);
+    const T Xu = exp_df(h, Eu_l + l);
+    num = Xt * tb + Xu * ta;
+    den = Pd * ta * tb;
+  }
+  T sn, cs;
+  sincos_pi(T(-0.5) * e.ap * (t1 + t2), sn, cs);
+  const T m = num / den;
+  A = {(e.pre_re * cs - e.pre_im * sn) * m, (e.pre_re * sn + e.pre_im * cs) * m};
+  return (x1 < T(1)) && (x2 < T(1));
+}
+
 template <typename T>
 GRN_HD void make_loop_event(const Consts &K, const Born &b, LoopEvent<T> &e) {
   e.p1x = T(b.p1x); e.p1y = T(b.p1y); e.p2x = T(b.p2x); e.p2y = T(b.p2y);
