@@ -91,8 +91,9 @@ struct grn_engine {
   int                 n_kt_nodes = 0, n_phi_nodes = 0;
   double              loop_norm_im = 0.0;
 
-  // staging for host arrays
-  DevBuf d_u, d_w, d_flags, d_aux;
+  // staging for host arrays; screened work list of grn_event_weights
+  DevBuf d_u, d_w, d_flags, d_aux, d_wlist, d_wcount;
+  int    loop_blocks = 0;
 
   // VEGAS
   int         bins = 0;
@@ -100,7 +101,8 @@ struct grn_engine {
   int64_t     ncall = 0;
   uint64_t    seed = 1;
   int         nblocks = 0;
-  DevBuf      d_xmat, d_xmat_prev, d_f2mat, d_f, d_part_hist, d_part_sc, d_sc;
+  DevBuf      d_xmat, d_xmat_prev, d_f2mat, d_f, d_acc, d_parts, d_sc;
+  DevBuf      d_lidx, d_lx, d_lvw, d_lbins;  // screened work list of a VEGAS pass
   double     *h_sc = nullptr;  // pinned
   double      sumdata = 0, sumchi2 = 0, sweight = 0;
   double      maxf = 0, maxW = 0;
@@ -323,10 +325,12 @@ grn_status grn_destroy(grn_engine *e) {
   if (!e) return GRN_OK;
   cudaSetDevice(e->device);
   if (e->stream) cudaStreamSynchronize(e->stream);
-  DevBuf *bufs[] = {&e->d_mbt, &e->d_msa, &e->d_eik_nodes, &e->d_xs, &e->d_lc_kt, &e->d_lc_phi,
-                    &e->d_u, &e->d_w, &e->d_flags, &e->d_aux, &e->d_xmat, &e->d_xmat_prev,
-                    &e->d_f2mat, &e->d_f, &e->d_part_hist, &e->d_part_sc, &e->d_sc,
-                    &e->d_uw_counts, &e->d_uw_misc, &e->d_uw_idx};
+  DevBuf *bufs[] = {&e->d_mbt,   &e->d_msa,    &e->d_eik_nodes, &e->d_xs,        &e->d_lc_kt,
+                    &e->d_lc_phi, &e->d_u,     &e->d_w,         &e->d_flags,     &e->d_aux,
+                    &e->d_wlist, &e->d_wcount, &e->d_xmat,      &e->d_xmat_prev, &e->d_f2mat,
+                    &e->d_f,     &e->d_acc,    &e->d_parts,     &e->d_sc,        &e->d_lidx,
+                    &e->d_lx,    &e->d_lvw,    &e->d_lbins,     &e->d_uw_counts, &e->d_uw_misc,
+                    &e->d_uw_idx};
   for (DevBuf *b : bufs) b->release();
   if (e->h_sc) cudaFreeHost(e->h_sc);
   if (e->ev0) cudaEventDestroy(e->ev0);
@@ -448,7 +452,12 @@ grn_status grn_event_weights(grn_engine *e, const double *u, int64_t n, int32_t 
     GRN_CUDA(e->d_flags.ensure(n));
     df = e->d_flags.as<uint8_t>();
   }
-  GRN_CUDA(grn::launch_event_weights(e->args(), prec, du, n, dim, dw, df, e->stream));
+  GRN_CUDA(e->d_wlist.ensure(n * sizeof(int64_t)));
+  GRN_CUDA(e->d_wcount.ensure(sizeof(unsigned long long)));
+  if (e->loop_blocks == 0) e->loop_blocks = grn::loop_grid_blocks(e->device);
+  GRN_CUDA(grn::launch_event_weights(e->args(), prec, du, n, dim, dw, df, e->d_wlist.as<int64_t>(),
+                                     e->d_wcount.as<unsigned long long>(), e->loop_blocks,
+                                     e->stream));
   if (!dev_w)
     GRN_CUDA(cudaMemcpyAsync(w_out, dw, n * sizeof(double), cudaMemcpyDeviceToHost, e->stream));
   if (flags && !dev_f)
@@ -504,17 +513,27 @@ grn_status grn_uniforms(grn_engine *e, uint64_t seed, uint32_t stream, int64_t f
 // ---------------------------------------------------------------------------
 // VEGAS
 
+// Per-call buffers of a VEGAS pass: f values and the screened work list.
+static grn_status vegas_alloc_calls(grn_engine *e, int64_t ncall) {
+  const size_t n = static_cast<size_t>(std::max<int64_t>(ncall, 1));
+  GRN_CUDA(e->d_f.ensure(n * sizeof(double)));
+  GRN_CUDA(e->d_lidx.ensure(n * sizeof(int64_t)));
+  GRN_CUDA(e->d_lx.ensure(8 * n * sizeof(double)));
+  GRN_CUDA(e->d_lvw.ensure(n * sizeof(double)));
+  GRN_CUDA(e->d_lbins.ensure(n * sizeof(uint64_t)));
+  return GRN_OK;
+}
+
 static grn_status vegas_alloc(grn_engine *e) {
   const int nh = e->bins * e->dim;
   GRN_CUDA(e->d_xmat.ensure(nh * sizeof(double)));
   GRN_CUDA(e->d_xmat_prev.ensure(nh * sizeof(double)));
   GRN_CUDA(e->d_f2mat.ensure(nh * sizeof(double)));
   GRN_CUDA(e->d_sc.ensure(grn::VS_COUNT * sizeof(double)));
+  GRN_CUDA(e->d_acc.ensure((grn::VS_COUNT + 1) * sizeof(unsigned long long)));
+  GRN_CUDA(e->d_parts.ensure(2 * grn::kVegasSumParts * sizeof(double)));
   if (e->nblocks == 0) e->nblocks = grn::vegas_grid_blocks(e->device);
-  GRN_CUDA(e->d_part_hist.ensure(static_cast<size_t>(e->nblocks) * nh * sizeof(double)));
-  GRN_CUDA(e->d_part_sc.ensure(static_cast<size_t>(e->nblocks) * grn::VS_COUNT * sizeof(double)));
-  GRN_CUDA(e->d_f.ensure(static_cast<size_t>(std::max<int64_t>(e->ncall, 1)) * sizeof(double)));
-  return GRN_OK;
+  return vegas_alloc_calls(e, e->ncall);
 }
 
 grn_status grn_vegas_init(grn_engine *e, const grn_vegas_params *vp) {
@@ -559,12 +578,14 @@ static grn_status vegas_iteration_impl(grn_engine *e, int prec, int mode, int re
   GRN_CUDA(cudaEventRecord(e->ev0, e->stream));
   GRN_CUDA(grn::launch_vegas_sample(e->args(), prec, e->d_xmat.as<double>(), e->bins, e->dim,
                                     e->ncall, e->seed, stream_id, mode != 0, e->d_f.as<double>(),
-                                    e->d_part_hist.as<double>(), e->d_part_sc.as<double>(),
-                                    e->nblocks, e->stream));
-  GRN_CUDA(cudaEventRecord(e->ev1, e->stream));
-  GRN_CUDA(grn::launch_vegas_reduce(e->d_part_hist.as<double>(), e->d_part_sc.as<double>(),
-                                    e->nblocks, nh, e->d_f2mat.as<double>(), e->d_sc.as<double>(),
+                                    e->d_f2mat.as<double>(), e->d_acc.as<unsigned long long>(),
+                                    e->d_lidx.as<int64_t>(), e->d_lx.as<double>(),
+                                    e->d_lvw.as<double>(), e->d_lbins.as<uint64_t>(), e->nblocks,
                                     e->stream));
+  GRN_CUDA(cudaEventRecord(e->ev1, e->stream));
+  GRN_CUDA(grn::launch_vegas_reduce(e->d_f.as<double>(), e->ncall,
+                                    e->d_acc.as<unsigned long long>(), e->d_parts.as<double>(),
+                                    e->d_sc.as<double>(), e->stream));
   GRN_CUDA(cudaMemcpyAsync(e->h_sc, e->d_sc.p, grn::VS_COUNT * sizeof(double),
                            cudaMemcpyDeviceToHost, e->stream));
   if (refine)
@@ -645,7 +666,8 @@ static grn_status vegas_run(grn_engine *e, const grn_vegas_params *vp, int init,
   *factor = 1;
   if (calls != e->ncall) {
     e->ncall = calls;
-    GRN_CUDA(e->d_f.ensure(static_cast<size_t>(calls) * sizeof(double)));
+    const grn_status st = vegas_alloc_calls(e, calls);
+    if (st != GRN_OK) return st;
   }
   if (init == 0) {
     GRN_CUDA(grn::launch_vegas_grid_init(e->d_xmat.as<double>(), e->bins, e->dim, e->stream));

@@ -41,7 +41,9 @@ enum VegasScalar {
 
 // Launchers (all stream-ordered, return cudaGetLastError of the launch).
 cudaError_t launch_event_weights(const KArgs &a, int prec, const double *u, int64_t n, int dim,
-                                 double *w, uint8_t *flags, cudaStream_t st);
+                                 double *w, uint8_t *flags, int64_t *list,
+                                 unsigned long long *count, int loop_blocks, cudaStream_t st);
+int         loop_grid_blocks(int device);
 cudaError_t launch_event_kinematics(const KArgs &a, const double *u, int64_t n, int dim,
                                     double *p4, double *ts, uint8_t *flags, cudaStream_t st);
 cudaError_t launch_uniforms(uint64_t seed, uint32_t stream, int64_t first, int64_t n, int dim,
@@ -57,12 +59,18 @@ cudaError_t launch_eikonal_xs(const double *mbt, int n_bt, double *xs, cudaStrea
 // VEGAS
 int         vegas_grid_blocks(int device);
 cudaError_t launch_vegas_grid_init(double *xmat, int bins, int dim, cudaStream_t st);
+// One VEGAS pass in two stages; acc holds VS_COUNT + 1 unsigned long long
+// accumulators (the last one is the work-list length); the list arrays have
+// capacity ncall (l_x: 8 x ncall, dimension-major).
 cudaError_t launch_vegas_sample(const KArgs &a, int prec, const double *xmat, int bins, int dim,
                                 int64_t ncall, uint64_t seed, uint32_t stream, int track_max,
-                                double *f_out, double *part_hist, double *part_sc, int nblocks,
+                                double *f_out, double *f2mat, unsigned long long *acc,
+                                int64_t *l_idx, double *l_x, double *l_vw, uint64_t *l_bins,
+                                int nblocks, cudaStream_t st);
+constexpr int kVegasSumParts = 256;
+cudaError_t launch_vegas_reduce(const double *f_out, int64_t ncall,
+                                const unsigned long long *acc, double *part, double *sc,
                                 cudaStream_t st);
-cudaError_t launch_vegas_reduce(const double *part_hist, const double *part_sc, int nblocks,
-                                int nhist, double *f2mat, double *sc, cudaStream_t st);
 cudaError_t launch_vegas_refine(double *xmat, double *f2mat, int bins, int dim, double lambda,
                                 cudaStream_t st);
 cudaError_t launch_vegas_points(const double *xmat, int bins, int dim, uint64_t seed,

@@ -11,6 +11,7 @@
 //   k_unweight_*        hit-or-miss acceptance + order-preserving compaction.
 #include <cuda_runtime.h>
 
+#include <algorithm>
 #include <cstdint>
 
 #include "grn_internal.cuh"
@@ -142,7 +143,7 @@ __device__ cx<double> loop_integral_fast(const KArgs &A, const Born &b, const Kt
     for (int i = 0; i < A.n_phi_nodes; ++i) {
       const PhiNode<float> ni = sphi[i];
       cx<float> a;
-      if (loop_point_amp_fast<float>(e, nj.kt * ni.c, nj.kt * ni.s, a)) {
+      if (loop_point_amp_fast<float>(e, nj.kt * ni.c, nj.kt * ni.s, nj.kt * nj.kt, a)) {
         kahan_add(ir, dr, ni.u * a.re);
         kahan_add(ii, di, ni.u * a.im);
       }
@@ -163,34 +164,45 @@ __device__ __forceinline__ cx<double> loop_dispatch(const KArgs &A, const Born &
   return loop_integral<T>(A, b, skt, sphi);
 }
 
-// One event weight (MContinuum::EventWeight, src/MContinuum.cc:164-193).
-template <typename T>
-__device__ double event_weight(const KArgs &A, const double *u, uint8_t &flags,
-                               const KtNode<T> *skt, const PhiNode<T> *sphi) {
-  Born       b;
-  const bool kin = born_kinematics(A.P, A.K, u, b);
+// Tree-level stage of one event: kinematics, cuts and, when the process is not
+// screened, the full weight. Returns true when the event still needs the kt-loop.
+__device__ __forceinline__ bool born_stage(const KArgs &A, const double *x, Born &b, double &W,
+                                           uint8_t &flags) {
+  const bool kin = born_kinematics(A.P, A.K, x, b);
   const bool fid = kin && fiducial_cuts(A.P, A.K, b);
-  double     W   = 0.0;
-  if (kin && fid) {
-    const cx<double> A0 = regge_me4<double>(A.P, A.K, b.t1, b.t2, log(b.s13), log(b.s14),
-                                            log(b.s23), log(b.s24), b.that, b.uhat);
-    double amp2;
-    if (A.P.screening) {
-      const cx<double> Al = loop_dispatch<T>(A, b, skt, sphi);
-      const double     re = A0.re + Al.re, im = A0.im + Al.im;
-      amp2                = re * re + im * im;
-    } else {
-      amp2 = A0.re * A0.re + A0.im * A0.im;
-    }
-    W = weight_jacobian(A.K, b) * amp2;
-  }
-  bool amp_ok = true;
-  if (!isfinite(W)) {
-    W      = 0.0;
-    amp_ok = false;
-  }
   flags = (kin ? GRN_FLAG_KINEMATICS_OK : 0) | (fid ? GRN_FLAG_FIDCUTS_OK : 0) |
-          GRN_FLAG_VETOCUTS_OK | (amp_ok ? GRN_FLAG_AMPLITUDE_OK : 0);
+          GRN_FLAG_VETOCUTS_OK | GRN_FLAG_AMPLITUDE_OK;
+  W = 0.0;
+  if (!(kin && fid)) return false;
+  if (A.P.screening) return true;
+  const cx<double> A0 = regge_me4<double>(A.P, A.K, b.t1, b.t2, log(b.s13), log(b.s14),
+                                          log(b.s23), log(b.s24), b.that, b.uhat);
+  W = weight_jacobian(A.K, b) * (A0.re * A0.re + A0.im * A0.im);
+  if (!isfinite(W)) {
+    W = 0.0;
+    flags &= ~GRN_FLAG_AMPLITUDE_OK;
+  }
+  return false;
+}
+
+// Screened weight of an event that passed the cuts (MContinuum::EventWeight with
+// MProcess::S3ScreenedAmp2, src/MContinuum.cc:164-193, src/MProcess.cc:157-288).
+template <typename T>
+__device__ double screened_weight(const KArgs &A, const double *x, uint8_t &flags,
+                                  const KtNode<T> *skt, const PhiNode<T> *sphi) {
+  Born b;
+  born_kinematics(A.P, A.K, x, b);
+  const cx<double> A0 = regge_me4<double>(A.P, A.K, b.t1, b.t2, log(b.s13), log(b.s14),
+                                          log(b.s23), log(b.s24), b.that, b.uhat);
+  const cx<double> Al = loop_dispatch<T>(A, b, skt, sphi);
+  const double re = A0.re + Al.re, im = A0.im + Al.im;
+  double W = weight_jacobian(A.K, b) * (re * re + im * im);
+  flags = GRN_FLAG_KINEMATICS_OK | GRN_FLAG_FIDCUTS_OK | GRN_FLAG_VETOCUTS_OK |
+          GRN_FLAG_AMPLITUDE_OK;
+  if (!isfinite(W)) {
+    W = 0.0;
+    flags &= ~GRN_FLAG_AMPLITUDE_OK;
+  }
   return W;
 }
 
@@ -204,35 +216,89 @@ __device__ void stage_nodes(const KArgs &A, KtNode<T> *skt, PhiNode<T> *sphi) {
     sphi[i] = {T(A.lc_phi[3 * i]), T(A.lc_phi[3 * i + 1]), T(A.lc_phi[3 * i + 2])};
 }
 
+// Warp-aggregated append to a work list: the slot of this lane, or -1.
+__device__ __forceinline__ int64_t list_append(bool pred, unsigned long long *count) {
+  const unsigned act = __activemask();
+  const unsigned m   = __ballot_sync(act, pred);
+  if (m == 0u) return -1;
+  const int lane   = threadIdx.x & 31;
+  const int leader = __ffs(m) - 1;
+  unsigned long long base = 0ull;
+  if (lane == leader) base = atomicAdd(count, static_cast<unsigned long long>(__popc(m)));
+  base = __shfl_sync(act, base, leader);
+  return pred ? static_cast<int64_t>(base + __popc(m & ((1u << lane) - 1u))) : -1;
+}
+
 constexpr int kWeightThreads = 128;
 
-template <typename T>
+// Stage A over a user point array: cuts, unscreened weights, screened work list.
 __global__ void __launch_bounds__(kWeightThreads)
-    k_event_weights(const KArgs A, const double *__restrict__ u, int64_t n, int dim,
-                    double *__restrict__ w, uint8_t *__restrict__ flags) {
-  __shared__ KtNode<T>  skt[kMaxLoopNodes];
-  __shared__ PhiNode<T> sphi[kMaxLoopNodes];
-  stage_nodes<T>(A, skt, sphi);
-  __syncthreads();
+    k_weights_born(const KArgs A, const double *__restrict__ u, int64_t n, int dim,
+                   double *__restrict__ w, uint8_t *__restrict__ flags,
+                   int64_t *__restrict__ list, unsigned long long *__restrict__ count) {
   const int64_t i = static_cast<int64_t>(blockIdx.x) * blockDim.x + threadIdx.x;
   if (i >= n) return;
   double x[8];
 #pragma unroll
   for (int d = 0; d < 8; ++d) x[d] = u[i * dim + d];
+  Born       b;
+  double     W;
   uint8_t    f;
-  const double W = event_weight<T>(A, x, f, skt, sphi);
-  w[i]           = W;
-  if (flags) flags[i] = f;
+  const bool loop = born_stage(A, x, b, W, f);
+  const int64_t slot = list_append(loop, count);
+  if (loop) {
+    list[slot] = i;
+  } else {
+    w[i] = W;
+    if (flags) flags[i] = f;
+  }
+}
+
+// Stage B: the kt-loop for the listed events (every lane does a full loop).
+template <typename T>
+__global__ void __launch_bounds__(kWeightThreads)
+    k_weights_loop(const KArgs A, const double *__restrict__ u, int dim,
+                   const int64_t *__restrict__ list, const unsigned long long *__restrict__ count,
+                   double *__restrict__ w, uint8_t *__restrict__ flags) {
+  __shared__ KtNode<T>  skt[kMaxLoopNodes];
+  __shared__ PhiNode<T> sphi[kMaxLoopNodes];
+  stage_nodes<T>(A, skt, sphi);
+  __syncthreads();
+  const int64_t cnt = static_cast<int64_t>(*count);
+  for (int64_t r = static_cast<int64_t>(blockIdx.x) * blockDim.x + threadIdx.x; r < cnt;
+       r += static_cast<int64_t>(gridDim.x) * blockDim.x) {
+    const int64_t i = list[r];
+    double x[8];
+#pragma unroll
+    for (int d = 0; d < 8; ++d) x[d] = u[i * dim + d];
+    uint8_t f;
+    w[i] = screened_weight<T>(A, x, f, skt, sphi);
+    if (flags) flags[i] = f;
+  }
+}
+
+int loop_grid_blocks(int device) {
+  int sms = 0, per = 0;
+  cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, device);
+  cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, k_weights_loop<float>, kWeightThreads, 0);
+  return sms * (per < 1 ? 1 : per);
 }
 
 cudaError_t launch_event_weights(const KArgs &a, int prec, const double *u, int64_t n, int dim,
-                                 double *w, uint8_t *flags, cudaStream_t st) {
+                                 double *w, uint8_t *flags, int64_t *list,
+                                 unsigned long long *count, int loop_blocks, cudaStream_t st) {
   if (n <= 0) return cudaSuccess;
+  cudaMemsetAsync(count, 0, sizeof(unsigned long long), st);
   const unsigned blocks = static_cast<unsigned>((n + kWeightThreads - 1) / kWeightThreads);
-  if (prec == GRN_PREC_MIXED)
-    k_event_weights<float><<<blocks, kWeightThreads, 0, st>>>(a, u, n, dim, w, flags);
-  else
-    k_event_weights<double><<<blocks, kWeightThreads, 0, st>>>(a, u, n, dim, w, flags);
+  k_weights_born<<<blocks, kWeightThreads, 0, st>>>(a, u, n, dim, w, flags, list, count);
+  if (a.P.screening) {
+    if (prec == GRN_PREC_MIXED)
+      k_weights_loop<float><<<loop_blocks, kWeightThreads, 0, st>>>(a, u, dim, list, count, w,
+                                                                    flags);
+    else
+      k_weights_loop<double><<<loop_blocks, kWeightThreads, 0, st>>>(a, u, dim, list, count, w,
+                                                                     flags);
+  }
   return cudaGetLastError();
 }
 
@@ -475,158 +541,265 @@ constexpr int kVegasThreads = 128;
 constexpr int kMaxBins      = 256;
 constexpr int kMaxDim       = 8;
 
-template <typename T>
+// Map a uniform point through the VEGAS grid in shared memory
+// (MGraniitti::VEGASMultiThread, src/MGraniitti.cc:1357-1375).
+__device__ __forceinline__ double vegas_map(const double *sx, int bins, int dim, const double *u,
+                                            double *x, uint64_t &packed_bins) {
+  const double dbins = static_cast<double>(bins);
+  double       vw    = 1.0;
+  packed_bins        = 0ull;
+  for (int j = 0; j < dim; ++j) {
+    const double zn = u[j] * dbins + 1.0;
+    int          k  = static_cast<int>(zn);
+    k               = max(1, min(k, bins));
+    double zo, ac;
+    if (k > 1) {
+      zo = sx[(k - 1) * dim + j] - sx[(k - 2) * dim + j];
+      ac = sx[(k - 2) * dim + j] + (zn - k) * zo;
+    } else {
+      zo = sx[(k - 1) * dim + j];
+      ac = (zn - k) * zo;
+    }
+    x[j] = ac;
+    packed_bins |= static_cast<uint64_t>(k - 1) << (8 * j);
+    vw *= zo * dbins;
+  }
+  return vw;
+}
+
+// Block-level accumulation shared by both VEGAS stages; flushed with one global
+// atomic per non-zero entry / counter at the end of the block.
+struct VegasBlockAcc {
+  double *sf2;  // shared f^2 histogram (bins * dim)
+};
+
+__device__ __forceinline__ void hist_add(double *sf2, int dim, uint64_t packed, double f2) {
+  if (f2 == 0.0) return;
+  for (int j = 0; j < dim; ++j) {
+    const int b = static_cast<int>((packed >> (8 * j)) & 0xFFu);
+    atomicAdd(&sf2[b * dim + j], f2);
+  }
+}
+
+__device__ void flush_block(double *sf2, int nh, double *f2mat, unsigned long long *acc,
+                            const unsigned long long cnt[VS_COUNT], double maxf, double maxW) {
+  // counters: warp sums, then one atomic per warp
+  for (int c = 0; c < VS_COUNT; ++c) {
+    if (c == VS_FSUM || c == VS_F2SUM || c == VS_MAXF || c == VS_MAXW) continue;
+    unsigned long long v = cnt[c];
+    for (int o = 16; o > 0; o >>= 1) v += __shfl_down_sync(0xffffffffu, v, o);
+    if ((threadIdx.x & 31) == 0 && v) atomicAdd(&acc[c], v);
+  }
+  for (int o = 16; o > 0; o >>= 1) {
+    maxf = fmax(maxf, __shfl_down_sync(0xffffffffu, maxf, o));
+    maxW = fmax(maxW, __shfl_down_sync(0xffffffffu, maxW, o));
+  }
+  // non-negative doubles order like their bit patterns
+  if ((threadIdx.x & 31) == 0) {
+    if (maxf > 0) atomicMax(&acc[VS_MAXF], static_cast<unsigned long long>(__double_as_longlong(maxf)));
+    if (maxW > 0) atomicMax(&acc[VS_MAXW], static_cast<unsigned long long>(__double_as_longlong(maxW)));
+  }
+  __syncthreads();
+  for (int i = threadIdx.x; i < nh; i += blockDim.x)
+    if (sf2[i] != 0.0) atomicAdd(&f2mat[i], sf2[i]);
+}
+
+// Stage A of a VEGAS pass: Philox points, grid map, tree-level kinematics and cuts.
+// Rejected and unscreened events are finished here; screened events that pass
+// the cuts go to the work list (index, mapped point, VEGAS weight, bins).
 __global__ void __launch_bounds__(kVegasThreads)
-    k_vegas_sample(const KArgs A, const double *__restrict__ xmat, int bins, int dim,
-                   int64_t ncall, uint64_t seed, uint32_t stream, int track_max,
-                   double *__restrict__ f_out, double *__restrict__ part_hist,
-                   double *__restrict__ part_sc) {
+    k_vegas_born(const KArgs A, const double *__restrict__ xmat, int bins, int dim, int64_t ncall,
+                 uint64_t seed, uint32_t stream, int track_max, double *__restrict__ f_out,
+                 double *__restrict__ f2mat, unsigned long long *__restrict__ acc,
+                 int64_t *__restrict__ l_idx, double *__restrict__ l_x, double *__restrict__ l_vw,
+                 uint64_t *__restrict__ l_bins, int64_t cap) {
   extern __shared__ double dsm[];
-  double *sx  = dsm;                   // bins * dim grid
-  double *sf2 = dsm + bins * dim;      // bins * dim f^2 histogram
-  __shared__ KtNode<T>  skt[kMaxLoopNodes];
-  __shared__ PhiNode<T> sphi[kMaxLoopNodes];
-  __shared__ double     ssc[VS_COUNT];
-  stage_nodes<T>(A, skt, sphi);
-  for (int i = threadIdx.x; i < bins * dim; i += blockDim.x) {
+  double   *sx = dsm, *sf2 = dsm + bins * dim;
+  const int nh = bins * dim;
+  for (int i = threadIdx.x; i < nh; i += blockDim.x) {
     sx[i]  = xmat[i];
     sf2[i] = 0.0;
   }
-  if (threadIdx.x < VS_COUNT) ssc[threadIdx.x] = 0.0;
   __syncthreads();
-
-  double fsum = 0.0, f2sum = 0.0, maxf = 0.0, maxW = 0.0;
-  double ev = 0.0, amp_ok = 0.0, kin_ok = 0.0, fid_ok = 0.0, veto_ok = 0.0, nan = 0.0;
-  const double dbins = static_cast<double>(bins);
+  unsigned long long cnt[VS_COUNT] = {};
+  double maxf = 0.0, maxW = 0.0;
   const int64_t stride = static_cast<int64_t>(gridDim.x) * blockDim.x;
-  for (int64_t e = static_cast<int64_t>(blockIdx.x) * blockDim.x + threadIdx.x; e < ncall;
+  const int64_t nfull  = ((ncall + stride - 1) / stride) * stride;  // uniform trip count
+  for (int64_t e = static_cast<int64_t>(blockIdx.x) * blockDim.x + threadIdx.x; e < nfull;
        e += stride) {
-    double u[kMaxDim], x[kMaxDim];
-    int    ind[kMaxDim];
-    philox_point(seed, stream, static_cast<uint64_t>(e), dim, u);
-    double vw = 1.0;
-    for (int j = 0; j < dim; ++j) {
-      const double zn = u[j] * dbins + 1.0;
-      int          k  = static_cast<int>(zn);
-      k               = max(1, min(k, bins));
-      double zo, ac;
-      if (k > 1) {
-        zo = sx[(k - 1) * dim + j] - sx[(k - 2) * dim + j];
-        ac = sx[(k - 2) * dim + j] + (zn - k) * zo;
-      } else {
-        zo = sx[(k - 1) * dim + j];
-        ac = (zn - k) * zo;
+    const bool active = e < ncall;
+    bool       loop   = false;
+    double     x[kMaxDim], vw = 0.0;
+    uint64_t   pb = 0ull;
+    if (active) {
+      double u[kMaxDim];
+      philox_point(seed, stream, static_cast<uint64_t>(e), dim, u);
+      vw = vegas_map(sx, bins, dim, u, x, pb);
+      Born    b;
+      double  W;
+      uint8_t fl;
+      loop = born_stage(A, x, b, W, fl);
+      cnt[VS_EVAL] += 1;
+      cnt[VS_KIN_OK] += (fl & GRN_FLAG_KINEMATICS_OK) ? 1 : 0;
+      cnt[VS_FID_OK] += (fl & GRN_FLAG_FIDCUTS_OK) ? 1 : 0;
+      cnt[VS_VETO_OK] += 1;
+      if (!loop) {
+        const double f = W * vw;
+        f_out[e]       = f;
+        hist_add(sf2, dim, pb, f * f);
+        cnt[VS_AMP_OK] += (fl & GRN_FLAG_AMPLITUDE_OK) ? 1 : 0;
+        cnt[VS_NAN] += (fl & GRN_FLAG_AMPLITUDE_OK) ? 0 : 1;
+        if (track_max) {
+          maxf = fmax(maxf, f);
+          maxW = fmax(maxW, W);
+        }
       }
-      x[j]   = ac;
-      ind[j] = k - 1;
-      vw *= zo * dbins;
     }
-    uint8_t      fl;
-    const double W = event_weight<T>(A, x, fl, skt, sphi);
-    const double f = W * vw;
-    f_out[e]       = f;
-    const double f2 = f * f;
-    fsum += f;
-    f2sum += f2;
-    for (int j = 0; j < dim; ++j) atomicAdd(&sf2[ind[j] * dim + j], f2);
-    if (track_max) {
-      maxW = fmax(maxW, W);
-      maxf = fmax(maxf, f);
+    const int64_t slot = list_append(loop, &acc[VS_COUNT]);
+    if (loop && slot < cap) {
+      l_idx[slot] = e;
+      for (int j = 0; j < kMaxDim; ++j) l_x[static_cast<int64_t>(j) * cap + slot] = x[j];
+      l_vw[slot]   = vw;
+      l_bins[slot] = pb;
     }
-    ev += 1.0;
-    amp_ok += (fl & GRN_FLAG_AMPLITUDE_OK) ? 1.0 : 0.0;
-    kin_ok += (fl & GRN_FLAG_KINEMATICS_OK) ? 1.0 : 0.0;
-    fid_ok += (fl & GRN_FLAG_FIDCUTS_OK) ? 1.0 : 0.0;
-    veto_ok += (fl & GRN_FLAG_VETOCUTS_OK) ? 1.0 : 0.0;
-    nan += (fl & GRN_FLAG_AMPLITUDE_OK) ? 0.0 : 1.0;
   }
-  // Warp reductions (fixed shuffle order), then one lane per warp into shared.
-  for (int o = 16; o > 0; o >>= 1) {
-    fsum += __shfl_down_sync(0xffffffffu, fsum, o);
-    f2sum += __shfl_down_sync(0xffffffffu, f2sum, o);
-    maxf = fmax(maxf, __shfl_down_sync(0xffffffffu, maxf, o));
-    maxW = fmax(maxW, __shfl_down_sync(0xffffffffu, maxW, o));
-    ev += __shfl_down_sync(0xffffffffu, ev, o);
-    amp_ok += __shfl_down_sync(0xffffffffu, amp_ok, o);
-    kin_ok += __shfl_down_sync(0xffffffffu, kin_ok, o);
-    fid_ok += __shfl_down_sync(0xffffffffu, fid_ok, o);
-    veto_ok += __shfl_down_sync(0xffffffffu, veto_ok, o);
-    nan += __shfl_down_sync(0xffffffffu, nan, o);
-  }
-  __shared__ double wsc[kVegasThreads / 32][VS_COUNT];
-  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
-  if (lane == 0) {
-    wsc[warp][VS_FSUM]    = fsum;
-    wsc[warp][VS_F2SUM]   = f2sum;
-    wsc[warp][VS_MAXF]    = maxf;
-    wsc[warp][VS_MAXW]    = maxW;
-    wsc[warp][VS_EVAL]    = ev;
-    wsc[warp][VS_AMP_OK]  = amp_ok;
-    wsc[warp][VS_KIN_OK]  = kin_ok;
-    wsc[warp][VS_FID_OK]  = fid_ok;
-    wsc[warp][VS_VETO_OK] = veto_ok;
-    wsc[warp][VS_NAN]     = nan;
-  }
+  flush_block(sf2, nh, f2mat, acc, cnt, maxf, maxW);
+}
+
+// Stage B of a VEGAS pass: screened weights of the listed events.
+template <typename T>
+__global__ void __launch_bounds__(kVegasThreads)
+    k_vegas_loop(const KArgs A, int bins, int dim, int track_max, double *__restrict__ f_out,
+                 double *__restrict__ f2mat, unsigned long long *__restrict__ acc,
+                 const int64_t *__restrict__ l_idx, const double *__restrict__ l_x,
+                 const double *__restrict__ l_vw, const uint64_t *__restrict__ l_bins,
+                 int64_t cap) {
+  extern __shared__ double dsm[];
+  double *sf2 = dsm;
+  __shared__ KtNode<T>  skt[kMaxLoopNodes];
+  __shared__ PhiNode<T> sphi[kMaxLoopNodes];
+  const int nh = bins * dim;
+  for (int i = threadIdx.x; i < nh; i += blockDim.x) sf2[i] = 0.0;
+  stage_nodes<T>(A, skt, sphi);
   __syncthreads();
-  if (threadIdx.x < VS_COUNT) {
-    const int c = threadIdx.x;
-    double    v = wsc[0][c];
-    for (int w = 1; w < kVegasThreads / 32; ++w)
-      v = (c == VS_MAXF || c == VS_MAXW) ? fmax(v, wsc[w][c]) : v + wsc[w][c];
-    part_sc[static_cast<int64_t>(blockIdx.x) * VS_COUNT + c] = v;
+  unsigned long long cnt[VS_COUNT] = {};
+  double maxf = 0.0, maxW = 0.0;
+  const int64_t n      = min(static_cast<int64_t>(acc[VS_COUNT]), cap);
+  const int64_t stride = static_cast<int64_t>(gridDim.x) * blockDim.x;
+  for (int64_t r = static_cast<int64_t>(blockIdx.x) * blockDim.x + threadIdx.x; r < n;
+       r += stride) {
+    double x[kMaxDim];
+    for (int j = 0; j < kMaxDim; ++j) x[j] = l_x[static_cast<int64_t>(j) * cap + r];
+    uint8_t      fl;
+    const double W = screened_weight<T>(A, x, fl, skt, sphi);
+    const double f = W * l_vw[r];
+    f_out[l_idx[r]] = f;
+    hist_add(sf2, dim, l_bins[r], f * f);
+    cnt[VS_AMP_OK] += (fl & GRN_FLAG_AMPLITUDE_OK) ? 1 : 0;
+    cnt[VS_NAN] += (fl & GRN_FLAG_AMPLITUDE_OK) ? 0 : 1;
+    if (track_max) {
+      maxf = fmax(maxf, f);
+      maxW = fmax(maxW, W);
+    }
   }
-  double *ph = part_hist + static_cast<int64_t>(blockIdx.x) * bins * dim;
-  for (int i = threadIdx.x; i < bins * dim; i += blockDim.x) ph[i] = sf2[i];
+  // all lanes of a warp reach the flush together (the loop above has no barrier)
+  __syncwarp();
+  flush_block(sf2, nh, f2mat, acc, cnt, maxf, maxW);
 }
 
 int vegas_grid_blocks(int device) {
-  int sms = 0;
+  int sms = 0, per = 0;
   cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, device);
-  int per = 0;
-  cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, k_vegas_sample<float>, kVegasThreads,
-                                                2 * kMaxBins * kMaxDim * sizeof(double));
+  cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, k_vegas_loop<float>, kVegasThreads,
+                                                kMaxBins * kMaxDim * sizeof(double));
   if (per < 1) per = 1;
   return sms * per;
 }
 
 cudaError_t launch_vegas_sample(const KArgs &a, int prec, const double *xmat, int bins, int dim,
                                 int64_t ncall, uint64_t seed, uint32_t stream, int track_max,
-                                double *f_out, double *part_hist, double *part_sc, int nblocks,
-                                cudaStream_t st) {
-  const size_t sm = 2 * static_cast<size_t>(bins) * dim * sizeof(double);
-  if (prec == GRN_PREC_MIXED)
-    k_vegas_sample<float><<<nblocks, kVegasThreads, sm, st>>>(
-        a, xmat, bins, dim, ncall, seed, stream, track_max, f_out, part_hist, part_sc);
-  else
-    k_vegas_sample<double><<<nblocks, kVegasThreads, sm, st>>>(
-        a, xmat, bins, dim, ncall, seed, stream, track_max, f_out, part_hist, part_sc);
+                                double *f_out, double *f2mat, unsigned long long *acc,
+                                int64_t *l_idx, double *l_x, double *l_vw, uint64_t *l_bins,
+                                int nblocks, cudaStream_t st) {
+  const int nh = bins * dim;
+  cudaMemsetAsync(f2mat, 0, nh * sizeof(double), st);
+  cudaMemsetAsync(acc, 0, (VS_COUNT + 1) * sizeof(unsigned long long), st);
+  int sms = 0, dev = 0;
+  cudaGetDevice(&dev);
+  cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+  const int64_t want = (ncall + kVegasThreads - 1) / kVegasThreads;
+  const int     ba   = static_cast<int>(std::min<int64_t>(want, static_cast<int64_t>(sms) * 16));
+  k_vegas_born<<<ba, kVegasThreads, 2 * nh * sizeof(double), st>>>(
+      a, xmat, bins, dim, ncall, seed, stream, track_max, f_out, f2mat, acc, l_idx, l_x, l_vw,
+      l_bins, ncall);
+  if (a.P.screening) {
+    if (prec == GRN_PREC_MIXED)
+      k_vegas_loop<float><<<nblocks, kVegasThreads, nh * sizeof(double), st>>>(
+          a, bins, dim, track_max, f_out, f2mat, acc, l_idx, l_x, l_vw, l_bins, ncall);
+    else
+      k_vegas_loop<double><<<nblocks, kVegasThreads, nh * sizeof(double), st>>>(
+          a, bins, dim, track_max, f_out, f2mat, acc, l_idx, l_x, l_vw, l_bins, ncall);
+  }
   return cudaGetLastError();
 }
 
-// Sum the per-block partials in block order (deterministic for a fixed grid).
-__global__ void k_vegas_reduce(const double *__restrict__ part_hist,
-                               const double *__restrict__ part_sc, int nblocks, int nhist,
-                               double *__restrict__ f2mat, double *__restrict__ sc) {
-  const int i = blockIdx.x * blockDim.x + threadIdx.x;
-  if (i < nhist) {
-    double v = 0.0;
-    for (int b = 0; b < nblocks; ++b) v += part_hist[static_cast<int64_t>(b) * nhist + i];
-    f2mat[i] = v;
-  } else if (i < nhist + VS_COUNT) {
-    const int c = i - nhist;
-    double    v = part_sc[c];
-    for (int b = 1; b < nblocks; ++b) {
-      const double x = part_sc[static_cast<int64_t>(b) * VS_COUNT + c];
-      v = (c == VS_MAXF || c == VS_MAXW) ? fmax(v, x) : v + x;
+// Deterministic sums of f and f^2 (fixed chunks, fixed tree order), then the
+// counters of the pass into the scalar record sc[VS_COUNT].
+constexpr int kSumBlocks = 256, kSumThreads = 256;
+
+__global__ void __launch_bounds__(kSumThreads)
+    k_vegas_sums(const double *__restrict__ f, int64_t n, double *__restrict__ part) {
+  __shared__ double s1[kSumThreads], s2[kSumThreads];
+  const int64_t chunk = (n + gridDim.x - 1) / gridDim.x;
+  const int64_t a = blockIdx.x * chunk, b = min(n, a + chunk);
+  double v1 = 0.0, v2 = 0.0;
+  for (int64_t i = a + threadIdx.x; i < b; i += kSumThreads) {
+    const double x = f[i];
+    v1 += x;
+    v2 += x * x;
+  }
+  s1[threadIdx.x] = v1;
+  s2[threadIdx.x] = v2;
+  __syncthreads();
+  for (int o = kSumThreads / 2; o > 0; o >>= 1) {
+    if (threadIdx.x < o) {
+      s1[threadIdx.x] += s1[threadIdx.x + o];
+      s2[threadIdx.x] += s2[threadIdx.x + o];
     }
-    sc[c] = v;
+    __syncthreads();
+  }
+  if (threadIdx.x == 0) {
+    part[2 * blockIdx.x]     = s1[0];
+    part[2 * blockIdx.x + 1] = s2[0];
   }
 }
 
-cudaError_t launch_vegas_reduce(const double *part_hist, const double *part_sc, int nblocks,
-                                int nhist, double *f2mat, double *sc, cudaStream_t st) {
-  const int n = nhist + VS_COUNT;
-  k_vegas_reduce<<<(n + 255) / 256, 256, 0, st>>>(part_hist, part_sc, nblocks, nhist, f2mat, sc);
+__global__ void k_vegas_finish(const double *__restrict__ part, int nparts,
+                               const unsigned long long *__restrict__ acc,
+                               double *__restrict__ sc) {
+  if (threadIdx.x != 0) return;
+  double v1 = 0.0, v2 = 0.0;
+  for (int i = 0; i < nparts; ++i) {
+    v1 += part[2 * i];
+    v2 += part[2 * i + 1];
+  }
+  sc[VS_FSUM]    = v1;
+  sc[VS_F2SUM]   = v2;
+  sc[VS_MAXF]    = __longlong_as_double(static_cast<long long>(acc[VS_MAXF]));
+  sc[VS_MAXW]    = __longlong_as_double(static_cast<long long>(acc[VS_MAXW]));
+  sc[VS_EVAL]    = static_cast<double>(acc[VS_EVAL]);
+  sc[VS_AMP_OK]  = static_cast<double>(acc[VS_AMP_OK]);
+  sc[VS_KIN_OK]  = static_cast<double>(acc[VS_KIN_OK]);
+  sc[VS_FID_OK]  = static_cast<double>(acc[VS_FID_OK]);
+  sc[VS_VETO_OK] = static_cast<double>(acc[VS_VETO_OK]);
+  sc[VS_NAN]     = static_cast<double>(acc[VS_NAN]);
+}
+
+cudaError_t launch_vegas_reduce(const double *f_out, int64_t ncall,
+                                const unsigned long long *acc, double *part, double *sc,
+                                cudaStream_t st) {
+  k_vegas_sums<<<kSumBlocks, kSumThreads, 0, st>>>(f_out, ncall, part);
+  k_vegas_finish<<<1, 32, 0, st>>>(part, kSumBlocks, acc, sc);
   return cudaGetLastError();
 }
 

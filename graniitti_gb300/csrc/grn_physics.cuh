@@ -354,50 +354,56 @@ GRN_HD bool loop_point_amp(const grn_process_params &P, const Consts &K, const L
 }
 
 // ---------------------------------------------------------------------------
-// Fast FP32 kt-loop point (one division per point).
+// Fast FP32 kt-loop point: increments over the tree-level point.
 //
-// Per event: a_i = (P+- - eps)/L and ia_i = 1/(1 - a_i). Because
-// c_i = mT^2/L^2 ~ 1e-8, the fixed point above closes after one step,
-//   x1 = a1 + c2 ia2,  x2 = a2 + c1 ia1,  1/(1 - x1) = ia1 (1 + c2 ia2 ia1),
-// with a relative truncation error ~ (c ia)^2 ~ 1e-16, below FP32 resolution.
-// The Regge exponent E = a1 ln s13 + a2 ln s24 (~20) is accumulated in
-// double-float (error-free two-sum / two-product) so that the FP32 rounding of
-// the intercept and of the sum of logarithms is not amplified by exp(); the
-// off-shell form factors of the exponential kinds are folded into E and the
-// rational factors share one division.
+// Every loop-point quantity is written as its tree-level value (FP64 per event)
+// plus an increment that is an explicit polynomial in the loop momentum k:
+//   pT1'^2 - pT1^2 = -2 p1T.k + k^2,   pT2'^2 - pT2^2 = 2 p2T.k + k^2,
+//   x1 = a1 + c2 ia2, x2 = a2 + c1 ia1, 1/(1 - x1) = ia1 (1 + c2 ia2 ia1)
+// with a_i = (P+- - eps)/L, ia_i = 1/(1 - a_i), c_i = mT_i^2/L^2 ~ 1e-8 (the
+// fixed point of solve_x closes after one step; truncation ~ (c ia)^2 ~ 1e-16),
+// and s13' = s13 + ds13, ..., so that ln s13' = ln s13 + ln(1 + ds13/s13). The
+// Regge exponent is then the Born exponent (kept in FP64, applied after the loop
+// sum) plus an O(1) increment, and every FP32 operand is an O(1) quantity: the
+// MUFU fast log2/exp2 paths keep ~1e-7 absolute accuracy on the exponent. The
+// off-shell form factors and proton form factors share the point's one division.
 
-GRN_HD float fmadd(float a, float b, float c) { return fmaf(a, b, c); }
-GRN_HD double fmadd(double a, double b, double c) { return fma(a, b, c); }
-
-// s + e = a + b exactly (Knuth two-sum).
-template <typename T>
-GRN_HD void two_sum(T a, T b, T &s, T &e) {
-  s        = a + b;
-  const T v = s - a;
-  e        = (a - (s - v)) + (b - v);
+GRN_HD float fast_log(float x) {
+#ifdef __CUDA_ARCH__
+  return __logf(x);
+#else
+  return std::log(x);
+#endif
 }
-
-// exp(ah + al) for a double-float argument, as exp(ah) (1 + al).
-template <typename T>
-GRN_HD T exp_df(T ah, T al) {
-  return exp(ah) * (T(1) + al);
+GRN_HD float fast_exp(float x) {
+#ifdef __CUDA_ARCH__
+  return __expf(x);
+#else
+  return std::exp(x);
+#endif
 }
 
 template <typename T>
 struct LoopEventF {
-  T p1x, p1y, p2x, p2y;
-  T p3x, p3y, p4x, p4y;
+  // tree-level transverse momenta
+  T p1x, p1y, p2x, p2y, p3x, p3y, p4x, p4y;
   T p3p, p3m, p4p, p4m;
-  T a1, a2, ia1, ia2;
-  T L, invL, invL2, eps, mp2, m3sq, m4sq, M2;
-  T a0h, a0l, ap, ifc1, ifc2;
-  T ff_b;      // b_POW (power law), b_EXP (exponential) or b_OREAR (Orear)
-  T ff_a2;     // a_OREAR^2
-  T ff_ab;     // a_OREAR * b_OREAR
-  T is0;       // 1 / s0
-  T eshift;    // per-event exponent offset: loop exponents are taken relative to it
-  double escale;  // exp(eshift), applied in FP64 after the loop sum
-  T pre_re, pre_im;  // ReggeEta(a0)^2 gN_P^2 (c0/gN_P)^2 [x b_POW^2 for the power law]
+  T ia1, ia2, q1c, q2c;      // 1/(1-a), ia1^2 ia2, ia2^2 ia1
+  T L, invL, invL2, mp2, M2;
+  T x10, x20, r10, r20;      // tree-level x and 1/(1-x) (linear closure)
+  T mT1s0, mT2s0, T1n0, T2n0;  // mT^2 and pT^2 + x^2 mp^2 at k = 0
+  T t10, t20;
+  T is13, is14, is23, is24;  // 1/s at k = 0
+  T L13, L14, L23, L24;      // ln(s/s0) at k = 0
+  T a10, a20, ap;            // trajectory at t1, t2 (k = 0) and slope
+  T dpa0, dma0, dpb0, dmb0;  // light-cone factors of t_hat, u_hat at k = 0
+  T c3x, c3y, c4x, c4y;      // p1T + p3T, p1T + p4T
+  T ifc1, ifc2;
+  T ff_b, ff_a2, ff_ab;
+  T fa0, fb0;                // 2 ln ff(t_hat), 2 ln ff(u_hat) at k = 0 (exponential kinds)
+  T rho_t, rho_u;            // exp(E_t0 - Emax), exp(E_u0 - Emax)
+  T pre_re, pre_im;          // couplings x ReggeEta^2 x tree-level phase [x b_POW^2]
+  double escale;             // exp(Emax), applied in FP64 after the loop sum
   int ffmode;
 };
 
@@ -408,110 +414,128 @@ GRN_HD void make_loop_event_fast(const grn_process_params &P, const Consts &K, c
   e.p3x = T(b.p3x); e.p3y = T(b.p3y); e.p4x = T(b.p4x); e.p4y = T(b.p4y);
   e.p3p = T(b.p3p); e.p3m = T(b.p3m); e.p4p = T(b.p4p); e.p4m = T(b.p4m);
   const double a1 = (b.p3p + b.p4p - K.eps) / K.L, a2 = (b.p3m + b.p4m - K.eps) / K.L;
-  e.a1 = T(a1); e.a2 = T(a2);
-  e.ia1 = T(1.0 / (1.0 - a1)); e.ia2 = T(1.0 / (1.0 - a2));
-  e.L = T(K.L); e.invL = T(1.0 / K.L); e.invL2 = T(1.0 / (K.L * K.L));
-  e.eps = T(K.eps); e.mp2 = T(K.mp2); e.m3sq = T(K.m3sq); e.m4sq = T(K.m4sq); e.M2 = T(K.M2prop);
+  const double ia1 = 1.0 / (1.0 - a1), ia2 = 1.0 / (1.0 - a2);
+  e.ia1 = T(ia1); e.ia2 = T(ia2); e.q1c = T(ia1 * ia1 * ia2); e.q2c = T(ia2 * ia2 * ia1);
+  const double L = K.L, invL = 1.0 / K.L, invL2 = invL * invL, mp2 = K.mp2;
+  e.L = T(L); e.invL = T(invL); e.invL2 = T(invL2); e.mp2 = T(mp2); e.M2 = T(K.M2prop);
+  // k = 0 values of the linear closure (same formulas as the loop point, in FP64)
+  const double mT1s = mp2 + b.pt1sq, mT2s = mp2 + b.pt2sq;
+  const double c1 = mT1s * invL2, c2 = mT2s * invL2;
+  const double x1 = a1 + c2 * ia2, x2 = a2 + c1 * ia1;
+  const double r1 = ia1 + ia1 * ia1 * ia2 * c2, r2 = ia2 + ia2 * ia2 * ia1 * c1;
+  const double p1p = (1.0 - x1) * L, p1m = mT1s * invL * r1;
+  const double p2m = (1.0 - x2) * L, p2p = mT2s * invL * r2;
+  const double T1n = b.pt1sq + x1 * x1 * mp2, T2n = b.pt2sq + x2 * x2 * mp2;
+  const double t1 = -T1n * r1, t2 = -T2n * r2;
+  e.x10 = T(x1); e.x20 = T(x2); e.r10 = T(r1); e.r20 = T(r2);
+  e.mT1s0 = T(mT1s); e.mT2s0 = T(mT2s); e.T1n0 = T(T1n); e.T2n0 = T(T2n);
+  e.t10 = T(t1); e.t20 = T(t2);
+  auto sinv = [&](double pp, double pm, double mq, double qp, double qm, double mr, double dot) {
+    return mq + mr + pp * qm + pm * qp - 2.0 * dot;
+  };
+  const double s13 = sinv(p1p, p1m, mp2, b.p3p, b.p3m, K.m3sq, b.p1x * b.p3x + b.p1y * b.p3y);
+  const double s14 = sinv(p1p, p1m, mp2, b.p4p, b.p4m, K.m4sq, b.p1x * b.p4x + b.p1y * b.p4y);
+  const double s23 = sinv(p2p, p2m, mp2, b.p3p, b.p3m, K.m3sq, b.p2x * b.p3x + b.p2y * b.p3y);
+  const double s24 = sinv(p2p, p2m, mp2, b.p4p, b.p4m, K.m4sq, b.p2x * b.p4x + b.p2y * b.p4y);
+  e.is13 = T(1.0 / s13); e.is14 = T(1.0 / s14); e.is23 = T(1.0 / s23); e.is24 = T(1.0 / s24);
+  const double l0 = log(P.regge.s0);
+  const double L13 = log(s13) - l0, L14 = log(s14) - l0, L23 = log(s23) - l0, L24 = log(s24) - l0;
+  e.L13 = T(L13); e.L14 = T(L14); e.L23 = T(L23); e.L24 = T(L24);
   const int k = K.active[0] ? 0 : (K.active[1] ? 1 : 2);
-  const double a0 = P.regge.a0[k];
-  e.a0h = T(a0);
-  e.a0l = T(a0 - double(T(a0)));
-  e.ap  = T(P.regge.ap[k]);
-  e.ifc1 = T(1.0 / P.soft.fc1);
-  e.ifc2 = T(1.0 / P.soft.fc2);
+  const double a0 = P.regge.a0[k], ap = P.regge.ap[k];
+  e.ap = T(ap);
+  e.a10 = T(a0 + ap * t1); e.a20 = T(a0 + ap * t2);
+  e.dpa0 = T(b.p4p - K.eps + p2p); e.dma0 = T(K.eps - p1m - b.p3m);
+  e.dpb0 = T(b.p3p - K.eps + p2p); e.dmb0 = T(K.eps - p1m - b.p4m);
+  e.c3x = T(b.p1x + b.p3x); e.c3y = T(b.p1y + b.p3y);
+  e.c4x = T(b.p1x + b.p4x); e.c4y = T(b.p1y + b.p4y);
+  e.ifc1 = T(1.0 / P.soft.fc1); e.ifc2 = T(1.0 / P.soft.fc2);
   e.ffmode = P.regge.offshellFF;
-  e.is0 = T(1.0 / P.regge.s0);
   e.ff_a2 = T(P.regge.a_OREAR * P.regge.a_OREAR);
   e.ff_ab = T(P.regge.a_OREAR * P.regge.b_OREAR);
   double pre = K.gN2 * K.g2;
+  // tree-level exponents E = a1 L13 + a2 L24 (+ exponential form factors)
+  double Et = (a0 + ap * t1) * L13 + (a0 + ap * t2) * L24;
+  double Eu = (a0 + ap * t1) * L14 + (a0 + ap * t2) * L23;
+  const double ta = (b.p4p - K.eps + p2p) * (K.eps - p1m - b.p3m) -
+                    ((b.p1x + b.p3x) * (b.p1x + b.p3x) + (b.p1y + b.p3y) * (b.p1y + b.p3y)) - K.M2prop;
+  const double tb = (b.p3p - K.eps + p2p) * (K.eps - p1m - b.p4m) -
+                    ((b.p1x + b.p4x) * (b.p1x + b.p4x) + (b.p1y + b.p4y) * (b.p1y + b.p4y)) - K.M2prop;
+  double fa = 0, fb = 0;
   if (e.ffmode == 2) {
     e.ff_b = T(P.regge.b_POW);
     pre *= P.regge.b_POW * P.regge.b_POW;
   } else if (e.ffmode == 0) {
     e.ff_b = T(P.regge.b_EXP);
+    fa = -2.0 * P.regge.b_EXP * fabs(ta);
+    fb = -2.0 * P.regge.b_EXP * fabs(tb);
   } else {
     e.ff_b = T(P.regge.b_OREAR);
+    fa = 2.0 * (P.regge.a_OREAR * P.regge.b_OREAR -
+                P.regge.b_OREAR * sqrt(fabs(ta) + P.regge.a_OREAR * P.regge.a_OREAR));
+    fb = 2.0 * (P.regge.a_OREAR * P.regge.b_OREAR -
+                P.regge.b_OREAR * sqrt(fabs(tb) + P.regge.a_OREAR * P.regge.a_OREAR));
   }
+  e.fa0 = T(fa); e.fb0 = T(fb);
+  Et += fa;
+  Eu += fb;
+  const double Em = Et > Eu ? Et : Eu;
+  e.rho_t = T(exp(Et - Em)); e.rho_u = T(exp(Eu - Em));
+  e.escale = exp(Em);
+  // couplings x ReggeEta(a0)^2 x exp(-i pi ap (t1 + t2)/2) at k = 0
   const double er = K.eta0_re[k], ei = K.eta0_im[k];
-  e.pre_re = T(pre * (er * er - ei * ei));
-  e.pre_im = T(pre * (2.0 * er * ei));
-  // Born t-channel exponent (FP64) as the offset that keeps exp() in FP32 range.
-  const double l0 = log(P.regge.s0);
-  const double L13 = log(b.s13) - l0, L24 = log(b.s24) - l0;
-  double Eb = (a0 + P.regge.ap[k] * b.t1) * L13 + (a0 + P.regge.ap[k] * b.t2) * L24;
-  const double ta = b.that - K.M2prop;
-  if (e.ffmode == 0) Eb += -2.0 * P.regge.b_EXP * fabs(ta);
-  if (e.ffmode == 1)
-    Eb += 2.0 * (P.regge.a_OREAR * P.regge.b_OREAR -
-                 P.regge.b_OREAR * sqrt(fabs(ta) + P.regge.a_OREAR * P.regge.a_OREAR));
-  e.eshift = T(Eb);
-  e.escale = exp(double(e.eshift));
+  const double e2r = er * er - ei * ei, e2i = 2.0 * er * ei;
+  double sn, cs;
+  sincos_pi(-0.5 * ap * (t1 + t2), sn, cs);
+  e.pre_re = T(pre * (e2r * cs - e2i * sn));
+  e.pre_im = T(pre * (e2r * sn + e2i * cs));
 }
 
-// Bare Regge amplitude at one kt-loop point, single active trajectory with
-// s0 = 1. Same quantity as loop_point_amp (src/MContinuum.cc:94-161 kinematics,
-// src/MRegge.cc:394-438 amplitude).
+// Bare Regge amplitude at loop momentum k = (kx, ky), k2 = kx^2 + ky^2, relative to
+// exp(Emax) of the event (single active trajectory). Same quantity as
+// loop_point_amp (src/MContinuum.cc:94-161 kinematics, src/MRegge.cc:394-438).
 template <typename T>
-GRN_HD bool loop_point_amp_fast(const LoopEventF<T> &e, T kx, T ky, cx<T> &A) {
-  const T q1x = e.p1x - kx, q1y = e.p1y - ky;
-  const T q2x = e.p2x + kx, q2y = e.p2y + ky;
-  const T pt1sq = q1x * q1x + q1y * q1y;
-  const T pt2sq = q2x * q2x + q2y * q2y;
-  const T mT1sq = e.mp2 + pt1sq, mT2sq = e.mp2 + pt2sq;
-  const T c1 = mT1sq * e.invL2, c2 = mT2sq * e.invL2;
-  const T x1 = e.a1 + c2 * e.ia2;
-  const T x2 = e.a2 + c1 * e.ia1;
-  const T r1 = e.ia1 + e.ia1 * e.ia1 * e.ia2 * c2;  // 1/(1 - x1)
-  const T r2 = e.ia2 + e.ia2 * e.ia2 * e.ia1 * c1;  // 1/(1 - x2)
-  const T p1p = (T(1) - x1) * e.L;
-  const T p1m = mT1sq * e.invL * r1;
-  const T p2m = (T(1) - x2) * e.L;
-  const T p2p = mT2sq * e.invL * r2;
-  const T t1  = -(pt1sq + x1 * x1 * e.mp2) * r1;
-  const T t2  = -(pt2sq + x2 * x2 * e.mp2) * r2;
-  const T s13 = e.mp2 + e.m3sq + p1p * e.p3m + p1m * e.p3p - T(2) * (q1x * e.p3x + q1y * e.p3y);
-  const T s14 = e.mp2 + e.m4sq + p1p * e.p4m + p1m * e.p4p - T(2) * (q1x * e.p4x + q1y * e.p4y);
-  const T s23 = e.mp2 + e.m3sq + p2p * e.p3m + p2m * e.p3p - T(2) * (q2x * e.p3x + q2y * e.p3y);
-  const T s24 = e.mp2 + e.m4sq + p2p * e.p4m + p2m * e.p4p - T(2) * (q2x * e.p4x + q2y * e.p4y);
-  T ta, tb;  // t_hat - M2, u_hat - M2
-  {
-    const T dp = e.p4p - e.eps + p2p;
-    const T dm = e.eps - p1m - e.p3m;
-    const T tx = q1x + e.p3x, ty = q1y + e.p3y;
-    ta         = dp * dm - (tx * tx + ty * ty) - e.M2;
-  }
-  {
-    const T dp = e.p3p - e.eps + p2p;
-    const T dm = e.eps - p1m - e.p4m;
-    const T tx = q1x + e.p4x, ty = q1y + e.p4y;
-    tb         = dp * dm - (tx * tx + ty * ty) - e.M2;
-  }
-  const T L13 = log(s13 * e.is0), L14 = log(s14 * e.is0), L23 = log(s23 * e.is0),
-          L24 = log(s24 * e.is0);
-  // Exponents E_t = a0 (L13 + L24) + ap (t1 L13 + t2 L24) (+ form factors), E_u likewise.
-  T St, St_l, Su, Su_l;
-  two_sum(L13, L24, St, St_l);
-  two_sum(L14, L23, Su, Su_l);
-  const T Pt_h = e.a0h * St, Pu_h = e.a0h * Su;
-  const T Et_l = fmadd(e.a0h, St, -Pt_h) + e.a0h * St_l + e.a0l * St;
-  const T Eu_l = fmadd(e.a0h, Su, -Pu_h) + e.a0h * Su_l + e.a0l * Su;
-  const T Et_h = Pt_h - e.eshift, Eu_h = Pu_h - e.eshift;  // exact: both near eshift
-  T Qt = e.ap * (t1 * L13 + t2 * L24);
-  T Qu = e.ap * (t1 * L14 + t2 * L23);
-  T num, den;
+GRN_HD bool loop_point_amp_fast(const LoopEventF<T> &e, T kx, T ky, T k2, cx<T> &A) {
+  const T kd1 = kx * e.p1x + ky * e.p1y;
+  const T kd2 = kx * e.p2x + ky * e.p2y;
+  const T dm1 = k2 - T(2) * kd1;  // d(mT1^2) = d(pT1^2)
+  const T dm2 = k2 + T(2) * kd2;
+  const T dc1 = dm1 * e.invL2, dc2 = dm2 * e.invL2;
+  const T dx1 = dc2 * e.ia2, dx2 = dc1 * e.ia1;
+  const T dr1 = e.q1c * dc2, dr2 = e.q2c * dc1;
+  const T r1 = e.r10 + dr1, r2 = e.r20 + dr2;
+  const T dp1m = e.invL * (dm1 * r1 + e.mT1s0 * dr1);
+  const T dp2p = e.invL * (dm2 * r2 + e.mT2s0 * dr2);
+  const T dp1p = -dx1 * e.L, dp2m = -dx2 * e.L;
+  const T k3 = kx * e.p3x + ky * e.p3y, k4 = kx * e.p4x + ky * e.p4y;
+  const T ds13 = dp1p * e.p3m + dp1m * e.p3p + T(2) * k3;
+  const T ds14 = dp1p * e.p4m + dp1m * e.p4p + T(2) * k4;
+  const T ds23 = dp2p * e.p3m + dp2m * e.p3p - T(2) * k3;
+  const T ds24 = dp2p * e.p4m + dp2m * e.p4p - T(2) * k4;
+  const T d13 = fast_log(T(1) + ds13 * e.is13);
+  const T d14 = fast_log(T(1) + ds14 * e.is14);
+  const T d23 = fast_log(T(1) + ds23 * e.is23);
+  const T d24 = fast_log(T(1) + ds24 * e.is24);
+  const T dt1 = -(dm1 + dx1 * (T(2) * e.x10 + dx1) * e.mp2) * r1 - e.T1n0 * dr1;
+  const T dt2 = -(dm2 + dx2 * (T(2) * e.x20 + dx2) * e.mp2) * r2 - e.T2n0 * dr2;
+  const T t1 = e.t10 + dt1, t2 = e.t20 + dt2;
+  T dEt = e.ap * (dt1 * (e.L13 + d13) + dt2 * (e.L24 + d24)) + e.a10 * d13 + e.a20 * d24;
+  T dEu = e.ap * (dt1 * (e.L14 + d14) + dt2 * (e.L23 + d23)) + e.a10 * d14 + e.a20 * d23;
+  // t_hat - M2 and u_hat - M2
+  const T ta = (e.dpa0 + dp2p) * (e.dma0 - dp1m) -
+               ((e.c3x - kx) * (e.c3x - kx) + (e.c3y - ky) * (e.c3y - ky)) - e.M2;
+  const T tb = (e.dpb0 + dp2p) * (e.dmb0 - dp1m) -
+               ((e.c4x - kx) * (e.c4x - kx) + (e.c4y - ky) * (e.c4y - ky)) - e.M2;
   const T Pd = (T(1) - t1 * e.ifc1) * (T(1) - t1 * e.ifc2) * (T(1) - t2 * e.ifc1) *
                (T(1) - t2 * e.ifc2);
+  T num, den;
   if (e.ffmode == 2) {
     const T Da = e.ff_b - ta, Db = e.ff_b - tb;
-    T h, l;
-    two_sum(Et_h, Qt, h, l);
-    const T Xt = exp_df(h, Et_l + l);
-    two_sum(Eu_h, Qu, h, l);
-    const T Xu = exp_df(h, Eu_l + l);
+    const T Xt = e.rho_t * fast_exp(dEt), Xu = e.rho_u * fast_exp(dEu);
     num = Xt * (Db * Db) * tb + Xu * (Da * Da) * ta;
     den = Pd * (Da * Da) * (Db * Db) * ta * tb;
   } else {
-    T fa, fb;  // 2 ln ff(t_hat), 2 ln ff(u_hat)
+    T fa, fb;
     if (e.ffmode == 0) {
       fa = T(-2) * e.ff_b * fabs(ta);
       fb = T(-2) * e.ff_b * fabs(tb);
@@ -519,19 +543,16 @@ GRN_HD bool loop_point_amp_fast(const LoopEventF<T> &e, T kx, T ky, cx<T> &A) {
       fa = T(2) * (e.ff_ab - e.ff_b * sqrt(fabs(ta) + e.ff_a2));
       fb = T(2) * (e.ff_ab - e.ff_b * sqrt(fabs(tb) + e.ff_a2));
     }
-    T h, l;
-    two_sum(Et_h, Qt + fa, h, l);
-    const T Xt = exp_df(h, Et_l + l);
-    two_sum(Eu_h, Qu + fb, h, l);
-    const T Xu = exp_df(h, Eu_l + l);
+    const T Xt = e.rho_t * fast_exp(dEt + (fa - e.fa0));
+    const T Xu = e.rho_u * fast_exp(dEu + (fb - e.fb0));
     num = Xt * tb + Xu * ta;
     den = Pd * ta * tb;
   }
   T sn, cs;
-  sincos_pi(T(-0.5) * e.ap * (t1 + t2), sn, cs);
+  sincos_pi(T(-0.5) * e.ap * (dt1 + dt2), sn, cs);
   const T m = num / den;
   A = {(e.pre_re * cs - e.pre_im * sn) * m, (e.pre_re * sn + e.pre_im * cs) * m};
-  return (x1 < T(1)) && (x2 < T(1));
+  return (e.x10 + dx1 < T(1)) && (e.x20 + dx2 < T(1));
 }
 
 template <typename T>
