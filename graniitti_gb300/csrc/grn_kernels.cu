@@ -716,11 +716,10 @@ int vegas_grid_blocks(int device) {
   return sms * per;
 }
 
-cudaError_t launch_vegas_sample(const KArgs &a, int prec, const double *xmat, int bins, int dim,
-                                int64_t ncall, uint64_t seed, uint32_t stream, int track_max,
-                                double *f_out, double *f2mat, unsigned long long *acc,
-                                int64_t *l_idx, double *l_x, double *l_vw, uint64_t *l_bins,
-                                int nblocks, cudaStream_t st) {
+cudaError_t launch_vegas_born(const KArgs &a, const double *xmat, int bins, int dim, int64_t ncall,
+                              uint64_t seed, uint32_t stream, int track_max, double *f_out,
+                              double *f2mat, unsigned long long *acc, int64_t *l_idx, double *l_x,
+                              double *l_vw, uint64_t *l_bins, cudaStream_t st) {
   const int nh = bins * dim;
   cudaMemsetAsync(f2mat, 0, nh * sizeof(double), st);
   cudaMemsetAsync(acc, 0, (VS_COUNT + 1) * sizeof(unsigned long long), st);
@@ -732,14 +731,21 @@ cudaError_t launch_vegas_sample(const KArgs &a, int prec, const double *xmat, in
   k_vegas_born<<<ba, kVegasThreads, 2 * nh * sizeof(double), st>>>(
       a, xmat, bins, dim, ncall, seed, stream, track_max, f_out, f2mat, acc, l_idx, l_x, l_vw,
       l_bins, ncall);
-  if (a.P.screening) {
-    if (prec == GRN_PREC_MIXED)
-      k_vegas_loop<float><<<nblocks, kVegasThreads, nh * sizeof(double), st>>>(
-          a, bins, dim, track_max, f_out, f2mat, acc, l_idx, l_x, l_vw, l_bins, ncall);
-    else
-      k_vegas_loop<double><<<nblocks, kVegasThreads, nh * sizeof(double), st>>>(
-          a, bins, dim, track_max, f_out, f2mat, acc, l_idx, l_x, l_vw, l_bins, ncall);
-  }
+  return cudaGetLastError();
+}
+
+cudaError_t launch_vegas_loop(const KArgs &a, int prec, int bins, int dim, int64_t ncall,
+                              int track_max, double *f_out, double *f2mat, unsigned long long *acc,
+                              const int64_t *l_idx, const double *l_x, const double *l_vw,
+                              const uint64_t *l_bins, int nblocks, cudaStream_t st) {
+  if (!a.P.screening) return cudaSuccess;
+  const int nh = bins * dim;
+  if (prec == GRN_PREC_MIXED)
+    k_vegas_loop<float><<<nblocks, kVegasThreads, nh * sizeof(double), st>>>(
+        a, bins, dim, track_max, f_out, f2mat, acc, l_idx, l_x, l_vw, l_bins, ncall);
+  else
+    k_vegas_loop<double><<<nblocks, kVegasThreads, nh * sizeof(double), st>>>(
+        a, bins, dim, track_max, f_out, f2mat, acc, l_idx, l_x, l_vw, l_bins, ncall);
   return cudaGetLastError();
 }
 

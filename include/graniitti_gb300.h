@@ -259,8 +259,9 @@ grn_status grn_vegas_points(grn_engine *e, const int64_t *idx, int64_t n, double
 /* ------------------------------------------------------------------------ */
 /* Measurement helpers (no counterpart in the reference)                      */
 /* ------------------------------------------------------------------------ */
-/* Device time of the VEGAS sampling kernel, accumulated from CUDA events
- * recorded around each launch on the engine stream since the last reset. */
+/* Device time of the dominant kernel of a VEGAS pass (the kt-loop stage when
+ * screening is on), accumulated from CUDA events recorded around each launch on
+ * the engine stream since the last reset. */
 grn_status grn_kernel_timing(grn_engine *e, int32_t reset, double *total_ms, int64_t *launches);
 /* FP32 FMA throughput of the device in TFLOP/s (2 flops per FMA), measured with
  * a register-resident FMA-chain kernel over every SM. */
