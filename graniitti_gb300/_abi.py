@@ -35,6 +35,7 @@ GRN_PROC_REGGE_CON = 1
 GRN_PS_CONTINUUM = 1
 GRN_PREC_FP64 = 0
 GRN_PREC_MIXED = 1
+GRN_NOALLOC_MAX_POINTS = 1048576
 
 
 class SoftParams(ctypes.Structure):
@@ -103,6 +104,8 @@ SIGNATURES = {
     "grn_eikonal_set": (c_int32, [c_void_p, c_int32, c_void_p, c_int32, c_void_p]),
     "grn_event_weights": (c_int32, [c_void_p, c_void_p, c_int64, c_int32, c_void_p, c_void_p,
                                     c_int32]),
+    "grn_event_weights_noalloc": (c_int32, [c_void_p, c_void_p, c_int64, c_int32, c_void_p,
+                                            c_void_p, c_int32]),
     "grn_event_kinematics": (c_int32, [c_void_p, c_void_p, c_int64, c_int32, c_void_p, c_void_p,
                                        c_void_p]),
     "grn_uniforms": (c_int32, [c_void_p, c_uint64, c_uint32, c_int64, c_int64, c_int32,

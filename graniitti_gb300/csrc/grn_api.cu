@@ -248,6 +248,26 @@ grn_status require_screening_ready(grn_engine *e) {
 
 }  // namespace
 
+namespace grn {
+// Used by the allocation-free entry point (grn_noalloc.cu): the engine's launch
+// state without touching any of its buffers.
+grn_status set_error(grn_status st, const char *msg) { return fail(st, msg); }
+
+grn_status engine_noalloc_view(grn_engine *e, KArgs *args, int *device, cudaStream_t *stream,
+                               int *loop_blocks, int *dim) {
+  if (!e) return fail(GRN_ERR_INVALID, "null engine");
+  const grn_status st = require_screening_ready(e);
+  if (st != GRN_OK) return st;
+  if (e->loop_blocks == 0) e->loop_blocks = grn::loop_grid_blocks(e->device);
+  *args        = e->args();
+  *device      = e->device;
+  *stream      = e->stream;
+  *loop_blocks = e->loop_blocks;
+  *dim         = e->dim;
+  return GRN_OK;
+}
+}  // namespace grn
+
 extern "C" {
 
 void grn_default_params(grn_process_params *p) {

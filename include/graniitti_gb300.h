@@ -178,6 +178,25 @@ grn_status grn_eikonal_set(grn_engine *e, int32_t n_bt, const double *mbt, int32
 grn_status grn_event_weights(grn_engine *e, const double *u, int64_t n, int32_t dim,
                              double *w_out, uint8_t *flags, int32_t prec);
 
+/* Allocation-free variant of grn_event_weights. It has no counterpart in the
+ * reference. For callers that may not allocate device memory while running (an
+ * application whose device memory belongs to its own pool allocator, a service that
+ * sizes its memory once at start-up and must not meet an out-of-memory error or the
+ * synchronisation of cudaFree mid-run), this call allocates nothing: its scratch
+ * (the screened work list) is a fixed 8 MiB array inside the library, held by every
+ * device that loads the library until the process exits.
+ *   - u, w_out and flags must be device pointers; n <= GRN_NOALLOC_MAX_POINTS,
+ *     larger batches are rejected with GRN_ERR_INVALID.
+ *   - Stream-ordered on the engine's stream; returns without synchronising.
+ *   - The first call on a device looks up the scratch address (one-time set-up);
+ *     make that first call before any stream capture.
+ *   - All calls on a device share the one scratch array: calls that overlap on the
+ *     GPU (two engines on different streams, concurrently) race; serialise them.
+ * Same results as grn_event_weights. */
+#define GRN_NOALLOC_MAX_POINTS 1048576
+grn_status grn_event_weights_noalloc(grn_engine *e, const double *u, int64_t n, int32_t dim,
+                                     double *w_out, uint8_t *flags, int32_t prec);
+
 /* Kinematics of the same points without the amplitude, for record building and
  * tests: per point 16 doubles = (px,py,pz,E) of the two forward legs and the two
  * central particles (LORENTZSCALAR::pfinal[1..4]), plus t1, t2 into ts (2 per
