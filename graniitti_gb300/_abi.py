@@ -33,6 +33,7 @@ GRN_FLAG_AMPLITUDE_OK = 8
 
 GRN_PROC_REGGE_CON = 1
 GRN_PS_CONTINUUM = 1
+GRN_PS_FACTORIZED = 2
 GRN_PREC_FP64 = 0
 GRN_PREC_MIXED = 1
 GRN_NOALLOC_MAX_POINTS = 1048576
@@ -53,7 +54,8 @@ class ReggeParams(ctypes.Structure):
 
 class GenCuts(ctypes.Structure):
     _fields_ = [(n, c_double) for n in
-                ("rap_min", "rap_max", "kt_min", "kt_max", "fpt_min", "fpt_max")]
+                ("rap_min", "rap_max", "kt_min", "kt_max", "fpt_min", "fpt_max",
+                 "Y_min", "Y_max", "M_min", "M_max")]
 
 
 class FidCuts(ctypes.Structure):

@@ -91,8 +91,8 @@ def build_params(card, process=None, tune=None):
     T = TUNES[tune]
     proc = process or pp["PROCESS"]
     istate, channel, cls, finals, _ = parse_process(proc)
-    if not (istate == "PP" and channel == "CON" and cls == "C" and len(finals) == 2):
-        raise UnsupportedProcess("engine implements PP[CON]<C> -> 2-body, got %r" % proc)
+    if not (istate == "PP" and channel == "CON" and cls in ("C", "F") and len(finals) == 2):
+        raise UnsupportedProcess("engine implements PP[CON]<C|F> -> 2-body, got %r" % proc)
     if int(pp.get("NSTARS", 0)) != 0:
         raise UnsupportedProcess("forward excitation (NSTARS > 0) is not implemented")
     if pp["BEAM"] != ["p+", "p+"]:
@@ -106,7 +106,7 @@ def build_params(card, process=None, tune=None):
     P.sqrt_s = 2.0 * E1
     P.m_beam = mb
     P.process = _abi.GRN_PROC_REGGE_CON
-    P.phase_space = _abi.GRN_PS_CONTINUUM
+    P.phase_space = _abi.GRN_PS_CONTINUUM if cls == "C" else _abi.GRN_PS_FACTORIZED
     P.n_central = 2
     P.screening = 1 if pp.get("POMLOOP", False) else 0
     for k, name in enumerate(finals):
@@ -125,6 +125,15 @@ def build_params(card, process=None, tune=None):
     P.gcuts.kt_min, P.gcuts.kt_max = kt
     pt = g.get("Pt", [0.0, 2.5])
     P.gcuts.fpt_min, P.gcuts.fpt_max = pt
+    # <F>: system rapidity and mass windows (MGraniitti::ReadGenCuts; GENCUT defaults)
+    gf = card.get("GENCUTS", {}).get("<F>", {})
+    P.gcuts.Y_min, P.gcuts.Y_max = gf.get("Rap", [-9.0, 9.0])
+    P.gcuts.M_min, P.gcuts.M_max = gf.get("M", [0.0, 0.0])
+    if cls == "F":
+        if "Rap" not in gf or "M" not in gf:
+            raise ValueError('<F> needs "GENCUTS" : { "<F>" : { "Rap" : [..], "M" : [..] } }')
+        if "Pt" in gf:
+            P.gcuts.fpt_min, P.gcuts.fpt_max = gf["Pt"]
 
     # Fiducial cuts (FIDCUT defaults, MKinematics.h:1579-1611).
     f = card.get("FIDCUTS", {})

@@ -49,7 +49,7 @@ int main() {
   P.process = GRN_PROC_REGGE_CON; P.phase_space = GRN_PS_CONTINUUM; P.n_central = 2;
   P.sqrt_s = 13000.0; P.m_beam = 0.938272081; P.m_central[0] = P.m_central[1] = 0.13957061;
   P.s_factor = 1.0;
-  P.gcuts = {-0.9, 0.9, 0.0, 5.0, 0.0, 2.5};
+  P.gcuts = {-0.9, 0.9, 0.0, 5.0, 0.0, 2.5, -0.9, 0.9, 0.0, 5.0};
   P.soft.gN_P = 8.2; P.soft.fc1 = 0.34; P.soft.fc2 = 5.0;
   P.regge.a0[0] = 1.088; P.regge.ap[0] = 0.20; P.regge.sgn[0] = 1; P.regge.s0 = 1.0;
   P.regge.active[0] = 1; P.regge.offshellFF = 2; P.regge.b_POW = 0.5; P.regge.c[0] = 35.00184;

@@ -140,8 +140,9 @@ namespace {
 
 grn_status derive_consts(const grn_process_params &P, grn::Consts &K) {
   using namespace grn;
-  if (P.process != GRN_PROC_REGGE_CON || P.phase_space != GRN_PS_CONTINUUM)
-    return fail(GRN_ERR_UNSUPPORTED, "only PP[CON]<C> (Regge continuum, <C> class) is implemented");
+  if (P.process != GRN_PROC_REGGE_CON ||
+      (P.phase_space != GRN_PS_CONTINUUM && P.phase_space != GRN_PS_FACTORIZED))
+    return fail(GRN_ERR_UNSUPPORTED, "only PP[CON]<C|F> (Regge continuum) is implemented");
   if (P.n_central != 2) return fail(GRN_ERR_UNSUPPORTED, "only 2-body central states");
   if (!(P.sqrt_s > 2 * P.m_beam)) return fail(GRN_ERR_INVALID, "sqrt_s below threshold");
   if (!(P.gcuts.fpt_max > 0) || !(P.gcuts.kt_max > P.gcuts.kt_min) ||
@@ -168,6 +169,22 @@ grn_status derive_consts(const grn_process_params &P, grn::Consts &K) {
                      fwd_log * fwd_log;
   K.w_const = (1.0 / P.s_factor) * (1.0 / std::pow(2.0, 2 * (Nf - 2))) *
               (1.0 / std::pow(2.0 * kPi, 3 * Nf - 4)) * vol * kGeV2barn / (2.0 * K.s);
+  if (P.phase_space == GRN_PS_FACTORIZED) {
+    // mass window (B51RandomKin, MFactorized.cc:263-291): M_MIN = sum of daughter masses
+    // + 1e-4 GeV, M_MAX = sqrt(s) - 2 m_beam, both clipped to the <F> generation cuts.
+    const double Mmin = std::max(K.m3 + K.m4 + 1e-4, P.gcuts.M_min);
+    const double Mmax = std::min(P.sqrt_s - 2.0 * P.m_beam, P.gcuts.M_max);
+    if (!(Mmin < Mmax)) return fail(GRN_ERR_INVALID, "<F> mass window is empty (GENCUTS <F> M)");
+    if (!(P.gcuts.Y_max > P.gcuts.Y_min)) return fail(GRN_ERR_INVALID, "<F> rapidity window");
+    K.M2min = Mmin * Mmin;
+    K.M2max = Mmax * Mmax;
+    // dPhi2/(2 pi) = p*/(8 pi^2 M_X) with p*/M_X per event; B51PhaseSpaceWeight,
+    // B51IntegralVolume (MFactorized.cc:418-450), ForwardVolume.
+    const double fwd = std::pow(2.0 * kPi, 2) * fwd_log * fwd_log;
+    K.w_const = (1.0 / P.s_factor) * (1.0 / (8.0 * kPi * kPi)) * 0.5 *
+                (1.0 / std::pow(2.0 * kPi, 5)) * (K.M2max - K.M2min) *
+                (P.gcuts.Y_max - P.gcuts.Y_min) * fwd * kGeV2barn / (2.0 * K.s);
+  }
   K.M2prop = K.m3sq;
   K.g2     = std::pow(P.regge.c[0] / P.soft.gN_P, 2);
   K.gN2    = P.soft.gN_P * P.soft.gN_P;
@@ -281,7 +298,7 @@ void grn_default_params(grn_process_params *p) {
   p->m_beam      = 9.38272081e-01;  // proton (modeldata/mass_width_2018.mcd)
   p->m_central[0] = p->m_central[1] = 1.3957061e-01;  // pi+-
   p->s_factor    = 1.0;
-  p->gcuts = {-0.9, 0.9, 0.0, 5.0, 0.0, 2.5};
+  p->gcuts = {-0.9, 0.9, 0.0, 5.0, 0.0, 2.5, -0.9, 0.9, 0.0, 5.0};
   p->fcuts.active = 1;
   p->fcuts.eta_min = -0.9;  p->fcuts.eta_max = 0.9;
   p->fcuts.rap_min = -10.0; p->fcuts.rap_max = 10.0;

@@ -847,41 +847,73 @@ cudaError_t launch_vegas_grid_init(double *xmat, int bins, int dim, cudaStream_t
 }
 
 // Smoothing of the f^2 histogram and damped rebinning
-// (VEGASData::OptimizeGrid, include/Graniitti/MVEGAS.h:107-142).
-__global__ void k_vegas_refine(double *xmat, double *f2mat, int bins, int dim, double lambda) {
-  extern __shared__ double sm[];
-  const int j = threadIdx.x;
-  if (j >= dim) return;
-  double *r = sm + j * 2 * bins, *xnew = r + bins;
+// (VEGASData::OptimizeGrid, include/Graniitti/MVEGAS.h:107-142). One block per
+// dimension: the three-point smoothing (which reads only unsmoothed neighbours)
+// and the importance weights r_i run in parallel over bins; the sums use a fixed
+// tree order; the rebinning walk is sequential (one thread) but has no
+// transcendentals.
+constexpr int kRefineThreads = 256;
+
+__global__ void __launch_bounds__(kRefineThreads)
+    k_vegas_refine(double *xmat, double *f2mat, int bins, int dim, double lambda) {
+  __shared__ double sm_f[kMaxBins], sm_r[kMaxBins], sm_x[kMaxBins], red[kRefineThreads];
+  const int j = blockIdx.x;
+  const int i = threadIdx.x;
   const double EPS = 1.0e-30;
-  double zo = f2mat[0 * dim + j], zn = f2mat[1 * dim + j];
-  f2mat[j]  = (zo + zn) / 2.0;
-  double d  = f2mat[j];
-  for (int i = 2; i < bins; ++i) {
-    const double ac          = zo + zn;
-    zo                       = zn;
-    zn                       = f2mat[i * dim + j];
-    f2mat[(i - 1) * dim + j] = (ac + zn) / 3.0;
-    d += f2mat[(i - 1) * dim + j];
+  double v = 0.0;
+  if (i < bins) {
+    const double c = f2mat[i * dim + j];
+    if (i == 0)
+      v = (c + f2mat[1 * dim + j]) / 2.0;
+    else if (i == bins - 1)
+      v = (f2mat[(bins - 2) * dim + j] + c) / 2.0;
+    else
+      v = (f2mat[(i - 1) * dim + j] + c + f2mat[(i + 1) * dim + j]) / 3.0;
   }
-  f2mat[(bins - 1) * dim + j] = (zo + zn) / 2.0;
-  d += f2mat[(bins - 1) * dim + j];
-  double ac = 0.0;
-  for (int i = 0; i < bins; ++i) {
-    double v = f2mat[i * dim + j];
+  red[i] = v;
+  __syncthreads();
+  for (int o = kRefineThreads / 2; o > 0; o >>= 1) {
+    if (i < o) red[i] += red[i + o];
+    __syncthreads();
+  }
+  const double d = red[0];
+  __syncthreads();
+  double ri = 0.0;
+  if (i < bins) {
     if (v < EPS) v = EPS;
     f2mat[i * dim + j] = v;
-    double ri = pow((1.0 - v / d) / (log(d) - log(v) + EPS), lambda);
+    ri = pow((1.0 - v / d) / (log(d) - log(v) + EPS), lambda);
     if (isnan(ri) || isinf(ri)) ri = EPS;
-    r[i] = ri;
-    ac += ri;
+    sm_r[i] = ri;
+    sm_x[i] = xmat[i * dim + j];
   }
-  rebin_dim(bins, dim, j, ac / bins, r, xnew, xmat);
+  red[i] = ri;
+  __syncthreads();
+  for (int o = kRefineThreads / 2; o > 0; o >>= 1) {
+    if (i < o) red[i] += red[i + o];
+    __syncthreads();
+  }
+  if (i == 0) {
+    const double ac = red[0] / bins;
+    // rebin on the block's copy of column j, then write it back
+    int    k  = 0;
+    double dr = 0.0, zn = 0.0, zo = 0.0;
+    for (int q = 0; q < bins - 1; ++q) {
+      while (ac > dr && k < bins) dr += sm_r[(++k) - 1];
+      if (k < 1) k = 1;
+      if (k > 1) zo = sm_x[k - 2];
+      zn = sm_x[k - 1];
+      dr -= ac;
+      sm_f[q] = zn - (zn - zo) * dr / sm_r[k - 1];
+    }
+    for (int q = 0; q < bins - 1; ++q) xmat[q * dim + j] = sm_f[q];
+    xmat[(bins - 1) * dim + j] = 1.0;
+  }
 }
 
 cudaError_t launch_vegas_refine(double *xmat, double *f2mat, int bins, int dim, double lambda,
                                 cudaStream_t st) {
-  k_vegas_refine<<<1, dim, 2 * bins * dim * sizeof(double), st>>>(xmat, f2mat, bins, dim, lambda);
+  k_vegas_refine<<<dim, kRefineThreads, 0, st>>>(xmat, f2mat, bins, dim, lambda);
   return cudaGetLastError();
 }
 

@@ -67,6 +67,7 @@ struct Consts {
   double m3, m4, m3sq, m4sq;
   double lnpt_lo, lnpt_hi;  // log(fpt_min + ZERO_EPS), log(fpt_max)
   double w_const;           // every u-independent factor of the weight
+  double M2min, M2max;      // <F>: central-system mass^2 window (B51RandomKin)
   double M2prop;            // off-shell propagator nominal mass^2 (ME4: first central mass)
   double g2;                // (c0 / gN_P)^2
   double gN2;               // gN_P^2
@@ -144,7 +145,7 @@ struct Born {
   double p3x, p3y, p4x, p4y;
   double p3p, p3m, p4p, p4m;
   double mt3, mt4, y3, y4;
-  double kt;                   // |q| of the difference momentum
+  double jx;                   // class-specific Jacobian factor: kt (<C>), p*/M_X (<F>)
   // invariants
   double t1, t2, s13, s14, s23, s24, that, uhat, m2;
 };
@@ -170,8 +171,10 @@ GRN_HD bool solve_x(T a1, T a2, T c1, T c2, T &x1, T &x2) {
 
 // BNRandomKin + BNBuildKin + GetLorentzScalars for Kf = 2
 // (src/MContinuum.cc:276-435, src/MProcess.cc:1499-1584).
-GRN_HD bool born_kinematics(const grn_process_params &P, const Consts &K, const double *u,
-                            Born &b) {
+GRN_HD bool born_invariants(const Consts &K, Born &b);
+
+GRN_HD bool born_kinematics_C(const grn_process_params &P, const Consts &K, const double *u,
+                              Born &b) {
   const grn_gencuts &g = P.gcuts;
   const double pt1 = exp(K.lnpt_lo + (K.lnpt_hi - K.lnpt_lo) * u[0]);
   const double pt2 = exp(K.lnpt_lo + (K.lnpt_hi - K.lnpt_lo) * u[1]);
@@ -182,7 +185,7 @@ GRN_HD bool born_kinematics(const grn_process_params &P, const Consts &K, const 
   sincos_pi(2.0 * u[5], sk, ck);
   b.y3 = g.rap_min + (g.rap_max - g.rap_min) * u[6];
   b.y4 = g.rap_min + (g.rap_max - g.rap_min) * u[7];
-  b.kt = kt;
+  b.jx = kt;
 
   b.p1x = pt1 * c1;
   b.p1y = pt1 * s1;
@@ -207,6 +210,15 @@ GRN_HD bool born_kinematics(const grn_process_params &P, const Consts &K, const 
   const double Pp = b.p3p + b.p4p, Pm = b.p3m + b.p4m;
   if (0.5 * (Pp + Pm) > K.sqrt_s) return false;  // crude energy check (MContinuum.cc:373)
 
+  return born_invariants(K, b);
+}
+
+// Forward legs (light-cone closure) and Lorentz scalars of the tree-level event from
+// the central pair (p3, p4 transverse and light-cone components) and the forward
+// transverse momenta already in b (MContinuum.cc:372-384, MFactorized.cc:327-343,
+// MProcess.cc:1499-1584).
+GRN_HD bool born_invariants(const Consts &K, Born &b) {
+  const double Pp = b.p3p + b.p4p, Pm = b.p3m + b.p4m;
   const double mT1sq = K.mp2 + b.pt1sq, mT2sq = K.mp2 + b.pt2sq;
   const double L2    = K.L * K.L;
   if (!solve_x((Pp - K.eps) / K.L, (Pm - K.eps) / K.L, mT1sq / L2, mT2sq / L2, b.x1, b.x2))
@@ -238,6 +250,72 @@ GRN_HD bool born_kinematics(const grn_process_params &P, const Consts &K, const 
     b.uhat = dp * dm - (tx * tx + ty * ty);
   }
   return true;
+}
+
+
+// B51RandomKin + B51BuildKin for a 2-body central system, the isotropic decay
+// angles lifted into u[6] (cos theta = 2 u6 - 1) and u[7] (phi = 2 pi u7), the
+// draws TwoBodyPhaseSpace makes (src/MFactorized.cc:245-412;
+// include/Graniitti/MKinematics.h:405-459).
+GRN_HD bool born_kinematics_F(const grn_process_params &P, const Consts &K, const double *u,
+                              Born &b) {
+  const grn_gencuts &g = P.gcuts;
+  const double pt1 = exp(K.lnpt_lo + (K.lnpt_hi - K.lnpt_lo) * u[0]);
+  const double pt2 = exp(K.lnpt_lo + (K.lnpt_hi - K.lnpt_lo) * u[1]);
+  double s1, c1, s2, c2;
+  sincos_pi(2.0 * u[2], s1, c1);
+  sincos_pi(2.0 * u[3], s2, c2);
+  const double yX  = g.Y_min + (g.Y_max - g.Y_min) * u[4];
+  const double m2X = K.M2min + (K.M2max - K.M2min) * u[5];
+  b.p1x = pt1 * c1;
+  b.p1y = pt1 * s1;
+  b.p2x = pt2 * c2;
+  b.p2y = pt2 * s2;
+  b.pt1sq = b.p1x * b.p1x + b.p1y * b.p1y;
+  b.pt2sq = b.p2x * b.p2x + b.p2y * b.p2y;
+  const double Xx = -(b.p1x + b.p2x), Xy = -(b.p1y + b.p2y);
+  const double mTX = sqrt(m2X + Xx * Xx + Xy * Xy);
+  const double eY  = exp(yX);
+  const double XP = mTX * eY, XM = mTX / eY;
+  const double EX = 0.5 * (XP + XM), ZX = 0.5 * (XP - XM);
+  if (EX > K.sqrt_s - 2.0 * sqrt(K.mp2)) return false;  // energy overflow (MFactorized.cc:323)
+  // isotropic decay in the central-system rest frame, boosted to the lab
+  const double MX = sqrt(m2X);
+  const double ms = K.m3 + K.m4, md = K.m3 - K.m4;
+  const double ps = sqrt(fmax(0.0, (MX - ms) * (MX + ms) * (MX + md) * (MX - md))) / (2.0 * MX);
+  const double ct = 2.0 * u[6] - 1.0;
+  const double st = sqrt(fmax(0.0, 1.0 - ct * ct));
+  double sp, cp;
+  sincos_pi(2.0 * u[7], sp, cp);
+  const double kx = ps * st * cp, ky = ps * st * sp, kz = ps * ct;
+  const double E3s = sqrt(K.m3sq + ps * ps), E4s = sqrt(K.m4sq + ps * ps);
+  const double bx = Xx / EX, by = Xy / EX, bz = ZX / EX, gam = EX / MX;
+  const double k1 = bx * kx + by * ky + bz * kz;
+  const double a3 = gam * (gam * k1 / (1.0 + gam) + E3s);
+  const double a4 = gam * (-gam * k1 / (1.0 + gam) + E4s);
+  b.p3x = kx + a3 * bx;
+  b.p3y = ky + a3 * by;
+  const double p3z = kz + a3 * bz, E3 = gam * (E3s + k1);
+  b.p4x = -kx + a4 * bx;
+  b.p4y = -ky + a4 * by;
+  const double p4z = -kz + a4 * bz, E4 = gam * (E4s - k1);
+  b.mt3 = sqrt(K.m3sq + b.p3x * b.p3x + b.p3y * b.p3y);
+  b.mt4 = sqrt(K.m4sq + b.p4x * b.p4x + b.p4y * b.p4y);
+  // light-cone components; the smaller one from mT^2 / larger (exact, no cancellation)
+  if (p3z >= 0) { b.p3p = E3 + p3z; b.p3m = b.mt3 * b.mt3 / b.p3p; }
+  else          { b.p3m = E3 - p3z; b.p3p = b.mt3 * b.mt3 / b.p3m; }
+  if (p4z >= 0) { b.p4p = E4 + p4z; b.p4m = b.mt4 * b.mt4 / b.p4p; }
+  else          { b.p4m = E4 - p4z; b.p4p = b.mt4 * b.mt4 / b.p4m; }
+  b.y3 = 0.5 * log(b.p3p / b.p3m);
+  b.y4 = 0.5 * log(b.p4p / b.p4m);
+  b.jx = ps / MX;
+  return born_invariants(K, b);
+}
+
+GRN_HD bool born_kinematics(const grn_process_params &P, const Consts &K, const double *u,
+                            Born &b) {
+  if (P.phase_space == GRN_PS_FACTORIZED) return born_kinematics_F(P, K, u, b);
+  return born_kinematics_C(P, K, u, b);
 }
 
 // Fiducial cuts (MProcess::CommonCuts + FindDecayCuts, src/MProcess.cc:1085-1154).
@@ -568,13 +646,15 @@ GRN_HD void make_loop_event(const Consts &K, const Born &b, LoopEvent<T> &e) {
 
 // u-independent part of the weight and the u-dependent Jacobians
 // (MContinuum::EventWeight, BNPhaseSpaceWeight, BNIntegralVolume and
-// ForwardVolume; src/MContinuum.cc:164-193, 619-656; src/MProcess.cc:1390-1415).
+// ForwardVolume; src/MContinuum.cc:164-193, 619-656; src/MProcess.cc:1390-1415;
+// for <F>: MFactorized::EventWeight, B51PhaseSpaceWeight, B51IntegralVolume and the
+// 2-body phase-space factor dPhi2/(2 pi), src/MFactorized.cc:142-184, 418-450).
 GRN_HD double weight_jacobian(const Consts &K, const Born &b) {
   const double E1 = 0.5 * (b.p1p + b.p1m), pz1 = 0.5 * (b.p1p - b.p1m);
   const double E2 = 0.5 * (b.p2p + b.p2m), pz2 = 0.5 * (b.p2p - b.p2m);
   const double J  = 1.0 / fabs(pz1 / E1 - pz2 / E2);
   const double pt1 = sqrt(b.pt1sq), pt2 = sqrt(b.pt2sq);
-  return K.w_const * (pt1 / (2.0 * E1)) * (pt2 / (2.0 * E2)) * J * b.kt * pt1 * pt2;
+  return K.w_const * (pt1 / (2.0 * E1)) * (pt2 / (2.0 * E2)) * J * b.jx * pt1 * pt2;
 }
 
 }  // namespace grn

@@ -56,7 +56,9 @@ enum {
 
 /* Phase-space classes (MProcess subclasses). */
 enum {
-  GRN_PS_CONTINUUM = 1 /* <C>: MContinuum (src/MContinuum.cc) */
+  GRN_PS_CONTINUUM  = 1, /* <C>: MContinuum (src/MContinuum.cc), 3 Nf - 4 = 8 dimensions */
+  GRN_PS_FACTORIZED = 2  /* <F>: MFactorized (src/MFactorized.cc), 5 + 1 dimensions plus the
+                            2-body decay angles (cos theta, phi) lifted into u[6], u[7] */
 };
 
 /* Arithmetic of the kt-loop (the tree-level kinematics is always FP64). */
@@ -88,6 +90,8 @@ typedef struct grn_gencuts { /* GENCUT, include/Graniitti/MKinematics.h:1554-157
   double rap_min, rap_max;       /* <C> final-state rapidity window */
   double kt_min, kt_max;         /* <C> intermediate kt (post_Constructor default 10/Kf) */
   double fpt_min, fpt_max;       /* forward-leg pT (SetTechnicalBoundaries default 0, 2.5) */
+  double Y_min, Y_max;           /* <F> central-system rapidity window */
+  double M_min, M_max;           /* <F> central-system mass window */
 } grn_gencuts;
 
 typedef struct grn_fidcuts { /* FIDCUT, include/Graniitti/MKinematics.h:1579-1611 */

@@ -181,7 +181,8 @@ double meson_ff(const grn_regge_params &rp, double that, double M2) {
 struct Event {
   V4     pb1, pb2;         // beams
   V4     pf[5];            // pfinal[0..4]: central system, forward 1, forward 2, central a, b
-  V4     q;                // intermediate difference momentum (pkt_[0])
+  V4     q;                // intermediate difference momentum (pkt_[0]), <C>
+  double dw = 0;           // <F>: 2-body phase-space weight dPhi2 (MFactorized.cc:381)
   double t1 = 0, t2 = 0, that = 0, uhat = 0, m2 = 0, Y = 0, Pt = 0;
   double ss[5][5] = {};
 };
@@ -297,12 +298,85 @@ bool build_kinematics(const Setup &S, const double *u, Event &ev) {
   return lorentz_scalars(S, ev);
 }
 
+// 2-body decay in the mother's rest frame with given (cos theta, phi), boosted to
+// the lab (TwoBodyPhaseSpace + Isotropic + LorentzBoost,
+// include/Graniitti/MKinematics.h:294-298, 384-459). Returns dPhi2 (MKinematics.h:267).
+double two_body(const V4 &mother, double M0, double m3, double m4, double ct, double phi,
+                V4 &p3, V4 &p4) {
+  const double x = M0, y = m3, z = m4;
+  const double pn = msqrt((x - y - z) * (x + y + z) * (x + y - z) * (x - y + z)) / (2.0 * x);
+  const double st = msqrt(1.0 - ct * ct);
+  const double k[3] = {pn * st * std::cos(phi), pn * st * std::sin(phi), pn * ct};
+  V4 d[2] = {V4(k[0], k[1], k[2], msqrt(m3 * m3 + pn * pn)),
+             V4(-k[0], -k[1], -k[2], msqrt(m4 * m4 + pn * pn))};
+  const double b[3] = {mother.x / mother.e, mother.y / mother.e, mother.z / mother.e};
+  const double gam = mother.e / M0;
+  for (V4 &p : d) {
+    const double k1 = b[0] * p.x + b[1] * p.y + b[2] * p.z;
+    const double k2 = gam * (gam * k1 / (1.0 + gam) + p.e);
+    p = V4(p.x + k2 * b[0], p.y + k2 * b[1], p.z + k2 * b[2], gam * (p.e + k1));
+  }
+  p3 = d[0];
+  p4 = d[1];
+  return 4.0 * PI * pn / (16.0 * PI * PI * M0);
+}
+
+// B51RandomKin + B51BuildKin for a 2-body central state, decay angles taken from
+// u[6] (cos theta = 2 u6 - 1) and u[7] (phi = 2 pi u7) (MFactorized.cc:245-412).
+bool build_kinematics_F(const Setup &S, const double *u, Event &ev) {
+  const grn_gencuts &g = S.p.gcuts;
+  const double lo  = std::log(g.fpt_min + ZERO_EPS);
+  const double hi  = std::log(g.fpt_max);
+  const double pt1 = std::exp(lo + (hi - lo) * u[0]);
+  const double pt2 = std::exp(lo + (hi - lo) * u[1]);
+  const double phi1 = 2.0 * PI * u[2];
+  const double phi2 = 2.0 * PI * u[3];
+  const double yX   = g.Y_min + (g.Y_max - g.Y_min) * u[4];
+  const double m3 = S.p.m_central[0], m4 = S.p.m_central[1];
+  const double Mmin = std::max(m3 + m4 + 1e-4, g.M_min);
+  const double Mmax = std::min(S.sqrt_s - (S.pb1.m() + S.pb2.m()), g.M_max);
+  const double m2X  = Mmin * Mmin + (Mmax * Mmax - Mmin * Mmin) * u[5];
+  V4 p1(pt1 * std::cos(phi1), pt1 * std::sin(phi1), 0, 0);
+  V4 p2(pt2 * std::cos(phi2), pt2 * std::sin(phi2), 0, 0);
+  V4 pX(-(p1.x + p2.x), -(p1.y + p2.y), 0, 0);
+  const double mtX = msqrt(m2X + pX.pt2());
+  pX.z = mtX * std::sinh(yX);
+  pX.e = mtX * std::cosh(yX);
+  if (pX.e > S.sqrt_s - 2.0 * S.p.m_beam) return false;
+  if (!forward_legs(S, pt1, p1.x, p1.y, pt2, p2.x, p2.y, pX, p1, p2)) return false;
+  ev.pf[0] = pX;
+  ev.pf[1] = p1;
+  ev.pf[2] = p2;
+  if (!check_emc((S.pb1 + S.pb2) - (p1 + p2 + pX))) return false;
+  ev.dw = two_body(pX, msqrt(m2X), m3, m4, 2.0 * u[6] - 1.0, 2.0 * PI * u[7], ev.pf[3], ev.pf[4]);
+  return lorentz_scalars(S, ev);
+}
+
 // LoopKinematics for Kf = 2 (MContinuum.cc:94-161): new forward transverse momenta,
 // central pair re-solved with the tree-level difference momentum, rapidities and
 // masses of the tree-level central particles.
 bool loop_kinematics(const Setup &S, const Event &born, double p1x, double p1y, double p2x,
                      double p2y, Event &ev) {
   const V4 p1T(p1x, p1y, 0, 0), p2T(p2x, p2y, 0, 0);
+  if (S.p.phase_space == GRN_PS_FACTORIZED) {
+    // MFactorized::LoopKinematics (src/MFactorized.cc:84-139): the central system keeps
+    // its mass and rapidity, its pT balances the new forward legs; the decay products
+    // keep their tree-level momenta.
+    const double mX = born.pf[0].m(), yX = born.pf[0].rap();
+    V4 pX(-(p1x + p2x), -(p1y + p2y), 0, 0);
+    const double mtX = msqrt(mX * mX + pX.pt2());
+    pX.z = mtX * std::sinh(yX);
+    pX.e = mtX * std::cosh(yX);
+    if (pX.e > S.sqrt_s - 2.0 * S.p.m_beam) return false;
+    V4 p1, p2;
+    if (!forward_legs(S, p1T.pt(), p1x, p1y, p2T.pt(), p2x, p2y, pX, p1, p2)) return false;
+    ev       = born;
+    ev.pf[0] = pX;
+    ev.pf[1] = p1;
+    ev.pf[2] = p2;
+    if (!check_emc((S.pb1 + S.pb2) - (p1 + p2 + pX))) return false;
+    return lorentz_scalars(S, ev);
+  }
   const double m[2] = {born.pf[3].m(), born.pf[4].m()};
   const double y[2] = {born.pf[3].rap(), born.pf[4].rap()};
   V4 c[2];
@@ -384,6 +458,19 @@ double screened_amp2(const Setup &S, const Event &born, const cplx &A0) {
 double ps_factor(const Setup &S, const Event &ev) {
   const grn_gencuts &g = S.p.gcuts;
   const double J = 1.0 / std::fabs(ev.pf[1].z / ev.pf[1].e - ev.pf[2].z / ev.pf[2].e);
+  if (S.p.phase_space == GRN_PS_FACTORIZED) {
+    // C_space = dPhi2/(2 pi), B51PhaseSpaceWeight x B51IntegralVolume (MFactorized.cc:160-183,
+    // 418-450)
+    const double m3 = S.p.m_central[0], m4 = S.p.m_central[1];
+    const double Mmin = std::max(m3 + m4 + 1e-4, g.M_min);
+    const double Mmax = std::min(S.sqrt_s - (S.pb1.m() + S.pb2.m()), g.M_max);
+    const double psw  = 0.5 * (1.0 / std::pow(2.0 * PI, 5)) * (ev.pf[1].pt() / (2.0 * ev.pf[1].e)) *
+                       (ev.pf[2].pt() / (2.0 * ev.pf[2].e)) * J;
+    const double fwd = sq(2.0 * PI) * ev.pf[1].pt() * ev.pf[2].pt() *
+                       sq(std::log(g.fpt_max) - std::log(g.fpt_min + ZERO_EPS));
+    const double vol = (Mmax * Mmax - Mmin * Mmin) * (g.Y_max - g.Y_min) * fwd;
+    return (ev.dw / (2.0 * PI)) * psw * vol;
+  }
   const int Nf = 4;
   const double psw = (1.0 / std::pow(2.0, 2 * (Nf - 2))) * (1.0 / std::pow(2.0 * PI, 3 * Nf - 4)) *
                      (ev.pf[1].pt() / (2.0 * ev.pf[1].e)) * (ev.pf[2].pt() / (2.0 * ev.pf[2].e)) *
@@ -418,7 +505,8 @@ bool fiducial(const Setup &S, const Event &ev) {
 // One event weight (MContinuum::EventWeight, src/MContinuum.cc:164-193).
 double event_weight(const Setup &S, const double *u, uint8_t &flags, Event &ev) {
   double W = 0.0;
-  const bool kin = build_kinematics(S, u, ev);
+  const bool kin = S.p.phase_space == GRN_PS_FACTORIZED ? build_kinematics_F(S, u, ev)
+                                                        : build_kinematics(S, u, ev);
   const bool fid = kin && fiducial(S, ev);
   const bool veto = true;
   if (kin && fid && veto) {

@@ -12,7 +12,11 @@
 //
 // Modes (all numbers little-endian binary doubles):
 //   weights <card> <process> <u.bin> <dim> <out.bin> [options]
-//       u.bin holds n*dim doubles, point-major. out.bin receives, per point,
+//       u.bin holds n*stride doubles, point-major (stride = dim unless --stride);
+//       the first dim coordinates are the process's hypercube vector. With
+//       --replay SPEC (comma list; 'h' = 0.5, k = coordinate k of the point) the
+//       listed values are served, in order, to the draws the process makes from its
+//       random-number generator (off-shell masses, decay angles) for that point. out.bin receives, per point,
 //       REC doubles: W, kin_ok, fid_ok, veto_ok, amp_ok, t1, t2, m2, then the
 //       4-momenta (px,py,pz,E) of pfinal[1], pfinal[2], pfinal[3], pfinal[4].
 //   eikonal <card> <process> <out.bin> [options]
@@ -22,7 +26,7 @@
 //   vegas <card> <process> [options]   prints "sigma err" [barn].
 //
 // Options: --nbt N --nkt2 N --loopkt N --loopphi N --maxloopkt X --offshellff K
-//          --ncall N --iter N --cores N --precision X
+//          --ncall N --iter N --cores N --precision X --stride S --replay SPEC
 
 #include <cstdio>
 #include <cstdlib>
@@ -39,6 +43,8 @@
 namespace {
 
 struct Opts {
+  int         stride = 0;
+  std::string replay;
   int    nbt = 0, nkt2 = 0;
   int    loopkt = -1, loopphi = -1;
   double maxloopkt = -1;
@@ -62,6 +68,8 @@ Opts parse_opts(int argc, char **argv, int first) {
     else if (k == "--iter") o.iter = std::atoi(v);
     else if (k == "--cores") o.cores = std::atoi(v);
     else if (k == "--precision") o.precision = std::atof(v);
+    else if (k == "--stride") o.stride = std::atoi(v);
+    else if (k == "--replay") o.replay = v;
     else {
       std::fprintf(stderr, "unknown option %s\n", k.c_str());
       std::exit(2);
@@ -147,14 +155,30 @@ int main(int argc, char **argv) {
       force_regge_init(proc, dim, o);
 
       const std::vector<double> u = read_doubles(ufile);
-      const std::size_t         n = u.size() / dim;
+      const unsigned            stride = o.stride > 0 ? o.stride : dim;
+      const std::size_t         n = u.size() / stride;
+      std::vector<int>          spec;  // -1 = 0.5, else coordinate index
+      for (std::size_t a = 0; a < o.replay.size();) {
+        std::size_t b = o.replay.find(',', a);
+        if (b == std::string::npos) b = o.replay.size();
+        const std::string tok = o.replay.substr(a, b - a);
+        spec.push_back(tok == "h" ? -1 : std::atoi(tok.c_str()));
+        a = b + 1;
+      }
       const int                 REC = 8 + 16;
       std::vector<double>       out(n * REC, 0.0);
       std::vector<double>       x(dim);
       for (std::size_t i = 0; i < n; ++i) {
-        for (unsigned d = 0; d < dim; ++d) x[d] = u[i * dim + d];
+        for (unsigned d = 0; d < dim; ++d) x[d] = u[i * stride + d];
+        gra::replay::clear();
+        for (int k : spec) gra::replay::push(k < 0 ? 0.5 : u[i * stride + k]);
         gra::AuxIntData aux;
         const double    W = proc->EventWeight(x, aux);
+        if (!spec.empty() && gra::replay::remaining() != 0) {
+          std::fprintf(stderr, "replay: %zu values not consumed at point %zu\n",
+                       gra::replay::remaining(), i);
+          return 5;
+        }
         double *        r = &out[i * REC];
         r[0]              = W;
         r[1]              = aux.kinematics_ok;

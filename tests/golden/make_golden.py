@@ -30,12 +30,18 @@ PROC = "PP[CON]<C> -> pi+ pi-"
 TMP = os.path.join(REPO, "_work", "golden_tmp")
 
 
-def run_weights(card, u, extra=()):
+def run_weights(card, u, extra=(), proc=PROC, dim=None):
+    """Reference weights of points u (n x 8). For <F> the process dimension is 6 and
+    the decay angles are served from u[:, 6:8] through the RNG replay (the two pion
+    off-shell mass draws, numerically inert at width 2.5e-17 GeV, take 0.5)."""
     os.makedirs(TMP, exist_ok=True)
     uf = os.path.join(TMP, "u.bin")
     wf = os.path.join(TMP, "w.bin")
     u.astype(np.float64).tofile(uf)
-    cmd = [REF_BIN, "weights", card, PROC, uf, str(u.shape[1]), wf] + list(extra)
+    dim = dim or u.shape[1]
+    cmd = [REF_BIN, "weights", card, proc, uf, str(dim), wf] + list(extra)
+    if dim != u.shape[1]:
+        cmd += ["--stride", str(u.shape[1])]
     subprocess.run(cmd, check=True, capture_output=True)
     r = np.fromfile(wf).reshape(-1, 24)
     return dict(w=r[:, 0], kin=r[:, 1].astype(np.uint8), fid=r[:, 2].astype(np.uint8),
@@ -107,6 +113,18 @@ def main():
     u = philox_np.uniforms(12, 96, 8)
     r = run_weights(CARD_SCR, u, ["--nbt", "1024", "--nkt2", "10000"])
     save("c2_screened_15x12_weights.npz", seed=12, u=u, n_bt=1024, n_kt2=10000, loop_kt=15,
+         loop_phi=12, loop_ktmax=1.75, **r)
+
+    # <F>: factorized phase space, decay angles lifted into u[6], u[7].
+    PROC_F = "PP[CON]<F> -> pi+ pi-"
+    REPLAY_F = ["--replay", "h,h,6,7"]
+    u = philox_np.uniforms(31, 2048, 8)
+    r = run_weights(CARD, u, REPLAY_F, proc=PROC_F, dim=6)
+    save("f_tree_weights.npz", seed=31, u=u, **r)
+    u = philox_np.uniforms(32, 96, 8)
+    r = run_weights(CARD_SCR, u, REPLAY_F + ["--nbt", "1024", "--nkt2", "10000"], proc=PROC_F,
+                    dim=6)
+    save("f_screened_15x12_weights.npz", seed=32, u=u, n_bt=1024, n_kt2=10000, loop_kt=15,
          loop_phi=12, loop_ktmax=1.75, **r)
 
     # VEGAS integration of c1 (reference ranlux48 points, 8 threads).

@@ -34,7 +34,13 @@ def test_identical_particles_symmetry_factor():
     assert P.s_factor == 2.0
 
 
-@pytest.mark.parametrize("proc", ["PP[RES]<C> -> pi+ pi-", "PP[CON]<F> -> pi+ pi-",
+def test_factorized_params():
+    P = card.build_params(card.read_card(CARD), "PP[CON]<F> -> pi+ pi-")
+    assert P.phase_space == 2 and (P.gcuts.Y_min, P.gcuts.Y_max) == (-0.9, 0.9)
+    assert (P.gcuts.M_min, P.gcuts.M_max) == (0.0, 5.0)
+
+
+@pytest.mark.parametrize("proc", ["PP[RES]<C> -> pi+ pi-", "PP[CON]<Q> -> pi+ pi-",
                                   "PP[CON]<C> -> pi+ pi- pi+ pi-", "yy[CON]<C> -> mu+ mu-"])
 def test_unsupported_processes_are_rejected(proc):
     with pytest.raises(card.UnsupportedProcess):

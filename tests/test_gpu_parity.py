@@ -163,3 +163,70 @@ def test_screened_mixed_vs_oracle_c2_grid(gpu, params_screened):
     print("mixed-precision screened weights: max rel %.3e, median %.3e, >1e-5: %d of %d" %
           (r.max(), np.median(r), int((r > 1e-5).sum()), r.size))
     assert ok
+
+
+def _params_F(screened=False):
+    from graniitti_gb300 import card
+    from conftest import CARD, CARD_SCR
+    return card.build_params(card.read_card(CARD_SCR if screened else CARD),
+                             "PP[CON]<F> -> pi+ pi-")
+
+
+def test_factorized_tree_vs_reference(gpu):
+    import graniitti_gb300 as g
+    gl = _load("f_tree_weights.npz")
+    P = _params_F()
+    e = _engine(P)
+    w, fl = e.event_weights(gl["u"], prec=g.FP64)
+    wo, flo = orc.weights(P, gl["u"])
+    assert np.array_equal(fl & 1, gl["kin"])
+    kin = gl["kin"] == 1
+    assert np.array_equal(((fl >> 1) & 1)[kin], gl["fid"][kin])
+    assert np.array_equal(fl, flo)
+    assert _rel(w, gl["w"]).max() < TOL_FP64_REF
+    assert _rel(w, wo).max() < TOL_FP64_ORC
+    p4, ts, _ = e.event_kinematics(gl["u"])
+    scale = np.abs(gl["p4"]).max(axis=2, keepdims=True)
+    assert (np.abs(p4 - gl["p4"])[kin] / scale[kin]).max() < 1e-12
+
+
+def test_factorized_screened_vs_reference(gpu):
+    import graniitti_gb300 as g
+    gl = _load("f_screened_15x12_weights.npz")
+    t = _load("eikonal_nbt1024_nkt10000.npz")
+    P = _params_F(True)
+    e = _engine(P)
+    e.eikonal_set(t["mbt"], t["msa"])
+    w, fl = e.event_weights(gl["u"], prec=g.FP64)
+    assert np.array_equal(fl & 1, gl["kin"])
+    assert _rel(w, gl["w"]).max() < 1e-9
+    wm, _ = e.event_weights(gl["u"], prec=g.MIXED)
+    import ctypes
+    Pb = type(P)()
+    ctypes.memmove(ctypes.byref(Pb), ctypes.byref(P), ctypes.sizeof(P))
+    Pb.screening = 0
+    wb, _ = _engine(Pb).event_weights(gl["u"], prec=g.FP64)
+    ok, rel = _mixed_ok(wm, w, wb)
+    assert ok, rel.max()
+
+
+def test_factorized_vegas_cross_section_vs_oracle_mc(gpu):
+    """<F> and <C> describe the same process: their integrated cross sections
+    agree within statistical errors (the reference's run_compare_PS check)."""
+    import graniitti_gb300 as g
+    from graniitti_gb300 import _abi
+    res = {}
+    for cls in ("C", "F"):
+        from graniitti_gb300 import card
+        from conftest import CARD
+        P = card.build_params(card.read_card(CARD), "PP[CON]<%s> -> pi+ pi-" % cls)
+        e = g.Engine(P, 0)
+        vp = _abi.VegasParams()
+        vp.bins, vp.iter, vp.ncall, vp.lambda_ = 128, 5, 1 << 20, 1.5
+        vp.chi2max, vp.precision, vp.burnin_iter, vp.prec, vp.seed = 10.0, 5e-4, 3, 0, 11
+        res[cls] = e.vegas_integrate(vp)
+    c, f = res["C"], res["F"]
+    pull = (c.sigma - f.sigma) / np.hypot(c.sigma_err, f.sigma_err)
+    print("sigma <C> %.5e +- %.1e, <F> %.5e +- %.1e, pull %.2f" %
+          (c.sigma, c.sigma_err, f.sigma, f.sigma_err, pull))
+    assert abs(pull) < 4

@@ -102,3 +102,27 @@ def test_vegas_grid_uniform_and_refine():
     x3 = orc.vegas_refine(x, f2)
     assert x3[63, 0] < x[63, 0] and np.all(np.diff(x3[:, 0]) > 0)
     assert np.allclose(x3[:, 1:], x[:, 1:], atol=1e-12)
+
+
+def _params_F(screened=False):
+    from graniitti_gb300 import card
+    from conftest import CARD, CARD_SCR
+    return card.build_params(card.read_card(CARD_SCR if screened else CARD),
+                             "PP[CON]<F> -> pi+ pi-")
+
+
+def test_factorized_tree_weights():
+    g = _load("f_tree_weights.npz")
+    w, fl, rec = orc.weights(_params_F(), g["u"], with_rec=True)
+    _check_weights(w, fl, g)
+    kin = g["kin"] == 1
+    p4 = rec[:, 3:].reshape(-1, 4, 4)
+    scale = np.abs(g["p4"]).max(axis=2, keepdims=True)
+    assert (np.abs(p4 - g["p4"])[kin] / scale[kin]).max() < 1e-12
+
+
+def test_factorized_screened_weights():
+    g = _load("f_screened_15x12_weights.npz")
+    t = _load("eikonal_nbt1024_nkt10000.npz")
+    w, fl = orc.weights(_params_F(True), g["u"], msa=t["msa"], nthreads=4)
+    _check_weights(w, fl, g, tol=1e-9)
