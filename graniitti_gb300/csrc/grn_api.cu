@@ -103,6 +103,7 @@ struct grn_engine {
   int         nblocks = 0;
   DevBuf      d_xmat, d_xmat_prev, d_f2mat, d_f, d_acc, d_parts, d_sc;
   DevBuf      d_lidx, d_lx, d_lvw, d_lbins;  // screened work list of a VEGAS pass
+  DevBuf      d_recf, d_recd;                // loop records (record mode), shared by calls
   double     *h_sc = nullptr;  // pinned
   double      sumdata = 0, sumchi2 = 0, sweight = 0;
   double      maxf = 0, maxW = 0;
@@ -367,7 +368,7 @@ grn_status grn_destroy(grn_engine *e) {
                     &e->d_wlist, &e->d_wcount, &e->d_xmat,      &e->d_xmat_prev, &e->d_f2mat,
                     &e->d_f,     &e->d_acc,    &e->d_parts,     &e->d_sc,        &e->d_lidx,
                     &e->d_lx,    &e->d_lvw,    &e->d_lbins,     &e->d_uw_counts, &e->d_uw_misc,
-                    &e->d_uw_idx};
+                    &e->d_uw_idx, &e->d_recf,  &e->d_recd};
   for (DevBuf *b : bufs) b->release();
   if (e->h_sc) cudaFreeHost(e->h_sc);
   if (e->ev0) cudaEventDestroy(e->ev0);
@@ -492,9 +493,19 @@ grn_status grn_event_weights(grn_engine *e, const double *u, int64_t n, int32_t 
   GRN_CUDA(e->d_wlist.ensure(n * sizeof(int64_t)));
   GRN_CUDA(e->d_wcount.ensure(sizeof(unsigned long long)));
   if (e->loop_blocks == 0) e->loop_blocks = grn::loop_grid_blocks(e->device);
-  GRN_CUDA(grn::launch_event_weights(e->args(), prec, du, n, dim, dw, df, e->d_wlist.as<int64_t>(),
-                                     e->d_wcount.as<unsigned long long>(), e->loop_blocks,
-                                     e->stream));
+  const KArgs a = e->args();
+  if (grn::record_mode(a, prec)) {
+    GRN_CUDA(e->d_recf.ensure(static_cast<size_t>(n) * grn::kLoopEventFields * sizeof(float)));
+    GRN_CUDA(e->d_recd.ensure(static_cast<size_t>(n) * grn::kRecordDoubles * sizeof(double)));
+    GRN_CUDA(grn::launch_event_weights_rec(a, du, n, dim, dw, df, e->d_wlist.as<int64_t>(),
+                                           e->d_recf.as<float>(), e->d_recd.as<double>(),
+                                           e->d_wcount.as<unsigned long long>(), e->loop_blocks,
+                                           e->stream));
+  } else {
+    GRN_CUDA(grn::launch_event_weights(a, prec, du, n, dim, dw, df, e->d_wlist.as<int64_t>(),
+                                       e->d_wcount.as<unsigned long long>(), e->loop_blocks,
+                                       e->stream));
+  }
   if (!dev_w)
     GRN_CUDA(cudaMemcpyAsync(w_out, dw, n * sizeof(double), cudaMemcpyDeviceToHost, e->stream));
   if (flags && !dev_f)
@@ -558,6 +569,10 @@ static grn_status vegas_alloc_calls(grn_engine *e, int64_t ncall) {
   GRN_CUDA(e->d_lx.ensure(8 * n * sizeof(double)));
   GRN_CUDA(e->d_lvw.ensure(n * sizeof(double)));
   GRN_CUDA(e->d_lbins.ensure(n * sizeof(uint64_t)));
+  if (e->P.screening) {
+    GRN_CUDA(e->d_recf.ensure(n * grn::kLoopEventFields * sizeof(float)));
+    GRN_CUDA(e->d_recd.ensure(n * grn::kRecordDoubles * sizeof(double)));
+  }
   return GRN_OK;
 }
 
@@ -612,18 +627,23 @@ static grn_status vegas_iteration_impl(grn_engine *e, int prec, int mode, int re
   const int nh = e->bins * e->dim;
   GRN_CUDA(cudaMemcpyAsync(e->d_xmat_prev.p, e->d_xmat.p, nh * sizeof(double),
                            cudaMemcpyDeviceToDevice, e->stream));
-  GRN_CUDA(grn::launch_vegas_born(e->args(), e->d_xmat.as<double>(), e->bins, e->dim, e->ncall,
-                                  e->seed, stream_id, mode != 0, e->d_f.as<double>(),
+  const KArgs a   = e->args();
+  const bool  rec = grn::record_mode(a, prec);
+  float      *rf  = rec ? e->d_recf.as<float>() : nullptr;
+  double     *rd  = rec ? e->d_recd.as<double>() : nullptr;
+  GRN_CUDA(grn::launch_vegas_born(a, e->d_xmat.as<double>(), e->bins, e->dim, e->ncall, e->seed,
+                                  stream_id, mode != 0, e->d_f.as<double>(),
                                   e->d_f2mat.as<double>(), e->d_acc.as<unsigned long long>(),
                                   e->d_lidx.as<int64_t>(), e->d_lx.as<double>(),
-                                  e->d_lvw.as<double>(), e->d_lbins.as<uint64_t>(), e->stream));
+                                  e->d_lvw.as<double>(), e->d_lbins.as<uint64_t>(), rf, rd,
+                                  e->stream));
   // the timed kernel: the kt-loop stage when screening is on
   GRN_CUDA(cudaEventRecord(e->ev0, e->stream));
-  GRN_CUDA(grn::launch_vegas_loop(e->args(), prec, e->bins, e->dim, e->ncall, mode != 0,
+  GRN_CUDA(grn::launch_vegas_loop(a, prec, e->bins, e->dim, e->ncall, mode != 0,
                                   e->d_f.as<double>(), e->d_f2mat.as<double>(),
                                   e->d_acc.as<unsigned long long>(), e->d_lidx.as<int64_t>(),
                                   e->d_lx.as<double>(), e->d_lvw.as<double>(),
-                                  e->d_lbins.as<uint64_t>(), e->nblocks, e->stream));
+                                  e->d_lbins.as<uint64_t>(), rf, rd, e->nblocks, e->stream));
   GRN_CUDA(cudaEventRecord(e->ev1, e->stream));
   GRN_CUDA(grn::launch_vegas_reduce(e->d_f.as<double>(), e->ncall,
                                     e->d_acc.as<unsigned long long>(), e->d_parts.as<double>(),

@@ -62,14 +62,25 @@ cudaError_t launch_vegas_grid_init(double *xmat, int bins, int dim, cudaStream_t
 // One VEGAS pass in two stages; acc holds VS_COUNT + 1 unsigned long long
 // accumulators (the last one is the work-list length); the list arrays have
 // capacity ncall (l_x: 8 x ncall, dimension-major).
+// rf/rd: loop records (record mode, see record_mode()); null for the point mode,
+// in which the mapped points l_x are stored and stage B recomputes the tree level.
 cudaError_t launch_vegas_born(const KArgs &a, const double *xmat, int bins, int dim, int64_t ncall,
                               uint64_t seed, uint32_t stream, int track_max, double *f_out,
                               double *f2mat, unsigned long long *acc, int64_t *l_idx, double *l_x,
-                              double *l_vw, uint64_t *l_bins, cudaStream_t st);
+                              double *l_vw, uint64_t *l_bins, float *rf, double *rd,
+                              cudaStream_t st);
 cudaError_t launch_vegas_loop(const KArgs &a, int prec, int bins, int dim, int64_t ncall,
                               int track_max, double *f_out, double *f2mat, unsigned long long *acc,
                               const int64_t *l_idx, const double *l_x, const double *l_vw,
-                              const uint64_t *l_bins, int nblocks, cudaStream_t st);
+                              const uint64_t *l_bins, const float *rf, const double *rd,
+                              int nblocks, cudaStream_t st);
+// Record mode: screened, FP32 loop, single active trajectory.
+bool        record_mode(const KArgs &a, int prec);
+constexpr int kRecordDoubles = 4;
+cudaError_t launch_event_weights_rec(const KArgs &a, const double *u, int64_t n, int dim,
+                                     double *w, uint8_t *flags, int64_t *list, float *rf,
+                                     double *rd, unsigned long long *count, int loop_blocks,
+                                     cudaStream_t st);
 constexpr int kVegasSumParts = 256;
 cudaError_t launch_vegas_reduce(const double *f_out, int64_t ncall,
                                 const unsigned long long *acc, double *part, double *sc,

@@ -16,6 +16,12 @@
 
 #include "grn_internal.cuh"
 
+// Resident blocks per SM requested for the FP32 loop kernels (register budget
+// 65536 / (128 threads x GRN_LOOP_MIN_BLOCKS)).
+#ifndef GRN_LOOP_MIN_BLOCKS
+#define GRN_LOOP_MIN_BLOCKS 4
+#endif
+
 namespace grn {
 
 // ---------------------------------------------------------------------------
@@ -164,6 +170,79 @@ __device__ __forceinline__ cx<double> loop_dispatch(const KArgs &A, const Born &
   return loop_integral<T>(A, b, skt, sphi);
 }
 
+// Loop records: stage A writes, per screened event that passed the cuts, the
+// per-event fields of the FP32 loop (kLoopEventFields floats) and four doubles
+// (exp(Emax), Re A0, Im A0, phase-space Jacobian), structure of arrays with
+// capacity cap; stage B reads them and runs only FP32 arithmetic.
+__device__ __forceinline__ void store_record(const LoopEventF<float> &e, double a0r, double a0i,
+                                             double jac, float *__restrict__ rf,
+                                             double *__restrict__ rd, int64_t slot,
+                                             int64_t cap) {
+  int k = 0;
+#define GRN_STORE(fld) rf[static_cast<int64_t>(k++) * cap + slot] = e.fld;
+  GRN_LOOP_EVENT_FIELDS(GRN_STORE)
+#undef GRN_STORE
+  rd[slot]           = e.escale;
+  rd[cap + slot]     = a0r;
+  rd[2 * cap + slot] = a0i;
+  rd[3 * cap + slot] = jac;
+}
+
+__device__ __forceinline__ void load_record(LoopEventF<float> &e, double &a0r, double &a0i,
+                                            double &jac, const float *__restrict__ rf,
+                                            const double *__restrict__ rd, int64_t slot,
+                                            int64_t cap) {
+  int k = 0;
+#define GRN_LOAD(fld) e.fld = rf[static_cast<int64_t>(k++) * cap + slot];
+  GRN_LOOP_EVENT_FIELDS(GRN_LOAD)
+#undef GRN_LOAD
+  e.escale = rd[slot];
+  a0r      = rd[cap + slot];
+  a0i      = rd[2 * cap + slot];
+  jac      = rd[3 * cap + slot];
+}
+
+// Loop integral of a loaded record (constants of e already set).
+__device__ __forceinline__ cx<double> loop_integral_rec(const KArgs &A, const LoopEventF<float> &e,
+                                                        const KtNode<float> *skt,
+                                                        const PhiNode<float> *sphi) {
+  float ar = 0.f, ai = 0.f, cr = 0.f, ci = 0.f;
+  for (int j = 0; j < A.n_kt_nodes; ++j) {
+    const KtNode<float> nj = skt[j];
+    const float         k2 = nj.kt * nj.kt;
+    float ir = 0.f, ii = 0.f, dr = 0.f, di = 0.f;
+    for (int i = 0; i < A.n_phi_nodes; ++i) {
+      const PhiNode<float> ni = sphi[i];
+      cx<float> a;
+      if (loop_point_amp_fast<float>(e, nj.kt * ni.c, nj.kt * ni.s, k2, a)) {
+        kahan_add(ir, dr, ni.u * a.re);
+        kahan_add(ii, di, ni.u * a.im);
+      }
+    }
+    kahan_add(ar, cr, nj.cre * ir - nj.cim * ii);
+    kahan_add(ai, ci, nj.cre * ii + nj.cim * ir);
+  }
+  const double sr = double(ar) * e.escale, si = double(ai) * e.escale;
+  return {A.loop_norm_re * sr - A.loop_norm_im * si, A.loop_norm_re * si + A.loop_norm_im * sr};
+}
+
+// Screened weight from a record: W = Jacobian x |A0 + A_loop|^2 (NaN/Inf -> 0).
+__device__ __forceinline__ double record_weight(const KArgs &A, const LoopEventF<float> &e,
+                                                double a0r, double a0i, double jac,
+                                                const KtNode<float> *skt,
+                                                const PhiNode<float> *sphi, uint8_t &flags) {
+  const cx<double> Al = loop_integral_rec(A, e, skt, sphi);
+  const double re = a0r + Al.re, im = a0i + Al.im;
+  double W = jac * (re * re + im * im);
+  flags = GRN_FLAG_KINEMATICS_OK | GRN_FLAG_FIDCUTS_OK | GRN_FLAG_VETOCUTS_OK |
+          GRN_FLAG_AMPLITUDE_OK;
+  if (!isfinite(W)) {
+    W = 0.0;
+    flags &= ~GRN_FLAG_AMPLITUDE_OK;
+  }
+  return W;
+}
+
 // Tree-level stage of one event: kinematics, cuts and, when the process is not
 // screened, the full weight. Returns true when the event still needs the kt-loop.
 __device__ __forceinline__ bool born_stage(const KArgs &A, const double *x, Born &b, double &W,
@@ -299,6 +378,75 @@ cudaError_t launch_event_weights(const KArgs &a, int prec, const double *u, int6
       k_weights_loop<double><<<loop_blocks, kWeightThreads, 0, st>>>(a, u, dim, list, count, w,
                                                                      flags);
   }
+  return cudaGetLastError();
+}
+
+// Record-mode user-array stages (FP32 loop, single active trajectory).
+__global__ void __launch_bounds__(kWeightThreads)
+    k_weights_born_rec(const KArgs A, const double *__restrict__ u, int64_t n, int dim,
+                       double *__restrict__ w, uint8_t *__restrict__ flags,
+                       int64_t *__restrict__ list, float *__restrict__ rf,
+                       double *__restrict__ rd, unsigned long long *__restrict__ count) {
+  const int64_t i = static_cast<int64_t>(blockIdx.x) * blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  double x[8];
+#pragma unroll
+  for (int d = 0; d < 8; ++d) x[d] = u[i * dim + d];
+  Born       b;
+  double     W;
+  uint8_t    f;
+  const bool loop = born_stage(A, x, b, W, f);
+  const int64_t slot = list_append(loop, count);
+  if (loop) {
+    LoopEventF<float> e;
+    double            a0r, a0i;
+    make_loop_event_fast<float>(A.P, A.K, b, e, &a0r, &a0i);
+    list[slot] = i;
+    store_record(e, a0r, a0i, weight_jacobian(A.K, b), rf, rd, slot, n);
+  } else {
+    w[i] = W;
+    if (flags) flags[i] = f;
+  }
+}
+
+__global__ void __launch_bounds__(kWeightThreads, GRN_LOOP_MIN_BLOCKS)
+    k_weights_loop_rec(const KArgs A, const int64_t *__restrict__ list,
+                       const float *__restrict__ rf, const double *__restrict__ rd, int64_t cap,
+                       const unsigned long long *__restrict__ count, double *__restrict__ w,
+                       uint8_t *__restrict__ flags) {
+  __shared__ KtNode<float>  skt[kMaxLoopNodes];
+  __shared__ PhiNode<float> sphi[kMaxLoopNodes];
+  stage_nodes<float>(A, skt, sphi);
+  __syncthreads();
+  LoopEventF<float> e;
+  make_loop_consts_fast<float>(A.P, A.K, e);
+  const int64_t cnt = static_cast<int64_t>(*count);
+  for (int64_t r = static_cast<int64_t>(blockIdx.x) * blockDim.x + threadIdx.x; r < cnt;
+       r += static_cast<int64_t>(gridDim.x) * blockDim.x) {
+    double a0r, a0i, jac;
+    load_record(e, a0r, a0i, jac, rf, rd, r, cap);
+    uint8_t f;
+    const int64_t i = list[r];
+    w[i] = record_weight(A, e, a0r, a0i, jac, skt, sphi, f);
+    if (flags) flags[i] = f;
+  }
+}
+
+bool record_mode(const KArgs &a, int prec) {
+  return a.P.screening && prec == GRN_PREC_MIXED && a.K.n_active == 1;
+}
+
+cudaError_t launch_event_weights_rec(const KArgs &a, const double *u, int64_t n, int dim,
+                                     double *w, uint8_t *flags, int64_t *list, float *rf,
+                                     double *rd, unsigned long long *count, int loop_blocks,
+                                     cudaStream_t st) {
+  if (n <= 0) return cudaSuccess;
+  cudaError_t e = cudaMemsetAsync(count, 0, sizeof(unsigned long long), st);
+  if (e != cudaSuccess) return e;
+  const unsigned blocks = static_cast<unsigned>((n + kWeightThreads - 1) / kWeightThreads);
+  k_weights_born_rec<<<blocks, kWeightThreads, 0, st>>>(a, u, n, dim, w, flags, list, rf, rd,
+                                                         count);
+  k_weights_loop_rec<<<loop_blocks, kWeightThreads, 0, st>>>(a, list, rf, rd, n, count, w, flags);
   return cudaGetLastError();
 }
 
@@ -612,7 +760,8 @@ __global__ void __launch_bounds__(kVegasThreads)
                  uint64_t seed, uint32_t stream, int track_max, double *__restrict__ f_out,
                  double *__restrict__ f2mat, unsigned long long *__restrict__ acc,
                  int64_t *__restrict__ l_idx, double *__restrict__ l_x, double *__restrict__ l_vw,
-                 uint64_t *__restrict__ l_bins, int64_t cap) {
+                 uint64_t *__restrict__ l_bins, int64_t cap, float *__restrict__ rf,
+                 double *__restrict__ rd) {
   extern __shared__ double dsm[];
   double   *sx = dsm, *sf2 = dsm + bins * dim;
   const int nh = bins * dim;
@@ -631,11 +780,11 @@ __global__ void __launch_bounds__(kVegasThreads)
     bool       loop   = false;
     double     x[kMaxDim], vw = 0.0;
     uint64_t   pb = 0ull;
+    Born       b;
     if (active) {
       double u[kMaxDim];
       philox_point(seed, stream, static_cast<uint64_t>(e), dim, u);
       vw = vegas_map(sx, bins, dim, u, x, pb);
-      Born    b;
       double  W;
       uint8_t fl;
       loop = born_stage(A, x, b, W, fl);
@@ -657,10 +806,17 @@ __global__ void __launch_bounds__(kVegasThreads)
     }
     const int64_t slot = list_append(loop, &acc[VS_COUNT]);
     if (loop && slot < cap) {
-      l_idx[slot] = e;
-      for (int j = 0; j < kMaxDim; ++j) l_x[static_cast<int64_t>(j) * cap + slot] = x[j];
+      l_idx[slot]  = e;
       l_vw[slot]   = vw;
       l_bins[slot] = pb;
+      if (rf) {
+        LoopEventF<float> le;
+        double            a0r, a0i;
+        make_loop_event_fast<float>(A.P, A.K, b, le, &a0r, &a0i);
+        store_record(le, a0r, a0i, weight_jacobian(A.K, b), rf, rd, slot, cap);
+      } else {
+        for (int j = 0; j < kMaxDim; ++j) l_x[static_cast<int64_t>(j) * cap + slot] = x[j];
+      }
     }
   }
   flush_block(sf2, nh, f2mat, acc, cnt, maxf, maxW);
@@ -707,10 +863,51 @@ __global__ void __launch_bounds__(kVegasThreads)
   flush_block(sf2, nh, f2mat, acc, cnt, maxf, maxW);
 }
 
+// Stage B, record mode: FP32 loop of the listed events from their records.
+__global__ void __launch_bounds__(kVegasThreads, GRN_LOOP_MIN_BLOCKS)
+    k_vegas_loop_rec(const KArgs A, int bins, int dim, int track_max, double *__restrict__ f_out,
+                     double *__restrict__ f2mat, unsigned long long *__restrict__ acc,
+                     const int64_t *__restrict__ l_idx, const double *__restrict__ l_vw,
+                     const uint64_t *__restrict__ l_bins, const float *__restrict__ rf,
+                     const double *__restrict__ rd, int64_t cap) {
+  extern __shared__ double dsm[];
+  double *sf2 = dsm;
+  __shared__ KtNode<float>  skt[kMaxLoopNodes];
+  __shared__ PhiNode<float> sphi[kMaxLoopNodes];
+  const int nh = bins * dim;
+  for (int i = threadIdx.x; i < nh; i += blockDim.x) sf2[i] = 0.0;
+  stage_nodes<float>(A, skt, sphi);
+  __syncthreads();
+  LoopEventF<float> e;
+  make_loop_consts_fast<float>(A.P, A.K, e);
+  unsigned long long cnt[VS_COUNT] = {};
+  double maxf = 0.0, maxW = 0.0;
+  const int64_t n      = min(static_cast<int64_t>(acc[VS_COUNT]), cap);
+  const int64_t stride = static_cast<int64_t>(gridDim.x) * blockDim.x;
+  for (int64_t r = static_cast<int64_t>(blockIdx.x) * blockDim.x + threadIdx.x; r < n;
+       r += stride) {
+    double a0r, a0i, jac;
+    load_record(e, a0r, a0i, jac, rf, rd, r, cap);
+    uint8_t      fl;
+    const double W = record_weight(A, e, a0r, a0i, jac, skt, sphi, fl);
+    const double f = W * l_vw[r];
+    f_out[l_idx[r]] = f;
+    hist_add(sf2, dim, l_bins[r], f * f);
+    cnt[VS_AMP_OK] += (fl & GRN_FLAG_AMPLITUDE_OK) ? 1 : 0;
+    cnt[VS_NAN] += (fl & GRN_FLAG_AMPLITUDE_OK) ? 0 : 1;
+    if (track_max) {
+      maxf = fmax(maxf, f);
+      maxW = fmax(maxW, W);
+    }
+  }
+  __syncwarp();
+  flush_block(sf2, nh, f2mat, acc, cnt, maxf, maxW);
+}
+
 int vegas_grid_blocks(int device) {
   int sms = 0, per = 0;
   cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, device);
-  cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, k_vegas_loop<float>, kVegasThreads,
+  cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, k_vegas_loop_rec, kVegasThreads,
                                                 kMaxBins * kMaxDim * sizeof(double));
   if (per < 1) per = 1;
   return sms * per;
@@ -719,7 +916,8 @@ int vegas_grid_blocks(int device) {
 cudaError_t launch_vegas_born(const KArgs &a, const double *xmat, int bins, int dim, int64_t ncall,
                               uint64_t seed, uint32_t stream, int track_max, double *f_out,
                               double *f2mat, unsigned long long *acc, int64_t *l_idx, double *l_x,
-                              double *l_vw, uint64_t *l_bins, cudaStream_t st) {
+                              double *l_vw, uint64_t *l_bins, float *rf, double *rd,
+                              cudaStream_t st) {
   const int nh = bins * dim;
   cudaMemsetAsync(f2mat, 0, nh * sizeof(double), st);
   cudaMemsetAsync(acc, 0, (VS_COUNT + 1) * sizeof(unsigned long long), st);
@@ -730,16 +928,22 @@ cudaError_t launch_vegas_born(const KArgs &a, const double *xmat, int bins, int 
   const int     ba   = static_cast<int>(std::min<int64_t>(want, static_cast<int64_t>(sms) * 16));
   k_vegas_born<<<ba, kVegasThreads, 2 * nh * sizeof(double), st>>>(
       a, xmat, bins, dim, ncall, seed, stream, track_max, f_out, f2mat, acc, l_idx, l_x, l_vw,
-      l_bins, ncall);
+      l_bins, ncall, rf, rd);
   return cudaGetLastError();
 }
 
 cudaError_t launch_vegas_loop(const KArgs &a, int prec, int bins, int dim, int64_t ncall,
                               int track_max, double *f_out, double *f2mat, unsigned long long *acc,
                               const int64_t *l_idx, const double *l_x, const double *l_vw,
-                              const uint64_t *l_bins, int nblocks, cudaStream_t st) {
+                              const uint64_t *l_bins, const float *rf, const double *rd,
+                              int nblocks, cudaStream_t st) {
   if (!a.P.screening) return cudaSuccess;
   const int nh = bins * dim;
+  if (rf) {
+    k_vegas_loop_rec<<<nblocks, kVegasThreads, nh * sizeof(double), st>>>(
+        a, bins, dim, track_max, f_out, f2mat, acc, l_idx, l_vw, l_bins, rf, rd, ncall);
+    return cudaGetLastError();
+  }
   if (prec == GRN_PREC_MIXED)
     k_vegas_loop<float><<<nblocks, kVegasThreads, nh * sizeof(double), st>>>(
         a, bins, dim, track_max, f_out, f2mat, acc, l_idx, l_x, l_vw, l_bins, ncall);

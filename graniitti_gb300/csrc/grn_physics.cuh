@@ -461,6 +461,16 @@ GRN_HD float fast_exp(float x) {
 #endif
 }
 
+// Per-event fields of the fast loop (stored between the two kernel stages).
+#define GRN_LOOP_EVENT_FIELDS(X)                                                              \
+  X(p1x) X(p1y) X(p2x) X(p2y) X(p3x) X(p3y) X(p4x) X(p4y) X(p3p) X(p3m) X(p4p) X(p4m) X(ia1) \
+  X(ia2) X(q1c) X(q2c) X(x10) X(x20) X(r10) X(r20) X(mT1s0) X(mT2s0) X(T1n0) X(T2n0) X(t10)   \
+  X(t20) X(is13) X(is14) X(is23) X(is24) X(L13) X(L14) X(L23) X(L24) X(a10) X(a20) X(dpa0)    \
+  X(dma0) X(dpb0) X(dmb0) X(c3x) X(c3y) X(c4x) X(c4y) X(fa0) X(fb0) X(rho_t) X(rho_u)         \
+  X(pre_re) X(pre_im)
+#define GRN_COUNT_FIELD(f) +1
+constexpr int kLoopEventFields = 0 GRN_LOOP_EVENT_FIELDS(GRN_COUNT_FIELD);
+
 template <typename T>
 struct LoopEventF {
   // tree-level transverse momenta
@@ -485,9 +495,29 @@ struct LoopEventF {
   int ffmode;
 };
 
+// Per-engine constants of the fast loop.
+template <typename T>
+GRN_HD void make_loop_consts_fast(const grn_process_params &P, const Consts &K,
+                                  LoopEventF<T> &e) {
+  const int k = K.active[0] ? 0 : (K.active[1] ? 1 : 2);
+  e.L = T(K.L); e.invL = T(1.0 / K.L); e.invL2 = T(1.0 / (K.L * K.L));
+  e.mp2 = T(K.mp2); e.M2 = T(K.M2prop);
+  e.ap = T(P.regge.ap[k]);
+  e.ifc1 = T(1.0 / P.soft.fc1); e.ifc2 = T(1.0 / P.soft.fc2);
+  e.ffmode = P.regge.offshellFF;
+  e.ff_a2 = T(P.regge.a_OREAR * P.regge.a_OREAR);
+  e.ff_ab = T(P.regge.a_OREAR * P.regge.b_OREAR);
+  e.ff_b = T(e.ffmode == 2 ? P.regge.b_POW : (e.ffmode == 0 ? P.regge.b_EXP : P.regge.b_OREAR));
+}
+
+// Per-event part of the fast loop from the tree-level event (FP64 here), and the
+// tree-level amplitude A0 from the same quantities (A0 = the fast loop point at
+// k = 0, evaluated in FP64 and multiplied by exp(Emax)).
 template <typename T>
 GRN_HD void make_loop_event_fast(const grn_process_params &P, const Consts &K, const Born &b,
-                                 LoopEventF<T> &e) {
+                                 LoopEventF<T> &e, double *A0re = nullptr,
+                                 double *A0im = nullptr) {
+  make_loop_consts_fast<T>(P, K, e);
   e.p1x = T(b.p1x); e.p1y = T(b.p1y); e.p2x = T(b.p2x); e.p2y = T(b.p2y);
   e.p3x = T(b.p3x); e.p3y = T(b.p3y); e.p4x = T(b.p4x); e.p4y = T(b.p4y);
   e.p3p = T(b.p3p); e.p3m = T(b.p3m); e.p4p = T(b.p4p); e.p4m = T(b.p4m);
@@ -495,7 +525,6 @@ GRN_HD void make_loop_event_fast(const grn_process_params &P, const Consts &K, c
   const double ia1 = 1.0 / (1.0 - a1), ia2 = 1.0 / (1.0 - a2);
   e.ia1 = T(ia1); e.ia2 = T(ia2); e.q1c = T(ia1 * ia1 * ia2); e.q2c = T(ia2 * ia2 * ia1);
   const double L = K.L, invL = 1.0 / K.L, invL2 = invL * invL, mp2 = K.mp2;
-  e.L = T(L); e.invL = T(invL); e.invL2 = T(invL2); e.mp2 = T(mp2); e.M2 = T(K.M2prop);
   // k = 0 values of the linear closure (same formulas as the loop point, in FP64)
   const double mT1s = mp2 + b.pt1sq, mT2s = mp2 + b.pt2sq;
   const double c1 = mT1s * invL2, c2 = mT2s * invL2;
@@ -521,16 +550,11 @@ GRN_HD void make_loop_event_fast(const grn_process_params &P, const Consts &K, c
   e.L13 = T(L13); e.L14 = T(L14); e.L23 = T(L23); e.L24 = T(L24);
   const int k = K.active[0] ? 0 : (K.active[1] ? 1 : 2);
   const double a0 = P.regge.a0[k], ap = P.regge.ap[k];
-  e.ap = T(ap);
   e.a10 = T(a0 + ap * t1); e.a20 = T(a0 + ap * t2);
   e.dpa0 = T(b.p4p - K.eps + p2p); e.dma0 = T(K.eps - p1m - b.p3m);
   e.dpb0 = T(b.p3p - K.eps + p2p); e.dmb0 = T(K.eps - p1m - b.p4m);
   e.c3x = T(b.p1x + b.p3x); e.c3y = T(b.p1y + b.p3y);
   e.c4x = T(b.p1x + b.p4x); e.c4y = T(b.p1y + b.p4y);
-  e.ifc1 = T(1.0 / P.soft.fc1); e.ifc2 = T(1.0 / P.soft.fc2);
-  e.ffmode = P.regge.offshellFF;
-  e.ff_a2 = T(P.regge.a_OREAR * P.regge.a_OREAR);
-  e.ff_ab = T(P.regge.a_OREAR * P.regge.b_OREAR);
   double pre = K.gN2 * K.g2;
   // tree-level exponents E = a1 L13 + a2 L24 (+ exponential form factors)
   double Et = (a0 + ap * t1) * L13 + (a0 + ap * t2) * L24;
@@ -541,14 +565,11 @@ GRN_HD void make_loop_event_fast(const grn_process_params &P, const Consts &K, c
                     ((b.p1x + b.p4x) * (b.p1x + b.p4x) + (b.p1y + b.p4y) * (b.p1y + b.p4y)) - K.M2prop;
   double fa = 0, fb = 0;
   if (e.ffmode == 2) {
-    e.ff_b = T(P.regge.b_POW);
     pre *= P.regge.b_POW * P.regge.b_POW;
   } else if (e.ffmode == 0) {
-    e.ff_b = T(P.regge.b_EXP);
     fa = -2.0 * P.regge.b_EXP * fabs(ta);
     fb = -2.0 * P.regge.b_EXP * fabs(tb);
   } else {
-    e.ff_b = T(P.regge.b_OREAR);
     fa = 2.0 * (P.regge.a_OREAR * P.regge.b_OREAR -
                 P.regge.b_OREAR * sqrt(fabs(ta) + P.regge.a_OREAR * P.regge.a_OREAR));
     fb = 2.0 * (P.regge.a_OREAR * P.regge.b_OREAR -
@@ -565,8 +586,24 @@ GRN_HD void make_loop_event_fast(const grn_process_params &P, const Consts &K, c
   const double e2r = er * er - ei * ei, e2i = 2.0 * er * ei;
   double sn, cs;
   sincos_pi(-0.5 * ap * (t1 + t2), sn, cs);
-  e.pre_re = T(pre * (e2r * cs - e2i * sn));
-  e.pre_im = T(pre * (e2r * sn + e2i * cs));
+  const double pr = pre * (e2r * cs - e2i * sn), pi = pre * (e2r * sn + e2i * cs);
+  e.pre_re = T(pr);
+  e.pre_im = T(pi);
+  if (A0re) {
+    // tree-level amplitude from the same factors (FP64)
+    const double Pd = (1.0 - t1 / P.soft.fc1) * (1.0 - t1 / P.soft.fc2) *
+                      (1.0 - t2 / P.soft.fc1) * (1.0 - t2 / P.soft.fc2);
+    const double rt = exp(Et - Em), ru = exp(Eu - Em);
+    double m;
+    if (e.ffmode == 2) {
+      const double Da = P.regge.b_POW - ta, Db = P.regge.b_POW - tb;
+      m = (rt * Db * Db * tb + ru * Da * Da * ta) / (Pd * Da * Da * Db * Db * ta * tb);
+    } else {
+      m = (rt * tb + ru * ta) / (Pd * ta * tb);
+    }
+    *A0re = pr * m * e.escale;
+    *A0im = pi * m * e.escale;
+  }
 }
 
 // Bare Regge amplitude at loop momentum k = (kx, ky), k2 = kx^2 + ky^2, relative to
