@@ -32,6 +32,7 @@ GRN_FLAG_VETOCUTS_OK = 4
 GRN_FLAG_AMPLITUDE_OK = 8
 
 GRN_PROC_REGGE_CON = 1
+GRN_PROC_TENSOR_CON = 2
 GRN_PS_CONTINUUM = 1
 GRN_PS_FACTORIZED = 2
 GRN_PREC_FP64 = 0
@@ -50,6 +51,11 @@ class ReggeParams(ctypes.Structure):
                 ("s0", c_double), ("active", c_int32 * 3), ("offshellFF", c_int32),
                 ("c", c_double * 3), ("b_EXP", c_double), ("a_OREAR", c_double),
                 ("b_OREAR", c_double), ("b_POW", c_double)]
+
+
+class TensorParams(ctypes.Structure):
+    _fields_ = [("delta_P", c_double), ("ap_P", c_double), ("gPNN", c_double), ("gPps", c_double),
+                ("em_kelly", c_int32), ("_pad", c_int32)]
 
 
 class GenCuts(ctypes.Structure):
@@ -75,7 +81,7 @@ class ProcessParams(ctypes.Structure):
                 ("screening", c_int32), ("sqrt_s", c_double), ("m_beam", c_double),
                 ("m_central", c_double * 8), ("s_factor", c_double),
                 ("gcuts", GenCuts), ("fcuts", FidCuts), ("soft", SoftParams),
-                ("regge", ReggeParams), ("loop", LoopNumerics)]
+                ("regge", ReggeParams), ("loop", LoopNumerics), ("tensor", TensorParams)]
 
 
 class VegasParams(ctypes.Structure):

@@ -91,8 +91,12 @@ def build_params(card, process=None, tune=None):
     T = TUNES[tune]
     proc = process or pp["PROCESS"]
     istate, channel, cls, finals, _ = parse_process(proc)
-    if not (istate == "PP" and channel == "CON" and cls in ("C", "F") and len(finals) == 2):
-        raise UnsupportedProcess("engine implements PP[CON]<C|F> -> 2-body, got %r" % proc)
+    if not (istate == "PP" and channel in ("CON", "CONTENSOR") and cls in ("C", "F") and
+            len(finals) == 2):
+        raise UnsupportedProcess("engine implements PP[CON|CONTENSOR]<C|F> -> 2-body, got %r"
+                                 % proc)
+    if channel == "CONTENSOR" and not all(f in ("pi+", "pi-", "K+", "K-", "pi0") for f in finals):
+        raise UnsupportedProcess("CONTENSOR is implemented for pseudoscalar pairs (2xS)")
     if int(pp.get("NSTARS", 0)) != 0:
         raise UnsupportedProcess("forward excitation (NSTARS > 0) is not implemented")
     if pp["BEAM"] != ["p+", "p+"]:
@@ -105,7 +109,7 @@ def build_params(card, process=None, tune=None):
     # s = (pbeam1 + pbeam2)^2 with equal energies (MProcess.cc:309-324)
     P.sqrt_s = 2.0 * E1
     P.m_beam = mb
-    P.process = _abi.GRN_PROC_REGGE_CON
+    P.process = _abi.GRN_PROC_REGGE_CON if channel == "CON" else _abi.GRN_PROC_TENSOR_CON
     P.phase_space = _abi.GRN_PS_CONTINUUM if cls == "C" else _abi.GRN_PS_FACTORIZED
     P.n_central = 2
     P.screening = 1 if pp.get("POMLOOP", False) else 0
@@ -183,6 +187,13 @@ def build_params(card, process=None, tune=None):
     for k in range(3):
         P.regge.c[k] = cpl["c"][k]
         P.regge.active[k] = 1 if cpl["n"][k] else 0
+
+    # Tensor-pomeron parameters (MTensorPomeronParam; pion or kaon coupling chosen by
+    # the first central mass, MTensorPomeron.cc:730).
+    tp = T["PARAM_TENSORPOM"]
+    P.tensor.delta_P, P.tensor.ap_P, P.tensor.gPNN = tp["delta_P"], tp["ap_P"], tp["gPNN"]
+    P.tensor.gPps = tp["gPpipi"] if P.m_central[0] < 0.2 else tp["gPKK"]
+    P.tensor.em_kelly = 1 if T["PARAM_STRUCTURE"]["EM"] == "KELLY" else 0
 
     # Loop numerics: defaults 15 x 12 moved by 3*ND (MEikonal.h:40-57), tables
     # 10000 intervals (modeldata/NUMERICS.json).

@@ -141,9 +141,13 @@ namespace {
 
 grn_status derive_consts(const grn_process_params &P, grn::Consts &K) {
   using namespace grn;
-  if (P.process != GRN_PROC_REGGE_CON ||
+  if ((P.process != GRN_PROC_REGGE_CON && P.process != GRN_PROC_TENSOR_CON) ||
       (P.phase_space != GRN_PS_CONTINUUM && P.phase_space != GRN_PS_FACTORIZED))
-    return fail(GRN_ERR_UNSUPPORTED, "only PP[CON]<C|F> (Regge continuum) is implemented");
+    return fail(GRN_ERR_UNSUPPORTED,
+                "only PP[CON|CONTENSOR]<C|F> 2-body continua are implemented");
+  if (P.process == GRN_PROC_TENSOR_CON &&
+      !(P.tensor.ap_P > 0 && P.tensor.gPNN > 0 && P.tensor.gPps > 0))
+    return fail(GRN_ERR_INVALID, "tensor-pomeron parameters are not set");
   if (P.n_central != 2) return fail(GRN_ERR_UNSUPPORTED, "only 2-body central states");
   if (!(P.sqrt_s > 2 * P.m_beam)) return fail(GRN_ERR_INVALID, "sqrt_s below threshold");
   if (!(P.gcuts.fpt_max > 0) || !(P.gcuts.kt_max > P.gcuts.kt_min) ||
@@ -325,6 +329,8 @@ void grn_default_params(grn_process_params *p) {
   r.b_EXP = 0.944; r.a_OREAR = 0.638; r.b_OREAR = 1.886; r.b_POW = 0.5;
   // Loop numerics: 15 x 12 intervals, kt in [1e-4, 1.75]; tables 10000 intervals
   p->loop = {15, 12, 1e-4, 1.75, 10000, 10000};
+  // TUNE0 PARAM_TENSORPOM, pion coupling; Kelly proton form factors (GENERAL.json:178-219)
+  p->tensor = {0.0808, 0.25, 1.87, 1.76, 1, 0};
 }
 
 const char *grn_last_error(void) { return g_last_error.c_str(); }

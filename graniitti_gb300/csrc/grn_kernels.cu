@@ -19,7 +19,7 @@
 // Resident blocks per SM requested for the FP32 loop kernels (register budget
 // 65536 / (128 threads x GRN_LOOP_MIN_BLOCKS)).
 #ifndef GRN_LOOP_MIN_BLOCKS
-#define GRN_LOOP_MIN_BLOCKS 4
+#define GRN_LOOP_MIN_BLOCKS 3
 #endif
 
 namespace grn {
@@ -165,7 +165,8 @@ template <typename T>
 __device__ __forceinline__ cx<double> loop_dispatch(const KArgs &A, const Born &b,
                                                     const KtNode<T> *skt, const PhiNode<T> *sphi) {
   if constexpr (sizeof(T) == sizeof(float)) {
-    if (A.K.n_active == 1) return loop_integral_fast(A, b, skt, sphi);
+    if (A.K.n_active == 1 && A.P.process == GRN_PROC_REGGE_CON)
+      return loop_integral_fast(A, b, skt, sphi);
   }
   return loop_integral<T>(A, b, skt, sphi);
 }
@@ -254,8 +255,7 @@ __device__ __forceinline__ bool born_stage(const KArgs &A, const double *x, Born
   W = 0.0;
   if (!(kin && fid)) return false;
   if (A.P.screening) return true;
-  const cx<double> A0 = regge_me4<double>(A.P, A.K, b.t1, b.t2, log(b.s13), log(b.s14),
-                                          log(b.s23), log(b.s24), b.that, b.uhat);
+  const cx<double> A0 = born_amp(A.P, A.K, b);
   W = weight_jacobian(A.K, b) * (A0.re * A0.re + A0.im * A0.im);
   if (!isfinite(W)) {
     W = 0.0;
@@ -271,8 +271,7 @@ __device__ double screened_weight(const KArgs &A, const double *x, uint8_t &flag
                                   const KtNode<T> *skt, const PhiNode<T> *sphi) {
   Born b;
   born_kinematics(A.P, A.K, x, b);
-  const cx<double> A0 = regge_me4<double>(A.P, A.K, b.t1, b.t2, log(b.s13), log(b.s14),
-                                          log(b.s23), log(b.s24), b.that, b.uhat);
+  const cx<double> A0 = born_amp(A.P, A.K, b);
   const cx<double> Al = loop_dispatch<T>(A, b, skt, sphi);
   const double re = A0.re + Al.re, im = A0.im + Al.im;
   double W = weight_jacobian(A.K, b) * (re * re + im * im);
@@ -433,7 +432,8 @@ __global__ void __launch_bounds__(kWeightThreads, GRN_LOOP_MIN_BLOCKS)
 }
 
 bool record_mode(const KArgs &a, int prec) {
-  return a.P.screening && prec == GRN_PREC_MIXED && a.K.n_active == 1;
+  return a.P.screening && prec == GRN_PREC_MIXED && a.K.n_active == 1 &&
+         a.P.process == GRN_PROC_REGGE_CON;
 }
 
 cudaError_t launch_event_weights_rec(const KArgs &a, const double *u, int64_t n, int dim,

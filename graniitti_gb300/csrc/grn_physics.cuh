@@ -134,6 +134,100 @@ GRN_HD cx<T> regge_prop(const Consts &K, const grn_regge_params &rp, T lns, T t)
 }
 
 // ---------------------------------------------------------------------------
+// Tensor-pomeron continuum of two pseudoscalars (MTensorPomeron::ME4 "2xS",
+// src/MTensorPomeron.cc:572-898). With the high-energy proton vertex
+// -3i gPNN F1(t) P_mu P_nu (P = p' + p, MTensorPomeron.cc:1388), the pomeron
+// propagator 1/(4s) (-i s ap)^(alpha(t)-1) (g g + g g - g g / 2) (2288) and the
+// traceless pomeron-pseudoscalar vertex -2i g FM(q^2) (Q_a Q_b - g_ab Q^2/4) (2203),
+// each exchange contracts to
+//   c(s, t) (-6 gPNN g F1(t) FM(t)) (2 (P.Q)^2 - P^2 Q^2 / 2).
+// Light-cone dot products a.b = (a+ b- + a- b+)/2 - aT.bT; every large product pairs
+// a sqrt(s)-size component with a cancellation-free one.
+constexpr double kMpPDG = 0.938272081;  // PDG::mp used by the form factors
+
+template <typename T>
+GRN_HD T dirac_f1(T Q2, int kelly) {
+  Q2 = fabs(Q2);
+  const T tau = Q2 / T(4.0 * kMpPDG * kMpPDG);
+  const T mu  = T(2.792847337);
+  T GE, GM;
+  if (kelly) {
+    GE = (T(1) - T(0.24) * tau) /
+         (T(1) + tau * (T(10.98) + tau * (T(12.82) + tau * T(21.97))));
+    GM = mu * (T(1) + T(0.12) * tau) /
+         (T(1) + tau * (T(10.97) + tau * (T(18.86) + tau * T(6.55))));
+  } else {
+    const T d = T(1) + Q2 / T(0.71);
+    GM = mu / (d * d);
+    GE = GM / mu;
+  }
+  return (GE + tau * GM) / (tau + T(1));
+}
+
+// Light-cone kinematics of one (tree-level or loop) point.
+template <typename T>
+struct LCKin {
+  T p1p, p1m, p1x, p1y, p2p, p2m, p2x, p2y;  // forward legs
+  T p3p, p3m, p3x, p3y, p4p, p4m, p4x, p4y;  // central pair
+  T L, eps, mp2;                             // beams: pa = (L, eps, 0), pb = (eps, L, 0)
+  T t1, t2, s13, s14, s23, s24, that, uhat;  // invariants
+};
+
+template <typename T>
+GRN_HD T lc_dot(T ap, T am, T ax, T ay, T bp, T bm, T bx, T by) {
+  return T(0.5) * (ap * bm + am * bp) - (ax * bx + ay * by);
+}
+
+// c(s, t) (-6 gPNN g F1(t) FM(t)) as a complex number.
+template <typename T>
+GRN_HD cx<T> tensor_exchange(const grn_tensor_params &tp, T s, T t) {
+  const T x   = T(tp.delta_P) + T(tp.ap_P) * t;   // alpha(t) - 1
+  const T mag = exp(x * log(s * T(tp.ap_P))) / (T(4) * s);
+  T sn, cs;
+  sincos_pi(T(-0.5) * x, sn, cs);                 // (-i)^x = exp(-i pi x / 2)
+  const T v = T(-6.0 * tp.gPNN * tp.gPps) * dirac_f1<T>(t, tp.em_kelly) / (T(1) - t / T(0.5));
+  return {mag * cs * v, mag * sn * v};
+}
+
+template <typename T>
+GRN_HD cx<T> tensor_me4_2xs(const grn_process_params &P, const Consts &K, const LCKin<T> &k) {
+  const T eps = k.eps, L = k.L;
+  // P1 = p1 + pa, P2 = p2 + pb
+  const T P1p = k.p1p + L, P1m = k.p1m + eps, P2p = k.p2p + eps, P2m = k.p2m + L;
+  const T P1sq = T(2) * k.mp2 + k.p1p * eps + k.p1m * L;
+  const T P2sq = T(2) * k.mp2 + k.p2m * eps + k.p2p * L;
+  // t-channel meson pt = pa - p1 - p3 (pt+ from conservation: p4+ - eps + p2+)
+  const T ptp = k.p4p - eps + k.p2p, ptm = eps - k.p1m - k.p3m;
+  const T ptx = -(k.p1x + k.p3x), pty = -(k.p1y + k.p3y);
+  // u-channel meson pu = p4 - pa + p1 (pu+ = -(p3+ - eps + p2+))
+  const T pup = -(k.p3p - eps + k.p2p), pum = k.p4m - eps + k.p1m;
+  const T pux = k.p4x + k.p1x, puy = k.p4y + k.p1y;
+  auto vtx = [&](T Pp, T Pm, T Px, T Py, T Psq, T Qp, T Qm, T Qx, T Qy) {
+    const T d  = lc_dot<T>(Pp, Pm, Px, Py, Qp, Qm, Qx, Qy);
+    const T Q2 = Qp * Qm - (Qx * Qx + Qy * Qy);
+    return T(2) * d * d - T(0.5) * Psq * Q2;
+  };
+  // t channel: Q13 = pt - p3, Q24 = p4 + pt; u channel: Q14 = p4 + pu, Q23 = pu - p3
+  const T v13 = vtx(P1p, P1m, k.p1x, k.p1y, P1sq, ptp - k.p3p, ptm - k.p3m, ptx - k.p3x,
+                    pty - k.p3y);
+  const T v24 = vtx(P2p, P2m, k.p2x, k.p2y, P2sq, k.p4p + ptp, k.p4m + ptm, k.p4x + ptx,
+                    k.p4y + pty);
+  const T v14 = vtx(P1p, P1m, k.p1x, k.p1y, P1sq, k.p4p + pup, k.p4m + pum, k.p4x + pux,
+                    k.p4y + puy);
+  const T v23 = vtx(P2p, P2m, k.p2x, k.p2y, P2sq, pup - k.p3p, pum - k.p3m, pux - k.p3x,
+                    puy - k.p3y);
+  const grn_tensor_params &tp = P.tensor;
+  const T M2 = T(K.M2prop);
+  const T fft = meson_ff<T>(P.regge, k.that, M2), ffu = meson_ff<T>(P.regge, k.uhat, M2);
+  // i / (p^2 - M^2) x ff^2, then the overall -i: Mt, Mu real prefactors
+  const T wt = fft * fft / (k.that - M2), wu = ffu * ffu / (k.uhat - M2);
+  const cx<T> At = cmul(tensor_exchange<T>(tp, k.s13, k.t1), tensor_exchange<T>(tp, k.s24, k.t2));
+  const cx<T> Au = cmul(tensor_exchange<T>(tp, k.s14, k.t1), tensor_exchange<T>(tp, k.s23, k.t2));
+  // M = -i (i wt v13 v24 At + i wu v14 v23 Au) = wt v13 v24 At + wu v14 v23 Au
+  return cadd(cscale(At, wt * v13 * v24), cscale(Au, wu * v14 * v23));
+}
+
+// ---------------------------------------------------------------------------
 // Born (tree-level) kinematics of p p -> p (a b) p in the <C> class, FP64.
 struct Born {
   // forward legs
@@ -427,6 +521,13 @@ GRN_HD bool loop_point_amp(const grn_process_params &P, const Consts &K, const L
     const T tx = q1x + e.p4x, ty = q1y + e.p4y;
     uhat       = dp * dm - (tx * tx + ty * ty);
   }
+  if (P.process == GRN_PROC_TENSOR_CON) {
+    const LCKin<T> kk{p1p,   p1m,   q1x,   q1y,   p2p,   p2m,   q2x,   q2y,   e.p3p, e.p3m, e.p3x,
+                      e.p3y, e.p4p, e.p4m, e.p4x, e.p4y, e.L,   e.eps, e.mp2, t1,    t2,    s13,
+                      s14,   s23,   s24,   that,  uhat};
+    A = tensor_me4_2xs<T>(P, K, kk);
+    return true;
+  }
   A = regge_me4<T>(P, K, t1, t2, log(s13), log(s14), log(s23), log(s24), that, uhat);
   return true;
 }
@@ -679,6 +780,18 @@ GRN_HD void make_loop_event(const Consts &K, const Born &b, LoopEvent<T> &e) {
   e.a2 = T((b.p3m + b.p4m - K.eps) / K.L);
   e.L = T(K.L); e.invL2 = T(1.0 / (K.L * K.L)); e.invL = T(1.0 / K.L);
   e.eps = T(K.eps); e.mp2 = T(K.mp2); e.m3sq = T(K.m3sq); e.m4sq = T(K.m4sq);
+}
+
+// Tree-level amplitude of the configured process from the Born kinematics (FP64).
+GRN_HD cx<double> born_amp(const grn_process_params &P, const Consts &K, const Born &b) {
+  if (P.process == GRN_PROC_TENSOR_CON) {
+    const LCKin<double> k{b.p1p, b.p1m, b.p1x, b.p1y, b.p2p, b.p2m, b.p2x,  b.p2y, b.p3p,
+                          b.p3m, b.p3x, b.p3y, b.p4p, b.p4m, b.p4x, b.p4y,  K.L,   K.eps,
+                          K.mp2, b.t1,  b.t2,  b.s13, b.s14, b.s23, b.s24, b.that, b.uhat};
+    return tensor_me4_2xs<double>(P, K, k);
+  }
+  return regge_me4<double>(P, K, b.t1, b.t2, log(b.s13), log(b.s14), log(b.s23), log(b.s24),
+                           b.that, b.uhat);
 }
 
 // u-independent part of the weight and the u-dependent Jacobians

@@ -1,7 +1,8 @@
 """Model and particle data the engine needs, bundled with the package.
 
 Values are those of the generator's TUNE0 parameter set
-(modeldata/TUNE0/GENERAL.json: PARAM_SOFT 9-29, PARAM_REGGE 90-129, PARAM_PI 146-149)
+(modeldata/TUNE0/GENERAL.json: PARAM_SOFT 9-29, PARAM_REGGE 90-129, PARAM_PI 146-149,
+PARAM_TENSORPOM 178-201, PARAM_STRUCTURE 207-219)
 and of its PDG 2018 mass/width table (modeldata/mass_width_2018.mcd). Only the
 entries the engine's processes use are carried; the layout is this package's own.
 """
@@ -16,6 +17,10 @@ TUNES = {
             "a0": [1.088, 0.55, 0.55], "ap": [0.20, 0.93, 0.93], "sgn": [1, -1, 1], "s0": 1.0,
             "offshellFF": 2, "b_EXP": 0.944, "a_OREAR": 0.638, "b_OREAR": 1.886, "b_POW": 0.500,
         },
+        "PARAM_TENSORPOM": {
+            "delta_P": 0.0808, "ap_P": 0.25, "gPNN": 1.87, "gPpipi": 1.76, "gPKK": 1.54,
+        },
+        "PARAM_STRUCTURE": {"EM": "KELLY"},
         # Final-state Reggeon couplings c and on/off flags n, by coupling class.
         "COUPLINGS": {
             "PARAM_PI": {"c": [35.00184, 81.63672, 10.86264], "n": [True, False, False]},

@@ -51,7 +51,9 @@ enum {
 
 /* Process kinds: the PROC_k wrappers of MSubProc.h the engine implements. */
 enum {
-  GRN_PROC_REGGE_CON = 1 /* "PP[CON]<C> -> a b", 2-body, MRegge::ME4 (MSubProc.h:361-380) */
+  GRN_PROC_REGGE_CON  = 1, /* "PP[CON]<C|F> -> a b", 2-body, MRegge::ME4 (MSubProc.h:361-380) */
+  GRN_PROC_TENSOR_CON = 2  /* "PP[CONTENSOR]<C|F> -> a b", 2 pseudoscalars, tensor-pomeron
+                              MTensorPomeron::ME4 "2xS" (MSubProc.h:288-300) */
 };
 
 /* Phase-space classes (MProcess subclasses). */
@@ -85,6 +87,14 @@ typedef struct grn_regge_params { /* PARAM_REGGE, src/MRegge.cc:950-1039 */
   double  c[3];       /* final-state couplings ("c") */
   double  b_EXP, a_OREAR, b_OREAR, b_POW;
 } grn_regge_params;
+
+typedef struct grn_tensor_params { /* MTensorPomeronParam, include/Graniitti/MTensorPomeron.h:29-99 */
+  double  delta_P, ap_P; /* pomeron trajectory: alpha(t) = 1 + delta_P + ap_P t */
+  double  gPNN;          /* pomeron-proton-proton coupling */
+  double  gPps;          /* pomeron-pseudoscalar coupling (gPpipi or gPKK) */
+  int32_t em_kelly;      /* proton Dirac form factor F1: 1 = Kelly, 0 = dipole (PARAM_STRUCTURE EM) */
+  int32_t _pad;
+} grn_tensor_params;
 
 typedef struct grn_gencuts { /* GENCUT, include/Graniitti/MKinematics.h:1554-1576 */
   double rap_min, rap_max;       /* <C> final-state rapidity window */
@@ -123,8 +133,9 @@ typedef struct grn_process_params {
   grn_gencuts       gcuts;
   grn_fidcuts       fcuts;
   grn_soft_params   soft;
-  grn_regge_params  regge;
+  grn_regge_params  regge;   /* also the off-shell meson form factor of the tensor model */
   grn_loop_numerics loop;
+  grn_tensor_params tensor;
 } grn_process_params;
 
 /* Fill every field with the reference defaults for "PP[CON]<C> -> pi+ pi-" at

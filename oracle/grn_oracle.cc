@@ -15,6 +15,7 @@
 // the two is a check of both. File:line citations refer to the GRANIITTI tree.
 
 #include <algorithm>
+#include <array>
 #include <cmath>
 #include <complex>
 #include <cstdint>
@@ -412,6 +413,103 @@ cplx regge_me4(const Setup &S, const Event &ev) {
   return At + Au;
 }
 
+
+// ---------------------------------------------------------------------------
+// Tensor-pomeron continuum of two pseudoscalars (MTensorPomeron::ME4, "2xS",
+// src/MTensorPomeron.cc:572-898), restated with explicit Lorentz-index sums as the
+// reference contracts them (covariant components, metric diag(+,-,-,-)).
+constexpr double MP_PDG = 0.938272081;  // PDG::mp (include/Graniitti/MPDG.h:54)
+
+// Sachs form factors and the Dirac form factor F1 (src/MForm.cc:541-645): Kelly
+// (PRC 70, 068202) or dipole parametrisation.
+double F1_em(double Q2, bool kelly) {
+  Q2 = std::fabs(Q2);
+  const double tau = Q2 / sq(2.0 * MP_PDG);
+  const double mu  = 2.792847337;
+  double GE, GM;
+  if (kelly) {
+    GE = (1.0 - 0.24 * tau) / (1.0 + 10.98 * tau + 12.82 * tau * tau + 21.97 * tau * tau * tau);
+    GM = mu * (1.0 + 0.12 * tau) / (1.0 + 10.97 * tau + 18.86 * tau * tau + 6.55 * tau * tau * tau);
+  } else {
+    GM = mu / sq(1.0 + Q2 / 0.71);
+    GE = GM / mu;
+  }
+  return 1.0 / (tau + 1.0) * GE + tau / (tau + 1.0) * GM;
+}
+
+typedef std::array<double, 4> L4;
+L4 lower(const V4 &p) { return {p.e, -p.x, -p.y, -p.z}; }
+const double G_METRIC[4] = {1.0, -1.0, -1.0, -1.0};
+
+// Rank-2 vertex tensors (covariant).
+struct T2 {
+  cplx c[4][4];
+};
+// Proton-pomeron-proton, high-energy limit (MTensorPomeron.cc:1388-1399).
+T2 vertex_ppP(const grn_process_params &p, const V4 &prime, const V4 &q) {
+  const V4   ps = prime + q;
+  const L4   l  = lower(ps);
+  const cplx f  = cplx(0, -1) * 3.0 * p.tensor.gPNN * F1_em((prime - q).m2(), p.tensor.em_kelly);
+  T2 T;
+  for (int u = 0; u < 4; ++u)
+    for (int v = 0; v < 4; ++v) T.c[u][v] = f * l[u] * l[v];
+  return T;
+}
+// Pomeron-pseudoscalar-pseudoscalar (MTensorPomeron.cc:2203-2215).
+T2 vertex_Pss(const grn_process_params &p, const V4 &prime, const V4 &q) {
+  const V4     ps = prime + q;
+  const L4     l  = lower(ps);
+  const double M2 = ps.m2();
+  const cplx   f  = cplx(0, -1) * 2.0 * p.tensor.gPps * (1.0 / (1.0 - (prime - q).m2() / 0.5));
+  T2 T;
+  for (int u = 0; u < 4; ++u)
+    for (int v = 0; v < 4; ++v)
+      T.c[u][v] = f * (l[u] * l[v] - 0.25 * (u == v ? G_METRIC[u] : 0.0) * M2);
+  return T;
+}
+// Pomeron propagator factor 1/(4s) (-i s ap)^(alpha(t)-1) (MTensorPomeron.cc:2288-2298);
+// its index structure g_uk g_vl + g_ul g_vk - g_uv g_kl / 2 is applied in contract().
+cplx pomeron_prop(const grn_process_params &p, double s, double t) {
+  const double a = 1.0 + p.tensor.delta_P + p.tensor.ap_P * t;
+  return 1.0 / (4.0 * s) * std::pow(cplx(0, -s * p.tensor.ap_P), a - 1.0);
+}
+// A_{mu nu} D^{mu nu, alpha beta} B_{alpha beta} as plain index sums.
+cplx contract(const T2 &A, cplx c, const T2 &B) {
+  cplx sum(0, 0);
+  for (int u = 0; u < 4; ++u)
+    for (int v = 0; v < 4; ++v)
+      for (int k = 0; k < 4; ++k)
+        for (int l = 0; l < 4; ++l) {
+          const double g = (u == k && v == l ? G_METRIC[u] * G_METRIC[v] : 0.0) +
+                           (u == l && v == k ? G_METRIC[u] * G_METRIC[v] : 0.0) -
+                           0.5 * (u == v ? G_METRIC[u] : 0.0) * (k == l ? G_METRIC[k] : 0.0);
+          if (g != 0.0) sum += A.c[u][v] * g * B.c[k][l];
+        }
+  return c * sum;
+}
+
+cplx tensor_me4_2xs(const Setup &S, const Event &ev) {
+  const grn_process_params &p = S.p;
+  const V4 &pa = S.pb1, &pb = S.pb2;
+  const V4 &p1 = ev.pf[1], &p2 = ev.pf[2], &p3 = ev.pf[3], &p4 = ev.pf[4];
+  const double M2  = sq(p.m_central[0]);
+  const V4     pt  = pa - p1 - p3;
+  const V4     pu  = p4 - pa + p1;
+  const V4     mp3 = V4(-p3.x, -p3.y, -p3.z, -p3.e);
+  const T2     G1a = vertex_ppP(p, p1, pa);
+  const T2     G2b = vertex_ppP(p, p2, pb);
+  const cplx   Mt  = contract(G1a, pomeron_prop(p, ev.ss[1][3], ev.t1), vertex_Pss(p, pt, mp3)) *
+                  contract(vertex_Pss(p, p4, pt), pomeron_prop(p, ev.ss[2][4], ev.t2), G2b) *
+                  (cplx(0, 1) / (pt.m2() - M2)) * sq(meson_ff(p.regge, pt.m2(), M2));
+  const cplx   Mu  = contract(G1a, pomeron_prop(p, ev.ss[1][4], ev.t1), vertex_Pss(p, p4, pu)) *
+                  contract(vertex_Pss(p, pu, mp3), pomeron_prop(p, ev.ss[2][3], ev.t2), G2b) *
+                  (cplx(0, 1) / (pu.m2() - M2)) * sq(meson_ff(p.regge, pu.m2(), M2));
+  return cplx(0, -1) * (Mt + Mu);
+}
+
+// Bare amplitude of the configured process.
+cplx bare_amp(const Setup &S, const Event &ev);
+
 // Linear interpolation on the kt^2 screening table (IArray1D::Interpolate1D,
 // src/MEikonal.cc:489-512).
 cplx msa_interp(const Setup &S, double a) {
@@ -444,13 +542,17 @@ double screened_amp2(const Setup &S, const Event &born, const cplx &A0) {
       if (!loop_kinematics(S, born, born.pf[1].x - kx, born.pf[1].y - ky, born.pf[2].x + kx,
                            born.pf[2].y + ky, lev))
         continue;
-      const cplx A = regge_me4(S, lev);
+      const cplx A = bare_amp(S, lev);
       sum += (U[i] * V[j]) * (Aeik * A * kt);
     }
   }
   const cplx norm = cplx(0, 1) / (8.0 * PI * PI * S.s);
   const cplx Aloop = norm * sum * (9.0 * stepPhi * stepKT / 64.0);
   return std::norm(A0 + Aloop);
+}
+
+cplx bare_amp(const Setup &S, const Event &ev) {
+  return S.p.process == GRN_PROC_TENSOR_CON ? tensor_me4_2xs(S, ev) : regge_me4(S, ev);
 }
 
 // Phase-space weight and integration volume (MContinuum.cc:619-656; ForwardVolume
@@ -510,7 +612,7 @@ double event_weight(const Setup &S, const double *u, uint8_t &flags, Event &ev) 
   const bool fid = kin && fiducial(S, ev);
   const bool veto = true;
   if (kin && fid && veto) {
-    const cplx A0 = regge_me4(S, ev);
+    const cplx A0 = bare_amp(S, ev);
     const double amp2 = S.p.screening ? screened_amp2(S, ev, A0) : std::norm(A0);
     W = (1.0 / S.p.s_factor) * ps_factor(S, ev) * amp2 * GEV2BARN / (2.0 * S.s);
   }

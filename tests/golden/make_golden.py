@@ -127,6 +127,19 @@ def main():
     save("f_screened_15x12_weights.npz", seed=32, u=u, n_bt=1024, n_kt2=10000, loop_kt=15,
          loop_phi=12, loop_ktmax=1.75, **r)
 
+    # Tensor-pomeron continuum of pi+ pi- (PROC_12, MTensorPomeron::ME4 2xS), <C> and <F>.
+    PROC_T = "PP[CONTENSOR]<C> -> pi+ pi-"
+    u = philox_np.uniforms(41, 2048, 8)
+    r = run_weights(CARD, u, proc=PROC_T)
+    save("t_tree_weights.npz", seed=41, u=u, **r)
+    u = philox_np.uniforms(42, 1024, 8)
+    r = run_weights(CARD, u, REPLAY_F, proc="PP[CONTENSOR]<F> -> pi+ pi-", dim=6)
+    save("tf_tree_weights.npz", seed=42, u=u, **r)
+    u = philox_np.uniforms(43, 96, 8)
+    r = run_weights(CARD_SCR, u, ["--nbt", "1024", "--nkt2", "10000"], proc=PROC_T)
+    save("t_screened_15x12_weights.npz", seed=43, u=u, n_bt=1024, n_kt2=10000, loop_kt=15,
+         loop_phi=12, loop_ktmax=1.75, **r)
+
     # VEGAS integration of c1 (reference ranlux48 points, 8 threads).
     out = subprocess.run([REF_BIN, "vegas", CARD, PROC, "--cores", "8"], check=True,
                          capture_output=True, text=True).stdout

@@ -40,6 +40,13 @@ def test_factorized_params():
     assert (P.gcuts.M_min, P.gcuts.M_max) == (0.0, 5.0)
 
 
+def test_tensor_params():
+    P = card.build_params(card.read_card(CARD), "PP[CONTENSOR]<C> -> pi+ pi-")
+    assert P.process == 2 and P.tensor.gPps == 1.76 and P.tensor.em_kelly == 1
+    PK = card.build_params(card.read_card(CARD), "PP[CONTENSOR]<C> -> K+ K-")
+    assert PK.tensor.gPps == 1.54
+
+
 @pytest.mark.parametrize("proc", ["PP[RES]<C> -> pi+ pi-", "PP[CON]<Q> -> pi+ pi-",
                                   "PP[CON]<C> -> pi+ pi- pi+ pi-", "yy[CON]<C> -> mu+ mu-"])
 def test_unsupported_processes_are_rejected(proc):

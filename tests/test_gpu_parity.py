@@ -230,3 +230,42 @@ def test_factorized_vegas_cross_section_vs_oracle_mc(gpu):
     print("sigma <C> %.5e +- %.1e, <F> %.5e +- %.1e, pull %.2f" %
           (c.sigma, c.sigma_err, f.sigma, f.sigma_err, pull))
     assert abs(pull) < 4
+
+
+@pytest.mark.parametrize("name,proc", [
+    ("t_tree_weights.npz", "PP[CONTENSOR]<C> -> pi+ pi-"),
+    ("tf_tree_weights.npz", "PP[CONTENSOR]<F> -> pi+ pi-")])
+def test_tensor_pomeron_tree_vs_reference(gpu, name, proc):
+    import graniitti_gb300 as g
+    from graniitti_gb300 import card
+    from conftest import CARD
+    gl = _load(name)
+    P = card.build_params(card.read_card(CARD), proc)
+    w, fl = _engine(P).event_weights(gl["u"], prec=g.FP64)
+    wo, flo = orc.weights(P, gl["u"])
+    assert np.array_equal(fl, flo) and np.array_equal(fl & 1, gl["kin"])
+    assert _rel(w, gl["w"]).max() < TOL_FP64_REF
+    assert _rel(w, wo).max() < TOL_FP64_ORC
+
+
+def test_tensor_pomeron_screened_vs_reference(gpu):
+    import ctypes
+    import graniitti_gb300 as g
+    from graniitti_gb300 import card
+    from conftest import CARD_SCR
+    gl = _load("t_screened_15x12_weights.npz")
+    t = _load("eikonal_nbt1024_nkt10000.npz")
+    P = card.build_params(card.read_card(CARD_SCR), "PP[CONTENSOR]<C> -> pi+ pi-")
+    e = _engine(P)
+    e.eikonal_set(t["mbt"], t["msa"])
+    w, fl = e.event_weights(gl["u"], prec=g.FP64)
+    assert np.array_equal(fl & 1, gl["kin"])
+    assert _rel(w, gl["w"]).max() < 1e-9
+    wm, _ = e.event_weights(gl["u"], prec=g.MIXED)
+    Pb = type(P)()
+    ctypes.memmove(ctypes.byref(Pb), ctypes.byref(P), ctypes.sizeof(P))
+    Pb.screening = 0
+    wb, _ = _engine(Pb).event_weights(gl["u"], prec=g.FP64)
+    ok, rel = _mixed_ok(wm, w, wb)
+    print("tensor mixed vs fp64: max rel %.3e" % rel.max())
+    assert ok, rel.max()

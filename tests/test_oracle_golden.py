@@ -126,3 +126,26 @@ def test_factorized_screened_weights():
     t = _load("eikonal_nbt1024_nkt10000.npz")
     w, fl = orc.weights(_params_F(True), g["u"], msa=t["msa"], nthreads=4)
     _check_weights(w, fl, g, tol=1e-9)
+
+
+def _params(proc, screened=False):
+    from graniitti_gb300 import card
+    from conftest import CARD, CARD_SCR
+    return card.build_params(card.read_card(CARD_SCR if screened else CARD), proc)
+
+
+@pytest.mark.parametrize("name,proc", [
+    ("t_tree_weights.npz", "PP[CONTENSOR]<C> -> pi+ pi-"),
+    ("tf_tree_weights.npz", "PP[CONTENSOR]<F> -> pi+ pi-")])
+def test_tensor_pomeron_tree_weights(name, proc):
+    g = _load(name)
+    w, fl = orc.weights(_params(proc), g["u"])
+    _check_weights(w, fl, g)
+
+
+def test_tensor_pomeron_screened_weights():
+    g = _load("t_screened_15x12_weights.npz")
+    t = _load("eikonal_nbt1024_nkt10000.npz")
+    w, fl = orc.weights(_params("PP[CONTENSOR]<C> -> pi+ pi-", True), g["u"], msa=t["msa"],
+                        nthreads=4)
+    _check_weights(w, fl, g, tol=1e-9)
