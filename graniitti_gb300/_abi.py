@@ -97,6 +97,26 @@ class VegasResult(ctypes.Structure):
                [("iterations", c_int64), ("nan_count", c_int64)]
 
 
+GRN_FLOW_LOSS_KL = 0
+GRN_FLOW_LOSS_VARIANCE = 1
+
+
+class FlowParams(ctypes.Structure):
+    _fields_ = [("dim", c_int32), ("layers", c_int32), ("hidden", c_int32), ("bins", c_int32),
+                ("seed", c_uint64)]
+
+
+class FlowTrainParams(ctypes.Structure):
+    _fields_ = [("n_train", c_int64), ("batch", c_int64), ("epochs", c_int32),
+                ("rounds", c_int32), ("lr", c_double), ("loss", c_int32), ("prec", c_int32),
+                ("seed_stream", c_uint32), ("_pad", c_uint32)]
+
+
+class FlowTrainResult(ctypes.Structure):
+    _fields_ = [("steps", c_int64)] + [(n, c_double) for n in (
+        "loss_first", "loss_last", "rel_var_start", "rel_var_flow", "train_ms")]
+
+
 # Every exported entry point with its ctypes signature (restype, argtypes).
 SIGNATURES = {
     "grn_default_params": (None, [c_void_p]),
@@ -129,6 +149,23 @@ SIGNATURES = {
     "grn_vegas_points": (c_int32, [c_void_p, c_void_p, c_int64, c_void_p]),
     "grn_kernel_timing": (c_int32, [c_void_p, c_int32, c_void_p, c_void_p]),
     "grn_fp32_peak": (c_int32, [c_int32, c_void_p]),
+    "grn_flow_default_params": (None, [c_void_p]),
+    "grn_flow_create": (c_int32, [c_void_p, c_void_p, c_void_p]),
+    "grn_flow_destroy": (c_int32, [c_void_p]),
+    "grn_flow_num_params": (c_int64, [c_void_p]),
+    "grn_flow_get_params": (c_int32, [c_void_p, c_void_p]),
+    "grn_flow_set_params": (c_int32, [c_void_p, c_void_p]),
+    "grn_flow_density": (c_int32, [c_void_p, c_void_p, c_int64, c_void_p, c_void_p]),
+    "grn_flow_inverse": (c_int32, [c_void_p, c_void_p, c_int64, c_void_p, c_void_p]),
+    "grn_flow_sample": (c_int32, [c_void_p, c_uint64, c_uint32, c_int64, c_int64, c_void_p,
+                                  c_void_p]),
+    "grn_flow_loss_grad": (c_int32, [c_void_p, c_void_p, c_void_p, c_int64, c_int32, c_void_p,
+                                     c_void_p]),
+    "grn_flow_train_step": (c_int32, [c_void_p, c_void_p, c_void_p, c_int64, c_int32, c_double,
+                                      c_void_p]),
+    "grn_flow_train": (c_int32, [c_void_p, c_void_p, c_void_p, c_void_p]),
+    "grn_flow_iteration": (c_int32, [c_void_p, c_void_p, c_int32, c_uint32, c_void_p]),
+    "grn_flow_integrate": (c_int32, [c_void_p, c_void_p, c_void_p, c_void_p]),
 }
 
 _lib = None

@@ -13,7 +13,7 @@ REPO = os.path.dirname(HERE)
 CSRC = os.path.join(HERE, "csrc")
 OUT = os.path.join(HERE, "_build")
 LIB = os.path.join(OUT, "libgrn.so")
-SOURCES = ["grn_kernels.cu", "grn_api.cu", "grn_noalloc.cu"]
+SOURCES = ["grn_kernels.cu", "grn_api.cu", "grn_noalloc.cu", "grn_flow.cu"]
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 
 

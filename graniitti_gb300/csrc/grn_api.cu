@@ -11,6 +11,7 @@
 #include <string>
 #include <vector>
 
+#include "grn_flow.cuh"
 #include "grn_internal.cuh"
 
 using grn::KArgs;
@@ -116,6 +117,7 @@ struct grn_engine {
   int64_t     last_ncall = 0;
   bool        vegas_ready = false;
   bool        have_last = false;
+  const float *last_fu = nullptr;  // flow points of the last pass (null: Philox points)
   // unweighting
   DevBuf      d_uw_counts, d_uw_misc, d_uw_idx;
   // timing of the sampling kernel
@@ -135,6 +137,20 @@ struct grn_engine {
     a.loop_norm_im = loop_norm_im;
     return a;
   }
+};
+
+// ---------------------------------------------------------------------------
+// Flow proposal state (grn_flow.cu holds the kernels).
+struct grn_flow {
+  grn_engine *e      = nullptr;
+  int         layers = 6;
+  uint64_t    seed   = 1;
+  int64_t     nparams = 0;
+  int64_t     adam_t  = 0;
+  DevBuf      d_theta, d_m, d_v, d_grad, d_w2p, d_w3p, d_loss;
+  DevBuf      d_x, d_z, d_lq, d_coef, d_xs;  // batch scratch
+  DevBuf      d_tu, d_tlq, d_tcoef;          // training set
+  DevBuf      d_fu, d_flq;                   // points of the last flow pass
 };
 
 namespace {
@@ -625,11 +641,11 @@ grn_status grn_vegas_clear(grn_engine *e) {
   return GRN_OK;
 }
 
-// One iteration with `prec` arithmetic; updates the global estimates as the
-// reference does after joining its threads (MGraniitti.cc:1222-1251).
-static grn_status vegas_iteration_impl(grn_engine *e, int prec, int mode, int refine,
-                                       uint32_t stream_id, int64_t iter_index,
-                                       grn_vegas_result *out) {
+// One sampling pass over e->ncall points with `prec` arithmetic: weights f into
+// d_f, pass scalars into h_sc, optional grid refinement. With fu / flq the points
+// come from the flow (dimension-major, leading dimension ncall) and carry 1/q.
+static grn_status vegas_pass(grn_engine *e, int prec, int track_max, int refine,
+                             uint32_t stream_id, const float *fu, const float *flq) {
   const int nh = e->bins * e->dim;
   GRN_CUDA(cudaMemcpyAsync(e->d_xmat_prev.p, e->d_xmat.p, nh * sizeof(double),
                            cudaMemcpyDeviceToDevice, e->stream));
@@ -638,14 +654,14 @@ static grn_status vegas_iteration_impl(grn_engine *e, int prec, int mode, int re
   float      *rf  = rec ? e->d_recf.as<float>() : nullptr;
   double     *rd  = rec ? e->d_recd.as<double>() : nullptr;
   GRN_CUDA(grn::launch_vegas_born(a, e->d_xmat.as<double>(), e->bins, e->dim, e->ncall, e->seed,
-                                  stream_id, mode != 0, e->d_f.as<double>(),
+                                  stream_id, track_max, e->d_f.as<double>(),
                                   e->d_f2mat.as<double>(), e->d_acc.as<unsigned long long>(),
                                   e->d_lidx.as<int64_t>(), e->d_lx.as<double>(),
                                   e->d_lvw.as<double>(), e->d_lbins.as<uint64_t>(), rf, rd,
-                                  e->stream));
+                                  e->stream, fu, flq));
   // the timed kernel: the kt-loop stage when screening is on
   GRN_CUDA(cudaEventRecord(e->ev0, e->stream));
-  GRN_CUDA(grn::launch_vegas_loop(a, prec, e->bins, e->dim, e->ncall, mode != 0,
+  GRN_CUDA(grn::launch_vegas_loop(a, prec, e->bins, e->dim, e->ncall, track_max,
                                   e->d_f.as<double>(), e->d_f2mat.as<double>(),
                                   e->d_acc.as<unsigned long long>(), e->d_lidx.as<int64_t>(),
                                   e->d_lx.as<double>(), e->d_lvw.as<double>(),
@@ -669,7 +685,14 @@ static grn_status vegas_iteration_impl(grn_engine *e, int prec, int mode, int re
   e->last_stream = stream_id;
   e->last_ncall  = e->ncall;
   e->have_last   = true;
+  e->last_fu     = fu;
+  return GRN_OK;
+}
 
+// Global estimates after a pass, as the reference combines them after joining its
+// threads (MGraniitti.cc:1222-1251).
+static grn_status vegas_accumulate(grn_engine *e, int mode, int64_t iter_index,
+                                   grn_vegas_result *out) {
   const double *sc    = e->h_sc;
   const double  calls = static_cast<double>(e->ncall);
   double fsum  = sc[grn::VS_FSUM] / calls;
@@ -713,6 +736,14 @@ static grn_status vegas_iteration_impl(grn_engine *e, int prec, int mode, int re
   if (e->nan_total > 50)
     return fail(GRN_ERR_NAN, "more than 50 NaN/Inf weights: check model parameters and cuts");
   return GRN_OK;
+}
+
+static grn_status vegas_iteration_impl(grn_engine *e, int prec, int mode, int refine,
+                                       uint32_t stream_id, int64_t iter_index,
+                                       grn_vegas_result *out) {
+  const grn_status st = vegas_pass(e, prec, mode != 0, refine, stream_id, nullptr, nullptr);
+  if (st != GRN_OK) return st;
+  return vegas_accumulate(e, mode, iter_index, out);
 }
 
 grn_status grn_vegas_iteration(grn_engine *e, int32_t mode, int32_t refine, uint32_t iter_id,
@@ -865,7 +896,7 @@ grn_status grn_vegas_points(grn_engine *e, const int64_t *idx, int64_t n, double
   GRN_CUDA(cudaMemcpyAsync(e->d_uw_idx.p, idx, n * sizeof(int64_t), cudaMemcpyDefault, e->stream));
   GRN_CUDA(grn::launch_vegas_points(e->d_xmat_prev.as<double>(), e->bins, e->dim, e->seed,
                                     e->last_stream, e->d_uw_idx.as<int64_t>(), n,
-                                    e->d_aux.as<double>(), e->stream));
+                                    e->d_aux.as<double>(), e->stream, e->last_fu, e->last_ncall));
   GRN_CUDA(cudaMemcpyAsync(u_out, e->d_aux.p, n * e->dim * sizeof(double), cudaMemcpyDefault,
                            e->stream));
   GRN_CUDA(cudaStreamSynchronize(e->stream));
@@ -916,6 +947,417 @@ grn_status grn_fp32_peak(int32_t device, double *tflops) {
   const cudaError_t ce = cudaGetLastError();
   if (ce != cudaSuccess) return fail(GRN_ERR_CUDA, cudaGetErrorString(ce));
   *tflops = best;
+  return GRN_OK;
+}
+
+
+// ---------------------------------------------------------------------------
+// Flow proposal (INTEGRATOR "NEURO": MGraniitti::SampleNeuro, src/MGraniitti.cc:1527-1620)
+
+}  // extern "C"
+
+namespace {
+
+// Host pointer -> device staging (device pointers pass through).
+template <typename T>
+grn_status stage_in(DevBuf &buf, const T *p, size_t count, cudaStream_t st, const T **out) {
+  if (is_device_ptr(p)) {
+    *out = p;
+    return GRN_OK;
+  }
+  GRN_CUDA(buf.ensure(count * sizeof(T)));
+  GRN_CUDA(cudaMemcpyAsync(buf.p, p, count * sizeof(T), cudaMemcpyHostToDevice, st));
+  *out = buf.as<T>();
+  return GRN_OK;
+}
+
+// SplitMix64 (Steele, Lea, Flood 2014): initial weights only.
+double splitmix_uniform(uint64_t &state) {
+  uint64_t z = (state += 0x9E3779B97F4A7C15ull);
+  z          = (z ^ (z >> 30)) * 0xBF58476D1CE4E5B9ull;
+  z          = (z ^ (z >> 27)) * 0x94D049BB133111EBull;
+  z ^= z >> 31;
+  return static_cast<double>(z >> 11) * 0x1.0p-53;
+}
+
+grn_status flow_pack(grn_flow *f) {
+  GRN_CUDA(grn::launch_flow_pack(f->d_theta.as<float>(), f->layers, f->d_w2p.p, f->d_w3p.p,
+                                 f->e->stream));
+  return GRN_OK;
+}
+
+// Forward pass of the training step (layer inputs kept) + backward into d_grad.
+grn_status flow_loss_grad(grn_flow *f, const float *x, int64_t ld, const float *coef, int64_t n,
+                          int kind, double *loss_slot) {
+  grn_engine *e = f->e;
+  GRN_CUDA(f->d_xs.ensure(static_cast<size_t>(f->layers) * grn::flow::kDim * n * sizeof(float)));
+  GRN_CUDA(f->d_lq.ensure(n * sizeof(float)));
+  GRN_CUDA(grn::launch_flow_forward(0, f->d_theta.as<float>(), f->d_w2p.p, f->d_w3p.p, f->layers,
+                                    x, ld, n, 0, 0, 0, nullptr, 0, f->d_lq.as<float>(),
+                                    f->d_xs.as<float>(), e->stream));
+  GRN_CUDA(cudaMemsetAsync(f->d_grad.p, 0, f->nparams * sizeof(float), e->stream));
+  GRN_CUDA(cudaMemsetAsync(loss_slot, 0, sizeof(double), e->stream));
+  GRN_CUDA(grn::launch_flow_backward(f->d_theta.as<float>(), f->d_w2p.p, f->d_w3p.p, f->layers,
+                                     f->d_xs.as<float>(), f->d_lq.as<float>(), coef, n, kind,
+                                     f->d_grad.as<float>(), loss_slot, e->stream));
+  return GRN_OK;
+}
+
+grn_status flow_adam(grn_flow *f, double lr) {
+  const double b1 = 0.9, b2 = 0.999, eps = 1e-8;
+  f->adam_t += 1;
+  const double c1 = 1.0 - std::pow(b1, static_cast<double>(f->adam_t));
+  const double c2 = 1.0 - std::pow(b2, static_cast<double>(f->adam_t));
+  GRN_CUDA(grn::launch_flow_adam(f->d_theta.as<float>(), f->d_m.as<float>(), f->d_v.as<float>(),
+                                 f->d_grad.as<float>(), f->nparams,
+                                 static_cast<float>(lr * std::sqrt(c2) / c1), static_cast<float>(b1),
+                                 static_cast<float>(b2), static_cast<float>(eps * std::sqrt(c2)),
+                                 f->e->stream));
+  return flow_pack(f);
+}
+
+grn_status check_flow(grn_flow *f) {
+  if (!f || !f->e) return fail(GRN_ERR_INVALID, "null flow");
+  GRN_CUDA(cudaSetDevice(f->e->device));
+  return GRN_OK;
+}
+
+}  // namespace
+
+extern "C" {
+
+void grn_flow_default_params(grn_flow_params *p) {
+  if (!p) return;
+  p->dim    = 8;
+  p->layers = 6;
+  p->hidden = grn::flow::kHid;
+  p->bins   = grn::flow::kBins;
+  p->seed   = 1;
+}
+
+grn_status grn_flow_create(grn_engine *e, const grn_flow_params *p, grn_flow **out) {
+  if (!e || !p || !out) return fail(GRN_ERR_INVALID, "null argument");
+  *out = nullptr;
+  if (p->dim != e->dim || p->dim != grn::flow::kDim)
+    return fail(GRN_ERR_UNSUPPORTED, "flow dimension must be 8 (the process dimension)");
+  if (p->hidden != grn::flow::kHid || p->bins != grn::flow::kBins)
+    return fail(GRN_ERR_UNSUPPORTED, "flow kernels are built for hidden = 128, bins = 16");
+  if (p->layers < 1 || p->layers > grn::flow::kMaxLayers)
+    return fail(GRN_ERR_INVALID, "flow layers must be in [1, 12]");
+  GRN_CUDA(cudaSetDevice(e->device));
+  auto *f    = new grn_flow();
+  f->e       = e;
+  f->layers  = p->layers;
+  f->seed    = p->seed;
+  f->nparams = static_cast<int64_t>(p->layers) * grn::flow::kLayerParams;
+  std::vector<float> th(f->nparams, 0.0f);
+  uint64_t           state = p->seed;
+  using namespace grn::flow;
+  const float b3d = static_cast<float>(std::log(std::expm1(1.0 - 1e-3)));
+  for (int l = 0; l < p->layers; ++l) {
+    float       *t  = th.data() + static_cast<size_t>(l) * kLayerParams;
+    const double l1 = std::sqrt(6.0 / kDA), l2 = std::sqrt(6.0 / kHid);
+    for (int i = 0; i < kDA * kHid; ++i) t[i] = static_cast<float>((2 * splitmix_uniform(state) - 1) * l1);
+    float *w2 = t + kDA * kHid + kHid;
+    for (int i = 0; i < kHid * kHid; ++i) w2[i] = static_cast<float>((2 * splitmix_uniform(state) - 1) * l2);
+    float *b3 = t + kLayerParams - kNOut;
+    for (int j = 0; j < kDA; ++j)
+      for (int r = 2 * kBins; r < kRaw; ++r) b3[j * kRaw + r] = b3d;
+  }
+  const size_t pb = f->nparams * sizeof(float);
+  grn_status   st = GRN_OK;
+  if (f->d_theta.ensure(pb) != cudaSuccess || f->d_m.ensure(pb) != cudaSuccess ||
+      f->d_v.ensure(pb) != cudaSuccess || f->d_grad.ensure(pb) != cudaSuccess ||
+      f->d_w2p.ensure(grn::flow_w2p_elems(f->layers) * 2) != cudaSuccess ||
+      f->d_w3p.ensure(grn::flow_w3p_elems(f->layers) * 2) != cudaSuccess ||
+      f->d_loss.ensure(sizeof(double)) != cudaSuccess) {
+    st = fail(GRN_ERR_CUDA, "flow: device allocation failed");
+  } else if (cudaMemcpy(f->d_theta.p, th.data(), pb, cudaMemcpyHostToDevice) != cudaSuccess ||
+             cudaMemset(f->d_m.p, 0, pb) != cudaSuccess ||
+             cudaMemset(f->d_v.p, 0, pb) != cudaSuccess) {
+    st = fail(GRN_ERR_CUDA, "flow: upload failed");
+  } else {
+    st = flow_pack(f);
+    if (st == GRN_OK && cudaStreamSynchronize(e->stream) != cudaSuccess)
+      st = fail(GRN_ERR_CUDA, "flow: pack failed");
+  }
+  if (st != GRN_OK) {
+    grn_flow_destroy(f);
+    return st;
+  }
+  *out = f;
+  return GRN_OK;
+}
+
+grn_status grn_flow_destroy(grn_flow *f) {
+  if (!f) return GRN_OK;
+  if (f->e) cudaSetDevice(f->e->device);
+  for (DevBuf *b : {&f->d_theta, &f->d_m, &f->d_v, &f->d_grad, &f->d_w2p, &f->d_w3p, &f->d_loss,
+                    &f->d_x, &f->d_z, &f->d_lq, &f->d_coef, &f->d_xs, &f->d_tu, &f->d_tlq,
+                    &f->d_tcoef, &f->d_fu, &f->d_flq})
+    b->release();
+  if (f->e && f->e->last_fu) f->e->last_fu = nullptr, f->e->have_last = false;
+  delete f;
+  return GRN_OK;
+}
+
+int64_t grn_flow_num_params(const grn_flow *f) { return f ? f->nparams : 0; }
+
+grn_status grn_flow_get_params(grn_flow *f, float *theta) {
+  grn_status st = check_flow(f);
+  if (st != GRN_OK) return st;
+  if (!theta) return fail(GRN_ERR_INVALID, "null argument");
+  GRN_CUDA(cudaMemcpyAsync(theta, f->d_theta.p, f->nparams * sizeof(float), cudaMemcpyDefault,
+                           f->e->stream));
+  GRN_CUDA(cudaStreamSynchronize(f->e->stream));
+  return GRN_OK;
+}
+
+grn_status grn_flow_set_params(grn_flow *f, const float *theta) {
+  grn_status st = check_flow(f);
+  if (st != GRN_OK) return st;
+  if (!theta) return fail(GRN_ERR_INVALID, "null argument");
+  const size_t pb = f->nparams * sizeof(float);
+  GRN_CUDA(cudaMemcpyAsync(f->d_theta.p, theta, pb, cudaMemcpyDefault, f->e->stream));
+  GRN_CUDA(cudaMemsetAsync(f->d_m.p, 0, pb, f->e->stream));
+  GRN_CUDA(cudaMemsetAsync(f->d_v.p, 0, pb, f->e->stream));
+  f->adam_t = 0;
+  st        = flow_pack(f);
+  if (st != GRN_OK) return st;
+  GRN_CUDA(cudaStreamSynchronize(f->e->stream));
+  return GRN_OK;
+}
+
+// Shared body of density / inverse / sample.
+static grn_status flow_map(grn_flow *f, int mode, const float *xin, uint64_t seed,
+                           uint32_t stream, int64_t first, int64_t n, float *xout, float *logq) {
+  grn_status st = check_flow(f);
+  if (st != GRN_OK) return st;
+  if (n < 0 || !logq) return fail(GRN_ERR_INVALID, "bad argument");
+  if (n == 0) return GRN_OK;
+  grn_engine  *e  = f->e;
+  const size_t nx = static_cast<size_t>(n) * grn::flow::kDim;
+  const float *dx = nullptr;
+  if (xin) {
+    st = stage_in(f->d_x, xin, nx, e->stream, &dx);
+    if (st != GRN_OK) return st;
+  }
+  const bool dev_out = !xout || is_device_ptr(xout), dev_lq = is_device_ptr(logq);
+  float     *dz = xout, *dl = logq;
+  if (xout && !dev_out) {
+    GRN_CUDA(f->d_z.ensure(nx * sizeof(float)));
+    dz = f->d_z.as<float>();
+  }
+  if (!dev_lq) {
+    GRN_CUDA(f->d_lq.ensure(n * sizeof(float)));
+    dl = f->d_lq.as<float>();
+  }
+  GRN_CUDA(grn::launch_flow_forward(mode, f->d_theta.as<float>(), f->d_w2p.p, f->d_w3p.p,
+                                    f->layers, dx, n, n, seed, stream, first, dz, n, dl, nullptr,
+                                    e->stream));
+  if (xout && !dev_out)
+    GRN_CUDA(cudaMemcpyAsync(xout, dz, nx * sizeof(float), cudaMemcpyDeviceToHost, e->stream));
+  if (!dev_lq)
+    GRN_CUDA(cudaMemcpyAsync(logq, dl, n * sizeof(float), cudaMemcpyDeviceToHost, e->stream));
+  GRN_CUDA(cudaStreamSynchronize(e->stream));
+  return GRN_OK;
+}
+
+grn_status grn_flow_density(grn_flow *f, const float *x, int64_t n, float *z_out, float *logq) {
+  if (!x) return fail(GRN_ERR_INVALID, "null argument");
+  return flow_map(f, 0, x, 0, 0, 0, n, z_out, logq);
+}
+
+grn_status grn_flow_inverse(grn_flow *f, const float *z, int64_t n, float *x_out, float *logq) {
+  if (!z || !x_out) return fail(GRN_ERR_INVALID, "null argument");
+  return flow_map(f, 1, z, 0, 0, 0, n, x_out, logq);
+}
+
+grn_status grn_flow_sample(grn_flow *f, uint64_t seed, uint32_t stream, int64_t first, int64_t n,
+                           float *x_out, float *logq) {
+  if (!x_out) return fail(GRN_ERR_INVALID, "null argument");
+  return flow_map(f, 1, nullptr, seed, stream, first, n, x_out, logq);
+}
+
+grn_status grn_flow_loss_grad(grn_flow *f, const float *x, const float *coef, int64_t n,
+                              int32_t kind, double *loss, float *grad) {
+  grn_status st = check_flow(f);
+  if (st != GRN_OK) return st;
+  if (!x || !coef || n < 1 || (kind != 0 && kind != 1)) return fail(GRN_ERR_INVALID, "bad argument");
+  grn_engine  *e  = f->e;
+  const float *dx = nullptr, *dc = nullptr;
+  st = stage_in(f->d_x, x, static_cast<size_t>(n) * grn::flow::kDim, e->stream, &dx);
+  if (st != GRN_OK) return st;
+  st = stage_in(f->d_coef, coef, static_cast<size_t>(n), e->stream, &dc);
+  if (st != GRN_OK) return st;
+  st = flow_loss_grad(f, dx, n, dc, n, kind, f->d_loss.as<double>());
+  if (st != GRN_OK) return st;
+  double l = 0.0;
+  GRN_CUDA(cudaMemcpyAsync(&l, f->d_loss.p, sizeof(double), cudaMemcpyDeviceToHost, e->stream));
+  if (grad)
+    GRN_CUDA(cudaMemcpyAsync(grad, f->d_grad.p, f->nparams * sizeof(float), cudaMemcpyDefault,
+                             e->stream));
+  GRN_CUDA(cudaStreamSynchronize(e->stream));
+  if (loss) *loss = l / static_cast<double>(n);
+  return GRN_OK;
+}
+
+grn_status grn_flow_train_step(grn_flow *f, const float *x, const float *coef, int64_t n,
+                               int32_t kind, double lr, double *loss) {
+  grn_status st = grn_flow_loss_grad(f, x, coef, n, kind, loss, nullptr);
+  if (st != GRN_OK) return st;
+  st = flow_adam(f, lr);
+  if (st != GRN_OK) return st;
+  GRN_CUDA(cudaStreamSynchronize(f->e->stream));
+  return GRN_OK;
+}
+
+// Points of a pass: Philox uniforms (q = 1) or a flow sample, into d_fu / d_flq
+// (dimension-major, leading dimension n) of `dst_u` / `dst_lq`.
+static grn_status flow_points(grn_flow *f, bool from_flow, uint32_t stream_id, int64_t n,
+                              DevBuf &dst_u, DevBuf &dst_lq) {
+  grn_engine *e = f->e;
+  GRN_CUDA(dst_u.ensure(static_cast<size_t>(n) * grn::flow::kDim * sizeof(float)));
+  GRN_CUDA(dst_lq.ensure(static_cast<size_t>(n) * sizeof(float)));
+  if (from_flow)
+    GRN_CUDA(grn::launch_flow_forward(1, f->d_theta.as<float>(), f->d_w2p.p, f->d_w3p.p,
+                                      f->layers, nullptr, n, n, e->seed ^ 0xF10Bull, stream_id, 0,
+                                      dst_u.as<float>(), n, dst_lq.as<float>(), nullptr,
+                                      e->stream));
+  else
+    GRN_CUDA(grn::launch_flow_uniform(e->seed ^ 0xF10Bull, stream_id, n, dst_u.as<float>(),
+                                      dst_lq.as<float>(), e->stream));
+  return GRN_OK;
+}
+
+static grn_status set_ncall(grn_engine *e, int64_t n) {
+  if (n != e->ncall) {
+    e->ncall = n;
+    return vegas_alloc_calls(e, n);
+  }
+  return GRN_OK;
+}
+
+grn_status grn_flow_train(grn_engine *e, grn_flow *f, const grn_flow_train_params *tp,
+                          grn_flow_train_result *out) {
+  if (!e || !f || !tp || f->e != e) return fail(GRN_ERR_INVALID, "bad argument");
+  if (!e->vegas_ready) return fail(GRN_ERR_STATE, "grn_vegas_init (and adapt the grid) first");
+  if (tp->n_train < 1 || tp->batch < 1 || tp->n_train % tp->batch || tp->epochs < 1 ||
+      tp->rounds < 1 || (tp->loss != 0 && tp->loss != 1) || !(tp->lr > 0))
+    return fail(GRN_ERR_INVALID, "bad training parameters (n_train must be a multiple of batch)");
+  grn_status st = require_screening_ready(e);
+  if (st != GRN_OK) return st;
+  GRN_CUDA(cudaSetDevice(e->device));
+  const int64_t ncall0 = e->ncall, n = tp->n_train, B = tp->batch;
+  const int64_t steps_per_round = (n / B) * tp->epochs;
+  const int64_t nsteps          = steps_per_round * tp->rounds;
+  DevBuf        d_losses;
+  GRN_CUDA(d_losses.ensure(nsteps * sizeof(double)));
+  cudaEvent_t t0, t1;
+  cudaEventCreate(&t0);
+  cudaEventCreate(&t1);
+  GRN_CUDA(cudaEventRecord(t0, e->stream));
+  grn_flow_train_result r{};
+  int64_t step = 0;
+  for (int round = 0; round < tp->rounds && st == GRN_OK; ++round) {
+    st = set_ncall(e, n);
+    if (st != GRN_OK) break;
+    const uint32_t sid = 0x20000000u | static_cast<uint32_t>(tp->seed_stream + round);
+    st = flow_points(f, round > 0, sid, n, f->d_tu, f->d_tlq);
+    if (st != GRN_OK) break;
+    st = vegas_pass(e, tp->prec, 0, 0, sid, f->d_tu.as<float>(), f->d_tlq.as<float>());
+    if (st != GRN_OK) break;
+    const double m1 = e->h_sc[grn::VS_FSUM] / n, m2 = e->h_sc[grn::VS_F2SUM] / n;
+    if (round == 0) r.rel_var_start = m2 / (m1 * m1) - 1.0;
+    if (!(m2 > 0)) {
+      st = fail(GRN_ERR_INVALID, "flow training: all weights are zero");
+      break;
+    }
+    GRN_CUDA(f->d_tcoef.ensure(n * sizeof(float)));
+    GRN_CUDA(grn::launch_flow_coef(e->d_f.as<double>(), round > 0 ? f->d_tlq.as<float>() : nullptr,
+                                   n, tp->loss, tp->loss == 1 ? m2 : m1, f->d_tcoef.as<float>(),
+                                   e->stream));
+    for (int ep = 0; ep < tp->epochs && st == GRN_OK; ++ep) {
+      for (int64_t b = 0; b < n / B && st == GRN_OK; ++b) {
+        st = flow_loss_grad(f, f->d_tu.as<float>() + b * B, n, f->d_tcoef.as<float>() + b * B, B,
+                            tp->loss, d_losses.as<double>() + step);
+        if (st == GRN_OK) st = flow_adam(f, tp->lr);
+        ++step;
+      }
+    }
+  }
+  if (st == GRN_OK) {
+    GRN_CUDA(cudaEventRecord(t1, e->stream));
+    std::vector<double> losses(nsteps);
+    GRN_CUDA(cudaMemcpyAsync(losses.data(), d_losses.p, nsteps * sizeof(double),
+                             cudaMemcpyDeviceToHost, e->stream));
+    GRN_CUDA(cudaStreamSynchronize(e->stream));
+    float ms = 0.f;
+    cudaEventElapsedTime(&ms, t0, t1);
+    r.train_ms   = ms;
+    r.steps      = nsteps;
+    r.loss_first = losses.front() / B;
+    r.loss_last  = losses.back() / B;
+    // evaluation pass through the trained flow: relative variance of the weights
+    const uint32_t sid = 0x20000000u | static_cast<uint32_t>(tp->seed_stream + tp->rounds);
+    st = flow_points(f, true, sid, n, f->d_tu, f->d_tlq);
+    if (st == GRN_OK)
+      st = vegas_pass(e, tp->prec, 0, 0, sid, f->d_tu.as<float>(), f->d_tlq.as<float>());
+    if (st == GRN_OK) {
+      const double m1 = e->h_sc[grn::VS_FSUM] / n, m2 = e->h_sc[grn::VS_F2SUM] / n;
+      r.rel_var_flow = m2 / (m1 * m1) - 1.0;
+    }
+  }
+  cudaEventDestroy(t0);
+  cudaEventDestroy(t1);
+  d_losses.release();
+  e->have_last = false;  // the training passes are not integration passes
+  e->last_fu   = nullptr;
+  const grn_status st2 = set_ncall(e, ncall0);
+  if (st == GRN_OK) st = st2;
+  if (out) *out = r;
+  return st;
+}
+
+grn_status grn_flow_iteration(grn_engine *e, grn_flow *f, int32_t mode, uint32_t iter_id,
+                              grn_vegas_result *out) {
+  if (!e || !f || f->e != e) return fail(GRN_ERR_INVALID, "bad argument");
+  if (!e->vegas_ready) return fail(GRN_ERR_STATE, "grn_vegas_init first");
+  grn_status st = require_screening_ready(e);
+  if (st != GRN_OK) return st;
+  GRN_CUDA(cudaSetDevice(e->device));
+  st = flow_points(f, true, iter_id, e->ncall, f->d_fu, f->d_flq);
+  if (st != GRN_OK) return st;
+  st = vegas_pass(e, e->prec, mode != 0, 0, iter_id, f->d_fu.as<float>(), f->d_flq.as<float>());
+  if (st != GRN_OK) return st;
+  grn_vegas_result r{};
+  st = vegas_accumulate(e, mode, e->iters_since_clear++, &r);
+  if (out) *out = r;
+  return st;
+}
+
+grn_status grn_flow_integrate(grn_engine *e, grn_flow *f, const grn_vegas_params *vp,
+                              grn_vegas_result *out) {
+  if (!e || !f || !vp || f->e != e) return fail(GRN_ERR_INVALID, "bad argument");
+  if (!e->vegas_ready) return fail(GRN_ERR_STATE, "grn_vegas_init first");
+  if (vp->ncall < 1 || !(vp->precision > 0)) return fail(GRN_ERR_INVALID, "bad VEGAS parameters");
+  grn_status st = set_ncall(e, vp->ncall);
+  if (st != GRN_OK) return st;
+  e->prec = vp->prec;
+  grn_vegas_clear(e);
+  grn_vegas_result r{};
+  int64_t its = 0;
+  const int64_t itmin = std::max<int32_t>(2, vp->iter), itmax = 10000;
+  for (; its < itmax; ++its) {
+    st = grn_flow_iteration(e, f, 1, e->next_stream++, &r);
+    if (st != GRN_OK) return st;
+    if (its + 1 >= itmin && r.sigma > 0 && r.sigma_err / r.sigma <= vp->precision) {
+      ++its;
+      break;
+    }
+  }
+  r.iterations = its;
+  if (out) *out = r;
   return GRN_OK;
 }
 

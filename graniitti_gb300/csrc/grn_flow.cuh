@@ -1,0 +1,54 @@
+// grn_flow.cuh — launch interface of the coupling-layer spline flow (grn_flow.cu).
+#pragma once
+
+#include <cuda_runtime.h>
+
+#include <cstddef>
+#include <cstdint>
+
+namespace grn {
+namespace flow {
+
+constexpr int kDim   = 8;                  // hypercube dimension
+constexpr int kDA    = kDim / 2;           // conditioning / transformed coordinates per layer
+constexpr int kBins  = 16;                 // spline bins
+constexpr int kRaw   = 3 * kBins + 1;      // widths, heights, knot derivatives
+constexpr int kRawP  = 56;                 // padded to whole 8-column MMA tiles
+constexpr int kHid   = 128;                // MLP width
+constexpr int kNOut  = kDA * kRaw;         // 196
+constexpr int kNOutP = kDA * kRawP;        // 224
+constexpr int kLayerParams = kDA * kHid + kHid + kHid * kHid + kHid + kHid * kNOut + kNOut;
+constexpr int kMaxLayers   = 12;
+
+}  // namespace flow
+
+size_t      flow_w2p_elems(int layers);  // BF16 elements of the packed W2 copies
+size_t      flow_w3p_elems(int layers);  // BF16 elements of the packed W3 copies
+cudaError_t launch_flow_pack(const float *theta, int layers, void *w2p, void *w3p,
+                             cudaStream_t st);
+// mode 0: density direction (xin = points x, xout = z); mode 1: sampling direction
+// (xin = z or, when null, Philox uniforms of points first..first+n-1 with key seed and
+// stream id `stream`; xout = x). Arrays are dimension-major with leading dimension
+// ld_in / ld_out. lq receives log q(x). xs_store (density mode, may be null) receives
+// each layer's input, layers x 8 x n.
+cudaError_t launch_flow_forward(int mode, const float *theta, const void *w2p, const void *w3p,
+                                int layers, const float *xin, int64_t ld_in, int64_t n,
+                                uint64_t seed, uint32_t stream, int64_t first, float *xout,
+                                int64_t ld_out, float *lq, float *xs_store, cudaStream_t st);
+// Loss over n points and its gradient (accumulated into grad, which the caller zeroes;
+// loss_sum receives sum_i l_i added to its value). kind 1: l = coef exp(-log q);
+// kind 0: l = -coef log q.
+cudaError_t launch_flow_backward(const float *theta, const void *w2p, const void *w3p, int layers,
+                                 const float *xs, const float *lq, const float *coef, int64_t n,
+                                 int kind, float *grad, double *loss_sum, cudaStream_t st);
+cudaError_t launch_flow_adam(float *theta, float *m, float *v, const float *grad, int64_t n,
+                             float lr_t, float b1, float b2, float eps_t, cudaStream_t st);
+// Training coefficients from the weights f of a pass and the sampling log density
+// lq0 (null = uniform): kind 1: coef = f^2 exp(lq0) / norm; kind 0: coef = f / norm.
+cudaError_t launch_flow_coef(const double *f, const float *lq0, int64_t n, int kind, double norm,
+                             float *coef, cudaStream_t st);
+// Philox uniforms as FP32, rounded down (dimension-major, leading dimension n).
+cudaError_t launch_flow_uniform(uint64_t seed, uint32_t stream, int64_t n, float *u, float *lq,
+                                cudaStream_t st);
+
+}  // namespace grn

@@ -68,7 +68,10 @@ cudaError_t launch_vegas_born(const KArgs &a, const double *xmat, int bins, int 
                               uint64_t seed, uint32_t stream, int track_max, double *f_out,
                               double *f2mat, unsigned long long *acc, int64_t *l_idx, double *l_x,
                               double *l_vw, uint64_t *l_bins, float *rf, double *rd,
-                              cudaStream_t st);
+                              cudaStream_t st, const float *fu = nullptr,
+                              const float *flq = nullptr);
+// fu / flq: points drawn from the flow (dimension-major, leading dimension ncall) and
+// their log density; the VEGAS weight of a point is then vw(u) / q(u).
 cudaError_t launch_vegas_loop(const KArgs &a, int prec, int bins, int dim, int64_t ncall,
                               int track_max, double *f_out, double *f2mat, unsigned long long *acc,
                               const int64_t *l_idx, const double *l_x, const double *l_vw,
@@ -89,7 +92,7 @@ cudaError_t launch_vegas_refine(double *xmat, double *f2mat, int bins, int dim, 
                                 cudaStream_t st);
 cudaError_t launch_vegas_points(const double *xmat, int bins, int dim, uint64_t seed,
                                 uint32_t stream, const int64_t *idx, int64_t n, double *u_out,
-                                cudaStream_t st);
+                                cudaStream_t st, const float *fu = nullptr, int64_t fu_ld = 0);
 
 // Unweighting
 cudaError_t launch_unweight(const double *f, int64_t n, double fmax, uint64_t seed,

@@ -15,6 +15,7 @@
 #include <cstdint>
 
 #include "grn_internal.cuh"
+#include "grn_philox.cuh"
 
 // Resident blocks per SM requested for the FP32 loop kernels (register budget
 // 65536 / (128 threads x GRN_LOOP_MIN_BLOCKS)).
@@ -23,43 +24,6 @@
 #endif
 
 namespace grn {
-
-// ---------------------------------------------------------------------------
-// Philox4x32-10 (Salmon et al., SC'11). counter = (index lo, index hi, block,
-// stream), key = seed. Each block gives two 53-bit doubles in [0, 1).
-__device__ __forceinline__ void philox_block(uint64_t seed, uint32_t stream, uint64_t idx,
-                                             uint32_t blk, double &r0, double &r1) {
-  uint32_t c0 = static_cast<uint32_t>(idx), c1 = static_cast<uint32_t>(idx >> 32), c2 = blk,
-           c3 = stream;
-  uint32_t k0 = static_cast<uint32_t>(seed), k1 = static_cast<uint32_t>(seed >> 32);
-#pragma unroll
-  for (int r = 0; r < 10; ++r) {
-    const uint32_t hi0 = __umulhi(0xD2511F53u, c0), lo0 = 0xD2511F53u * c0;
-    const uint32_t hi1 = __umulhi(0xCD9E8D57u, c2), lo1 = 0xCD9E8D57u * c2;
-    const uint32_t n0 = hi1 ^ c1 ^ k0;
-    const uint32_t n2 = hi0 ^ c3 ^ k1;
-    c0 = n0;
-    c1 = lo1;
-    c2 = n2;
-    c3 = lo0;
-    k0 += 0x9E3779B9u;
-    k1 += 0xBB67AE85u;
-  }
-  const uint64_t a = (static_cast<uint64_t>(c1) << 32) | c0;
-  const uint64_t b = (static_cast<uint64_t>(c3) << 32) | c2;
-  r0 = static_cast<double>(a >> 11) * 0x1.0p-53;
-  r1 = static_cast<double>(b >> 11) * 0x1.0p-53;
-}
-
-__device__ __forceinline__ void philox_point(uint64_t seed, uint32_t stream, uint64_t idx,
-                                             int dim, double *u) {
-  for (int blk = 0; 2 * blk < dim; ++blk) {
-    double r0, r1;
-    philox_block(seed, stream, idx, blk, r0, r1);
-    u[2 * blk] = r0;
-    if (2 * blk + 1 < dim) u[2 * blk + 1] = r1;
-  }
-}
 
 // ---------------------------------------------------------------------------
 // Bessel J0: Abramowitz & Stegun 9.4 rational / asymptotic approximation, the
@@ -761,7 +725,8 @@ __global__ void __launch_bounds__(kVegasThreads)
                  double *__restrict__ f2mat, unsigned long long *__restrict__ acc,
                  int64_t *__restrict__ l_idx, double *__restrict__ l_x, double *__restrict__ l_vw,
                  uint64_t *__restrict__ l_bins, int64_t cap, float *__restrict__ rf,
-                 double *__restrict__ rd) {
+                 double *__restrict__ rd, const float *__restrict__ fu,
+                 const float *__restrict__ flq) {
   extern __shared__ double dsm[];
   double   *sx = dsm, *sf2 = dsm + bins * dim;
   const int nh = bins * dim;
@@ -783,8 +748,13 @@ __global__ void __launch_bounds__(kVegasThreads)
     Born       b;
     if (active) {
       double u[kMaxDim];
-      philox_point(seed, stream, static_cast<uint64_t>(e), dim, u);
+      if (fu) {
+        for (int j = 0; j < dim; ++j) u[j] = fu[static_cast<int64_t>(j) * ncall + e];
+      } else {
+        philox_point(seed, stream, static_cast<uint64_t>(e), dim, u);
+      }
       vw = vegas_map(sx, bins, dim, u, x, pb);
+      if (flq) vw *= exp(-static_cast<double>(flq[e]));
       double  W;
       uint8_t fl;
       loop = born_stage(A, x, b, W, fl);
@@ -917,7 +887,7 @@ cudaError_t launch_vegas_born(const KArgs &a, const double *xmat, int bins, int 
                               uint64_t seed, uint32_t stream, int track_max, double *f_out,
                               double *f2mat, unsigned long long *acc, int64_t *l_idx, double *l_x,
                               double *l_vw, uint64_t *l_bins, float *rf, double *rd,
-                              cudaStream_t st) {
+                              cudaStream_t st, const float *fu, const float *flq) {
   const int nh = bins * dim;
   cudaMemsetAsync(f2mat, 0, nh * sizeof(double), st);
   cudaMemsetAsync(acc, 0, (VS_COUNT + 1) * sizeof(unsigned long long), st);
@@ -928,7 +898,7 @@ cudaError_t launch_vegas_born(const KArgs &a, const double *xmat, int bins, int 
   const int     ba   = static_cast<int>(std::min<int64_t>(want, static_cast<int64_t>(sms) * 16));
   k_vegas_born<<<ba, kVegasThreads, 2 * nh * sizeof(double), st>>>(
       a, xmat, bins, dim, ncall, seed, stream, track_max, f_out, f2mat, acc, l_idx, l_x, l_vw,
-      l_bins, ncall, rf, rd);
+      l_bins, ncall, rf, rd, fu, flq);
   return cudaGetLastError();
 }
 
@@ -1122,12 +1092,24 @@ cudaError_t launch_vegas_refine(double *xmat, double *f2mat, int bins, int dim, 
 }
 
 // Regenerate the hypercube points of given indices of an iteration.
+// With fu (dimension-major, leading dimension fu_ld) the points come from the
+// flow sample of the pass instead of Philox.
 __global__ void k_vegas_points(const double *xmat, int bins, int dim, uint64_t seed,
-                               uint32_t stream, const int64_t *idx, int64_t n, double *out) {
+                               uint32_t stream, const int64_t *idx, int64_t n, double *out,
+                               const float *fu, int64_t fu_ld) {
   const int64_t i = static_cast<int64_t>(blockIdx.x) * blockDim.x + threadIdx.x;
   if (i >= n) return;
   double u[kMaxDim];
-  philox_point(seed, stream, static_cast<uint64_t>(idx[i]), dim, u);
+  if (fu) {
+    const int64_t k = idx[i];
+    if (k < 0 || k >= fu_ld) {  // not a point of the pass
+      for (int j = 0; j < dim; ++j) out[i * dim + j] = nan("");
+      return;
+    }
+    for (int j = 0; j < dim; ++j) u[j] = fu[static_cast<int64_t>(j) * fu_ld + k];
+  } else {
+    philox_point(seed, stream, static_cast<uint64_t>(idx[i]), dim, u);
+  }
   for (int j = 0; j < dim; ++j) {
     const double zn = u[j] * bins + 1.0;
     int          k  = max(1, min(static_cast<int>(zn), bins));
@@ -1145,10 +1127,10 @@ __global__ void k_vegas_points(const double *xmat, int bins, int dim, uint64_t s
 
 cudaError_t launch_vegas_points(const double *xmat, int bins, int dim, uint64_t seed,
                                 uint32_t stream, const int64_t *idx, int64_t n, double *u_out,
-                                cudaStream_t st) {
+                                cudaStream_t st, const float *fu, int64_t fu_ld) {
   if (n <= 0) return cudaSuccess;
-  k_vegas_points<<<static_cast<unsigned>((n + 127) / 128), 128, 0, st>>>(xmat, bins, dim, seed,
-                                                                        stream, idx, n, u_out);
+  k_vegas_points<<<static_cast<unsigned>((n + 127) / 128), 128, 0, st>>>(
+      xmat, bins, dim, seed, stream, idx, n, u_out, fu, fu_ld);
   return cudaGetLastError();
 }
 

@@ -152,6 +152,114 @@ class Engine:
         return out
 
 
+class Flow:
+    """Coupling-layer spline flow in front of the engine's VEGAS map (grn_flow_*).
+
+    Point arrays are float32, dimension-major (dim x n)."""
+
+    def __init__(self, engine, layers=6, seed=1):
+        self.engine = engine
+        self.lib = engine.lib
+        p = _abi.FlowParams()
+        self.lib.grn_flow_default_params(ctypes.byref(p))
+        p.layers = layers
+        p.seed = seed
+        h = ctypes.c_void_p()
+        _abi.check(self.lib.grn_flow_create(engine.h, ctypes.byref(p), ctypes.byref(h)))
+        self.h = h
+        self.layers = layers
+        self.dim = engine.dim
+        self.n_params = self.lib.grn_flow_num_params(h)
+
+    def close(self):
+        if getattr(self, "h", None):
+            self.lib.grn_flow_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def get_params(self):
+        t = np.zeros(self.n_params, dtype=np.float32)
+        _abi.check(self.lib.grn_flow_get_params(self.h, _ptr(t)))
+        return t
+
+    def set_params(self, theta):
+        t = np.ascontiguousarray(theta, dtype=np.float32)
+        if t.shape != (self.n_params,):
+            raise ValueError("expected %d parameters" % self.n_params)
+        _abi.check(self.lib.grn_flow_set_params(self.h, _ptr(t)))
+
+    def _pts(self, x):
+        x = np.ascontiguousarray(x, dtype=np.float32)
+        if x.ndim != 2 or x.shape[0] != self.dim:
+            raise ValueError("points must be %d x n (dimension-major)" % self.dim)
+        return x
+
+    def density(self, x):
+        x = self._pts(x)
+        n = x.shape[1]
+        z = np.zeros_like(x)
+        lq = np.zeros(n, dtype=np.float32)
+        _abi.check(self.lib.grn_flow_density(self.h, _ptr(x), n, _ptr(z), _ptr(lq)))
+        return z, lq
+
+    def inverse(self, z):
+        z = self._pts(z)
+        n = z.shape[1]
+        x = np.zeros_like(z)
+        lq = np.zeros(n, dtype=np.float32)
+        _abi.check(self.lib.grn_flow_inverse(self.h, _ptr(z), n, _ptr(x), _ptr(lq)))
+        return x, lq
+
+    def sample(self, seed, n, stream=0, first=0):
+        x = np.zeros((self.dim, n), dtype=np.float32)
+        lq = np.zeros(n, dtype=np.float32)
+        _abi.check(self.lib.grn_flow_sample(self.h, seed, stream, first, n, _ptr(x), _ptr(lq)))
+        return x, lq
+
+    def loss_grad(self, x, coef, kind=_abi.GRN_FLOW_LOSS_VARIANCE):
+        x = self._pts(x)
+        coef = np.ascontiguousarray(coef, dtype=np.float32)
+        g = np.zeros(self.n_params, dtype=np.float32)
+        loss = ctypes.c_double()
+        _abi.check(self.lib.grn_flow_loss_grad(self.h, _ptr(x), _ptr(coef), x.shape[1], kind,
+                                               ctypes.byref(loss), _ptr(g)))
+        return loss.value, g
+
+    def train_step(self, x, coef, lr=1e-3, kind=_abi.GRN_FLOW_LOSS_VARIANCE):
+        x = self._pts(x)
+        coef = np.ascontiguousarray(coef, dtype=np.float32)
+        loss = ctypes.c_double()
+        _abi.check(self.lib.grn_flow_train_step(self.h, _ptr(x), _ptr(coef), x.shape[1], kind,
+                                                lr, ctypes.byref(loss)))
+        return loss.value
+
+    def train(self, n_train=1 << 22, batch=65536, epochs=4, rounds=1, lr=1e-3,
+              loss=_abi.GRN_FLOW_LOSS_VARIANCE, prec=FP64, seed_stream=1):
+        tp = _abi.FlowTrainParams(n_train=n_train, batch=batch, epochs=epochs, rounds=rounds,
+                                  lr=lr, loss=loss, prec=prec, seed_stream=seed_stream)
+        r = _abi.FlowTrainResult()
+        _abi.check(self.lib.grn_flow_train(self.engine.h, self.h, ctypes.byref(tp),
+                                           ctypes.byref(r)))
+        return r
+
+    def iteration(self, mode=1, iter_id=1):
+        r = _abi.VegasResult()
+        _abi.check(self.lib.grn_flow_iteration(self.engine.h, self.h, mode, iter_id,
+                                               ctypes.byref(r)))
+        return r
+
+    def integrate(self, vp):
+        r = _abi.VegasResult()
+        _abi.check(self.lib.grn_flow_integrate(self.engine.h, self.h, ctypes.byref(vp),
+                                               ctypes.byref(r)))
+        return r
+
+
 class Graniitti:
     """MGraniitti-style driver (src/MGraniitti.cc) over the GPU engine."""
 

@@ -291,6 +291,95 @@ grn_status grn_unweight(grn_engine *e, double fmax, uint64_t seed, int64_t *n_ac
 grn_status grn_vegas_points(grn_engine *e, const int64_t *idx, int64_t n, double *u_out);
 
 /* ------------------------------------------------------------------------ */
+/* Learned proposal: coupling-layer spline flow in front of the VEGAS map     */
+/* ------------------------------------------------------------------------ */
+/* Counterpart of the reference's neural-network integrator (INTEGRATOR
+ * "NEURO": MGraniitti::SampleNeuro, src/MGraniitti.cc:1527-1620, network and
+ * optimiser in include/Graniitti/MNeuroJacobian.h), which samples u through a
+ * trained map and weighs each point by EventWeight(u) * |det du/dz| / p(z).
+ * Here the map is a normalizing flow over the hypercube placed in front of the
+ * VEGAS grid: z uniform -> u = T^{-1}(z) (flow) -> x = VEGAS map(u) -> W(x);
+ * the exact weight of a point is f = W(x) * vw(u) / q(u), so the estimator is
+ * unbiased whatever the training reached. Architecture: `layers` coupling
+ * layers (the transformed half alternates through six fixed masks), each a
+ * rational-quadratic spline with `bins` bins whose parameters come from an MLP
+ * 4 -> hidden -> ReLU -> hidden -> ReLU -> 4 * (3 bins + 1); BF16 operands on the
+ * tensor cores with FP32 accumulation, FP32 splines, FP32 master weights.
+ * Points are dimension-major float arrays (dim x n). */
+typedef struct grn_flow grn_flow;
+
+typedef struct grn_flow_params {
+  int32_t  dim;     /* must equal grn_dim() (8) */
+  int32_t  layers;  /* coupling layers, 1..12 (default 6) */
+  int32_t  hidden;  /* MLP width (128) */
+  int32_t  bins;    /* spline bins (16) */
+  uint64_t seed;    /* initial weights */
+} grn_flow_params;
+
+#define GRN_FLOW_LOSS_KL       0 /* weighted maximum likelihood: -E[f log q] */
+#define GRN_FLOW_LOSS_VARIANCE 1 /* variance of the weights: E[f^2 q0 / q] */
+
+typedef struct grn_flow_train_params {
+  int64_t  n_train;     /* points per training round (multiple of batch) */
+  int64_t  batch;       /* points per Adam step */
+  int32_t  epochs;      /* passes over a round's points */
+  int32_t  rounds;      /* round 0 draws plain VEGAS points, later rounds the flow's */
+  double   lr;          /* Adam step size */
+  int32_t  loss;        /* GRN_FLOW_LOSS_* */
+  int32_t  prec;        /* GRN_PREC_* of the training weights */
+  uint32_t seed_stream; /* first Philox stream id of the training passes */
+  uint32_t _pad;
+} grn_flow_train_params;
+
+typedef struct grn_flow_train_result {
+  int64_t steps;          /* Adam steps taken */
+  double  loss_first;     /* batch loss of the first and the last step */
+  double  loss_last;
+  double  rel_var_start;  /* <f^2>/<f>^2 - 1 of the first training pass (plain VEGAS points) */
+  double  rel_var_flow;   /* the same over a fresh pass drawn from the trained flow */
+  double  train_ms;       /* device time of the training (passes + steps) */
+} grn_flow_train_result;
+
+void       grn_flow_default_params(grn_flow_params *p);
+/* The flow lives on the engine's device and stream. */
+grn_status grn_flow_create(grn_engine *e, const grn_flow_params *p, grn_flow **out);
+grn_status grn_flow_destroy(grn_flow *f);
+int64_t    grn_flow_num_params(const grn_flow *f);
+/* FP32 master weights, layer after layer: W1[4][H], b1[H], W2[H][H], b2[H],
+ * W3[H][4(3K+1)], b3[4(3K+1)] (row-major [in][out]). Host or device pointer.
+ * Setting them resets the optimiser state. */
+grn_status grn_flow_get_params(grn_flow *f, float *theta);
+grn_status grn_flow_set_params(grn_flow *f, const float *theta);
+/* Density direction: z = T(x) (z_out may be NULL) and log q(x). */
+grn_status grn_flow_density(grn_flow *f, const float *x, int64_t n, float *z_out, float *logq);
+/* Sampling direction from given z: x = T^{-1}(z) and log q(x). */
+grn_status grn_flow_inverse(grn_flow *f, const float *z, int64_t n, float *x_out, float *logq);
+/* Sampling with z = Philox uniforms of points first..first+n-1 (key seed, stream id). */
+grn_status grn_flow_sample(grn_flow *f, uint64_t seed, uint32_t stream, int64_t first, int64_t n,
+                           float *x_out, float *logq);
+/* Batch loss (mean over n points) and its gradient with respect to the master
+ * weights (grad: grn_flow_num_params floats, may be NULL). loss kind as
+ * GRN_FLOW_LOSS_*: variance: mean coef exp(-log q); KL: -mean coef log q. */
+grn_status grn_flow_loss_grad(grn_flow *f, const float *x, const float *coef, int64_t n,
+                              int32_t kind, double *loss, float *grad);
+/* grn_flow_loss_grad followed by one Adam step (beta1 0.9, beta2 0.999, eps 1e-8). */
+grn_status grn_flow_train_step(grn_flow *f, const float *x, const float *coef, int64_t n,
+                               int32_t kind, double lr, double *loss);
+/* Train on weights the engine generates with its current VEGAS grid (which the
+ * flow then sits in front of; keep the grid fixed afterwards). */
+grn_status grn_flow_train(grn_engine *e, grn_flow *f, const grn_flow_train_params *tp,
+                          grn_flow_train_result *out);
+/* One integration pass of e's ncall points drawn from the flow; no grid
+ * refinement; updates the global estimates like grn_vegas_iteration and leaves
+ * f on the device for grn_unweight / grn_vegas_points. */
+grn_status grn_flow_iteration(grn_engine *e, grn_flow *f, int32_t mode, uint32_t iter_id,
+                              grn_vegas_result *out);
+/* Clear the estimates, then flow passes of vp->ncall points until
+ * sigma_err / sigma <= vp->precision (at least max(2, vp->iter) passes). */
+grn_status grn_flow_integrate(grn_engine *e, grn_flow *f, const grn_vegas_params *vp,
+                              grn_vegas_result *out);
+
+/* ------------------------------------------------------------------------ */
 /* Measurement helpers (no counterpart in the reference)                      */
 /* ------------------------------------------------------------------------ */
 /* Device time of the dominant kernel of a VEGAS pass (the kt-loop stage when

@@ -1,0 +1,189 @@
+"""Flow proposal on the GPU against the CPU oracle (oracle/flow_ref.py): density
+and sampling directions, the training gradient and the Adam step; then the
+trained flow in front of the VEGAS map on the physics process."""
+import numpy as np
+import pytest
+
+from oracle import flow_ref as F
+
+pytestmark = pytest.mark.gpu
+
+# Tolerances. The GPU computes the conditioner products from BF16 operands with
+# FP32 accumulation and the splines in FP32; the oracle rounds the same operands
+# to BF16 and does the rest in FP64. A BF16 rounding that lands on the other side
+# because of FP32 vs FP64 accumulation moves an activation by one BF16 ulp, so
+# rare points differ by more than the FP32 floor.
+TOL_Z_P99 = 1e-5       # 99th percentile of |z_gpu - z_oracle|
+TOL_Z_MAX = 2e-3       # any point
+TOL_LQ_P99 = 2e-4      # 99th percentile of |log q_gpu - log q_oracle|
+TOL_LQ_MAX = 1e-1      # any point
+TOL_GRAD_REL = 2e-2    # ||g_gpu - g_oracle|| / ||g_oracle|| per parameter block
+TOL_LOSS_REL = 1e-4
+
+
+def _theta(seed, scale=0.03):
+    rng = np.random.default_rng(seed)
+    th = F.init_params(seed=seed)
+    P = F.unpack(th, 8, 6, 128, 16)
+    for p in P:
+        p["W3"] += rng.normal(0, scale, p["W3"].shape)
+        p["b3"] += rng.normal(0, 0.3, p["b3"].shape)
+        p["b1"] += rng.normal(0, 0.1, p["b1"].shape)
+        p["b2"] += rng.normal(0, 0.1, p["b2"].shape)
+    return th.astype(np.float32).astype(np.float64)
+
+
+@pytest.fixture(scope="module")
+def flow(gpu, params):
+    import graniitti_gb300 as g
+    e = g.Engine(params, 0)
+    f = g.Flow(e, layers=6, seed=1)
+    yield e, f
+    f.close()
+    e.close()
+
+
+def test_param_count(flow):
+    _, f = flow
+    assert f.n_params == F.n_params(8, 6, 128, 16) == 6 * 42436
+
+
+def test_initial_flow_is_identity(flow):
+    _, f = flow
+    g0 = f.get_params()
+    f.set_params(F.init_params(seed=1).astype(np.float32))
+    x = np.random.default_rng(2).random((8, 1000)).astype(np.float32)
+    z, lq = f.density(x)
+    assert np.max(np.abs(z - x)) < 2e-6 and np.max(np.abs(lq)) < 1e-4
+    f.set_params(g0)
+
+
+def test_density_matches_oracle(flow):
+    _, f = flow
+    th = _theta(11)
+    f.set_params(th.astype(np.float32))
+    x = np.random.default_rng(12).random((8, 4099)).astype(np.float32)  # ragged tail tile
+    z, lq = f.density(x)
+    lq_o, z_o = F.log_density(x.T.astype(np.float64), th, bf=True)
+    dz = np.abs(z.T - z_o)
+    dl = np.abs(lq - lq_o)
+    print("density: max |dz| %.3e  p99 |dlq| %.3e  max |dlq| %.3e  (lq range %.2f..%.2f)"
+          % (dz.max(), np.percentile(dl, 99), dl.max(), lq_o.min(), lq_o.max()))
+    assert np.ptp(lq_o) > 1.0  # the test flow is far from the identity
+    assert np.percentile(dz, 99) < TOL_Z_P99 and dz.max() < TOL_Z_MAX
+    assert np.percentile(dl, 99) < TOL_LQ_P99 and dl.max() < TOL_LQ_MAX
+
+
+def test_inverse_matches_oracle_and_roundtrips(flow):
+    _, f = flow
+    th = _theta(21)
+    f.set_params(th.astype(np.float32))
+    zin = np.random.default_rng(22).random((8, 3000)).astype(np.float32)
+    x, lq = f.inverse(zin)
+    assert np.all(np.isfinite(x)) and x.min() >= 0 and x.max() <= 1
+    x_o, lq_o = F.sample(zin.T.astype(np.float64), th, bf=True)
+    dx = np.abs(x.T - x_o)
+    dl = np.abs(lq - lq_o)
+    print("inverse: max |dx| %.3e  p99 |dlq| %.3e  max |dlq| %.3e"
+          % (dx.max(), np.percentile(dl, 99), dl.max()))
+    assert np.percentile(dx, 99) < TOL_Z_P99 and dx.max() < TOL_Z_MAX
+    assert np.percentile(dl, 99) < TOL_LQ_P99 and dl.max() < TOL_LQ_MAX
+    # GPU round trip: density(inverse(z)) = z with the same log q
+    z2, lq2 = f.density(x)
+    assert np.percentile(np.abs(z2 - zin), 99.9) < 1e-4
+    assert np.percentile(np.abs(lq2 - lq), 99.9) < 1e-3
+
+
+def test_sample_is_deterministic_and_uniform_at_identity(flow):
+    import philox_np
+    _, f = flow
+    f.set_params(F.init_params(seed=1).astype(np.float32))
+    x, lq = f.sample(seed=5, n=2048, stream=3, first=100)
+    u = philox_np.uniforms(5, 2148, 8, stream=3)[100:]
+    assert np.max(np.abs(x.T - u)) < 1e-6
+    x2, _ = f.sample(seed=5, n=2048, stream=3, first=100)
+    assert np.array_equal(x, x2)
+
+
+@pytest.mark.parametrize("kind", [1, 0])
+def test_gradient_matches_oracle(flow, kind):
+    _, f = flow
+    th = _theta(31 + kind, scale=0.03)
+    f.set_params(th.astype(np.float32))
+    rng = np.random.default_rng(33)
+    n = 2000
+    x = rng.random((8, n)).astype(np.float32)
+    coef = (rng.random(n) + 0.25).astype(np.float32)
+    loss, g = f.loss_grad(x, coef, kind=kind)
+    lo, go, _ = F.loss_and_grad(x.T.astype(np.float64), coef.astype(np.float64), th, kind,
+                                bf=True)
+    assert abs(loss / lo - 1) < TOL_LOSS_REL
+    Pg, Po = F.unpack(g.astype(np.float64), 8, 6, 128, 16), F.unpack(go, 8, 6, 128, 16)
+    worst = 0.0
+    for l in range(6):
+        for name in ("W1", "b1", "W2", "b2", "W3", "b3"):
+            a, b = Pg[l][name], Po[l][name]
+            nb = np.linalg.norm(b)
+            if nb == 0:
+                assert np.linalg.norm(a) == 0
+                continue
+            rel = np.linalg.norm(a - b) / nb
+            worst = max(worst, rel)
+            assert rel < TOL_GRAD_REL, (l, name, rel)
+    print("kind %d: loss %.6e vs %.6e, worst block rel err %.3e" % (kind, loss, lo, worst))
+
+
+def test_adam_step_matches_oracle(flow):
+    _, f = flow
+    th = _theta(41, scale=0.03)
+    f.set_params(th.astype(np.float32))
+    rng = np.random.default_rng(42)
+    x = rng.random((8, 1024)).astype(np.float32)
+    coef = (rng.random(1024) + 0.5).astype(np.float32)
+    _, g = f.loss_grad(x, coef)
+    f.train_step(x, coef, lr=1e-3)
+    th1 = f.get_params().astype(np.float64)
+    m, v = np.zeros_like(th), np.zeros_like(th)
+    th_o = F.adam_step(th.astype(np.float32).astype(np.float64).copy(), g.astype(np.float64), m, v,
+                       1, 1e-3)
+    assert np.max(np.abs(th1 - th_o)) < 1e-6
+
+
+def _vp(ncall, bins=128, iters=3, precision=1e-3, prec=0, seed=3):
+    from graniitti_gb300 import _abi
+    vp = _abi.VegasParams()
+    vp.bins, vp.iter, vp.ncall, vp.lambda_ = bins, iters, ncall, 1.5
+    vp.chi2max, vp.precision, vp.burnin_iter, vp.prec, vp.seed = 10.0, precision, 3, prec, seed
+    return vp
+
+
+def test_trained_flow_reduces_variance_and_keeps_sigma(gpu, params):
+    """Train the flow in front of an adapted VEGAS grid; the weight variance drops
+    and the flow-sampled cross section agrees with plain VEGAS."""
+    import graniitti_gb300 as g
+    e = g.Engine(params, 0)
+    e.vegas_init(_vp(1 << 18))
+    for it in range(8):
+        e.vegas_iteration(mode=0, refine=True, iter_id=100 + it)
+    e.vegas_clear()
+    plain = [e.vegas_iteration(mode=1, refine=False, iter_id=200 + it) for it in range(4)][-1]
+    f = g.Flow(e, layers=6, seed=7)
+    r = f.train(n_train=1 << 19, batch=1 << 14, epochs=6, rounds=2, lr=1e-3)
+    print("train: steps %d loss %.4f -> %.4f rel var %.3f -> %.3f (%.0f ms)"
+          % (r.steps, r.loss_first, r.loss_last, r.rel_var_start, r.rel_var_flow, r.train_ms))
+    assert r.rel_var_flow < 0.8 * r.rel_var_start
+    e.vegas_clear()
+    rf = [f.iteration(mode=1, iter_id=300 + it) for it in range(4)][-1]
+    pull = (rf.sigma - plain.sigma) / np.hypot(rf.sigma_err, plain.sigma_err)
+    print("sigma plain %.6e +- %.2e  flow %.6e +- %.2e  pull %.2f"
+          % (plain.sigma, plain.sigma_err, rf.sigma, rf.sigma_err, pull))
+    assert abs(pull) < 4
+    assert rf.sigma_err < plain.sigma_err
+    # unweighting of a flow pass and regeneration of its points
+    na, no, idx = e.unweight(rf.maxf, seed=3, cap=1 << 18)
+    assert na > 0
+    pts = e.vegas_points(idx[:16])
+    w, _ = e.event_weights(pts)
+    assert np.all(w > 0)
+    f.close()
+    e.close()
