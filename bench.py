@@ -4,19 +4,25 @@ Workload (the screened configuration of the generator):
   PP[CON]<C> -> pi+ pi-, sqrt(s) = 13 TeV, TUNE0, |eta| < 0.9, pT > 0.1 GeV,
   eikonal screening with a 1024-interval impact-parameter density table and a
   10000-interval kt^2 screening table, kt-loop of 63 x 33 intervals (64 x 34 points)
-  with kt <= 3 GeV; 2^22 Philox points per VEGAS iteration, 128 bins per dimension.
-A step is one VEGAS iteration: points -> grid map -> event weight (FP64 kinematics,
-FP32 compensated kt-loop) -> f, f^2 histograms -> grid refinement.
+  with kt <= 3 GeV; 2^22 points per integration pass, VEGAS grid of 128 bins per
+  dimension.
+A step is one integration pass: points -> (flow) -> VEGAS map -> event weight (FP64
+kinematics, FP32 compensated kt-loop) -> f = W vw / q -> sums and max.
 
-value  = evaluations/s x eps_unw over the timed iterations, eps_unw = <f>/max f
-         (reference semantics: max f over integration iterations), inputs resident
-         on the device (counter-based points generated in the kernel).
-e2e    = the same metric through grn_event_weights with pinned HOST buffers: the
-         VEGAS-mapped points of a step are copied in and the weights out inside
-         the timed region.
+Three samplers run on the same engine, in this order:
+  plain VEGAS, mixed precision   burn-in, then timed passes (grid refined each pass)
+  flow proposal (the headline)   trained (untimed, reported) on 2^22 weighted points
+                                 of the adapted grid, then timed passes, grid frozen
+  plain VEGAS, FP64 throughout   two timed passes on the adapted grid
+value  = evaluations/s x eps_unw of the flow passes, eps_unw = <f>/max f
+         (reference semantics: max f over the integration passes), points generated
+         on the device.
+e2e    = unweighted events delivered to pinned host memory through the C ABI:
+         grn_flow_iteration + grn_unweight (hit-or-miss against that max f) +
+         grn_vegas_points, timed on the host clock.
 
 --impl reference times the CPU restatement of the reference path (oracle port, all
-host threads) on the same workload, metric and unit.
+host threads) running plain VEGAS on the same workload, metric and unit.
 """
 import argparse
 import json
@@ -183,6 +189,33 @@ def run_reference(args, rank, world):
     print(json.dumps(line), flush=True)
 
 
+FLOW_LAYERS, FLOW_BATCH, FLOW_LR = 6, 65536, 1e-3
+# multiply-adds of the conditioner per point and layer: 4x128, 128x128, 128x196
+FLOW_FLOPS_PER_POINT = FLOW_LAYERS * 2 * (4 * 128 + 128 * 128 + 128 * 196)
+
+
+def _timed_passes(torch, stream, fn, steps):
+    t0 = torch.cuda.Event(enable_timing=True)
+    t1 = torch.cuda.Event(enable_timing=True)
+    t0.record(stream)
+    out = [fn(it) for it in range(steps)]
+    t1.record(stream)
+    torch.cuda.synchronize()
+    return t0.elapsed_time(t1), out
+
+
+def _summary(results, ms, npts, steps):
+    """Unweighted events/s and the time to a 0.1% statistical error of a run."""
+    r = results[-1]
+    eps = r.sigma / r.maxf if r.maxf > 0 else 0.0
+    evals_s = npts * steps / (ms * 1e-3)
+    rel_var = max(r.I2_this * npts / r.I_this ** 2, 0.0) if r.I_this else None
+    t01 = rel_var / 1e-6 / evals_s if rel_var is not None else None
+    return {"value": evals_s * eps, "eps_unw": eps, "evaluations_per_s": evals_s,
+            "sigma_barn": r.sigma, "sigma_rel_err": r.sigma_err / r.sigma if r.sigma else None,
+            "rel_var_per_point": rel_var, "seconds_to_0.1pct": t01, "ms_per_step": ms / steps}
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -190,7 +223,9 @@ def main():
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="engine", choices=["engine", "reference"])
     ap.add_argument("--points", type=int, default=1 << 22)
+    ap.add_argument("--flow-epochs", type=int, default=4)
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--no-fp64", action="store_true")
     args = ap.parse_args()
     if args.warmup < 3:
         args.warmup = 3
@@ -209,6 +244,8 @@ def main():
             dist.barrier()
         return
 
+    import ctypes
+
     import torch
     import graniitti_gb300 as g
     from graniitti_gb300 import _abi
@@ -223,12 +260,29 @@ def main():
     vp.chi2max, vp.precision, vp.burnin_iter = 10.0, 1e-3, args.warmup
     vp.prec, vp.seed = g.MIXED, 1000 + rank
     eng.vegas_init(vp)
-    # burn-in (untimed): grid adaptation
+    stream = torch.cuda.ExternalStream(eng.stream)
+    n = args.points
+
+    # -- plain VEGAS, mixed precision: burn-in, then timed integration passes ----
     for it in range(args.warmup):
         eng.vegas_iteration(mode=0, refine=True, iter_id=1 + it)
     eng.vegas_clear()
+    ms_plain, res_plain = _timed_passes(
+        torch, stream, lambda it: eng.vegas_iteration(mode=1, refine=True, iter_id=100 + it),
+        args.steps)
+    plain = _summary(res_plain, ms_plain, n, args.steps)
+    xmat = eng.vegas_grid()
+
+    # -- flow proposal in front of the adapted grid (training untimed, reported) -
+    flow = g.Flow(eng, layers=FLOW_LAYERS, seed=1 + rank)
+    tr = flow.train(n_train=n, batch=FLOW_BATCH, epochs=args.flow_epochs, rounds=1, lr=FLOW_LR,
+                    prec=g.MIXED, seed_stream=1)
+    eng.vegas_clear()
+    for it in range(2):
+        flow.iteration(mode=0, iter_id=200 + it)
+    eng.vegas_clear()
+    eng.set_maxweight(0.0)  # the flow integration keeps its own maximum weight
     kernel_timing(eng, reset=True)
-    stream = torch.cuda.ExternalStream(eng.stream)
 
     clocks = ClockSampler(local)
     if dist:
@@ -236,47 +290,85 @@ def main():
     torch.cuda.synchronize()
     clocks.start()
     time.sleep(0.3)
-    t_start = torch.cuda.Event(enable_timing=True)
-    t_end = torch.cuda.Event(enable_timing=True)
-    t_start.record(stream)
-    results = []
-    for it in range(args.steps):
-        results.append(eng.vegas_iteration(mode=1, refine=True, iter_id=100 + it))
-    t_end.record(stream)
-    torch.cuda.synchronize()
+    ms, res_flow = _timed_passes(torch, stream,
+                                 lambda it: flow.iteration(mode=1, iter_id=300 + it), args.steps)
     clk = clocks.stop()
-    ms = t_start.elapsed_time(t_end)
     k_ms, k_n = kernel_timing(eng, reset=True)
     if dist:
         t = torch.tensor([ms], dtype=torch.float64)
         dist.all_reduce(t, op=dist.ReduceOp.MAX)
         ms = float(t[0])
-    r = results[-1]
-    eps = r.sigma / r.maxf if r.maxf > 0 else 0.0
-    evals = args.points * args.steps * world
+    fl = _summary(res_flow, ms, n, args.steps)
+    r = res_flow[-1]
+    fl_maxf = r.maxf
+    eps = fl["eps_unw"]
+    evals = n * args.steps * world
     value = evals * eps / (ms * 1e-3)
 
-    # -- e2e through the C ABI with pinned host buffers ------------------------
-    idx = np.arange(args.points, dtype=np.int64)
-    x_host = torch.empty((args.points, 8), dtype=torch.float64).pin_memory()
-    x_host.numpy()[:] = eng.vegas_points(idx)
-    w_host = torch.empty(args.points, dtype=torch.float64).pin_memory()
-    f_host = torch.empty(args.points, dtype=torch.uint8).pin_memory()
-    xn, wn, fn = x_host.numpy(), w_host.numpy(), f_host.numpy()
-    eng.event_weights(xn, prec=g.MIXED, w=wn, flags=fn)  # warm
+    # -- flow kernel alone (sampling direction, device buffers, engine stream) ---
+    xs_dev = torch.empty((8, n), dtype=torch.float32, device="cuda")
+    lq_dev = torch.empty(n, dtype=torch.float32, device="cuda")
+    def _sample(it):
+        _abi.check(eng.lib.grn_flow_sample(flow.h, 99, 500 + it, 0, n,
+                                           ctypes.c_void_p(xs_dev.data_ptr()),
+                                           ctypes.c_void_p(lq_dev.data_ptr())))
+    _sample(0)
+    ms_f, _ = _timed_passes(torch, stream, _sample, 3)
+    flow_s = ms_f / 3 * 1e-3
+    flow_tflops = n * FLOW_FLOPS_PER_POINT / flow_s / 1e12
+    bf16_peak = None
+    peaks_file = os.path.join(REPO, "MEASURED_PEAKS.json")
+    if os.path.exists(peaks_file):
+        bf16_peak = json.load(open(peaks_file)).get("bf16_tflops")
+
+    # -- plain VEGAS, FP64 throughout, on the same adapted grid ----------------
+    fp64 = None
+    if not args.no_fp64:
+        vp64 = _abi.VegasParams.from_buffer_copy(vp)
+        vp64.prec = g.FP64
+        eng.vegas_init(vp64)
+        eng.vegas_set_grid(xmat)
+        eng.vegas_iteration(mode=0, refine=True, iter_id=400)
+        eng.vegas_clear()
+        eng.set_maxweight(0.0)
+        k64 = 2
+        ms64, res64 = _timed_passes(
+            torch, stream, lambda it: eng.vegas_iteration(mode=1, refine=True, iter_id=410 + it),
+            k64)
+        fp64 = _summary(res64, ms64, n, k64)
+        eng.vegas_init(vp)
+        eng.vegas_set_grid(xmat)
+        eng.set_maxweight(fl_maxf)
+        kernel_timing(eng, reset=True)
+
+    # -- e2e: unweighted events delivered to pinned host memory through the C ABI
+    #    (flow pass -> hit-or-miss against the integration's max f -> points) ---
+    fmax = r.maxf
+    idx_h = torch.empty(n, dtype=torch.int64).pin_memory()
+    pts_h = torch.empty((n, 8), dtype=torch.float64).pin_memory()
+    na, no = ctypes.c_int64(), ctypes.c_int64()
+
+    def gen_step(it):
+        flow.iteration(mode=2, iter_id=600 + it)
+        _abi.check(eng.lib.grn_unweight(eng.h, fmax, 17 + it, ctypes.byref(na), ctypes.byref(no),
+                                        ctypes.c_void_p(idx_h.data_ptr()), n))
+        _abi.check(eng.lib.grn_vegas_points(eng.h, ctypes.c_void_p(idx_h.data_ptr()), na.value,
+                                            ctypes.c_void_p(pts_h.data_ptr())))
+        return na.value
+
+    gen_step(0)
     torch.cuda.synchronize()
     e2e_steps = max(2, min(args.steps, 3))
     t0 = time.perf_counter()
-    for _ in range(e2e_steps):
-        eng.event_weights(xn, prec=g.MIXED, w=wn, flags=fn)
-    e2e_s = (time.perf_counter() - t0) / e2e_steps
-    e2e_value = args.points * world * eps / e2e_s
+    accepted = [gen_step(1 + it) for it in range(e2e_steps)]
+    e2e_s = time.perf_counter() - t0
+    e2e_value = sum(accepted) * world / e2e_s
+    acc_step = sum(accepted) / e2e_steps
 
-    # -- roofline of the dominant kernel (VEGAS sampling pass) -----------------
+    # -- roofline of the dominant kernel (kt-loop stage of a pass) -------------
     cnt = flops_per_loop_point()
     passed = r.fidcuts_ok / r.evaluations if r.evaluations else 0.0
-    # algorithmic work of one k_vegas_loop launch: listed (passing) events x loop points
-    flops_launch = args.points * passed * LOOP_POINTS * cnt["flops"]
+    flops_launch = n * passed * LOOP_POINTS * cnt["flops"]
     k_avg_s = (k_ms / max(k_n, 1)) * 1e-3
     peak = fp32_peak(local)
     achieved = flops_launch / k_avg_s / 1e12
@@ -284,40 +376,55 @@ def main():
     if os.path.exists(TRAFFIC_FILE):
         traffic = json.load(open(TRAFFIC_FILE)).get("bytes_per_launch")
 
+    cfg = dict(config(n, world), sigma_barn=r.sigma, sigma_rel_err=fl["sigma_rel_err"],
+               eps_unw=eps, evaluations_per_s=evals / (ms * 1e-3), fid_pass=passed,
+               sampler="flow proposal (6 coupling layers, RQ splines 16 bins, MLP 128x2, "
+                       "BF16/FP32) in front of the adapted VEGAS grid; FP64 kinematics, "
+                       "FP32 compensated kt-loop",
+               flow=dict(fl, train_ms=tr.train_ms, train_steps=tr.steps, batch=FLOW_BATCH,
+                         rel_var_vegas_points=tr.rel_var_start,
+                         rel_var_flow_points=tr.rel_var_flow,
+                         sample_kernel_ms=flow_s * 1e3, sample_tflops=flow_tflops,
+                         sample_frac_of_measured_bf16=(flow_tflops / bf16_peak
+                                                       if bf16_peak else None)),
+               plain_vegas_mixed=plain, plain_vegas_fp64=fp64,
+               flow_over_plain_mixed=value / plain["value"] if plain["value"] else None,
+               flow_over_plain_fp64=(value / fp64["value"]) if fp64 and fp64["value"] else None)
     line = {"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
             "warmup": args.warmup, "ms_per_step": ms / args.steps, "higher_is_better": True,
-            "scaling": "weak", "vs_baseline": None, "dtype": "f64+f32", "data": "synthetic",
-            "config": dict(config(args.points, world), eps_unw=eps, sigma_barn=r.sigma,
-                           sigma_rel_err=r.sigma_err / r.sigma if r.sigma else None,
-                           evaluations_per_s=evals / (ms * 1e-3), fid_pass=passed),
+            "scaling": "weak", "vs_baseline": None, "dtype": "f64+f32+bf16", "data": "synthetic",
+            "config": cfg,
             "e2e": {"value": e2e_value, "unit": UNIT,
-                    "h2d_bytes_per_step": int(args.points * 8 * 8),
-                    "d2h_bytes_per_step": int(args.points * 9)},
+                    "h2d_bytes_per_step": int(acc_step * 8),
+                    "d2h_bytes_per_step": int(acc_step * (8 + 64) + 2 * 8 + 8 * 10),
+                    "what": "grn_flow_iteration + grn_unweight + grn_vegas_points per step, "
+                            "accepted events' hypercube vectors into pinned host memory"},
             "gpu_launches": 5 * args.steps,
             "roofline": {"bound": "fp32", "achieved": achieved, "peak": peak,
                          "unit": "TFLOP/s", "frac": achieved / peak if peak else None,
                          "traffic": traffic,
                          "peak_source": "measured FP32 FMA-chain probe (MEASURED_PEAKS.json "
                                         "carries no FP32 figure)",
+                         "kernel": "k_vegas_loop_rec",
                          "flops_per_loop_point": cnt["flops"],
                          "sfu_per_loop_point": cnt["transcendentals"],
                          "kernel_ms": k_avg_s * 1e3},
             "clocks": clk}
     if rank == 0 and not args.no_cpu_baseline:
-        from oracle import oracle_api as orc
         nthreads = os.cpu_count() or 1
         _, msa = eng.eikonal_tables(N_BT, N_KT2)
         n_cpu = 16 * nthreads
         dt, _ = cpu_vegas_sample(P, msa, n_cpu, nthreads)
         n_cpu = int(min(1 << 18, max(n_cpu, n_cpu * 10.0 / max(dt, 1e-3))))
         dt, _ = cpu_vegas_sample(P, msa, n_cpu, nthreads, seed=4343)
-        line["cpu_baseline"] = {"value": n_cpu / dt * eps, "unit": UNIT, "cores": nthreads,
-                                "kind": "port",
+        line["cpu_baseline"] = {"value": n_cpu / dt * plain["eps_unw"], "unit": UNIT,
+                                "cores": nthreads, "kind": "port",
                                 "sample": "%d uniform points of the same workload through the "
-                                          "oracle port on %d threads (%.1f s), x the GPU run's "
-                                          "eps_unw" % (n_cpu, nthreads, dt)}
+                                          "oracle port on %d threads (%.1f s), x the plain-VEGAS "
+                                          "eps_unw of the GPU run" % (n_cpu, nthreads, dt)}
     if rank == 0:
         print(json.dumps(line), flush=True)
+    flow.close()
     eng.close()
     if dist:
         dist.barrier()

@@ -144,6 +144,8 @@ SIGNATURES = {
     "grn_vegas_get_grid": (c_int32, [c_void_p, c_void_p]),
     "grn_vegas_set_grid": (c_int32, [c_void_p, c_void_p]),
     "grn_vegas_clear": (c_int32, [c_void_p]),
+    "grn_get_maxweight": (c_int32, [c_void_p, c_void_p]),
+    "grn_set_maxweight": (c_int32, [c_void_p, c_double]),
     "grn_unweight": (c_int32, [c_void_p, c_double, c_uint64, c_void_p, c_void_p, c_void_p,
                                c_int64]),
     "grn_vegas_points": (c_int32, [c_void_p, c_void_p, c_int64, c_void_p]),

@@ -641,6 +641,20 @@ grn_status grn_vegas_clear(grn_engine *e) {
   return GRN_OK;
 }
 
+grn_status grn_get_maxweight(grn_engine *e, double *maxf) {
+  if (!e || !maxf) return fail(GRN_ERR_INVALID, "null argument");
+  *maxf = e->maxf;
+  return GRN_OK;
+}
+
+grn_status grn_set_maxweight(grn_engine *e, double maxf) {
+  if (!e) return fail(GRN_ERR_INVALID, "null engine");
+  if (!(maxf >= 0.0) || std::isinf(maxf)) return fail(GRN_ERR_INVALID, "maximum weight must be >= 0");
+  e->maxf = maxf;
+  e->maxW = 0.0;
+  return GRN_OK;
+}
+
 // One sampling pass over e->ncall points with `prec` arithmetic: weights f into
 // d_f, pass scalars into h_sc, optional grid refinement. With fu / flq the points
 // come from the flow (dimension-major, leading dimension ncall) and carry 1/q.
@@ -1345,6 +1359,7 @@ grn_status grn_flow_integrate(grn_engine *e, grn_flow *f, const grn_vegas_params
   if (st != GRN_OK) return st;
   e->prec = vp->prec;
   grn_vegas_clear(e);
+  e->maxf = e->maxW = 0.0;
   grn_vegas_result r{};
   int64_t its = 0;
   const int64_t itmin = std::max<int32_t>(2, vp->iter), itmax = 10000;

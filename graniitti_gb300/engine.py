@@ -129,6 +129,14 @@ class Engine:
     def vegas_clear(self):
         _abi.check(self.lib.grn_vegas_clear(self.h))
 
+    def get_maxweight(self):
+        m = ctypes.c_double()
+        _abi.check(self.lib.grn_get_maxweight(self.h, ctypes.byref(m)))
+        return m.value
+
+    def set_maxweight(self, maxf):
+        _abi.check(self.lib.grn_set_maxweight(self.h, maxf))
+
     def vegas_grid(self):
         x = np.zeros((self.vp.bins, self.dim))
         _abi.check(self.lib.grn_vegas_get_grid(self.h, _ptr(x)))

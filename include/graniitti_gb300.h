@@ -275,6 +275,12 @@ grn_status grn_vegas_get_grid(grn_engine *e, double *xmat);
 grn_status grn_vegas_set_grid(grn_engine *e, const double *xmat);
 /* Clear the global (sumdata, sumchi2, sweight) estimates: VEGASData::ClearIntegral. */
 grn_status grn_vegas_clear(grn_engine *e);
+/* Maximum weight used for unweighting: max f = W * vw (divided by q for flow
+ * passes) over the integration passes so far (MGraniitti::GetMaxweight /
+ * SetMaxweight, src/MGraniitti.cc:966-985). Setting 0 starts a fresh maximum
+ * (the reference requires > 0: one generator object runs one integration). */
+grn_status grn_get_maxweight(grn_engine *e, double *maxf);
+grn_status grn_set_maxweight(grn_engine *e, double maxf);
 
 /* ------------------------------------------------------------------------ */
 /* Unweighting                                                                */
@@ -374,7 +380,7 @@ grn_status grn_flow_train(grn_engine *e, grn_flow *f, const grn_flow_train_param
  * f on the device for grn_unweight / grn_vegas_points. */
 grn_status grn_flow_iteration(grn_engine *e, grn_flow *f, int32_t mode, uint32_t iter_id,
                               grn_vegas_result *out);
-/* Clear the estimates, then flow passes of vp->ncall points until
+/* Clear the estimates and the maximum weight, then flow passes of vp->ncall points until
  * sigma_err / sigma <= vp->precision (at least max(2, vp->iter) passes). */
 grn_status grn_flow_integrate(grn_engine *e, grn_flow *f, const grn_vegas_params *vp,
                               grn_vegas_result *out);
