@@ -147,7 +147,7 @@ struct grn_flow {
   uint64_t    seed   = 1;
   int64_t     nparams = 0;
   int64_t     adam_t  = 0;
-  DevBuf      d_theta, d_m, d_v, d_grad, d_w2p, d_w3p, d_loss;
+  DevBuf      d_theta, d_m, d_v, d_grad, d_w2p, d_w3p, d_w2c, d_w3c, d_loss, d_err;
   DevBuf      d_x, d_z, d_lq, d_coef, d_xs;  // batch scratch
   DevBuf      d_tu, d_tlq, d_tcoef;          // training set
   DevBuf      d_fu, d_flq;                   // points of the last flow pass
@@ -996,7 +996,18 @@ double splitmix_uniform(uint64_t &state) {
 
 grn_status flow_pack(grn_flow *f) {
   GRN_CUDA(grn::launch_flow_pack(f->d_theta.as<float>(), f->layers, f->d_w2p.p, f->d_w3p.p,
-                                 f->e->stream));
+                                 f->d_w2c.p, f->d_w3c.p, f->e->stream));
+  return GRN_OK;
+}
+
+// Bounded waits inside the forward kernel report through d_err (read after a sync).
+grn_status flow_check_err(grn_flow *f) {
+  int h = 0;
+  GRN_CUDA(cudaMemcpy(&h, f->d_err.p, sizeof(int), cudaMemcpyDeviceToHost));
+  if (h) {
+    cudaMemset(f->d_err.p, 0, sizeof(int));
+    return fail(GRN_ERR_CUDA, "flow kernel: a bounded wait gave up (tensor-core or copy stall)");
+  }
   return GRN_OK;
 }
 
@@ -1006,9 +1017,9 @@ grn_status flow_loss_grad(grn_flow *f, const float *x, int64_t ld, const float *
   grn_engine *e = f->e;
   GRN_CUDA(f->d_xs.ensure(static_cast<size_t>(f->layers) * grn::flow::kDim * n * sizeof(float)));
   GRN_CUDA(f->d_lq.ensure(n * sizeof(float)));
-  GRN_CUDA(grn::launch_flow_forward(0, f->d_theta.as<float>(), f->d_w2p.p, f->d_w3p.p, f->layers,
+  GRN_CUDA(grn::launch_flow_forward(0, f->d_theta.as<float>(), f->d_w2c.p, f->d_w3c.p, f->layers,
                                     x, ld, n, 0, 0, 0, nullptr, 0, f->d_lq.as<float>(),
-                                    f->d_xs.as<float>(), e->stream));
+                                    f->d_xs.as<float>(), f->d_err.as<int>(), e->stream));
   GRN_CUDA(cudaMemsetAsync(f->d_grad.p, 0, f->nparams * sizeof(float), e->stream));
   GRN_CUDA(cudaMemsetAsync(loss_slot, 0, sizeof(double), e->stream));
   GRN_CUDA(grn::launch_flow_backward(f->d_theta.as<float>(), f->d_w2p.p, f->d_w3p.p, f->layers,
@@ -1084,11 +1095,15 @@ grn_status grn_flow_create(grn_engine *e, const grn_flow_params *p, grn_flow **o
       f->d_v.ensure(pb) != cudaSuccess || f->d_grad.ensure(pb) != cudaSuccess ||
       f->d_w2p.ensure(grn::flow_w2p_elems(f->layers) * 2) != cudaSuccess ||
       f->d_w3p.ensure(grn::flow_w3p_elems(f->layers) * 2) != cudaSuccess ||
-      f->d_loss.ensure(sizeof(double)) != cudaSuccess) {
+      f->d_w2c.ensure(grn::flow_w2c_elems(f->layers) * 2) != cudaSuccess ||
+      f->d_w3c.ensure(grn::flow_w3c_elems(f->layers) * 2) != cudaSuccess ||
+      f->d_loss.ensure(sizeof(double)) != cudaSuccess ||
+      f->d_err.ensure(sizeof(int)) != cudaSuccess) {
     st = fail(GRN_ERR_CUDA, "flow: device allocation failed");
   } else if (cudaMemcpy(f->d_theta.p, th.data(), pb, cudaMemcpyHostToDevice) != cudaSuccess ||
              cudaMemset(f->d_m.p, 0, pb) != cudaSuccess ||
-             cudaMemset(f->d_v.p, 0, pb) != cudaSuccess) {
+             cudaMemset(f->d_v.p, 0, pb) != cudaSuccess ||
+             cudaMemset(f->d_err.p, 0, sizeof(int)) != cudaSuccess) {
     st = fail(GRN_ERR_CUDA, "flow: upload failed");
   } else {
     st = flow_pack(f);
@@ -1106,7 +1121,8 @@ grn_status grn_flow_create(grn_engine *e, const grn_flow_params *p, grn_flow **o
 grn_status grn_flow_destroy(grn_flow *f) {
   if (!f) return GRN_OK;
   if (f->e) cudaSetDevice(f->e->device);
-  for (DevBuf *b : {&f->d_theta, &f->d_m, &f->d_v, &f->d_grad, &f->d_w2p, &f->d_w3p, &f->d_loss,
+  for (DevBuf *b : {&f->d_theta, &f->d_m, &f->d_v, &f->d_grad, &f->d_w2p, &f->d_w3p, &f->d_w2c,
+                    &f->d_w3c, &f->d_err, &f->d_loss,
                     &f->d_x, &f->d_z, &f->d_lq, &f->d_coef, &f->d_xs, &f->d_tu, &f->d_tlq,
                     &f->d_tcoef, &f->d_fu, &f->d_flq})
     b->release();
@@ -1166,15 +1182,15 @@ static grn_status flow_map(grn_flow *f, int mode, const float *xin, uint64_t see
     GRN_CUDA(f->d_lq.ensure(n * sizeof(float)));
     dl = f->d_lq.as<float>();
   }
-  GRN_CUDA(grn::launch_flow_forward(mode, f->d_theta.as<float>(), f->d_w2p.p, f->d_w3p.p,
+  GRN_CUDA(grn::launch_flow_forward(mode, f->d_theta.as<float>(), f->d_w2c.p, f->d_w3c.p,
                                     f->layers, dx, n, n, seed, stream, first, dz, n, dl, nullptr,
-                                    e->stream));
+                                    f->d_err.as<int>(), e->stream));
   if (xout && !dev_out)
     GRN_CUDA(cudaMemcpyAsync(xout, dz, nx * sizeof(float), cudaMemcpyDeviceToHost, e->stream));
   if (!dev_lq)
     GRN_CUDA(cudaMemcpyAsync(logq, dl, n * sizeof(float), cudaMemcpyDeviceToHost, e->stream));
   GRN_CUDA(cudaStreamSynchronize(e->stream));
-  return GRN_OK;
+  return flow_check_err(f);
 }
 
 grn_status grn_flow_density(grn_flow *f, const float *x, int64_t n, float *z_out, float *logq) {
@@ -1213,7 +1229,7 @@ grn_status grn_flow_loss_grad(grn_flow *f, const float *x, const float *coef, in
                              e->stream));
   GRN_CUDA(cudaStreamSynchronize(e->stream));
   if (loss) *loss = l / static_cast<double>(n);
-  return GRN_OK;
+  return flow_check_err(f);
 }
 
 grn_status grn_flow_train_step(grn_flow *f, const float *x, const float *coef, int64_t n,
@@ -1234,10 +1250,10 @@ static grn_status flow_points(grn_flow *f, bool from_flow, uint32_t stream_id, i
   GRN_CUDA(dst_u.ensure(static_cast<size_t>(n) * grn::flow::kDim * sizeof(float)));
   GRN_CUDA(dst_lq.ensure(static_cast<size_t>(n) * sizeof(float)));
   if (from_flow)
-    GRN_CUDA(grn::launch_flow_forward(1, f->d_theta.as<float>(), f->d_w2p.p, f->d_w3p.p,
+    GRN_CUDA(grn::launch_flow_forward(1, f->d_theta.as<float>(), f->d_w2c.p, f->d_w3c.p,
                                       f->layers, nullptr, n, n, e->seed ^ 0xF10Bull, stream_id, 0,
                                       dst_u.as<float>(), n, dst_lq.as<float>(), nullptr,
-                                      e->stream));
+                                      f->d_err.as<int>(), e->stream));
   else
     GRN_CUDA(grn::launch_flow_uniform(e->seed ^ 0xF10Bull, stream_id, n, dst_u.as<float>(),
                                       dst_lq.as<float>(), e->stream));
@@ -1306,6 +1322,8 @@ grn_status grn_flow_train(grn_engine *e, grn_flow *f, const grn_flow_train_param
     GRN_CUDA(cudaMemcpyAsync(losses.data(), d_losses.p, nsteps * sizeof(double),
                              cudaMemcpyDeviceToHost, e->stream));
     GRN_CUDA(cudaStreamSynchronize(e->stream));
+    st = flow_check_err(f);
+    if (st != GRN_OK) return st;
     float ms = 0.f;
     cudaEventElapsedTime(&ms, t0, t1);
     r.train_ms   = ms;
@@ -1343,6 +1361,8 @@ grn_status grn_flow_iteration(grn_engine *e, grn_flow *f, int32_t mode, uint32_t
   st = flow_points(f, true, iter_id, e->ncall, f->d_fu, f->d_flq);
   if (st != GRN_OK) return st;
   st = vegas_pass(e, e->prec, mode != 0, 0, iter_id, f->d_fu.as<float>(), f->d_flq.as<float>());
+  if (st != GRN_OK) return st;
+  st = flow_check_err(f);
   if (st != GRN_OK) return st;
   grn_vegas_result r{};
   st = vegas_accumulate(e, mode, e->iters_since_clear++, &r);

@@ -17,9 +17,10 @@
 //
 // Kernels
 //   k_flow_pack    FP32 master weights -> BF16 operand copies, padded layouts
-//   k_flow_fwd     density (x -> z, log q) or sampling (z -> x, log q), 128-point
-//                  tiles; the 128x128 and 128x224 products run on the tensor cores
-//                  (BF16 operands, FP32 accumulation); splines in FP32
+//   k_flow_fwd     density (x -> z, log q) or sampling (z -> x, log q): tcgen05
+//                  products (BF16 operands, FP32 accumulators in TMEM), weights
+//                  staged by bulk copies, FP32 splines from the thread's TMEM row
+//   (backward)     warp-level BF16 mma.sync products from ldmatrix fragments
 //   k_flow_bwd     loss gradient w.r.t. all parameters, 64-point tiles; recomputes
 //                  the activations of each layer from its saved input
 //   k_flow_adam    Adam update of the FP32 master weights
@@ -174,42 +175,6 @@ __device__ __forceinline__ Bin spline_bin(const float *rp, float v, bool by) {
   b.d0 = kMinD + softplusf(rp[2 * kBins + k]);
   b.d1 = kMinD + softplusf(rp[2 * kBins + k + 1]);
   return b;
-}
-
-// log dy/dx at relative position xi of bin b.
-__device__ __forceinline__ float spline_logdet(const Bin &b, float xi) {
-  const float s   = b.h / b.w;
-  const float om  = xi * (1.f - xi);
-  const float den = s + (b.d0 + b.d1 - 2.f * s) * om;
-  const float q   = b.d1 * xi * xi + 2.f * s * om + b.d0 * (1.f - xi) * (1.f - xi);
-  return logf(s * s * q / (den * den));
-}
-
-__device__ __forceinline__ float spline_forward(const float *rp, float x, float &ld) {
-  const Bin b   = spline_bin(rp, x, false);
-  const float s = b.h / b.w;
-  float xi      = (x - b.xk) / b.w;
-  xi            = fminf(fmaxf(xi, 0.f), 1.f);
-  const float om  = xi * (1.f - xi);
-  const float den = s + (b.d0 + b.d1 - 2.f * s) * om;
-  ld              = spline_logdet(b, xi);
-  return b.yk + b.h * (s * xi * xi + b.d0 * om) / den;
-}
-
-__device__ __forceinline__ float spline_inverse(const float *rp, float y, float &ld) {
-  const Bin   b  = spline_bin(rp, y, true);
-  const float s  = b.h / b.w;
-  const float dy = y - b.yk;
-  const float t  = b.d1 + b.d0 - 2.f * s;
-  const float qa = b.h * (s - b.d0) + dy * t;
-  const float qb = b.h * b.d0 - dy * t;
-  const float qc = -s * dy;
-  const float disc = fmaxf(qb * qb - 4.f * qa * qc, 0.f);
-  const float dn   = -qb - sqrtf(disc);
-  float xi         = dn != 0.f ? 2.f * qc / dn : 0.f;
-  xi               = fminf(fmaxf(xi, 0.f), 1.f);
-  ld               = spline_logdet(b, xi);
-  return fminf(b.xk + xi * b.w, 1.f);
 }
 
 // Gradient of gy * y + gl * log dy/dx with respect to x (returned) and to the raw
@@ -392,93 +357,446 @@ __device__ __forceinline__ void warp_raw(const bf16 *sH2, const bf16 *sW3, const
 }
 
 // ---------------------------------------------------------------------------
-// Forward kernel: 128-point tiles, 8 warps (16 rows each), persistent grid.
+// Forward kernel on the 5th-generation tensor cores.
+//
+// One CTA = 256 threads = two warpgroups; thread t owns point t of a 256-point
+// subtile (warpgroup g = t / 128 owns rows 0..127 of its own M = 128 products).
+// Per layer the CTA stages W2 and W3 once with two bulk copies (TMA engine,
+// completion on an mbarrier) and runs four subtiles (a 1024-point supertile)
+// through it:
+//   h1 = relu(x_A W1 + b1)            CUDA cores, BF16 into the A tile (canonical layout)
+//   D2 = h1 . W2                      tcgen05.mma, M=128 N=128 K=128, FP32 in TMEM
+//   h2 = relu(D2 + b2)                tcgen05.ld -> BF16 into the A tile
+//   D3 = h2 . W3                      tcgen05.mma, M=128 N=256 K=128, FP32 in TMEM
+//   splines                           tcgen05.ld of the thread's own row: 4 x 49 values
+// Operand layout in shared memory (no swizzle, K-major): element (r, k) of an
+// R-row tile at byte (k / 8) * 16R + r * 16 + (k % 8) * 2, i.e. 8x16-byte core
+// matrices with leading-byte offset 16R (next 8 columns of k) and stride-byte
+// offset 128 (next 8 rows). TMEM: D2 of warpgroup g in columns [128g, 128g+128),
+// D3 in [256g, 256g+256) with coordinate jb in columns [64jb, 64jb+49) of it (every
+// TMEM load starts on a multiple of its width); 512 columns, one CTA per SM.
 
-constexpr int kFwdTile = 128, kFwdThreads = 256;
-constexpr size_t kFwdSmem = size_t(kHid) * HS * 2 + size_t(kHid) * W3S * 2 +
-                            size_t(kFwdTile) * HS * 2 + size_t(2) * kFwdTile * RS * 4 +
-                            size_t(kDim) * kFwdTile * 4 + size_t(kFwdTile) * 4 + sizeof(SmallW);
+constexpr int kFwdThreads = 256, kSub = 256, kSubs = 4, kSuper = kSub * kSubs;
+constexpr int kTmemCols = 512;
+constexpr int kRawF = 64, kNOutF = kDA * kRawF;   // D3 columns per coordinate / in all (256)
+constexpr uint32_t kW2Bytes = kHid * kHid * 2;    // 32768
+constexpr uint32_t kW3Bytes = kNOutF * kHid * 2;  // 65536
+constexpr uint32_t kABytes  = 128 * kHid * 2;     // 32768 per warpgroup
+constexpr uint32_t kOffW2 = 0, kOffW3 = kOffW2 + kW2Bytes, kOffA = kOffW3 + kW3Bytes;
+constexpr uint32_t kOffX  = kOffA + 2 * kABytes;
+constexpr uint32_t kOffLq = kOffX + kDim * kSuper * 4;
+constexpr uint32_t kOffSw = kOffLq + kSuper * 4;
+constexpr uint32_t kOffBar = (kOffSw + sizeof(SmallW) + 15) / 16 * 16;
+constexpr size_t   kFwdSmem = kOffBar + 32;
+constexpr int      kSpinLimit = 1 << 22;
+static_assert(kW2Bytes % 16 == 0 && kW3Bytes % 16 == 0 && kOffA % 16 == 0 && kOffX % 16 == 0,
+              "bulk copies and descriptors need 16-byte alignment");
+
+__device__ __forceinline__ uint64_t umma_desc(uint32_t saddr, uint32_t lbo, uint32_t sbo) {
+  uint64_t d = 0;
+  d |= static_cast<uint64_t>((saddr >> 4) & 0x3FFFu);
+  d |= static_cast<uint64_t>((lbo >> 4) & 0x3FFFu) << 16;
+  d |= static_cast<uint64_t>((sbo >> 4) & 0x3FFFu) << 32;
+  d |= static_cast<uint64_t>(1) << 46;  // descriptor version (sm_100 family); no swizzle
+  return d;
+}
+
+// kind::f16 instruction descriptor: BF16 A and B, FP32 D, both K-major.
+__host__ __device__ constexpr uint32_t umma_idesc(int M, int N) {
+  return (1u << 4) | (1u << 7) | (1u << 10) | (static_cast<uint32_t>(N >> 3) << 17) |
+         (static_cast<uint32_t>(M >> 4) << 24);
+}
+
+__device__ __forceinline__ void umma_bf16(uint32_t d_tmem, uint64_t a, uint64_t b, uint32_t idesc,
+                                          uint32_t acc) {
+  asm volatile(
+      "{\n\t.reg .pred p;\n\tsetp.ne.b32 p, %4, 0;\n\t"
+      "tcgen05.mma.cta_group::1.kind::f16 [%0], %1, %2, %3, p;\n\t}\n" ::"r"(d_tmem),
+      "l"(a), "l"(b), "r"(idesc), "r"(acc));
+}
+
+__device__ __forceinline__ void umma_commit(uint32_t bar) {
+  asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(
+                   bar)
+               : "memory");
+}
+
+__device__ __forceinline__ void tc_fence_before() {
+  asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
+}
+__device__ __forceinline__ void tc_fence_after() {
+  asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+}
+__device__ __forceinline__ void fence_async_smem() {
+  asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+}
+
+__device__ __forceinline__ void mbar_init(uint32_t bar, uint32_t count) {
+  asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(bar), "r"(count) : "memory");
+}
+
+__device__ __forceinline__ bool mbar_try(uint32_t bar, uint32_t parity) {
+  uint32_t ok;
+  asm volatile(
+      "{\n\t.reg .pred p;\n\tmbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n\t"
+      "selp.u32 %0, 1, 0, p;\n\t}\n"
+      : "=r"(ok)
+      : "r"(bar), "r"(parity)
+      : "memory");
+  return ok != 0;
+}
+
+// Bounded wait: false after kSpinLimit polls.
+__device__ __forceinline__ bool mbar_wait(uint32_t bar, uint32_t parity) {
+  for (int i = 0; i < kSpinLimit; ++i)
+    if (mbar_try(bar, parity)) return true;
+  return false;
+}
+
+__device__ __forceinline__ void bulk_g2s(uint32_t dst, const void *src, uint32_t bytes,
+                                         uint32_t bar) {
+  asm volatile(
+      "cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];" ::"r"(
+          dst),
+      "l"(src), "r"(bytes), "r"(bar)
+      : "memory");
+}
+
+__device__ __forceinline__ void mbar_expect_tx(uint32_t bar, uint32_t bytes) {
+  asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(bar), "r"(bytes)
+               : "memory");
+}
+
+// TMEM loads: 32 lanes x 32-bit, N consecutive columns per thread.
+__device__ __forceinline__ void tmem_ld32(uint32_t taddr, float (&v)[32]) {
+  uint32_t r[32];
+  asm volatile(
+      "tcgen05.ld.sync.aligned.32x32b.x32.b32 {%0,%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,%13,"
+      "%14,%15,%16,%17,%18,%19,%20,%21,%22,%23,%24,%25,%26,%27,%28,%29,%30,%31}, [%32];"
+      : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]), "=r"(r[6]),
+        "=r"(r[7]), "=r"(r[8]), "=r"(r[9]), "=r"(r[10]), "=r"(r[11]), "=r"(r[12]), "=r"(r[13]),
+        "=r"(r[14]), "=r"(r[15]), "=r"(r[16]), "=r"(r[17]), "=r"(r[18]), "=r"(r[19]),
+        "=r"(r[20]), "=r"(r[21]), "=r"(r[22]), "=r"(r[23]), "=r"(r[24]), "=r"(r[25]),
+        "=r"(r[26]), "=r"(r[27]), "=r"(r[28]), "=r"(r[29]), "=r"(r[30]), "=r"(r[31])
+      : "r"(taddr));
+  asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
+#pragma unroll
+  for (int i = 0; i < 32; ++i) v[i] = __uint_as_float(r[i]);
+}
+
+__device__ __forceinline__ void tmem_ld16(uint32_t taddr, float *v) {
+  uint32_t r[16];
+  asm volatile(
+      "tcgen05.ld.sync.aligned.32x32b.x16.b32 {%0,%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,%13,"
+      "%14,%15}, [%16];"
+      : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]), "=r"(r[6]),
+        "=r"(r[7]), "=r"(r[8]), "=r"(r[9]), "=r"(r[10]), "=r"(r[11]), "=r"(r[12]), "=r"(r[13]),
+        "=r"(r[14]), "=r"(r[15])
+      : "r"(taddr));
+  asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
+#pragma unroll
+  for (int i = 0; i < 16; ++i) v[i] = __uint_as_float(r[i]);
+}
+
+__device__ __forceinline__ void tmem_ld8(uint32_t taddr, float *v) {
+  uint32_t r[8];
+  asm volatile("tcgen05.ld.sync.aligned.32x32b.x8.b32 {%0,%1,%2,%3,%4,%5,%6,%7}, [%8];"
+               : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]),
+                 "=r"(r[6]), "=r"(r[7])
+               : "r"(taddr));
+  asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
+#pragma unroll
+  for (int i = 0; i < 8; ++i) v[i] = __uint_as_float(r[i]);
+}
+
+// Spline of one coordinate from its 3K+1 parameters held in registers (static
+// indexing only: the bin is selected with predicated moves).
+template <bool INV>
+__device__ __forceinline__ float spline_reg(const float (&r)[kRawP], float v, float &ld) {
+  float mw = r[0], mh = r[kBins];
+#pragma unroll
+  for (int k = 1; k < kBins; ++k) {
+    mw = fmaxf(mw, r[k]);
+    mh = fmaxf(mh, r[kBins + k]);
+  }
+  float ew[kBins], eh[kBins], sw = 0.f, sh = 0.f;
+#pragma unroll
+  for (int k = 0; k < kBins; ++k) {
+    ew[k] = __expf(r[k] - mw);
+    eh[k] = __expf(r[kBins + k] - mh);
+    sw += ew[k];
+    sh += eh[k];
+  }
+  const float cw = (1.f - kBins * kMinW) / sw, ch = (1.f - kBins * kMinH) / sh;
+  float X = 0.f, Y = 0.f;
+  float xk = 0.f, yk = 0.f, w = kMinW + cw * ew[0], h = kMinH + ch * eh[0];
+  float r0 = r[2 * kBins], r1 = r[2 * kBins + 1];
+#pragma unroll
+  for (int k = 1; k < kBins; ++k) {
+    X += kMinW + cw * ew[k - 1];
+    Y += kMinH + ch * eh[k - 1];
+    const bool sel = INV ? (v >= Y) : (v >= X);
+    if (sel) {
+      xk = X;
+      yk = Y;
+      w  = (k == kBins - 1) ? 1.f - X : kMinW + cw * ew[k];
+      h  = (k == kBins - 1) ? 1.f - Y : kMinH + ch * eh[k];
+      r0 = r[2 * kBins + k];
+      r1 = r[2 * kBins + k + 1];
+    }
+  }
+  const float d0 = kMinD + softplusf(r0), d1 = kMinD + softplusf(r1);
+  const float s = h / w;
+  float       xi, out;
+  if (INV) {
+    const float dy = v - yk;
+    const float t  = d1 + d0 - 2.f * s;
+    const float qa = h * (s - d0) + dy * t;
+    const float qb = h * d0 - dy * t;
+    const float qc = -s * dy;
+    const float dn = -qb - sqrtf(fmaxf(qb * qb - 4.f * qa * qc, 0.f));
+    xi             = dn != 0.f ? 2.f * qc / dn : 0.f;
+    xi             = fminf(fmaxf(xi, 0.f), 1.f);
+    out            = fminf(xk + xi * w, 1.f);
+  } else {
+    xi = fminf(fmaxf((v - xk) / w, 0.f), 1.f);
+  }
+  const float om  = xi * (1.f - xi);
+  const float den = s + (d0 + d1 - 2.f * s) * om;
+  const float q   = d1 * xi * xi + 2.f * s * om + d0 * (1.f - xi) * (1.f - xi);
+  ld              = logf(s * s * q / (den * den));
+  if (!INV) out = yk + h * (s * xi * xi + d0 * om) / den;
+  return out;
+}
 
 template <int MODE>
 __global__ void __launch_bounds__(kFwdThreads, 1)
-    k_flow_fwd(const float *__restrict__ theta, const bf16 *__restrict__ w2p,
-               const bf16 *__restrict__ w3p, int layers, const float *__restrict__ xin,
+    k_flow_fwd(const float *__restrict__ theta, const bf16 *__restrict__ w2c,
+               const bf16 *__restrict__ w3c, int layers, const float *__restrict__ xin,
                int64_t ld_in, int64_t n, uint64_t seed, uint32_t stream, int64_t first,
                float *__restrict__ xout, int64_t ld_out, float *__restrict__ lq_out,
-               float *__restrict__ xs_store) {
-  extern __shared__ __align__(16) unsigned char smem[];
-  bf16   *sW2  = reinterpret_cast<bf16 *>(smem);
-  bf16   *sW3  = sW2 + kHid * HS;
-  bf16   *sH   = sW3 + kHid * W3S;
-  float  *sRaw = reinterpret_cast<float *>(sH + kFwdTile * HS);
-  float  *sX   = sRaw + 2 * kFwdTile * RS;
-  float  *sLq  = sX + kDim * kFwdTile;
-  SmallW *sw   = reinterpret_cast<SmallW *>(sLq + kFwdTile);
+               float *__restrict__ xs_store, int *__restrict__ err) {
+  extern __shared__ __align__(1024) unsigned char fwd_smem[];
+  unsigned char *smem = fwd_smem;
+  float    *sX  = reinterpret_cast<float *>(smem + kOffX);
+  float    *sLq = reinterpret_cast<float *>(smem + kOffLq);
+  SmallW   *sw  = reinterpret_cast<SmallW *>(smem + kOffSw);
+  uint64_t *bars = reinterpret_cast<uint64_t *>(smem + kOffBar);
+  uint32_t *tslot = reinterpret_cast<uint32_t *>(smem + kOffBar + 16);
+  const uint32_t s_base = smem_u32(smem);
+  const uint32_t bar_w = smem_u32(&bars[0]), bar_m = smem_u32(&bars[1]);
+  const int      t = threadIdx.x, warp = t >> 5, wg = t >> 7, row = t & 127;
 
-  const int     warp = threadIdx.x >> 5;
-  const int     m0   = warp * 16;
-  const int64_t ntiles = (n + kFwdTile - 1) / kFwdTile;
-  for (int64_t tile = blockIdx.x; tile < ntiles; tile += gridDim.x) {
-    const int64_t base = tile * kFwdTile;
-    // load the tile (dimension-major)
-    for (int i = threadIdx.x; i < kFwdTile; i += blockDim.x) {
+  if (t == 0) {
+    mbar_init(bar_w, 1);
+    mbar_init(bar_m, 1);
+    asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+  }
+  if (warp == 0) {
+    asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(
+                     smem_u32(tslot)),
+                 "r"(kTmemCols)
+                 : "memory");
+    asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;" ::: "memory");
+  }
+  tc_fence_before();
+  __syncthreads();
+  tc_fence_after();
+  const uint32_t tmem = *tslot;
+  // this thread's TMEM row (lane) and its warpgroup's column bases
+  const uint32_t t_lane = static_cast<uint32_t>((warp & 3) * 32) << 16;
+  const uint32_t d2_col = 128u * wg, d3_col = 256u * wg;
+  uint8_t       *gA = smem + kOffA + wg * kABytes;
+  constexpr uint32_t idesc2 = umma_idesc(128, kHid), idesc3 = umma_idesc(128, kNOutF);
+  uint32_t n_w = 0, n_m = 0;  // phases issued on the weight / product barriers
+  bool     aborted = false;
+
+  const int64_t nsup = (n + kSuper - 1) / kSuper;
+  for (int64_t sup = blockIdx.x; sup < nsup && !aborted; sup += gridDim.x) {
+    const int64_t base = sup * kSuper;
+    for (int i = t; i < kSuper; i += kFwdThreads) {
       const int64_t e = base + i;
       if (MODE == 1 && xin == nullptr) {
         double u[kDim];
         if (e < n) philox_point(seed, stream, static_cast<uint64_t>(first + e), kDim, u);
 #pragma unroll
-        for (int j = 0; j < kDim; ++j) sX[j * kFwdTile + i] = e < n ? __double2float_rd(u[j]) : 0.5f;
+        for (int j = 0; j < kDim; ++j) sX[j * kSuper + i] = e < n ? __double2float_rd(u[j]) : 0.5f;
       } else {
 #pragma unroll
-        for (int j = 0; j < kDim; ++j) sX[j * kFwdTile + i] = e < n ? xin[j * ld_in + e] : 0.5f;
+        for (int j = 0; j < kDim; ++j) sX[j * kSuper + i] = e < n ? xin[j * ld_in + e] : 0.5f;
       }
+      sLq[i] = 0.f;
     }
-    float lq = 0.f;
-    for (int s = 0; s < layers; ++s) {
-      const int l    = MODE == 0 ? s : layers - 1 - s;
+    for (int s = 0; s < layers && !aborted; ++s) {
+      const int l = MODE == 0 ? s : layers - 1 - s;
       const int mask = l % 6;
-      __syncthreads();  // previous layer done with weights, sX settled
+      __syncthreads();  // previous layer's products are complete; sX settled
+      ++n_w;
+      if (t == 0) {
+        mbar_expect_tx(bar_w, kW2Bytes + kW3Bytes);
+        bulk_g2s(s_base + kOffW2, w2c + static_cast<size_t>(l) * (kW2Bytes / 2), kW2Bytes, bar_w);
+        bulk_g2s(s_base + kOffW3, w3c + static_cast<size_t>(l) * (kW3Bytes / 2), kW3Bytes, bar_w);
+      }
+      {
+        const float *th = theta + static_cast<size_t>(l) * kLayerParams;
+        for (int i = t; i < kDA * kHid; i += kFwdThreads) sw->W1[i] = bfr(th[oW1 + i]);
+        for (int i = t; i < kHid; i += kFwdThreads) {
+          sw->b1[i] = th[ob1 + i];
+          sw->b2[i] = th[ob2 + i];
+        }
+        for (int i = t; i < kNOutP; i += kFwdThreads) {
+          const int j = i / kRawP, r = i % kRawP;
+          sw->b3[i] = r < kRaw ? th[ob3 + j * kRaw + r] : 0.f;
+        }
+      }
       if (xs_store) {
-        for (int i = threadIdx.x; i < kFwdTile * kDim; i += blockDim.x) {
-          const int j = i / kFwdTile, p = i % kFwdTile;
+        for (int i = t; i < kSuper * kDim; i += kFwdThreads) {
+          const int j = i / kSuper, p = i % kSuper;
           if (base + p < n) xs_store[(static_cast<int64_t>(l) * kDim + j) * n + base + p] = sX[i];
         }
       }
-      stage_layer(theta, w2p, w3p, l, sW2, sW3, sw);
-      __syncthreads();
-      layer_h1(sX, kFwdTile, mask, sw, sH);
-      __syncthreads();
-      warp_h2(sH, sW2, sw->b2, sH, m0);  // warp-private rows: in place
-      for (int pr = 0; pr < 2; ++pr) {
-        warp_raw(sH, sW3, sw->b3, sRaw, kFwdTile, m0, pr);
-        __syncthreads();
+      const bool okw = mbar_wait(bar_w, (n_w - 1) & 1u);
+      if (__syncthreads_or(!okw)) {
+        aborted = true;
+        break;
+      }
+      for (int sub = 0; sub < kSubs; ++sub) {
+        const int p = sub * kSub + t;
+        // h1 = relu(bf16(x_A) bf16(W1) + b1) -> BF16 A tile, row `row`
         {
-          const int p = threadIdx.x % kFwdTile, jj = threadIdx.x / kFwdTile;
-          const int j = cB[mask][2 * pr + jj];
-          float    *rp = sRaw + (jj * kFwdTile + p) * RS;
-          spline_normalize(rp);
-          float ld;
-          const float v = sX[j * kFwdTile + p];
-          sX[j * kFwdTile + p] = MODE == 0 ? spline_forward(rp, v, ld) : spline_inverse(rp, v, ld);
+          float xa[kDA];
+#pragma unroll
+          for (int i = 0; i < kDA; ++i) xa[i] = bfr(sX[cA[mask][i] * kSuper + p]);
+#pragma unroll 2
+          for (int c = 0; c < kHid / 8; ++c) {
+            float v[8];
+#pragma unroll
+            for (int q = 0; q < 8; ++q) {
+              const int col = c * 8 + q;
+              float     a   = sw->b1[col];
+#pragma unroll
+              for (int i = 0; i < kDA; ++i) a = fmaf(xa[i], sw->W1[i * kHid + col], a);
+              v[q] = fmaxf(a, 0.f);
+            }
+            uint4 pk;
+            pk.x = pack_bf2(v[0], v[1]);
+            pk.y = pack_bf2(v[2], v[3]);
+            pk.z = pack_bf2(v[4], v[5]);
+            pk.w = pack_bf2(v[6], v[7]);
+            *reinterpret_cast<uint4 *>(gA + c * (16 * 128) + row * 16) = pk;
+          }
+        }
+        fence_async_smem();
+        tc_fence_before();
+        __syncthreads();
+        if (t == 0) {
+          tc_fence_after();
+#pragma unroll 1
+          for (int g = 0; g < 2; ++g) {
+            const uint32_t a0 = s_base + kOffA + g * kABytes;
+#pragma unroll
+            for (int kk = 0; kk < kHid / 16; ++kk)
+              umma_bf16(tmem + 128u * g, umma_desc(a0 + kk * 2 * 2048, 2048, 128),
+                        umma_desc(s_base + kOffW2 + kk * 2 * 2048, 2048, 128), idesc2, kk > 0);
+          }
+          umma_commit(bar_m);
+        }
+        ++n_m;
+        bool ok = mbar_wait(bar_m, (n_m - 1) & 1u);
+        if (__syncthreads_or(!ok)) {
+          aborted = true;
+          break;
+        }
+        tc_fence_after();
+        // h2 = relu(D2 + b2) -> BF16 A tile (the products that read h1 are complete)
+#pragma unroll 1
+        for (int c = 0; c < kHid / 32; ++c) {
+          float v[32];
+          tmem_ld32(tmem + t_lane + d2_col + 32u * c, v);
+#pragma unroll
+          for (int q = 0; q < 4; ++q) {
+            uint4       pk;
+            const int   col = c * 32 + q * 8;
+            const float *b2 = sw->b2 + col;
+            pk.x = pack_bf2(fmaxf(v[q * 8 + 0] + b2[0], 0.f), fmaxf(v[q * 8 + 1] + b2[1], 0.f));
+            pk.y = pack_bf2(fmaxf(v[q * 8 + 2] + b2[2], 0.f), fmaxf(v[q * 8 + 3] + b2[3], 0.f));
+            pk.z = pack_bf2(fmaxf(v[q * 8 + 4] + b2[4], 0.f), fmaxf(v[q * 8 + 5] + b2[5], 0.f));
+            pk.w = pack_bf2(fmaxf(v[q * 8 + 6] + b2[6], 0.f), fmaxf(v[q * 8 + 7] + b2[7], 0.f));
+            *reinterpret_cast<uint4 *>(gA + (col / 8) * (16 * 128) + row * 16) = pk;
+          }
+        }
+        fence_async_smem();
+        tc_fence_before();
+        __syncthreads();
+        if (t == 0) {
+          tc_fence_after();
+#pragma unroll 1
+          for (int g = 0; g < 2; ++g) {
+            const uint32_t a0 = s_base + kOffA + g * kABytes;
+#pragma unroll
+            for (int kk = 0; kk < kHid / 16; ++kk)
+              umma_bf16(tmem + 256u * g, umma_desc(a0 + kk * 2 * 2048, 2048, 128),
+                        umma_desc(s_base + kOffW3 + kk * 2 * (16 * kNOutF), 16 * kNOutF, 128),
+                        idesc3, kk > 0);
+          }
+          umma_commit(bar_m);
+        }
+        ++n_m;
+        ok = mbar_wait(bar_m, (n_m - 1) & 1u);
+        if (__syncthreads_or(!ok)) {
+          aborted = true;
+          break;
+        }
+        tc_fence_after();
+        // splines of the four transformed coordinates of this thread's point
+        float lq = 0.f;
+#pragma unroll 1
+        for (int jb = 0; jb < kDA; ++jb) {
+          float r[kRawP];
+          const uint32_t ta = tmem + t_lane + d3_col + static_cast<uint32_t>(jb * kRawF);
+          float v32[32];
+          tmem_ld32(ta, v32);
+#pragma unroll
+          for (int i = 0; i < 32; ++i) r[i] = v32[i];
+          tmem_ld16(ta + 32, r + 32);
+          tmem_ld8(ta + 48, r + 48);
+#pragma unroll
+          for (int i = 0; i < kRaw; ++i) r[i] += sw->b3[jb * kRawP + i];
+          const int j  = cB[mask][jb];
+          float     ld;
+          const float vin = sX[j * kSuper + p];
+          sX[j * kSuper + p] = spline_reg<MODE == 1>(r, vin, ld);
           lq += ld;
         }
-        __syncthreads();
+        sLq[p] += lq;
+        tc_fence_before();
+        __syncthreads();  // D3 read out before the next subtile's D2 overwrites it
       }
     }
-    // combine the two threads of each point
-    if (threadIdx.x >= kFwdTile) sLq[threadIdx.x - kFwdTile] = lq;
+    if (aborted) break;
     __syncthreads();
-    if (threadIdx.x < kFwdTile) {
-      const int64_t e = base + threadIdx.x;
-      if (e < n) lq_out[e] = lq + sLq[threadIdx.x];
-    }
+    for (int i = t; i < kSuper; i += kFwdThreads)
+      if (base + i < n) lq_out[base + i] = sLq[i];
     if (xout) {
-      for (int i = threadIdx.x; i < kFwdTile * kDim; i += blockDim.x) {
-        const int j = i / kFwdTile, p = i % kFwdTile;
+      for (int i = t; i < kSuper * kDim; i += kFwdThreads) {
+        const int j = i / kSuper, p = i % kSuper;
         if (base + p < n) xout[static_cast<int64_t>(j) * ld_out + base + p] = sX[i];
       }
     }
-    __syncthreads();
+  }
+  if (aborted) {
+    if (t == 0) atomicExch(err, 1);
+    // let outstanding copies and products land before the memory is released
+    if (n_w) mbar_wait(bar_w, (n_w - 1) & 1u);
+    if (n_m) mbar_wait(bar_m, (n_m - 1) & 1u);
+  }
+  tc_fence_before();
+  __syncthreads();
+  if (warp == 0) {
+    tc_fence_after();
+    asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem),
+                 "r"(kTmemCols)
+                 : "memory");
   }
 }
 
@@ -784,18 +1102,25 @@ __global__ void __launch_bounds__(kBwdThreads, 1)
 // ---------------------------------------------------------------------------
 // Packing and Adam.
 
+// FP32 master weights -> BF16 operand copies:
+//   w2p, w3p  padded row-major [k][n] tiles for the backward kernel (ldmatrix)
+//   w2c, w3c  canonical K-major layouts of W2^T and W3^T for the forward kernel
+//             (element (n, k) of an N-row operand at (k/8)*8N + n*8 + k%8)
 __global__ void k_flow_pack(const float *__restrict__ theta, int layers, bf16 *__restrict__ w2p,
-                            bf16 *__restrict__ w3p) {
+                            bf16 *__restrict__ w3p, bf16 *__restrict__ w2c,
+                            bf16 *__restrict__ w3c) {
   const int64_t n2 = static_cast<int64_t>(layers) * kHid * HS;
   const int64_t n3 = static_cast<int64_t>(layers) * kHid * W3S;
-  for (int64_t i = blockIdx.x * static_cast<int64_t>(blockDim.x) + threadIdx.x; i < n2 + n3;
-       i += static_cast<int64_t>(gridDim.x) * blockDim.x) {
+  const int64_t c2 = static_cast<int64_t>(layers) * kHid * kHid;
+  const int64_t c3 = static_cast<int64_t>(layers) * kNOutF * kHid;
+  for (int64_t i = blockIdx.x * static_cast<int64_t>(blockDim.x) + threadIdx.x;
+       i < n2 + n3 + c2 + c3; i += static_cast<int64_t>(gridDim.x) * blockDim.x) {
     if (i < n2) {
       const int64_t l = i / (kHid * HS);
       const int     r = static_cast<int>(i % (kHid * HS));
       const int     k = r / HS, c = r % HS;
       w2p[i] = __float2bfloat16_rn(c < kHid ? theta[l * kLayerParams + oW2 + k * kHid + c] : 0.f);
-    } else {
+    } else if (i < n2 + n3) {
       const int64_t i3 = i - n2;
       const int64_t l  = i3 / (kHid * W3S);
       const int     r  = static_cast<int>(i3 % (kHid * W3S));
@@ -804,6 +1129,20 @@ __global__ void k_flow_pack(const float *__restrict__ theta, int layers, bf16 *_
       const bool    real = c < kNOutP && q < kRaw;
       w3p[i3] = __float2bfloat16_rn(real ? theta[l * kLayerParams + oW3 + k * kNOut + j * kRaw + q]
                                          : 0.f);
+    } else if (i < n2 + n3 + c2) {
+      const int64_t i2 = i - n2 - n3;
+      const int64_t l  = i2 / (kHid * kHid);
+      const int     r  = static_cast<int>(i2 % (kHid * kHid));
+      const int     kc = r / (8 * kHid), nn = (r / 8) % kHid, k = kc * 8 + r % 8;
+      w2c[i2] = __float2bfloat16_rn(theta[l * kLayerParams + oW2 + k * kHid + nn]);
+    } else {
+      const int64_t i3 = i - n2 - n3 - c2;
+      const int64_t l  = i3 / (kNOutF * kHid);
+      const int     r  = static_cast<int>(i3 % (kNOutF * kHid));
+      const int     kc = r / (8 * kNOutF), nn = (r / 8) % kNOutF, k = kc * 8 + r % 8;
+      const int     j = nn / kRawF, q = nn % kRawF;
+      w3c[i3] = __float2bfloat16_rn(q < kRaw ? theta[l * kLayerParams + oW3 + k * kNOut + j * kRaw + q]
+                                             : 0.f);
     }
   }
 }
@@ -857,6 +1196,8 @@ using flow::bf16;
 
 size_t flow_w2p_elems(int layers) { return size_t(layers) * flow::kHid * flow::HS; }
 size_t flow_w3p_elems(int layers) { return size_t(layers) * flow::kHid * flow::W3S; }
+size_t flow_w2c_elems(int layers) { return size_t(layers) * flow::kHid * flow::kHid; }
+size_t flow_w3c_elems(int layers) { return size_t(layers) * flow::kNOutF * flow::kHid; }
 
 static int sm_count() {
   int dev = 0, sms = 0;
@@ -865,31 +1206,32 @@ static int sm_count() {
   return sms;
 }
 
-cudaError_t launch_flow_pack(const float *theta, int layers, void *w2p, void *w3p,
-                             cudaStream_t st) {
-  flow::k_flow_pack<<<4 * sm_count(), 256, 0, st>>>(theta, layers, static_cast<bf16 *>(w2p),
-                                                    static_cast<bf16 *>(w3p));
+cudaError_t launch_flow_pack(const float *theta, int layers, void *w2p, void *w3p, void *w2c,
+                             void *w3c, cudaStream_t st) {
+  flow::k_flow_pack<<<4 * sm_count(), 256, 0, st>>>(
+      theta, layers, static_cast<bf16 *>(w2p), static_cast<bf16 *>(w3p), static_cast<bf16 *>(w2c),
+      static_cast<bf16 *>(w3c));
   return cudaGetLastError();
 }
 
-cudaError_t launch_flow_forward(int mode, const float *theta, const void *w2p, const void *w3p,
+cudaError_t launch_flow_forward(int mode, const float *theta, const void *w2c, const void *w3c,
                                 int layers, const float *xin, int64_t ld_in, int64_t n,
                                 uint64_t seed, uint32_t stream, int64_t first, float *xout,
-                                int64_t ld_out, float *lq, float *xs_store, cudaStream_t st) {
+                                int64_t ld_out, float *lq, float *xs_store, int *err,
+                                cudaStream_t st) {
   if (n <= 0) return cudaSuccess;
-  const int64_t tiles = (n + flow::kFwdTile - 1) / flow::kFwdTile;
-  const int     grid  = static_cast<int>(std::min<int64_t>(tiles, sm_count()));
-  const size_t  sm    = flow::kFwdSmem;
+  const int64_t sup  = (n + flow::kSuper - 1) / flow::kSuper;
+  const int     grid = static_cast<int>(std::min<int64_t>(sup, sm_count()));
+  const int     sm   = static_cast<int>(flow::kFwdSmem);
+  const bf16   *a = static_cast<const bf16 *>(w2c), *b = static_cast<const bf16 *>(w3c);
   if (mode == 0) {
-    cudaFuncSetAttribute(flow::k_flow_fwd<0>, cudaFuncAttributeMaxDynamicSharedMemorySize, int(sm));
+    cudaFuncSetAttribute(flow::k_flow_fwd<0>, cudaFuncAttributeMaxDynamicSharedMemorySize, sm);
     flow::k_flow_fwd<0><<<grid, flow::kFwdThreads, sm, st>>>(
-        theta, static_cast<const bf16 *>(w2p), static_cast<const bf16 *>(w3p), layers, xin,
-        ld_in, n, seed, stream, first, xout, ld_out, lq, xs_store);
+        theta, a, b, layers, xin, ld_in, n, seed, stream, first, xout, ld_out, lq, xs_store, err);
   } else {
-    cudaFuncSetAttribute(flow::k_flow_fwd<1>, cudaFuncAttributeMaxDynamicSharedMemorySize, int(sm));
+    cudaFuncSetAttribute(flow::k_flow_fwd<1>, cudaFuncAttributeMaxDynamicSharedMemorySize, sm);
     flow::k_flow_fwd<1><<<grid, flow::kFwdThreads, sm, st>>>(
-        theta, static_cast<const bf16 *>(w2p), static_cast<const bf16 *>(w3p), layers, xin,
-        ld_in, n, seed, stream, first, xout, ld_out, lq, xs_store);
+        theta, a, b, layers, xin, ld_in, n, seed, stream, first, xout, ld_out, lq, xs_store, err);
   }
   return cudaGetLastError();
 }

@@ -22,19 +22,23 @@ constexpr int kMaxLayers   = 12;
 
 }  // namespace flow
 
-size_t      flow_w2p_elems(int layers);  // BF16 elements of the packed W2 copies
-size_t      flow_w3p_elems(int layers);  // BF16 elements of the packed W3 copies
-cudaError_t launch_flow_pack(const float *theta, int layers, void *w2p, void *w3p,
-                             cudaStream_t st);
+size_t      flow_w2p_elems(int layers);  // BF16 elements of the padded W2 copies (backward)
+size_t      flow_w3p_elems(int layers);  // BF16 elements of the padded W3 copies (backward)
+size_t      flow_w2c_elems(int layers);  // BF16 elements of the canonical W2^T copies (forward)
+size_t      flow_w3c_elems(int layers);  // BF16 elements of the canonical W3^T copies (forward)
+cudaError_t launch_flow_pack(const float *theta, int layers, void *w2p, void *w3p, void *w2c,
+                             void *w3c, cudaStream_t st);
 // mode 0: density direction (xin = points x, xout = z); mode 1: sampling direction
 // (xin = z or, when null, Philox uniforms of points first..first+n-1 with key seed and
 // stream id `stream`; xout = x). Arrays are dimension-major with leading dimension
 // ld_in / ld_out. lq receives log q(x). xs_store (density mode, may be null) receives
-// each layer's input, layers x 8 x n.
-cudaError_t launch_flow_forward(int mode, const float *theta, const void *w2p, const void *w3p,
+// each layer's input, layers x 8 x n. err: device int set to 1 when a bounded wait of
+// the kernel gave up (its outputs are then invalid).
+cudaError_t launch_flow_forward(int mode, const float *theta, const void *w2c, const void *w3c,
                                 int layers, const float *xin, int64_t ld_in, int64_t n,
                                 uint64_t seed, uint32_t stream, int64_t first, float *xout,
-                                int64_t ld_out, float *lq, float *xs_store, cudaStream_t st);
+                                int64_t ld_out, float *lq, float *xs_store, int *err,
+                                cudaStream_t st);
 // Loss over n points and its gradient (accumulated into grad, which the caller zeroes;
 // loss_sum receives sum_i l_i added to its value). kind 1: l = coef exp(-log q);
 // kind 0: l = -coef log q.
