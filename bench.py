@@ -43,7 +43,7 @@ METRIC = "unweighted events/s at 0.1% sigma stat err (screened pi+pi- continuum,
 UNIT = "events/s"
 N_BT, N_KT2, LOOP_KT, LOOP_PHI, LOOP_KTMAX = 1024, 10000, 63, 33, 3.0
 LOOP_POINTS = (LOOP_KT + 1) * (LOOP_PHI + 1)
-TRAFFIC_FILE = os.path.join(REPO, "profiles", "vegas_sample_c2_traffic.json")  # k_vegas_loop
+TRAFFIC_FILE = os.path.join(REPO, "profiles", "k_vegas_loop_rec_traffic.json")
 
 
 def workload_params():
