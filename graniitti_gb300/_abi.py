@@ -103,7 +103,7 @@ GRN_FLOW_LOSS_VARIANCE = 1
 
 class FlowParams(ctypes.Structure):
     _fields_ = [("dim", c_int32), ("layers", c_int32), ("hidden", c_int32), ("bins", c_int32),
-                ("seed", c_uint64)]
+                ("seed", c_uint64), ("mix_uniform", c_double)]
 
 
 class FlowTrainParams(ctypes.Structure):

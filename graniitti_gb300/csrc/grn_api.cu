@@ -147,6 +147,7 @@ struct grn_flow {
   uint64_t    seed   = 1;
   int64_t     nparams = 0;
   int64_t     adam_t  = 0;
+  double      mix     = 0.0;  // weight of the uniform component of the proposal
   DevBuf      d_theta, d_m, d_v, d_grad, d_w2p, d_w3p, d_w2c, d_w3c, d_loss, d_err;
   DevBuf      d_x, d_z, d_lq, d_coef, d_xs;  // batch scratch
   DevBuf      d_tu, d_tlq, d_tcoef;          // training set
@@ -1058,6 +1059,7 @@ void grn_flow_default_params(grn_flow_params *p) {
   p->hidden = grn::flow::kHid;
   p->bins   = grn::flow::kBins;
   p->seed   = 1;
+  p->mix_uniform = 0.0;
 }
 
 grn_status grn_flow_create(grn_engine *e, const grn_flow_params *p, grn_flow **out) {
@@ -1069,11 +1071,14 @@ grn_status grn_flow_create(grn_engine *e, const grn_flow_params *p, grn_flow **o
     return fail(GRN_ERR_UNSUPPORTED, "flow kernels are built for hidden = 128, bins = 16");
   if (p->layers < 1 || p->layers > grn::flow::kMaxLayers)
     return fail(GRN_ERR_INVALID, "flow layers must be in [1, 12]");
+  if (!(p->mix_uniform >= 0.0 && p->mix_uniform < 1.0))
+    return fail(GRN_ERR_INVALID, "flow mix_uniform must be in [0, 1)");
   GRN_CUDA(cudaSetDevice(e->device));
   auto *f    = new grn_flow();
   f->e       = e;
   f->layers  = p->layers;
   f->seed    = p->seed;
+  f->mix     = p->mix_uniform;
   f->nparams = static_cast<int64_t>(p->layers) * grn::flow::kLayerParams;
   std::vector<float> th(f->nparams, 0.0f);
   uint64_t           state = p->seed;
@@ -1242,21 +1247,32 @@ grn_status grn_flow_train_step(grn_flow *f, const float *x, const float *coef, i
   return GRN_OK;
 }
 
-// Points of a pass: Philox uniforms (q = 1) or a flow sample, into d_fu / d_flq
-// (dimension-major, leading dimension n) of `dst_u` / `dst_lq`.
+// Points of a pass (dimension-major, leading dimension n) and their log density:
+// Philox uniforms (q = 1), or the proposal alpha * uniform + (1 - alpha) * flow whose first
+// floor(alpha n) points are the uniform component (flow density from the density
+// direction) and the rest flow samples.
 static grn_status flow_points(grn_flow *f, bool from_flow, uint32_t stream_id, int64_t n,
                               DevBuf &dst_u, DevBuf &dst_lq) {
   grn_engine *e = f->e;
   GRN_CUDA(dst_u.ensure(static_cast<size_t>(n) * grn::flow::kDim * sizeof(float)));
   GRN_CUDA(dst_lq.ensure(static_cast<size_t>(n) * sizeof(float)));
-  if (from_flow)
-    GRN_CUDA(grn::launch_flow_forward(1, f->d_theta.as<float>(), f->d_w2c.p, f->d_w3c.p,
-                                      f->layers, nullptr, n, n, e->seed ^ 0xF10Bull, stream_id, 0,
-                                      dst_u.as<float>(), n, dst_lq.as<float>(), nullptr,
+  float         *u = dst_u.as<float>(), *lq = dst_lq.as<float>();
+  const uint64_t key = e->seed ^ 0xF10Bull;
+  if (!from_flow) {
+    GRN_CUDA(grn::launch_flow_uniform(key, stream_id, 0, n, n, u, lq, e->stream));
+    return GRN_OK;
+  }
+  const int64_t nu = static_cast<int64_t>(f->mix * static_cast<double>(n));
+  if (nu > 0) {
+    GRN_CUDA(grn::launch_flow_uniform(key, stream_id, 0, nu, n, u, nullptr, e->stream));
+    GRN_CUDA(grn::launch_flow_forward(0, f->d_theta.as<float>(), f->d_w2c.p, f->d_w3c.p,
+                                      f->layers, u, n, nu, 0, 0, 0, nullptr, 0, lq, nullptr,
                                       f->d_err.as<int>(), e->stream));
-  else
-    GRN_CUDA(grn::launch_flow_uniform(e->seed ^ 0xF10Bull, stream_id, n, dst_u.as<float>(),
-                                      dst_lq.as<float>(), e->stream));
+  }
+  GRN_CUDA(grn::launch_flow_forward(1, f->d_theta.as<float>(), f->d_w2c.p, f->d_w3c.p, f->layers,
+                                    nullptr, n, n - nu, key, stream_id, nu, u + nu, n, lq + nu,
+                                    nullptr, f->d_err.as<int>(), e->stream));
+  if (f->mix > 0.0) GRN_CUDA(grn::launch_flow_mix(lq, n, f->mix, e->stream));
   return GRN_OK;
 }
 

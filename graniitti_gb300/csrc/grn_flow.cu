@@ -1175,16 +1175,23 @@ __global__ void k_flow_coef(const double *__restrict__ f, const float *__restric
   }
 }
 
-__global__ void k_flow_uniform(uint64_t seed, uint32_t stream, int64_t n, float *__restrict__ u,
-                               float *__restrict__ lq) {
+__global__ void k_flow_uniform(uint64_t seed, uint32_t stream, int64_t first, int64_t n,
+                               int64_t ld, float *__restrict__ u, float *__restrict__ lq) {
   for (int64_t i = blockIdx.x * static_cast<int64_t>(blockDim.x) + threadIdx.x; i < n;
        i += static_cast<int64_t>(gridDim.x) * blockDim.x) {
     double v[kDim];
-    philox_point(seed, stream, static_cast<uint64_t>(i), kDim, v);
+    philox_point(seed, stream, static_cast<uint64_t>(first + i), kDim, v);
 #pragma unroll
-    for (int j = 0; j < kDim; ++j) u[j * n + i] = __double2float_rd(v[j]);
+    for (int j = 0; j < kDim; ++j) u[j * ld + i] = __double2float_rd(v[j]);
     if (lq) lq[i] = 0.f;
   }
+}
+
+// Density of the defensive mixture alpha * uniform + (1 - alpha) * flow from the flow's log q.
+__global__ void k_flow_mix(float *__restrict__ lq, int64_t n, double alpha) {
+  for (int64_t i = blockIdx.x * static_cast<int64_t>(blockDim.x) + threadIdx.x; i < n;
+       i += static_cast<int64_t>(gridDim.x) * blockDim.x)
+    lq[i] = static_cast<float>(log(alpha + (1.0 - alpha) * exp(static_cast<double>(lq[i]))));
 }
 
 }  // namespace flow
@@ -1263,10 +1270,16 @@ cudaError_t launch_flow_coef(const double *f, const float *lq0, int64_t n, int k
   return cudaGetLastError();
 }
 
-cudaError_t launch_flow_uniform(uint64_t seed, uint32_t stream, int64_t n, float *u, float *lq,
-                                cudaStream_t st) {
+cudaError_t launch_flow_uniform(uint64_t seed, uint32_t stream, int64_t first, int64_t n,
+                                int64_t ld, float *u, float *lq, cudaStream_t st) {
   if (n <= 0) return cudaSuccess;
-  flow::k_flow_uniform<<<4 * sm_count(), 256, 0, st>>>(seed, stream, n, u, lq);
+  flow::k_flow_uniform<<<4 * sm_count(), 256, 0, st>>>(seed, stream, first, n, ld, u, lq);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_flow_mix(float *lq, int64_t n, double alpha, cudaStream_t st) {
+  if (n <= 0) return cudaSuccess;
+  flow::k_flow_mix<<<4 * sm_count(), 256, 0, st>>>(lq, n, alpha);
   return cudaGetLastError();
 }
 

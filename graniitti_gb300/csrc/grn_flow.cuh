@@ -51,8 +51,11 @@ cudaError_t launch_flow_adam(float *theta, float *m, float *v, const float *grad
 // lq0 (null = uniform): kind 1: coef = f^2 exp(lq0) / norm; kind 0: coef = f / norm.
 cudaError_t launch_flow_coef(const double *f, const float *lq0, int64_t n, int kind, double norm,
                              float *coef, cudaStream_t st);
-// Philox uniforms as FP32, rounded down (dimension-major, leading dimension n).
-cudaError_t launch_flow_uniform(uint64_t seed, uint32_t stream, int64_t n, float *u, float *lq,
-                                cudaStream_t st);
+// Philox uniforms of points first..first+n-1 as FP32, rounded down (dimension-major,
+// leading dimension ld); lq (may be null) <- 0.
+cudaError_t launch_flow_uniform(uint64_t seed, uint32_t stream, int64_t first, int64_t n,
+                                int64_t ld, float *u, float *lq, cudaStream_t st);
+// lq <- log(alpha + (1 - alpha) exp(lq)): the defensive mixture with the uniform density.
+cudaError_t launch_flow_mix(float *lq, int64_t n, double alpha, cudaStream_t st);
 
 }  // namespace grn

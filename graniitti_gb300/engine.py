@@ -165,13 +165,14 @@ class Flow:
 
     Point arrays are float32, dimension-major (dim x n)."""
 
-    def __init__(self, engine, layers=6, seed=1):
+    def __init__(self, engine, layers=6, seed=1, mix_uniform=0.0):
         self.engine = engine
         self.lib = engine.lib
         p = _abi.FlowParams()
         self.lib.grn_flow_default_params(ctypes.byref(p))
         p.layers = layers
         p.seed = seed
+        p.mix_uniform = mix_uniform
         h = ctypes.c_void_p()
         _abi.check(self.lib.grn_flow_create(engine.h, ctypes.byref(p), ctypes.byref(h)))
         self.h = h

@@ -320,6 +320,8 @@ typedef struct grn_flow_params {
   int32_t  hidden;  /* MLP width (128) */
   int32_t  bins;    /* spline bins (16) */
   uint64_t seed;    /* initial weights */
+  double   mix_uniform; /* alpha in [0, 1): passes sample alpha * uniform + (1 - alpha) * flow,
+                           so every weight is at most (plain VEGAS weight) / alpha (default 0) */
 } grn_flow_params;
 
 #define GRN_FLOW_LOSS_KL       0 /* weighted maximum likelihood: -E[f log q] */

@@ -186,4 +186,28 @@ def test_trained_flow_reduces_variance_and_keeps_sigma(gpu, params):
     w, _ = e.event_weights(pts)
     assert np.all(w > 0)
     f.close()
+    # defensive mixture: 20% of each pass uniform, the same trained weights
+    fm = g.Flow(e, layers=6, seed=7, mix_uniform=0.2)
+    rm = fm.train(n_train=1 << 19, batch=1 << 14, epochs=6, rounds=2, lr=1e-3)
+    assert rm.rel_var_flow < rm.rel_var_start
+    e.vegas_clear()
+    rmx = [fm.iteration(mode=1, iter_id=400 + it) for it in range(4)][-1]
+    pull = (rmx.sigma - plain.sigma) / np.hypot(rmx.sigma_err, plain.sigma_err)
+    print("mixture: rel var %.3f -> %.3f, sigma %.6e pull %.2f"
+          % (rm.rel_var_start, rm.rel_var_flow, rmx.sigma, pull))
+    assert abs(pull) < 4
+    fm.close()
+    e.close()
+
+
+def test_flow_rejects_bad_parameters(gpu, params):
+    import graniitti_gb300 as g
+    from graniitti_gb300 import _abi
+    e = g.Engine(params, 0)
+    for kw in (dict(layers=0), dict(layers=13), dict(mix_uniform=1.0), dict(mix_uniform=-0.1)):
+        with pytest.raises(_abi.GrnError):
+            g.Flow(e, **kw)
+    f = g.Flow(e)
+    with pytest.raises(_abi.GrnError):   # grid not initialised
+        f.train(n_train=1 << 16, batch=1 << 14)
     e.close()
