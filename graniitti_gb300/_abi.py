@@ -97,6 +97,11 @@ class VegasResult(ctypes.Structure):
                [("iterations", c_int64), ("nan_count", c_int64)]
 
 
+class FlatParams(ctypes.Structure):
+    _fields_ = [("ncall", c_int64), ("precision", c_double), ("min_events", c_int64),
+                ("prec", c_int32), ("_pad", c_int32), ("seed", c_uint64)]
+
+
 GRN_FLOW_LOSS_KL = 0
 GRN_FLOW_LOSS_VARIANCE = 1
 
@@ -141,6 +146,7 @@ SIGNATURES = {
     "grn_vegas_init": (c_int32, [c_void_p, c_void_p]),
     "grn_vegas_iteration": (c_int32, [c_void_p, c_int32, c_int32, c_uint32, c_void_p]),
     "grn_vegas_integrate": (c_int32, [c_void_p, c_void_p, c_void_p]),
+    "grn_flat_integrate": (c_int32, [c_void_p, c_void_p, c_void_p]),
     "grn_vegas_get_grid": (c_int32, [c_void_p, c_void_p]),
     "grn_vegas_set_grid": (c_int32, [c_void_p, c_void_p]),
     "grn_vegas_clear": (c_int32, [c_void_p]),

@@ -103,6 +103,7 @@ struct grn_engine {
   uint64_t    seed = 1;
   int         nblocks = 0;
   DevBuf      d_xmat, d_xmat_prev, d_f2mat, d_f, d_acc, d_parts, d_sc;
+  DevBuf      d_xmat_flat;  // uniform grid of FLAT passes (x = u, vw = 1)
   DevBuf      d_lidx, d_lx, d_lvw, d_lbins;  // screened work list of a VEGAS pass
   DevBuf      d_recf, d_recd;                // loop records (record mode), shared by calls
   double     *h_sc = nullptr;  // pinned
@@ -120,6 +121,8 @@ struct grn_engine {
   const float *last_fu = nullptr;  // flow points of the last pass (null: Philox points)
   // unweighting
   DevBuf      d_uw_counts, d_uw_misc, d_uw_idx;
+  // flows created on this engine (detached when the engine is destroyed first)
+  std::vector<grn_flow *> flows;
   // timing of the sampling kernel
   cudaEvent_t ev0 = nullptr, ev1 = nullptr;
   double      sample_ms = 0.0;
@@ -142,7 +145,8 @@ struct grn_engine {
 // ---------------------------------------------------------------------------
 // Flow proposal state (grn_flow.cu holds the kernels).
 struct grn_flow {
-  grn_engine *e      = nullptr;
+  grn_engine *e      = nullptr;  // null once the engine has been destroyed
+  int         device = 0;
   int         layers = 6;
   uint64_t    seed   = 1;
   int64_t     nparams = 0;
@@ -391,8 +395,9 @@ grn_status grn_destroy(grn_engine *e) {
                     &e->d_wlist, &e->d_wcount, &e->d_xmat,      &e->d_xmat_prev, &e->d_f2mat,
                     &e->d_f,     &e->d_acc,    &e->d_parts,     &e->d_sc,        &e->d_lidx,
                     &e->d_lx,    &e->d_lvw,    &e->d_lbins,     &e->d_uw_counts, &e->d_uw_misc,
-                    &e->d_uw_idx, &e->d_recf,  &e->d_recd};
+                    &e->d_uw_idx, &e->d_recf,  &e->d_recd,      &e->d_xmat_flat};
   for (DevBuf *b : bufs) b->release();
+  for (grn_flow *f : e->flows) f->e = nullptr;  // they stay valid for grn_flow_destroy
   if (e->h_sc) cudaFreeHost(e->h_sc);
   if (e->ev0) cudaEventDestroy(e->ev0);
   if (e->ev1) cudaEventDestroy(e->ev1);
@@ -611,6 +616,14 @@ static grn_status vegas_alloc(grn_engine *e) {
   return vegas_alloc_calls(e, e->ncall);
 }
 
+static grn_status set_ncall(grn_engine *e, int64_t n) {
+  if (n != e->ncall) {
+    e->ncall = n;
+    return vegas_alloc_calls(e, n);
+  }
+  return GRN_OK;
+}
+
 grn_status grn_vegas_init(grn_engine *e, const grn_vegas_params *vp) {
   if (!e || !vp) return fail(GRN_ERR_INVALID, "null argument");
   if (vp->bins < 2 || vp->bins % 2 || vp->bins > 256)
@@ -660,15 +673,17 @@ grn_status grn_set_maxweight(grn_engine *e, double maxf) {
 // d_f, pass scalars into h_sc, optional grid refinement. With fu / flq the points
 // come from the flow (dimension-major, leading dimension ncall) and carry 1/q.
 static grn_status vegas_pass(grn_engine *e, int prec, int track_max, int refine,
-                             uint32_t stream_id, const float *fu, const float *flq) {
+                             uint32_t stream_id, const float *fu, const float *flq,
+                             const double *grid = nullptr) {
   const int nh = e->bins * e->dim;
-  GRN_CUDA(cudaMemcpyAsync(e->d_xmat_prev.p, e->d_xmat.p, nh * sizeof(double),
+  const double *xmat = grid ? grid : e->d_xmat.as<double>();
+  GRN_CUDA(cudaMemcpyAsync(e->d_xmat_prev.p, xmat, nh * sizeof(double),
                            cudaMemcpyDeviceToDevice, e->stream));
   const KArgs a   = e->args();
   const bool  rec = grn::record_mode(a, prec);
   float      *rf  = rec ? e->d_recf.as<float>() : nullptr;
   double     *rd  = rec ? e->d_recd.as<double>() : nullptr;
-  GRN_CUDA(grn::launch_vegas_born(a, e->d_xmat.as<double>(), e->bins, e->dim, e->ncall, e->seed,
+  GRN_CUDA(grn::launch_vegas_born(a, xmat, e->bins, e->dim, e->ncall, e->seed,
                                   stream_id, track_max, e->d_f.as<double>(),
                                   e->d_f2mat.as<double>(), e->d_acc.as<unsigned long long>(),
                                   e->d_lidx.as<int64_t>(), e->d_lx.as<double>(),
@@ -840,6 +855,77 @@ grn_status grn_vegas_integrate(grn_engine *e, const grn_vegas_params *vp, grn_ve
     if (factor == 1) break;
     ncall *= factor;
     burnin *= 2;
+  }
+  if (out) *out = r;
+  return GRN_OK;
+}
+
+// The reference's FLAT integrator (MGraniitti::SampleFlat, GMODE = 0,
+// src/MGraniitti.cc:1446-1524; estimate Stats::CalculateCrossSection,
+// include/Graniitti/MGraniitti.h:59-66): uniform points, sigma = sum W / N,
+// sigma_err = sqrt((sum W^2 / N - sigma^2) / N), until sigma_err / sigma < precision
+// and N > min_events. Passes of fp->ncall Philox points through a uniform grid.
+grn_status grn_flat_integrate(grn_engine *e, const grn_flat_params *fp, grn_vegas_result *out) {
+  if (!e || !fp) return fail(GRN_ERR_INVALID, "null argument");
+  if (fp->ncall < 1 || !(fp->precision > 0) || fp->min_events < 0 ||
+      (fp->prec != GRN_PREC_FP64 && fp->prec != GRN_PREC_MIXED))
+    return fail(GRN_ERR_INVALID, "bad FLAT parameters");
+  grn_status st = require_screening_ready(e);
+  if (st != GRN_OK) return st;
+  GRN_CUDA(cudaSetDevice(e->device));
+  if (!e->vegas_ready) {
+    e->bins   = 128;
+    e->lambda = 1.5;
+    e->ncall  = fp->ncall;
+    st        = vegas_alloc(e);
+    if (st != GRN_OK) return st;
+    GRN_CUDA(grn::launch_vegas_grid_init(e->d_xmat.as<double>(), e->bins, e->dim, e->stream));
+    e->vegas_ready = true;
+  }
+  st = set_ncall(e, fp->ncall);
+  if (st != GRN_OK) return st;
+  const int nh = e->bins * e->dim;
+  GRN_CUDA(e->d_xmat_flat.ensure(nh * sizeof(double)));
+  GRN_CUDA(grn::launch_vegas_grid_init(e->d_xmat_flat.as<double>(), e->bins, e->dim, e->stream));
+  e->seed = fp->seed;
+  e->prec = fp->prec;
+  e->maxf = e->maxW = 0.0;
+  double wsum = 0.0, w2sum = 0.0, nev = 0.0;
+  grn_vegas_result r{};
+  for (int64_t it = 0; it < 100000; ++it) {
+    st = vegas_pass(e, fp->prec, 1, 0, e->next_stream++, nullptr, nullptr,
+                    e->d_xmat_flat.as<double>());
+    if (st != GRN_OK) return st;
+    const double *sc = e->h_sc;
+    wsum += sc[grn::VS_FSUM];
+    w2sum += sc[grn::VS_F2SUM];
+    nev += static_cast<double>(e->ncall);
+    e->maxf = std::max(e->maxf, sc[grn::VS_MAXF]);
+    e->maxW = std::max(e->maxW, sc[grn::VS_MAXW]);
+    e->evaluations += sc[grn::VS_EVAL];
+    e->amp_ok += sc[grn::VS_AMP_OK];
+    e->kin_ok += sc[grn::VS_KIN_OK];
+    e->fid_ok += sc[grn::VS_FID_OK];
+    e->veto_ok += sc[grn::VS_VETO_OK];
+    e->nan_total += static_cast<int64_t>(sc[grn::VS_NAN]);
+    if (e->nan_total > 50)
+      return fail(GRN_ERR_NAN, "more than 50 NaN/Inf weights: check model parameters and cuts");
+    const double sigma = wsum / nev;
+    const double var   = std::max(w2sum / nev - sigma * sigma, 0.0);
+    r.sigma            = sigma;
+    r.sigma_err        = std::sqrt(var / nev);
+    r.I_this           = sc[grn::VS_FSUM] / static_cast<double>(e->ncall);
+    r.I2_this          = var / static_cast<double>(e->ncall);
+    r.maxf             = e->maxf;
+    r.maxW             = e->maxW;
+    r.evaluations      = e->evaluations;
+    r.amplitude_ok     = e->amp_ok;
+    r.kinematics_ok    = e->kin_ok;
+    r.fidcuts_ok       = e->fid_ok;
+    r.vetocuts_ok      = e->veto_ok;
+    r.iterations       = it + 1;
+    r.nan_count        = e->nan_total;
+    if (sigma > 0 && r.sigma_err / sigma < fp->precision && nev > fp->min_events) break;
   }
   if (out) *out = r;
   return GRN_OK;
@@ -1043,7 +1129,8 @@ grn_status flow_adam(grn_flow *f, double lr) {
 }
 
 grn_status check_flow(grn_flow *f) {
-  if (!f || !f->e) return fail(GRN_ERR_INVALID, "null flow");
+  if (!f) return fail(GRN_ERR_INVALID, "null flow");
+  if (!f->e) return fail(GRN_ERR_STATE, "the flow's engine has been destroyed");
   GRN_CUDA(cudaSetDevice(f->e->device));
   return GRN_OK;
 }
@@ -1076,6 +1163,8 @@ grn_status grn_flow_create(grn_engine *e, const grn_flow_params *p, grn_flow **o
   GRN_CUDA(cudaSetDevice(e->device));
   auto *f    = new grn_flow();
   f->e       = e;
+  f->device  = e->device;
+  e->flows.push_back(f);
   f->layers  = p->layers;
   f->seed    = p->seed;
   f->mix     = p->mix_uniform;
@@ -1125,13 +1214,21 @@ grn_status grn_flow_create(grn_engine *e, const grn_flow_params *p, grn_flow **o
 
 grn_status grn_flow_destroy(grn_flow *f) {
   if (!f) return GRN_OK;
-  if (f->e) cudaSetDevice(f->e->device);
+  cudaSetDevice(f->device);
+  if (f->e) {
+    auto &v = f->e->flows;
+    v.erase(std::remove(v.begin(), v.end(), f), v.end());
+    cudaStreamSynchronize(f->e->stream);
+  }
   for (DevBuf *b : {&f->d_theta, &f->d_m, &f->d_v, &f->d_grad, &f->d_w2p, &f->d_w3p, &f->d_w2c,
                     &f->d_w3c, &f->d_err, &f->d_loss,
                     &f->d_x, &f->d_z, &f->d_lq, &f->d_coef, &f->d_xs, &f->d_tu, &f->d_tlq,
                     &f->d_tcoef, &f->d_fu, &f->d_flq})
     b->release();
-  if (f->e && f->e->last_fu) f->e->last_fu = nullptr, f->e->have_last = false;
+  if (f->e && f->e->last_fu) {
+    f->e->last_fu   = nullptr;
+    f->e->have_last = false;
+  }
   delete f;
   return GRN_OK;
 }
@@ -1273,14 +1370,6 @@ static grn_status flow_points(grn_flow *f, bool from_flow, uint32_t stream_id, i
                                     nullptr, n, n - nu, key, stream_id, nu, u + nu, n, lq + nu,
                                     nullptr, f->d_err.as<int>(), e->stream));
   if (f->mix > 0.0) GRN_CUDA(grn::launch_flow_mix(lq, n, f->mix, e->stream));
-  return GRN_OK;
-}
-
-static grn_status set_ncall(grn_engine *e, int64_t n) {
-  if (n != e->ncall) {
-    e->ncall = n;
-    return vegas_alloc_calls(e, n);
-  }
   return GRN_OK;
 }
 

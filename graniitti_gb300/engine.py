@@ -126,6 +126,14 @@ class Engine:
         _abi.check(self.lib.grn_vegas_integrate(self.h, ctypes.byref(vp), ctypes.byref(r)))
         return r
 
+    def flat_integrate(self, ncall=1 << 20, precision=0.05, min_events=1000000, prec=FP64,
+                       seed=1):
+        fp = _abi.FlatParams(ncall=ncall, precision=precision, min_events=min_events, prec=prec,
+                             seed=seed)
+        r = _abi.VegasResult()
+        _abi.check(self.lib.grn_flat_integrate(self.h, ctypes.byref(fp), ctypes.byref(r)))
+        return r
+
     def vegas_clear(self):
         _abi.check(self.lib.grn_vegas_clear(self.h))
 
@@ -270,7 +278,20 @@ class Flow:
 
 
 class Graniitti:
-    """MGraniitti-style driver (src/MGraniitti.cc) over the GPU engine."""
+    """MGraniitti-style driver (src/MGraniitti.cc) over the GPU engine.
+
+    INTEGRATOR (GENERALPARAM, as in the generator's cards):
+      "VEGAS"  SampleVegas: burn-in + integration iterations (grn_vegas_integrate)
+      "FLAT"   SampleFlat: uniform points until FLAT::PRECISION and MIN_EVENTS
+      "NEURO"  the learned proposal: VEGAS adapts the grid, the coupling-layer flow is
+               trained in front of it, then integration and generation run through the
+               flow (the reference's NEURO prototype, SampleNeuro, samples through its own
+               small network). Optional card block INTEGRALPARAM.FLOW (an extension of the
+               card format): LAYERS, NTRAIN, BATCH, EPOCHS, ROUNDS, LR, MIX.
+    """
+
+    FLOW_DEFAULTS = {"LAYERS": 6, "NTRAIN": 1 << 22, "BATCH": 16384, "EPOCHS": 4, "ROUNDS": 1,
+                     "LR": 1e-3, "MIX": 0.05}
 
     def __init__(self, device=0):
         self.device = device
@@ -279,12 +300,29 @@ class Graniitti:
         self.vp = None
         self.result = None
         self.prec = FP64
+        self.integrator = "VEGAS"
+        self.flow = None
+        self.train_result = None
 
     def ReadInput(self, inputfile, cmd_PROCESS=None):
         self.card = _card.read_card(inputfile)
         self.params = _card.build_params(self.card, cmd_PROCESS)
         self.vp = _card.vegas_params(self.card, prec=self.prec)
+        self.integrator = self.card.get("GENERALPARAM", {}).get("INTEGRATOR", "VEGAS")
+        if self.integrator not in ("VEGAS", "FLAT", "NEURO"):
+            raise ValueError("MGraniitti::CallIntegrator: Unknown INTEGRATOR = %s "
+                             "(use VEGAS, FLAT, NEURO)" % self.integrator)
+        ip = self.card.get("INTEGRALPARAM", {})
+        fl = ip.get("FLAT", {})
+        self.flat = {"PRECISION": float(fl.get("PRECISION", 0.05)),
+                     "MIN_EVENTS": int(fl.get("MIN_EVENTS", 1000000))}
+        self.flowp = dict(self.FLOW_DEFAULTS, **ip.get("FLOW", {}))
         self.engine = Engine(self.params, self.device)
+
+    def SetIntegrator(self, name):
+        if name not in ("VEGAS", "FLAT", "NEURO"):
+            raise ValueError("unknown integrator %s" % name)
+        self.integrator = name
 
     def SetVegasParam(self, **kw):
         for k, v in kw.items():
@@ -298,21 +336,43 @@ class Graniitti:
     def Initialize(self):
         if self.params.screening:
             self.engine.eikonal_build()
+        if self.integrator == "FLAT":
+            self.result = self.engine.flat_integrate(
+                ncall=int(self.vp.ncall), precision=self.flat["PRECISION"],
+                min_events=self.flat["MIN_EVENTS"], prec=self.vp.prec, seed=self.vp.seed)
+            return self.result
         self.result = self.engine.vegas_integrate(self.vp)
+        if self.integrator == "NEURO":
+            fp = self.flowp
+            ntrain = int(fp["NTRAIN"]) // int(fp["BATCH"]) * int(fp["BATCH"])
+            self.flow = Flow(self.engine, layers=int(fp["LAYERS"]), seed=int(self.vp.seed),
+                             mix_uniform=float(fp["MIX"]))
+            self.train_result = self.flow.train(
+                n_train=ntrain, batch=int(fp["BATCH"]), epochs=int(fp["EPOCHS"]),
+                rounds=int(fp["ROUNDS"]), lr=float(fp["LR"]), prec=self.vp.prec)
+            self.result = self.flow.integrate(self.vp)
         return self.result
 
     def GetXS(self):
         return self.result.sigma, self.result.sigma_err
 
+    def GetMaxweight(self):
+        return self.engine.get_maxweight()
+
     def Generate(self, nevents, seed=11, max_iter=1000):
-        """Unweighted events: generation-mode VEGAS passes (frozen grid) with
-        hit-or-miss against the integration's max weight (MGraniitti.cc:1131-1134,
-        1651-1664). Returns (points, n_trials, n_overflow)."""
-        fmax = self.result.maxf
+        """Unweighted events: generation-mode passes (frozen grid, through the flow for
+        NEURO) with hit-or-miss against the integration's max weight
+        (MGraniitti.cc:1131-1134, 1651-1664). Returns (points, n_trials, n_overflow)."""
+        if self.integrator == "FLAT":
+            raise NotImplementedError("generation from FLAT integration is not provided")
+        fmax = self.engine.get_maxweight()
         pts, trials, ovf = [], 0, 0
         it = 0
         while sum(len(p) for p in pts) < nevents and it < max_iter:
-            self.engine.vegas_iteration(mode=2, refine=False, iter_id=0x40000000 + it)
+            if self.integrator == "NEURO":
+                self.flow.iteration(mode=2, iter_id=0x40000000 + it)
+            else:
+                self.engine.vegas_iteration(mode=2, refine=False, iter_id=0x40000000 + it)
             cap = int(self.vp.ncall)
             na, no, idx = self.engine.unweight(fmax, seed=seed + it, cap=cap)
             need = nevents - sum(len(p) for p in pts)

@@ -270,6 +270,21 @@ grn_status grn_vegas_iteration(grn_engine *e, int32_t mode, int32_t refine, uint
  * iterations until PRECISION and CHI2MAX are met (chi2 > 50 restarts with 10x
  * calls). */
 grn_status grn_vegas_integrate(grn_engine *e, const grn_vegas_params *vp, grn_vegas_result *out);
+/* FLAT integrator (INTEGRATOR "FLAT": MGraniitti::SampleFlat, src/MGraniitti.cc:1446-1524):
+ * uniform points, sigma = sum W / N, sigma_err = sqrt((sum W^2 / N - sigma^2) / N)
+ * (Stats::CalculateCrossSection, include/Graniitti/MGraniitti.h:59-66), passes of ncall
+ * points until sigma_err / sigma < precision and N > min_events (FLATPARAM). The maximum
+ * weight (grn_get_maxweight) is max W. The last pass stays on the device for
+ * grn_unweight / grn_vegas_points. */
+typedef struct grn_flat_params {
+  int64_t  ncall;      /* points per pass */
+  double   precision;  /* FLAT::PRECISION */
+  int64_t  min_events; /* FLAT::MIN_EVENTS */
+  int32_t  prec;       /* GRN_PREC_* */
+  int32_t  _pad;
+  uint64_t seed;       /* Philox key */
+} grn_flat_params;
+grn_status grn_flat_integrate(grn_engine *e, const grn_flat_params *fp, grn_vegas_result *out);
 /* Grid access: xmat as bins x dim doubles, bin-major (VEGASData::xmat). Host. */
 grn_status grn_vegas_get_grid(grn_engine *e, double *xmat);
 grn_status grn_vegas_set_grid(grn_engine *e, const double *xmat);

@@ -211,3 +211,12 @@ def test_flow_rejects_bad_parameters(gpu, params):
     with pytest.raises(_abi.GrnError):   # grid not initialised
         f.train(n_train=1 << 16, batch=1 << 14)
     e.close()
+    # the flow outlives its engine: calls fail cleanly, destruction is safe
+    with pytest.raises(_abi.GrnError) as ex:
+        f.density(np.full((8, 4), 0.5, dtype=np.float32))
+    assert ex.value.status == _abi.GRN_ERR_STATE
+    f.close()
+    # and leaves no CUDA error behind for the next engine
+    e2 = g.Engine(params, 0)
+    w, _ = e2.event_weights(np.full((4, 8), 0.5))
+    e2.close()
