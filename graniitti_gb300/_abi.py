@@ -102,6 +102,11 @@ class FlatParams(ctypes.Structure):
                 ("prec", c_int32), ("_pad", c_int32), ("seed", c_uint64)]
 
 
+GRN_FORMAT_HEPMC3 = 0
+GRN_FORMAT_HEPMC2 = 1
+GRN_FORMAT_HEPEVT = 2
+FORMATS = {"hepmc3": GRN_FORMAT_HEPMC3, "hepmc2": GRN_FORMAT_HEPMC2, "hepevt": GRN_FORMAT_HEPEVT}
+
 GRN_FLOW_LOSS_KL = 0
 GRN_FLOW_LOSS_VARIANCE = 1
 
@@ -147,6 +152,14 @@ SIGNATURES = {
     "grn_vegas_iteration": (c_int32, [c_void_p, c_int32, c_int32, c_uint32, c_void_p]),
     "grn_vegas_integrate": (c_int32, [c_void_p, c_void_p, c_void_p]),
     "grn_flat_integrate": (c_int32, [c_void_p, c_void_p, c_void_p]),
+    "grn_engine_params": (c_void_p, [c_void_p]),
+    "grn_writer_open": (c_int32, [ctypes.c_char_p, c_int32, ctypes.c_char_p, ctypes.c_char_p,
+                                  c_void_p]),
+    "grn_writer_close": (c_int32, [c_void_p]),
+    "grn_write_events": (c_int32, [c_void_p, c_void_p, c_void_p, c_int64, c_void_p, c_double,
+                                   c_double, c_double, c_void_p]),
+    "grn_write_records": (c_int32, [c_void_p, c_void_p, c_int64, c_void_p, c_void_p, c_double,
+                                    c_double, c_double, c_double]),
     "grn_vegas_get_grid": (c_int32, [c_void_p, c_void_p]),
     "grn_vegas_set_grid": (c_int32, [c_void_p, c_void_p]),
     "grn_vegas_clear": (c_int32, [c_void_p]),

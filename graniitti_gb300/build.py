@@ -13,7 +13,7 @@ REPO = os.path.dirname(HERE)
 CSRC = os.path.join(HERE, "csrc")
 OUT = os.path.join(HERE, "_build")
 LIB = os.path.join(OUT, "libgrn.so")
-SOURCES = ["grn_kernels.cu", "grn_api.cu", "grn_noalloc.cu", "grn_flow.cu"]
+SOURCES = ["grn_kernels.cu", "grn_api.cu", "grn_noalloc.cu", "grn_flow.cu", "grn_record.cc"]
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 
 
@@ -38,7 +38,7 @@ def build_library(verbose=False, extra=(), force=False):
         t = os.path.getmtime(LIB)
         if all(os.path.getmtime(d) <= t for d in deps):
             return LIB
-    objs = [os.path.join(OUT, os.path.basename(s).replace(".cu", ".o")) for s in srcs]
+    objs = [os.path.join(OUT, os.path.splitext(os.path.basename(s))[0] + ".o") for s in srcs]
 
     def compile_one(pair):
         src, obj = pair

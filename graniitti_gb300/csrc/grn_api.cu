@@ -406,6 +406,8 @@ grn_status grn_destroy(grn_engine *e) {
   return GRN_OK;
 }
 
+const grn_process_params *grn_engine_params(const grn_engine *e) { return e ? &e->P : nullptr; }
+
 void   *grn_engine_stream(grn_engine *e) { return e ? static_cast<void *>(e->stream) : nullptr; }
 int32_t grn_dim(const grn_engine *e) { return e ? e->dim : 0; }
 

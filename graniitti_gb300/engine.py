@@ -359,12 +359,20 @@ class Graniitti:
     def GetMaxweight(self):
         return self.engine.get_maxweight()
 
-    def Generate(self, nevents, seed=11, max_iter=1000):
+    def Generate(self, nevents, seed=11, max_iter=1000, output=None, fmt=None):
         """Unweighted events: generation-mode passes (frozen grid, through the flow for
         NEURO) with hit-or-miss against the integration's max weight
-        (MGraniitti.cc:1131-1134, 1651-1664). Returns (points, n_trials, n_overflow)."""
+        (MGraniitti.cc:1131-1134, 1651-1664). Returns (points, n_trials, n_overflow).
+        With `output` (a path) the events are also written as event records in FORMAT
+        (`fmt`, default the card's GENERALPARAM FORMAT), weight 1, cross section in pb."""
         if self.integrator == "FLAT":
             raise NotImplementedError("generation from FLAT integration is not provided")
+        writer = None
+        if output is not None:
+            from .record import EventWriter
+            fmt = fmt or self.card.get("GENERALPARAM", {}).get("FORMAT", "hepmc3")
+            writer = EventWriter(output, fmt, tool="GRANIITTI (%s)" %
+                                 self.card.get("GENERALPARAM", {}).get("MODELPARAM", "TUNE0"))
         fmax = self.engine.get_maxweight()
         pts, trials, ovf = [], 0, 0
         it = 0
@@ -381,7 +389,20 @@ class Graniitti:
             trials += int(self.vp.ncall) if need >= na else int(idx[-1]) + 1
             ovf += no
             it += 1
-        return np.concatenate(pts) if pts else np.zeros((0, 8)), trials, ovf
+        out = np.concatenate(pts) if pts else np.zeros((0, 8))
+        if writer is not None:
+            pdg = self.card_pdg()
+            writer.write_points(self.engine, out, pdg, self.result.sigma * 1e12,
+                                self.result.sigma_err * 1e12)
+            writer.close()
+        return out, trials, ovf
+
+    def card_pdg(self):
+        """PDG codes of the beam and the two central final states of the process."""
+        from .modeldata import PARTICLES
+        proc = self.card["PROCESSPARAM"]["PROCESS"]
+        finals = _card.parse_process(proc)[3]
+        return [PARTICLES["p+"][0], PARTICLES[finals[0]][0], PARTICLES[finals[1]][0]]
 
 
 def kernel_timing(engine, reset=True):

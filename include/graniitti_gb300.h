@@ -155,6 +155,8 @@ grn_status grn_destroy(grn_engine *e);
 void *grn_engine_stream(grn_engine *e);
 /* Phase-space dimension (MProcess::GetdLIPSDim, include/Graniitti/MProcess.h:160). */
 int32_t grn_dim(const grn_engine *e);
+/* The parameters the engine was created with (owned by the engine). */
+const grn_process_params *grn_engine_params(const grn_engine *e);
 /* Message of the last failing call on this thread (never NULL). */
 const char *grn_last_error(void);
 /* Library version string. */
@@ -401,6 +403,40 @@ grn_status grn_flow_iteration(grn_engine *e, grn_flow *f, int32_t mode, uint32_t
  * sigma_err / sigma <= vp->precision (at least max(2, vp->iter) passes). */
 grn_status grn_flow_integrate(grn_engine *e, grn_flow *f, const grn_vegas_params *vp,
                               grn_vegas_result *out);
+
+/* ------------------------------------------------------------------------ */
+/* Event records: the output path of MGraniitti::SaveEvent                   */
+/* ------------------------------------------------------------------------ */
+/* Writes unweighted (or weighted) events in the generator's output formats
+ * (FORMAT "hepmc3", "hepmc2", "hepevt"; src/MGraniitti.cc:180-211, 1665-1715) with the
+ * event-record layout of MProcess::CommonRecord (src/MProcess.cc:1588-1680): beams
+ * (status 4), forward protons (1), two generic propagators (PDG 99, status 81), the
+ * central system (PDG 90, status 81) and its two daughters (1); four vertices; the
+ * cross section in pb with every event (GenCrossSection) and the event weight.
+ * The text is produced by the library itself (HepMC3's ASCII v3 / HepMC2 IO_GenEvent /
+ * HEPEVT layouts), so no HepMC installation is needed. */
+typedef struct grn_writer grn_writer;
+enum { GRN_FORMAT_HEPMC3 = 0, GRN_FORMAT_HEPMC2 = 1, GRN_FORMAT_HEPEVT = 2 };
+/* tool / card: the generator name and the steering-card path recorded in the run
+ * information (may be NULL). */
+grn_status grn_writer_open(const char *path, int32_t format, const char *tool, const char *card,
+                           grn_writer **out);
+grn_status grn_writer_close(grn_writer *w);
+/* Events from hypercube points u (n x dim, host, point-major: e.g. from
+ * grn_vegas_points): kinematics by grn_event_kinematics, PDG codes of the beams and
+ * the two central particles in pdg[3], weight written with every event (1 for
+ * unweighted events), cross section and error in pb. Event numbers continue from the
+ * writer's count. Points whose kinematics fail are skipped (*written says how many
+ * were written). */
+grn_status grn_write_events(grn_writer *w, grn_engine *e, const double *u, int64_t n,
+                            const int32_t pdg[3], double weight, double sigma_pb,
+                            double sigma_err_pb, int64_t *written);
+/* The same from 4-vectors already at hand: p4 = n x 16 doubles, (px, py, pz, E) of the
+ * two forward legs and the two central particles (the layout of grn_event_kinematics);
+ * mass = beam and the two central masses; symmetric beams of total energy sqrt_s. */
+grn_status grn_write_records(grn_writer *w, const double *p4, int64_t n, const int32_t pdg[3],
+                             const double mass[3], double sqrt_s, double weight, double sigma_pb,
+                             double sigma_err_pb);
 
 /* ------------------------------------------------------------------------ */
 /* Measurement helpers (no counterpart in the reference)                      */

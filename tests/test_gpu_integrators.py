@@ -70,3 +70,30 @@ def test_unknown_integrator_rejected(tmp_path):
     gen = g.Graniitti()
     with pytest.raises(ValueError):
         gen.ReadInput(p)
+
+
+def test_generated_events_written_as_records(gpu, tmp_path):
+    """Generation with an output file: records of the accepted points, momentum conserved,
+    central pions inside the fiducial cuts of the card, cross section in pb."""
+    import graniitti_gb300 as g
+    from graniitti_gb300.record import read_hepmc3
+    gen = g.Graniitti()
+    gen.ReadInput(_card(tmp_path, "VEGAS"))
+    gen.Initialize()
+    out = str(tmp_path / "events.hepmc3")
+    pts, trials, ovf = gen.Generate(300, output=out)
+    ev = read_hepmc3(out)
+    assert len(ev) == 300
+    s, e = gen.GetXS()
+    for k in range(300):
+        P = ev[k]["particles"]
+        assert ev[k]["xs"][0] == pytest.approx(s * 1e12, rel=1e-15)
+        p = {i: P[i][2] for i in P}
+        tot = p[2] + p[5] + p[8] + p[9]
+        assert np.allclose(tot, p[1] + p[4], atol=1e-8 * 13000)
+        for i in (8, 9):
+            px, py, pz, E = p[i]
+            pt = np.hypot(px, py)
+            eta = np.arcsinh(pz / pt)
+            assert abs(eta) < 0.9 and pt > 0.1
+        assert sorted([P[8][1], P[9][1]]) == [-211, 211]
