@@ -36,11 +36,15 @@ inline CF sqrt(CF a) { g_cnt.sqrt++; return CF(std::sqrt(a.v)); }
 inline CF fabs(CF a) { return CF(std::fabs(a.v)); }
 inline CF fast_log(CF a) { g_cnt.log++; return CF(std::log(a.v)); }
 inline CF fast_exp(CF a) { g_cnt.exp++; return CF(std::exp(a.v)); }
+inline CF fast_log2(CF a) { g_cnt.log++; return CF(std::log2(a.v)); }
+inline CF fast_exp2(CF a) { g_cnt.exp++; return CF(std::exp2(a.v)); }
+inline CF fast_div(CF a, CF b) { g_cnt.div++; return CF(a.v / b.v); }
 inline void sincos_pi(CF x, CF &s, CF &c) {
   g_cnt.sincos++;
   s = CF(std::sin(grn::kPi * x.v));
   c = CF(std::cos(grn::kPi * x.v));
 }
+inline void fast_sincos_pi(CF x, CF &s, CF &c) { sincos_pi(x, s, c); }
 
 int main() {
   grn_process_params P;

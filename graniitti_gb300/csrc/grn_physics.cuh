@@ -561,6 +561,42 @@ GRN_HD float fast_exp(float x) {
   return std::exp(x);
 #endif
 }
+// Base-2 forms (one MUFU instruction each on the device): the fast loop keeps its
+// logarithms and exponents in log2 units, so no ln 2 scalings are executed.
+GRN_HD float fast_log2(float x) {
+#ifdef __CUDA_ARCH__
+  return __log2f(x);
+#else
+  return std::log2(x);
+#endif
+}
+GRN_HD float fast_exp2(float x) {
+#ifdef __CUDA_ARCH__
+  return exp2f(x);
+#else
+  return std::exp2(x);
+#endif
+}
+// a / b through the reciprocal unit (about 2 ulp); b in the normal range.
+GRN_HD float fast_div(float a, float b) {
+#ifdef __CUDA_ARCH__
+  return __fdividef(a, b);
+#else
+  return a / b;
+#endif
+}
+// sin(pi x), cos(pi x) for the loop phase: x reduced by its period 2 to [-1, 1], then
+// the hardware sine / cosine of pi r (absolute error ~5e-7, |pi r| <= pi).
+GRN_HD void fast_sincos_pi(float x, float &s, float &c) {
+#ifdef __CUDA_ARCH__
+  const float r = fmaf(-2.f, rintf(0.5f * x), x);
+  __sincosf(float(kPi) * r, &s, &c);
+#else
+  s = std::sin(float(kPi) * x);
+  c = std::cos(float(kPi) * x);
+#endif
+}
+constexpr double kLog2e = 1.4426950408889634074;
 
 // Per-event fields of the fast loop (stored between the two kernel stages).
 #define GRN_LOOP_EVENT_FIELDS(X)                                                              \
@@ -583,13 +619,13 @@ struct LoopEventF {
   T mT1s0, mT2s0, T1n0, T2n0;  // mT^2 and pT^2 + x^2 mp^2 at k = 0
   T t10, t20;
   T is13, is14, is23, is24;  // 1/s at k = 0
-  T L13, L14, L23, L24;      // ln(s/s0) at k = 0
+  T L13, L14, L23, L24;      // log2(s/s0) at k = 0
   T a10, a20, ap;            // trajectory at t1, t2 (k = 0) and slope
   T dpa0, dma0, dpb0, dmb0;  // light-cone factors of t_hat, u_hat at k = 0
   T c3x, c3y, c4x, c4y;      // p1T + p3T, p1T + p4T
   T ifc1, ifc2;
   T ff_b, ff_a2, ff_ab;
-  T fa0, fb0;                // 2 ln ff(t_hat), 2 ln ff(u_hat) at k = 0 (exponential kinds)
+  T fa0, fb0;                // 2 log2 ff(t_hat), 2 log2 ff(u_hat) at k = 0 (exponential kinds)
   T rho_t, rho_u;            // exp(E_t0 - Emax), exp(E_u0 - Emax)
   T pre_re, pre_im;          // couplings x ReggeEta^2 x tree-level phase [x b_POW^2]
   double escale;             // exp(Emax), applied in FP64 after the loop sum
@@ -648,7 +684,8 @@ GRN_HD void make_loop_event_fast(const grn_process_params &P, const Consts &K, c
   e.is13 = T(1.0 / s13); e.is14 = T(1.0 / s14); e.is23 = T(1.0 / s23); e.is24 = T(1.0 / s24);
   const double l0 = log(P.regge.s0);
   const double L13 = log(s13) - l0, L14 = log(s14) - l0, L23 = log(s23) - l0, L24 = log(s24) - l0;
-  e.L13 = T(L13); e.L14 = T(L14); e.L23 = T(L23); e.L24 = T(L24);
+  e.L13 = T(L13 * kLog2e); e.L14 = T(L14 * kLog2e); e.L23 = T(L23 * kLog2e);
+  e.L24 = T(L24 * kLog2e);
   const int k = K.active[0] ? 0 : (K.active[1] ? 1 : 2);
   const double a0 = P.regge.a0[k], ap = P.regge.ap[k];
   e.a10 = T(a0 + ap * t1); e.a20 = T(a0 + ap * t2);
@@ -676,7 +713,7 @@ GRN_HD void make_loop_event_fast(const grn_process_params &P, const Consts &K, c
     fb = 2.0 * (P.regge.a_OREAR * P.regge.b_OREAR -
                 P.regge.b_OREAR * sqrt(fabs(tb) + P.regge.a_OREAR * P.regge.a_OREAR));
   }
-  e.fa0 = T(fa); e.fb0 = T(fb);
+  e.fa0 = T(fa * kLog2e); e.fb0 = T(fb * kLog2e);
   Et += fa;
   Eu += fb;
   const double Em = Et > Eu ? Et : Eu;
@@ -728,10 +765,11 @@ GRN_HD bool loop_point_amp_fast(const LoopEventF<T> &e, T kx, T ky, T k2, cx<T> 
   const T ds14 = dp1p * e.p4m + dp1m * e.p4p + T(2) * k4;
   const T ds23 = dp2p * e.p3m + dp2m * e.p3p - T(2) * k3;
   const T ds24 = dp2p * e.p4m + dp2m * e.p4p - T(2) * k4;
-  const T d13 = fast_log(T(1) + ds13 * e.is13);
-  const T d14 = fast_log(T(1) + ds14 * e.is14);
-  const T d23 = fast_log(T(1) + ds23 * e.is23);
-  const T d24 = fast_log(T(1) + ds24 * e.is24);
+  // log2 of the s ratios; exponents below are in log2 units
+  const T d13 = fast_log2(T(1) + ds13 * e.is13);
+  const T d14 = fast_log2(T(1) + ds14 * e.is14);
+  const T d23 = fast_log2(T(1) + ds23 * e.is23);
+  const T d24 = fast_log2(T(1) + ds24 * e.is24);
   const T dt1 = -(dm1 + dx1 * (T(2) * e.x10 + dx1) * e.mp2) * r1 - e.T1n0 * dr1;
   const T dt2 = -(dm2 + dx2 * (T(2) * e.x20 + dx2) * e.mp2) * r2 - e.T2n0 * dr2;
   const T t1 = e.t10 + dt1, t2 = e.t20 + dt2;
@@ -747,26 +785,26 @@ GRN_HD bool loop_point_amp_fast(const LoopEventF<T> &e, T kx, T ky, T k2, cx<T> 
   T num, den;
   if (e.ffmode == 2) {
     const T Da = e.ff_b - ta, Db = e.ff_b - tb;
-    const T Xt = e.rho_t * fast_exp(dEt), Xu = e.rho_u * fast_exp(dEu);
+    const T Xt = e.rho_t * fast_exp2(dEt), Xu = e.rho_u * fast_exp2(dEu);
     num = Xt * (Db * Db) * tb + Xu * (Da * Da) * ta;
     den = Pd * (Da * Da) * (Db * Db) * ta * tb;
   } else {
-    T fa, fb;
+    T fa, fb;  // 2 log2 of the off-shell form factors
     if (e.ffmode == 0) {
-      fa = T(-2) * e.ff_b * fabs(ta);
-      fb = T(-2) * e.ff_b * fabs(tb);
+      fa = T(-2.0 * kLog2e) * e.ff_b * fabs(ta);
+      fb = T(-2.0 * kLog2e) * e.ff_b * fabs(tb);
     } else {
-      fa = T(2) * (e.ff_ab - e.ff_b * sqrt(fabs(ta) + e.ff_a2));
-      fb = T(2) * (e.ff_ab - e.ff_b * sqrt(fabs(tb) + e.ff_a2));
+      fa = T(2.0 * kLog2e) * (e.ff_ab - e.ff_b * sqrt(fabs(ta) + e.ff_a2));
+      fb = T(2.0 * kLog2e) * (e.ff_ab - e.ff_b * sqrt(fabs(tb) + e.ff_a2));
     }
-    const T Xt = e.rho_t * fast_exp(dEt + (fa - e.fa0));
-    const T Xu = e.rho_u * fast_exp(dEu + (fb - e.fb0));
+    const T Xt = e.rho_t * fast_exp2(dEt + (fa - e.fa0));
+    const T Xu = e.rho_u * fast_exp2(dEu + (fb - e.fb0));
     num = Xt * tb + Xu * ta;
     den = Pd * ta * tb;
   }
   T sn, cs;
-  sincos_pi(T(-0.5) * e.ap * (dt1 + dt2), sn, cs);
-  const T m = num / den;
+  fast_sincos_pi(T(-0.5) * e.ap * (dt1 + dt2), sn, cs);
+  const T m = fast_div(num, den);
   A = {(e.pre_re * cs - e.pre_im * sn) * m, (e.pre_re * sn + e.pre_im * cs) * m};
   return (e.x10 + dx1 < T(1)) && (e.x20 + dx2 < T(1));
 }
