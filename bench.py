@@ -257,6 +257,14 @@ def main():
     P = workload_params()
     eng = g.Engine(P, local)
     eng.eikonal_build(N_BT, N_KT2)
+    # the engine's autotuner picks the kt-loop kernel variant and grid (untimed set-up)
+    tune = eng.autotune(sample=1 << 18)
+    tuned = {"loop_events_per_thread": 1 + tune.best.loop_pair,
+             "loop_blocks": tune.best.vegas_blocks,
+             "candidates_ms": {"%d/thread x %d blocks" % (1 + tune.cand[k].loop_pair,
+                                                         tune.cand[k].vegas_blocks):
+                               round(tune.ms[k], 4) for k in range(tune.n_candidates)},
+             "sample_events": tune.sample_events}
     vp = _abi.VegasParams()
     vp.bins, vp.iter, vp.ncall, vp.lambda_ = 128, args.steps, args.points, 1.5
     vp.chi2max, vp.precision, vp.burnin_iter = 10.0, 1e-3, args.warmup
@@ -390,7 +398,7 @@ def main():
                          sample_kernel_ms=flow_s * 1e3, sample_tflops=flow_tflops,
                          sample_frac_of_measured_bf16=(flow_tflops / bf16_peak
                                                        if bf16_peak else None)),
-               plain_vegas_mixed=plain, plain_vegas_fp64=fp64,
+               plain_vegas_mixed=plain, plain_vegas_fp64=fp64, autotune=tuned,
                flow_over_plain_mixed=value / plain["value"] if plain["value"] else None,
                flow_over_plain_fp64=(value / fp64["value"]) if fp64 and fp64["value"] else None)
     line = {"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
@@ -408,7 +416,8 @@ def main():
                          "traffic": traffic,
                          "peak_source": "measured FP32 FMA-chain probe (MEASURED_PEAKS.json "
                                         "carries no FP32 figure)",
-                         "kernel": "k_vegas_loop_rec",
+                         "kernel": ("k_vegas_loop_rec2 (2 events per thread, packed FP32x2)"
+                                    if tune.best.loop_pair else "k_vegas_loop_rec"),
                          "flops_per_loop_point": cnt["flops"],
                          "sfu_per_loop_point": cnt["transcendentals"],
                          "kernel_ms": k_avg_s * 1e3},

@@ -102,6 +102,16 @@ class FlatParams(ctypes.Structure):
                 ("prec", c_int32), ("_pad", c_int32), ("seed", c_uint64)]
 
 
+class Tuning(ctypes.Structure):
+    _fields_ = [("loop_pair", c_int32), ("vegas_blocks", c_int32), ("weight_blocks", c_int32),
+                ("_pad", c_int32)]
+
+
+class TuneResult(ctypes.Structure):
+    _fields_ = [("best", Tuning), ("n_candidates", c_int32), ("_pad", c_int32),
+                ("ms", c_double * 8), ("cand", Tuning * 8), ("sample_events", c_int64)]
+
+
 GRN_FORMAT_HEPMC3 = 0
 GRN_FORMAT_HEPMC2 = 1
 GRN_FORMAT_HEPEVT = 2
@@ -153,6 +163,9 @@ SIGNATURES = {
     "grn_vegas_integrate": (c_int32, [c_void_p, c_void_p, c_void_p]),
     "grn_flat_integrate": (c_int32, [c_void_p, c_void_p, c_void_p]),
     "grn_engine_params": (c_void_p, [c_void_p]),
+    "grn_get_tuning": (c_int32, [c_void_p, c_void_p]),
+    "grn_set_tuning": (c_int32, [c_void_p, c_void_p]),
+    "grn_autotune": (c_int32, [c_void_p, c_int64, c_void_p]),
     "grn_writer_open": (c_int32, [ctypes.c_char_p, c_int32, ctypes.c_char_p, ctypes.c_char_p,
                                   c_void_p]),
     "grn_writer_close": (c_int32, [c_void_p]),

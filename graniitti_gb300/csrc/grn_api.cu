@@ -95,6 +95,7 @@ struct grn_engine {
   // staging for host arrays; screened work list of grn_event_weights
   DevBuf d_u, d_w, d_flags, d_aux, d_wlist, d_wcount;
   int    loop_blocks = 0;
+  int    loop_pair   = 0;  // record-mode loop: events per thread - 1 (set by grn_autotune)
 
   // VEGAS
   int         bins = 0;
@@ -138,6 +139,7 @@ struct grn_engine {
     a.n_phi_nodes  = n_phi_nodes;
     a.loop_norm_re = 0.0;
     a.loop_norm_im = loop_norm_im;
+    a.loop_pair    = loop_pair;
     return a;
   }
 };
@@ -1004,6 +1006,93 @@ grn_status grn_vegas_points(grn_engine *e, const int64_t *idx, int64_t n, double
                            e->stream));
   GRN_CUDA(cudaStreamSynchronize(e->stream));
   return GRN_OK;
+}
+
+// ---------------------------------------------------------------------------
+// Launch configuration of the kt-loop stage and its autotuner (no counterpart in the
+// reference).
+
+grn_status grn_get_tuning(grn_engine *e, grn_tuning *t) {
+  if (!e || !t) return fail(GRN_ERR_INVALID, "null argument");
+  if (e->loop_blocks == 0) e->loop_blocks = grn::loop_grid_blocks(e->device);
+  if (e->nblocks == 0) e->nblocks = grn::vegas_grid_blocks(e->device);
+  t->loop_pair     = e->loop_pair;
+  t->vegas_blocks  = e->nblocks;
+  t->weight_blocks = e->loop_blocks;
+  t->_pad          = 0;
+  return GRN_OK;
+}
+
+grn_status grn_set_tuning(grn_engine *e, const grn_tuning *t) {
+  if (!e || !t) return fail(GRN_ERR_INVALID, "null argument");
+  if ((t->loop_pair != 0 && t->loop_pair != 1) || t->vegas_blocks < 1 || t->weight_blocks < 1 ||
+      t->vegas_blocks > (1 << 20) || t->weight_blocks > (1 << 20))
+    return fail(GRN_ERR_INVALID, "bad tuning");
+  e->loop_pair   = t->loop_pair;
+  e->nblocks     = t->vegas_blocks;
+  e->loop_blocks = t->weight_blocks;
+  return GRN_OK;
+}
+
+grn_status grn_autotune(grn_engine *e, int64_t sample, grn_tune_result *out) {
+  if (!e || !out || sample < 1) return fail(GRN_ERR_INVALID, "bad argument");
+  std::memset(out, 0, sizeof(*out));
+  grn_status st = require_screening_ready(e);
+  if (st != GRN_OK) return st;
+  GRN_CUDA(cudaSetDevice(e->device));
+  st = grn_get_tuning(e, &out->best);
+  if (st != GRN_OK) return st;
+  KArgs a = e->args();
+  if (!grn::record_mode(a, GRN_PREC_MIXED)) return GRN_OK;  // nothing to choose
+  const int64_t n = sample;
+  GRN_CUDA(e->d_u.ensure(static_cast<size_t>(n) * e->dim * sizeof(double)));
+  GRN_CUDA(e->d_w.ensure(static_cast<size_t>(n) * sizeof(double)));
+  GRN_CUDA(e->d_flags.ensure(static_cast<size_t>(n)));
+  GRN_CUDA(e->d_wlist.ensure(static_cast<size_t>(n) * sizeof(int64_t)));
+  GRN_CUDA(e->d_wcount.ensure(sizeof(unsigned long long)));
+  GRN_CUDA(e->d_recf.ensure(static_cast<size_t>(n) * grn::kLoopEventFields * sizeof(float)));
+  GRN_CUDA(e->d_recd.ensure(static_cast<size_t>(n) * grn::kRecordDoubles * sizeof(double)));
+  GRN_CUDA(grn::launch_uniforms(0x7E57ull, 0, 0, n, e->dim, e->d_u.as<double>(), e->stream));
+  GRN_CUDA(grn::launch_weights_born_rec(a, e->d_u.as<double>(), n, e->dim, e->d_w.as<double>(),
+                                        e->d_flags.as<uint8_t>(), e->d_wlist.as<int64_t>(),
+                                        e->d_recf.as<float>(), e->d_recd.as<double>(),
+                                        e->d_wcount.as<unsigned long long>(), e->stream));
+  int sms = 0;
+  GRN_CUDA(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, e->device));
+  double best = 1e300;
+  int    nc   = 0;
+  for (int pair = 0; pair < 2; ++pair) {
+    for (int mult = 1; mult <= 4; mult *= 2) {
+      a.loop_pair      = pair;
+      const int blocks = sms * grn::loop_rec_blocks_per_sm(pair) * mult;
+      double    tmin   = 1e300;
+      for (int rep = 0; rep < 3; ++rep) {
+        GRN_CUDA(cudaEventRecord(e->ev0, e->stream));
+        GRN_CUDA(grn::launch_weights_loop_rec(a, n, e->d_w.as<double>(), e->d_flags.as<uint8_t>(),
+                                              e->d_wlist.as<int64_t>(), e->d_recf.as<float>(),
+                                              e->d_recd.as<double>(),
+                                              e->d_wcount.as<unsigned long long>(), blocks,
+                                              e->stream));
+        GRN_CUDA(cudaEventRecord(e->ev1, e->stream));
+        GRN_CUDA(cudaEventSynchronize(e->ev1));
+        float ms = 0.f;
+        GRN_CUDA(cudaEventElapsedTime(&ms, e->ev0, e->ev1));
+        if (rep > 0) tmin = std::min(tmin, static_cast<double>(ms));  // first launch warms up
+      }
+      out->cand[nc] = {pair, blocks, blocks, 0};
+      out->ms[nc]   = tmin;
+      if (tmin < best) {
+        best      = tmin;
+        out->best = out->cand[nc];
+      }
+      ++nc;
+    }
+  }
+  out->n_candidates = nc;
+  unsigned long long listed = 0;
+  GRN_CUDA(cudaMemcpy(&listed, e->d_wcount.p, sizeof(listed), cudaMemcpyDeviceToHost));
+  out->sample_events = static_cast<int64_t>(listed);
+  return grn_set_tuning(e, &out->best);
 }
 
 grn_status grn_kernel_timing(grn_engine *e, int32_t reset, double *total_ms, int64_t *launches) {

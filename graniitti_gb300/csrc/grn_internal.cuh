@@ -20,6 +20,7 @@ struct KArgs {
   int           n_kt_nodes;
   int           n_phi_nodes;
   double        loop_norm_re, loop_norm_im;  // i/(8 pi^2 s) * 9 h_phi h_kt / 64
+  int           loop_pair;  // record-mode loop: 0 one event per thread, 1 two (packed FP32x2)
 };
 
 constexpr int kMaxLoopNodes = 256;  // per axis
@@ -80,6 +81,16 @@ cudaError_t launch_vegas_loop(const KArgs &a, int prec, int bins, int dim, int64
 // Record mode: screened, FP32 loop, single active trajectory.
 bool        record_mode(const KArgs &a, int prec);
 constexpr int kRecordDoubles = 4;
+// The two stages of launch_event_weights_rec separately (the loop stage reads the list
+// length from *count and may be re-run on the same records).
+cudaError_t launch_weights_born_rec(const KArgs &a, const double *u, int64_t n, int dim, double *w,
+                                    uint8_t *flags, int64_t *list, float *rf, double *rd,
+                                    unsigned long long *count, cudaStream_t st);
+cudaError_t launch_weights_loop_rec(const KArgs &a, int64_t n, double *w, uint8_t *flags,
+                                    const int64_t *list, const float *rf, const double *rd,
+                                    const unsigned long long *count, int loop_blocks,
+                                    cudaStream_t st);
+int         loop_rec_blocks_per_sm(int pair);
 cudaError_t launch_event_weights_rec(const KArgs &a, const double *u, int64_t n, int dim,
                                      double *w, uint8_t *flags, int64_t *list, float *rf,
                                      double *rd, unsigned long long *count, int loop_blocks,

@@ -15,6 +15,7 @@
 #include <cstdint>
 
 #include "grn_internal.cuh"
+#include "grn_loop2.cuh"
 #include "grn_philox.cuh"
 
 // Resident blocks per SM requested for the FP32 loop kernels (register budget
@@ -208,6 +209,55 @@ __device__ __forceinline__ double record_weight(const KArgs &A, const LoopEventF
   return W;
 }
 
+// Loop nodes as duplicated pairs for the two-events-per-thread loop.
+__device__ void stage_nodes2(const KArgs &A, KtNode2 *skt, PhiNode2 *sphi) {
+  for (int j = threadIdx.x; j < A.n_kt_nodes; j += blockDim.x) {
+    const float kt = float(A.lc_kt[3 * j]);
+    skt[j] = {f2s(kt), f2s(kt * kt), f2s(float(A.lc_kt[3 * j + 1])),
+              f2s(float(A.lc_kt[3 * j + 2]))};
+  }
+  for (int i = threadIdx.x; i < A.n_phi_nodes; i += blockDim.x)
+    sphi[i] = {f2s(float(A.lc_phi[3 * i])), f2s(float(A.lc_phi[3 * i + 1])),
+               f2s(float(A.lc_phi[3 * i + 2]))};
+}
+
+// Screened weights of records ra and rb (rb may repeat ra; then only wa is meaningful).
+__device__ __forceinline__ void record_weights2(const KArgs &A, const LoopEventF<float> &consts,
+                                                const float *__restrict__ rf,
+                                                const double *__restrict__ rd, int64_t cap,
+                                                int64_t ra, int64_t rb, const KtNode2 *skt,
+                                                const PhiNode2 *sphi, double &wa, double &wb,
+                                                uint8_t &fa, uint8_t &fb) {
+  LoopEventF<float> ea = consts, eb = consts;
+  double            a0r[2], a0i[2], jac[2];
+  load_record(ea, a0r[0], a0i[0], jac[0], rf, rd, ra, cap);
+  load_record(eb, a0r[1], a0i[1], jac[1], rf, rd, rb, cap);
+  LoopEvent2 e;
+  make_loop_event2(ea, eb, e);
+  float2 sr, si;
+  loop_integral2(e, A.n_kt_nodes, A.n_phi_nodes, skt, sphi, sr, si);
+  const double esc[2] = {ea.escale, eb.escale};
+  const float  lr[2]  = {sr.x, sr.y}, li[2] = {si.x, si.y};
+  double       W[2];
+  uint8_t      F[2];
+  for (int k = 0; k < 2; ++k) {
+    const double xr = double(lr[k]) * esc[k], xi = double(li[k]) * esc[k];
+    const double re = a0r[k] + (A.loop_norm_re * xr - A.loop_norm_im * xi);
+    const double im = a0i[k] + (A.loop_norm_re * xi + A.loop_norm_im * xr);
+    W[k] = jac[k] * (re * re + im * im);
+    F[k] = GRN_FLAG_KINEMATICS_OK | GRN_FLAG_FIDCUTS_OK | GRN_FLAG_VETOCUTS_OK |
+           GRN_FLAG_AMPLITUDE_OK;
+    if (!isfinite(W[k])) {
+      W[k] = 0.0;
+      F[k] &= ~GRN_FLAG_AMPLITUDE_OK;
+    }
+  }
+  wa = W[0];
+  wb = W[1];
+  fa = F[0];
+  fb = F[1];
+}
+
 // Tree-level stage of one event: kinematics, cuts and, when the process is not
 // screened, the full weight. Returns true when the event still needs the kt-loop.
 __device__ __forceinline__ bool born_stage(const KArgs &A, const double *x, Born &b, double &W,
@@ -395,23 +445,72 @@ __global__ void __launch_bounds__(kWeightThreads, GRN_LOOP_MIN_BLOCKS)
   }
 }
 
+// Record mode, two events per thread on the packed FP32x2 loop.
+__global__ void __launch_bounds__(kWeightThreads, 2)
+    k_weights_loop_rec2(const KArgs A, const int64_t *__restrict__ list,
+                        const float *__restrict__ rf, const double *__restrict__ rd, int64_t cap,
+                        const unsigned long long *__restrict__ count, double *__restrict__ w,
+                        uint8_t *__restrict__ flags) {
+  __shared__ KtNode2  skt[kMaxLoopNodes];
+  __shared__ PhiNode2 sphi[kMaxLoopNodes];
+  stage_nodes2(A, skt, sphi);
+  __syncthreads();
+  LoopEventF<float> c;
+  make_loop_consts_fast<float>(A.P, A.K, c);
+  const int64_t cnt = static_cast<int64_t>(*count), npair = (cnt + 1) / 2;
+  for (int64_t q = static_cast<int64_t>(blockIdx.x) * blockDim.x + threadIdx.x; q < npair;
+       q += static_cast<int64_t>(gridDim.x) * blockDim.x) {
+    const int64_t ra = 2 * q, rb = (2 * q + 1 < cnt) ? 2 * q + 1 : 2 * q;
+    double  wa, wb;
+    uint8_t fa, fb;
+    record_weights2(A, c, rf, rd, cap, ra, rb, skt, sphi, wa, wb, fa, fb);
+    w[list[ra]] = wa;
+    if (flags) flags[list[ra]] = fa;
+    if (rb != ra) {
+      w[list[rb]] = wb;
+      if (flags) flags[list[rb]] = fb;
+    }
+  }
+}
+
 bool record_mode(const KArgs &a, int prec) {
   return a.P.screening && prec == GRN_PREC_MIXED && a.K.n_active == 1 &&
          a.P.process == GRN_PROC_REGGE_CON;
 }
 
-cudaError_t launch_event_weights_rec(const KArgs &a, const double *u, int64_t n, int dim,
-                                     double *w, uint8_t *flags, int64_t *list, float *rf,
-                                     double *rd, unsigned long long *count, int loop_blocks,
-                                     cudaStream_t st) {
+cudaError_t launch_weights_born_rec(const KArgs &a, const double *u, int64_t n, int dim, double *w,
+                                    uint8_t *flags, int64_t *list, float *rf, double *rd,
+                                    unsigned long long *count, cudaStream_t st) {
   if (n <= 0) return cudaSuccess;
   cudaError_t e = cudaMemsetAsync(count, 0, sizeof(unsigned long long), st);
   if (e != cudaSuccess) return e;
   const unsigned blocks = static_cast<unsigned>((n + kWeightThreads - 1) / kWeightThreads);
   k_weights_born_rec<<<blocks, kWeightThreads, 0, st>>>(a, u, n, dim, w, flags, list, rf, rd,
                                                          count);
-  k_weights_loop_rec<<<loop_blocks, kWeightThreads, 0, st>>>(a, list, rf, rd, n, count, w, flags);
   return cudaGetLastError();
+}
+
+cudaError_t launch_weights_loop_rec(const KArgs &a, int64_t n, double *w, uint8_t *flags,
+                                    const int64_t *list, const float *rf, const double *rd,
+                                    const unsigned long long *count, int loop_blocks,
+                                    cudaStream_t st) {
+  if (n <= 0) return cudaSuccess;
+  if (a.loop_pair)
+    k_weights_loop_rec2<<<loop_blocks, kWeightThreads, 0, st>>>(a, list, rf, rd, n, count, w,
+                                                                flags);
+  else
+    k_weights_loop_rec<<<loop_blocks, kWeightThreads, 0, st>>>(a, list, rf, rd, n, count, w,
+                                                               flags);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_event_weights_rec(const KArgs &a, const double *u, int64_t n, int dim,
+                                     double *w, uint8_t *flags, int64_t *list, float *rf,
+                                     double *rd, unsigned long long *count, int loop_blocks,
+                                     cudaStream_t st) {
+  cudaError_t e = launch_weights_born_rec(a, u, n, dim, w, flags, list, rf, rd, count, st);
+  if (e != cudaSuccess) return e;
+  return launch_weights_loop_rec(a, n, w, flags, list, rf, rd, count, loop_blocks, st);
 }
 
 // Kinematics only: pfinal[1..4] as (px, py, pz, E), and t1, t2.
@@ -874,6 +973,62 @@ __global__ void __launch_bounds__(kVegasThreads, GRN_LOOP_MIN_BLOCKS)
   flush_block(sf2, nh, f2mat, acc, cnt, maxf, maxW);
 }
 
+// Stage B, record mode, two events per thread on the packed FP32x2 loop.
+__global__ void __launch_bounds__(kVegasThreads, 2)
+    k_vegas_loop_rec2(const KArgs A, int bins, int dim, int track_max, double *__restrict__ f_out,
+                      double *__restrict__ f2mat, unsigned long long *__restrict__ acc,
+                      const int64_t *__restrict__ l_idx, const double *__restrict__ l_vw,
+                      const uint64_t *__restrict__ l_bins, const float *__restrict__ rf,
+                      const double *__restrict__ rd, int64_t cap) {
+  extern __shared__ double dsm[];
+  double *sf2 = dsm;
+  __shared__ KtNode2  skt[kMaxLoopNodes];
+  __shared__ PhiNode2 sphi[kMaxLoopNodes];
+  const int nh = bins * dim;
+  for (int i = threadIdx.x; i < nh; i += blockDim.x) sf2[i] = 0.0;
+  stage_nodes2(A, skt, sphi);
+  __syncthreads();
+  LoopEventF<float> c;
+  make_loop_consts_fast<float>(A.P, A.K, c);
+  unsigned long long cnt[VS_COUNT] = {};
+  double maxf = 0.0, maxW = 0.0;
+  const int64_t n = min(static_cast<int64_t>(acc[VS_COUNT]), cap), npair = (n + 1) / 2;
+  const int64_t stride = static_cast<int64_t>(gridDim.x) * blockDim.x;
+  for (int64_t q = static_cast<int64_t>(blockIdx.x) * blockDim.x + threadIdx.x; q < npair;
+       q += stride) {
+    const int64_t ra = 2 * q, rb = (2 * q + 1 < n) ? 2 * q + 1 : 2 * q;
+    double  W[2];
+    uint8_t F[2];
+    record_weights2(A, c, rf, rd, cap, ra, rb, skt, sphi, W[0], W[1], F[0], F[1]);
+    for (int k = 0; k < (rb != ra ? 2 : 1); ++k) {
+      const int64_t r = k ? rb : ra;
+      const double  f = W[k] * l_vw[r];
+      f_out[l_idx[r]] = f;
+      hist_add(sf2, dim, l_bins[r], f * f);
+      cnt[VS_AMP_OK] += (F[k] & GRN_FLAG_AMPLITUDE_OK) ? 1 : 0;
+      cnt[VS_NAN] += (F[k] & GRN_FLAG_AMPLITUDE_OK) ? 0 : 1;
+      if (track_max) {
+        maxf = fmax(maxf, f);
+        maxW = fmax(maxW, W[k]);
+      }
+    }
+  }
+  __syncwarp();
+  flush_block(sf2, nh, f2mat, acc, cnt, maxf, maxW);
+}
+
+// Resident blocks per SM of the record-mode loop kernels (one or two events per thread).
+int loop_rec_blocks_per_sm(int pair) {
+  int per = 0;
+  if (pair)
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, k_vegas_loop_rec2, kVegasThreads,
+                                                  kMaxBins * kMaxDim * sizeof(double));
+  else
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, k_vegas_loop_rec, kVegasThreads,
+                                                  kMaxBins * kMaxDim * sizeof(double));
+  return per < 1 ? 1 : per;
+}
+
 int vegas_grid_blocks(int device) {
   int sms = 0, per = 0;
   cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, device);
@@ -910,8 +1065,12 @@ cudaError_t launch_vegas_loop(const KArgs &a, int prec, int bins, int dim, int64
   if (!a.P.screening) return cudaSuccess;
   const int nh = bins * dim;
   if (rf) {
-    k_vegas_loop_rec<<<nblocks, kVegasThreads, nh * sizeof(double), st>>>(
-        a, bins, dim, track_max, f_out, f2mat, acc, l_idx, l_vw, l_bins, rf, rd, ncall);
+    if (a.loop_pair)
+      k_vegas_loop_rec2<<<nblocks, kVegasThreads, nh * sizeof(double), st>>>(
+          a, bins, dim, track_max, f_out, f2mat, acc, l_idx, l_vw, l_bins, rf, rd, ncall);
+    else
+      k_vegas_loop_rec<<<nblocks, kVegasThreads, nh * sizeof(double), st>>>(
+          a, bins, dim, track_max, f_out, f2mat, acc, l_idx, l_vw, l_bins, rf, rd, ncall);
     return cudaGetLastError();
   }
   if (prec == GRN_PREC_MIXED)

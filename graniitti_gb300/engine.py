@@ -137,6 +137,26 @@ class Engine:
     def vegas_clear(self):
         _abi.check(self.lib.grn_vegas_clear(self.h))
 
+    def tuning(self):
+        t = _abi.Tuning()
+        _abi.check(self.lib.grn_get_tuning(self.h, ctypes.byref(t)))
+        return t
+
+    def set_tuning(self, loop_pair=None, vegas_blocks=None, weight_blocks=None):
+        t = self.tuning()
+        if loop_pair is not None:
+            t.loop_pair = loop_pair
+        if vegas_blocks is not None:
+            t.vegas_blocks = vegas_blocks
+        if weight_blocks is not None:
+            t.weight_blocks = weight_blocks
+        _abi.check(self.lib.grn_set_tuning(self.h, ctypes.byref(t)))
+
+    def autotune(self, sample=1 << 18):
+        r = _abi.TuneResult()
+        _abi.check(self.lib.grn_autotune(self.h, sample, ctypes.byref(r)))
+        return r
+
     def get_maxweight(self):
         m = ctypes.c_double()
         _abi.check(self.lib.grn_get_maxweight(self.h, ctypes.byref(m)))
@@ -336,6 +356,8 @@ class Graniitti:
     def Initialize(self):
         if self.params.screening:
             self.engine.eikonal_build()
+            if self.vp.prec == MIXED:
+                self.engine.autotune(sample=1 << 16)
         if self.integrator == "FLAT":
             self.result = self.engine.flat_integrate(
                 ncall=int(self.vp.ncall), precision=self.flat["PRECISION"],

@@ -439,6 +439,34 @@ grn_status grn_write_records(grn_writer *w, const double *p4, int64_t n, const i
                              double sigma_err_pb);
 
 /* ------------------------------------------------------------------------ */
+/* Launch configuration and autotuner (no counterpart in the reference)       */
+/* ------------------------------------------------------------------------ */
+/* The kt-loop stage in record mode (screened, GRN_PREC_MIXED, one trajectory) has two
+ * kernels: one event per thread, or two events per thread on the packed FP32x2
+ * arithmetic (same results up to FP32 rounding), each with a grid size. */
+typedef struct grn_tuning {
+  int32_t loop_pair;     /* 0 one event per thread, 1 two events per thread */
+  int32_t vegas_blocks;  /* grid of the loop stage of VEGAS and flow passes */
+  int32_t weight_blocks; /* grid of the loop stage of grn_event_weights */
+  int32_t _pad;
+} grn_tuning;
+grn_status grn_get_tuning(grn_engine *e, grn_tuning *t);
+grn_status grn_set_tuning(grn_engine *e, const grn_tuning *t);
+
+typedef struct grn_tune_result {
+  grn_tuning best;           /* the configuration kept */
+  int32_t    n_candidates;
+  int32_t    _pad;
+  double     ms[8];          /* loop-stage time of each candidate (best of 2 after a warm-up) */
+  grn_tuning cand[8];
+  int64_t    sample_events;  /* listed (screened) events the candidates were timed on */
+} grn_tune_result;
+/* Times every candidate (events per thread x grid of 1, 2, 4 times the resident blocks)
+ * on the loop records of `sample` Philox points, CUDA events on the engine stream, and
+ * keeps the fastest. Needs the eikonal tables; a no-op outside record mode. */
+grn_status grn_autotune(grn_engine *e, int64_t sample, grn_tune_result *out);
+
+/* ------------------------------------------------------------------------ */
 /* Measurement helpers (no counterpart in the reference)                      */
 /* ------------------------------------------------------------------------ */
 /* Device time of the dominant kernel of a VEGAS pass (the kt-loop stage when

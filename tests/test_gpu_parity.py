@@ -269,3 +269,55 @@ def test_tensor_pomeron_screened_vs_reference(gpu):
     ok, rel = _mixed_ok(wm, w, wb)
     print("tensor mixed vs fp64: max rel %.3e" % rel.max())
     assert ok, rel.max()
+
+
+@pytest.mark.parametrize("n", [2048, 2047])
+def test_paired_loop_kernel_vs_fp64(gpu, params_screened, n):
+    """The kt-loop with two events per thread (packed FP32x2 arithmetic) against the FP64
+    loop, on the benchmark grid; odd n leaves the last thread with one event."""
+    import ctypes
+    import graniitti_gb300 as g
+    P = params_screened
+    P.loop.n_kt, P.loop.n_phi, P.loop.kt_max = 63, 33, 3.0
+    e = _engine(P)
+    e.eikonal_build(1024, 10000)
+    u = e.uniforms(seed=9, n=n)
+    w64, f64 = e.event_weights(u, prec=g.FP64)
+    e.set_tuning(loop_pair=0)
+    w1, f1 = e.event_weights(u, prec=g.MIXED)
+    e.set_tuning(loop_pair=1)
+    w2, f2 = e.event_weights(u, prec=g.MIXED)
+    assert np.array_equal(f2, f64) and np.array_equal(f1, f64)
+    Pb = type(P)()
+    ctypes.memmove(ctypes.byref(Pb), ctypes.byref(P), ctypes.sizeof(P))
+    Pb.screening = 0
+    wb, _ = _engine(Pb).event_weights(u, prec=g.FP64)
+    ok, r = _mixed_ok(w2, w64, wb)
+    nz = w1 > 0
+    d12 = np.abs(w2[nz] / w1[nz] - 1)
+    print("paired loop: max rel vs FP64 %.3e (median %.3e); vs one-event kernel max %.3e"
+          % (r.max(), np.median(r), d12.max()))
+    assert ok and d12.max() < 1e-5
+
+
+def test_autotune_keeps_fastest_and_results(gpu, params_screened):
+    import graniitti_gb300 as g
+    P = params_screened
+    P.loop.n_kt, P.loop.n_phi, P.loop.kt_max = 63, 33, 3.0
+    e = _engine(P)
+    e.eikonal_build(1024, 10000)
+    r = e.autotune(sample=1 << 16)
+    ms = list(r.ms)[:r.n_candidates]
+    print("autotune: %d candidates on %d events, ms %s, best pair=%d blocks=%d" %
+          (r.n_candidates, r.sample_events, np.round(ms, 3), r.best.loop_pair,
+           r.best.vegas_blocks))
+    assert r.n_candidates == 6 and r.sample_events > 0
+    k = int(np.argmin(ms))
+    assert (r.best.loop_pair, r.best.vegas_blocks) == (r.cand[k].loop_pair, r.cand[k].vegas_blocks)
+    t = e.tuning()
+    assert (t.loop_pair, t.vegas_blocks) == (r.best.loop_pair, r.best.vegas_blocks)
+    u = e.uniforms(seed=10, n=512)
+    wm, _ = e.event_weights(u, prec=g.MIXED)
+    w64, _ = e.event_weights(u, prec=g.FP64)
+    nz = w64 > 0
+    assert np.max(np.abs(wm[nz] / w64[nz] - 1)) < 1e-4
