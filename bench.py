@@ -11,10 +11,11 @@ kinematics, FP32 compensated kt-loop) -> f = W vw / q -> sums and max.
 
 Three samplers run on the same engine, in this order:
   plain VEGAS, mixed precision   burn-in, then timed passes (grid refined each pass)
-  flow proposal (the headline)   trained (untimed, reported: 4 epochs of batch 16384) on
-                                 2^22 weighted points of the adapted grid, then timed
-                                 passes, grid frozen; 5% of each pass is drawn uniformly
-                                 (defensive mixture)
+  flow proposal (the headline)   trained (untimed, reported) in 3 rounds of 3 epochs,
+                                 batch 16384, on 2^22 weighted points each (round 1 from
+                                 the adapted grid, later rounds from the flow itself), then
+                                 timed passes, grid frozen; 5% of each pass is drawn
+                                 uniformly (defensive mixture)
   plain VEGAS, FP64 throughout   two timed passes on the adapted grid
 value  = evaluations/s x eps_unw of the flow passes, eps_unw = <f>/max f
          (reference semantics: max f over the integration passes), points generated
@@ -225,7 +226,8 @@ def main():
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="engine", choices=["engine", "reference"])
     ap.add_argument("--points", type=int, default=1 << 22)
-    ap.add_argument("--flow-epochs", type=int, default=4)
+    ap.add_argument("--flow-epochs", type=int, default=3)
+    ap.add_argument("--flow-rounds", type=int, default=3)
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-fp64", action="store_true")
     args = ap.parse_args()
@@ -285,8 +287,8 @@ def main():
 
     # -- flow proposal in front of the adapted grid (training untimed, reported) -
     flow = g.Flow(eng, layers=FLOW_LAYERS, seed=1 + rank, mix_uniform=FLOW_MIX)
-    tr = flow.train(n_train=n, batch=FLOW_BATCH, epochs=args.flow_epochs, rounds=1, lr=FLOW_LR,
-                    prec=g.MIXED, seed_stream=1)
+    tr = flow.train(n_train=n, batch=FLOW_BATCH, epochs=args.flow_epochs,
+                    rounds=args.flow_rounds, lr=FLOW_LR, prec=g.MIXED, seed_stream=1)
     eng.vegas_clear()
     for it in range(2):
         flow.iteration(mode=0, iter_id=200 + it)
@@ -392,7 +394,7 @@ def main():
                        "BF16/FP32; 5%% uniform defensive component) in front of the adapted "
                        "VEGAS grid; FP64 kinematics, FP32 compensated kt-loop",
                flow=dict(fl, train_ms=tr.train_ms, train_steps=tr.steps, batch=FLOW_BATCH,
-                         mix_uniform=FLOW_MIX,
+                         epochs=args.flow_epochs, rounds=args.flow_rounds, mix_uniform=FLOW_MIX,
                          rel_var_vegas_points=tr.rel_var_start,
                          rel_var_flow_points=tr.rel_var_flow,
                          sample_kernel_ms=flow_s * 1e3, sample_tflops=flow_tflops,
