@@ -124,6 +124,7 @@ struct grn_engine {
   DevBuf      d_uw_counts, d_uw_misc, d_uw_idx;
   // flows created on this engine (detached when the engine is destroyed first)
   std::vector<grn_flow *> flows;
+  int                     in_batches = 0;  // batches holding this engine
   // timing of the sampling kernel
   cudaEvent_t ev0 = nullptr, ev1 = nullptr;
   double      sample_ms = 0.0;
@@ -390,6 +391,7 @@ grn_status grn_create(const grn_process_params *p, int32_t device, grn_engine **
 
 grn_status grn_destroy(grn_engine *e) {
   if (!e) return GRN_OK;
+  if (e->in_batches > 0) return fail(GRN_ERR_STATE, "engine belongs to a batch: destroy it first");
   cudaSetDevice(e->device);
   if (e->stream) cudaStreamSynchronize(e->stream);
   DevBuf *bufs[] = {&e->d_mbt,   &e->d_msa,    &e->d_eik_nodes, &e->d_xs,        &e->d_lc_kt,
@@ -1006,6 +1008,214 @@ grn_status grn_vegas_points(grn_engine *e, const int64_t *idx, int64_t n, double
                            e->stream));
   GRN_CUDA(cudaStreamSynchronize(e->stream));
   return GRN_OK;
+}
+
+// ---------------------------------------------------------------------------
+// Several processes in one pass: one fused launch per stage, replayed as a CUDA graph.
+
+}  // extern "C"
+
+struct grn_batch {
+  std::vector<grn_engine *> eng;
+  int                       device = 0;
+  cudaStream_t              stream = nullptr;
+  DevBuf                    d_procs, d_counter;
+  grn::BatchProc           *h_procs = nullptr;  // pinned: uploaded by the graph every pass
+  int                       born_blocks = 0, loop_blocks = 0;
+  cudaGraphExec_t           exec[2] = {nullptr, nullptr};  // without / with grid refinement
+  cudaEvent_t               ev0 = nullptr, ev1 = nullptr;
+  double                    last_ms = 0.0;
+  bool                      registered = false;  // counted in the engines' in_batches
+};
+
+namespace {
+
+grn_status batch_capture(grn_batch *b, int refine) {
+  const int np = static_cast<int>(b->eng.size());
+  GRN_CUDA(cudaStreamBeginCapture(b->stream, cudaStreamCaptureModeThreadLocal));
+  cudaError_t ce = cudaMemcpyAsync(b->d_procs.p, b->h_procs, np * sizeof(grn::BatchProc),
+                                   cudaMemcpyHostToDevice, b->stream);
+  for (int p = 0; p < np && ce == cudaSuccess; ++p) {
+    grn_engine *e  = b->eng[p];
+    const int   nh = e->bins * e->dim;
+    ce = cudaMemcpyAsync(e->d_xmat_prev.p, e->d_xmat.p, nh * sizeof(double),
+                         cudaMemcpyDeviceToDevice, b->stream);
+    if (ce == cudaSuccess) ce = cudaMemsetAsync(e->d_f2mat.p, 0, nh * sizeof(double), b->stream);
+    if (ce == cudaSuccess)
+      ce = cudaMemsetAsync(e->d_acc.p, 0, (grn::VS_COUNT + 1) * sizeof(unsigned long long),
+                           b->stream);
+  }
+  if (ce == cudaSuccess)
+    ce = cudaMemsetAsync(b->d_counter.p, 0, sizeof(unsigned long long), b->stream);
+  const grn::BatchProc *dp = b->d_procs.as<grn::BatchProc>();
+  if (ce == cudaSuccess) ce = grn::launch_batch_born(dp, np, b->born_blocks, b->stream);
+  if (ce == cudaSuccess)
+    ce = grn::launch_batch_loop(dp, np, b->d_counter.as<unsigned long long>(), b->loop_blocks,
+                                b->stream);
+  for (int p = 0; p < np && ce == cudaSuccess; ++p) {
+    grn_engine *e = b->eng[p];
+    ce = grn::launch_vegas_reduce(e->d_f.as<double>(), e->ncall, e->d_acc.as<unsigned long long>(),
+                                  e->d_parts.as<double>(), e->d_sc.as<double>(), b->stream);
+    if (ce == cudaSuccess)
+      ce = cudaMemcpyAsync(e->h_sc, e->d_sc.p, grn::VS_COUNT * sizeof(double),
+                           cudaMemcpyDeviceToHost, b->stream);
+    if (ce == cudaSuccess && refine)
+      ce = grn::launch_vegas_refine(e->d_xmat.as<double>(), e->d_f2mat.as<double>(), e->bins,
+                                    e->dim, e->lambda, b->stream);
+  }
+  cudaGraph_t       g  = nullptr;
+  const cudaError_t ce2 = cudaStreamEndCapture(b->stream, &g);
+  if (ce != cudaSuccess || ce2 != cudaSuccess) {
+    if (g) cudaGraphDestroy(g);
+    cudaGetLastError();
+    return fail(GRN_ERR_CUDA, std::string("batch capture: ") +
+                                  cudaGetErrorString(ce != cudaSuccess ? ce : ce2));
+  }
+  const cudaError_t ce3 = cudaGraphInstantiate(&b->exec[refine], g, 0);
+  cudaGraphDestroy(g);
+  if (ce3 != cudaSuccess) return fail(GRN_ERR_CUDA, cudaGetErrorString(ce3));
+  return GRN_OK;
+}
+
+}  // namespace
+
+extern "C" {
+
+grn_status grn_batch_create(grn_engine *const *engines, int32_t n, grn_batch **out) {
+  if (!engines || !out || n < 1 || n > grn::kMaxBatch)
+    return fail(GRN_ERR_INVALID, "a batch holds 1 to 8 engines");
+  *out = nullptr;
+  const int dev = engines[0] ? engines[0]->device : 0;
+  for (int p = 0; p < n; ++p) {
+    grn_engine *e = engines[p];
+    if (!e) return fail(GRN_ERR_INVALID, "null engine");
+    for (int q = 0; q < p; ++q)
+      if (engines[q] == e) return fail(GRN_ERR_INVALID, "an engine appears twice");
+    if (e->device != dev) return fail(GRN_ERR_INVALID, "engines of a batch share one device");
+    if (!e->vegas_ready) return fail(GRN_ERR_STATE, "grn_vegas_init every engine first");
+    const grn_status st = require_screening_ready(e);
+    if (st != GRN_OK) return st;
+    if (e->P.screening && e->prec != GRN_PREC_MIXED)
+      return fail(GRN_ERR_UNSUPPORTED, "batched screened processes use GRN_PREC_MIXED");
+  }
+  GRN_CUDA(cudaSetDevice(dev));
+  auto *b   = new grn_batch();
+  b->device = dev;
+  b->eng.assign(engines, engines + n);
+  grn_status st = GRN_OK;
+  if (cudaStreamCreateWithFlags(&b->stream, cudaStreamNonBlocking) != cudaSuccess ||
+      cudaMallocHost(reinterpret_cast<void **>(&b->h_procs), n * sizeof(grn::BatchProc)) !=
+          cudaSuccess ||
+      b->d_procs.ensure(n * sizeof(grn::BatchProc)) != cudaSuccess ||
+      b->d_counter.ensure(sizeof(unsigned long long)) != cudaSuccess ||
+      cudaEventCreate(&b->ev0) != cudaSuccess || cudaEventCreate(&b->ev1) != cudaSuccess) {
+    cudaGetLastError();
+    st = fail(GRN_ERR_CUDA, "batch: allocation failed");
+  }
+  // stage-A blocks in proportion to the points of each process
+  int sms = 0;
+  cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+  int64_t total = 0;
+  for (grn_engine *e : b->eng) total += e->ncall;
+  const int nb = std::max(n, sms * 16);
+  int       blk = 0;
+  for (int p = 0; p < n && st == GRN_OK; ++p) {
+    grn_engine *e = b->eng[p];
+    st            = vegas_alloc_calls(e, e->ncall);
+    if (st != GRN_OK) break;
+    grn::BatchProc &q = b->h_procs[p];
+    std::memset(&q, 0, sizeof(q));
+    q.A         = e->args();
+    const bool rec = grn::record_mode(q.A, GRN_PREC_MIXED);
+    q.xmat      = e->d_xmat.as<double>();
+    q.bins      = e->bins;
+    q.dim       = e->dim;
+    q.ncall     = e->ncall;
+    q.seed      = e->seed;
+    q.f_out     = e->d_f.as<double>();
+    q.f2mat     = e->d_f2mat.as<double>();
+    q.acc       = e->d_acc.as<unsigned long long>();
+    q.l_idx     = e->d_lidx.as<int64_t>();
+    q.l_x       = e->d_lx.as<double>();
+    q.l_vw      = e->d_lvw.as<double>();
+    q.l_bins    = e->d_lbins.as<uint64_t>();
+    q.rf        = rec ? e->d_recf.as<float>() : nullptr;
+    q.rd        = rec ? e->d_recd.as<double>() : nullptr;
+    const int k = (p == n - 1) ? nb - blk
+                               : std::max<int>(1, static_cast<int>(nb * (double(e->ncall) / total)));
+    q.blk0 = blk;
+    q.blk1 = std::min(nb - (n - 1 - p), blk + k);
+    blk    = q.blk1;
+  }
+  b->born_blocks = nb;
+  b->loop_blocks = grn::batch_loop_blocks(dev);
+  if (st != GRN_OK) {
+    grn_batch_destroy(b);
+    return st;
+  }
+  for (grn_engine *e : b->eng) e->in_batches += 1;
+  b->registered = true;
+  *out = b;
+  return GRN_OK;
+}
+
+grn_status grn_batch_destroy(grn_batch *b) {
+  if (!b) return GRN_OK;
+  cudaSetDevice(b->device);
+  if (b->stream) cudaStreamSynchronize(b->stream);
+  for (cudaGraphExec_t &x : b->exec)
+    if (x) cudaGraphExecDestroy(x);
+  if (b->h_procs) cudaFreeHost(b->h_procs);
+  b->d_procs.release();
+  b->d_counter.release();
+  if (b->ev0) cudaEventDestroy(b->ev0);
+  if (b->ev1) cudaEventDestroy(b->ev1);
+  if (b->stream) cudaStreamDestroy(b->stream);
+  if (b->registered)
+    for (grn_engine *e : b->eng) e->in_batches -= 1;
+  delete b;
+  return GRN_OK;
+}
+
+grn_status grn_batch_iteration(grn_batch *b, int32_t mode, int32_t refine, uint32_t iter_id,
+                               grn_vegas_result *results, double *device_ms) {
+  if (!b) return fail(GRN_ERR_INVALID, "null batch");
+  GRN_CUDA(cudaSetDevice(b->device));
+  const int np = static_cast<int>(b->eng.size());
+  for (int p = 0; p < np; ++p) {
+    grn_engine *e = b->eng[p];
+    if (e->ncall != b->h_procs[p].ncall || e->d_f.as<double>() != b->h_procs[p].f_out)
+      return fail(GRN_ERR_STATE, "an engine's call buffers changed after grn_batch_create");
+    GRN_CUDA(cudaStreamSynchronize(e->stream));  // the batch works on the engines' buffers
+    b->h_procs[p].stream    = iter_id;
+    b->h_procs[p].track_max = mode != 0;
+  }
+  const int r = refine ? 1 : 0;
+  if (!b->exec[r]) {
+    const grn_status st = batch_capture(b, r);
+    if (st != GRN_OK) return st;
+  }
+  GRN_CUDA(cudaEventRecord(b->ev0, b->stream));
+  GRN_CUDA(cudaGraphLaunch(b->exec[r], b->stream));
+  GRN_CUDA(cudaEventRecord(b->ev1, b->stream));
+  GRN_CUDA(cudaStreamSynchronize(b->stream));
+  float ms = 0.f;
+  GRN_CUDA(cudaEventElapsedTime(&ms, b->ev0, b->ev1));
+  b->last_ms = ms;
+  if (device_ms) *device_ms = ms;
+  grn_status st = GRN_OK;
+  for (int p = 0; p < np; ++p) {
+    grn_engine *e  = b->eng[p];
+    e->last_stream = iter_id;
+    e->last_ncall  = e->ncall;
+    e->have_last   = true;
+    e->last_fu     = nullptr;
+    grn_vegas_result res{};
+    const grn_status s2 = vegas_accumulate(e, mode, e->iters_since_clear++, &res);
+    if (results) results[p] = res;
+    if (s2 != GRN_OK && st == GRN_OK) st = s2;
+  }
+  return st;
 }
 
 // ---------------------------------------------------------------------------

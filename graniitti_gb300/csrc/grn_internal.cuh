@@ -112,6 +112,34 @@ cudaError_t launch_unweight(const double *f, int64_t n, double fmax, uint64_t se
                             cudaStream_t st);
 int unweight_blocks(int64_t n);
 
+// Several processes in one pass (grn_batch): one entry per process, in device memory.
+constexpr int kMaxBatch = 8;
+struct BatchProc {
+  KArgs               A;
+  const double       *xmat;
+  int                 bins, dim;
+  int64_t             ncall;
+  uint64_t            seed;
+  uint32_t            stream;     // Philox stream id of the pass (updated every pass)
+  int                 track_max;  // integration pass: track the maximum weight
+  double             *f_out, *f2mat;
+  unsigned long long *acc;
+  int64_t            *l_idx;
+  double             *l_x, *l_vw;
+  uint64_t           *l_bins;
+  float              *rf;
+  double             *rd;
+  int                 blk0, blk1;  // stage-A blocks of this process: [blk0, blk1)
+};
+// Stage A of every process in one launch (block b serves the process whose range holds b).
+cudaError_t launch_batch_born(const BatchProc *procs, int np, int nblocks, cudaStream_t st);
+// Stage B of every process in one persistent launch: blocks take chunks of work from
+// the counter (zeroed by the caller) over the listed events of all processes; record-mode
+// processes run two events per thread, the others the one-event FP32 loop.
+cudaError_t launch_batch_loop(const BatchProc *procs, int np, unsigned long long *counter,
+                              int nblocks, cudaStream_t st);
+int         batch_loop_blocks(int device);
+
 // FP32 FMA throughput probe: returns flops executed by one launch.
 double      fma_probe_flops(int blocks, int threads, int iters);
 cudaError_t launch_fma_probe(int blocks, int threads, int iters, float *sink, cudaStream_t st);

@@ -815,18 +815,17 @@ __device__ void flush_block(double *sf2, int nh, double *f2mat, unsigned long lo
     if (sf2[i] != 0.0) atomicAdd(&f2mat[i], sf2[i]);
 }
 
-// Stage A of a VEGAS pass: Philox points, grid map, tree-level kinematics and cuts.
-// Rejected and unscreened events are finished here; screened events that pass
-// the cuts go to the work list (index, mapped point, VEGAS weight, bins).
-__global__ void __launch_bounds__(kVegasThreads)
-    k_vegas_born(const KArgs A, const double *__restrict__ xmat, int bins, int dim, int64_t ncall,
-                 uint64_t seed, uint32_t stream, int track_max, double *__restrict__ f_out,
-                 double *__restrict__ f2mat, unsigned long long *__restrict__ acc,
-                 int64_t *__restrict__ l_idx, double *__restrict__ l_x, double *__restrict__ l_vw,
-                 uint64_t *__restrict__ l_bins, int64_t cap, float *__restrict__ rf,
-                 double *__restrict__ rd, const float *__restrict__ fu,
-                 const float *__restrict__ flq) {
-  extern __shared__ double dsm[];
+// Stage A of a VEGAS pass: Philox (or flow) points, grid map, tree-level kinematics and
+// cuts. Rejected and unscreened events are finished here; screened events that pass the
+// cuts go to the work list (index, VEGAS weight, bins, and the loop record or the mapped
+// point). Block `bid` of `nbid` blocks serving this pass; dsm: 2 * bins * dim doubles.
+__device__ __forceinline__ void born_pass_body(
+    const KArgs &A, const double *__restrict__ xmat, int bins, int dim, int64_t ncall,
+    uint64_t seed, uint32_t stream, int track_max, double *__restrict__ f_out,
+    double *__restrict__ f2mat, unsigned long long *__restrict__ acc, int64_t *__restrict__ l_idx,
+    double *__restrict__ l_x, double *__restrict__ l_vw, uint64_t *__restrict__ l_bins,
+    int64_t cap, float *__restrict__ rf, double *__restrict__ rd, const float *__restrict__ fu,
+    const float *__restrict__ flq, double *dsm, int bid, int nbid) {
   double   *sx = dsm, *sf2 = dsm + bins * dim;
   const int nh = bins * dim;
   for (int i = threadIdx.x; i < nh; i += blockDim.x) {
@@ -836,9 +835,9 @@ __global__ void __launch_bounds__(kVegasThreads)
   __syncthreads();
   unsigned long long cnt[VS_COUNT] = {};
   double maxf = 0.0, maxW = 0.0;
-  const int64_t stride = static_cast<int64_t>(gridDim.x) * blockDim.x;
+  const int64_t stride = static_cast<int64_t>(nbid) * blockDim.x;
   const int64_t nfull  = ((ncall + stride - 1) / stride) * stride;  // uniform trip count
-  for (int64_t e = static_cast<int64_t>(blockIdx.x) * blockDim.x + threadIdx.x; e < nfull;
+  for (int64_t e = static_cast<int64_t>(bid) * blockDim.x + threadIdx.x; e < nfull;
        e += stride) {
     const bool active = e < ncall;
     bool       loop   = false;
@@ -889,6 +888,19 @@ __global__ void __launch_bounds__(kVegasThreads)
     }
   }
   flush_block(sf2, nh, f2mat, acc, cnt, maxf, maxW);
+}
+
+__global__ void __launch_bounds__(kVegasThreads)
+    k_vegas_born(const KArgs A, const double *__restrict__ xmat, int bins, int dim, int64_t ncall,
+                 uint64_t seed, uint32_t stream, int track_max, double *__restrict__ f_out,
+                 double *__restrict__ f2mat, unsigned long long *__restrict__ acc,
+                 int64_t *__restrict__ l_idx, double *__restrict__ l_x, double *__restrict__ l_vw,
+                 uint64_t *__restrict__ l_bins, int64_t cap, float *__restrict__ rf,
+                 double *__restrict__ rd, const float *__restrict__ fu,
+                 const float *__restrict__ flq) {
+  extern __shared__ double dsm[];
+  born_pass_body(A, xmat, bins, dim, ncall, seed, stream, track_max, f_out, f2mat, acc, l_idx,
+                 l_x, l_vw, l_bins, cap, rf, rd, fu, flq, dsm, blockIdx.x, gridDim.x);
 }
 
 // Stage B of a VEGAS pass: screened weights of the listed events.
@@ -1079,6 +1091,141 @@ cudaError_t launch_vegas_loop(const KArgs &a, int prec, int bins, int dim, int64
   else
     k_vegas_loop<double><<<nblocks, kVegasThreads, nh * sizeof(double), st>>>(
         a, bins, dim, track_max, f_out, f2mat, acc, l_idx, l_x, l_vw, l_bins, ncall);
+  return cudaGetLastError();
+}
+
+// ---------------------------------------------------------------------------
+// Several processes in one pass.
+
+__global__ void __launch_bounds__(kVegasThreads)
+    k_batch_born(const BatchProc *__restrict__ procs, int np) {
+  extern __shared__ double dsm[];
+  int p = 0;
+  while (p + 1 < np && static_cast<int>(blockIdx.x) >= procs[p].blk1) ++p;
+  const BatchProc &q = procs[p];
+  born_pass_body(q.A, q.xmat, q.bins, q.dim, q.ncall, q.seed, q.stream, q.track_max, q.f_out,
+                 q.f2mat, q.acc, q.l_idx, q.l_x, q.l_vw, q.l_bins, q.ncall, q.rf, q.rd, nullptr,
+                 nullptr, dsm, static_cast<int>(blockIdx.x) - q.blk0, q.blk1 - q.blk0);
+}
+
+cudaError_t launch_batch_born(const BatchProc *procs, int np, int nblocks, cudaStream_t st) {
+  k_batch_born<<<nblocks, kVegasThreads, 2 * kMaxBins * kMaxDim * sizeof(double), st>>>(procs,
+                                                                                        np);
+  return cudaGetLastError();
+}
+
+constexpr int kBatchChunk = kVegasThreads;  // work units per grab (one per thread)
+
+__global__ void __launch_bounds__(kVegasThreads, 2)
+    k_batch_loop(const BatchProc *__restrict__ procs, int np,
+                 unsigned long long *__restrict__ counter) {
+  extern __shared__ double dsm[];
+  double *sf2 = dsm;
+  __shared__ KtNode2         skt2[kMaxLoopNodes];
+  __shared__ PhiNode2        sphi2[kMaxLoopNodes];
+  __shared__ KtNode<float>   skt[kMaxLoopNodes];
+  __shared__ PhiNode<float>  sphi[kMaxLoopNodes];
+  __shared__ int64_t         s_begin[kMaxBatch + 1];  // unit ranges, padded to whole chunks
+  __shared__ int64_t         s_n[kMaxBatch];          // listed events per process
+  __shared__ unsigned long long s_chunk;
+  if (threadIdx.x == 0) {
+    int64_t off = 0;
+    for (int p = 0; p < np; ++p) {
+      const BatchProc &q = procs[p];
+      const int64_t    n = min(static_cast<int64_t>(q.acc[VS_COUNT]), q.ncall);
+      const int64_t    units = q.rf ? (n + 1) / 2 : n;
+      s_begin[p] = off;
+      s_n[p]     = n;
+      off += ((units + kBatchChunk - 1) / kBatchChunk) * kBatchChunk;
+    }
+    s_begin[np] = off;
+  }
+  __syncthreads();
+  const int64_t total = s_begin[np];
+  int           cur = -1, nh = 0;
+  LoopEventF<float> c;
+  unsigned long long cnt[VS_COUNT] = {};
+  double maxf = 0.0, maxW = 0.0;
+  while (true) {
+    if (threadIdx.x == 0) s_chunk = atomicAdd(counter, static_cast<unsigned long long>(kBatchChunk));
+    __syncthreads();
+    const int64_t chunk = static_cast<int64_t>(s_chunk);
+    __syncthreads();  // every thread has read s_chunk before the next grab
+    if (chunk >= total) break;
+    int p = 0;
+    while (p + 1 < np && chunk >= s_begin[p + 1]) ++p;
+    if (p != cur) {  // block-uniform: flush the previous process, stage this one
+      if (cur >= 0) {
+        const BatchProc &o = procs[cur];
+        flush_block(sf2, nh, o.f2mat, o.acc, cnt, maxf, maxW);
+        for (int k = 0; k < VS_COUNT; ++k) cnt[k] = 0;
+        maxf = maxW = 0.0;
+      }
+      cur = p;
+      const BatchProc &q = procs[p];
+      nh = q.bins * q.dim;
+      __syncthreads();
+      for (int i = threadIdx.x; i < nh; i += blockDim.x) sf2[i] = 0.0;
+      if (q.rf) stage_nodes2(q.A, skt2, sphi2);
+      else stage_nodes<float>(q.A, skt, sphi);
+      make_loop_consts_fast<float>(q.A.P, q.A.K, c);
+      __syncthreads();
+    }
+    const BatchProc &q = procs[cur];
+    const int64_t    unit = chunk - s_begin[cur] + threadIdx.x, n = s_n[cur];
+    if (q.rf) {
+      if (2 * unit < n) {
+        const int64_t ra = 2 * unit, rb = (2 * unit + 1 < n) ? 2 * unit + 1 : 2 * unit;
+        double  W[2];
+        uint8_t F[2];
+        record_weights2(q.A, c, q.rf, q.rd, q.ncall, ra, rb, skt2, sphi2, W[0], W[1], F[0], F[1]);
+        for (int k = 0; k < (rb != ra ? 2 : 1); ++k) {
+          const int64_t r = k ? rb : ra;
+          const double  f = W[k] * q.l_vw[r];
+          q.f_out[q.l_idx[r]] = f;
+          hist_add(sf2, q.dim, q.l_bins[r], f * f);
+          cnt[VS_AMP_OK] += (F[k] & GRN_FLAG_AMPLITUDE_OK) ? 1 : 0;
+          cnt[VS_NAN] += (F[k] & GRN_FLAG_AMPLITUDE_OK) ? 0 : 1;
+          if (q.track_max) {
+            maxf = fmax(maxf, f);
+            maxW = fmax(maxW, W[k]);
+          }
+        }
+      }
+    } else if (unit < n) {
+      double x[kMaxDim];
+      for (int j = 0; j < kMaxDim; ++j) x[j] = q.l_x[static_cast<int64_t>(j) * q.ncall + unit];
+      uint8_t      fl;
+      const double W = screened_weight<float>(q.A, x, fl, skt, sphi);
+      const double f = W * q.l_vw[unit];
+      q.f_out[q.l_idx[unit]] = f;
+      hist_add(sf2, q.dim, q.l_bins[unit], f * f);
+      cnt[VS_AMP_OK] += (fl & GRN_FLAG_AMPLITUDE_OK) ? 1 : 0;
+      cnt[VS_NAN] += (fl & GRN_FLAG_AMPLITUDE_OK) ? 0 : 1;
+      if (q.track_max) {
+        maxf = fmax(maxf, f);
+        maxW = fmax(maxW, W);
+      }
+    }
+  }
+  if (cur >= 0) {
+    const BatchProc &o = procs[cur];
+    flush_block(sf2, nh, o.f2mat, o.acc, cnt, maxf, maxW);
+  }
+}
+
+int batch_loop_blocks(int device) {
+  int sms = 0, per = 0;
+  cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, device);
+  cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, k_batch_loop, kVegasThreads,
+                                                kMaxBins * kMaxDim * sizeof(double));
+  return sms * (per < 1 ? 1 : per);
+}
+
+cudaError_t launch_batch_loop(const BatchProc *procs, int np, unsigned long long *counter,
+                              int nblocks, cudaStream_t st) {
+  k_batch_loop<<<nblocks, kVegasThreads, kMaxBins * kMaxDim * sizeof(double), st>>>(procs, np,
+                                                                                     counter);
   return cudaGetLastError();
 }
 

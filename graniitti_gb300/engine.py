@@ -297,6 +297,37 @@ class Flow:
         return r
 
 
+class Batch:
+    """Several engines (processes) run one pass together: fused stage launches replayed
+    as a CUDA graph (grn_batch_*)."""
+
+    def __init__(self, engines):
+        self.lib = engines[0].lib
+        self.engines = list(engines)
+        arr = (ctypes.c_void_p * len(engines))(*[e.h.value for e in engines])
+        h = ctypes.c_void_p()
+        _abi.check(self.lib.grn_batch_create(arr, len(engines), ctypes.byref(h)))
+        self.h = h
+
+    def iteration(self, mode=1, refine=True, iter_id=1):
+        res = (_abi.VegasResult * len(self.engines))()
+        ms = ctypes.c_double()
+        _abi.check(self.lib.grn_batch_iteration(self.h, mode, 1 if refine else 0, iter_id, res,
+                                                ctypes.byref(ms)))
+        return list(res), ms.value
+
+    def close(self):
+        if getattr(self, "h", None):
+            self.lib.grn_batch_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
 class Graniitti:
     """MGraniitti-style driver (src/MGraniitti.cc) over the GPU engine.
 

@@ -439,6 +439,27 @@ grn_status grn_write_records(grn_writer *w, const double *p4, int64_t n, const i
                              double sigma_err_pb);
 
 /* ------------------------------------------------------------------------ */
+/* Several processes in one pass (no counterpart in the reference)            */
+/* ------------------------------------------------------------------------ */
+/* A batch runs one integration pass of every engine it holds (1..8 processes on one
+ * device, each with its own VEGAS grid, ncall, seed and buffers) as two fused launches:
+ * stage A of all processes (blocks in proportion to their points), then one persistent
+ * stage-B launch whose blocks take chunks of work from a queue over the screened events
+ * of all processes (dynamic balance between processes of different cost). The pass is
+ * captured once as a CUDA graph (one per refine setting) and replayed; per-pass values
+ * reach the graph through a pinned table it uploads. Results, the f values of the pass
+ * (grn_unweight / grn_vegas_points) and the estimates of each engine are as after
+ * grn_vegas_iteration on that engine. Screened processes run the FP32 loop
+ * (GRN_PREC_MIXED). Engines cannot be destroyed while a batch holds them. */
+typedef struct grn_batch grn_batch;
+grn_status grn_batch_create(grn_engine *const *engines, int32_t n, grn_batch **out);
+grn_status grn_batch_destroy(grn_batch *b);
+/* results: one grn_vegas_result per engine (may be NULL); device_ms: device time of the
+ * whole pass (may be NULL). */
+grn_status grn_batch_iteration(grn_batch *b, int32_t mode, int32_t refine, uint32_t iter_id,
+                               grn_vegas_result *results, double *device_ms);
+
+/* ------------------------------------------------------------------------ */
 /* Launch configuration and autotuner (no counterpart in the reference)       */
 /* ------------------------------------------------------------------------ */
 /* The kt-loop stage in record mode (screened, GRN_PREC_MIXED, one trajectory) has two

@@ -1,0 +1,86 @@
+"""Several processes in one pass (grn_batch): the fused, graph-replayed pass gives each
+process exactly the pass it gets alone, and a batched integration the same cross sections."""
+import ctypes
+
+import numpy as np
+import pytest
+
+from conftest import CARD_SCR
+
+pytestmark = pytest.mark.gpu
+
+
+def _engines(n_call):
+    import graniitti_gb300 as g
+    from graniitti_gb300 import _abi, card
+    c = card.read_card(CARD_SCR)
+    procs = ["PP[CON]<C> -> pi+ pi-", "PP[CON]<C> -> K+ K-", "PP[CONTENSOR]<C> -> pi+ pi-"]
+    out = []
+    for k, proc in enumerate(procs):
+        P = card.build_params(c, proc)
+        P.loop.n_kt, P.loop.n_phi, P.loop.kt_max = 15, 12, 1.75
+        e = g.Engine(P, 0)
+        e.eikonal_build(512, 2000)
+        e.set_tuning(loop_pair=1)
+        vp = _abi.VegasParams()
+        vp.bins, vp.iter, vp.ncall, vp.lambda_ = 128, 5, n_call[k], 1.5
+        vp.chi2max, vp.precision, vp.burnin_iter, vp.prec, vp.seed = 10.0, 1e-3, 3, g.MIXED, 11 + k
+        e.vegas_init(vp)
+        out.append(e)
+    return out
+
+
+def test_batched_pass_equals_separate_passes(gpu):
+    import graniitti_gb300 as g
+    calls = [1 << 16, 3 << 14, 1 << 15]
+    es = _engines(calls)
+    grids = [e.vegas_grid() for e in es]
+    sep = [e.vegas_iteration(mode=1, refine=False, iter_id=7) for e in es]
+    for e, x in zip(es, grids):
+        e.vegas_clear()
+        e.vegas_set_grid(x)
+    b = g.Batch(es)
+    res, ms = b.iteration(mode=1, refine=False, iter_id=7)
+    for r0, r1 in zip(sep, res):
+        # the engines' counters accumulate over both passes
+        assert r1.evaluations == 2 * r0.evaluations and r1.kinematics_ok == 2 * r0.kinematics_ok
+        assert r1.amplitude_ok == 2 * r0.amplitude_ok and r1.nan_count == 2 * r0.nan_count
+        assert r1.I_this == pytest.approx(r0.I_this, rel=1e-14)
+        assert r1.maxf == pytest.approx(r0.maxf, rel=1e-14)
+    print("batched pass of 3 processes: %.2f ms; I = %s" % (ms, [r.I_this for r in res]))
+    # an engine in a batch cannot be destroyed
+    with pytest.raises(Exception):
+        from graniitti_gb300 import _abi
+        _abi.check(es[0].lib.grn_destroy(es[0].h))
+    b.close()
+    for e in es:
+        e.close()
+
+
+def test_batched_integration_matches_separate(gpu):
+    import graniitti_gb300 as g
+    calls = [1 << 16, 1 << 16, 1 << 16]
+    es = _engines(calls)
+    b = g.Batch(es)
+    for it in range(4):
+        b.iteration(mode=0, refine=True, iter_id=100 + it)
+    for e in es:
+        e.vegas_clear()
+    for it in range(6):
+        res, ms = b.iteration(mode=1, refine=True, iter_id=200 + it)
+    b.close()
+    sep = []
+    for e in _engines(calls):
+        for it in range(4):
+            e.vegas_iteration(mode=0, refine=True, iter_id=300 + it)
+        e.vegas_clear()
+        for it in range(6):
+            r = e.vegas_iteration(mode=1, refine=True, iter_id=400 + it)
+        sep.append(r)
+    for rb, rs in zip(res, sep):
+        pull = (rb.sigma - rs.sigma) / np.hypot(rb.sigma_err, rs.sigma_err)
+        print("batched %.5e +- %.1e vs separate %.5e +- %.1e: pull %.2f"
+              % (rb.sigma, rb.sigma_err, rs.sigma, rs.sigma_err, pull))
+        assert abs(pull) < 4
+    for e in es:
+        e.close()
