@@ -219,6 +219,77 @@ def _summary(results, ms, npts, steps):
             "rel_var_per_point": rel_var, "seconds_to_0.1pct": t01, "ms_per_step": ms / steps}
 
 
+BATCH_MIX = [("PP[CON]<C> -> pi+ pi-", 0.5), ("PP[CON]<C> -> K+ K-", 0.3),
+             ("PP[CONTENSOR]<C> -> pi+ pi-", 0.2)]
+
+
+def batched_leg(g, _abi, torch, total, steps, warmup, device):
+    """Screened 2-body continua batched in one pass (fused launches, CUDA graph) against
+    the same processes run one after another; the same points, grids and results."""
+    from graniitti_gb300 import card
+    c = card.read_card(CARD_SCR)
+
+    def engines(seed0):
+        out = []
+        for k, (proc, frac) in enumerate(BATCH_MIX):
+            P = card.build_params(c, proc)
+            P.loop.n_kt, P.loop.n_phi, P.loop.kt_max = LOOP_KT, LOOP_PHI, LOOP_KTMAX
+            P.loop.n_bt, P.loop.n_kt2 = N_BT, N_KT2
+            e = g.Engine(P, device)
+            e.eikonal_build(N_BT, N_KT2)
+            e.autotune(sample=1 << 16)
+            vp = _abi.VegasParams()
+            vp.bins, vp.iter, vp.ncall, vp.lambda_ = 128, steps, int(total * frac) // 128 * 128, 1.5
+            vp.chi2max, vp.precision, vp.burnin_iter = 10.0, 1e-3, warmup
+            vp.prec, vp.seed = g.MIXED, seed0 + k
+            e.vegas_init(vp)
+            for it in range(warmup):
+                e.vegas_iteration(mode=0, refine=True, iter_id=1 + it)
+            e.vegas_clear()
+            out.append(e)
+        return out
+
+    es = engines(500)
+    b = g.Batch(es)
+    b.iteration(mode=0, refine=True, iter_id=50)  # graph capture + warm-up
+    for e in es:
+        e.vegas_clear()
+        e.set_maxweight(0.0)
+    t0 = torch.cuda.Event(enable_timing=True)
+    t1 = torch.cuda.Event(enable_timing=True)
+    torch.cuda.synchronize()
+    t0.record()
+    for it in range(steps):
+        res, _ = b.iteration(mode=1, refine=True, iter_id=100 + it)
+    t1.record()
+    torch.cuda.synchronize()
+    ms_b = t0.elapsed_time(t1) / steps
+    b.close()
+    for e in es:
+        e.vegas_clear()
+        e.set_maxweight(0.0)
+    torch.cuda.synchronize()
+    t0.record()
+    for it in range(steps):
+        for e in es:
+            e.vegas_iteration(mode=1, refine=True, iter_id=100 + it)
+    t1.record()
+    torch.cuda.synchronize()
+    ms_s = t0.elapsed_time(t1) / steps
+    procs = []
+    for (proc, frac), e, r in zip(BATCH_MIX, es, res):
+        procs.append({"process": proc, "points_per_step": int(e.vp.ncall),
+                      "eps_unw": r.sigma / r.maxf if r.maxf > 0 else None,
+                      "sigma_barn": r.sigma, "sigma_rel_err": r.sigma_err / r.sigma})
+        e.close()
+    n = sum(p["points_per_step"] for p in procs)
+    return {"workload": "screened 2-body continua, %s of %d points per pass, one fused pass"
+                        % ("/".join(str(int(f * 100)) for _, f in BATCH_MIX), n),
+            "ms_per_step_batched": ms_b, "ms_per_step_separate": ms_s,
+            "evaluations_per_s_batched": n / (ms_b * 1e-3),
+            "speedup_over_separate": ms_s / ms_b, "processes": procs}
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -230,6 +301,7 @@ def main():
     ap.add_argument("--flow-rounds", type=int, default=3)
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-fp64", action="store_true")
+    ap.add_argument("--no-batch", action="store_true")
     args = ap.parse_args()
     if args.warmup < 3:
         args.warmup = 3
@@ -353,6 +425,9 @@ def main():
         eng.set_maxweight(fl_maxf)
         kernel_timing(eng, reset=True)
 
+    # -- several processes in one pass (fused launches, CUDA graph) ------------
+    batched = None if args.no_batch else batched_leg(g, _abi, torch, n, 3, args.warmup, local)
+
     # -- e2e: unweighted events delivered to pinned host memory through the C ABI
     #    (flow pass -> hit-or-miss against the integration's max f -> points) ---
     fmax = r.maxf
@@ -400,7 +475,7 @@ def main():
                          sample_kernel_ms=flow_s * 1e3, sample_tflops=flow_tflops,
                          sample_frac_of_measured_bf16=(flow_tflops / bf16_peak
                                                        if bf16_peak else None)),
-               plain_vegas_mixed=plain, plain_vegas_fp64=fp64, autotune=tuned,
+               plain_vegas_mixed=plain, plain_vegas_fp64=fp64, autotune=tuned, batched=batched,
                flow_over_plain_mixed=value / plain["value"] if plain["value"] else None,
                flow_over_plain_fp64=(value / fp64["value"]) if fp64 and fp64["value"] else None)
     line = {"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,

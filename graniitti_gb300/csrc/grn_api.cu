@@ -1019,10 +1019,13 @@ struct grn_batch {
   std::vector<grn_engine *> eng;
   int                       device = 0;
   cudaStream_t              stream = nullptr;
-  DevBuf                    d_procs, d_counter;
+  DevBuf                    d_counter;        // work queues of the two stage-B kinds
   grn::BatchProc           *h_procs = nullptr;  // pinned: uploaded by the graph every pass
   int                       born_blocks = 0, loop_blocks = 0;
-  cudaGraphExec_t           exec[2] = {nullptr, nullptr};  // without / with grid refinement
+  bool                      has_kind[2] = {false, false};  // generic / record-mode processes
+  cudaStream_t              side = nullptr;     // second branch of the captured graph
+  cudaEvent_t               fork = nullptr, join = nullptr;
+  cudaGraphExec_t           exec[4] = {};  // by (refine, maximum tracking)
   cudaEvent_t               ev0 = nullptr, ev1 = nullptr;
   double                    last_ms = 0.0;
   bool                      registered = false;  // counted in the engines' in_batches
@@ -1030,11 +1033,10 @@ struct grn_batch {
 
 namespace {
 
-grn_status batch_capture(grn_batch *b, int refine) {
+grn_status batch_capture(grn_batch *b, int refine, int track_max) {
   const int np = static_cast<int>(b->eng.size());
   GRN_CUDA(cudaStreamBeginCapture(b->stream, cudaStreamCaptureModeThreadLocal));
-  cudaError_t ce = cudaMemcpyAsync(b->d_procs.p, b->h_procs, np * sizeof(grn::BatchProc),
-                                   cudaMemcpyHostToDevice, b->stream);
+  cudaError_t ce = grn::upload_batch_procs(b->h_procs, np, b->stream);
   for (int p = 0; p < np && ce == cudaSuccess; ++p) {
     grn_engine *e  = b->eng[p];
     const int   nh = e->bins * e->dim;
@@ -1047,11 +1049,27 @@ grn_status batch_capture(grn_batch *b, int refine) {
   }
   if (ce == cudaSuccess)
     ce = cudaMemsetAsync(b->d_counter.p, 0, sizeof(unsigned long long), b->stream);
-  const grn::BatchProc *dp = b->d_procs.as<grn::BatchProc>();
-  if (ce == cudaSuccess) ce = grn::launch_batch_born(dp, np, b->born_blocks, b->stream);
-  if (ce == cudaSuccess)
-    ce = grn::launch_batch_loop(dp, np, b->d_counter.as<unsigned long long>(), b->loop_blocks,
+  if (ce == cudaSuccess) ce = grn::launch_batch_born(np, b->born_blocks, b->stream);
+  // stage B: the record-mode processes in one persistent launch; the processes on the
+  // generic loop in their own launches on a second branch of the graph (concurrent)
+  const bool two = b->has_kind[0] && b->has_kind[1];
+  if (ce == cudaSuccess && two) ce = cudaEventRecord(b->fork, b->stream);
+  if (ce == cudaSuccess && two) ce = cudaStreamWaitEvent(b->side, b->fork, 0);
+  if (ce == cudaSuccess && b->has_kind[1])
+    ce = grn::launch_batch_loop(np, b->d_counter.as<unsigned long long>(), b->loop_blocks,
                                 b->stream);
+  for (int p = 0; p < np && ce == cudaSuccess; ++p) {
+    grn_engine *e = b->eng[p];
+    if (!e->P.screening || b->h_procs[p].rf) continue;
+    ce = grn::launch_vegas_loop(b->h_procs[p].A, GRN_PREC_MIXED, e->bins, e->dim, e->ncall,
+                                track_max, e->d_f.as<double>(), e->d_f2mat.as<double>(),
+                                e->d_acc.as<unsigned long long>(), e->d_lidx.as<int64_t>(),
+                                e->d_lx.as<double>(), e->d_lvw.as<double>(),
+                                e->d_lbins.as<uint64_t>(), nullptr, nullptr, e->nblocks,
+                                two ? b->side : b->stream);
+  }
+  if (ce == cudaSuccess && two) ce = cudaEventRecord(b->join, b->side);
+  if (ce == cudaSuccess && two) ce = cudaStreamWaitEvent(b->stream, b->join, 0);
   for (int p = 0; p < np && ce == cudaSuccess; ++p) {
     grn_engine *e = b->eng[p];
     ce = grn::launch_vegas_reduce(e->d_f.as<double>(), e->ncall, e->d_acc.as<unsigned long long>(),
@@ -1071,7 +1089,7 @@ grn_status batch_capture(grn_batch *b, int refine) {
     return fail(GRN_ERR_CUDA, std::string("batch capture: ") +
                                   cudaGetErrorString(ce != cudaSuccess ? ce : ce2));
   }
-  const cudaError_t ce3 = cudaGraphInstantiate(&b->exec[refine], g, 0);
+  const cudaError_t ce3 = cudaGraphInstantiate(&b->exec[2 * refine + track_max], g, 0);
   cudaGraphDestroy(g);
   if (ce3 != cudaSuccess) return fail(GRN_ERR_CUDA, cudaGetErrorString(ce3));
   return GRN_OK;
@@ -1104,11 +1122,13 @@ grn_status grn_batch_create(grn_engine *const *engines, int32_t n, grn_batch **o
   b->eng.assign(engines, engines + n);
   grn_status st = GRN_OK;
   if (cudaStreamCreateWithFlags(&b->stream, cudaStreamNonBlocking) != cudaSuccess ||
+      cudaStreamCreateWithFlags(&b->side, cudaStreamNonBlocking) != cudaSuccess ||
       cudaMallocHost(reinterpret_cast<void **>(&b->h_procs), n * sizeof(grn::BatchProc)) !=
           cudaSuccess ||
-      b->d_procs.ensure(n * sizeof(grn::BatchProc)) != cudaSuccess ||
-      b->d_counter.ensure(sizeof(unsigned long long)) != cudaSuccess ||
-      cudaEventCreate(&b->ev0) != cudaSuccess || cudaEventCreate(&b->ev1) != cudaSuccess) {
+      b->d_counter.ensure(2 * sizeof(unsigned long long)) != cudaSuccess ||
+      cudaEventCreate(&b->ev0) != cudaSuccess || cudaEventCreate(&b->ev1) != cudaSuccess ||
+      cudaEventCreateWithFlags(&b->fork, cudaEventDisableTiming) != cudaSuccess ||
+      cudaEventCreateWithFlags(&b->join, cudaEventDisableTiming) != cudaSuccess) {
     cudaGetLastError();
     st = fail(GRN_ERR_CUDA, "batch: allocation failed");
   }
@@ -1141,6 +1161,7 @@ grn_status grn_batch_create(grn_engine *const *engines, int32_t n, grn_batch **o
     q.l_bins    = e->d_lbins.as<uint64_t>();
     q.rf        = rec ? e->d_recf.as<float>() : nullptr;
     q.rd        = rec ? e->d_recd.as<double>() : nullptr;
+    if (e->P.screening) b->has_kind[rec ? 1 : 0] = true;
     const int k = (p == n - 1) ? nb - blk
                                : std::max<int>(1, static_cast<int>(nb * (double(e->ncall) / total)));
     q.blk0 = blk;
@@ -1166,10 +1187,12 @@ grn_status grn_batch_destroy(grn_batch *b) {
   for (cudaGraphExec_t &x : b->exec)
     if (x) cudaGraphExecDestroy(x);
   if (b->h_procs) cudaFreeHost(b->h_procs);
-  b->d_procs.release();
   b->d_counter.release();
   if (b->ev0) cudaEventDestroy(b->ev0);
   if (b->ev1) cudaEventDestroy(b->ev1);
+  if (b->fork) cudaEventDestroy(b->fork);
+  if (b->join) cudaEventDestroy(b->join);
+  if (b->side) cudaStreamDestroy(b->side);
   if (b->stream) cudaStreamDestroy(b->stream);
   if (b->registered)
     for (grn_engine *e : b->eng) e->in_batches -= 1;
@@ -1190,13 +1213,13 @@ grn_status grn_batch_iteration(grn_batch *b, int32_t mode, int32_t refine, uint3
     b->h_procs[p].stream    = iter_id;
     b->h_procs[p].track_max = mode != 0;
   }
-  const int r = refine ? 1 : 0;
-  if (!b->exec[r]) {
-    const grn_status st = batch_capture(b, r);
+  const int r = refine ? 1 : 0, tm = mode != 0 ? 1 : 0;
+  if (!b->exec[2 * r + tm]) {
+    const grn_status st = batch_capture(b, r, tm);
     if (st != GRN_OK) return st;
   }
   GRN_CUDA(cudaEventRecord(b->ev0, b->stream));
-  GRN_CUDA(cudaGraphLaunch(b->exec[r], b->stream));
+  GRN_CUDA(cudaGraphLaunch(b->exec[2 * r + tm], b->stream));
   GRN_CUDA(cudaEventRecord(b->ev1, b->stream));
   GRN_CUDA(cudaStreamSynchronize(b->stream));
   float ms = 0.f;

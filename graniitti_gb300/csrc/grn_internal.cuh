@@ -131,13 +131,14 @@ struct BatchProc {
   double             *rd;
   int                 blk0, blk1;  // stage-A blocks of this process: [blk0, blk1)
 };
+// The process table of a batch, copied into constant memory (stream-ordered).
+cudaError_t upload_batch_procs(const BatchProc *h_procs, int np, cudaStream_t st);
 // Stage A of every process in one launch (block b serves the process whose range holds b).
-cudaError_t launch_batch_born(const BatchProc *procs, int np, int nblocks, cudaStream_t st);
-// Stage B of every process in one persistent launch: blocks take chunks of work from
-// the counter (zeroed by the caller) over the listed events of all processes; record-mode
-// processes run two events per thread, the others the one-event FP32 loop.
-cudaError_t launch_batch_loop(const BatchProc *procs, int np, unsigned long long *counter,
-                              int nblocks, cudaStream_t st);
+cudaError_t launch_batch_born(int np, int nblocks, cudaStream_t st);
+// Stage B of the record-mode processes in one persistent launch (two events per thread):
+// blocks take chunks of work from the counter (zeroed by the caller) over the listed events
+// of those processes.
+cudaError_t launch_batch_loop(int np, unsigned long long *counter, int nblocks, cudaStream_t st);
 int         batch_loop_blocks(int device);
 
 // FP32 FMA throughput probe: returns flops executed by one launch.

@@ -12,6 +12,7 @@
 #include <cuda_runtime.h>
 
 #include <algorithm>
+#include <type_traits>
 #include <cstdint>
 
 #include "grn_internal.cuh"
@@ -1095,45 +1096,56 @@ cudaError_t launch_vegas_loop(const KArgs &a, int prec, int bins, int dim, int64
 }
 
 // ---------------------------------------------------------------------------
-// Several processes in one pass.
+// Several processes in one pass. The process table lives in constant memory: a block
+// reads its process's arguments at a block-uniform index, served by the constant cache.
 
-__global__ void __launch_bounds__(kVegasThreads)
-    k_batch_born(const BatchProc *__restrict__ procs, int np) {
+__constant__ BatchProc c_procs[kMaxBatch];
+
+cudaError_t upload_batch_procs(const BatchProc *h_procs, int np, cudaStream_t st) {
+  return cudaMemcpyToSymbolAsync(c_procs, h_procs, np * sizeof(BatchProc), 0,
+                                 cudaMemcpyHostToDevice, st);
+}
+
+__global__ void __launch_bounds__(kVegasThreads, 3) k_batch_born(int np) {
   extern __shared__ double dsm[];
   int p = 0;
-  while (p + 1 < np && static_cast<int>(blockIdx.x) >= procs[p].blk1) ++p;
-  const BatchProc &q = procs[p];
+  while (p + 1 < np && static_cast<int>(blockIdx.x) >= c_procs[p].blk1) ++p;
+  const BatchProc &q = c_procs[p];
   born_pass_body(q.A, q.xmat, q.bins, q.dim, q.ncall, q.seed, q.stream, q.track_max, q.f_out,
                  q.f2mat, q.acc, q.l_idx, q.l_x, q.l_vw, q.l_bins, q.ncall, q.rf, q.rd, nullptr,
                  nullptr, dsm, static_cast<int>(blockIdx.x) - q.blk0, q.blk1 - q.blk0);
 }
 
-cudaError_t launch_batch_born(const BatchProc *procs, int np, int nblocks, cudaStream_t st) {
-  k_batch_born<<<nblocks, kVegasThreads, 2 * kMaxBins * kMaxDim * sizeof(double), st>>>(procs,
-                                                                                        np);
+cudaError_t launch_batch_born(int np, int nblocks, cudaStream_t st) {
+  k_batch_born<<<nblocks, kVegasThreads, 2 * kMaxBins * kMaxDim * sizeof(double), st>>>(np);
   return cudaGetLastError();
 }
 
 constexpr int kBatchChunk = kVegasThreads;  // work units per grab (one per thread)
 
+// Stage B of the record-mode processes (two events per thread) as one persistent launch
+// over a shared work queue. (Processes on the generic loop keep their own launches: their
+// amplitude reads many process constants per loop point, which a kernel parameter serves
+// as free operands and a table at a runtime index does not.)
+template <bool REC>
 __global__ void __launch_bounds__(kVegasThreads, 2)
-    k_batch_loop(const BatchProc *__restrict__ procs, int np,
-                 unsigned long long *__restrict__ counter) {
+    k_batch_loop(int np, unsigned long long *__restrict__ counter) {
   extern __shared__ double dsm[];
   double *sf2 = dsm;
-  __shared__ KtNode2         skt2[kMaxLoopNodes];
-  __shared__ PhiNode2        sphi2[kMaxLoopNodes];
-  __shared__ KtNode<float>   skt[kMaxLoopNodes];
-  __shared__ PhiNode<float>  sphi[kMaxLoopNodes];
-  __shared__ int64_t         s_begin[kMaxBatch + 1];  // unit ranges, padded to whole chunks
-  __shared__ int64_t         s_n[kMaxBatch];          // listed events per process
+  using KT = typename std::conditional<REC, KtNode2, KtNode<float>>::type;
+  using PT = typename std::conditional<REC, PhiNode2, PhiNode<float>>::type;
+  __shared__ KT                 skt[kMaxLoopNodes];
+  __shared__ PT                 sphi[kMaxLoopNodes];
+  __shared__ int64_t            s_begin[kMaxBatch + 1];  // unit ranges, padded to whole chunks
+  __shared__ int64_t            s_n[kMaxBatch];          // listed events per process
   __shared__ unsigned long long s_chunk;
   if (threadIdx.x == 0) {
     int64_t off = 0;
     for (int p = 0; p < np; ++p) {
-      const BatchProc &q = procs[p];
-      const int64_t    n = min(static_cast<int64_t>(q.acc[VS_COUNT]), q.ncall);
-      const int64_t    units = q.rf ? (n + 1) / 2 : n;
+      const BatchProc &q = c_procs[p];
+      const bool       mine = (q.rf != nullptr) == REC;
+      const int64_t    n = mine ? min(static_cast<int64_t>(q.acc[VS_COUNT]), q.ncall) : 0;
+      const int64_t    units = REC ? (n + 1) / 2 : n;
       s_begin[p] = off;
       s_n[p]     = n;
       off += ((units + kBatchChunk - 1) / kBatchChunk) * kBatchChunk;
@@ -1156,29 +1168,32 @@ __global__ void __launch_bounds__(kVegasThreads, 2)
     while (p + 1 < np && chunk >= s_begin[p + 1]) ++p;
     if (p != cur) {  // block-uniform: flush the previous process, stage this one
       if (cur >= 0) {
-        const BatchProc &o = procs[cur];
+        const BatchProc &o = c_procs[cur];
         flush_block(sf2, nh, o.f2mat, o.acc, cnt, maxf, maxW);
         for (int k = 0; k < VS_COUNT; ++k) cnt[k] = 0;
         maxf = maxW = 0.0;
       }
       cur = p;
-      const BatchProc &q = procs[p];
+      const BatchProc &q = c_procs[p];
       nh = q.bins * q.dim;
       __syncthreads();
       for (int i = threadIdx.x; i < nh; i += blockDim.x) sf2[i] = 0.0;
-      if (q.rf) stage_nodes2(q.A, skt2, sphi2);
-      else stage_nodes<float>(q.A, skt, sphi);
-      make_loop_consts_fast<float>(q.A.P, q.A.K, c);
+      if constexpr (REC) {
+        stage_nodes2(q.A, skt, sphi);
+        make_loop_consts_fast<float>(q.A.P, q.A.K, c);
+      } else {
+        stage_nodes<float>(q.A, skt, sphi);
+      }
       __syncthreads();
     }
-    const BatchProc &q = procs[cur];
+    const BatchProc &q = c_procs[cur];
     const int64_t    unit = chunk - s_begin[cur] + threadIdx.x, n = s_n[cur];
-    if (q.rf) {
+    if constexpr (REC) {
       if (2 * unit < n) {
         const int64_t ra = 2 * unit, rb = (2 * unit + 1 < n) ? 2 * unit + 1 : 2 * unit;
         double  W[2];
         uint8_t F[2];
-        record_weights2(q.A, c, q.rf, q.rd, q.ncall, ra, rb, skt2, sphi2, W[0], W[1], F[0], F[1]);
+        record_weights2(q.A, c, q.rf, q.rd, q.ncall, ra, rb, skt, sphi, W[0], W[1], F[0], F[1]);
         for (int k = 0; k < (rb != ra ? 2 : 1); ++k) {
           const int64_t r = k ? rb : ra;
           const double  f = W[k] * q.l_vw[r];
@@ -1209,7 +1224,7 @@ __global__ void __launch_bounds__(kVegasThreads, 2)
     }
   }
   if (cur >= 0) {
-    const BatchProc &o = procs[cur];
+    const BatchProc &o = c_procs[cur];
     flush_block(sf2, nh, o.f2mat, o.acc, cnt, maxf, maxW);
   }
 }
@@ -1217,15 +1232,14 @@ __global__ void __launch_bounds__(kVegasThreads, 2)
 int batch_loop_blocks(int device) {
   int sms = 0, per = 0;
   cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, device);
-  cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, k_batch_loop, kVegasThreads,
+  cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, k_batch_loop<true>, kVegasThreads,
                                                 kMaxBins * kMaxDim * sizeof(double));
   return sms * (per < 1 ? 1 : per);
 }
 
-cudaError_t launch_batch_loop(const BatchProc *procs, int np, unsigned long long *counter,
-                              int nblocks, cudaStream_t st) {
-  k_batch_loop<<<nblocks, kVegasThreads, kMaxBins * kMaxDim * sizeof(double), st>>>(procs, np,
-                                                                                     counter);
+cudaError_t launch_batch_loop(int np, unsigned long long *counter, int nblocks, cudaStream_t st) {
+  k_batch_loop<true><<<nblocks, kVegasThreads, kMaxBins * kMaxDim * sizeof(double), st>>>(
+      np, counter);
   return cudaGetLastError();
 }
 
