@@ -157,6 +157,7 @@ struct grn_flow {
   double      mix     = 0.0;  // weight of the uniform component of the proposal
   DevBuf      d_theta, d_m, d_v, d_grad, d_w2p, d_w3p, d_w2c, d_w3c, d_loss, d_err;
   DevBuf      d_x, d_z, d_lq, d_coef, d_xs;  // batch scratch
+  DevBuf      d_gpart, d_lpart;                // per-block gradient / loss slices
   DevBuf      d_tu, d_tlq, d_tcoef;          // training set
   DevBuf      d_fu, d_flq;                   // points of the last flow pass
 };
@@ -1431,10 +1432,12 @@ grn_status flow_loss_grad(grn_flow *f, const float *x, int64_t ld, const float *
   GRN_CUDA(grn::launch_flow_forward(0, f->d_theta.as<float>(), f->d_w2c.p, f->d_w3c.p, f->layers,
                                     x, ld, n, 0, 0, 0, nullptr, 0, f->d_lq.as<float>(),
                                     f->d_xs.as<float>(), f->d_err.as<int>(), e->stream));
-  GRN_CUDA(cudaMemsetAsync(f->d_grad.p, 0, f->nparams * sizeof(float), e->stream));
-  GRN_CUDA(cudaMemsetAsync(loss_slot, 0, sizeof(double), e->stream));
+  const int slices = grn::flow_backward_slices();
+  GRN_CUDA(f->d_gpart.ensure(static_cast<size_t>(slices) * f->nparams * sizeof(float)));
+  GRN_CUDA(f->d_lpart.ensure(static_cast<size_t>(slices) * sizeof(double)));
   GRN_CUDA(grn::launch_flow_backward(f->d_theta.as<float>(), f->d_w2p.p, f->d_w3p.p, f->layers,
                                      f->d_xs.as<float>(), f->d_lq.as<float>(), coef, n, kind,
+                                     f->d_gpart.as<float>(), f->d_lpart.as<double>(),
                                      f->d_grad.as<float>(), loss_slot, e->stream));
   return GRN_OK;
 }
@@ -1546,7 +1549,8 @@ grn_status grn_flow_destroy(grn_flow *f) {
   }
   for (DevBuf *b : {&f->d_theta, &f->d_m, &f->d_v, &f->d_grad, &f->d_w2p, &f->d_w3p, &f->d_w2c,
                     &f->d_w3c, &f->d_err, &f->d_loss,
-                    &f->d_x, &f->d_z, &f->d_lq, &f->d_coef, &f->d_xs, &f->d_tu, &f->d_tlq,
+                    &f->d_x, &f->d_z, &f->d_lq, &f->d_coef, &f->d_xs, &f->d_gpart,
+                    &f->d_lpart, &f->d_tu, &f->d_tlq,
                     &f->d_tcoef, &f->d_fu, &f->d_flq})
     b->release();
   if (f->e && f->e->last_fu) {

@@ -809,8 +809,9 @@ constexpr size_t kBwdSmem = size_t(kHid) * HS * 2 + size_t(kHid) * W3S * 2 +
                             size_t(2) * kBwdTile * RS * 4 + 2 * size_t(kDim) * kBwdTile * 4 +
                             size_t(kBwdTile) * 4 + sizeof(SmallW);
 
-// Column sums over the warp's 16 rows of an accumulator tile, added to g[col].
-__device__ __forceinline__ void colsum_atomic(const float (&c)[4], float *g, int col) {
+// Column sums over the warp's 16 rows of an accumulator tile into this warp's row of the
+// staging array (summed over the warps in a fixed order afterwards).
+__device__ __forceinline__ void colsum_stage(const float (&c)[4], float *scol, int col) {
   float v0 = c[0] + c[2], v1 = c[1] + c[3];
 #pragma unroll
   for (int o = 4; o < 32; o <<= 1) {
@@ -818,8 +819,8 @@ __device__ __forceinline__ void colsum_atomic(const float (&c)[4], float *g, int
     v1 += __shfl_xor_sync(0xffffffffu, v1, o);
   }
   if ((threadIdx.x & 31) < 4) {
-    atomicAdd(g + col, v0);
-    atomicAdd(g + col + 1, v1);
+    scol[(threadIdx.x >> 5) * kHid + col]     = v0;
+    scol[(threadIdx.x >> 5) * kHid + col + 1] = v1;
   }
 }
 
@@ -827,7 +828,10 @@ __global__ void __launch_bounds__(kBwdThreads, 1)
     k_flow_bwd(const float *__restrict__ theta, const bf16 *__restrict__ w2p,
                const bf16 *__restrict__ w3p, int layers, const float *__restrict__ xs,
                const float *__restrict__ lq, const float *__restrict__ coef, int64_t n,
-               int kind, float inv_n, float *__restrict__ grad, double *__restrict__ loss) {
+               int kind, float inv_n, float *__restrict__ part, double *__restrict__ loss_part) {
+  // this block's private slice of the gradient: every element has one writer at a time,
+  // so the accumulation order (and the result) is fixed
+  float *__restrict__ grad = part + static_cast<int64_t>(blockIdx.x) * layers * kLayerParams;
   extern __shared__ __align__(16) unsigned char smem[];
   bf16   *sW2   = reinterpret_cast<bf16 *>(smem);
   bf16   *sW3   = sW2 + kHid * HS;
@@ -840,6 +844,7 @@ __global__ void __launch_bounds__(kBwdThreads, 1)
   float  *sGld  = sG + kDim * kBwdTile;
   SmallW *sw    = reinterpret_cast<SmallW *>(sGld + kBwdTile);
   __shared__ double sLoss[kBwdThreads / 32];
+  __shared__ float  sCol2[(kBwdThreads / 32) * kHid], sCol1[(kBwdThreads / 32) * kHid];
 
   const int     lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
   const int     g = lane >> 2, t = lane & 3;
@@ -899,7 +904,7 @@ __global__ void __launch_bounds__(kBwdThreads, 1)
           const int jj = threadIdx.x / kRaw, r = threadIdx.x % kRaw;
           float     s  = 0.f;
           for (int p = 0; p < kBwdTile; ++p) s += sRaw[(jj * kBwdTile + p) * RS + r];
-          if (s != 0.f) atomicAdd(grad + lo + ob3 + (2 * pr + jj) * kRaw + r, s);
+          grad[lo + ob3 + (2 * pr + jj) * kRaw + r] += s;
         }
         __syncthreads();
       }
@@ -940,12 +945,12 @@ __global__ void __launch_bounds__(kBwdThreads, 1)
               const int h0 = warp * 32 + a * 16 + g;
               float *gw = grad + lo + oW3 + ch * kRaw;
               if (r < kRaw) {
-                atomicAdd(gw + h0 * kNOut + r, acc[a][nt][0]);
-                atomicAdd(gw + (h0 + 8) * kNOut + r, acc[a][nt][2]);
+                gw[h0 * kNOut + r] += acc[a][nt][0];
+                gw[(h0 + 8) * kNOut + r] += acc[a][nt][2];
               }
               if (r + 1 < kRaw) {
-                atomicAdd(gw + h0 * kNOut + r + 1, acc[a][nt][1]);
-                atomicAdd(gw + (h0 + 8) * kNOut + r + 1, acc[a][nt][3]);
+                gw[h0 * kNOut + r + 1] += acc[a][nt][1];
+                gw[(h0 + 8) * kNOut + r + 1] += acc[a][nt][3];
               }
             }
         }
@@ -977,7 +982,7 @@ __global__ void __launch_bounds__(kBwdThreads, 1)
           if (!(__bfloat162float(h0[1]) > 0.f)) acc[nt][1] = 0.f;
           if (!(__bfloat162float(h1[0]) > 0.f)) acc[nt][2] = 0.f;
           if (!(__bfloat162float(h1[1]) > 0.f)) acc[nt][3] = 0.f;
-          colsum_atomic(acc[nt], grad + lo + ob2, col);
+          colsum_stage(acc[nt], sCol2, col);
         }
         __syncwarp();
 #pragma unroll
@@ -988,6 +993,11 @@ __global__ void __launch_bounds__(kBwdThreads, 1)
         }
       }
       __syncthreads();
+      if (threadIdx.x < kHid) {  // b2 gradient: the warps' column sums in a fixed order
+        float v = 0.f;
+        for (int w = 0; w < kBwdThreads / 32; ++w) v += sCol2[w * kHid + threadIdx.x];
+        grad[lo + ob2 + threadIdx.x] += v;
+      }
       // dW2 = H1^T . dH2  (M = 128 in: warp rows 32w..; N = 128 out in 2 chunks of 64)
       for (int ch = 0; ch < 2; ++ch) {
         float acc[2][8][4];
@@ -1019,10 +1029,10 @@ __global__ void __launch_bounds__(kBwdThreads, 1)
             const int col = ch * 64 + nt * 8 + 2 * t;
             const int h0  = warp * 32 + a * 16 + g;
             float *gw = grad + lo + oW2;
-            atomicAdd(gw + h0 * kHid + col, acc[a][nt][0]);
-            atomicAdd(gw + h0 * kHid + col + 1, acc[a][nt][1]);
-            atomicAdd(gw + (h0 + 8) * kHid + col, acc[a][nt][2]);
-            atomicAdd(gw + (h0 + 8) * kHid + col + 1, acc[a][nt][3]);
+            gw[h0 * kHid + col] += acc[a][nt][0];
+            gw[h0 * kHid + col + 1] += acc[a][nt][1];
+            gw[(h0 + 8) * kHid + col] += acc[a][nt][2];
+            gw[(h0 + 8) * kHid + col + 1] += acc[a][nt][3];
           }
       }
       // dh1 = (dH2 . W2^T) * [h1 > 0]  (warp rows m0; N = 128 in; K = 128 out)
@@ -1051,9 +1061,14 @@ __global__ void __launch_bounds__(kBwdThreads, 1)
           if (!(__bfloat162float(h0[1]) > 0.f)) acc[nt][1] = 0.f;
           if (!(__bfloat162float(h1[0]) > 0.f)) acc[nt][2] = 0.f;
           if (!(__bfloat162float(h1[1]) > 0.f)) acc[nt][3] = 0.f;
-          colsum_atomic(acc[nt], grad + lo + ob1, col);
+          colsum_stage(acc[nt], sCol1, col);
         }
         __syncthreads();  // every warp is done reading H1 (dW2) before it is replaced
+        if (threadIdx.x < kHid) {  // b1 gradient: the warps' column sums in a fixed order
+          float v = 0.f;
+          for (int w = 0; w < kBwdThreads / 32; ++w) v += sCol1[w * kHid + threadIdx.x];
+          grad[lo + ob1 + threadIdx.x] += v;
+        }
 #pragma unroll
         for (int nt = 0; nt < 16; ++nt) {
           const int col = nt * 8 + 2 * t;
@@ -1073,7 +1088,7 @@ __global__ void __launch_bounds__(kBwdThreads, 1)
         }
 #pragma unroll
         for (int a = 0; a < kDA; ++a)
-          if (s[a] != 0.f) atomicAdd(grad + lo + oW1 + a * kHid + c, s[a]);
+          grad[lo + oW1 + a * kHid + c] += s[a];
       }
       {
         const int p = threadIdx.x % kBwdTile, ap = threadIdx.x / kBwdTile;
@@ -1095,7 +1110,24 @@ __global__ void __launch_bounds__(kBwdThreads, 1)
   if (threadIdx.x == 0) {
     double s = 0.0;
     for (int w = 0; w < kBwdThreads / 32; ++w) s += sLoss[w];
-    atomicAdd(loss, s);
+    loss_part[blockIdx.x] = s;
+  }
+}
+
+// grad[i] = sum over the blocks' slices in block order; loss = sum of the block losses.
+__global__ void k_flow_grad_reduce(const float *__restrict__ part, int nslices, int64_t np,
+                                   float *__restrict__ grad, const double *__restrict__ loss_part,
+                                   double *__restrict__ loss) {
+  for (int64_t i = blockIdx.x * static_cast<int64_t>(blockDim.x) + threadIdx.x; i < np;
+       i += static_cast<int64_t>(gridDim.x) * blockDim.x) {
+    float v = 0.f;
+    for (int c = 0; c < nslices; ++c) v += part[c * np + i];
+    grad[i] = v;
+  }
+  if (blockIdx.x == 0 && threadIdx.x == 0) {
+    double v = 0.0;
+    for (int c = 0; c < nslices; ++c) v += loss_part[c];
+    *loss = v;
   }
 }
 
@@ -1243,17 +1275,24 @@ cudaError_t launch_flow_forward(int mode, const float *theta, const void *w2c, c
   return cudaGetLastError();
 }
 
+int flow_backward_slices() { return sm_count(); }
+
 cudaError_t launch_flow_backward(const float *theta, const void *w2p, const void *w3p, int layers,
                                  const float *xs, const float *lq, const float *coef, int64_t n,
-                                 int kind, float *grad, double *loss, cudaStream_t st) {
+                                 int kind, float *part, double *loss_part, float *grad,
+                                 double *loss, cudaStream_t st) {
   if (n <= 0) return cudaSuccess;
-  const int64_t tiles = (n + flow::kBwdTile - 1) / flow::kBwdTile;
-  const int     grid  = static_cast<int>(std::min<int64_t>(tiles, sm_count()));
-  const size_t  sm    = flow::kBwdSmem;
+  const int64_t tiles  = (n + flow::kBwdTile - 1) / flow::kBwdTile;
+  const int     grid   = static_cast<int>(std::min<int64_t>(tiles, sm_count()));
+  const size_t  sm     = flow::kBwdSmem;
+  const int64_t np     = static_cast<int64_t>(layers) * flow::kLayerParams;
+  cudaError_t   e      = cudaMemsetAsync(part, 0, static_cast<size_t>(grid) * np * sizeof(float), st);
+  if (e != cudaSuccess) return e;
   cudaFuncSetAttribute(flow::k_flow_bwd, cudaFuncAttributeMaxDynamicSharedMemorySize, int(sm));
   flow::k_flow_bwd<<<grid, flow::kBwdThreads, sm, st>>>(
       theta, static_cast<const bf16 *>(w2p), static_cast<const bf16 *>(w3p), layers, xs, lq,
-      coef, n, kind, 1.0f / static_cast<float>(n), grad, loss);
+      coef, n, kind, 1.0f / static_cast<float>(n), part, loss_part);
+  flow::k_flow_grad_reduce<<<2 * sm_count(), 256, 0, st>>>(part, grid, np, grad, loss_part, loss);
   return cudaGetLastError();
 }
 

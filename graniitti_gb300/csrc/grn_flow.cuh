@@ -39,12 +39,16 @@ cudaError_t launch_flow_forward(int mode, const float *theta, const void *w2c, c
                                 uint64_t seed, uint32_t stream, int64_t first, float *xout,
                                 int64_t ld_out, float *lq, float *xs_store, int *err,
                                 cudaStream_t st);
-// Loss over n points and its gradient (accumulated into grad, which the caller zeroes;
-// loss_sum receives sum_i l_i added to its value). kind 1: l = coef exp(-log q);
+// Loss over n points and its gradient: grad <- d(sum_i l_i / n)/d theta and loss_sum <-
+// sum_i l_i, both deterministic (each backward block accumulates a private slice of part,
+// flow_backward_slices() x parameters floats, and loss_part, flow_backward_slices()
+// doubles; the slices are summed in block order). kind 1: l = coef exp(-log q);
 // kind 0: l = -coef log q.
+int         flow_backward_slices();
 cudaError_t launch_flow_backward(const float *theta, const void *w2p, const void *w3p, int layers,
                                  const float *xs, const float *lq, const float *coef, int64_t n,
-                                 int kind, float *grad, double *loss_sum, cudaStream_t st);
+                                 int kind, float *part, double *loss_part, float *grad,
+                                 double *loss_sum, cudaStream_t st);
 cudaError_t launch_flow_adam(float *theta, float *m, float *v, const float *grad, int64_t n,
                              float lr_t, float b1, float b2, float eps_t, cudaStream_t st);
 // Training coefficients from the weights f of a pass and the sampling log density

@@ -220,3 +220,31 @@ def test_flow_rejects_bad_parameters(gpu, params):
     e2 = g.Engine(params, 0)
     w, _ = e2.event_weights(np.full((4, 8), 0.5))
     e2.close()
+
+
+def test_gradient_and_training_are_deterministic(gpu, params):
+    """Gradient accumulation has a fixed order: the same inputs give bit-identical
+    gradients, and the same training gives bit-identical weights."""
+    import graniitti_gb300 as g
+    e = g.Engine(params, 0)
+    f = g.Flow(e, seed=3)
+    th = _theta(51, scale=0.03).astype(np.float32)
+    f.set_params(th)
+    rng = np.random.default_rng(52)
+    x = rng.random((8, 3000)).astype(np.float32)
+    coef = (rng.random(3000) + 0.5).astype(np.float32)
+    l1, g1 = f.loss_grad(x, coef)
+    l2, g2 = f.loss_grad(x, coef)
+    assert l1 == l2 and np.array_equal(g1, g2)
+    e.vegas_init(_vp(1 << 16))
+    for it in range(3):
+        e.vegas_iteration(mode=0, refine=True, iter_id=1 + it)
+    out = []
+    for rep in range(2):
+        fr = g.Flow(e, seed=9)
+        fr.train(n_train=1 << 16, batch=1 << 13, epochs=2, rounds=2, lr=1e-3)
+        out.append(fr.get_params())
+        fr.close()
+    assert np.array_equal(out[0], out[1])
+    f.close()
+    e.close()
