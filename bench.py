@@ -11,7 +11,7 @@ kinematics, FP32 compensated kt-loop) -> f = W vw / q -> sums and max.
 
 Three samplers run on the same engine, in this order:
   plain VEGAS, mixed precision   burn-in, then timed passes (grid refined each pass)
-  flow proposal (the headline)   trained (untimed, reported) in 3 rounds of 3 epochs,
+  flow proposal (the headline)   trained (untimed, reported) in 4 rounds of 3 epochs,
                                  batch 16384, on 2^22 weighted points each (round 1 from
                                  the adapted grid, later rounds from the flow itself), then
                                  timed passes, grid frozen; 5% of each pass is drawn
@@ -298,7 +298,7 @@ def main():
     ap.add_argument("--impl", default="engine", choices=["engine", "reference"])
     ap.add_argument("--points", type=int, default=1 << 22)
     ap.add_argument("--flow-epochs", type=int, default=3)
-    ap.add_argument("--flow-rounds", type=int, default=3)
+    ap.add_argument("--flow-rounds", type=int, default=4)
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-fp64", action="store_true")
     ap.add_argument("--no-batch", action="store_true")

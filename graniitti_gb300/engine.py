@@ -341,7 +341,7 @@ class Graniitti:
                card format): LAYERS, NTRAIN, BATCH, EPOCHS, ROUNDS, LR, MIX.
     """
 
-    FLOW_DEFAULTS = {"LAYERS": 6, "NTRAIN": 1 << 22, "BATCH": 16384, "EPOCHS": 3, "ROUNDS": 3,
+    FLOW_DEFAULTS = {"LAYERS": 6, "NTRAIN": 1 << 22, "BATCH": 16384, "EPOCHS": 3, "ROUNDS": 4,
                      "LR": 1e-3, "MIX": 0.05}
 
     def __init__(self, device=0):
