@@ -487,7 +487,9 @@ def main():
                     "d2h_bytes_per_step": int(acc_step * (8 + 64) + 2 * 8 + 8 * 10),
                     "what": "grn_flow_iteration + grn_unweight + grn_vegas_points per step, "
                             "accepted events' hypercube vectors into pinned host memory"},
-            "gpu_launches": 5 * args.steps,
+            # per flow pass: uniform points, density of the uniform share, flow sample,
+            # mixture density (4), stage A, kt-loop stage, sums, finish (4)
+            "gpu_launches": (8 if FLOW_MIX > 0 else 5) * args.steps,
             "roofline": {"bound": "fp32", "achieved": achieved, "peak": peak,
                          "unit": "TFLOP/s", "frac": achieved / peak if peak else None,
                          "traffic": traffic,

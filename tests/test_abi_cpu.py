@@ -60,3 +60,32 @@ def test_create_without_device_fails_cleanly(lib_built):
     h = ctypes.c_void_p()
     st = lib.grn_create(ctypes.byref(P), 0, ctypes.byref(h))
     assert st == _abi.GRN_ERR_NO_DEVICE and not h.value
+
+
+STRUCTS = ["grn_soft_params", "grn_regge_params", "grn_tensor_params", "grn_gencuts",
+           "grn_fidcuts", "grn_loop_numerics", "grn_process_params", "grn_vegas_params",
+           "grn_vegas_result", "grn_flat_params", "grn_flow_params", "grn_flow_train_params",
+           "grn_flow_train_result", "grn_tuning", "grn_tune_result"]
+MIRROR = {"grn_soft_params": "SoftParams", "grn_regge_params": "ReggeParams",
+          "grn_tensor_params": "TensorParams", "grn_gencuts": "GenCuts", "grn_fidcuts": "FidCuts",
+          "grn_loop_numerics": "LoopNumerics", "grn_process_params": "ProcessParams",
+          "grn_vegas_params": "VegasParams", "grn_vegas_result": "VegasResult",
+          "grn_flat_params": "FlatParams", "grn_flow_params": "FlowParams",
+          "grn_flow_train_params": "FlowTrainParams", "grn_flow_train_result": "FlowTrainResult",
+          "grn_tuning": "Tuning", "grn_tune_result": "TuneResult"}
+
+
+def test_ctypes_struct_sizes_match_the_c_compiler(tmp_path):
+    """Every struct of the header has the same size in C and in the ctypes mirror."""
+    from graniitti_gb300 import _abi
+    src = tmp_path / "sizes.c"
+    src.write_text('#include <stdio.h>\n#include "graniitti_gb300.h"\nint main(void) {\n' +
+                   "".join('  printf("%%s %%zu\\n", "%s", sizeof(%s));\n' % (n, n) for n in STRUCTS) +
+                   "  return 0;\n}\n")
+    exe = tmp_path / "sizes"
+    subprocess.run(["gcc", "-std=c11", "-I", os.path.dirname(HEADER), str(src), "-o", str(exe)],
+                   check=True)
+    out = subprocess.run([str(exe)], capture_output=True, text=True, check=True).stdout
+    for line in out.splitlines():
+        name, size = line.split()
+        assert ctypes.sizeof(getattr(_abi, MIRROR[name])) == int(size), name
