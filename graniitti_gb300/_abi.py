@@ -33,6 +33,8 @@ GRN_FLAG_AMPLITUDE_OK = 8
 
 GRN_PROC_REGGE_CON = 1
 GRN_PROC_TENSOR_CON = 2
+GRN_PROC_TENSOR_RES = 3
+GRN_MAX_RESONANCES = 4
 GRN_PS_CONTINUUM = 1
 GRN_PS_FACTORIZED = 2
 GRN_PREC_FP64 = 0
@@ -76,12 +78,19 @@ class LoopNumerics(ctypes.Structure):
                 ("n_bt", c_int32), ("n_kt2", c_int32)]
 
 
+class Resonance(ctypes.Structure):
+    _fields_ = [("J", c_int32), ("P", c_int32), ("M", c_double), ("W", c_double),
+                ("g_tensor", c_double * 7), ("g_decay", c_double)]
+
+
 class ProcessParams(ctypes.Structure):
     _fields_ = [("process", c_int32), ("phase_space", c_int32), ("n_central", c_int32),
                 ("screening", c_int32), ("sqrt_s", c_double), ("m_beam", c_double),
                 ("m_central", c_double * 8), ("s_factor", c_double),
                 ("gcuts", GenCuts), ("fcuts", FidCuts), ("soft", SoftParams),
-                ("regge", ReggeParams), ("loop", LoopNumerics), ("tensor", TensorParams)]
+                ("regge", ReggeParams), ("loop", LoopNumerics), ("tensor", TensorParams),
+                ("n_res", c_int32), ("_pad_res", c_int32),
+                ("res", Resonance * GRN_MAX_RESONANCES)]
 
 
 class VegasParams(ctypes.Structure):
@@ -140,6 +149,7 @@ class FlowTrainResult(ctypes.Structure):
 # Every exported entry point with its ctypes signature (restype, argtypes).
 SIGNATURES = {
     "grn_default_params": (None, [c_void_p]),
+    "grn_tensor_decay_coupling": (c_double, [c_int32, c_double, c_double, c_double, c_double]),
     "grn_create": (c_int32, [c_void_p, c_int32, c_void_p]),
     "grn_destroy": (c_int32, [c_void_p]),
     "grn_engine_stream": (c_void_p, [c_void_p]),

@@ -11,7 +11,7 @@ import math
 import re
 
 from . import _abi
-from .modeldata import PARTICLES, TUNES
+from .modeldata import BRANCHING, PARTICLES, RESONANCES, TUNES
 
 _PROC_RE = re.compile(r"^\s*([A-Za-z]+)\[([A-Z+]+)\]<([A-Z])>\s*$")
 
@@ -55,17 +55,52 @@ def read_card(path):
         return json.loads(strip_json5(f.read()))
 
 
+def split_commands(proc):
+    """The '@' commands of a process string (aux::SplitCommands, src/MAux.cc:690-800):
+    '@ID[t1,t2]{k1:v1, k2:v2}' -> (ID, [t1, t2], {k1: v1, k2: v2}); a singlet '@ID:VALUE'
+    (or '@ID') -> (ID, [], {'_SINGLET_': VALUE or 'true'})."""
+    if "@" not in proc:
+        return []
+    out = []
+    for blk in proc[proc.index("@"):].split("@")[1:]:
+        blk = " ".join(blk.split())
+        targets, args = [], {}
+        if ("[" in blk) != ("]" in blk):
+            raise ValueError("incomplete @ID[]{} syntax: %r" % blk)
+        if "[" in blk:
+            l, r = blk.index("["), blk.index("]")
+            targets = [t.strip() for t in blk[l + 1:r].split(",") if t.strip()]
+            blk = blk[:l] + blk[r + 1:]
+        if ("{" in blk) != ("}" in blk):
+            raise ValueError("incomplete @ID[]{} syntax: %r" % blk)
+        if "{" in blk:
+            l, r = blk.index("{"), blk.index("}")
+            ident = blk[:l].strip()
+            for kv in blk[l + 1:r].split(","):
+                if kv.strip():
+                    if ":" not in kv:
+                        raise ValueError("@%s{} argument %r is not key:value" % (ident, kv))
+                    k, v = kv.split(":", 1)
+                    args[k.strip()] = v.strip()
+        else:
+            parts = blk.split(":")
+            ident = parts[0].strip()
+            if len(parts) > 2:
+                raise ValueError("invalid @ singlet %r" % blk)
+            args["_SINGLET_"] = parts[1].strip() if len(parts) == 2 else "true"
+        out.append((ident, targets, args))
+    return out
+
+
 def parse_process(proc):
-    """'PP[CON]<C> -> pi+ pi-' -> (istate, channel, class, [final states], options)."""
+    """'PP[CON]<C> -> pi+ pi-' -> (istate, channel, class, [final states], options);
+    options holds the singlet '@ID:VALUE' commands (split_commands gives all of them)."""
     opts = {}
     if "@" in proc:
-        head, tail = proc.split("@", 1)
-        for tok in ("@" + tail).split("@")[1:]:
-            tok = tok.strip()
-            if ":" in tok:
-                k, v = tok.split(":", 1)
-                opts[k.strip()] = v.strip()
-        proc = head
+        for ident, _, args in split_commands(proc):
+            if "_SINGLET_" in args:
+                opts[ident] = args["_SINGLET_"]
+        proc = proc[:proc.index("@")]
     if "->" not in proc:
         raise ValueError("process string needs '->': %r" % proc)
     left, right = proc.split("->", 1)
@@ -91,12 +126,14 @@ def build_params(card, process=None, tune=None):
     T = TUNES[tune]
     proc = process or pp["PROCESS"]
     istate, channel, cls, finals, _ = parse_process(proc)
-    if not (istate == "PP" and channel in ("CON", "CONTENSOR") and cls in ("C", "F") and
-            len(finals) == 2):
-        raise UnsupportedProcess("engine implements PP[CON|CONTENSOR]<C|F> -> 2-body, got %r"
-                                 % proc)
+    if not (istate == "PP" and channel in ("CON", "CONTENSOR", "RESTENSOR") and
+            cls in ("C", "F") and len(finals) == 2):
+        raise UnsupportedProcess(
+            "engine implements PP[CON|CONTENSOR|RESTENSOR]<C|F> -> 2-body, got %r" % proc)
     if channel == "CONTENSOR" and not all(f in ("pi+", "pi-", "K+", "K-", "pi0") for f in finals):
         raise UnsupportedProcess("CONTENSOR is implemented for pseudoscalar pairs (2xS)")
+    if channel == "RESTENSOR" and sorted(finals) not in (["pi+", "pi-"], ["K+", "K-"]):
+        raise UnsupportedProcess("RESTENSOR is implemented for pi+ pi- and K+ K- decays")
     if int(pp.get("NSTARS", 0)) != 0:
         raise UnsupportedProcess("forward excitation (NSTARS > 0) is not implemented")
     if pp["BEAM"] != ["p+", "p+"]:
@@ -109,7 +146,8 @@ def build_params(card, process=None, tune=None):
     # s = (pbeam1 + pbeam2)^2 with equal energies (MProcess.cc:309-324)
     P.sqrt_s = 2.0 * E1
     P.m_beam = mb
-    P.process = _abi.GRN_PROC_REGGE_CON if channel == "CON" else _abi.GRN_PROC_TENSOR_CON
+    P.process = {"CON": _abi.GRN_PROC_REGGE_CON, "CONTENSOR": _abi.GRN_PROC_TENSOR_CON,
+                 "RESTENSOR": _abi.GRN_PROC_TENSOR_RES}[channel]
     P.phase_space = _abi.GRN_PS_CONTINUUM if cls == "C" else _abi.GRN_PS_FACTORIZED
     P.n_central = 2
     P.screening = 1 if pp.get("POMLOOP", False) else 0
@@ -195,6 +233,9 @@ def build_params(card, process=None, tune=None):
     P.tensor.gPps = tp["gPpipi"] if P.m_central[0] < 0.2 else tp["gPKK"]
     P.tensor.em_kelly = 1 if T["PARAM_STRUCTURE"]["EM"] == "KELLY" else 0
 
+    if channel == "RESTENSOR":
+        set_resonances(P, pp, proc, tune, finals)
+
     # Loop numerics: defaults 15 x 12 moved by 3*ND (MEikonal.h:40-57), tables
     # 10000 intervals (modeldata/NUMERICS.json).
     nd = int(card.get("INTEGRALPARAM", {}).get("POMLOOP", {}).get("ND", 0))
@@ -205,6 +246,64 @@ def build_params(card, process=None, tune=None):
     P.loop.n_bt = 10000
     P.loop.n_kt2 = 10000
     return P
+
+
+def resonance_list(pp, proc):
+    """Resonance names: the card's PROCESSPARAM RES list, replaced by an @RES{name:1, ...}
+    command (MGraniitti::ReadProcessParam, src/MGraniitti.cc:456-477)."""
+    names = list(pp.get("RES", []))
+    for ident, _, args in split_commands(proc):
+        if ident == "RES":
+            names = [k for k, v in args.items() if v in ("true", "1")]
+    return names
+
+
+def set_resonances(P, pp, proc, tune, finals):
+    """Resonance parameters (PARAM_RES), '@R[name]{M:.., W:.., gN:..}' overrides
+    (src/MGraniitti.cc:480-575) and the decay couplings (MProcess::SetupBranching,
+    src/MProcess.cc:471-520), in the order the reference applies them."""
+    table = RESONANCES.get(tune, {})
+    names = resonance_list(pp, proc)
+    if not names:
+        raise ValueError("RESTENSOR needs resonances: PROCESSPARAM RES or @RES{name:1}")
+    if len(names) > _abi.GRN_MAX_RESONANCES:
+        raise UnsupportedProcess("at most %d resonances in the coherent sum"
+                                 % _abi.GRN_MAX_RESONANCES)
+    res = {}
+    for n in names:
+        if n not in table:
+            raise UnsupportedProcess("resonance %s (decaying to %s) is not available"
+                                     % (n, " ".join(finals)))
+        res[n] = dict(table[n], g_Tensor=list(table[n]["g_Tensor"]))
+    for ident, targets, args in split_commands(proc):
+        if ident != "R":
+            continue
+        if len(targets) != 1 or targets[0] not in res:
+            raise ValueError("@R[] needs one target among the resonances: %r" % targets)
+        r = res[targets[0]]
+        for k, v in args.items():
+            if k == "M":
+                r["M"] = float(v)
+            elif k == "W":
+                r["W"] = float(v)
+            elif k.startswith("g") and k[1:].isdigit() and int(k[1:]) < len(r["g_Tensor"]):
+                r["g_Tensor"][int(k[1:])] = float(v)
+    lib = _abi.load_library()
+    pair = tuple(sorted(finals))  # ("pi+", "pi-"), ("K+", "K-")
+    P.n_res = len(names)
+    for i, n in enumerate(names):
+        r = res[n]
+        if r["J"] == 2 and any(abs(g) > 1e-6 for g in r["g_Tensor"][1:]):
+            raise UnsupportedProcess("%s: J = 2 coupling structures 1..6 are not implemented" % n)
+        br = BRANCHING.get(r["pdg"], {}).get(pair)
+        if br is None:
+            raise UnsupportedProcess("no branching ratio for %s -> %s" % (n, " ".join(finals)))
+        R = P.res[i]
+        R.J, R.P, R.M, R.W = r["J"], r["P"], r["M"], r["W"]
+        for k, g in enumerate(r["g_Tensor"]):
+            R.g_tensor[k] = g
+        R.g_decay = lib.grn_tensor_decay_coupling(r["J"], r["M"], r["W"], PARTICLES[finals[0]][1],
+                                                  br)
 
 
 def vegas_params(card, prec=_abi.GRN_PREC_FP64, seed=1):

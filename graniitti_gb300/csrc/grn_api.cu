@@ -166,13 +166,50 @@ namespace {
 
 grn_status derive_consts(const grn_process_params &P, grn::Consts &K) {
   using namespace grn;
-  if ((P.process != GRN_PROC_REGGE_CON && P.process != GRN_PROC_TENSOR_CON) ||
+  if ((P.process != GRN_PROC_REGGE_CON && P.process != GRN_PROC_TENSOR_CON &&
+       P.process != GRN_PROC_TENSOR_RES) ||
       (P.phase_space != GRN_PS_CONTINUUM && P.phase_space != GRN_PS_FACTORIZED))
     return fail(GRN_ERR_UNSUPPORTED,
-                "only PP[CON|CONTENSOR]<C|F> 2-body continua are implemented");
+                "only PP[CON|CONTENSOR|RESTENSOR]<C|F> 2-body processes are implemented");
   if (P.process == GRN_PROC_TENSOR_CON &&
       !(P.tensor.ap_P > 0 && P.tensor.gPNN > 0 && P.tensor.gPps > 0))
     return fail(GRN_ERR_INVALID, "tensor-pomeron parameters are not set");
+  K.n_res = 0;
+  if (P.process == GRN_PROC_TENSOR_RES) {
+    if (!(P.tensor.ap_P > 0 && P.tensor.gPNN > 0))
+      return fail(GRN_ERR_INVALID, "tensor-pomeron parameters are not set");
+    if (P.n_res < 1 || P.n_res > GRN_MAX_RESONANCES)
+      return fail(GRN_ERR_INVALID, "RESTENSOR needs 1 to 4 resonances");
+    if (std::fabs(P.m_central[0] - P.m_central[1]) > 1e-9)
+      return fail(GRN_ERR_UNSUPPORTED, "RESTENSOR decays to an equal-mass pseudoscalar pair");
+    const double g2 = P.tensor.gPNN * P.tensor.gPNN;
+    for (int r = 0; r < P.n_res; ++r) {
+      const grn_resonance &R = P.res[r];
+      if (!(R.M > 0) || !(R.W >= 0) || !std::isfinite(R.g_decay))
+        return fail(GRN_ERR_INVALID, "resonance mass, width or decay coupling invalid");
+      // the reference skips structures with |g| <= 1e-6 (MTensorPomeron.cc:1660-1670)
+      const int first_unsupported = R.J == 2 ? 1 : 2;
+      for (int i = first_unsupported; i < 7; ++i)
+        if (std::fabs(R.g_tensor[i]) > 1e-6)
+          return fail(GRN_ERR_UNSUPPORTED,
+                      R.J == 2 ? "J = 2 resonances: only the coupling structure g0 is implemented"
+                               : "J = 0 resonances have two coupling structures");
+      if (R.J == 2) {
+        K.res_c0[r] = -9.0 * g2 * R.g_tensor[0] * R.g_decay;
+        K.res_c1[r] = 0.0;
+      } else if (R.J == 0 && R.P == 1) {
+        K.res_c0[r] = 18.0 * g2 * R.g_decay * R.g_tensor[0];
+        K.res_c1[r] = 18.0 * g2 * R.g_decay * R.g_tensor[1];
+      } else {
+        return fail(GRN_ERR_UNSUPPORTED,
+                    "RESTENSOR to two pseudoscalars is implemented for J = 0 (P = +1) and J = 2");
+      }
+      K.res_J[r]  = R.J;
+      K.res_M2[r] = R.M * R.M;
+      K.res_MW[r] = R.M * R.W;
+    }
+    K.n_res = P.n_res;
+  }
   if (P.n_central != 2) return fail(GRN_ERR_UNSUPPORTED, "only 2-body central states");
   if (!(P.sqrt_s > 2 * P.m_beam)) return fail(GRN_ERR_INVALID, "sqrt_s below threshold");
   if (!(P.gcuts.fpt_max > 0) || !(P.gcuts.kt_max > P.gcuts.kt_min) ||
@@ -356,6 +393,33 @@ void grn_default_params(grn_process_params *p) {
   p->loop = {15, 12, 1e-4, 1.75, 10000, 10000};
   // TUNE0 PARAM_TENSORPOM, pion coupling; Kelly proton form factors (GENERAL.json:178-219)
   p->tensor = {0.0808, 0.25, 1.87, 1.76, 1, 0};
+}
+
+double grn_tensor_decay_coupling(int32_t J, double M, double W, double m_daughter, double BR) {
+  // partial width = coupling^2 x phase space x |vertex|^2 (MTensorPomeron::GDecay)
+  auto gdecay = [&](double Mr) {
+    const double pw = W * BR;
+    const double b  = std::sqrt(1.0 - 4.0 * (m_daughter / Mr) * (m_daughter / Mr));
+    if (J == 0) return std::sqrt(pw / (1.0 / (16.0 * grn::kPi * Mr) * b));
+    if (J == 1) return std::sqrt(pw / (Mr / (192.0 * grn::kPi) * b * b * b));
+    if (J == 2) return std::sqrt(pw / (Mr / (480.0 * grn::kPi) * Mr * Mr * b * b * b * b * b));
+    if (J == 4) return 1.0;
+    return std::nan("");
+  };
+  // two-body phase space PDW2body with |A|^2 = 1: zero below threshold
+  auto ps = [&](double Mr) {
+    const double x = Mr * Mr, y = m_daughter * m_daughter;
+    const double l = x * x + 2.0 * y * y - 2.0 * (2.0 * x * y + y * y);
+    return std::sqrt(std::max(0.0, l)) / (16.0 * grn::kPi * x * Mr);
+  };
+  double g = gdecay(M);
+  if (std::fabs(ps(M)) < 1e-12) {
+    for (int i = 1; i <= 3; ++i) {
+      g = gdecay(M + i * W);
+      if (ps(M + i * W) > 1e-12) break;
+    }
+  }
+  return g;
 }
 
 const char *grn_last_error(void) { return g_last_error.c_str(); }

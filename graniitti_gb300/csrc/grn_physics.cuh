@@ -75,6 +75,12 @@ struct Consts {
   double lns0;              // log(s0)
   int    n_active;          // number of active trajectories
   int    active[3];
+  // PP[RESTENSOR] resonances: spin, M0^2, M0 W and the real prefactors of the collapsed
+  // contractions (tensor_me3)
+  int    n_res;
+  int    res_J[GRN_MAX_RESONANCES];
+  double res_M2[GRN_MAX_RESONANCES], res_MW[GRN_MAX_RESONANCES];
+  double res_c0[GRN_MAX_RESONANCES], res_c1[GRN_MAX_RESONANCES];
 };
 
 // sin(pi x), cos(pi x) without rounding pi x first.
@@ -171,7 +177,16 @@ struct LCKin {
   T p3p, p3m, p3x, p3y, p4p, p4m, p4x, p4y;  // central pair
   T L, eps, mp2;                             // beams: pa = (L, eps, 0), pb = (eps, L, 0)
   T t1, t2, s13, s14, s23, s24, that, uhat;  // invariants
+  T q1p, q1m, q2p, q2m;                      // light-cone parts of q1 = pa - p1, q2 = pb - p2
 };
+
+// q1+ = x1 L and q1- = -(pT1^2 + x1 mp^2) / ((1 - x1) L), both free of cancellation
+// (and likewise for q2 with + and - exchanged).
+template <typename T>
+GRN_HD void q_lightcone(T x, T ptsq, T mp2, T L, T &big, T &small) {
+  big   = x * L;
+  small = -(ptsq + x * mp2) / ((T(1) - x) * L);
+}
 
 template <typename T>
 GRN_HD T lc_dot(T ap, T am, T ax, T ay, T bp, T bm, T bx, T by) {
@@ -225,6 +240,151 @@ GRN_HD cx<T> tensor_me4_2xs(const grn_process_params &P, const Consts &K, const 
   const cx<T> Au = cmul(tensor_exchange<T>(tp, k.s14, k.t1), tensor_exchange<T>(tp, k.s23, k.t2));
   // M = -i (i wt v13 v24 At + i wu v14 v23 Au) = wt v13 v24 At + wu v14 v23 Au
   return cadd(cscale(At, wt * v13 * v24), cscale(Au, wu * v14 * v23));
+}
+
+// ---------------------------------------------------------------------------
+// Tensor-pomeron resonances decaying to two pseudoscalars, coherent sum
+// (MTensorPomeron::ME3, src/MTensorPomeron.cc:164-565, PROC_11). The proton vertex
+// -3i gPNN F1(t) P_mu P_nu (P = p' + p, :1388) through the pomeron propagator
+// 1/(4s) (-i s ap)^(alpha(t)-1) (g g + g g - g g / 2) (:2288), with s_i = (p_i + X)^2
+// (MProcess.cc:1533), gives per leg c(s_i,t_i) (-3i gPNN F1(t_i)) W_i with the traceless
+//   W_i = 2 P_i P_i - P_i^2 g / 2.
+// Contracted with traceless tensors the vertex structures collapse:
+//  J = 2, iG_PPT_00 (:1701-1731) with the tensor propagator iD_TMES (:2422-2446) and the
+//    decay vertex iG_f2psps (:2121-2137):
+//      A = -9 gPNN^2 g0 g_d C F^2 Delta tr(W1 W2 Pi),  Pi = kh kh + kh^2 ghat / 3,
+//      ghat = -g + X X / m^2, kh = ghat.(p3 - p4),
+//      tr(W1 W2 Pi) = 4 a Pi(P2,P1) - b2 Pi(P1,P1) - b1 Pi(P2,P2);
+//  J = 0, iG_PPS_0 + iG_PPS_1 (:1536-1571) with iD_MES (:2383) and iG_f0ss (:2028):
+//      A = 18 gPNN^2 g_d C F^2 Delta [g0 (4 a^2 - b1 b2) + g1 (4 a E + 5/4 b1 b2 q1.q2)];
+// C = c(s1,t1) c(s2,t2) F1(t1) F1(t2) FM(t1) FM(t2), FM(q^2) = 1/(1 - q^2), F = exp(-(m^2 -
+// M0^2)^2) (the production and the decay form factor), Delta = 1/(m^2 - M0^2 + i M0 W),
+// a = P1.P2, b_i = P_i^2 = 4 mp^2 - t_i, q_i = p_beam,i - p_i (P_i.q_i = 0), and
+// E = (P1.q2)(P2.q1) - a q1.q2 evaluated as the bivector contraction (P1^q1).(q2^P2),
+// which has no O(s^2) cancellation between its terms. The prefactors gPNN^2 g g_d per
+// resonance are Consts::res_c0 / res_c1.
+template <typename T>
+GRN_HD T lc_bivector_dot(T ap, T am, T ax, T ay, T bp, T bm, T bx, T by,   // B = a ^ b
+                         T cp, T cm, T cx_, T cy, T dp, T dm, T dx, T dy) {  // C = c ^ d
+  const T Bpm = ap * bm - am * bp, Cpm = cp * dm - cm * dp;
+  const T Bmx = am * bx - ax * bm, Cpx = cp * dx - cx_ * dp;
+  const T Bmy = am * by - ay * bm, Cpy = cp * dy - cy * dp;
+  const T Bpx = ap * bx - ax * bp, Cmx = cm * dx - cx_ * dm;
+  const T Bpy = ap * by - ay * bp, Cmy = cm * dy - cy * dm;
+  const T Bxy = ax * by - ay * bx, Cxy = cx_ * dy - cy * dx;
+  return T(-0.25) * Bpm * Cpm - T(0.5) * (Bmx * Cpx + Bmy * Cpy + Bpx * Cmx + Bpy * Cmy) +
+         Bxy * Cxy;
+}
+
+// What depends on the central system only, which the kt-loop leaves unchanged, comes from
+// the tree-level point in FP64: the resonance sums R2 = sum_{J=2} c0 F^2 Delta,
+// R0 = sum_{J=0} c0 F^2 Delta, R1 = sum_{J=0} c1 F^2 Delta, and Pi(n-, n+) with the light-cone
+// vectors n+ = (+ 1, - 0, 0), n- = (+ 0, - 1, 0). With P1 = 2L n+ + d1, P2 = 2L n- + d2
+// (d1 = (-q1+, P1-, p1T), d2 = (P2+, -q2-, p2T), all O(1)) the leading part of
+// Pi(P2, P1) is 4 L^2 Pi(n-, n+): near the zero of the d-wave decay distribution it cancels
+// between terms 10^4 times larger than itself, which only the FP64 evaluation survives.
+template <typename T>
+struct ResSums {
+  cx<T> R2, R0, R1;
+  T     pinn;  // Pi(n-, n+)
+};
+
+// Resonance-side vectors: X = p3 + p4, kh = ghat.(p3 - p4) and kh^2 (kh^2 = (p3 - p4)^2 -
+// (X.k)^2 / m^2 with X.k = m3^2 - m4^2).
+template <typename T>
+struct ResVec {
+  T Xp, Xm, Xx, Xy, m2, khp, khm, khx, khy, kh2;
+};
+
+template <typename T>
+GRN_HD ResVec<T> res_vectors(const Consts &K, T p3p, T p3m, T p3x, T p3y, T p4p, T p4m, T p4x,
+                             T p4y) {
+  ResVec<T> v;
+  v.Xp = p3p + p4p; v.Xm = p3m + p4m; v.Xx = p3x + p4x; v.Xy = p3y + p4y;
+  v.m2 = v.Xp * v.Xm - (v.Xx * v.Xx + v.Xy * v.Xy);
+  const T pk = T(K.m3sq - K.m4sq);
+  const T c  = pk / v.m2;
+  v.khp = -(p3p - p4p) + c * v.Xp;
+  v.khm = -(p3m - p4m) + c * v.Xm;
+  v.khx = -(p3x - p4x) + c * v.Xx;
+  v.khy = -(p3y - p4y) + c * v.Xy;
+  v.kh2 = T(2) * T(K.m3sq + K.m4sq) - v.m2 - pk * c;
+  return v;
+}
+
+GRN_HD ResSums<double> resonance_sums(const Consts &K, double m2, const ResVec<double> &v) {
+  ResSums<double> R{{0, 0}, {0, 0}, {0, 0}, 0};
+  for (int r = 0; r < K.n_res; ++r) {
+    const double dm = m2 - K.res_M2[r], mw = K.res_MW[r];
+    const double f2 = exp(-2.0 * dm * dm) / (dm * dm + mw * mw);  // F^2 / |m^2 - M0^2 + i M0 W|^2
+    const cx<double> D{dm * f2, -mw * f2};
+    if (K.res_J[r] == 2) {
+      R.R2 = cadd(R.R2, cscale(D, K.res_c0[r]));
+    } else {
+      R.R0 = cadd(R.R0, cscale(D, K.res_c0[r]));
+      R.R1 = cadd(R.R1, cscale(D, K.res_c1[r]));
+    }
+  }
+  // Pi(n-, n+) = kh+ kh- / 4 + kh^2 / 3 (X+ X- / (4 m^2) - 1/2)
+  R.pinn = 0.25 * v.khp * v.khm + v.kh2 / 3.0 * (0.25 * v.Xp * v.Xm / v.m2 - 0.5);
+  return R;
+}
+
+template <typename T>
+GRN_HD cx<T> tensor_me3(const grn_process_params &P, const Consts &K, const LCKin<T> &k,
+                        const ResSums<T> &R) {
+  const T L = k.L, eps = k.eps;
+  const T P1p = k.p1p + L, P1m = k.p1m + eps, P2p = k.p2p + eps, P2m = k.p2m + L;
+  const T b1 = T(4) * k.mp2 - k.t1, b2 = T(4) * k.mp2 - k.t2;
+  const T a  = lc_dot<T>(P1p, P1m, k.p1x, k.p1y, P2p, P2m, k.p2x, k.p2y);
+  // central system X = p3 + p4, its invariant mass and kh
+  const ResVec<T> v = res_vectors<T>(K, k.p3p, k.p3m, k.p3x, k.p3y, k.p4p, k.p4m, k.p4x, k.p4y);
+  const T Xp = v.Xp, Xm = v.Xm, Xx = v.Xx, Xy = v.Xy, m2 = v.m2;
+  const T s1 = k.mp2 + m2 + k.p1p * Xm + k.p1m * Xp - T(2) * (k.p1x * Xx + k.p1y * Xy);
+  const T s2 = k.mp2 + m2 + k.p2p * Xm + k.p2m * Xp - T(2) * (k.p2x * Xx + k.p2y * Xy);
+  const cx<T> R2 = R.R2, R0 = R.R0, R1 = R.R1;
+  cx<T> G{T(0), T(0)};
+  if (R2.re != T(0) || R2.im != T(0)) {
+    const T khp = v.khp, khm = v.khm, khx = v.khx, khy = v.khy;
+    const T kv1 = lc_dot<T>(khp, khm, khx, khy, P1p, P1m, k.p1x, k.p1y);
+    const T kv2 = lc_dot<T>(khp, khm, khx, khy, P2p, P2m, k.p2x, k.p2y);
+    const T pv1 = lc_dot<T>(Xp, Xm, Xx, Xy, P1p, P1m, k.p1x, k.p1y);
+    const T pv2 = lc_dot<T>(Xp, Xm, Xx, Xy, P2p, P2m, k.p2x, k.p2y);
+    const T im2 = T(1) / m2, third = v.kh2 * T(1.0 / 3.0);
+    // Pi(P2, P1) = 4 L^2 Pi(n-, n+) + 2 L (Pi(n-, d1) + Pi(d2, n+)) + Pi(d2, d1)
+    const T d1p = -k.q1p, d1m = P1m, d2p = P2p, d2m = -k.q2m;
+    const T kd1 = lc_dot<T>(khp, khm, khx, khy, d1p, d1m, k.p1x, k.p1y);
+    const T kd2 = lc_dot<T>(khp, khm, khx, khy, d2p, d2m, k.p2x, k.p2y);
+    const T Xd1 = lc_dot<T>(Xp, Xm, Xx, Xy, d1p, d1m, k.p1x, k.p1y);
+    const T Xd2 = lc_dot<T>(Xp, Xm, Xx, Xy, d2p, d2m, k.p2x, k.p2y);
+    const T d12 = lc_dot<T>(d1p, d1m, k.p1x, k.p1y, d2p, d2m, k.p2x, k.p2y);
+    const T Pin1 = T(0.5) * khp * kd1 + third * T(0.5) * (Xp * Xd1 * im2 - d1p);
+    const T Pi2n = T(0.5) * khm * kd2 + third * T(0.5) * (Xm * Xd2 * im2 - d2m);
+    const T Pidd = kd2 * kd1 + third * (Xd2 * Xd1 * im2 - d12);
+    const T Pi21 = T(4) * L * L * R.pinn + T(2) * L * (Pin1 + Pi2n) + Pidd;
+    const T Pi11 = kv1 * kv1 + third * (pv1 * pv1 * im2 - b1);
+    const T Pi22 = kv2 * kv2 + third * (pv2 * pv2 * im2 - b2);
+    const T Tr   = T(4) * a * Pi21 - b2 * Pi11 - b1 * Pi22;
+    G = cscale(R2, Tr);
+  }
+  if (R0.re != T(0) || R0.im != T(0) || R1.re != T(0) || R1.im != T(0)) {
+    // q1 = (q1p, q1m, -p1T), q2 = (q2p, q2m, -p2T)
+    const T q1q2 = lc_dot<T>(k.q1p, k.q1m, -k.p1x, -k.p1y, k.q2p, k.q2m, -k.p2x, -k.p2y);
+    const T E    = lc_bivector_dot<T>(P1p, P1m, k.p1x, k.p1y, k.q1p, k.q1m, -k.p1x, -k.p1y,
+                                      k.q2p, k.q2m, -k.p2x, -k.p2y, P2p, P2m, k.p2x, k.p2y);
+    const T S0 = T(4) * a * a - b1 * b2;
+    const T S1 = T(4) * a * E + T(1.25) * b1 * b2 * q1q2;
+    G = cadd(G, cadd(cscale(R0, S0), cscale(R1, S1)));
+  }
+  // C = c(s1,t1) c(s2,t2) F1 F1 FM FM with c(s,t) = (s ap)^x e^{-i pi x/2} / (4s), x = alpha(t)-1
+  const grn_tensor_params &tp = P.tensor;
+  const T x1 = T(tp.delta_P) + T(tp.ap_P) * k.t1, x2 = T(tp.delta_P) + T(tp.ap_P) * k.t2;
+  const T mag = exp(x1 * log(s1 * T(tp.ap_P)) + x2 * log(s2 * T(tp.ap_P))) / (T(16) * s1 * s2) *
+                dirac_f1<T>(k.t1, tp.em_kelly) * dirac_f1<T>(k.t2, tp.em_kelly) /
+                ((T(1) - k.t1) * (T(1) - k.t2));
+  T sn, cs;
+  sincos_pi(T(-0.5) * (x1 + x2), sn, cs);
+  return cmul(G, cx<T>{mag * cs, mag * sn});
 }
 
 // ---------------------------------------------------------------------------
@@ -486,6 +646,7 @@ struct LoopEvent {
   T p3p, p3m, p4p, p4m;
   T a1, a2;                 // (P+ - eps)/L, (P- - eps)/L
   T invL, invL2, L, eps, mp2, m3sq, m4sq;
+  ResSums<T> res;           // PP[RESTENSOR]: resonance sums of the tree-level central mass
 };
 
 template <typename T>
@@ -521,11 +682,17 @@ GRN_HD bool loop_point_amp(const grn_process_params &P, const Consts &K, const L
     const T tx = q1x + e.p4x, ty = q1y + e.p4y;
     uhat       = dp * dm - (tx * tx + ty * ty);
   }
-  if (P.process == GRN_PROC_TENSOR_CON) {
-    const LCKin<T> kk{p1p,   p1m,   q1x,   q1y,   p2p,   p2m,   q2x,   q2y,   e.p3p, e.p3m, e.p3x,
-                      e.p3y, e.p4p, e.p4m, e.p4x, e.p4y, e.L,   e.eps, e.mp2, t1,    t2,    s13,
-                      s14,   s23,   s24,   that,  uhat};
-    A = tensor_me4_2xs<T>(P, K, kk);
+  if (P.process == GRN_PROC_TENSOR_CON || P.process == GRN_PROC_TENSOR_RES) {
+    LCKin<T> kk{p1p,   p1m,   q1x,   q1y,   p2p,   p2m,   q2x,   q2y,   e.p3p, e.p3m, e.p3x,
+                e.p3y, e.p4p, e.p4m, e.p4x, e.p4y, e.L,   e.eps, e.mp2, t1,    t2,    s13,
+                s14,   s23,   s24,   that,  uhat};
+    if (P.process == GRN_PROC_TENSOR_CON) {
+      A = tensor_me4_2xs<T>(P, K, kk);
+    } else {
+      q_lightcone<T>(x1, pt1sq, e.mp2, e.L, kk.q1p, kk.q1m);
+      q_lightcone<T>(x2, pt2sq, e.mp2, e.L, kk.q2m, kk.q2p);
+      A = tensor_me3<T>(P, K, kk, e.res);
+    }
     return true;
   }
   A = regge_me4<T>(P, K, t1, t2, log(s13), log(s14), log(s23), log(s24), that, uhat);
@@ -818,15 +985,29 @@ GRN_HD void make_loop_event(const Consts &K, const Born &b, LoopEvent<T> &e) {
   e.a2 = T((b.p3m + b.p4m - K.eps) / K.L);
   e.L = T(K.L); e.invL2 = T(1.0 / (K.L * K.L)); e.invL = T(1.0 / K.L);
   e.eps = T(K.eps); e.mp2 = T(K.mp2); e.m3sq = T(K.m3sq); e.m4sq = T(K.m4sq);
+  if (K.n_res > 0) {
+    const ResVec<double> v =
+        res_vectors<double>(K, b.p3p, b.p3m, b.p3x, b.p3y, b.p4p, b.p4m, b.p4x, b.p4y);
+    const ResSums<double> R = resonance_sums(K, b.m2, v);
+    e.res = {{T(R.R2.re), T(R.R2.im)}, {T(R.R0.re), T(R.R0.im)}, {T(R.R1.re), T(R.R1.im)},
+             T(R.pinn)};
+  } else {
+    e.res = {{T(0), T(0)}, {T(0), T(0)}, {T(0), T(0)}, T(0)};
+  }
 }
 
 // Tree-level amplitude of the configured process from the Born kinematics (FP64).
 GRN_HD cx<double> born_amp(const grn_process_params &P, const Consts &K, const Born &b) {
-  if (P.process == GRN_PROC_TENSOR_CON) {
-    const LCKin<double> k{b.p1p, b.p1m, b.p1x, b.p1y, b.p2p, b.p2m, b.p2x,  b.p2y, b.p3p,
-                          b.p3m, b.p3x, b.p3y, b.p4p, b.p4m, b.p4x, b.p4y,  K.L,   K.eps,
-                          K.mp2, b.t1,  b.t2,  b.s13, b.s14, b.s23, b.s24, b.that, b.uhat};
-    return tensor_me4_2xs<double>(P, K, k);
+  if (P.process == GRN_PROC_TENSOR_CON || P.process == GRN_PROC_TENSOR_RES) {
+    LCKin<double> k{b.p1p, b.p1m, b.p1x, b.p1y, b.p2p, b.p2m, b.p2x,  b.p2y, b.p3p,
+                    b.p3m, b.p3x, b.p3y, b.p4p, b.p4m, b.p4x, b.p4y,  K.L,   K.eps,
+                    K.mp2, b.t1,  b.t2,  b.s13, b.s14, b.s23, b.s24, b.that, b.uhat};
+    if (P.process == GRN_PROC_TENSOR_CON) return tensor_me4_2xs<double>(P, K, k);
+    q_lightcone<double>(b.x1, b.pt1sq, K.mp2, K.L, k.q1p, k.q1m);
+    q_lightcone<double>(b.x2, b.pt2sq, K.mp2, K.L, k.q2m, k.q2p);
+    const ResVec<double> v =
+        res_vectors<double>(K, b.p3p, b.p3m, b.p3x, b.p3y, b.p4p, b.p4m, b.p4x, b.p4y);
+    return tensor_me3<double>(P, K, k, resonance_sums(K, b.m2, v));
   }
   return regge_me4<double>(P, K, b.t1, b.t2, log(b.s13), log(b.s14), log(b.s23), log(b.s24),
                            b.that, b.uhat);

@@ -2,7 +2,8 @@
 
 Values are those of the generator's TUNE0 parameter set
 (modeldata/TUNE0/GENERAL.json: PARAM_SOFT 9-29, PARAM_REGGE 90-129, PARAM_PI 146-149,
-PARAM_TENSORPOM 178-201, PARAM_STRUCTURE 207-219)
+PARAM_TENSORPOM 178-201, PARAM_STRUCTURE 207-219; RES_*.json and BRANCHING.json for the
+resonances)
 and of its PDG 2018 mass/width table (modeldata/mass_width_2018.mcd). Only the
 entries the engine's processes use are carried; the layout is this package's own.
 """
@@ -31,6 +32,35 @@ TUNES = {
             "PARAM_X": {"c": [15.0, 0.0, 0.0], "n": [True, False, False]},
         },
     }
+}
+
+# Resonances of the tensor-pomeron model that decay to pseudoscalar pairs, TUNE0
+# (modeldata/TUNE0/RES_*.json: PARAM_RES M, W, J, P, g_Tensor), by the generator's names.
+RESONANCES = {
+    "TUNE0": {
+        "f0_500": dict(pdg=9000221, M=0.5, W=0.4, J=0, P=1, g_Tensor=[0.1, 0.0]),
+        "f0_980": dict(pdg=9010221, M=0.980, W=0.08, J=0, P=1, g_Tensor=[0.4, 2.0]),
+        "f0_1500": dict(pdg=9030221, M=1.506, W=0.112, J=0, P=1, g_Tensor=[0.1, 0.0]),
+        "f0_1710": dict(pdg=10331, M=1.704, W=0.123, J=0, P=1, g_Tensor=[0.45, 2.6]),
+        "f2_1270": dict(pdg=225, M=1.2755, W=0.1867, J=2, P=1,
+                        g_Tensor=[2.0, 0.0, 0.0, 0.0, 0.0, 0.0, 0.0]),
+        "f2_1525": dict(pdg=335, M=1.525, W=0.073, J=2, P=1,
+                        g_Tensor=[0.0, 0.5, 0.0, 0.0, 0.0, 0.0, 0.0]),
+        "f2_1950": dict(pdg=9050225, M=1.936, W=0.464, J=2, P=1,
+                        g_Tensor=[1.0, 0.0, 0.0, 0.0, 0.0, 0.0, 0.0]),
+    }
+}
+
+# Branching ratios of the pseudoscalar-pair decay modes (modeldata/TUNE0/BRANCHING.json),
+# by resonance PDG code and unordered daughter pair.
+BRANCHING = {
+    225: {("pi+", "pi-"): 0.562, ("K+", "K-"): 0.0227},
+    335: {("K+", "K-"): 0.4435, ("pi+", "pi-"): 0.00546},
+    9050225: {("pi+", "pi-"): 1.0},
+    9010221: {("pi+", "pi-"): 0.5, ("K+", "K-"): 0.345},
+    9030221: {("pi+", "pi-"): 0.2299, ("K+", "K-"): 0.0425},
+    10331: {("K+", "K-"): 0.18, ("pi+", "pi-"): 0.0552},
+    9000221: {("pi+", "pi-"): 1.0, ("K+", "K-"): 0.01},
 }
 
 # name -> (pdg, mass GeV, width GeV, coupling class)

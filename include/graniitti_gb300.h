@@ -52,8 +52,12 @@ enum {
 /* Process kinds: the PROC_k wrappers of MSubProc.h the engine implements. */
 enum {
   GRN_PROC_REGGE_CON  = 1, /* "PP[CON]<C|F> -> a b", 2-body, MRegge::ME4 (MSubProc.h:361-380) */
-  GRN_PROC_TENSOR_CON = 2  /* "PP[CONTENSOR]<C|F> -> a b", 2 pseudoscalars, tensor-pomeron
+  GRN_PROC_TENSOR_CON = 2, /* "PP[CONTENSOR]<C|F> -> a b", 2 pseudoscalars, tensor-pomeron
                               MTensorPomeron::ME4 "2xS" (MSubProc.h:288-300) */
+  GRN_PROC_TENSOR_RES = 3  /* "PP[RESTENSOR]<F|C> -> a b", 2 pseudoscalars: coherent sum of
+                              tensor-pomeron resonances, MTensorPomeron::ME3 (MSubProc.h:
+                              278-285; src/MTensorPomeron.cc:164-565), J = 0 (P = +1) and
+                              J = 2 with the pseudoscalar-pair decay */
 };
 
 /* Phase-space classes (MProcess subclasses). */
@@ -96,6 +100,18 @@ typedef struct grn_tensor_params { /* MTensorPomeronParam, include/Graniitti/MTe
   int32_t _pad;
 } grn_tensor_params;
 
+/* One resonance of PP[RESTENSOR]: PARAM_RES (src/MForm.cc:250-340) and the decay
+ * coupling of its pseudoscalar-pair mode (HELMatrix::g_decay_tensor[0]). */
+#define GRN_MAX_RESONANCES 4
+typedef struct grn_resonance {
+  int32_t J;           /* spin: 0 or 2 */
+  int32_t P;           /* parity: +1 (J = 0 with P = -1 decays to photon or vector pairs) */
+  double  M, W;        /* peak mass and full width [GeV] (the BW propagators use W fixed) */
+  double  g_tensor[7]; /* production couplings g_Tensor: [0], [1] for J = 0 (structures
+                          iG_PPS_0, iG_PPS_1); [0] for J = 2 (iG_PPT_00; [1..6] must be 0) */
+  double  g_decay;     /* decay coupling, grn_tensor_decay_coupling() unless the model gives it */
+} grn_resonance;
+
 typedef struct grn_gencuts { /* GENCUT, include/Graniitti/MKinematics.h:1554-1576 */
   double rap_min, rap_max;       /* <C> final-state rapidity window */
   double kt_min, kt_max;         /* <C> intermediate kt (post_Constructor default 10/Kf) */
@@ -136,11 +152,21 @@ typedef struct grn_process_params {
   grn_regge_params  regge;   /* also the off-shell meson form factor of the tensor model */
   grn_loop_numerics loop;
   grn_tensor_params tensor;
+  int32_t           n_res;   /* GRN_PROC_TENSOR_RES: resonances in the coherent sum (1..4) */
+  int32_t           _pad_res;
+  grn_resonance     res[GRN_MAX_RESONANCES];
 } grn_process_params;
 
 /* Fill every field with the reference defaults for "PP[CON]<C> -> pi+ pi-" at
  * sqrt(s) = 13 TeV, TUNE0 (modeldata/TUNE0/GENERAL.json), cuts as documented. */
 void grn_default_params(grn_process_params *p);
+
+/* Decay coupling of a spin-J resonance (mass M, full width W) to two pseudoscalars of mass
+ * m_daughter with branching ratio BR: MTensorPomeron::GDecay (src/MTensorPomeron.cc:134-156)
+ * with the threshold retry of MProcess::ProcessHelicityDecay (src/MProcess.cc:683-703): when
+ * M is below 2 m_daughter the coupling is taken at M + i W, i = 1, 2, 3, the first one above
+ * threshold. Returns NaN for J other than 0, 1, 2. */
+double grn_tensor_decay_coupling(int32_t J, double M, double W, double m_daughter, double BR);
 
 /* ------------------------------------------------------------------------ */
 /* Engine lifetime                                                            */

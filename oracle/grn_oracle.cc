@@ -507,6 +507,153 @@ cplx tensor_me4_2xs(const Setup &S, const Event &ev) {
   return cplx(0, -1) * (Mt + Mu);
 }
 
+// ---------------------------------------------------------------------------
+// Tensor-pomeron resonances decaying to two pseudoscalars (MTensorPomeron::ME3,
+// src/MTensorPomeron.cc:164-565), restated with explicit Lorentz-index sums in the
+// reference's own order: rank-6 pomeron-pomeron-tensor vertex, tensor propagator,
+// decay vertex, pomeron propagators and proton vertices, contracted as plain sums over
+// index values (the reference's tensors carry the index positions that make these
+// sums Lorentz contractions).
+inline double gm(int u, int v) { return u == v ? G_METRIC[u] : 0.0; }
+inline double up(const V4 &p, int u) { return u == 0 ? p.e : (u == 1 ? p.x : (u == 2 ? p.y : p.z)); }
+inline double dn(const V4 &p, int u) { return u == 0 ? p.e : -up(p, u); }
+inline int    i6(int u, int v, int k, int l, int r, int s) {
+  return ((((u * 4 + v) * 4 + k) * 4 + l) * 4 + r) * 4 + s;
+}
+
+// Auxiliary tensor R_{abcd} = g_ac g_bd / 2 + g_ad g_bc / 2 + g_ab g_cd / 4 with the sign of
+// the last term as MTensorPomeron::CalcRTensor sets it (src/MTensorPomeron.cc:2563-2564).
+double R_dddd(int a, int b, int c, int d) {
+  return 0.5 * gm(a, c) * gm(b, d) + 0.5 * gm(a, d) * gm(b, c) + 0.25 * gm(a, b) * gm(c, d);
+}
+
+// Coupling structure #0 of the pomeron-pomeron-tensor vertex, kinematics independent:
+// 2 i S0 R_{uv,s1 v1} R_{kl,v1 l1} R_{rs,l1 s1} with the three contractions carried by
+// metric factors (iG_PPT_00, src/MTensorPomeron.cc:1701-1731).
+const std::vector<cplx> &ppt_structure0() {
+  static const std::vector<cplx> T = [] {
+    std::vector<cplx> t(4096, cplx(0, 0));
+    const cplx f(0, 2.0);
+    for (int u = 0; u < 4; ++u)
+      for (int v = 0; v < 4; ++v)
+        for (int k = 0; k < 4; ++k)
+          for (int l = 0; l < 4; ++l)
+            for (int r = 0; r < 4; ++r)
+              for (int s = 0; s < 4; ++s) {
+                cplx sum(0, 0);
+                for (int v1 = 0; v1 < 4; ++v1)
+                  for (int l1 = 0; l1 < 4; ++l1)
+                    for (int s1 = 0; s1 < 4; ++s1)
+                      sum += f * R_dddd(u, v, s1, v1) * R_dddd(k, l, v1, l1) *
+                             R_dddd(r, s, l1, s1) * G_METRIC[v1] * G_METRIC[l1] * G_METRIC[s1];
+                t[i6(u, v, k, l, r, s)] = sum;
+              }
+    return t;
+  }();
+  return T;
+}
+
+// Resonance form factor exp(-(q^2 - M0^2)^2 / Lambda^4) (MTensorPomeron::F, :2489) and the
+// pion-electromagnetic-type FM(q^2) = 1 / (1 - q^2 / Lambda^2) with Lambda^2 = 1 (:2485).
+double ff_res(double q2, double M0) { return std::exp(-sq(q2 - M0 * M0)); }
+double ff_M(double q2) { return 1.0 / (1.0 - q2 / 1.0); }
+
+cplx tensor_me3(const Setup &S, const Event &ev) {
+  const grn_process_params &p = S.p;
+  const V4 &pa = S.pb1, &pb = S.pb2;
+  const V4 &p1 = ev.pf[1], &p2 = ev.pf[2], &p3 = ev.pf[3], &p4 = ev.pf[4];
+  const V4 &X  = ev.pf[0];
+  const V4  q1 = pa - p1, q2 = pb - p2;
+  // X1^{ab} = iG_1a(mu, nu) iDP_1(mu, nu, a, b), X2 likewise (pomeron propagators iD_P(s_i,
+  // t_i) with s_i = (p_i + X)^2, src/MTensorPomeron.cc:196-197, 2288-2298)
+  const T2   G1a = vertex_ppP(p, p1, pa);
+  const T2   G2b = vertex_ppP(p, p2, pb);
+  const cplx c1  = pomeron_prop(p, ev.ss[1][0], ev.t1);
+  const cplx c2  = pomeron_prop(p, ev.ss[2][0], ev.t2);
+  cplx X1[4][4], X2[4][4];
+  for (int a = 0; a < 4; ++a)
+    for (int b = 0; b < 4; ++b) {
+      cplx s1(0, 0), s2(0, 0);
+      for (int u = 0; u < 4; ++u)
+        for (int v = 0; v < 4; ++v) {
+          const double g = gm(u, a) * gm(v, b) + gm(u, b) * gm(v, a) - 0.5 * gm(u, v) * gm(a, b);
+          if (g == 0.0) continue;
+          s1 += G1a.c[u][v] * g;
+          s2 += G2b.c[u][v] * g;
+        }
+      X1[a][b] = c1 * s1;
+      X2[a][b] = c2 * s2;
+    }
+  const double m2   = X.m2();
+  const double Ft   = ff_M(q1.m2()) * ff_M(q2.m2());  // times F((q1+q2)^2, M0) per resonance
+  const V4     q12  = q1 + q2;
+  cplx         A(0, 0);
+  for (int r = 0; r < p.n_res; ++r) {
+    const grn_resonance &R = p.res[r];
+    const double F_tilde   = Ft * ff_res(q12.m2(), R.M);
+    const cplx   Delta     = 1.0 / cplx(m2 - R.M * R.M, R.M * R.W);
+    cplx cvtx[4][4][4][4];
+    if (R.J == 2) {
+      // tensor propagator, upper indices (iD_TMES, :2422-2446) x decay vertex (iG_f2psps,
+      // :2121-2137), then the rank-6 vertex (iG_PPT_total, :1646-1692; only #0 is used)
+      auto ghat = [&](int u, int v) { return -gm(u, v) + up(X, u) * up(X, v) / m2; };
+      const V4   k   = p3 - p4;
+      const cplx fd  = cplx(0, -1) * R.g_decay / 2.0 * ff_res((p3 + p4).m2(), R.M);
+      const double k2 = k.m2();
+      cplx dec[4][4];
+      for (int u = 0; u < 4; ++u)
+        for (int v = 0; v < 4; ++v) dec[u][v] = fd * (dn(k, u) * dn(k, v) - 0.25 * gm(u, v) * k2);
+      cplx D[4][4];
+      for (int u = 0; u < 4; ++u)
+        for (int v = 0; v < 4; ++v) {
+          cplx sum(0, 0);
+          for (int a = 0; a < 4; ++a)
+            for (int b = 0; b < 4; ++b)
+              sum += cplx(0, 1) * Delta *
+                     (0.5 * (ghat(u, a) * ghat(v, b) + ghat(u, b) * ghat(v, a)) -
+                      1.0 / 3.0 * ghat(u, v) * ghat(a, b)) *
+                     dec[a][b];
+          D[u][v] = sum;
+        }
+      const std::vector<cplx> &G0 = ppt_structure0();
+      const double             g0 = R.g_tensor[0] * F_tilde;
+      for (int u = 0; u < 4; ++u)
+        for (int v = 0; v < 4; ++v)
+          for (int k_ = 0; k_ < 4; ++k_)
+            for (int l = 0; l < 4; ++l) {
+              cplx sum(0, 0);
+              for (int a = 0; a < 4; ++a)
+                for (int b = 0; b < 4; ++b) sum += G0[i6(u, v, k_, l, a, b)] * g0 * D[a][b];
+              cvtx[u][v][k_][l] = sum;
+            }
+    } else {
+      // scalar: (g0 iG_PPS_0 + iG_PPS_1) F_tilde (:1492-1571) x iD_MES (:2383-2387) x
+      // iG_f0ss (:2028-2038)
+      const double q1q2 = q1.e * q2.e - (q1.x * q2.x + q1.y * q2.y + q1.z * q2.z);
+      const cplx   f1   = cplx(0, 1) * R.g_tensor[1] / 2.0;
+      const cplx   tail = cplx(0, 1) * Delta * cplx(0, 1) * R.g_decay * ff_res((p3 + p4).m2(), R.M);
+      for (int u = 0; u < 4; ++u)
+        for (int v = 0; v < 4; ++v)
+          for (int k_ = 0; k_ < 4; ++k_)
+            for (int l = 0; l < 4; ++l) {
+              const double gg = gm(u, k_) * gm(v, l) + gm(u, l) * gm(v, k_);
+              const cplx   t0 = cplx(0, 1) * (gg - 0.5 * gm(u, v) * gm(k_, l));
+              const cplx   t1 = f1 * (dn(q1, k_) * dn(q2, u) * gm(v, l) + dn(q1, k_) * dn(q2, v) * gm(u, l) +
+                                    dn(q1, l) * dn(q2, u) * gm(v, k_) + dn(q1, l) * dn(q2, v) * gm(u, k_) -
+                                    2.0 * q1q2 * gg);
+              cvtx[u][v][k_][l] = (R.g_tensor[0] * t0 + t1) * F_tilde * tail;
+            }
+    }
+    cplx sum(0, 0);
+    for (int a = 0; a < 4; ++a)
+      for (int b = 0; b < 4; ++b)
+        for (int c = 0; c < 4; ++c)
+          for (int d = 0; d < 4; ++d) sum += X1[a][b] * cvtx[a][b][c][d] * X2[c][d];
+    A += cplx(0, -1) * sum;
+  }
+  return A;
+}
+
 // Bare amplitude of the configured process.
 cplx bare_amp(const Setup &S, const Event &ev);
 
@@ -552,6 +699,7 @@ double screened_amp2(const Setup &S, const Event &born, const cplx &A0) {
 }
 
 cplx bare_amp(const Setup &S, const Event &ev) {
+  if (S.p.process == GRN_PROC_TENSOR_RES) return tensor_me3(S, ev);
   return S.p.process == GRN_PROC_TENSOR_CON ? tensor_me4_2xs(S, ev) : regge_me4(S, ev);
 }
 

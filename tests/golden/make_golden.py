@@ -8,7 +8,7 @@ reference does not. Steps:
   3. build the eikonal tables with the reference's MEikonal::S3Constructor
   4. run the reference VEGAS integration for the cross section
 
-Usage: python tests/golden/make_golden.py [--ref /root/reference]
+Usage: python tests/golden/make_golden.py [--ref /root/reference] [--only resonances]
 """
 import argparse
 import json
@@ -54,12 +54,61 @@ def save(name, **arrays):
     print("wrote", name)
 
 
+CARD_RES = os.path.join(HERE, "cards", "pp_res_pipi.json")
+CARD_RES_SCR = os.path.join(HERE, "cards", "pp_res_pipi_screened.json")
+
+
+def resonance_fixtures():
+    """Tensor-pomeron resonances (PROC_11, MTensorPomeron::ME3): f2(1270) alone, four
+    resonances with an @R override, the K+ K- decay (f0(980) below threshold), the <C>
+    class, and the screened amplitude."""
+    REPLAY_F = ["--replay", "h,h,6,7"]
+    cases = [
+        ("rf_tree_weights.npz", 61, 2048, CARD_RES, "PP[RESTENSOR]<F> -> pi+ pi-", REPLAY_F, 6),
+        ("rf_mix_tree_weights.npz", 62, 1024, CARD_RES,
+         "PP[RESTENSOR]<F> -> pi+ pi- @RES{f0_980:1, f2_1270:1, f0_1500:1, f0_1710:1} "
+         "@R[f2_1270]{M:1.3, W:0.2, g0:1.5}", REPLAY_F, 6),
+        ("rf_kk_tree_weights.npz", 63, 512, CARD_RES,
+         "PP[RESTENSOR]<F> -> K+ K- @RES{f0_980:1, f2_1270:1}", REPLAY_F, 6),
+        ("rc_tree_weights.npz", 64, 1024, CARD_RES,
+         "PP[RESTENSOR]<C> -> pi+ pi- @RES{f0_980:1, f2_1270:1}", [], 8),
+    ]
+    for name, seed, n, card, proc, extra, dim in cases:
+        u = philox_np.uniforms(seed, n, 8)
+        r = run_weights(card, u, extra, proc=proc, dim=dim)
+        save(name, seed=seed, u=u, card=os.path.basename(card), proc=proc, **r)
+    proc = "PP[RESTENSOR]<F> -> pi+ pi- @RES{f0_980:1, f2_1270:1}"
+    u = philox_np.uniforms(65, 96, 8)
+    r = run_weights(CARD_RES_SCR, u, REPLAY_F + ["--nbt", "1024", "--nkt2", "10000"], proc=proc,
+                    dim=6)
+    save("rf_screened_15x12_weights.npz", seed=65, u=u, card=os.path.basename(CARD_RES_SCR),
+         proc=proc, n_bt=1024, n_kt2=10000, loop_kt=15, loop_phi=12, loop_ktmax=1.75, **r)
+    # VEGAS cross section of the f2(1270) card (reference ranlux48 points, 8 threads).
+    out = subprocess.run([REF_BIN, "vegas", CARD_RES, "PP[RESTENSOR]<F> -> pi+ pi-", "--cores",
+                          "8"], check=True, capture_output=True, text=True).stdout
+    write_sigma("rf_vegas_sigma.json", out, "PP[RESTENSOR]<F> -> pi+ pi-",
+                os.path.basename(CARD_RES))
+
+
+def write_sigma(name, out, proc, card):
+    line = [l for l in out.splitlines() if l.startswith("RESULT")][-1]
+    sigma, err = map(float, line.split()[1:3])
+    with open(os.path.join(HERE, name), "w") as f:
+        json.dump({"process": proc, "card": card, "sigma_barn": sigma, "sigma_err_barn": err,
+                   "ncall": 100000, "iter": 5, "precision": 0.001}, f, indent=1)
+    print(name, "sigma", sigma, "+-", err)
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--ref", default="/root/reference")
+    ap.add_argument("--only", choices=["all", "resonances"], default="all")
     a = ap.parse_args()
     subprocess.check_call(["make", "-s", "-C", os.path.join(REPO, "oracle", "refbuild"), "-j8",
                            "REF=" + a.ref])
+    resonance_fixtures()
+    if a.only == "resonances":
+        return
 
     # c1: tree-level weights, TUNE0 (power-law off-shell form factor) and the
     # exponential form-factor variant.

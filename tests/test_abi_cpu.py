@@ -62,12 +62,14 @@ def test_create_without_device_fails_cleanly(lib_built):
     assert st == _abi.GRN_ERR_NO_DEVICE and not h.value
 
 
-STRUCTS = ["grn_soft_params", "grn_regge_params", "grn_tensor_params", "grn_gencuts",
+STRUCTS = ["grn_soft_params", "grn_regge_params", "grn_tensor_params", "grn_resonance",
+           "grn_gencuts",
            "grn_fidcuts", "grn_loop_numerics", "grn_process_params", "grn_vegas_params",
            "grn_vegas_result", "grn_flat_params", "grn_flow_params", "grn_flow_train_params",
            "grn_flow_train_result", "grn_tuning", "grn_tune_result"]
 MIRROR = {"grn_soft_params": "SoftParams", "grn_regge_params": "ReggeParams",
-          "grn_tensor_params": "TensorParams", "grn_gencuts": "GenCuts", "grn_fidcuts": "FidCuts",
+          "grn_tensor_params": "TensorParams", "grn_resonance": "Resonance",
+          "grn_gencuts": "GenCuts", "grn_fidcuts": "FidCuts",
           "grn_loop_numerics": "LoopNumerics", "grn_process_params": "ProcessParams",
           "grn_vegas_params": "VegasParams", "grn_vegas_result": "VegasResult",
           "grn_flat_params": "FlatParams", "grn_flow_params": "FlowParams",

@@ -47,6 +47,56 @@ def test_tensor_params():
     assert PK.tensor.gPps == 1.54
 
 
+def test_split_commands():
+    cmds = card.split_commands("PP[RESTENSOR]<F> -> pi+ pi- @RES{f0_980:1, f2_1270:true} "
+                               "@R[f2_1270]{g0:1.5, M:1.3} @OFFSHELL:0 @FLAG")
+    assert cmds == [("RES", [], {"f0_980": "1", "f2_1270": "true"}),
+                    ("R", ["f2_1270"], {"g0": "1.5", "M": "1.3"}),
+                    ("OFFSHELL", [], {"_SINGLET_": "0"}), ("FLAG", [], {"_SINGLET_": "true"})]
+    with pytest.raises(ValueError):
+        card.split_commands("X -> a b @R[f2{g0:1}")
+
+
+# Decay couplings the reference prints for these resonances ("Tensor Pomeron decay
+# couplings", MProcess::ProcessHelicityDecay): f2(1270) -> pi+ pi- 9.285, f0(980) -> pi+ pi-
+# 1.434, f0(980) -> K+ K- 2.010 (below threshold: taken at M + W), f2(1270) -> K+ K- 5.503,
+# f2 with @R{M:1.3, W:0.2} -> pi+ pi- 9.317.
+def test_resonance_params_and_decay_couplings(lib_built):
+    from conftest import GOLDEN
+    import os
+    c = card.read_card(os.path.join(GOLDEN, "cards", "pp_res_pipi.json"))
+    P = card.build_params(c)
+    assert P.process == 3 and P.phase_space == 2 and P.n_res == 1
+    r = P.res[0]
+    assert (r.J, r.P, r.M, r.W, r.g_tensor[0]) == (2, 1, 1.2755, 0.1867, 2.0)
+    assert round(r.g_decay, 3) == 9.285
+    P = card.build_params(c, "PP[RESTENSOR]<F> -> K+ K- @RES{f0_980:1, f2_1270:1}")
+    assert [round(P.res[i].g_decay, 3) for i in range(2)] == [2.010, 5.503]
+    P = card.build_params(c, "PP[RESTENSOR]<F> -> pi+ pi- @RES{f0_980:1, f2_1270:1} "
+                             "@R[f2_1270]{M:1.3, W:0.2, g0:1.5}")
+    assert [round(P.res[i].g_decay, 3) for i in range(2)] == [1.434, 9.317]
+    assert (P.res[1].M, P.res[1].W, P.res[1].g_tensor[0]) == (1.3, 0.2, 1.5)
+    assert (P.res[0].J, P.res[0].g_tensor[0], P.res[0].g_tensor[1]) == (0, 0.4, 2.0)
+    from graniitti_gb300 import _abi
+    lib = _abi.load_library()
+    assert lib.grn_tensor_decay_coupling(4, 2.6, 0.1, 0.14, 1.0) == 1.0
+    assert lib.grn_tensor_decay_coupling(3, 2.6, 0.1, 0.14, 1.0) != \
+        lib.grn_tensor_decay_coupling(3, 2.6, 0.1, 0.14, 1.0)  # NaN
+
+
+@pytest.mark.parametrize("proc", [
+    "PP[RESTENSOR]<F> -> pi+ pi- @RES{f2_1525:1}",       # coupling structure g1 (J = 2)
+    "PP[RESTENSOR]<F> -> pi+ pi- @RES{rho_770:1}",       # no pseudoscalar-pair resonance
+    "PP[RESTENSOR]<F> -> pi0 pi0 @RES{f2_1270:1}",
+    "PP[RESTENSOR]<F> -> pi+ pi- @RES{f0_500:1, f0_980:1, f0_1500:1, f0_1710:1, f2_1270:1}"])
+def test_unsupported_resonances_are_rejected(lib_built, proc):
+    from conftest import GOLDEN
+    import os
+    c = card.read_card(os.path.join(GOLDEN, "cards", "pp_res_pipi.json"))
+    with pytest.raises(card.UnsupportedProcess):
+        card.build_params(c, proc)
+
+
 @pytest.mark.parametrize("proc", ["PP[RES]<C> -> pi+ pi-", "PP[CON]<Q> -> pi+ pi-",
                                   "PP[CON]<C> -> pi+ pi- pi+ pi-", "yy[CON]<C> -> mu+ mu-"])
 def test_unsupported_processes_are_rejected(proc):

@@ -1,0 +1,154 @@
+"""Tensor-pomeron resonances (PP[RESTENSOR], MTensorPomeron::ME3) on the GPU through the C ABI:
+FP64 weights against the reference's golden vectors and the CPU oracle, the FP32 kt-loop
+against FP64, the cross section against the reference's VEGAS, and parameter validation."""
+import ctypes
+import json
+import os
+
+import numpy as np
+import pytest
+
+from conftest import GOLDEN
+from oracle import oracle_api as orc
+from test_gpu_parity import _mixed_ok
+
+pytestmark = pytest.mark.gpu
+
+# The tensor amplitude has zeros in the decay angle where the reference's Cartesian
+# contractions lose relative precision (a few points at 1e-9, median 2e-11); the GPU's
+# light-cone contraction is the more accurate of the two.
+RES_TOL = 5e-9
+
+
+def _load(name):
+    return np.load(os.path.join(GOLDEN, name))
+
+
+def _params(g):
+    from graniitti_gb300 import card
+    return card.build_params(card.read_card(os.path.join(GOLDEN, "cards", str(g["card"]))),
+                             str(g["proc"]))
+
+
+def _engine(P):
+    import graniitti_gb300 as g
+    return g.Engine(P, 0)
+
+
+def _rel(w, wr):
+    nz = wr > 0
+    assert np.array_equal(w > 0, nz)
+    return np.abs(w[nz] - wr[nz]) / wr[nz]
+
+
+@pytest.mark.parametrize("name", ["rf_tree_weights.npz", "rf_mix_tree_weights.npz",
+                                  "rf_kk_tree_weights.npz", "rc_tree_weights.npz"])
+def test_resonance_tree_vs_reference(gpu, name):
+    import graniitti_gb300 as g
+    gl = _load(name)
+    P = _params(gl)
+    e = _engine(P)
+    w, fl = e.event_weights(gl["u"], prec=g.FP64)
+    wo, flo = orc.weights(P, gl["u"])
+    assert np.array_equal(fl, flo) and np.array_equal(fl & 1, gl["kin"])
+    kin = gl["kin"] == 1
+    assert np.array_equal(((fl >> 1) & 1)[kin], gl["fid"][kin])
+    r = _rel(w, gl["w"])
+    print("%s: GPU vs reference max rel %.2e, median %.2e" % (name, r.max(), np.median(r)))
+    assert r.max() < RES_TOL and np.median(r) < 1e-10
+    assert _rel(w, wo).max() < RES_TOL
+    # tree-level weights do not depend on the loop precision
+    wm, _ = e.event_weights(gl["u"], prec=g.MIXED)
+    assert np.array_equal(wm, w)
+
+
+def test_resonance_screened_vs_reference(gpu):
+    import graniitti_gb300 as g
+    gl = _load("rf_screened_15x12_weights.npz")
+    t = _load("eikonal_nbt1024_nkt10000.npz")
+    P = _params(gl)
+    assert P.screening == 1
+    e = _engine(P)
+    e.eikonal_set(t["mbt"], t["msa"])
+    w, fl = e.event_weights(gl["u"], prec=g.FP64)
+    assert np.array_equal(fl & 1, gl["kin"])
+    r = _rel(w, gl["w"])
+    print("screened resonances: GPU FP64 vs reference max rel %.2e" % r.max())
+    assert r.max() < RES_TOL
+    wm, _ = e.event_weights(gl["u"], prec=g.MIXED)
+    Pb = type(P)()
+    ctypes.memmove(ctypes.byref(Pb), ctypes.byref(P), ctypes.sizeof(P))
+    Pb.screening = 0
+    wb, _ = _engine(Pb).event_weights(gl["u"], prec=g.FP64)
+    ok, rel = _mixed_ok(wm, w, wb)
+    print("screened resonances: mixed vs fp64 max rel %.3e" % rel.max())
+    assert ok, rel.max()
+    # screening suppresses the resonance on average
+    nz = wb > 0
+    assert np.sum(w[nz]) < np.sum(wb[nz])
+
+
+def test_resonance_mixed_loop_vs_fp64_many_points(gpu):
+    """FP32 kt-loop of the resonance amplitude against the FP64 loop on 4096 points of the
+    screened f0(980) + f2(1270) process (tables built on the device)."""
+    import graniitti_gb300 as g
+    import philox_np
+    gl = _load("rf_screened_15x12_weights.npz")
+    P = _params(gl)
+    e = _engine(P)
+    e.eikonal_build()
+    u = philox_np.uniforms(66, 4096, 8)
+    w64, fl = e.event_weights(u, prec=g.FP64)
+    wm, flm = e.event_weights(u, prec=g.MIXED)
+    assert np.array_equal(fl, flm)
+    Pb = type(P)()
+    ctypes.memmove(ctypes.byref(Pb), ctypes.byref(P), ctypes.sizeof(P))
+    Pb.screening = 0
+    wb, _ = _engine(Pb).event_weights(u, prec=g.FP64)
+    ok, rel = _mixed_ok(wm, w64, wb)
+    print("resonance mixed vs fp64 (4096 points): max rel %.3e, median %.3e" %
+          (rel.max(), np.median(rel)))
+    assert ok, rel.max()
+
+
+def test_resonance_cross_section_vs_reference_vegas(gpu):
+    """Integrated f2(1270) -> pi+ pi- cross section against the reference's own VEGAS run."""
+    import graniitti_gb300 as g
+    from graniitti_gb300 import _abi, card
+    ref = json.load(open(os.path.join(GOLDEN, "rf_vegas_sigma.json")))
+    P = card.build_params(card.read_card(os.path.join(GOLDEN, "cards", ref["card"])))
+    e = g.Engine(P, 0)
+    vp = _abi.VegasParams()
+    vp.bins, vp.iter, vp.ncall, vp.lambda_ = 128, 8, 1 << 21, 1.5
+    vp.chi2max, vp.precision, vp.burnin_iter, vp.prec, vp.seed = 10.0, 2e-4, 3, 0, 21
+    r = e.vegas_integrate(vp)
+    pull = (r.sigma - ref["sigma_barn"]) / np.hypot(r.sigma_err, ref["sigma_err_barn"])
+    print("sigma f2(1270): GPU %.5e +- %.1e, reference %.5e +- %.1e, pull %.2f" %
+          (r.sigma, r.sigma_err, ref["sigma_barn"], ref["sigma_err_barn"], pull))
+    assert abs(pull) < 4
+
+
+def test_resonance_parameter_validation(gpu):
+    import graniitti_gb300 as g
+    from graniitti_gb300 import _abi
+    gl = _load("rf_tree_weights.npz")
+    P = _params(gl)
+    lib = _abi.load_library()
+
+    def status(mod):
+        Q = type(P)()
+        ctypes.memmove(ctypes.byref(Q), ctypes.byref(P), ctypes.sizeof(P))
+        mod(Q)
+        h = ctypes.c_void_p()
+        st = lib.grn_create(ctypes.byref(Q), 0, ctypes.byref(h))
+        if h.value:
+            lib.grn_destroy(h)
+        return st
+
+    assert status(lambda Q: None) == _abi.GRN_OK
+    assert status(lambda Q: setattr(Q, "n_res", 0)) == _abi.GRN_ERR_INVALID
+    assert status(lambda Q: setattr(Q, "n_res", 5)) == _abi.GRN_ERR_INVALID
+    assert status(lambda Q: Q.res[0].g_tensor.__setitem__(1, 0.5)) == _abi.GRN_ERR_UNSUPPORTED
+    assert status(lambda Q: setattr(Q.res[0], "J", 1)) == _abi.GRN_ERR_UNSUPPORTED
+    assert status(lambda Q: setattr(Q.res[0], "M", -1.0)) == _abi.GRN_ERR_INVALID
+    assert status(lambda Q: Q.m_central.__setitem__(1, 0.2)) == _abi.GRN_ERR_UNSUPPORTED

@@ -149,3 +149,33 @@ def test_tensor_pomeron_screened_weights():
     w, fl = orc.weights(_params("PP[CONTENSOR]<C> -> pi+ pi-", True), g["u"], msa=t["msa"],
                         nthreads=4)
     _check_weights(w, fl, g, tol=1e-9)
+
+
+# Tensor-pomeron resonances (PROC_11, MTensorPomeron::ME3): the fixtures carry their card and
+# process string (with the @RES / @R commands the reference parsed).
+def _params_res(g):
+    from graniitti_gb300 import card
+    return card.build_params(card.read_card(os.path.join(GOLDEN, "cards", str(g["card"]))),
+                             str(g["proc"]))
+
+
+# The tensor amplitude has zeros in the decay angle; near them the reference's Cartesian
+# contractions of 13 TeV 4-vectors (and the oracle's) lose relative precision, which puts
+# a few points at 1e-9 while the median stays at 2e-11.
+RES_TOL = 5e-9
+
+
+@pytest.mark.parametrize("name", ["rf_tree_weights.npz", "rf_mix_tree_weights.npz",
+                                  "rf_kk_tree_weights.npz", "rc_tree_weights.npz"])
+def test_tensor_resonance_tree_weights(lib_built, name):
+    g = _load(name)
+    w, fl = orc.weights(_params_res(g), g["u"])
+    rel = _check_weights(w, fl, g, tol=RES_TOL)
+    assert np.median(rel) < 1e-10
+
+
+def test_tensor_resonance_screened_weights(lib_built):
+    g = _load("rf_screened_15x12_weights.npz")
+    t = _load("eikonal_nbt1024_nkt10000.npz")
+    w, fl = orc.weights(_params_res(g), g["u"], msa=t["msa"], nthreads=4)
+    _check_weights(w, fl, g, tol=1e-9)
