@@ -57,7 +57,7 @@ class ReggeParams(ctypes.Structure):
 
 class TensorParams(ctypes.Structure):
     _fields_ = [("delta_P", c_double), ("ap_P", c_double), ("gPNN", c_double), ("gPps", c_double),
-                ("em_kelly", c_int32), ("_pad", c_int32)]
+                ("em_kelly", c_int32), ("_pad", c_int32), ("gPvv", c_double * 2)]
 
 
 class GenCuts(ctypes.Structure):
@@ -90,7 +90,9 @@ class ProcessParams(ctypes.Structure):
                 ("gcuts", GenCuts), ("fcuts", FidCuts), ("soft", SoftParams),
                 ("regge", ReggeParams), ("loop", LoopNumerics), ("tensor", TensorParams),
                 ("n_res", c_int32), ("_pad_res", c_int32),
-                ("res", Resonance * GRN_MAX_RESONANCES)]
+                ("res", Resonance * GRN_MAX_RESONANCES),
+                ("n_decay", c_int32), ("central_spin", c_int32), ("width", c_double * 2),
+                ("m_daughter", c_double * 4)]
 
 
 class VegasParams(ctypes.Structure):

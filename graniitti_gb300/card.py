@@ -11,7 +11,7 @@ import math
 import re
 
 from . import _abi
-from .modeldata import BRANCHING, PARTICLES, RESONANCES, TUNES
+from .modeldata import BRANCHING, PARTICLES, RESONANCES, SPIN, TUNES, VECTOR_COUPLING
 
 _PROC_RE = re.compile(r"^\s*([A-Za-z]+)\[([A-Z+]+)\]<([A-Z])>\s*$")
 
@@ -107,8 +107,37 @@ def parse_process(proc):
     m = _PROC_RE.match(left)
     if not m:
         raise ValueError("cannot parse process %r" % left)
-    finals = right.split()
+    finals = [name for name, _ in decay_tree(right)]
     return m.group(1), m.group(2), m.group(3), finals, opts
+
+
+def decay_tree(text):
+    """'rho(770)0 > {pi+ pi-} rho(770)0 > {pi+ pi-}' -> [(name, [daughters]), ...], the
+    decay syntax of the process string (MProcess::SetDecayMode, src/MProcess.cc:355-440)."""
+    toks = text.replace("{", " { ").replace("}", " } ").split()
+
+    def items(i, closing):
+        out = []
+        while i < len(toks):
+            t = toks[i]
+            if t == "}":
+                if not closing:
+                    raise ValueError("unbalanced '}' in %r" % text)
+                return out, i + 1
+            if t in (">", "{"):
+                raise ValueError("decay syntax error at %r in %r" % (t, text))
+            name, i = t, i + 1
+            kids = []
+            if i < len(toks) and toks[i] == ">":
+                if i + 1 >= len(toks) or toks[i + 1] != "{":
+                    raise ValueError("'>' must be followed by '{...}' in %r" % text)
+                kids, i = items(i + 2, True)
+            out.append((name, kids))
+        if closing:
+            raise ValueError("unbalanced '{' in %r" % text)
+        return out, i
+
+    return items(0, False)[0]
 
 
 class UnsupportedProcess(ValueError):
@@ -126,12 +155,30 @@ def build_params(card, process=None, tune=None):
     T = TUNES[tune]
     proc = process or pp["PROCESS"]
     istate, channel, cls, finals, _ = parse_process(proc)
+    tree = decay_tree(proc.split("@")[0].split("->", 1)[1])
+    casc = [kids for _, kids in tree]
+    if any(casc):
+        # two-body cascades "a > {c d} b > {e f}" of both central particles (<F>)
+        if not (all(len(k) == 2 and all(not g for _, g in k) for k in casc) and len(casc) == 2):
+            raise UnsupportedProcess("decay trees: both central particles decay to two stable "
+                                     "particles")
+        if cls != "F":
+            raise UnsupportedProcess("decay cascades are implemented in the <F> class")
+        if channel == "RESTENSOR":
+            raise UnsupportedProcess("RESTENSOR decays directly to two pseudoscalars")
+    elif any(f in PARTICLES and PARTICLES[f][2] > 1e-6 for f in finals):
+        # the reference draws Breit-Wigner masses for them (MProcess::GetOffShellMass)
+        raise UnsupportedProcess("unstable central particles need their decays: a > {c d}")
     if not (istate == "PP" and channel in ("CON", "CONTENSOR", "RESTENSOR") and
             cls in ("C", "F") and len(finals) == 2):
         raise UnsupportedProcess(
             "engine implements PP[CON|CONTENSOR|RESTENSOR]<C|F> -> 2-body, got %r" % proc)
-    if channel == "CONTENSOR" and not all(f in ("pi+", "pi-", "K+", "K-", "pi0") for f in finals):
-        raise UnsupportedProcess("CONTENSOR is implemented for pseudoscalar pairs (2xS)")
+    vec = all(SPIN.get(f, 0) == 1 for f in finals)
+    if channel == "CONTENSOR" and not (
+            all(f in ("pi+", "pi-", "K+", "K-", "pi0") for f in finals) or
+            (vec and finals[0] == finals[1] and finals[0] in VECTOR_COUPLING)):
+        raise UnsupportedProcess("CONTENSOR is implemented for pseudoscalar pairs (2xS) and "
+                                 "rho rho / phi phi (2xV)")
     if channel == "RESTENSOR" and sorted(finals) not in (["pi+", "pi-"], ["K+", "K-"]):
         raise UnsupportedProcess("RESTENSOR is implemented for pi+ pi- and K+ K- decays")
     if int(pp.get("NSTARS", 0)) != 0:
@@ -157,6 +204,15 @@ def build_params(card, process=None, tune=None):
         P.m_central[k] = PARTICLES[name][1]
     # identical-particle factor (MProcess.cc:449-468)
     P.s_factor = float(math.factorial(2) if finals[0] == finals[1] else 1)
+    P.central_spin = 1 if vec else 0
+    if any(casc):
+        P.n_decay = 2
+        for k, name in enumerate(finals):
+            P.width[k] = PARTICLES[name][2]
+        for k, (name, _) in enumerate(casc[0] + casc[1]):
+            if name not in PARTICLES:
+                raise UnsupportedProcess("unknown final state %s" % name)
+            P.m_daughter[k] = PARTICLES[name][1]
 
     # Generation cuts with post_Constructor defaults (MContinuum.cc:64-89,
     # MProcess.cc:1369-1386).
@@ -232,6 +288,9 @@ def build_params(card, process=None, tune=None):
     P.tensor.delta_P, P.tensor.ap_P, P.tensor.gPNN = tp["delta_P"], tp["ap_P"], tp["gPNN"]
     P.tensor.gPps = tp["gPpipi"] if P.m_central[0] < 0.2 else tp["gPKK"]
     P.tensor.em_kelly = 1 if T["PARAM_STRUCTURE"]["EM"] == "KELLY" else 0
+    if vec and finals[0] in VECTOR_COUPLING:
+        # pomeron-vector-vector couplings of rho or phi (MTensorPomeron.cc:811-823)
+        P.tensor.gPvv[0], P.tensor.gPvv[1] = tp[VECTOR_COUPLING[finals[0]]]
 
     if channel == "RESTENSOR":
         set_resonances(P, pp, proc, tune, finals)

@@ -392,7 +392,7 @@ void grn_default_params(grn_process_params *p) {
   // Loop numerics: 15 x 12 intervals, kt in [1e-4, 1.75]; tables 10000 intervals
   p->loop = {15, 12, 1e-4, 1.75, 10000, 10000};
   // TUNE0 PARAM_TENSORPOM, pion coupling; Kelly proton form factors (GENERAL.json:178-219)
-  p->tensor = {0.0808, 0.25, 1.87, 1.76, 1, 0};
+  p->tensor = {0.0808, 0.25, 1.87, 1.76, 1, 0, {0.70, 6.20}};
 }
 
 double grn_tensor_decay_coupling(int32_t J, double M, double W, double m_daughter, double BR) {

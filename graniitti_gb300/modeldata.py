@@ -20,6 +20,7 @@ TUNES = {
         },
         "PARAM_TENSORPOM": {
             "delta_P": 0.0808, "ap_P": 0.25, "gPNN": 1.87, "gPpipi": 1.76, "gPKK": 1.54,
+            "gPrhorho": [0.70, 6.20], "gPphiphi": [0.49, 4.27],
         },
         "PARAM_STRUCTURE": {"EM": "KELLY"},
         # Final-state Reggeon couplings c and on/off flags n, by coupling class.
@@ -71,5 +72,13 @@ PARTICLES = {
     "pi-": (-211, 1.3957061e-01, 2.5284e-17, "PARAM_PI"),
     "pi0": (111, 1.349770e-01, 7.73e-09, "PARAM_PI"),
     "K+": (321, 4.93677e-01, 5.317e-17, "PARAM_K"),
+    "rho(770)0": (113, 7.7526e-01, 1.491e-01, "PARAM_RHO"),
+    "phi(1020)0": (333, 1.019461e+00, 4.249e-03, "PARAM_PHI"),
     "K-": (-321, 4.93677e-01, 5.317e-17, "PARAM_K"),
 }
+
+# Spin of the central particles that are not spin 0 (PDG table, J).
+SPIN = {"rho(770)0": 1, "phi(1020)0": 1}
+
+# Tensor-pomeron vector-vector coupling pair of each vector meson (PARAM_TENSORPOM key).
+VECTOR_COUPLING = {"rho(770)0": "gPrhorho", "phi(1020)0": "gPphiphi"}

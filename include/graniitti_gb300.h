@@ -98,6 +98,7 @@ typedef struct grn_tensor_params { /* MTensorPomeronParam, include/Graniitti/MTe
   double  gPps;          /* pomeron-pseudoscalar coupling (gPpipi or gPKK) */
   int32_t em_kelly;      /* proton Dirac form factor F1: 1 = Kelly, 0 = dipole (PARAM_STRUCTURE EM) */
   int32_t _pad;
+  double  gPvv[2];       /* pomeron-vector-vector couplings (gPrhorho or gPphiphi) [GeV^-3, GeV^-1] */
 } grn_tensor_params;
 
 /* One resonance of PP[RESTENSOR]: PARAM_RES (src/MForm.cc:250-340) and the decay
@@ -155,6 +156,17 @@ typedef struct grn_process_params {
   int32_t           n_res;   /* GRN_PROC_TENSOR_RES: resonances in the coherent sum (1..4) */
   int32_t           _pad_res;
   grn_resonance     res[GRN_MAX_RESONANCES];
+  /* Decay cascade of the two central particles, "a > {c d} b > {e f}" (MDecayBranch legs,
+   * include/Graniitti/MParticle.h:60-90): each central particle has an off-shell mass drawn
+   * from a relativistic Breit-Wigner within +-5 widths (MProcess::GetOffShellMass,
+   * src/MProcess.cc:753-812) and decays isotropically to two daughters
+   * (ConstructDecayKinematics, :1231-1283). The draws are extra hypercube coordinates:
+   * u[8], u[9] the two masses, u[10..11] and u[12..13] the two decays (cos theta, phi), so a
+   * cascade process has 14 dimensions (<F> only). */
+  int32_t           n_decay;      /* 0: stable central particles; 2: two-body cascades */
+  int32_t           central_spin; /* spin of the central particles (0 or 1: "2xS" / "2xV") */
+  double            width[2];     /* widths of the central particles [GeV] */
+  double            m_daughter[4];/* daughter masses: central 1 -> [0], [1]; 2 -> [2], [3] */
 } grn_process_params;
 
 /* Fill every field with the reference defaults for "PP[CON]<C> -> pi+ pi-" at

@@ -184,6 +184,8 @@ struct Event {
   V4     pf[5];            // pfinal[0..4]: central system, forward 1, forward 2, central a, b
   V4     q;                // intermediate difference momentum (pkt_[0]), <C>
   double dw = 0;           // <F>: 2-body phase-space weight dPhi2 (MFactorized.cc:381)
+  double m2lo = 0, m2hi = 0;  // <F>: central mass^2 window of this point
+  V4     leaf[4];          // cascades: final-state daughters (central 1: 0, 1; central 2: 2, 3)
   double t1 = 0, t2 = 0, that = 0, uhat = 0, m2 = 0, Y = 0, Pt = 0;
   double ss[5][5] = {};
 };
@@ -299,6 +301,19 @@ bool build_kinematics(const Setup &S, const double *u, Event &ev) {
   return lorentz_scalars(S, ev);
 }
 
+// Relativistic Breit-Wigner mass by inverse CDF in m^2, truncated to [max(M_MIN, m0 - 5 W),
+// m0 + 5 W] (MRandom::RelativisticBWRandom, src/MRandom.cc:82-104, OFFSHELL = 5 widths,
+// include/Graniitti/MProcess.h:363), from the uniform R.
+double bw_mass(double m0, double W, double M_MIN, double R) {
+  if (W < 1e-40) return m0;
+  const double m2    = m0 * m0;
+  const double m2max = sq(m0 + 5.0 * W);
+  const double m2min = std::max(std::max(0.0, M_MIN * M_MIN), sq(m0 - 5.0 * W));
+  const double a = std::atan2(m2min - m2, m0 * W), b = std::atan2(m2max - m2, m0 * W);
+  const double v = m2 + m0 * W * std::tan(a + R * (b - a));
+  return std::max(M_MIN, msqrt(v));
+}
+
 // 2-body decay in the mother's rest frame with given (cos theta, phi), boosted to
 // the lab (TwoBodyPhaseSpace + Isotropic + LorentzBoost,
 // include/Graniitti/MKinematics.h:294-298, 384-459). Returns dPhi2 (MKinematics.h:267).
@@ -333,10 +348,19 @@ bool build_kinematics_F(const Setup &S, const double *u, Event &ev) {
   const double phi1 = 2.0 * PI * u[2];
   const double phi2 = 2.0 * PI * u[3];
   const double yX   = g.Y_min + (g.Y_max - g.Y_min) * u[4];
-  const double m3 = S.p.m_central[0], m4 = S.p.m_central[1];
+  double m3 = S.p.m_central[0], m4 = S.p.m_central[1];
+  if (S.p.n_decay == 2) {
+    // off-shell masses of the central particles (GetOffShellMass: daughters' mass sum +
+    // 1e-5 GeV bounds the Breit-Wigner from below)
+    m3 = bw_mass(m3, S.p.width[0], S.p.m_daughter[0] + S.p.m_daughter[1] + 1e-5, u[8]);
+    m4 = bw_mass(m4, S.p.width[1], S.p.m_daughter[2] + S.p.m_daughter[3] + 1e-5, u[9]);
+  }
   const double Mmin = std::max(m3 + m4 + 1e-4, g.M_min);
   const double Mmax = std::min(S.sqrt_s - (S.pb1.m() + S.pb2.m()), g.M_max);
+  if (!(Mmin < Mmax)) return false;
   const double m2X  = Mmin * Mmin + (Mmax * Mmax - Mmin * Mmin) * u[5];
+  ev.m2lo = Mmin * Mmin;
+  ev.m2hi = Mmax * Mmax;
   V4 p1(pt1 * std::cos(phi1), pt1 * std::sin(phi1), 0, 0);
   V4 p2(pt2 * std::cos(phi2), pt2 * std::sin(phi2), 0, 0);
   V4 pX(-(p1.x + p2.x), -(p1.y + p2.y), 0, 0);
@@ -350,6 +374,12 @@ bool build_kinematics_F(const Setup &S, const double *u, Event &ev) {
   ev.pf[2] = p2;
   if (!check_emc((S.pb1 + S.pb2) - (p1 + p2 + pX))) return false;
   ev.dw = two_body(pX, msqrt(m2X), m3, m4, 2.0 * u[6] - 1.0, 2.0 * PI * u[7], ev.pf[3], ev.pf[4]);
+  if (S.p.n_decay == 2) {
+    two_body(ev.pf[3], m3, S.p.m_daughter[0], S.p.m_daughter[1], 2.0 * u[10] - 1.0,
+             2.0 * PI * u[11], ev.leaf[0], ev.leaf[1]);
+    two_body(ev.pf[4], m4, S.p.m_daughter[2], S.p.m_daughter[3], 2.0 * u[12] - 1.0,
+             2.0 * PI * u[13], ev.leaf[2], ev.leaf[3]);
+  }
   return lorentz_scalars(S, ev);
 }
 
@@ -553,6 +583,195 @@ const std::vector<cplx> &ppt_structure0() {
   return T;
 }
 
+// Mixed-position versions of R (MTensorPomeron::CalcRTensor, :2566-2569): raised indices
+// carry the metric factor of their slot.
+double R_dddu(int a, int b, int c, int d) { return R_dddd(a, b, c, d) * G_METRIC[d]; }
+double R_dduu(int a, int b, int c, int d) {
+  return R_dddd(a, b, c, d) * G_METRIC[c] * G_METRIC[d];
+}
+double R_uudd(int a, int b, int c, int d) {
+  return R_dddd(a, b, c, d) * G_METRIC[a] * G_METRIC[b];
+}
+inline int i8(int u, int v, int k, int l, int r, int s, int a, int b) {
+  return i6(u, v, k, l, r, s) * 16 + a * 4 + b;
+}
+
+// Pre-contracted R products of coupling structures #1, #2 (the FIX1/FIX2/FIX3 tensors of
+// MTensorPomeron::CalcRTensor, :2583-2631).
+struct PPTFix {
+  std::vector<double> T1, T2, T3;
+  PPTFix() : T1(4096, 0.0), T2(65536, 0.0), T3(65536, 0.0) {
+    for (int u = 0; u < 4; ++u)
+      for (int v = 0; v < 4; ++v)
+        for (int k = 0; k < 4; ++k)
+          for (int l = 0; l < 4; ++l)
+            for (int r = 0; r < 4; ++r)
+              for (int s = 0; s < 4; ++s)
+                for (int a1 = 0; a1 < 4; ++a1)
+                  for (int x = 0; x < 4; ++x)
+                    for (int y = 0; y < 4; ++y) {
+                      // T1: sum over a1, r1 = x, s1 = y
+                      T1[i6(u, v, k, l, r, s)] +=
+                          R_dddd(u, v, x, a1) * R_dddu(k, l, y, a1) * R_dduu(r, s, x, y);
+                    }
+    for (int u = 0; u < 4; ++u)
+      for (int v = 0; v < 4; ++v)
+        for (int k = 0; k < 4; ++k)
+          for (int l = 0; l < 4; ++l)
+            for (int r = 0; r < 4; ++r)
+              for (int s = 0; s < 4; ++s)
+                for (int a1 = 0; a1 < 4; ++a1)
+                  for (int m = 0; m < 4; ++m)
+                    for (int n = 0; n < 4; ++n) {
+                      // T2(.., u1 = m, r1 = n) = sum_{a1, s1} R(u,v,u1,a1) R_DDDU(k,l,s1,a1)
+                      //                                       R_DDUU(r,s,r1,s1)
+                      // T3(.., u1 = m, s1 = n) = sum_{a1, r1} R(u,v,r1,a1) R_DDDU(k,l,u1,a1)
+                      //                                       R_DDUU(r,s,r1,s1)
+                      for (int j = 0; j < 4; ++j) {
+                        T2[i8(u, v, k, l, r, s, m, n)] +=
+                            R_dddd(u, v, m, a1) * R_dddu(k, l, j, a1) * R_dduu(r, s, n, j);
+                        T3[i8(u, v, k, l, r, s, m, n)] +=
+                            R_dddd(u, v, j, a1) * R_dddu(k, l, m, a1) * R_dduu(r, s, j, n);
+                      }
+                    }
+  }
+};
+const PPTFix &ppt_fix() {
+  static const PPTFix F;
+  return F;
+}
+
+// Kinematics-dependent coupling structures #1..#6 (iG_PPT_12 :1738-1780, iG_PPT_03
+// :1786-1834, iG_PPT_04 :1839-1906, iG_PPT_05 :1911-1983, iG_PPT_06 :1988-2014), each with its
+// coupling g applied, added into T.
+void ppt_structures(const V4 &q1, const V4 &q2, const double *g, std::vector<cplx> &T) {
+  const double q1q2 = q1.e * q2.e - (q1.x * q2.x + q1.y * q2.y + q1.z * q2.z);
+  const PPTFix &F   = ppt_fix();
+  const double  EPS = 1e-6;  // structures with |g| <= 1e-6 are skipped (:1659-1670)
+  for (int mode = 1; mode <= 2; ++mode) {
+    if (!(std::fabs(g[mode]) > EPS)) continue;
+    const cplx   f    = cplx(0, -2.0) * g[mode];
+    const double sign = mode == 1 ? -1.0 : 1.0;
+    for (int u = 0; u < 4; ++u)
+      for (int v = 0; v < 4; ++v)
+        for (int k = 0; k < 4; ++k)
+          for (int l = 0; l < 4; ++l)
+            for (int r = 0; r < 4; ++r)
+              for (int s = 0; s < 4; ++s) {
+                double t = q1q2 * F.T1[i6(u, v, k, l, r, s)];
+                for (int a = 0; a < 4; ++a)
+                  for (int b = 0; b < 4; ++b) {
+                    t += sign * up(q2, a) * dn(q1, b) * F.T2[i8(u, v, k, l, r, s, a, b)];
+                    t += sign * up(q1, a) * dn(q2, b) * F.T3[i8(u, v, k, l, r, s, a, b)];
+                    t += dn(q1, a) * dn(q2, b) * R_dddd(u, v, k, l) * R_dduu(r, s, a, b);
+                  }
+                T[i6(u, v, k, l, r, s)] += f * t;
+              }
+  }
+  if (std::fabs(g[3]) > EPS) {
+    const cplx f = cplx(0, -1.0) * g[3];
+    double A[4][4][4] = {}, B[4][4][4] = {};
+    for (int u = 0; u < 4; ++u)
+      for (int v = 0; v < 4; ++v)
+        for (int k = 0; k < 4; ++k)
+          for (int x = 0; x < 4; ++x) {
+            A[u][v][k] += up(q2, x) * R_dddd(u, v, x, k);
+            B[u][v][k] += up(q1, x) * R_dddd(u, v, x, k);
+          }
+    for (int u = 0; u < 4; ++u)
+      for (int v = 0; v < 4; ++v)
+        for (int k = 0; k < 4; ++k)
+          for (int l = 0; l < 4; ++l)
+            for (int r = 0; r < 4; ++r)
+              for (int s = 0; s < 4; ++s) {
+                double t = 0;
+                for (int v1 = 0; v1 < 4; ++v1)
+                  for (int l1 = 0; l1 < 4; ++l1)
+                    t += (A[u][v][v1] * B[k][l][l1] + A[u][v][l1] * B[k][l][v1]) *
+                         R_uudd(v1, l1, r, s);
+                T[i6(u, v, k, l, r, s)] += f * t;
+              }
+  }
+  if (std::fabs(g[4]) > EPS) {
+    const cplx f = cplx(0, -2.0) * g[4];
+    double A[4][4][4][4] = {}, B[4][4][4][4] = {}, C[4][4] = {};
+    for (int u = 0; u < 4; ++u)
+      for (int v = 0; v < 4; ++v)
+        for (int k = 0; k < 4; ++k)
+          for (int l = 0; l < 4; ++l)
+            for (int u1 = 0; u1 < 4; ++u1)
+              for (int v1 = 0; v1 < 4; ++v1)
+                for (int a1 = 0; a1 < 4; ++a1) {
+                  A[u][v][k][l] += up(q2, v1) * R_dddd(u, v, v1, a1) * up(q1, u1) *
+                                   R_dddu(k, l, u1, a1);
+                  B[u][v][k][l] += up(q2, u1) * R_dddd(u, v, u1, a1) * up(q1, v1) *
+                                   R_dddu(k, l, v1, a1);
+                }
+    for (int r = 0; r < 4; ++r)
+      for (int s = 0; s < 4; ++s)
+        for (int a1 = 0; a1 < 4; ++a1)
+          for (int l1 = 0; l1 < 4; ++l1) C[r][s] += dn(q1, a1) * dn(q2, l1) * R_uudd(a1, l1, r, s);
+    for (int u = 0; u < 4; ++u)
+      for (int v = 0; v < 4; ++v)
+        for (int k = 0; k < 4; ++k)
+          for (int l = 0; l < 4; ++l)
+            for (int r = 0; r < 4; ++r)
+              for (int s = 0; s < 4; ++s)
+                T[i6(u, v, k, l, r, s)] +=
+                    f * (A[u][v][k][l] + B[u][v][k][l] - 2.0 * q1q2 * R_dddd(u, v, k, l)) * C[r][s];
+  }
+  if (std::fabs(g[5]) > EPS) {
+    const cplx f = cplx(0, 1.0) * g[5];
+    double A[4][4][4][4] = {}, C[4][4][4][4] = {}, B[4][4] = {}, D[4][4] = {};
+    for (int u = 0; u < 4; ++u)
+      for (int v = 0; v < 4; ++v)
+        for (int r = 0; r < 4; ++r)
+          for (int s = 0; s < 4; ++s)
+            for (int u1 = 0; u1 < 4; ++u1)
+              for (int v1 = 0; v1 < 4; ++v1)
+                for (int r1 = 0; r1 < 4; ++r1) {
+                  A[u][v][r][s] += up(q2, u1) * R_dddd(u, v, u1, v1) * dn(q2, r1) *
+                                   R_uudd(v1, r1, r, s);
+                  C[u][v][r][s] += up(q1, u1) * R_dddd(u, v, u1, v1) * dn(q1, r1) *
+                                   R_uudd(v1, r1, r, s);
+                }
+    for (int a = 0; a < 4; ++a)
+      for (int b = 0; b < 4; ++b)
+        for (int c = 0; c < 4; ++c)
+          for (int d = 0; d < 4; ++d) {
+            B[a][b] += up(q1, c) * up(q1, d) * R_dddd(a, b, c, d);
+            D[a][b] += up(q2, c) * up(q2, d) * R_dddd(a, b, c, d);
+          }
+    for (int u = 0; u < 4; ++u)
+      for (int v = 0; v < 4; ++v)
+        for (int k = 0; k < 4; ++k)
+          for (int l = 0; l < 4; ++l)
+            for (int r = 0; r < 4; ++r)
+              for (int s = 0; s < 4; ++s)
+                T[i6(u, v, k, l, r, s)] +=
+                    f * (A[u][v][r][s] * B[k][l] + C[k][l][r][s] * D[u][v]);
+  }
+  if (std::fabs(g[6]) > EPS) {
+    const cplx f = cplx(0, -2.0) * g[6];
+    double A[4][4] = {}, B[4][4] = {}, C[4][4] = {};
+    for (int a = 0; a < 4; ++a)
+      for (int b = 0; b < 4; ++b)
+        for (int c = 0; c < 4; ++c)
+          for (int d = 0; d < 4; ++d) {
+            A[a][b] += up(q2, c) * up(q2, d) * R_dddd(a, b, c, d);
+            B[a][b] += up(q1, c) * up(q1, d) * R_dddd(a, b, c, d);
+            C[a][b] += up(q1, c) * up(q2, d) * R_dddd(a, b, c, d);
+          }
+    for (int u = 0; u < 4; ++u)
+      for (int v = 0; v < 4; ++v)
+        for (int k = 0; k < 4; ++k)
+          for (int l = 0; l < 4; ++l)
+            for (int r = 0; r < 4; ++r)
+              for (int s = 0; s < 4; ++s)
+                T[i6(u, v, k, l, r, s)] += f * A[u][v] * B[k][l] * C[r][s];
+  }
+}
+
 // Resonance form factor exp(-(q^2 - M0^2)^2 / Lambda^4) (MTensorPomeron::F, :2489) and the
 // pion-electromagnetic-type FM(q^2) = 1 / (1 - q^2 / Lambda^2) with Lambda^2 = 1 (:2485).
 double ff_res(double q2, double M0) { return std::exp(-sq(q2 - M0 * M0)); }
@@ -616,14 +835,16 @@ cplx tensor_me3(const Setup &S, const Event &ev) {
           D[u][v] = sum;
         }
       const std::vector<cplx> &G0 = ppt_structure0();
-      const double             g0 = R.g_tensor[0] * F_tilde;
+      std::vector<cplx>        Gt(4096);
+      for (int i = 0; i < 4096; ++i) Gt[i] = G0[i] * R.g_tensor[0];
+      ppt_structures(q1, q2, R.g_tensor, Gt);
       for (int u = 0; u < 4; ++u)
         for (int v = 0; v < 4; ++v)
           for (int k_ = 0; k_ < 4; ++k_)
             for (int l = 0; l < 4; ++l) {
               cplx sum(0, 0);
               for (int a = 0; a < 4; ++a)
-                for (int b = 0; b < 4; ++b) sum += G0[i6(u, v, k_, l, a, b)] * g0 * D[a][b];
+                for (int b = 0; b < 4; ++b) sum += Gt[i6(u, v, k_, l, a, b)] * F_tilde * D[a][b];
               cvtx[u][v][k_][l] = sum;
             }
     } else {
@@ -654,8 +875,154 @@ cplx tensor_me3(const Setup &S, const Event &ev) {
   return A;
 }
 
+// ---------------------------------------------------------------------------
+// Tensor-pomeron continuum of two vector mesons, "2xV" (MTensorPomeron::ME4,
+// src/MTensorPomeron.cc:808-888), with the explicit index sums of the reference.
+typedef std::array<std::array<std::array<std::array<cplx, 4>, 4>, 4>, 4> T4;
+
+// Gamma^(0) and Gamma^(2) of the pomeron-vector-vector vertex (:2500-2529).
+double vv_gamma0(const V4 &k1, const V4 &k2, int u, int v, int k, int l) {
+  const double k1k2 = k1.e * k2.e - (k1.x * k2.x + k1.y * k2.y + k1.z * k2.z);
+  return (k1k2 * gm(u, v) - dn(k2, u) * dn(k1, v)) *
+         (dn(k1, k) * dn(k2, l) + dn(k2, k) * dn(k1, l) - 0.5 * k1k2 * gm(k, l));
+}
+double vv_gamma2(const V4 &k1, const V4 &k2, int u, int v, int k, int l) {
+  const double k1k2 = k1.e * k2.e - (k1.x * k2.x + k1.y * k2.y + k1.z * k2.z);
+  return k1k2 * (gm(u, k) * gm(v, l) + gm(u, l) * gm(v, k)) +
+         gm(u, v) * (dn(k1, k) * dn(k2, l) + dn(k2, k) * dn(k1, l)) -
+         dn(k1, v) * dn(k2, l) * gm(u, k) - dn(k1, v) * dn(k2, k) * gm(u, l) -
+         dn(k2, u) * dn(k1, l) * gm(v, k) - dn(k2, u) * dn(k1, k) * gm(v, l) -
+         (k1k2 * gm(u, v) - dn(k2, u) * dn(k1, v)) * gm(k, l);
+}
+// i Gamma_{alpha beta gamma delta}(p', p) = i FM((p' - p)^2, 0.5) (2 g1 Gamma0(p', -p) -
+// g2 Gamma2(p', -p)) (iG_Pvv, :2224-2237).
+T4 vertex_Pvv(const grn_process_params &p, const V4 &prime, const V4 &q) {
+  const V4   mq(-q.x, -q.y, -q.z, -q.e);
+  const cplx f = cplx(0, 1) * (1.0 / (1.0 - (prime - q).m2() / 0.5));
+  T4 T;
+  for (int u = 0; u < 4; ++u)
+    for (int v = 0; v < 4; ++v)
+      for (int k = 0; k < 4; ++k)
+        for (int l = 0; l < 4; ++l)
+          T[u][v][k][l] = f * (2.0 * p.tensor.gPvv[0] * vv_gamma0(prime, mq, u, v, k, l) -
+                               p.tensor.gPvv[1] * vv_gamma2(prime, mq, u, v, k, l));
+  return T;
+}
+// Reggeized vector propagator factor -1/(m^2 - M0^2) (e^{i phi} s34 / (4 M0^2))^(alpha - 1)
+// with alpha = 0.5 + 0.9 m^2 (iD_V, :2353-2369); its index structure g^{uv} is applied in
+// the contraction.
+cplx vector_prop(const V4 &p, double M0, double s34) {
+  const double m2    = p.m2();
+  const double alpha = 0.5 + 0.9 * m2;
+  const double sth   = 4.0 * M0 * M0;
+  const double phi   = PI / 2.0 * std::exp((sth - s34) / sth) - PI / 2.0;
+  const cplx   R     = std::pow(std::exp(cplx(0, phi)) * s34 / sth, alpha - 1.0);
+  return -1.0 / (m2 - M0 * M0) * R;
+}
+
+// A real basis of the polarization states of a massive vector of momentum p (upper
+// components): two transverse unit vectors and the longitudinal (|p|/m, E p^/m)
+// (MDirac::EpsMassiveSpin1, src/MDirac.cc:435-456, in a linear instead of the helicity
+// basis; the sum over states of |amplitude|^2 is the same).
+void vector_basis(const V4 &p, double e[3][4]) {
+  const double P = std::sqrt(p.x * p.x + p.y * p.y + p.z * p.z);
+  const double m = msqrt(p.m2());
+  double n[3] = {0, 0, 1};
+  if (P > 1e-12) {
+    n[0] = p.x / P;
+    n[1] = p.y / P;
+    n[2] = p.z / P;
+  }
+  // first transverse direction: z x n (or x x n near the z axis), normalised
+  double a[3] = {0, 0, 1};
+  if (std::fabs(n[2]) > 0.9) { a[0] = 1; a[2] = 0; }
+  double t1[3] = {a[1] * n[2] - a[2] * n[1], a[2] * n[0] - a[0] * n[2], a[0] * n[1] - a[1] * n[0]};
+  const double nt = std::sqrt(t1[0] * t1[0] + t1[1] * t1[1] + t1[2] * t1[2]);
+  for (double &x : t1) x /= nt;
+  const double t2[3] = {n[1] * t1[2] - n[2] * t1[1], n[2] * t1[0] - n[0] * t1[2],
+                        n[0] * t1[1] - n[1] * t1[0]};
+  e[0][0] = 0; e[0][1] = t1[0]; e[0][2] = t1[1]; e[0][3] = t1[2];
+  e[1][0] = 0; e[1][1] = t2[0]; e[1][2] = t2[1]; e[1][3] = t2[2];
+  e[2][0] = P / m; e[2][1] = p.e / m * n[0]; e[2][2] = p.e / m * n[1]; e[2][3] = p.e / m * n[2];
+}
+
+// The nine amplitudes e3_i^a e4_j^b M_ab of one proton helicity configuration.
+int tensor_me4_2xv(const Setup &S, const Event &ev, cplx *out) {
+  const grn_process_params &p = S.p;
+  const V4 &pa = S.pb1, &pb = S.pb2;
+  const V4 &p1 = ev.pf[1], &p2 = ev.pf[2], &p3 = ev.pf[3], &p4 = ev.pf[4];
+  const double M0 = p.m_central[0], M2 = M0 * M0;
+  const V4     pt  = pa - p1 - p3;
+  const V4     pu  = p4 - pa + p1;
+  const V4     mp3 = V4(-p3.x, -p3.y, -p3.z, -p3.e);
+  const V4     mpt = V4(-pt.x, -pt.y, -pt.z, -pt.e);
+  const T2     G1a = vertex_ppP(p, p1, pa);
+  const T2     G2b = vertex_ppP(p, p2, pb);
+  // X^{ab} = G(mu, nu) iD_P(mu, nu, a, b) for the four pomeron propagators
+  auto legX = [&](const T2 &G, double s, double t, cplx X[4][4]) {
+    const cplx c = pomeron_prop(p, s, t);
+    for (int a = 0; a < 4; ++a)
+      for (int b = 0; b < 4; ++b) {
+        cplx sum(0, 0);
+        for (int u = 0; u < 4; ++u)
+          for (int v = 0; v < 4; ++v) {
+            const double g = gm(u, a) * gm(v, b) + gm(u, b) * gm(v, a) - 0.5 * gm(u, v) * gm(a, b);
+            if (g != 0.0) sum += G.c[u][v] * g;
+          }
+        X[a][b] = c * sum;
+      }
+  };
+  cplx X13[4][4], X24[4][4], X14[4][4], X23[4][4];
+  legX(G1a, ev.ss[1][3], ev.t1, X13);
+  legX(G2b, ev.ss[2][4], ev.t2, X24);
+  legX(G1a, ev.ss[1][4], ev.t1, X14);
+  legX(G2b, ev.ss[2][3], ev.t2, X23);
+  // contract the pomeron leg into the last two indices of a vertex
+  auto vblock = [&](const T4 &G, const cplx X[4][4], cplx out2[4][4]) {
+    for (int u = 0; u < 4; ++u)
+      for (int v = 0; v < 4; ++v) {
+        cplx sum(0, 0);
+        for (int a = 0; a < 4; ++a)
+          for (int b = 0; b < 4; ++b) sum += X[a][b] * G[u][v][a][b];
+        out2[u][v] = sum;
+      }
+  };
+  cplx At[4][4], Bt[4][4], Au[4][4], Bu[4][4];
+  vblock(vertex_Pvv(p, pt, mp3), X13, At);   // At(rho1, rho3)
+  vblock(vertex_Pvv(p, p4, pt), X24, Bt);    // Bt(rho4, rho2)
+  vblock(vertex_Pvv(p, p4, pu), X14, Au);    // Au(rho4, rho1)
+  vblock(vertex_Pvv(p, pu, mp3), X23, Bu);   // Bu(rho2, rho3)
+  (void)mpt;
+  const double s34 = ev.pf[0].m2();
+  const cplx   Dt  = vector_prop(pt, M0, s34) * sq(meson_ff(p.regge, pt.m2(), M2));
+  const cplx   Du  = vector_prop(pu, M0, s34) * sq(meson_ff(p.regge, pu.m2(), M2));
+  cplx M[4][4];
+  for (int r3 = 0; r3 < 4; ++r3)
+    for (int r4 = 0; r4 < 4; ++r4) {
+      cplx mt(0, 0), mu(0, 0);
+      for (int r1 = 0; r1 < 4; ++r1) {
+        // iD_V carries g^{r1 r2}: diagonal
+        mt += At[r1][r3] * G_METRIC[r1] * Bt[r4][r1];
+        mu += Au[r4][r1] * G_METRIC[r1] * Bu[r1][r3];
+      }
+      M[r3][r4] = cplx(0, -1) * (mt * Dt + mu * Du);
+    }
+  double e3[3][4], e4[3][4];
+  vector_basis(p3, e3);
+  vector_basis(p4, e4);
+  for (int i = 0; i < 3; ++i)
+    for (int j = 0; j < 3; ++j) {
+      cplx sum(0, 0);
+      for (int a = 0; a < 4; ++a)
+        for (int b = 0; b < 4; ++b) sum += e3[i][a] * e4[j][b] * M[a][b];
+      out[3 * i + j] = sum;
+    }
+  return 9;
+}
+
 // Bare amplitude of the configured process.
 cplx bare_amp(const Setup &S, const Event &ev);
+int  bare_amps(const Setup &S, const Event &ev, cplx *A);
 
 // Linear interpolation on the kt^2 screening table (IArray1D::Interpolate1D,
 // src/MEikonal.cc:489-512).
@@ -671,14 +1038,15 @@ cplx msa_interp(const Setup &S, double a) {
   return y0 + (a - r0[0]) * ((y1 - y0) / (r1[0] - r0[0]));
 }
 
-// Eikonal kt-loop screened |M|^2 (MProcess::S3ScreenedAmp2, src/MProcess.cc:157-288).
-double screened_amp2(const Setup &S, const Event &born, const cplx &A0) {
+// Eikonal kt-loop screened |M|^2 (MProcess::S3ScreenedAmp2, src/MProcess.cc:157-288): every
+// helicity amplitude is screened on its own and the |.|^2 are summed.
+double screened_amp2(const Setup &S, const Event &born, const cplx *A0, int nh) {
   const grn_loop_numerics &L = S.p.loop;
   const double stepKT  = (L.kt_max - L.kt_min) / L.n_kt;
   const double stepPhi = 2.0 * PI / L.n_phi;
   const std::vector<double> U = simpson38_weights(L.n_phi);
   const std::vector<double> V = simpson38_weights(L.n_kt);
-  cplx sum(0, 0);
+  cplx sum[9];
   Event lev;
   for (int i = 0; i <= L.n_phi; ++i) {
     const double phi = i * stepPhi;
@@ -689,18 +1057,30 @@ double screened_amp2(const Setup &S, const Event &born, const cplx &A0) {
       if (!loop_kinematics(S, born, born.pf[1].x - kx, born.pf[1].y - ky, born.pf[2].x + kx,
                            born.pf[2].y + ky, lev))
         continue;
-      const cplx A = bare_amp(S, lev);
-      sum += (U[i] * V[j]) * (Aeik * A * kt);
+      cplx A[9];
+      bare_amps(S, lev, A);
+      for (int h = 0; h < nh; ++h) sum[h] += (U[i] * V[j]) * (Aeik * A[h] * kt);
     }
   }
   const cplx norm = cplx(0, 1) / (8.0 * PI * PI * S.s);
-  const cplx Aloop = norm * sum * (9.0 * stepPhi * stepKT / 64.0);
-  return std::norm(A0 + Aloop);
+  double amp2 = 0;
+  for (int h = 0; h < nh; ++h)
+    amp2 += std::norm(A0[h] + norm * sum[h] * (9.0 * stepPhi * stepKT / 64.0));
+  return amp2;
 }
 
 cplx bare_amp(const Setup &S, const Event &ev) {
   if (S.p.process == GRN_PROC_TENSOR_RES) return tensor_me3(S, ev);
   return S.p.process == GRN_PROC_TENSOR_CON ? tensor_me4_2xs(S, ev) : regge_me4(S, ev);
+}
+
+// All helicity amplitudes of one proton helicity configuration (the high-energy proton
+// vertex makes the four proton configurations equal, so |M|^2 = sum over these).
+int bare_amps(const Setup &S, const Event &ev, cplx *A) {
+  if (S.p.process == GRN_PROC_TENSOR_CON && S.p.central_spin == 1)
+    return tensor_me4_2xv(S, ev, A);
+  A[0] = bare_amp(S, ev);
+  return 1;
 }
 
 // Phase-space weight and integration volume (MContinuum.cc:619-656; ForwardVolume
@@ -712,13 +1092,13 @@ double ps_factor(const Setup &S, const Event &ev) {
     // C_space = dPhi2/(2 pi), B51PhaseSpaceWeight x B51IntegralVolume (MFactorized.cc:160-183,
     // 418-450)
     const double m3 = S.p.m_central[0], m4 = S.p.m_central[1];
-    const double Mmin = std::max(m3 + m4 + 1e-4, g.M_min);
-    const double Mmax = std::min(S.sqrt_s - (S.pb1.m() + S.pb2.m()), g.M_max);
+    (void)m3;
+    (void)m4;
     const double psw  = 0.5 * (1.0 / std::pow(2.0 * PI, 5)) * (ev.pf[1].pt() / (2.0 * ev.pf[1].e)) *
                        (ev.pf[2].pt() / (2.0 * ev.pf[2].e)) * J;
     const double fwd = sq(2.0 * PI) * ev.pf[1].pt() * ev.pf[2].pt() *
                        sq(std::log(g.fpt_max) - std::log(g.fpt_min + ZERO_EPS));
-    const double vol = (Mmax * Mmax - Mmin * Mmin) * (g.Y_max - g.Y_min) * fwd;
+    const double vol = (ev.m2hi - ev.m2lo) * (g.Y_max - g.Y_min) * fwd;
     return (ev.dw / (2.0 * PI)) * psw * vol;
   }
   const int Nf = 4;
@@ -742,8 +1122,10 @@ bool fiducial(const Setup &S, const Event &ev) {
         ev.Pt <= f.Pt_max))
     return false;
   bool ok = true;
-  for (int k = 3; k <= 4; ++k) {
-    const V4 &p = ev.pf[k];
+  // final-state particles: the central pair, or the leaves of its decays (FindDecayCuts)
+  const bool casc = S.p.n_decay == 2;
+  for (int k = 0; k < (casc ? 4 : 2); ++k) {
+    const V4 &p = casc ? ev.leaf[k] : ev.pf[3 + k];
     const double pt = p.pt(), et = p.mt(), eta = p.eta(), rap = p.rap();
     if (!(pt >= f.pt_min && pt <= f.pt_max && et >= f.Et_min && et <= f.Et_max &&
           eta >= f.eta_min && eta <= f.eta_max && rap >= f.rap_min && rap <= f.rap_max))
@@ -760,8 +1142,14 @@ double event_weight(const Setup &S, const double *u, uint8_t &flags, Event &ev) 
   const bool fid = kin && fiducial(S, ev);
   const bool veto = true;
   if (kin && fid && veto) {
-    const cplx A0 = bare_amp(S, ev);
-    const double amp2 = S.p.screening ? screened_amp2(S, ev, A0) : std::norm(A0);
+    cplx A0[9];
+    const int nh = bare_amps(S, ev, A0);
+    double amp2 = 0;
+    if (S.p.screening) {
+      amp2 = screened_amp2(S, ev, A0, nh);
+    } else {
+      for (int h = 0; h < nh; ++h) amp2 += std::norm(A0[h]);
+    }
     W = (1.0 / S.p.s_factor) * ps_factor(S, ev) * amp2 * GEV2BARN / (2.0 * S.s);
   }
   bool amp_ok = true;
@@ -830,7 +1218,8 @@ extern "C" {
 // t1, t2, m2 and the 4-vectors pfinal[1..4] (19 doubles).
 int orc_weights(const grn_process_params *p, const double *u, int64_t n, int32_t dim, double *w,
                 uint8_t *flags, double *rec, const double *msa, int32_t n_kt2, int32_t nthreads) {
-  if (!p || !u || !w || dim != 8 || p->n_central != 2) return GRN_ERR_INVALID;
+  const int32_t want = p && p->n_decay == 2 ? 14 : 8;
+  if (!p || !u || !w || dim != want || p->n_central != 2) return GRN_ERR_INVALID;
   if (p->screening && (!msa || n_kt2 < 2)) return GRN_ERR_STATE;
   const orc::Setup S = orc::make_setup(p, msa, n_kt2);
   orc::parallel_for(n, nthreads, [&](int64_t a, int64_t b) {
@@ -841,12 +1230,12 @@ int orc_weights(const grn_process_params *p, const double *u, int64_t n, int32_t
       w[i]      = orc::event_weight(S, u + i * dim, f, ev);
       if (flags) flags[i] = f;
       if (rec) {
-        double *r = rec + i * 19;
+        double *r = rec + i * 35;
         r[0] = ev.t1;
         r[1] = ev.t2;
         r[2] = ev.m2;
-        for (int k = 0; k < 4; ++k) {
-          const orc::V4 &v = ev.pf[k + 1];
+        for (int k = 0; k < 8; ++k) {
+          const orc::V4 &v = k < 4 ? ev.pf[k + 1] : ev.leaf[k - 4];
           r[3 + 4 * k + 0] = v.x;
           r[3 + 4 * k + 1] = v.y;
           r[3 + 4 * k + 2] = v.z;

@@ -47,12 +47,14 @@ def _p(a):
 
 
 def weights(params, u, msa=None, nthreads=1, with_rec=False):
-    """(w, flags[, rec]) for u of shape (n, 8)."""
+    """(w, flags[, rec]) for u of shape (n, 8), or (n, 14) for two-body cascades. rec per
+    point: t1, t2, m2, the 4-momenta (px, py, pz, E) of pfinal[1..4] and of the four cascade
+    daughters."""
     u = np.ascontiguousarray(u, dtype=np.float64)
     n, dim = u.shape
     w = np.zeros(n)
     fl = np.zeros(n, dtype=np.uint8)
-    rec = np.zeros((n, 19)) if with_rec else None
+    rec = np.zeros((n, 35)) if with_rec else None
     n_kt2 = 0
     if msa is not None:
         msa = np.ascontiguousarray(msa, dtype=np.float64)

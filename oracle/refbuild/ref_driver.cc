@@ -27,9 +27,12 @@
 //
 // Options: --nbt N --nkt2 N --loopkt N --loopphi N --maxloopkt X --offshellff K
 //          --ncall N --iter N --cores N --precision X --stride S --replay SPEC
+//          --leaves N (append the 4-momenta of the first N final-state leaves of the
+//          central decay tree to each record)
 
 #include <cstdio>
 #include <cstdlib>
+#include <functional>
 #include <cstring>
 #include <fstream>
 #include <iostream>
@@ -51,6 +54,7 @@ struct Opts {
   int    offshellff = -1;
   int    ncall = -1, iter = -1, cores = -1;
   double precision = -1;
+  int    leaves = 0;
 };
 
 Opts parse_opts(int argc, char **argv, int first) {
@@ -70,6 +74,7 @@ Opts parse_opts(int argc, char **argv, int first) {
     else if (k == "--precision") o.precision = std::atof(v);
     else if (k == "--stride") o.stride = std::atoi(v);
     else if (k == "--replay") o.replay = v;
+    else if (k == "--leaves") o.leaves = std::atoi(v);
     else {
       std::fprintf(stderr, "unknown option %s\n", k.c_str());
       std::exit(2);
@@ -165,7 +170,7 @@ int main(int argc, char **argv) {
         spec.push_back(tok == "h" ? -1 : std::atoi(tok.c_str()));
         a = b + 1;
       }
-      const int                 REC = 8 + 16;
+      const int                 REC = 8 + 16 + 4 * o.leaves;
       std::vector<double>       out(n * REC, 0.0);
       std::vector<double>       x(dim);
       for (std::size_t i = 0; i < n; ++i) {
@@ -194,6 +199,24 @@ int main(int argc, char **argv) {
           r[8 + 4 * k + 1]    = p.Py();
           r[8 + 4 * k + 2]    = p.Pz();
           r[8 + 4 * k + 3]    = p.E();
+        }
+        // final-state leaves of the central decay tree, depth first
+        if (o.leaves > 0) {
+          std::vector<gra::M4Vec> lv;
+          std::function<void(const gra::MDecayBranch &)> walk = [&](const gra::MDecayBranch &b) {
+            if (b.legs.empty()) {
+              lv.push_back(b.p4);
+              return;
+            }
+            for (const auto &l : b.legs) walk(l);
+          };
+          for (const auto &b : proc->lts.decaytree) walk(b);
+          for (int k = 0; k < o.leaves && k < static_cast<int>(lv.size()); ++k) {
+            r[24 + 4 * k + 0] = lv[k].Px();
+            r[24 + 4 * k + 1] = lv[k].Py();
+            r[24 + 4 * k + 2] = lv[k].Pz();
+            r[24 + 4 * k + 3] = lv[k].E();
+          }
         }
       }
       write_doubles(ofile, out);

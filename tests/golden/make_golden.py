@@ -8,7 +8,7 @@ reference does not. Steps:
   3. build the eikonal tables with the reference's MEikonal::S3Constructor
   4. run the reference VEGAS integration for the cross section
 
-Usage: python tests/golden/make_golden.py [--ref /root/reference] [--only resonances]
+Usage: python tests/golden/make_golden.py [--ref /root/reference] [--only resonances|cascades]
 """
 import argparse
 import json
@@ -30,7 +30,7 @@ PROC = "PP[CON]<C> -> pi+ pi-"
 TMP = os.path.join(REPO, "_work", "golden_tmp")
 
 
-def run_weights(card, u, extra=(), proc=PROC, dim=None):
+def run_weights(card, u, extra=(), proc=PROC, dim=None, leaves=0):
     """Reference weights of points u (n x 8). For <F> the process dimension is 6 and
     the decay angles are served from u[:, 6:8] through the RNG replay (the two pion
     off-shell mass draws, numerically inert at width 2.5e-17 GeV, take 0.5)."""
@@ -42,11 +42,16 @@ def run_weights(card, u, extra=(), proc=PROC, dim=None):
     cmd = [REF_BIN, "weights", card, proc, uf, str(dim), wf] + list(extra)
     if dim != u.shape[1]:
         cmd += ["--stride", str(u.shape[1])]
+    if leaves:
+        cmd += ["--leaves", str(leaves)]
     subprocess.run(cmd, check=True, capture_output=True)
-    r = np.fromfile(wf).reshape(-1, 24)
-    return dict(w=r[:, 0], kin=r[:, 1].astype(np.uint8), fid=r[:, 2].astype(np.uint8),
-                veto=r[:, 3].astype(np.uint8), amp=r[:, 4].astype(np.uint8), t1=r[:, 5],
-                t2=r[:, 6], m2=r[:, 7], p4=r[:, 8:24].reshape(-1, 4, 4))
+    r = np.fromfile(wf).reshape(-1, 24 + 4 * leaves)
+    out = dict(w=r[:, 0], kin=r[:, 1].astype(np.uint8), fid=r[:, 2].astype(np.uint8),
+               veto=r[:, 3].astype(np.uint8), amp=r[:, 4].astype(np.uint8), t1=r[:, 5],
+               t2=r[:, 6], m2=r[:, 7], p4=r[:, 8:24].reshape(-1, 4, 4))
+    if leaves:
+        out["leaves"] = r[:, 24:].reshape(-1, leaves, 4)
+    return out
 
 
 def save(name, **arrays):
@@ -99,13 +104,44 @@ def write_sigma(name, out, proc, card):
     print(name, "sigma", sigma, "+-", err)
 
 
+def cascade_fixtures():
+    """Vector-meson pairs with two-body cascades (<F>, 14 dimensions): tensor-pomeron 2xV
+    (MTensorPomeron::ME4) and Regge continuum rho rho -> pi+ pi- pi+ pi-, tensor phi phi ->
+    K+ K- K+ K-, and the screened tensor rho rho. Replay order of the reference's draws: the
+    two daughter masses then the mass of each central particle (u[8], u[9]), the central
+    decay angles (u[6], u[7]), then per central particle its daughters' masses and decay
+    angles (u[10..11], u[12..13]); daughter masses of width ~1e-17 GeV take 0.5."""
+    REPLAY = ["--replay", "h,h,8,h,h,9,6,7,h,h,10,11,h,h,12,13"]
+    RR = "rho(770)0 > {pi+ pi-} rho(770)0 > {pi+ pi-}"
+    cases = [
+        ("rr_tree_weights.npz", 81, 2048, CARD, "PP[CONTENSOR]<F> -> " + RR),
+        ("rr_regge_tree_weights.npz", 82, 1024, CARD, "PP[CON]<F> -> " + RR),
+        ("ff_tree_weights.npz", 83, 512, CARD,
+         "PP[CONTENSOR]<F> -> phi(1020)0 > {K+ K-} phi(1020)0 > {K+ K-}"),
+    ]
+    for name, seed, n, card, proc in cases:
+        u = philox_np.uniforms(seed, n, 14)
+        r = run_weights(card, u, REPLAY, proc=proc, dim=6, leaves=4)
+        save(name, seed=seed, u=u, card=os.path.basename(card), proc=proc, **r)
+    proc = "PP[CONTENSOR]<F> -> " + RR
+    u = philox_np.uniforms(84, 256, 14)
+    r = run_weights(CARD_SCR, u, REPLAY + ["--nbt", "1024", "--nkt2", "10000"], proc=proc, dim=6,
+                    leaves=4)
+    save("rr_screened_15x12_weights.npz", seed=84, u=u, card=os.path.basename(CARD_SCR),
+         proc=proc, n_bt=1024, n_kt2=10000, loop_kt=15, loop_phi=12, loop_ktmax=1.75, **r)
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--ref", default="/root/reference")
-    ap.add_argument("--only", choices=["all", "resonances"], default="all")
+    ap.add_argument("--only", choices=["all", "resonances", "cascades"], default="all")
     a = ap.parse_args()
     subprocess.check_call(["make", "-s", "-C", os.path.join(REPO, "oracle", "refbuild"), "-j8",
                            "REF=" + a.ref])
+    if a.only in ("all", "cascades"):
+        cascade_fixtures()
+    if a.only == "cascades":
+        return
     resonance_fixtures()
     if a.only == "resonances":
         return

@@ -44,7 +44,7 @@ def test_tree_weights(params, name, ff):
     _check_weights(w, fl, g)
     kin = g["kin"] == 1
     # forward legs and central particles (px, py, pz, E)
-    p4 = rec[:, 3:].reshape(-1, 4, 4)
+    p4 = rec[:, 3:19].reshape(-1, 4, 4)
     scale = np.abs(g["p4"]).max(axis=2, keepdims=True)
     assert (np.abs(p4 - g["p4"])[kin] / scale[kin]).max() < 1e-12
     # invariants: m2 everywhere, t1/t2 where |t| is not cancellation-limited in the reference
@@ -116,7 +116,7 @@ def test_factorized_tree_weights():
     w, fl, rec = orc.weights(_params_F(), g["u"], with_rec=True)
     _check_weights(w, fl, g)
     kin = g["kin"] == 1
-    p4 = rec[:, 3:].reshape(-1, 4, 4)
+    p4 = rec[:, 3:19].reshape(-1, 4, 4)
     scale = np.abs(g["p4"]).max(axis=2, keepdims=True)
     assert (np.abs(p4 - g["p4"])[kin] / scale[kin]).max() < 1e-12
 
@@ -179,3 +179,20 @@ def test_tensor_resonance_screened_weights(lib_built):
     t = _load("eikonal_nbt1024_nkt10000.npz")
     w, fl = orc.weights(_params_res(g), g["u"], msa=t["msa"], nthreads=4)
     _check_weights(w, fl, g, tol=1e-9)
+
+
+# Two-body cascades of vector-meson pairs (<F>, 14 dimensions): tensor-pomeron 2xV
+# (MTensorPomeron::ME4 :808-888) and the Regge continuum, with the final-state daughters.
+@pytest.mark.parametrize("name", ["rr_tree_weights.npz", "rr_regge_tree_weights.npz",
+                                  "ff_tree_weights.npz", "rr_screened_15x12_weights.npz"])
+def test_vector_pair_cascade_weights(name):
+    g = _load(name)
+    P = _params_res(g)
+    assert P.n_decay == 2 and P.central_spin == 1
+    msa = _load("eikonal_nbt1024_nkt10000.npz")["msa"] if P.screening else None
+    w, fl, rec = orc.weights(P, g["u"], msa=msa, nthreads=4, with_rec=True)
+    _check_weights(w, fl, g, tol=W_TOL)
+    kin = g["kin"] == 1
+    leaves = rec[:, 19:35].reshape(-1, 4, 4)
+    scale = np.abs(g["leaves"]).max(axis=2, keepdims=True)
+    assert (np.abs(leaves - g["leaves"])[kin] / scale[kin]).max() < 1e-12
