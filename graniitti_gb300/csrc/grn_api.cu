@@ -105,7 +105,7 @@ struct grn_engine {
   int         nblocks = 0;
   DevBuf      d_xmat, d_xmat_prev, d_f2mat, d_f, d_acc, d_parts, d_sc;
   DevBuf      d_xmat_flat;  // uniform grid of FLAT passes (x = u, vw = 1)
-  DevBuf      d_lidx, d_lx, d_lvw, d_lbins;  // screened work list of a VEGAS pass
+  DevBuf      d_lidx, d_lx, d_lvw, d_lbins, d_lbins_hi;  // screened work list of a VEGAS pass
   DevBuf      d_recf, d_recd;                // loop records (record mode), shared by calls
   double     *h_sc = nullptr;  // pinned
   double      sumdata = 0, sumchi2 = 0, sweight = 0;
@@ -211,6 +211,32 @@ grn_status derive_consts(const grn_process_params &P, grn::Consts &K) {
     K.n_res = P.n_res;
   }
   if (P.n_central != 2) return fail(GRN_ERR_UNSUPPORTED, "only 2-body central states");
+  if (P.n_decay != 0 && P.n_decay != 2)
+    return fail(GRN_ERR_UNSUPPORTED, "central decays: none or two-body cascades of both");
+  if (P.central_spin != 0 && P.central_spin != 1)
+    return fail(GRN_ERR_UNSUPPORTED, "central particles of spin 0 or 1");
+  if (P.n_decay == 2) {
+    if (P.phase_space != GRN_PS_FACTORIZED)
+      return fail(GRN_ERR_UNSUPPORTED, "decay cascades are implemented in the <F> class");
+    if (P.process == GRN_PROC_TENSOR_RES)
+      return fail(GRN_ERR_UNSUPPORTED, "RESTENSOR decays directly to two pseudoscalars");
+    for (int k = 0; k < 4; ++k)
+      if (!(P.m_daughter[k] >= 0))
+        return fail(GRN_ERR_INVALID, "daughter masses must be non-negative");
+    for (int k = 0; k < 2; ++k)
+      if (!(P.width[k] >= 0) ||
+          !(P.m_central[k] + 5.0 * P.width[k] > P.m_daughter[2 * k] + P.m_daughter[2 * k + 1]))
+        return fail(GRN_ERR_INVALID, "central width, or decay kinematically closed");
+  }
+  if (P.process == GRN_PROC_TENSOR_CON && P.central_spin == 1) {
+    if (!(P.tensor.gPvv[0] != 0 || P.tensor.gPvv[1] != 0))
+      return fail(GRN_ERR_INVALID, "tensor-pomeron vector couplings gPvv are not set");
+    // unstable vector mesons: the reference draws their masses (GetOffShellMass)
+    if (P.n_decay != 2)
+      return fail(GRN_ERR_UNSUPPORTED, "vector-meson pairs need their two-body decays");
+  }
+  if (P.process == GRN_PROC_TENSOR_RES && P.central_spin != 0)
+    return fail(GRN_ERR_UNSUPPORTED, "RESTENSOR decays to pseudoscalars");
   if (!(P.sqrt_s > 2 * P.m_beam)) return fail(GRN_ERR_INVALID, "sqrt_s below threshold");
   if (!(P.gcuts.fpt_max > 0) || !(P.gcuts.kt_max > P.gcuts.kt_min) ||
       !(P.gcuts.rap_max > P.gcuts.rap_min))
@@ -246,11 +272,13 @@ grn_status derive_consts(const grn_process_params &P, grn::Consts &K) {
     K.M2min = Mmin * Mmin;
     K.M2max = Mmax * Mmax;
     // dPhi2/(2 pi) = p*/(8 pi^2 M_X) with p*/M_X per event; B51PhaseSpaceWeight,
-    // B51IntegralVolume (MFactorized.cc:418-450), ForwardVolume.
+    // B51IntegralVolume (MFactorized.cc:418-450), ForwardVolume. The mass^2 window of the
+    // volume is per event (it depends on the off-shell masses of a cascade) and sits in
+    // the per-event Jacobian factor with p*/M_X.
     const double fwd = std::pow(2.0 * kPi, 2) * fwd_log * fwd_log;
     K.w_const = (1.0 / P.s_factor) * (1.0 / (8.0 * kPi * kPi)) * 0.5 *
-                (1.0 / std::pow(2.0 * kPi, 5)) * (K.M2max - K.M2min) *
-                (P.gcuts.Y_max - P.gcuts.Y_min) * fwd * kGeV2barn / (2.0 * K.s);
+                (1.0 / std::pow(2.0 * kPi, 5)) * (P.gcuts.Y_max - P.gcuts.Y_min) * fwd *
+                kGeV2barn / (2.0 * K.s);
   }
   K.M2prop = K.m3sq;
   K.g2     = std::pow(P.regge.c[0] / P.soft.gN_P, 2);
@@ -442,6 +470,7 @@ grn_status grn_create(const grn_process_params *p, int32_t device, grn_engine **
   e->device     = device;
   e->P          = *p;
   e->K          = K;
+  e->dim        = p->n_decay == 2 ? 14 : 8;
   cudaError_t ce = cudaStreamCreateWithFlags(&e->stream, cudaStreamNonBlocking);
   if (ce == cudaSuccess) ce = cudaMallocHost(&e->h_sc, grn::VS_COUNT * sizeof(double));
   if (ce == cudaSuccess) ce = cudaEventCreate(&e->ev0);
@@ -464,6 +493,7 @@ grn_status grn_destroy(grn_engine *e) {
                     &e->d_wlist, &e->d_wcount, &e->d_xmat,      &e->d_xmat_prev, &e->d_f2mat,
                     &e->d_f,     &e->d_acc,    &e->d_parts,     &e->d_sc,        &e->d_lidx,
                     &e->d_lx,    &e->d_lvw,    &e->d_lbins,     &e->d_uw_counts, &e->d_uw_misc,
+                    &e->d_lbins_hi,
                     &e->d_uw_idx, &e->d_recf,  &e->d_recd,      &e->d_xmat_flat};
   for (DevBuf *b : bufs) b->release();
   for (grn_flow *f : e->flows) f->e = nullptr;  // they stay valid for grn_flow_destroy
@@ -564,7 +594,7 @@ grn_status grn_eikonal_set(grn_engine *e, int32_t n_bt, const double *mbt, int32
 grn_status grn_event_weights(grn_engine *e, const double *u, int64_t n, int32_t dim,
                              double *w_out, uint8_t *flags, int32_t prec) {
   if (!e || !u || !w_out || n < 0) return fail(GRN_ERR_INVALID, "null argument");
-  if (dim != e->dim) return fail(GRN_ERR_INVALID, "dim must equal grn_dim() = 8");
+  if (dim != e->dim) return fail(GRN_ERR_INVALID, "dim must equal grn_dim()");
   if (prec != GRN_PREC_FP64 && prec != GRN_PREC_MIXED) return fail(GRN_ERR_INVALID, "bad prec");
   grn_status st = require_screening_ready(e);
   if (st != GRN_OK) return st;
@@ -616,7 +646,7 @@ grn_status grn_event_weights(grn_engine *e, const double *u, int64_t n, int32_t 
 grn_status grn_event_kinematics(grn_engine *e, const double *u, int64_t n, int32_t dim,
                                 double *p4_out, double *ts_out, uint8_t *flags) {
   if (!e || !u || n < 0) return fail(GRN_ERR_INVALID, "null argument");
-  if (dim != e->dim) return fail(GRN_ERR_INVALID, "dim must equal grn_dim() = 8");
+  if (dim != e->dim) return fail(GRN_ERR_INVALID, "dim must equal grn_dim()");
   if (n == 0) return GRN_OK;
   GRN_CUDA(cudaSetDevice(e->device));
   // Host-staged path only (diagnostics / record building).
@@ -660,14 +690,20 @@ grn_status grn_uniforms(grn_engine *e, uint64_t seed, uint32_t stream, int64_t f
 // ---------------------------------------------------------------------------
 // VEGAS
 
+// Bin indices of dimensions 8..15 of the screened work list (null for 8 dimensions).
+static uint64_t *lbins_hi(grn_engine *e) {
+  return e->dim > 8 ? e->d_lbins_hi.as<uint64_t>() : nullptr;
+}
+
 // Per-call buffers of a VEGAS pass: f values and the screened work list.
 static grn_status vegas_alloc_calls(grn_engine *e, int64_t ncall) {
   const size_t n = static_cast<size_t>(std::max<int64_t>(ncall, 1));
   GRN_CUDA(e->d_f.ensure(n * sizeof(double)));
   GRN_CUDA(e->d_lidx.ensure(n * sizeof(int64_t)));
-  GRN_CUDA(e->d_lx.ensure(8 * n * sizeof(double)));
+  GRN_CUDA(e->d_lx.ensure(static_cast<size_t>(e->dim) * n * sizeof(double)));
   GRN_CUDA(e->d_lvw.ensure(n * sizeof(double)));
   GRN_CUDA(e->d_lbins.ensure(n * sizeof(uint64_t)));
+  if (e->dim > 8) GRN_CUDA(e->d_lbins_hi.ensure(n * sizeof(uint64_t)));
   if (e->P.screening) {
     GRN_CUDA(e->d_recf.ensure(n * grn::kLoopEventFields * sizeof(float)));
     GRN_CUDA(e->d_recd.ensure(n * grn::kRecordDoubles * sizeof(double)));
@@ -758,7 +794,8 @@ static grn_status vegas_pass(grn_engine *e, int prec, int track_max, int refine,
                                   stream_id, track_max, e->d_f.as<double>(),
                                   e->d_f2mat.as<double>(), e->d_acc.as<unsigned long long>(),
                                   e->d_lidx.as<int64_t>(), e->d_lx.as<double>(),
-                                  e->d_lvw.as<double>(), e->d_lbins.as<uint64_t>(), rf, rd,
+                                  e->d_lvw.as<double>(), e->d_lbins.as<uint64_t>(), lbins_hi(e),
+                                  rf, rd,
                                   e->stream, fu, flq));
   // the timed kernel: the kt-loop stage when screening is on
   GRN_CUDA(cudaEventRecord(e->ev0, e->stream));
@@ -766,7 +803,8 @@ static grn_status vegas_pass(grn_engine *e, int prec, int track_max, int refine,
                                   e->d_f.as<double>(), e->d_f2mat.as<double>(),
                                   e->d_acc.as<unsigned long long>(), e->d_lidx.as<int64_t>(),
                                   e->d_lx.as<double>(), e->d_lvw.as<double>(),
-                                  e->d_lbins.as<uint64_t>(), rf, rd, e->nblocks, e->stream));
+                                  e->d_lbins.as<uint64_t>(), lbins_hi(e), rf, rd, e->nblocks,
+                                  e->stream));
   GRN_CUDA(cudaEventRecord(e->ev1, e->stream));
   GRN_CUDA(grn::launch_vegas_reduce(e->d_f.as<double>(), e->ncall,
                                     e->d_acc.as<unsigned long long>(), e->d_parts.as<double>(),
@@ -1087,6 +1125,7 @@ struct grn_batch {
   DevBuf                    d_counter;        // work queues of the two stage-B kinds
   grn::BatchProc           *h_procs = nullptr;  // pinned: uploaded by the graph every pass
   int                       born_blocks = 0, loop_blocks = 0;
+  int                       max_dim     = 8;  // largest hypercube dimension of the batch
   bool                      has_kind[2] = {false, false};  // generic / record-mode processes
   cudaStream_t              side = nullptr;     // second branch of the captured graph
   cudaEvent_t               fork = nullptr, join = nullptr;
@@ -1114,7 +1153,7 @@ grn_status batch_capture(grn_batch *b, int refine, int track_max) {
   }
   if (ce == cudaSuccess)
     ce = cudaMemsetAsync(b->d_counter.p, 0, sizeof(unsigned long long), b->stream);
-  if (ce == cudaSuccess) ce = grn::launch_batch_born(np, b->born_blocks, b->stream);
+  if (ce == cudaSuccess) ce = grn::launch_batch_born(np, b->born_blocks, b->max_dim, b->stream);
   // stage B: the record-mode processes in one persistent launch; the processes on the
   // generic loop in their own launches on a second branch of the graph (concurrent)
   const bool two = b->has_kind[0] && b->has_kind[1];
@@ -1130,7 +1169,8 @@ grn_status batch_capture(grn_batch *b, int refine, int track_max) {
                                 track_max, e->d_f.as<double>(), e->d_f2mat.as<double>(),
                                 e->d_acc.as<unsigned long long>(), e->d_lidx.as<int64_t>(),
                                 e->d_lx.as<double>(), e->d_lvw.as<double>(),
-                                e->d_lbins.as<uint64_t>(), nullptr, nullptr, e->nblocks,
+                                e->d_lbins.as<uint64_t>(), lbins_hi(e), nullptr, nullptr,
+                                e->nblocks,
                                 two ? b->side : b->stream);
   }
   if (ce == cudaSuccess && two) ce = cudaEventRecord(b->join, b->side);
@@ -1224,6 +1264,8 @@ grn_status grn_batch_create(grn_engine *const *engines, int32_t n, grn_batch **o
     q.l_x       = e->d_lx.as<double>();
     q.l_vw      = e->d_lvw.as<double>();
     q.l_bins    = e->d_lbins.as<uint64_t>();
+    q.l_bins_hi = lbins_hi(e);
+    b->max_dim  = std::max(b->max_dim, e->dim);
     q.rf        = rec ? e->d_recf.as<float>() : nullptr;
     q.rd        = rec ? e->d_recd.as<double>() : nullptr;
     if (e->P.screening) b->has_kind[rec ? 1 : 0] = true;

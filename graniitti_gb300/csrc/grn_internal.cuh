@@ -24,6 +24,7 @@ struct KArgs {
 };
 
 constexpr int kMaxLoopNodes = 256;  // per axis
+constexpr int kMaxDim       = 16;   // hypercube dimensions: 8 (2-body), 14 (two-body cascades)
 
 // Scalars accumulated per block by the VEGAS sampling kernel.
 enum VegasScalar {
@@ -62,22 +63,22 @@ int         vegas_grid_blocks(int device);
 cudaError_t launch_vegas_grid_init(double *xmat, int bins, int dim, cudaStream_t st);
 // One VEGAS pass in two stages; acc holds VS_COUNT + 1 unsigned long long
 // accumulators (the last one is the work-list length); the list arrays have
-// capacity ncall (l_x: 8 x ncall, dimension-major).
+// capacity ncall (l_x: dim x ncall, dimension-major; l_bins_hi only for dim > 8).
 // rf/rd: loop records (record mode, see record_mode()); null for the point mode,
 // in which the mapped points l_x are stored and stage B recomputes the tree level.
 cudaError_t launch_vegas_born(const KArgs &a, const double *xmat, int bins, int dim, int64_t ncall,
                               uint64_t seed, uint32_t stream, int track_max, double *f_out,
                               double *f2mat, unsigned long long *acc, int64_t *l_idx, double *l_x,
-                              double *l_vw, uint64_t *l_bins, float *rf, double *rd,
-                              cudaStream_t st, const float *fu = nullptr,
+                              double *l_vw, uint64_t *l_bins, uint64_t *l_bins_hi, float *rf,
+                              double *rd, cudaStream_t st, const float *fu = nullptr,
                               const float *flq = nullptr);
 // fu / flq: points drawn from the flow (dimension-major, leading dimension ncall) and
 // their log density; the VEGAS weight of a point is then vw(u) / q(u).
 cudaError_t launch_vegas_loop(const KArgs &a, int prec, int bins, int dim, int64_t ncall,
                               int track_max, double *f_out, double *f2mat, unsigned long long *acc,
                               const int64_t *l_idx, const double *l_x, const double *l_vw,
-                              const uint64_t *l_bins, const float *rf, const double *rd,
-                              int nblocks, cudaStream_t st);
+                              const uint64_t *l_bins, const uint64_t *l_bins_hi, const float *rf,
+                              const double *rd, int nblocks, cudaStream_t st);
 // Record mode: screened, FP32 loop, single active trajectory.
 bool        record_mode(const KArgs &a, int prec);
 constexpr int kRecordDoubles = 4;
@@ -126,7 +127,7 @@ struct BatchProc {
   unsigned long long *acc;
   int64_t            *l_idx;
   double             *l_x, *l_vw;
-  uint64_t           *l_bins;
+  uint64_t           *l_bins, *l_bins_hi;  // bin indices of dimensions 0..7, 8..15
   float              *rf;
   double             *rd;
   int                 blk0, blk1;  // stage-A blocks of this process: [blk0, blk1)
@@ -134,7 +135,7 @@ struct BatchProc {
 // The process table of a batch, copied into constant memory (stream-ordered).
 cudaError_t upload_batch_procs(const BatchProc *h_procs, int np, cudaStream_t st);
 // Stage A of every process in one launch (block b serves the process whose range holds b).
-cudaError_t launch_batch_born(int np, int nblocks, cudaStream_t st);
+cudaError_t launch_batch_born(int np, int nblocks, int max_dim, cudaStream_t st);
 // Stage B of the record-mode processes in one persistent launch (two events per thread):
 // blocks take chunks of work from the counter (zeroed by the caller) over the listed events
 // of those processes.

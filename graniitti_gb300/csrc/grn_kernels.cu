@@ -127,6 +127,51 @@ __device__ cx<double> loop_integral_fast(const KArgs &A, const Born &b, const Kt
   return {A.loop_norm_re * sr - A.loop_norm_im * si, A.loop_norm_re * si + A.loop_norm_im * sr};
 }
 
+// Screened |M|^2 of a vector pair: the nine helicity amplitudes in the polarization basis
+// of the (loop-invariant) central pair, each screened on its own (S3ScreenedAmp2 screens every
+// entry of lts.hamp), |A0_h + A_loop,h|^2 summed. The complex node weight U_i c_j is applied
+// per point so that only the nine compensated sums stay live.
+template <typename T>
+__device__ double screened_amp2_vv(const KArgs &A, const Born &b, const KtNode<T> *skt,
+                                   const PhiNode<T> *sphi) {
+  cx<double> A0[9];
+  born_amps_2xv(A.P, A.K, b, A0);
+  LoopEvent<T> e;
+  make_loop_event<T>(A.K, b, e);
+  LV<T> e3[3], e4[3];
+  vector_basis<T>(T(b.p3p), T(b.p3m), T(b.p3x), T(b.p3y), e3);
+  vector_basis<T>(T(b.p4p), T(b.p4m), T(b.p4x), T(b.p4y), e4);
+  const T s34 = T(b.m2);
+  T sr[9], si[9], cr[9], ci[9];
+#pragma unroll
+  for (int h = 0; h < 9; ++h) sr[h] = si[h] = cr[h] = ci[h] = T(0);
+  for (int j = 0; j < A.n_kt_nodes; ++j) {
+    const KtNode<T> nj = skt[j];
+    for (int i = 0; i < A.n_phi_nodes; ++i) {
+      const PhiNode<T> ni = sphi[i];
+      LCKin<T>         kk;
+      if (!loop_point_kin<T>(e, nj.kt * ni.c, nj.kt * ni.s, kk)) continue;
+      cx<T> a[9];
+      tensor_me4_2xv<T>(A.P, A.K, kk, s34, e3, e4, a);
+      const T wr = ni.u * nj.cre, wi = ni.u * nj.cim;
+#pragma unroll
+      for (int h = 0; h < 9; ++h) {
+        kahan_add(sr[h], cr[h], wr * a[h].re - wi * a[h].im);
+        kahan_add(si[h], ci[h], wr * a[h].im + wi * a[h].re);
+      }
+    }
+  }
+  double amp2 = 0.0;
+#pragma unroll
+  for (int h = 0; h < 9; ++h) {
+    const double xr = double(sr[h]), xi = double(si[h]);
+    const double re = A0[h].re + (A.loop_norm_re * xr - A.loop_norm_im * xi);
+    const double im = A0[h].im + (A.loop_norm_re * xi + A.loop_norm_im * xr);
+    amp2 += re * re + im * im;
+  }
+  return amp2;
+}
+
 template <typename T>
 __device__ __forceinline__ cx<double> loop_dispatch(const KArgs &A, const Born &b,
                                                     const KtNode<T> *skt, const PhiNode<T> *sphi) {
@@ -261,17 +306,18 @@ __device__ __forceinline__ void record_weights2(const KArgs &A, const LoopEventF
 
 // Tree-level stage of one event: kinematics, cuts and, when the process is not
 // screened, the full weight. Returns true when the event still needs the kt-loop.
+// CASC: instantiation for 14-dimensional points (two-body cascades, vector pairs).
+template <bool CASC>
 __device__ __forceinline__ bool born_stage(const KArgs &A, const double *x, Born &b, double &W,
                                            uint8_t &flags) {
-  const bool kin = born_kinematics(A.P, A.K, x, b);
+  const bool kin = born_kinematics<CASC>(A.P, A.K, x, b);
   const bool fid = kin && fiducial_cuts(A.P, A.K, b);
   flags = (kin ? GRN_FLAG_KINEMATICS_OK : 0) | (fid ? GRN_FLAG_FIDCUTS_OK : 0) |
           GRN_FLAG_VETOCUTS_OK | GRN_FLAG_AMPLITUDE_OK;
   W = 0.0;
   if (!(kin && fid)) return false;
   if (A.P.screening) return true;
-  const cx<double> A0 = born_amp(A.P, A.K, b);
-  W = weight_jacobian(A.K, b) * (A0.re * A0.re + A0.im * A0.im);
+  W = weight_jacobian(A.K, b) * born_amp2<CASC>(A.P, A.K, b);
   if (!isfinite(W)) {
     W = 0.0;
     flags &= ~GRN_FLAG_AMPLITUDE_OK;
@@ -281,15 +327,21 @@ __device__ __forceinline__ bool born_stage(const KArgs &A, const double *x, Born
 
 // Screened weight of an event that passed the cuts (MContinuum::EventWeight with
 // MProcess::S3ScreenedAmp2, src/MContinuum.cc:164-193, src/MProcess.cc:157-288).
-template <typename T>
+template <typename T, bool CASC>
 __device__ double screened_weight(const KArgs &A, const double *x, uint8_t &flags,
                                   const KtNode<T> *skt, const PhiNode<T> *sphi) {
   Born b;
-  born_kinematics(A.P, A.K, x, b);
-  const cx<double> A0 = born_amp(A.P, A.K, b);
-  const cx<double> Al = loop_dispatch<T>(A, b, skt, sphi);
-  const double re = A0.re + Al.re, im = A0.im + Al.im;
-  double W = weight_jacobian(A.K, b) * (re * re + im * im);
+  born_kinematics<CASC>(A.P, A.K, x, b);
+  double amp2;
+  if (CASC && is_vector_pair(A.P)) {
+    amp2 = screened_amp2_vv<T>(A, b, skt, sphi);
+  } else {
+    const cx<double> A0 = born_amp(A.P, A.K, b);
+    const cx<double> Al = loop_dispatch<T>(A, b, skt, sphi);
+    const double re = A0.re + Al.re, im = A0.im + Al.im;
+    amp2 = re * re + im * im;
+  }
+  double W = weight_jacobian(A.K, b) * amp2;
   flags = GRN_FLAG_KINEMATICS_OK | GRN_FLAG_FIDCUTS_OK | GRN_FLAG_VETOCUTS_OK |
           GRN_FLAG_AMPLITUDE_OK;
   if (!isfinite(W)) {
@@ -325,19 +377,20 @@ __device__ __forceinline__ int64_t list_append(bool pred, unsigned long long *co
 constexpr int kWeightThreads = 128;
 
 // Stage A over a user point array: cuts, unscreened weights, screened work list.
+template <int MAXD>
 __global__ void __launch_bounds__(kWeightThreads)
     k_weights_born(const KArgs A, const double *__restrict__ u, int64_t n, int dim,
                    double *__restrict__ w, uint8_t *__restrict__ flags,
                    int64_t *__restrict__ list, unsigned long long *__restrict__ count) {
   const int64_t i = static_cast<int64_t>(blockIdx.x) * blockDim.x + threadIdx.x;
   if (i >= n) return;
-  double x[8];
+  double x[MAXD];
 #pragma unroll
-  for (int d = 0; d < 8; ++d) x[d] = u[i * dim + d];
+  for (int d = 0; d < MAXD; ++d) x[d] = d < dim ? u[i * dim + d] : 0.0;
   Born       b;
   double     W;
   uint8_t    f;
-  const bool loop = born_stage(A, x, b, W, f);
+  const bool loop = born_stage<(MAXD > 8)>(A, x, b, W, f);
   const int64_t slot = list_append(loop, count);
   if (loop) {
     list[slot] = i;
@@ -348,7 +401,7 @@ __global__ void __launch_bounds__(kWeightThreads)
 }
 
 // Stage B: the kt-loop for the listed events (every lane does a full loop).
-template <typename T>
+template <typename T, int MAXD>
 __global__ void __launch_bounds__(kWeightThreads)
     k_weights_loop(const KArgs A, const double *__restrict__ u, int dim,
                    const int64_t *__restrict__ list, const unsigned long long *__restrict__ count,
@@ -361,11 +414,11 @@ __global__ void __launch_bounds__(kWeightThreads)
   for (int64_t r = static_cast<int64_t>(blockIdx.x) * blockDim.x + threadIdx.x; r < cnt;
        r += static_cast<int64_t>(gridDim.x) * blockDim.x) {
     const int64_t i = list[r];
-    double x[8];
+    double x[MAXD];
 #pragma unroll
-    for (int d = 0; d < 8; ++d) x[d] = u[i * dim + d];
+    for (int d = 0; d < MAXD; ++d) x[d] = d < dim ? u[i * dim + d] : 0.0;
     uint8_t f;
-    w[i] = screened_weight<T>(A, x, f, skt, sphi);
+    w[i] = screened_weight<T, (MAXD > 8)>(A, x, f, skt, sphi);
     if (flags) flags[i] = f;
   }
 }
@@ -373,7 +426,8 @@ __global__ void __launch_bounds__(kWeightThreads)
 int loop_grid_blocks(int device) {
   int sms = 0, per = 0;
   cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, device);
-  cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, k_weights_loop<float>, kWeightThreads, 0);
+  cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, k_weights_loop<float, 8>, kWeightThreads,
+                                                0);
   return sms * (per < 1 ? 1 : per);
 }
 
@@ -383,19 +437,33 @@ cudaError_t launch_event_weights(const KArgs &a, int prec, const double *u, int6
   if (n <= 0) return cudaSuccess;
   cudaMemsetAsync(count, 0, sizeof(unsigned long long), st);
   const unsigned blocks = static_cast<unsigned>((n + kWeightThreads - 1) / kWeightThreads);
-  k_weights_born<<<blocks, kWeightThreads, 0, st>>>(a, u, n, dim, w, flags, list, count);
+  if (dim <= 8)
+    k_weights_born<8><<<blocks, kWeightThreads, 0, st>>>(a, u, n, dim, w, flags, list, count);
+  else
+    k_weights_born<kMaxDim><<<blocks, kWeightThreads, 0, st>>>(a, u, n, dim, w, flags, list,
+                                                                count);
   if (a.P.screening) {
-    if (prec == GRN_PREC_MIXED)
-      k_weights_loop<float><<<loop_blocks, kWeightThreads, 0, st>>>(a, u, dim, list, count, w,
-                                                                    flags);
-    else
-      k_weights_loop<double><<<loop_blocks, kWeightThreads, 0, st>>>(a, u, dim, list, count, w,
-                                                                     flags);
+    if (dim <= 8) {
+      if (prec == GRN_PREC_MIXED)
+        k_weights_loop<float, 8><<<loop_blocks, kWeightThreads, 0, st>>>(a, u, dim, list, count,
+                                                                         w, flags);
+      else
+        k_weights_loop<double, 8><<<loop_blocks, kWeightThreads, 0, st>>>(a, u, dim, list,
+                                                                          count, w, flags);
+    } else {
+      if (prec == GRN_PREC_MIXED)
+        k_weights_loop<float, kMaxDim><<<loop_blocks, kWeightThreads, 0, st>>>(
+            a, u, dim, list, count, w, flags);
+      else
+        k_weights_loop<double, kMaxDim><<<loop_blocks, kWeightThreads, 0, st>>>(
+            a, u, dim, list, count, w, flags);
+    }
   }
   return cudaGetLastError();
 }
 
 // Record-mode user-array stages (FP32 loop, single active trajectory).
+template <int MAXD>
 __global__ void __launch_bounds__(kWeightThreads)
     k_weights_born_rec(const KArgs A, const double *__restrict__ u, int64_t n, int dim,
                        double *__restrict__ w, uint8_t *__restrict__ flags,
@@ -403,13 +471,13 @@ __global__ void __launch_bounds__(kWeightThreads)
                        double *__restrict__ rd, unsigned long long *__restrict__ count) {
   const int64_t i = static_cast<int64_t>(blockIdx.x) * blockDim.x + threadIdx.x;
   if (i >= n) return;
-  double x[8];
+  double x[MAXD];
 #pragma unroll
-  for (int d = 0; d < 8; ++d) x[d] = u[i * dim + d];
+  for (int d = 0; d < MAXD; ++d) x[d] = d < dim ? u[i * dim + d] : 0.0;
   Born       b;
   double     W;
   uint8_t    f;
-  const bool loop = born_stage(A, x, b, W, f);
+  const bool loop = born_stage<(MAXD > 8)>(A, x, b, W, f);
   const int64_t slot = list_append(loop, count);
   if (loop) {
     LoopEventF<float> e;
@@ -486,8 +554,12 @@ cudaError_t launch_weights_born_rec(const KArgs &a, const double *u, int64_t n, 
   cudaError_t e = cudaMemsetAsync(count, 0, sizeof(unsigned long long), st);
   if (e != cudaSuccess) return e;
   const unsigned blocks = static_cast<unsigned>((n + kWeightThreads - 1) / kWeightThreads);
-  k_weights_born_rec<<<blocks, kWeightThreads, 0, st>>>(a, u, n, dim, w, flags, list, rf, rd,
-                                                         count);
+  if (dim <= 8)
+    k_weights_born_rec<8><<<blocks, kWeightThreads, 0, st>>>(a, u, n, dim, w, flags, list, rf,
+                                                              rd, count);
+  else
+    k_weights_born_rec<kMaxDim><<<blocks, kWeightThreads, 0, st>>>(a, u, n, dim, w, flags, list,
+                                                                    rf, rd, count);
   return cudaGetLastError();
 }
 
@@ -520,11 +592,10 @@ __global__ void k_event_kinematics(const KArgs A, const double *__restrict__ u, 
                                    uint8_t *__restrict__ flags) {
   const int64_t i = static_cast<int64_t>(blockIdx.x) * blockDim.x + threadIdx.x;
   if (i >= n) return;
-  double x[8];
-#pragma unroll
-  for (int d = 0; d < 8; ++d) x[d] = u[i * dim + d];
+  double x[kMaxDim];
+  for (int d = 0; d < kMaxDim; ++d) x[d] = d < dim ? u[i * dim + d] : 0.0;
   Born       b;
-  const bool kin = born_kinematics(A.P, A.K, x, b);
+  const bool kin = born_kinematics<true>(A.P, A.K, x, b);
   const bool fid = kin && fiducial_cuts(A.P, A.K, b);
   if (p4) {
     double *o = p4 + i * 16;
@@ -751,15 +822,16 @@ cudaError_t launch_eikonal_xs(const double *mbt, int n_bt, double *xs, cudaStrea
 
 constexpr int kVegasThreads = 128;
 constexpr int kMaxBins      = 256;
-constexpr int kMaxDim       = 8;
 
 // Map a uniform point through the VEGAS grid in shared memory
 // (MGraniitti::VEGASMultiThread, src/MGraniitti.cc:1357-1375).
+// Bin indices are packed 8 bits per dimension: dimensions 0..7 in lo, 8..15 in hi.
 __device__ __forceinline__ double vegas_map(const double *sx, int bins, int dim, const double *u,
-                                            double *x, uint64_t &packed_bins) {
+                                            double *x, uint64_t &packed_bins, uint64_t &packed_hi) {
   const double dbins = static_cast<double>(bins);
   double       vw    = 1.0;
   packed_bins        = 0ull;
+  packed_hi          = 0ull;
   for (int j = 0; j < dim; ++j) {
     const double zn = u[j] * dbins + 1.0;
     int          k  = static_cast<int>(zn);
@@ -773,7 +845,10 @@ __device__ __forceinline__ double vegas_map(const double *sx, int bins, int dim,
       ac = (zn - k) * zo;
     }
     x[j] = ac;
-    packed_bins |= static_cast<uint64_t>(k - 1) << (8 * j);
+    if (j < 8)
+      packed_bins |= static_cast<uint64_t>(k - 1) << (8 * j);
+    else
+      packed_hi |= static_cast<uint64_t>(k - 1) << (8 * (j - 8));
     vw *= zo * dbins;
   }
   return vw;
@@ -785,10 +860,11 @@ struct VegasBlockAcc {
   double *sf2;  // shared f^2 histogram (bins * dim)
 };
 
-__device__ __forceinline__ void hist_add(double *sf2, int dim, uint64_t packed, double f2) {
+__device__ __forceinline__ void hist_add(double *sf2, int dim, uint64_t packed, uint64_t hi,
+                                         double f2) {
   if (f2 == 0.0) return;
   for (int j = 0; j < dim; ++j) {
-    const int b = static_cast<int>((packed >> (8 * j)) & 0xFFu);
+    const int b = static_cast<int>(((j < 8 ? packed : hi) >> (8 * (j & 7))) & 0xFFu);
     atomicAdd(&sf2[b * dim + j], f2);
   }
 }
@@ -820,13 +896,14 @@ __device__ void flush_block(double *sf2, int nh, double *f2mat, unsigned long lo
 // cuts. Rejected and unscreened events are finished here; screened events that pass the
 // cuts go to the work list (index, VEGAS weight, bins, and the loop record or the mapped
 // point). Block `bid` of `nbid` blocks serving this pass; dsm: 2 * bins * dim doubles.
+template <int MAXD>
 __device__ __forceinline__ void born_pass_body(
     const KArgs &A, const double *__restrict__ xmat, int bins, int dim, int64_t ncall,
     uint64_t seed, uint32_t stream, int track_max, double *__restrict__ f_out,
     double *__restrict__ f2mat, unsigned long long *__restrict__ acc, int64_t *__restrict__ l_idx,
     double *__restrict__ l_x, double *__restrict__ l_vw, uint64_t *__restrict__ l_bins,
-    int64_t cap, float *__restrict__ rf, double *__restrict__ rd, const float *__restrict__ fu,
-    const float *__restrict__ flq, double *dsm, int bid, int nbid) {
+    uint64_t *__restrict__ l_bins_hi, int64_t cap, float *__restrict__ rf, double *__restrict__ rd,
+    const float *__restrict__ fu, const float *__restrict__ flq, double *dsm, int bid, int nbid) {
   double   *sx = dsm, *sf2 = dsm + bins * dim;
   const int nh = bins * dim;
   for (int i = threadIdx.x; i < nh; i += blockDim.x) {
@@ -842,21 +919,21 @@ __device__ __forceinline__ void born_pass_body(
        e += stride) {
     const bool active = e < ncall;
     bool       loop   = false;
-    double     x[kMaxDim], vw = 0.0;
-    uint64_t   pb = 0ull;
+    double     x[MAXD], vw = 0.0;
+    uint64_t   pb = 0ull, pbh = 0ull;
     Born       b;
     if (active) {
-      double u[kMaxDim];
+      double u[MAXD];
       if (fu) {
         for (int j = 0; j < dim; ++j) u[j] = fu[static_cast<int64_t>(j) * ncall + e];
       } else {
         philox_point(seed, stream, static_cast<uint64_t>(e), dim, u);
       }
-      vw = vegas_map(sx, bins, dim, u, x, pb);
+      vw = vegas_map(sx, bins, dim, u, x, pb, pbh);
       if (flq) vw *= exp(-static_cast<double>(flq[e]));
       double  W;
       uint8_t fl;
-      loop = born_stage(A, x, b, W, fl);
+      loop = born_stage<(MAXD > 8)>(A, x, b, W, fl);
       cnt[VS_EVAL] += 1;
       cnt[VS_KIN_OK] += (fl & GRN_FLAG_KINEMATICS_OK) ? 1 : 0;
       cnt[VS_FID_OK] += (fl & GRN_FLAG_FIDCUTS_OK) ? 1 : 0;
@@ -864,7 +941,7 @@ __device__ __forceinline__ void born_pass_body(
       if (!loop) {
         const double f = W * vw;
         f_out[e]       = f;
-        hist_add(sf2, dim, pb, f * f);
+        hist_add(sf2, dim, pb, pbh, f * f);
         cnt[VS_AMP_OK] += (fl & GRN_FLAG_AMPLITUDE_OK) ? 1 : 0;
         cnt[VS_NAN] += (fl & GRN_FLAG_AMPLITUDE_OK) ? 0 : 1;
         if (track_max) {
@@ -878,40 +955,44 @@ __device__ __forceinline__ void born_pass_body(
       l_idx[slot]  = e;
       l_vw[slot]   = vw;
       l_bins[slot] = pb;
+      if (l_bins_hi) l_bins_hi[slot] = pbh;
       if (rf) {
         LoopEventF<float> le;
         double            a0r, a0i;
         make_loop_event_fast<float>(A.P, A.K, b, le, &a0r, &a0i);
         store_record(le, a0r, a0i, weight_jacobian(A.K, b), rf, rd, slot, cap);
       } else {
-        for (int j = 0; j < kMaxDim; ++j) l_x[static_cast<int64_t>(j) * cap + slot] = x[j];
+        for (int j = 0; j < MAXD; ++j)
+          if (j < dim) l_x[static_cast<int64_t>(j) * cap + slot] = x[j];
       }
     }
   }
   flush_block(sf2, nh, f2mat, acc, cnt, maxf, maxW);
 }
 
+template <int MAXD>
 __global__ void __launch_bounds__(kVegasThreads)
     k_vegas_born(const KArgs A, const double *__restrict__ xmat, int bins, int dim, int64_t ncall,
                  uint64_t seed, uint32_t stream, int track_max, double *__restrict__ f_out,
                  double *__restrict__ f2mat, unsigned long long *__restrict__ acc,
                  int64_t *__restrict__ l_idx, double *__restrict__ l_x, double *__restrict__ l_vw,
-                 uint64_t *__restrict__ l_bins, int64_t cap, float *__restrict__ rf,
-                 double *__restrict__ rd, const float *__restrict__ fu,
+                 uint64_t *__restrict__ l_bins, uint64_t *__restrict__ l_bins_hi, int64_t cap,
+                 float *__restrict__ rf, double *__restrict__ rd, const float *__restrict__ fu,
                  const float *__restrict__ flq) {
   extern __shared__ double dsm[];
-  born_pass_body(A, xmat, bins, dim, ncall, seed, stream, track_max, f_out, f2mat, acc, l_idx,
-                 l_x, l_vw, l_bins, cap, rf, rd, fu, flq, dsm, blockIdx.x, gridDim.x);
+  born_pass_body<MAXD>(A, xmat, bins, dim, ncall, seed, stream, track_max, f_out, f2mat, acc,
+                       l_idx, l_x, l_vw, l_bins, l_bins_hi, cap, rf, rd, fu, flq, dsm, blockIdx.x,
+                       gridDim.x);
 }
 
 // Stage B of a VEGAS pass: screened weights of the listed events.
-template <typename T>
+template <typename T, int MAXD>
 __global__ void __launch_bounds__(kVegasThreads)
     k_vegas_loop(const KArgs A, int bins, int dim, int track_max, double *__restrict__ f_out,
                  double *__restrict__ f2mat, unsigned long long *__restrict__ acc,
                  const int64_t *__restrict__ l_idx, const double *__restrict__ l_x,
                  const double *__restrict__ l_vw, const uint64_t *__restrict__ l_bins,
-                 int64_t cap) {
+                 const uint64_t *__restrict__ l_bins_hi, int64_t cap) {
   extern __shared__ double dsm[];
   double *sf2 = dsm;
   __shared__ KtNode<T>  skt[kMaxLoopNodes];
@@ -926,13 +1007,13 @@ __global__ void __launch_bounds__(kVegasThreads)
   const int64_t stride = static_cast<int64_t>(gridDim.x) * blockDim.x;
   for (int64_t r = static_cast<int64_t>(blockIdx.x) * blockDim.x + threadIdx.x; r < n;
        r += stride) {
-    double x[kMaxDim];
-    for (int j = 0; j < kMaxDim; ++j) x[j] = l_x[static_cast<int64_t>(j) * cap + r];
+    double x[MAXD];
+    for (int j = 0; j < MAXD; ++j) x[j] = j < dim ? l_x[static_cast<int64_t>(j) * cap + r] : 0.0;
     uint8_t      fl;
-    const double W = screened_weight<T>(A, x, fl, skt, sphi);
+    const double W = screened_weight<T, (MAXD > 8)>(A, x, fl, skt, sphi);
     const double f = W * l_vw[r];
     f_out[l_idx[r]] = f;
-    hist_add(sf2, dim, l_bins[r], f * f);
+    hist_add(sf2, dim, l_bins[r], l_bins_hi ? l_bins_hi[r] : 0ull, f * f);
     cnt[VS_AMP_OK] += (fl & GRN_FLAG_AMPLITUDE_OK) ? 1 : 0;
     cnt[VS_NAN] += (fl & GRN_FLAG_AMPLITUDE_OK) ? 0 : 1;
     if (track_max) {
@@ -950,8 +1031,8 @@ __global__ void __launch_bounds__(kVegasThreads, GRN_LOOP_MIN_BLOCKS)
     k_vegas_loop_rec(const KArgs A, int bins, int dim, int track_max, double *__restrict__ f_out,
                      double *__restrict__ f2mat, unsigned long long *__restrict__ acc,
                      const int64_t *__restrict__ l_idx, const double *__restrict__ l_vw,
-                     const uint64_t *__restrict__ l_bins, const float *__restrict__ rf,
-                     const double *__restrict__ rd, int64_t cap) {
+                     const uint64_t *__restrict__ l_bins, const uint64_t *__restrict__ l_bins_hi,
+                     const float *__restrict__ rf, const double *__restrict__ rd, int64_t cap) {
   extern __shared__ double dsm[];
   double *sf2 = dsm;
   __shared__ KtNode<float>  skt[kMaxLoopNodes];
@@ -974,7 +1055,7 @@ __global__ void __launch_bounds__(kVegasThreads, GRN_LOOP_MIN_BLOCKS)
     const double W = record_weight(A, e, a0r, a0i, jac, skt, sphi, fl);
     const double f = W * l_vw[r];
     f_out[l_idx[r]] = f;
-    hist_add(sf2, dim, l_bins[r], f * f);
+    hist_add(sf2, dim, l_bins[r], l_bins_hi ? l_bins_hi[r] : 0ull, f * f);
     cnt[VS_AMP_OK] += (fl & GRN_FLAG_AMPLITUDE_OK) ? 1 : 0;
     cnt[VS_NAN] += (fl & GRN_FLAG_AMPLITUDE_OK) ? 0 : 1;
     if (track_max) {
@@ -991,8 +1072,8 @@ __global__ void __launch_bounds__(kVegasThreads, 2)
     k_vegas_loop_rec2(const KArgs A, int bins, int dim, int track_max, double *__restrict__ f_out,
                       double *__restrict__ f2mat, unsigned long long *__restrict__ acc,
                       const int64_t *__restrict__ l_idx, const double *__restrict__ l_vw,
-                      const uint64_t *__restrict__ l_bins, const float *__restrict__ rf,
-                      const double *__restrict__ rd, int64_t cap) {
+                      const uint64_t *__restrict__ l_bins, const uint64_t *__restrict__ l_bins_hi,
+                      const float *__restrict__ rf, const double *__restrict__ rd, int64_t cap) {
   extern __shared__ double dsm[];
   double *sf2 = dsm;
   __shared__ KtNode2  skt[kMaxLoopNodes];
@@ -1017,7 +1098,7 @@ __global__ void __launch_bounds__(kVegasThreads, 2)
       const int64_t r = k ? rb : ra;
       const double  f = W[k] * l_vw[r];
       f_out[l_idx[r]] = f;
-      hist_add(sf2, dim, l_bins[r], f * f);
+      hist_add(sf2, dim, l_bins[r], l_bins_hi ? l_bins_hi[r] : 0ull, f * f);
       cnt[VS_AMP_OK] += (F[k] & GRN_FLAG_AMPLITUDE_OK) ? 1 : 0;
       cnt[VS_NAN] += (F[k] & GRN_FLAG_AMPLITUDE_OK) ? 0 : 1;
       if (track_max) {
@@ -1054,8 +1135,8 @@ int vegas_grid_blocks(int device) {
 cudaError_t launch_vegas_born(const KArgs &a, const double *xmat, int bins, int dim, int64_t ncall,
                               uint64_t seed, uint32_t stream, int track_max, double *f_out,
                               double *f2mat, unsigned long long *acc, int64_t *l_idx, double *l_x,
-                              double *l_vw, uint64_t *l_bins, float *rf, double *rd,
-                              cudaStream_t st, const float *fu, const float *flq) {
+                              double *l_vw, uint64_t *l_bins, uint64_t *l_bins_hi, float *rf,
+                              double *rd, cudaStream_t st, const float *fu, const float *flq) {
   const int nh = bins * dim;
   cudaMemsetAsync(f2mat, 0, nh * sizeof(double), st);
   cudaMemsetAsync(acc, 0, (VS_COUNT + 1) * sizeof(unsigned long long), st);
@@ -1064,34 +1145,51 @@ cudaError_t launch_vegas_born(const KArgs &a, const double *xmat, int bins, int 
   cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
   const int64_t want = (ncall + kVegasThreads - 1) / kVegasThreads;
   const int     ba   = static_cast<int>(std::min<int64_t>(want, static_cast<int64_t>(sms) * 16));
-  k_vegas_born<<<ba, kVegasThreads, 2 * nh * sizeof(double), st>>>(
-      a, xmat, bins, dim, ncall, seed, stream, track_max, f_out, f2mat, acc, l_idx, l_x, l_vw,
-      l_bins, ncall, rf, rd, fu, flq);
+  if (dim <= 8)
+    k_vegas_born<8><<<ba, kVegasThreads, 2 * nh * sizeof(double), st>>>(
+        a, xmat, bins, dim, ncall, seed, stream, track_max, f_out, f2mat, acc, l_idx, l_x, l_vw,
+        l_bins, l_bins_hi, ncall, rf, rd, fu, flq);
+  else
+    k_vegas_born<kMaxDim><<<ba, kVegasThreads, 2 * nh * sizeof(double), st>>>(
+        a, xmat, bins, dim, ncall, seed, stream, track_max, f_out, f2mat, acc, l_idx, l_x, l_vw,
+        l_bins, l_bins_hi, ncall, rf, rd, fu, flq);
   return cudaGetLastError();
 }
 
 cudaError_t launch_vegas_loop(const KArgs &a, int prec, int bins, int dim, int64_t ncall,
                               int track_max, double *f_out, double *f2mat, unsigned long long *acc,
                               const int64_t *l_idx, const double *l_x, const double *l_vw,
-                              const uint64_t *l_bins, const float *rf, const double *rd,
-                              int nblocks, cudaStream_t st) {
+                              const uint64_t *l_bins, const uint64_t *l_bins_hi, const float *rf,
+                              const double *rd, int nblocks, cudaStream_t st) {
   if (!a.P.screening) return cudaSuccess;
   const int nh = bins * dim;
   if (rf) {
     if (a.loop_pair)
       k_vegas_loop_rec2<<<nblocks, kVegasThreads, nh * sizeof(double), st>>>(
-          a, bins, dim, track_max, f_out, f2mat, acc, l_idx, l_vw, l_bins, rf, rd, ncall);
+          a, bins, dim, track_max, f_out, f2mat, acc, l_idx, l_vw, l_bins, l_bins_hi, rf, rd,
+          ncall);
     else
       k_vegas_loop_rec<<<nblocks, kVegasThreads, nh * sizeof(double), st>>>(
-          a, bins, dim, track_max, f_out, f2mat, acc, l_idx, l_vw, l_bins, rf, rd, ncall);
+          a, bins, dim, track_max, f_out, f2mat, acc, l_idx, l_vw, l_bins, l_bins_hi, rf, rd,
+          ncall);
     return cudaGetLastError();
   }
-  if (prec == GRN_PREC_MIXED)
-    k_vegas_loop<float><<<nblocks, kVegasThreads, nh * sizeof(double), st>>>(
-        a, bins, dim, track_max, f_out, f2mat, acc, l_idx, l_x, l_vw, l_bins, ncall);
-  else
-    k_vegas_loop<double><<<nblocks, kVegasThreads, nh * sizeof(double), st>>>(
-        a, bins, dim, track_max, f_out, f2mat, acc, l_idx, l_x, l_vw, l_bins, ncall);
+  const size_t sm = nh * sizeof(double);
+  if (dim <= 8) {
+    if (prec == GRN_PREC_MIXED)
+      k_vegas_loop<float, 8><<<nblocks, kVegasThreads, sm, st>>>(
+          a, bins, dim, track_max, f_out, f2mat, acc, l_idx, l_x, l_vw, l_bins, l_bins_hi, ncall);
+    else
+      k_vegas_loop<double, 8><<<nblocks, kVegasThreads, sm, st>>>(
+          a, bins, dim, track_max, f_out, f2mat, acc, l_idx, l_x, l_vw, l_bins, l_bins_hi, ncall);
+  } else {
+    if (prec == GRN_PREC_MIXED)
+      k_vegas_loop<float, kMaxDim><<<nblocks, kVegasThreads, sm, st>>>(
+          a, bins, dim, track_max, f_out, f2mat, acc, l_idx, l_x, l_vw, l_bins, l_bins_hi, ncall);
+    else
+      k_vegas_loop<double, kMaxDim><<<nblocks, kVegasThreads, sm, st>>>(
+          a, bins, dim, track_max, f_out, f2mat, acc, l_idx, l_x, l_vw, l_bins, l_bins_hi, ncall);
+  }
   return cudaGetLastError();
 }
 
@@ -1106,18 +1204,25 @@ cudaError_t upload_batch_procs(const BatchProc *h_procs, int np, cudaStream_t st
                                  cudaMemcpyHostToDevice, st);
 }
 
+template <int MAXD>
 __global__ void __launch_bounds__(kVegasThreads, 3) k_batch_born(int np) {
   extern __shared__ double dsm[];
   int p = 0;
   while (p + 1 < np && static_cast<int>(blockIdx.x) >= c_procs[p].blk1) ++p;
   const BatchProc &q = c_procs[p];
-  born_pass_body(q.A, q.xmat, q.bins, q.dim, q.ncall, q.seed, q.stream, q.track_max, q.f_out,
-                 q.f2mat, q.acc, q.l_idx, q.l_x, q.l_vw, q.l_bins, q.ncall, q.rf, q.rd, nullptr,
-                 nullptr, dsm, static_cast<int>(blockIdx.x) - q.blk0, q.blk1 - q.blk0);
+  born_pass_body<MAXD>(q.A, q.xmat, q.bins, q.dim, q.ncall, q.seed, q.stream, q.track_max,
+                       q.f_out, q.f2mat, q.acc, q.l_idx, q.l_x, q.l_vw, q.l_bins, q.l_bins_hi,
+                       q.ncall, q.rf, q.rd, nullptr, nullptr, dsm,
+                       static_cast<int>(blockIdx.x) - q.blk0, q.blk1 - q.blk0);
 }
 
-cudaError_t launch_batch_born(int np, int nblocks, cudaStream_t st) {
-  k_batch_born<<<nblocks, kVegasThreads, 2 * kMaxBins * kMaxDim * sizeof(double), st>>>(np);
+cudaError_t launch_batch_born(int np, int nblocks, int max_dim, cudaStream_t st) {
+  // shared memory: grid and f^2 histogram of the largest process (bins * dim each)
+  const size_t sm = 2 * static_cast<size_t>(kMaxBins) * max_dim * sizeof(double);
+  if (max_dim <= 8)
+    k_batch_born<8><<<nblocks, kVegasThreads, sm, st>>>(np);
+  else
+    k_batch_born<kMaxDim><<<nblocks, kVegasThreads, sm, st>>>(np);
   return cudaGetLastError();
 }
 
@@ -1198,7 +1303,7 @@ __global__ void __launch_bounds__(kVegasThreads, 2)
           const int64_t r = k ? rb : ra;
           const double  f = W[k] * q.l_vw[r];
           q.f_out[q.l_idx[r]] = f;
-          hist_add(sf2, q.dim, q.l_bins[r], f * f);
+          hist_add(sf2, q.dim, q.l_bins[r], q.l_bins_hi ? q.l_bins_hi[r] : 0ull, f * f);
           cnt[VS_AMP_OK] += (F[k] & GRN_FLAG_AMPLITUDE_OK) ? 1 : 0;
           cnt[VS_NAN] += (F[k] & GRN_FLAG_AMPLITUDE_OK) ? 0 : 1;
           if (q.track_max) {
@@ -1209,12 +1314,13 @@ __global__ void __launch_bounds__(kVegasThreads, 2)
       }
     } else if (unit < n) {
       double x[kMaxDim];
-      for (int j = 0; j < kMaxDim; ++j) x[j] = q.l_x[static_cast<int64_t>(j) * q.ncall + unit];
+      for (int j = 0; j < kMaxDim; ++j)
+        x[j] = j < q.dim ? q.l_x[static_cast<int64_t>(j) * q.ncall + unit] : 0.0;
       uint8_t      fl;
-      const double W = screened_weight<float>(q.A, x, fl, skt, sphi);
+      const double W = screened_weight<float, true>(q.A, x, fl, skt, sphi);
       const double f = W * q.l_vw[unit];
       q.f_out[q.l_idx[unit]] = f;
-      hist_add(sf2, q.dim, q.l_bins[unit], f * f);
+      hist_add(sf2, q.dim, q.l_bins[unit], q.l_bins_hi ? q.l_bins_hi[unit] : 0ull, f * f);
       cnt[VS_AMP_OK] += (fl & GRN_FLAG_AMPLITUDE_OK) ? 1 : 0;
       cnt[VS_NAN] += (fl & GRN_FLAG_AMPLITUDE_OK) ? 0 : 1;
       if (q.track_max) {

@@ -16,8 +16,12 @@
 
 #ifdef __CUDACC__
 #define GRN_HD __host__ __device__ __forceinline__
+// Rarely taken paths (cascade decays, vector-pair amplitudes) stay out of line so that they
+// do not raise the register count of the kernels that inline the common path.
+#define GRN_HD_COLD static __host__ __device__ __noinline__
 #else
 #define GRN_HD inline
+#define GRN_HD_COLD static inline
 #endif
 
 namespace grn {
@@ -388,6 +392,131 @@ GRN_HD cx<T> tensor_me3(const grn_process_params &P, const Consts &K, const LCKi
 }
 
 // ---------------------------------------------------------------------------
+// Tensor-pomeron continuum of two vector mesons, "2xV" (MTensorPomeron::ME4,
+// src/MTensorPomeron.cc:808-888). Each pomeron-vector-vector vertex iG_Pvv (:2224-2237,
+// i FM(q^2, 0.5) (2 g1 Gamma0 - g2 Gamma2), :2500-2529) is contracted with its pomeron leg
+// W = 2 P P - P^2 g / 2 (proton vertex through the pomeron propagator, as for 2xS) and with
+// the polarization vector e of its external vector meson (e.x = 0). With x the external and
+// y the other meson momentum of the vertex (Gamma(k1, k2) with {k1, k2} = {y, x}):
+//   vertex . W . e = ce e + cx x + cP P,
+//   ce = 4 g1 (yWx)(x.y) + g2 (b x.y - 2 yWx),
+//   cx = -4 g1 (yWx)(y.e) - g2 (b y.e - 2 eWy),
+//   cP = -4 g2 ((x.y)(P.e) - (y.e)(P.x)),
+// so that the two vertices of a channel meet through the vector propagator iD_V (:2353-2369)
+// as one Minkowski product of two vectors. The nine amplitudes e3_i.M.e4_j of a real
+// polarization basis give the reference's sum over the helicity states (MassiveSpin1PolSum,
+// :1243-1263) of |amplitude|^2.
+template <typename T>
+struct LV {
+  T p, m, x, y;  // light-cone components (+, -) and transverse
+};
+template <typename T>
+GRN_HD T ldot(const LV<T> &a, const LV<T> &b) {
+  return lc_dot<T>(a.p, a.m, a.x, a.y, b.p, b.m, b.x, b.y);
+}
+
+template <typename T>
+GRN_HD LV<T> vv_vertex(const LV<T> &e, const LV<T> &x, const LV<T> &y, const LV<T> &P, T b, T g1,
+                       T g2) {
+  const T xy = ldot(x, y), Px = ldot(P, x), Py = ldot(P, y), Pe = ldot(P, e), ye = ldot(y, e);
+  const T yWx = T(2) * Py * Px - T(0.5) * b * xy;
+  const T eWy = T(2) * Pe * Py - T(0.5) * b * ye;
+  const T ce  = T(4) * g1 * yWx * xy + g2 * (b * xy - T(2) * yWx);
+  const T cx_ = -T(4) * g1 * yWx * ye - g2 * (b * ye - T(2) * eWy);
+  const T cP  = -T(4) * g2 * (xy * Pe - ye * Px);
+  return {ce * e.p + cx_ * x.p + cP * P.p, ce * e.m + cx_ * x.m + cP * P.m,
+          ce * e.x + cx_ * x.x + cP * P.x, ce * e.y + cx_ * x.y + cP * P.y};
+}
+
+// Real polarization basis of a massive vector (light-cone momentum): two transverse unit
+// vectors (z x p^, p^ x t1; x x p^ near the z axis) and the longitudinal (|p|/m, E p^/m).
+template <typename T>
+GRN_HD void vector_basis(T pp, T pm, T px, T py, LV<T> e[3]) {
+  const T E = T(0.5) * (pp + pm), pz = T(0.5) * (pp - pm);
+  const T m = sqrt(pp * pm - (px * px + py * py));
+  const T P = sqrt(px * px + py * py + pz * pz);
+  T n[3] = {T(0), T(0), T(1)};
+  if (P > T(1e-12)) { n[0] = px / P; n[1] = py / P; n[2] = pz / P; }
+  T a[3] = {T(0), T(0), T(1)};
+  if (fabs(n[2]) > T(0.9)) { a[0] = T(1); a[2] = T(0); }
+  T t1[3] = {a[1] * n[2] - a[2] * n[1], a[2] * n[0] - a[0] * n[2], a[0] * n[1] - a[1] * n[0]};
+  const T nt = sqrt(t1[0] * t1[0] + t1[1] * t1[1] + t1[2] * t1[2]);
+  t1[0] /= nt; t1[1] /= nt; t1[2] /= nt;
+  const T t2[3] = {n[1] * t1[2] - n[2] * t1[1], n[2] * t1[0] - n[0] * t1[2],
+                   n[0] * t1[1] - n[1] * t1[0]};
+  e[0] = {t1[2], -t1[2], t1[0], t1[1]};
+  e[1] = {t2[2], -t2[2], t2[0], t2[1]};
+  const T l0 = P / m, ls = E / m;
+  e[2] = {l0 + ls * n[2], l0 - ls * n[2], ls * n[0], ls * n[1]};
+}
+
+// Reggeized vector-propagator factor -(e^{i phi} s34 / (4 M0^2))^(alpha - 1) / (p^2 - M0^2),
+// alpha = 0.5 + 0.9 p^2, phi = pi/2 exp((4 M0^2 - s34) / (4 M0^2)) - pi/2 (iD_V).
+template <typename T>
+GRN_HD cx<T> vector_prop(T p2, T M0sq, T s34) {
+  const T sth = T(4) * M0sq;
+  const T ph  = T(0.5) * (exp((sth - s34) / sth) - T(1));  // phi / pi
+  const T a1  = T(-0.5) + T(0.9) * p2;                     // alpha - 1
+  const T mag = -exp(a1 * log(s34 / sth)) / (p2 - M0sq);
+  T sn, cs;
+  sincos_pi(a1 * ph, sn, cs);
+  return {mag * cs, mag * sn};
+}
+
+// Pomeron propagator factor 1/(4s) (-i s ap)^(alpha(t) - 1) (iD_P, :2288-2298).
+template <typename T>
+GRN_HD cx<T> pomeron_c(const grn_tensor_params &tp, T s, T t) {
+  const T x   = T(tp.delta_P) + T(tp.ap_P) * t;
+  const T mag = exp(x * log(s * T(tp.ap_P))) / (T(4) * s);
+  T sn, cs;
+  sincos_pi(T(-0.5) * x, sn, cs);
+  return {mag * cs, mag * sn};
+}
+
+// The nine amplitudes A[3 i + j] = e3_i . M . e4_j of one proton helicity configuration.
+template <typename T>
+GRN_HD void tensor_me4_2xv(const grn_process_params &P, const Consts &K, const LCKin<T> &k,
+                           T s34, const LV<T> e3[3], const LV<T> e4[3], cx<T> A[9]) {
+  const grn_tensor_params &tp = P.tensor;
+  const T L = k.L, eps = k.eps;
+  const LV<T> P1{k.p1p + L, k.p1m + eps, k.p1x, k.p1y};
+  const LV<T> P2{k.p2p + eps, k.p2m + L, k.p2x, k.p2y};
+  const T b1 = T(4) * k.mp2 - k.t1, b2 = T(4) * k.mp2 - k.t2;
+  const LV<T> p3{k.p3p, k.p3m, k.p3x, k.p3y}, p4{k.p4p, k.p4m, k.p4x, k.p4y};
+  // pt = q1 - p3, pu = p4 - q1 (q1 = pa - p1 = (q1+, q1-, -p1T))
+  const LV<T> pt{k.q1p - k.p3p, k.q1m - k.p3m, -k.p1x - k.p3x, -k.p1y - k.p3y};
+  const LV<T> mpt{-pt.p, -pt.m, -pt.x, -pt.y};
+  const LV<T> pu{k.p4p - k.q1p, k.p4m - k.q1m, k.p4x + k.p1x, k.p4y + k.p1y};
+  const LV<T> mpu{-pu.p, -pu.m, -pu.x, -pu.y};
+  const T g1 = T(tp.gPvv[0]), g2 = T(tp.gPvv[1]);
+  // channel constants (-3i gPNN F1)^2 (i FM)^2 c c ff^2 D_V = 9 gPNN^2 F1 F1 FM FM c c ff^2 D_V
+  const T M0sq = T(K.M2prop);
+  const T com  = T(9.0 * tp.gPNN * tp.gPNN) * dirac_f1<T>(k.t1, tp.em_kelly) *
+                dirac_f1<T>(k.t2, tp.em_kelly) / ((T(1) - k.t1 / T(0.5)) * (T(1) - k.t2 / T(0.5)));
+  const T fft = meson_ff<T>(P.regge, k.that, M0sq), ffu = meson_ff<T>(P.regge, k.uhat, M0sq);
+  const cx<T> Ct = cscale(cmul(cmul(pomeron_c<T>(tp, k.s13, k.t1), pomeron_c<T>(tp, k.s24, k.t2)),
+                               vector_prop<T>(k.that, M0sq, s34)),
+                          com * fft * fft);
+  const cx<T> Cu = cscale(cmul(cmul(pomeron_c<T>(tp, k.s14, k.t1), pomeron_c<T>(tp, k.s23, k.t2)),
+                               vector_prop<T>(k.uhat, M0sq, s34)),
+                          com * ffu * ffu);
+  LV<T> at[3], bt[3], au[3], bu[3];
+  for (int i = 0; i < 3; ++i) {
+    at[i] = vv_vertex<T>(e3[i], p3, pt, P1, b1, g1, g2);   // upper, t channel
+    bt[i] = vv_vertex<T>(e4[i], p4, mpt, P2, b2, g1, g2);  // lower, t channel
+    au[i] = vv_vertex<T>(e4[i], p4, mpu, P1, b1, g1, g2);  // upper, u channel
+    bu[i] = vv_vertex<T>(e3[i], p3, pu, P2, b2, g1, g2);   // lower, u channel
+  }
+  // M = -i (M_t + M_u)
+  for (int i = 0; i < 3; ++i)
+    for (int j = 0; j < 3; ++j) {
+      const T dt = ldot(at[i], bt[j]), du = ldot(au[j], bu[i]);
+      const T re = Ct.re * dt + Cu.re * du, im = Ct.im * dt + Cu.im * du;
+      A[3 * i + j] = {im, -re};
+    }
+}
+
+// ---------------------------------------------------------------------------
 // Born (tree-level) kinematics of p p -> p (a b) p in the <C> class, FP64.
 struct Born {
   // forward legs
@@ -399,7 +528,10 @@ struct Born {
   double p3x, p3y, p4x, p4y;
   double p3p, p3m, p4p, p4m;
   double mt3, mt4, y3, y4;
-  double jx;                   // class-specific Jacobian factor: kt (<C>), p*/M_X (<F>)
+  double jx;                   // class-specific Jacobian factor: kt (<C>),
+                               // p*/M_X x (M_max^2 - M_min^2) (<F>)
+  double m3sq, m4sq;           // central masses^2 (off-shell ones for cascades)
+  int    leafok;               // cascades: all four daughters pass the particle cuts
   // invariants
   double t1, t2, s13, s14, s23, s24, that, uhat, m2;
 };
@@ -454,6 +586,9 @@ GRN_HD bool born_kinematics_C(const grn_process_params &P, const Consts &K, cons
   b.p3y = 0.5 * (qy - wy);
   b.p4x = 0.5 * (-qx - wx);
   b.p4y = 0.5 * (-qy - wy);
+  b.m3sq = K.m3sq;
+  b.m4sq = K.m4sq;
+  b.leafok = 1;
   b.mt3 = sqrt(K.m3sq + b.p3x * b.p3x + b.p3y * b.p3y);
   b.mt4 = sqrt(K.m4sq + b.p4x * b.p4x + b.p4y * b.p4y);
   const double e3 = exp(b.y3), e4 = exp(b.y4);
@@ -485,11 +620,11 @@ GRN_HD bool born_invariants(const Consts &K, Born &b) {
   // Invariants: (pa + pb)^2 = ma^2 + mb^2 + pa+ pb- + pa- pb+ - 2 paT.pbT
   b.t1  = -(b.pt1sq + b.x1 * b.x1 * K.mp2) / (1.0 - b.x1);
   b.t2  = -(b.pt2sq + b.x2 * b.x2 * K.mp2) / (1.0 - b.x2);
-  b.s13 = K.mp2 + K.m3sq + b.p1p * b.p3m + b.p1m * b.p3p - 2.0 * (b.p1x * b.p3x + b.p1y * b.p3y);
-  b.s14 = K.mp2 + K.m4sq + b.p1p * b.p4m + b.p1m * b.p4p - 2.0 * (b.p1x * b.p4x + b.p1y * b.p4y);
-  b.s23 = K.mp2 + K.m3sq + b.p2p * b.p3m + b.p2m * b.p3p - 2.0 * (b.p2x * b.p3x + b.p2y * b.p3y);
-  b.s24 = K.mp2 + K.m4sq + b.p2p * b.p4m + b.p2m * b.p4p - 2.0 * (b.p2x * b.p4x + b.p2y * b.p4y);
-  b.m2  = K.m3sq + K.m4sq + b.p3p * b.p4m + b.p3m * b.p4p - 2.0 * (b.p3x * b.p4x + b.p3y * b.p4y);
+  b.s13 = K.mp2 + b.m3sq + b.p1p * b.p3m + b.p1m * b.p3p - 2.0 * (b.p1x * b.p3x + b.p1y * b.p3y);
+  b.s14 = K.mp2 + b.m4sq + b.p1p * b.p4m + b.p1m * b.p4p - 2.0 * (b.p1x * b.p4x + b.p1y * b.p4y);
+  b.s23 = K.mp2 + b.m3sq + b.p2p * b.p3m + b.p2m * b.p3p - 2.0 * (b.p2x * b.p3x + b.p2y * b.p3y);
+  b.s24 = K.mp2 + b.m4sq + b.p2p * b.p4m + b.p2m * b.p4p - 2.0 * (b.p2x * b.p4x + b.p2y * b.p4y);
+  b.m2  = b.m3sq + b.m4sq + b.p3p * b.p4m + b.p3m * b.p4p - 2.0 * (b.p3x * b.p4x + b.p3y * b.p4y);
   // t_hat = (q1 - p3)^2 with q1 = pb1 - p1: (q1+ - p3+) = p4+ - eps + p2+ by conservation.
   {
     const double dp = b.p4p - K.eps + b.p2p;
@@ -507,10 +642,80 @@ GRN_HD bool born_invariants(const Consts &K, Born &b) {
 }
 
 
+// Relativistic Breit-Wigner mass by inverse CDF in m^2 on [max(M_MIN, m0 - 5 W)^2,
+// (m0 + 5 W)^2] (MRandom::RelativisticBWRandom, src/MRandom.cc:82-104; OFFSHELL = 5 widths,
+// include/Graniitti/MProcess.h:363) from the uniform R.
+GRN_HD double bw_mass(double m0, double W, double M_MIN, double R) {
+  if (W < 1e-40) return m0;
+  const double m2    = m0 * m0;
+  const double m2max = (m0 + 5.0 * W) * (m0 + 5.0 * W);
+  const double m2min = fmax(fmax(0.0, M_MIN * M_MIN), (m0 - 5.0 * W) * (m0 - 5.0 * W));
+  const double a = atan2(m2min - m2, m0 * W), c = atan2(m2max - m2, m0 * W);
+  const double v = m2 + m0 * W * tan(a + R * (c - a));
+  return fmax(M_MIN, sqrt(fmax(0.0, v)));
+}
+
+// Two-body decay of a mother (px, py, pz, E; mass M) into masses ma, mb with (cos theta,
+// phi) in its rest frame, boosted to the lab (TwoBodyPhaseSpace, LorentzBoost,
+// include/Graniitti/MKinematics.h:384-459); out: (px, py, pz, E) of a and b.
+GRN_HD void decay2(double px, double py, double pz, double E, double M, double ma, double mb,
+                   double ct, double phi_frac, double a[4], double bb[4]) {
+  const double ms = ma + mb, md = ma - mb;
+  const double pn = sqrt(fmax(0.0, (M - ms) * (M + ms) * (M + md) * (M - md))) / (2.0 * M);
+  const double st = sqrt(fmax(0.0, 1.0 - ct * ct));
+  double sp, cp;
+  sincos_pi(2.0 * phi_frac, sp, cp);
+  const double kx = pn * st * cp, ky = pn * st * sp, kz = pn * ct;
+  const double Ea = sqrt(ma * ma + pn * pn), Eb = sqrt(mb * mb + pn * pn);
+  const double bx = px / E, by = py / E, bz = pz / E, gam = E / M;
+  const double k1 = bx * kx + by * ky + bz * kz;
+  const double ca = gam * (gam * k1 / (1.0 + gam) + Ea);
+  const double cb = gam * (-gam * k1 / (1.0 + gam) + Eb);
+  a[0] = kx + ca * bx;  a[1] = ky + ca * by;  a[2] = kz + ca * bz;  a[3] = gam * (Ea + k1);
+  bb[0] = -kx + cb * bx; bb[1] = -ky + cb * by; bb[2] = -kz + cb * bz; bb[3] = gam * (Eb - k1);
+}
+
+// The four daughters of the two central particles, decay angles from u[10..13].
+GRN_HD_COLD void cascade_daughters(const grn_process_params &P, double p3x, double p3y, double p3z,
+                              double E3, double m3, double p4x, double p4y, double p4z, double E4,
+                              double m4, const double *u, double d[4][4]) {
+  decay2(p3x, p3y, p3z, E3, m3, P.m_daughter[0], P.m_daughter[1], 2.0 * u[10] - 1.0, u[11], d[0],
+         d[1]);
+  decay2(p4x, p4y, p4z, E4, m4, P.m_daughter[2], P.m_daughter[3], 2.0 * u[12] - 1.0, u[13], d[2],
+         d[3]);
+}
+
+// Particle cuts of one final-state particle (px, py, pz, E) (FIDCUT PARTICLE block).
+GRN_HD bool particle_cuts(const grn_process_params &P, const double *p) {
+  const grn_fidcuts &f = P.fcuts;
+  const double ptsq = p[0] * p[0] + p[1] * p[1];
+  const double pt   = sqrt(ptsq);
+  const double mt   = sqrt(fmax(0.0, p[3] * p[3] - p[2] * p[2]));
+  const double pa   = sqrt(ptsq + p[2] * p[2]);
+  const double eta  = 0.5 * log((pa + p[2]) / (pa - p[2]));
+  const double y    = 0.5 * log((p[3] + p[2]) / (p[3] - p[2]));
+  return pt >= f.pt_min && pt <= f.pt_max && mt >= f.Et_min && mt <= f.Et_max &&
+         eta >= f.eta_min && eta <= f.eta_max && y >= f.rap_min && y <= f.rap_max;
+}
+
+// All four cascade daughters pass the particle cuts.
+GRN_HD_COLD int cascade_cuts(const grn_process_params &P, double p3x, double p3y, double p3z,
+                             double E3, double m3, double p4x, double p4y, double p4z, double E4,
+                             double m4, const double *u) {
+  double d[4][4];
+  cascade_daughters(P, p3x, p3y, p3z, E3, m3, p4x, p4y, p4z, E4, m4, u, d);
+  int ok = 1;
+  for (int k = 0; k < 4; ++k) ok &= particle_cuts(P, d[k]) ? 1 : 0;
+  return ok;
+}
+
 // B51RandomKin + B51BuildKin for a 2-body central system, the isotropic decay
 // angles lifted into u[6] (cos theta = 2 u6 - 1) and u[7] (phi = 2 pi u7), the
 // draws TwoBodyPhaseSpace makes (src/MFactorized.cc:245-412;
 // include/Graniitti/MKinematics.h:405-459).
+// CASC: the instantiation serves two-body cascades (14-dimensional points); the 8-dimensional
+// one leaves the cascade code out.
+template <bool CASC>
 GRN_HD bool born_kinematics_F(const grn_process_params &P, const Consts &K, const double *u,
                               Born &b) {
   const grn_gencuts &g = P.gcuts;
@@ -520,7 +725,20 @@ GRN_HD bool born_kinematics_F(const grn_process_params &P, const Consts &K, cons
   sincos_pi(2.0 * u[2], s1, c1);
   sincos_pi(2.0 * u[3], s2, c2);
   const double yX  = g.Y_min + (g.Y_max - g.Y_min) * u[4];
-  const double m2X = K.M2min + (K.M2max - K.M2min) * u[5];
+  double m3 = K.m3, m4 = K.m4, M2lo = K.M2min, M2hi = K.M2max;
+  if (CASC && P.n_decay == 2) {
+    // off-shell central masses (GetOffShellMass: the daughters' mass sum + 1e-5 GeV bounds
+    // the Breit-Wigner from below) and the mass window they leave (B51RandomKin)
+    m3   = bw_mass(P.m_central[0], P.width[0], P.m_daughter[0] + P.m_daughter[1] + 1e-5, u[8]);
+    m4   = bw_mass(P.m_central[1], P.width[1], P.m_daughter[2] + P.m_daughter[3] + 1e-5, u[9]);
+    const double Mmin = fmax(m3 + m4 + 1e-4, g.M_min);
+    if (!(Mmin * Mmin < M2hi)) return false;
+    M2lo = Mmin * Mmin;
+  }
+  b.m3sq = m3 * m3;
+  b.m4sq = m4 * m4;
+  b.leafok = 1;
+  const double m2X = M2lo + (M2hi - M2lo) * u[5];
   b.p1x = pt1 * c1;
   b.p1y = pt1 * s1;
   b.p2x = pt2 * c2;
@@ -535,14 +753,14 @@ GRN_HD bool born_kinematics_F(const grn_process_params &P, const Consts &K, cons
   if (EX > K.sqrt_s - 2.0 * sqrt(K.mp2)) return false;  // energy overflow (MFactorized.cc:323)
   // isotropic decay in the central-system rest frame, boosted to the lab
   const double MX = sqrt(m2X);
-  const double ms = K.m3 + K.m4, md = K.m3 - K.m4;
+  const double ms = m3 + m4, md = m3 - m4;
   const double ps = sqrt(fmax(0.0, (MX - ms) * (MX + ms) * (MX + md) * (MX - md))) / (2.0 * MX);
   const double ct = 2.0 * u[6] - 1.0;
   const double st = sqrt(fmax(0.0, 1.0 - ct * ct));
   double sp, cp;
   sincos_pi(2.0 * u[7], sp, cp);
   const double kx = ps * st * cp, ky = ps * st * sp, kz = ps * ct;
-  const double E3s = sqrt(K.m3sq + ps * ps), E4s = sqrt(K.m4sq + ps * ps);
+  const double E3s = sqrt(b.m3sq + ps * ps), E4s = sqrt(b.m4sq + ps * ps);
   const double bx = Xx / EX, by = Xy / EX, bz = ZX / EX, gam = EX / MX;
   const double k1 = bx * kx + by * ky + bz * kz;
   const double a3 = gam * (gam * k1 / (1.0 + gam) + E3s);
@@ -553,8 +771,8 @@ GRN_HD bool born_kinematics_F(const grn_process_params &P, const Consts &K, cons
   b.p4x = -kx + a4 * bx;
   b.p4y = -ky + a4 * by;
   const double p4z = -kz + a4 * bz, E4 = gam * (E4s - k1);
-  b.mt3 = sqrt(K.m3sq + b.p3x * b.p3x + b.p3y * b.p3y);
-  b.mt4 = sqrt(K.m4sq + b.p4x * b.p4x + b.p4y * b.p4y);
+  b.mt3 = sqrt(b.m3sq + b.p3x * b.p3x + b.p3y * b.p3y);
+  b.mt4 = sqrt(b.m4sq + b.p4x * b.p4x + b.p4y * b.p4y);
   // light-cone components; the smaller one from mT^2 / larger (exact, no cancellation)
   if (p3z >= 0) { b.p3p = E3 + p3z; b.p3m = b.mt3 * b.mt3 / b.p3p; }
   else          { b.p3m = E3 - p3z; b.p3p = b.mt3 * b.mt3 / b.p3m; }
@@ -562,13 +780,19 @@ GRN_HD bool born_kinematics_F(const grn_process_params &P, const Consts &K, cons
   else          { b.p4m = E4 - p4z; b.p4p = b.mt4 * b.mt4 / b.p4m; }
   b.y3 = 0.5 * log(b.p3p / b.p3m);
   b.y4 = 0.5 * log(b.p4p / b.p4m);
-  b.jx = ps / MX;
+  b.jx = ps / MX * (M2hi - M2lo);
+  if (CASC && P.n_decay == 2) {
+    // isotropic decays of the two central particles (ConstructDecayKinematics); the particle
+    // cuts act on the four daughters (FindDecayCuts, src/MProcess.cc:1140-1154)
+    b.leafok = cascade_cuts(P, b.p3x, b.p3y, p3z, E3, m3, b.p4x, b.p4y, p4z, E4, m4, u);
+  }
   return born_invariants(K, b);
 }
 
+template <bool CASC = false>
 GRN_HD bool born_kinematics(const grn_process_params &P, const Consts &K, const double *u,
                             Born &b) {
-  if (P.phase_space == GRN_PS_FACTORIZED) return born_kinematics_F(P, K, u, b);
+  if (P.phase_space == GRN_PS_FACTORIZED) return born_kinematics_F<CASC>(P, K, u, b);
   return born_kinematics_C(P, K, u, b);
 }
 
@@ -585,6 +809,7 @@ GRN_HD bool fiducial_cuts(const grn_process_params &P, const Consts &K, const Bo
   if (!(M >= f.M_min && M <= f.M_max && Y >= f.Y_min && Y <= f.Y_max && Pt >= f.Pt_min &&
         Pt <= f.Pt_max))
     return false;
+  if (P.n_decay == 2) return b.leafok != 0;
   bool ok = true;
   const double px[2] = {b.p3x, b.p4x}, py[2] = {b.p3y, b.p4y};
   const double mt[2] = {b.mt3, b.mt4}, y[2] = {b.y3, b.y4};
@@ -649,9 +874,9 @@ struct LoopEvent {
   ResSums<T> res;           // PP[RESTENSOR]: resonance sums of the tree-level central mass
 };
 
+// Kinematics of one kt-loop point; false when it is kinematically invalid.
 template <typename T>
-GRN_HD bool loop_point_amp(const grn_process_params &P, const Consts &K, const LoopEvent<T> &e,
-                           T kx, T ky, cx<T> &A) {
+GRN_HD bool loop_point_kin(const LoopEvent<T> &e, T kx, T ky, LCKin<T> &kk) {
   const T q1x = e.p1x - kx, q1y = e.p1y - ky;
   const T q2x = e.p2x + kx, q2y = e.p2y + ky;
   const T pt1sq = q1x * q1x + q1y * q1y;
@@ -663,39 +888,47 @@ GRN_HD bool loop_point_amp(const grn_process_params &P, const Consts &K, const L
   const T p1m = mT1sq / p1p;
   const T p2m = (T(1) - x2) * e.L;
   const T p2p = mT2sq / p2m;
-  const T t1  = -(pt1sq + x1 * x1 * e.mp2) / (T(1) - x1);
-  const T t2  = -(pt2sq + x2 * x2 * e.mp2) / (T(1) - x2);
-  const T s13 = e.mp2 + e.m3sq + p1p * e.p3m + p1m * e.p3p - T(2) * (q1x * e.p3x + q1y * e.p3y);
-  const T s14 = e.mp2 + e.m4sq + p1p * e.p4m + p1m * e.p4p - T(2) * (q1x * e.p4x + q1y * e.p4y);
-  const T s23 = e.mp2 + e.m3sq + p2p * e.p3m + p2m * e.p3p - T(2) * (q2x * e.p3x + q2y * e.p3y);
-  const T s24 = e.mp2 + e.m4sq + p2p * e.p4m + p2m * e.p4p - T(2) * (q2x * e.p4x + q2y * e.p4y);
-  T that, uhat;
+  kk.p1p = p1p; kk.p1m = p1m; kk.p1x = q1x; kk.p1y = q1y;
+  kk.p2p = p2p; kk.p2m = p2m; kk.p2x = q2x; kk.p2y = q2y;
+  kk.p3p = e.p3p; kk.p3m = e.p3m; kk.p3x = e.p3x; kk.p3y = e.p3y;
+  kk.p4p = e.p4p; kk.p4m = e.p4m; kk.p4x = e.p4x; kk.p4y = e.p4y;
+  kk.L = e.L; kk.eps = e.eps; kk.mp2 = e.mp2;
+  kk.t1  = -(pt1sq + x1 * x1 * e.mp2) / (T(1) - x1);
+  kk.t2  = -(pt2sq + x2 * x2 * e.mp2) / (T(1) - x2);
+  kk.s13 = e.mp2 + e.m3sq + p1p * e.p3m + p1m * e.p3p - T(2) * (q1x * e.p3x + q1y * e.p3y);
+  kk.s14 = e.mp2 + e.m4sq + p1p * e.p4m + p1m * e.p4p - T(2) * (q1x * e.p4x + q1y * e.p4y);
+  kk.s23 = e.mp2 + e.m3sq + p2p * e.p3m + p2m * e.p3p - T(2) * (q2x * e.p3x + q2y * e.p3y);
+  kk.s24 = e.mp2 + e.m4sq + p2p * e.p4m + p2m * e.p4p - T(2) * (q2x * e.p4x + q2y * e.p4y);
   {
     const T dp = e.p4p - e.eps + p2p;
     const T dm = e.eps - p1m - e.p3m;
     const T tx = q1x + e.p3x, ty = q1y + e.p3y;
-    that       = dp * dm - (tx * tx + ty * ty);
+    kk.that    = dp * dm - (tx * tx + ty * ty);
   }
   {
     const T dp = e.p3p - e.eps + p2p;
     const T dm = e.eps - p1m - e.p4m;
     const T tx = q1x + e.p4x, ty = q1y + e.p4y;
-    uhat       = dp * dm - (tx * tx + ty * ty);
+    kk.uhat    = dp * dm - (tx * tx + ty * ty);
   }
-  if (P.process == GRN_PROC_TENSOR_CON || P.process == GRN_PROC_TENSOR_RES) {
-    LCKin<T> kk{p1p,   p1m,   q1x,   q1y,   p2p,   p2m,   q2x,   q2y,   e.p3p, e.p3m, e.p3x,
-                e.p3y, e.p4p, e.p4m, e.p4x, e.p4y, e.L,   e.eps, e.mp2, t1,    t2,    s13,
-                s14,   s23,   s24,   that,  uhat};
-    if (P.process == GRN_PROC_TENSOR_CON) {
-      A = tensor_me4_2xs<T>(P, K, kk);
-    } else {
-      q_lightcone<T>(x1, pt1sq, e.mp2, e.L, kk.q1p, kk.q1m);
-      q_lightcone<T>(x2, pt2sq, e.mp2, e.L, kk.q2m, kk.q2p);
-      A = tensor_me3<T>(P, K, kk, e.res);
-    }
-    return true;
+  q_lightcone<T>(x1, pt1sq, e.mp2, e.L, kk.q1p, kk.q1m);
+  q_lightcone<T>(x2, pt2sq, e.mp2, e.L, kk.q2m, kk.q2p);
+  return true;
+}
+
+template <typename T>
+GRN_HD bool loop_point_amp(const grn_process_params &P, const Consts &K, const LoopEvent<T> &e,
+                           T kx, T ky, cx<T> &A) {
+  LCKin<T> kk;
+  if (!loop_point_kin<T>(e, kx, ky, kk)) return false;
+  if (P.process == GRN_PROC_TENSOR_CON) {
+    A = tensor_me4_2xs<T>(P, K, kk);
+  } else if (P.process == GRN_PROC_TENSOR_RES) {
+    A = tensor_me3<T>(P, K, kk, e.res);
+  } else {
+    A = regge_me4<T>(P, K, kk.t1, kk.t2, log(kk.s13), log(kk.s14), log(kk.s23), log(kk.s24),
+                     kk.that, kk.uhat);
   }
-  A = regge_me4<T>(P, K, t1, t2, log(s13), log(s14), log(s23), log(s24), that, uhat);
   return true;
 }
 
@@ -844,10 +1077,10 @@ GRN_HD void make_loop_event_fast(const grn_process_params &P, const Consts &K, c
   auto sinv = [&](double pp, double pm, double mq, double qp, double qm, double mr, double dot) {
     return mq + mr + pp * qm + pm * qp - 2.0 * dot;
   };
-  const double s13 = sinv(p1p, p1m, mp2, b.p3p, b.p3m, K.m3sq, b.p1x * b.p3x + b.p1y * b.p3y);
-  const double s14 = sinv(p1p, p1m, mp2, b.p4p, b.p4m, K.m4sq, b.p1x * b.p4x + b.p1y * b.p4y);
-  const double s23 = sinv(p2p, p2m, mp2, b.p3p, b.p3m, K.m3sq, b.p2x * b.p3x + b.p2y * b.p3y);
-  const double s24 = sinv(p2p, p2m, mp2, b.p4p, b.p4m, K.m4sq, b.p2x * b.p4x + b.p2y * b.p4y);
+  const double s13 = sinv(p1p, p1m, mp2, b.p3p, b.p3m, b.m3sq, b.p1x * b.p3x + b.p1y * b.p3y);
+  const double s14 = sinv(p1p, p1m, mp2, b.p4p, b.p4m, b.m4sq, b.p1x * b.p4x + b.p1y * b.p4y);
+  const double s23 = sinv(p2p, p2m, mp2, b.p3p, b.p3m, b.m3sq, b.p2x * b.p3x + b.p2y * b.p3y);
+  const double s24 = sinv(p2p, p2m, mp2, b.p4p, b.p4m, b.m4sq, b.p2x * b.p4x + b.p2y * b.p4y);
   e.is13 = T(1.0 / s13); e.is14 = T(1.0 / s14); e.is23 = T(1.0 / s23); e.is24 = T(1.0 / s24);
   const double l0 = log(P.regge.s0);
   const double L13 = log(s13) - l0, L14 = log(s14) - l0, L23 = log(s23) - l0, L24 = log(s24) - l0;
@@ -984,7 +1217,7 @@ GRN_HD void make_loop_event(const Consts &K, const Born &b, LoopEvent<T> &e) {
   e.a1 = T((b.p3p + b.p4p - K.eps) / K.L);
   e.a2 = T((b.p3m + b.p4m - K.eps) / K.L);
   e.L = T(K.L); e.invL2 = T(1.0 / (K.L * K.L)); e.invL = T(1.0 / K.L);
-  e.eps = T(K.eps); e.mp2 = T(K.mp2); e.m3sq = T(K.m3sq); e.m4sq = T(K.m4sq);
+  e.eps = T(K.eps); e.mp2 = T(K.mp2); e.m3sq = T(b.m3sq); e.m4sq = T(b.m4sq);
   if (K.n_res > 0) {
     const ResVec<double> v =
         res_vectors<double>(K, b.p3p, b.p3m, b.p3x, b.p3y, b.p4p, b.p4m, b.p4x, b.p4y);
@@ -1011,6 +1244,40 @@ GRN_HD cx<double> born_amp(const grn_process_params &P, const Consts &K, const B
   }
   return regge_me4<double>(P, K, b.t1, b.t2, log(b.s13), log(b.s14), log(b.s23), log(b.s24),
                            b.that, b.uhat);
+}
+
+// Processes whose |M|^2 is a sum over several helicity amplitudes (vector pairs, "2xV").
+GRN_HD bool is_vector_pair(const grn_process_params &P) {
+  return P.process == GRN_PROC_TENSOR_CON && P.central_spin == 1;
+}
+
+// Tree-level 2xV amplitudes (FP64) in the polarization basis of the central pair.
+GRN_HD_COLD void born_amps_2xv(const grn_process_params &P, const Consts &K, const Born &b,
+                          cx<double> A[9]) {
+  LCKin<double> k{b.p1p, b.p1m, b.p1x, b.p1y, b.p2p, b.p2m, b.p2x,  b.p2y, b.p3p,
+                  b.p3m, b.p3x, b.p3y, b.p4p, b.p4m, b.p4x, b.p4y,  K.L,   K.eps,
+                  K.mp2, b.t1,  b.t2,  b.s13, b.s14, b.s23, b.s24, b.that, b.uhat};
+  q_lightcone<double>(b.x1, b.pt1sq, K.mp2, K.L, k.q1p, k.q1m);
+  q_lightcone<double>(b.x2, b.pt2sq, K.mp2, K.L, k.q2m, k.q2p);
+  LV<double> e3[3], e4[3];
+  vector_basis<double>(b.p3p, b.p3m, b.p3x, b.p3y, e3);
+  vector_basis<double>(b.p4p, b.p4m, b.p4x, b.p4y, e4);
+  tensor_me4_2xv<double>(P, K, k, b.m2, e3, e4, A);
+}
+
+// Unscreened |M|^2 of the tree-level point (sum over the helicity amplitudes; the four
+// proton helicity configurations of the high-energy vertex are equal and averaged).
+template <bool VV = false>
+GRN_HD double born_amp2(const grn_process_params &P, const Consts &K, const Born &b) {
+  if (VV && is_vector_pair(P)) {
+    cx<double> A[9];
+    born_amps_2xv(P, K, b, A);
+    double s = 0.0;
+    for (int h = 0; h < 9; ++h) s += A[h].re * A[h].re + A[h].im * A[h].im;
+    return s;
+  }
+  const cx<double> A0 = born_amp(P, K, b);
+  return A0.re * A0.re + A0.im * A0.im;
 }
 
 // u-independent part of the weight and the u-dependent Jacobians

@@ -1,0 +1,155 @@
+"""Vector-meson pairs with two-body cascades on the GPU through the C ABI: rho rho ->
+pi+ pi- pi+ pi- and phi phi -> K+ K- K+ K- in the <F> class (14-dimensional points), the
+tensor-pomeron 2xV amplitude and the Regge continuum, against the reference's golden vectors
+and the CPU oracle; FP32 kt-loop against FP64; VEGAS integration in 14 dimensions."""
+import ctypes
+import os
+
+import numpy as np
+import pytest
+
+from conftest import GOLDEN
+from oracle import oracle_api as orc
+from test_gpu_parity import _mixed_ok
+
+pytestmark = pytest.mark.gpu
+
+TOL = 5e-10
+
+
+def _load(name):
+    return np.load(os.path.join(GOLDEN, name))
+
+
+def _params(g):
+    from graniitti_gb300 import card
+    return card.build_params(card.read_card(os.path.join(GOLDEN, "cards", str(g["card"]))),
+                             str(g["proc"]))
+
+
+def _rel(w, wr):
+    nz = wr > 0
+    assert np.array_equal(w > 0, nz)
+    return np.abs(w[nz] - wr[nz]) / wr[nz]
+
+
+@pytest.mark.parametrize("name", ["rr_tree_weights.npz", "rr_regge_tree_weights.npz",
+                                  "ff_tree_weights.npz"])
+def test_cascade_tree_vs_reference(gpu, name):
+    import graniitti_gb300 as g
+    gl = _load(name)
+    P = _params(gl)
+    e = g.Engine(P, 0)
+    assert e.dim == 14
+    w, fl = e.event_weights(gl["u"], prec=g.FP64)
+    wo, flo = orc.weights(P, gl["u"])
+    assert np.array_equal(fl, flo) and np.array_equal(fl & 1, gl["kin"])
+    kin = gl["kin"] == 1
+    assert np.array_equal(((fl >> 1) & 1)[kin], gl["fid"][kin])
+    r = _rel(w, gl["w"])
+    print("%s: GPU vs reference max rel %.2e, median %.2e (%d weights)" %
+          (name, r.max(), np.median(r), r.size))
+    assert r.max() < TOL
+    assert _rel(w, wo).max() < TOL
+    # the central pair (off-shell masses) as the reference has it
+    p4, _, _ = e.event_kinematics(gl["u"])
+    scale = np.abs(gl["p4"]).max(axis=2, keepdims=True)
+    assert (np.abs(p4 - gl["p4"])[kin] / scale[kin]).max() < 1e-12
+
+
+def test_cascade_screened_vs_reference(gpu):
+    import graniitti_gb300 as g
+    gl = _load("rr_screened_15x12_weights.npz")
+    t = _load("eikonal_nbt1024_nkt10000.npz")
+    P = _params(gl)
+    e = g.Engine(P, 0)
+    e.eikonal_set(t["mbt"], t["msa"])
+    w, fl = e.event_weights(gl["u"], prec=g.FP64)
+    assert np.array_equal(fl & 1, gl["kin"])
+    r = _rel(w, gl["w"])
+    print("screened rho rho (2xV): GPU FP64 vs reference max rel %.2e" % r.max())
+    assert r.max() < 1e-9
+    wm, _ = e.event_weights(gl["u"], prec=g.MIXED)
+    Pb = type(P)()
+    ctypes.memmove(ctypes.byref(Pb), ctypes.byref(P), ctypes.sizeof(P))
+    Pb.screening = 0
+    wb, _ = g.Engine(Pb, 0).event_weights(gl["u"], prec=g.FP64)
+    ok, rel = _mixed_ok(wm, w, wb)
+    print("screened rho rho: mixed vs fp64 max rel %.3e" % rel.max())
+    assert ok, rel.max()
+
+
+@pytest.mark.parametrize("proc", [
+    "PP[CONTENSOR]<F> -> rho(770)0 > {pi+ pi-} rho(770)0 > {pi+ pi-}",
+    "PP[CON]<F> -> rho(770)0 > {pi+ pi-} rho(770)0 > {pi+ pi-}"])
+def test_cascade_mixed_loop_vs_fp64(gpu, proc):
+    """FP32 kt-loop against the FP64 loop on 4096 points (tables built on the device)."""
+    import graniitti_gb300 as g
+    import philox_np
+    from graniitti_gb300 import card
+    from conftest import CARD_SCR
+    P = card.build_params(card.read_card(CARD_SCR), proc)
+    e = g.Engine(P, 0)
+    e.eikonal_build()
+    u = philox_np.uniforms(85, 4096, 14)
+    w64, fl = e.event_weights(u, prec=g.FP64)
+    wm, flm = e.event_weights(u, prec=g.MIXED)
+    assert np.array_equal(fl, flm)
+    Pb = type(P)()
+    ctypes.memmove(ctypes.byref(Pb), ctypes.byref(P), ctypes.sizeof(P))
+    Pb.screening = 0
+    wb, _ = g.Engine(Pb, 0).event_weights(u, prec=g.FP64)
+    ok, rel = _mixed_ok(wm, w64, wb)
+    print("%s: mixed vs fp64 (4096 points, %d screened) max rel %.3e, median %.3e" %
+          (proc.split("]")[0], int((w64 > 0).sum()), rel.max(), np.median(rel)))
+    assert ok, rel.max()
+
+
+def test_cascade_vegas_matches_oracle_mc(gpu):
+    """VEGAS over 14 dimensions: the integral of the tensor rho rho process agrees with a
+    plain Monte Carlo estimate from the oracle on uniform points."""
+    import graniitti_gb300 as g
+    import philox_np
+    from graniitti_gb300 import _abi, card
+    from conftest import CARD
+    proc = "PP[CONTENSOR]<F> -> rho(770)0 > {pi+ pi-} rho(770)0 > {pi+ pi-}"
+    P = card.build_params(card.read_card(CARD), proc)
+    e = g.Engine(P, 0)
+    vp = _abi.VegasParams()
+    vp.bins, vp.iter, vp.ncall, vp.lambda_ = 128, 6, 1 << 20, 1.5
+    vp.chi2max, vp.precision, vp.burnin_iter, vp.prec, vp.seed = 10.0, 1e-3, 3, 0, 5
+    r = e.vegas_integrate(vp)
+    u = philox_np.uniforms(86, 1 << 18, 14)
+    wo, _ = orc.weights(P, u, nthreads=16)
+    mc, err = wo.mean(), wo.std() / np.sqrt(len(wo))
+    pull = (r.sigma - mc) / np.hypot(r.sigma_err, err)
+    print("sigma rho rho (2xV, unscreened): VEGAS %.5e +- %.1e, oracle MC %.5e +- %.1e, "
+          "pull %.2f" % (r.sigma, r.sigma_err, mc, err, pull))
+    assert abs(pull) < 4
+
+
+def test_cascade_rejections(gpu):
+    import graniitti_gb300 as g
+    from graniitti_gb300 import _abi
+    gl = _load("rr_tree_weights.npz")
+    P = _params(gl)
+    lib = _abi.load_library()
+
+    def status(mod):
+        Q = type(P)()
+        ctypes.memmove(ctypes.byref(Q), ctypes.byref(P), ctypes.sizeof(P))
+        mod(Q)
+        h = ctypes.c_void_p()
+        st = lib.grn_create(ctypes.byref(Q), 0, ctypes.byref(h))
+        if h.value:
+            lib.grn_destroy(h)
+        return st
+
+    assert status(lambda Q: None) == _abi.GRN_OK
+    assert status(lambda Q: setattr(Q, "phase_space", _abi.GRN_PS_CONTINUUM)) == \
+        _abi.GRN_ERR_UNSUPPORTED
+    assert status(lambda Q: setattr(Q, "n_decay", 0)) == _abi.GRN_ERR_UNSUPPORTED
+    assert status(lambda Q: setattr(Q, "n_decay", 3)) == _abi.GRN_ERR_UNSUPPORTED
+    e = g.Engine(P, 0)
+    with pytest.raises(Exception):
+        g.Flow(e)  # the flow kernels are built for 8 dimensions
