@@ -219,21 +219,25 @@ def _summary(results, ms, npts, steps):
             "rel_var_per_point": rel_var, "seconds_to_0.1pct": t01, "ms_per_step": ms / steps}
 
 
-BATCH_MIX = [("PP[CON]<C> -> pi+ pi-", 0.5), ("PP[CON]<C> -> K+ K-", 0.3),
-             ("PP[CONTENSOR]<C> -> pi+ pi-", 0.2)]
+# The mixed workload of uneven multiplicity: tensor-pomeron f2(1270) -> pi+ pi- (2-body),
+# the Regge pi+ pi- continuum (2-body) and tensor-pomeron rho rho -> pi+ pi- pi+ pi- (4-body,
+# 14 dimensions), 50/30/20, screened with the generator's default loop grid (15 x 12
+# intervals, kt <= 1.75 GeV).
+BATCH_MIX = [("PP[RESTENSOR]<F> -> pi+ pi-", 0.5), ("PP[CON]<C> -> pi+ pi-", 0.3),
+             ("PP[CONTENSOR]<F> -> rho(770)0 > {pi+ pi-} rho(770)0 > {pi+ pi-}", 0.2)]
 
 
 def batched_leg(g, _abi, torch, total, steps, warmup, device):
-    """Screened 2-body continua batched in one pass (fused launches, CUDA graph) against
-    the same processes run one after another; the same points, grids and results."""
+    """The mixed 2- and 4-body workload batched in one pass (fused launches, CUDA graph)
+    against the same processes run one after another; the same points, grids and results."""
     from graniitti_gb300 import card
     c = card.read_card(CARD_SCR)
+    c["PROCESSPARAM"]["RES"] = ["f2_1270"]
 
     def engines(seed0):
         out = []
         for k, (proc, frac) in enumerate(BATCH_MIX):
             P = card.build_params(c, proc)
-            P.loop.n_kt, P.loop.n_phi, P.loop.kt_max = LOOP_KT, LOOP_PHI, LOOP_KTMAX
             P.loop.n_bt, P.loop.n_kt2 = N_BT, N_KT2
             e = g.Engine(P, device)
             e.eikonal_build(N_BT, N_KT2)
@@ -283,7 +287,9 @@ def batched_leg(g, _abi, torch, total, steps, warmup, device):
                       "sigma_barn": r.sigma, "sigma_rel_err": r.sigma_err / r.sigma})
         e.close()
     n = sum(p["points_per_step"] for p in procs)
-    return {"workload": "screened 2-body continua, %s of %d points per pass, one fused pass"
+    return {"workload": "screened f2(1270) -> pi+ pi- (tensor pomeron) + pi+ pi- continuum "
+                        "(Regge) + rho rho -> 4 pi (tensor pomeron, 14 dims), %s of %d points per "
+                        "pass, loop grid 15 x 12, one fused pass"
                         % ("/".join(str(int(f * 100)) for _, f in BATCH_MIX), n),
             "ms_per_step_batched": ms_b, "ms_per_step_separate": ms_s,
             "evaluations_per_s_batched": n / (ms_b * 1e-3),

@@ -184,8 +184,11 @@ SIGNATURES = {
     "grn_writer_open": (c_int32, [ctypes.c_char_p, c_int32, ctypes.c_char_p, ctypes.c_char_p,
                                   c_void_p]),
     "grn_writer_close": (c_int32, [c_void_p]),
-    "grn_write_events": (c_int32, [c_void_p, c_void_p, c_void_p, c_int64, c_void_p, c_double,
-                                   c_double, c_double, c_void_p]),
+    "grn_write_events": (c_int32, [c_void_p, c_void_p, c_void_p, c_int64, c_void_p, c_int32,
+                                   c_double, c_double, c_double, c_void_p]),
+    "grn_write_cascade_records": (c_int32, [c_void_p, c_void_p, c_void_p, c_int64, c_void_p,
+                                            c_void_p, c_double, c_double, c_double, c_double]),
+    "grn_event_daughters": (c_int32, [c_void_p, c_void_p, c_int64, c_int32, c_void_p]),
     "grn_write_records": (c_int32, [c_void_p, c_void_p, c_int64, c_void_p, c_void_p, c_double,
                                     c_double, c_double, c_double]),
     "grn_vegas_get_grid": (c_int32, [c_void_p, c_void_p]),

@@ -668,6 +668,26 @@ grn_status grn_event_kinematics(grn_engine *e, const double *u, int64_t n, int32
   return GRN_OK;
 }
 
+grn_status grn_event_daughters(grn_engine *e, const double *u, int64_t n, int32_t dim,
+                               double *pd_out) {
+  if (!e || !u || !pd_out || n < 0) return fail(GRN_ERR_INVALID, "null argument");
+  if (dim != e->dim) return fail(GRN_ERR_INVALID, "dim must equal grn_dim()");
+  if (e->P.n_decay != 2) return fail(GRN_ERR_STATE, "the process has no decay cascades");
+  if (n == 0) return GRN_OK;
+  GRN_CUDA(cudaSetDevice(e->device));
+  GRN_CUDA(e->d_u.ensure(n * dim * sizeof(double)));
+  GRN_CUDA(e->d_aux.ensure(n * 16 * sizeof(double)));
+  GRN_CUDA(cudaMemcpyAsync(e->d_u.p, u, n * dim * sizeof(double),
+                           is_device_ptr(u) ? cudaMemcpyDeviceToDevice : cudaMemcpyHostToDevice,
+                           e->stream));
+  GRN_CUDA(grn::launch_event_daughters(e->args(), e->d_u.as<double>(), n, dim,
+                                       e->d_aux.as<double>(), e->stream));
+  GRN_CUDA(cudaMemcpyAsync(pd_out, e->d_aux.p, n * 16 * sizeof(double), cudaMemcpyDefault,
+                           e->stream));
+  GRN_CUDA(cudaStreamSynchronize(e->stream));
+  return GRN_OK;
+}
+
 grn_status grn_uniforms(grn_engine *e, uint64_t seed, uint32_t stream, int64_t first, int64_t n,
                         int32_t dim, double *out) {
   if (!e || !out || n < 0 || dim < 1 || dim > 16) return fail(GRN_ERR_INVALID, "bad argument");
@@ -1126,6 +1146,7 @@ struct grn_batch {
   grn::BatchProc           *h_procs = nullptr;  // pinned: uploaded by the graph every pass
   int                       born_blocks = 0, loop_blocks = 0;
   int                       max_dim     = 8;  // largest hypercube dimension of the batch
+  int                       max_nh      = 0;  // largest bins * dim of the batch
   bool                      has_kind[2] = {false, false};  // generic / record-mode processes
   cudaStream_t              side = nullptr;     // second branch of the captured graph
   cudaEvent_t               fork = nullptr, join = nullptr;
@@ -1153,7 +1174,8 @@ grn_status batch_capture(grn_batch *b, int refine, int track_max) {
   }
   if (ce == cudaSuccess)
     ce = cudaMemsetAsync(b->d_counter.p, 0, sizeof(unsigned long long), b->stream);
-  if (ce == cudaSuccess) ce = grn::launch_batch_born(np, b->born_blocks, b->max_dim, b->stream);
+  if (ce == cudaSuccess)
+    ce = grn::launch_batch_born(np, b->born_blocks, b->max_dim, b->max_nh, b->stream);
   // stage B: the record-mode processes in one persistent launch; the processes on the
   // generic loop in their own launches on a second branch of the graph (concurrent)
   const bool two = b->has_kind[0] && b->has_kind[1];
@@ -1161,6 +1183,7 @@ grn_status batch_capture(grn_batch *b, int refine, int track_max) {
   if (ce == cudaSuccess && two) ce = cudaStreamWaitEvent(b->side, b->fork, 0);
   if (ce == cudaSuccess && b->has_kind[1])
     ce = grn::launch_batch_loop(np, b->d_counter.as<unsigned long long>(), b->loop_blocks,
+                                b->max_nh,
                                 b->stream);
   for (int p = 0; p < np && ce == cudaSuccess; ++p) {
     grn_engine *e = b->eng[p];
@@ -1266,6 +1289,7 @@ grn_status grn_batch_create(grn_engine *const *engines, int32_t n, grn_batch **o
     q.l_bins    = e->d_lbins.as<uint64_t>();
     q.l_bins_hi = lbins_hi(e);
     b->max_dim  = std::max(b->max_dim, e->dim);
+    b->max_nh   = std::max(b->max_nh, e->bins * e->dim);
     q.rf        = rec ? e->d_recf.as<float>() : nullptr;
     q.rd        = rec ? e->d_recd.as<double>() : nullptr;
     if (e->P.screening) b->has_kind[rec ? 1 : 0] = true;
@@ -1276,7 +1300,7 @@ grn_status grn_batch_create(grn_engine *const *engines, int32_t n, grn_batch **o
     blk    = q.blk1;
   }
   b->born_blocks = nb;
-  b->loop_blocks = grn::batch_loop_blocks(dev);
+  b->loop_blocks = grn::batch_loop_blocks(dev, b->max_nh);
   if (st != GRN_OK) {
     grn_batch_destroy(b);
     return st;

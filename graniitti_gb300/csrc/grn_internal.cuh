@@ -48,6 +48,8 @@ cudaError_t launch_event_weights(const KArgs &a, int prec, const double *u, int6
 int         loop_grid_blocks(int device);
 cudaError_t launch_event_kinematics(const KArgs &a, const double *u, int64_t n, int dim,
                                     double *p4, double *ts, uint8_t *flags, cudaStream_t st);
+cudaError_t launch_event_daughters(const KArgs &a, const double *u, int64_t n, int dim,
+                                   double *pd, cudaStream_t st);
 cudaError_t launch_uniforms(uint64_t seed, uint32_t stream, int64_t first, int64_t n, int dim,
                             double *out, cudaStream_t st);
 
@@ -135,12 +137,14 @@ struct BatchProc {
 // The process table of a batch, copied into constant memory (stream-ordered).
 cudaError_t upload_batch_procs(const BatchProc *h_procs, int np, cudaStream_t st);
 // Stage A of every process in one launch (block b serves the process whose range holds b).
-cudaError_t launch_batch_born(int np, int nblocks, int max_dim, cudaStream_t st);
+// max_dim / max_nh: largest hypercube dimension / bins * dim of the batch's processes.
+cudaError_t launch_batch_born(int np, int nblocks, int max_dim, int max_nh, cudaStream_t st);
 // Stage B of the record-mode processes in one persistent launch (two events per thread):
 // blocks take chunks of work from the counter (zeroed by the caller) over the listed events
 // of those processes.
-cudaError_t launch_batch_loop(int np, unsigned long long *counter, int nblocks, cudaStream_t st);
-int         batch_loop_blocks(int device);
+cudaError_t launch_batch_loop(int np, unsigned long long *counter, int nblocks, int max_nh,
+                              cudaStream_t st);
+int         batch_loop_blocks(int device, int max_nh);
 
 // FP32 FMA throughput probe: returns flops executed by one launch.
 double      fma_probe_flops(int blocks, int threads, int iters);

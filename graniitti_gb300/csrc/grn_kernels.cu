@@ -613,6 +613,29 @@ __global__ void k_event_kinematics(const KArgs A, const double *__restrict__ u, 
                GRN_FLAG_VETOCUTS_OK | GRN_FLAG_AMPLITUDE_OK;
 }
 
+// Cascade daughters (px, py, pz, E) of the points (zeros where the kinematics fail).
+__global__ void k_event_daughters(const KArgs A, const double *__restrict__ u, int64_t n, int dim,
+                                  double *__restrict__ pd) {
+  const int64_t i = static_cast<int64_t>(blockIdx.x) * blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  double x[kMaxDim];
+  for (int d = 0; d < kMaxDim; ++d) x[d] = d < dim ? u[i * dim + d] : 0.0;
+  Born   b;
+  double d4[4][4] = {};
+  if (born_kinematics<true>(A.P, A.K, x, b))
+    cascade_daughters(A.P, b.p3x, b.p3y, b.mt3 * sinh(b.y3), b.mt3 * cosh(b.y3), sqrt(b.m3sq),
+                      b.p4x, b.p4y, b.mt4 * sinh(b.y4), b.mt4 * cosh(b.y4), sqrt(b.m4sq), x, d4);
+  for (int k = 0; k < 16; ++k) pd[i * 16 + k] = d4[k / 4][k % 4];
+}
+
+cudaError_t launch_event_daughters(const KArgs &a, const double *u, int64_t n, int dim,
+                                   double *pd, cudaStream_t st) {
+  if (n <= 0) return cudaSuccess;
+  const unsigned blocks = static_cast<unsigned>((n + 127) / 128);
+  k_event_daughters<<<blocks, 128, 0, st>>>(a, u, n, dim, pd);
+  return cudaGetLastError();
+}
+
 cudaError_t launch_event_kinematics(const KArgs &a, const double *u, int64_t n, int dim,
                                     double *p4, double *ts, uint8_t *flags, cudaStream_t st) {
   if (n <= 0) return cudaSuccess;
@@ -1111,15 +1134,17 @@ __global__ void __launch_bounds__(kVegasThreads, 2)
   flush_block(sf2, nh, f2mat, acc, cnt, maxf, maxW);
 }
 
-// Resident blocks per SM of the record-mode loop kernels (one or two events per thread).
+// Resident blocks per SM of the record-mode loop kernels (one or two events per thread),
+// for the f^2 histogram of an 8-dimensional process with the largest bin count.
+constexpr size_t kHistBytes8 = kMaxBins * 8 * sizeof(double);
 int loop_rec_blocks_per_sm(int pair) {
   int per = 0;
   if (pair)
     cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, k_vegas_loop_rec2, kVegasThreads,
-                                                  kMaxBins * kMaxDim * sizeof(double));
+                                                  kHistBytes8);
   else
     cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, k_vegas_loop_rec, kVegasThreads,
-                                                  kMaxBins * kMaxDim * sizeof(double));
+                                                  kHistBytes8);
   return per < 1 ? 1 : per;
 }
 
@@ -1127,7 +1152,7 @@ int vegas_grid_blocks(int device) {
   int sms = 0, per = 0;
   cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, device);
   cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, k_vegas_loop_rec, kVegasThreads,
-                                                kMaxBins * kMaxDim * sizeof(double));
+                                                kHistBytes8);
   if (per < 1) per = 1;
   return sms * per;
 }
@@ -1216,9 +1241,9 @@ __global__ void __launch_bounds__(kVegasThreads, 3) k_batch_born(int np) {
                        static_cast<int>(blockIdx.x) - q.blk0, q.blk1 - q.blk0);
 }
 
-cudaError_t launch_batch_born(int np, int nblocks, int max_dim, cudaStream_t st) {
+cudaError_t launch_batch_born(int np, int nblocks, int max_dim, int max_nh, cudaStream_t st) {
   // shared memory: grid and f^2 histogram of the largest process (bins * dim each)
-  const size_t sm = 2 * static_cast<size_t>(kMaxBins) * max_dim * sizeof(double);
+  const size_t sm = 2 * static_cast<size_t>(max_nh) * sizeof(double);
   if (max_dim <= 8)
     k_batch_born<8><<<nblocks, kVegasThreads, sm, st>>>(np);
   else
@@ -1335,17 +1360,17 @@ __global__ void __launch_bounds__(kVegasThreads, 2)
   }
 }
 
-int batch_loop_blocks(int device) {
+int batch_loop_blocks(int device, int max_nh) {
   int sms = 0, per = 0;
   cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, device);
   cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, k_batch_loop<true>, kVegasThreads,
-                                                kMaxBins * kMaxDim * sizeof(double));
+                                                max_nh * sizeof(double));
   return sms * (per < 1 ? 1 : per);
 }
 
-cudaError_t launch_batch_loop(int np, unsigned long long *counter, int nblocks, cudaStream_t st) {
-  k_batch_loop<true><<<nblocks, kVegasThreads, kMaxBins * kMaxDim * sizeof(double), st>>>(
-      np, counter);
+cudaError_t launch_batch_loop(int np, unsigned long long *counter, int nblocks, int max_nh,
+                              cudaStream_t st) {
+  k_batch_loop<true><<<nblocks, kVegasThreads, max_nh * sizeof(double), st>>>(np, counter);
   return cudaGetLastError();
 }
 

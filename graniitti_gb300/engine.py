@@ -357,6 +357,7 @@ class Graniitti:
 
     def ReadInput(self, inputfile, cmd_PROCESS=None):
         self.card = _card.read_card(inputfile)
+        self.process = cmd_PROCESS or self.card["PROCESSPARAM"]["PROCESS"]
         self.params = _card.build_params(self.card, cmd_PROCESS)
         self.vp = _card.vegas_params(self.card, prec=self.prec)
         self.integrator = self.card.get("GENERALPARAM", {}).get("INTEGRATOR", "VEGAS")
@@ -442,7 +443,7 @@ class Graniitti:
             trials += int(self.vp.ncall) if need >= na else int(idx[-1]) + 1
             ovf += no
             it += 1
-        out = np.concatenate(pts) if pts else np.zeros((0, 8))
+        out = np.concatenate(pts) if pts else np.zeros((0, self.engine.dim))
         if writer is not None:
             pdg = self.card_pdg()
             writer.write_points(self.engine, out, pdg, self.result.sigma * 1e12,
@@ -451,11 +452,14 @@ class Graniitti:
         return out, trials, ovf
 
     def card_pdg(self):
-        """PDG codes of the beam and the two central final states of the process."""
+        """PDG codes of the beam and the two central particles of the process, followed for
+        decay cascades by the four daughters."""
         from .modeldata import PARTICLES
-        proc = self.card["PROCESSPARAM"]["PROCESS"]
-        finals = _card.parse_process(proc)[3]
-        return [PARTICLES["p+"][0], PARTICLES[finals[0]][0], PARTICLES[finals[1]][0]]
+        tree = _card.decay_tree(self.process.split("@")[0].split("->", 1)[1])
+        out = [PARTICLES["p+"][0]] + [PARTICLES[name][0] for name, _ in tree]
+        for _, kids in tree:
+            out += [PARTICLES[name][0] for name, _ in kids]
+        return out
 
 
 def kernel_timing(engine, reset=True):

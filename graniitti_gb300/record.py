@@ -27,13 +27,14 @@ class EventWriter:
         self.written = 0
 
     def write_points(self, engine, u, pdg, sigma_pb, sigma_err_pb, weight=1.0):
-        """Events of hypercube points u (n x dim): kinematics on the engine, then records."""
+        """Events of hypercube points u (n x dim): kinematics on the engine, then records.
+        pdg: beam, the two central particles and, for cascades, the four daughters."""
         u = np.ascontiguousarray(u, dtype=np.float64)
-        pd = (ctypes.c_int32 * 3)(*pdg)
+        pd = (ctypes.c_int32 * len(pdg))(*pdg)
         n = ctypes.c_int64()
         _abi.check(self.lib.grn_write_events(self.h, engine.h, u.ctypes.data_as(ctypes.c_void_p),
-                                             u.shape[0], pd, weight, sigma_pb, sigma_err_pb,
-                                             ctypes.byref(n)))
+                                             u.shape[0], pd, len(pdg), weight, sigma_pb,
+                                             sigma_err_pb, ctypes.byref(n)))
         self.written += n.value
         return n.value
 
@@ -45,6 +46,20 @@ class EventWriter:
         _abi.check(self.lib.grn_write_records(self.h, p4.ctypes.data_as(ctypes.c_void_p),
                                               p4.shape[0], pd, ms, sqrt_s, weight, sigma_pb,
                                               sigma_err_pb))
+        self.written += p4.shape[0]
+
+    def write_cascade_momenta(self, p4, pd, pdg, masses, sqrt_s, sigma_pb, sigma_err_pb,
+                              weight=1.0):
+        """Cascade events from 4-vectors: p4 (n x 4 x 4) as for write_momenta with the
+        central particles off shell, pd (n x 4 x 4) their four daughters; pdg, masses: beam,
+        the two central particles, the four daughters."""
+        p4 = np.ascontiguousarray(p4, dtype=np.float64)
+        pd = np.ascontiguousarray(pd, dtype=np.float64)
+        ids = (ctypes.c_int32 * 7)(*pdg)
+        ms = (ctypes.c_double * 7)(*masses)
+        _abi.check(self.lib.grn_write_cascade_records(
+            self.h, p4.ctypes.data_as(ctypes.c_void_p), pd.ctypes.data_as(ctypes.c_void_p),
+            p4.shape[0], ids, ms, sqrt_s, weight, sigma_pb, sigma_err_pb))
         self.written += p4.shape[0]
 
     def close(self):

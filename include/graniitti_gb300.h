@@ -259,6 +259,13 @@ grn_status grn_event_weights_noalloc(grn_engine *e, const double *u, int64_t n, 
 grn_status grn_event_kinematics(grn_engine *e, const double *u, int64_t n, int32_t dim,
                                 double *p4_out, double *ts_out, uint8_t *flags);
 
+/* Cascade processes (n_decay = 2): the four daughters of the two central particles, per
+ * point 16 doubles (px, py, pz, E) in the order central 1 -> 2 daughters, central 2 -> 2
+ * daughters (the leaves of lts.decaytree, ConstructDecayKinematics). GRN_ERR_STATE for an
+ * engine without cascades. */
+grn_status grn_event_daughters(grn_engine *e, const double *u, int64_t n, int32_t dim,
+                               double *pd_out);
+
 /* ------------------------------------------------------------------------ */
 /* Counter-based uniforms (Philox4x32-10, Salmon et al., SC'11)               */
 /* ------------------------------------------------------------------------ */
@@ -461,13 +468,15 @@ grn_status grn_writer_open(const char *path, int32_t format, const char *tool, c
                            grn_writer **out);
 grn_status grn_writer_close(grn_writer *w);
 /* Events from hypercube points u (n x dim, host, point-major: e.g. from
- * grn_vegas_points): kinematics by grn_event_kinematics, PDG codes of the beams and
- * the two central particles in pdg[3], weight written with every event (1 for
- * unweighted events), cross section and error in pb. Event numbers continue from the
- * writer's count. Points whose kinematics fail are skipped (*written says how many
- * were written). */
+ * grn_vegas_points): kinematics by grn_event_kinematics (and grn_event_daughters), PDG codes
+ * in pdg[n_pdg]: the beams and the two central particles (n_pdg = 3), followed for cascades
+ * by the four daughters (n_pdg = 7; the central particles are then written with status 2 and
+ * their decay vertices, WriteDecayKinematics, src/MProcess.cc:1289-1315, at the origin),
+ * weight written with every event (1 for unweighted events), cross section and error in pb.
+ * Event numbers continue from the writer's count. Points whose kinematics fail are skipped
+ * (*written says how many were written). */
 grn_status grn_write_events(grn_writer *w, grn_engine *e, const double *u, int64_t n,
-                            const int32_t pdg[3], double weight, double sigma_pb,
+                            const int32_t *pdg, int32_t n_pdg, double weight, double sigma_pb,
                             double sigma_err_pb, int64_t *written);
 /* The same from 4-vectors already at hand: p4 = n x 16 doubles, (px, py, pz, E) of the
  * two forward legs and the two central particles (the layout of grn_event_kinematics);
@@ -475,6 +484,12 @@ grn_status grn_write_events(grn_writer *w, grn_engine *e, const double *u, int64
 grn_status grn_write_records(grn_writer *w, const double *p4, int64_t n, const int32_t pdg[3],
                              const double mass[3], double sqrt_s, double weight, double sigma_pb,
                              double sigma_err_pb);
+/* Cascades from 4-vectors: p4 as for grn_write_records (the central particles with their
+ * off-shell masses), pd = n x 16 doubles of the four daughters (grn_event_daughters);
+ * pdg, mass: beam, the two central particles, the four daughters. */
+grn_status grn_write_cascade_records(grn_writer *w, const double *p4, const double *pd, int64_t n,
+                                     const int32_t pdg[7], const double mass[7], double sqrt_s,
+                                     double weight, double sigma_pb, double sigma_err_pb);
 
 /* ------------------------------------------------------------------------ */
 /* Several processes in one pass (no counterpart in the reference)            */

@@ -129,6 +129,10 @@ def cascade_fixtures():
                     leaves=4)
     save("rr_screened_15x12_weights.npz", seed=84, u=u, card=os.path.basename(CARD_SCR),
          proc=proc, n_bt=1024, n_kt2=10000, loop_kt=15, loop_phi=12, loop_ktmax=1.75, **r)
+    # VEGAS cross section of the tensor rho rho process (reference ranlux48 points, 8 threads)
+    out = subprocess.run([REF_BIN, "vegas", CARD, proc, "--cores", "8"], check=True,
+                         capture_output=True, text=True).stdout
+    write_sigma("rr_vegas_sigma.json", out, proc, os.path.basename(CARD))
 
 
 def main():

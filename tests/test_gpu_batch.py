@@ -84,3 +84,44 @@ def test_batched_integration_matches_separate(gpu):
         assert abs(pull) < 4
     for e in es:
         e.close()
+
+
+def test_batched_mixed_multiplicity_equals_separate(gpu):
+    """The mixed workload of uneven multiplicity: tensor-pomeron f2(1270) -> pi+ pi- (2-body),
+    the Regge pi+ pi- continuum (2-body, record mode) and tensor-pomeron rho rho ->
+    pi+ pi- pi+ pi- (4-body, 14 dimensions), 50/30/20, screened, in one batched pass."""
+    import graniitti_gb300 as g
+    from graniitti_gb300 import _abi, card
+    c = card.read_card(CARD_SCR)
+    c["GENCUTS"]["<F>"]["M"] = [0.5, 3.0]
+    c["PROCESSPARAM"]["RES"] = ["f2_1270"]
+    procs = ["PP[RESTENSOR]<F> -> pi+ pi-", "PP[CON]<C> -> pi+ pi-",
+             "PP[CONTENSOR]<F> -> rho(770)0 > {pi+ pi-} rho(770)0 > {pi+ pi-}"]
+    total = 1 << 17
+    calls = [total // 2, 3 * total // 10, total - total // 2 - 3 * total // 10]
+    es = []
+    for k, proc in enumerate(procs):
+        P = card.build_params(c, proc)
+        e = g.Engine(P, 0)
+        e.eikonal_build(512, 2000)
+        vp = _abi.VegasParams()
+        vp.bins, vp.iter, vp.ncall, vp.lambda_ = 128, 5, calls[k], 1.5
+        vp.chi2max, vp.precision, vp.burnin_iter, vp.prec, vp.seed = 10.0, 1e-3, 3, g.MIXED, 31 + k
+        e.vegas_init(vp)
+        es.append(e)
+    assert [e.dim for e in es] == [8, 8, 14]
+    grids = [e.vegas_grid() for e in es]
+    sep = [e.vegas_iteration(mode=1, refine=False, iter_id=9) for e in es]
+    for e, x in zip(es, grids):
+        e.vegas_clear()
+        e.vegas_set_grid(x)
+    b = g.Batch(es)
+    res, ms = b.iteration(mode=1, refine=False, iter_id=9)
+    for r0, r1 in zip(sep, res):
+        assert r1.evaluations == 2 * r0.evaluations and r1.fidcuts_ok == 2 * r0.fidcuts_ok
+        assert r1.I_this == pytest.approx(r0.I_this, rel=1e-14)
+        assert r1.maxf == pytest.approx(r0.maxf, rel=1e-14)
+    print("batched 2-body + 4-body pass: %.2f ms; I = %s" % (ms, [r.I_this for r in res]))
+    b.close()
+    for e in es:
+        e.close()

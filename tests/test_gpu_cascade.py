@@ -105,26 +105,23 @@ def test_cascade_mixed_loop_vs_fp64(gpu, proc):
     assert ok, rel.max()
 
 
-def test_cascade_vegas_matches_oracle_mc(gpu):
-    """VEGAS over 14 dimensions: the integral of the tensor rho rho process agrees with a
-    plain Monte Carlo estimate from the oracle on uniform points."""
+def test_cascade_cross_section_vs_reference_vegas(gpu):
+    """VEGAS over 14 dimensions: the tensor-pomeron rho rho -> pi+ pi- pi+ pi- cross section
+    against the reference's own VEGAS run."""
+    import json
     import graniitti_gb300 as g
-    import philox_np
     from graniitti_gb300 import _abi, card
-    from conftest import CARD
-    proc = "PP[CONTENSOR]<F> -> rho(770)0 > {pi+ pi-} rho(770)0 > {pi+ pi-}"
-    P = card.build_params(card.read_card(CARD), proc)
+    ref = json.load(open(os.path.join(GOLDEN, "rr_vegas_sigma.json")))
+    P = card.build_params(card.read_card(os.path.join(GOLDEN, "cards", ref["card"])),
+                          ref["process"])
     e = g.Engine(P, 0)
     vp = _abi.VegasParams()
     vp.bins, vp.iter, vp.ncall, vp.lambda_ = 128, 6, 1 << 20, 1.5
     vp.chi2max, vp.precision, vp.burnin_iter, vp.prec, vp.seed = 10.0, 1e-3, 3, 0, 5
     r = e.vegas_integrate(vp)
-    u = philox_np.uniforms(86, 1 << 18, 14)
-    wo, _ = orc.weights(P, u, nthreads=16)
-    mc, err = wo.mean(), wo.std() / np.sqrt(len(wo))
-    pull = (r.sigma - mc) / np.hypot(r.sigma_err, err)
-    print("sigma rho rho (2xV, unscreened): VEGAS %.5e +- %.1e, oracle MC %.5e +- %.1e, "
-          "pull %.2f" % (r.sigma, r.sigma_err, mc, err, pull))
+    pull = (r.sigma - ref["sigma_barn"]) / np.hypot(r.sigma_err, ref["sigma_err_barn"])
+    print("sigma rho rho (2xV, unscreened): GPU %.5e +- %.1e, reference %.5e +- %.1e, pull %.2f"
+          % (r.sigma, r.sigma_err, ref["sigma_barn"], ref["sigma_err_barn"], pull))
     assert abs(pull) < 4
 
 
@@ -153,3 +150,31 @@ def test_cascade_rejections(gpu):
     e = g.Engine(P, 0)
     with pytest.raises(Exception):
         g.Flow(e)  # the flow kernels are built for 8 dimensions
+
+
+def test_cascade_events_written(gpu, tmp_path):
+    """Unweighted rho rho -> pi+ pi- pi+ pi- events through the driver into HepMC3: six
+    vertices, four-momentum conserved, the four pions inside the fiducial cuts."""
+    import graniitti_gb300 as g
+    from graniitti_gb300.record import read_hepmc3
+    from conftest import CARD
+    gr = g.Graniitti()
+    gr.ReadInput(CARD, "PP[CONTENSOR]<F> -> rho(770)0 > {pi+ pi-} rho(770)0 > {pi+ pi-}")
+    gr.SetVegasParam(NCALL=1 << 18, ITER=3, PRECISION=0.01)
+    gr.Initialize()
+    path = str(tmp_path / "rr.hepmc3")
+    u, trials, ovf = gr.Generate(200, output=path, fmt="hepmc3")
+    assert u.shape == (200, 14)
+    ev = read_hepmc3(path)
+    assert len(ev) == 200
+    for e in ev:
+        P = e["particles"]
+        assert e["nv"] == 6 and [P[i][1] for i in range(8, 14)] == [113, 113, 211, -211, 211, -211]
+        p = {i: P[i][2] for i in P}
+        assert np.allclose(p[8], p[10] + p[11], atol=1e-10)
+        assert np.allclose(p[9], p[12] + p[13], atol=1e-10)
+        assert np.allclose(p[1] + p[4], p[2] + p[5] + p[10] + p[11] + p[12] + p[13], atol=1e-7)
+        for i in range(10, 14):
+            pt = np.hypot(p[i][0], p[i][1])
+            eta = np.arcsinh(p[i][2] / pt)
+            assert pt >= 0.1 and abs(eta) <= 0.9

@@ -81,3 +81,74 @@ def test_writer_rejects_bad_format(tmp_path):
     from graniitti_gb300.record import EventWriter
     with pytest.raises(ValueError):
         EventWriter(str(tmp_path / "x"), "lhe")
+
+
+def _boost(v, P):
+    """Boost v (px, py, pz, E) from the rest frame of P to the frame of P."""
+    M = np.sqrt(P[3] ** 2 - P[:3] @ P[:3])
+    b = P[:3] / P[3]
+    g = P[3] / M
+    bp = b @ v[:3]
+    e = g * (v[3] + bp)
+    p = v[:3] + (((g - 1) * bp / (b @ b) if b @ b > 0 else 0.0) + g * v[3]) * b
+    return np.array([p[0], p[1], p[2], e])
+
+
+def _decay(P, m, rng):
+    M = np.sqrt(P[3] ** 2 - P[:3] @ P[:3])
+    pst = np.sqrt(M * M / 4 - m * m)
+    ct, ph = rng.uniform(-1, 1), rng.uniform(0, 2 * np.pi)
+    st = np.sqrt(1 - ct * ct)
+    k = np.array([pst * st * np.cos(ph), pst * st * np.sin(ph), pst * ct, M / 2])
+    kb = k.copy()
+    kb[:3] *= -1
+    return _boost(k, P), _boost(kb, P)
+
+
+@pytest.mark.parametrize("fmt", ["hepmc3", "hepmc2", "hepevt"])
+def test_cascade_records(tmp_path, fmt):
+    """rho rho -> pi+ pi- pi+ pi- records: the central particles with status 2 and their decay
+    vertices (WriteDecayKinematics), four-momentum conserved at all six vertices."""
+    from graniitti_gb300.record import EventWriter, read_hepmc3
+    rng = np.random.default_rng(3)
+    p4 = _events(200, seed=2)
+    mX = np.sqrt(np.maximum(0, (p4[:, 2, 3] + p4[:, 3, 3]) ** 2 -
+                            ((p4[:, 2, :3] + p4[:, 3, :3]) ** 2).sum(axis=1)))
+    p4 = p4[mX > 1.7][:10].copy()  # central systems heavy enough for two 0.78 GeV states
+    assert len(p4) == 10
+    pd = np.zeros((10, 4, 4))
+    for i in range(10):
+        X = p4[i, 2] + p4[i, 3]
+        r1, r2 = _decay(X, 0.78, rng)  # the central pair as two off-shell vector mesons
+        p4[i, 2], p4[i, 3] = r1, r2
+        pd[i, 0], pd[i, 1] = _decay(r1, MPI, rng)
+        pd[i, 2], pd[i, 3] = _decay(r2, MPI, rng)
+    path = str(tmp_path / ("cas." + fmt))
+    with EventWriter(path, fmt) as w:
+        w.write_cascade_momenta(p4, pd, [2212, 113, 113, 211, -211, 211, -211],
+                                [MP, 0.77526, 0.77526, MPI, MPI, MPI, MPI], SQRT_S, 1e3, 10.0)
+    text = open(path).read()
+    if fmt == "hepmc3":
+        ev = read_hepmc3(path)
+        assert len(ev) == 10
+        for k, e in enumerate(ev):
+            P = e["particles"]
+            assert e["nv"] == 6 and e["np"] == 13 and len(P) == 13
+            assert [P[i][1] for i in range(1, 14)] == [2212, 2212, 99, 2212, 2212, 99, 90, 113,
+                                                      113, 211, -211, 211, -211]
+            assert [P[i][4] for i in range(1, 14)] == [4, 1, 81, 4, 1, 81, 81, 2, 2, 1, 1, 1, 1]
+            assert [P[i][0] for i in range(8, 14)] == [7, 7, 8, 8, 9, 9]
+            p = {i: P[i][2] for i in P}
+            assert np.allclose(p[7], p[8] + p[9], atol=1e-9 * SQRT_S)
+            assert np.allclose(p[8], p[10] + p[11], atol=1e-12)
+            assert np.allclose(p[9], p[12] + p[13], atol=1e-12)
+            assert abs(P[8][3] - 0.78) < 1e-9  # off-shell mass of the central particle
+    elif fmt == "hepmc2":
+        assert text.count("\nE ") == 10 and text.count("\nV ") == 60 and text.count("\nP ") == 130
+    else:
+        lines = text.strip().split("\n")
+        assert len(lines) == 10 * 14
+        rows = [l.split() for l in lines[1:14]]
+        assert [int(r[0]) for r in rows[7:9]] == [2, 2]
+        assert [int(x) for x in rows[7][2:6]] == [7, 7, 10, 11]
+        assert [int(x) for x in rows[12][2:6]] == [9, 9, 0, 0]
