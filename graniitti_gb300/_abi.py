@@ -105,7 +105,7 @@ class VegasResult(ctypes.Structure):
     _fields_ = [(n, c_double) for n in (
         "sigma", "sigma_err", "chi2", "I_this", "I2_this", "maxf", "maxW", "evaluations",
         "amplitude_ok", "kinematics_ok", "fidcuts_ok", "vetocuts_ok")] + \
-               [("iterations", c_int64), ("nan_count", c_int64)]
+               [("iterations", c_int64), ("nan_count", c_int64), ("refined", c_int64)]
 
 
 class FlatParams(ctypes.Structure):
@@ -115,7 +115,7 @@ class FlatParams(ctypes.Structure):
 
 class Tuning(ctypes.Structure):
     _fields_ = [("loop_pair", c_int32), ("vegas_blocks", c_int32), ("weight_blocks", c_int32),
-                ("_pad", c_int32)]
+                ("fp64_refine", c_int32)]
 
 
 class TuneResult(ctypes.Structure):

@@ -352,8 +352,6 @@ def set_resonances(P, pp, proc, tune, finals):
     P.n_res = len(names)
     for i, n in enumerate(names):
         r = res[n]
-        if r["J"] == 2 and any(abs(g) > 1e-6 for g in r["g_Tensor"][1:]):
-            raise UnsupportedProcess("%s: J = 2 coupling structures 1..6 are not implemented" % n)
         br = BRANCHING.get(r["pdg"], {}).get(pair)
         if br is None:
             raise UnsupportedProcess("no branching ratio for %s -> %s" % (n, " ".join(finals)))

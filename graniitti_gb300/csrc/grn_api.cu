@@ -93,9 +93,10 @@ struct grn_engine {
   double              loop_norm_im = 0.0;
 
   // staging for host arrays; screened work list of grn_event_weights
-  DevBuf d_u, d_w, d_flags, d_aux, d_wlist, d_wcount;
+  DevBuf d_u, d_w, d_flags, d_aux, d_wlist, d_wrlist, d_wcount;
   int    loop_blocks = 0;
   int    loop_pair   = 0;  // record-mode loop: events per thread - 1 (set by grn_autotune)
+  int    fp64_refine = 1;  // FP32 generic loop: redo badly conditioned events in FP64
 
   // VEGAS
   int         bins = 0;
@@ -106,6 +107,7 @@ struct grn_engine {
   DevBuf      d_xmat, d_xmat_prev, d_f2mat, d_f, d_acc, d_parts, d_sc;
   DevBuf      d_xmat_flat;  // uniform grid of FLAT passes (x = u, vw = 1)
   DevBuf      d_lidx, d_lx, d_lvw, d_lbins, d_lbins_hi;  // screened work list of a VEGAS pass
+  DevBuf      d_rlist;  // slots of that list refined in FP64
   DevBuf      d_recf, d_recd;                // loop records (record mode), shared by calls
   double     *h_sc = nullptr;  // pinned
   double      sumdata = 0, sumchi2 = 0, sweight = 0;
@@ -141,6 +143,7 @@ struct grn_engine {
     a.loop_norm_re = 0.0;
     a.loop_norm_im = loop_norm_im;
     a.loop_pair    = loop_pair;
+    a.refine_tol   = fp64_refine ? grn::kRefineTol : 0.0;
     return a;
   }
 };
@@ -174,7 +177,8 @@ grn_status derive_consts(const grn_process_params &P, grn::Consts &K) {
   if (P.process == GRN_PROC_TENSOR_CON &&
       !(P.tensor.ap_P > 0 && P.tensor.gPNN > 0 && P.tensor.gPps > 0))
     return fail(GRN_ERR_INVALID, "tensor-pomeron parameters are not set");
-  K.n_res = 0;
+  K.n_res     = 0;
+  K.res_smask = 0;
   if (P.process == GRN_PROC_TENSOR_RES) {
     if (!(P.tensor.ap_P > 0 && P.tensor.gPNN > 0))
       return fail(GRN_ERR_INVALID, "tensor-pomeron parameters are not set");
@@ -187,16 +191,20 @@ grn_status derive_consts(const grn_process_params &P, grn::Consts &K) {
       const grn_resonance &R = P.res[r];
       if (!(R.M > 0) || !(R.W >= 0) || !std::isfinite(R.g_decay))
         return fail(GRN_ERR_INVALID, "resonance mass, width or decay coupling invalid");
-      // the reference skips structures with |g| <= 1e-6 (MTensorPomeron.cc:1660-1670)
-      const int first_unsupported = R.J == 2 ? 1 : 2;
-      for (int i = first_unsupported; i < 7; ++i)
-        if (std::fabs(R.g_tensor[i]) > 1e-6)
-          return fail(GRN_ERR_UNSUPPORTED,
-                      R.J == 2 ? "J = 2 resonances: only the coupling structure g0 is implemented"
-                               : "J = 0 resonances have two coupling structures");
+      if (R.J == 0)
+        for (int i = 2; i < 7; ++i)
+          if (std::fabs(R.g_tensor[i]) > 1e-6)
+            return fail(GRN_ERR_UNSUPPORTED, "J = 0 resonances have two coupling structures");
       if (R.J == 2) {
-        K.res_c0[r] = -9.0 * g2 * R.g_tensor[0] * R.g_decay;
+        K.res_c0[r] = -4.5 * g2 * R.g_decay;
         K.res_c1[r] = 0.0;
+        for (int i = 0; i < 7; ++i) {
+          K.res_g[r][i] = R.g_tensor[i];
+          // structures with |g| <= 1e-6 are skipped (iG_PPT_total, MTensorPomeron.cc:1659-1670;
+          // #0 always enters)
+          if (i == 0 || std::fabs(R.g_tensor[i]) > 1e-6) K.res_smask |= 1 << i;
+          if (i > 0 && !(std::fabs(R.g_tensor[i]) > 1e-6)) K.res_g[r][i] = 0.0;
+        }
       } else if (R.J == 0 && R.P == 1) {
         K.res_c0[r] = 18.0 * g2 * R.g_decay * R.g_tensor[0];
         K.res_c1[r] = 18.0 * g2 * R.g_decay * R.g_tensor[1];
@@ -493,7 +501,7 @@ grn_status grn_destroy(grn_engine *e) {
                     &e->d_wlist, &e->d_wcount, &e->d_xmat,      &e->d_xmat_prev, &e->d_f2mat,
                     &e->d_f,     &e->d_acc,    &e->d_parts,     &e->d_sc,        &e->d_lidx,
                     &e->d_lx,    &e->d_lvw,    &e->d_lbins,     &e->d_uw_counts, &e->d_uw_misc,
-                    &e->d_lbins_hi,
+                    &e->d_lbins_hi, &e->d_rlist, &e->d_wrlist,
                     &e->d_uw_idx, &e->d_recf,  &e->d_recd,      &e->d_xmat_flat};
   for (DevBuf *b : bufs) b->release();
   for (grn_flow *f : e->flows) f->e = nullptr;  // they stay valid for grn_flow_destroy
@@ -620,7 +628,8 @@ grn_status grn_event_weights(grn_engine *e, const double *u, int64_t n, int32_t 
     df = e->d_flags.as<uint8_t>();
   }
   GRN_CUDA(e->d_wlist.ensure(n * sizeof(int64_t)));
-  GRN_CUDA(e->d_wcount.ensure(sizeof(unsigned long long)));
+  GRN_CUDA(e->d_wrlist.ensure(n * sizeof(int64_t)));
+  GRN_CUDA(e->d_wcount.ensure(2 * sizeof(unsigned long long)));
   if (e->loop_blocks == 0) e->loop_blocks = grn::loop_grid_blocks(e->device);
   const KArgs a = e->args();
   if (grn::record_mode(a, prec)) {
@@ -632,6 +641,7 @@ grn_status grn_event_weights(grn_engine *e, const double *u, int64_t n, int32_t 
                                            e->stream));
   } else {
     GRN_CUDA(grn::launch_event_weights(a, prec, du, n, dim, dw, df, e->d_wlist.as<int64_t>(),
+                                       e->d_wrlist.as<int64_t>(),
                                        e->d_wcount.as<unsigned long long>(), e->loop_blocks,
                                        e->stream));
   }
@@ -720,6 +730,7 @@ static grn_status vegas_alloc_calls(grn_engine *e, int64_t ncall) {
   const size_t n = static_cast<size_t>(std::max<int64_t>(ncall, 1));
   GRN_CUDA(e->d_f.ensure(n * sizeof(double)));
   GRN_CUDA(e->d_lidx.ensure(n * sizeof(int64_t)));
+  GRN_CUDA(e->d_rlist.ensure(n * sizeof(int64_t)));
   GRN_CUDA(e->d_lx.ensure(static_cast<size_t>(e->dim) * n * sizeof(double)));
   GRN_CUDA(e->d_lvw.ensure(n * sizeof(double)));
   GRN_CUDA(e->d_lbins.ensure(n * sizeof(uint64_t)));
@@ -737,7 +748,7 @@ static grn_status vegas_alloc(grn_engine *e) {
   GRN_CUDA(e->d_xmat_prev.ensure(nh * sizeof(double)));
   GRN_CUDA(e->d_f2mat.ensure(nh * sizeof(double)));
   GRN_CUDA(e->d_sc.ensure(grn::VS_COUNT * sizeof(double)));
-  GRN_CUDA(e->d_acc.ensure((grn::VS_COUNT + 1) * sizeof(unsigned long long)));
+  GRN_CUDA(e->d_acc.ensure(grn::kAccSlots * sizeof(unsigned long long)));
   GRN_CUDA(e->d_parts.ensure(2 * grn::kVegasSumParts * sizeof(double)));
   if (e->nblocks == 0) e->nblocks = grn::vegas_grid_blocks(e->device);
   return vegas_alloc_calls(e, e->ncall);
@@ -823,8 +834,8 @@ static grn_status vegas_pass(grn_engine *e, int prec, int track_max, int refine,
                                   e->d_f.as<double>(), e->d_f2mat.as<double>(),
                                   e->d_acc.as<unsigned long long>(), e->d_lidx.as<int64_t>(),
                                   e->d_lx.as<double>(), e->d_lvw.as<double>(),
-                                  e->d_lbins.as<uint64_t>(), lbins_hi(e), rf, rd, e->nblocks,
-                                  e->stream));
+                                  e->d_lbins.as<uint64_t>(), lbins_hi(e), rf, rd,
+                                  e->d_rlist.as<int64_t>(), e->nblocks, e->stream));
   GRN_CUDA(cudaEventRecord(e->ev1, e->stream));
   GRN_CUDA(grn::launch_vegas_reduce(e->d_f.as<double>(), e->ncall,
                                     e->d_acc.as<unsigned long long>(), e->d_parts.as<double>(),
@@ -891,6 +902,7 @@ static grn_status vegas_accumulate(grn_engine *e, int mode, int64_t iter_index,
     out->vetocuts_ok   = e->veto_ok;
     out->iterations    = 1;
     out->nan_count     = e->nan_total;
+    out->refined       = static_cast<int64_t>(sc[grn::VS_REFINED]);
   }
   if (e->nan_total > 50)
     return fail(GRN_ERR_NAN, "more than 50 NaN/Inf weights: check model parameters and cuts");
@@ -1054,6 +1066,7 @@ grn_status grn_flat_integrate(grn_engine *e, const grn_flat_params *fp, grn_vega
     r.vetocuts_ok      = e->veto_ok;
     r.iterations       = it + 1;
     r.nan_count        = e->nan_total;
+    r.refined          = static_cast<int64_t>(sc[grn::VS_REFINED]);
     if (sigma > 0 && r.sigma_err / sigma < fp->precision && nev > fp->min_events) break;
   }
   if (out) *out = r;
@@ -1169,7 +1182,7 @@ grn_status batch_capture(grn_batch *b, int refine, int track_max) {
                          cudaMemcpyDeviceToDevice, b->stream);
     if (ce == cudaSuccess) ce = cudaMemsetAsync(e->d_f2mat.p, 0, nh * sizeof(double), b->stream);
     if (ce == cudaSuccess)
-      ce = cudaMemsetAsync(e->d_acc.p, 0, (grn::VS_COUNT + 1) * sizeof(unsigned long long),
+      ce = cudaMemsetAsync(e->d_acc.p, 0, grn::kAccSlots * sizeof(unsigned long long),
                            b->stream);
   }
   if (ce == cudaSuccess)
@@ -1193,7 +1206,7 @@ grn_status batch_capture(grn_batch *b, int refine, int track_max) {
                                 e->d_acc.as<unsigned long long>(), e->d_lidx.as<int64_t>(),
                                 e->d_lx.as<double>(), e->d_lvw.as<double>(),
                                 e->d_lbins.as<uint64_t>(), lbins_hi(e), nullptr, nullptr,
-                                e->nblocks,
+                                e->d_rlist.as<int64_t>(), e->nblocks,
                                 two ? b->side : b->stream);
   }
   if (ce == cudaSuccess && two) ce = cudaEventRecord(b->join, b->side);
@@ -1383,16 +1396,18 @@ grn_status grn_get_tuning(grn_engine *e, grn_tuning *t) {
   t->loop_pair     = e->loop_pair;
   t->vegas_blocks  = e->nblocks;
   t->weight_blocks = e->loop_blocks;
-  t->_pad          = 0;
+  t->fp64_refine   = e->fp64_refine;
   return GRN_OK;
 }
 
 grn_status grn_set_tuning(grn_engine *e, const grn_tuning *t) {
   if (!e || !t) return fail(GRN_ERR_INVALID, "null argument");
   if ((t->loop_pair != 0 && t->loop_pair != 1) || t->vegas_blocks < 1 || t->weight_blocks < 1 ||
-      t->vegas_blocks > (1 << 20) || t->weight_blocks > (1 << 20))
+      t->vegas_blocks > (1 << 20) || t->weight_blocks > (1 << 20) ||
+      (t->fp64_refine != 0 && t->fp64_refine != 1))
     return fail(GRN_ERR_INVALID, "bad tuning");
   e->loop_pair   = t->loop_pair;
+  e->fp64_refine = t->fp64_refine;
   e->nblocks     = t->vegas_blocks;
   e->loop_blocks = t->weight_blocks;
   return GRN_OK;
@@ -1413,7 +1428,7 @@ grn_status grn_autotune(grn_engine *e, int64_t sample, grn_tune_result *out) {
   GRN_CUDA(e->d_w.ensure(static_cast<size_t>(n) * sizeof(double)));
   GRN_CUDA(e->d_flags.ensure(static_cast<size_t>(n)));
   GRN_CUDA(e->d_wlist.ensure(static_cast<size_t>(n) * sizeof(int64_t)));
-  GRN_CUDA(e->d_wcount.ensure(sizeof(unsigned long long)));
+  GRN_CUDA(e->d_wcount.ensure(2 * sizeof(unsigned long long)));
   GRN_CUDA(e->d_recf.ensure(static_cast<size_t>(n) * grn::kLoopEventFields * sizeof(float)));
   GRN_CUDA(e->d_recd.ensure(static_cast<size_t>(n) * grn::kRecordDoubles * sizeof(double)));
   GRN_CUDA(grn::launch_uniforms(0x7E57ull, 0, 0, n, e->dim, e->d_u.as<double>(), e->stream));

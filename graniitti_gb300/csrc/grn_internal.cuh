@@ -21,7 +21,16 @@ struct KArgs {
   int           n_phi_nodes;
   double        loop_norm_re, loop_norm_im;  // i/(8 pi^2 s) * 9 h_phi h_kt / 64
   int           loop_pair;  // record-mode loop: 0 one event per thread, 1 two (packed FP32x2)
+  // FP32 generic loop: an event whose estimated relative weight error exceeds refine_tol is
+  // listed for the FP64 loop (0: never)
+  double        refine_tol;
 };
+
+// Error estimate of the FP32 generic loop: |error of the loop sum| ~ kRefineKappa u
+// sum_ij |U_i c_j| |A_ij| (u = 2^-24), calibrated on the tensor-pomeron structures, whose
+// phi-rings cancel by up to 10^12 at small forward pT.
+constexpr double kRefineKappa = 8.0;
+constexpr double kRefineTol   = 1e-5;
 
 constexpr int kMaxLoopNodes = 256;  // per axis
 constexpr int kMaxDim       = 16;   // hypercube dimensions: 8 (2-body), 14 (two-body cascades)
@@ -38,12 +47,18 @@ enum VegasScalar {
   VS_FID_OK,
   VS_VETO_OK,
   VS_NAN,
+  VS_REFINED,  // events of the FP32 loop recomputed in FP64
   VS_COUNT
 };
+// acc layout: the VegasScalar accumulators, then the screened work-list length
+// (acc[VS_COUNT]) and the length of the FP64 refinement list (acc[kAccRefine]).
+constexpr int kAccRefine = VS_COUNT + 1;
+constexpr int kAccSlots  = VS_COUNT + 2;
 
 // Launchers (all stream-ordered, return cudaGetLastError of the launch).
+// count: two counters (screened work list, FP64 refinement list rlist; both capacity n).
 cudaError_t launch_event_weights(const KArgs &a, int prec, const double *u, int64_t n, int dim,
-                                 double *w, uint8_t *flags, int64_t *list,
+                                 double *w, uint8_t *flags, int64_t *list, int64_t *rlist,
                                  unsigned long long *count, int loop_blocks, cudaStream_t st);
 int         loop_grid_blocks(int device);
 cudaError_t launch_event_kinematics(const KArgs &a, const double *u, int64_t n, int dim,
@@ -63,8 +78,8 @@ cudaError_t launch_eikonal_xs(const double *mbt, int n_bt, double *xs, cudaStrea
 // VEGAS
 int         vegas_grid_blocks(int device);
 cudaError_t launch_vegas_grid_init(double *xmat, int bins, int dim, cudaStream_t st);
-// One VEGAS pass in two stages; acc holds VS_COUNT + 1 unsigned long long
-// accumulators (the last one is the work-list length); the list arrays have
+// One VEGAS pass in two stages; acc holds kAccSlots unsigned long long
+// accumulators (see kAccRefine); the list arrays have
 // capacity ncall (l_x: dim x ncall, dimension-major; l_bins_hi only for dim > 8).
 // rf/rd: loop records (record mode, see record_mode()); null for the point mode,
 // in which the mapped points l_x are stored and stage B recomputes the tree level.
@@ -76,11 +91,13 @@ cudaError_t launch_vegas_born(const KArgs &a, const double *xmat, int bins, int 
                               const float *flq = nullptr);
 // fu / flq: points drawn from the flow (dimension-major, leading dimension ncall) and
 // their log density; the VEGAS weight of a point is then vw(u) / q(u).
+// r_list (capacity ncall): slots of the FP32 generic loop whose error estimate exceeds
+// a.refine_tol, finished by an FP64 pass over them in the same call.
 cudaError_t launch_vegas_loop(const KArgs &a, int prec, int bins, int dim, int64_t ncall,
                               int track_max, double *f_out, double *f2mat, unsigned long long *acc,
                               const int64_t *l_idx, const double *l_x, const double *l_vw,
                               const uint64_t *l_bins, const uint64_t *l_bins_hi, const float *rf,
-                              const double *rd, int nblocks, cudaStream_t st);
+                              const double *rd, int64_t *r_list, int nblocks, cudaStream_t st);
 // Record mode: screened, FP32 loop, single active trajectory.
 bool        record_mode(const KArgs &a, int prec);
 constexpr int kRecordDoubles = 4;

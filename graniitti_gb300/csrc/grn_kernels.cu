@@ -79,26 +79,33 @@ __device__ __forceinline__ void kahan_add(T &sum, T &comp, T x) {
 // (MProcess::S3ScreenedAmp2, src/MProcess.cc:157-261; Simpson38Integral2D,
 // include/Graniitti/MMath.h:457-472). The kt-node factor c_j = V_j kt_j A_eik(kt_j^2)
 // is shared by all events and precomputed.
+// For T = float, *mag receives sum_ij |U_i c_j| (|Re A_ij| + |Im A_ij|), the scale of the
+// rounding error of the sum (the phi-ring sums can be many orders of magnitude smaller than
+// their terms).
 template <typename T>
 __device__ cx<double> loop_integral(const KArgs &A, const Born &b, const KtNode<T> *skt,
-                                    const PhiNode<T> *sphi) {
+                                    const PhiNode<T> *sphi, double *mag = nullptr) {
+  constexpr bool kMag = sizeof(T) == sizeof(float);
   LoopEvent<T> e;
   make_loop_event<T>(A.K, b, e);
-  T ar = T(0), ai = T(0), cr = T(0), ci = T(0);
+  T ar = T(0), ai = T(0), cr = T(0), ci = T(0), m = T(0);
   for (int j = 0; j < A.n_kt_nodes; ++j) {
     const KtNode<T> nj = skt[j];
-    T ir = T(0), ii = T(0), dr = T(0), di = T(0);
+    T ir = T(0), ii = T(0), dr = T(0), di = T(0), ab = T(0);
     for (int i = 0; i < A.n_phi_nodes; ++i) {
       const PhiNode<T> ni = sphi[i];
       cx<T> a;
       if (loop_point_amp<T>(A.P, A.K, e, nj.kt * ni.c, nj.kt * ni.s, a)) {
         kahan_add(ir, dr, ni.u * a.re);
         kahan_add(ii, di, ni.u * a.im);
+        if constexpr (kMag) ab += ni.u * (fabs(a.re) + fabs(a.im));
       }
     }
     kahan_add(ar, cr, nj.cre * ir - nj.cim * ii);
     kahan_add(ai, ci, nj.cre * ii + nj.cim * ir);
+    if constexpr (kMag) m += sqrt(nj.cre * nj.cre + nj.cim * nj.cim) * ab;
   }
+  if (mag) *mag = double(m);
   const double sr = double(ar), si = double(ai);
   return {A.loop_norm_re * sr - A.loop_norm_im * si, A.loop_norm_re * si + A.loop_norm_im * sr};
 }
@@ -133,7 +140,9 @@ __device__ cx<double> loop_integral_fast(const KArgs &A, const Born &b, const Kt
 // per point so that only the nine compensated sums stay live.
 template <typename T>
 __device__ double screened_amp2_vv(const KArgs &A, const Born &b, const KtNode<T> *skt,
-                                   const PhiNode<T> *sphi) {
+                                   const PhiNode<T> *sphi, double *mag = nullptr) {
+  constexpr bool kMag = sizeof(T) == sizeof(float);
+  T m = T(0);
   cx<double> A0[9];
   born_amps_2xv(A.P, A.K, b, A0);
   LoopEvent<T> e;
@@ -154,13 +163,17 @@ __device__ double screened_amp2_vv(const KArgs &A, const Born &b, const KtNode<T
       cx<T> a[9];
       tensor_me4_2xv<T>(A.P, A.K, kk, s34, e3, e4, a);
       const T wr = ni.u * nj.cre, wi = ni.u * nj.cim;
+      T ab = T(0);
 #pragma unroll
       for (int h = 0; h < 9; ++h) {
         kahan_add(sr[h], cr[h], wr * a[h].re - wi * a[h].im);
         kahan_add(si[h], ci[h], wr * a[h].im + wi * a[h].re);
+        if constexpr (kMag) ab += fabs(a[h].re) + fabs(a[h].im);
       }
+      if constexpr (kMag) m += sqrt(wr * wr + wi * wi) * ab;
     }
   }
+  if (mag) *mag = double(m);
   double amp2 = 0.0;
 #pragma unroll
   for (int h = 0; h < 9; ++h) {
@@ -172,14 +185,19 @@ __device__ double screened_amp2_vv(const KArgs &A, const Born &b, const KtNode<T
   return amp2;
 }
 
+// *mag: see loop_integral (0 from the single-trajectory Regge loop, whose increment form
+// keeps every FP32 operand O(1) and whose rings do not cancel).
 template <typename T>
 __device__ __forceinline__ cx<double> loop_dispatch(const KArgs &A, const Born &b,
-                                                    const KtNode<T> *skt, const PhiNode<T> *sphi) {
+                                                    const KtNode<T> *skt, const PhiNode<T> *sphi,
+                                                    double *mag) {
   if constexpr (sizeof(T) == sizeof(float)) {
-    if (A.K.n_active == 1 && A.P.process == GRN_PROC_REGGE_CON)
+    if (A.K.n_active == 1 && A.P.process == GRN_PROC_REGGE_CON) {
+      *mag = 0.0;
       return loop_integral_fast(A, b, skt, sphi);
+    }
   }
-  return loop_integral<T>(A, b, skt, sphi);
+  return loop_integral<T>(A, b, skt, sphi, mag);
 }
 
 // Loop records: stage A writes, per screened event that passed the cuts, the
@@ -327,19 +345,30 @@ __device__ __forceinline__ bool born_stage(const KArgs &A, const double *x, Born
 
 // Screened weight of an event that passed the cuts (MContinuum::EventWeight with
 // MProcess::S3ScreenedAmp2, src/MContinuum.cc:164-193, src/MProcess.cc:157-288).
+// With T = float and refine non-null, *refine tells whether the estimated relative error
+// of W, 2 kRefineKappa u |norm| mag / |A0 + A_loop| (for vector pairs with sqrt(sum |A_h|^2)),
+// exceeds A.refine_tol (or is not finite): the caller then recomputes the event in FP64.
 template <typename T, bool CASC>
 __device__ double screened_weight(const KArgs &A, const double *x, uint8_t &flags,
-                                  const KtNode<T> *skt, const PhiNode<T> *sphi) {
+                                  const KtNode<T> *skt, const PhiNode<T> *sphi,
+                                  bool *refine = nullptr) {
   Born b;
   born_kinematics<CASC>(A.P, A.K, x, b);
-  double amp2;
+  double amp2, mag = 0.0;
   if (CASC && is_vector_pair(A.P)) {
-    amp2 = screened_amp2_vv<T>(A, b, skt, sphi);
+    amp2 = screened_amp2_vv<T>(A, b, skt, sphi, &mag);
   } else {
     const cx<double> A0 = born_amp(A.P, A.K, b);
-    const cx<double> Al = loop_dispatch<T>(A, b, skt, sphi);
+    const cx<double> Al = loop_dispatch<T>(A, b, skt, sphi, &mag);
     const double re = A0.re + Al.re, im = A0.im + Al.im;
     amp2 = re * re + im * im;
+  }
+  if constexpr (sizeof(T) == sizeof(float)) {
+    if (refine) {
+      const double norm = sqrt(A.loop_norm_re * A.loop_norm_re + A.loop_norm_im * A.loop_norm_im);
+      const double est  = 2.0 * kRefineKappa * 0x1p-24 * norm * mag;
+      *refine = A.refine_tol > 0.0 && !(est <= A.refine_tol * sqrt(amp2));
+    }
   }
   double W = weight_jacobian(A.K, b) * amp2;
   flags = GRN_FLAG_KINEMATICS_OK | GRN_FLAG_FIDCUTS_OK | GRN_FLAG_VETOCUTS_OK |
@@ -401,11 +430,14 @@ __global__ void __launch_bounds__(kWeightThreads)
 }
 
 // Stage B: the kt-loop for the listed events (every lane does a full loop).
+// FP32 (rlist non-null): events whose error estimate exceeds A.refine_tol are appended to
+// rlist (length rcount) for the FP64 instantiation, which then runs with list = rlist.
 template <typename T, int MAXD>
 __global__ void __launch_bounds__(kWeightThreads)
     k_weights_loop(const KArgs A, const double *__restrict__ u, int dim,
                    const int64_t *__restrict__ list, const unsigned long long *__restrict__ count,
-                   double *__restrict__ w, uint8_t *__restrict__ flags) {
+                   double *__restrict__ w, uint8_t *__restrict__ flags,
+                   int64_t *__restrict__ rlist, unsigned long long *__restrict__ rcount) {
   __shared__ KtNode<T>  skt[kMaxLoopNodes];
   __shared__ PhiNode<T> sphi[kMaxLoopNodes];
   stage_nodes<T>(A, skt, sphi);
@@ -418,8 +450,13 @@ __global__ void __launch_bounds__(kWeightThreads)
 #pragma unroll
     for (int d = 0; d < MAXD; ++d) x[d] = d < dim ? u[i * dim + d] : 0.0;
     uint8_t f;
-    w[i] = screened_weight<T, (MAXD > 8)>(A, x, f, skt, sphi);
+    bool    redo = false;
+    w[i] = screened_weight<T, (MAXD > 8)>(A, x, f, skt, sphi, rlist ? &redo : nullptr);
     if (flags) flags[i] = f;
+    if (rlist) {
+      const int64_t slot = list_append(redo, rcount);
+      if (redo) rlist[slot] = i;
+    }
   }
 }
 
@@ -432,10 +469,11 @@ int loop_grid_blocks(int device) {
 }
 
 cudaError_t launch_event_weights(const KArgs &a, int prec, const double *u, int64_t n, int dim,
-                                 double *w, uint8_t *flags, int64_t *list,
+                                 double *w, uint8_t *flags, int64_t *list, int64_t *rlist,
                                  unsigned long long *count, int loop_blocks, cudaStream_t st) {
   if (n <= 0) return cudaSuccess;
-  cudaMemsetAsync(count, 0, sizeof(unsigned long long), st);
+  cudaMemsetAsync(count, 0, 2 * sizeof(unsigned long long), st);
+  int64_t *rl = (prec == GRN_PREC_MIXED && a.refine_tol > 0.0) ? rlist : nullptr;
   const unsigned blocks = static_cast<unsigned>((n + kWeightThreads - 1) / kWeightThreads);
   if (dim <= 8)
     k_weights_born<8><<<blocks, kWeightThreads, 0, st>>>(a, u, n, dim, w, flags, list, count);
@@ -445,18 +483,18 @@ cudaError_t launch_event_weights(const KArgs &a, int prec, const double *u, int6
   if (a.P.screening) {
     if (dim <= 8) {
       if (prec == GRN_PREC_MIXED)
-        k_weights_loop<float, 8><<<loop_blocks, kWeightThreads, 0, st>>>(a, u, dim, list, count,
-                                                                         w, flags);
-      else
-        k_weights_loop<double, 8><<<loop_blocks, kWeightThreads, 0, st>>>(a, u, dim, list,
-                                                                          count, w, flags);
+        k_weights_loop<float, 8><<<loop_blocks, kWeightThreads, 0, st>>>(
+            a, u, dim, list, count, w, flags, rl, count + 1);
+      if (prec != GRN_PREC_MIXED || rl)
+        k_weights_loop<double, 8><<<loop_blocks, kWeightThreads, 0, st>>>(
+            a, u, dim, rl ? rl : list, rl ? count + 1 : count, w, flags, nullptr, nullptr);
     } else {
       if (prec == GRN_PREC_MIXED)
         k_weights_loop<float, kMaxDim><<<loop_blocks, kWeightThreads, 0, st>>>(
-            a, u, dim, list, count, w, flags);
-      else
+            a, u, dim, list, count, w, flags, rl, count + 1);
+      if (prec != GRN_PREC_MIXED || rl)
         k_weights_loop<double, kMaxDim><<<loop_blocks, kWeightThreads, 0, st>>>(
-            a, u, dim, list, count, w, flags);
+            a, u, dim, rl ? rl : list, rl ? count + 1 : count, w, flags, nullptr, nullptr);
     }
   }
   return cudaGetLastError();
@@ -1008,14 +1046,17 @@ __global__ void __launch_bounds__(kVegasThreads)
                        gridDim.x);
 }
 
-// Stage B of a VEGAS pass: screened weights of the listed events.
+// Stage B of a VEGAS pass: screened weights of the listed events. FP32 with r_list: the
+// slots whose error estimate exceeds A.refine_tol go to r_list (length acc[kAccRefine]) and
+// are left to the FP64 instantiation, which then runs over the slots of sel = r_list.
 template <typename T, int MAXD>
 __global__ void __launch_bounds__(kVegasThreads)
     k_vegas_loop(const KArgs A, int bins, int dim, int track_max, double *__restrict__ f_out,
                  double *__restrict__ f2mat, unsigned long long *__restrict__ acc,
                  const int64_t *__restrict__ l_idx, const double *__restrict__ l_x,
                  const double *__restrict__ l_vw, const uint64_t *__restrict__ l_bins,
-                 const uint64_t *__restrict__ l_bins_hi, int64_t cap) {
+                 const uint64_t *__restrict__ l_bins_hi, int64_t cap, int64_t *__restrict__ r_list,
+                 const int64_t *__restrict__ sel) {
   extern __shared__ double dsm[];
   double *sf2 = dsm;
   __shared__ KtNode<T>  skt[kMaxLoopNodes];
@@ -1026,14 +1067,23 @@ __global__ void __launch_bounds__(kVegasThreads)
   __syncthreads();
   unsigned long long cnt[VS_COUNT] = {};
   double maxf = 0.0, maxW = 0.0;
-  const int64_t n      = min(static_cast<int64_t>(acc[VS_COUNT]), cap);
+  const int64_t n = min(static_cast<int64_t>(acc[sel ? kAccRefine : VS_COUNT]), cap);
   const int64_t stride = static_cast<int64_t>(gridDim.x) * blockDim.x;
-  for (int64_t r = static_cast<int64_t>(blockIdx.x) * blockDim.x + threadIdx.x; r < n;
-       r += stride) {
+  for (int64_t q = static_cast<int64_t>(blockIdx.x) * blockDim.x + threadIdx.x; q < n;
+       q += stride) {
+    const int64_t r = sel ? sel[q] : q;
     double x[MAXD];
     for (int j = 0; j < MAXD; ++j) x[j] = j < dim ? l_x[static_cast<int64_t>(j) * cap + r] : 0.0;
     uint8_t      fl;
-    const double W = screened_weight<T, (MAXD > 8)>(A, x, fl, skt, sphi);
+    bool         redo = false;
+    const double W = screened_weight<T, (MAXD > 8)>(A, x, fl, skt, sphi, r_list ? &redo : nullptr);
+    if (r_list) {
+      const int64_t slot = list_append(redo, &acc[kAccRefine]);
+      if (redo) {
+        r_list[slot] = r;
+        continue;
+      }
+    }
     const double f = W * l_vw[r];
     f_out[l_idx[r]] = f;
     hist_add(sf2, dim, l_bins[r], l_bins_hi ? l_bins_hi[r] : 0ull, f * f);
@@ -1164,7 +1214,7 @@ cudaError_t launch_vegas_born(const KArgs &a, const double *xmat, int bins, int 
                               double *rd, cudaStream_t st, const float *fu, const float *flq) {
   const int nh = bins * dim;
   cudaMemsetAsync(f2mat, 0, nh * sizeof(double), st);
-  cudaMemsetAsync(acc, 0, (VS_COUNT + 1) * sizeof(unsigned long long), st);
+  cudaMemsetAsync(acc, 0, kAccSlots * sizeof(unsigned long long), st);
   int sms = 0, dev = 0;
   cudaGetDevice(&dev);
   cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
@@ -1185,7 +1235,7 @@ cudaError_t launch_vegas_loop(const KArgs &a, int prec, int bins, int dim, int64
                               int track_max, double *f_out, double *f2mat, unsigned long long *acc,
                               const int64_t *l_idx, const double *l_x, const double *l_vw,
                               const uint64_t *l_bins, const uint64_t *l_bins_hi, const float *rf,
-                              const double *rd, int nblocks, cudaStream_t st) {
+                              const double *rd, int64_t *r_list, int nblocks, cudaStream_t st) {
   if (!a.P.screening) return cudaSuccess;
   const int nh = bins * dim;
   if (rf) {
@@ -1200,20 +1250,26 @@ cudaError_t launch_vegas_loop(const KArgs &a, int prec, int bins, int dim, int64
     return cudaGetLastError();
   }
   const size_t sm = nh * sizeof(double);
+  int64_t     *rl = (prec == GRN_PREC_MIXED && a.refine_tol > 0.0) ? r_list : nullptr;
+  // MIXED: FP32 pass, then the FP64 pass over the refinement list (when refining)
   if (dim <= 8) {
     if (prec == GRN_PREC_MIXED)
       k_vegas_loop<float, 8><<<nblocks, kVegasThreads, sm, st>>>(
-          a, bins, dim, track_max, f_out, f2mat, acc, l_idx, l_x, l_vw, l_bins, l_bins_hi, ncall);
-    else
+          a, bins, dim, track_max, f_out, f2mat, acc, l_idx, l_x, l_vw, l_bins, l_bins_hi, ncall,
+          rl, nullptr);
+    if (prec != GRN_PREC_MIXED || rl)
       k_vegas_loop<double, 8><<<nblocks, kVegasThreads, sm, st>>>(
-          a, bins, dim, track_max, f_out, f2mat, acc, l_idx, l_x, l_vw, l_bins, l_bins_hi, ncall);
+          a, bins, dim, track_max, f_out, f2mat, acc, l_idx, l_x, l_vw, l_bins, l_bins_hi, ncall,
+          nullptr, rl);
   } else {
     if (prec == GRN_PREC_MIXED)
       k_vegas_loop<float, kMaxDim><<<nblocks, kVegasThreads, sm, st>>>(
-          a, bins, dim, track_max, f_out, f2mat, acc, l_idx, l_x, l_vw, l_bins, l_bins_hi, ncall);
-    else
+          a, bins, dim, track_max, f_out, f2mat, acc, l_idx, l_x, l_vw, l_bins, l_bins_hi, ncall,
+          rl, nullptr);
+    if (prec != GRN_PREC_MIXED || rl)
       k_vegas_loop<double, kMaxDim><<<nblocks, kVegasThreads, sm, st>>>(
-          a, bins, dim, track_max, f_out, f2mat, acc, l_idx, l_x, l_vw, l_bins, l_bins_hi, ncall);
+          a, bins, dim, track_max, f_out, f2mat, acc, l_idx, l_x, l_vw, l_bins, l_bins_hi, ncall,
+          nullptr, rl);
   }
   return cudaGetLastError();
 }
@@ -1424,6 +1480,7 @@ __global__ void k_vegas_finish(const double *__restrict__ part, int nparts,
   sc[VS_FID_OK]  = static_cast<double>(acc[VS_FID_OK]);
   sc[VS_VETO_OK] = static_cast<double>(acc[VS_VETO_OK]);
   sc[VS_NAN]     = static_cast<double>(acc[VS_NAN]);
+  sc[VS_REFINED] = static_cast<double>(acc[kAccRefine]);
 }
 
 cudaError_t launch_vegas_reduce(const double *f_out, int64_t ncall,

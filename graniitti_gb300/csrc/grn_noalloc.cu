@@ -9,9 +9,10 @@
 // middle of a run. grn_event_weights_noalloc serves them: its scratch is a fixed
 // file-scope device array of this library, so the call itself allocates nothing.
 //
-// Scratch layout: one 256-byte slot holding the work-list counter, then
-// GRN_NOALLOC_MAX_POINTS 64-bit point indices (8 MiB in total, resident on every
-// device that loads the library until the process exits).
+// Scratch layout: one 256-byte slot holding the counters of the screened work list and
+// of the FP64 refinement list, then GRN_NOALLOC_MAX_POINTS 64-bit point indices for each
+// list (16 MiB in total, resident on every device that loads the library until the
+// process exits).
 #include <cuda_runtime.h>
 
 #include <mutex>
@@ -22,8 +23,8 @@
 namespace {
 
 constexpr size_t kCounterSlot = 256;
-constexpr size_t kScratchBytes =
-    kCounterSlot + static_cast<size_t>(GRN_NOALLOC_MAX_POINTS) * sizeof(int64_t);
+constexpr size_t kListBytes = static_cast<size_t>(GRN_NOALLOC_MAX_POINTS) * sizeof(int64_t);
+constexpr size_t kScratchBytes = kCounterSlot + 2 * kListBytes;
 
 // The scratch itself. Device code may name it directly; host code only ever uses
 // the device address obtained from cudaGetSymbolAddress (the host-side symbol is
@@ -98,9 +99,11 @@ extern "C" grn_status grn_event_weights_noalloc(grn_engine *e, const double *u, 
                                          cudaGetErrorString(ce)).c_str());
   auto *count = static_cast<unsigned long long *>(base);
   auto *list  = reinterpret_cast<int64_t *>(static_cast<unsigned char *>(base) + kCounterSlot);
-  // launch_event_weights clears the counter (cudaMemsetAsync) before stage A.
-  ce = grn::launch_event_weights(args, prec, u, n, dim, w_out, flags, list, count, loop_blocks,
-                                 stream);
+  auto *rlist = reinterpret_cast<int64_t *>(static_cast<unsigned char *>(base) + kCounterSlot +
+                                            kListBytes);
+  // launch_event_weights clears both counters (cudaMemsetAsync) before stage A.
+  ce = grn::launch_event_weights(args, prec, u, n, dim, w_out, flags, list, rlist, count,
+                                 loop_blocks, stream);
   if (ce != cudaSuccess) return grn::set_error(GRN_ERR_CUDA, cudaGetErrorString(ce));
   return GRN_OK;
 }

@@ -83,8 +83,10 @@ struct Consts {
   // contractions (tensor_me3)
   int    n_res;
   int    res_J[GRN_MAX_RESONANCES];
+  int    res_smask;         // J = 2 coupling structures in use (bit j: g_j != 0)
   double res_M2[GRN_MAX_RESONANCES], res_MW[GRN_MAX_RESONANCES];
   double res_c0[GRN_MAX_RESONANCES], res_c1[GRN_MAX_RESONANCES];
+  double res_g[GRN_MAX_RESONANCES][7];  // J = 2 couplings g_Tensor[0..6]
 };
 
 // sin(pi x), cos(pi x) without rounding pi x first.
@@ -254,19 +256,29 @@ GRN_HD cx<T> tensor_me4_2xs(const grn_process_params &P, const Consts &K, const 
 // (MProcess.cc:1533), gives per leg c(s_i,t_i) (-3i gPNN F1(t_i)) W_i with the traceless
 //   W_i = 2 P_i P_i - P_i^2 g / 2.
 // Contracted with traceless tensors the vertex structures collapse:
-//  J = 2, iG_PPT_00 (:1701-1731) with the tensor propagator iD_TMES (:2422-2446) and the
-//    decay vertex iG_f2psps (:2121-2137):
-//      A = -9 gPNN^2 g0 g_d C F^2 Delta tr(W1 W2 Pi),  Pi = kh kh + kh^2 ghat / 3,
-//      ghat = -g + X X / m^2, kh = ghat.(p3 - p4),
-//      tr(W1 W2 Pi) = 4 a Pi(P2,P1) - b2 Pi(P1,P1) - b1 Pi(P2,P2);
+//  J = 2, iG_PPT_total (:1646-1692) with the tensor propagator iD_TMES (:2422-2446) and the
+//    decay vertex iG_f2psps (:2121-2137): D = Delta (g_d / 2) F Pi, Pi = kh kh + kh^2 ghat / 3,
+//    ghat = -g + X X / m^2, kh = ghat.(p3 - p4), and
+//      A = -(9/2) gPNN^2 g_d C F^2 Delta sum_j g_j gamma_j
+//    over the seven coupling structures (iG_PPT_00, _12 modes 1 and 2, _03, _04, _05, _06):
+//      gamma_0 = 2 tr(W1 W2 Pi),  tr(W1 W2 Pi) = 4 a Pi(P2,P1) - b2 Pi(P1,P1) - b1 Pi(P2,P2),
+//      gamma_1 = -2 [4 a M(q1,P1;q2,P2) + 2 beta M(q1,P1;q2,P1) + 2 alpha M(q1,P2;q2,P2)
+//                    + 2 alpha beta Pi(q1,q2)],  alpha = -b1/2, beta = -b2/2,
+//      gamma_2 = -2 [q1.q2 tr(W1 W2 Pi) + q2 W1 W2 Pi q1 + q1 W2 W1 Pi q2 + tr(W1 W2) Pi(q1,q2)],
+//      gamma_3 = -2 Pi(W1 q2, W2 q1),  gamma_4 = -4 E' Pi(q1,q2),
+//      gamma_5 = Pi(W1 q2, q2) q1W2q1 + Pi(W2 q1, q1) q2W1q2,
+//      gamma_6 = -2 (q2W1q2)(q1W2q1) Pi(q1,q2),
+//    with M(a,b;c,d) = (a.c) Pi(b,d) - (a.d) Pi(b,c) - (b.c) Pi(a,d) + (b.d) Pi(a,c) the
+//    contraction of the bivectors a^b and c^d (its four products cancel at leading order in
+//    s: structure 1 is the difference of structures T2/T3 and T1/R R, (l,s) = (2,0) - (2,2));
 //  J = 0, iG_PPS_0 + iG_PPS_1 (:1536-1571) with iD_MES (:2383) and iG_f0ss (:2028):
-//      A = 18 gPNN^2 g_d C F^2 Delta [g0 (4 a^2 - b1 b2) + g1 (4 a E + 5/4 b1 b2 q1.q2)];
+//      A = 18 gPNN^2 g_d C F^2 Delta [g0 (4 a^2 - b1 b2) + g1 E'],  E' = 4 a E + 5/4 b1 b2 q1.q2;
 // C = c(s1,t1) c(s2,t2) F1(t1) F1(t2) FM(t1) FM(t2), FM(q^2) = 1/(1 - q^2), F = exp(-(m^2 -
 // M0^2)^2) (the production and the decay form factor), Delta = 1/(m^2 - M0^2 + i M0 W),
-// a = P1.P2, b_i = P_i^2 = 4 mp^2 - t_i, q_i = p_beam,i - p_i (P_i.q_i = 0), and
-// E = (P1.q2)(P2.q1) - a q1.q2 evaluated as the bivector contraction (P1^q1).(q2^P2),
-// which has no O(s^2) cancellation between its terms. The prefactors gPNN^2 g g_d per
-// resonance are Consts::res_c0 / res_c1.
+// a = P1.P2, b_i = P_i^2 = 4 mp^2 - t_i, q_i = p_beam,i - p_i (P_i.q_i = 0),
+// tr(W1 W2) = 4 a^2 - b1 b2, and E = (P1.q2)(P2.q1) - a q1.q2 = M-type bivector contraction of
+// P1^q1 and q2^P2 with the metric. The resonance prefactors are Consts::res_c0 (-(9/2) gPNN^2
+// g_d for J = 2; 18 gPNN^2 g_d g0 for J = 0), res_c1 (18 gPNN^2 g_d g1, J = 0), res_g.
 template <typename T>
 GRN_HD T lc_bivector_dot(T ap, T am, T ax, T ay, T bp, T bm, T bx, T by,   // B = a ^ b
                          T cp, T cm, T cx_, T cy, T dp, T dm, T dx, T dy) {  // C = c ^ d
@@ -280,17 +292,64 @@ GRN_HD T lc_bivector_dot(T ap, T am, T ax, T ay, T bp, T bm, T bx, T by,   // B 
          Bxy * Cxy;
 }
 
-// What depends on the central system only, which the kt-loop leaves unchanged, comes from
-// the tree-level point in FP64: the resonance sums R2 = sum_{J=2} c0 F^2 Delta,
-// R0 = sum_{J=0} c0 F^2 Delta, R1 = sum_{J=0} c1 F^2 Delta, and Pi(n-, n+) with the light-cone
-// vectors n+ = (+ 1, - 0, 0), n- = (+ 0, - 1, 0). With P1 = 2L n+ + d1, P2 = 2L n- + d2
-// (d1 = (-q1+, P1-, p1T), d2 = (P2+, -q2-, p2T), all O(1)) the leading part of
-// Pi(P2, P1) is 4 L^2 Pi(n-, n+): near the zero of the d-wave decay distribution it cancels
-// between terms 10^4 times larger than itself, which only the FP64 evaluation survives.
+// Pi_ab = Pi(e_a, e_b) on the light-cone basis e+, e-, ex, ey (v = v+ e+ + v- e- + vx ex +
+// vy ey), symmetric: ++ +- +x +y -- -x -y xx xy yy. It depends on the central system only,
+// which the kt-loop leaves unchanged, so it comes from the tree-level point in FP64 and every
+// Pi(v, w) of a loop point is a sum of products of accurate factors: with P1 ~ 2L e+ and
+// P2 ~ 2L e- the leading 4 L^2 Pi_+- of Pi(P2,P1) would otherwise cancel, near the zero of the
+// d-wave decay distribution, between terms 10^4 times larger than itself.
+template <typename T>
+struct PiMat {
+  T pp, pm, px, py, mm, mx, my, xx, xy, yy;
+};
+
+template <typename T>
+GRN_HD T pi_form(const PiMat<T> &M, T ap, T am, T ax, T ay, T bp, T bm, T bx, T by) {
+  return ap * bp * M.pp + (ap * bm + am * bp) * M.pm + (ap * bx + ax * bp) * M.px +
+         (ap * by + ay * bp) * M.py + am * bm * M.mm + (am * bx + ax * bm) * M.mx +
+         (am * by + ay * bm) * M.my + ax * bx * M.xx + (ax * by + ay * bx) * M.xy + ay * by * M.yy;
+}
+
+// M(a,b;c,d) = sum B^{mu nu} g_{mu rho} C^{rho sigma} Pi_{nu sigma}, B = a^b, C = c^d, metric
+// g_{+-} = 1/2, g_xx = g_yy = -1 on the light-cone basis.
+template <typename T>
+GRN_HD T pi_bivector(const PiMat<T> &M, const T a[4], const T b[4], const T c[4], const T d[4]) {
+  // components above the diagonal only: the diagonal is zero exactly (a contracted
+  // a[i] b[i] - a[i] b[i] would leave the rounding error of one product), below it antisymmetric
+  T B[4][4], C[4][4];
+#pragma unroll
+  for (int i = 0; i < 4; ++i) {
+    B[i][i] = C[i][i] = T(0);
+#pragma unroll
+    for (int j = i + 1; j < 4; ++j) {
+      B[i][j] = a[i] * b[j] - a[j] * b[i];
+      C[i][j] = c[i] * d[j] - c[j] * d[i];
+      B[j][i] = -B[i][j];
+      C[j][i] = -C[i][j];
+    }
+  }
+  const T Pi[4][4] = {{M.pp, M.pm, M.px, M.py},
+                      {M.pm, M.mm, M.mx, M.my},
+                      {M.px, M.mx, M.xx, M.xy},
+                      {M.py, M.my, M.xy, M.yy}};
+  T out = T(0);
+#pragma unroll
+  for (int nu = 0; nu < 4; ++nu)
+#pragma unroll
+    for (int sg = 0; sg < 4; ++sg) {
+      const T Y = T(0.5) * (B[0][nu] * C[1][sg] + B[1][nu] * C[0][sg]) - B[2][nu] * C[2][sg] -
+                  B[3][nu] * C[3][sg];
+      out += Y * Pi[nu][sg];
+    }
+  return out;
+}
+
+// Resonance sums of the tree-level central mass: Rs[j] = sum_{J=2} res_c0 g_j F^2 Delta,
+// R0 = sum_{J=0} res_c0 F^2 Delta, R1 = sum_{J=0} res_c1 F^2 Delta; and Pi on the basis.
 template <typename T>
 struct ResSums {
-  cx<T> R2, R0, R1;
-  T     pinn;  // Pi(n-, n+)
+  cx<T>    Rs[7], R0, R1;
+  PiMat<T> pi;
 };
 
 // Resonance-side vectors: X = p3 + p4, kh = ghat.(p3 - p4) and kh^2 (kh^2 = (p3 - p4)^2 -
@@ -316,21 +375,34 @@ GRN_HD ResVec<T> res_vectors(const Consts &K, T p3p, T p3m, T p3x, T p3y, T p4p,
   return v;
 }
 
+// Pi_ab = kappa_a kappa_b + kh^2/3 (xi_a xi_b / m^2 - g_ab) with kappa_a = kh.e_a,
+// xi_a = X.e_a (e+.v = v-/2, e-.v = v+/2, ex.v = -vx, ey.v = -vy).
+GRN_HD PiMat<double> pi_matrix(const ResVec<double> &v) {
+  const double k[4] = {0.5 * v.khm, 0.5 * v.khp, -v.khx, -v.khy};
+  const double x[4] = {0.5 * v.Xm, 0.5 * v.Xp, -v.Xx, -v.Xy};
+  const double t = v.kh2 / 3.0, im2 = 1.0 / v.m2;
+  auto e = [&](int i, int j, double g) { return k[i] * k[j] + t * (x[i] * x[j] * im2 - g); };
+  return {e(0, 0, 0.0), e(0, 1, 0.5), e(0, 2, 0.0), e(0, 3, 0.0), e(1, 1, 0.0),
+          e(1, 2, 0.0), e(1, 3, 0.0), e(2, 2, -1.0), e(2, 3, 0.0), e(3, 3, -1.0)};
+}
+
 GRN_HD ResSums<double> resonance_sums(const Consts &K, double m2, const ResVec<double> &v) {
-  ResSums<double> R{{0, 0}, {0, 0}, {0, 0}, 0};
+  ResSums<double> R;
+  for (int j = 0; j < 7; ++j) R.Rs[j] = {0, 0};
+  R.R0 = R.R1 = {0, 0};
   for (int r = 0; r < K.n_res; ++r) {
     const double dm = m2 - K.res_M2[r], mw = K.res_MW[r];
     const double f2 = exp(-2.0 * dm * dm) / (dm * dm + mw * mw);  // F^2 / |m^2 - M0^2 + i M0 W|^2
     const cx<double> D{dm * f2, -mw * f2};
     if (K.res_J[r] == 2) {
-      R.R2 = cadd(R.R2, cscale(D, K.res_c0[r]));
+      for (int j = 0; j < 7; ++j)
+        R.Rs[j] = cadd(R.Rs[j], cscale(D, K.res_c0[r] * K.res_g[r][j]));
     } else {
       R.R0 = cadd(R.R0, cscale(D, K.res_c0[r]));
       R.R1 = cadd(R.R1, cscale(D, K.res_c1[r]));
     }
   }
-  // Pi(n-, n+) = kh+ kh- / 4 + kh^2 / 3 (X+ X- / (4 m^2) - 1/2)
-  R.pinn = 0.25 * v.khp * v.khm + v.kh2 / 3.0 * (0.25 * v.Xp * v.Xm / v.m2 - 0.5);
+  R.pi = pi_matrix(v);
   return R;
 }
 
@@ -341,44 +413,75 @@ GRN_HD cx<T> tensor_me3(const grn_process_params &P, const Consts &K, const LCKi
   const T P1p = k.p1p + L, P1m = k.p1m + eps, P2p = k.p2p + eps, P2m = k.p2m + L;
   const T b1 = T(4) * k.mp2 - k.t1, b2 = T(4) * k.mp2 - k.t2;
   const T a  = lc_dot<T>(P1p, P1m, k.p1x, k.p1y, P2p, P2m, k.p2x, k.p2y);
-  // central system X = p3 + p4, its invariant mass and kh
-  const ResVec<T> v = res_vectors<T>(K, k.p3p, k.p3m, k.p3x, k.p3y, k.p4p, k.p4m, k.p4x, k.p4y);
-  const T Xp = v.Xp, Xm = v.Xm, Xx = v.Xx, Xy = v.Xy, m2 = v.m2;
+  const T Xp = k.p3p + k.p4p, Xm = k.p3m + k.p4m, Xx = k.p3x + k.p4x, Xy = k.p3y + k.p4y;
+  const T m2 = Xp * Xm - (Xx * Xx + Xy * Xy);
   const T s1 = k.mp2 + m2 + k.p1p * Xm + k.p1m * Xp - T(2) * (k.p1x * Xx + k.p1y * Xy);
   const T s2 = k.mp2 + m2 + k.p2p * Xm + k.p2m * Xp - T(2) * (k.p2x * Xx + k.p2y * Xy);
-  const cx<T> R2 = R.R2, R0 = R.R0, R1 = R.R1;
+  // P_i and q_i = p_beam,i - p_i = (q+, q-, -p_iT)
+  const T P1[4] = {P1p, P1m, k.p1x, k.p1y}, P2[4] = {P2p, P2m, k.p2x, k.p2y};
+  const T q1[4] = {k.q1p, k.q1m, -k.p1x, -k.p1y}, q2[4] = {k.q2p, k.q2m, -k.p2x, -k.p2y};
+  auto pif = [&](const T *u, const T *w) {
+    return pi_form<T>(R.pi, u[0], u[1], u[2], u[3], w[0], w[1], w[2], w[3]);
+  };
+  auto dot = [&](const T *u, const T *w) {
+    return lc_dot<T>(u[0], u[1], u[2], u[3], w[0], w[1], w[2], w[3]);
+  };
+  const int mask = K.res_smask;
   cx<T> G{T(0), T(0)};
-  if (R2.re != T(0) || R2.im != T(0)) {
-    const T khp = v.khp, khm = v.khm, khx = v.khx, khy = v.khy;
-    const T kv1 = lc_dot<T>(khp, khm, khx, khy, P1p, P1m, k.p1x, k.p1y);
-    const T kv2 = lc_dot<T>(khp, khm, khx, khy, P2p, P2m, k.p2x, k.p2y);
-    const T pv1 = lc_dot<T>(Xp, Xm, Xx, Xy, P1p, P1m, k.p1x, k.p1y);
-    const T pv2 = lc_dot<T>(Xp, Xm, Xx, Xy, P2p, P2m, k.p2x, k.p2y);
-    const T im2 = T(1) / m2, third = v.kh2 * T(1.0 / 3.0);
-    // Pi(P2, P1) = 4 L^2 Pi(n-, n+) + 2 L (Pi(n-, d1) + Pi(d2, n+)) + Pi(d2, d1)
-    const T d1p = -k.q1p, d1m = P1m, d2p = P2p, d2m = -k.q2m;
-    const T kd1 = lc_dot<T>(khp, khm, khx, khy, d1p, d1m, k.p1x, k.p1y);
-    const T kd2 = lc_dot<T>(khp, khm, khx, khy, d2p, d2m, k.p2x, k.p2y);
-    const T Xd1 = lc_dot<T>(Xp, Xm, Xx, Xy, d1p, d1m, k.p1x, k.p1y);
-    const T Xd2 = lc_dot<T>(Xp, Xm, Xx, Xy, d2p, d2m, k.p2x, k.p2y);
-    const T d12 = lc_dot<T>(d1p, d1m, k.p1x, k.p1y, d2p, d2m, k.p2x, k.p2y);
-    const T Pin1 = T(0.5) * khp * kd1 + third * T(0.5) * (Xp * Xd1 * im2 - d1p);
-    const T Pi2n = T(0.5) * khm * kd2 + third * T(0.5) * (Xm * Xd2 * im2 - d2m);
-    const T Pidd = kd2 * kd1 + third * (Xd2 * Xd1 * im2 - d12);
-    const T Pi21 = T(4) * L * L * R.pinn + T(2) * L * (Pin1 + Pi2n) + Pidd;
-    const T Pi11 = kv1 * kv1 + third * (pv1 * pv1 * im2 - b1);
-    const T Pi22 = kv2 * kv2 + third * (pv2 * pv2 * im2 - b2);
-    const T Tr   = T(4) * a * Pi21 - b2 * Pi11 - b1 * Pi22;
-    G = cscale(R2, Tr);
+  const bool j0 = R.R0.re != T(0) || R.R0.im != T(0) || R.R1.re != T(0) || R.R1.im != T(0);
+  T q1q2 = T(0), Ep = T(0);
+  if (j0 || (mask & 0x16)) {  // E' for J = 0 and structure 4; q1.q2 for structures 1, 2, 4
+    q1q2 = dot(q1, q2);
+    const T E = lc_bivector_dot<T>(P1p, P1m, k.p1x, k.p1y, q1[0], q1[1], q1[2], q1[3], q2[0],
+                                   q2[1], q2[2], q2[3], P2p, P2m, k.p2x, k.p2y);
+    Ep = T(4) * a * E + T(1.25) * b1 * b2 * q1q2;
   }
-  if (R0.re != T(0) || R0.im != T(0) || R1.re != T(0) || R1.im != T(0)) {
-    // q1 = (q1p, q1m, -p1T), q2 = (q2p, q2m, -p2T)
-    const T q1q2 = lc_dot<T>(k.q1p, k.q1m, -k.p1x, -k.p1y, k.q2p, k.q2m, -k.p2x, -k.p2y);
-    const T E    = lc_bivector_dot<T>(P1p, P1m, k.p1x, k.p1y, k.q1p, k.q1m, -k.p1x, -k.p1y,
-                                      k.q2p, k.q2m, -k.p2x, -k.p2y, P2p, P2m, k.p2x, k.p2y);
+  if (mask) {
+    const T Pi21 = pif(P2, P1), Pi11 = pif(P1, P1), Pi22 = pif(P2, P2);
+    const T Tr   = T(4) * a * Pi21 - b2 * Pi11 - b1 * Pi22;
+    G = cadd(G, cscale(R.Rs[0], T(2) * Tr));
+    if (mask & ~1) {
+      const T trW  = T(4) * a * a - b1 * b2;
+      const T P1q2 = dot(P1, q2), P2q1 = dot(P2, q1);
+      const T Pq12 = pif(q1, q2);
+      const T al = T(-0.5) * b1, be = T(-0.5) * b2;
+      if (mask & 2) {  // (l,s) = (2,0) - (2,2): bivector form
+        const T F1 = T(4) * a * pi_bivector<T>(R.pi, q1, P1, q2, P2) +
+                     T(2) * be * pi_bivector<T>(R.pi, q1, P1, q2, P1) +
+                     T(2) * al * pi_bivector<T>(R.pi, q1, P2, q2, P2) + T(2) * al * be * Pq12;
+        G = cadd(G, cscale(R.Rs[1], T(-2) * F1));
+      }
+      const T PP1q1 = pif(P1, q1), PP2q2 = pif(P2, q2);
+      if (mask & 4) {  // (l,s) = (2,0) + (2,2)
+        const T Pu1q1 = T(2) * P1q2 * PP1q1 - T(0.5) * b1 * Pq12;
+        const T Pu2q2 = T(2) * P2q1 * PP2q2 - T(0.5) * b2 * Pq12;
+        const T c12   = T(4) * a * P1q2 * pif(P2, q1) - T(0.5) * b2 * Pu1q1;
+        const T c21   = T(4) * a * P2q1 * pif(P1, q2) - T(0.5) * b1 * Pu2q2;
+        G = cadd(G, cscale(R.Rs[2], T(-2) * (q1q2 * Tr + c12 + c21 + trW * Pq12)));
+      }
+      if (mask & 8) {  // (l,s) = (2,4): Pi(W1 q2, W2 q1)
+        const T Pu1u2 = T(4) * P1q2 * P2q1 * Pi21 - b2 * P1q2 * PP1q1 - b1 * P2q1 * PP2q2 +
+                        T(0.25) * b1 * b2 * Pq12;
+        G = cadd(G, cscale(R.Rs[3], T(-2) * Pu1u2));
+      }
+      if (mask & 16)  // (l,s) = (4,2)
+        G = cadd(G, cscale(R.Rs[4], T(-4) * Ep * Pq12));
+      if (mask & 0x60) {
+        const T X1 = T(2) * P1q2 * P1q2 - T(0.5) * b1 * k.t2;  // q2 W1 q2
+        const T X2 = T(2) * P2q1 * P2q1 - T(0.5) * b2 * k.t1;  // q1 W2 q1
+        if (mask & 32) {  // (l,s) = (4,4)
+          const T Pu1q2 = T(2) * P1q2 * pif(P1, q2) - T(0.5) * b1 * pif(q2, q2);
+          const T Pu2q1 = T(2) * P2q1 * pif(P2, q1) - T(0.5) * b2 * pif(q1, q1);
+          G = cadd(G, cscale(R.Rs[5], Pu1q2 * X2 + Pu2q1 * X1));
+        }
+        if (mask & 64)  // (l,s) = (6,4)
+          G = cadd(G, cscale(R.Rs[6], T(-2) * X1 * X2 * Pq12));
+      }
+    }
+  }
+  if (j0) {
     const T S0 = T(4) * a * a - b1 * b2;
-    const T S1 = T(4) * a * E + T(1.25) * b1 * b2 * q1q2;
-    G = cadd(G, cadd(cscale(R0, S0), cscale(R1, S1)));
+    G = cadd(G, cadd(cscale(R.R0, S0), cscale(R.R1, Ep)));
   }
   // C = c(s1,t1) c(s2,t2) F1 F1 FM FM with c(s,t) = (s ap)^x e^{-i pi x/2} / (4s), x = alpha(t)-1
   const grn_tensor_params &tp = P.tensor;
@@ -1222,10 +1325,13 @@ GRN_HD void make_loop_event(const Consts &K, const Born &b, LoopEvent<T> &e) {
     const ResVec<double> v =
         res_vectors<double>(K, b.p3p, b.p3m, b.p3x, b.p3y, b.p4p, b.p4m, b.p4x, b.p4y);
     const ResSums<double> R = resonance_sums(K, b.m2, v);
-    e.res = {{T(R.R2.re), T(R.R2.im)}, {T(R.R0.re), T(R.R0.im)}, {T(R.R1.re), T(R.R1.im)},
-             T(R.pinn)};
+    for (int j = 0; j < 7; ++j) e.res.Rs[j] = {T(R.Rs[j].re), T(R.Rs[j].im)};
+    e.res.R0 = {T(R.R0.re), T(R.R0.im)};
+    e.res.R1 = {T(R.R1.re), T(R.R1.im)};
+    e.res.pi = {T(R.pi.pp), T(R.pi.pm), T(R.pi.px), T(R.pi.py), T(R.pi.mm),
+                T(R.pi.mx), T(R.pi.my), T(R.pi.xx), T(R.pi.xy), T(R.pi.yy)};
   } else {
-    e.res = {{T(0), T(0)}, {T(0), T(0)}, {T(0), T(0)}, T(0)};
+    e.res = ResSums<T>{};
   }
 }
 

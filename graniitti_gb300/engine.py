@@ -142,8 +142,11 @@ class Engine:
         _abi.check(self.lib.grn_get_tuning(self.h, ctypes.byref(t)))
         return t
 
-    def set_tuning(self, loop_pair=None, vegas_blocks=None, weight_blocks=None):
+    def set_tuning(self, loop_pair=None, vegas_blocks=None, weight_blocks=None,
+                   fp64_refine=None):
         t = self.tuning()
+        if fp64_refine is not None:
+            t.fp64_refine = int(fp64_refine)
         if loop_pair is not None:
             t.loop_pair = loop_pair
         if vegas_blocks is not None:

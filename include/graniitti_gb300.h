@@ -238,8 +238,8 @@ grn_status grn_event_weights(grn_engine *e, const double *u, int64_t n, int32_t 
  * application whose device memory belongs to its own pool allocator, a service that
  * sizes its memory once at start-up and must not meet an out-of-memory error or the
  * synchronisation of cudaFree mid-run), this call allocates nothing: its scratch
- * (the screened work list) is a fixed 8 MiB array inside the library, held by every
- * device that loads the library until the process exits.
+ * (the screened work list and its FP64 refinement list) is a fixed 16 MiB array inside
+ * the library, held by every device that loads the library until the process exits.
  *   - u, w_out and flags must be device pointers; n <= GRN_NOALLOC_MAX_POINTS,
  *     larger batches are rejected with GRN_ERR_INVALID.
  *   - Stream-ordered on the engine's stream; returns without synchronising.
@@ -299,6 +299,8 @@ typedef struct grn_vegas_result {
   double  amplitude_ok, kinematics_ok, fidcuts_ok, vetocuts_ok; /* pass counts */
   int64_t iterations;              /* iterations run in this call */
   int64_t nan_count;               /* NaN/Inf weights zeroed */
+  int64_t refined;                 /* events of the last pass whose FP32 kt-loop was redone
+                                      in FP64 (error estimate above tolerance, see grn_tuning) */
 } grn_vegas_result;
 
 /* VEGASData::Init (MVEGAS.h:38-56) with init = 0 (fresh uniform grid). */
@@ -517,12 +519,17 @@ grn_status grn_batch_iteration(grn_batch *b, int32_t mode, int32_t refine, uint3
 /* ------------------------------------------------------------------------ */
 /* The kt-loop stage in record mode (screened, GRN_PREC_MIXED, one trajectory) has two
  * kernels: one event per thread, or two events per thread on the packed FP32x2
- * arithmetic (same results up to FP32 rounding), each with a grid size. */
+ * arithmetic (same results up to FP32 rounding), each with a grid size.
+ * fp64_refine (default 1): with GRN_PREC_MIXED, the FP32 generic kt-loop (tensor pomeron,
+ * resonances, vector pairs, several Regge trajectories) also sums |U_i c_j| |A_ij| over
+ * its points; an event whose estimated relative weight error 16 2^-24 |norm| sum / |A| is
+ * above 1e-5 is recomputed with the FP64 loop in a second pass of the same call (the phi
+ * integrals of some tensor couplings cancel by up to 10^12). 0 keeps every FP32 weight. */
 typedef struct grn_tuning {
   int32_t loop_pair;     /* 0 one event per thread, 1 two events per thread */
   int32_t vegas_blocks;  /* grid of the loop stage of VEGAS and flow passes */
   int32_t weight_blocks; /* grid of the loop stage of grn_event_weights */
-  int32_t _pad;
+  int32_t fp64_refine;   /* 1 recompute badly conditioned FP32-loop events in FP64, 0 never */
 } grn_tuning;
 grn_status grn_get_tuning(grn_engine *e, grn_tuning *t);
 grn_status grn_set_tuning(grn_engine *e, const grn_tuning *t);

@@ -82,6 +82,24 @@ def resonance_fixtures():
         u = philox_np.uniforms(seed, n, 8)
         r = run_weights(card, u, extra, proc=proc, dim=dim)
         save(name, seed=seed, u=u, card=os.path.basename(card), proc=proc, **r)
+    # The J = 2 coupling structures one at a time (g_j = 1, the others 0), and TUNE0's
+    # f2(1525) (structure 1), at forward pT >= 0.05 GeV (u[0], u[1] >= 0.86): structures 1 and
+    # 4 vanish as the forward pT go to zero, and the reference's Cartesian contractions leave
+    # only rounding noise there.
+    for j in range(1, 7):
+        g = ", ".join("g%d:%s" % (i, "1.0" if i == j else "0.0") for i in range(7))
+        proc = "PP[RESTENSOR]<F> -> pi+ pi- @RES{f2_1270:1} @R[f2_1270]{%s}" % g
+        u = philox_np.uniforms(70 + j, 256, 8)
+        u[:, :2] = 0.86 + 0.14 * u[:, :2]
+        r = run_weights(CARD_RES, u, REPLAY_F, proc=proc, dim=6)
+        save("rf_s%d_tree_weights.npz" % j, seed=70 + j, u=u, card=os.path.basename(CARD_RES),
+             proc=proc, **r)
+    proc = "PP[RESTENSOR]<F> -> pi+ pi- @RES{f2_1525:1, f2_1270:1}"
+    u = philox_np.uniforms(77, 256, 8)
+    u[:, :2] = 0.86 + 0.14 * u[:, :2]
+    r = run_weights(CARD_RES, u, REPLAY_F, proc=proc, dim=6)
+    save("rf_f2_1525_tree_weights.npz", seed=77, u=u, card=os.path.basename(CARD_RES), proc=proc,
+         **r)
     proc = "PP[RESTENSOR]<F> -> pi+ pi- @RES{f0_980:1, f2_1270:1}"
     u = philox_np.uniforms(65, 96, 8)
     r = run_weights(CARD_RES_SCR, u, REPLAY_F + ["--nbt", "1024", "--nkt2", "10000"], proc=proc,

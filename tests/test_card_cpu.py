@@ -85,7 +85,6 @@ def test_resonance_params_and_decay_couplings(lib_built):
 
 
 @pytest.mark.parametrize("proc", [
-    "PP[RESTENSOR]<F> -> pi+ pi- @RES{f2_1525:1}",       # coupling structure g1 (J = 2)
     "PP[RESTENSOR]<F> -> pi+ pi- @RES{rho_770:1}",       # no pseudoscalar-pair resonance
     "PP[RESTENSOR]<F> -> pi0 pi0 @RES{f2_1270:1}",
     "PP[RESTENSOR]<F> -> pi+ pi- @RES{f0_500:1, f0_980:1, f0_1500:1, f0_1710:1, f2_1270:1}"])

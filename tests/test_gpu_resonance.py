@@ -42,7 +42,9 @@ def _rel(w, wr):
 
 
 @pytest.mark.parametrize("name", ["rf_tree_weights.npz", "rf_mix_tree_weights.npz",
-                                  "rf_kk_tree_weights.npz", "rc_tree_weights.npz"])
+                                  "rf_kk_tree_weights.npz", "rc_tree_weights.npz",
+                                  "rf_f2_1525_tree_weights.npz"] +
+                         ["rf_s%d_tree_weights.npz" % j for j in range(1, 7)])
 def test_resonance_tree_vs_reference(gpu, name):
     import graniitti_gb300 as g
     gl = _load(name)
@@ -148,7 +150,93 @@ def test_resonance_parameter_validation(gpu):
     assert status(lambda Q: None) == _abi.GRN_OK
     assert status(lambda Q: setattr(Q, "n_res", 0)) == _abi.GRN_ERR_INVALID
     assert status(lambda Q: setattr(Q, "n_res", 5)) == _abi.GRN_ERR_INVALID
-    assert status(lambda Q: Q.res[0].g_tensor.__setitem__(1, 0.5)) == _abi.GRN_ERR_UNSUPPORTED
+    assert status(lambda Q: Q.res[0].g_tensor.__setitem__(1, 0.5)) == _abi.GRN_OK
+    assert status(lambda Q: (setattr(Q.res[0], "J", 0), Q.res[0].g_tensor.__setitem__(2, 0.5))) \
+        == _abi.GRN_ERR_UNSUPPORTED
     assert status(lambda Q: setattr(Q.res[0], "J", 1)) == _abi.GRN_ERR_UNSUPPORTED
     assert status(lambda Q: setattr(Q.res[0], "M", -1.0)) == _abi.GRN_ERR_INVALID
     assert status(lambda Q: Q.m_central.__setitem__(1, 0.2)) == _abi.GRN_ERR_UNSUPPORTED
+
+
+@pytest.mark.parametrize("g", ["g0:0, g1:1", "g0:0, g2:1", "g0:0, g3:1", "g0:0, g4:1",
+                               "g0:0, g5:1", "g0:0, g6:1", "g0:2, g1:1, g4:0.5"])
+def test_tensor_structures_mixed_loop_vs_fp64(gpu, g):
+    """FP32 kt-loop of each J = 2 coupling structure against the FP64 loop, 4096 points
+    (events whose FP32 error estimate exceeds 1e-5 are redone in FP64)."""
+    import graniitti_gb300 as gg
+    import philox_np
+    from graniitti_gb300 import card
+    c = card.read_card(os.path.join(GOLDEN, "cards", "pp_res_pipi_screened.json"))
+    P = card.build_params(c, "PP[RESTENSOR]<F> -> pi+ pi- @R[f2_1270]{%s}" % g)
+    e = _engine(P)
+    e.eikonal_build()
+    u = philox_np.uniforms(67, 4096, 8)
+    w64, fl = e.event_weights(u, prec=gg.FP64)
+    wm, flm = e.event_weights(u, prec=gg.MIXED)
+    assert np.array_equal(fl, flm)
+    Pb = type(P)()
+    ctypes.memmove(ctypes.byref(Pb), ctypes.byref(P), ctypes.sizeof(P))
+    Pb.screening = 0
+    wb, _ = _engine(Pb).event_weights(u, prec=gg.FP64)
+    ok, rel = _mixed_ok(wm, w64, wb)
+    print("structures {%s}: mixed vs fp64 max rel %.3e, median %.3e" %
+          (g, rel.max(), np.median(rel)))
+    assert ok, rel.max()
+
+
+def _structure1_engine():
+    from graniitti_gb300 import card
+    c = card.read_card(os.path.join(GOLDEN, "cards", "pp_res_pipi_screened.json"))
+    P = card.build_params(c, "PP[RESTENSOR]<F> -> pi+ pi- @R[f2_1270]{g0:0, g1:1}")
+    e = _engine(P)
+    e.eikonal_build()
+    return P, e
+
+
+def test_fp32_loop_refinement_structure1(gpu):
+    """Structure 1 ((l,s) = (2,0) - (2,2)) at small forward pT: its phi-rings cancel by up to
+    10^12, so the plain FP32 loop is wrong by orders of magnitude on many events; the error
+    estimate sends those to the FP64 loop and the mixed weights meet the FP64 ones."""
+    import graniitti_gb300 as gg
+    import philox_np
+    P, e = _structure1_engine()
+    u = philox_np.uniforms(67, 4096, 8)
+    w64, _ = e.event_weights(u, prec=gg.FP64)
+    Pb = type(P)()
+    ctypes.memmove(ctypes.byref(Pb), ctypes.byref(P), ctypes.sizeof(P))
+    Pb.screening = 0
+    wb, _ = _engine(Pb).event_weights(u, prec=gg.FP64)
+    e.set_tuning(fp64_refine=0)
+    assert e.tuning().fp64_refine == 0
+    w32, _ = e.event_weights(u, prec=gg.MIXED)
+    ok32, rel32 = _mixed_ok(w32, w64, wb)
+    e.set_tuning(fp64_refine=1)
+    wm, _ = e.event_weights(u, prec=gg.MIXED)
+    ok, rel = _mixed_ok(wm, w64, wb)
+    print("structure 1: plain FP32 loop max rel %.2e (median %.2e); refined %.2e" %
+          (rel32.max(), np.median(rel32), rel.max()))
+    assert not ok32 and rel32.max() > 1e-2
+    assert ok, rel.max()
+
+
+def test_fp32_loop_refinement_vegas_pass(gpu):
+    """A VEGAS pass of structure 1 on the mixed loop reports the refined events and gives
+    the FP64 pass's integral on the same points."""
+    import graniitti_gb300 as gg
+    from graniitti_gb300 import _abi
+    res = {}
+    for prec in (gg.FP64, gg.MIXED):
+        _, e = _structure1_engine()
+        vp = _abi.VegasParams()
+        vp.bins, vp.iter, vp.ncall, vp.lambda_ = 128, 5, 1 << 16, 1.5
+        vp.chi2max, vp.precision, vp.burnin_iter, vp.prec, vp.seed = 10.0, 1e-3, 3, prec, 5
+        e.vegas_init(vp)
+        res[prec] = e.vegas_iteration(mode=1, refine=False, iter_id=3)
+        e.close()
+    r64, rm = res[gg.FP64], res[gg.MIXED]
+    print("structure 1 VEGAS pass: %d of %d screened events refined; I mixed %.8e, FP64 %.8e"
+          % (rm.refined, int(rm.fidcuts_ok), rm.I_this, r64.I_this))
+    assert r64.refined == 0 and 0 < rm.refined <= rm.fidcuts_ok
+    assert rm.I_this == pytest.approx(r64.I_this, rel=1e-5)
+    assert rm.maxf == pytest.approx(r64.maxf, rel=1e-5)
+    assert rm.nan_count == r64.nan_count

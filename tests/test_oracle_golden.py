@@ -166,7 +166,9 @@ RES_TOL = 5e-9
 
 
 @pytest.mark.parametrize("name", ["rf_tree_weights.npz", "rf_mix_tree_weights.npz",
-                                  "rf_kk_tree_weights.npz", "rc_tree_weights.npz"])
+                                  "rf_kk_tree_weights.npz", "rc_tree_weights.npz",
+                                  "rf_f2_1525_tree_weights.npz"] +
+                         ["rf_s%d_tree_weights.npz" % j for j in range(1, 7)])
 def test_tensor_resonance_tree_weights(lib_built, name):
     g = _load(name)
     w, fl = orc.weights(_params_res(g), g["u"])
