@@ -1,6 +1,6 @@
 """In-tree build of the CUDA library graniitti_gb300/_build/libgrn.so (sm_103a).
 
-Two translation units compiled in parallel by nvcc, linked as a shared library
+The translation units compiled in parallel by nvcc, linked as a shared library
 with the CUDA runtime linked statically (nothing else to ship).
 """
 import os
@@ -13,7 +13,8 @@ REPO = os.path.dirname(HERE)
 CSRC = os.path.join(HERE, "csrc")
 OUT = os.path.join(HERE, "_build")
 LIB = os.path.join(OUT, "libgrn.so")
-SOURCES = ["grn_kernels.cu", "grn_api.cu", "grn_noalloc.cu", "grn_flow.cu", "grn_record.cc"]
+SOURCES = ["grn_kernels.cu", "grn_api.cu", "grn_noalloc.cu", "grn_flow.cu", "grn_flow_wide.cu",
+           "grn_record.cc"]
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 
 

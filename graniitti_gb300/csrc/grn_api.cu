@@ -154,11 +154,15 @@ struct grn_flow {
   grn_engine *e      = nullptr;  // null once the engine has been destroyed
   int         device = 0;
   int         layers = 6;
+  int         dim    = 8;      // hypercube dimension (the process's)
+  int         hidden = 128;    // MLP width
+  bool        wide   = false;  // (dim, hidden) != (8, 128): the kernels of grn_flow_wide.cu
   uint64_t    seed   = 1;
   int64_t     nparams = 0;
   int64_t     adam_t  = 0;
   double      mix     = 0.0;  // weight of the uniform component of the proposal
   DevBuf      d_theta, d_m, d_v, d_grad, d_w2p, d_w3p, d_w2c, d_w3c, d_loss, d_err;
+  DevBuf      d_w2t, d_w2r, d_w3t, d_w3r;    // wide shapes: backward operand copies
   DevBuf      d_x, d_z, d_lq, d_coef, d_xs;  // batch scratch
   DevBuf      d_gpart, d_lpart;                // per-block gradient / loss slices
   DevBuf      d_tu, d_tlq, d_tcoef;          // training set
@@ -1551,10 +1555,31 @@ double splitmix_uniform(uint64_t &state) {
   return static_cast<double>(z >> 11) * 0x1.0p-53;
 }
 
+grn::FlowWideBufs wide_bufs(grn_flow *f) {
+  return {f->d_w2c.p, f->d_w3c.p, f->d_w2t.p, f->d_w2r.p, f->d_w3t.p, f->d_w3r.p};
+}
+
 grn_status flow_pack(grn_flow *f) {
-  GRN_CUDA(grn::launch_flow_pack(f->d_theta.as<float>(), f->layers, f->d_w2p.p, f->d_w3p.p,
-                                 f->d_w2c.p, f->d_w3c.p, f->e->stream));
+  if (f->wide)
+    GRN_CUDA(grn::launch_wflow_pack(f->dim, f->hidden, f->d_theta.as<float>(), f->layers,
+                                    wide_bufs(f), f->e->stream));
+  else
+    GRN_CUDA(grn::launch_flow_pack(f->d_theta.as<float>(), f->layers, f->d_w2p.p, f->d_w3p.p,
+                                   f->d_w2c.p, f->d_w3c.p, f->e->stream));
   return GRN_OK;
+}
+
+// Forward pass of the flow's shape (see launch_flow_forward).
+cudaError_t flow_forward(grn_flow *f, int mode, const float *xin, int64_t ld_in, int64_t n,
+                         uint64_t seed, uint32_t stream, int64_t first, float *xout,
+                         int64_t ld_out, float *lq, float *xs_store) {
+  if (f->wide)
+    return grn::launch_wflow_forward(f->dim, f->hidden, mode, f->d_theta.as<float>(),
+                                     wide_bufs(f), f->layers, xin, ld_in, n, seed, stream, first,
+                                     xout, ld_out, lq, xs_store, f->d_err.as<int>(), f->e->stream);
+  return grn::launch_flow_forward(mode, f->d_theta.as<float>(), f->d_w2c.p, f->d_w3c.p,
+                                  f->layers, xin, ld_in, n, seed, stream, first, xout, ld_out, lq,
+                                  xs_store, f->d_err.as<int>(), f->e->stream);
 }
 
 // Bounded waits inside the forward kernel report through d_err (read after a sync).
@@ -1572,18 +1597,23 @@ grn_status flow_check_err(grn_flow *f) {
 grn_status flow_loss_grad(grn_flow *f, const float *x, int64_t ld, const float *coef, int64_t n,
                           int kind, double *loss_slot) {
   grn_engine *e = f->e;
-  GRN_CUDA(f->d_xs.ensure(static_cast<size_t>(f->layers) * grn::flow::kDim * n * sizeof(float)));
+  GRN_CUDA(f->d_xs.ensure(static_cast<size_t>(f->layers) * f->dim * n * sizeof(float)));
   GRN_CUDA(f->d_lq.ensure(n * sizeof(float)));
-  GRN_CUDA(grn::launch_flow_forward(0, f->d_theta.as<float>(), f->d_w2c.p, f->d_w3c.p, f->layers,
-                                    x, ld, n, 0, 0, 0, nullptr, 0, f->d_lq.as<float>(),
-                                    f->d_xs.as<float>(), f->d_err.as<int>(), e->stream));
+  GRN_CUDA(flow_forward(f, 0, x, ld, n, 0, 0, 0, nullptr, 0, f->d_lq.as<float>(),
+                        f->d_xs.as<float>()));
   const int slices = grn::flow_backward_slices();
   GRN_CUDA(f->d_gpart.ensure(static_cast<size_t>(slices) * f->nparams * sizeof(float)));
   GRN_CUDA(f->d_lpart.ensure(static_cast<size_t>(slices) * sizeof(double)));
-  GRN_CUDA(grn::launch_flow_backward(f->d_theta.as<float>(), f->d_w2p.p, f->d_w3p.p, f->layers,
-                                     f->d_xs.as<float>(), f->d_lq.as<float>(), coef, n, kind,
-                                     f->d_gpart.as<float>(), f->d_lpart.as<double>(),
-                                     f->d_grad.as<float>(), loss_slot, e->stream));
+  if (f->wide)
+    GRN_CUDA(grn::launch_wflow_backward(f->dim, f->hidden, f->d_theta.as<float>(), wide_bufs(f),
+                                        f->layers, f->d_xs.as<float>(), f->d_lq.as<float>(), coef,
+                                        n, kind, f->d_gpart.as<float>(), f->d_lpart.as<double>(),
+                                        f->d_grad.as<float>(), loss_slot, e->stream));
+  else
+    GRN_CUDA(grn::launch_flow_backward(f->d_theta.as<float>(), f->d_w2p.p, f->d_w3p.p, f->layers,
+                                       f->d_xs.as<float>(), f->d_lq.as<float>(), coef, n, kind,
+                                       f->d_gpart.as<float>(), f->d_lpart.as<double>(),
+                                       f->d_grad.as<float>(), loss_slot, e->stream));
   return GRN_OK;
 }
 
@@ -1624,10 +1654,13 @@ void grn_flow_default_params(grn_flow_params *p) {
 grn_status grn_flow_create(grn_engine *e, const grn_flow_params *p, grn_flow **out) {
   if (!e || !p || !out) return fail(GRN_ERR_INVALID, "null argument");
   *out = nullptr;
-  if (p->dim != e->dim || p->dim != grn::flow::kDim)
-    return fail(GRN_ERR_UNSUPPORTED, "flow dimension must be 8 (the process dimension)");
-  if (p->hidden != grn::flow::kHid || p->bins != grn::flow::kBins)
-    return fail(GRN_ERR_UNSUPPORTED, "flow kernels are built for hidden = 128, bins = 16");
+  if (p->dim != e->dim)
+    return fail(GRN_ERR_UNSUPPORTED, "flow dimension must be the process dimension");
+  const bool base = p->dim == grn::flow::kDim && p->hidden == grn::flow::kHid;
+  if (p->bins != grn::flow::kBins || !(base || grn::flow_wide_supported(p->dim, p->hidden)))
+    return fail(GRN_ERR_UNSUPPORTED,
+                "flow kernels are built for bins = 16 and (dim, hidden) = (8, 128), (8, 256), "
+                "(14, 128), (14, 256)");
   if (p->layers < 1 || p->layers > grn::flow::kMaxLayers)
     return fail(GRN_ERR_INVALID, "flow layers must be in [1, 12]");
   if (!(p->mix_uniform >= 0.0 && p->mix_uniform < 1.0))
@@ -1638,31 +1671,45 @@ grn_status grn_flow_create(grn_engine *e, const grn_flow_params *p, grn_flow **o
   f->device  = e->device;
   e->flows.push_back(f);
   f->layers  = p->layers;
+  f->dim     = p->dim;
+  f->hidden  = p->hidden;
+  f->wide    = !base;
   f->seed    = p->seed;
   f->mix     = p->mix_uniform;
-  f->nparams = static_cast<int64_t>(p->layers) * grn::flow::kLayerParams;
+  const int64_t lp = grn::flow_layer_params(f->dim, f->hidden);
+  f->nparams = static_cast<int64_t>(p->layers) * lp;
   std::vector<float> th(f->nparams, 0.0f);
   uint64_t           state = p->seed;
-  using namespace grn::flow;
+  using grn::flow::kBins;
+  using grn::flow::kRaw;
+  const int   da = f->dim / 2, hid = f->hidden, nout = da * kRaw;
   const float b3d = static_cast<float>(std::log(std::expm1(1.0 - 1e-3)));
   for (int l = 0; l < p->layers; ++l) {
-    float       *t  = th.data() + static_cast<size_t>(l) * kLayerParams;
-    const double l1 = std::sqrt(6.0 / kDA), l2 = std::sqrt(6.0 / kHid);
-    for (int i = 0; i < kDA * kHid; ++i) t[i] = static_cast<float>((2 * splitmix_uniform(state) - 1) * l1);
-    float *w2 = t + kDA * kHid + kHid;
-    for (int i = 0; i < kHid * kHid; ++i) w2[i] = static_cast<float>((2 * splitmix_uniform(state) - 1) * l2);
-    float *b3 = t + kLayerParams - kNOut;
-    for (int j = 0; j < kDA; ++j)
+    float       *t  = th.data() + static_cast<size_t>(l) * lp;
+    const double l1 = std::sqrt(6.0 / da), l2 = std::sqrt(6.0 / hid);
+    for (int i = 0; i < da * hid; ++i) t[i] = static_cast<float>((2 * splitmix_uniform(state) - 1) * l1);
+    float *w2 = t + da * hid + hid;
+    for (int i = 0; i < hid * hid; ++i) w2[i] = static_cast<float>((2 * splitmix_uniform(state) - 1) * l2);
+    float *b3 = t + lp - nout;
+    for (int j = 0; j < da; ++j)
       for (int r = 2 * kBins; r < kRaw; ++r) b3[j * kRaw + r] = b3d;
   }
   const size_t pb = f->nparams * sizeof(float);
   grn_status   st = GRN_OK;
-  if (f->d_theta.ensure(pb) != cudaSuccess || f->d_m.ensure(pb) != cudaSuccess ||
+  bool         ok_w = true;
+  if (f->wide) {
+    const grn::FlowWideSizes z = grn::flow_wide_sizes(f->dim, f->hidden, f->layers);
+    ok_w = f->d_w2c.ensure(z.w2c * 2) == cudaSuccess && f->d_w3c.ensure(z.w3c * 2) == cudaSuccess &&
+           f->d_w2t.ensure(z.w2t * 2) == cudaSuccess && f->d_w2r.ensure(z.w2r * 2) == cudaSuccess &&
+           f->d_w3t.ensure(z.w3t * 2) == cudaSuccess && f->d_w3r.ensure(z.w3r * 2) == cudaSuccess;
+  } else {
+    ok_w = f->d_w2p.ensure(grn::flow_w2p_elems(f->layers) * 2) == cudaSuccess &&
+           f->d_w3p.ensure(grn::flow_w3p_elems(f->layers) * 2) == cudaSuccess &&
+           f->d_w2c.ensure(grn::flow_w2c_elems(f->layers) * 2) == cudaSuccess &&
+           f->d_w3c.ensure(grn::flow_w3c_elems(f->layers) * 2) == cudaSuccess;
+  }
+  if (!ok_w || f->d_theta.ensure(pb) != cudaSuccess || f->d_m.ensure(pb) != cudaSuccess ||
       f->d_v.ensure(pb) != cudaSuccess || f->d_grad.ensure(pb) != cudaSuccess ||
-      f->d_w2p.ensure(grn::flow_w2p_elems(f->layers) * 2) != cudaSuccess ||
-      f->d_w3p.ensure(grn::flow_w3p_elems(f->layers) * 2) != cudaSuccess ||
-      f->d_w2c.ensure(grn::flow_w2c_elems(f->layers) * 2) != cudaSuccess ||
-      f->d_w3c.ensure(grn::flow_w3c_elems(f->layers) * 2) != cudaSuccess ||
       f->d_loss.ensure(sizeof(double)) != cudaSuccess ||
       f->d_err.ensure(sizeof(int)) != cudaSuccess) {
     st = fail(GRN_ERR_CUDA, "flow: device allocation failed");
@@ -1693,7 +1740,7 @@ grn_status grn_flow_destroy(grn_flow *f) {
     cudaStreamSynchronize(f->e->stream);
   }
   for (DevBuf *b : {&f->d_theta, &f->d_m, &f->d_v, &f->d_grad, &f->d_w2p, &f->d_w3p, &f->d_w2c,
-                    &f->d_w3c, &f->d_err, &f->d_loss,
+                    &f->d_w3c, &f->d_w2t, &f->d_w2r, &f->d_w3t, &f->d_w3r, &f->d_err, &f->d_loss,
                     &f->d_x, &f->d_z, &f->d_lq, &f->d_coef, &f->d_xs, &f->d_gpart,
                     &f->d_lpart, &f->d_tu, &f->d_tlq,
                     &f->d_tcoef, &f->d_fu, &f->d_flq})
@@ -1741,7 +1788,7 @@ static grn_status flow_map(grn_flow *f, int mode, const float *xin, uint64_t see
   if (n < 0 || !logq) return fail(GRN_ERR_INVALID, "bad argument");
   if (n == 0) return GRN_OK;
   grn_engine  *e  = f->e;
-  const size_t nx = static_cast<size_t>(n) * grn::flow::kDim;
+  const size_t nx = static_cast<size_t>(n) * f->dim;
   const float *dx = nullptr;
   if (xin) {
     st = stage_in(f->d_x, xin, nx, e->stream, &dx);
@@ -1757,9 +1804,7 @@ static grn_status flow_map(grn_flow *f, int mode, const float *xin, uint64_t see
     GRN_CUDA(f->d_lq.ensure(n * sizeof(float)));
     dl = f->d_lq.as<float>();
   }
-  GRN_CUDA(grn::launch_flow_forward(mode, f->d_theta.as<float>(), f->d_w2c.p, f->d_w3c.p,
-                                    f->layers, dx, n, n, seed, stream, first, dz, n, dl, nullptr,
-                                    f->d_err.as<int>(), e->stream));
+  GRN_CUDA(flow_forward(f, mode, dx, n, n, seed, stream, first, dz, n, dl, nullptr));
   if (xout && !dev_out)
     GRN_CUDA(cudaMemcpyAsync(xout, dz, nx * sizeof(float), cudaMemcpyDeviceToHost, e->stream));
   if (!dev_lq)
@@ -1791,7 +1836,7 @@ grn_status grn_flow_loss_grad(grn_flow *f, const float *x, const float *coef, in
   if (!x || !coef || n < 1 || (kind != 0 && kind != 1)) return fail(GRN_ERR_INVALID, "bad argument");
   grn_engine  *e  = f->e;
   const float *dx = nullptr, *dc = nullptr;
-  st = stage_in(f->d_x, x, static_cast<size_t>(n) * grn::flow::kDim, e->stream, &dx);
+  st = stage_in(f->d_x, x, static_cast<size_t>(n) * f->dim, e->stream, &dx);
   if (st != GRN_OK) return st;
   st = stage_in(f->d_coef, coef, static_cast<size_t>(n), e->stream, &dc);
   if (st != GRN_OK) return st;
@@ -1824,24 +1869,22 @@ grn_status grn_flow_train_step(grn_flow *f, const float *x, const float *coef, i
 static grn_status flow_points(grn_flow *f, bool from_flow, uint32_t stream_id, int64_t n,
                               DevBuf &dst_u, DevBuf &dst_lq) {
   grn_engine *e = f->e;
-  GRN_CUDA(dst_u.ensure(static_cast<size_t>(n) * grn::flow::kDim * sizeof(float)));
+  GRN_CUDA(dst_u.ensure(static_cast<size_t>(n) * f->dim * sizeof(float)));
   GRN_CUDA(dst_lq.ensure(static_cast<size_t>(n) * sizeof(float)));
   float         *u = dst_u.as<float>(), *lq = dst_lq.as<float>();
   const uint64_t key = e->seed ^ 0xF10Bull;
   if (!from_flow) {
-    GRN_CUDA(grn::launch_flow_uniform(key, stream_id, 0, n, n, u, lq, e->stream));
+    GRN_CUDA(grn::launch_flow_uniform_dim(f->dim, key, stream_id, 0, n, n, u, lq, e->stream));
     return GRN_OK;
   }
   const int64_t nu = static_cast<int64_t>(f->mix * static_cast<double>(n));
   if (nu > 0) {
-    GRN_CUDA(grn::launch_flow_uniform(key, stream_id, 0, nu, n, u, nullptr, e->stream));
-    GRN_CUDA(grn::launch_flow_forward(0, f->d_theta.as<float>(), f->d_w2c.p, f->d_w3c.p,
-                                      f->layers, u, n, nu, 0, 0, 0, nullptr, 0, lq, nullptr,
-                                      f->d_err.as<int>(), e->stream));
+    GRN_CUDA(grn::launch_flow_uniform_dim(f->dim, key, stream_id, 0, nu, n, u, nullptr,
+                                          e->stream));
+    GRN_CUDA(flow_forward(f, 0, u, n, nu, 0, 0, 0, nullptr, 0, lq, nullptr));
   }
-  GRN_CUDA(grn::launch_flow_forward(1, f->d_theta.as<float>(), f->d_w2c.p, f->d_w3c.p, f->layers,
-                                    nullptr, n, n - nu, key, stream_id, nu, u + nu, n, lq + nu,
-                                    nullptr, f->d_err.as<int>(), e->stream));
+  GRN_CUDA(flow_forward(f, 1, nullptr, n, n - nu, key, stream_id, nu, u + nu, n, lq + nu,
+                        nullptr));
   if (f->mix > 0.0) GRN_CUDA(grn::launch_flow_mix(lq, n, f->mix, e->stream));
   return GRN_OK;
 }

@@ -61,5 +61,43 @@ cudaError_t launch_flow_uniform(uint64_t seed, uint32_t stream, int64_t first, i
                                 int64_t ld, float *u, float *lq, cudaStream_t st);
 // lq <- log(alpha + (1 - alpha) exp(lq)): the defensive mixture with the uniform density.
 cudaError_t launch_flow_mix(float *lq, int64_t n, double alpha, cudaStream_t st);
+// grad[i] = sum of the nslices slices of part (np floats each) in slice order; loss = sum of
+// loss_part[0..nslices).
+cudaError_t launch_flow_grad_reduce(const float *part, int nslices, int64_t np, float *grad,
+                                    const double *loss_part, double *loss, cudaStream_t st);
+
+// ---------------------------------------------------------------------------
+// The same flow for other shapes (grn_flow_wide.cu): dimension D = 8 or 14, MLP width H = 128
+// or 256 ((8, 128) is served by the kernels above). Parameters per layer
+// flow_layer_params(D, H), same layout. BF16 operand copies (element counts for all layers):
+struct FlowWideSizes {
+  size_t w2c, w3c;       // forward: 64-column chunks in the K-major canonical layout
+  size_t w2t, w2r;       // backward: W2 as [out][in] and [in][out] row-major
+  size_t w3t, w3r;       // backward: W3 as [56 j + r][h] and [h][o] row-major
+};
+struct FlowWideBufs {
+  void *w2c, *w3c, *w2t, *w2r, *w3t, *w3r;
+};
+bool          flow_wide_supported(int dim, int hidden);
+int64_t       flow_layer_params(int dim, int hidden);
+FlowWideSizes flow_wide_sizes(int dim, int hidden, int layers);
+cudaError_t   launch_wflow_pack(int dim, int hidden, const float *theta, int layers,
+                                const FlowWideBufs &b, cudaStream_t st);
+// Same contract as launch_flow_forward (xs_store: layers x D x n).
+cudaError_t   launch_wflow_forward(int dim, int hidden, int mode, const float *theta,
+                                   const FlowWideBufs &b, int layers, const float *xin,
+                                   int64_t ld_in, int64_t n, uint64_t seed, uint32_t stream,
+                                   int64_t first, float *xout, int64_t ld_out, float *lq,
+                                   float *xs_store, int *err, cudaStream_t st);
+// Same contract as launch_flow_backward (part: flow_backward_slices() slices).
+cudaError_t   launch_wflow_backward(int dim, int hidden, const float *theta,
+                                    const FlowWideBufs &b, int layers, const float *xs,
+                                    const float *lq, const float *coef, int64_t n, int kind,
+                                    float *part, double *loss_part, float *grad, double *loss,
+                                    cudaStream_t st);
+// launch_flow_uniform for D = 8 or 14.
+cudaError_t   launch_flow_uniform_dim(int dim, uint64_t seed, uint32_t stream, int64_t first,
+                                      int64_t n, int64_t ld, float *u, float *lq,
+                                      cudaStream_t st);
 
 }  // namespace grn

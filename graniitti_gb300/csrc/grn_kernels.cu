@@ -138,11 +138,16 @@ __device__ cx<double> loop_integral_fast(const KArgs &A, const Born &b, const Kt
 // of the (loop-invariant) central pair, each screened on its own (S3ScreenedAmp2 screens every
 // entry of lts.hamp), |A0_h + A_loop,h|^2 summed. The complex node weight U_i c_j is applied
 // per point so that only the nine compensated sums stay live.
+// For T = float, *mag receives sum_h |A_h| mag_h / sqrt(sum_h |A_h|^2) with mag_h the
+// rounding scale of helicity h (see loop_integral): the error of sum_h |A_h|^2 is then about
+// 2 u |norm| mag sqrt(sum_h |A_h|^2), each helicity weighted by its own size.
 template <typename T>
 __device__ double screened_amp2_vv(const KArgs &A, const Born &b, const KtNode<T> *skt,
                                    const PhiNode<T> *sphi, double *mag = nullptr) {
   constexpr bool kMag = sizeof(T) == sizeof(float);
-  T m = T(0);
+  T mh[9];
+#pragma unroll
+  for (int h = 0; h < 9; ++h) mh[h] = T(0);
   cx<double> A0[9];
   born_amps_2xv(A.P, A.K, b, A0);
   LoopEvent<T> e;
@@ -163,25 +168,25 @@ __device__ double screened_amp2_vv(const KArgs &A, const Born &b, const KtNode<T
       cx<T> a[9];
       tensor_me4_2xv<T>(A.P, A.K, kk, s34, e3, e4, a);
       const T wr = ni.u * nj.cre, wi = ni.u * nj.cim;
-      T ab = T(0);
+      const T aw = kMag ? sqrt(wr * wr + wi * wi) : T(0);
 #pragma unroll
       for (int h = 0; h < 9; ++h) {
         kahan_add(sr[h], cr[h], wr * a[h].re - wi * a[h].im);
         kahan_add(si[h], ci[h], wr * a[h].im + wi * a[h].re);
-        if constexpr (kMag) ab += fabs(a[h].re) + fabs(a[h].im);
+        if constexpr (kMag) mh[h] += aw * (fabs(a[h].re) + fabs(a[h].im));
       }
-      if constexpr (kMag) m += sqrt(wr * wr + wi * wi) * ab;
     }
   }
-  if (mag) *mag = double(m);
-  double amp2 = 0.0;
+  double amp2 = 0.0, wmag = 0.0;
 #pragma unroll
   for (int h = 0; h < 9; ++h) {
     const double xr = double(sr[h]), xi = double(si[h]);
     const double re = A0[h].re + (A.loop_norm_re * xr - A.loop_norm_im * xi);
     const double im = A0[h].im + (A.loop_norm_re * xi + A.loop_norm_im * xr);
     amp2 += re * re + im * im;
+    if constexpr (kMag) wmag += sqrt(re * re + im * im) * double(mh[h]);
   }
+  if (mag) *mag = wmag / sqrt(amp2);
   return amp2;
 }
 
@@ -346,8 +351,9 @@ __device__ __forceinline__ bool born_stage(const KArgs &A, const double *x, Born
 // Screened weight of an event that passed the cuts (MContinuum::EventWeight with
 // MProcess::S3ScreenedAmp2, src/MContinuum.cc:164-193, src/MProcess.cc:157-288).
 // With T = float and refine non-null, *refine tells whether the estimated relative error
-// of W, 2 kRefineKappa u |norm| mag / |A0 + A_loop| (for vector pairs with sqrt(sum |A_h|^2)),
-// exceeds A.refine_tol (or is not finite): the caller then recomputes the event in FP64.
+// of W, 2 kRefineKappa u |norm| mag / |A0 + A_loop| (for vector pairs mag is the
+// helicity-weighted scale of screened_amp2_vv, over sqrt(sum |A_h|^2)), exceeds A.refine_tol
+// (or is not finite): the caller then recomputes the event in FP64.
 template <typename T, bool CASC>
 __device__ double screened_weight(const KArgs &A, const double *x, uint8_t &flags,
                                   const KtNode<T> *skt, const PhiNode<T> *sphi,

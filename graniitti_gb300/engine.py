@@ -196,11 +196,13 @@ class Flow:
 
     Point arrays are float32, dimension-major (dim x n)."""
 
-    def __init__(self, engine, layers=6, seed=1, mix_uniform=0.0):
+    def __init__(self, engine, layers=6, seed=1, mix_uniform=0.0, hidden=128):
         self.engine = engine
         self.lib = engine.lib
         p = _abi.FlowParams()
         self.lib.grn_flow_default_params(ctypes.byref(p))
+        p.dim = engine.dim
+        p.hidden = hidden
         p.layers = layers
         p.seed = seed
         p.mix_uniform = mix_uniform
@@ -208,6 +210,7 @@ class Flow:
         _abi.check(self.lib.grn_flow_create(engine.h, ctypes.byref(p), ctypes.byref(h)))
         self.h = h
         self.layers = layers
+        self.hidden = hidden
         self.dim = engine.dim
         self.n_params = self.lib.grn_flow_num_params(h)
 

@@ -379,9 +379,9 @@ grn_status grn_vegas_points(grn_engine *e, const int64_t *idx, int64_t n, double
 typedef struct grn_flow grn_flow;
 
 typedef struct grn_flow_params {
-  int32_t  dim;     /* must equal grn_dim() (8) */
+  int32_t  dim;     /* must equal grn_dim(): 8 (2-body) or 14 (two-body cascades) */
   int32_t  layers;  /* coupling layers, 1..12 (default 6) */
-  int32_t  hidden;  /* MLP width (128) */
+  int32_t  hidden;  /* MLP width: 128 (default) or 256 */
   int32_t  bins;    /* spline bins (16) */
   uint64_t seed;    /* initial weights */
   double   mix_uniform; /* alpha in [0, 1): passes sample alpha * uniform + (1 - alpha) * flow,

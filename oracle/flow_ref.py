@@ -25,9 +25,15 @@ MIN_D = 1e-3
 
 
 def masks(dim):
-    """Conditioning (A) and transformed (B) index sets of the six layers (D = 8)."""
-    assert dim == 8
-    A = [[0, 1, 2, 3], [4, 5, 6, 7], [0, 2, 4, 6], [1, 3, 5, 7], [0, 1, 4, 5], [2, 3, 6, 7]]
+    """Conditioning (A) and transformed (B) index sets of the six masks; layer l uses
+    mask l % 6 (D = 8 or 14): halves, even / odd, neighbour pairs, each then swapped."""
+    if dim == 8:
+        A = [[0, 1, 2, 3], [4, 5, 6, 7], [0, 2, 4, 6], [1, 3, 5, 7], [0, 1, 4, 5], [2, 3, 6, 7]]
+    elif dim == 14:
+        A = [list(range(7)), list(range(7, 14)), list(range(0, 14, 2)), list(range(1, 14, 2)),
+             [0, 1, 4, 5, 8, 9, 12], [2, 3, 6, 7, 10, 11, 13]]
+    else:
+        raise ValueError("flow masks exist for D = 8 and 14")
     return [(a, [j for j in range(dim) if j not in a]) for a in A]
 
 
@@ -135,7 +141,9 @@ def log_density(x, theta, dim=8, layers=6, hidden=128, bins=16, bf=True):
     P = unpack(theta, dim, layers, hidden, bins)
     x = np.array(x, dtype=np.float64)
     logq = np.zeros(len(x))
-    for l, (A, B) in enumerate(masks(dim)):
+    ml = masks(dim)
+    for l in range(layers):
+        A, B = ml[l % 6]
         raw = conditioner(x[:, A], P[l], bf).reshape(len(x), len(B), 3 * bins + 1)
         for jj, j in enumerate(B):
             y, ld = rqs_forward(x[:, j], raw[:, jj, :], bins)
@@ -150,7 +158,7 @@ def sample(z, theta, dim=8, layers=6, hidden=128, bins=16, bf=True):
     x = np.array(z, dtype=np.float64)
     ml = masks(dim)
     for l in reversed(range(layers)):
-        A, B = ml[l]
+        A, B = ml[l % 6]
         raw = conditioner(x[:, A], P[l], bf).reshape(len(x), len(B), 3 * bins + 1)
         for jj, j in enumerate(B):
             x[:, j] = rqs_inverse(x[:, j], raw[:, jj, :], bins)
@@ -264,7 +272,7 @@ def loss_and_grad(x, coef, theta, kind=1, dim=8, layers=6, hidden=128, bins=16, 
     saved = []
     logq = np.zeros(n)
     for l in range(layers):
-        A, B = ml[l]
+        A, B = ml[l % 6]
         p = P[l]
         xa = cur[:, A]
         a1 = q(xa) @ q(p["W1"]) + p["b1"]
@@ -287,7 +295,7 @@ def loss_and_grad(x, coef, theta, kind=1, dim=8, layers=6, hidden=128, bins=16, 
     grads = []
     gcur = np.zeros((n, dim))  # dL/d(output of the layer being processed)
     for l in reversed(range(layers)):
-        A, B = ml[l]
+        A, B = ml[l % 6]
         p = P[l]
         xin, xa, h1, h2, raw = saved[l]
         graw = np.zeros((n, nB, 3 * bins + 1))

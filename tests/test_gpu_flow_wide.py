@@ -1,0 +1,174 @@
+"""The flow for the other shapes (grn_flow_wide.cu): D = 8 with width 256, and D = 14 (the
+vector-pair cascades) with width 128 and 256, 8 coupling layers. Density and sampling
+directions, the training gradient against the CPU oracle (oracle/flow_ref.py), and a
+trained 14-dimensional flow in front of the VEGAS map of rho rho -> pi+ pi- pi+ pi-."""
+import numpy as np
+import pytest
+
+from oracle import flow_ref as F
+
+pytestmark = pytest.mark.gpu
+
+# BF16 operands, FP32 accumulation and splines on the GPU; the oracle rounds the same
+# operands to BF16 and does the rest in FP64, so an activation whose FP32 and FP64 sums round
+# to different BF16 neighbours moves log q. Eight layers of width 256 hold 2.7 times the BF16
+# activations per point of the (8, 128) test network, and the test flows' log q is 3.4 times
+# as sensitive to their rounding (oracle, BF16 vs FP64: p99 0.24 against 0.07), so the log q
+# tails are allowed up to 25 times the (8, 128) bounds; the medians stay tight.
+TOL_Z_P99, TOL_Z_MAX, TOL_Z_MED = 3e-5, 2e-3, 1e-6
+TOL_LQ_P99, TOL_LQ_MAX, TOL_LQ_MED = 5e-3, 1e-1, 3e-5
+TOL_GRAD_REL, TOL_LOSS_REL = 2e-2, 1e-4
+LAYERS = 8
+SHAPES = [(8, 256), (14, 128), (14, 256)]
+RHO = "PP[CONTENSOR]<F> -> rho(770)0 > {pi+ pi-} rho(770)0 > {pi+ pi-}"
+
+
+def _theta(dim, hidden, seed, scale=0.03):
+    rng = np.random.default_rng(seed)
+    th = F.init_params(dim=dim, layers=LAYERS, hidden=hidden, seed=seed)
+    for p in F.unpack(th, dim, LAYERS, hidden, 16):
+        p["W3"] += rng.normal(0, scale, p["W3"].shape)
+        p["b3"] += rng.normal(0, 0.3, p["b3"].shape)
+        p["b1"] += rng.normal(0, 0.1, p["b1"].shape)
+        p["b2"] += rng.normal(0, 0.1, p["b2"].shape)
+    return th.astype(np.float32).astype(np.float64)
+
+
+@pytest.fixture(scope="module")
+def engines(gpu, params):
+    import graniitti_gb300 as g
+    from graniitti_gb300 import card
+    from conftest import CARD
+    e8 = g.Engine(params, 0)
+    e14 = g.Engine(card.build_params(card.read_card(CARD), RHO), 0)
+    assert (e8.dim, e14.dim) == (8, 14)
+    yield {8: e8, 14: e14}
+    e8.close()
+    e14.close()
+
+
+def _flow(engines, dim, hidden):
+    import graniitti_gb300 as g
+    return g.Flow(engines[dim], layers=LAYERS, hidden=hidden, seed=1)
+
+
+@pytest.mark.parametrize("shape", SHAPES)
+def test_param_count_and_identity(engines, shape):
+    dim, hidden = shape
+    f = _flow(engines, dim, hidden)
+    assert f.n_params == F.n_params(dim, LAYERS, hidden, 16)
+    f.set_params(F.init_params(dim=dim, layers=LAYERS, hidden=hidden, seed=1).astype(np.float32))
+    x = np.random.default_rng(2).random((dim, 1000)).astype(np.float32)
+    z, lq = f.density(x)
+    assert np.max(np.abs(z - x)) < 2e-6 and np.max(np.abs(lq)) < 1e-4
+    f.close()
+
+
+@pytest.mark.parametrize("shape", SHAPES)
+def test_density_and_inverse_match_oracle(engines, shape):
+    dim, hidden = shape
+    f = _flow(engines, dim, hidden)
+    th = _theta(dim, hidden, 11)
+    f.set_params(th.astype(np.float32))
+    kw = dict(dim=dim, layers=LAYERS, hidden=hidden, bins=16, bf=True)
+    x = np.random.default_rng(12).random((dim, 1299)).astype(np.float32)  # ragged last subtile
+    z, lq = f.density(x)
+    lq_o, z_o = F.log_density(x.T.astype(np.float64), th, **kw)
+    dz, dl = np.abs(z.T - z_o), np.abs(lq - lq_o)
+    print("(%d, %d) density: max |dz| %.3e  |dlq| median %.2e p99 %.3e max %.3e (lq %.2f..%.2f)"
+          % (dim, hidden, dz.max(), np.median(dl), np.percentile(dl, 99), dl.max(), lq_o.min(),
+             lq_o.max()))
+    assert np.ptp(lq_o) > 1.0
+    assert np.percentile(dz, 99) < TOL_Z_P99 and dz.max() < TOL_Z_MAX
+    assert np.median(dz) < TOL_Z_MED and np.median(dl) < TOL_LQ_MED
+    assert np.percentile(dl, 99) < TOL_LQ_P99 and dl.max() < TOL_LQ_MAX
+    zin = np.random.default_rng(13).random((dim, 1100)).astype(np.float32)
+    xs, lqs = f.inverse(zin)
+    x_o, lqs_o = F.sample(zin.T.astype(np.float64), th, **kw)
+    dx, dl = np.abs(xs.T - x_o), np.abs(lqs - lqs_o)
+    print("(%d, %d) inverse: max |dx| %.3e  |dlq| median %.2e p99 %.3e" %
+          (dim, hidden, dx.max(), np.median(dl), np.percentile(dl, 99)))
+    assert np.percentile(dx, 99) < TOL_Z_P99 and dx.max() < TOL_Z_MAX
+    assert np.median(dx) < TOL_Z_MED and np.median(dl) < TOL_LQ_MED
+    assert np.percentile(dl, 99) < TOL_LQ_P99 and dl.max() < TOL_LQ_MAX
+    z2, lq2 = f.density(xs)
+    assert np.percentile(np.abs(z2 - zin), 99.9) < 1e-4
+    assert np.percentile(np.abs(lq2 - lqs), 99.9) < 1e-3
+    f.close()
+
+
+@pytest.mark.parametrize("shape", SHAPES)
+def test_sample_is_philox_at_identity(engines, shape):
+    import philox_np
+    dim, hidden = shape
+    f = _flow(engines, dim, hidden)
+    f.set_params(F.init_params(dim=dim, layers=LAYERS, hidden=hidden, seed=1).astype(np.float32))
+    x, lq = f.sample(seed=5, n=700, stream=3, first=100)
+    u = philox_np.uniforms(5, 800, dim, stream=3)[100:]
+    assert np.max(np.abs(x.T - u)) < 1e-6 and np.max(np.abs(lq)) < 1e-4
+    f.close()
+
+
+@pytest.mark.parametrize("shape", SHAPES)
+def test_gradient_matches_oracle(engines, shape):
+    dim, hidden = shape
+    f = _flow(engines, dim, hidden)
+    th = _theta(dim, hidden, 31, scale=0.03)
+    f.set_params(th.astype(np.float32))
+    rng = np.random.default_rng(33)
+    n = 700
+    x = rng.random((dim, n)).astype(np.float32)
+    coef = (rng.random(n) + 0.25).astype(np.float32)
+    loss, g = f.loss_grad(x, coef, kind=1)
+    lo, go, _ = F.loss_and_grad(x.T.astype(np.float64), coef.astype(np.float64), th, 1,
+                                dim=dim, layers=LAYERS, hidden=hidden, bins=16, bf=True)
+    assert abs(loss / lo - 1) < TOL_LOSS_REL
+    Pg = F.unpack(g.astype(np.float64), dim, LAYERS, hidden, 16)
+    Po = F.unpack(go, dim, LAYERS, hidden, 16)
+    worst = 0.0
+    for l in range(LAYERS):
+        for name in ("W1", "b1", "W2", "b2", "W3", "b3"):
+            a, b = Pg[l][name], Po[l][name]
+            nb = np.linalg.norm(b)
+            if nb == 0:
+                assert np.linalg.norm(a) == 0
+                continue
+            rel = np.linalg.norm(a - b) / nb
+            worst = max(worst, rel)
+            assert rel < TOL_GRAD_REL, (l, name, rel)
+    print("(%d, %d): loss %.6e vs %.6e, worst block rel err %.3e" % (dim, hidden, loss, lo, worst))
+    f.close()
+
+
+def test_wide_flow_on_rho_rho_reduces_variance_and_keeps_sigma(gpu):
+    """8 coupling layers of width 256 over the 14-dimensional rho rho -> 4 pi hypercube (no
+    screening), trained behind an adapted VEGAS grid; the flow passes keep sigma."""
+    import graniitti_gb300 as g
+    from graniitti_gb300 import _abi, card
+    from conftest import CARD
+    e = g.Engine(card.build_params(card.read_card(CARD), RHO), 0)
+    vp = _abi.VegasParams()
+    vp.bins, vp.iter, vp.ncall, vp.lambda_ = 128, 5, 1 << 18, 1.5
+    vp.chi2max, vp.precision, vp.burnin_iter, vp.prec, vp.seed = 10.0, 1e-3, 3, g.FP64, 3
+    e.vegas_init(vp)
+    for it in range(6):
+        e.vegas_iteration(mode=0, refine=True, iter_id=10 + it)
+    e.vegas_clear()
+    plain = [e.vegas_iteration(mode=1, refine=False, iter_id=30 + it) for it in range(3)][-1]
+    f = g.Flow(e, layers=LAYERS, hidden=256, seed=2, mix_uniform=0.05)
+    tr = f.train(n_train=1 << 19, batch=16384, epochs=4, rounds=2, lr=1e-3, prec=g.FP64)
+    print("rho rho flow (8 x 256, 14 dims): %d steps, rel var %.3f -> %.3f, loss %.4f -> %.4f, "
+          "%.0f ms" % (tr.steps, tr.rel_var_start, tr.rel_var_flow, tr.loss_first, tr.loss_last,
+                       tr.train_ms))
+    assert tr.steps == 256 and tr.loss_last < tr.loss_first
+    e.vegas_clear()
+    e.set_maxweight(0.0)
+    r = None
+    for it in range(3):
+        r = f.iteration(mode=1, iter_id=50 + it)
+    pull = (r.sigma - plain.sigma) / np.hypot(r.sigma_err, plain.sigma_err)
+    print("sigma: flow %.5e +- %.1e, plain VEGAS %.5e +- %.1e, pull %.2f"
+          % (r.sigma, r.sigma_err, plain.sigma, plain.sigma_err, pull))
+    assert abs(pull) < 4
+    f.close()
+    e.close()
