@@ -285,15 +285,106 @@ def batched_leg(g, _abi, torch, total, steps, warmup, device):
         procs.append({"process": proc, "points_per_step": int(e.vp.ncall),
                       "eps_unw": r.sigma / r.maxf if r.maxf > 0 else None,
                       "sigma_barn": r.sigma, "sigma_rel_err": r.sigma_err / r.sigma})
-        e.close()
     n = sum(p["points_per_step"] for p in procs)
+    full = full_form(g, _abi, torch, es, res, ms_b, ms_s, steps)
+    for e in es:
+        e.close()
     return {"workload": "screened f2(1270) -> pi+ pi- (tensor pomeron) + pi+ pi- continuum "
                         "(Regge) + rho rho -> 4 pi (tensor pomeron, 14 dims), %s of %d points per "
                         "pass, loop grid 15 x 12, one fused pass"
                         % ("/".join(str(int(f * 100)) for _, f in BATCH_MIX), n),
             "ms_per_step_batched": ms_b, "ms_per_step_separate": ms_s,
             "evaluations_per_s_batched": n / (ms_b * 1e-3),
-            "speedup_over_separate": ms_s / ms_b, "processes": procs}
+            "speedup_over_separate": ms_s / ms_b, "processes": procs, "full_form": full}
+
+
+def _unweighted_per_s(es, res, ms):
+    """Unweighted events per second of a pass over all members: sum_p ncall_p eps_p / time,
+    eps_p = <f>/max f of member p over its integration passes."""
+    return sum(int(e.vp.ncall) * (r.sigma / r.maxf) for e, r in zip(es, res) if r.maxf > 0) / (
+        ms * 1e-3)
+
+
+def full_form(g, _abi, torch, es, res_plain, ms_b, ms_s, steps):
+    """The full form of the mixed workload: the 4-body member (rho rho -> 4 pi, 14 dimensions)
+    draws its points from a learned proposal, 8 coupling layers of width 256 (trained untimed
+    in front of its adapted grid), batched with the 2-body members; against the same members
+    on plain VEGAS (batched, one after another, and FP64 one after another)."""
+    # the 2-body members: 6 coupling layers of width 128 (8 dims); rho rho: 8 of width 256
+    shapes = [(6, 128), (6, 128), (8, 256)]
+    flows, trs = [], []
+    for k, (e, (layers, hidden)) in enumerate(zip(es, shapes)):
+        f = g.Flow(e, layers=layers, hidden=hidden, seed=5 + k, mix_uniform=0.05)
+        nt = max(16384, int(e.vp.ncall) // 16384 * 16384)
+        trs.append(f.train(n_train=nt, batch=16384, epochs=3, rounds=3, lr=1e-3, prec=g.MIXED,
+                           seed_stream=7 + k))
+        flows.append(f)
+    for e in es:
+        e.vegas_clear()
+        e.set_maxweight(0.0)
+    bf = g.Batch(es)
+    for k, f in enumerate(flows):
+        bf.set_flow(k, f)
+    bf.iteration(mode=0, refine=False, iter_id=70)  # graph capture + warm-up
+    for e in es:
+        e.vegas_clear()
+        e.set_maxweight(0.0)
+    t0 = torch.cuda.Event(enable_timing=True)
+    t1 = torch.cuda.Event(enable_timing=True)
+    torch.cuda.synchronize()
+    t0.record()
+    for it in range(steps):
+        res_f, _ = bf.iteration(mode=1, refine=False, iter_id=300 + it)
+    t1.record()
+    torch.cuda.synchronize()
+    ms_f = t0.elapsed_time(t1) / steps
+    bf.close()
+    # plain FP64 VEGAS, one member after another: the evaluation rate of each member on 1/16
+    # of its points (same adapted grid; eps_unw as the mixed-precision plain passes)
+    fp64_s = 0.0
+    for e in es:
+        grid = e.vegas_grid()
+        vp = e.vp
+        n16 = max(128, int(vp.ncall) // 16 // 128 * 128)
+        vq = _abi.VegasParams()
+        ctypes_copy(vq, vp)
+        vq.ncall, vq.prec = n16, g.FP64
+        e.vegas_init(vq)
+        e.vegas_set_grid(grid)
+        torch.cuda.synchronize()
+        t0.record()
+        e.vegas_iteration(mode=1, refine=False, iter_id=900)
+        t1.record()
+        torch.cuda.synchronize()
+        fp64_s += t0.elapsed_time(t1) * 1e-3 * (int(vp.ncall) / n16)
+        e.vp = vp
+    for f in flows:
+        f.close()
+    u_flow = _unweighted_per_s(es, res_f, ms_f)
+    u_batch = _unweighted_per_s(es, res_plain, ms_b)
+    u_sep = _unweighted_per_s(es, res_plain, ms_s)
+    u_fp64 = _unweighted_per_s(es, res_plain, fp64_s * 1e3)
+    return {"flow": "per member, RQ splines 16 bins, BF16 (tcgen05), 5% uniform mixture, trained "
+                    "untimed: 2-body members 6 coupling layers of MLP 128 x 2 (8 dims), rho rho 8 "
+                    "coupling layers of MLP 256 x 2 (14 dims)",
+            "train_ms": [t.train_ms for t in trs], "train_steps": [t.steps for t in trs],
+            "rel_var": {"plain": [t.rel_var_start for t in trs],
+                        "flow": [t.rel_var_flow for t in trs]},
+            "eps_unw_plain": [r.sigma / r.maxf if r.maxf > 0 else None for r in res_plain],
+            "ms_per_step_flow_batched": ms_f, "ms_per_step_fp64_separate": fp64_s * 1e3,
+            "unweighted_per_s": {"flow_batched": u_flow, "plain_batched": u_batch,
+                                 "plain_separate": u_sep, "plain_fp64_separate": u_fp64},
+            "flow_batched_over_plain_separate": u_flow / u_sep,
+            "flow_batched_over_plain_fp64": u_flow / u_fp64,
+            "eps_unw_flow": [r.sigma / r.maxf if r.maxf > 0 else None for r in res_f],
+            "sigma_flow_vs_plain_pull": [
+                (rf.sigma - rp.sigma) / (rf.sigma_err ** 2 + rp.sigma_err ** 2) ** 0.5
+                for rf, rp in zip(res_f, res_plain)]}
+
+
+def ctypes_copy(dst, src):
+    import ctypes
+    ctypes.memmove(ctypes.byref(dst), ctypes.byref(src), ctypes.sizeof(src))
 
 
 def main():

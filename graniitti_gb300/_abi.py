@@ -178,6 +178,7 @@ SIGNATURES = {
     "grn_batch_create": (c_int32, [c_void_p, c_int32, c_void_p]),
     "grn_batch_destroy": (c_int32, [c_void_p]),
     "grn_batch_iteration": (c_int32, [c_void_p, c_int32, c_int32, c_uint32, c_void_p, c_void_p]),
+    "grn_batch_set_flow": (c_int32, [c_void_p, c_int32, c_void_p]),
     "grn_get_tuning": (c_int32, [c_void_p, c_void_p]),
     "grn_set_tuning": (c_int32, [c_void_p, c_void_p]),
     "grn_autotune": (c_int32, [c_void_p, c_int64, c_void_p]),

@@ -167,6 +167,7 @@ struct grn_flow {
   DevBuf      d_gpart, d_lpart;                // per-block gradient / loss slices
   DevBuf      d_tu, d_tlq, d_tcoef;          // training set
   DevBuf      d_fu, d_flq;                   // points of the last flow pass
+  int         in_batches = 0;                // batches that draw a member's points from it
 };
 
 namespace {
@@ -1171,7 +1172,16 @@ struct grn_batch {
   cudaEvent_t               ev0 = nullptr, ev1 = nullptr;
   double                    last_ms = 0.0;
   bool                      registered = false;  // counted in the engines' in_batches
+  std::vector<grn_flow *>   flows;               // per member: proposal of its points (or null)
 };
+
+extern "C" {
+static grn_status flow_points(grn_flow *f, bool from_flow, uint32_t stream_id, int64_t n,
+                              DevBuf &dst_u, DevBuf &dst_lq);
+}
+namespace {
+grn_status flow_check_err(grn_flow *f);
+}
 
 namespace {
 
@@ -1324,7 +1334,20 @@ grn_status grn_batch_create(grn_engine *const *engines, int32_t n, grn_batch **o
   }
   for (grn_engine *e : b->eng) e->in_batches += 1;
   b->registered = true;
+  b->flows.assign(n, nullptr);
   *out = b;
+  return GRN_OK;
+}
+
+grn_status grn_batch_set_flow(grn_batch *b, int32_t index, grn_flow *f) {
+  if (!b || index < 0 || index >= static_cast<int32_t>(b->eng.size()))
+    return fail(GRN_ERR_INVALID, "bad batch member");
+  if (f && f->e != b->eng[index])
+    return fail(GRN_ERR_INVALID, "the flow belongs to another engine");
+  if (b->flows[index]) b->flows[index]->in_batches -= 1;
+  b->flows[index] = f;
+  if (f) f->in_batches += 1;
+  b->h_procs[index].fu = b->h_procs[index].flq = nullptr;
   return GRN_OK;
 }
 
@@ -1344,6 +1367,8 @@ grn_status grn_batch_destroy(grn_batch *b) {
   if (b->stream) cudaStreamDestroy(b->stream);
   if (b->registered)
     for (grn_engine *e : b->eng) e->in_batches -= 1;
+  for (grn_flow *f : b->flows)
+    if (f) f->in_batches -= 1;
   delete b;
   return GRN_OK;
 }
@@ -1353,6 +1378,17 @@ grn_status grn_batch_iteration(grn_batch *b, int32_t mode, int32_t refine, uint3
   if (!b) return fail(GRN_ERR_INVALID, "null batch");
   GRN_CUDA(cudaSetDevice(b->device));
   const int np = static_cast<int>(b->eng.size());
+  // members with a flow proposal: their points (as grn_flow_iteration draws them) on the
+  // engines' streams, all before the pass
+  for (int p = 0; p < np; ++p) {
+    grn_flow *f = b->flows[p];
+    if (!f) continue;
+    if (!f->e) return fail(GRN_ERR_STATE, "a member's flow lost its engine");
+    const grn_status st = flow_points(f, true, iter_id, b->eng[p]->ncall, f->d_fu, f->d_flq);
+    if (st != GRN_OK) return st;
+    b->h_procs[p].fu  = f->d_fu.as<float>();
+    b->h_procs[p].flq = f->d_flq.as<float>();
+  }
   for (int p = 0; p < np; ++p) {
     grn_engine *e = b->eng[p];
     if (e->ncall != b->h_procs[p].ncall || e->d_f.as<double>() != b->h_procs[p].f_out)
@@ -1361,6 +1397,11 @@ grn_status grn_batch_iteration(grn_batch *b, int32_t mode, int32_t refine, uint3
     b->h_procs[p].stream    = iter_id;
     b->h_procs[p].track_max = mode != 0;
   }
+  for (int p = 0; p < np; ++p)
+    if (b->flows[p]) {
+      const grn_status st = flow_check_err(b->flows[p]);
+      if (st != GRN_OK) return st;
+    }
   const int r = refine ? 1 : 0, tm = mode != 0 ? 1 : 0;
   if (!b->exec[2 * r + tm]) {
     const grn_status st = batch_capture(b, r, tm);
@@ -1380,7 +1421,7 @@ grn_status grn_batch_iteration(grn_batch *b, int32_t mode, int32_t refine, uint3
     e->last_stream = iter_id;
     e->last_ncall  = e->ncall;
     e->have_last   = true;
-    e->last_fu     = nullptr;
+    e->last_fu     = b->flows[p] ? b->flows[p]->d_fu.as<float>() : nullptr;
     grn_vegas_result res{};
     const grn_status s2 = vegas_accumulate(e, mode, e->iters_since_clear++, &res);
     if (results) results[p] = res;
@@ -1733,6 +1774,7 @@ grn_status grn_flow_create(grn_engine *e, const grn_flow_params *p, grn_flow **o
 
 grn_status grn_flow_destroy(grn_flow *f) {
   if (!f) return GRN_OK;
+  if (f->in_batches > 0) return fail(GRN_ERR_STATE, "the flow serves a batch: destroy it first");
   cudaSetDevice(f->device);
   if (f->e) {
     auto &v = f->e->flows;

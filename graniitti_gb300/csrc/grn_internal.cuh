@@ -149,6 +149,7 @@ struct BatchProc {
   uint64_t           *l_bins, *l_bins_hi;  // bin indices of dimensions 0..7, 8..15
   float              *rf;
   double             *rd;
+  const float        *fu, *flq;    // flow points of the pass and their log density (or null)
   int                 blk0, blk1;  // stage-A blocks of this process: [blk0, blk1)
 };
 // The process table of a batch, copied into constant memory (stream-ordered).

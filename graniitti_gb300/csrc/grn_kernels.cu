@@ -1299,7 +1299,7 @@ __global__ void __launch_bounds__(kVegasThreads, 3) k_batch_born(int np) {
   const BatchProc &q = c_procs[p];
   born_pass_body<MAXD>(q.A, q.xmat, q.bins, q.dim, q.ncall, q.seed, q.stream, q.track_max,
                        q.f_out, q.f2mat, q.acc, q.l_idx, q.l_x, q.l_vw, q.l_bins, q.l_bins_hi,
-                       q.ncall, q.rf, q.rd, nullptr, nullptr, dsm,
+                       q.ncall, q.rf, q.rd, q.fu, q.flq, dsm,
                        static_cast<int>(blockIdx.x) - q.blk0, q.blk1 - q.blk0);
 }
 

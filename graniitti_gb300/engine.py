@@ -315,6 +315,10 @@ class Batch:
         _abi.check(self.lib.grn_batch_create(arr, len(engines), ctypes.byref(h)))
         self.h = h
 
+    def set_flow(self, index, flow):
+        """Member `index` draws its points from `flow` (None: Philox points)."""
+        _abi.check(self.lib.grn_batch_set_flow(self.h, index, flow.h if flow else None))
+
     def iteration(self, mode=1, refine=True, iter_id=1):
         res = (_abi.VegasResult * len(self.engines))()
         ms = ctypes.c_double()

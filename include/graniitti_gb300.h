@@ -513,6 +513,11 @@ grn_status grn_batch_destroy(grn_batch *b);
  * whole pass (may be NULL). */
 grn_status grn_batch_iteration(grn_batch *b, int32_t mode, int32_t refine, uint32_t iter_id,
                                grn_vegas_result *results, double *device_ms);
+/* Member `index` draws its points from the flow f (created on that member's engine; NULL:
+ * Philox points again): each grn_batch_iteration first samples them on the engine's stream
+ * exactly as grn_flow_iteration with the same iter_id, then the member's weights are
+ * f = W vw / q. A flow that serves a batch cannot be destroyed. */
+grn_status grn_batch_set_flow(grn_batch *b, int32_t index, grn_flow *f);
 
 /* ------------------------------------------------------------------------ */
 /* Launch configuration and autotuner (no counterpart in the reference)       */

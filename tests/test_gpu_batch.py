@@ -125,3 +125,50 @@ def test_batched_mixed_multiplicity_equals_separate(gpu):
     b.close()
     for e in es:
         e.close()
+
+
+def test_batched_flow_member_equals_flow_iteration(gpu):
+    """A member with a flow proposal (rho rho -> 4 pi, 14 dimensions, 8 layers of width 256)
+    gets in the batched pass exactly the pass grn_flow_iteration gives it alone; the flow
+    cannot be destroyed while the batch holds it."""
+    import graniitti_gb300 as g
+    from graniitti_gb300 import _abi, card
+    from oracle import flow_ref as F
+    c = card.read_card(CARD_SCR)
+    procs = ["PP[CON]<C> -> pi+ pi-",
+             "PP[CONTENSOR]<F> -> rho(770)0 > {pi+ pi-} rho(770)0 > {pi+ pi-}"]
+    es = []
+    for k, proc in enumerate(procs):
+        e = g.Engine(card.build_params(c, proc), 0)
+        e.eikonal_build(512, 2000)
+        e.set_tuning(loop_pair=1)  # the batched record-mode loop pairs events
+        vp = _abi.VegasParams()
+        vp.bins, vp.iter, vp.ncall, vp.lambda_ = 128, 5, 1 << 15, 1.5
+        vp.chi2max, vp.precision, vp.burnin_iter, vp.prec, vp.seed = 10.0, 1e-3, 3, g.MIXED, 41 + k
+        e.vegas_init(vp)
+        es.append(e)
+    f = g.Flow(es[1], layers=8, hidden=256, seed=3, mix_uniform=0.1)
+    th = F.init_params(dim=14, layers=8, hidden=256, seed=3)
+    rng = np.random.default_rng(4)
+    for p in F.unpack(th, 14, 8, 256, 16):
+        p["W3"] += rng.normal(0, 0.02, p["W3"].shape)
+        p["b3"] += rng.normal(0, 0.2, p["b3"].shape)
+    f.set_params(th.astype(np.float32))
+    grids = [e.vegas_grid() for e in es]
+    sep = [es[0].vegas_iteration(mode=1, refine=False, iter_id=5), f.iteration(mode=1, iter_id=5)]
+    for e, x in zip(es, grids):
+        e.vegas_clear()
+        e.vegas_set_grid(x)
+    b = g.Batch(es)
+    b.set_flow(1, f)
+    with pytest.raises(Exception):
+        _abi.check(f.lib.grn_flow_destroy(f.h))
+    res, ms = b.iteration(mode=1, refine=False, iter_id=5)
+    for r0, r1 in zip(sep, res):
+        assert r1.I_this == pytest.approx(r0.I_this, rel=1e-14)
+        assert r1.maxf == pytest.approx(r0.maxf, rel=1e-14)
+    print("batched pass with a flow member: %.2f ms; I = %s" % (ms, [r.I_this for r in res]))
+    b.close()
+    f.close()
+    for e in es:
+        e.close()
