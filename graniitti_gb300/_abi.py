@@ -34,6 +34,7 @@ GRN_FLAG_AMPLITUDE_OK = 8
 GRN_PROC_REGGE_CON = 1
 GRN_PROC_TENSOR_CON = 2
 GRN_PROC_TENSOR_RES = 3
+GRN_PROC_TENSOR_RESCON = 4
 GRN_MAX_RESONANCES = 4
 GRN_PS_CONTINUUM = 1
 GRN_PS_FACTORIZED = 2

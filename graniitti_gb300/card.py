@@ -169,18 +169,20 @@ def build_params(card, process=None, tune=None):
     elif any(f in PARTICLES and PARTICLES[f][2] > 1e-6 for f in finals):
         # the reference draws Breit-Wigner masses for them (MProcess::GetOffShellMass)
         raise UnsupportedProcess("unstable central particles need their decays: a > {c d}")
-    if not (istate == "PP" and channel in ("CON", "CONTENSOR", "RESTENSOR") and
+    if not (istate == "PP" and channel in ("CON", "CONTENSOR", "RESTENSOR", "RES+CONTENSOR") and
             cls in ("C", "F") and len(finals) == 2):
         raise UnsupportedProcess(
-            "engine implements PP[CON|CONTENSOR|RESTENSOR]<C|F> -> 2-body, got %r" % proc)
+            "engine implements PP[CON|CONTENSOR|RESTENSOR|RES+CONTENSOR]<C|F> -> 2-body, got %r"
+            % proc)
     vec = all(SPIN.get(f, 0) == 1 for f in finals)
     if channel == "CONTENSOR" and not (
             all(f in ("pi+", "pi-", "K+", "K-", "pi0") for f in finals) or
             (vec and finals[0] == finals[1] and finals[0] in VECTOR_COUPLING)):
         raise UnsupportedProcess("CONTENSOR is implemented for pseudoscalar pairs (2xS) and "
                                  "rho rho / phi phi (2xV)")
-    if channel == "RESTENSOR" and sorted(finals) not in (["pi+", "pi-"], ["K+", "K-"]):
-        raise UnsupportedProcess("RESTENSOR is implemented for pi+ pi- and K+ K- decays")
+    if channel in ("RESTENSOR", "RES+CONTENSOR") and \
+            sorted(finals) not in (["pi+", "pi-"], ["K+", "K-"]):
+        raise UnsupportedProcess("%s is implemented for pi+ pi- and K+ K- decays" % channel)
     if int(pp.get("NSTARS", 0)) != 0:
         raise UnsupportedProcess("forward excitation (NSTARS > 0) is not implemented")
     if pp["BEAM"] != ["p+", "p+"]:
@@ -194,7 +196,8 @@ def build_params(card, process=None, tune=None):
     P.sqrt_s = 2.0 * E1
     P.m_beam = mb
     P.process = {"CON": _abi.GRN_PROC_REGGE_CON, "CONTENSOR": _abi.GRN_PROC_TENSOR_CON,
-                 "RESTENSOR": _abi.GRN_PROC_TENSOR_RES}[channel]
+                 "RESTENSOR": _abi.GRN_PROC_TENSOR_RES,
+                 "RES+CONTENSOR": _abi.GRN_PROC_TENSOR_RESCON}[channel]
     P.phase_space = _abi.GRN_PS_CONTINUUM if cls == "C" else _abi.GRN_PS_FACTORIZED
     P.n_central = 2
     P.screening = 1 if pp.get("POMLOOP", False) else 0
@@ -292,8 +295,8 @@ def build_params(card, process=None, tune=None):
         # pomeron-vector-vector couplings of rho or phi (MTensorPomeron.cc:811-823)
         P.tensor.gPvv[0], P.tensor.gPvv[1] = tp[VECTOR_COUPLING[finals[0]]]
 
-    if channel == "RESTENSOR":
-        set_resonances(P, pp, proc, tune, finals)
+    if channel in ("RESTENSOR", "RES+CONTENSOR"):
+        set_resonances(P, pp, proc, tune, finals, allow_none=channel == "RES+CONTENSOR")
 
     # Loop numerics: defaults 15 x 12 moved by 3*ND (MEikonal.h:40-57), tables
     # 10000 intervals (modeldata/NUMERICS.json).
@@ -317,12 +320,16 @@ def resonance_list(pp, proc):
     return names
 
 
-def set_resonances(P, pp, proc, tune, finals):
+def set_resonances(P, pp, proc, tune, finals, allow_none=False):
     """Resonance parameters (PARAM_RES), '@R[name]{M:.., W:.., gN:..}' overrides
     (src/MGraniitti.cc:480-575) and the decay couplings (MProcess::SetupBranching,
-    src/MProcess.cc:471-520), in the order the reference applies them."""
+    src/MProcess.cc:471-520), in the order the reference applies them. With allow_none
+    (RES+CONTENSOR) an empty list leaves the continuum alone (MSubProc.h:333)."""
     table = RESONANCES.get(tune, {})
     names = resonance_list(pp, proc)
+    if not names and allow_none:
+        P.n_res = 0
+        return
     if not names:
         raise ValueError("RESTENSOR needs resonances: PROCESSPARAM RES or @RES{name:1}")
     if len(names) > _abi.GRN_MAX_RESONANCES:

@@ -174,17 +174,18 @@ namespace {
 
 grn_status derive_consts(const grn_process_params &P, grn::Consts &K) {
   using namespace grn;
+  const bool rescon = P.process == GRN_PROC_TENSOR_RESCON;
   if ((P.process != GRN_PROC_REGGE_CON && P.process != GRN_PROC_TENSOR_CON &&
-       P.process != GRN_PROC_TENSOR_RES) ||
+       P.process != GRN_PROC_TENSOR_RES && !rescon) ||
       (P.phase_space != GRN_PS_CONTINUUM && P.phase_space != GRN_PS_FACTORIZED))
-    return fail(GRN_ERR_UNSUPPORTED,
-                "only PP[CON|CONTENSOR|RESTENSOR]<C|F> 2-body processes are implemented");
-  if (P.process == GRN_PROC_TENSOR_CON &&
+    return fail(GRN_ERR_UNSUPPORTED, "only PP[CON|CONTENSOR|RESTENSOR|RES+CONTENSOR]<C|F> "
+                                     "2-body processes are implemented");
+  if ((P.process == GRN_PROC_TENSOR_CON || rescon) &&
       !(P.tensor.ap_P > 0 && P.tensor.gPNN > 0 && P.tensor.gPps > 0))
     return fail(GRN_ERR_INVALID, "tensor-pomeron parameters are not set");
   K.n_res     = 0;
   K.res_smask = 0;
-  if (P.process == GRN_PROC_TENSOR_RES) {
+  if (P.process == GRN_PROC_TENSOR_RES || (rescon && P.n_res > 0)) {
     if (!(P.tensor.ap_P > 0 && P.tensor.gPNN > 0))
       return fail(GRN_ERR_INVALID, "tensor-pomeron parameters are not set");
     if (P.n_res < 1 || P.n_res > GRN_MAX_RESONANCES)
@@ -228,10 +229,12 @@ grn_status derive_consts(const grn_process_params &P, grn::Consts &K) {
     return fail(GRN_ERR_UNSUPPORTED, "central decays: none or two-body cascades of both");
   if (P.central_spin != 0 && P.central_spin != 1)
     return fail(GRN_ERR_UNSUPPORTED, "central particles of spin 0 or 1");
+  if (rescon && (P.n_res < 0 || P.n_res > GRN_MAX_RESONANCES))
+    return fail(GRN_ERR_INVALID, "RES+CONTENSOR takes 0 to 4 resonances");
   if (P.n_decay == 2) {
     if (P.phase_space != GRN_PS_FACTORIZED)
       return fail(GRN_ERR_UNSUPPORTED, "decay cascades are implemented in the <F> class");
-    if (P.process == GRN_PROC_TENSOR_RES)
+    if (P.process == GRN_PROC_TENSOR_RES || rescon)
       return fail(GRN_ERR_UNSUPPORTED, "RESTENSOR decays directly to two pseudoscalars");
     for (int k = 0; k < 4; ++k)
       if (!(P.m_daughter[k] >= 0))
@@ -248,7 +251,7 @@ grn_status derive_consts(const grn_process_params &P, grn::Consts &K) {
     if (P.n_decay != 2)
       return fail(GRN_ERR_UNSUPPORTED, "vector-meson pairs need their two-body decays");
   }
-  if (P.process == GRN_PROC_TENSOR_RES && P.central_spin != 0)
+  if ((P.process == GRN_PROC_TENSOR_RES || rescon) && P.central_spin != 0)
     return fail(GRN_ERR_UNSUPPORTED, "RESTENSOR decays to pseudoscalars");
   if (!(P.sqrt_s > 2 * P.m_beam)) return fail(GRN_ERR_INVALID, "sqrt_s below threshold");
   if (!(P.gcuts.fpt_max > 0) || !(P.gcuts.kt_max > P.gcuts.kt_min) ||

@@ -1028,6 +1028,9 @@ GRN_HD bool loop_point_amp(const grn_process_params &P, const Consts &K, const L
     A = tensor_me4_2xs<T>(P, K, kk);
   } else if (P.process == GRN_PROC_TENSOR_RES) {
     A = tensor_me3<T>(P, K, kk, e.res);
+  } else if (P.process == GRN_PROC_TENSOR_RESCON) {
+    A = tensor_me4_2xs<T>(P, K, kk);
+    if (K.n_res > 0) A = cadd(A, tensor_me3<T>(P, K, kk, e.res));
   } else {
     A = regge_me4<T>(P, K, kk.t1, kk.t2, log(kk.s13), log(kk.s14), log(kk.s23), log(kk.s24),
                      kk.that, kk.uhat);
@@ -1337,16 +1340,22 @@ GRN_HD void make_loop_event(const Consts &K, const Born &b, LoopEvent<T> &e) {
 
 // Tree-level amplitude of the configured process from the Born kinematics (FP64).
 GRN_HD cx<double> born_amp(const grn_process_params &P, const Consts &K, const Born &b) {
-  if (P.process == GRN_PROC_TENSOR_CON || P.process == GRN_PROC_TENSOR_RES) {
+  if (P.process == GRN_PROC_TENSOR_CON || P.process == GRN_PROC_TENSOR_RES ||
+      P.process == GRN_PROC_TENSOR_RESCON) {
     LCKin<double> k{b.p1p, b.p1m, b.p1x, b.p1y, b.p2p, b.p2m, b.p2x,  b.p2y, b.p3p,
                     b.p3m, b.p3x, b.p3y, b.p4p, b.p4m, b.p4x, b.p4y,  K.L,   K.eps,
                     K.mp2, b.t1,  b.t2,  b.s13, b.s14, b.s23, b.s24, b.that, b.uhat};
     if (P.process == GRN_PROC_TENSOR_CON) return tensor_me4_2xs<double>(P, K, k);
+    // RES+CONTENSOR: the 2xS continuum and the resonances summed coherently (MSubProc.h:319-351;
+    // all four non-flip proton helicity amplitudes of each are equal)
+    const cx<double> Ac = P.process == GRN_PROC_TENSOR_RESCON ? tensor_me4_2xs<double>(P, K, k)
+                                                               : cx<double>{0.0, 0.0};
+    if (K.n_res == 0) return Ac;
     q_lightcone<double>(b.x1, b.pt1sq, K.mp2, K.L, k.q1p, k.q1m);
     q_lightcone<double>(b.x2, b.pt2sq, K.mp2, K.L, k.q2m, k.q2p);
     const ResVec<double> v =
         res_vectors<double>(K, b.p3p, b.p3m, b.p3x, b.p3y, b.p4p, b.p4m, b.p4x, b.p4y);
-    return tensor_me3<double>(P, K, k, resonance_sums(K, b.m2, v));
+    return cadd(Ac, tensor_me3<double>(P, K, k, resonance_sums(K, b.m2, v)));
   }
   return regge_me4<double>(P, K, b.t1, b.t2, log(b.s13), log(b.s14), log(b.s23), log(b.s24),
                            b.that, b.uhat);

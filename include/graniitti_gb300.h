@@ -54,10 +54,13 @@ enum {
   GRN_PROC_REGGE_CON  = 1, /* "PP[CON]<C|F> -> a b", 2-body, MRegge::ME4 (MSubProc.h:361-380) */
   GRN_PROC_TENSOR_CON = 2, /* "PP[CONTENSOR]<C|F> -> a b", 2 pseudoscalars, tensor-pomeron
                               MTensorPomeron::ME4 "2xS" (MSubProc.h:288-300) */
-  GRN_PROC_TENSOR_RES = 3  /* "PP[RESTENSOR]<F|C> -> a b", 2 pseudoscalars: coherent sum of
+  GRN_PROC_TENSOR_RES = 3, /* "PP[RESTENSOR]<F|C> -> a b", 2 pseudoscalars: coherent sum of
                               tensor-pomeron resonances, MTensorPomeron::ME3 (MSubProc.h:
                               278-285; src/MTensorPomeron.cc:164-565), J = 0 (P = +1) and
                               J = 2 with the pseudoscalar-pair decay */
+  GRN_PROC_TENSOR_RESCON = 4 /* "PP[RES+CONTENSOR]<F|C> -> a b", 2 pseudoscalars: the 2xS
+                              continuum and the resonances (0..4) summed coherently
+                              (MSubProc.h:319-351) */
 };
 
 /* Phase-space classes (MProcess subclasses). */

@@ -1069,8 +1069,13 @@ double screened_amp2(const Setup &S, const Event &born, const cplx *A0, int nh) 
   return amp2;
 }
 
+// RES+CONTENSOR (MSubProc.h:319-351): the continuum's and the resonances' helicity amplitudes
+// are added per proton configuration; with the high-energy proton vertex all four are equal,
+// so the sum of one configuration carries |M|^2.
 cplx bare_amp(const Setup &S, const Event &ev) {
   if (S.p.process == GRN_PROC_TENSOR_RES) return tensor_me3(S, ev);
+  if (S.p.process == GRN_PROC_TENSOR_RESCON)
+    return tensor_me4_2xs(S, ev) + (S.p.n_res > 0 ? tensor_me3(S, ev) : cplx(0.0));
   return S.p.process == GRN_PROC_TENSOR_CON ? tensor_me4_2xs(S, ev) : regge_me4(S, ev);
 }
 

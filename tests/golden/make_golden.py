@@ -8,7 +8,8 @@ reference does not. Steps:
   3. build the eikonal tables with the reference's MEikonal::S3Constructor
   4. run the reference VEGAS integration for the cross section
 
-Usage: python tests/golden/make_golden.py [--ref /root/reference] [--only resonances|cascades]
+Usage: python tests/golden/make_golden.py [--ref /root/reference]
+                                          [--only resonances|cascades|rescon]
 """
 import argparse
 import json
@@ -113,6 +114,30 @@ def resonance_fixtures():
                 os.path.basename(CARD_RES))
 
 
+def rescon_fixtures():
+    """Tensor-pomeron resonances + 2xS continuum (PROC_14, RES+CONTENSOR): the coherent sum
+    exercises the relative phase of the two amplitudes (<F> and <C>, K+ K-, screened)."""
+    REPLAY_F = ["--replay", "h,h,6,7"]
+    cases = [
+        ("rcf_tree_weights.npz", 91, 1024, CARD_RES,
+         "PP[RES+CONTENSOR]<F> -> pi+ pi- @RES{f0_980:1, f2_1270:1}", REPLAY_F, 6),
+        ("rcc_tree_weights.npz", 92, 1024, CARD_RES,
+         "PP[RES+CONTENSOR]<C> -> pi+ pi- @RES{f0_980:1, f2_1270:1, f0_1500:1}", [], 8),
+        ("rck_tree_weights.npz", 93, 512, CARD_RES,
+         "PP[RES+CONTENSOR]<F> -> K+ K- @RES{f0_980:1, f2_1270:1, f2_1525:1}", REPLAY_F, 6),
+    ]
+    for name, seed, n, card, proc, extra, dim in cases:
+        u = philox_np.uniforms(seed, n, 8)
+        r = run_weights(card, u, extra, proc=proc, dim=dim)
+        save(name, seed=seed, u=u, card=os.path.basename(card), proc=proc, **r)
+    proc = "PP[RES+CONTENSOR]<F> -> pi+ pi- @RES{f0_980:1, f2_1270:1}"
+    u = philox_np.uniforms(94, 96, 8)
+    r = run_weights(CARD_RES_SCR, u, REPLAY_F + ["--nbt", "1024", "--nkt2", "10000"], proc=proc,
+                    dim=6)
+    save("rcf_screened_15x12_weights.npz", seed=94, u=u, card=os.path.basename(CARD_RES_SCR),
+         proc=proc, n_bt=1024, n_kt2=10000, loop_kt=15, loop_phi=12, loop_ktmax=1.75, **r)
+
+
 def write_sigma(name, out, proc, card):
     line = [l for l in out.splitlines() if l.startswith("RESULT")][-1]
     sigma, err = map(float, line.split()[1:3])
@@ -156,10 +181,14 @@ def cascade_fixtures():
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--ref", default="/root/reference")
-    ap.add_argument("--only", choices=["all", "resonances", "cascades"], default="all")
+    ap.add_argument("--only", choices=["all", "resonances", "cascades", "rescon"], default="all")
     a = ap.parse_args()
     subprocess.check_call(["make", "-s", "-C", os.path.join(REPO, "oracle", "refbuild"), "-j8",
                            "REF=" + a.ref])
+    if a.only in ("all", "rescon"):
+        rescon_fixtures()
+    if a.only == "rescon":
+        return
     if a.only in ("all", "cascades"):
         cascade_fixtures()
     if a.only == "cascades":

@@ -84,6 +84,21 @@ def test_resonance_params_and_decay_couplings(lib_built):
         lib.grn_tensor_decay_coupling(3, 2.6, 0.1, 0.14, 1.0)  # NaN
 
 
+def test_resonances_plus_continuum_params(lib_built):
+    from conftest import GOLDEN
+    import os
+    from graniitti_gb300 import _abi
+    c = card.read_card(os.path.join(GOLDEN, "cards", "pp_res_pipi.json"))
+    P = card.build_params(c, "PP[RES+CONTENSOR]<F> -> pi+ pi- @RES{f0_980:1, f2_1270:1}")
+    assert P.process == _abi.GRN_PROC_TENSOR_RESCON and P.n_res == 2
+    assert P.tensor.gPps == 1.76 and round(P.res[1].g_decay, 3) == 9.285
+    c["PROCESSPARAM"]["RES"] = []
+    P = card.build_params(c, "PP[RES+CONTENSOR]<C> -> K+ K-")  # the continuum alone
+    assert P.n_res == 0 and P.tensor.gPps == 1.54
+    with pytest.raises(ValueError):
+        card.build_params(c, "PP[RESTENSOR]<C> -> K+ K-")
+
+
 @pytest.mark.parametrize("proc", [
     "PP[RESTENSOR]<F> -> pi+ pi- @RES{rho_770:1}",       # no pseudoscalar-pair resonance
     "PP[RESTENSOR]<F> -> pi0 pi0 @RES{f2_1270:1}",

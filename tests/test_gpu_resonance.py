@@ -44,7 +44,8 @@ def _rel(w, wr):
 @pytest.mark.parametrize("name", ["rf_tree_weights.npz", "rf_mix_tree_weights.npz",
                                   "rf_kk_tree_weights.npz", "rc_tree_weights.npz",
                                   "rf_f2_1525_tree_weights.npz"] +
-                         ["rf_s%d_tree_weights.npz" % j for j in range(1, 7)])
+                         ["rf_s%d_tree_weights.npz" % j for j in range(1, 7)] +
+                         ["rcf_tree_weights.npz", "rcc_tree_weights.npz", "rck_tree_weights.npz"])
 def test_resonance_tree_vs_reference(gpu, name):
     import graniitti_gb300 as g
     gl = _load(name)
@@ -64,9 +65,11 @@ def test_resonance_tree_vs_reference(gpu, name):
     assert np.array_equal(wm, w)
 
 
-def test_resonance_screened_vs_reference(gpu):
+@pytest.mark.parametrize("name", ["rf_screened_15x12_weights.npz",
+                                  "rcf_screened_15x12_weights.npz"])
+def test_resonance_screened_vs_reference(gpu, name):
     import graniitti_gb300 as g
-    gl = _load("rf_screened_15x12_weights.npz")
+    gl = _load(name)
     t = _load("eikonal_nbt1024_nkt10000.npz")
     P = _params(gl)
     assert P.screening == 1

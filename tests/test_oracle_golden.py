@@ -168,7 +168,8 @@ RES_TOL = 5e-9
 @pytest.mark.parametrize("name", ["rf_tree_weights.npz", "rf_mix_tree_weights.npz",
                                   "rf_kk_tree_weights.npz", "rc_tree_weights.npz",
                                   "rf_f2_1525_tree_weights.npz"] +
-                         ["rf_s%d_tree_weights.npz" % j for j in range(1, 7)])
+                         ["rf_s%d_tree_weights.npz" % j for j in range(1, 7)] +
+                         ["rcf_tree_weights.npz", "rcc_tree_weights.npz", "rck_tree_weights.npz"])
 def test_tensor_resonance_tree_weights(lib_built, name):
     g = _load(name)
     w, fl = orc.weights(_params_res(g), g["u"])
@@ -176,8 +177,10 @@ def test_tensor_resonance_tree_weights(lib_built, name):
     assert np.median(rel) < 1e-10
 
 
-def test_tensor_resonance_screened_weights(lib_built):
-    g = _load("rf_screened_15x12_weights.npz")
+@pytest.mark.parametrize("name", ["rf_screened_15x12_weights.npz",
+                                  "rcf_screened_15x12_weights.npz"])
+def test_tensor_resonance_screened_weights(lib_built, name):
+    g = _load(name)
     t = _load("eikonal_nbt1024_nkt10000.npz")
     w, fl = orc.weights(_params_res(g), g["u"], msa=t["msa"], nthreads=4)
     _check_weights(w, fl, g, tol=1e-9)
