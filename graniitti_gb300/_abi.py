@@ -35,6 +35,9 @@ GRN_PROC_REGGE_CON = 1
 GRN_PROC_TENSOR_CON = 2
 GRN_PROC_TENSOR_RES = 3
 GRN_PROC_TENSOR_RESCON = 4
+GRN_PROC_REGGE_RES = 5
+GRN_PROC_REGGE_RESCON = 6
+GRN_FRAME_CM, GRN_FRAME_HX, GRN_FRAME_CS = 0, 1, 2
 GRN_MAX_RESONANCES = 4
 GRN_PS_CONTINUUM = 1
 GRN_PS_FACTORIZED = 2
@@ -81,7 +84,9 @@ class LoopNumerics(ctypes.Structure):
 
 class Resonance(ctypes.Structure):
     _fields_ = [("J", c_int32), ("P", c_int32), ("M", c_double), ("W", c_double),
-                ("g_tensor", c_double * 7), ("g_decay", c_double)]
+                ("g_tensor", c_double * 7), ("g_decay", c_double),
+                ("g_regge", c_double * 2), ("g_ff", c_double), ("bw", c_int32),
+                ("_pad_bw", c_int32), ("rho", (c_double * 25) * 2)]
 
 
 class ProcessParams(ctypes.Structure):
@@ -93,7 +98,9 @@ class ProcessParams(ctypes.Structure):
                 ("n_res", c_int32), ("_pad_res", c_int32),
                 ("res", Resonance * GRN_MAX_RESONANCES),
                 ("n_decay", c_int32), ("central_spin", c_int32), ("width", c_double * 2),
-                ("m_daughter", c_double * 4)]
+                ("m_daughter", c_double * 4),
+                ("spin_gen", c_int32), ("spin_dec", c_int32), ("spin_frame", c_int32),
+                ("_pad_spin", c_int32), ("omega", c_double)]
 
 
 class VegasParams(ctypes.Structure):
@@ -153,6 +160,7 @@ class FlowTrainResult(ctypes.Structure):
 SIGNATURES = {
     "grn_default_params": (None, [c_void_p]),
     "grn_tensor_decay_coupling": (c_double, [c_int32, c_double, c_double, c_double, c_double]),
+    "grn_regge_decay_coupling": (c_double, [c_double, c_double, c_double, c_double]),
     "grn_create": (c_int32, [c_void_p, c_int32, c_void_p]),
     "grn_destroy": (c_int32, [c_void_p]),
     "grn_engine_stream": (c_void_p, [c_void_p]),

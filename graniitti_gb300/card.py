@@ -169,18 +169,19 @@ def build_params(card, process=None, tune=None):
     elif any(f in PARTICLES and PARTICLES[f][2] > 1e-6 for f in finals):
         # the reference draws Breit-Wigner masses for them (MProcess::GetOffShellMass)
         raise UnsupportedProcess("unstable central particles need their decays: a > {c d}")
-    if not (istate == "PP" and channel in ("CON", "CONTENSOR", "RESTENSOR", "RES+CONTENSOR") and
+    if not (istate == "PP" and channel in ("CON", "RES", "RES+CON", "CONTENSOR", "RESTENSOR",
+                                           "RES+CONTENSOR") and
             cls in ("C", "F") and len(finals) == 2):
         raise UnsupportedProcess(
-            "engine implements PP[CON|CONTENSOR|RESTENSOR|RES+CONTENSOR]<C|F> -> 2-body, got %r"
-            % proc)
+            "engine implements PP[CON|RES|RES+CON|CONTENSOR|RESTENSOR|RES+CONTENSOR]<C|F> -> "
+            "2-body, got %r" % proc)
     vec = all(SPIN.get(f, 0) == 1 for f in finals)
     if channel == "CONTENSOR" and not (
             all(f in ("pi+", "pi-", "K+", "K-", "pi0") for f in finals) or
             (vec and finals[0] == finals[1] and finals[0] in VECTOR_COUPLING)):
         raise UnsupportedProcess("CONTENSOR is implemented for pseudoscalar pairs (2xS) and "
                                  "rho rho / phi phi (2xV)")
-    if channel in ("RESTENSOR", "RES+CONTENSOR") and \
+    if channel in ("RES", "RES+CON", "RESTENSOR", "RES+CONTENSOR") and \
             sorted(finals) not in (["pi+", "pi-"], ["K+", "K-"]):
         raise UnsupportedProcess("%s is implemented for pi+ pi- and K+ K- decays" % channel)
     if int(pp.get("NSTARS", 0)) != 0:
@@ -197,7 +198,8 @@ def build_params(card, process=None, tune=None):
     P.m_beam = mb
     P.process = {"CON": _abi.GRN_PROC_REGGE_CON, "CONTENSOR": _abi.GRN_PROC_TENSOR_CON,
                  "RESTENSOR": _abi.GRN_PROC_TENSOR_RES,
-                 "RES+CONTENSOR": _abi.GRN_PROC_TENSOR_RESCON}[channel]
+                 "RES+CONTENSOR": _abi.GRN_PROC_TENSOR_RESCON,
+                 "RES": _abi.GRN_PROC_REGGE_RES, "RES+CON": _abi.GRN_PROC_REGGE_RESCON}[channel]
     P.phase_space = _abi.GRN_PS_CONTINUUM if cls == "C" else _abi.GRN_PS_FACTORIZED
     P.n_central = 2
     P.screening = 1 if pp.get("POMLOOP", False) else 0
@@ -297,6 +299,22 @@ def build_params(card, process=None, tune=None):
 
     if channel in ("RESTENSOR", "RES+CONTENSOR"):
         set_resonances(P, pp, proc, tune, finals, allow_none=channel == "RES+CONTENSOR")
+    if channel in ("RES", "RES+CON"):
+        set_resonances(P, pp, proc, tune, finals, allow_none=channel == "RES+CON", regge=True)
+    # spin correlations and frame of the Regge resonances (GENERAL.json PARAM_SPIN, then the
+    # @SPINGEN / @SPINDEC / @FRAME commands, src/MGraniitti.cc:590-593)
+    sp = dict(T.get("PARAM_SPIN", {"SPINGEN": True, "SPINDEC": True, "FRAME": "CS"}))
+    for ident, _, args in split_commands(proc):
+        if ident in ("SPINGEN", "SPINDEC"):
+            sp[ident] = args.get("_SINGLET_", "true") == "true"
+        elif ident == "FRAME":
+            sp["FRAME"] = args.get("_SINGLET_", "")
+    frames = {"CM": _abi.GRN_FRAME_CM, "HX": _abi.GRN_FRAME_HX, "CS": _abi.GRN_FRAME_CS}
+    if sp["FRAME"] not in frames:
+        raise UnsupportedProcess("spin frame %r (CM, HX and CS are implemented)" % sp["FRAME"])
+    P.spin_gen, P.spin_dec = int(bool(sp["SPINGEN"])), int(bool(sp["SPINDEC"]))
+    P.spin_frame = frames[sp["FRAME"]]
+    P.omega = float(r.get("omega", 0.5))
 
     # Loop numerics: defaults 15 x 12 moved by 3*ND (MEikonal.h:40-57), tables
     # 10000 intervals (modeldata/NUMERICS.json).
@@ -320,11 +338,13 @@ def resonance_list(pp, proc):
     return names
 
 
-def set_resonances(P, pp, proc, tune, finals, allow_none=False):
-    """Resonance parameters (PARAM_RES), '@R[name]{M:.., W:.., gN:..}' overrides
+def set_resonances(P, pp, proc, tune, finals, allow_none=False, regge=False):
+    """Resonance parameters (PARAM_RES), '@R[name]{M:.., W:.., gN:.., JZn:..}' overrides
     (src/MGraniitti.cc:480-575) and the decay couplings (MProcess::SetupBranching,
     src/MProcess.cc:471-520), in the order the reference applies them. With allow_none
-    (RES+CONTENSOR) an empty list leaves the continuum alone (MSubProc.h:333)."""
+    (RES+CONTENSOR, RES+CON) an empty list leaves the continuum alone (MSubProc.h:333).
+    regge: the Regge model's coupling g_A exp(i g_phi), form factor, Breit-Wigner form,
+    spin density matrix and decay coupling sqrt(BR W / Gamma_PS)."""
     table = RESONANCES.get(tune, {})
     names = resonance_list(pp, proc)
     if not names and allow_none:
@@ -341,12 +361,28 @@ def set_resonances(P, pp, proc, tune, finals, allow_none=False):
             raise UnsupportedProcess("resonance %s (decaying to %s) is not available"
                                      % (n, " ".join(finals)))
         res[n] = dict(table[n], g_Tensor=list(table[n]["g_Tensor"]))
+        if "rho" in table[n]:
+            res[n]["rho"] = list(table[n]["rho"])
     for ident, targets, args in split_commands(proc):
         if ident != "R":
             continue
         if len(targets) != 1 or targets[0] not in res:
             raise ValueError("@R[] needs one target among the resonances: %r" % targets)
         r = res[targets[0]]
+        # JZn: diagonal spin density entries of M = +-n, then normalised to unit trace
+        jz = {int(k[2:]): float(v) for k, v in args.items() if k.startswith("JZ") and k[2:].isdigit()}
+        if jz and r["J"] != 0:
+            J = r["J"]
+            diag = [0.0] * (2 * J + 1)
+            for n_, v in jz.items():
+                if v < 0:
+                    raise ValueError("@R[] JZ value < 0")
+                if n_ <= J:
+                    diag[J - n_] = diag[J + n_] = v
+            tr = sum(diag)
+            if not tr > 0:
+                raise ValueError("@R[] spin density with zero trace")
+            r["rho"] = [d / tr for d in diag]
         for k, v in args.items():
             if k == "M":
                 r["M"] = float(v)
@@ -366,8 +402,17 @@ def set_resonances(P, pp, proc, tune, finals, allow_none=False):
         R.J, R.P, R.M, R.W = r["J"], r["P"], r["M"], r["W"]
         for k, g in enumerate(r["g_Tensor"]):
             R.g_tensor[k] = g
-        R.g_decay = lib.grn_tensor_decay_coupling(r["J"], r["M"], r["W"], PARTICLES[finals[0]][1],
-                                                  br)
+        if regge:
+            R.g_decay = lib.grn_regge_decay_coupling(r["M"], r["W"], PARTICLES[finals[0]][1], br)
+            R.g_regge[0] = r["g_A"] * math.cos(r["g_phi"])
+            R.g_regge[1] = r["g_A"] * math.sin(r["g_phi"])
+            R.g_ff, R.bw = r["g_FF"], r["BW"]
+            if r["J"] == 2:
+                for m_, d in enumerate(r["rho"]):
+                    R.rho[0][6 * m_] = d
+        else:
+            R.g_decay = lib.grn_tensor_decay_coupling(r["J"], r["M"], r["W"],
+                                                      PARTICLES[finals[0]][1], br)
 
 
 def vegas_params(card, prec=_abi.GRN_PREC_FP64, seed=1):

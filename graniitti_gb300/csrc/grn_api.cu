@@ -175,11 +175,50 @@ namespace {
 grn_status derive_consts(const grn_process_params &P, grn::Consts &K) {
   using namespace grn;
   const bool rescon = P.process == GRN_PROC_TENSOR_RESCON;
+  const bool rr = P.process == GRN_PROC_REGGE_RES || P.process == GRN_PROC_REGGE_RESCON;
   if ((P.process != GRN_PROC_REGGE_CON && P.process != GRN_PROC_TENSOR_CON &&
-       P.process != GRN_PROC_TENSOR_RES && !rescon) ||
+       P.process != GRN_PROC_TENSOR_RES && !rescon && !rr) ||
       (P.phase_space != GRN_PS_CONTINUUM && P.phase_space != GRN_PS_FACTORIZED))
-    return fail(GRN_ERR_UNSUPPORTED, "only PP[CON|CONTENSOR|RESTENSOR|RES+CONTENSOR]<C|F> "
-                                     "2-body processes are implemented");
+    return fail(GRN_ERR_UNSUPPORTED, "only PP[CON|RES|RES+CON|CONTENSOR|RESTENSOR|RES+CONTENSOR]"
+                                     "<C|F> 2-body processes are implemented");
+  K.rr_n = 0;
+  if (rr) {
+    if (P.n_res < (P.process == GRN_PROC_REGGE_RES ? 1 : 0) || P.n_res > GRN_MAX_RESONANCES)
+      return fail(GRN_ERR_INVALID, "PP[RES] needs 1 to 4 resonances (PP[RES+CON] 0 to 4)");
+    if (P.spin_frame != GRN_FRAME_CM && P.spin_frame != GRN_FRAME_HX &&
+        P.spin_frame != GRN_FRAME_CS)
+      return fail(GRN_ERR_UNSUPPORTED, "spin frames CM, HX and CS are implemented");
+    if (!std::isfinite(P.omega)) return fail(GRN_ERR_INVALID, "flux exponent omega");
+    for (int r = 0; r < P.n_res; ++r) {
+      const grn_resonance &R = P.res[r];
+      if (!(R.M > 0) || !(R.W >= 0) || !std::isfinite(R.g_decay) || !(R.g_ff > 0))
+        return fail(GRN_ERR_INVALID, "resonance mass, width, form factor or decay coupling");
+      if (!((R.J == 0 || R.J == 2) && R.P == 1))
+        return fail(GRN_ERR_UNSUPPORTED, "Regge resonances to two pseudoscalars: J^P = 0+, 2+");
+      if (R.bw < 1 || R.bw > 4) return fail(GRN_ERR_INVALID, "Breit-Wigner form 1..4");
+      if (R.J == 2) {
+        double tr = 0.0;
+        for (int i = 0; i < 5; ++i) {
+          tr += R.rho[0][6 * i];
+          if (!(R.rho[0][6 * i] >= 0) || R.rho[1][6 * i] != 0.0)
+            return fail(GRN_ERR_INVALID, "spin density diagonal must be real and >= 0");
+          for (int j = 0; j < 5; ++j)
+            if (R.rho[0][5 * i + j] != R.rho[0][5 * j + i] ||
+                R.rho[1][5 * i + j] != -R.rho[1][5 * j + i])
+              return fail(GRN_ERR_INVALID, "spin density matrix must be Hermitian");
+        }
+        if (!(std::fabs(tr - 1.0) < 1e-6)) return fail(GRN_ERR_INVALID, "spin density trace 1");
+      }
+      K.rr_J[r]    = R.J;
+      K.rr_bw[r]   = R.bw;
+      K.rr_M[r]    = R.M;
+      K.rr_W[r]    = R.W;
+      K.rr_iff4[r] = 1.0 / (R.g_ff * R.g_ff * R.g_ff * R.g_ff);
+      K.rr_g_re[r] = R.g_regge[0] * R.g_decay;
+      K.rr_g_im[r] = R.g_regge[1] * R.g_decay;
+    }
+    K.rr_n = P.n_res;
+  }
   if ((P.process == GRN_PROC_TENSOR_CON || rescon) &&
       !(P.tensor.ap_P > 0 && P.tensor.gPNN > 0 && P.tensor.gPps > 0))
     return fail(GRN_ERR_INVALID, "tensor-pomeron parameters are not set");
@@ -234,7 +273,7 @@ grn_status derive_consts(const grn_process_params &P, grn::Consts &K) {
   if (P.n_decay == 2) {
     if (P.phase_space != GRN_PS_FACTORIZED)
       return fail(GRN_ERR_UNSUPPORTED, "decay cascades are implemented in the <F> class");
-    if (P.process == GRN_PROC_TENSOR_RES || rescon)
+    if (P.process == GRN_PROC_TENSOR_RES || rescon || rr)
       return fail(GRN_ERR_UNSUPPORTED, "RESTENSOR decays directly to two pseudoscalars");
     for (int k = 0; k < 4; ++k)
       if (!(P.m_daughter[k] >= 0))
@@ -251,8 +290,8 @@ grn_status derive_consts(const grn_process_params &P, grn::Consts &K) {
     if (P.n_decay != 2)
       return fail(GRN_ERR_UNSUPPORTED, "vector-meson pairs need their two-body decays");
   }
-  if ((P.process == GRN_PROC_TENSOR_RES || rescon) && P.central_spin != 0)
-    return fail(GRN_ERR_UNSUPPORTED, "RESTENSOR decays to pseudoscalars");
+  if ((P.process == GRN_PROC_TENSOR_RES || rescon || rr) && P.central_spin != 0)
+    return fail(GRN_ERR_UNSUPPORTED, "the resonances decay to pseudoscalars");
   if (!(P.sqrt_s > 2 * P.m_beam)) return fail(GRN_ERR_INVALID, "sqrt_s below threshold");
   if (!(P.gcuts.fpt_max > 0) || !(P.gcuts.kt_max > P.gcuts.kt_min) ||
       !(P.gcuts.rap_max > P.gcuts.rap_min))
@@ -464,6 +503,23 @@ double grn_tensor_decay_coupling(int32_t J, double M, double W, double m_daughte
     }
   }
   return g;
+}
+
+double grn_regge_decay_coupling(double M, double W, double m_daughter, double BR) {
+  // |A_decay|^2 = BR Gamma / Gamma_PS with the two-body width Gamma_PS of |A|^2 = 1, the
+  // mother mass raised by 1..3 widths while the decay is closed
+  auto ps = [&](double Mr) {
+    const double x = Mr * Mr, y = m_daughter * m_daughter;
+    const double l = x * x + 2.0 * y * y - 2.0 * (2.0 * x * y + y * y);
+    return std::sqrt(std::max(0.0, l)) / (16.0 * grn::kPi * x * Mr);
+  };
+  double p = ps(M);
+  if (std::fabs(p) < 1e-12)
+    for (int i = 1; i <= 3; ++i) {
+      p = ps(M + i * W);
+      if (p > 1e-12) break;
+    }
+  return std::sqrt(std::max(0.0, BR * W / p));
 }
 
 const char *grn_last_error(void) { return g_last_error.c_str(); }

@@ -190,6 +190,55 @@ __device__ double screened_amp2_vv(const KArgs &A, const Born &b, const KtNode<T
   return amp2;
 }
 
+// kt-loop of the Regge resonances (+ continuum): the resonances' loop-invariant factors and
+// rotated density matrices per event in FP64 (regge_res_event), the rest per point in T;
+// *mag as in loop_integral.
+template <typename T>
+__device__ __noinline__ cx<double> loop_integral_rr(const KArgs &A, const Born &b,
+                                                    const KtNode<T> *skt,
+                                                    const PhiNode<T> *sphi, double *mag) {
+  constexpr bool kMag = sizeof(T) == sizeof(float);
+  LoopEvent<T> e;
+  make_loop_event<T>(A.K, b, e);
+  RegRes<double> Rd;
+  regge_res_event(A.P, A.K, b.p3p, b.p3m, b.p3x, b.p3y, b.p4p, b.p4m, b.p4x, b.p4y, Rd);
+  RegRes<T> R;
+  for (int r = 0; r < A.K.rr_n; ++r) {
+    R.C[r] = {T(Rd.C[r].re), T(Rd.C[r].im)};
+    for (int k = 0; k < 25; ++k) R.rho[r][k] = T(Rd.rho[r][k]);
+  }
+  R.Xe = T(Rd.Xe); R.Xx = T(Rd.Xx); R.Xy = T(Rd.Xy); R.Xz = T(Rd.Xz); R.M = T(Rd.M);
+  const T Xp = T(b.p3p + b.p4p), Xm = T(b.p3m + b.p4m), c12 = T(A.K.mp2 + b.m2);
+  const bool con = A.P.process == GRN_PROC_REGGE_RESCON;
+  T ar = T(0), ai = T(0), cr = T(0), ci = T(0), m = T(0);
+  for (int j = 0; j < A.n_kt_nodes; ++j) {
+    const KtNode<T> nj = skt[j];
+    T ir = T(0), ii = T(0), dr = T(0), di = T(0), ab = T(0);
+    for (int i = 0; i < A.n_phi_nodes; ++i) {
+      const PhiNode<T> ni = sphi[i];
+      LCKin<T>         kk;
+      if (!loop_point_kin<T>(e, nj.kt * ni.c, nj.kt * ni.s, kk)) continue;
+      const T s1 = c12 + kk.p1p * Xm + kk.p1m * Xp - T(2) * (kk.p1x * R.Xx + kk.p1y * R.Xy);
+      const T s2 = c12 + kk.p2p * Xm + kk.p2m * Xp - T(2) * (kk.p2x * R.Xx + kk.p2y * R.Xy);
+      cx<T> a = regge_res_amp<T>(A.P, A.K, R, kk.t1, kk.t2, log(s1), log(s2),
+                                 T(0.5) * (kk.q1p + kk.q1m), -kk.p1x, -kk.p1y,
+                                 T(0.5) * (kk.q1p - kk.q1m));
+      if (con)
+        a = cadd(a, regge_me4<T>(A.P, A.K, kk.t1, kk.t2, log(kk.s13), log(kk.s14), log(kk.s23),
+                                 log(kk.s24), kk.that, kk.uhat));
+      kahan_add(ir, dr, ni.u * a.re);
+      kahan_add(ii, di, ni.u * a.im);
+      if constexpr (kMag) ab += ni.u * (fabs(a.re) + fabs(a.im));
+    }
+    kahan_add(ar, cr, nj.cre * ir - nj.cim * ii);
+    kahan_add(ai, ci, nj.cre * ii + nj.cim * ir);
+    if constexpr (kMag) m += sqrt(nj.cre * nj.cre + nj.cim * nj.cim) * ab;
+  }
+  *mag = double(m);
+  const double sr = double(ar), si = double(ai);
+  return {A.loop_norm_re * sr - A.loop_norm_im * si, A.loop_norm_re * si + A.loop_norm_im * sr};
+}
+
 // *mag: see loop_integral (0 from the single-trajectory Regge loop, whose increment form
 // keeps every FP32 operand O(1) and whose rings do not cancel).
 template <typename T>
@@ -202,6 +251,7 @@ __device__ __forceinline__ cx<double> loop_dispatch(const KArgs &A, const Born &
       return loop_integral_fast(A, b, skt, sphi);
     }
   }
+  if (is_regge_res(A.P)) return loop_integral_rr<T>(A, b, skt, sphi, mag);
   return loop_integral<T>(A, b, skt, sphi, mag);
 }
 

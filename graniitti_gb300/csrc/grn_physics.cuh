@@ -87,6 +87,12 @@ struct Consts {
   double res_M2[GRN_MAX_RESONANCES], res_MW[GRN_MAX_RESONANCES];
   double res_c0[GRN_MAX_RESONANCES], res_c1[GRN_MAX_RESONANCES];
   double res_g[GRN_MAX_RESONANCES][7];  // J = 2 couplings g_Tensor[0..6]
+  // PP[RES], PP[RES+CON] (Regge resonances, regge_res_*): count, and per resonance the
+  // Breit-Wigner form, M0, width, 1 / S0^4 of the form factor, g_regge x g_decay
+  int    rr_n;
+  int    rr_J[GRN_MAX_RESONANCES], rr_bw[GRN_MAX_RESONANCES];
+  double rr_M[GRN_MAX_RESONANCES], rr_W[GRN_MAX_RESONANCES], rr_iff4[GRN_MAX_RESONANCES];
+  double rr_g_re[GRN_MAX_RESONANCES], rr_g_im[GRN_MAX_RESONANCES];
 };
 
 // sin(pi x), cos(pi x) without rounding pi x first.
@@ -963,6 +969,220 @@ GRN_HD cx<T> regge_me4(const grn_process_params &P, const Consts &K, T t1, T t2,
   return cscale(cadd(At, Au), vtx);
 }
 
+// ---------------------------------------------------------------------------
+// Regge resonances (PP[RES], PP[RES+CON]; MRegge::ME3, src/MRegge.cc:677-712, with
+// spin::ProdAmp / DecayAmp, src/MSpin.cc:280-480, and the Breit-Wigner forms of
+// src/MForm.cc:743-830). Per resonance r
+//   A_r = 2 P(s1,t1) P(s2,t2) gN^2 F(t1) F(t2) CBW_r(m^2) exp(-(m^2 - M_r^2)^2 / S0^4)
+//         (1/m^2)^omega g_r g_decay,r S^prod_r S^dec_r
+// with P(s,t) the Regge propagator sum and F the proton form factor as in the continuum,
+// s_i = (p_i + X)^2. For J = 2 the spin factors (SPINGEN / SPINDEC) are
+//   S = sqrt(5) sqrt(Re f rho_rot f^+),  f_M = d^2_{0M}(theta) e^{i M phi},  M = -2..2,
+// with (theta, phi) the direction of the momentum transfer q1 (production) or of the first
+// daughter (decay) in the X rest frame reached by a pure boost, and rho_rot = D^+ rho D the
+// resonance's density matrix rotated by D_{MM'} = d^2_{MM'}(theta_R) e^{i M' phi_R} to the
+// chosen frame (CM: none; HX: X's lab direction; CS: the beams' bisector in the X frame).
+// J = 0: S = 1 (and the decay T-matrix element of two pseudoscalars is 1).
+
+// Wigner small-d d^2_{m m'}(theta) from c = cos(theta/2), s = sin(theta/2) (sum over k of the
+// standard closed formula, in the sign convention of MSpin.cc:927-961).
+GRN_HD double wigner_d2(int m, int mp, double c, double s) {
+  const double f[5] = {1.0, 1.0, 2.0, 6.0, 24.0};
+  double sum = 0.0;
+  for (int k = 0; k <= 4; ++k) {
+    if (2 - mp - k < 0 || 2 + m - k < 0 || k + mp - m < 0) continue;
+    double v = (((mp - m + k) & 1) ? -1.0 : 1.0) / (f[2 - mp - k] * f[2 + m - k] * f[k + mp - m] * f[k]);
+    for (int e = 0; e < 4 + m - mp - 2 * k; ++e) v *= c;
+    for (int e = 0; e < mp - m + 2 * k; ++e) v *= s;
+    sum += v;
+  }
+  return sqrt(f[2 + m] * f[2 - m] * f[2 + mp] * f[2 - mp]) * sum;
+}
+
+// Direction of (x, y, z): cos(theta), sin(theta), e^{i phi} (phi = 0 on the z axis).
+template <typename T>
+GRN_HD void direction(T x, T y, T z, T &ct, T &st, T &cp, T &sp) {
+  const T rt = sqrt(x * x + y * y), r = sqrt(rt * rt + z * z);
+  ct = r > T(0) ? z / r : T(1);
+  st = r > T(0) ? rt / r : T(0);
+  cp = rt > T(0) ? x / rt : T(1);
+  sp = rt > T(0) ? y / rt : T(0);
+}
+
+// Re(f rho f^+) for f_M = d^2_{0M}(theta) e^{i M phi}; rho Hermitian packed as its 5 diagonal
+// entries, then the real and the imaginary parts of the 10 entries above it (row-major).
+template <typename T>
+GRN_HD T spin2_form(const T *rho, T ct, T st, T cp, T sp) {
+  const T a = T(0.6123724356957945) * st * st;  // sqrt(3/8) sin^2
+  const T b = T(1.224744871391589) * st * ct;   // sqrt(3/2) sin cos
+  const T d[5] = {a, b, T(1.5) * ct * ct - T(0.5), -b, a};  // d^2_{0M}, M = -2..2
+  // e^{i k phi}, k = 1..4 (the phase of entry (j, l) is e^{i (M_j - M_l) phi})
+  T c[5], sn[5];
+  c[0] = T(1); sn[0] = T(0);
+  for (int k = 1; k < 5; ++k) {
+    c[k]  = c[k - 1] * cp - sn[k - 1] * sp;
+    sn[k] = sn[k - 1] * cp + c[k - 1] * sp;
+  }
+  T q = T(0);
+  for (int j = 0; j < 5; ++j) q += d[j] * d[j] * rho[j];
+  int u = 0;
+  for (int j = 0; j < 5; ++j)
+    for (int l = j + 1; l < 5; ++l, ++u) {
+      // 2 Re(rho_jl e^{i (M_j - M_l) phi}), M_j - M_l = j - l < 0
+      const int k = l - j;
+      q += T(2) * d[j] * d[l] * (rho[5 + u] * c[k] + rho[15 + u] * sn[k]);
+    }
+  return q;
+}
+
+// Per-event data of the Regge resonances: the loop-invariant factor of each resonance, the
+// rotated density matrices (packed as in spin2_form) of the J = 2 resonances (SPINGEN), and
+// X for the boost of q1 into its rest frame.
+template <typename T>
+struct RegRes {
+  cx<T> C[GRN_MAX_RESONANCES];
+  T     rho[GRN_MAX_RESONANCES][25];
+  T     Xe, Xx, Xy, Xz, M;
+};
+
+// q = (E, x, y, z) into the rest frame of X (MKinematics.h:384-401 with sign -1): spatial part.
+template <typename T>
+GRN_HD void boost_to_rest(T Xe, T Xx, T Xy, T Xz, T M, T E, T &x, T &y, T &z) {
+  const T k = (Xx * x + Xy * y + Xz * z) / (M * (Xe + M)) - E / M;
+  x += k * Xx;
+  y += k * Xy;
+  z += k * Xz;
+}
+
+GRN_HD_COLD void regge_res_event(const grn_process_params &P, const Consts &K, double p3p,
+                                 double p3m, double p3x, double p3y, double p4p, double p4m,
+                                 double p4x, double p4y, RegRes<double> &R) {
+  const double Xp = p3p + p4p, Xm = p3m + p4m;
+  R.Xe = 0.5 * (Xp + Xm);
+  R.Xz = 0.5 * (Xp - Xm);
+  R.Xx = p3x + p4x;
+  R.Xy = p3y + p4y;
+  const double m2 = Xp * Xm - (R.Xx * R.Xx + R.Xy * R.Xy);
+  R.M = sqrt(m2);
+  // frame rotation (theta_R, phi_R) as half-angle cos / sin and e^{i phi_R}
+  double ct = 1.0, st = 0.0, cp = 1.0, sp = 0.0;
+  if (P.spin_frame == GRN_FRAME_HX) {
+    direction<double>(R.Xx, R.Xy, R.Xz, ct, st, cp, sp);
+  } else if (P.spin_frame == GRN_FRAME_CS) {
+    const double E = 0.5 * K.sqrt_s, pz = 0.5 * (K.L - K.eps);
+    double ax = 0, ay = 0, az = pz, bx = 0, by = 0, bz = -pz;
+    boost_to_rest(R.Xe, R.Xx, R.Xy, R.Xz, R.M, E, ax, ay, az);
+    boost_to_rest(R.Xe, R.Xx, R.Xy, R.Xz, R.M, E, bx, by, bz);
+    const double na = sqrt(ax * ax + ay * ay + az * az), nb = sqrt(bx * bx + by * by + bz * bz);
+    direction<double>(ax / na - bx / nb, ay / na - by / nb, az / na - bz / nb, ct, st, cp, sp);
+  }
+  const double hc = sqrt(fmax(0.0, 0.5 * (1.0 + ct))), hs = sqrt(fmax(0.0, 0.5 * (1.0 - ct)));
+  // D_{ij} = d^2_{M_i M_j}(theta_R) e^{i M_j phi_R}
+  double Dr[5][5], Di[5][5];
+  for (int j = 0; j < 5; ++j) {
+    // e^{i M_j phi_R}, M_j = j - 2
+    double er = 1.0, ei = 0.0;
+    const int mj = j - 2;
+    for (int k = 0; k < (mj < 0 ? -mj : mj); ++k) {
+      const double t = er * cp - ei * sp * (mj < 0 ? -1.0 : 1.0);
+      ei = ei * cp + er * sp * (mj < 0 ? -1.0 : 1.0);
+      er = t;
+    }
+    for (int i = 0; i < 5; ++i) {
+      const double d = wigner_d2(i - 2, mj, hc, hs);
+      Dr[i][j] = d * er;
+      Di[i][j] = d * ei;
+    }
+  }
+  // daughter direction in the X rest frame
+  double dx = p3x, dy = p3y, dz = 0.5 * (p3p - p3m);
+  boost_to_rest(R.Xe, R.Xx, R.Xy, R.Xz, R.M, 0.5 * (p3p + p3m), dx, dy, dz);
+  double dct, dst, dcp, dsp;
+  direction<double>(dx, dy, dz, dct, dst, dcp, dsp);
+  const double lm2 = log(m2);
+  for (int r = 0; r < K.rr_n; ++r) {
+    const double M0 = K.rr_M[r], W = K.rr_W[r], M02 = M0 * M0, dm = m2 - M02;
+    // complex Breit-Wigner -1/den (times a numerator for form 4)
+    double dre = dm, dim = M0 * W, num = 1.0;
+    if (K.rr_bw[r] == 2) {
+      dim = sqrt(m2) * W;
+    } else if (K.rr_bw[r] == 3) {
+      const double ma = sqrt(K.m3sq), mb = sqrt(K.m4sq);
+      const double u = sqrt(fmax(0.0, (m2 - (ma + mb) * (ma + mb)) * (m2 - (ma - mb) * (ma - mb)))) /
+                       (2.0 * sqrt(m2));
+      const double v = sqrt(fmax(0.0, (M02 - (ma + mb) * (ma + mb)) * (M02 - (ma - mb) * (ma - mb)))) /
+                       (2.0 * M0);
+      dim = W * M02 / sqrt(m2) * pow(u / v, 2.0 * K.rr_J[r] + 1.0);
+    } else if (K.rr_bw[r] == 4 && K.rr_J[r] == 2) {
+      const double x = m2 / M02;
+      num = 7.0 / 6.0 - (4.0 / 3.0) * x + (2.0 / 3.0) * x * x;
+    }
+    const double id = -num / (dre * dre + dim * dim);
+    const cx<double> bw{dre * id, -dim * id};
+    // form factor, flux, 2, and g_regge g_decay
+    double f = 2.0 * exp(-dm * dm * K.rr_iff4[r] - P.omega * lm2);
+    if (K.rr_J[r] == 2) {
+      // rho_rot = D^+ rho D, packed
+      const double *rr = P.res[r].rho[0], *ri = P.res[r].rho[1];
+      double Rr[5][5], Ri[5][5];
+      for (int i = 0; i < 5; ++i)
+        for (int k = 0; k < 5; ++k) {
+          double sr = 0.0, si = 0.0;
+          for (int j = 0; j < 5; ++j)
+            for (int l = 0; l < 5; ++l) {
+              // conj(D_ji) rho_jl D_lk
+              const double ar = Dr[j][i], ai = -Di[j][i];
+              const double br = rr[5 * j + l], bi = ri[5 * j + l];
+              const double cr = ar * br - ai * bi, ci = ar * bi + ai * br;
+              sr += cr * Dr[l][k] - ci * Di[l][k];
+              si += cr * Di[l][k] + ci * Dr[l][k];
+            }
+          Rr[i][k] = sr;
+          Ri[i][k] = si;
+        }
+      double pk[25];
+      int    u = 0;
+      for (int j = 0; j < 5; ++j) pk[j] = Rr[j][j];
+      for (int j = 0; j < 5; ++j)
+        for (int l = j + 1; l < 5; ++l, ++u) {
+          pk[5 + u]  = Rr[j][l];
+          pk[15 + u] = Ri[j][l];
+        }
+      for (int k = 0; k < 25; ++k) R.rho[r][k] = pk[k];
+      if (P.spin_dec) f *= sqrt(5.0) * sqrt(fmax(0.0, spin2_form<double>(pk, dct, dst, dcp, dsp)));
+    } else {
+      for (int k = 0; k < 25; ++k) R.rho[r][k] = 0.0;
+    }
+    R.C[r] = cscale(cmul(bw, cx<double>{K.rr_g_re[r], K.rr_g_im[r]}), f);
+  }
+}
+
+// Resonance amplitude at a point: q1 = (qE, qx, qy, qz), s1, s2, t1, t2.
+template <typename T>
+GRN_HD cx<T> regge_res_amp(const grn_process_params &P, const Consts &K, const RegRes<T> &R, T t1,
+                           T t2, T lns1, T lns2, T qE, T qx, T qy, T qz) {
+  cx<T> sum{T(0), T(0)};
+  T     ct = T(1), st = T(0), cp = T(1), sp = T(0);
+  bool  dir = false;
+  for (int r = 0; r < K.rr_n; ++r) {
+    T s = T(1);
+    if (K.rr_J[r] == 2 && P.spin_gen) {
+      if (!dir) {
+        boost_to_rest<T>(R.Xe, R.Xx, R.Xy, R.Xz, R.M, qE, qx, qy, qz);
+        direction<T>(qx, qy, qz, ct, st, cp, sp);
+        dir = true;
+      }
+      s = T(2.23606797749979) * sqrt(fmax(T(0), spin2_form<T>(R.rho[r], ct, st, cp, sp)));
+    }
+    sum = cadd(sum, cscale(R.C[r], s));
+  }
+  const grn_regge_params &rp = P.regge;
+  const T vtx = T(K.gN2) * proton_ff<T>(T(P.soft.fc1), T(P.soft.fc2), t1) *
+                proton_ff<T>(T(P.soft.fc1), T(P.soft.fc2), t2);
+  return cscale(cmul(sum, cmul(regge_prop<T>(K, rp, lns1, t1), regge_prop<T>(K, rp, lns2, t2))),
+                vtx);
+}
+
 // Bare amplitude at one kt-loop point: forward legs p1T - k, p2T + k with the
 // tree-level central pair (for Kf = 2 the pair is unchanged because p1T + p2T is
 // loop invariant; MContinuum::LoopKinematics, src/MContinuum.cc:94-161).
@@ -1338,8 +1558,30 @@ GRN_HD void make_loop_event(const Consts &K, const Born &b, LoopEvent<T> &e) {
   }
 }
 
+GRN_HD bool is_regge_res(const grn_process_params &P) {
+  return P.process == GRN_PROC_REGGE_RES || P.process == GRN_PROC_REGGE_RESCON;
+}
+
+// Tree-level Regge resonances (+ continuum for PP[RES+CON]) from the Born kinematics.
+GRN_HD_COLD cx<double> regge_res_born(const grn_process_params &P, const Consts &K, const Born &b) {
+  RegRes<double> R;
+  regge_res_event(P, K, b.p3p, b.p3m, b.p3x, b.p3y, b.p4p, b.p4m, b.p4x, b.p4y, R);
+  const double Xp = b.p3p + b.p4p, Xm = b.p3m + b.p4m, Xx = b.p3x + b.p4x, Xy = b.p3y + b.p4y;
+  const double s1 = K.mp2 + b.m2 + b.p1p * Xm + b.p1m * Xp - 2.0 * (b.p1x * Xx + b.p1y * Xy);
+  const double s2 = K.mp2 + b.m2 + b.p2p * Xm + b.p2m * Xp - 2.0 * (b.p2x * Xx + b.p2y * Xy);
+  double q1p, q1m;
+  q_lightcone<double>(b.x1, b.pt1sq, K.mp2, K.L, q1p, q1m);
+  cx<double> A = regge_res_amp<double>(P, K, R, b.t1, b.t2, log(s1), log(s2), 0.5 * (q1p + q1m),
+                                       -b.p1x, -b.p1y, 0.5 * (q1p - q1m));
+  if (P.process == GRN_PROC_REGGE_RESCON)
+    A = cadd(A, regge_me4<double>(P, K, b.t1, b.t2, log(b.s13), log(b.s14), log(b.s23),
+                                  log(b.s24), b.that, b.uhat));
+  return A;
+}
+
 // Tree-level amplitude of the configured process from the Born kinematics (FP64).
 GRN_HD cx<double> born_amp(const grn_process_params &P, const Consts &K, const Born &b) {
+  if (is_regge_res(P)) return regge_res_born(P, K, b);
   if (P.process == GRN_PROC_TENSOR_CON || P.process == GRN_PROC_TENSOR_RES ||
       P.process == GRN_PROC_TENSOR_RESCON) {
     LCKin<double> k{b.p1p, b.p1m, b.p1x, b.p1y, b.p2p, b.p2m, b.p2x,  b.p2y, b.p3p,

@@ -17,7 +17,10 @@ TUNES = {
         "PARAM_REGGE": {
             "a0": [1.088, 0.55, 0.55], "ap": [0.20, 0.93, 0.93], "sgn": [1, -1, 1], "s0": 1.0,
             "offshellFF": 2, "b_EXP": 0.944, "a_OREAR": 0.638, "b_OREAR": 1.886, "b_POW": 0.500,
+            "omega": 0.5,
         },
+        # Spin correlations of the Regge resonances (GENERAL.json PARAM_SPIN).
+        "PARAM_SPIN": {"SPINGEN": True, "SPINDEC": True, "FRAME": "CS"},
         "PARAM_TENSORPOM": {
             "delta_P": 0.0808, "ap_P": 0.25, "gPNN": 1.87, "gPpipi": 1.76, "gPKK": 1.54,
             "gPrhorho": [0.70, 6.20], "gPphiphi": [0.49, 4.27],
@@ -35,20 +38,28 @@ TUNES = {
     }
 }
 
-# Resonances of the tensor-pomeron model that decay to pseudoscalar pairs, TUNE0
-# (modeldata/TUNE0/RES_*.json: PARAM_RES M, W, J, P, g_Tensor), by the generator's names.
+# Resonances that decay to pseudoscalar pairs, TUNE0 (modeldata/TUNE0/RES_*.json: PARAM_RES
+# M, W, J, P, g_Tensor for the tensor pomeron; BW, g_A, g_phi, g_FF and the diagonal of the
+# spin density matrix, M = -J..J, for the Regge model), by the generator's names.
 RESONANCES = {
     "TUNE0": {
-        "f0_500": dict(pdg=9000221, M=0.5, W=0.4, J=0, P=1, g_Tensor=[0.1, 0.0]),
-        "f0_980": dict(pdg=9010221, M=0.980, W=0.08, J=0, P=1, g_Tensor=[0.4, 2.0]),
-        "f0_1500": dict(pdg=9030221, M=1.506, W=0.112, J=0, P=1, g_Tensor=[0.1, 0.0]),
-        "f0_1710": dict(pdg=10331, M=1.704, W=0.123, J=0, P=1, g_Tensor=[0.45, 2.6]),
+        "f0_500": dict(pdg=9000221, M=0.5, W=0.4, J=0, P=1, g_Tensor=[0.1, 0.0],
+                       BW=2, g_A=0.05, g_phi=-3.14159, g_FF=1.0),
+        "f0_980": dict(pdg=9010221, M=0.980, W=0.08, J=0, P=1, g_Tensor=[0.4, 2.0],
+                       BW=2, g_A=0.065, g_phi=-3.14159, g_FF=1.0),
+        "f0_1500": dict(pdg=9030221, M=1.506, W=0.112, J=0, P=1, g_Tensor=[0.1, 0.0],
+                        BW=2, g_A=0.03, g_phi=-3.14159, g_FF=1.0),
+        "f0_1710": dict(pdg=10331, M=1.704, W=0.123, J=0, P=1, g_Tensor=[0.45, 2.6],
+                        BW=2, g_A=0.03, g_phi=-3.14159, g_FF=1.0),
         "f2_1270": dict(pdg=225, M=1.2755, W=0.1867, J=2, P=1,
-                        g_Tensor=[2.0, 0.0, 0.0, 0.0, 0.0, 0.0, 0.0]),
+                        g_Tensor=[2.0, 0.0, 0.0, 0.0, 0.0, 0.0, 0.0],
+                        BW=2, g_A=0.7, g_phi=-1.57, g_FF=1.0, rho=[0.5, 0, 0, 0, 0.5]),
         "f2_1525": dict(pdg=335, M=1.525, W=0.073, J=2, P=1,
-                        g_Tensor=[0.0, 0.5, 0.0, 0.0, 0.0, 0.0, 0.0]),
+                        g_Tensor=[0.0, 0.5, 0.0, 0.0, 0.0, 0.0, 0.0],
+                        BW=2, g_A=0.19, g_phi=-1.57, g_FF=1.0, rho=[0.5, 0, 0, 0, 0.5]),
         "f2_1950": dict(pdg=9050225, M=1.936, W=0.464, J=2, P=1,
-                        g_Tensor=[1.0, 0.0, 0.0, 0.0, 0.0, 0.0, 0.0]),
+                        g_Tensor=[1.0, 0.0, 0.0, 0.0, 0.0, 0.0, 0.0],
+                        BW=2, g_A=0.1, g_phi=-1.57, g_FF=1.0, rho=[0.5, 0, 0, 0, 0.5]),
     }
 }
 

@@ -58,9 +58,13 @@ enum {
                               tensor-pomeron resonances, MTensorPomeron::ME3 (MSubProc.h:
                               278-285; src/MTensorPomeron.cc:164-565), J = 0 (P = +1) and
                               J = 2 with the pseudoscalar-pair decay */
-  GRN_PROC_TENSOR_RESCON = 4 /* "PP[RES+CONTENSOR]<F|C> -> a b", 2 pseudoscalars: the 2xS
+  GRN_PROC_TENSOR_RESCON = 4, /* "PP[RES+CONTENSOR]<F|C> -> a b", 2 pseudoscalars: the 2xS
                               continuum and the resonances (0..4) summed coherently
                               (MSubProc.h:319-351) */
+  GRN_PROC_REGGE_RES = 5,  /* "PP[RES]<F|C> -> a b", 2 pseudoscalars: Regge resonances
+                              (MRegge::ME3 with spin::ProdAmp / DecayAmp), J^P = 0+ and 2+ */
+  GRN_PROC_REGGE_RESCON = 6 /* "PP[RES+CON]<F|C> -> a b": the Regge continuum (MRegge::ME4)
+                              and the Regge resonances summed coherently (MSubProc.h:398-433) */
 };
 
 /* Phase-space classes (MProcess subclasses). */
@@ -114,7 +118,17 @@ typedef struct grn_resonance {
   double  g_tensor[7]; /* production couplings g_Tensor: [0], [1] for J = 0 (structures
                           iG_PPS_0, iG_PPS_1); [0] for J = 2 (iG_PPT_00; [1..6] must be 0) */
   double  g_decay;     /* decay coupling, grn_tensor_decay_coupling() unless the model gives it */
+  /* Regge model (PP[RES], PP[RES+CON]; PARAM_RES of modeldata RES_*.json): */
+  double  g_regge[2];  /* production coupling g_A exp(i g_phi): (re, im) */
+  double  g_ff;        /* resonance form factor scale S0 [GeV]: exp(-(m^2 - M^2)^2 / S0^4) */
+  int32_t bw;          /* Breit-Wigner form: 1 fixed width, 2 running width, 3 spin barrier,
+                          4 spin dependent (MForm.cc:743-830) */
+  int32_t _pad_bw;
+  double  rho[2][25];  /* spin density matrix of J = 2 (re, im), rows M = -2..2 (J = 0: unused) */
 } grn_resonance;
+
+/* Spin polarization frame of the Regge resonances' density matrices (MSpin.cc:544-600). */
+enum { GRN_FRAME_CM = 0, GRN_FRAME_HX = 1, GRN_FRAME_CS = 2 };
 
 typedef struct grn_gencuts { /* GENCUT, include/Graniitti/MKinematics.h:1554-1576 */
   double rap_min, rap_max;       /* <C> final-state rapidity window */
@@ -170,6 +184,10 @@ typedef struct grn_process_params {
   int32_t           central_spin; /* spin of the central particles (0 or 1: "2xS" / "2xV") */
   double            width[2];     /* widths of the central particles [GeV] */
   double            m_daughter[4];/* daughter masses: central 1 -> [0], [1]; 2 -> [2], [3] */
+  /* Regge resonances: spin correlations of production (SPINGEN) and decay (SPINDEC), the
+   * frame of the density matrices (GRN_FRAME_*), the flux exponent (PARAM_REGGE omega) */
+  int32_t           spin_gen, spin_dec, spin_frame, _pad_spin;
+  double            omega;
 } grn_process_params;
 
 /* Fill every field with the reference defaults for "PP[CON]<C> -> pi+ pi-" at
@@ -182,6 +200,10 @@ void grn_default_params(grn_process_params *p);
  * M is below 2 m_daughter the coupling is taken at M + i W, i = 1, 2, 3, the first one above
  * threshold. Returns NaN for J other than 0, 1, 2. */
 double grn_tensor_decay_coupling(int32_t J, double M, double W, double m_daughter, double BR);
+/* Decay coupling of the Regge resonances (PP[RES], PP[RES+CON]) to two particles of mass
+ * m_daughter: sqrt(BR W / Gamma_PS), Gamma_PS the two-body width with |A|^2 = 1
+ * (MProcess::ProcessHelicityDecay, src/MProcess.cc:670-713), with the same threshold retry. */
+double grn_regge_decay_coupling(double M, double W, double m_daughter, double BR);
 
 /* ------------------------------------------------------------------------ */
 /* Engine lifetime                                                            */

@@ -1069,6 +1069,120 @@ double screened_amp2(const Setup &S, const Event &born, const cplx *A0, int nh) 
   return amp2;
 }
 
+// ---------------------------------------------------------------------------
+// Regge resonances (PP[RES], PP[RES+CON]; MRegge::ME3, src/MRegge.cc:677-712, with
+// spin::ProdAmp / DecayAmp, src/MSpin.cc:280-480, and CBW, src/MForm.cc:743-830), restated
+// with explicit (2J+1)-dimensional matrices: per resonance
+//   A_r = 2 P(s1,t1) FF_A CBW RFF P(s2,t2) FF_B (1/m^2)^omega [g NORM sqrt(Re Tr f0 R f0^+)]
+//         [g_decay NORM sqrt(Re Tr f R f^+)],  R = D^+ rho D,  NORM = sqrt(2J+1),
+// f0 (f) the row D^J_{0M}(theta, phi) of q1 (of the first daughter) boosted to the X rest
+// frame, D_{MM'} = D^J_{MM'}(theta_R, phi_R) of the frame; J = 0: both brackets g, g_decay.
+double fact(int n) { double f = 1; for (int i = 2; i <= n; ++i) f *= i; return f; }
+// Wigner small-d by its closed sum over k (as MSpin.cc:927-961 writes it), integer J.
+double wigner_small_d(double theta, int m, int mp, int J) {
+  double s = 0;
+  for (int k = 0; k <= 2 * J; ++k) {
+    if (J - mp - k < 0 || J + m - k < 0 || k + mp - m < 0) continue;
+    s += std::pow(-1.0, mp - m + k) /
+         (fact(J - mp - k) * fact(J + m - k) * fact(k + mp - m) * fact(k)) *
+         std::pow(std::cos(theta / 2), 2 * J + m - mp - 2 * k) *
+         std::pow(std::sin(theta / 2), mp - m + 2 * k);
+  }
+  return std::sqrt(fact(J + m) * fact(J - m) * fact(J + mp) * fact(J - mp)) * s;
+}
+cplx wigner_D(double theta, double phi, int m, int mp, int J) {
+  return wigner_small_d(theta, m, mp, J) * std::exp(cplx(0, 1) * double(mp) * phi);
+}
+// p in the rest frame of X (kinematics::LorentzBoost with sign -1, MKinematics.h:384-401).
+V4 to_rest(const V4 &X, const V4 &p) {
+  const double M = X.m(), g = X.e / M;
+  const double bx = -X.x / X.e, by = -X.y / X.e, bz = -X.z / X.e;
+  const double k1 = bx * p.x + by * p.y + bz * p.z;
+  const double k2 = g * (g * k1 / (1.0 + g) + p.e);
+  return V4(p.x + k2 * bx, p.y + k2 * by, p.z + k2 * bz, g * (p.e + k1));
+}
+double theta_of(const V4 &v) {
+  return (v.x == 0 && v.y == 0 && v.z == 0) ? 0.0 : std::atan2(v.pt(), v.z);
+}
+double phi_of(const V4 &v) { return (v.x == 0 && v.y == 0) ? 0.0 : std::atan2(v.y, v.x); }
+
+double spin_weight(const std::vector<std::vector<cplx>> &R, double theta, double phi, int J) {
+  const int n = 2 * J + 1;
+  std::vector<cplx> f(n);
+  for (int j = 0; j < n; ++j) f[j] = wigner_D(theta, phi, 0, j - J, J);
+  cplx t = 0;
+  for (int j = 0; j < n; ++j)
+    for (int l = 0; l < n; ++l) t += f[j] * R[j][l] * std::conj(f[l]);
+  return std::real(t);
+}
+
+cplx regge_res(const Setup &S, const Event &ev) {
+  const grn_process_params &p = S.p;
+  const V4 &X = ev.pf[0];
+  const double m2 = ev.m2;
+  // frame rotation angles (spin::GetRhoRotation, MSpin.cc:544-600)
+  double thR = 0, phR = 0;
+  if (p.spin_frame == GRN_FRAME_HX) {
+    thR = theta_of(X);
+    phR = phi_of(X);
+  } else if (p.spin_frame == GRN_FRAME_CS) {
+    const V4 a = to_rest(X, S.pb1), b = to_rest(X, S.pb2);
+    const double na = a.p3(), nb = b.p3();
+    V4 z(a.x / na - b.x / nb, a.y / na - b.y / nb, a.z / na - b.z / nb, 0);
+    const double nz = z.p3();
+    z = V4(z.x / nz, z.y / nz, z.z / nz, 0);
+    thR = theta_of(z);
+    phR = phi_of(z);
+  }
+  const V4 q1  = to_rest(X, S.pb1 - ev.pf[1]);
+  const V4 dau = to_rest(X, ev.pf[3]);
+  const double FFA = p.soft.gN_P * proton_ff(p.soft, ev.t1);
+  const double FFB = p.soft.gN_P * proton_ff(p.soft, ev.t2);
+  const cplx   prop = regge_prop(p.regge, ev.ss[1][0], ev.t1) * FFA *
+                    regge_prop(p.regge, ev.ss[2][0], ev.t2) * FFB;
+  cplx sum = 0;
+  for (int r = 0; r < p.n_res; ++r) {
+    const grn_resonance &R = p.res[r];
+    const int    J = R.J;
+    const double M0 = R.M, W = R.W;
+    cplx den(m2 - M0 * M0, M0 * W), num = 1.0;
+    if (R.bw == 2) den = cplx(m2 - M0 * M0, std::sqrt(m2) * W);
+    if (R.bw == 3) {
+      const double ma = p.m_central[0], mb = p.m_central[1];
+      const double u = msqrt((m2 - sq(ma + mb)) * (m2 - sq(ma - mb))) / (2 * std::sqrt(m2));
+      const double d = msqrt((M0 * M0 - sq(ma + mb)) * (M0 * M0 - sq(ma - mb))) / (2 * M0);
+      den = cplx(m2 - M0 * M0, W * M0 * M0 / std::sqrt(m2) * std::pow(u / d, 2 * J + 1));
+    }
+    if (R.bw == 4 && J == 2)
+      num = 7.0 / 6.0 - (4.0 / 3.0) * (m2 / (M0 * M0)) + (2.0 / 3.0) * sq(m2) / sq(sq(M0));
+    const cplx   cbw = -num / den;
+    const double rff = std::exp(-sq(m2 - M0 * M0) / sq(sq(R.g_ff)));
+    const double V   = std::pow(1.0 / m2, p.omega);
+    cplx prod = cplx(R.g_regge[0], R.g_regge[1]);
+    double dec = R.g_decay;
+    if (J == 2) {
+      const int n = 5;
+      std::vector<std::vector<cplx>> D(n, std::vector<cplx>(n)), rho = D, Rr = D;
+      for (int i = 0; i < n; ++i)
+        for (int j = 0; j < n; ++j) {
+          D[i][j]   = wigner_D(thR, phR, i - 2, j - 2, 2);
+          rho[i][j] = cplx(R.rho[0][5 * i + j], R.rho[1][5 * i + j]);
+        }
+      for (int i = 0; i < n; ++i)
+        for (int k = 0; k < n; ++k) {
+          cplx t = 0;
+          for (int j = 0; j < n; ++j)
+            for (int l = 0; l < n; ++l) t += std::conj(D[j][i]) * rho[j][l] * D[l][k];
+          Rr[i][k] = t;
+        }
+      if (p.spin_gen) prod *= std::sqrt(5.0) * msqrt(spin_weight(Rr, theta_of(q1), phi_of(q1), 2));
+      if (p.spin_dec) dec *= std::sqrt(5.0) * msqrt(spin_weight(Rr, theta_of(dau), phi_of(dau), 2));
+    }
+    sum += 2.0 * cbw * rff * V * prod * dec;
+  }
+  return prop * sum;
+}
+
 // RES+CONTENSOR (MSubProc.h:319-351): the continuum's and the resonances' helicity amplitudes
 // are added per proton configuration; with the high-energy proton vertex all four are equal,
 // so the sum of one configuration carries |M|^2.
@@ -1076,6 +1190,8 @@ cplx bare_amp(const Setup &S, const Event &ev) {
   if (S.p.process == GRN_PROC_TENSOR_RES) return tensor_me3(S, ev);
   if (S.p.process == GRN_PROC_TENSOR_RESCON)
     return tensor_me4_2xs(S, ev) + (S.p.n_res > 0 ? tensor_me3(S, ev) : cplx(0.0));
+  if (S.p.process == GRN_PROC_REGGE_RES) return regge_res(S, ev);
+  if (S.p.process == GRN_PROC_REGGE_RESCON) return regge_me4(S, ev) + regge_res(S, ev);
   return S.p.process == GRN_PROC_TENSOR_CON ? tensor_me4_2xs(S, ev) : regge_me4(S, ev);
 }
 

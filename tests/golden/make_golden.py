@@ -9,7 +9,7 @@ reference does not. Steps:
   4. run the reference VEGAS integration for the cross section
 
 Usage: python tests/golden/make_golden.py [--ref /root/reference]
-                                          [--only resonances|cascades|rescon]
+                                          [--only resonances|cascades|rescon|regge_res]
 """
 import argparse
 import json
@@ -138,6 +138,46 @@ def rescon_fixtures():
          proc=proc, n_bt=1024, n_kt2=10000, loop_kt=15, loop_phi=12, loop_ktmax=1.75, **r)
 
 
+def regge_res_fixtures():
+    """Regge resonances (PROC_9 PP[RES], PROC_17 PP[RES+CON]; MRegge::ME3 with the spin
+    density-matrix production and decay amplitudes): the Collins-Soper, helicity and
+    non-rotated frames, a JZ density override, SPINGEN off, K+ K- (f0(980) below threshold),
+    <C>, and the screened amplitude."""
+    REPLAY_F = ["--replay", "h,h,6,7"]
+    cases = [
+        ("gr_tree_weights.npz", 101, 1024, CARD_RES,
+         "PP[RES]<F> -> pi+ pi- @RES{f0_980:1, f2_1270:1}", REPLAY_F, 6),
+        ("grc_tree_weights.npz", 102, 1024, CARD_RES,
+         "PP[RES+CON]<F> -> pi+ pi- @RES{f0_500:1, f0_980:1, f2_1270:1, f2_1525:1}", REPLAY_F, 6),
+        ("grc_hx_tree_weights.npz", 103, 512, CARD_RES,
+         "PP[RES+CON]<F> -> pi+ pi- @RES{f0_980:1, f2_1270:1} @FRAME:HX", REPLAY_F, 6),
+        ("grc_cm_jz_tree_weights.npz", 104, 512, CARD_RES,
+         "PP[RES+CON]<F> -> pi+ pi- @RES{f2_1270:1} @FRAME:CM @R[f2_1270]{JZ0:1, JZ1:0.5, JZ2:0.2}",
+         REPLAY_F, 6),
+        ("grc_nogen_tree_weights.npz", 105, 512, CARD_RES,
+         "PP[RES+CON]<F> -> pi+ pi- @RES{f2_1270:1, f2_1950:1} @SPINGEN:false", REPLAY_F, 6),
+        ("grc_kk_tree_weights.npz", 106, 512, CARD_RES,
+         "PP[RES+CON]<F> -> K+ K- @RES{f0_980:1, f2_1270:1, f2_1525:1}", REPLAY_F, 6),
+        ("grc_c_tree_weights.npz", 107, 1024, CARD_RES,
+         "PP[RES+CON]<C> -> pi+ pi- @RES{f0_980:1, f2_1270:1}", [], 8),
+    ]
+    for name, seed, n, card, proc, extra, dim in cases:
+        u = philox_np.uniforms(seed, n, 8)
+        r = run_weights(card, u, extra, proc=proc, dim=dim)
+        save(name, seed=seed, u=u, card=os.path.basename(card), proc=proc, **r)
+    proc = "PP[RES+CON]<F> -> pi+ pi- @RES{f0_980:1, f2_1270:1}"
+    u = philox_np.uniforms(108, 96, 8)
+    r = run_weights(CARD_RES_SCR, u, REPLAY_F + ["--nbt", "1024", "--nkt2", "10000"], proc=proc,
+                    dim=6)
+    save("grc_screened_15x12_weights.npz", seed=108, u=u, card=os.path.basename(CARD_RES_SCR),
+         proc=proc, n_bt=1024, n_kt2=10000, loop_kt=15, loop_phi=12, loop_ktmax=1.75, **r)
+    # VEGAS cross section (reference ranlux48 points, 8 threads)
+    proc = "PP[RES+CON]<F> -> pi+ pi- @RES{f0_980:1, f2_1270:1}"
+    out = subprocess.run([REF_BIN, "vegas", CARD_RES, proc, "--cores", "8"], check=True,
+                         capture_output=True, text=True).stdout
+    write_sigma("grc_vegas_sigma.json", out, proc, os.path.basename(CARD_RES))
+
+
 def write_sigma(name, out, proc, card):
     line = [l for l in out.splitlines() if l.startswith("RESULT")][-1]
     sigma, err = map(float, line.split()[1:3])
@@ -181,10 +221,15 @@ def cascade_fixtures():
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--ref", default="/root/reference")
-    ap.add_argument("--only", choices=["all", "resonances", "cascades", "rescon"], default="all")
+    ap.add_argument("--only", choices=["all", "resonances", "cascades", "rescon", "regge_res"],
+                    default="all")
     a = ap.parse_args()
     subprocess.check_call(["make", "-s", "-C", os.path.join(REPO, "oracle", "refbuild"), "-j8",
                            "REF=" + a.ref])
+    if a.only in ("all", "regge_res"):
+        regge_res_fixtures()
+    if a.only == "regge_res":
+        return
     if a.only in ("all", "rescon"):
         rescon_fixtures()
     if a.only == "rescon":

@@ -111,7 +111,28 @@ def test_unsupported_resonances_are_rejected(lib_built, proc):
         card.build_params(c, proc)
 
 
-@pytest.mark.parametrize("proc", ["PP[RES]<C> -> pi+ pi-", "PP[CON]<Q> -> pi+ pi-",
+def test_regge_resonance_params(lib_built):
+    from conftest import GOLDEN
+    import os
+    from graniitti_gb300 import _abi
+    c = card.read_card(os.path.join(GOLDEN, "cards", "pp_res_pipi.json"))
+    P = card.build_params(c, "PP[RES+CON]<F> -> pi+ pi- @RES{f0_980:1, f2_1270:1} @FRAME:HX "
+                             "@SPINDEC:false @R[f2_1270]{JZ0:1, JZ2:1}")
+    assert P.process == _abi.GRN_PROC_REGGE_RESCON and P.n_res == 2
+    assert (P.spin_gen, P.spin_dec, P.spin_frame, P.omega) == (1, 0, _abi.GRN_FRAME_HX, 0.5)
+    f0, f2 = P.res[0], P.res[1]
+    assert (f0.bw, f0.g_ff) == (2, 1.0) and abs(f0.g_regge[0] + 0.065) < 1e-6
+    assert abs(complex(f2.g_regge[0], f2.g_regge[1]) - 0.7j * -1) < 1e-3  # 0.7 exp(-1.57 i)
+    assert [f2.rho[0][6 * m] for m in range(5)] == [1 / 3, 0, 1 / 3, 0, 1 / 3]
+    # sqrt(BR W / Gamma_PS): f2(1270) -> pi+ pi-, BR 0.562
+    assert abs(f2.g_decay - 2.6257) < 1e-3
+    P = card.build_params(c, "PP[RES]<C> -> K+ K- @RES{f0_980:1}")  # f0(980) below threshold
+    assert P.process == _abi.GRN_PROC_REGGE_RES and P.n_res == 1 and P.spin_frame == 2
+    with pytest.raises(card.UnsupportedProcess):
+        card.build_params(c, "PP[RES]<C> -> pi+ pi- @FRAME:GJ")
+
+
+@pytest.mark.parametrize("proc", ["PP[RESHEL]<C> -> pi+ pi-", "PP[CON]<Q> -> pi+ pi-",
                                   "PP[CON]<C> -> pi+ pi- pi+ pi-", "yy[CON]<C> -> mu+ mu-"])
 def test_unsupported_processes_are_rejected(proc):
     with pytest.raises(card.UnsupportedProcess):

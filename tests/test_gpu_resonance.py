@@ -18,6 +18,10 @@ pytestmark = pytest.mark.gpu
 # contractions lose relative precision (a few points at 1e-9, median 2e-11); the GPU's
 # light-cone contraction is the more accurate of the two.
 RES_TOL = 5e-9
+# Regge resonances: near a zero of the d-wave decay distribution the quadratic form
+# f rho_rot f^+ of the spin factor is a small difference of O(1) terms, summed in another
+# order on the GPU than in the reference (one point at 9e-9; medians 1e-11 to 2e-11).
+REGGE_TOL = 2e-8
 
 
 def _load(name):
@@ -45,7 +49,10 @@ def _rel(w, wr):
                                   "rf_kk_tree_weights.npz", "rc_tree_weights.npz",
                                   "rf_f2_1525_tree_weights.npz"] +
                          ["rf_s%d_tree_weights.npz" % j for j in range(1, 7)] +
-                         ["rcf_tree_weights.npz", "rcc_tree_weights.npz", "rck_tree_weights.npz"])
+                         ["rcf_tree_weights.npz", "rcc_tree_weights.npz", "rck_tree_weights.npz"] +
+                         ["gr_tree_weights.npz", "grc_tree_weights.npz", "grc_hx_tree_weights.npz",
+                          "grc_cm_jz_tree_weights.npz", "grc_nogen_tree_weights.npz",
+                          "grc_kk_tree_weights.npz", "grc_c_tree_weights.npz"])
 def test_resonance_tree_vs_reference(gpu, name):
     import graniitti_gb300 as g
     gl = _load(name)
@@ -58,15 +65,17 @@ def test_resonance_tree_vs_reference(gpu, name):
     assert np.array_equal(((fl >> 1) & 1)[kin], gl["fid"][kin])
     r = _rel(w, gl["w"])
     print("%s: GPU vs reference max rel %.2e, median %.2e" % (name, r.max(), np.median(r)))
-    assert r.max() < RES_TOL and np.median(r) < 1e-10
-    assert _rel(w, wo).max() < RES_TOL
+    tol = REGGE_TOL if name.startswith("gr") else RES_TOL
+    assert r.max() < tol and np.median(r) < 1e-10
+    assert _rel(w, wo).max() < tol
     # tree-level weights do not depend on the loop precision
     wm, _ = e.event_weights(gl["u"], prec=g.MIXED)
     assert np.array_equal(wm, w)
 
 
 @pytest.mark.parametrize("name", ["rf_screened_15x12_weights.npz",
-                                  "rcf_screened_15x12_weights.npz"])
+                                  "rcf_screened_15x12_weights.npz",
+                                  "grc_screened_15x12_weights.npz"])
 def test_resonance_screened_vs_reference(gpu, name):
     import graniitti_gb300 as g
     gl = _load(name)
@@ -116,20 +125,23 @@ def test_resonance_mixed_loop_vs_fp64_many_points(gpu):
     assert ok, rel.max()
 
 
-def test_resonance_cross_section_vs_reference_vegas(gpu):
-    """Integrated f2(1270) -> pi+ pi- cross section against the reference's own VEGAS run."""
+@pytest.mark.parametrize("name", ["rf_vegas_sigma.json", "grc_vegas_sigma.json"])
+def test_resonance_cross_section_vs_reference_vegas(gpu, name):
+    """Integrated cross sections against the reference's own VEGAS runs: tensor-pomeron
+    f2(1270) -> pi+ pi-, and the Regge f0(980) + f2(1270) + continuum -> pi+ pi-."""
     import graniitti_gb300 as g
     from graniitti_gb300 import _abi, card
-    ref = json.load(open(os.path.join(GOLDEN, "rf_vegas_sigma.json")))
-    P = card.build_params(card.read_card(os.path.join(GOLDEN, "cards", ref["card"])))
+    ref = json.load(open(os.path.join(GOLDEN, name)))
+    P = card.build_params(card.read_card(os.path.join(GOLDEN, "cards", ref["card"])),
+                          ref["process"])
     e = g.Engine(P, 0)
     vp = _abi.VegasParams()
     vp.bins, vp.iter, vp.ncall, vp.lambda_ = 128, 8, 1 << 21, 1.5
     vp.chi2max, vp.precision, vp.burnin_iter, vp.prec, vp.seed = 10.0, 2e-4, 3, 0, 21
     r = e.vegas_integrate(vp)
     pull = (r.sigma - ref["sigma_barn"]) / np.hypot(r.sigma_err, ref["sigma_err_barn"])
-    print("sigma f2(1270): GPU %.5e +- %.1e, reference %.5e +- %.1e, pull %.2f" %
-          (r.sigma, r.sigma_err, ref["sigma_barn"], ref["sigma_err_barn"], pull))
+    print("sigma %s: GPU %.5e +- %.1e, reference %.5e +- %.1e, pull %.2f" %
+          (ref["process"], r.sigma, r.sigma_err, ref["sigma_barn"], ref["sigma_err_barn"], pull))
     assert abs(pull) < 4
 
 

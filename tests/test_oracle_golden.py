@@ -169,7 +169,10 @@ RES_TOL = 5e-9
                                   "rf_kk_tree_weights.npz", "rc_tree_weights.npz",
                                   "rf_f2_1525_tree_weights.npz"] +
                          ["rf_s%d_tree_weights.npz" % j for j in range(1, 7)] +
-                         ["rcf_tree_weights.npz", "rcc_tree_weights.npz", "rck_tree_weights.npz"])
+                         ["rcf_tree_weights.npz", "rcc_tree_weights.npz", "rck_tree_weights.npz"] +
+                         ["gr_tree_weights.npz", "grc_tree_weights.npz", "grc_hx_tree_weights.npz",
+                          "grc_cm_jz_tree_weights.npz", "grc_nogen_tree_weights.npz",
+                          "grc_kk_tree_weights.npz", "grc_c_tree_weights.npz"])
 def test_tensor_resonance_tree_weights(lib_built, name):
     g = _load(name)
     w, fl = orc.weights(_params_res(g), g["u"])
@@ -178,7 +181,8 @@ def test_tensor_resonance_tree_weights(lib_built, name):
 
 
 @pytest.mark.parametrize("name", ["rf_screened_15x12_weights.npz",
-                                  "rcf_screened_15x12_weights.npz"])
+                                  "rcf_screened_15x12_weights.npz",
+                                  "grc_screened_15x12_weights.npz"])
 def test_tensor_resonance_screened_weights(lib_built, name):
     g = _load(name)
     t = _load("eikonal_nbt1024_nkt10000.npz")
