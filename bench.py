@@ -428,14 +428,6 @@ def main():
     P = workload_params()
     eng = g.Engine(P, local)
     eng.eikonal_build(N_BT, N_KT2)
-    # the engine's autotuner picks the kt-loop kernel variant and grid (untimed set-up)
-    tune = eng.autotune(sample=1 << 18)
-    tuned = {"loop_events_per_thread": 1 + tune.best.loop_pair,
-             "loop_blocks": tune.best.vegas_blocks,
-             "candidates_ms": {"%d/thread x %d blocks" % (1 + tune.cand[k].loop_pair,
-                                                         tune.cand[k].vegas_blocks):
-                               round(tune.ms[k], 4) for k in range(tune.n_candidates)},
-             "sample_events": tune.sample_events}
     vp = _abi.VegasParams()
     vp.bins, vp.iter, vp.ncall, vp.lambda_ = 128, args.steps, args.points, 1.5
     vp.chi2max, vp.precision, vp.burnin_iter = 10.0, 1e-3, args.warmup
@@ -447,6 +439,16 @@ def main():
     # -- plain VEGAS, mixed precision: burn-in, then timed integration passes ----
     for it in range(args.warmup):
         eng.vegas_iteration(mode=0, refine=True, iter_id=1 + it)
+    # the engine's autotuner picks the kt-loop kernel variant and grid on the loop stage of a
+    # full pass over the adapted grid (untimed set-up)
+    tune = eng.autotune()
+    variant = {0: "1 event/thread", 1: "2 events/thread", 2: "2 events/thread, 3 blocks/SM"}
+    tuned = {"loop_variant": variant[tune.best.loop_pair],
+             "loop_blocks": tune.best.vegas_blocks,
+             "candidates_ms": {"%s x %d blocks" % (variant[tune.cand[k].loop_pair],
+                                                  tune.cand[k].vegas_blocks):
+                               round(tune.ms[k], 4) for k in range(tune.n_candidates)},
+             "listed_events": tune.sample_events}
     eng.vegas_clear()
     ms_plain, res_plain = _timed_passes(
         torch, stream, lambda it: eng.vegas_iteration(mode=1, refine=True, iter_id=100 + it),
@@ -592,8 +594,10 @@ def main():
                          "traffic": traffic,
                          "peak_source": "measured FP32 FMA-chain probe (MEASURED_PEAKS.json "
                                         "carries no FP32 figure)",
-                         "kernel": ("k_vegas_loop_rec2 (2 events per thread, packed FP32x2)"
-                                    if tune.best.loop_pair else "k_vegas_loop_rec"),
+                         "kernel": {0: "k_vegas_loop_rec",
+                                    1: "k_vegas_loop_rec2<2> (2 events per thread, packed FP32x2)",
+                                    2: "k_vegas_loop_rec2<3> (2 events per thread, packed FP32x2, "
+                                       "3 blocks per SM)"}[tune.best.loop_pair],
                          "flops_per_loop_point": cnt["flops"],
                          "sfu_per_loop_point": cnt["transcendentals"],
                          "kernel_ms": k_avg_s * 1e3},

@@ -1506,7 +1506,7 @@ grn_status grn_get_tuning(grn_engine *e, grn_tuning *t) {
 
 grn_status grn_set_tuning(grn_engine *e, const grn_tuning *t) {
   if (!e || !t) return fail(GRN_ERR_INVALID, "null argument");
-  if ((t->loop_pair != 0 && t->loop_pair != 1) || t->vegas_blocks < 1 || t->weight_blocks < 1 ||
+  if (t->loop_pair < 0 || t->loop_pair > 2 || t->vegas_blocks < 1 || t->weight_blocks < 1 ||
       t->vegas_blocks > (1 << 20) || t->weight_blocks > (1 << 20) ||
       (t->fp64_refine != 0 && t->fp64_refine != 1))
     return fail(GRN_ERR_INVALID, "bad tuning");
@@ -1527,6 +1527,59 @@ grn_status grn_autotune(grn_engine *e, int64_t sample, grn_tune_result *out) {
   if (st != GRN_OK) return st;
   KArgs a = e->args();
   if (!grn::record_mode(a, GRN_PREC_MIXED)) return GRN_OK;  // nothing to choose
+  int sms = 0;
+  GRN_CUDA(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, e->device));
+  // candidates: kernel variant x grid (multiples of the resident blocks)
+  const int mults[3][3] = {{1, 4, 0}, {2, 4, 8}, {2, 4, 8}};
+  if (e->vegas_ready) {
+    // the loop stage of a full VEGAS pass on the engine's grid: stage A once (records), then
+    // every candidate's stage B on the same list (its outputs are rewritten by the next pass)
+    const int64_t nc0 = e->ncall;
+    GRN_CUDA(grn::launch_vegas_born(a, e->d_xmat.as<double>(), e->bins, e->dim, nc0, e->seed,
+                                    0xA7A7A7u, 0, e->d_f.as<double>(), e->d_f2mat.as<double>(),
+                                    e->d_acc.as<unsigned long long>(), e->d_lidx.as<int64_t>(),
+                                    e->d_lx.as<double>(), e->d_lvw.as<double>(),
+                                    e->d_lbins.as<uint64_t>(), lbins_hi(e), e->d_recf.as<float>(),
+                                    e->d_recd.as<double>(), e->stream));
+    double best = 1e300;
+    int    nc   = 0;
+    for (int pair = 0; pair < 3; ++pair)
+      for (int m = 0; m < 3 && mults[pair][m]; ++m) {
+        a.loop_pair      = pair;
+        const int blocks = sms * grn::loop_rec_blocks_per_sm(pair) * mults[pair][m];
+        double    tmin   = 1e300;
+        for (int rep = 0; rep < 2; ++rep) {
+          GRN_CUDA(cudaEventRecord(e->ev0, e->stream));
+          GRN_CUDA(grn::launch_vegas_loop(a, GRN_PREC_MIXED, e->bins, e->dim, nc0, 0,
+                                          e->d_f.as<double>(), e->d_f2mat.as<double>(),
+                                          e->d_acc.as<unsigned long long>(),
+                                          e->d_lidx.as<int64_t>(), e->d_lx.as<double>(),
+                                          e->d_lvw.as<double>(), e->d_lbins.as<uint64_t>(),
+                                          lbins_hi(e), e->d_recf.as<float>(),
+                                          e->d_recd.as<double>(), e->d_rlist.as<int64_t>(),
+                                          blocks, e->stream));
+          GRN_CUDA(cudaEventRecord(e->ev1, e->stream));
+          GRN_CUDA(cudaEventSynchronize(e->ev1));
+          float ms = 0.f;
+          GRN_CUDA(cudaEventElapsedTime(&ms, e->ev0, e->ev1));
+          if (rep > 0) tmin = std::min(tmin, static_cast<double>(ms));
+        }
+        out->cand[nc] = {pair, blocks, blocks, e->fp64_refine};
+        out->ms[nc]   = tmin;
+        if (tmin < best) {
+          best      = tmin;
+          out->best = out->cand[nc];
+        }
+        ++nc;
+      }
+    out->n_candidates = nc;
+    unsigned long long listed = 0;
+    GRN_CUDA(cudaMemcpy(&listed, e->d_acc.as<unsigned long long>() + grn::VS_COUNT,
+                        sizeof(listed), cudaMemcpyDeviceToHost));
+    out->sample_events = static_cast<int64_t>(listed);
+    e->have_last = false;  // the tuning pass is not an integration pass
+    return grn_set_tuning(e, &out->best);
+  }
   const int64_t n = sample;
   GRN_CUDA(e->d_u.ensure(static_cast<size_t>(n) * e->dim * sizeof(double)));
   GRN_CUDA(e->d_w.ensure(static_cast<size_t>(n) * sizeof(double)));
@@ -1540,14 +1593,12 @@ grn_status grn_autotune(grn_engine *e, int64_t sample, grn_tune_result *out) {
                                         e->d_flags.as<uint8_t>(), e->d_wlist.as<int64_t>(),
                                         e->d_recf.as<float>(), e->d_recd.as<double>(),
                                         e->d_wcount.as<unsigned long long>(), e->stream));
-  int sms = 0;
-  GRN_CUDA(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, e->device));
   double best = 1e300;
   int    nc   = 0;
-  for (int pair = 0; pair < 2; ++pair) {
-    for (int mult = 1; mult <= 4; mult *= 2) {
+  for (int pair = 0; pair < 3; ++pair) {
+    for (int m = 0; m < 3 && mults[pair][m]; ++m) {
       a.loop_pair      = pair;
-      const int blocks = sms * grn::loop_rec_blocks_per_sm(pair) * mult;
+      const int blocks = sms * grn::loop_rec_blocks_per_sm(pair) * mults[pair][m];
       double    tmin   = 1e300;
       for (int rep = 0; rep < 3; ++rep) {
         GRN_CUDA(cudaEventRecord(e->ev0, e->stream));
@@ -1562,7 +1613,7 @@ grn_status grn_autotune(grn_engine *e, int64_t sample, grn_tune_result *out) {
         GRN_CUDA(cudaEventElapsedTime(&ms, e->ev0, e->ev1));
         if (rep > 0) tmin = std::min(tmin, static_cast<double>(ms));  // first launch warms up
       }
-      out->cand[nc] = {pair, blocks, blocks, 0};
+      out->cand[nc] = {pair, blocks, blocks, e->fp64_refine};
       out->ms[nc]   = tmin;
       if (tmin < best) {
         best      = tmin;

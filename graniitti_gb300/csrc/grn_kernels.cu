@@ -608,8 +608,10 @@ __global__ void __launch_bounds__(kWeightThreads, GRN_LOOP_MIN_BLOCKS)
   }
 }
 
-// Record mode, two events per thread on the packed FP32x2 loop.
-__global__ void __launch_bounds__(kWeightThreads, 2)
+// Record mode, two events per thread on the packed FP32x2 loop; MINB resident blocks per SM
+// (2: 226 registers; 3: capped at 168, a few spills for 50% more warps).
+template <int MINB>
+__global__ void __launch_bounds__(kWeightThreads, MINB)
     k_weights_loop_rec2(const KArgs A, const int64_t *__restrict__ list,
                         const float *__restrict__ rf, const double *__restrict__ rd, int64_t cap,
                         const unsigned long long *__restrict__ count, double *__restrict__ w,
@@ -662,9 +664,12 @@ cudaError_t launch_weights_loop_rec(const KArgs &a, int64_t n, double *w, uint8_
                                     const unsigned long long *count, int loop_blocks,
                                     cudaStream_t st) {
   if (n <= 0) return cudaSuccess;
-  if (a.loop_pair)
-    k_weights_loop_rec2<<<loop_blocks, kWeightThreads, 0, st>>>(a, list, rf, rd, n, count, w,
-                                                                flags);
+  if (a.loop_pair == 2)
+    k_weights_loop_rec2<3><<<loop_blocks, kWeightThreads, 0, st>>>(a, list, rf, rd, n, count, w,
+                                                                   flags);
+  else if (a.loop_pair)
+    k_weights_loop_rec2<2><<<loop_blocks, kWeightThreads, 0, st>>>(a, list, rf, rd, n, count, w,
+                                                                   flags);
   else
     k_weights_loop_rec<<<loop_blocks, kWeightThreads, 0, st>>>(a, list, rf, rd, n, count, w,
                                                                flags);
@@ -1196,8 +1201,10 @@ __global__ void __launch_bounds__(kVegasThreads, GRN_LOOP_MIN_BLOCKS)
   flush_block(sf2, nh, f2mat, acc, cnt, maxf, maxW);
 }
 
-// Stage B, record mode, two events per thread on the packed FP32x2 loop.
-__global__ void __launch_bounds__(kVegasThreads, 2)
+// Stage B, record mode, two events per thread on the packed FP32x2 loop (MINB as for
+// k_weights_loop_rec2).
+template <int MINB>
+__global__ void __launch_bounds__(kVegasThreads, MINB)
     k_vegas_loop_rec2(const KArgs A, int bins, int dim, int track_max, double *__restrict__ f_out,
                       double *__restrict__ f2mat, unsigned long long *__restrict__ acc,
                       const int64_t *__restrict__ l_idx, const double *__restrict__ l_vw,
@@ -1245,8 +1252,11 @@ __global__ void __launch_bounds__(kVegasThreads, 2)
 constexpr size_t kHistBytes8 = kMaxBins * 8 * sizeof(double);
 int loop_rec_blocks_per_sm(int pair) {
   int per = 0;
-  if (pair)
-    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, k_vegas_loop_rec2, kVegasThreads,
+  if (pair == 2)
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, k_vegas_loop_rec2<3>, kVegasThreads,
+                                                  kHistBytes8);
+  else if (pair)
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, k_vegas_loop_rec2<2>, kVegasThreads,
                                                   kHistBytes8);
   else
     cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, k_vegas_loop_rec, kVegasThreads,
@@ -1295,8 +1305,12 @@ cudaError_t launch_vegas_loop(const KArgs &a, int prec, int bins, int dim, int64
   if (!a.P.screening) return cudaSuccess;
   const int nh = bins * dim;
   if (rf) {
-    if (a.loop_pair)
-      k_vegas_loop_rec2<<<nblocks, kVegasThreads, nh * sizeof(double), st>>>(
+    if (a.loop_pair == 2)
+      k_vegas_loop_rec2<3><<<nblocks, kVegasThreads, nh * sizeof(double), st>>>(
+          a, bins, dim, track_max, f_out, f2mat, acc, l_idx, l_vw, l_bins, l_bins_hi, rf, rd,
+          ncall);
+    else if (a.loop_pair)
+      k_vegas_loop_rec2<2><<<nblocks, kVegasThreads, nh * sizeof(double), st>>>(
           a, bins, dim, track_max, f_out, f2mat, acc, l_idx, l_vw, l_bins, l_bins_hi, rf, rd,
           ncall);
     else

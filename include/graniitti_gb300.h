@@ -556,7 +556,8 @@ grn_status grn_batch_set_flow(grn_batch *b, int32_t index, grn_flow *f);
  * above 1e-5 is recomputed with the FP64 loop in a second pass of the same call (the phi
  * integrals of some tensor couplings cancel by up to 10^12). 0 keeps every FP32 weight. */
 typedef struct grn_tuning {
-  int32_t loop_pair;     /* 0 one event per thread, 1 two events per thread */
+  int32_t loop_pair;     /* 0 one event per thread, 1 two events per thread, 2 two events per
+                            thread with 3 resident blocks per SM (168 registers) */
   int32_t vegas_blocks;  /* grid of the loop stage of VEGAS and flow passes */
   int32_t weight_blocks; /* grid of the loop stage of grn_event_weights */
   int32_t fp64_refine;   /* 1 recompute badly conditioned FP32-loop events in FP64, 0 never */
@@ -572,9 +573,11 @@ typedef struct grn_tune_result {
   grn_tuning cand[8];
   int64_t    sample_events;  /* listed (screened) events the candidates were timed on */
 } grn_tune_result;
-/* Times every candidate (events per thread x grid of 1, 2, 4 times the resident blocks)
- * on the loop records of `sample` Philox points, CUDA events on the engine stream, and
- * keeps the fastest. Needs the eikonal tables; a no-op outside record mode. */
+/* Times every candidate (kernel variant x grid of 1 to 8 times the resident blocks): once
+ * grn_vegas_init has run, on the loop stage of a full VEGAS pass of the engine (ncall points,
+ * its grid; sample is then unused), otherwise on the loop records of `sample` Philox points
+ * through grn_event_weights' kernels; CUDA events on the engine stream, the fastest is kept.
+ * Needs the eikonal tables; a no-op outside record mode. */
 grn_status grn_autotune(grn_engine *e, int64_t sample, grn_tune_result *out);
 
 /* ------------------------------------------------------------------------ */

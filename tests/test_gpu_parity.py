@@ -287,7 +287,9 @@ def test_paired_loop_kernel_vs_fp64(gpu, params_screened, n):
     w1, f1 = e.event_weights(u, prec=g.MIXED)
     e.set_tuning(loop_pair=1)
     w2, f2 = e.event_weights(u, prec=g.MIXED)
-    assert np.array_equal(f2, f64) and np.array_equal(f1, f64)
+    e.set_tuning(loop_pair=2)  # the same kernel capped at 168 registers (3 blocks per SM)
+    w3, f3 = e.event_weights(u, prec=g.MIXED)
+    assert np.array_equal(f2, f64) and np.array_equal(f1, f64) and np.array_equal(f3, f64)
     Pb = type(P)()
     ctypes.memmove(ctypes.byref(Pb), ctypes.byref(P), ctypes.sizeof(P))
     Pb.screening = 0
@@ -298,6 +300,7 @@ def test_paired_loop_kernel_vs_fp64(gpu, params_screened, n):
     print("paired loop: max rel vs FP64 %.3e (median %.3e); vs one-event kernel max %.3e"
           % (r.max(), np.median(r), d12.max()))
     assert ok and d12.max() < 1e-5
+    assert np.max(np.abs(w3[nz] / w2[nz] - 1)) < 1e-6
 
 
 def test_autotune_keeps_fastest_and_results(gpu, params_screened):
@@ -311,7 +314,7 @@ def test_autotune_keeps_fastest_and_results(gpu, params_screened):
     print("autotune: %d candidates on %d events, ms %s, best pair=%d blocks=%d" %
           (r.n_candidates, r.sample_events, np.round(ms, 3), r.best.loop_pair,
            r.best.vegas_blocks))
-    assert r.n_candidates == 6 and r.sample_events > 0
+    assert r.n_candidates == 8 and r.sample_events > 0
     k = int(np.argmin(ms))
     assert (r.best.loop_pair, r.best.vegas_blocks) == (r.cand[k].loop_pair, r.cand[k].vegas_blocks)
     t = e.tuning()
@@ -321,3 +324,31 @@ def test_autotune_keeps_fastest_and_results(gpu, params_screened):
     w64, _ = e.event_weights(u, prec=g.FP64)
     nz = w64 > 0
     assert np.max(np.abs(wm[nz] / w64[nz] - 1)) < 1e-4
+
+
+def test_autotune_on_the_vegas_loop_stage(gpu, params_screened):
+    """With VEGAS initialised the autotuner times the loop stage of a full pass on the
+    engine's grid; the passes after it integrate as before."""
+    import graniitti_gb300 as g
+    from graniitti_gb300 import _abi
+    P = params_screened
+    e = _engine(P)
+    e.eikonal_build(512, 2000)
+    vp = _abi.VegasParams()
+    vp.bins, vp.iter, vp.ncall, vp.lambda_ = 128, 5, 1 << 17, 1.5
+    vp.chi2max, vp.precision, vp.burnin_iter, vp.prec, vp.seed = 10.0, 1e-3, 3, g.MIXED, 3
+    e.vegas_init(vp)
+    for it in range(2):
+        e.vegas_iteration(mode=0, refine=True, iter_id=1 + it)
+    grid = e.vegas_grid()
+    r = e.autotune()
+    ms = list(r.ms)[:r.n_candidates]
+    print("VEGAS-stage autotune: %d candidates on %d listed events, ms %s, best %d x %d" %
+          (r.n_candidates, r.sample_events, np.round(ms, 3), r.best.loop_pair,
+           r.best.vegas_blocks))
+    assert r.n_candidates == 8 and 0 < r.sample_events <= vp.ncall
+    assert np.array_equal(e.vegas_grid(), grid)  # tuning does not refine
+    res = [e.vegas_iteration(mode=1, refine=True, iter_id=10 + it) for it in range(2)]
+    e.set_tuning(loop_pair=0)
+    e.vegas_set_grid(grid)
+    assert res[-1].sigma > 0 and res[-1].nan_count == 0
