@@ -121,6 +121,18 @@ class FlatParams(ctypes.Structure):
                 ("prec", c_int32), ("_pad", c_int32), ("seed", c_uint64)]
 
 
+OBS = ["M", "Y", "PT", "DPHI_PP", "PT1", "M0", "RAP3", "RAP4",
+       "COSTH_CS", "PHI_CS", "COSTH_HX", "PHI_HX", "COSTH_AH", "PHI_AH", "COSTH_PG", "PHI_PG",
+       "COSTH_CM", "PHI_CM", "COSTH_LA", "PHI_LA"]
+GRN_NUM_OBS = len(OBS)
+GRN_MAX_HIST = 32
+
+
+class HistSpec(ctypes.Structure):
+    _fields_ = [("obs", c_int32), ("nbins", c_int32), ("lo", c_double), ("hi", c_double),
+                ("obs2", c_int32), ("nbins2", c_int32), ("lo2", c_double), ("hi2", c_double)]
+
+
 class Tuning(ctypes.Structure):
     _fields_ = [("loop_pair", c_int32), ("vegas_blocks", c_int32), ("weight_blocks", c_int32),
                 ("fp64_refine", c_int32)]
@@ -209,6 +221,11 @@ SIGNATURES = {
     "grn_unweight": (c_int32, [c_void_p, c_double, c_uint64, c_void_p, c_void_p, c_void_p,
                                c_int64]),
     "grn_vegas_points": (c_int32, [c_void_p, c_void_p, c_int64, c_void_p]),
+    "grn_pass_weights": (c_int32, [c_void_p, c_void_p, c_int64]),
+    "grn_hist_define": (c_int32, [c_void_p, c_void_p, c_int32]),
+    "grn_hist_fill": (c_int32, [c_void_p]),
+    "grn_hist_get": (c_int32, [c_void_p, c_int32, c_void_p, c_void_p, c_void_p, c_void_p]),
+    "grn_hist_clear": (c_int32, [c_void_p]),
     "grn_kernel_timing": (c_int32, [c_void_p, c_int32, c_void_p, c_void_p]),
     "grn_fp32_peak": (c_int32, [c_int32, c_void_p]),
     "grn_flow_default_params": (None, [c_void_p]),

@@ -108,6 +108,10 @@ struct grn_engine {
   DevBuf      d_xmat_flat;  // uniform grid of FLAT passes (x = u, vw = 1)
   DevBuf      d_lidx, d_lx, d_lvw, d_lbins, d_lbins_hi;  // screened work list of a VEGAS pass
   DevBuf      d_rlist;  // slots of that list refined in FP64
+  // on-the-fly histograms: specs (host copy and device), bin offsets, sums
+  std::vector<grn_hist_spec> hist;
+  std::vector<int>           hist_off;
+  DevBuf                     d_hspec, d_hoff, d_hw, d_hw2, d_hcnt, d_hout;
   DevBuf      d_recf, d_recd;                // loop records (record mode), shared by calls
   double     *h_sc = nullptr;  // pinned
   double      sumdata = 0, sumchi2 = 0, sweight = 0;
@@ -565,7 +569,8 @@ grn_status grn_destroy(grn_engine *e) {
                     &e->d_wlist, &e->d_wcount, &e->d_xmat,      &e->d_xmat_prev, &e->d_f2mat,
                     &e->d_f,     &e->d_acc,    &e->d_parts,     &e->d_sc,        &e->d_lidx,
                     &e->d_lx,    &e->d_lvw,    &e->d_lbins,     &e->d_uw_counts, &e->d_uw_misc,
-                    &e->d_lbins_hi, &e->d_rlist, &e->d_wrlist,
+                    &e->d_lbins_hi, &e->d_rlist, &e->d_wrlist, &e->d_hspec, &e->d_hoff,
+                    &e->d_hw, &e->d_hw2, &e->d_hcnt, &e->d_hout,
                     &e->d_uw_idx, &e->d_recf,  &e->d_recd,      &e->d_xmat_flat};
   for (DevBuf *b : bufs) b->release();
   for (grn_flow *f : e->flows) f->e = nullptr;  // they stay valid for grn_flow_destroy
@@ -1206,6 +1211,111 @@ grn_status grn_vegas_points(grn_engine *e, const int64_t *idx, int64_t n, double
                                     e->d_aux.as<double>(), e->stream, e->last_fu, e->last_ncall));
   GRN_CUDA(cudaMemcpyAsync(u_out, e->d_aux.p, n * e->dim * sizeof(double), cudaMemcpyDefault,
                            e->stream));
+  GRN_CUDA(cudaStreamSynchronize(e->stream));
+  return GRN_OK;
+}
+
+grn_status grn_pass_weights(grn_engine *e, double *f_out, int64_t n) {
+  if (!e || !f_out) return fail(GRN_ERR_INVALID, "null argument");
+  if (!e->have_last) return fail(GRN_ERR_STATE, "no VEGAS iteration");
+  if (n != e->last_ncall) return fail(GRN_ERR_INVALID, "n must be the last pass's ncall");
+  GRN_CUDA(cudaSetDevice(e->device));
+  GRN_CUDA(cudaMemcpyAsync(f_out, e->d_f.p, n * sizeof(double), cudaMemcpyDefault, e->stream));
+  GRN_CUDA(cudaStreamSynchronize(e->stream));
+  return GRN_OK;
+}
+
+// ---------------------------------------------------------------------------
+// On-the-fly histograms
+
+static int hist_bins(const grn_hist_spec &s) { return s.nbins * (s.nbins2 > 0 ? s.nbins2 : 1); }
+
+grn_status grn_hist_define(grn_engine *e, const grn_hist_spec *specs, int32_t n) {
+  if (!e || (n > 0 && !specs) || n < 0 || n > GRN_MAX_HIST)
+    return fail(GRN_ERR_INVALID, "bad histogram list (at most GRN_MAX_HIST)");
+  int total = 0;
+  std::vector<int> off(n);
+  for (int h = 0; h < n; ++h) {
+    const grn_hist_spec &s = specs[h];
+    const bool two = s.nbins2 > 0;
+    if (s.obs < 0 || s.obs >= GRN_NUM_OBS || s.nbins < 1 || s.nbins > 100000 ||
+        !(s.hi > s.lo) || (two && (s.obs2 < 0 || s.obs2 >= GRN_NUM_OBS || s.nbins2 > 100000 ||
+                                   !(s.hi2 > s.lo2))))
+      return fail(GRN_ERR_INVALID, "bad histogram spec");
+    off[h] = total;
+    total += hist_bins(s);
+    if (total > (1 << 24)) return fail(GRN_ERR_INVALID, "too many histogram bins");
+  }
+  GRN_CUDA(cudaSetDevice(e->device));
+  e->hist.assign(specs, specs + n);
+  e->hist_off = off;
+  const size_t nb = std::max(total, 1);
+  GRN_CUDA(e->d_hspec.ensure(std::max(n, 1) * sizeof(grn_hist_spec)));
+  GRN_CUDA(e->d_hoff.ensure(std::max(n, 1) * sizeof(int)));
+  GRN_CUDA(e->d_hw.ensure(nb * sizeof(double)));
+  GRN_CUDA(e->d_hw2.ensure(nb * sizeof(double)));
+  GRN_CUDA(e->d_hcnt.ensure(nb * sizeof(unsigned long long)));
+  GRN_CUDA(e->d_hout.ensure(3 * std::max(n, 1) * sizeof(unsigned long long)));
+  if (n > 0) {
+    GRN_CUDA(cudaMemcpyAsync(e->d_hspec.p, specs, n * sizeof(grn_hist_spec),
+                             cudaMemcpyHostToDevice, e->stream));
+    GRN_CUDA(cudaMemcpyAsync(e->d_hoff.p, off.data(), n * sizeof(int), cudaMemcpyHostToDevice,
+                             e->stream));
+  }
+  return grn_hist_clear(e);
+}
+
+grn_status grn_hist_clear(grn_engine *e) {
+  if (!e) return fail(GRN_ERR_INVALID, "null engine");
+  GRN_CUDA(cudaSetDevice(e->device));
+  const int n = static_cast<int>(e->hist.size());
+  int total = 0;
+  for (const grn_hist_spec &s : e->hist) total += hist_bins(s);
+  if (total > 0) {
+    GRN_CUDA(cudaMemsetAsync(e->d_hw.p, 0, total * sizeof(double), e->stream));
+    GRN_CUDA(cudaMemsetAsync(e->d_hw2.p, 0, total * sizeof(double), e->stream));
+    GRN_CUDA(cudaMemsetAsync(e->d_hcnt.p, 0, total * sizeof(unsigned long long), e->stream));
+  }
+  if (n > 0)
+    GRN_CUDA(cudaMemsetAsync(e->d_hout.p, 0, 3 * n * sizeof(unsigned long long), e->stream));
+  GRN_CUDA(cudaStreamSynchronize(e->stream));
+  return GRN_OK;
+}
+
+grn_status grn_hist_fill(grn_engine *e) {
+  if (!e) return fail(GRN_ERR_INVALID, "null engine");
+  if (!e->have_last) return fail(GRN_ERR_STATE, "no VEGAS iteration");
+  if (e->hist.empty()) return GRN_OK;
+  GRN_CUDA(cudaSetDevice(e->device));
+  GRN_CUDA(grn::launch_hist_fill(e->args(), e->d_xmat_prev.as<double>(), e->bins, e->dim,
+                                 e->last_ncall, e->seed, e->last_stream, e->last_fu,
+                                 e->d_f.as<double>(), e->d_hspec.as<grn_hist_spec>(),
+                                 e->d_hoff.as<int>(), static_cast<int>(e->hist.size()),
+                                 e->d_hw.as<double>(), e->d_hw2.as<double>(),
+                                 e->d_hcnt.as<unsigned long long>(),
+                                 e->d_hout.as<unsigned long long>(), e->stream));
+  GRN_CUDA(cudaStreamSynchronize(e->stream));
+  return GRN_OK;
+}
+
+grn_status grn_hist_get(grn_engine *e, int32_t h, double *w, double *w2, int64_t *counts,
+                        int64_t *outside) {
+  if (!e || h < 0 || h >= static_cast<int32_t>(e->hist.size()))
+    return fail(GRN_ERR_INVALID, "bad histogram index");
+  GRN_CUDA(cudaSetDevice(e->device));
+  const int off = e->hist_off[h], nb = hist_bins(e->hist[h]);
+  if (w)
+    GRN_CUDA(cudaMemcpyAsync(w, e->d_hw.as<double>() + off, nb * sizeof(double),
+                             cudaMemcpyDefault, e->stream));
+  if (w2)
+    GRN_CUDA(cudaMemcpyAsync(w2, e->d_hw2.as<double>() + off, nb * sizeof(double),
+                             cudaMemcpyDefault, e->stream));
+  if (counts)
+    GRN_CUDA(cudaMemcpyAsync(counts, e->d_hcnt.as<unsigned long long>() + off,
+                             nb * sizeof(int64_t), cudaMemcpyDefault, e->stream));
+  if (outside)
+    GRN_CUDA(cudaMemcpyAsync(outside, e->d_hout.as<unsigned long long>() + 3 * h,
+                             3 * sizeof(int64_t), cudaMemcpyDefault, e->stream));
   GRN_CUDA(cudaStreamSynchronize(e->stream));
   return GRN_OK;
 }

@@ -164,6 +164,16 @@ cudaError_t launch_batch_loop(int np, unsigned long long *counter, int nblocks, 
                               cudaStream_t st);
 int         batch_loop_blocks(int device, int max_nh);
 
+// On-the-fly histograms: every point e < ncall of the last pass with f[e] > 0 (its point from
+// Philox (seed, stream) or the flow points fu, ld ncall; the grid xmat of that pass) adds f[e]
+// to the bin of each of the nh histograms (specs on the device; w, w2, cnt at offsets off[h];
+// outside: 3 counters per histogram).
+cudaError_t launch_hist_fill(const KArgs &a, const double *xmat, int bins, int dim, int64_t ncall,
+                             uint64_t seed, uint32_t stream, const float *fu, const double *f,
+                             const grn_hist_spec *specs, const int *off, int nh, double *w,
+                             double *w2, unsigned long long *cnt, unsigned long long *outside,
+                             cudaStream_t st);
+
 // FP32 FMA throughput probe: returns flops executed by one launch.
 double      fma_probe_flops(int blocks, int threads, int iters);
 cudaError_t launch_fma_probe(int blocks, int threads, int iters, float *sink, cudaStream_t st);

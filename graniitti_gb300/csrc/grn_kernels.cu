@@ -1014,6 +1014,79 @@ __device__ void flush_block(double *sf2, int nh, double *f2mat, unsigned long lo
     if (sf2[i] != 0.0) atomicAdd(&f2mat[i], sf2[i]);
 }
 
+// ---------------------------------------------------------------------------
+// On-the-fly histograms (MUserHistograms::FillHistograms, src/MUserHistograms.cc:60-125).
+
+__device__ __forceinline__ int hist_bin(double v, int n, double lo, double hi) {
+  if (v != v) return -3;
+  if (v < lo) return -1;
+  if (v >= hi) return -2;
+  const int k = static_cast<int>((v - lo) / (hi - lo) * n);
+  return k < n ? k : n - 1;
+}
+
+template <int MAXD>
+__global__ void __launch_bounds__(128)
+    k_hist_fill(const KArgs A, const double *__restrict__ xmat, int bins, int dim, int64_t ncall,
+                uint64_t seed, uint32_t stream, const float *__restrict__ fu,
+                const double *__restrict__ f, const grn_hist_spec *__restrict__ specs,
+                const int *__restrict__ off, int nh, double *__restrict__ w,
+                double *__restrict__ w2, unsigned long long *__restrict__ cnt,
+                unsigned long long *__restrict__ outside) {
+  for (int64_t e = static_cast<int64_t>(blockIdx.x) * blockDim.x + threadIdx.x; e < ncall;
+       e += static_cast<int64_t>(gridDim.x) * blockDim.x) {
+    const double fe = f[e];
+    if (!(fe > 0.0)) continue;
+    double u[MAXD], x[MAXD];
+    if (fu) {
+      for (int j = 0; j < dim; ++j) u[j] = fu[static_cast<int64_t>(j) * ncall + e];
+    } else {
+      philox_point(seed, stream, static_cast<uint64_t>(e), dim, u);
+    }
+    uint64_t pb, pbh;
+    vegas_map(xmat, bins, dim, u, x, pb, pbh);
+    Born b;
+    if (!born_kinematics<(MAXD > 8)>(A.P, A.K, x, b)) continue;
+    double o[GRN_NUM_OBS];
+    event_observables(A.K, b, o);
+    for (int h = 0; h < nh; ++h) {
+      const grn_hist_spec s = specs[h];
+      int k = hist_bin(o[s.obs], s.nbins, s.lo, s.hi);
+      if (k >= 0 && s.nbins2 > 0) {
+        const int k2 = hist_bin(o[s.obs2], s.nbins2, s.lo2, s.hi2);
+        k = k2 < 0 ? k2 : k * s.nbins2 + k2;
+      }
+      if (k < 0) {
+        atomicAdd(&outside[3 * h + (k == -1 ? 0 : (k == -2 ? 1 : 2))], 1ull);
+        continue;
+      }
+      atomicAdd(&w[off[h] + k], fe);
+      atomicAdd(&w2[off[h] + k], fe * fe);
+      atomicAdd(&cnt[off[h] + k], 1ull);
+    }
+  }
+}
+
+cudaError_t launch_hist_fill(const KArgs &a, const double *xmat, int bins, int dim, int64_t ncall,
+                             uint64_t seed, uint32_t stream, const float *fu, const double *f,
+                             const grn_hist_spec *specs, const int *off, int nh, double *w,
+                             double *w2, unsigned long long *cnt, unsigned long long *outside,
+                             cudaStream_t st) {
+  if (ncall <= 0 || nh <= 0) return cudaSuccess;
+  int sms = 0, dev = 0;
+  cudaGetDevice(&dev);
+  cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+  const int64_t want = (ncall + 127) / 128;
+  const int grid = static_cast<int>(std::min<int64_t>(want, static_cast<int64_t>(sms) * 8));
+  if (dim <= 8)
+    k_hist_fill<8><<<grid, 128, 0, st>>>(a, xmat, bins, dim, ncall, seed, stream, fu, f, specs,
+                                          off, nh, w, w2, cnt, outside);
+  else
+    k_hist_fill<kMaxDim><<<grid, 128, 0, st>>>(a, xmat, bins, dim, ncall, seed, stream, fu, f,
+                                                specs, off, nh, w, w2, cnt, outside);
+  return cudaGetLastError();
+}
+
 // Stage A of a VEGAS pass: Philox (or flow) points, grid map, tree-level kinematics and
 // cuts. Rejected and unscreened events are finished here; screened events that pass the
 // cuts go to the work list (index, VEGAS weight, bins, and the loop record or the mapped

@@ -1558,6 +1558,66 @@ GRN_HD void make_loop_event(const Consts &K, const Born &b, LoopEvent<T> &e) {
   }
 }
 
+// Observables of a Born point (GRN_OBS_* order), for the on-the-fly histograms.
+GRN_HD_COLD void event_observables(const Consts &K, const Born &b, double *o) {
+  const double Xp = b.p3p + b.p4p, Xm = b.p3m + b.p4m, Xx = b.p3x + b.p4x, Xy = b.p3y + b.p4y;
+  const double Xe = 0.5 * (Xp + Xm), Xz = 0.5 * (Xp - Xm), M = sqrt(fmax(b.m2, 0.0));
+  o[GRN_OBS_M]  = M;
+  o[GRN_OBS_Y]  = 0.5 * log(Xp / Xm);
+  o[GRN_OBS_PT] = sqrt(Xx * Xx + Xy * Xy);
+  double dphi   = atan2(b.p1y, b.p1x) - atan2(b.p2y, b.p2x);
+  while (dphi >= kPi) dphi -= 2.0 * kPi;
+  while (dphi < -kPi) dphi += 2.0 * kPi;
+  o[GRN_OBS_DPHI_PP] = fabs(dphi);
+  o[GRN_OBS_PT1]     = sqrt(b.pt1sq);
+  o[GRN_OBS_M0]      = sqrt(b.m3sq);
+  o[GRN_OBS_RAP3]    = b.y3;
+  o[GRN_OBS_RAP4]    = b.y4;
+  // first central particle and the beams in the X rest frame
+  double px = b.p3x, py = b.p3y, pz = 0.5 * (b.p3p - b.p3m);
+  const double pe = 0.5 * (b.p3p + b.p3m);
+  o[GRN_OBS_COSTH_LA] = pz / sqrt(px * px + py * py + pz * pz);
+  o[GRN_OBS_PHI_LA]   = atan2(py, px);
+  boost_to_rest<double>(Xe, Xx, Xy, Xz, M, pe, px, py, pz);
+  const double E = 0.5 * K.sqrt_s, bz = 0.5 * (K.L - K.eps);
+  double a[3] = {0.0, 0.0, bz}, c[3] = {0.0, 0.0, -bz};
+  boost_to_rest<double>(Xe, Xx, Xy, Xz, M, E, a[0], a[1], a[2]);
+  boost_to_rest<double>(Xe, Xx, Xy, Xz, M, E, c[0], c[1], c[2]);
+  auto unit = [](double *v) {
+    const double n = sqrt(v[0] * v[0] + v[1] * v[1] + v[2] * v[2]);
+    v[0] /= n; v[1] /= n; v[2] /= n;
+  };
+  auto cross = [](const double *u, const double *v, double *w) {
+    w[0] = u[1] * v[2] - u[2] * v[1];
+    w[1] = u[2] * v[0] - u[0] * v[2];
+    w[2] = u[0] * v[1] - u[1] * v[0];
+  };
+  double ua[3] = {a[0], a[1], a[2]}, uc[3] = {c[0], c[1], c[2]};
+  unit(ua);
+  unit(uc);
+  double y[3];
+  cross(ua, uc, y);
+  unit(y);
+  const double pn = sqrt(px * px + py * py + pz * pz);
+  for (int f = 0; f < 5; ++f) {  // CS, HX, AH, PG, CM
+    double z[3], yy[3] = {y[0], y[1], y[2]};
+    if (f == 0) { z[0] = ua[0] - uc[0]; z[1] = ua[1] - uc[1]; z[2] = ua[2] - uc[2]; }
+    if (f == 1) { z[0] = -(a[0] + c[0]); z[1] = -(a[1] + c[1]); z[2] = -(a[2] + c[2]); }
+    if (f == 2) { z[0] = ua[0] + uc[0]; z[1] = ua[1] + uc[1]; z[2] = ua[2] + uc[2]; }
+    if (f == 3) { z[0] = c[0]; z[1] = c[1]; z[2] = c[2]; }
+    if (f == 4) { z[0] = 0.0; z[1] = 0.0; z[2] = 1.0; yy[0] = 0.0; yy[1] = 1.0; yy[2] = 0.0; }
+    unit(z);
+    double x[3];
+    cross(yy, z, x);
+    unit(x);
+    const double qx = px * x[0] + py * x[1] + pz * x[2];
+    const double qy = px * yy[0] + py * yy[1] + pz * yy[2];
+    const double qz = px * z[0] + py * z[1] + pz * z[2];
+    o[GRN_OBS_COSTH_CS + 2 * f] = qz / pn;
+    o[GRN_OBS_PHI_CS + 2 * f]   = (qx == 0.0 && qy == 0.0) ? 0.0 : atan2(qy, qx);
+  }
+}
+
 GRN_HD bool is_regge_res(const grn_process_params &P) {
   return P.process == GRN_PROC_REGGE_RES || P.process == GRN_PROC_REGGE_RESCON;
 }

@@ -190,6 +190,42 @@ class Engine:
         _abi.check(self.lib.grn_vegas_points(self.h, _ptr(idx), idx.shape[0], _ptr(out)))
         return out
 
+    def pass_weights(self, n):
+        """f of every point of the last iteration (n = its ncall)."""
+        f = np.zeros(n)
+        _abi.check(self.lib.grn_pass_weights(self.h, _ptr(f), n))
+        return f
+
+    # On-the-fly histograms: specs are (obs, nbins, lo, hi) or
+    # (obs, nbins, lo, hi, obs2, nbins2, lo2, hi2) with obs a name of _abi.OBS.
+    def hist_define(self, specs):
+        arr = (_abi.HistSpec * max(len(specs), 1))()
+        self.hist_shapes = []
+        for k, s in enumerate(specs):
+            a = arr[k]
+            a.obs, a.nbins, a.lo, a.hi = _abi.OBS.index(s[0]), s[1], s[2], s[3]
+            if len(s) > 4:
+                a.obs2, a.nbins2, a.lo2, a.hi2 = _abi.OBS.index(s[4]), s[5], s[6], s[7]
+                self.hist_shapes.append((s[1], s[5]))
+            else:
+                self.hist_shapes.append((s[1],))
+        _abi.check(self.lib.grn_hist_define(self.h, arr, len(specs)))
+
+    def hist_fill(self):
+        _abi.check(self.lib.grn_hist_fill(self.h))
+
+    def hist_clear(self):
+        _abi.check(self.lib.grn_hist_clear(self.h))
+
+    def hist_get(self, h):
+        """(sum of weights, sum of squared weights, fill counts, [below, above, NaN])."""
+        shape = self.hist_shapes[h]
+        nb = int(np.prod(shape))
+        w, w2 = np.zeros(nb), np.zeros(nb)
+        c, out = np.zeros(nb, dtype=np.int64), np.zeros(3, dtype=np.int64)
+        _abi.check(self.lib.grn_hist_get(self.h, h, _ptr(w), _ptr(w2), _ptr(c), _ptr(out)))
+        return w.reshape(shape), w2.reshape(shape), c.reshape(shape), out
+
 
 class Flow:
     """Coupling-layer spline flow in front of the engine's VEGAS map (grn_flow_*).

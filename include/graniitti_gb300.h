@@ -385,6 +385,47 @@ grn_status grn_unweight(grn_engine *e, double fmax, uint64_t seed, int64_t *n_ac
  * building (MProcess::EventRecord on the host). */
 grn_status grn_vegas_points(grn_engine *e, const int64_t *idx, int64_t n, double *u_out);
 
+/* The weights f = W vw (/ q for flow passes) of every point of the last iteration, in point
+ * order (n = the pass's ncall; host or device). */
+grn_status grn_pass_weights(grn_engine *e, double *f_out, int64_t n);
+
+/* ------------------------------------------------------------------------ */
+/* On-the-fly histograms (MUserHistograms, src/MUserHistograms.cc:23-125)     */
+/* ------------------------------------------------------------------------ */
+/* Observables of a point (the reference's level-1 and level-2 histograms): central system
+ * mass, rapidity, pT; |delta phi| and pT of the forward legs; mass of the first central
+ * particle (cascades); rapidities of the two central particles; cos(theta) and phi of the
+ * first central particle in the Collins-Soper, helicity, anti-helicity, pseudo-Gottfried-Jackson
+ * (beam 2) and non-rotated rest frames of the system (kinematics::LorentzFrame,
+ * MKinematics.h:952-1011) and in the lab. */
+enum {
+  GRN_OBS_M = 0, GRN_OBS_Y, GRN_OBS_PT, GRN_OBS_DPHI_PP, GRN_OBS_PT1, GRN_OBS_M0,
+  GRN_OBS_RAP3, GRN_OBS_RAP4,
+  GRN_OBS_COSTH_CS, GRN_OBS_PHI_CS, GRN_OBS_COSTH_HX, GRN_OBS_PHI_HX,
+  GRN_OBS_COSTH_AH, GRN_OBS_PHI_AH, GRN_OBS_COSTH_PG, GRN_OBS_PHI_PG,
+  GRN_OBS_COSTH_CM, GRN_OBS_PHI_CM, GRN_OBS_COSTH_LA, GRN_OBS_PHI_LA,
+  GRN_NUM_OBS
+};
+/* One histogram: nbins uniform bins of [lo, hi) of obs; 2D with nbins2 > 0 (bin index
+ * ix * nbins2 + iy). */
+typedef struct grn_hist_spec {
+  int32_t obs, nbins;
+  double  lo, hi;
+  int32_t obs2, nbins2;
+  double  lo2, hi2;
+} grn_hist_spec;
+#define GRN_MAX_HIST 32
+/* Replace the engine's histograms by n specs (cleared). */
+grn_status grn_hist_define(grn_engine *e, const grn_hist_spec *specs, int32_t n);
+/* Add the points of the last iteration (VEGAS, flow or batched pass) with f > 0, each with
+ * weight f (the reference's total weight W x VEGAS weight), on the device. */
+grn_status grn_hist_fill(grn_engine *e);
+/* Histogram h: sum of weights and of squared weights and the fill count per bin; outside[3]:
+ * fills below, above (either coordinate) and NaN. Any pointer may be NULL. */
+grn_status grn_hist_get(grn_engine *e, int32_t h, double *w, double *w2, int64_t *counts,
+                        int64_t *outside);
+grn_status grn_hist_clear(grn_engine *e);
+
 /* ------------------------------------------------------------------------ */
 /* Learned proposal: coupling-layer spline flow in front of the VEGAS map     */
 /* ------------------------------------------------------------------------ */

@@ -1183,6 +1183,52 @@ cplx regge_res(const Setup &S, const Event &ev) {
   return prop * sum;
 }
 
+// ---------------------------------------------------------------------------
+// Observables of the on-the-fly histograms (MUserHistograms::FillHistograms,
+// src/MUserHistograms.cc:60-125, frames of kinematics::LorentzFrame, MKinematics.h:952-1011):
+// order M, Y, Pt, |dphi_pp|, pT1, m(first central), y3, y4, then (cos theta, phi) of the first
+// central particle in CS, HX, AH, PG (beam 2), CM and the lab.
+void observables(const Setup &S, const Event &ev, double *o) {
+  const V4 &X = ev.pf[0];
+  o[0] = X.m();
+  o[1] = X.rap();
+  o[2] = X.pt();
+  double D = std::atan2(ev.pf[1].y, ev.pf[1].x) - std::atan2(ev.pf[2].y, ev.pf[2].x);
+  while (D >= PI) D -= 2 * PI;
+  while (D < -PI) D += 2 * PI;
+  o[3] = std::fabs(D);
+  o[4] = ev.pf[1].pt();
+  o[5] = ev.pf[3].m();
+  o[6] = ev.pf[3].rap();
+  o[7] = ev.pf[4].rap();
+  const V4 p = to_rest(X, ev.pf[3]), b1 = to_rest(X, S.pb1), b2 = to_rest(X, S.pb2);
+  using A3 = std::array<double, 3>;
+  auto unit = [](A3 v) {
+    const double n = std::sqrt(v[0] * v[0] + v[1] * v[1] + v[2] * v[2]);
+    return A3{v[0] / n, v[1] / n, v[2] / n};
+  };
+  auto cross = [](const A3 &u, const A3 &v) {
+    return A3{u[1] * v[2] - u[2] * v[1], u[2] * v[0] - u[0] * v[2], u[0] * v[1] - u[1] * v[0]};
+  };
+  const A3 P3 = {p.x, p.y, p.z}, B1 = {b1.x, b1.y, b1.z}, B2 = {b2.x, b2.y, b2.z};
+  const A3 u1 = unit(B1), u2 = unit(B2);
+  const A3 zs[5] = {unit({u1[0] - u2[0], u1[1] - u2[1], u1[2] - u2[2]}),
+                    unit({-(B1[0] + B2[0]), -(B1[1] + B2[1]), -(B1[2] + B2[2])}),
+                    unit({u1[0] + u2[0], u1[1] + u2[1], u1[2] + u2[2]}), u2, A3{0, 0, 1}};
+  for (int f = 0; f < 5; ++f) {
+    const A3 y = f == 4 ? A3{0, 1, 0} : unit(cross(u1, u2));
+    const A3 x = unit(cross(y, zs[f]));
+    const double qx = x[0] * P3[0] + x[1] * P3[1] + x[2] * P3[2];
+    const double qy = y[0] * P3[0] + y[1] * P3[1] + y[2] * P3[2];
+    const double qz = zs[f][0] * P3[0] + zs[f][1] * P3[1] + zs[f][2] * P3[2];
+    o[8 + 2 * f] = std::cos(std::atan2(std::sqrt(qx * qx + qy * qy), qz));
+    o[9 + 2 * f] = (qx == 0 && qy == 0) ? 0.0 : std::atan2(qy, qx);
+  }
+  const V4 &l = ev.pf[3];
+  o[18] = std::cos(std::atan2(l.pt(), l.z));
+  o[19] = (l.x == 0 && l.y == 0) ? 0.0 : std::atan2(l.y, l.x);
+}
+
 // RES+CONTENSOR (MSubProc.h:319-351): the continuum's and the resonances' helicity amplitudes
 // are added per proton configuration; with the high-energy proton vertex all four are equal,
 // so the sum of one configuration carries |M|^2.
@@ -1363,6 +1409,27 @@ int orc_weights(const grn_process_params *p, const double *u, int64_t n, int32_t
           r[3 + 4 * k + 3] = v.e;
         }
       }
+    }
+  });
+  return GRN_OK;
+}
+
+// Histogram observables (20 per point, see orc::observables) of the points that pass the
+// kinematics (ok[i] = 1), from the tree-level event.
+int orc_observables(const grn_process_params *p, const double *u, int64_t n, int32_t dim,
+                    double *obs, uint8_t *ok, int32_t nthreads) {
+  const int32_t want = p && p->n_decay == 2 ? 14 : 8;
+  if (!p || !u || !obs || dim != want || p->n_central != 2) return GRN_ERR_INVALID;
+  grn_process_params q = *p;
+  q.screening = 0;
+  const orc::Setup S = orc::make_setup(&q, nullptr, 0);
+  orc::parallel_for(n, nthreads, [&](int64_t a, int64_t b) {
+    for (int64_t i = a; i < b; ++i) {
+      uint8_t    f  = 0;
+      orc::Event ev = orc::Event();
+      orc::event_weight(S, u + i * dim, f, ev);
+      ok[i] = (f & GRN_FLAG_KINEMATICS_OK) ? 1 : 0;
+      if (ok[i]) orc::observables(S, ev, obs + i * 20);
     }
   });
   return GRN_OK;

@@ -30,6 +30,9 @@ def lib():
                                   ctypes.c_int32, ctypes.c_int32]
         L.orc_eikonal.restype = ctypes.c_int
         L.orc_eikonal.argtypes = [vp, ctypes.c_int32, ctypes.c_int32, vp, vp, vp, ctypes.c_int32]
+        L.orc_observables.restype = ctypes.c_int
+        L.orc_observables.argtypes = [vp, vp, ctypes.c_int64, ctypes.c_int32, vp, vp,
+                                      ctypes.c_int32]
         L.orc_bessel_j0.restype = ctypes.c_double
         L.orc_bessel_j0.argtypes = [ctypes.c_double]
         L.orc_vegas_grid_init.argtypes = [ctypes.c_int32, ctypes.c_int32, vp]
@@ -64,6 +67,19 @@ def weights(params, u, msa=None, nthreads=1, with_rec=False):
     if st != 0:
         raise RuntimeError("orc_weights status %d" % st)
     return (w, fl, rec) if with_rec else (w, fl)
+
+
+def observables(params, u, nthreads=4):
+    """(obs (n, 20), ok (n,)): the histogram observables (GRN_OBS_* order) of each point that
+    passes the kinematics."""
+    u = np.ascontiguousarray(u, dtype=np.float64)
+    n, dim = u.shape
+    obs = np.full((n, 20), np.nan)
+    ok = np.zeros(n, dtype=np.uint8)
+    st = lib().orc_observables(ctypes.byref(params), _p(u), n, dim, _p(obs), _p(ok), nthreads)
+    if st != 0:
+        raise RuntimeError("orc_observables status %d" % st)
+    return obs, ok.astype(bool)
 
 
 def eikonal(params, n_bt, n_kt2, nthreads=8, with_msa=True):

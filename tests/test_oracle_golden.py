@@ -205,3 +205,77 @@ def test_vector_pair_cascade_weights(name):
     leaves = rec[:, 19:35].reshape(-1, 4, 4)
     scale = np.abs(g["leaves"]).max(axis=2, keepdims=True)
     assert (np.abs(leaves - g["leaves"])[kin] / scale[kin]).max() < 1e-12
+
+
+def _np_rest(X, p):
+    """p (n, 4: px, py, pz, E) boosted to the rest frame of X (n, 4)."""
+    m = np.sqrt(X[:, 3] ** 2 - (X[:, :3] ** 2).sum(1))
+    b = X[:, :3] / X[:, 3:4]
+    g = X[:, 3] / m
+    bp = (b * p[:, :3]).sum(1)
+    b2 = (b * b).sum(1)
+    k = np.where(b2 > 0, (g - 1) * bp / np.where(b2 > 0, b2, 1), 0.0) - g * p[:, 3]
+    return np.column_stack([p[:, :3] + k[:, None] * b, g * (p[:, 3] - bp)])
+
+
+def test_histogram_observables_from_reference_kinematics(params):
+    """orc_observables against a numpy restatement of the reference's observables
+    (MUserHistograms::FillHistograms, src/MUserHistograms.cc:60-125; frames of
+    kinematics::LorentzFrame, MKinematics.h:952-1011) evaluated on the reference's own
+    4-momenta of the same points."""
+    from graniitti_gb300 import _abi
+    g = _load("c1_tune0_weights.npz")
+    kin = g["kin"] == 1
+    obs, ok = orc.observables(params, g["u"])
+    assert np.array_equal(ok, kin)
+    p4 = g["p4"][kin]  # forward leg 1, forward leg 2, central 3, central 4
+    o = obs[kin]
+    X = p4[:, 2] + p4[:, 3]
+    n = len(X)
+    ref = {}
+    ref["M"] = np.sqrt(X[:, 3] ** 2 - (X[:, :3] ** 2).sum(1))
+    ref["Y"] = 0.5 * np.log((X[:, 3] + X[:, 2]) / (X[:, 3] - X[:, 2]))
+    ref["PT"] = np.hypot(X[:, 0], X[:, 1])
+    d = np.arctan2(p4[:, 0, 1], p4[:, 0, 0]) - np.arctan2(p4[:, 1, 1], p4[:, 1, 0])
+    d = np.where(d >= np.pi, d - 2 * np.pi, d)
+    d = np.where(d < -np.pi, d + 2 * np.pi, d)
+    ref["DPHI_PP"] = np.abs(d)
+    ref["PT1"] = np.hypot(p4[:, 0, 0], p4[:, 0, 1])
+    for k, j in (("RAP3", 2), ("RAP4", 3)):
+        ref[k] = 0.5 * np.log((p4[:, j, 3] + p4[:, j, 2]) / (p4[:, j, 3] - p4[:, j, 2]))
+    ref["M0"] = np.sqrt(np.maximum(p4[:, 2, 3] ** 2 - (p4[:, 2, :3] ** 2).sum(1), 0))
+    E = 0.5 * params.sqrt_s
+    pz = np.sqrt(E * E - params.m_beam ** 2)
+    b1 = _np_rest(X, np.tile([0, 0, pz, E], (n, 1)))[:, :3]
+    b2 = _np_rest(X, np.tile([0, 0, -pz, E], (n, 1)))[:, :3]
+    p = _np_rest(X, p4[:, 2])[:, :3]
+
+    def unit(v):
+        return v / np.linalg.norm(v, axis=1, keepdims=True)
+
+    u1, u2 = unit(b1), unit(b2)
+    yax = unit(np.cross(u1, u2))
+    frames = {"CS": unit(u1 - u2), "HX": unit(-(b1 + b2)), "AH": unit(u1 + u2), "PG": u2}
+    for name, z in frames.items():
+        x = unit(np.cross(yax, z))
+        q = np.column_stack([(p * x).sum(1), (p * yax).sum(1), (p * z).sum(1)])
+        ref["COSTH_" + name] = q[:, 2] / np.linalg.norm(q, axis=1)
+        ref["PHI_" + name] = np.arctan2(q[:, 1], q[:, 0])
+    ref["COSTH_CM"] = p[:, 2] / np.linalg.norm(p, axis=1)
+    ref["PHI_CM"] = np.arctan2(p[:, 1], p[:, 0])
+    lab = p4[:, 2, :3]
+    ref["COSTH_LA"] = lab[:, 2] / np.linalg.norm(lab, axis=1)
+    ref["PHI_LA"] = np.arctan2(lab[:, 1], lab[:, 0])
+    assert set(ref) == set(_abi.OBS)
+    # the anti-helicity axis is the sum of two nearly opposite unit vectors: its direction
+    # carries the rounding of both divided by their sum's length
+    ah_cond = 1.0 / np.linalg.norm(u1 + u2, axis=1)
+    for k, v in ref.items():
+        mine = o[:, _abi.OBS.index(k)]
+        if k.startswith("PHI"):  # compare angles on the circle
+            diff = np.abs(np.angle(np.exp(1j * (mine - v))))
+        else:
+            diff = np.abs(mine - v) / np.maximum(1.0, np.abs(v))
+        if k.endswith("_AH"):
+            diff = diff / ah_cond
+        assert diff.max() < 1e-8, (k, diff.max())
