@@ -10,6 +10,8 @@ import json
 import math
 import re
 
+import numpy as np
+
 from . import _abi
 from .modeldata import BRANCHING, PARTICLES, RESONANCES, SPIN, TUNES, VECTOR_COUPLING
 
@@ -169,12 +171,15 @@ def build_params(card, process=None, tune=None):
     elif any(f in PARTICLES and PARTICLES[f][2] > 1e-6 for f in finals):
         # the reference draws Breit-Wigner masses for them (MProcess::GetOffShellMass)
         raise UnsupportedProcess("unstable central particles need their decays: a > {c d}")
+    four = len(finals) == 4 and channel == "CON" and cls == "F" and not any(casc)
     if not (istate == "PP" and channel in ("CON", "RES", "RES+CON", "CONTENSOR", "RESTENSOR",
                                            "RES+CONTENSOR") and
-            cls in ("C", "F") and len(finals) == 2):
+            cls in ("C", "F") and (len(finals) == 2 or four)):
         raise UnsupportedProcess(
             "engine implements PP[CON|RES|RES+CON|CONTENSOR|RESTENSOR|RES+CONTENSOR]<C|F> -> "
-            "2-body, got %r" % proc)
+            "2-body and PP[CON]<F> -> 4-body, got %r" % proc)
+    if four and any(SPIN.get(f, 0) != 0 for f in finals):
+        raise UnsupportedProcess("4-body central states of spin-0 particles")
     vec = all(SPIN.get(f, 0) == 1 for f in finals)
     if channel == "CONTENSOR" and not (
             all(f in ("pi+", "pi-", "K+", "K-", "pi0") for f in finals) or
@@ -201,14 +206,14 @@ def build_params(card, process=None, tune=None):
                  "RES+CONTENSOR": _abi.GRN_PROC_TENSOR_RESCON,
                  "RES": _abi.GRN_PROC_REGGE_RES, "RES+CON": _abi.GRN_PROC_REGGE_RESCON}[channel]
     P.phase_space = _abi.GRN_PS_CONTINUUM if cls == "C" else _abi.GRN_PS_FACTORIZED
-    P.n_central = 2
+    P.n_central = len(finals)
     P.screening = 1 if pp.get("POMLOOP", False) else 0
     for k, name in enumerate(finals):
         if name not in PARTICLES:
             raise UnsupportedProcess("unknown final state %s" % name)
         P.m_central[k] = PARTICLES[name][1]
-    # identical-particle factor (MProcess.cc:449-468)
-    P.s_factor = float(math.factorial(2) if finals[0] == finals[1] else 1)
+    # identical-particle factor: product of the multiplicities' factorials (MProcess.cc:449-468)
+    P.s_factor = float(np.prod([math.factorial(finals.count(f)) for f in sorted(set(finals))]))
     P.central_spin = 1 if vec else 0
     if any(casc):
         P.n_decay = 2

@@ -267,7 +267,18 @@ grn_status derive_consts(const grn_process_params &P, grn::Consts &K) {
     }
     K.n_res = P.n_res;
   }
-  if (P.n_central != 2) return fail(GRN_ERR_UNSUPPORTED, "only 2-body central states");
+  const bool nbody = P.n_central == 4;
+  if (P.n_central != 2 && !nbody)
+    return fail(GRN_ERR_UNSUPPORTED, "central states of 2 or 4 particles");
+  if (nbody) {
+    // PP[CON]<F> -> a b c d (MRegge::ME6 with the N-body phase space)
+    if (P.process != GRN_PROC_REGGE_CON || P.phase_space != GRN_PS_FACTORIZED)
+      return fail(GRN_ERR_UNSUPPORTED, "4-body central states: PP[CON]<F> (Regge ME6)");
+    if (P.n_decay != 0 || P.central_spin != 0)
+      return fail(GRN_ERR_UNSUPPORTED, "4-body central states of stable spin-0 particles");
+    for (int k = 0; k < 4; ++k)
+      if (!(P.m_central[k] >= 0)) return fail(GRN_ERR_INVALID, "central masses");
+  }
   if (P.n_decay != 0 && P.n_decay != 2)
     return fail(GRN_ERR_UNSUPPORTED, "central decays: none or two-body cascades of both");
   if (P.central_spin != 0 && P.central_spin != 1)
@@ -324,7 +335,9 @@ grn_status derive_consts(const grn_process_params &P, grn::Consts &K) {
   if (P.phase_space == GRN_PS_FACTORIZED) {
     // mass window (B51RandomKin, MFactorized.cc:263-291): M_MIN = sum of daughter masses
     // + 1e-4 GeV, M_MAX = sqrt(s) - 2 m_beam, both clipped to the <F> generation cuts.
-    const double Mmin = std::max(K.m3 + K.m4 + 1e-4, P.gcuts.M_min);
+    double msum = K.m3 + K.m4;
+    if (nbody) msum = P.m_central[0] + P.m_central[1] + P.m_central[2] + P.m_central[3];
+    const double Mmin = std::max(msum + 1e-4, P.gcuts.M_min);
     const double Mmax = std::min(P.sqrt_s - 2.0 * P.m_beam, P.gcuts.M_max);
     if (!(Mmin < Mmax)) return fail(GRN_ERR_INVALID, "<F> mass window is empty (GENCUTS <F> M)");
     if (!(P.gcuts.Y_max > P.gcuts.Y_min)) return fail(GRN_ERR_INVALID, "<F> rapidity window");
@@ -338,8 +351,11 @@ grn_status derive_consts(const grn_process_params &P, grn::Consts &K) {
     K.w_const = (1.0 / P.s_factor) * (1.0 / (8.0 * kPi * kPi)) * 0.5 *
                 (1.0 / std::pow(2.0 * kPi, 5)) * (P.gcuts.Y_max - P.gcuts.Y_min) * fwd *
                 kGeV2barn / (2.0 * K.s);
+    // N-body: C_space = dPhi_N / (2 pi) comes per event (nbody_jacobian)
+    if (nbody) K.w_const *= 8.0 * kPi * kPi;
   }
-  K.M2prop = K.m3sq;
+  K.M2prop  = K.m3sq;
+  K.M2propB = nbody ? P.m_central[2] * P.m_central[2] : K.m3sq;
   K.g2     = std::pow(P.regge.c[0] / P.soft.gN_P, 2);
   K.gN2    = P.soft.gN_P * P.soft.gN_P;
   K.lns0   = std::log(P.regge.s0);
@@ -546,7 +562,7 @@ grn_status grn_create(const grn_process_params *p, int32_t device, grn_engine **
   e->device     = device;
   e->P          = *p;
   e->K          = K;
-  e->dim        = p->n_decay == 2 ? 14 : 8;
+  e->dim        = (p->n_decay == 2 || p->n_central == 4) ? 14 : 8;
   cudaError_t ce = cudaStreamCreateWithFlags(&e->stream, cudaStreamNonBlocking);
   if (ce == cudaSuccess) ce = cudaMallocHost(&e->h_sc, grn::VS_COUNT * sizeof(double));
   if (ce == cudaSuccess) ce = cudaEventCreate(&e->ev0);
@@ -726,6 +742,8 @@ grn_status grn_event_kinematics(grn_engine *e, const double *u, int64_t n, int32
                                 double *p4_out, double *ts_out, uint8_t *flags) {
   if (!e || !u || n < 0) return fail(GRN_ERR_INVALID, "null argument");
   if (dim != e->dim) return fail(GRN_ERR_INVALID, "dim must equal grn_dim()");
+  if (e->P.n_central != 2)
+    return fail(GRN_ERR_UNSUPPORTED, "event kinematics of 2-body central states only");
   if (n == 0) return GRN_OK;
   GRN_CUDA(cudaSetDevice(e->device));
   // Host-staged path only (diagnostics / record building).
@@ -1285,6 +1303,8 @@ grn_status grn_hist_clear(grn_engine *e) {
 grn_status grn_hist_fill(grn_engine *e) {
   if (!e) return fail(GRN_ERR_INVALID, "null engine");
   if (!e->have_last) return fail(GRN_ERR_STATE, "no VEGAS iteration");
+  if (e->P.n_central != 2)
+    return fail(GRN_ERR_UNSUPPORTED, "histogram observables of 2-body central states only");
   if (e->hist.empty()) return GRN_OK;
   GRN_CUDA(cudaSetDevice(e->device));
   GRN_CUDA(grn::launch_hist_fill(e->args(), e->d_xmat_prev.as<double>(), e->bins, e->dim,

@@ -75,6 +75,10 @@ __device__ __forceinline__ void kahan_add(T &sum, T &comp, T x) {
   sum       = t;
 }
 
+}  // namespace grn
+#include "grn_nbody.cuh"
+namespace grn {
+
 // A_loop = i/(8 pi^2 s) * (9 h_phi h_kt / 64) * sum_ij U_i V_j A_eik(kt_j^2) kt_j A(i, j)
 // (MProcess::S3ScreenedAmp2, src/MProcess.cc:157-261; Simpson38Integral2D,
 // include/Graniitti/MMath.h:457-472). The kt-node factor c_j = V_j kt_j A_eik(kt_j^2)
@@ -383,6 +387,7 @@ __device__ __forceinline__ void record_weights2(const KArgs &A, const LoopEventF
 template <bool CASC>
 __device__ __forceinline__ bool born_stage(const KArgs &A, const double *x, Born &b, double &W,
                                            uint8_t &flags) {
+  if (CASC && is_nbody(A.P)) return nbody_born_stage(A, x, W, flags);
   const bool kin = born_kinematics<CASC>(A.P, A.K, x, b);
   const bool fid = kin && fiducial_cuts(A.P, A.K, b);
   flags = (kin ? GRN_FLAG_KINEMATICS_OK : 0) | (fid ? GRN_FLAG_FIDCUTS_OK : 0) |
@@ -408,6 +413,10 @@ template <typename T, bool CASC>
 __device__ double screened_weight(const KArgs &A, const double *x, uint8_t &flags,
                                   const KtNode<T> *skt, const PhiNode<T> *sphi,
                                   bool *refine = nullptr) {
+  if (CASC && is_nbody(A.P)) {
+    if (refine) *refine = false;
+    return nbody_screened_weight<T>(A, x, flags, skt, sphi);
+  }
   Born b;
   born_kinematics<CASC>(A.P, A.K, x, b);
   double amp2, mag = 0.0;
@@ -640,7 +649,7 @@ __global__ void __launch_bounds__(kWeightThreads, MINB)
 
 bool record_mode(const KArgs &a, int prec) {
   return a.P.screening && prec == GRN_PREC_MIXED && a.K.n_active == 1 &&
-         a.P.process == GRN_PROC_REGGE_CON;
+         a.P.process == GRN_PROC_REGGE_CON && a.P.n_central == 2;
 }
 
 cudaError_t launch_weights_born_rec(const KArgs &a, const double *u, int64_t n, int dim, double *w,

@@ -1,0 +1,347 @@
+// Regge continuum of four central particles in the factorized class: PP[CON]<F> -> a b c d
+// (MRegge::ME6, src/MRegge.cc:470-534), with the central system decayed by the flat N-body
+// phase space of MKinematics.h:523-691 (NBodySetup, NBodyPhaseSpace) and the event weight of
+// MFactorized::EventWeight (src/MFactorized.cc:142-184).
+//
+// Hypercube (14 coordinates): u[0..5] the factorized skeleton (log pT of the forward legs,
+// their azimuths, the system rapidity and mass^2), u[6], u[7] the two intermediate-mass draws
+// of NBodySetup (used in ascending order), u[8 + 2 k], u[9 + 2 k] (cos theta = 2 u - 1,
+// phi = 2 pi u) of the k-th decay of the recursion (particles 3, 2, 1 of the decay list in
+// that order). These are the draws the reference takes from its random-number generator
+// inside EventWeight, in the same order.
+//
+// The amplitude is the sum over the 24 orderings (a, b, c, d) of the four particles along
+// the ladder:
+//   R(s_1a, t1) FF(t1) ff(t_a, MA) / (t_a - MA) ff(t_ab, MA) R(s_bc, t_ab) ff(t_ab, MB)
+//   / (t_d - MB) ff(t_d, MB) R(s_2d, t2) FF(t2) g^4
+// with t_a = (q1 - p_a)^2, t_ab = (q1 - p_a - p_b)^2, t_d = (q2 - p_d)^2, R the Regge
+// propagator sum and ff the off-shell meson form factor; MA, MB the masses of the first and
+// third particle of the decay list. Invariants are formed from light-cone components (no
+// cancellation against the beam energy). Screened events run the kt-loop in FP64 (the
+// loop kinematics of MFactorized::LoopKinematics, src/MFactorized.cc:84-139: the central
+// system and its decay products keep their momenta, the forward legs take p1T - kT, p2T + kT).
+#pragma once
+
+#include "grn_physics.cuh"
+
+namespace grn {
+
+constexpr int kNb = 4;  // central particles of the N-body processes
+
+GRN_HD bool is_nbody(const grn_process_params &P) { return P.n_central == kNb; }
+
+// Light-cone 4-vector (p = E + pz, m = E - pz).
+struct LC4 {
+  double p, m, x, y;
+};
+
+GRN_HD double lc_dot(const LC4 &a, const LC4 &b) {
+  return 0.5 * (a.p * b.m + a.m * b.p) - a.x * b.x - a.y * b.y;
+}
+
+// Lab 4-vector (px, py, pz, E) to light-cone with the smaller component from mT^2.
+GRN_HD LC4 lc_from_lab(double px, double py, double pz, double E, double m2) {
+  const double mt2 = m2 + px * px + py * py;
+  LC4 r;
+  r.x = px;
+  r.y = py;
+  if (pz >= 0) {
+    r.p = E + pz;
+    r.m = mt2 / r.p;
+  } else {
+    r.m = E - pz;
+    r.p = mt2 / r.m;
+  }
+  return r;
+}
+
+struct NBEvent {
+  LC4    X;                 // central system
+  LC4    c[kNb];            // central particles in decay-list order
+  double m2[kNb];           // their masses^2
+  double p1x, p1y, p2x, p2y, pt1sq, pt2sq;  // tree-level forward transverse momenta
+  double a1, a2;            // (X+ - eps)/L, (X- - eps)/L: forward-leg closure constants
+  double dw;                // N-body phase-space weight (NBodySetup volume x momenta)
+  double m2w;               // mass^2 window of the system (B51IntegralVolume)
+  double sbc[kNb][kNb];     // (p_b + p_c)^2 of central pairs
+  bool   cuts;              // the central particles pass the particle cuts
+};
+
+// Forward legs at transverse momenta (q1x, q1y), (q2x, q2y): light-cone closure (the
+// solution kinematics::SolvePz picks), t1, t2 and q1 = pb1 - p1, q2 = pb2 - p2.
+struct NBLegs {
+  LC4    p1, p2, q1, q2;
+  double t1, t2;
+};
+
+GRN_HD bool nbody_legs(const Consts &K, const NBEvent &e, double p1x, double p1y, double p2x,
+                       double p2y, NBLegs &g) {
+  const double pt1sq = p1x * p1x + p1y * p1y, pt2sq = p2x * p2x + p2y * p2y;
+  const double mT1sq = K.mp2 + pt1sq, mT2sq = K.mp2 + pt2sq;
+  const double L2 = K.L * K.L;
+  double x1, x2;
+  if (!solve_x(e.a1, e.a2, mT1sq / L2, mT2sq / L2, x1, x2)) return false;
+  g.p1 = {(1.0 - x1) * K.L, 0.0, p1x, p1y};
+  g.p1.m = mT1sq / g.p1.p;
+  g.p2 = {0.0, (1.0 - x2) * K.L, p2x, p2y};
+  g.p2.p = mT2sq / g.p2.m;
+  g.t1 = -(pt1sq + x1 * x1 * K.mp2) / (1.0 - x1);
+  g.t2 = -(pt2sq + x2 * x2 * K.mp2) / (1.0 - x2);
+  q_lightcone<double>(x1, pt1sq, K.mp2, K.L, g.q1.p, g.q1.m);
+  q_lightcone<double>(x2, pt2sq, K.mp2, K.L, g.q2.m, g.q2.p);
+  g.q1.x = -p1x;
+  g.q1.y = -p1y;
+  g.q2.x = -p2x;
+  g.q2.y = -p2y;
+  return true;
+}
+
+// B51RandomKin / B51BuildKin with the N-body decay of the central system
+// (src/MFactorized.cc:245-407): false when the point is kinematically impossible.
+GRN_HD bool nbody_kinematics(const grn_process_params &P, const Consts &K, const double *u,
+                             NBEvent &e) {
+  const grn_gencuts &g = P.gcuts;
+  const double pt1 = exp(K.lnpt_lo + (K.lnpt_hi - K.lnpt_lo) * u[0]);
+  const double pt2 = exp(K.lnpt_lo + (K.lnpt_hi - K.lnpt_lo) * u[1]);
+  double s1, c1, s2, c2;
+  sincos_pi(2.0 * u[2], s1, c1);
+  sincos_pi(2.0 * u[3], s2, c2);
+  const double yX  = g.Y_min + (g.Y_max - g.Y_min) * u[4];
+  const double m2X = K.M2min + (K.M2max - K.M2min) * u[5];
+  e.m2w = K.M2max - K.M2min;
+  e.p1x = pt1 * c1;
+  e.p1y = pt1 * s1;
+  e.p2x = pt2 * c2;
+  e.p2y = pt2 * s2;
+  e.pt1sq = e.p1x * e.p1x + e.p1y * e.p1y;
+  e.pt2sq = e.p2x * e.p2x + e.p2y * e.p2y;
+  const double Xx = -(e.p1x + e.p2x), Xy = -(e.p1y + e.p2y);
+  const double mTX = sqrt(m2X + Xx * Xx + Xy * Xy);
+  const double eY = exp(yX);
+  e.X = {mTX * eY, mTX / eY, Xx, Xy};
+  const double EX = 0.5 * (e.X.p + e.X.m), ZX = 0.5 * (e.X.p - e.X.m);
+  if (EX > K.sqrt_s - 2.0 * sqrt(K.mp2)) return false;  // energy overflow (MFactorized.cc:323)
+  e.a1 = (e.X.p - K.eps) / K.L;
+  e.a2 = (e.X.m - K.eps) / K.L;
+  double x1, x2;
+  if (!solve_x(e.a1, e.a2, (K.mp2 + e.pt1sq) / (K.L * K.L), (K.mp2 + e.pt2sq) / (K.L * K.L),
+               x1, x2))
+    return false;
+
+  // NBodySetup (MKinematics.h:529-605), weighted: intermediate masses from the ordered draws,
+  // decay momenta, volume 1 / (2 (2 pi)^(2N-3)) DELTA^(N-2) / (N-2)! / M0
+  const double M0 = sqrt(m2X);
+  double m[kNb], sum[kNb];
+  for (int i = 0; i < kNb; ++i) {
+    m[i]   = P.m_central[i];
+    sum[i] = (i ? sum[i - 1] : 0.0) + m[i];
+    e.m2[i] = m[i] * m[i];
+  }
+  const double D = M0 - sum[kNb - 1];
+  if (!(D > 0)) return false;
+  const double r0 = fmin(u[6], u[7]), r1 = fmax(u[6], u[7]);
+  const double Meff[kNb] = {m[0], sum[1] + r0 * D, sum[2] + r1 * D, M0};
+  double pn[kNb];
+  double w = 1.0;
+  for (int i = 1; i < kNb; ++i) {
+    const double x = Meff[i], y = Meff[i - 1], z = m[i];
+    pn[i] = sqrt(fmax(0.0, (x - y - z) * (x + y + z) * (x + y - z) * (x - y + z))) / (2.0 * x);
+    w *= pn[i];
+  }
+  const double tp = 2.0 * kPi;
+  e.dw = w / (2.0 * (tp * tp * tp * tp * tp)) * (D * D) / 2.0 / M0;
+
+  // NBodyPhaseSpace (MKinematics.h:643-691): from the last particle down, an isotropic
+  // momentum in the rest frame of what is left, boosted to the lab with that system's
+  // lab momentum, then subtracted from it; the first particle takes the remainder.
+  double kx = Xx, ky = Xy, kz = ZX, kE = EX;
+  for (int i = kNb - 1; i >= 1; --i) {
+    const int    j  = 8 + 2 * (kNb - 1 - i);
+    const double ct = 2.0 * u[j] - 1.0;
+    const double st = sqrt(fmax(0.0, 1.0 - ct * ct));
+    double sp, cp;
+    sincos_pi(2.0 * u[j + 1], sp, cp);
+    const double px = pn[i] * st * cp, py = pn[i] * st * sp, pz = pn[i] * ct;
+    const double pE = sqrt(e.m2[i] + pn[i] * pn[i]);
+    const double kM = sqrt(fmax(0.0, kE * kE - kx * kx - ky * ky - kz * kz));
+    const double bx = kx / kE, by = ky / kE, bz = kz / kE, gam = kE / kM;
+    const double k1 = bx * px + by * py + bz * pz;
+    const double k2 = gam * (gam * k1 / (1.0 + gam) + pE);
+    const double lx = px + k2 * bx, ly = py + k2 * by, lz = pz + k2 * bz, lE = gam * (pE + k1);
+    e.c[i] = lc_from_lab(lx, ly, lz, lE, e.m2[i]);
+    kx -= lx;
+    ky -= ly;
+    kz -= lz;
+    kE -= lE;
+  }
+  e.c[0] = lc_from_lab(kx, ky, kz, kE, e.m2[0]);
+
+  // s-type invariants among the central particles (GetLorentzScalars, MProcess.cc:1515-1530)
+  for (int a = 0; a < kNb; ++a)
+    for (int b = a + 1; b < kNb; ++b) {
+      e.sbc[a][b] = e.m2[a] + e.m2[b] + 2.0 * lc_dot(e.c[a], e.c[b]);
+      e.sbc[b][a] = e.sbc[a][b];
+      if (e.sbc[a][b] < 0) return false;
+    }
+
+  // particle cuts on the central particles (CommonCuts, MProcess.cc:1085-1138)
+  const grn_fidcuts &f = P.fcuts;
+  e.cuts = true;
+  if (f.active) {
+    for (int a = 0; a < kNb; ++a) {
+      const double pt = sqrt(e.c[a].x * e.c[a].x + e.c[a].y * e.c[a].y);
+      const double mt = sqrt(e.m2[a] + pt * pt);
+      const double y   = 0.5 * log(e.c[a].p / e.c[a].m);
+      const double eta = asinh(0.5 * (e.c[a].p - e.c[a].m) / pt);
+      if (!(pt >= f.pt_min && pt <= f.pt_max && mt >= f.Et_min && mt <= f.Et_max &&
+            eta >= f.eta_min && eta <= f.eta_max && y >= f.rap_min && y <= f.rap_max))
+        e.cuts = false;
+    }
+  }
+  return true;
+}
+
+// Event-level cuts: forward |t| and the system's mass, rapidity and pT (CommonCuts), plus
+// the particle cuts; t from the tree-level legs.
+GRN_HD bool nbody_fiducial(const grn_process_params &P, const NBEvent &e, const NBLegs &g) {
+  const grn_fidcuts &f = P.fcuts;
+  if (!f.active) return true;
+  const double at1 = fabs(g.t1), at2 = fabs(g.t2);
+  if (!(at1 >= f.ft_min && at1 <= f.ft_max && at2 >= f.ft_min && at2 <= f.ft_max)) return false;
+  const double M  = sqrt(fmax(0.0, e.X.p * e.X.m - e.X.x * e.X.x - e.X.y * e.X.y));
+  const double Y  = 0.5 * log(e.X.p / e.X.m);
+  const double Pt = sqrt(e.X.x * e.X.x + e.X.y * e.X.y);
+  if (!(M >= f.M_min && M <= f.M_max && Y >= f.Y_min && Y <= f.Y_max && Pt >= f.Pt_min &&
+        Pt <= f.Pt_max))
+    return false;
+  return e.cuts;
+}
+
+// ME6 (MRegge.cc:470-534) at forward legs g; false when an invariant check fails
+// (GetLorentzScalars: negative s-type invariants or positive t1, t2).
+GRN_HD bool nbody_amp(const grn_process_params &P, const Consts &K, const NBEvent &e,
+                      const NBLegs &g, cx<double> &A) {
+  const grn_regge_params &rp = P.regge;
+  if (g.t1 > 0 || g.t2 > 0) return false;
+  double lns1[kNb], lns2[kNb], d1[kNb], f1[kNb], f2[kNb];
+  cx<double> R1[kNb], R2[kNb];
+  const double MA = K.m3sq, MB = K.M2propB;
+  for (int a = 0; a < kNb; ++a) {
+    const double s1 = K.mp2 + e.m2[a] + 2.0 * lc_dot(g.p1, e.c[a]);
+    const double s2 = K.mp2 + e.m2[a] + 2.0 * lc_dot(g.p2, e.c[a]);
+    if (s1 < 0 || s2 < 0) return false;
+    lns1[a] = log(s1);
+    lns2[a] = log(s2);
+    d1[a] = lc_dot(g.q1, e.c[a]);
+    const double ta = g.t1 + e.m2[a] - 2.0 * d1[a];
+    const double td = g.t2 + e.m2[a] - 2.0 * lc_dot(g.q2, e.c[a]);
+    f1[a] = meson_ff<double>(rp, ta, MA) / (ta - MA);
+    f2[a] = meson_ff<double>(rp, td, MB) / (td - MB);
+    R1[a] = regge_prop<double>(K, rp, lns1[a], g.t1);
+    R2[a] = regge_prop<double>(K, rp, lns2[a], g.t2);
+  }
+  cx<double> S{0.0, 0.0};
+  for (int a = 0; a < kNb; ++a)
+    for (int b = 0; b < kNb; ++b) {
+      if (b == a) continue;
+      const double tab = g.t1 + e.sbc[a][b] - 2.0 * (d1[a] + d1[b]);
+      const double fab = meson_ff<double>(rp, tab, MA) * meson_ff<double>(rp, tab, MB);
+      for (int c = 0; c < kNb; ++c) {
+        if (c == a || c == b) continue;
+        const int d = 6 - a - b - c;
+        const cx<double> Rm = regge_prop<double>(K, rp, log(e.sbc[b][c]), tab);
+        const cx<double> t  = cscale(cmul(cmul(R1[a], Rm), R2[d]), f1[a] * fab * f2[d]);
+        S = cadd(S, t);
+      }
+    }
+  const double g2 = K.g2;
+  const double vtx = K.gN2 * proton_ff<double>(P.soft.fc1, P.soft.fc2, g.t1) *
+                     proton_ff<double>(P.soft.fc1, P.soft.fc2, g.t2) * g2 * g2;
+  A = cscale(S, vtx);
+  return true;
+}
+
+// Event weight factor without |M|^2: C_space = dPhi_N / (2 pi), B51PhaseSpaceWeight x
+// B51IntegralVolume, 1 / S, GeV^-2 -> barn and the flux (MFactorized.cc:160-183, 418-450).
+GRN_HD double nbody_jacobian(const Consts &K, const NBEvent &e, const NBLegs &g) {
+  const double E1 = 0.5 * (g.p1.p + g.p1.m), pz1 = 0.5 * (g.p1.p - g.p1.m);
+  const double E2 = 0.5 * (g.p2.p + g.p2.m), pz2 = 0.5 * (g.p2.p - g.p2.m);
+  const double J  = 1.0 / fabs(pz1 / E1 - pz2 / E2);
+  const double pt1 = sqrt(e.pt1sq), pt2 = sqrt(e.pt2sq);
+  return K.w_const * (pt1 / (2.0 * E1)) * (pt2 / (2.0 * E2)) * J * pt1 * pt2 * e.m2w *
+         e.dw / (2.0 * kPi);
+}
+
+// kt-loop of the N-body amplitude in FP64 (MProcess::S3ScreenedAmp2 with the node tables of
+// the 2-body loop).
+template <typename T>
+__device__ cx<double> nbody_loop(const KArgs &A, const NBEvent &e, const KtNode<T> *skt,
+                                 const PhiNode<T> *sphi) {
+  double ar = 0.0, ai = 0.0;
+  for (int j = 0; j < A.n_kt_nodes; ++j) {
+    const KtNode<T> nj = skt[j];
+    double ir = 0.0, ii = 0.0;
+    for (int i = 0; i < A.n_phi_nodes; ++i) {
+      const PhiNode<T> ni = sphi[i];
+      const double     kx = double(nj.kt) * double(ni.c), ky = double(nj.kt) * double(ni.s);
+      NBLegs           g;
+      if (!nbody_legs(A.K, e, e.p1x - kx, e.p1y - ky, e.p2x + kx, e.p2y + ky, g)) continue;
+      cx<double> a;
+      if (!nbody_amp(A.P, A.K, e, g, a)) continue;
+      ir += double(ni.u) * a.re;
+      ii += double(ni.u) * a.im;
+    }
+    ar += double(nj.cre) * ir - double(nj.cim) * ii;
+    ai += double(nj.cre) * ii + double(nj.cim) * ir;
+  }
+  return {A.loop_norm_re * ar - A.loop_norm_im * ai, A.loop_norm_re * ai + A.loop_norm_im * ar};
+}
+
+// Stage A of an N-body point: kinematics, cuts and (unscreened) the weight; true when the
+// point needs the kt-loop. Flags as born_stage.
+__device__ __noinline__ bool nbody_born_stage(const KArgs &A, const double *x, double &W,
+                                              uint8_t &flags) {
+  NBEvent e;
+  NBLegs  g;
+  bool kin = nbody_kinematics(A.P, A.K, x, e);
+  kin = kin && nbody_legs(A.K, e, e.p1x, e.p1y, e.p2x, e.p2y, g);
+  cx<double> A0{0.0, 0.0};
+  kin = kin && nbody_amp(A.P, A.K, e, g, A0);
+  const bool fid = kin && nbody_fiducial(A.P, e, g);
+  flags = (kin ? GRN_FLAG_KINEMATICS_OK : 0) | (fid ? GRN_FLAG_FIDCUTS_OK : 0) |
+          GRN_FLAG_VETOCUTS_OK | GRN_FLAG_AMPLITUDE_OK;
+  W = 0.0;
+  if (!(kin && fid)) return false;
+  if (A.P.screening) return true;
+  W = nbody_jacobian(A.K, e, g) * (A0.re * A0.re + A0.im * A0.im);
+  if (!isfinite(W)) {
+    W = 0.0;
+    flags &= ~GRN_FLAG_AMPLITUDE_OK;
+  }
+  return false;
+}
+
+// Screened weight of an N-body point that passed stage A (FP64 loop whatever T).
+template <typename T>
+__device__ __noinline__ double nbody_screened_weight(const KArgs &A, const double *x,
+                                                     uint8_t &flags, const KtNode<T> *skt,
+                                                     const PhiNode<T> *sphi) {
+  NBEvent e;
+  NBLegs  g;
+  cx<double> A0{0.0, 0.0};
+  nbody_kinematics(A.P, A.K, x, e);
+  nbody_legs(A.K, e, e.p1x, e.p1y, e.p2x, e.p2y, g);
+  nbody_amp(A.P, A.K, e, g, A0);
+  const cx<double> Al = nbody_loop<T>(A, e, skt, sphi);
+  const double re = A0.re + Al.re, im = A0.im + Al.im;
+  double W = nbody_jacobian(A.K, e, g) * (re * re + im * im);
+  flags = GRN_FLAG_KINEMATICS_OK | GRN_FLAG_FIDCUTS_OK | GRN_FLAG_VETOCUTS_OK |
+          GRN_FLAG_AMPLITUDE_OK;
+  if (!isfinite(W)) {
+    W = 0.0;
+    flags &= ~GRN_FLAG_AMPLITUDE_OK;
+  }
+  return W;
+}
+
+}  // namespace grn

@@ -73,6 +73,7 @@ struct Consts {
   double w_const;           // every u-independent factor of the weight
   double M2min, M2max;      // <F>: central-system mass^2 window (B51RandomKin)
   double M2prop;            // off-shell propagator nominal mass^2 (ME4: first central mass)
+  double M2propB;           // ME6: mass^2 of the third central particle (second propagator)
   double g2;                // (c0 / gN_P)^2
   double gN2;               // gN_P^2
   double eta0_re[3], eta0_im[3];  // ReggeEta(a0_k, sgn_k)

@@ -181,13 +181,16 @@ double meson_ff(const grn_regge_params &rp, double that, double M2) {
 // Kinematics state of one event (the part of LORENTZSCALAR the path uses).
 struct Event {
   V4     pb1, pb2;         // beams
-  V4     pf[5];            // pfinal[0..4]: central system, forward 1, forward 2, central a, b
+  V4     pf[7];            // pfinal[0..6]: central system, forward 1, forward 2, central a, b
+                           // (c, d for 4-body central states)
   V4     q;                // intermediate difference momentum (pkt_[0]), <C>
   double dw = 0;           // <F>: 2-body phase-space weight dPhi2 (MFactorized.cc:381)
   double m2lo = 0, m2hi = 0;  // <F>: central mass^2 window of this point
   V4     leaf[4];          // cascades: final-state daughters (central 1: 0, 1; central 2: 2, 3)
   double t1 = 0, t2 = 0, that = 0, uhat = 0, m2 = 0, Y = 0, Pt = 0;
-  double ss[5][5] = {};
+  double ss[7][7] = {};
+  // 4-body central states: (q1 - p_i)^2, (q2 - p_i)^2, (q1 - p_i - p_j)^2 (MProcess.cc:1556-1561)
+  double tt1[7] = {}, tt2[7] = {}, ttxy[7][7] = {};
 };
 
 struct Setup {
@@ -220,8 +223,9 @@ bool check_emc(const V4 &d) {
 
 // Lorentz scalars of a 2 -> 4 event (MProcess.cc:1499-1584, Nf = 4).
 bool lorentz_scalars(const Setup &S, Event &ev) {
-  for (int i = 0; i <= 4; ++i)
-    for (int j = i + 1; j <= 4; ++j) {
+  const int Nf = 2 + S.p.n_central;
+  for (int i = 0; i <= Nf; ++i)
+    for (int j = i + 1; j <= Nf; ++j) {
       ev.ss[i][j] = (ev.pf[i] + ev.pf[j]).m2();
       ev.ss[j][i] = ev.ss[i][j];
       if (ev.ss[i][j] < 0) return false;
@@ -234,6 +238,13 @@ bool lorentz_scalars(const Setup &S, Event &ev) {
   if (ev.t1 > 0 || ev.t2 > 0) return false;
   ev.that = (q1 - ev.pf[3]).m2();
   ev.uhat = (q1 - ev.pf[4]).m2();
+  if (Nf > 4) {
+    for (int i = 3; i <= Nf; ++i) {
+      ev.tt1[i] = (q1 - ev.pf[i]).m2();
+      ev.tt2[i] = (q2 - ev.pf[i]).m2();
+      for (int j = 3; j <= Nf; ++j) ev.ttxy[i][j] = (q1 - ev.pf[i] - ev.pf[j]).m2();
+    }
+  }
   ev.m2   = ev.pf[0].m2();
   ev.Y    = ev.pf[0].rap();
   ev.Pt   = ev.pf[0].pt();
@@ -337,6 +348,51 @@ double two_body(const V4 &mother, double M0, double m3, double m4, double ct, do
   return 4.0 * PI * pn / (16.0 * PI * PI * M0);
 }
 
+// LorentzBoost (include/Graniitti/MKinematics.h:384-401), sign +1: p from the rest frame of
+// the system b (mass M0) to the frame where b has its given momentum.
+V4 boost_from_rest(const V4 &b, double M0, const V4 &p) {
+  const double bx = b.x / b.e, by = b.y / b.e, bz = b.z / b.e;
+  const double gam = b.e / M0;
+  const double k1  = bx * p.x + by * p.y + bz * p.z;
+  const double k2  = gam * (gam * k1 / (1.0 + gam) + p.e);
+  return V4(p.x + k2 * bx, p.y + k2 * by, p.z + k2 * bz, gam * (p.e + k1));
+}
+
+// Flat N-body phase space, weighted (NBodySetup with unweight = false + NBodyPhaseSpace,
+// include/Graniitti/MKinematics.h:523-691) for N = 4, the reference's generator draws taken
+// from r: r[0], r[1] the intermediate masses (sorted), then (cos theta, phi) pairs for
+// particles 3, 2, 1. Returns the weight prod(p*) x volume, or -1.
+double n_body(const V4 &mother, double M0, const double *m, const double *r, V4 *p) {
+  const int N = 4;
+  double sum[N];
+  for (int i = 0; i < N; ++i) sum[i] = (i ? sum[i - 1] : 0.0) + m[i];
+  const double D = M0 - sum[N - 1];
+  if (!(D > 0)) return -1.0;
+  double rv[2] = {r[0], r[1]};
+  std::sort(rv, rv + 2);
+  const double Meff[N] = {m[0], sum[1] + rv[0] * D, sum[2] + rv[1] * D, M0};
+  double pn[N] = {0, 0, 0, 0};
+  double w = 1.0;
+  for (int i = 1; i < N; ++i) {
+    const double x = Meff[i], y = Meff[i - 1], z = m[i];
+    pn[i] = msqrt((x - y - z) * (x + y + z) * (x + y - z) * (x - y + z)) / (2.0 * x);
+    w *= pn[i];
+  }
+  const double volume = 1.0 / (2.0 * std::pow(2.0 * PI, 2 * N - 3)) * std::pow(D, N - 2) / 2.0 / M0;
+  V4 k = mother;
+  for (int i = N - 1, j = 2; i >= 1; --i, j += 2) {
+    const double ct = 2.0 * r[j] - 1.0;
+    const double st = msqrt(1.0 - ct * ct);
+    const double ph = 2.0 * PI * r[j + 1];
+    const V4 q(pn[i] * st * std::cos(ph), pn[i] * st * std::sin(ph), pn[i] * ct,
+               msqrt(m[i] * m[i] + pn[i] * pn[i]));
+    p[i] = boost_from_rest(k, k.m(), q);
+    k = k - p[i];
+  }
+  p[0] = k;
+  return w * volume;
+}
+
 // B51RandomKin + B51BuildKin for a 2-body central state, decay angles taken from
 // u[6] (cos theta = 2 u6 - 1) and u[7] (phi = 2 pi u7) (MFactorized.cc:245-412).
 bool build_kinematics_F(const Setup &S, const double *u, Event &ev) {
@@ -349,6 +405,7 @@ bool build_kinematics_F(const Setup &S, const double *u, Event &ev) {
   const double phi2 = 2.0 * PI * u[3];
   const double yX   = g.Y_min + (g.Y_max - g.Y_min) * u[4];
   double m3 = S.p.m_central[0], m4 = S.p.m_central[1];
+  if (S.p.n_central == 4) m4 = S.p.m_central[1] + S.p.m_central[2] + S.p.m_central[3];
   if (S.p.n_decay == 2) {
     // off-shell masses of the central particles (GetOffShellMass: daughters' mass sum +
     // 1e-5 GeV bounds the Breit-Wigner from below)
@@ -373,6 +430,12 @@ bool build_kinematics_F(const Setup &S, const double *u, Event &ev) {
   ev.pf[1] = p1;
   ev.pf[2] = p2;
   if (!check_emc((S.pb1 + S.pb2) - (p1 + p2 + pX))) return false;
+  if (S.p.n_central == 4) {
+    ev.dw = n_body(pX, msqrt(m2X), S.p.m_central, u + 6, ev.pf + 3);
+    if (!(ev.dw >= 0)) return false;
+    for (int k = 0; k < 4; ++k) ev.leaf[k] = ev.pf[3 + k];
+    return lorentz_scalars(S, ev);
+  }
   ev.dw = two_body(pX, msqrt(m2X), m3, m4, 2.0 * u[6] - 1.0, 2.0 * PI * u[7], ev.pf[3], ev.pf[4]);
   if (S.p.n_decay == 2) {
     two_body(ev.pf[3], m3, S.p.m_daughter[0], S.p.m_daughter[1], 2.0 * u[10] - 1.0,
@@ -443,6 +506,29 @@ cplx regge_me4(const Setup &S, const Event &ev) {
   return At + Au;
 }
 
+
+// Regge continuum amplitude for a 4-body central state (MRegge::ME6, src/MRegge.cc:470-534):
+// all 24 orderings (a, b, c, d) of the central particles along the ladder (GetAmpPerm(4, 1),
+// include/Graniitti/MMath.h:723-770), off-shell propagator masses of the first and third
+// particle of the decay list.
+cplx regge_me6(const Setup &S, const Event &ev) {
+  const grn_regge_params &rp = S.p.regge;
+  const double MA  = sq(S.p.m_central[0]), MB = sq(S.p.m_central[2]);
+  const double FFA = S.p.soft.gN_P * proton_ff(S.p.soft, ev.t1);
+  const double FFB = S.p.soft.gN_P * proton_ff(S.p.soft, ev.t2);
+  const double g   = rp.c[0] / S.p.soft.gN_P;
+  int perm[4] = {3, 4, 5, 6};
+  cplx A(0, 0);
+  do {
+    const int a = perm[0], b = perm[1], c = perm[2], d = perm[3];
+    const double tab = ev.tt1[a], tbc = ev.ttxy[a][b], tcd = ev.tt2[d];
+    A += regge_prop(rp, ev.ss[1][a], ev.t1) * FFA * meson_ff(rp, tab, MA) * g *
+         (1.0 / (tab - MA)) * meson_ff(rp, tbc, MA) * g * regge_prop(rp, ev.ss[b][c], tbc) *
+         meson_ff(rp, tbc, MB) * g * (1.0 / (tcd - MB)) * meson_ff(rp, tcd, MB) * g *
+         regge_prop(rp, ev.ss[2][d], ev.t2) * FFB;
+  } while (std::next_permutation(perm, perm + 4));
+  return A;
+}
 
 // ---------------------------------------------------------------------------
 // Tensor-pomeron continuum of two pseudoscalars (MTensorPomeron::ME4, "2xS",
@@ -1233,6 +1319,7 @@ void observables(const Setup &S, const Event &ev, double *o) {
 // are added per proton configuration; with the high-energy proton vertex all four are equal,
 // so the sum of one configuration carries |M|^2.
 cplx bare_amp(const Setup &S, const Event &ev) {
+  if (S.p.n_central == 4) return regge_me6(S, ev);
   if (S.p.process == GRN_PROC_TENSOR_RES) return tensor_me3(S, ev);
   if (S.p.process == GRN_PROC_TENSOR_RESCON)
     return tensor_me4_2xs(S, ev) + (S.p.n_res > 0 ? tensor_me3(S, ev) : cplx(0.0));
@@ -1291,7 +1378,8 @@ bool fiducial(const Setup &S, const Event &ev) {
   bool ok = true;
   // final-state particles: the central pair, or the leaves of its decays (FindDecayCuts)
   const bool casc = S.p.n_decay == 2;
-  for (int k = 0; k < (casc ? 4 : 2); ++k) {
+  const int  np   = (casc || S.p.n_central == 4) ? 4 : 2;
+  for (int k = 0; k < np; ++k) {
     const V4 &p = casc ? ev.leaf[k] : ev.pf[3 + k];
     const double pt = p.pt(), et = p.mt(), eta = p.eta(), rap = p.rap();
     if (!(pt >= f.pt_min && pt <= f.pt_max && et >= f.Et_min && et <= f.Et_max &&
@@ -1385,8 +1473,12 @@ extern "C" {
 // t1, t2, m2 and the 4-vectors pfinal[1..4] (19 doubles).
 int orc_weights(const grn_process_params *p, const double *u, int64_t n, int32_t dim, double *w,
                 uint8_t *flags, double *rec, const double *msa, int32_t n_kt2, int32_t nthreads) {
-  const int32_t want = p && p->n_decay == 2 ? 14 : 8;
-  if (!p || !u || !w || dim != want || p->n_central != 2) return GRN_ERR_INVALID;
+  const int32_t want = p && (p->n_decay == 2 || p->n_central == 4) ? 14 : 8;
+  if (!p || !u || !w || dim != want || (p->n_central != 2 && p->n_central != 4))
+    return GRN_ERR_INVALID;
+  if (p->n_central == 4 &&
+      (p->process != GRN_PROC_REGGE_CON || p->phase_space != GRN_PS_FACTORIZED))
+    return GRN_ERR_INVALID;
   if (p->screening && (!msa || n_kt2 < 2)) return GRN_ERR_STATE;
   const orc::Setup S = orc::make_setup(p, msa, n_kt2);
   orc::parallel_for(n, nthreads, [&](int64_t a, int64_t b) {

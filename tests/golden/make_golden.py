@@ -138,6 +138,55 @@ def rescon_fixtures():
          proc=proc, n_bt=1024, n_kt2=10000, loop_kt=15, loop_phi=12, loop_ktmax=1.75, **r)
 
 
+def nbody_fixtures():
+    """Regge continuum of four central particles (PP[CON]<F> -> 4 bodies, MRegge::ME6 with
+    NBodyPhaseSpace): pi+ pi- pi+ pi- and pi+ pi- K+ K- at tree level, the screened
+    amplitude, and the reference's VEGAS cross section of the 4 pi process. The generator
+    draws inside EventWeight, in order: four off-shell masses of the stable central
+    particles (inert, 0.5), the two intermediate masses u[6], u[7], the acceptance draw of the
+    weighted N-body setup (inert, 0.5), then (cos theta, phi) of three decays, u[8..13]."""
+    replay = ["--replay", "h,h,h,h,6,7,h,8,9,10,11,12,13"]
+    proc4 = "PP[CON]<F> -> pi+ pi- pi+ pi-"
+    cases = [("f4_tree_weights.npz", 111, 2048, CARD, proc4),
+             ("f4_kk_tree_weights.npz", 112, 1024, CARD, "PP[CON]<F> -> pi+ pi- K+ K-")]
+    for name, seed, n, card, proc in cases:
+        u = philox_np.uniforms(seed, n, 14)
+        r = run_weights(card, u, replay, proc=proc, dim=6, leaves=4)
+        save(name, seed=seed, u=u, card=os.path.basename(card), proc=proc, **r)
+    u = philox_np.uniforms(113, 96, 14)
+    r = run_weights(CARD_SCR, u, replay + ["--nbt", "1024", "--nkt2", "10000"], proc=proc4,
+                    dim=6, leaves=4)
+    save("f4_screened_weights.npz", seed=113, u=u, card=os.path.basename(CARD_SCR), proc=proc4,
+         n_bt=1024, n_kt2=10000, **r)
+    # Cross section of the 4 pi process. The integrand is heavy-tailed (in flat sampling the
+    # top 100 of 4e5 points carry 90% of the integral), and the reference's VEGAS (6
+    # dimensions, the 8 decay draws inside EventWeight) settles on 1.67e-10 b +- 0.1%, a
+    # factor 8 below the mean of its own EventWeight over uniform points. The fixture keeps
+    # both: the VEGAS number and the flat-sampling mean of the reference's EventWeight (its
+    # own generator draws) over 8 x 5e5 Philox points, with its standard error.
+    out = subprocess.run([REF_BIN, "vegas", CARD, proc4, "--cores", "8"], check=True,
+                         capture_output=True, text=True).stdout
+    line = [l for l in out.splitlines() if l.startswith("RESULT")][-1]
+    vegas = list(map(float, line.split()[1:3]))
+    os.makedirs(TMP, exist_ok=True)
+    procs, parts = [], []
+    for k in range(8):
+        uf, wf = os.path.join(TMP, "f%d.bin" % k), os.path.join(TMP, "fw%d.bin" % k)
+        philox_np.uniforms(120 + k, 500000, 6).astype(np.float64).tofile(uf)
+        procs.append(subprocess.Popen([REF_BIN, "weights", CARD, proc4, uf, "6", wf],
+                                      stdout=subprocess.DEVNULL, stderr=subprocess.DEVNULL))
+        parts.append(wf)
+    for pr in procs:
+        assert pr.wait() == 0
+    w = np.concatenate([np.fromfile(f).reshape(-1, 24)[:, 0] for f in parts])
+    flat = [float(w.mean()), float(w.std() / np.sqrt(len(w)))]
+    with open(os.path.join(HERE, "f4_sigma.json"), "w") as fh:
+        json.dump({"process": proc4, "card": os.path.basename(CARD), "flat_points": len(w),
+                   "flat_sigma_barn": flat[0], "flat_sigma_err_barn": flat[1],
+                   "vegas_sigma_barn": vegas[0], "vegas_sigma_err_barn": vegas[1]}, fh, indent=1)
+    print("f4: flat", flat, "vegas", vegas)
+
+
 def regge_res_fixtures():
     """Regge resonances (PROC_9 PP[RES], PROC_17 PP[RES+CON]; MRegge::ME3 with the spin
     density-matrix production and decay amplitudes): the Collins-Soper, helicity and
@@ -221,11 +270,16 @@ def cascade_fixtures():
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--ref", default="/root/reference")
-    ap.add_argument("--only", choices=["all", "resonances", "cascades", "rescon", "regge_res"],
+    ap.add_argument("--only", choices=["all", "resonances", "cascades", "rescon", "regge_res",
+                                       "nbody"],
                     default="all")
     a = ap.parse_args()
     subprocess.check_call(["make", "-s", "-C", os.path.join(REPO, "oracle", "refbuild"), "-j8",
                            "REF=" + a.ref])
+    if a.only in ("all", "nbody"):
+        nbody_fixtures()
+    if a.only == "nbody":
+        return
     if a.only in ("all", "regge_res"):
         regge_res_fixtures()
     if a.only == "regge_res":

@@ -207,6 +207,22 @@ def test_vector_pair_cascade_weights(name):
     assert (np.abs(leaves - g["leaves"])[kin] / scale[kin]).max() < 1e-12
 
 
+@pytest.mark.parametrize("name", ["f4_tree_weights.npz", "f4_kk_tree_weights.npz",
+                                  "f4_screened_weights.npz"])
+def test_four_body_continuum_weights(name):
+    """PP[CON]<F> -> 4 bodies (MRegge::ME6 with the weighted N-body phase space)."""
+    g = _load(name)
+    P = _params_res(g)
+    assert P.n_central == 4
+    msa = _load("eikonal_nbt1024_nkt10000.npz")["msa"] if P.screening else None
+    w, fl, rec = orc.weights(P, g["u"], msa=msa, nthreads=4, with_rec=True)
+    _check_weights(w, fl, g, tol=W_TOL)
+    kin = g["kin"] == 1
+    cen = rec[:, 19:35].reshape(-1, 4, 4)
+    scale = np.abs(g["leaves"]).max(axis=2, keepdims=True)
+    assert (np.abs(cen - g["leaves"])[kin] / scale[kin]).max() < 1e-12
+
+
 def _np_rest(X, p):
     """p (n, 4: px, py, pz, E) boosted to the rest frame of X (n, 4)."""
     m = np.sqrt(X[:, 3] ** 2 - (X[:, :3] ** 2).sum(1))
