@@ -742,8 +742,6 @@ grn_status grn_event_kinematics(grn_engine *e, const double *u, int64_t n, int32
                                 double *p4_out, double *ts_out, uint8_t *flags) {
   if (!e || !u || n < 0) return fail(GRN_ERR_INVALID, "null argument");
   if (dim != e->dim) return fail(GRN_ERR_INVALID, "dim must equal grn_dim()");
-  if (e->P.n_central != 2)
-    return fail(GRN_ERR_UNSUPPORTED, "event kinematics of 2-body central states only");
   if (n == 0) return GRN_OK;
   GRN_CUDA(cudaSetDevice(e->device));
   // Host-staged path only (diagnostics / record building).
@@ -769,7 +767,8 @@ grn_status grn_event_daughters(grn_engine *e, const double *u, int64_t n, int32_
                                double *pd_out) {
   if (!e || !u || !pd_out || n < 0) return fail(GRN_ERR_INVALID, "null argument");
   if (dim != e->dim) return fail(GRN_ERR_INVALID, "dim must equal grn_dim()");
-  if (e->P.n_decay != 2) return fail(GRN_ERR_STATE, "the process has no decay cascades");
+  if (e->P.n_decay != 2 && e->P.n_central != 4)
+    return fail(GRN_ERR_STATE, "the process has no decay cascades or 4-body central states");
   if (n == 0) return GRN_OK;
   GRN_CUDA(cudaSetDevice(e->device));
   GRN_CUDA(e->d_u.ensure(n * dim * sizeof(double)));
@@ -1303,8 +1302,6 @@ grn_status grn_hist_clear(grn_engine *e) {
 grn_status grn_hist_fill(grn_engine *e) {
   if (!e) return fail(GRN_ERR_INVALID, "null engine");
   if (!e->have_last) return fail(GRN_ERR_STATE, "no VEGAS iteration");
-  if (e->P.n_central != 2)
-    return fail(GRN_ERR_UNSUPPORTED, "histogram observables of 2-body central states only");
   if (e->hist.empty()) return GRN_OK;
   GRN_CUDA(cudaSetDevice(e->device));
   GRN_CUDA(grn::launch_hist_fill(e->args(), e->d_xmat_prev.as<double>(), e->bins, e->dim,

@@ -702,6 +702,35 @@ __global__ void k_event_kinematics(const KArgs A, const double *__restrict__ u, 
   if (i >= n) return;
   double x[kMaxDim];
   for (int d = 0; d < kMaxDim; ++d) x[d] = d < dim ? u[i * dim + d] : 0.0;
+  if (is_nbody(A.P)) {
+    // forward legs and the first two central particles; the four central particles come from
+    // k_event_daughters
+    NBEvent    e;
+    NBLegs     g;
+    cx<double> a0;
+    bool kin = nbody_kinematics(A.P, A.K, x, e);
+    kin      = kin && nbody_legs(A.K, e, e.p1x, e.p1y, e.p2x, e.p2y, g);
+    kin      = kin && nbody_amp(A.P, A.K, e, g, a0);
+    const bool fid = kin && nbody_fiducial(A.P, e, g);
+    if (p4) {
+      const LC4 *v[4] = {&g.p1, &g.p2, &e.c[0], &e.c[1]};
+      for (int k = 0; k < 4; ++k) {
+        double *o = p4 + i * 16 + 4 * k;
+        o[0] = kin ? v[k]->x : 0.0;
+        o[1] = kin ? v[k]->y : 0.0;
+        o[2] = kin ? 0.5 * (v[k]->p - v[k]->m) : 0.0;
+        o[3] = kin ? 0.5 * (v[k]->p + v[k]->m) : 0.0;
+      }
+    }
+    if (ts) {
+      ts[2 * i]     = kin ? g.t1 : 0.0;
+      ts[2 * i + 1] = kin ? g.t2 : 0.0;
+    }
+    if (flags)
+      flags[i] = (kin ? GRN_FLAG_KINEMATICS_OK : 0) | (fid ? GRN_FLAG_FIDCUTS_OK : 0) |
+                 GRN_FLAG_VETOCUTS_OK | GRN_FLAG_AMPLITUDE_OK;
+    return;
+  }
   Born       b;
   const bool kin = born_kinematics<true>(A.P, A.K, x, b);
   const bool fid = kin && fiducial_cuts(A.P, A.K, b);
@@ -728,8 +757,20 @@ __global__ void k_event_daughters(const KArgs A, const double *__restrict__ u, i
   if (i >= n) return;
   double x[kMaxDim];
   for (int d = 0; d < kMaxDim; ++d) x[d] = d < dim ? u[i * dim + d] : 0.0;
-  Born   b;
   double d4[4][4] = {};
+  if (is_nbody(A.P)) {  // the four central particles
+    NBEvent e;
+    if (nbody_kinematics(A.P, A.K, x, e))
+      for (int k = 0; k < 4; ++k) {
+        d4[k][0] = e.c[k].x;
+        d4[k][1] = e.c[k].y;
+        d4[k][2] = 0.5 * (e.c[k].p - e.c[k].m);
+        d4[k][3] = 0.5 * (e.c[k].p + e.c[k].m);
+      }
+    for (int k = 0; k < 16; ++k) pd[i * 16 + k] = d4[k / 4][k % 4];
+    return;
+  }
+  Born b;
   if (born_kinematics<true>(A.P, A.K, x, b))
     cascade_daughters(A.P, b.p3x, b.p3y, b.mt3 * sinh(b.y3), b.mt3 * cosh(b.y3), sqrt(b.m3sq),
                       b.p4x, b.p4y, b.mt4 * sinh(b.y4), b.mt4 * cosh(b.y4), sqrt(b.m4sq), x, d4);
@@ -1054,10 +1095,19 @@ __global__ void __launch_bounds__(128)
     }
     uint64_t pb, pbh;
     vegas_map(xmat, bins, dim, u, x, pb, pbh);
-    Born b;
-    if (!born_kinematics<(MAXD > 8)>(A.P, A.K, x, b)) continue;
     double o[GRN_NUM_OBS];
-    event_observables(A.K, b, o);
+    if (MAXD > 8 && is_nbody(A.P)) {
+      NBEvent ev;
+      if (!nbody_kinematics(A.P, A.K, x, ev)) continue;
+      const LC4   &X = ev.X, &c = ev.c[0];
+      const double m2 = X.p * X.m - X.x * X.x - X.y * X.y;
+      observables_core(A.K, X.p, X.m, X.x, X.y, m2, ev.p1x, ev.p1y, ev.p2x, ev.p2y, c.p, c.m,
+                       c.x, c.y, ev.m2[0], 0.5 * log(ev.c[1].p / ev.c[1].m), o);
+    } else {
+      Born b;
+      if (!born_kinematics<(MAXD > 8)>(A.P, A.K, x, b)) continue;
+      event_observables(A.K, b, o);
+    }
     for (int h = 0; h < nh; ++h) {
       const grn_hist_spec s = specs[h];
       int k = hist_bin(o[s.obs], s.nbins, s.lo, s.hi);

@@ -1560,23 +1560,28 @@ GRN_HD void make_loop_event(const Consts &K, const Born &b, LoopEvent<T> &e) {
 }
 
 // Observables of a Born point (GRN_OBS_* order), for the on-the-fly histograms.
-GRN_HD_COLD void event_observables(const Consts &K, const Born &b, double *o) {
-  const double Xp = b.p3p + b.p4p, Xm = b.p3m + b.p4m, Xx = b.p3x + b.p4x, Xy = b.p3y + b.p4y;
-  const double Xe = 0.5 * (Xp + Xm), Xz = 0.5 * (Xp - Xm), M = sqrt(fmax(b.m2, 0.0));
+// Observables from the system X (light-cone Xp, Xm, transverse Xx, Xy, mass^2 m2), the
+// forward transverse momenta, and the first two central particles (light-cone, transverse,
+// mass^2 of the first).
+GRN_HD_COLD void observables_core(const Consts &K, double Xp, double Xm, double Xx, double Xy,
+                                  double m2, double p1x, double p1y, double p2x, double p2y,
+                                  double p3p, double p3m, double p3x, double p3y, double m3sq,
+                                  double y4, double *o) {
+  const double Xe = 0.5 * (Xp + Xm), Xz = 0.5 * (Xp - Xm), M = sqrt(fmax(m2, 0.0));
   o[GRN_OBS_M]  = M;
   o[GRN_OBS_Y]  = 0.5 * log(Xp / Xm);
   o[GRN_OBS_PT] = sqrt(Xx * Xx + Xy * Xy);
-  double dphi   = atan2(b.p1y, b.p1x) - atan2(b.p2y, b.p2x);
+  double dphi   = atan2(p1y, p1x) - atan2(p2y, p2x);
   while (dphi >= kPi) dphi -= 2.0 * kPi;
   while (dphi < -kPi) dphi += 2.0 * kPi;
   o[GRN_OBS_DPHI_PP] = fabs(dphi);
-  o[GRN_OBS_PT1]     = sqrt(b.pt1sq);
-  o[GRN_OBS_M0]      = sqrt(b.m3sq);
-  o[GRN_OBS_RAP3]    = b.y3;
-  o[GRN_OBS_RAP4]    = b.y4;
+  o[GRN_OBS_PT1]     = sqrt(p1x * p1x + p1y * p1y);
+  o[GRN_OBS_M0]      = sqrt(m3sq);
+  o[GRN_OBS_RAP3]    = 0.5 * log(p3p / p3m);
+  o[GRN_OBS_RAP4]    = y4;
   // first central particle and the beams in the X rest frame
-  double px = b.p3x, py = b.p3y, pz = 0.5 * (b.p3p - b.p3m);
-  const double pe = 0.5 * (b.p3p + b.p3m);
+  double px = p3x, py = p3y, pz = 0.5 * (p3p - p3m);
+  const double pe = 0.5 * (p3p + p3m);
   o[GRN_OBS_COSTH_LA] = pz / sqrt(px * px + py * py + pz * pz);
   o[GRN_OBS_PHI_LA]   = atan2(py, px);
   boost_to_rest<double>(Xe, Xx, Xy, Xz, M, pe, px, py, pz);
@@ -1617,6 +1622,11 @@ GRN_HD_COLD void event_observables(const Consts &K, const Born &b, double *o) {
     o[GRN_OBS_COSTH_CS + 2 * f] = qz / pn;
     o[GRN_OBS_PHI_CS + 2 * f]   = (qx == 0.0 && qy == 0.0) ? 0.0 : atan2(qy, qx);
   }
+}
+
+GRN_HD_COLD void event_observables(const Consts &K, const Born &b, double *o) {
+  observables_core(K, b.p3p + b.p4p, b.p3m + b.p4m, b.p3x + b.p4x, b.p3y + b.p4y, b.m2, b.p1x,
+                   b.p1y, b.p2x, b.p2y, b.p3p, b.p3m, b.p3x, b.p3y, b.m3sq, b.y4, o);
 }
 
 GRN_HD bool is_regge_res(const grn_process_params &P) {

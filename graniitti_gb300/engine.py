@@ -71,6 +71,13 @@ class Engine:
                                               prec))
         return w, flags
 
+    def event_daughters(self, u):
+        """Cascade daughters, or the four central particles of a 4-body state (n, 4, 4)."""
+        u = np.ascontiguousarray(u, dtype=np.float64)
+        pd = np.zeros((u.shape[0], 4, 4))
+        _abi.check(self.lib.grn_event_daughters(self.h, _ptr(u), u.shape[0], self.dim, _ptr(pd)))
+        return pd
+
     def event_kinematics(self, u):
         u = np.ascontiguousarray(u, dtype=np.float64)
         n = u.shape[0]

@@ -1510,8 +1510,9 @@ int orc_weights(const grn_process_params *p, const double *u, int64_t n, int32_t
 // kinematics (ok[i] = 1), from the tree-level event.
 int orc_observables(const grn_process_params *p, const double *u, int64_t n, int32_t dim,
                     double *obs, uint8_t *ok, int32_t nthreads) {
-  const int32_t want = p && p->n_decay == 2 ? 14 : 8;
-  if (!p || !u || !obs || dim != want || p->n_central != 2) return GRN_ERR_INVALID;
+  const int32_t want = p && (p->n_decay == 2 || p->n_central == 4) ? 14 : 8;
+  if (!p || !u || !obs || dim != want || (p->n_central != 2 && p->n_central != 4))
+    return GRN_ERR_INVALID;
   grn_process_params q = *p;
   q.screening = 0;
   const orc::Setup S = orc::make_setup(&q, nullptr, 0);

@@ -149,7 +149,7 @@ def test_cascade_rejections(gpu):
     assert status(lambda Q: setattr(Q, "n_decay", 3)) == _abi.GRN_ERR_UNSUPPORTED
     e = g.Engine(P, 0)
     with pytest.raises(Exception):
-        g.Flow(e)  # the flow kernels are built for 8 dimensions
+        g.Flow(e, hidden=64)  # 14-dimensional flows are built for widths 128 and 256
 
 
 def test_cascade_events_written(gpu, tmp_path):

@@ -105,12 +105,51 @@ def test_four_body_vegas_cross_section(gpu):
     e.close()
 
 
-def test_four_body_unsupported_paths_fail_loudly(gpu, params):
-    """Record kinematics and histogram observables are built for 2-body central states."""
+def test_four_body_histograms(gpu):
+    """On-the-fly histograms of a 4-body pass: the system observables and the angles of the
+    first central particle, against the oracle's observables of the same points."""
     import graniitti_gb300 as g
-    from graniitti_gb300 import _abi, card
+    from test_gpu_histograms import _compare, _vegas
+    from graniitti_gb300 import card
     from conftest import CARD
-    e = g.Engine(card.build_params(card.read_card(CARD), "PP[CON]<F> -> pi+ pi- pi+ pi-"), 0)
-    with pytest.raises(_abi.GrnError):
-        e.event_kinematics(np.full((4, 14), 0.5))
+    P = card.build_params(card.read_card(CARD), "PP[CON]<F> -> pi+ pi- pi+ pi-")
+    e = g.Engine(P, 0)
+    _vegas(e, g, ncall=1 << 15)
+    f = e.pass_weights(1 << 15)
+    specs = [("M", 30, 0.5, 5.0), ("Y", 18, -0.9, 0.9), ("PT", 20, 0.0, 2.0),
+             ("RAP3", 20, -1.0, 1.0), ("COSTH_CS", 10, -1.0, 1.0, "PHI_CS", 10, -np.pi, np.pi),
+             ("COSTH_LA", 20, -1.0, 1.0)]
+    e.hist_define(specs)
+    e.hist_clear()
+    e.hist_fill()
+    _compare(e, P, specs, f)
+    e.close()
+
+
+def test_four_body_record_kinematics_and_events(gpu, tmp_path):
+    """Forward legs and the four central particles against the reference's pfinal of the same
+    points, and the HepMC3 record (CommonRecord: system -> four stable particles)."""
+    import graniitti_gb300 as g
+    from graniitti_gb300.record import EventWriter
+    gl = _load("f4_tree_weights.npz")
+    e = g.Engine(_params(gl), 0)
+    p4, ts, fl = e.event_kinematics(gl["u"])
+    kin = gl["kin"] == 1
+    assert np.array_equal(fl & 1, gl["kin"])
+    scale = np.abs(gl["p4"]).max(axis=2, keepdims=True)
+    assert (np.abs(p4 - gl["p4"])[kin] / scale[kin]).max() < 1e-11
+    pd = e.event_daughters(gl["u"])
+    sc = np.abs(gl["leaves"]).max(axis=2, keepdims=True)
+    assert (np.abs(pd - gl["leaves"])[kin] / sc[kin]).max() < 1e-11
+    assert np.allclose(ts[kin, 0], gl["t1"][kin], rtol=1e-6)
+    path = str(tmp_path / "f4.hepmc3")
+    idx = np.nonzero(gl["w"] > 0)[0][:20]
+    with EventWriter(path, "hepmc3") as w:
+        n = w.write_points(e, gl["u"][idx], [2212, 211, -211, 211, -211], 1.0, 0.1)
+    assert n == len(idx)
+    parts = [l.split() for l in open(path) if l.startswith("P ")]
+    assert len(parts) == 11 * len(idx)
+    last = np.array([[float(v) for v in p[4:8]] for p in parts]).reshape(len(idx), 11, 4)[:, 7:]
+    assert np.allclose(last, pd[idx], rtol=1e-12, atol=1e-12)
+    assert [int(p[3]) for p in parts[7:11]] == [211, -211, 211, -211]
     e.close()
