@@ -171,13 +171,13 @@ def build_params(card, process=None, tune=None):
     elif any(f in PARTICLES and PARTICLES[f][2] > 1e-6 for f in finals):
         # the reference draws Breit-Wigner masses for them (MProcess::GetOffShellMass)
         raise UnsupportedProcess("unstable central particles need their decays: a > {c d}")
-    four = len(finals) == 4 and channel == "CON" and cls == "F" and not any(casc)
+    four = len(finals) == 4 and channel == "CON" and not any(casc)
     if not (istate == "PP" and channel in ("CON", "RES", "RES+CON", "CONTENSOR", "RESTENSOR",
                                            "RES+CONTENSOR") and
             cls in ("C", "F") and (len(finals) == 2 or four)):
         raise UnsupportedProcess(
             "engine implements PP[CON|RES|RES+CON|CONTENSOR|RESTENSOR|RES+CONTENSOR]<C|F> -> "
-            "2-body and PP[CON]<F> -> 4-body, got %r" % proc)
+            "2-body and PP[CON]<C|F> -> 4-body, got %r" % proc)
     if four and any(SPIN.get(f, 0) != 0 for f in finals):
         raise UnsupportedProcess("4-body central states of spin-0 particles")
     vec = all(SPIN.get(f, 0) == 1 for f in finals)
@@ -229,7 +229,7 @@ def build_params(card, process=None, tune=None):
     g = card.get("GENCUTS", {}).get("<C>", {})
     rap = g.get("Rap", [-9.0, 9.0])
     P.gcuts.rap_min, P.gcuts.rap_max = rap
-    kt = g.get("Kt", [0.0, 10.0 / 2])
+    kt = g.get("Kt", [0.0, 10.0 / len(finals)])
     P.gcuts.kt_min, P.gcuts.kt_max = kt
     pt = g.get("Pt", [0.0, 2.5])
     P.gcuts.fpt_min, P.gcuts.fpt_max = pt

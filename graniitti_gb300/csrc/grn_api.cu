@@ -272,8 +272,8 @@ grn_status derive_consts(const grn_process_params &P, grn::Consts &K) {
     return fail(GRN_ERR_UNSUPPORTED, "central states of 2 or 4 particles");
   if (nbody) {
     // PP[CON]<F> -> a b c d (MRegge::ME6 with the N-body phase space)
-    if (P.process != GRN_PROC_REGGE_CON || P.phase_space != GRN_PS_FACTORIZED)
-      return fail(GRN_ERR_UNSUPPORTED, "4-body central states: PP[CON]<F> (Regge ME6)");
+    if (P.process != GRN_PROC_REGGE_CON)
+      return fail(GRN_ERR_UNSUPPORTED, "4-body central states: PP[CON]<F|C> (Regge ME6)");
     if (P.n_decay != 0 || P.central_spin != 0)
       return fail(GRN_ERR_UNSUPPORTED, "4-body central states of stable spin-0 particles");
     for (int k = 0; k < 4; ++k)
@@ -332,6 +332,16 @@ grn_status derive_consts(const grn_process_params &P, grn::Consts &K) {
                      fwd_log * fwd_log;
   K.w_const = (1.0 / P.s_factor) * (1.0 / std::pow(2.0, 2 * (Nf - 2))) *
               (1.0 / std::pow(2.0 * kPi, 3 * Nf - 4)) * vol * kGeV2barn / (2.0 * K.s);
+  if (nbody && P.phase_space == GRN_PS_CONTINUUM) {
+    // BNPhaseSpaceWeight x BNIntegralVolume for Nf = 6 (MContinuum.cc:619-656): kt, phi and
+    // rapidity volumes of 3 difference momenta and 4 central particles
+    const int    N6  = 6;
+    const double v6 = std::pow(P.gcuts.kt_max - P.gcuts.kt_min, 3) * std::pow(2.0 * kPi, 3) *
+                      std::pow(P.gcuts.rap_max - P.gcuts.rap_min, 4) * std::pow(2.0 * kPi, 2) *
+                      fwd_log * fwd_log;
+    K.w_const = (1.0 / P.s_factor) * (1.0 / std::pow(2.0, 2 * (N6 - 2))) *
+                (1.0 / std::pow(2.0 * kPi, 3 * N6 - 4)) * v6 * kGeV2barn / (2.0 * K.s);
+  }
   if (P.phase_space == GRN_PS_FACTORIZED) {
     // mass window (B51RandomKin, MFactorized.cc:263-291): M_MIN = sum of daughter masses
     // + 1e-4 GeV, M_MAX = sqrt(s) - 2 m_beam, both clipped to the <F> generation cuts.

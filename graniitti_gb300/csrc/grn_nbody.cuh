@@ -1,9 +1,10 @@
-// Regge continuum of four central particles in the factorized class: PP[CON]<F> -> a b c d
-// (MRegge::ME6, src/MRegge.cc:470-534), with the central system decayed by the flat N-body
+// Regge continuum of four central particles: PP[CON]<F|C> -> a b c d (MRegge::ME6,
+// src/MRegge.cc:470-534). Factorized class: the central system decayed by the flat N-body
 // phase space of MKinematics.h:523-691 (NBodySetup, NBodyPhaseSpace) and the event weight of
-// MFactorized::EventWeight (src/MFactorized.cc:142-184).
+// MFactorized::EventWeight (src/MFactorized.cc:142-184). Continuum class: the 14-dimensional
+// phase space of MContinuum::BNRandomKin / BNBuildKin (src/MContinuum.cc:276-435).
 //
-// Hypercube (14 coordinates): u[0..5] the factorized skeleton (log pT of the forward legs,
+// Factorized hypercube (14 coordinates): u[0..5] the factorized skeleton (log pT of the forward legs,
 // their azimuths, the system rapidity and mass^2), u[6], u[7] the two intermediate-mass draws
 // of NBodySetup (used in ascending order), u[8 + 2 k], u[9 + 2 k] (cos theta = 2 u - 1,
 // phi = 2 pi u) of the k-th decay of the recursion (particles 3, 2, 1 of the decay list in
@@ -17,9 +18,11 @@
 // with t_a = (q1 - p_a)^2, t_ab = (q1 - p_a - p_b)^2, t_d = (q2 - p_d)^2, R the Regge
 // propagator sum and ff the off-shell meson form factor; MA, MB the masses of the first and
 // third particle of the decay list. Invariants are formed from light-cone components (no
-// cancellation against the beam energy). Screened events run the kt-loop in FP64 (the
-// loop kinematics of MFactorized::LoopKinematics, src/MFactorized.cc:84-139: the central
-// system and its decay products keep their momenta, the forward legs take p1T - kT, p2T + kT).
+// cancellation against the beam energy). Screened events run the kt-loop in FP64: the
+// forward legs take p1T - kT, p2T + kT; in the factorized class the central system and its
+// decay products keep their momenta (MFactorized::LoopKinematics, src/MFactorized.cc:84-139),
+// in the continuum class the central transverse momenta are re-solved with the tree-level
+// difference momenta, rapidities and masses (MContinuum::LoopKinematics).
 #pragma once
 
 #include "grn_physics.cuh"
@@ -65,6 +68,9 @@ struct NBEvent {
   double m2w;               // mass^2 window of the system (B51IntegralVolume)
   double sbc[kNb][kNb];     // (p_b + p_c)^2 of central pairs
   bool   cuts;              // the central particles pass the particle cuts
+  double jx;                // per-event phase-space factor: F dPhi_N / (2 pi) x mass^2 window,
+                            // C the product of the difference momenta kt_i
+  double kx[kNb - 1], ky[kNb - 1], y[kNb];  // C: difference momenta, rapidities
 };
 
 // Forward legs at transverse momenta (q1x, q1y), (q2x, q2y): light-cone closure (the
@@ -96,11 +102,111 @@ GRN_HD bool nbody_legs(const Consts &K, const NBEvent &e, double p1x, double p1y
   return true;
 }
 
+// Pair invariants and particle cuts of the central particles in e.c (GetLorentzScalars,
+// MProcess.cc:1515-1530; CommonCuts, MProcess.cc:1085-1138); false for a negative pair mass^2.
+GRN_HD bool nbody_finish(const grn_process_params &P, NBEvent &e) {
+  for (int a = 0; a < kNb; ++a)
+    for (int b = a + 1; b < kNb; ++b) {
+      e.sbc[a][b] = e.m2[a] + e.m2[b] + 2.0 * lc_dot(e.c[a], e.c[b]);
+      e.sbc[b][a] = e.sbc[a][b];
+      if (e.sbc[a][b] < 0) return false;
+    }
+  const grn_fidcuts &f = P.fcuts;
+  e.cuts = true;
+  if (f.active) {
+    for (int a = 0; a < kNb; ++a) {
+      const double pt  = sqrt(e.c[a].x * e.c[a].x + e.c[a].y * e.c[a].y);
+      const double mt  = sqrt(e.m2[a] + pt * pt);
+      const double y   = 0.5 * log(e.c[a].p / e.c[a].m);
+      const double eta = asinh(0.5 * (e.c[a].p - e.c[a].m) / pt);
+      if (!(pt >= f.pt_min && pt <= f.pt_max && mt >= f.Et_min && mt <= f.Et_max &&
+            eta >= f.eta_min && eta <= f.eta_max && y >= f.rap_min && y <= f.rap_max))
+        e.cuts = false;
+    }
+  }
+  return true;
+}
+
+// Continuum class (MContinuum::BNBuildKin, src/MContinuum.cc:334-435): central transverse
+// momenta from the linear system of MContinuum::BLinearSystem for four particles,
+//   2 p0 = q0 - w - p2 - p3,  2 p1 = -q0 - w - p2 - p3,  2 p2 = -q1 - w - p0 - p3,
+//   2 p3 = -q2 - w - p0 - p1,  w = p1T + p2T,
+// solved with the inverse of its matrix; rapidities and masses fixed, the system X their sum,
+// the forward-leg closure constants from X. Also the loop kinematics of the class
+// (MContinuum::LoopKinematics, src/MContinuum.cc:94-161) at new forward transverse momenta.
+GRN_HD bool nbody_build_C(const Consts &K, NBEvent &e, double p1x, double p1y, double p2x,
+                          double p2y) {
+  constexpr double Ai[kNb][kNb] = {{0.875, 0.125, -0.5, -0.25},
+                                   {0.375, 0.625, -0.5, -0.25},
+                                   {-0.125, 0.125, 0.5, -0.25},
+                                   {-0.625, -0.375, 0.5, 0.75}};
+  const double wx = p1x + p2x, wy = p1y + p2y;
+  const double bx[kNb] = {e.kx[0] - wx, -e.kx[0] - wx, -e.kx[1] - wx, -e.kx[2] - wx};
+  const double by[kNb] = {e.ky[0] - wy, -e.ky[0] - wy, -e.ky[1] - wy, -e.ky[2] - wy};
+  LC4    X{0.0, 0.0, 0.0, 0.0};
+  double msum = 0.0;
+  for (int i = 0; i < kNb; ++i) {
+    double px = 0.0, py = 0.0;
+    for (int j = 0; j < kNb; ++j) {
+      px += Ai[i][j] * bx[j];
+      py += Ai[i][j] * by[j];
+    }
+    const double mt = sqrt(e.m2[i] + px * px + py * py);
+    const double ey = exp(e.y[i]);
+    e.c[i] = {mt * ey, mt / ey, px, py};
+    X.p += e.c[i].p;
+    X.m += e.c[i].m;
+    X.x += px;
+    X.y += py;
+    msum += sqrt(e.m2[i]);
+  }
+  e.X = X;
+  if (0.5 * (X.p + X.m) > K.sqrt_s) return false;  // energy check (MContinuum.cc:373)
+  if (!(X.p * X.m - X.x * X.x - X.y * X.y >= msum * msum)) return false;
+  e.a1 = (X.p - K.eps) / K.L;
+  e.a2 = (X.m - K.eps) / K.L;
+  return true;
+}
+
 // B51RandomKin / B51BuildKin with the N-body decay of the central system
 // (src/MFactorized.cc:245-407): false when the point is kinematically impossible.
 GRN_HD bool nbody_kinematics(const grn_process_params &P, const Consts &K, const double *u,
                              NBEvent &e) {
   const grn_gencuts &g = P.gcuts;
+  if (P.phase_space == GRN_PS_CONTINUUM) {
+    // BNRandomKin (src/MContinuum.cc:276-331): forward legs u[0..3], difference momenta kt
+    // u[4..6] and azimuths u[7..9], rapidities u[10..13]
+    const double pt1 = exp(K.lnpt_lo + (K.lnpt_hi - K.lnpt_lo) * u[0]);
+    const double pt2 = exp(K.lnpt_lo + (K.lnpt_hi - K.lnpt_lo) * u[1]);
+    double s1, c1, s2, c2;
+    sincos_pi(2.0 * u[2], s1, c1);
+    sincos_pi(2.0 * u[3], s2, c2);
+    e.p1x = pt1 * c1;
+    e.p1y = pt1 * s1;
+    e.p2x = pt2 * c2;
+    e.p2y = pt2 * s2;
+    e.pt1sq = e.p1x * e.p1x + e.p1y * e.p1y;
+    e.pt2sq = e.p2x * e.p2x + e.p2y * e.p2y;
+    e.jx = 1.0;
+    for (int i = 0; i < kNb - 1; ++i) {
+      const double kt = g.kt_min + (g.kt_max - g.kt_min) * u[4 + i];
+      double sk, ck;
+      sincos_pi(2.0 * u[7 + i], sk, ck);
+      e.kx[i] = kt * ck;
+      e.ky[i] = kt * sk;
+      e.jx *= kt;
+    }
+    for (int i = 0; i < kNb; ++i) {
+      e.y[i]  = g.rap_min + (g.rap_max - g.rap_min) * u[10 + i];
+      e.m2[i] = P.m_central[i] * P.m_central[i];
+    }
+    if (!nbody_build_C(K, e, e.p1x, e.p1y, e.p2x, e.p2y)) return false;
+    double x1, x2;
+    if (!solve_x(e.a1, e.a2, (K.mp2 + e.pt1sq) / (K.L * K.L), (K.mp2 + e.pt2sq) / (K.L * K.L),
+                 x1, x2))
+      return false;
+    return nbody_finish(P, e);
+  }
   const double pt1 = exp(K.lnpt_lo + (K.lnpt_hi - K.lnpt_lo) * u[0]);
   const double pt2 = exp(K.lnpt_lo + (K.lnpt_hi - K.lnpt_lo) * u[1]);
   double s1, c1, s2, c2;
@@ -150,6 +256,7 @@ GRN_HD bool nbody_kinematics(const grn_process_params &P, const Consts &K, const
   }
   const double tp = 2.0 * kPi;
   e.dw = w / (2.0 * (tp * tp * tp * tp * tp)) * (D * D) / 2.0 / M0;
+  e.jx = e.m2w * e.dw / (2.0 * kPi);
 
   // NBodyPhaseSpace (MKinematics.h:643-691): from the last particle down, an isotropic
   // momentum in the rest frame of what is left, boosted to the lab with that system's
@@ -176,29 +283,7 @@ GRN_HD bool nbody_kinematics(const grn_process_params &P, const Consts &K, const
   }
   e.c[0] = lc_from_lab(kx, ky, kz, kE, e.m2[0]);
 
-  // s-type invariants among the central particles (GetLorentzScalars, MProcess.cc:1515-1530)
-  for (int a = 0; a < kNb; ++a)
-    for (int b = a + 1; b < kNb; ++b) {
-      e.sbc[a][b] = e.m2[a] + e.m2[b] + 2.0 * lc_dot(e.c[a], e.c[b]);
-      e.sbc[b][a] = e.sbc[a][b];
-      if (e.sbc[a][b] < 0) return false;
-    }
-
-  // particle cuts on the central particles (CommonCuts, MProcess.cc:1085-1138)
-  const grn_fidcuts &f = P.fcuts;
-  e.cuts = true;
-  if (f.active) {
-    for (int a = 0; a < kNb; ++a) {
-      const double pt = sqrt(e.c[a].x * e.c[a].x + e.c[a].y * e.c[a].y);
-      const double mt = sqrt(e.m2[a] + pt * pt);
-      const double y   = 0.5 * log(e.c[a].p / e.c[a].m);
-      const double eta = asinh(0.5 * (e.c[a].p - e.c[a].m) / pt);
-      if (!(pt >= f.pt_min && pt <= f.pt_max && mt >= f.Et_min && mt <= f.Et_max &&
-            eta >= f.eta_min && eta <= f.eta_max && y >= f.rap_min && y <= f.rap_max))
-        e.cuts = false;
-    }
-  }
-  return true;
+  return nbody_finish(P, e);
 }
 
 // Event-level cuts: forward |t| and the system's mass, rapidity and pT (CommonCuts), plus
@@ -261,15 +346,15 @@ GRN_HD bool nbody_amp(const grn_process_params &P, const Consts &K, const NBEven
   return true;
 }
 
-// Event weight factor without |M|^2: C_space = dPhi_N / (2 pi), B51PhaseSpaceWeight x
-// B51IntegralVolume, 1 / S, GeV^-2 -> barn and the flux (MFactorized.cc:160-183, 418-450).
+// Event weight factor without |M|^2: F: C_space = dPhi_N / (2 pi), B51PhaseSpaceWeight x
+// B51IntegralVolume (MFactorized.cc:160-183, 418-450); C: BNPhaseSpaceWeight x
+// BNIntegralVolume (MContinuum.cc:619-656); 1 / S, GeV^-2 -> barn and the flux.
 GRN_HD double nbody_jacobian(const Consts &K, const NBEvent &e, const NBLegs &g) {
   const double E1 = 0.5 * (g.p1.p + g.p1.m), pz1 = 0.5 * (g.p1.p - g.p1.m);
   const double E2 = 0.5 * (g.p2.p + g.p2.m), pz2 = 0.5 * (g.p2.p - g.p2.m);
   const double J  = 1.0 / fabs(pz1 / E1 - pz2 / E2);
   const double pt1 = sqrt(e.pt1sq), pt2 = sqrt(e.pt2sq);
-  return K.w_const * (pt1 / (2.0 * E1)) * (pt2 / (2.0 * E2)) * J * pt1 * pt2 * e.m2w *
-         e.dw / (2.0 * kPi);
+  return K.w_const * (pt1 / (2.0 * E1)) * (pt2 / (2.0 * E2)) * J * pt1 * pt2 * e.jx;
 }
 
 // kt-loop of the N-body amplitude in FP64 (MProcess::S3ScreenedAmp2 with the node tables of
@@ -277,6 +362,7 @@ GRN_HD double nbody_jacobian(const Consts &K, const NBEvent &e, const NBLegs &g)
 template <typename T>
 __device__ cx<double> nbody_loop(const KArgs &A, const NBEvent &e, const KtNode<T> *skt,
                                  const PhiNode<T> *sphi) {
+  const bool cls_c = A.P.phase_space == GRN_PS_CONTINUUM;
   double ar = 0.0, ai = 0.0;
   for (int j = 0; j < A.n_kt_nodes; ++j) {
     const KtNode<T> nj = skt[j];
@@ -284,10 +370,19 @@ __device__ cx<double> nbody_loop(const KArgs &A, const NBEvent &e, const KtNode<
     for (int i = 0; i < A.n_phi_nodes; ++i) {
       const PhiNode<T> ni = sphi[i];
       const double     kx = double(nj.kt) * double(ni.c), ky = double(nj.kt) * double(ni.s);
+      const double     q1x = e.p1x - kx, q1y = e.p1y - ky, q2x = e.p2x + kx, q2y = e.p2y + ky;
       NBLegs           g;
-      if (!nbody_legs(A.K, e, e.p1x - kx, e.p1y - ky, e.p2x + kx, e.p2y + ky, g)) continue;
-      cx<double> a;
-      if (!nbody_amp(A.P, A.K, e, g, a)) continue;
+      cx<double>       a;
+      if (cls_c) {
+        NBEvent el = e;
+        if (!nbody_build_C(A.K, el, q1x, q1y, q2x, q2y)) continue;
+        if (!nbody_finish(A.P, el)) continue;
+        if (!nbody_legs(A.K, el, q1x, q1y, q2x, q2y, g)) continue;
+        if (!nbody_amp(A.P, A.K, el, g, a)) continue;
+      } else {
+        if (!nbody_legs(A.K, e, q1x, q1y, q2x, q2y, g)) continue;
+        if (!nbody_amp(A.P, A.K, e, g, a)) continue;
+      }
       ir += double(ni.u) * a.re;
       ii += double(ni.u) * a.im;
     }

@@ -184,6 +184,7 @@ struct Event {
   V4     pf[7];            // pfinal[0..6]: central system, forward 1, forward 2, central a, b
                            // (c, d for 4-body central states)
   V4     q;                // intermediate difference momentum (pkt_[0]), <C>
+  V4     kq[3];            // <C> with 4 central particles: the difference momenta pkt_[0..2]
   double dw = 0;           // <F>: 2-body phase-space weight dPhi2 (MFactorized.cc:381)
   double m2lo = 0, m2hi = 0;  // <F>: central mass^2 window of this point
   V4     leaf[4];          // cascades: final-state daughters (central 1: 0, 1; central 2: 2, 3)
@@ -279,7 +280,86 @@ bool forward_legs(const Setup &S, double pt1, double phi1x, double phi1y, double
 }
 
 // BNRandomKin + BNBuildKin for Kf = 2 (MContinuum.cc:276-435).
+// Central particles of the <C> class with four central particles: transverse momenta from
+// the linear system of MContinuum::BLinearSystem (MContinuum.cc:438-560),
+//   2 p0 = q0 - w - p2 - p3,  2 p1 = -q0 - w - p2 - p3,  2 p2 = -q1 - w - p0 - p3,
+//   2 p3 = -q2 - w - p0 - p1,  w = p1T + p2T,
+// solved here by Gaussian elimination; (pz, E) from the rapidities and masses.
+void central_four(const V4 *q, const V4 &p1, const V4 &p2, const double *m, const double *y,
+                  V4 *out) {
+  double Mx[4][5], My[4][5];
+  const double coef[4][4] = {{2, 0, 1, 1}, {0, 2, 1, 1}, {1, 0, 2, 1}, {1, 1, 0, 2}};
+  const double wx = p1.x + p2.x, wy = p1.y + p2.y;
+  const double bx[4] = {q[0].x - wx, -q[0].x - wx, -q[1].x - wx, -q[2].x - wx};
+  const double by[4] = {q[0].y - wy, -q[0].y - wy, -q[1].y - wy, -q[2].y - wy};
+  for (int i = 0; i < 4; ++i) {
+    for (int j = 0; j < 4; ++j) Mx[i][j] = My[i][j] = coef[i][j];
+    Mx[i][4] = bx[i];
+    My[i][4] = by[i];
+  }
+  double px[4], py[4];
+  for (auto *Mp : {&Mx, &My}) {
+    double (&M)[4][5] = *Mp;
+    for (int c = 0; c < 4; ++c) {
+      int piv = c;
+      for (int r = c + 1; r < 4; ++r)
+        if (std::fabs(M[r][c]) > std::fabs(M[piv][c])) piv = r;
+      for (int k = 0; k < 5; ++k) std::swap(M[c][k], M[piv][k]);
+      for (int r = 0; r < 4; ++r) {
+        if (r == c) continue;
+        const double f = M[r][c] / M[c][c];
+        for (int k = 0; k < 5; ++k) M[r][k] -= f * M[c][k];
+      }
+    }
+    double *dst = Mp == &Mx ? px : py;
+    for (int i = 0; i < 4; ++i) dst[i] = M[i][4] / M[i][i];
+  }
+  for (int i = 0; i < 4; ++i) {
+    const double mt = msqrt(m[i] * m[i] + px[i] * px[i] + py[i] * py[i]);
+    out[i]          = V4(px[i], py[i], mt * std::sinh(y[i]), mt * std::cosh(y[i]));
+  }
+}
+
+// BNRandomKin + BNBuildKin for four central particles (MContinuum.cc:276-435): forward legs
+// u[0..3], kt u[4..6], azimuths u[7..9], rapidities u[10..13].
+bool build_kinematics_c4(const Setup &S, const double *u, Event &ev) {
+  const grn_gencuts &g = S.p.gcuts;
+  const double lo  = std::log(g.fpt_min + ZERO_EPS);
+  const double hi  = std::log(g.fpt_max);
+  const double pt1 = std::exp(lo + (hi - lo) * u[0]);
+  const double pt2 = std::exp(lo + (hi - lo) * u[1]);
+  const double phi1 = 2.0 * PI * u[2];
+  const double phi2 = 2.0 * PI * u[3];
+  for (int i = 0; i < 3; ++i) {
+    const double kt = g.kt_min + (g.kt_max - g.kt_min) * u[4 + i];
+    const double ph = 2.0 * PI * u[7 + i];
+    ev.kq[i] = V4(kt * std::cos(ph), kt * std::sin(ph), 0, 0);
+  }
+  double y[4];
+  for (int i = 0; i < 4; ++i) y[i] = g.rap_min + (g.rap_max - g.rap_min) * u[10 + i];
+  V4 p1(pt1 * std::cos(phi1), pt1 * std::sin(phi1), 0, 0);
+  V4 p2(pt2 * std::cos(phi2), pt2 * std::sin(phi2), 0, 0);
+  V4 c[4];
+  central_four(ev.kq, p1, p2, S.p.m_central, y, c);
+  const V4 sumP = c[0] + c[1] + c[2] + c[3];
+  if (sumP.e > S.sqrt_s) return false;
+  if (!forward_legs(S, pt1, p1.x, p1.y, pt2, p2.x, p2.y, sumP, p1, p2)) return false;
+  ev.pf[0] = sumP;
+  ev.pf[1] = p1;
+  ev.pf[2] = p2;
+  double msum = 0;
+  for (int i = 0; i < 4; ++i) {
+    ev.pf[3 + i] = c[i];
+    ev.leaf[i]   = c[i];
+    msum += c[i].m();
+  }
+  if (sumP.m() < msum) return false;
+  if (!check_emc((S.pb1 + S.pb2) - (p1 + p2 + sumP))) return false;
+  return lorentz_scalars(S, ev);
+}
+
 bool build_kinematics(const Setup &S, const double *u, Event &ev) {
+  if (S.p.n_central == 4) return build_kinematics_c4(S, u, ev);
   const grn_gencuts &g = S.p.gcuts;
   const double lo  = std::log(g.fpt_min + ZERO_EPS);
   const double hi  = std::log(g.fpt_max);
@@ -469,6 +549,27 @@ bool loop_kinematics(const Setup &S, const Event &born, double p1x, double p1y, 
     ev.pf[1] = p1;
     ev.pf[2] = p2;
     if (!check_emc((S.pb1 + S.pb2) - (p1 + p2 + pX))) return false;
+    return lorentz_scalars(S, ev);
+  }
+  if (S.p.n_central == 4) {
+    // MContinuum::LoopKinematics: central transverse momenta re-solved with the tree-level
+    // difference momenta, rapidities and masses
+    double m4[4], y4[4];
+    for (int i = 0; i < 4; ++i) {
+      m4[i] = born.pf[3 + i].m();
+      y4[i] = born.pf[3 + i].rap();
+    }
+    V4 c[4];
+    central_four(born.kq, p1T, p2T, m4, y4, c);
+    const V4 sumP = c[0] + c[1] + c[2] + c[3];
+    V4 p1, p2;
+    if (!forward_legs(S, p1T.pt(), p1x, p1y, p2T.pt(), p2x, p2y, sumP, p1, p2)) return false;
+    ev       = born;
+    ev.pf[0] = sumP;
+    ev.pf[1] = p1;
+    ev.pf[2] = p2;
+    for (int i = 0; i < 4; ++i) ev.pf[3 + i] = c[i];
+    if (!check_emc((S.pb1 + S.pb2) - (p1 + p2 + sumP))) return false;
     return lorentz_scalars(S, ev);
   }
   const double m[2] = {born.pf[3].m(), born.pf[4].m()};
@@ -1355,13 +1456,16 @@ double ps_factor(const Setup &S, const Event &ev) {
     const double vol = (ev.m2hi - ev.m2lo) * (g.Y_max - g.Y_min) * fwd;
     return (ev.dw / (2.0 * PI)) * psw * vol;
   }
-  const int Nf = 4;
+  const int Kf = S.p.n_central, Nf = Kf + 2;
+  double prod = ev.q.pt();
+  if (Kf == 4) prod = ev.kq[0].pt() * ev.kq[1].pt() * ev.kq[2].pt();
   const double psw = (1.0 / std::pow(2.0, 2 * (Nf - 2))) * (1.0 / std::pow(2.0 * PI, 3 * Nf - 4)) *
                      (ev.pf[1].pt() / (2.0 * ev.pf[1].e)) * (ev.pf[2].pt() / (2.0 * ev.pf[2].e)) *
-                     J * ev.q.pt();
+                     J * prod;
   const double fwd = sq(2.0 * PI) * ev.pf[1].pt() * ev.pf[2].pt() *
                      sq(std::log(g.fpt_max) - std::log(g.fpt_min + ZERO_EPS));
-  const double vol = (g.kt_max - g.kt_min) * (2.0 * PI) * sq(g.rap_max - g.rap_min) * fwd;
+  const double vol = std::pow(g.kt_max - g.kt_min, Kf - 1) * std::pow(2.0 * PI, Kf - 1) *
+                     std::pow(g.rap_max - g.rap_min, Kf) * fwd;
   return psw * vol;
 }
 
@@ -1476,9 +1580,7 @@ int orc_weights(const grn_process_params *p, const double *u, int64_t n, int32_t
   const int32_t want = p && (p->n_decay == 2 || p->n_central == 4) ? 14 : 8;
   if (!p || !u || !w || dim != want || (p->n_central != 2 && p->n_central != 4))
     return GRN_ERR_INVALID;
-  if (p->n_central == 4 &&
-      (p->process != GRN_PROC_REGGE_CON || p->phase_space != GRN_PS_FACTORIZED))
-    return GRN_ERR_INVALID;
+  if (p->n_central == 4 && p->process != GRN_PROC_REGGE_CON) return GRN_ERR_INVALID;
   if (p->screening && (!msa || n_kt2 < 2)) return GRN_ERR_STATE;
   const orc::Setup S = orc::make_setup(p, msa, n_kt2);
   orc::parallel_for(n, nthreads, [&](int64_t a, int64_t b) {

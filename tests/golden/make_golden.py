@@ -187,6 +187,22 @@ def nbody_fixtures():
     print("f4: flat", flat, "vegas", vegas)
 
 
+def nbody_c_fixtures():
+    """Regge continuum of four central particles in the continuum class (PP[CON]<C> ->
+    pi+ pi- pi+ pi-, MRegge::ME6 with MContinuum::BNRandomKin / BNBuildKin): tree level and
+    screened. The generator draws inside EventWeight are the four inert off-shell masses."""
+    replay = ["--replay", "h,h,h,h"]
+    proc = "PP[CON]<C> -> pi+ pi- pi+ pi-"
+    u = philox_np.uniforms(131, 2048, 14)
+    r = run_weights(CARD, u, replay, proc=proc, leaves=4)
+    save("c4_tree_weights.npz", seed=131, u=u, card=os.path.basename(CARD), proc=proc, **r)
+    u = philox_np.uniforms(132, 64, 14)
+    r = run_weights(CARD_SCR, u, replay + ["--nbt", "1024", "--nkt2", "10000"], proc=proc,
+                    leaves=4)
+    save("c4_screened_weights.npz", seed=132, u=u, card=os.path.basename(CARD_SCR), proc=proc,
+         n_bt=1024, n_kt2=10000, **r)
+
+
 def regge_res_fixtures():
     """Regge resonances (PROC_9 PP[RES], PROC_17 PP[RES+CON]; MRegge::ME3 with the spin
     density-matrix production and decay amplitudes): the Collins-Soper, helicity and
@@ -271,11 +287,15 @@ def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--ref", default="/root/reference")
     ap.add_argument("--only", choices=["all", "resonances", "cascades", "rescon", "regge_res",
-                                       "nbody"],
+                                       "nbody", "nbody_c"],
                     default="all")
     a = ap.parse_args()
     subprocess.check_call(["make", "-s", "-C", os.path.join(REPO, "oracle", "refbuild"), "-j8",
                            "REF=" + a.ref])
+    if a.only in ("all", "nbody_c"):
+        nbody_c_fixtures()
+    if a.only == "nbody_c":
+        return
     if a.only in ("all", "nbody"):
         nbody_fixtures()
     if a.only == "nbody":

@@ -32,7 +32,8 @@ def _rel(w, wr):
     return np.abs(w[nz] - wr[nz]) / wr[nz]
 
 
-@pytest.mark.parametrize("name", ["f4_tree_weights.npz", "f4_kk_tree_weights.npz"])
+@pytest.mark.parametrize("name", ["f4_tree_weights.npz", "f4_kk_tree_weights.npz",
+                                  "c4_tree_weights.npz"])
 def test_four_body_tree_weights_match_reference(gpu, name):
     import graniitti_gb300 as g
     gl = _load(name)
@@ -53,9 +54,10 @@ def test_four_body_tree_weights_match_reference(gpu, name):
     e.close()
 
 
-def test_four_body_screened_weights_match_reference(gpu):
+@pytest.mark.parametrize("name", ["f4_screened_weights.npz", "c4_screened_weights.npz"])
+def test_four_body_screened_weights_match_reference(gpu, name):
     import graniitti_gb300 as g
-    gl = _load("f4_screened_weights.npz")
+    gl = _load(name)
     t = _load("eikonal_nbt1024_nkt10000.npz")
     P = _params(gl)
     assert P.screening
@@ -64,12 +66,12 @@ def test_four_body_screened_weights_match_reference(gpu):
     w, fl = e.event_weights(gl["u"], prec=g.FP64)
     assert np.array_equal(fl & 1, gl["kin"])
     r = _rel(w, gl["w"])
-    print("screened 4 pi: GPU FP64 vs reference max rel %.2e" % r.max())
+    print("%s: GPU FP64 vs reference max rel %.2e" % (name, r.max()))
     assert r.max() < 1e-9
     # the FP32 pass runs the 4-body loop in FP64 from FP32-rounded loop nodes
     wm, _ = e.event_weights(gl["u"], prec=g.MIXED)
     rm = _rel(wm, gl["w"])
-    print("screened 4 pi: GPU MIXED vs reference max rel %.2e" % rm.max())
+    print("%s: GPU MIXED vs reference max rel %.2e" % (name, rm.max()))
     assert rm.max() < 1e-5
     e.close()
 

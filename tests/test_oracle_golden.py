@@ -208,9 +208,11 @@ def test_vector_pair_cascade_weights(name):
 
 
 @pytest.mark.parametrize("name", ["f4_tree_weights.npz", "f4_kk_tree_weights.npz",
-                                  "f4_screened_weights.npz"])
+                                  "f4_screened_weights.npz", "c4_tree_weights.npz",
+                                  "c4_screened_weights.npz"])
 def test_four_body_continuum_weights(name):
-    """PP[CON]<F> -> 4 bodies (MRegge::ME6 with the weighted N-body phase space)."""
+    """PP[CON]<F|C> -> 4 bodies (MRegge::ME6 with the weighted N-body phase space, or the
+    continuum class's 14-dimensional phase space)."""
     g = _load(name)
     P = _params_res(g)
     assert P.n_central == 4
