@@ -133,7 +133,8 @@ def test_regge_resonance_params(lib_built):
 
 
 @pytest.mark.parametrize("proc", ["PP[RESHEL]<C> -> pi+ pi-", "PP[CON]<Q> -> pi+ pi-",
-                                  "PP[CON]<C> -> pi+ pi- pi+ pi-", "yy[CON]<C> -> mu+ mu-"])
+                                  "PP[CON]<C> -> pi+ pi- pi+ pi- pi+ pi-", "yy[CON]<C> -> mu+ mu-",
+                                  "PP[CONTENSOR]<F> -> pi+ pi- pi+ pi-"])
 def test_unsupported_processes_are_rejected(proc):
     with pytest.raises(card.UnsupportedProcess):
         card.build_params(card.read_card(CARD), proc)
