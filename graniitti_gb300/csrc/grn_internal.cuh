@@ -33,7 +33,7 @@ constexpr double kRefineKappa = 8.0;
 constexpr double kRefineTol   = 1e-5;
 
 constexpr int kMaxLoopNodes = 256;  // per axis
-constexpr int kMaxDim       = 16;   // hypercube dimensions: 8 (2-body), 14 (two-body cascades)
+constexpr int kMaxDim       = 16;   // hypercube dimensions: 8 (2-body), 14 (cascades, 4-body)
 
 // Scalars accumulated per block by the VEGAS sampling kernel.
 enum VegasScalar {
