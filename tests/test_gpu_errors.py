@@ -13,7 +13,7 @@ def test_status_codes(gpu, params, params_screened):
     lib = _abi.load_library()
     bad = _abi.ProcessParams()
     ctypes.memmove(ctypes.byref(bad), ctypes.byref(params), ctypes.sizeof(bad))
-    bad.n_central = 4
+    bad.n_central = 3  # 2- and 4-body central states are built
     h = ctypes.c_void_p()
     assert lib.grn_create(ctypes.byref(bad), 0, ctypes.byref(h)) == _abi.GRN_ERR_UNSUPPORTED
     bad.n_central = 2
