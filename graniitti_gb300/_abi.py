@@ -39,6 +39,7 @@ GRN_PROC_REGGE_RES = 5
 GRN_PROC_REGGE_RESCON = 6
 GRN_FRAME_CM, GRN_FRAME_HX, GRN_FRAME_CS = 0, 1, 2
 GRN_MAX_RESONANCES = 4
+GRN_MAX_VETO = 8
 GRN_PS_CONTINUUM = 1
 GRN_PS_FACTORIZED = 2
 GRN_PREC_FP64 = 0
@@ -100,7 +101,10 @@ class ProcessParams(ctypes.Structure):
                 ("n_decay", c_int32), ("central_spin", c_int32), ("width", c_double * 2),
                 ("m_daughter", c_double * 4),
                 ("spin_gen", c_int32), ("spin_dec", c_int32), ("spin_frame", c_int32),
-                ("_pad_spin", c_int32), ("omega", c_double)]
+                ("_pad_spin", c_int32), ("omega", c_double),
+                ("veto_active", c_int32), ("n_veto", c_int32),
+                ("veto_eta_min", c_double * GRN_MAX_VETO), ("veto_eta_max", c_double * GRN_MAX_VETO),
+                ("veto_pt_min", c_double * GRN_MAX_VETO), ("veto_pt_max", c_double * GRN_MAX_VETO)]
 
 
 class VegasParams(ctypes.Structure):

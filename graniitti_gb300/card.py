@@ -265,8 +265,21 @@ def build_params(card, process=None, tune=None):
     for key, (lo, hi) in vals.items():
         setattr(fc, key + "_min", float(lo))
         setattr(fc, key + "_max", float(hi))
-    if card.get("VETOCUTS", {}).get("active", False):
-        raise UnsupportedProcess("veto cuts are not implemented")
+    # Veto domains "0", "1", ... with Eta and Pt ranges (MGraniitti::ReadVetoCuts,
+    # src/MGraniitti.cc:921-962: the search stops at the first missing number)
+    vc = card.get("VETOCUTS", {})
+    P.veto_active = 1 if vc.get("active", False) else 0
+    P.n_veto = 0
+    if P.veto_active:
+        doms = []
+        while str(len(doms)) in vc and "Eta" in vc[str(len(doms))] and "Pt" in vc[str(len(doms))]:
+            doms.append(vc[str(len(doms))])
+        if len(doms) > _abi.GRN_MAX_VETO:
+            raise UnsupportedProcess("at most %d veto domains" % _abi.GRN_MAX_VETO)
+        for k, d in enumerate(doms):
+            (P.veto_eta_min[k], P.veto_eta_max[k]), (P.veto_pt_min[k], P.veto_pt_max[k]) = \
+                map(float, d["Eta"]), map(float, d["Pt"])
+        P.n_veto = len(doms)
 
     # Model parameters.
     s = T["PARAM_SOFT"]

@@ -312,6 +312,8 @@ grn_status derive_consts(const grn_process_params &P, grn::Consts &K) {
       !(P.gcuts.rap_max > P.gcuts.rap_min))
     return fail(GRN_ERR_INVALID, "invalid generation cuts");
   if (!(P.s_factor >= 1.0)) return fail(GRN_ERR_INVALID, "s_factor must be >= 1");
+  if (P.veto_active && (P.n_veto < 0 || P.n_veto > GRN_MAX_VETO))
+    return fail(GRN_ERR_INVALID, "veto cuts: 0 to 8 domains");
   K.sqrt_s = P.sqrt_s;
   K.s      = P.sqrt_s * P.sqrt_s;
   const double E  = 0.5 * P.sqrt_s;

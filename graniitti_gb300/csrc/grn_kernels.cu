@@ -388,12 +388,13 @@ template <bool CASC>
 __device__ __forceinline__ bool born_stage(const KArgs &A, const double *x, Born &b, double &W,
                                            uint8_t &flags) {
   if (CASC && is_nbody(A.P)) return nbody_born_stage(A, x, W, flags);
-  const bool kin = born_kinematics<CASC>(A.P, A.K, x, b);
-  const bool fid = kin && fiducial_cuts(A.P, A.K, b);
+  const bool kin  = born_kinematics<CASC>(A.P, A.K, x, b);
+  const bool fid  = kin && fiducial_cuts(A.P, A.K, b);
+  const bool veto = !kin || veto_cuts(A.P, b);
   flags = (kin ? GRN_FLAG_KINEMATICS_OK : 0) | (fid ? GRN_FLAG_FIDCUTS_OK : 0) |
-          GRN_FLAG_VETOCUTS_OK | GRN_FLAG_AMPLITUDE_OK;
+          (veto ? GRN_FLAG_VETOCUTS_OK : 0) | GRN_FLAG_AMPLITUDE_OK;
   W = 0.0;
-  if (!(kin && fid)) return false;
+  if (!(kin && fid && veto)) return false;
   if (A.P.screening) return true;
   W = weight_jacobian(A.K, b) * born_amp2<CASC>(A.P, A.K, b);
   if (!isfinite(W)) {
@@ -711,7 +712,8 @@ __global__ void k_event_kinematics(const KArgs A, const double *__restrict__ u, 
     bool kin = nbody_kinematics(A.P, A.K, x, e);
     kin      = kin && nbody_legs(A.K, e, e.p1x, e.p1y, e.p2x, e.p2y, g);
     kin      = kin && nbody_amp(A.P, A.K, e, g, a0);
-    const bool fid = kin && nbody_fiducial(A.P, e, g);
+    const bool fid  = kin && nbody_fiducial(A.P, e, g);
+    const bool veto = !kin || !e.veto;
     if (p4) {
       const LC4 *v[4] = {&g.p1, &g.p2, &e.c[0], &e.c[1]};
       for (int k = 0; k < 4; ++k) {
@@ -728,12 +730,13 @@ __global__ void k_event_kinematics(const KArgs A, const double *__restrict__ u, 
     }
     if (flags)
       flags[i] = (kin ? GRN_FLAG_KINEMATICS_OK : 0) | (fid ? GRN_FLAG_FIDCUTS_OK : 0) |
-                 GRN_FLAG_VETOCUTS_OK | GRN_FLAG_AMPLITUDE_OK;
+                 (veto ? GRN_FLAG_VETOCUTS_OK : 0) | GRN_FLAG_AMPLITUDE_OK;
     return;
   }
   Born       b;
-  const bool kin = born_kinematics<true>(A.P, A.K, x, b);
-  const bool fid = kin && fiducial_cuts(A.P, A.K, b);
+  const bool kin  = born_kinematics<true>(A.P, A.K, x, b);
+  const bool fid  = kin && fiducial_cuts(A.P, A.K, b);
+  const bool veto = !kin || veto_cuts(A.P, b);
   if (p4) {
     double *o = p4 + i * 16;
     o[0] = b.p1x; o[1] = b.p1y; o[2] = 0.5 * (b.p1p - b.p1m); o[3] = 0.5 * (b.p1p + b.p1m);
@@ -747,7 +750,7 @@ __global__ void k_event_kinematics(const KArgs A, const double *__restrict__ u, 
   }
   if (flags)
     flags[i] = (kin ? GRN_FLAG_KINEMATICS_OK : 0) | (fid ? GRN_FLAG_FIDCUTS_OK : 0) |
-               GRN_FLAG_VETOCUTS_OK | GRN_FLAG_AMPLITUDE_OK;
+               (veto ? GRN_FLAG_VETOCUTS_OK : 0) | GRN_FLAG_AMPLITUDE_OK;
 }
 
 // Cascade daughters (px, py, pz, E) of the points (zeros where the kinematics fail).

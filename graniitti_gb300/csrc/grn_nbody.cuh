@@ -68,6 +68,7 @@ struct NBEvent {
   double m2w;               // mass^2 window of the system (B51IntegralVolume)
   double sbc[kNb][kNb];     // (p_b + p_c)^2 of central pairs
   bool   cuts;              // the central particles pass the particle cuts
+  bool   veto;              // a central particle hits a veto domain
   double jx;                // per-event phase-space factor: F dPhi_N / (2 pi) x mass^2 window,
                             // C the product of the difference momenta kt_i
   double kx[kNb - 1], ky[kNb - 1], y[kNb];  // C: difference momenta, rapidities
@@ -111,6 +112,10 @@ GRN_HD bool nbody_finish(const grn_process_params &P, NBEvent &e) {
       e.sbc[b][a] = e.sbc[a][b];
       if (e.sbc[a][b] < 0) return false;
     }
+  e.veto = false;
+  if (P.veto_active)
+    for (int a = 0; a < kNb; ++a)
+      e.veto |= veto_hit(P, e.c[a].x, e.c[a].y, 0.5 * (e.c[a].p - e.c[a].m));
   const grn_fidcuts &f = P.fcuts;
   e.cuts = true;
   if (f.active) {
@@ -402,11 +407,12 @@ __device__ __noinline__ bool nbody_born_stage(const KArgs &A, const double *x, d
   kin = kin && nbody_legs(A.K, e, e.p1x, e.p1y, e.p2x, e.p2y, g);
   cx<double> A0{0.0, 0.0};
   kin = kin && nbody_amp(A.P, A.K, e, g, A0);
-  const bool fid = kin && nbody_fiducial(A.P, e, g);
+  const bool fid  = kin && nbody_fiducial(A.P, e, g);
+  const bool veto = !kin || !e.veto;
   flags = (kin ? GRN_FLAG_KINEMATICS_OK : 0) | (fid ? GRN_FLAG_FIDCUTS_OK : 0) |
-          GRN_FLAG_VETOCUTS_OK | GRN_FLAG_AMPLITUDE_OK;
+          (veto ? GRN_FLAG_VETOCUTS_OK : 0) | GRN_FLAG_AMPLITUDE_OK;
   W = 0.0;
-  if (!(kin && fid)) return false;
+  if (!(kin && fid && veto)) return false;
   if (A.P.screening) return true;
   W = nbody_jacobian(A.K, e, g) * (A0.re * A0.re + A0.im * A0.im);
   if (!isfinite(W)) {

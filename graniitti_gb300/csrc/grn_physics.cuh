@@ -809,14 +809,29 @@ GRN_HD bool particle_cuts(const grn_process_params &P, const double *p) {
 }
 
 // All four cascade daughters pass the particle cuts.
+// Veto cuts (MProcess::FindVetoCuts, src/MProcess.cc:1157-1175): true when a final-state
+// particle (px, py, pz) lies in one of the veto domains.
+GRN_HD bool veto_hit(const grn_process_params &P, double px, double py, double pz) {
+  const double pt = sqrt(px * px + py * py), eta = asinh(pz / pt);
+  bool hit = false;
+  for (int k = 0; k < P.n_veto; ++k)
+    hit |= pt >= P.veto_pt_min[k] && pt <= P.veto_pt_max[k] && eta >= P.veto_eta_min[k] &&
+           eta <= P.veto_eta_max[k];
+  return hit;
+}
+
+// bit 0: the four daughters pass the particle cuts; bit 1: one of them hits a veto domain.
 GRN_HD_COLD int cascade_cuts(const grn_process_params &P, double p3x, double p3y, double p3z,
                              double E3, double m3, double p4x, double p4y, double p4z, double E4,
                              double m4, const double *u) {
   double d[4][4];
   cascade_daughters(P, p3x, p3y, p3z, E3, m3, p4x, p4y, p4z, E4, m4, u, d);
-  int ok = 1;
-  for (int k = 0; k < 4; ++k) ok &= particle_cuts(P, d[k]) ? 1 : 0;
-  return ok;
+  int ok = 1, veto = 0;
+  for (int k = 0; k < 4; ++k) {
+    ok &= particle_cuts(P, d[k]) ? 1 : 0;
+    if (P.veto_active) veto |= veto_hit(P, d[k][0], d[k][1], d[k][2]) ? 2 : 0;
+  }
+  return ok | veto;
 }
 
 // B51RandomKin + B51BuildKin for a 2-body central system, the isotropic decay
@@ -919,7 +934,7 @@ GRN_HD bool fiducial_cuts(const grn_process_params &P, const Consts &K, const Bo
   if (!(M >= f.M_min && M <= f.M_max && Y >= f.Y_min && Y <= f.Y_max && Pt >= f.Pt_min &&
         Pt <= f.Pt_max))
     return false;
-  if (P.n_decay == 2) return b.leafok != 0;
+  if (P.n_decay == 2) return (b.leafok & 1) != 0;
   bool ok = true;
   const double px[2] = {b.p3x, b.p4x}, py[2] = {b.p3y, b.p4y};
   const double mt[2] = {b.mt3, b.mt4}, y[2] = {b.y3, b.y4};
@@ -933,6 +948,15 @@ GRN_HD bool fiducial_cuts(const grn_process_params &P, const Consts &K, const Bo
       ok = false;
   }
   return ok;
+}
+
+// Veto cuts on the final-state leaves (MProcess::VetoCuts, src/MProcess.cc:1069-1082): true
+// when the event is not vetoed.
+GRN_HD bool veto_cuts(const grn_process_params &P, const Born &b) {
+  if (!P.veto_active) return true;
+  if (P.n_decay == 2) return (b.leafok & 2) == 0;
+  return !veto_hit(P, b.p3x, b.p3y, 0.5 * (b.p3p - b.p3m)) &&
+         !veto_hit(P, b.p4x, b.p4y, 0.5 * (b.p4p - b.p4m));
 }
 
 // Regge continuum amplitude of a 2-body central state, sign +1

@@ -155,6 +155,8 @@ typedef struct grn_loop_numerics { /* MEikonalNumerics, include/Graniitti/MEikon
   int32_t n_kt2;     /* NumberKT2: screening-table intervals (even) */
 } grn_loop_numerics;
 
+#define GRN_MAX_VETO 8 /* veto domains */
+
 typedef struct grn_process_params {
   int32_t process;        /* GRN_PROC_* */
   int32_t phase_space;    /* GRN_PS_* */
@@ -188,6 +190,14 @@ typedef struct grn_process_params {
    * frame of the density matrices (GRN_FRAME_*), the flux exponent (PARAM_REGGE omega) */
   int32_t           spin_gen, spin_dec, spin_frame, _pad_spin;
   double            omega;
+  /* Veto cuts (VETOCUTS, MProcess::VetoCuts / FindVetoCuts, src/MProcess.cc:1069-1175): an
+   * event is rejected when any final-state particle of the central system (the leaves of the
+   * decay tree) has pt_min[k] <= pT <= pt_max[k] and eta_min[k] <= eta <= eta_max[k] for some
+   * domain k < n_veto. Elastic forward protons are not tested (the reference tests only the
+   * fragments of excited forward systems). */
+  int32_t           veto_active, n_veto;
+  double            veto_eta_min[GRN_MAX_VETO], veto_eta_max[GRN_MAX_VETO];
+  double            veto_pt_min[GRN_MAX_VETO], veto_pt_max[GRN_MAX_VETO];
 } grn_process_params;
 
 /* Fill every field with the reference defaults for "PP[CON]<C> -> pi+ pi-" at

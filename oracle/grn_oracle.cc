@@ -1493,13 +1493,31 @@ bool fiducial(const Setup &S, const Event &ev) {
   return ok;
 }
 
+// Veto cuts (MProcess::VetoCuts + FindVetoCuts, MProcess.cc:1069-1082, 1157-1175): false when
+// a final-state particle of the central system lies in a veto domain (elastic forward
+// protons have no fragments to test).
+bool veto_cuts(const Setup &S, const Event &ev) {
+  if (!S.p.veto_active) return true;
+  const bool leaves = S.p.n_decay == 2 || S.p.n_central == 4;
+  const int  np     = leaves ? 4 : 2;
+  for (int k = 0; k < np; ++k) {
+    const V4 &p = leaves ? ev.leaf[k] : ev.pf[3 + k];
+    const double pt = p.pt(), eta = p.eta();
+    for (int d = 0; d < S.p.n_veto; ++d)
+      if (pt >= S.p.veto_pt_min[d] && pt <= S.p.veto_pt_max[d] && eta >= S.p.veto_eta_min[d] &&
+          eta <= S.p.veto_eta_max[d])
+        return false;
+  }
+  return true;
+}
+
 // One event weight (MContinuum::EventWeight, src/MContinuum.cc:164-193).
 double event_weight(const Setup &S, const double *u, uint8_t &flags, Event &ev) {
   double W = 0.0;
   const bool kin = S.p.phase_space == GRN_PS_FACTORIZED ? build_kinematics_F(S, u, ev)
                                                         : build_kinematics(S, u, ev);
   const bool fid = kin && fiducial(S, ev);
-  const bool veto = true;
+  const bool veto = !kin || veto_cuts(S, ev);
   if (kin && fid && veto) {
     cplx A0[9];
     const int nh = bare_amps(S, ev, A0);

@@ -187,6 +187,23 @@ def nbody_fixtures():
     print("f4: flat", flat, "vegas", vegas)
 
 
+def veto_fixtures():
+    """Veto cuts (VETOCUTS; MProcess::VetoCuts on the final-state leaves) with two domains, for
+    the <C> pi+ pi- continuum, the tensor rho rho cascade (its four pions) and the 4 pi
+    continuum (<F>)."""
+    card = os.path.join(HERE, "cards", "pp_con_pipi_veto.json")
+    cases = [("veto_c_weights.npz", 141, "PP[CON]<C> -> pi+ pi-", [], 8, 8),
+             ("veto_rr_weights.npz", 142,
+              "PP[CONTENSOR]<F> -> rho(770)0 > {pi+ pi-} rho(770)0 > {pi+ pi-}",
+              ["--replay", "h,h,8,h,h,9,6,7,h,h,10,11,h,h,12,13"], 6, 14),
+             ("veto_f4_weights.npz", 143, "PP[CON]<F> -> pi+ pi- pi+ pi-",
+              ["--replay", "h,h,h,h,6,7,h,8,9,10,11,12,13"], 6, 14)]
+    for name, seed, proc, extra, dim, width in cases:
+        u = philox_np.uniforms(seed, 2048, width)
+        r = run_weights(card, u, extra, proc=proc, dim=dim)
+        save(name, seed=seed, u=u, card=os.path.basename(card), proc=proc, **r)
+
+
 def nbody_c_fixtures():
     """Regge continuum of four central particles in the continuum class (PP[CON]<C> ->
     pi+ pi- pi+ pi-, MRegge::ME6 with MContinuum::BNRandomKin / BNBuildKin): tree level and
@@ -287,11 +304,15 @@ def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--ref", default="/root/reference")
     ap.add_argument("--only", choices=["all", "resonances", "cascades", "rescon", "regge_res",
-                                       "nbody", "nbody_c"],
+                                       "nbody", "nbody_c", "veto"],
                     default="all")
     a = ap.parse_args()
     subprocess.check_call(["make", "-s", "-C", os.path.join(REPO, "oracle", "refbuild"), "-j8",
                            "REF=" + a.ref])
+    if a.only in ("all", "veto"):
+        veto_fixtures()
+    if a.only == "veto":
+        return
     if a.only in ("all", "nbody_c"):
         nbody_c_fixtures()
     if a.only == "nbody_c":

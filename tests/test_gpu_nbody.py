@@ -155,3 +155,22 @@ def test_four_body_record_kinematics_and_events(gpu, tmp_path):
     assert np.allclose(last, pd[idx], rtol=1e-12, atol=1e-12)
     assert [int(p[3]) for p in parts[7:11]] == [211, -211, 211, -211]
     e.close()
+
+
+@pytest.mark.parametrize("name", ["veto_c_weights.npz", "veto_rr_weights.npz",
+                                  "veto_f4_weights.npz"])
+def test_veto_cuts_match_reference(gpu, name):
+    """Veto cuts (two domains on the final-state leaves) for a 2-body continuum, a cascade
+    and a 4-body state: veto flags and weights as the reference's."""
+    import graniitti_gb300 as g
+    gl = _load(name)
+    e = g.Engine(_params(gl), 0)
+    w, fl = e.event_weights(gl["u"], prec=g.FP64)
+    kin = gl["kin"] == 1
+    assert np.array_equal(fl & 1, gl["kin"])
+    assert np.array_equal(((fl >> 2) & 1)[kin], gl["veto"][kin])
+    r = _rel(w, gl["w"])
+    print("%s: %d vetoed, GPU vs reference max rel %.2e" % (name, (gl["veto"][kin] == 0).sum(),
+                                                           r.max()))
+    assert r.max() < 1e-9
+    e.close()

@@ -297,3 +297,17 @@ def test_histogram_observables_from_reference_kinematics(params):
         if k.endswith("_AH"):
             diff = diff / ah_cond
         assert diff.max() < 1e-8, (k, diff.max())
+
+
+@pytest.mark.parametrize("name", ["veto_c_weights.npz", "veto_rr_weights.npz",
+                                  "veto_f4_weights.npz"])
+def test_veto_cuts(name):
+    """Veto domains on the final-state leaves: flags and weights as the reference's."""
+    g = _load(name)
+    P = _params_res(g)
+    assert P.veto_active == 1 and P.n_veto == 2
+    w, fl = orc.weights(P, g["u"], nthreads=4)
+    _check_weights(w, fl, g, tol=W_TOL)
+    kin = g["kin"] == 1
+    assert np.array_equal(((fl >> 2) & 1)[kin], g["veto"][kin])
+    assert (g["veto"][kin] == 0).sum() > 100
