@@ -66,6 +66,18 @@ bool is_device_ptr(const void *ptr) {
   return a.type == cudaMemoryTypeDevice || a.type == cudaMemoryTypeManaged;
 }
 
+// Device memory of another GPU than `device` (unmanaged): the kernels would reach it
+// through peer addressing that the engine never enables.
+bool on_other_device(const void *ptr, int device) {
+  if (!ptr) return false;
+  cudaPointerAttributes a;
+  if (cudaPointerGetAttributes(&a, ptr) != cudaSuccess) {
+    cudaGetLastError();
+    return false;
+  }
+  return a.type == cudaMemoryTypeDevice && a.device != device;
+}
+
 std::vector<double> simpson38_weights(int N) {
   std::vector<double> w(N + 1, 3.0);
   w[0] = w[N] = 1.0;
@@ -106,7 +118,8 @@ struct grn_engine {
   int         nblocks = 0;
   DevBuf      d_xmat, d_xmat_prev, d_f2mat, d_f, d_acc, d_parts, d_sc;
   DevBuf      d_xmat_flat;  // uniform grid of FLAT passes (x = u, vw = 1)
-  DevBuf      d_lidx, d_lx, d_lvw, d_lbins, d_lbins_hi;  // screened work list of a VEGAS pass
+  DevBuf      d_lidx, d_lx, d_lvw;  // screened work list of a VEGAS pass
+  DevBuf      d_hpart;              // partial f^2 histograms of a pass (kHistBlocks x bins x dim)
   DevBuf      d_rlist;  // slots of that list refined in FP64
   // on-the-fly histograms: specs (host copy and device), bin offsets, sums
   std::vector<grn_hist_spec> hist;
@@ -596,8 +609,8 @@ grn_status grn_destroy(grn_engine *e) {
                     &e->d_lc_phi, &e->d_u,     &e->d_w,         &e->d_flags,     &e->d_aux,
                     &e->d_wlist, &e->d_wcount, &e->d_xmat,      &e->d_xmat_prev, &e->d_f2mat,
                     &e->d_f,     &e->d_acc,    &e->d_parts,     &e->d_sc,        &e->d_lidx,
-                    &e->d_lx,    &e->d_lvw,    &e->d_lbins,     &e->d_uw_counts, &e->d_uw_misc,
-                    &e->d_lbins_hi, &e->d_rlist, &e->d_wrlist, &e->d_hspec, &e->d_hoff,
+                    &e->d_lx,    &e->d_lvw,    &e->d_hpart,     &e->d_uw_counts, &e->d_uw_misc,
+                    &e->d_rlist, &e->d_wrlist, &e->d_hspec, &e->d_hoff,
                     &e->d_hw, &e->d_hw2, &e->d_hcnt, &e->d_hout,
                     &e->d_uw_idx, &e->d_recf,  &e->d_recd,      &e->d_xmat_flat};
   for (DevBuf *b : bufs) b->release();
@@ -705,6 +718,9 @@ grn_status grn_event_weights(grn_engine *e, const double *u, int64_t n, int32_t 
   if (st != GRN_OK) return st;
   if (n == 0) return GRN_OK;
   GRN_CUDA(cudaSetDevice(e->device));
+  if (on_other_device(u, e->device) || on_other_device(w_out, e->device) ||
+      on_other_device(flags, e->device))
+    return fail(GRN_ERR_INVALID, "device arrays must be on the engine's device");
   const bool dev_u = is_device_ptr(u), dev_w = is_device_ptr(w_out);
   const bool dev_f = flags ? is_device_ptr(flags) : true;
   const double *du = u;
@@ -819,9 +835,6 @@ grn_status grn_uniforms(grn_engine *e, uint64_t seed, uint32_t stream, int64_t f
 // VEGAS
 
 // Bin indices of dimensions 8..15 of the screened work list (null for 8 dimensions).
-static uint64_t *lbins_hi(grn_engine *e) {
-  return e->dim > 8 ? e->d_lbins_hi.as<uint64_t>() : nullptr;
-}
 
 // Per-call buffers of a VEGAS pass: f values and the screened work list.
 static grn_status vegas_alloc_calls(grn_engine *e, int64_t ncall) {
@@ -831,8 +844,6 @@ static grn_status vegas_alloc_calls(grn_engine *e, int64_t ncall) {
   GRN_CUDA(e->d_rlist.ensure(n * sizeof(int64_t)));
   GRN_CUDA(e->d_lx.ensure(static_cast<size_t>(e->dim) * n * sizeof(double)));
   GRN_CUDA(e->d_lvw.ensure(n * sizeof(double)));
-  GRN_CUDA(e->d_lbins.ensure(n * sizeof(uint64_t)));
-  if (e->dim > 8) GRN_CUDA(e->d_lbins_hi.ensure(n * sizeof(uint64_t)));
   if (e->P.screening) {
     GRN_CUDA(e->d_recf.ensure(n * grn::kLoopEventFields * sizeof(float)));
     GRN_CUDA(e->d_recd.ensure(n * grn::kRecordDoubles * sizeof(double)));
@@ -845,6 +856,8 @@ static grn_status vegas_alloc(grn_engine *e) {
   GRN_CUDA(e->d_xmat.ensure(nh * sizeof(double)));
   GRN_CUDA(e->d_xmat_prev.ensure(nh * sizeof(double)));
   GRN_CUDA(e->d_f2mat.ensure(nh * sizeof(double)));
+  GRN_CUDA(e->d_hpart.ensure(static_cast<size_t>(grn::kHistBlocks) * nh * sizeof(double)));
+  GRN_CUDA(grn::vegas_hist_prepare());
   GRN_CUDA(e->d_sc.ensure(grn::VS_COUNT * sizeof(double)));
   GRN_CUDA(e->d_acc.ensure(grn::kAccSlots * sizeof(unsigned long long)));
   GRN_CUDA(e->d_parts.ensure(2 * grn::kVegasSumParts * sizeof(double)));
@@ -921,28 +934,29 @@ static grn_status vegas_pass(grn_engine *e, int prec, int track_max, int refine,
   double     *rd  = rec ? e->d_recd.as<double>() : nullptr;
   GRN_CUDA(grn::launch_vegas_born(a, xmat, e->bins, e->dim, e->ncall, e->seed,
                                   stream_id, track_max, e->d_f.as<double>(),
-                                  e->d_f2mat.as<double>(), e->d_acc.as<unsigned long long>(),
-                                  e->d_lidx.as<int64_t>(), e->d_lx.as<double>(),
-                                  e->d_lvw.as<double>(), e->d_lbins.as<uint64_t>(), lbins_hi(e),
-                                  rf, rd,
+                                  e->d_acc.as<unsigned long long>(), e->d_lidx.as<int64_t>(),
+                                  e->d_lx.as<double>(), e->d_lvw.as<double>(), rf, rd,
                                   e->stream, fu, flq));
   // the timed kernel: the kt-loop stage when screening is on
   GRN_CUDA(cudaEventRecord(e->ev0, e->stream));
   GRN_CUDA(grn::launch_vegas_loop(a, prec, e->bins, e->dim, e->ncall, track_max,
-                                  e->d_f.as<double>(), e->d_f2mat.as<double>(),
-                                  e->d_acc.as<unsigned long long>(), e->d_lidx.as<int64_t>(),
-                                  e->d_lx.as<double>(), e->d_lvw.as<double>(),
-                                  e->d_lbins.as<uint64_t>(), lbins_hi(e), rf, rd,
-                                  e->d_rlist.as<int64_t>(), e->nblocks, e->stream));
+                                  e->d_f.as<double>(), e->d_acc.as<unsigned long long>(),
+                                  e->d_lidx.as<int64_t>(), e->d_lx.as<double>(),
+                                  e->d_lvw.as<double>(), rf, rd, e->d_rlist.as<int64_t>(),
+                                  e->nblocks, e->stream));
   GRN_CUDA(cudaEventRecord(e->ev1, e->stream));
   GRN_CUDA(grn::launch_vegas_reduce(e->d_f.as<double>(), e->ncall,
                                     e->d_acc.as<unsigned long long>(), e->d_parts.as<double>(),
                                     e->d_sc.as<double>(), e->stream));
   GRN_CUDA(cudaMemcpyAsync(e->h_sc, e->d_sc.p, grn::VS_COUNT * sizeof(double),
                            cudaMemcpyDeviceToHost, e->stream));
-  if (refine)
+  if (refine) {
+    GRN_CUDA(grn::launch_vegas_hist(e->bins, e->dim, e->ncall, e->seed, stream_id, fu,
+                                    e->d_f.as<double>(), e->d_hpart.as<double>(),
+                                    e->d_f2mat.as<double>(), e->stream));
     GRN_CUDA(grn::launch_vegas_refine(e->d_xmat.as<double>(), e->d_f2mat.as<double>(), e->bins,
                                       e->dim, e->lambda, e->stream));
+  }
   GRN_CUDA(cudaStreamSynchronize(e->stream));
   {
     float ms = 0.f;
@@ -1392,7 +1406,6 @@ grn_status batch_capture(grn_batch *b, int refine, int track_max) {
     const int   nh = e->bins * e->dim;
     ce = cudaMemcpyAsync(e->d_xmat_prev.p, e->d_xmat.p, nh * sizeof(double),
                          cudaMemcpyDeviceToDevice, b->stream);
-    if (ce == cudaSuccess) ce = cudaMemsetAsync(e->d_f2mat.p, 0, nh * sizeof(double), b->stream);
     if (ce == cudaSuccess)
       ce = cudaMemsetAsync(e->d_acc.p, 0, grn::kAccSlots * sizeof(unsigned long long),
                            b->stream);
@@ -1414,10 +1427,9 @@ grn_status batch_capture(grn_batch *b, int refine, int track_max) {
     grn_engine *e = b->eng[p];
     if (!e->P.screening || b->h_procs[p].rf) continue;
     ce = grn::launch_vegas_loop(b->h_procs[p].A, GRN_PREC_MIXED, e->bins, e->dim, e->ncall,
-                                track_max, e->d_f.as<double>(), e->d_f2mat.as<double>(),
-                                e->d_acc.as<unsigned long long>(), e->d_lidx.as<int64_t>(),
-                                e->d_lx.as<double>(), e->d_lvw.as<double>(),
-                                e->d_lbins.as<uint64_t>(), lbins_hi(e), nullptr, nullptr,
+                                track_max, e->d_f.as<double>(), e->d_acc.as<unsigned long long>(),
+                                e->d_lidx.as<int64_t>(), e->d_lx.as<double>(),
+                                e->d_lvw.as<double>(), nullptr, nullptr,
                                 e->d_rlist.as<int64_t>(), e->nblocks,
                                 two ? b->side : b->stream);
   }
@@ -1430,6 +1442,9 @@ grn_status batch_capture(grn_batch *b, int refine, int track_max) {
     if (ce == cudaSuccess)
       ce = cudaMemcpyAsync(e->h_sc, e->d_sc.p, grn::VS_COUNT * sizeof(double),
                            cudaMemcpyDeviceToHost, b->stream);
+    if (ce == cudaSuccess && refine)
+      ce = grn::launch_batch_hist(p, e->bins, e->dim, e->d_hpart.as<double>(),
+                                  e->d_f2mat.as<double>(), b->stream);
     if (ce == cudaSuccess && refine)
       ce = grn::launch_vegas_refine(e->d_xmat.as<double>(), e->d_f2mat.as<double>(), e->bins,
                                     e->dim, e->lambda, b->stream);
@@ -1506,13 +1521,11 @@ grn_status grn_batch_create(grn_engine *const *engines, int32_t n, grn_batch **o
     q.ncall     = e->ncall;
     q.seed      = e->seed;
     q.f_out     = e->d_f.as<double>();
-    q.f2mat     = e->d_f2mat.as<double>();
+    q.hpart     = e->d_hpart.as<double>();
     q.acc       = e->d_acc.as<unsigned long long>();
     q.l_idx     = e->d_lidx.as<int64_t>();
     q.l_x       = e->d_lx.as<double>();
     q.l_vw      = e->d_lvw.as<double>();
-    q.l_bins    = e->d_lbins.as<uint64_t>();
-    q.l_bins_hi = lbins_hi(e);
     b->max_dim  = std::max(b->max_dim, e->dim);
     b->max_nh   = std::max(b->max_nh, e->bins * e->dim);
     q.rf        = rec ? e->d_recf.as<float>() : nullptr;
@@ -1675,11 +1688,10 @@ grn_status grn_autotune(grn_engine *e, int64_t sample, grn_tune_result *out) {
     // every candidate's stage B on the same list (its outputs are rewritten by the next pass)
     const int64_t nc0 = e->ncall;
     GRN_CUDA(grn::launch_vegas_born(a, e->d_xmat.as<double>(), e->bins, e->dim, nc0, e->seed,
-                                    0xA7A7A7u, 0, e->d_f.as<double>(), e->d_f2mat.as<double>(),
+                                    0xA7A7A7u, 0, e->d_f.as<double>(),
                                     e->d_acc.as<unsigned long long>(), e->d_lidx.as<int64_t>(),
                                     e->d_lx.as<double>(), e->d_lvw.as<double>(),
-                                    e->d_lbins.as<uint64_t>(), lbins_hi(e), e->d_recf.as<float>(),
-                                    e->d_recd.as<double>(), e->stream));
+                                    e->d_recf.as<float>(), e->d_recd.as<double>(), e->stream));
     double best = 1e300;
     int    nc   = 0;
     for (int pair = 0; pair < 3; ++pair)
@@ -1690,11 +1702,9 @@ grn_status grn_autotune(grn_engine *e, int64_t sample, grn_tune_result *out) {
         for (int rep = 0; rep < 2; ++rep) {
           GRN_CUDA(cudaEventRecord(e->ev0, e->stream));
           GRN_CUDA(grn::launch_vegas_loop(a, GRN_PREC_MIXED, e->bins, e->dim, nc0, 0,
-                                          e->d_f.as<double>(), e->d_f2mat.as<double>(),
-                                          e->d_acc.as<unsigned long long>(),
+                                          e->d_f.as<double>(), e->d_acc.as<unsigned long long>(),
                                           e->d_lidx.as<int64_t>(), e->d_lx.as<double>(),
-                                          e->d_lvw.as<double>(), e->d_lbins.as<uint64_t>(),
-                                          lbins_hi(e), e->d_recf.as<float>(),
+                                          e->d_lvw.as<double>(), e->d_recf.as<float>(),
                                           e->d_recd.as<double>(), e->d_rlist.as<int64_t>(),
                                           blocks, e->stream));
           GRN_CUDA(cudaEventRecord(e->ev1, e->stream));

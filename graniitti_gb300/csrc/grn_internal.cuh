@@ -80,24 +80,33 @@ int         vegas_grid_blocks(int device);
 cudaError_t launch_vegas_grid_init(double *xmat, int bins, int dim, cudaStream_t st);
 // One VEGAS pass in two stages; acc holds kAccSlots unsigned long long
 // accumulators (see kAccRefine); the list arrays have
-// capacity ncall (l_x: dim x ncall, dimension-major; l_bins_hi only for dim > 8).
+// capacity ncall (l_x: dim x ncall, dimension-major).
 // rf/rd: loop records (record mode, see record_mode()); null for the point mode,
 // in which the mapped points l_x are stored and stage B recomputes the tree level.
 cudaError_t launch_vegas_born(const KArgs &a, const double *xmat, int bins, int dim, int64_t ncall,
                               uint64_t seed, uint32_t stream, int track_max, double *f_out,
-                              double *f2mat, unsigned long long *acc, int64_t *l_idx, double *l_x,
-                              double *l_vw, uint64_t *l_bins, uint64_t *l_bins_hi, float *rf,
-                              double *rd, cudaStream_t st, const float *fu = nullptr,
+                              unsigned long long *acc, int64_t *l_idx, double *l_x, double *l_vw,
+                              float *rf, double *rd, cudaStream_t st, const float *fu = nullptr,
                               const float *flq = nullptr);
 // fu / flq: points drawn from the flow (dimension-major, leading dimension ncall) and
 // their log density; the VEGAS weight of a point is then vw(u) / q(u).
 // r_list (capacity ncall): slots of the FP32 generic loop whose error estimate exceeds
 // a.refine_tol, finished by an FP64 pass over them in the same call.
 cudaError_t launch_vegas_loop(const KArgs &a, int prec, int bins, int dim, int64_t ncall,
-                              int track_max, double *f_out, double *f2mat, unsigned long long *acc,
+                              int track_max, double *f_out, unsigned long long *acc,
                               const int64_t *l_idx, const double *l_x, const double *l_vw,
-                              const uint64_t *l_bins, const uint64_t *l_bins_hi, const float *rf,
-                              const double *rd, int64_t *r_list, int nblocks, cudaStream_t st);
+                              const float *rf, const double *rd, int64_t *r_list, int nblocks,
+                              cudaStream_t st);
+// The f^2 histogram of a finished pass (bins x dim, the input of launch_vegas_refine) from its
+// f array and its points (Philox (seed, stream), or the flow points fu with leading dimension
+// ncall), summed in a fixed order: equal f arrays give equal histograms bit for bit.
+// part: kHistBlocks * bins * dim doubles of scratch. vegas_hist_prepare() (once per device,
+// outside stream capture) allows the shared memory of the largest histograms.
+constexpr int kHistBlocks = 256;
+cudaError_t vegas_hist_prepare();
+cudaError_t launch_vegas_hist(int bins, int dim, int64_t ncall, uint64_t seed, uint32_t stream,
+                              const float *fu, const double *f, double *part, double *f2mat,
+                              cudaStream_t st);
 // Record mode: screened, FP32 loop, single active trajectory.
 bool        record_mode(const KArgs &a, int prec);
 constexpr int kRecordDoubles = 4;
@@ -142,11 +151,10 @@ struct BatchProc {
   uint64_t            seed;
   uint32_t            stream;     // Philox stream id of the pass (updated every pass)
   int                 track_max;  // integration pass: track the maximum weight
-  double             *f_out, *f2mat;
+  double             *f_out, *hpart;  // f array; partial f^2 histograms (kHistBlocks x nh)
   unsigned long long *acc;
   int64_t            *l_idx;
   double             *l_x, *l_vw;
-  uint64_t           *l_bins, *l_bins_hi;  // bin indices of dimensions 0..7, 8..15
   float              *rf;
   double             *rd;
   const float        *fu, *flq;    // flow points of the pass and their log density (or null)
@@ -161,6 +169,9 @@ cudaError_t launch_batch_born(int np, int nblocks, int max_dim, int max_nh, cuda
 // blocks take chunks of work from the counter (zeroed by the caller) over the listed events
 // of those processes.
 cudaError_t launch_batch_loop(int np, unsigned long long *counter, int nblocks, int max_nh,
+                              cudaStream_t st);
+// The f^2 histogram of member p of the uploaded table into f2mat (part: its q.hpart).
+cudaError_t launch_batch_hist(int p, int bins, int dim, const double *part, double *f2mat,
                               cudaStream_t st);
 int         batch_loop_blocks(int device, int max_nh);
 

@@ -998,19 +998,22 @@ cudaError_t launch_eikonal_xs(const double *mbt, int n_bt, double *xs, cudaStrea
 constexpr int kVegasThreads = 128;
 constexpr int kMaxBins      = 256;
 
+// Bin (0-based) of coordinate u in a grid of `bins` bins: the bin of the VEGAS map
+// (src/MGraniitti.cc:1362-1366), a function of u alone.
+__device__ __forceinline__ int vegas_bin(double u, double dbins, int bins) {
+  const int k = static_cast<int>(u * dbins + 1.0);
+  return max(1, min(k, bins)) - 1;
+}
+
 // Map a uniform point through the VEGAS grid in shared memory
 // (MGraniitti::VEGASMultiThread, src/MGraniitti.cc:1357-1375).
-// Bin indices are packed 8 bits per dimension: dimensions 0..7 in lo, 8..15 in hi.
 __device__ __forceinline__ double vegas_map(const double *sx, int bins, int dim, const double *u,
-                                            double *x, uint64_t &packed_bins, uint64_t &packed_hi) {
+                                            double *x) {
   const double dbins = static_cast<double>(bins);
   double       vw    = 1.0;
-  packed_bins        = 0ull;
-  packed_hi          = 0ull;
   for (int j = 0; j < dim; ++j) {
     const double zn = u[j] * dbins + 1.0;
-    int          k  = static_cast<int>(zn);
-    k               = max(1, min(k, bins));
+    const int    k  = vegas_bin(u[j], dbins, bins) + 1;
     double zo, ac;
     if (k > 1) {
       zo = sx[(k - 1) * dim + j] - sx[(k - 2) * dim + j];
@@ -1020,33 +1023,17 @@ __device__ __forceinline__ double vegas_map(const double *sx, int bins, int dim,
       ac = (zn - k) * zo;
     }
     x[j] = ac;
-    if (j < 8)
-      packed_bins |= static_cast<uint64_t>(k - 1) << (8 * j);
-    else
-      packed_hi |= static_cast<uint64_t>(k - 1) << (8 * (j - 8));
     vw *= zo * dbins;
   }
   return vw;
 }
 
-// Block-level accumulation shared by both VEGAS stages; flushed with one global
-// atomic per non-zero entry / counter at the end of the block.
-struct VegasBlockAcc {
-  double *sf2;  // shared f^2 histogram (bins * dim)
-};
-
-__device__ __forceinline__ void hist_add(double *sf2, int dim, uint64_t packed, uint64_t hi,
-                                         double f2) {
-  if (f2 == 0.0) return;
-  for (int j = 0; j < dim; ++j) {
-    const int b = static_cast<int>(((j < 8 ? packed : hi) >> (8 * (j & 7))) & 0xFFu);
-    atomicAdd(&sf2[b * dim + j], f2);
-  }
-}
-
-__device__ void flush_block(double *sf2, int nh, double *f2mat, unsigned long long *acc,
-                            const unsigned long long cnt[VS_COUNT], double maxf, double maxW) {
-  // counters: warp sums, then one atomic per warp
+// Pass counters and maxima of a block, flushed at its end: warp sums, then one integer
+// atomic per warp and counter (exact, so order-free); maxima of non-negative doubles as
+// atomicMax on their bit patterns. The f^2 histogram of the grid refinement is built
+// after the pass from the f array (k_vegas_hist), in a fixed order.
+__device__ void flush_counters(unsigned long long *acc, const unsigned long long cnt[VS_COUNT],
+                               double maxf, double maxW) {
   for (int c = 0; c < VS_COUNT; ++c) {
     if (c == VS_FSUM || c == VS_F2SUM || c == VS_MAXF || c == VS_MAXW) continue;
     unsigned long long v = cnt[c];
@@ -1062,9 +1049,6 @@ __device__ void flush_block(double *sf2, int nh, double *f2mat, unsigned long lo
     if (maxf > 0) atomicMax(&acc[VS_MAXF], static_cast<unsigned long long>(__double_as_longlong(maxf)));
     if (maxW > 0) atomicMax(&acc[VS_MAXW], static_cast<unsigned long long>(__double_as_longlong(maxW)));
   }
-  __syncthreads();
-  for (int i = threadIdx.x; i < nh; i += blockDim.x)
-    if (sf2[i] != 0.0) atomicAdd(&f2mat[i], sf2[i]);
 }
 
 // ---------------------------------------------------------------------------
@@ -1096,8 +1080,7 @@ __global__ void __launch_bounds__(128)
     } else {
       philox_point(seed, stream, static_cast<uint64_t>(e), dim, u);
     }
-    uint64_t pb, pbh;
-    vegas_map(xmat, bins, dim, u, x, pb, pbh);
+    vegas_map(xmat, bins, dim, u, x);
     double o[GRN_NUM_OBS];
     if (MAXD > 8 && is_nbody(A.P)) {
       NBEvent ev;
@@ -1151,22 +1134,18 @@ cudaError_t launch_hist_fill(const KArgs &a, const double *xmat, int bins, int d
 
 // Stage A of a VEGAS pass: Philox (or flow) points, grid map, tree-level kinematics and
 // cuts. Rejected and unscreened events are finished here; screened events that pass the
-// cuts go to the work list (index, VEGAS weight, bins, and the loop record or the mapped
-// point). Block `bid` of `nbid` blocks serving this pass; dsm: 2 * bins * dim doubles.
+// cuts go to the work list (index, VEGAS weight, and the loop record or the mapped
+// point). Block `bid` of `nbid` blocks serving this pass; dsm: bins * dim doubles (the grid).
 template <int MAXD>
 __device__ __forceinline__ void born_pass_body(
     const KArgs &A, const double *__restrict__ xmat, int bins, int dim, int64_t ncall,
     uint64_t seed, uint32_t stream, int track_max, double *__restrict__ f_out,
-    double *__restrict__ f2mat, unsigned long long *__restrict__ acc, int64_t *__restrict__ l_idx,
-    double *__restrict__ l_x, double *__restrict__ l_vw, uint64_t *__restrict__ l_bins,
-    uint64_t *__restrict__ l_bins_hi, int64_t cap, float *__restrict__ rf, double *__restrict__ rd,
+    unsigned long long *__restrict__ acc, int64_t *__restrict__ l_idx, double *__restrict__ l_x,
+    double *__restrict__ l_vw, int64_t cap, float *__restrict__ rf, double *__restrict__ rd,
     const float *__restrict__ fu, const float *__restrict__ flq, double *dsm, int bid, int nbid) {
-  double   *sx = dsm, *sf2 = dsm + bins * dim;
+  double   *sx = dsm;
   const int nh = bins * dim;
-  for (int i = threadIdx.x; i < nh; i += blockDim.x) {
-    sx[i]  = xmat[i];
-    sf2[i] = 0.0;
-  }
+  for (int i = threadIdx.x; i < nh; i += blockDim.x) sx[i] = xmat[i];
   __syncthreads();
   unsigned long long cnt[VS_COUNT] = {};
   double maxf = 0.0, maxW = 0.0;
@@ -1177,7 +1156,6 @@ __device__ __forceinline__ void born_pass_body(
     const bool active = e < ncall;
     bool       loop   = false;
     double     x[MAXD], vw = 0.0;
-    uint64_t   pb = 0ull, pbh = 0ull;
     Born       b;
     if (active) {
       double u[MAXD];
@@ -1186,7 +1164,7 @@ __device__ __forceinline__ void born_pass_body(
       } else {
         philox_point(seed, stream, static_cast<uint64_t>(e), dim, u);
       }
-      vw = vegas_map(sx, bins, dim, u, x, pb, pbh);
+      vw = vegas_map(sx, bins, dim, u, x);
       if (flq) vw *= exp(-static_cast<double>(flq[e]));
       double  W;
       uint8_t fl;
@@ -1198,7 +1176,6 @@ __device__ __forceinline__ void born_pass_body(
       if (!loop) {
         const double f = W * vw;
         f_out[e]       = f;
-        hist_add(sf2, dim, pb, pbh, f * f);
         cnt[VS_AMP_OK] += (fl & GRN_FLAG_AMPLITUDE_OK) ? 1 : 0;
         cnt[VS_NAN] += (fl & GRN_FLAG_AMPLITUDE_OK) ? 0 : 1;
         if (track_max) {
@@ -1211,8 +1188,6 @@ __device__ __forceinline__ void born_pass_body(
     if (loop && slot < cap) {
       l_idx[slot]  = e;
       l_vw[slot]   = vw;
-      l_bins[slot] = pb;
-      if (l_bins_hi) l_bins_hi[slot] = pbh;
       if (rf) {
         LoopEventF<float> le;
         double            a0r, a0i;
@@ -1224,22 +1199,20 @@ __device__ __forceinline__ void born_pass_body(
       }
     }
   }
-  flush_block(sf2, nh, f2mat, acc, cnt, maxf, maxW);
+  flush_counters(acc, cnt, maxf, maxW);
 }
 
 template <int MAXD>
 __global__ void __launch_bounds__(kVegasThreads)
     k_vegas_born(const KArgs A, const double *__restrict__ xmat, int bins, int dim, int64_t ncall,
                  uint64_t seed, uint32_t stream, int track_max, double *__restrict__ f_out,
-                 double *__restrict__ f2mat, unsigned long long *__restrict__ acc,
-                 int64_t *__restrict__ l_idx, double *__restrict__ l_x, double *__restrict__ l_vw,
-                 uint64_t *__restrict__ l_bins, uint64_t *__restrict__ l_bins_hi, int64_t cap,
+                 unsigned long long *__restrict__ acc, int64_t *__restrict__ l_idx,
+                 double *__restrict__ l_x, double *__restrict__ l_vw, int64_t cap,
                  float *__restrict__ rf, double *__restrict__ rd, const float *__restrict__ fu,
                  const float *__restrict__ flq) {
   extern __shared__ double dsm[];
-  born_pass_body<MAXD>(A, xmat, bins, dim, ncall, seed, stream, track_max, f_out, f2mat, acc,
-                       l_idx, l_x, l_vw, l_bins, l_bins_hi, cap, rf, rd, fu, flq, dsm, blockIdx.x,
-                       gridDim.x);
+  born_pass_body<MAXD>(A, xmat, bins, dim, ncall, seed, stream, track_max, f_out, acc, l_idx,
+                       l_x, l_vw, cap, rf, rd, fu, flq, dsm, blockIdx.x, gridDim.x);
 }
 
 // Stage B of a VEGAS pass: screened weights of the listed events. FP32 with r_list: the
@@ -1248,17 +1221,12 @@ __global__ void __launch_bounds__(kVegasThreads)
 template <typename T, int MAXD>
 __global__ void __launch_bounds__(kVegasThreads)
     k_vegas_loop(const KArgs A, int bins, int dim, int track_max, double *__restrict__ f_out,
-                 double *__restrict__ f2mat, unsigned long long *__restrict__ acc,
+                 unsigned long long *__restrict__ acc,
                  const int64_t *__restrict__ l_idx, const double *__restrict__ l_x,
-                 const double *__restrict__ l_vw, const uint64_t *__restrict__ l_bins,
-                 const uint64_t *__restrict__ l_bins_hi, int64_t cap, int64_t *__restrict__ r_list,
+                 const double *__restrict__ l_vw, int64_t cap, int64_t *__restrict__ r_list,
                  const int64_t *__restrict__ sel) {
-  extern __shared__ double dsm[];
-  double *sf2 = dsm;
   __shared__ KtNode<T>  skt[kMaxLoopNodes];
   __shared__ PhiNode<T> sphi[kMaxLoopNodes];
-  const int nh = bins * dim;
-  for (int i = threadIdx.x; i < nh; i += blockDim.x) sf2[i] = 0.0;
   stage_nodes<T>(A, skt, sphi);
   __syncthreads();
   unsigned long long cnt[VS_COUNT] = {};
@@ -1282,7 +1250,6 @@ __global__ void __launch_bounds__(kVegasThreads)
     }
     const double f = W * l_vw[r];
     f_out[l_idx[r]] = f;
-    hist_add(sf2, dim, l_bins[r], l_bins_hi ? l_bins_hi[r] : 0ull, f * f);
     cnt[VS_AMP_OK] += (fl & GRN_FLAG_AMPLITUDE_OK) ? 1 : 0;
     cnt[VS_NAN] += (fl & GRN_FLAG_AMPLITUDE_OK) ? 0 : 1;
     if (track_max) {
@@ -1292,22 +1259,17 @@ __global__ void __launch_bounds__(kVegasThreads)
   }
   // all lanes of a warp reach the flush together (the loop above has no barrier)
   __syncwarp();
-  flush_block(sf2, nh, f2mat, acc, cnt, maxf, maxW);
+  flush_counters(acc, cnt, maxf, maxW);
 }
 
 // Stage B, record mode: FP32 loop of the listed events from their records.
 __global__ void __launch_bounds__(kVegasThreads, GRN_LOOP_MIN_BLOCKS)
     k_vegas_loop_rec(const KArgs A, int bins, int dim, int track_max, double *__restrict__ f_out,
-                     double *__restrict__ f2mat, unsigned long long *__restrict__ acc,
+                     unsigned long long *__restrict__ acc,
                      const int64_t *__restrict__ l_idx, const double *__restrict__ l_vw,
-                     const uint64_t *__restrict__ l_bins, const uint64_t *__restrict__ l_bins_hi,
                      const float *__restrict__ rf, const double *__restrict__ rd, int64_t cap) {
-  extern __shared__ double dsm[];
-  double *sf2 = dsm;
   __shared__ KtNode<float>  skt[kMaxLoopNodes];
   __shared__ PhiNode<float> sphi[kMaxLoopNodes];
-  const int nh = bins * dim;
-  for (int i = threadIdx.x; i < nh; i += blockDim.x) sf2[i] = 0.0;
   stage_nodes<float>(A, skt, sphi);
   __syncthreads();
   LoopEventF<float> e;
@@ -1324,7 +1286,6 @@ __global__ void __launch_bounds__(kVegasThreads, GRN_LOOP_MIN_BLOCKS)
     const double W = record_weight(A, e, a0r, a0i, jac, skt, sphi, fl);
     const double f = W * l_vw[r];
     f_out[l_idx[r]] = f;
-    hist_add(sf2, dim, l_bins[r], l_bins_hi ? l_bins_hi[r] : 0ull, f * f);
     cnt[VS_AMP_OK] += (fl & GRN_FLAG_AMPLITUDE_OK) ? 1 : 0;
     cnt[VS_NAN] += (fl & GRN_FLAG_AMPLITUDE_OK) ? 0 : 1;
     if (track_max) {
@@ -1333,7 +1294,7 @@ __global__ void __launch_bounds__(kVegasThreads, GRN_LOOP_MIN_BLOCKS)
     }
   }
   __syncwarp();
-  flush_block(sf2, nh, f2mat, acc, cnt, maxf, maxW);
+  flush_counters(acc, cnt, maxf, maxW);
 }
 
 // Stage B, record mode, two events per thread on the packed FP32x2 loop (MINB as for
@@ -1341,16 +1302,11 @@ __global__ void __launch_bounds__(kVegasThreads, GRN_LOOP_MIN_BLOCKS)
 template <int MINB>
 __global__ void __launch_bounds__(kVegasThreads, MINB)
     k_vegas_loop_rec2(const KArgs A, int bins, int dim, int track_max, double *__restrict__ f_out,
-                      double *__restrict__ f2mat, unsigned long long *__restrict__ acc,
+                      unsigned long long *__restrict__ acc,
                       const int64_t *__restrict__ l_idx, const double *__restrict__ l_vw,
-                      const uint64_t *__restrict__ l_bins, const uint64_t *__restrict__ l_bins_hi,
                       const float *__restrict__ rf, const double *__restrict__ rd, int64_t cap) {
-  extern __shared__ double dsm[];
-  double *sf2 = dsm;
   __shared__ KtNode2  skt[kMaxLoopNodes];
   __shared__ PhiNode2 sphi[kMaxLoopNodes];
-  const int nh = bins * dim;
-  for (int i = threadIdx.x; i < nh; i += blockDim.x) sf2[i] = 0.0;
   stage_nodes2(A, skt, sphi);
   __syncthreads();
   LoopEventF<float> c;
@@ -1369,7 +1325,6 @@ __global__ void __launch_bounds__(kVegasThreads, MINB)
       const int64_t r = k ? rb : ra;
       const double  f = W[k] * l_vw[r];
       f_out[l_idx[r]] = f;
-      hist_add(sf2, dim, l_bins[r], l_bins_hi ? l_bins_hi[r] : 0ull, f * f);
       cnt[VS_AMP_OK] += (F[k] & GRN_FLAG_AMPLITUDE_OK) ? 1 : 0;
       cnt[VS_NAN] += (F[k] & GRN_FLAG_AMPLITUDE_OK) ? 0 : 1;
       if (track_max) {
@@ -1379,42 +1334,35 @@ __global__ void __launch_bounds__(kVegasThreads, MINB)
     }
   }
   __syncwarp();
-  flush_block(sf2, nh, f2mat, acc, cnt, maxf, maxW);
+  flush_counters(acc, cnt, maxf, maxW);
 }
 
-// Resident blocks per SM of the record-mode loop kernels (one or two events per thread),
-// for the f^2 histogram of an 8-dimensional process with the largest bin count.
-constexpr size_t kHistBytes8 = kMaxBins * 8 * sizeof(double);
+// Resident blocks per SM of the record-mode loop kernels (one or two events per thread).
 int loop_rec_blocks_per_sm(int pair) {
   int per = 0;
   if (pair == 2)
-    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, k_vegas_loop_rec2<3>, kVegasThreads,
-                                                  kHistBytes8);
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, k_vegas_loop_rec2<3>, kVegasThreads, 0);
   else if (pair)
-    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, k_vegas_loop_rec2<2>, kVegasThreads,
-                                                  kHistBytes8);
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, k_vegas_loop_rec2<2>, kVegasThreads, 0);
   else
-    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, k_vegas_loop_rec, kVegasThreads,
-                                                  kHistBytes8);
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, k_vegas_loop_rec, kVegasThreads, 0);
   return per < 1 ? 1 : per;
 }
 
 int vegas_grid_blocks(int device) {
   int sms = 0, per = 0;
   cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, device);
-  cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, k_vegas_loop_rec, kVegasThreads,
-                                                kHistBytes8);
+  cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, k_vegas_loop_rec, kVegasThreads, 0);
   if (per < 1) per = 1;
   return sms * per;
 }
 
 cudaError_t launch_vegas_born(const KArgs &a, const double *xmat, int bins, int dim, int64_t ncall,
                               uint64_t seed, uint32_t stream, int track_max, double *f_out,
-                              double *f2mat, unsigned long long *acc, int64_t *l_idx, double *l_x,
-                              double *l_vw, uint64_t *l_bins, uint64_t *l_bins_hi, float *rf,
-                              double *rd, cudaStream_t st, const float *fu, const float *flq) {
+                              unsigned long long *acc, int64_t *l_idx, double *l_x, double *l_vw,
+                              float *rf, double *rd, cudaStream_t st, const float *fu,
+                              const float *flq) {
   const int nh = bins * dim;
-  cudaMemsetAsync(f2mat, 0, nh * sizeof(double), st);
   cudaMemsetAsync(acc, 0, kAccSlots * sizeof(unsigned long long), st);
   int sms = 0, dev = 0;
   cudaGetDevice(&dev);
@@ -1422,61 +1370,167 @@ cudaError_t launch_vegas_born(const KArgs &a, const double *xmat, int bins, int 
   const int64_t want = (ncall + kVegasThreads - 1) / kVegasThreads;
   const int     ba   = static_cast<int>(std::min<int64_t>(want, static_cast<int64_t>(sms) * 16));
   if (dim <= 8)
-    k_vegas_born<8><<<ba, kVegasThreads, 2 * nh * sizeof(double), st>>>(
-        a, xmat, bins, dim, ncall, seed, stream, track_max, f_out, f2mat, acc, l_idx, l_x, l_vw,
-        l_bins, l_bins_hi, ncall, rf, rd, fu, flq);
+    k_vegas_born<8><<<ba, kVegasThreads, nh * sizeof(double), st>>>(
+        a, xmat, bins, dim, ncall, seed, stream, track_max, f_out, acc, l_idx, l_x, l_vw, ncall,
+        rf, rd, fu, flq);
   else
-    k_vegas_born<kMaxDim><<<ba, kVegasThreads, 2 * nh * sizeof(double), st>>>(
-        a, xmat, bins, dim, ncall, seed, stream, track_max, f_out, f2mat, acc, l_idx, l_x, l_vw,
-        l_bins, l_bins_hi, ncall, rf, rd, fu, flq);
+    k_vegas_born<kMaxDim><<<ba, kVegasThreads, nh * sizeof(double), st>>>(
+        a, xmat, bins, dim, ncall, seed, stream, track_max, f_out, acc, l_idx, l_x, l_vw, ncall,
+        rf, rd, fu, flq);
   return cudaGetLastError();
 }
 
 cudaError_t launch_vegas_loop(const KArgs &a, int prec, int bins, int dim, int64_t ncall,
-                              int track_max, double *f_out, double *f2mat, unsigned long long *acc,
+                              int track_max, double *f_out, unsigned long long *acc,
                               const int64_t *l_idx, const double *l_x, const double *l_vw,
-                              const uint64_t *l_bins, const uint64_t *l_bins_hi, const float *rf,
-                              const double *rd, int64_t *r_list, int nblocks, cudaStream_t st) {
+                              const float *rf, const double *rd, int64_t *r_list, int nblocks,
+                              cudaStream_t st) {
   if (!a.P.screening) return cudaSuccess;
-  const int nh = bins * dim;
   if (rf) {
     if (a.loop_pair == 2)
-      k_vegas_loop_rec2<3><<<nblocks, kVegasThreads, nh * sizeof(double), st>>>(
-          a, bins, dim, track_max, f_out, f2mat, acc, l_idx, l_vw, l_bins, l_bins_hi, rf, rd,
-          ncall);
+      k_vegas_loop_rec2<3><<<nblocks, kVegasThreads, 0, st>>>(a, bins, dim, track_max, f_out, acc,
+                                                             l_idx, l_vw, rf, rd, ncall);
     else if (a.loop_pair)
-      k_vegas_loop_rec2<2><<<nblocks, kVegasThreads, nh * sizeof(double), st>>>(
-          a, bins, dim, track_max, f_out, f2mat, acc, l_idx, l_vw, l_bins, l_bins_hi, rf, rd,
-          ncall);
+      k_vegas_loop_rec2<2><<<nblocks, kVegasThreads, 0, st>>>(a, bins, dim, track_max, f_out, acc,
+                                                             l_idx, l_vw, rf, rd, ncall);
     else
-      k_vegas_loop_rec<<<nblocks, kVegasThreads, nh * sizeof(double), st>>>(
-          a, bins, dim, track_max, f_out, f2mat, acc, l_idx, l_vw, l_bins, l_bins_hi, rf, rd,
-          ncall);
+      k_vegas_loop_rec<<<nblocks, kVegasThreads, 0, st>>>(a, bins, dim, track_max, f_out, acc,
+                                                         l_idx, l_vw, rf, rd, ncall);
     return cudaGetLastError();
   }
-  const size_t sm = nh * sizeof(double);
-  int64_t     *rl = (prec == GRN_PREC_MIXED && a.refine_tol > 0.0) ? r_list : nullptr;
+  int64_t *rl = (prec == GRN_PREC_MIXED && a.refine_tol > 0.0) ? r_list : nullptr;
   // MIXED: FP32 pass, then the FP64 pass over the refinement list (when refining)
   if (dim <= 8) {
     if (prec == GRN_PREC_MIXED)
-      k_vegas_loop<float, 8><<<nblocks, kVegasThreads, sm, st>>>(
-          a, bins, dim, track_max, f_out, f2mat, acc, l_idx, l_x, l_vw, l_bins, l_bins_hi, ncall,
-          rl, nullptr);
+      k_vegas_loop<float, 8><<<nblocks, kVegasThreads, 0, st>>>(
+          a, bins, dim, track_max, f_out, acc, l_idx, l_x, l_vw, ncall, rl, nullptr);
     if (prec != GRN_PREC_MIXED || rl)
-      k_vegas_loop<double, 8><<<nblocks, kVegasThreads, sm, st>>>(
-          a, bins, dim, track_max, f_out, f2mat, acc, l_idx, l_x, l_vw, l_bins, l_bins_hi, ncall,
-          nullptr, rl);
+      k_vegas_loop<double, 8><<<nblocks, kVegasThreads, 0, st>>>(
+          a, bins, dim, track_max, f_out, acc, l_idx, l_x, l_vw, ncall, nullptr, rl);
   } else {
     if (prec == GRN_PREC_MIXED)
-      k_vegas_loop<float, kMaxDim><<<nblocks, kVegasThreads, sm, st>>>(
-          a, bins, dim, track_max, f_out, f2mat, acc, l_idx, l_x, l_vw, l_bins, l_bins_hi, ncall,
-          rl, nullptr);
+      k_vegas_loop<float, kMaxDim><<<nblocks, kVegasThreads, 0, st>>>(
+          a, bins, dim, track_max, f_out, acc, l_idx, l_x, l_vw, ncall, rl, nullptr);
     if (prec != GRN_PREC_MIXED || rl)
-      k_vegas_loop<double, kMaxDim><<<nblocks, kVegasThreads, sm, st>>>(
-          a, bins, dim, track_max, f_out, f2mat, acc, l_idx, l_x, l_vw, l_bins, l_bins_hi, ncall,
-          nullptr, rl);
+      k_vegas_loop<double, kMaxDim><<<nblocks, kVegasThreads, 0, st>>>(
+          a, bins, dim, track_max, f_out, acc, l_idx, l_x, l_vw, ncall, nullptr, rl);
   }
   return cudaGetLastError();
+}
+
+// ---------------------------------------------------------------------------
+// The f^2 histogram of a pass (the importance data of the grid refinement; the reference
+// fills it under its global mutex, src/MGraniitti.cc:1404-1411), in a fixed order so that
+// the same f array gives the same histogram bit for bit. Block b of kHistBlocks takes the
+// point range [b chunk, (b + 1) chunk); warp w of it the 32-point groups w, w + 4, ... of
+// that range. In a group, the points with f != 0 are added in lane order: lane j adds the
+// point's f^2 to column j (dimension j) of the warp's private histogram, so no two lanes
+// touch the same entry. The block's warp histograms are summed in warp order into its
+// partial; k_vegas_hist_sum adds the partials in block order. No atomics anywhere.
+
+constexpr int kHistThreads = 128, kHistWarps = kHistThreads / 32;
+
+__device__ void vegas_hist_body(int bins, int dim, int64_t ncall, uint64_t seed,
+                                uint32_t stream, const float *__restrict__ fu,
+                                const double *__restrict__ f, double *__restrict__ part,
+                                double *sh) {
+  const int nh = bins * dim;
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  double   *hw = sh + warp * nh;
+  for (int i = threadIdx.x; i < kHistWarps * nh; i += blockDim.x) sh[i] = 0.0;
+  __syncthreads();
+  const int64_t chunk = ((ncall + gridDim.x - 1) / gridDim.x + 31) / 32 * 32;
+  const int64_t a = static_cast<int64_t>(blockIdx.x) * chunk, b = min(ncall, a + chunk);
+  const double  dbins = static_cast<double>(bins);
+  for (int64_t g0 = a + 32 * warp; g0 < b; g0 += kHistThreads) {
+    const int64_t e  = g0 + lane;
+    double        f2 = 0.0;
+    if (e < b) {
+      const double fe = f[e];
+      f2              = fe * fe;
+    }
+    uint64_t lo = 0ull, hi = 0ull;  // bins of dimensions 0..7 and 8..15, one byte each
+    if (f2 != 0.0) {
+      double u[kMaxDim];
+      if (fu) {
+        for (int j = 0; j < dim; ++j) u[j] = fu[static_cast<int64_t>(j) * ncall + e];
+      } else {
+        philox_point(seed, stream, static_cast<uint64_t>(e), dim, u);
+      }
+      for (int j = 0; j < dim; ++j) {
+        const uint64_t k = static_cast<uint64_t>(vegas_bin(u[j], dbins, bins));
+        if (j < 8)
+          lo |= k << (8 * j);
+        else
+          hi |= k << (8 * (j - 8));
+      }
+    }
+    unsigned m = __ballot_sync(0xffffffffu, f2 != 0.0);
+    while (m) {
+      const int src = __ffs(m) - 1;
+      m &= m - 1;
+      const double   v  = __shfl_sync(0xffffffffu, f2, src);
+      const uint64_t pl = __shfl_sync(0xffffffffu, lo, src);
+      const uint64_t ph = __shfl_sync(0xffffffffu, hi, src);
+      if (lane < dim) {
+        const int k = static_cast<int>(((lane < 8 ? pl : ph) >> (8 * (lane & 7))) & 0xFFu);
+        hw[k * dim + lane] += v;
+      }
+    }
+  }
+  __syncthreads();
+  for (int i = threadIdx.x; i < nh; i += blockDim.x) {
+    double s = 0.0;
+    for (int w = 0; w < kHistWarps; ++w) s += sh[w * nh + i];
+    part[static_cast<int64_t>(blockIdx.x) * nh + i] = s;
+  }
+}
+
+__global__ void __launch_bounds__(kHistThreads)
+    k_vegas_hist(int bins, int dim, int64_t ncall, uint64_t seed, uint32_t stream,
+                 const float *__restrict__ fu, const double *__restrict__ f,
+                 double *__restrict__ part) {
+  extern __shared__ double dsm[];
+  vegas_hist_body(bins, dim, ncall, seed, stream, fu, f, part, dsm);
+}
+
+// f2mat[i] = sum over blocks b = 0, 1, ... of part[b][i]: thread (tx, ty) of a 32 x 8 block
+// sums the blocks ty, ty + 8, ... of entry i = 32 blockIdx.x + tx, then the 8 sums are added
+// in ty order.
+__global__ void __launch_bounds__(256)
+    k_vegas_hist_sum(const double *__restrict__ part, int nparts, int nh,
+                     double *__restrict__ f2mat) {
+  __shared__ double red[8][33];
+  const int tx = threadIdx.x & 31, ty = threadIdx.x >> 5;
+  const int i  = 32 * blockIdx.x + tx;
+  double    s  = 0.0;
+  if (i < nh)
+    for (int b = ty; b < nparts; b += 8) s += part[static_cast<int64_t>(b) * nh + i];
+  red[ty][tx] = s;
+  __syncthreads();
+  if (ty == 0 && i < nh) {
+    double t = 0.0;
+    for (int k = 0; k < 8; ++k) t += red[k][tx];
+    f2mat[i] = t;
+  }
+}
+
+size_t vegas_hist_smem(int nh) { return static_cast<size_t>(kHistWarps) * nh * sizeof(double); }
+
+cudaError_t launch_vegas_hist_sum(const double *part, int nh, double *f2mat, cudaStream_t st) {
+  k_vegas_hist_sum<<<(nh + 31) / 32, 256, 0, st>>>(part, kHistBlocks, nh, f2mat);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_vegas_hist(int bins, int dim, int64_t ncall, uint64_t seed, uint32_t stream,
+                              const float *fu, const double *f, double *part, double *f2mat,
+                              cudaStream_t st) {
+  const int nh = bins * dim;
+  k_vegas_hist<<<kHistBlocks, kHistThreads, vegas_hist_smem(nh), st>>>(bins, dim, ncall, seed,
+                                                                       stream, fu, f, part);
+  const cudaError_t ce = cudaGetLastError();
+  if (ce != cudaSuccess) return ce;
+  return launch_vegas_hist_sum(part, nh, f2mat, st);
 }
 
 // ---------------------------------------------------------------------------
@@ -1497,14 +1551,14 @@ __global__ void __launch_bounds__(kVegasThreads, 3) k_batch_born(int np) {
   while (p + 1 < np && static_cast<int>(blockIdx.x) >= c_procs[p].blk1) ++p;
   const BatchProc &q = c_procs[p];
   born_pass_body<MAXD>(q.A, q.xmat, q.bins, q.dim, q.ncall, q.seed, q.stream, q.track_max,
-                       q.f_out, q.f2mat, q.acc, q.l_idx, q.l_x, q.l_vw, q.l_bins, q.l_bins_hi,
-                       q.ncall, q.rf, q.rd, q.fu, q.flq, dsm,
+                       q.f_out, q.acc, q.l_idx, q.l_x, q.l_vw, q.ncall, q.rf, q.rd, q.fu,
+                       q.flq, dsm,
                        static_cast<int>(blockIdx.x) - q.blk0, q.blk1 - q.blk0);
 }
 
 cudaError_t launch_batch_born(int np, int nblocks, int max_dim, int max_nh, cudaStream_t st) {
-  // shared memory: grid and f^2 histogram of the largest process (bins * dim each)
-  const size_t sm = 2 * static_cast<size_t>(max_nh) * sizeof(double);
+  // shared memory: the grid of the largest process (bins * dim)
+  const size_t sm = static_cast<size_t>(max_nh) * sizeof(double);
   if (max_dim <= 8)
     k_batch_born<8><<<nblocks, kVegasThreads, sm, st>>>(np);
   else
@@ -1521,8 +1575,6 @@ constexpr int kBatchChunk = kVegasThreads;  // work units per grab (one per thre
 template <bool REC>
 __global__ void __launch_bounds__(kVegasThreads, 2)
     k_batch_loop(int np, unsigned long long *__restrict__ counter) {
-  extern __shared__ double dsm[];
-  double *sf2 = dsm;
   using KT = typename std::conditional<REC, KtNode2, KtNode<float>>::type;
   using PT = typename std::conditional<REC, PhiNode2, PhiNode<float>>::type;
   __shared__ KT                 skt[kMaxLoopNodes];
@@ -1545,7 +1597,7 @@ __global__ void __launch_bounds__(kVegasThreads, 2)
   }
   __syncthreads();
   const int64_t total = s_begin[np];
-  int           cur = -1, nh = 0;
+  int           cur = -1;
   LoopEventF<float> c;
   unsigned long long cnt[VS_COUNT] = {};
   double maxf = 0.0, maxW = 0.0;
@@ -1559,16 +1611,13 @@ __global__ void __launch_bounds__(kVegasThreads, 2)
     while (p + 1 < np && chunk >= s_begin[p + 1]) ++p;
     if (p != cur) {  // block-uniform: flush the previous process, stage this one
       if (cur >= 0) {
-        const BatchProc &o = c_procs[cur];
-        flush_block(sf2, nh, o.f2mat, o.acc, cnt, maxf, maxW);
+        flush_counters(c_procs[cur].acc, cnt, maxf, maxW);
         for (int k = 0; k < VS_COUNT; ++k) cnt[k] = 0;
         maxf = maxW = 0.0;
       }
       cur = p;
       const BatchProc &q = c_procs[p];
-      nh = q.bins * q.dim;
       __syncthreads();
-      for (int i = threadIdx.x; i < nh; i += blockDim.x) sf2[i] = 0.0;
       if constexpr (REC) {
         stage_nodes2(q.A, skt, sphi);
         make_loop_consts_fast<float>(q.A.P, q.A.K, c);
@@ -1589,7 +1638,6 @@ __global__ void __launch_bounds__(kVegasThreads, 2)
           const int64_t r = k ? rb : ra;
           const double  f = W[k] * q.l_vw[r];
           q.f_out[q.l_idx[r]] = f;
-          hist_add(sf2, q.dim, q.l_bins[r], q.l_bins_hi ? q.l_bins_hi[r] : 0ull, f * f);
           cnt[VS_AMP_OK] += (F[k] & GRN_FLAG_AMPLITUDE_OK) ? 1 : 0;
           cnt[VS_NAN] += (F[k] & GRN_FLAG_AMPLITUDE_OK) ? 0 : 1;
           if (q.track_max) {
@@ -1606,7 +1654,6 @@ __global__ void __launch_bounds__(kVegasThreads, 2)
       const double W = screened_weight<float, true>(q.A, x, fl, skt, sphi);
       const double f = W * q.l_vw[unit];
       q.f_out[q.l_idx[unit]] = f;
-      hist_add(sf2, q.dim, q.l_bins[unit], q.l_bins_hi ? q.l_bins_hi[unit] : 0ull, f * f);
       cnt[VS_AMP_OK] += (fl & GRN_FLAG_AMPLITUDE_OK) ? 1 : 0;
       cnt[VS_NAN] += (fl & GRN_FLAG_AMPLITUDE_OK) ? 0 : 1;
       if (q.track_max) {
@@ -1615,25 +1662,48 @@ __global__ void __launch_bounds__(kVegasThreads, 2)
       }
     }
   }
-  if (cur >= 0) {
-    const BatchProc &o = c_procs[cur];
-    flush_block(sf2, nh, o.f2mat, o.acc, cnt, maxf, maxW);
-  }
+  if (cur >= 0) flush_counters(c_procs[cur].acc, cnt, maxf, maxW);
 }
 
 int batch_loop_blocks(int device, int max_nh) {
   int sms = 0, per = 0;
   cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, device);
-  cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, k_batch_loop<true>, kVegasThreads,
-                                                max_nh * sizeof(double));
+  cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, k_batch_loop<true>, kVegasThreads, 0);
   return sms * (per < 1 ? 1 : per);
 }
 
 cudaError_t launch_batch_loop(int np, unsigned long long *counter, int nblocks, int max_nh,
                               cudaStream_t st) {
-  k_batch_loop<true><<<nblocks, kVegasThreads, max_nh * sizeof(double), st>>>(np, counter);
+  k_batch_loop<true><<<nblocks, kVegasThreads, 0, st>>>(np, counter);
   return cudaGetLastError();
 }
+
+// The f^2 histogram of batch member p (its pass's stream id and flow points come from the
+// process table, as in stage A), then the fixed-order sum of its partials into f2mat.
+__global__ void __launch_bounds__(kHistThreads) k_batch_hist(int p) {
+  extern __shared__ double dsm[];
+  const BatchProc &q = c_procs[p];
+  vegas_hist_body(q.bins, q.dim, q.ncall, q.seed, q.stream, q.fu, q.f_out, q.hpart, dsm);
+}
+
+cudaError_t launch_batch_hist(int p, int bins, int dim, const double *part, double *f2mat,
+                              cudaStream_t st) {
+  const int nh = bins * dim;
+  k_batch_hist<<<kHistBlocks, kHistThreads, vegas_hist_smem(nh), st>>>(p);
+  const cudaError_t ce = cudaGetLastError();
+  if (ce != cudaSuccess) return ce;
+  return launch_vegas_hist_sum(part, nh, f2mat, st);
+}
+
+cudaError_t vegas_hist_prepare() {
+  const int most = static_cast<int>(vegas_hist_smem(kMaxBins * kMaxDim));
+  cudaError_t ce = cudaFuncSetAttribute(k_vegas_hist, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                        most);
+  if (ce != cudaSuccess) return ce;
+  return cudaFuncSetAttribute(k_batch_hist, cudaFuncAttributeMaxDynamicSharedMemorySize, most);
+}
+
+
 
 // Deterministic sums of f and f^2 (fixed chunks, fixed tree order), then the
 // counters of the pass into the scalar record sc[VS_COUNT].

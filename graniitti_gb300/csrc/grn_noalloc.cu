@@ -37,7 +37,8 @@ void         *g_scratch_addr[kMaxDevices] = {};
 
 // Device address of the scratch on the current device, looked up once per
 // device (the first call on a device does this set-up; it should come before any
-// stream capture).
+// stream capture). The address stays valid for the life of the device's primary
+// context: the library must not be used across a cudaDeviceReset.
 cudaError_t scratch_address(int device, void **addr) {
   if (device < 0 || device >= kMaxDevices) return cudaErrorInvalidDevice;
   std::lock_guard<std::mutex> lock(g_setup_mutex);
@@ -51,13 +52,16 @@ cudaError_t scratch_address(int device, void **addr) {
   return cudaSuccess;
 }
 
-bool on_device(const void *ptr) {
+// A device (or managed) pointer of `device` itself: memory of another GPU would be read
+// through peer addressing that nothing here enables.
+bool on_device(const void *ptr, int device) {
   cudaPointerAttributes a;
   if (cudaPointerGetAttributes(&a, ptr) != cudaSuccess) {
     cudaGetLastError();
     return false;
   }
-  return a.type == cudaMemoryTypeDevice || a.type == cudaMemoryTypeManaged;
+  if (a.type == cudaMemoryTypeManaged) return true;
+  return a.type == cudaMemoryTypeDevice && a.device == device;
 }
 
 }  // namespace
@@ -78,7 +82,9 @@ extern "C" grn_status grn_event_weights_noalloc(grn_engine *e, const double *u, 
   const grn_status st = grn::engine_noalloc_view(e, &args, &device, &stream, &loop_blocks, &edim);
   if (st != GRN_OK) return st;
   if (!u || !w_out) return grn::set_error(GRN_ERR_INVALID, "null argument");
-  if (dim != edim) return grn::set_error(GRN_ERR_INVALID, "dim must equal grn_dim() = 8");
+  if (dim != edim)
+    return grn::set_error(GRN_ERR_INVALID, ("grn_event_weights_noalloc: dim must equal "
+                                            "grn_dim() = " + std::to_string(edim)).c_str());
   if (prec != GRN_PREC_FP64 && prec != GRN_PREC_MIXED)
     return grn::set_error(GRN_ERR_INVALID, "bad prec");
   if (n < 0 || n > GRN_NOALLOC_MAX_POINTS)
@@ -88,10 +94,10 @@ extern "C" grn_status grn_event_weights_noalloc(grn_engine *e, const double *u, 
   if (n == 0) return GRN_OK;
   cudaError_t ce = cudaSetDevice(device);
   if (ce != cudaSuccess) return grn::set_error(GRN_ERR_CUDA, cudaGetErrorString(ce));
-  if (!on_device(u) || !on_device(w_out) || (flags && !on_device(flags)))
+  if (!on_device(u, device) || !on_device(w_out, device) || (flags && !on_device(flags, device)))
     return grn::set_error(GRN_ERR_INVALID,
                           "grn_event_weights_noalloc: u, w_out and flags must be device "
-                          "pointers (host staging would allocate)");
+                          "pointers on the engine's device (host staging would allocate)");
   void *base = nullptr;
   ce = scratch_address(device, &base);
   if (ce != cudaSuccess)
@@ -101,7 +107,11 @@ extern "C" grn_status grn_event_weights_noalloc(grn_engine *e, const double *u, 
   auto *list  = reinterpret_cast<int64_t *>(static_cast<unsigned char *>(base) + kCounterSlot);
   auto *rlist = reinterpret_cast<int64_t *>(static_cast<unsigned char *>(base) + kCounterSlot +
                                             kListBytes);
-  // launch_event_weights clears both counters (cudaMemsetAsync) before stage A.
+  // launch_event_weights clears both counters (cudaMemsetAsync) before stage A. It is the
+  // generic two-stage path (FP32 loop with FP64 refinement in MIXED) for every process;
+  // grn_event_weights takes the record-mode loop for screened single-trajectory Regge
+  // processes in MIXED, so there the two agree to the FP32-loop tolerance (1e-5), and
+  // exactly in FP64.
   ce = grn::launch_event_weights(args, prec, u, n, dim, w_out, flags, list, rlist, count,
                                  loop_blocks, stream);
   if (ce != cudaSuccess) return grn::set_error(GRN_ERR_CUDA, cudaGetErrorString(ce));

@@ -282,7 +282,13 @@ grn_status grn_event_weights(grn_engine *e, const double *u, int64_t n, int32_t 
  *     make that first call before any stream capture.
  *   - All calls on a device share the one scratch array: calls that overlap on the
  *     GPU (two engines on different streams, concurrently) race; serialise them.
- * Same results as grn_event_weights. */
+ *   - The scratch address is kept for the life of the device's primary context: do
+ *     not use the library across a cudaDeviceReset.
+ *   - dim must equal grn_dim(e) (8 for 2-body states, 14 for cascades and 4-body).
+ * Results: identical to grn_event_weights in FP64. In MIXED this call runs the generic
+ * FP32 kt-loop with FP64 refinement for every process, while grn_event_weights takes
+ * the record-mode loop for screened single-trajectory Regge processes: there the two
+ * agree to the FP32-loop tolerance (1e-5 relative), elsewhere exactly. */
 #define GRN_NOALLOC_MAX_POINTS 1048576
 grn_status grn_event_weights_noalloc(grn_engine *e, const double *u, int64_t n, int32_t dim,
                                      double *w_out, uint8_t *flags, int32_t prec);

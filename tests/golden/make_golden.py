@@ -8,7 +8,7 @@ reference does not. Steps:
   3. build the eikonal tables with the reference's MEikonal::S3Constructor
   4. run the reference VEGAS integration for the cross section
 
-Usage: python tests/golden/make_golden.py [--ref /root/reference]
+Usage: python tests/golden/make_golden.py [--ref <reference source tree>]
                                           [--only resonances|cascades|rescon|regge_res]
 """
 import argparse
@@ -16,6 +16,7 @@ import json
 import os
 import subprocess
 import sys
+import tempfile
 
 import numpy as np
 
@@ -28,7 +29,11 @@ REF_BIN = os.path.join(REPO, "oracle", "_ref", "bin", "grn_ref")
 CARD = os.path.join(HERE, "cards", "pp_con_pipi.json")
 CARD_SCR = os.path.join(HERE, "cards", "pp_con_pipi_screened.json")
 PROC = "PP[CON]<C> -> pi+ pi-"
-TMP = os.path.join(REPO, "_work", "golden_tmp")
+# point and weight files exchanged with the reference driver (a fresh temporary folder)
+TMP = tempfile.mkdtemp(prefix="grn_golden_")
+# the reference source tree: $GRANIITTI_REFERENCE, else a "reference" folder beside the repo
+REF_DEFAULT = os.environ.get("GRANIITTI_REFERENCE",
+                             os.path.join(os.path.dirname(REPO), "reference"))
 
 
 def run_weights(card, u, extra=(), proc=PROC, dim=None, leaves=0):
@@ -302,7 +307,7 @@ def cascade_fixtures():
 
 def main():
     ap = argparse.ArgumentParser()
-    ap.add_argument("--ref", default="/root/reference")
+    ap.add_argument("--ref", default=REF_DEFAULT)
     ap.add_argument("--only", choices=["all", "resonances", "cascades", "rescon", "regge_res",
                                        "nbody", "nbody_c", "veto"],
                     default="all")

@@ -123,6 +123,20 @@ def test_batched_mixed_multiplicity_equals_separate(gpu):
         assert r1.maxf == pytest.approx(r0.maxf, rel=1e-14)
     print("batched 2-body + 4-body pass: %.2f ms; I = %s" % (ms, [r.I_this for r in res]))
     b.close()
+    # a refined pass: the batched graph builds each member's f^2 histogram in the same fixed
+    # order as the engine alone, so the refined grids are equal bit for bit
+    for e, x in zip(es, grids):
+        e.vegas_set_grid(x)
+    sep = [e.vegas_iteration(mode=1, refine=True, iter_id=10) for e in es]
+    new_sep = [e.vegas_grid() for e in es]
+    for e, x in zip(es, grids):
+        e.vegas_set_grid(x)
+    b = g.Batch(es)
+    res, _ = b.iteration(mode=1, refine=True, iter_id=10)
+    b.close()
+    for e, x, r0, r1 in zip(es, new_sep, sep, res):
+        assert np.array_equal(e.vegas_grid(), x)
+        assert r1.I_this == r0.I_this and r1.maxf == r0.maxf
     for e in es:
         e.close()
 
