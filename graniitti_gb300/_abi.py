@@ -101,7 +101,7 @@ class ProcessParams(ctypes.Structure):
                 ("n_decay", c_int32), ("central_spin", c_int32), ("width", c_double * 2),
                 ("m_daughter", c_double * 4),
                 ("spin_gen", c_int32), ("spin_dec", c_int32), ("spin_frame", c_int32),
-                ("_pad_spin", c_int32), ("omega", c_double),
+                ("offshell_user", c_int32), ("omega", c_double), ("offshell", c_double),
                 ("veto_active", c_int32), ("n_veto", c_int32),
                 ("veto_eta_min", c_double * GRN_MAX_VETO), ("veto_eta_max", c_double * GRN_MAX_VETO),
                 ("veto_pt_min", c_double * GRN_MAX_VETO), ("veto_pt_max", c_double * GRN_MAX_VETO)]

@@ -160,12 +160,10 @@ def build_params(card, process=None, tune=None):
     tree = decay_tree(proc.split("@")[0].split("->", 1)[1])
     casc = [kids for _, kids in tree]
     if any(casc):
-        # two-body cascades "a > {c d} b > {e f}" of both central particles (<F>)
+        # two-body cascades "a > {c d} b > {e f}" of both central particles (<C> and <F>)
         if not (all(len(k) == 2 and all(not g for _, g in k) for k in casc) and len(casc) == 2):
             raise UnsupportedProcess("decay trees: both central particles decay to two stable "
                                      "particles")
-        if cls != "F":
-            raise UnsupportedProcess("decay cascades are implemented in the <F> class")
         if channel == "RESTENSOR":
             raise UnsupportedProcess("RESTENSOR decays directly to two pseudoscalars")
     elif any(f in PARTICLES and PARTICLES[f][2] > 1e-6 for f in finals):
@@ -215,6 +213,12 @@ def build_params(card, process=None, tune=None):
     # identical-particle factor: product of the multiplicities' factorials (MProcess.cc:449-468)
     P.s_factor = float(np.prod([math.factorial(finals.count(f)) for f in sorted(set(finals))]))
     P.central_spin = 1 if vec else 0
+    # @OFFSHELL:x, widths of the cascades' Breit-Wigner mass draws (MProcess::SetOFFSHELL,
+    # src/MGraniitti.cc:588); the reference default (5) otherwise
+    for ident, _, args in split_commands(proc):
+        if ident == "OFFSHELL":
+            P.offshell_user = 1
+            P.offshell = float(args["_SINGLET_"])
     if any(casc):
         P.n_decay = 2
         for k, name in enumerate(finals):

@@ -298,9 +298,14 @@ grn_status derive_consts(const grn_process_params &P, grn::Consts &K) {
     return fail(GRN_ERR_UNSUPPORTED, "central particles of spin 0 or 1");
   if (rescon && (P.n_res < 0 || P.n_res > GRN_MAX_RESONANCES))
     return fail(GRN_ERR_INVALID, "RES+CONTENSOR takes 0 to 4 resonances");
+  // OFFSHELL: widths of the cascades' Breit-Wigner mass draws (the reference default 5 unless
+  // set by @OFFSHELL, MProcess::SetOFFSHELL); with 0 the central particles keep their pole
+  // masses and the decay coordinates follow the 8 of the 2-body point directly
+  K.offshell = P.offshell_user ? P.offshell : 5.0;
+  K.dec0     = K.offshell > 0.0 ? 10 : 8;
   if (P.n_decay == 2) {
-    if (P.phase_space != GRN_PS_FACTORIZED)
-      return fail(GRN_ERR_UNSUPPORTED, "decay cascades are implemented in the <F> class");
+    if (!(K.offshell >= 0.0 && K.offshell <= 1e3))
+      return fail(GRN_ERR_INVALID, "OFFSHELL must be in [0, 1000] widths");
     if (P.process == GRN_PROC_TENSOR_RES || rescon || rr)
       return fail(GRN_ERR_UNSUPPORTED, "RESTENSOR decays directly to two pseudoscalars");
     for (int k = 0; k < 4; ++k)
@@ -308,7 +313,8 @@ grn_status derive_consts(const grn_process_params &P, grn::Consts &K) {
         return fail(GRN_ERR_INVALID, "daughter masses must be non-negative");
     for (int k = 0; k < 2; ++k)
       if (!(P.width[k] >= 0) ||
-          !(P.m_central[k] + 5.0 * P.width[k] > P.m_daughter[2 * k] + P.m_daughter[2 * k + 1]))
+          !(P.m_central[k] + K.offshell * P.width[k] >
+            P.m_daughter[2 * k] + P.m_daughter[2 * k + 1]))
         return fail(GRN_ERR_INVALID, "central width, or decay kinematically closed");
   }
   if (P.process == GRN_PROC_TENSOR_CON && P.central_spin == 1) {
@@ -587,7 +593,9 @@ grn_status grn_create(const grn_process_params *p, int32_t device, grn_engine **
   e->device     = device;
   e->P          = *p;
   e->K          = K;
-  e->dim        = (p->n_decay == 2 || p->n_central == 4) ? 14 : 8;
+  // hypercube dimension: 8 for a 2-body point; cascades add the decay angles (4) and, unless
+  // OFFSHELL = 0, the two masses (2); 4-body central states have 14
+  e->dim = p->n_central == 4 ? 14 : (p->n_decay == 2 ? K.dec0 + 4 : 8);
   cudaError_t ce = cudaStreamCreateWithFlags(&e->stream, cudaStreamNonBlocking);
   if (ce == cudaSuccess) ce = cudaMallocHost(&e->h_sc, grn::VS_COUNT * sizeof(double));
   if (ce == cudaSuccess) ce = cudaEventCreate(&e->ev0);
@@ -1960,7 +1968,7 @@ grn_status grn_flow_create(grn_engine *e, const grn_flow_params *p, grn_flow **o
   if (p->bins != grn::flow::kBins || !(base || grn::flow_wide_supported(p->dim, p->hidden)))
     return fail(GRN_ERR_UNSUPPORTED,
                 "flow kernels are built for bins = 16 and (dim, hidden) = (8, 128), (8, 256), "
-                "(14, 128), (14, 256)");
+                "(12, 128), (12, 256), (14, 128), (14, 256)");
   if (p->layers < 1 || p->layers > grn::flow::kMaxLayers)
     return fail(GRN_ERR_INVALID, "flow layers must be in [1, 12]");
   if (!(p->mix_uniform >= 0.0 && p->mix_uniform < 1.0))

@@ -73,14 +73,23 @@ __constant__ int8_t cB14[6][7] = {{7, 8, 9, 10, 11, 12, 13},  {0, 1, 2, 3, 4, 5,
                                   {1, 3, 5, 7, 9, 11, 13},    {0, 2, 4, 6, 8, 10, 12},
                                   {2, 3, 6, 7, 10, 11, 13},   {0, 1, 4, 5, 8, 9, 12}};
 
+__constant__ int8_t cA12[6][6] = {{0, 1, 2, 3, 4, 5},        {6, 7, 8, 9, 10, 11},
+                                  {0, 2, 4, 6, 8, 10},       {1, 3, 5, 7, 9, 11},
+                                  {0, 1, 4, 5, 8, 9},        {2, 3, 6, 7, 10, 11}};
+__constant__ int8_t cB12[6][6] = {{6, 7, 8, 9, 10, 11},      {0, 1, 2, 3, 4, 5},
+                                  {1, 3, 5, 7, 9, 11},       {0, 2, 4, 6, 8, 10},
+                                  {2, 3, 6, 7, 10, 11},      {0, 1, 4, 5, 8, 9}};
+
 template <int D>
 __device__ __forceinline__ int mask_a(int m, int i) {
   if constexpr (D == 8) return cA8[m][i];
+  else if constexpr (D == 12) return cA12[m][i];
   else return cA14[m][i];
 }
 template <int D>
 __device__ __forceinline__ int mask_b(int m, int i) {
   if constexpr (D == 8) return cB8[m][i];
+  else if constexpr (D == 12) return cB12[m][i];
   else return cB14[m][i];
 }
 
@@ -942,8 +951,8 @@ cudaError_t backward_impl(const float *theta, const FlowWideBufs &b, int layers,
 
 }  // namespace
 
-// The shapes built here: (8, 256), (14, 128), (14, 256).
-#define GRN_WIDE_SHAPES(X) X(8, 256) X(14, 128) X(14, 256)
+// The shapes built here: (8, 256), (12, 128), (12, 256), (14, 128), (14, 256).
+#define GRN_WIDE_SHAPES(X) X(8, 256) X(12, 128) X(12, 256) X(14, 128) X(14, 256)
 
 bool flow_wide_supported(int dim, int hidden) {
 #define GRN_X(d, h) if (dim == d && hidden == h) return true;
@@ -1008,8 +1017,14 @@ cudaError_t launch_flow_uniform_dim(int dim, uint64_t seed, uint32_t stream, int
                                     int64_t n, int64_t ld, float *u, float *lq, cudaStream_t st) {
   if (n <= 0) return cudaSuccess;
   if (dim == 8) return launch_flow_uniform(seed, stream, first, n, ld, u, lq, st);
-  if (dim != 14) return cudaErrorInvalidValue;
-  flow::wide::k_wuniform<14><<<4 * sm_count_w(), 256, 0, st>>>(seed, stream, first, n, ld, u, lq);
+  if (dim == 12)
+    flow::wide::k_wuniform<12><<<4 * sm_count_w(), 256, 0, st>>>(seed, stream, first, n, ld, u,
+                                                                  lq);
+  else if (dim == 14)
+    flow::wide::k_wuniform<14><<<4 * sm_count_w(), 256, 0, st>>>(seed, stream, first, n, ld, u,
+                                                                  lq);
+  else
+    return cudaErrorInvalidValue;
   return cudaGetLastError();
 }
 

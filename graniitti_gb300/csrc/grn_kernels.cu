@@ -775,7 +775,7 @@ __global__ void k_event_daughters(const KArgs A, const double *__restrict__ u, i
   }
   Born b;
   if (born_kinematics<true>(A.P, A.K, x, b))
-    cascade_daughters(A.P, b.p3x, b.p3y, b.mt3 * sinh(b.y3), b.mt3 * cosh(b.y3), sqrt(b.m3sq),
+    cascade_daughters(A.P, A.K.dec0, b.p3x, b.p3y, b.mt3 * sinh(b.y3), b.mt3 * cosh(b.y3), sqrt(b.m3sq),
                       b.p4x, b.p4y, b.mt4 * sinh(b.y4), b.mt4 * cosh(b.y4), sqrt(b.m4sq), x, d4);
   for (int k = 0; k < 16; ++k) pd[i * 16 + k] = d4[k / 4][k % 4];
 }

@@ -72,6 +72,8 @@ struct Consts {
   double lnpt_lo, lnpt_hi;  // log(fpt_min + ZERO_EPS), log(fpt_max)
   double w_const;           // every u-independent factor of the weight
   double M2min, M2max;      // <F>: central-system mass^2 window (B51RandomKin)
+  double offshell;          // cascades: widths of the Breit-Wigner mass draws (OFFSHELL)
+  int    dec0;              // cascades: first decay coordinate (10; 8 with OFFSHELL = 0)
   double M2prop;            // off-shell propagator nominal mass^2 (ME4: first central mass)
   double M2propB;           // ME6: mass^2 of the third central particle (second propagator)
   double g2;                // (c0 / gN_P)^2
@@ -669,6 +671,15 @@ GRN_HD bool solve_x(T a1, T a2, T c1, T c2, T &x1, T &x2) {
 // (src/MContinuum.cc:276-435, src/MProcess.cc:1499-1584).
 GRN_HD bool born_invariants(const Consts &K, Born &b);
 
+GRN_HD void cascade_masses(const grn_process_params &P, const Consts &K, const double *u,
+                           double &m3, double &m4);
+GRN_HD_COLD int cascade_cuts(const grn_process_params &P, int dec0, double p3x, double p3y,
+                             double p3z, double E3, double m3, double p4x, double p4y, double p4z,
+                             double E4, double m4, const double *u);
+
+// CASC: the instantiation serves two-body cascades of the central particles (their masses
+// from cascade_masses, the daughters from the decay coordinates, particle cuts on them).
+template <bool CASC>
 GRN_HD bool born_kinematics_C(const grn_process_params &P, const Consts &K, const double *u,
                               Born &b) {
   const grn_gencuts &g = P.gcuts;
@@ -696,11 +707,17 @@ GRN_HD bool born_kinematics_C(const grn_process_params &P, const Consts &K, cons
   b.p3y = 0.5 * (qy - wy);
   b.p4x = 0.5 * (-qx - wx);
   b.p4y = 0.5 * (-qy - wy);
+  double m3 = K.m3, m4 = K.m4;
   b.m3sq = K.m3sq;
   b.m4sq = K.m4sq;
+  if (CASC && P.n_decay == 2) {
+    cascade_masses(P, K, u, m3, m4);  // BNRandomKin: GetOffShellMass of each central particle
+    b.m3sq = m3 * m3;
+    b.m4sq = m4 * m4;
+  }
   b.leafok = 1;
-  b.mt3 = sqrt(K.m3sq + b.p3x * b.p3x + b.p3y * b.p3y);
-  b.mt4 = sqrt(K.m4sq + b.p4x * b.p4x + b.p4y * b.p4y);
+  b.mt3 = sqrt(b.m3sq + b.p3x * b.p3x + b.p3y * b.p3y);
+  b.mt4 = sqrt(b.m4sq + b.p4x * b.p4x + b.p4y * b.p4y);
   const double e3 = exp(b.y3), e4 = exp(b.y4);
   b.p3p = b.mt3 * e3;
   b.p3m = b.mt3 / e3;
@@ -708,7 +725,12 @@ GRN_HD bool born_kinematics_C(const grn_process_params &P, const Consts &K, cons
   b.p4m = b.mt4 / e4;
   const double Pp = b.p3p + b.p4p, Pm = b.p3m + b.p4m;
   if (0.5 * (Pp + Pm) > K.sqrt_s) return false;  // crude energy check (MContinuum.cc:373)
-
+  if (CASC && P.n_decay == 2) {
+    // isotropic decays of the two central particles (ConstructDecayKinematics); the particle
+    // cuts act on the four daughters (FindDecayCuts, src/MProcess.cc:1140-1154)
+    b.leafok = cascade_cuts(P, K.dec0, b.p3x, b.p3y, b.mt3 * sinh(b.y3), b.mt3 * cosh(b.y3), m3,
+                            b.p4x, b.p4y, b.mt4 * sinh(b.y4), b.mt4 * cosh(b.y4), m4, u);
+  }
   return born_invariants(K, b);
 }
 
@@ -752,17 +774,30 @@ GRN_HD bool born_invariants(const Consts &K, Born &b) {
 }
 
 
-// Relativistic Breit-Wigner mass by inverse CDF in m^2 on [max(M_MIN, m0 - 5 W)^2,
-// (m0 + 5 W)^2] (MRandom::RelativisticBWRandom, src/MRandom.cc:82-104; OFFSHELL = 5 widths,
-// include/Graniitti/MProcess.h:363) from the uniform R.
-GRN_HD double bw_mass(double m0, double W, double M_MIN, double R) {
+// Relativistic Breit-Wigner mass by inverse CDF in m^2 on [max(M_MIN, m0 - n W)^2,
+// (m0 + n W)^2], n = OFFSHELL widths (MRandom::RelativisticBWRandom, src/MRandom.cc:82-104;
+// include/Graniitti/MProcess.h:363) from the uniform R; n = 0 gives the pole mass.
+GRN_HD double bw_mass(double m0, double W, double n, double M_MIN, double R) {
   if (W < 1e-40) return m0;
   const double m2    = m0 * m0;
-  const double m2max = (m0 + 5.0 * W) * (m0 + 5.0 * W);
-  const double m2min = fmax(fmax(0.0, M_MIN * M_MIN), (m0 - 5.0 * W) * (m0 - 5.0 * W));
+  const double m2max = (m0 + n * W) * (m0 + n * W);
+  const double m2min = fmax(fmax(0.0, M_MIN * M_MIN), (m0 - n * W) * (m0 - n * W));
   const double a = atan2(m2min - m2, m0 * W), c = atan2(m2max - m2, m0 * W);
   const double v = m2 + m0 * W * tan(a + R * (c - a));
   return fmax(M_MIN, sqrt(fmax(0.0, v)));
+}
+
+// Off-shell masses of the two central particles of a cascade (GetOffShellMass: the
+// daughters' mass sum + 1e-5 GeV bounds the Breit-Wigner from below) from u[8], u[9]; the
+// pole masses when OFFSHELL = 0 (no mass coordinates).
+GRN_HD void cascade_masses(const grn_process_params &P, const Consts &K, const double *u,
+                           double &m3, double &m4) {
+  m3 = P.m_central[0];
+  m4 = P.m_central[1];
+  if (K.offshell > 0.0) {
+    m3 = bw_mass(m3, P.width[0], K.offshell, P.m_daughter[0] + P.m_daughter[1] + 1e-5, u[8]);
+    m4 = bw_mass(m4, P.width[1], K.offshell, P.m_daughter[2] + P.m_daughter[3] + 1e-5, u[9]);
+  }
 }
 
 // Two-body decay of a mother (px, py, pz, E; mass M) into masses ma, mb with (cos theta,
@@ -785,13 +820,15 @@ GRN_HD void decay2(double px, double py, double pz, double E, double M, double m
   bb[0] = -kx + cb * bx; bb[1] = -ky + cb * by; bb[2] = -kz + cb * bz; bb[3] = gam * (Eb - k1);
 }
 
-// The four daughters of the two central particles, decay angles from u[10..13].
-GRN_HD_COLD void cascade_daughters(const grn_process_params &P, double p3x, double p3y, double p3z,
-                              double E3, double m3, double p4x, double p4y, double p4z, double E4,
-                              double m4, const double *u, double d[4][4]) {
-  decay2(p3x, p3y, p3z, E3, m3, P.m_daughter[0], P.m_daughter[1], 2.0 * u[10] - 1.0, u[11], d[0],
+// The four daughters of the two central particles, decay angles from u[dec0..dec0 + 3].
+GRN_HD_COLD void cascade_daughters(const grn_process_params &P, int dec0, double p3x, double p3y,
+                                   double p3z, double E3, double m3, double p4x, double p4y,
+                                   double p4z, double E4, double m4, const double *u,
+                                   double d[4][4]) {
+  const double *v = u + dec0;
+  decay2(p3x, p3y, p3z, E3, m3, P.m_daughter[0], P.m_daughter[1], 2.0 * v[0] - 1.0, v[1], d[0],
          d[1]);
-  decay2(p4x, p4y, p4z, E4, m4, P.m_daughter[2], P.m_daughter[3], 2.0 * u[12] - 1.0, u[13], d[2],
+  decay2(p4x, p4y, p4z, E4, m4, P.m_daughter[2], P.m_daughter[3], 2.0 * v[2] - 1.0, v[3], d[2],
          d[3]);
 }
 
@@ -821,11 +858,11 @@ GRN_HD bool veto_hit(const grn_process_params &P, double px, double py, double p
 }
 
 // bit 0: the four daughters pass the particle cuts; bit 1: one of them hits a veto domain.
-GRN_HD_COLD int cascade_cuts(const grn_process_params &P, double p3x, double p3y, double p3z,
-                             double E3, double m3, double p4x, double p4y, double p4z, double E4,
-                             double m4, const double *u) {
+GRN_HD_COLD int cascade_cuts(const grn_process_params &P, int dec0, double p3x, double p3y,
+                             double p3z, double E3, double m3, double p4x, double p4y, double p4z,
+                             double E4, double m4, const double *u) {
   double d[4][4];
-  cascade_daughters(P, p3x, p3y, p3z, E3, m3, p4x, p4y, p4z, E4, m4, u, d);
+  cascade_daughters(P, dec0, p3x, p3y, p3z, E3, m3, p4x, p4y, p4z, E4, m4, u, d);
   int ok = 1, veto = 0;
   for (int k = 0; k < 4; ++k) {
     ok &= particle_cuts(P, d[k]) ? 1 : 0;
@@ -852,10 +889,8 @@ GRN_HD bool born_kinematics_F(const grn_process_params &P, const Consts &K, cons
   const double yX  = g.Y_min + (g.Y_max - g.Y_min) * u[4];
   double m3 = K.m3, m4 = K.m4, M2lo = K.M2min, M2hi = K.M2max;
   if (CASC && P.n_decay == 2) {
-    // off-shell central masses (GetOffShellMass: the daughters' mass sum + 1e-5 GeV bounds
-    // the Breit-Wigner from below) and the mass window they leave (B51RandomKin)
-    m3   = bw_mass(P.m_central[0], P.width[0], P.m_daughter[0] + P.m_daughter[1] + 1e-5, u[8]);
-    m4   = bw_mass(P.m_central[1], P.width[1], P.m_daughter[2] + P.m_daughter[3] + 1e-5, u[9]);
+    // off-shell central masses and the mass window they leave (B51RandomKin)
+    cascade_masses(P, K, u, m3, m4);
     const double Mmin = fmax(m3 + m4 + 1e-4, g.M_min);
     if (!(Mmin * Mmin < M2hi)) return false;
     M2lo = Mmin * Mmin;
@@ -909,7 +944,8 @@ GRN_HD bool born_kinematics_F(const grn_process_params &P, const Consts &K, cons
   if (CASC && P.n_decay == 2) {
     // isotropic decays of the two central particles (ConstructDecayKinematics); the particle
     // cuts act on the four daughters (FindDecayCuts, src/MProcess.cc:1140-1154)
-    b.leafok = cascade_cuts(P, b.p3x, b.p3y, p3z, E3, m3, b.p4x, b.p4y, p4z, E4, m4, u);
+    b.leafok =
+        cascade_cuts(P, K.dec0, b.p3x, b.p3y, p3z, E3, m3, b.p4x, b.p4y, p4z, E4, m4, u);
   }
   return born_invariants(K, b);
 }
@@ -918,7 +954,7 @@ template <bool CASC = false>
 GRN_HD bool born_kinematics(const grn_process_params &P, const Consts &K, const double *u,
                             Born &b) {
   if (P.phase_space == GRN_PS_FACTORIZED) return born_kinematics_F<CASC>(P, K, u, b);
-  return born_kinematics_C(P, K, u, b);
+  return born_kinematics_C<CASC>(P, K, u, b);
 }
 
 // Fiducial cuts (MProcess::CommonCuts + FindDecayCuts, src/MProcess.cc:1085-1154).

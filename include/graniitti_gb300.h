@@ -176,20 +176,27 @@ typedef struct grn_process_params {
   int32_t           _pad_res;
   grn_resonance     res[GRN_MAX_RESONANCES];
   /* Decay cascade of the two central particles, "a > {c d} b > {e f}" (MDecayBranch legs,
-   * include/Graniitti/MParticle.h:60-90): each central particle has an off-shell mass drawn
-   * from a relativistic Breit-Wigner within +-5 widths (MProcess::GetOffShellMass,
-   * src/MProcess.cc:753-812) and decays isotropically to two daughters
-   * (ConstructDecayKinematics, :1231-1283). The draws are extra hypercube coordinates:
-   * u[8], u[9] the two masses, u[10..11] and u[12..13] the two decays (cos theta, phi), so a
-   * cascade process has 14 dimensions (<F> only). */
+   * include/Graniitti/MParticle.h:60-90), in the <C> and <F> classes: each central particle
+   * has an off-shell mass drawn from a relativistic Breit-Wigner within +-OFFSHELL widths
+   * (MProcess::GetOffShellMass, src/MProcess.cc:753-812) and decays isotropically to two
+   * daughters (ConstructDecayKinematics, :1231-1283). The draws are extra hypercube
+   * coordinates after the 8 of the 2-body point: u[8], u[9] the two masses, u[10..11] and
+   * u[12..13] the two decays (cos theta, phi), 14 dimensions; with OFFSHELL = 0 (process
+   * command @OFFSHELL:0) the masses are the pole masses and the decays take u[8..11], 12
+   * dimensions. */
   int32_t           n_decay;      /* 0: stable central particles; 2: two-body cascades */
   int32_t           central_spin; /* spin of the central particles (0 or 1: "2xS" / "2xV") */
   double            width[2];     /* widths of the central particles [GeV] */
   double            m_daughter[4];/* daughter masses: central 1 -> [0], [1]; 2 -> [2], [3] */
   /* Regge resonances: spin correlations of production (SPINGEN) and decay (SPINDEC), the
    * frame of the density matrices (GRN_FRAME_*), the flux exponent (PARAM_REGGE omega) */
-  int32_t           spin_gen, spin_dec, spin_frame, _pad_spin;
+  int32_t           spin_gen, spin_dec, spin_frame;
+  /* OFFSHELL, the number of widths of the Breit-Wigner mass draws of cascades
+   * (include/Graniitti/MProcess.h:363): offshell when offshell_user is set (process command
+   * @OFFSHELL:x, MProcess::SetOFFSHELL), else the reference default 5 */
+  int32_t           offshell_user;
   double            omega;
+  double            offshell;
   /* Veto cuts (VETOCUTS, MProcess::VetoCuts / FindVetoCuts, src/MProcess.cc:1069-1175): an
    * event is rejected when any final-state particle of the central system (the leaves of the
    * decay tree) has pt_min[k] <= pT <= pt_max[k] and eta_min[k] <= eta <= eta_max[k] for some
@@ -284,7 +291,8 @@ grn_status grn_event_weights(grn_engine *e, const double *u, int64_t n, int32_t 
  *     GPU (two engines on different streams, concurrently) race; serialise them.
  *   - The scratch address is kept for the life of the device's primary context: do
  *     not use the library across a cudaDeviceReset.
- *   - dim must equal grn_dim(e) (8 for 2-body states, 14 for cascades and 4-body).
+ *   - dim must equal grn_dim(e) (8 for 2-body states, 12 or 14 for cascades, 14 for
+ *     4-body states).
  * Results: identical to grn_event_weights in FP64. In MIXED this call runs the generic
  * FP32 kt-loop with FP64 refinement for every process, while grn_event_weights takes
  * the record-mode loop for screened single-trajectory Regge processes: there the two
@@ -462,7 +470,7 @@ grn_status grn_hist_clear(grn_engine *e);
 typedef struct grn_flow grn_flow;
 
 typedef struct grn_flow_params {
-  int32_t  dim;     /* must equal grn_dim(): 8 (2-body) or 14 (two-body cascades) */
+  int32_t  dim;     /* must equal grn_dim(): 8 (2-body), 12 or 14 (two-body cascades) */
   int32_t  layers;  /* coupling layers, 1..12 (default 6) */
   int32_t  hidden;  /* MLP width: 128 (default) or 256 */
   int32_t  bins;    /* spline bins (16) */

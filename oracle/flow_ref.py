@@ -26,14 +26,17 @@ MIN_D = 1e-3
 
 def masks(dim):
     """Conditioning (A) and transformed (B) index sets of the six masks; layer l uses
-    mask l % 6 (D = 8 or 14): halves, even / odd, neighbour pairs, each then swapped."""
+    mask l % 6 (D = 8, 12 or 14): halves, even / odd, neighbour pairs, each then swapped."""
     if dim == 8:
         A = [[0, 1, 2, 3], [4, 5, 6, 7], [0, 2, 4, 6], [1, 3, 5, 7], [0, 1, 4, 5], [2, 3, 6, 7]]
+    elif dim == 12:
+        A = [list(range(6)), list(range(6, 12)), list(range(0, 12, 2)), list(range(1, 12, 2)),
+             [0, 1, 4, 5, 8, 9], [2, 3, 6, 7, 10, 11]]
     elif dim == 14:
         A = [list(range(7)), list(range(7, 14)), list(range(0, 14, 2)), list(range(1, 14, 2)),
              [0, 1, 4, 5, 8, 9, 12], [2, 3, 6, 7, 10, 11, 13]]
     else:
-        raise ValueError("flow masks exist for D = 8 and 14")
+        raise ValueError("flow masks exist for D = 8, 12 and 14")
     return [(a, [j for j in range(dim) if j not in a]) for a in A]
 
 

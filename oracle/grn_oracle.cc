@@ -358,6 +358,9 @@ bool build_kinematics_c4(const Setup &S, const double *u, Event &ev) {
   return lorentz_scalars(S, ev);
 }
 
+void cascade_masses(const grn_process_params &p, const double *u, double &m3, double &m4);
+void cascade_decays(const Setup &S, const double *u, double m3, double m4, Event &ev);
+
 bool build_kinematics(const Setup &S, const double *u, Event &ev) {
   if (S.p.n_central == 4) return build_kinematics_c4(S, u, ev);
   const grn_gencuts &g = S.p.gcuts;
@@ -376,8 +379,12 @@ bool build_kinematics(const Setup &S, const double *u, Event &ev) {
   V4 p2(pt2 * std::cos(phi2), pt2 * std::sin(phi2), 0, 0);
   ev.q = V4(kt * std::cos(phik), kt * std::sin(phik), 0, 0);
 
+  // central masses: the stable particles' masses, or the off-shell masses of a cascade
+  // (BNRandomKin: GetOffShellMass of each first-level particle)
+  double m[2] = {S.p.m_central[0], S.p.m_central[1]};
+  if (S.p.n_decay == 2) cascade_masses(S.p, u, m[0], m[1]);
   V4 c[2];
-  central_pair(ev.q, p1, p2, S.p.m_central, y, c);
+  central_pair(ev.q, p1, p2, m, y, c);
   const V4 sumP = c[0] + c[1];
   if (sumP.e > S.sqrt_s) return false;
   if (!forward_legs(S, pt1, p1.x, p1.y, pt2, p2.x, p2.y, sumP, p1, p2)) return false;
@@ -389,20 +396,49 @@ bool build_kinematics(const Setup &S, const double *u, Event &ev) {
   ev.pf[4] = c[1];
   if (sumP.m() < c[0].m() + c[1].m()) return false;
   if (!check_emc((S.pb1 + S.pb2) - (p1 + p2 + sumP))) return false;
+  // decay tree (BNBuildKin: ConstructDecayKinematics after the checks); the decays use the
+  // mothers' masses from their 4-momenta (branch.p4.M())
+  if (S.p.n_decay == 2) cascade_decays(S, u, c[0].m(), c[1].m(), ev);
   return lorentz_scalars(S, ev);
 }
 
-// Relativistic Breit-Wigner mass by inverse CDF in m^2, truncated to [max(M_MIN, m0 - 5 W),
-// m0 + 5 W] (MRandom::RelativisticBWRandom, src/MRandom.cc:82-104, OFFSHELL = 5 widths,
-// include/Graniitti/MProcess.h:363), from the uniform R.
-double bw_mass(double m0, double W, double M_MIN, double R) {
+// Relativistic Breit-Wigner mass by inverse CDF in m^2, truncated to [max(M_MIN, m0 - n W),
+// m0 + n W] with n = OFFSHELL widths (MRandom::RelativisticBWRandom, src/MRandom.cc:82-104),
+// from the uniform R; n = 0 gives the pole mass.
+double bw_mass(double m0, double W, double n, double M_MIN, double R) {
   if (W < 1e-40) return m0;
   const double m2    = m0 * m0;
-  const double m2max = sq(m0 + 5.0 * W);
-  const double m2min = std::max(std::max(0.0, M_MIN * M_MIN), sq(m0 - 5.0 * W));
+  const double m2max = sq(m0 + n * W);
+  const double m2min = std::max(std::max(0.0, M_MIN * M_MIN), sq(m0 - n * W));
   const double a = std::atan2(m2min - m2, m0 * W), b = std::atan2(m2max - m2, m0 * W);
   const double v = m2 + m0 * W * std::tan(a + R * (b - a));
   return std::max(M_MIN, msqrt(v));
+}
+
+// OFFSHELL of a cascade: the process command's value, else 5 widths
+// (include/Graniitti/MProcess.h:363, MProcess::SetOFFSHELL).
+double offshell_widths(const grn_process_params &p) { return p.offshell_user ? p.offshell : 5.0; }
+
+// First hypercube coordinate of the cascade decays: after the 8 of the 2-body point and,
+// unless OFFSHELL = 0, the two Breit-Wigner mass draws.
+int decay_coord(const grn_process_params &p) { return offshell_widths(p) > 0 ? 10 : 8; }
+
+// Hypercube dimension of a process.
+int point_dim(const grn_process_params &p) {
+  if (p.n_central == 4) return 14;
+  return p.n_decay == 2 ? decay_coord(p) + 4 : 8;
+}
+
+// Off-shell masses of the two central particles of a cascade (GetOffShellMass, the
+// daughters' mass sum + 1e-5 GeV bounding the Breit-Wigner from below) from u[8], u[9].
+void cascade_masses(const grn_process_params &p, const double *u, double &m3, double &m4) {
+  const double n = offshell_widths(p);
+  m3 = p.m_central[0];
+  m4 = p.m_central[1];
+  if (n > 0) {
+    m3 = bw_mass(m3, p.width[0], n, p.m_daughter[0] + p.m_daughter[1] + 1e-5, u[8]);
+    m4 = bw_mass(m4, p.width[1], n, p.m_daughter[2] + p.m_daughter[3] + 1e-5, u[9]);
+  }
 }
 
 // 2-body decay in the mother's rest frame with given (cos theta, phi), boosted to
@@ -426,6 +462,17 @@ double two_body(const V4 &mother, double M0, double m3, double m4, double ct, do
   p3 = d[0];
   p4 = d[1];
   return 4.0 * PI * pn / (16.0 * PI * PI * M0);
+}
+
+// Isotropic two-body decays of the two central particles of a cascade, (cos theta, phi) from
+// u[dec0..dec0 + 3] (ConstructDecayKinematics, src/MProcess.cc:1231-1283: TwoBodyPhaseSpace
+// with FlatIsotropic draws in the mother's rest frame).
+void cascade_decays(const Setup &S, const double *u, double m3, double m4, Event &ev) {
+  const double *v = u + decay_coord(S.p);
+  two_body(ev.pf[3], m3, S.p.m_daughter[0], S.p.m_daughter[1], 2.0 * v[0] - 1.0, 2.0 * PI * v[1],
+           ev.leaf[0], ev.leaf[1]);
+  two_body(ev.pf[4], m4, S.p.m_daughter[2], S.p.m_daughter[3], 2.0 * v[2] - 1.0, 2.0 * PI * v[3],
+           ev.leaf[2], ev.leaf[3]);
 }
 
 // LorentzBoost (include/Graniitti/MKinematics.h:384-401), sign +1: p from the rest frame of
@@ -486,12 +533,7 @@ bool build_kinematics_F(const Setup &S, const double *u, Event &ev) {
   const double yX   = g.Y_min + (g.Y_max - g.Y_min) * u[4];
   double m3 = S.p.m_central[0], m4 = S.p.m_central[1];
   if (S.p.n_central == 4) m4 = S.p.m_central[1] + S.p.m_central[2] + S.p.m_central[3];
-  if (S.p.n_decay == 2) {
-    // off-shell masses of the central particles (GetOffShellMass: daughters' mass sum +
-    // 1e-5 GeV bounds the Breit-Wigner from below)
-    m3 = bw_mass(m3, S.p.width[0], S.p.m_daughter[0] + S.p.m_daughter[1] + 1e-5, u[8]);
-    m4 = bw_mass(m4, S.p.width[1], S.p.m_daughter[2] + S.p.m_daughter[3] + 1e-5, u[9]);
-  }
+  if (S.p.n_decay == 2) cascade_masses(S.p, u, m3, m4);  // off-shell central masses
   const double Mmin = std::max(m3 + m4 + 1e-4, g.M_min);
   const double Mmax = std::min(S.sqrt_s - (S.pb1.m() + S.pb2.m()), g.M_max);
   if (!(Mmin < Mmax)) return false;
@@ -517,12 +559,7 @@ bool build_kinematics_F(const Setup &S, const double *u, Event &ev) {
     return lorentz_scalars(S, ev);
   }
   ev.dw = two_body(pX, msqrt(m2X), m3, m4, 2.0 * u[6] - 1.0, 2.0 * PI * u[7], ev.pf[3], ev.pf[4]);
-  if (S.p.n_decay == 2) {
-    two_body(ev.pf[3], m3, S.p.m_daughter[0], S.p.m_daughter[1], 2.0 * u[10] - 1.0,
-             2.0 * PI * u[11], ev.leaf[0], ev.leaf[1]);
-    two_body(ev.pf[4], m4, S.p.m_daughter[2], S.p.m_daughter[3], 2.0 * u[12] - 1.0,
-             2.0 * PI * u[13], ev.leaf[2], ev.leaf[3]);
-  }
+  if (S.p.n_decay == 2) cascade_decays(S, u, m3, m4, ev);
   return lorentz_scalars(S, ev);
 }
 
@@ -1595,7 +1632,7 @@ extern "C" {
 // t1, t2, m2 and the 4-vectors pfinal[1..4] (19 doubles).
 int orc_weights(const grn_process_params *p, const double *u, int64_t n, int32_t dim, double *w,
                 uint8_t *flags, double *rec, const double *msa, int32_t n_kt2, int32_t nthreads) {
-  const int32_t want = p && (p->n_decay == 2 || p->n_central == 4) ? 14 : 8;
+  const int32_t want = p ? orc::point_dim(*p) : 8;
   if (!p || !u || !w || dim != want || (p->n_central != 2 && p->n_central != 4))
     return GRN_ERR_INVALID;
   if (p->n_central == 4 && p->process != GRN_PROC_REGGE_CON) return GRN_ERR_INVALID;
@@ -1630,7 +1667,7 @@ int orc_weights(const grn_process_params *p, const double *u, int64_t n, int32_t
 // kinematics (ok[i] = 1), from the tree-level event.
 int orc_observables(const grn_process_params *p, const double *u, int64_t n, int32_t dim,
                     double *obs, uint8_t *ok, int32_t nthreads) {
-  const int32_t want = p && (p->n_decay == 2 || p->n_central == 4) ? 14 : 8;
+  const int32_t want = p ? orc::point_dim(*p) : 8;
   if (!p || !u || !obs || dim != want || (p->n_central != 2 && p->n_central != 4))
     return GRN_ERR_INVALID;
   grn_process_params q = *p;

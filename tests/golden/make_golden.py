@@ -305,15 +305,56 @@ def cascade_fixtures():
     write_sigma("rr_vegas_sigma.json", out, proc, os.path.basename(CARD))
 
 
+def ccascade_fixtures():
+    """Vector-meson pair cascades in the continuum class <C> (BNRandomKin draws the off-shell
+    masses, BNBuildKin decays the central pair with ConstructDecayKinematics), and <F> with
+    @OFFSHELL:0. Replay order of the reference's draws in <C>: per central particle its two
+    daughters' masses, then its own mass (GetOffShellMass, u[8] and u[9] unless OFFSHELL = 0,
+    where the Breit-Wigner collapses to the pole mass and the value is 0.5); then per central
+    particle its daughters' masses and its decay angles (the four coordinates after the 8 of
+    the 2-body point, or after the two masses). Pion masses (width ~1e-17 GeV) take 0.5."""
+    RR = "rho(770)0 > {pi+ pi-} rho(770)0 > {pi+ pi-}"
+    REPLAY_C12 = ["--replay", "h,h,h,h,h,h,h,h,8,9,h,h,10,11"]
+    REPLAY_C14 = ["--replay", "h,h,8,h,h,9,h,h,10,11,h,h,12,13"]
+    REPLAY_F12 = ["--replay", "h,h,h,h,h,h,6,7,h,h,8,9,h,h,10,11"]
+    cases = [
+        ("rrc_tree_weights.npz", 91, 2048, CARD, "PP[CONTENSOR]<C> -> " + RR + " @OFFSHELL:0",
+         12, 8, REPLAY_C12),
+        ("rrc_regge_tree_weights.npz", 92, 1024, CARD, "PP[CON]<C> -> " + RR + " @OFFSHELL:0",
+         12, 8, REPLAY_C12),
+        ("rrc14_tree_weights.npz", 93, 1024, CARD, "PP[CONTENSOR]<C> -> " + RR, 14, 8,
+         REPLAY_C14),
+        ("rrf12_tree_weights.npz", 94, 1024, CARD, "PP[CONTENSOR]<F> -> " + RR + " @OFFSHELL:0",
+         12, 6, REPLAY_F12),
+    ]
+    for name, seed, n, card, proc, D, pdim, rep in cases:
+        u = philox_np.uniforms(seed, n, D)
+        r = run_weights(card, u, rep, proc=proc, dim=pdim, leaves=4)
+        save(name, seed=seed, u=u, card=os.path.basename(card), proc=proc, **r)
+    proc = "PP[CONTENSOR]<C> -> " + RR + " @OFFSHELL:0"
+    u = philox_np.uniforms(95, 256, 12)
+    r = run_weights(CARD_SCR, u, REPLAY_C12 + ["--nbt", "1024", "--nkt2", "10000"], proc=proc,
+                    dim=8, leaves=4)
+    save("rrc_screened_15x12_weights.npz", seed=95, u=u, card=os.path.basename(CARD_SCR),
+         proc=proc, n_bt=1024, n_kt2=10000, loop_kt=15, loop_phi=12, loop_ktmax=1.75, **r)
+    out = subprocess.run([REF_BIN, "vegas", CARD, proc, "--cores", "8"], check=True,
+                         capture_output=True, text=True).stdout
+    write_sigma("rrc_vegas_sigma.json", out, proc, os.path.basename(CARD))
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--ref", default=REF_DEFAULT)
     ap.add_argument("--only", choices=["all", "resonances", "cascades", "rescon", "regge_res",
-                                       "nbody", "nbody_c", "veto"],
+                                       "nbody", "nbody_c", "veto", "ccascades"],
                     default="all")
     a = ap.parse_args()
     subprocess.check_call(["make", "-s", "-C", os.path.join(REPO, "oracle", "refbuild"), "-j8",
                            "REF=" + a.ref])
+    if a.only in ("all", "ccascades"):
+        ccascade_fixtures()
+    if a.only == "ccascades":
+        return
     if a.only in ("all", "veto"):
         veto_fixtures()
     if a.only == "veto":

@@ -143,3 +143,18 @@ def test_unsupported_processes_are_rejected(proc):
 def test_vegas_params():
     vp = card.vegas_params(card.read_card(CARD))
     assert (vp.bins, vp.ncall, vp.iter, vp.lambda_, vp.precision) == (128, 100000, 5, 1.5, 0.001)
+
+
+def test_offshell_command_and_continuum_cascades():
+    """@OFFSHELL:x sets the widths of the cascades' Breit-Wigner draws (MProcess::SetOFFSHELL);
+    the continuum class <C> takes two-body cascades of both central particles."""
+    from graniitti_gb300 import _abi
+    rr = "rho(770)0 > {pi+ pi-} rho(770)0 > {pi+ pi-}"
+    c = card.read_card(CARD)
+    P = card.build_params(c, "PP[CONTENSOR]<C> -> " + rr + " @OFFSHELL:0")
+    assert P.phase_space == _abi.GRN_PS_CONTINUUM and P.n_decay == 2 and P.central_spin == 1
+    assert (P.offshell_user, P.offshell) == (1, 0.0)
+    P = card.build_params(c, "PP[CON]<F> -> " + rr + " @OFFSHELL:2.5")
+    assert (P.offshell_user, P.offshell) == (1, 2.5)
+    P = card.build_params(c, "PP[CONTENSOR]<C> -> " + rr)
+    assert P.offshell_user == 0  # the reference default, 5 widths

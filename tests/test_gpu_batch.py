@@ -104,6 +104,7 @@ def test_batched_mixed_multiplicity_equals_separate(gpu):
         P = card.build_params(c, proc)
         e = g.Engine(P, 0)
         e.eikonal_build(512, 2000)
+        e.set_tuning(loop_pair=1)  # the batched record-mode loop pairs events
         vp = _abi.VegasParams()
         vp.bins, vp.iter, vp.ncall, vp.lambda_ = 128, 5, calls[k], 1.5
         vp.chi2max, vp.precision, vp.burnin_iter, vp.prec, vp.seed = 10.0, 1e-3, 3, g.MIXED, 31 + k
@@ -124,7 +125,8 @@ def test_batched_mixed_multiplicity_equals_separate(gpu):
     print("batched 2-body + 4-body pass: %.2f ms; I = %s" % (ms, [r.I_this for r in res]))
     b.close()
     # a refined pass: the batched graph builds each member's f^2 histogram in the same fixed
-    # order as the engine alone, so the refined grids are equal bit for bit
+    # order as the engine alone (and every member's points get the same weights, the record-
+    # mode member on the same paired loop kernel), so the refined grids are equal bit for bit
     for e, x in zip(es, grids):
         e.vegas_set_grid(x)
     sep = [e.vegas_iteration(mode=1, refine=True, iter_id=10) for e in es]

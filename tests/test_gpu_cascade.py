@@ -34,13 +34,16 @@ def _rel(w, wr):
 
 
 @pytest.mark.parametrize("name", ["rr_tree_weights.npz", "rr_regge_tree_weights.npz",
-                                  "ff_tree_weights.npz"])
+                                  "ff_tree_weights.npz", "rrc_tree_weights.npz",
+                                  "rrc_regge_tree_weights.npz", "rrc14_tree_weights.npz",
+                                  "rrf12_tree_weights.npz"])
 def test_cascade_tree_vs_reference(gpu, name):
+    """<F> and <C> cascades (12 dimensions with @OFFSHELL:0, else 14) against the reference."""
     import graniitti_gb300 as g
     gl = _load(name)
     P = _params(gl)
     e = g.Engine(P, 0)
-    assert e.dim == 14
+    assert e.dim == gl["u"].shape[1]
     w, fl = e.event_weights(gl["u"], prec=g.FP64)
     wo, flo = orc.weights(P, gl["u"])
     assert np.array_equal(fl, flo) and np.array_equal(fl & 1, gl["kin"])
@@ -57,9 +60,11 @@ def test_cascade_tree_vs_reference(gpu, name):
     assert (np.abs(p4 - gl["p4"])[kin] / scale[kin]).max() < 1e-12
 
 
-def test_cascade_screened_vs_reference(gpu):
+@pytest.mark.parametrize("name", ["rr_screened_15x12_weights.npz",
+                                  "rrc_screened_15x12_weights.npz"])
+def test_cascade_screened_vs_reference(gpu, name):
     import graniitti_gb300 as g
-    gl = _load("rr_screened_15x12_weights.npz")
+    gl = _load(name)
     t = _load("eikonal_nbt1024_nkt10000.npz")
     P = _params(gl)
     e = g.Engine(P, 0)
@@ -81,7 +86,8 @@ def test_cascade_screened_vs_reference(gpu):
 
 @pytest.mark.parametrize("proc", [
     "PP[CONTENSOR]<F> -> rho(770)0 > {pi+ pi-} rho(770)0 > {pi+ pi-}",
-    "PP[CON]<F> -> rho(770)0 > {pi+ pi-} rho(770)0 > {pi+ pi-}"])
+    "PP[CON]<F> -> rho(770)0 > {pi+ pi-} rho(770)0 > {pi+ pi-}",
+    "PP[CONTENSOR]<C> -> rho(770)0 > {pi+ pi-} rho(770)0 > {pi+ pi-} @OFFSHELL:0"])
 def test_cascade_mixed_loop_vs_fp64(gpu, proc):
     """FP32 kt-loop against the FP64 loop on 4096 points (tables built on the device)."""
     import graniitti_gb300 as g
@@ -91,7 +97,7 @@ def test_cascade_mixed_loop_vs_fp64(gpu, proc):
     P = card.build_params(card.read_card(CARD_SCR), proc)
     e = g.Engine(P, 0)
     e.eikonal_build()
-    u = philox_np.uniforms(85, 4096, 14)
+    u = philox_np.uniforms(85, 4096, e.dim)
     w64, fl = e.event_weights(u, prec=g.FP64)
     wm, flm = e.event_weights(u, prec=g.MIXED)
     assert np.array_equal(fl, flm)
@@ -105,13 +111,14 @@ def test_cascade_mixed_loop_vs_fp64(gpu, proc):
     assert ok, rel.max()
 
 
-def test_cascade_cross_section_vs_reference_vegas(gpu):
-    """VEGAS over 14 dimensions: the tensor-pomeron rho rho -> pi+ pi- pi+ pi- cross section
-    against the reference's own VEGAS run."""
+@pytest.mark.parametrize("name", ["rr_vegas_sigma.json", "rrc_vegas_sigma.json"])
+def test_cascade_cross_section_vs_reference_vegas(gpu, name):
+    """VEGAS over 14 (<F>) and 12 (<C>, @OFFSHELL:0) dimensions: the tensor-pomeron
+    rho rho -> pi+ pi- pi+ pi- cross section against the reference's own VEGAS run."""
     import json
     import graniitti_gb300 as g
     from graniitti_gb300 import _abi, card
-    ref = json.load(open(os.path.join(GOLDEN, "rr_vegas_sigma.json")))
+    ref = json.load(open(os.path.join(GOLDEN, name)))
     P = card.build_params(card.read_card(os.path.join(GOLDEN, "cards", ref["card"])),
                           ref["process"])
     e = g.Engine(P, 0)
@@ -143,8 +150,9 @@ def test_cascade_rejections(gpu):
         return st
 
     assert status(lambda Q: None) == _abi.GRN_OK
-    assert status(lambda Q: setattr(Q, "phase_space", _abi.GRN_PS_CONTINUUM)) == \
-        _abi.GRN_ERR_UNSUPPORTED
+    assert status(lambda Q: setattr(Q, "phase_space", _abi.GRN_PS_CONTINUUM)) == _abi.GRN_OK
+    assert status(lambda Q: (setattr(Q, "offshell_user", 1), setattr(Q, "offshell", -1.0))) == \
+        _abi.GRN_ERR_INVALID
     assert status(lambda Q: setattr(Q, "n_decay", 0)) == _abi.GRN_ERR_UNSUPPORTED
     assert status(lambda Q: setattr(Q, "n_decay", 3)) == _abi.GRN_ERR_UNSUPPORTED
     e = g.Engine(P, 0)

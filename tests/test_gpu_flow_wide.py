@@ -1,5 +1,6 @@
-"""The flow for the other shapes (grn_flow_wide.cu): D = 8 with width 256, and D = 14 (the
-vector-pair cascades) with width 128 and 256, 8 coupling layers. Density and sampling
+"""The flow for the other shapes (grn_flow_wide.cu): D = 8 with width 256, and D = 12 and 14
+(the vector-pair cascades with on-shell and Breit-Wigner masses) with width 128 and 256, 8
+coupling layers. Density and sampling
 directions, the training gradient against the CPU oracle (oracle/flow_ref.py), and a
 trained 14-dimensional flow in front of the VEGAS map of rho rho -> pi+ pi- pi+ pi-."""
 import numpy as np
@@ -19,8 +20,9 @@ TOL_Z_P99, TOL_Z_MAX, TOL_Z_MED = 3e-5, 2e-3, 1e-6
 TOL_LQ_P99, TOL_LQ_MAX, TOL_LQ_MED = 5e-3, 1e-1, 3e-5
 TOL_GRAD_REL, TOL_LOSS_REL = 2e-2, 1e-4
 LAYERS = 8
-SHAPES = [(8, 256), (14, 128), (14, 256)]
+SHAPES = [(8, 256), (12, 128), (12, 256), (14, 128), (14, 256)]
 RHO = "PP[CONTENSOR]<F> -> rho(770)0 > {pi+ pi-} rho(770)0 > {pi+ pi-}"
+RHO_C12 = "PP[CONTENSOR]<C> -> rho(770)0 > {pi+ pi-} rho(770)0 > {pi+ pi-} @OFFSHELL:0"
 
 
 def _theta(dim, hidden, seed, scale=0.03):
@@ -41,9 +43,11 @@ def engines(gpu, params):
     from conftest import CARD
     e8 = g.Engine(params, 0)
     e14 = g.Engine(card.build_params(card.read_card(CARD), RHO), 0)
-    assert (e8.dim, e14.dim) == (8, 14)
-    yield {8: e8, 14: e14}
+    e12 = g.Engine(card.build_params(card.read_card(CARD), RHO_C12), 0)
+    assert (e8.dim, e12.dim, e14.dim) == (8, 12, 14)
+    yield {8: e8, 12: e12, 14: e14}
     e8.close()
+    e12.close()
     e14.close()
 
 

@@ -190,14 +190,20 @@ def test_tensor_resonance_screened_weights(lib_built, name):
     _check_weights(w, fl, g, tol=1e-9)
 
 
-# Two-body cascades of vector-meson pairs (<F>, 14 dimensions): tensor-pomeron 2xV
-# (MTensorPomeron::ME4 :808-888) and the Regge continuum, with the final-state daughters.
+# Two-body cascades of vector-meson pairs: tensor-pomeron 2xV (MTensorPomeron::ME4 :808-888)
+# and the Regge continuum, with the final-state daughters; <F> (14 dimensions, or 12 with
+# @OFFSHELL:0) and the continuum class <C> (MContinuum::BNRandomKin / BNBuildKin with
+# ConstructDecayKinematics: 12 dimensions with @OFFSHELL:0, 14 with the Breit-Wigner masses).
 @pytest.mark.parametrize("name", ["rr_tree_weights.npz", "rr_regge_tree_weights.npz",
-                                  "ff_tree_weights.npz", "rr_screened_15x12_weights.npz"])
+                                  "ff_tree_weights.npz", "rr_screened_15x12_weights.npz",
+                                  "rrc_tree_weights.npz", "rrc_regge_tree_weights.npz",
+                                  "rrc14_tree_weights.npz", "rrf12_tree_weights.npz",
+                                  "rrc_screened_15x12_weights.npz"])
 def test_vector_pair_cascade_weights(name):
     g = _load(name)
     P = _params_res(g)
     assert P.n_decay == 2 and P.central_spin == 1
+    assert g["u"].shape[1] == (12 if "@OFFSHELL:0" in str(g["proc"]) else 14)
     msa = _load("eikonal_nbt1024_nkt10000.npz")["msa"] if P.screening else None
     w, fl, rec = orc.weights(P, g["u"], msa=msa, nthreads=4, with_rec=True)
     _check_weights(w, fl, g, tol=W_TOL)
