@@ -27,6 +27,13 @@ e2e    = unweighted events delivered to pinned host memory through the C ABI:
          grn_flow_iteration + grn_unweight (hit-or-miss against that max f) +
          grn_vegas_points, timed on the host clock.
 
+Two more legs run the mixed workload of uneven multiplicity (screened tensor-pomeron
+f2(1270) -> pi+ pi-, pi+ pi- continuum and rho rho -> pi+ pi- pi+ pi- with on-shell rho, all
+in the continuum class, 50/30/20, on the same loop grid): at 2^24 points per pass on plain
+VEGAS (batched against one member after another and against plain FP64), and its full form
+at 2^26 points per pass with a learned proposal on every member (rho rho: 8 coupling layers
+of width 256 over its 12 dimensions), batched, against plain VEGAS and plain FP64.
+
 --impl reference times the CPU restatement of the reference path (oracle port, all
 host threads) running plain VEGAS on the same workload, metric and unit.
 """
@@ -222,136 +229,84 @@ def _summary(results, ms, npts, steps):
             "rel_var_per_point": rel_var, "seconds_to_0.1pct": t01, "ms_per_step": ms / steps}
 
 
-# The mixed workload of uneven multiplicity: tensor-pomeron f2(1270) -> pi+ pi- (2-body),
-# the Regge pi+ pi- continuum (2-body) and tensor-pomeron rho rho -> pi+ pi- pi+ pi- (4-body,
-# 14 dimensions), 50/30/20, screened with the generator's default loop grid (15 x 12
-# intervals, kt <= 1.75 GeV).
-BATCH_MIX = [("PP[RESTENSOR]<F> -> pi+ pi-", 0.5), ("PP[CON]<C> -> pi+ pi-", 0.3),
-             ("PP[CONTENSOR]<F> -> rho(770)0 > {pi+ pi-} rho(770)0 > {pi+ pi-}", 0.2)]
+# The mixed workload of uneven multiplicity (continuum class <C>, screened, the 63 x 33 loop
+# grid with kt <= 3 GeV of the screened pi+ pi- configuration): tensor-pomeron
+# f2(1270) -> pi+ pi- (2-body, 8 dims), the tensor-pomeron pi+ pi- continuum (2-body, 8 dims)
+# and tensor-pomeron rho rho -> pi+ pi- pi+ pi- with on-shell rho (4-body, 12 dims), 50/30/20;
+# flow shapes per member for the full form.
+RR_C = "PP[CONTENSOR]<C> -> rho(770)0 > {pi+ pi-} rho(770)0 > {pi+ pi-} @OFFSHELL:0"
+MIX = [("PP[RESTENSOR]<C> -> pi+ pi- @RES{f2_1270:1}", 0.5, (6, 128)),
+       ("PP[CONTENSOR]<C> -> pi+ pi-", 0.3, (6, 128)),
+       (RR_C, 0.2, (8, 256))]
+MIX_POINTS, FULL_POINTS, BURN_POINTS = 1 << 24, 1 << 26, 1 << 22
 
 
-def batched_leg(g, _abi, torch, total, steps, warmup, device):
-    """The mixed 2- and 4-body workload batched in one pass (fused launches, CUDA graph)
-    against the same processes run one after another; the same points, grids and results."""
+def _mix_workload(total, flows=False):
+    s = ("screened tensor-pomeron f2(1270) -> pi+ pi- (<C>, 8 dims) + pi+ pi- continuum (<C>, 8 "
+         "dims) + rho rho -> 4 pi (<C>, @OFFSHELL:0, 12 dims), %s of %d points per pass, loop "
+         "grid %d x %d (kt <= %g GeV), one batched pass" %
+         ("/".join(str(int(f * 100)) for _, f, _ in MIX), total, LOOP_KT, LOOP_PHI, LOOP_KTMAX))
+    if flows:
+        s += ", a learned proposal on every member (%s)" % ", ".join(
+            "%d x %d" % sh for _, _, sh in MIX)
+    return s
+
+
+def mix_engines(g, _abi, total, burn, device, seed0):
+    """The MIX members with their share of `total` points per pass, grids adapted by `burn`
+    refined plain-VEGAS passes over BURN_POINTS points (untimed set-up)."""
     from graniitti_gb300 import card
     c = card.read_card(CARD_SCR)
     c["PROCESSPARAM"]["RES"] = ["f2_1270"]
-
-    def engines(seed0):
-        out = []
-        for k, (proc, frac) in enumerate(BATCH_MIX):
-            P = card.build_params(c, proc)
-            P.loop.n_bt, P.loop.n_kt2 = N_BT, N_KT2
-            e = g.Engine(P, device)
-            e.eikonal_build(N_BT, N_KT2)
-            e.autotune(sample=1 << 16)
-            vp = _abi.VegasParams()
-            vp.bins, vp.iter, vp.ncall, vp.lambda_ = 128, steps, int(total * frac) // 128 * 128, 1.5
-            vp.chi2max, vp.precision, vp.burnin_iter = 10.0, 1e-3, warmup
-            vp.prec, vp.seed = g.MIXED, seed0 + k
-            e.vegas_init(vp)
-            for it in range(warmup):
-                e.vegas_iteration(mode=0, refine=True, iter_id=1 + it)
-            e.vegas_clear()
-            out.append(e)
-        return out
-
-    es = engines(500)
-    b = g.Batch(es)
-    b.iteration(mode=0, refine=True, iter_id=50)  # graph capture + warm-up
-    for e in es:
-        e.vegas_clear()
-        e.set_maxweight(0.0)
-    t0 = torch.cuda.Event(enable_timing=True)
-    t1 = torch.cuda.Event(enable_timing=True)
-    torch.cuda.synchronize()
-    t0.record()
-    for it in range(steps):
-        res, _ = b.iteration(mode=1, refine=True, iter_id=100 + it)
-    t1.record()
-    torch.cuda.synchronize()
-    ms_b = t0.elapsed_time(t1) / steps
-    b.close()
-    for e in es:
-        e.vegas_clear()
-        e.set_maxweight(0.0)
-    torch.cuda.synchronize()
-    t0.record()
-    for it in range(steps):
-        for e in es:
-            e.vegas_iteration(mode=1, refine=True, iter_id=100 + it)
-    t1.record()
-    torch.cuda.synchronize()
-    ms_s = t0.elapsed_time(t1) / steps
-    procs = []
-    for (proc, frac), e, r in zip(BATCH_MIX, es, res):
-        procs.append({"process": proc, "points_per_step": int(e.vp.ncall),
-                      "eps_unw": r.sigma / r.maxf if r.maxf > 0 else None,
-                      "sigma_barn": r.sigma, "sigma_rel_err": r.sigma_err / r.sigma})
-    n = sum(p["points_per_step"] for p in procs)
-    full = full_form(g, _abi, torch, es, res, ms_b, ms_s, steps)
-    for e in es:
-        e.close()
-    return {"workload": "screened f2(1270) -> pi+ pi- (tensor pomeron) + pi+ pi- continuum "
-                        "(Regge) + rho rho -> 4 pi (tensor pomeron, 14 dims), %s of %d points per "
-                        "pass, loop grid 15 x 12, one fused pass"
-                        % ("/".join(str(int(f * 100)) for _, f in BATCH_MIX), n),
-            "ms_per_step_batched": ms_b, "ms_per_step_separate": ms_s,
-            "evaluations_per_s_batched": n / (ms_b * 1e-3),
-            "speedup_over_separate": ms_s / ms_b, "processes": procs, "full_form": full}
-
-
-def _unweighted_per_s(es, res, ms):
-    """Unweighted events per second of a pass over all members: sum_p ncall_p eps_p / time,
-    eps_p = <f>/max f of member p over its integration passes."""
-    return sum(int(e.vp.ncall) * (r.sigma / r.maxf) for e, r in zip(es, res) if r.maxf > 0) / (
-        ms * 1e-3)
-
-
-def full_form(g, _abi, torch, es, res_plain, ms_b, ms_s, steps):
-    """The full form of the mixed workload: the 4-body member (rho rho -> 4 pi, 14 dimensions)
-    draws its points from a learned proposal, 8 coupling layers of width 256 (trained untimed
-    in front of its adapted grid), batched with the 2-body members; against the same members
-    on plain VEGAS (batched, one after another, and FP64 one after another)."""
-    # the 2-body members: 6 coupling layers of width 128 (8 dims); rho rho: 8 of width 256
-    shapes = [(6, 128), (6, 128), (8, 256)]
-    flows, trs = [], []
-    for k, (e, (layers, hidden)) in enumerate(zip(es, shapes)):
-        f = g.Flow(e, layers=layers, hidden=hidden, seed=5 + k, mix_uniform=0.05)
-        nt = max(16384, int(e.vp.ncall) // 16384 * 16384)
-        trs.append(f.train(n_train=nt, batch=16384, epochs=3, rounds=3, lr=1e-3, prec=g.MIXED,
-                           seed_stream=7 + k))
-        flows.append(f)
-    for e in es:
-        e.vegas_clear()
-        e.set_maxweight(0.0)
-    bf = g.Batch(es)
-    for k, f in enumerate(flows):
-        bf.set_flow(k, f)
-    bf.iteration(mode=0, refine=False, iter_id=70)  # graph capture + warm-up
-    for e in es:
-        e.vegas_clear()
-        e.set_maxweight(0.0)
-    t0 = torch.cuda.Event(enable_timing=True)
-    t1 = torch.cuda.Event(enable_timing=True)
-    torch.cuda.synchronize()
-    t0.record()
-    for it in range(steps):
-        res_f, _ = bf.iteration(mode=1, refine=False, iter_id=300 + it)
-    t1.record()
-    torch.cuda.synchronize()
-    ms_f = t0.elapsed_time(t1) / steps
-    bf.close()
-    # plain FP64 VEGAS, one member after another: the evaluation rate of each member on 1/16
-    # of its points (same adapted grid; eps_unw as the mixed-precision plain passes)
-    fp64_s = 0.0
-    for e in es:
+    es = []
+    for k, (proc, frac, _) in enumerate(MIX):
+        P = card.build_params(c, proc)
+        P.loop.n_kt, P.loop.n_phi, P.loop.kt_max = LOOP_KT, LOOP_PHI, LOOP_KTMAX
+        P.loop.n_bt, P.loop.n_kt2 = N_BT, N_KT2
+        e = g.Engine(P, device)
+        e.eikonal_build(N_BT, N_KT2)
+        vp = _abi.VegasParams()
+        vp.bins, vp.iter, vp.ncall, vp.lambda_ = 128, 5, int(BURN_POINTS * frac) // 128 * 128, 1.5
+        vp.chi2max, vp.precision, vp.burnin_iter = 10.0, 1e-3, burn
+        vp.prec, vp.seed = g.MIXED, seed0 + k
+        e.vegas_init(vp)
+        for it in range(burn):
+            e.vegas_iteration(mode=0, refine=True, iter_id=1 + it)
         grid = e.vegas_grid()
-        vp = e.vp
-        n16 = max(128, int(vp.ncall) // 16 // 128 * 128)
+        vp.ncall = int(total * frac) // 128 * 128
+        e.vegas_init(vp)
+        e.vegas_set_grid(grid)
+        e.vp = vp
+        es.append(e)
+    return es
+
+
+def _timed_batch(torch, b, es, steps, refine, iter0):
+    for e in es:
+        e.vegas_clear()
+        e.set_maxweight(0.0)
+    t0 = torch.cuda.Event(enable_timing=True)
+    t1 = torch.cuda.Event(enable_timing=True)
+    torch.cuda.synchronize()
+    t0.record()
+    for it in range(steps):
+        res, _ = b.iteration(mode=1, refine=refine, iter_id=iter0 + it)
+    t1.record()
+    torch.cuda.synchronize()
+    return res, t0.elapsed_time(t1) / steps
+
+
+def _fp64_pass_ms(g, _abi, torch, es, frac_points=64):
+    """Plain FP64 VEGAS, member after member: the pass time at each member's full point count
+    from a pass over 1/frac_points of its points on the same adapted grid."""
+    t0 = torch.cuda.Event(enable_timing=True)
+    t1 = torch.cuda.Event(enable_timing=True)
+    total = 0.0
+    for e in es:
+        grid, vp = e.vegas_grid(), e.vp
         vq = _abi.VegasParams()
         ctypes_copy(vq, vp)
-        vq.ncall, vq.prec = n16, g.FP64
+        vq.ncall, vq.prec = max(128, int(vp.ncall) // frac_points // 128 * 128), g.FP64
         e.vegas_init(vq)
         e.vegas_set_grid(grid)
         torch.cuda.synchronize()
@@ -359,30 +314,121 @@ def full_form(g, _abi, torch, es, res_plain, ms_b, ms_s, steps):
         e.vegas_iteration(mode=1, refine=False, iter_id=900)
         t1.record()
         torch.cuda.synchronize()
-        fp64_s += t0.elapsed_time(t1) * 1e-3 * (int(vp.ncall) / n16)
+        total += t0.elapsed_time(t1) * (int(vp.ncall) / int(vq.ncall))
+        e.vegas_init(vp)
+        e.vegas_set_grid(grid)
         e.vp = vp
+    return total
+
+
+def _member_stats(es, res, ms):
+    out = []
+    for (proc, frac, _), e, r in zip(MIX, es, res):
+        n = int(e.vp.ncall)
+        rel_var = max(r.I2_this * n / r.I_this ** 2, 0.0) if r.I_this else None
+        evals_s = n / (ms * 1e-3)
+        out.append({"process": proc, "points_per_step": n,
+                    "eps_unw": r.sigma / r.maxf if r.maxf > 0 else None,
+                    "sigma_barn": r.sigma, "sigma_rel_err": r.sigma_err / r.sigma if r.sigma else None,
+                    "rel_var_per_point": rel_var, "refined_fp64": int(r.refined),
+                    "seconds_to_0.1pct": rel_var / 1e-6 / evals_s if rel_var else None})
+    return out
+
+
+def mix_leg(g, _abi, torch, steps, burn, device):
+    """The mixed workload at MIX_POINTS points per pass on plain VEGAS: one batched pass (fused
+    stage A, graph-replayed) against the members one after another, and plain FP64."""
+    es = mix_engines(g, _abi, MIX_POINTS, burn, device, 500)
+    grids = [e.vegas_grid() for e in es]
+    b = g.Batch(es)
+    res_b, ms_b = _timed_batch(torch, b, es, steps, False, 100)
+    b.close()
+    for e, x in zip(es, grids):
+        e.vegas_clear()
+        e.set_maxweight(0.0)
+        e.vegas_set_grid(x)
+    t0 = torch.cuda.Event(enable_timing=True)
+    t1 = torch.cuda.Event(enable_timing=True)
+    torch.cuda.synchronize()
+    t0.record()
+    for it in range(steps):
+        res_s = [e.vegas_iteration(mode=1, refine=False, iter_id=100 + it) for e in es]
+    t1.record()
+    torch.cuda.synchronize()
+    ms_s = t0.elapsed_time(t1) / steps
+    ms64 = _fp64_pass_ms(g, _abi, torch, es)
+    out = {"workload": _mix_workload(MIX_POINTS), "steps": steps,
+           "ms_per_step_batched": ms_b, "ms_per_step_separate": ms_s,
+           "ms_per_step_fp64_separate": ms64,
+           "evaluations_per_s_batched": MIX_POINTS / (ms_b * 1e-3),
+           "speedup_over_separate": ms_s / ms_b,
+           "unweighted_per_s": {"plain_batched": _unweighted_per_s(es, res_b, ms_b),
+                                "plain_separate": _unweighted_per_s(es, res_s, ms_s),
+                                "plain_fp64_separate": _unweighted_per_s(es, res_s, ms64)},
+           "processes": _member_stats(es, res_b, ms_b)}
+    for e in es:
+        e.close()
+    return out
+
+
+def full_form_leg(g, _abi, torch, steps, burn, device):
+    """The full form at FULL_POINTS points per pass: every member draws its points from a
+    learned proposal (rho rho: 8 coupling layers of width 256 over its 12 dimensions; the
+    2-body members 6 of width 128), trained untimed in front of its adapted grid, all members
+    in one batched pass; against the same members on plain VEGAS (batched) and on plain FP64
+    VEGAS (member after member)."""
+    es = mix_engines(g, _abi, FULL_POINTS, burn, device, 700)
+    flows, trs = [], []
+    for k, (e, (_, _, (layers, hidden))) in enumerate(zip(es, MIX)):
+        f = g.Flow(e, layers=layers, hidden=hidden, seed=5 + k, mix_uniform=0.05)
+        nt = max(16384, int(BURN_POINTS * MIX[k][1]) // 16384 * 16384)
+        trs.append(f.train(n_train=nt, batch=16384, epochs=3, rounds=3, lr=1e-3, prec=g.MIXED,
+                           seed_stream=7 + k))
+        flows.append(f)
+    grids = [e.vegas_grid() for e in es]
+    bf = g.Batch(es)
+    for k, f in enumerate(flows):
+        bf.set_flow(k, f)
+    res_f, ms_f = _timed_batch(torch, bf, es, steps, False, 300)
+    bf.close()
+    for e, x in zip(es, grids):
+        e.vegas_set_grid(x)
+    b = g.Batch(es)
+    res_p, ms_p = _timed_batch(torch, b, es, steps, False, 400)
+    b.close()
+    ms64 = _fp64_pass_ms(g, _abi, torch, es)
     for f in flows:
         f.close()
     u_flow = _unweighted_per_s(es, res_f, ms_f)
-    u_batch = _unweighted_per_s(es, res_plain, ms_b)
-    u_sep = _unweighted_per_s(es, res_plain, ms_s)
-    u_fp64 = _unweighted_per_s(es, res_plain, fp64_s * 1e3)
-    return {"flow": "per member, RQ splines 16 bins, BF16 (tcgen05), 5% uniform mixture, trained "
-                    "untimed: 2-body members 6 coupling layers of MLP 128 x 2 (8 dims), rho rho 8 "
-                    "coupling layers of MLP 256 x 2 (14 dims)",
-            "train_ms": [t.train_ms for t in trs], "train_steps": [t.steps for t in trs],
-            "rel_var": {"plain": [t.rel_var_start for t in trs],
-                        "flow": [t.rel_var_flow for t in trs]},
-            "eps_unw_plain": [r.sigma / r.maxf if r.maxf > 0 else None for r in res_plain],
-            "ms_per_step_flow_batched": ms_f, "ms_per_step_fp64_separate": fp64_s * 1e3,
-            "unweighted_per_s": {"flow_batched": u_flow, "plain_batched": u_batch,
-                                 "plain_separate": u_sep, "plain_fp64_separate": u_fp64},
-            "flow_batched_over_plain_separate": u_flow / u_sep,
-            "flow_batched_over_plain_fp64": u_flow / u_fp64,
-            "eps_unw_flow": [r.sigma / r.maxf if r.maxf > 0 else None for r in res_f],
-            "sigma_flow_vs_plain_pull": [
-                (rf.sigma - rp.sigma) / (rf.sigma_err ** 2 + rp.sigma_err ** 2) ** 0.5
-                for rf, rp in zip(res_f, res_plain)]}
+    u_plain = _unweighted_per_s(es, res_p, ms_p)
+    u_fp64 = _unweighted_per_s(es, res_p, ms64)
+    out = {"workload": _mix_workload(FULL_POINTS, flows=True), "steps": steps,
+           "flow": "RQ splines 16 bins, BF16 (tcgen05), 5% uniform mixture, trained untimed "
+                   "(3 rounds x 3 epochs, batch 16384) on the adapted grids",
+           "train_ms": [t.train_ms for t in trs], "train_steps": [t.steps for t in trs],
+           "rel_var_train": {"plain": [t.rel_var_start for t in trs],
+                             "flow": [t.rel_var_flow for t in trs]},
+           "ms_per_step_flow_batched": ms_f, "ms_per_step_plain_batched": ms_p,
+           "ms_per_step_fp64_separate": ms64,
+           "unweighted_per_s": {"flow_batched": u_flow, "plain_batched": u_plain,
+                                "plain_fp64_separate": u_fp64},
+           "flow_batched_over_plain": u_flow / u_plain if u_plain else None,
+           "flow_batched_over_plain_fp64": u_flow / u_fp64 if u_fp64 else None,
+           "processes_flow": _member_stats(es, res_f, ms_f),
+           "processes_plain": _member_stats(es, res_p, ms_p),
+           "sigma_flow_vs_plain_pull": [
+               (rf.sigma - rp.sigma) / (rf.sigma_err ** 2 + rp.sigma_err ** 2) ** 0.5
+               for rf, rp in zip(res_f, res_p)]}
+    for e in es:
+        e.close()
+    return out
+
+
+def _unweighted_per_s(es, res, ms):
+    """Unweighted events per second of a pass over all members: sum_p ncall_p eps_p / time,
+    eps_p = <f>/max f of member p over its integration passes."""
+    return sum(int(e.vp.ncall) * (r.sigma / r.maxf) for e, r in zip(es, res) if r.maxf > 0) / (
+        ms * 1e-3)
 
 
 def ctypes_copy(dst, src):
@@ -403,6 +449,8 @@ def main():
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-fp64", action="store_true")
     ap.add_argument("--no-batch", action="store_true")
+    ap.add_argument("--mix-steps", type=int, default=2,
+                    help="timed passes of the mixed-workload legs (2^24 and 2^26 points)")
     args = ap.parse_args()
     if args.warmup < 3:
         args.warmup = 3
@@ -545,8 +593,10 @@ def main():
         eng.set_maxweight(fl_maxf)
         kernel_timing(eng, reset=True)
 
-    # -- several processes in one pass (fused launches, CUDA graph) ------------
-    batched = None if args.no_batch else batched_leg(g, _abi, torch, n, 3, args.warmup, local)
+    # -- several processes in one pass (fused launches, CUDA graph): the mixed workload
+    #    on plain VEGAS, and its full form with a learned proposal on every member --------
+    mixed = None if args.no_batch else mix_leg(g, _abi, torch, args.mix_steps, 3, local)
+    full = None if args.no_batch else full_form_leg(g, _abi, torch, args.mix_steps, 3, local)
 
     # -- e2e: unweighted events delivered to pinned host memory through the C ABI
     #    (flow pass -> hit-or-miss against the integration's max f -> points) ---
@@ -599,7 +649,8 @@ def main():
                          sample_kernel_ms=flow_s * 1e3, sample_tflops=flow_tflops,
                          sample_frac_of_measured_bf16=(flow_tflops / bf16_peak
                                                        if bf16_peak else None)),
-               plain_vegas_mixed=plain, plain_vegas_fp64=fp64, autotune=tuned, batched=batched,
+               plain_vegas_mixed=plain, plain_vegas_fp64=fp64, autotune=tuned,
+               mixed_workload=mixed, full_form=full,
                flow_over_plain_mixed=value / plain["value"] if plain["value"] else None,
                flow_over_plain_fp64=(value / fp64["value"]) if fp64 and fp64["value"] else None)
     line = {"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
