@@ -159,7 +159,7 @@ __device__ double screened_amp2_vv(const KArgs &A, const Born &b, const KtNode<T
   LV<T> e3[3], e4[3];
   vector_basis<T>(T(b.p3p), T(b.p3m), T(b.p3x), T(b.p3y), e3);
   vector_basis<T>(T(b.p4p), T(b.p4m), T(b.p4x), T(b.p4y), e4);
-  const T s34 = T(b.m2);
+  const VProp<T> vp = vector_prop_consts<T>(T(A.K.M2prop), T(b.m2));
   T sr[9], si[9], cr[9], ci[9];
 #pragma unroll
   for (int h = 0; h < 9; ++h) sr[h] = si[h] = cr[h] = ci[h] = T(0);
@@ -170,7 +170,7 @@ __device__ double screened_amp2_vv(const KArgs &A, const Born &b, const KtNode<T
       LCKin<T>         kk;
       if (!loop_point_kin<T>(e, nj.kt * ni.c, nj.kt * ni.s, kk)) continue;
       cx<T> a[9];
-      tensor_me4_2xv<T>(A.P, A.K, kk, s34, e3, e4, a);
+      tensor_me4_2xv<T>(A.P, A.K, kk, vp, e3, e4, a);
       const T wr = ni.u * nj.cre, wi = ni.u * nj.cim;
       const T aw = kMag ? sqrt(wr * wr + wi * wi) : T(0);
 #pragma unroll

@@ -166,23 +166,32 @@ GRN_HD cx<T> regge_prop(const Consts &K, const grn_regge_params &rp, T lns, T t)
 // a sqrt(s)-size component with a cancellation-free one.
 constexpr double kMpPDG = 0.938272081;  // PDG::mp used by the form factors
 
+// Dirac form factor F1(Q^2) = (GE + tau GM) / (1 + tau) as numerator / denominator (no
+// division): Kelly's parameterisation of GE, GM or the dipole.
+template <typename T>
+GRN_HD void dirac_f1_nd(T Q2, int kelly, T &num, T &den) {
+  Q2 = fabs(Q2);
+  const T tau = Q2 * T(1.0 / (4.0 * kMpPDG * kMpPDG));
+  const T mu  = T(2.792847337);
+  if (kelly) {
+    const T nE = T(1) - T(0.24) * tau;
+    const T dE = T(1) + tau * (T(10.98) + tau * (T(12.82) + tau * T(21.97)));
+    const T nM = mu * (T(1) + T(0.12) * tau);
+    const T dM = T(1) + tau * (T(10.97) + tau * (T(18.86) + tau * T(6.55)));
+    num = nE * dM + tau * nM * dE;
+    den = dE * dM * (tau + T(1));
+  } else {
+    const T d = T(1) + Q2 * T(1.0 / 0.71);
+    num = T(1) + tau * mu;
+    den = d * d * (tau + T(1));
+  }
+}
+
 template <typename T>
 GRN_HD T dirac_f1(T Q2, int kelly) {
-  Q2 = fabs(Q2);
-  const T tau = Q2 / T(4.0 * kMpPDG * kMpPDG);
-  const T mu  = T(2.792847337);
-  T GE, GM;
-  if (kelly) {
-    GE = (T(1) - T(0.24) * tau) /
-         (T(1) + tau * (T(10.98) + tau * (T(12.82) + tau * T(21.97))));
-    GM = mu * (T(1) + T(0.12) * tau) /
-         (T(1) + tau * (T(10.97) + tau * (T(18.86) + tau * T(6.55))));
-  } else {
-    const T d = T(1) + Q2 / T(0.71);
-    GM = mu / (d * d);
-    GE = GM / mu;
-  }
-  return (GE + tau * GM) / (tau + T(1));
+  T n, d;
+  dirac_f1_nd<T>(Q2, kelly, n, d);
+  return n / d;
 }
 
 // Light-cone kinematics of one (tree-level or loop) point.
@@ -208,17 +217,39 @@ GRN_HD T lc_dot(T ap, T am, T ax, T ay, T bp, T bm, T bx, T by) {
   return T(0.5) * (ap * bm + am * bp) - (ax * bx + ay * by);
 }
 
-// c(s, t) (-6 gPNN g F1(t) FM(t)) as a complex number.
+// Proton legs of a tensor-pomeron amplitude: F1(t1) FM(t1) F1(t2) FM(t2) with FM(t) =
+// 1 / (1 - t / 0.5), as numerator / denominator.
 template <typename T>
-GRN_HD cx<T> tensor_exchange(const grn_tensor_params &tp, T s, T t) {
-  const T x   = T(tp.delta_P) + T(tp.ap_P) * t;   // alpha(t) - 1
-  const T mag = exp(x * log(s * T(tp.ap_P))) / (T(4) * s);
-  T sn, cs;
-  sincos_pi(T(-0.5) * x, sn, cs);                 // (-i)^x = exp(-i pi x / 2)
-  const T v = T(-6.0 * tp.gPNN * tp.gPps) * dirac_f1<T>(t, tp.em_kelly) / (T(1) - t / T(0.5));
-  return {mag * cs * v, mag * sn * v};
+GRN_HD void proton_legs_nd(const grn_tensor_params &tp, T t1, T t2, T &num, T &den) {
+  T n1, d1, n2, d2;
+  dirac_f1_nd<T>(t1, tp.em_kelly, n1, d1);
+  dirac_f1_nd<T>(t2, tp.em_kelly, n2, d2);
+  num = n1 * n2;
+  den = d1 * d2 * ((T(1) - T(2) * t1) * (T(1) - T(2) * t2));
 }
 
+// Off-shell meson form factor squared over the propagator denominator,
+// ff(p^2)^2 / (p^2 - M2), as numerator / denominator (meson_ff).
+template <typename T>
+GRN_HD void meson_prop_nd(const grn_regge_params &rp, T p2, T M2, T &num, T &den) {
+  const T tp = p2 - M2;
+  if (rp.offshellFF == 2) {  // (1 / (1 - tp / b))^2 = b^2 / (b - tp)^2
+    const T b = T(rp.b_POW), d = b - tp;
+    num = b * b;
+    den = d * d * tp;
+  } else {
+    const T f = meson_ff<T>(rp, p2, M2);
+    num = f * f;
+    den = tp;
+  }
+}
+
+// Tensor-pomeron continuum of two pseudoscalars (MTensorPomeron::ME4 "2xS"): per exchange
+// c(s, t) (-6 gPNN g F1(t) FM(t)) (2 (P.Q)^2 - P^2 Q^2 / 2), c(s, t) = (1/4s) (s ap)^x
+// e^{-i pi x / 2}, x = alpha(t) - 1. The t and u channels share t1 and t2, hence the phase
+// e^{-i pi (x1 + x2) / 2} and the proton legs F1 FM of both; per channel remains the real
+// (ap s)^x1 (ap s')^x2 / (16 s s') with its meson propagator:
+//   M = e^{-i pi (x1 + x2)/2} (6 gPNN g)^2 F1 FM F1 FM [w_t v13 v24 R_t + w_u v14 v23 R_u].
 template <typename T>
 GRN_HD cx<T> tensor_me4_2xs(const grn_process_params &P, const Consts &K, const LCKin<T> &k) {
   const T eps = k.eps, L = k.L;
@@ -247,14 +278,22 @@ GRN_HD cx<T> tensor_me4_2xs(const grn_process_params &P, const Consts &K, const 
   const T v23 = vtx(P2p, P2m, k.p2x, k.p2y, P2sq, pup - k.p3p, pum - k.p3m, pux - k.p3x,
                     puy - k.p3y);
   const grn_tensor_params &tp = P.tensor;
-  const T M2 = T(K.M2prop);
-  const T fft = meson_ff<T>(P.regge, k.that, M2), ffu = meson_ff<T>(P.regge, k.uhat, M2);
-  // i / (p^2 - M^2) x ff^2, then the overall -i: Mt, Mu real prefactors
-  const T wt = fft * fft / (k.that - M2), wu = ffu * ffu / (k.uhat - M2);
-  const cx<T> At = cmul(tensor_exchange<T>(tp, k.s13, k.t1), tensor_exchange<T>(tp, k.s24, k.t2));
-  const cx<T> Au = cmul(tensor_exchange<T>(tp, k.s14, k.t1), tensor_exchange<T>(tp, k.s23, k.t2));
+  const T M2 = T(K.M2prop), ap = T(tp.ap_P);
+  const T x1 = T(tp.delta_P) + ap * k.t1, x2 = T(tp.delta_P) + ap * k.t2;
+  T wtn, wtd, wun, wud, ln, ld;
+  meson_prop_nd<T>(P.regge, k.that, M2, wtn, wtd);
+  meson_prop_nd<T>(P.regge, k.uhat, M2, wun, wud);
+  proton_legs_nd<T>(tp, k.t1, k.t2, ln, ld);
+  const T Rt = exp(x1 * log(ap * k.s13) + x2 * log(ap * k.s24));
+  const T Ru = exp(x1 * log(ap * k.s14) + x2 * log(ap * k.s23));
   // M = -i (i wt v13 v24 At + i wu v14 v23 Au) = wt v13 v24 At + wu v14 v23 Au
-  return cadd(cscale(At, wt * v13 * v24), cscale(Au, wu * v14 * v23));
+  const T B = (wtn * v13 * v24 * Rt) / (T(16) * wtd * k.s13 * k.s24) +
+              (wun * v14 * v23 * Ru) / (T(16) * wud * k.s14 * k.s23);
+  const T g6 = T(6.0 * tp.gPNN * tp.gPps);
+  const T mag = g6 * g6 * B * ln / ld;
+  T sn, cs;
+  sincos_pi(T(-0.5) * (x1 + x2), sn, cs);
+  return {mag * cs, mag * sn};
 }
 
 // ---------------------------------------------------------------------------
@@ -562,33 +601,27 @@ GRN_HD void vector_basis(T pp, T pm, T px, T py, LV<T> e[3]) {
   e[2] = {l0 + ls * n[2], l0 - ls * n[2], ls * n[0], ls * n[1]};
 }
 
-// Reggeized vector-propagator factor -(e^{i phi} s34 / (4 M0^2))^(alpha - 1) / (p^2 - M0^2),
-// alpha = 0.5 + 0.9 p^2, phi = pi/2 exp((4 M0^2 - s34) / (4 M0^2)) - pi/2 (iD_V).
+// Reggeized vector propagator iD_V (:2353-2369): -(e^{i phi} s34 / (4 M0^2))^(alpha - 1) /
+// (p^2 - M0^2), alpha = 0.5 + 0.9 p^2, phi = pi/2 exp((4 M0^2 - s34) / (4 M0^2)) - pi/2. Its
+// s34-dependent factors are constants of an event (the central pair does not change in the
+// loop): lns = ln(s34 / (4 M0^2)) and phi / pi.
 template <typename T>
-GRN_HD cx<T> vector_prop(T p2, T M0sq, T s34) {
+struct VProp {
+  T lns, ph;
+};
+template <typename T>
+GRN_HD VProp<T> vector_prop_consts(T M0sq, T s34) {
   const T sth = T(4) * M0sq;
-  const T ph  = T(0.5) * (exp((sth - s34) / sth) - T(1));  // phi / pi
-  const T a1  = T(-0.5) + T(0.9) * p2;                     // alpha - 1
-  const T mag = -exp(a1 * log(s34 / sth)) / (p2 - M0sq);
-  T sn, cs;
-  sincos_pi(a1 * ph, sn, cs);
-  return {mag * cs, mag * sn};
+  return {log(s34 / sth), T(0.5) * (exp((sth - s34) / sth) - T(1))};
 }
 
-// Pomeron propagator factor 1/(4s) (-i s ap)^(alpha(t) - 1) (iD_P, :2288-2298).
-template <typename T>
-GRN_HD cx<T> pomeron_c(const grn_tensor_params &tp, T s, T t) {
-  const T x   = T(tp.delta_P) + T(tp.ap_P) * t;
-  const T mag = exp(x * log(s * T(tp.ap_P))) / (T(4) * s);
-  T sn, cs;
-  sincos_pi(T(-0.5) * x, sn, cs);
-  return {mag * cs, mag * sn};
-}
-
-// The nine amplitudes A[3 i + j] = e3_i . M . e4_j of one proton helicity configuration.
+// The nine amplitudes A[3 i + j] = e3_i . M . e4_j of one proton helicity configuration. Both
+// channels share t1 and t2, hence the pomeron phase e^{-i pi (x1 + x2) / 2} and the proton
+// legs; per channel remain the pomeron magnitudes (ap s)^x1 (ap s')^x2 / (16 s s'), the vector
+// propagator and the off-shell form factors, with one exponential and one phase each.
 template <typename T>
 GRN_HD void tensor_me4_2xv(const grn_process_params &P, const Consts &K, const LCKin<T> &k,
-                           T s34, const LV<T> e3[3], const LV<T> e4[3], cx<T> A[9]) {
+                           const VProp<T> &vp, const LV<T> e3[3], const LV<T> e4[3], cx<T> A[9]) {
   const grn_tensor_params &tp = P.tensor;
   const T L = k.L, eps = k.eps;
   const LV<T> P1{k.p1p + L, k.p1m + eps, k.p1x, k.p1y};
@@ -602,27 +635,34 @@ GRN_HD void tensor_me4_2xv(const grn_process_params &P, const Consts &K, const L
   const LV<T> mpu{-pu.p, -pu.m, -pu.x, -pu.y};
   const T g1 = T(tp.gPvv[0]), g2 = T(tp.gPvv[1]);
   // channel constants (-3i gPNN F1)^2 (i FM)^2 c c ff^2 D_V = 9 gPNN^2 F1 F1 FM FM c c ff^2 D_V
-  const T M0sq = T(K.M2prop);
-  const T com  = T(9.0 * tp.gPNN * tp.gPNN) * dirac_f1<T>(k.t1, tp.em_kelly) *
-                dirac_f1<T>(k.t2, tp.em_kelly) / ((T(1) - k.t1 / T(0.5)) * (T(1) - k.t2 / T(0.5)));
-  const T fft = meson_ff<T>(P.regge, k.that, M0sq), ffu = meson_ff<T>(P.regge, k.uhat, M0sq);
-  const cx<T> Ct = cscale(cmul(cmul(pomeron_c<T>(tp, k.s13, k.t1), pomeron_c<T>(tp, k.s24, k.t2)),
-                               vector_prop<T>(k.that, M0sq, s34)),
-                          com * fft * fft);
-  const cx<T> Cu = cscale(cmul(cmul(pomeron_c<T>(tp, k.s14, k.t1), pomeron_c<T>(tp, k.s23, k.t2)),
-                               vector_prop<T>(k.uhat, M0sq, s34)),
-                          com * ffu * ffu);
-  LV<T> at[3], bt[3], au[3], bu[3];
+  const T M0sq = T(K.M2prop), ap = T(tp.ap_P);
+  const T x1 = T(tp.delta_P) + ap * k.t1, x2 = T(tp.delta_P) + ap * k.t2;
+  T ln, ld, wtn, wtd, wun, wud;
+  proton_legs_nd<T>(tp, k.t1, k.t2, ln, ld);
+  meson_prop_nd<T>(P.regge, k.that, M0sq, wtn, wtd);  // ff^2 / (p^2 - M0^2)
+  meson_prop_nd<T>(P.regge, k.uhat, M0sq, wun, wud);
+  const T at = T(-0.5) + T(0.9) * k.that, au = T(-0.5) + T(0.9) * k.uhat;  // alpha - 1
+  const T com = T(-9.0 * tp.gPNN * tp.gPNN / 16.0) * ln / ld;
+  const T mt = com * wtn * exp(x1 * log(ap * k.s13) + x2 * log(ap * k.s24) + at * vp.lns) /
+               (wtd * k.s13 * k.s24);
+  const T mu = com * wun * exp(x1 * log(ap * k.s14) + x2 * log(ap * k.s23) + au * vp.lns) /
+               (wud * k.s14 * k.s23);
+  const T ph0 = T(-0.5) * (x1 + x2);
+  T snt, cst, snu, csu;
+  sincos_pi(ph0 + at * vp.ph, snt, cst);
+  sincos_pi(ph0 + au * vp.ph, snu, csu);
+  const cx<T> Ct{mt * cst, mt * snt}, Cu{mu * csu, mu * snu};
+  LV<T> a_t[3], b_t[3], a_u[3], b_u[3];
   for (int i = 0; i < 3; ++i) {
-    at[i] = vv_vertex<T>(e3[i], p3, pt, P1, b1, g1, g2);   // upper, t channel
-    bt[i] = vv_vertex<T>(e4[i], p4, mpt, P2, b2, g1, g2);  // lower, t channel
-    au[i] = vv_vertex<T>(e4[i], p4, mpu, P1, b1, g1, g2);  // upper, u channel
-    bu[i] = vv_vertex<T>(e3[i], p3, pu, P2, b2, g1, g2);   // lower, u channel
+    a_t[i] = vv_vertex<T>(e3[i], p3, pt, P1, b1, g1, g2);   // upper, t channel
+    b_t[i] = vv_vertex<T>(e4[i], p4, mpt, P2, b2, g1, g2);  // lower, t channel
+    a_u[i] = vv_vertex<T>(e4[i], p4, mpu, P1, b1, g1, g2);  // upper, u channel
+    b_u[i] = vv_vertex<T>(e3[i], p3, pu, P2, b2, g1, g2);   // lower, u channel
   }
   // M = -i (M_t + M_u)
   for (int i = 0; i < 3; ++i)
     for (int j = 0; j < 3; ++j) {
-      const T dt = ldot(at[i], bt[j]), du = ldot(au[j], bu[i]);
+      const T dt = ldot(a_t[i], b_t[j]), du = ldot(a_u[j], b_u[i]);
       const T re = Ct.re * dt + Cu.re * du, im = Ct.im * dt + Cu.im * du;
       A[3 * i + j] = {im, -re};
     }
@@ -1254,11 +1294,16 @@ struct LoopEvent {
   T p3x, p3y, p4x, p4y;
   T p3p, p3m, p4p, p4m;
   T a1, a2;                 // (P+ - eps)/L, (P- - eps)/L
+  T ia1, ia2;               // 1/(1 - a1), 1/(1 - a2)
   T invL, invL2, L, eps, mp2, m3sq, m4sq;
   ResSums<T> res;           // PP[RESTENSOR]: resonance sums of the tree-level central mass
 };
 
 // Kinematics of one kt-loop point; false when it is kinematically invalid.
+// The light-cone closure x1 = a1 + c2 / (1 - x2), x2 = a2 + c1 / (1 - x1) (solve_x) in two
+// steps: the first from the event's 1/(1 - a_i), the second from r_i = 1/(1 - x_i) of the
+// first, which then serve as 1/(1 - x_i) of the point (c_i = mT_i^2 / L^2 ~ 1e-8: the second
+// step moves x_i by O(c^2) ~ 1e-16 relative, r_i by as little); two reciprocals per point.
 template <typename T>
 GRN_HD bool loop_point_kin(const LoopEvent<T> &e, T kx, T ky, LCKin<T> &kk) {
   const T q1x = e.p1x - kx, q1y = e.p1y - ky;
@@ -1266,19 +1311,22 @@ GRN_HD bool loop_point_kin(const LoopEvent<T> &e, T kx, T ky, LCKin<T> &kk) {
   const T pt1sq = q1x * q1x + q1y * q1y;
   const T pt2sq = q2x * q2x + q2y * q2y;
   const T mT1sq = e.mp2 + pt1sq, mT2sq = e.mp2 + pt2sq;
-  T x1, x2;
-  if (!solve_x<T>(e.a1, e.a2, mT1sq * e.invL2, mT2sq * e.invL2, x1, x2)) return false;
+  const T c1 = mT1sq * e.invL2, c2 = mT2sq * e.invL2;
+  const T r1 = T(1) / (T(1) - (e.a1 + c2 * e.ia2));
+  const T r2 = T(1) / (T(1) - (e.a2 + c1 * e.ia1));
+  const T x1 = e.a1 + c2 * r2, x2 = e.a2 + c1 * r1;
+  if (!((x1 > T(0)) && (x2 > T(0)) && (x1 < T(1)) && (x2 < T(1)))) return false;
   const T p1p = (T(1) - x1) * e.L;
-  const T p1m = mT1sq / p1p;
+  const T p1m = mT1sq * r1 * e.invL;
   const T p2m = (T(1) - x2) * e.L;
-  const T p2p = mT2sq / p2m;
+  const T p2p = mT2sq * r2 * e.invL;
   kk.p1p = p1p; kk.p1m = p1m; kk.p1x = q1x; kk.p1y = q1y;
   kk.p2p = p2p; kk.p2m = p2m; kk.p2x = q2x; kk.p2y = q2y;
   kk.p3p = e.p3p; kk.p3m = e.p3m; kk.p3x = e.p3x; kk.p3y = e.p3y;
   kk.p4p = e.p4p; kk.p4m = e.p4m; kk.p4x = e.p4x; kk.p4y = e.p4y;
   kk.L = e.L; kk.eps = e.eps; kk.mp2 = e.mp2;
-  kk.t1  = -(pt1sq + x1 * x1 * e.mp2) / (T(1) - x1);
-  kk.t2  = -(pt2sq + x2 * x2 * e.mp2) / (T(1) - x2);
+  kk.t1  = -(pt1sq + x1 * x1 * e.mp2) * r1;
+  kk.t2  = -(pt2sq + x2 * x2 * e.mp2) * r2;
   kk.s13 = e.mp2 + e.m3sq + p1p * e.p3m + p1m * e.p3p - T(2) * (q1x * e.p3x + q1y * e.p3y);
   kk.s14 = e.mp2 + e.m4sq + p1p * e.p4m + p1m * e.p4p - T(2) * (q1x * e.p4x + q1y * e.p4y);
   kk.s23 = e.mp2 + e.m3sq + p2p * e.p3m + p2m * e.p3p - T(2) * (q2x * e.p3x + q2y * e.p3y);
@@ -1295,8 +1343,11 @@ GRN_HD bool loop_point_kin(const LoopEvent<T> &e, T kx, T ky, LCKin<T> &kk) {
     const T tx = q1x + e.p4x, ty = q1y + e.p4y;
     kk.uhat    = dp * dm - (tx * tx + ty * ty);
   }
-  q_lightcone<T>(x1, pt1sq, e.mp2, e.L, kk.q1p, kk.q1m);
-  q_lightcone<T>(x2, pt2sq, e.mp2, e.L, kk.q2m, kk.q2p);
+  // q1 = pa - p1: q1+ = x1 L, q1- = -(pT1^2 + x1 mp^2) / ((1 - x1) L) (q_lightcone)
+  kk.q1p = x1 * e.L;
+  kk.q1m = -(pt1sq + x1 * e.mp2) * r1 * e.invL;
+  kk.q2m = x2 * e.L;
+  kk.q2p = -(pt2sq + x2 * e.mp2) * r2 * e.invL;
   return true;
 }
 
@@ -1601,8 +1652,11 @@ GRN_HD void make_loop_event(const Consts &K, const Born &b, LoopEvent<T> &e) {
   e.p1x = T(b.p1x); e.p1y = T(b.p1y); e.p2x = T(b.p2x); e.p2y = T(b.p2y);
   e.p3x = T(b.p3x); e.p3y = T(b.p3y); e.p4x = T(b.p4x); e.p4y = T(b.p4y);
   e.p3p = T(b.p3p); e.p3m = T(b.p3m); e.p4p = T(b.p4p); e.p4m = T(b.p4m);
-  e.a1 = T((b.p3p + b.p4p - K.eps) / K.L);
-  e.a2 = T((b.p3m + b.p4m - K.eps) / K.L);
+  const double a1 = (b.p3p + b.p4p - K.eps) / K.L, a2 = (b.p3m + b.p4m - K.eps) / K.L;
+  e.a1 = T(a1);
+  e.a2 = T(a2);
+  e.ia1 = T(1.0 / (1.0 - a1));
+  e.ia2 = T(1.0 / (1.0 - a2));
   e.L = T(K.L); e.invL2 = T(1.0 / (K.L * K.L)); e.invL = T(1.0 / K.L);
   e.eps = T(K.eps); e.mp2 = T(K.mp2); e.m3sq = T(b.m3sq); e.m4sq = T(b.m4sq);
   if (K.n_res > 0) {
@@ -1750,7 +1804,7 @@ GRN_HD_COLD void born_amps_2xv(const grn_process_params &P, const Consts &K, con
   LV<double> e3[3], e4[3];
   vector_basis<double>(b.p3p, b.p3m, b.p3x, b.p3y, e3);
   vector_basis<double>(b.p4p, b.p4m, b.p4x, b.p4y, e4);
-  tensor_me4_2xv<double>(P, K, k, b.m2, e3, e4, A);
+  tensor_me4_2xv<double>(P, K, k, vector_prop_consts<double>(K.M2prop, b.m2), e3, e4, A);
 }
 
 // Unscreened |M|^2 of the tree-level point (sum over the helicity amplitudes; the four

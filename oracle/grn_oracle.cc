@@ -27,44 +27,78 @@
 
 namespace orc {
 
-using cplx = std::complex<double>;
+// Arithmetic type of the restatement: double, or long double for the extended-precision
+// build (liborc_ld.so) that shows which side of an FP64 disagreement sits nearer the exact
+// value of the reference's own formulas (same inputs and constants, smaller rounding).
+#ifndef ORC_REAL
+#define ORC_REAL double
+#endif
+using real = ORC_REAL;
 
-constexpr double PI       = 3.14159265358979323846264338327950288;
-constexpr double ZERO_EPS = 1e-12;  // MProcess.h: ZERO_EPS used as log(0 + ZERO_EPS)
+using cplx = std::complex<real>;
+// Mixed operations of the complex type with double constants and parameters (needed when
+// real is long double; the double build never selects them).
+template <typename D, typename = std::enable_if_t<std::is_same<D, double>::value &&
+                                                  !std::is_same<real, double>::value>>
+inline cplx operator*(const cplx &a, D b) { return a * real(b); }
+template <typename D, typename = std::enable_if_t<std::is_same<D, double>::value &&
+                                                  !std::is_same<real, double>::value>>
+inline cplx operator*(D b, const cplx &a) { return real(b) * a; }
+template <typename D, typename = std::enable_if_t<std::is_same<D, double>::value &&
+                                                  !std::is_same<real, double>::value>>
+inline cplx operator/(const cplx &a, D b) { return a / real(b); }
+template <typename D, typename = std::enable_if_t<std::is_same<D, double>::value &&
+                                                  !std::is_same<real, double>::value>>
+inline cplx operator/(D b, const cplx &a) { return real(b) / a; }
+template <typename D, typename = std::enable_if_t<std::is_same<D, double>::value &&
+                                                  !std::is_same<real, double>::value>>
+inline cplx operator+(D b, const cplx &a) { return real(b) + a; }
+template <typename D, typename = std::enable_if_t<std::is_same<D, double>::value &&
+                                                  !std::is_same<real, double>::value>>
+inline cplx operator+(const cplx &a, D b) { return a + real(b); }
+template <typename D, typename = std::enable_if_t<std::is_same<D, double>::value &&
+                                                  !std::is_same<real, double>::value>>
+inline cplx operator-(D b, const cplx &a) { return real(b) - a; }
+template <typename D, typename = std::enable_if_t<std::is_same<D, double>::value &&
+                                                  !std::is_same<real, double>::value>>
+inline cplx operator-(const cplx &a, D b) { return a - real(b); }
+
+constexpr real PI       = 3.14159265358979323846264338327950288;
+constexpr real ZERO_EPS = 1e-12;  // MProcess.h: ZERO_EPS used as log(0 + ZERO_EPS)
 // Unit conversions (include/Graniitti/MPDG.h:63-78).
-constexpr double HBAR     = 6.582119514E-25;
-constexpr double C_LIGHT  = 2.99792458E8;
-constexpr double GEV2M    = HBAR * C_LIGHT;
-constexpr double GEV2FM   = GEV2M * 1E15;
-constexpr double GEV2BARN = (GEV2M * GEV2M) / 1E-28;
-constexpr double MPI_SOFT = 0.13957018;  // PDG::mpi used by S3PomAlpha (MPDG.h:56)
+constexpr real HBAR     = 6.582119514E-25;
+constexpr real C_LIGHT  = 2.99792458E8;
+constexpr real GEV2M    = HBAR * C_LIGHT;
+constexpr real GEV2FM   = GEV2M * 1E15;
+constexpr real GEV2BARN = (GEV2M * GEV2M) / 1E-28;
+constexpr real MPI_SOFT = 0.13957018;  // PDG::mpi used by S3PomAlpha (MPDG.h:56)
 
 // Eikonal numerics constants (include/Graniitti/MEikonal.h:27-40).
-constexpr double MIN_KT2 = 1E-6, MAX_KT2 = 25.0;
-constexpr double MIN_BT = 1E-6;
-constexpr double MAX_BT = 10.0 / GEV2FM;
-constexpr double FB_MIN_KT = 1E-9, FB_MAX_KT = 30.0;
+constexpr real MIN_KT2 = 1E-6, MAX_KT2 = 25.0;
+constexpr real MIN_BT = 1E-6;
+constexpr real MAX_BT = 10.0 / GEV2FM;
+constexpr real FB_MIN_KT = 1E-9, FB_MAX_KT = 30.0;
 constexpr int    FB_N = 10000;
 
-inline double sq(double x) { return x * x; }
-inline double msqrt(double x) { return std::sqrt(std::max(0.0, x)); }
+inline real sq(real x) { return x * x; }
+inline real msqrt(real x) { return std::sqrt(std::max<real>(0, x)); }
 
 // ---------------------------------------------------------------------------
 // Minimal 4-vector (px, py, pz, E), metric (+,-,-,-).
 struct V4 {
-  double x = 0, y = 0, z = 0, e = 0;
+  real x = 0, y = 0, z = 0, e = 0;
   V4() {}
-  V4(double x_, double y_, double z_, double e_) : x(x_), y(y_), z(z_), e(e_) {}
+  V4(real x_, real y_, real z_, real e_) : x(x_), y(y_), z(z_), e(e_) {}
   V4     operator+(const V4 &o) const { return V4(x + o.x, y + o.y, z + o.z, e + o.e); }
   V4     operator-(const V4 &o) const { return V4(x - o.x, y - o.y, z - o.z, e - o.e); }
-  double m2() const { return e * e - (x * x + y * y + z * z); }
-  double m() const { const double v = m2(); return v > 0 ? std::sqrt(v) : -std::sqrt(-v); }
-  double pt2() const { return x * x + y * y; }
-  double pt() const { return msqrt(pt2()); }
-  double p3() const { return msqrt(x * x + y * y + z * z); }
-  double rap() const { return 0.5 * std::log((e + z) / (e - z)); }
-  double eta() const { const double p = p3(); return 0.5 * std::log((p + z) / (p - z)); }
-  double mt() const { return msqrt(m2() + pt2()); }
+  real m2() const { return e * e - (x * x + y * y + z * z); }
+  real m() const { const real v = m2(); return v > 0 ? std::sqrt(v) : -std::sqrt(-v); }
+  real pt2() const { return x * x + y * y; }
+  real pt() const { return msqrt(pt2()); }
+  real p3() const { return msqrt(x * x + y * y + z * z); }
+  real rap() const { return 0.5 * std::log((e + z) / (e - z)); }
+  real eta() const { const real p = p3(); return 0.5 * std::log((p + z) / (p - z)); }
+  real mt() const { return msqrt(m2() + pt2()); }
 };
 
 // ---------------------------------------------------------------------------
@@ -72,25 +106,25 @@ struct V4 {
 // form for |x| >= 8, as published in Abramowitz & Stegun (1965) 9.4 and used by
 // the reference's BESSJ0 (libs/extmath.hpp:12-46). The coefficient tables are the
 // published ones; they must be identical for table parity.
-double bessel_j0(double x) {
+real bessel_j0(real x) {
   if (x == 0.0) return 1.0;
-  const double ax = std::fabs(x);
+  const real ax = std::fabs(x);
   if (ax < 8.0) {
-    const double y   = x * x;
-    const double num = 57568490574.0 +
+    const real y   = x * x;
+    const real num = 57568490574.0 +
                        y * (-13362590354.0 + y * (651619640.7 + y * (-11214424.18 +
                        y * (77392.33017 + y * (-184.9052456)))));
-    const double den = 57568490411.0 +
+    const real den = 57568490411.0 +
                        y * (1029532985.0 + y * (9494680.718 + y * (59272.64853 +
                        y * (267.8532712 + y * 1.0))));
     return num / den;
   }
-  const double z  = 8.0 / ax;
-  const double y  = z * z;
-  const double xx = ax - 0.785398164;
-  const double p  = 1.0 + y * (-0.1098628627E-2 + y * (0.2734510407E-4 +
+  const real z  = 8.0 / ax;
+  const real y  = z * z;
+  const real xx = ax - 0.785398164;
+  const real p  = 1.0 + y * (-0.1098628627E-2 + y * (0.2734510407E-4 +
                     y * (-0.2073370639E-5 + y * 0.2093887211E-6)));
-  const double q  = -0.1562499995E-1 + y * (0.1430488765E-3 + y * (-0.6911147651E-5 +
+  const real q  = -0.1562499995E-1 + y * (0.1430488765E-3 + y * (-0.6911147651E-5 +
                     y * (0.7621095161E-6 + y * (-0.9349451520E-7))));
   return std::sqrt(0.636619772 / ax) * (p * std::cos(xx) - z * q * std::sin(xx));
 }
@@ -98,7 +132,7 @@ double bessel_j0(double x) {
 // Composite Simpson 1/3 rule over N+1 equidistant samples, N even
 // (include/Graniitti/MMath.h:378-394).
 template <typename T>
-T simpson13(const std::vector<T> &f, double h) {
+T simpson13(const std::vector<T> &f, real h) {
   const std::size_t N = f.size() - 1;
   T even = 0.0, odd = 0.0;
   for (std::size_t j = 1; j + 1 <= N / 2; ++j) even += f[2 * j];
@@ -108,8 +142,8 @@ T simpson13(const std::vector<T> &f, double h) {
 
 // Simpson 3/8 weights 1,3,3,2,3,3,2,...,3,3,1 over N+1 points, N % 3 == 0
 // (include/Graniitti/MMath.h:502-516).
-std::vector<double> simpson38_weights(int N) {
-  std::vector<double> w(N + 1, 3.0);
+std::vector<real> simpson38_weights(int N) {
+  std::vector<real> w(N + 1, 3.0);
   w[0] = w[N] = 1.0;
   for (int i = 3; i < N; i += 3) w[i] = 2.0;
   return w;
@@ -119,56 +153,56 @@ std::vector<double> simpson38_weights(int N) {
 // Model functions.
 
 // Regge signature factor (src/MForm.cc:382-385).
-cplx regge_eta(double alpha, double sigma) {
+cplx regge_eta(real alpha, real sigma) {
   const cplx i(0, 1);
   return -(1.0 + sigma * std::exp(-i * PI * alpha)) / std::sin(PI * alpha);
 }
 // Linear-trajectory signature factor (src/MForm.cc:394-396).
-cplx regge_eta_linear(double t, double a0, double ap, double sigma) {
+cplx regge_eta_linear(real t, real a0, real ap, real sigma) {
   const cplx i(0, 1);
   return regge_eta(a0, sigma) * std::exp(-i * PI / 2.0 * ap * t);
 }
-// Proton form factor, double pole (src/MForm.cc:433-435).
-double proton_ff(const grn_soft_params &sp, double t) {
+// Proton form factor, real pole (src/MForm.cc:433-435).
+real proton_ff(const grn_soft_params &sp, real t) {
   return (1.0 / (1.0 - t / sp.fc1)) * (1.0 / (1.0 - t / sp.fc2));
 }
 // Pion-loop insert of the non-linear pomeron trajectory (src/MForm.cc:418-427).
-double pion_loop(const grn_soft_params &sp, double tau, double t) {
-  const double sqt = std::sqrt(1.0 + tau);
-  const double fpi = 1.0 / (1.0 - t / sp.fc3);
+real pion_loop(const grn_soft_params &sp, real tau, real t) {
+  const real sqt = std::sqrt(1.0 + tau);
+  const real fpi = 1.0 / (1.0 - t / sp.fc3);
   return (4.0 / tau) * fpi * fpi *
          (2.0 * tau - std::pow(1.0 + tau, 1.5) * std::log((sqt + 1.0) / (sqt - 1.0)) +
           std::log(1.0 / (MPI_SOFT * MPI_SOFT)));
 }
 // Non-linear pomeron trajectory (src/MForm.cc:402-413).
-double pomeron_alpha(const grn_soft_params &sp, double t) {
-  const double beta_pi = (2.0 / 3.0) * sp.gN_P;
-  const double pic     = (beta_pi * beta_pi * MPI_SOFT * MPI_SOFT) / (32.0 * PI * PI * PI);
-  const double h       = pic * pion_loop(sp, 4.0 * MPI_SOFT * MPI_SOFT / std::fabs(t), t);
+real pomeron_alpha(const grn_soft_params &sp, real t) {
+  const real beta_pi = (2.0 / 3.0) * sp.gN_P;
+  const real pic     = (beta_pi * beta_pi * MPI_SOFT * MPI_SOFT) / (32.0 * PI * PI * PI);
+  const real h       = pic * pion_loop(sp, 4.0 * MPI_SOFT * MPI_SOFT / std::fabs(t), t);
   return 1.0 + sp.delta_P + sp.alpha_P * t - h;
 }
 // Single pomeron elastic amplitude (src/MEikonal.cc:139-162), C-even only.
-cplx elastic_amp(const grn_soft_params &sp, double s, double t) {
-  const double F = proton_ff(sp, t);
-  const double a = pomeron_alpha(sp, t);
+cplx elastic_amp(const grn_soft_params &sp, real s, real t) {
+  const real F = proton_ff(sp, t);
+  const real a = pomeron_alpha(sp, t);
   cplx A = sp.gN_P * sp.gN_P * F * F * regge_eta(a, 1.0) * std::pow(s, a);
   if (sp.odderon_on) A += sp.gN_O * sp.gN_O * F * F * regge_eta(a, -1.0) * std::pow(s, a);
   return A;
 }
 
 // Regge propagator sum (s/s0)^alpha(t) with signature factors (src/MRegge.cc:888-906).
-cplx regge_prop(const grn_regge_params &rp, double s, double t) {
+cplx regge_prop(const grn_regge_params &rp, real s, real t) {
   cplx M(0, 0);
   for (int k = 0; k < 3; ++k) {
     if (!rp.active[k]) continue;
-    const double alpha = rp.a0[k] + rp.ap[k] * t;
+    const real alpha = rp.a0[k] + rp.ap[k] * t;
     M += regge_eta_linear(t, rp.a0[k], rp.ap[k], rp.sgn[k]) * std::pow(s / rp.s0, alpha);
   }
   return M;
 }
 // Off-shell meson form factor (src/MRegge.cc:1155-1174).
-double meson_ff(const grn_regge_params &rp, double that, double M2) {
-  const double tp = that - M2;
+real meson_ff(const grn_regge_params &rp, real that, real M2) {
+  const real tp = that - M2;
   switch (rp.offshellFF) {
     case 0: return std::exp(-rp.b_EXP * std::fabs(tp));
     case 1: return std::exp(-rp.b_OREAR * msqrt(std::fabs(tp) + sq(rp.a_OREAR)) +
@@ -185,20 +219,20 @@ struct Event {
                            // (c, d for 4-body central states)
   V4     q;                // intermediate difference momentum (pkt_[0]), <C>
   V4     kq[3];            // <C> with 4 central particles: the difference momenta pkt_[0..2]
-  double dw = 0;           // <F>: 2-body phase-space weight dPhi2 (MFactorized.cc:381)
-  double m2lo = 0, m2hi = 0;  // <F>: central mass^2 window of this point
+  real dw = 0;           // <F>: 2-body phase-space weight dPhi2 (MFactorized.cc:381)
+  real m2lo = 0, m2hi = 0;  // <F>: central mass^2 window of this point
   V4     leaf[4];          // cascades: final-state daughters (central 1: 0, 1; central 2: 2, 3)
-  double t1 = 0, t2 = 0, that = 0, uhat = 0, m2 = 0, Y = 0, Pt = 0;
-  double ss[7][7] = {};
+  real t1 = 0, t2 = 0, that = 0, uhat = 0, m2 = 0, Y = 0, Pt = 0;
+  real ss[7][7] = {};
   // 4-body central states: (q1 - p_i)^2, (q2 - p_i)^2, (q1 - p_i - p_j)^2 (MProcess.cc:1556-1561)
-  double tt1[7] = {}, tt2[7] = {}, ttxy[7][7] = {};
+  real tt1[7] = {}, tt2[7] = {}, ttxy[7][7] = {};
 };
 
 struct Setup {
   grn_process_params p;
-  double             s = 0, sqrt_s = 0;
+  real             s = 0, sqrt_s = 0;
   V4                 pb1, pb2;
-  const double      *msa = nullptr;  // (x, re, im) rows
+  const double      *msa = nullptr;  // (x, re, im) rows (the table as given, double)
   int                n_kt2 = 0;
 };
 
@@ -206,19 +240,19 @@ struct Setup {
 // forward legs carry transverse masses a = m3^2+pt3^2, b = m4^2+pt4^2 and share the
 // energy-momentum (E_R, pz_R) = (sqrt(s) - E5, -pz5); the forward-going root of the
 // two-body problem. Same quantity as kinematics::SolvePz (MKinematics.h:220-229).
-double solve_pz(double m3, double m4, double pt3, double pt4, double pz5, double E5, double s) {
-  const double ER  = std::sqrt(s) - E5;
-  const double pzR = -pz5;
-  const double MR2 = ER * ER - pzR * pzR;
-  const double a   = m3 * m3 + pt3 * pt3;
-  const double b   = m4 * m4 + pt4 * pt4;
-  const double lam = sq(MR2 - a - b) - 4.0 * a * b;
+real solve_pz(real m3, real m4, real pt3, real pt4, real pz5, real E5, real s) {
+  const real ER  = std::sqrt(s) - E5;
+  const real pzR = -pz5;
+  const real MR2 = ER * ER - pzR * pzR;
+  const real a   = m3 * m3 + pt3 * pt3;
+  const real b   = m4 * m4 + pt4 * pt4;
+  const real lam = sq(MR2 - a - b) - 4.0 * a * b;
   return (pzR * (MR2 + a - b) + ER * std::sqrt(lam)) / (2.0 * MR2);
 }
 
 // Energy-momentum conservation check with 1e-6 tolerance (MMath.h:191-198).
 bool check_emc(const V4 &d) {
-  const double eps = 1e-6;
+  const real eps = 1e-6;
   return !(std::fabs(d.x) > eps || std::fabs(d.y) > eps || std::fabs(d.z) > eps || d.e > eps);
 }
 
@@ -254,25 +288,25 @@ bool lorentz_scalars(const Setup &S, Event &ev) {
 
 // Central particles from the 2x2 linear system (MContinuum.cc:438-550, Kf = 2):
 // 2 p_a = q - w, 2 p_b = -q - w with w = p1T + p2T, then (pz, E) from rapidity.
-void central_pair(const V4 &q, const V4 &p1, const V4 &p2, const double m[2], const double y[2],
+void central_pair(const V4 &q, const V4 &p1, const V4 &p2, const real m[2], const real y[2],
                   V4 out[2]) {
-  const double wx = p1.x + p2.x, wy = p1.y + p2.y;
-  const double px[2] = {0.5 * (q.x - wx), 0.5 * (-q.x - wx)};
-  const double py[2] = {0.5 * (q.y - wy), 0.5 * (-q.y - wy)};
+  const real wx = p1.x + p2.x, wy = p1.y + p2.y;
+  const real px[2] = {0.5 * (q.x - wx), 0.5 * (-q.x - wx)};
+  const real py[2] = {0.5 * (q.y - wy), 0.5 * (-q.y - wy)};
   for (int i = 0; i < 2; ++i) {
-    const double mt = msqrt(m[i] * m[i] + px[i] * px[i] + py[i] * py[i]);
+    const real mt = msqrt(m[i] * m[i] + px[i] * px[i] + py[i] * py[i]);
     out[i]          = V4(px[i], py[i], mt * std::sinh(y[i]), mt * std::cosh(y[i]));
   }
 }
 
 // Forward legs from the central system (MContinuum.cc:372-384); false when the
 // event fails the crude energy check or the forward-direction check.
-bool forward_legs(const Setup &S, double pt1, double phi1x, double phi1y, double pt2,
-                  double phi2x, double phi2y, const V4 &sumP, V4 &p1, V4 &p2) {
+bool forward_legs(const Setup &S, real pt1, real phi1x, real phi1y, real pt2,
+                  real phi2x, real phi2y, const V4 &sumP, V4 &p1, V4 &p2) {
   (void)phi1x;
-  const double m1 = S.p.m_beam, m2 = S.p.m_beam;
-  const double p1z = solve_pz(m1, m2, pt1, pt2, sumP.z, sumP.e, S.s);
-  const double p2z = -(sumP.z + p1z);
+  const real m1 = S.p.m_beam, m2 = S.p.m_beam;
+  const real p1z = solve_pz(m1, m2, pt1, pt2, sumP.z, sumP.e, S.s);
+  const real p2z = -(sumP.z + p1z);
   if (p1z < 0 || p2z > 0) return false;
   p1 = V4(phi1x, phi1y, p1z, msqrt(m1 * m1 + pt1 * pt1 + p1z * p1z));
   p2 = V4(phi2x, phi2y, p2z, msqrt(m2 * m2 + pt2 * pt2 + p2z * p2z));
@@ -285,21 +319,21 @@ bool forward_legs(const Setup &S, double pt1, double phi1x, double phi1y, double
 //   2 p0 = q0 - w - p2 - p3,  2 p1 = -q0 - w - p2 - p3,  2 p2 = -q1 - w - p0 - p3,
 //   2 p3 = -q2 - w - p0 - p1,  w = p1T + p2T,
 // solved here by Gaussian elimination; (pz, E) from the rapidities and masses.
-void central_four(const V4 *q, const V4 &p1, const V4 &p2, const double *m, const double *y,
+void central_four(const V4 *q, const V4 &p1, const V4 &p2, const real *m, const real *y,
                   V4 *out) {
-  double Mx[4][5], My[4][5];
-  const double coef[4][4] = {{2, 0, 1, 1}, {0, 2, 1, 1}, {1, 0, 2, 1}, {1, 1, 0, 2}};
-  const double wx = p1.x + p2.x, wy = p1.y + p2.y;
-  const double bx[4] = {q[0].x - wx, -q[0].x - wx, -q[1].x - wx, -q[2].x - wx};
-  const double by[4] = {q[0].y - wy, -q[0].y - wy, -q[1].y - wy, -q[2].y - wy};
+  real Mx[4][5], My[4][5];
+  const real coef[4][4] = {{2, 0, 1, 1}, {0, 2, 1, 1}, {1, 0, 2, 1}, {1, 1, 0, 2}};
+  const real wx = p1.x + p2.x, wy = p1.y + p2.y;
+  const real bx[4] = {q[0].x - wx, -q[0].x - wx, -q[1].x - wx, -q[2].x - wx};
+  const real by[4] = {q[0].y - wy, -q[0].y - wy, -q[1].y - wy, -q[2].y - wy};
   for (int i = 0; i < 4; ++i) {
     for (int j = 0; j < 4; ++j) Mx[i][j] = My[i][j] = coef[i][j];
     Mx[i][4] = bx[i];
     My[i][4] = by[i];
   }
-  double px[4], py[4];
+  real px[4], py[4];
   for (auto *Mp : {&Mx, &My}) {
-    double (&M)[4][5] = *Mp;
+    real (&M)[4][5] = *Mp;
     for (int c = 0; c < 4; ++c) {
       int piv = c;
       for (int r = c + 1; r < 4; ++r)
@@ -307,47 +341,49 @@ void central_four(const V4 *q, const V4 &p1, const V4 &p2, const double *m, cons
       for (int k = 0; k < 5; ++k) std::swap(M[c][k], M[piv][k]);
       for (int r = 0; r < 4; ++r) {
         if (r == c) continue;
-        const double f = M[r][c] / M[c][c];
+        const real f = M[r][c] / M[c][c];
         for (int k = 0; k < 5; ++k) M[r][k] -= f * M[c][k];
       }
     }
-    double *dst = Mp == &Mx ? px : py;
+    real *dst = Mp == &Mx ? px : py;
     for (int i = 0; i < 4; ++i) dst[i] = M[i][4] / M[i][i];
   }
   for (int i = 0; i < 4; ++i) {
-    const double mt = msqrt(m[i] * m[i] + px[i] * px[i] + py[i] * py[i]);
+    const real mt = msqrt(m[i] * m[i] + px[i] * px[i] + py[i] * py[i]);
     out[i]          = V4(px[i], py[i], mt * std::sinh(y[i]), mt * std::cosh(y[i]));
   }
 }
 
 // BNRandomKin + BNBuildKin for four central particles (MContinuum.cc:276-435): forward legs
 // u[0..3], kt u[4..6], azimuths u[7..9], rapidities u[10..13].
-bool build_kinematics_c4(const Setup &S, const double *u, Event &ev) {
+bool build_kinematics_c4(const Setup &S, const real *u, Event &ev) {
   const grn_gencuts &g = S.p.gcuts;
-  const double lo  = std::log(g.fpt_min + ZERO_EPS);
-  const double hi  = std::log(g.fpt_max);
-  const double pt1 = std::exp(lo + (hi - lo) * u[0]);
-  const double pt2 = std::exp(lo + (hi - lo) * u[1]);
-  const double phi1 = 2.0 * PI * u[2];
-  const double phi2 = 2.0 * PI * u[3];
+  const real lo  = std::log(g.fpt_min + ZERO_EPS);
+  const real hi  = std::log(g.fpt_max);
+  const real pt1 = std::exp(lo + (hi - lo) * u[0]);
+  const real pt2 = std::exp(lo + (hi - lo) * u[1]);
+  const real phi1 = 2.0 * PI * u[2];
+  const real phi2 = 2.0 * PI * u[3];
   for (int i = 0; i < 3; ++i) {
-    const double kt = g.kt_min + (g.kt_max - g.kt_min) * u[4 + i];
-    const double ph = 2.0 * PI * u[7 + i];
+    const real kt = g.kt_min + (g.kt_max - g.kt_min) * u[4 + i];
+    const real ph = 2.0 * PI * u[7 + i];
     ev.kq[i] = V4(kt * std::cos(ph), kt * std::sin(ph), 0, 0);
   }
-  double y[4];
+  real y[4];
   for (int i = 0; i < 4; ++i) y[i] = g.rap_min + (g.rap_max - g.rap_min) * u[10 + i];
   V4 p1(pt1 * std::cos(phi1), pt1 * std::sin(phi1), 0, 0);
   V4 p2(pt2 * std::cos(phi2), pt2 * std::sin(phi2), 0, 0);
   V4 c[4];
-  central_four(ev.kq, p1, p2, S.p.m_central, y, c);
+  real mc[4];
+  for (int i = 0; i < 4; ++i) mc[i] = S.p.m_central[i];
+  central_four(ev.kq, p1, p2, mc, y, c);
   const V4 sumP = c[0] + c[1] + c[2] + c[3];
   if (sumP.e > S.sqrt_s) return false;
   if (!forward_legs(S, pt1, p1.x, p1.y, pt2, p2.x, p2.y, sumP, p1, p2)) return false;
   ev.pf[0] = sumP;
   ev.pf[1] = p1;
   ev.pf[2] = p2;
-  double msum = 0;
+  real msum = 0;
   for (int i = 0; i < 4; ++i) {
     ev.pf[3 + i] = c[i];
     ev.leaf[i]   = c[i];
@@ -358,21 +394,21 @@ bool build_kinematics_c4(const Setup &S, const double *u, Event &ev) {
   return lorentz_scalars(S, ev);
 }
 
-void cascade_masses(const grn_process_params &p, const double *u, double &m3, double &m4);
-void cascade_decays(const Setup &S, const double *u, double m3, double m4, Event &ev);
+void cascade_masses(const grn_process_params &p, const real *u, real &m3, real &m4);
+void cascade_decays(const Setup &S, const real *u, real m3, real m4, Event &ev);
 
-bool build_kinematics(const Setup &S, const double *u, Event &ev) {
+bool build_kinematics(const Setup &S, const real *u, Event &ev) {
   if (S.p.n_central == 4) return build_kinematics_c4(S, u, ev);
   const grn_gencuts &g = S.p.gcuts;
-  const double lo  = std::log(g.fpt_min + ZERO_EPS);
-  const double hi  = std::log(g.fpt_max);
-  const double pt1 = std::exp(lo + (hi - lo) * u[0]);
-  const double pt2 = std::exp(lo + (hi - lo) * u[1]);
-  const double phi1 = 2.0 * PI * u[2];
-  const double phi2 = 2.0 * PI * u[3];
-  const double kt   = g.kt_min + (g.kt_max - g.kt_min) * u[4];
-  const double phik = 2.0 * PI * u[5];
-  const double y[2] = {g.rap_min + (g.rap_max - g.rap_min) * u[6],
+  const real lo  = std::log(g.fpt_min + ZERO_EPS);
+  const real hi  = std::log(g.fpt_max);
+  const real pt1 = std::exp(lo + (hi - lo) * u[0]);
+  const real pt2 = std::exp(lo + (hi - lo) * u[1]);
+  const real phi1 = 2.0 * PI * u[2];
+  const real phi2 = 2.0 * PI * u[3];
+  const real kt   = g.kt_min + (g.kt_max - g.kt_min) * u[4];
+  const real phik = 2.0 * PI * u[5];
+  const real y[2] = {g.rap_min + (g.rap_max - g.rap_min) * u[6],
                        g.rap_min + (g.rap_max - g.rap_min) * u[7]};
 
   V4 p1(pt1 * std::cos(phi1), pt1 * std::sin(phi1), 0, 0);
@@ -381,7 +417,7 @@ bool build_kinematics(const Setup &S, const double *u, Event &ev) {
 
   // central masses: the stable particles' masses, or the off-shell masses of a cascade
   // (BNRandomKin: GetOffShellMass of each first-level particle)
-  double m[2] = {S.p.m_central[0], S.p.m_central[1]};
+  real m[2] = {S.p.m_central[0], S.p.m_central[1]};
   if (S.p.n_decay == 2) cascade_masses(S.p, u, m[0], m[1]);
   V4 c[2];
   central_pair(ev.q, p1, p2, m, y, c);
@@ -405,19 +441,19 @@ bool build_kinematics(const Setup &S, const double *u, Event &ev) {
 // Relativistic Breit-Wigner mass by inverse CDF in m^2, truncated to [max(M_MIN, m0 - n W),
 // m0 + n W] with n = OFFSHELL widths (MRandom::RelativisticBWRandom, src/MRandom.cc:82-104),
 // from the uniform R; n = 0 gives the pole mass.
-double bw_mass(double m0, double W, double n, double M_MIN, double R) {
+real bw_mass(real m0, real W, real n, real M_MIN, real R) {
   if (W < 1e-40) return m0;
-  const double m2    = m0 * m0;
-  const double m2max = sq(m0 + n * W);
-  const double m2min = std::max(std::max(0.0, M_MIN * M_MIN), sq(m0 - n * W));
-  const double a = std::atan2(m2min - m2, m0 * W), b = std::atan2(m2max - m2, m0 * W);
-  const double v = m2 + m0 * W * std::tan(a + R * (b - a));
-  return std::max(M_MIN, msqrt(v));
+  const real m2    = m0 * m0;
+  const real m2max = sq(m0 + n * W);
+  const real m2min = std::max<real>(std::max<real>(0, M_MIN * M_MIN), sq(m0 - n * W));
+  const real a = std::atan2(m2min - m2, m0 * W), b = std::atan2(m2max - m2, m0 * W);
+  const real v = m2 + m0 * W * std::tan(a + R * (b - a));
+  return std::max<real>(M_MIN, msqrt(v));
 }
 
 // OFFSHELL of a cascade: the process command's value, else 5 widths
 // (include/Graniitti/MProcess.h:363, MProcess::SetOFFSHELL).
-double offshell_widths(const grn_process_params &p) { return p.offshell_user ? p.offshell : 5.0; }
+real offshell_widths(const grn_process_params &p) { return p.offshell_user ? p.offshell : 5.0; }
 
 // First hypercube coordinate of the cascade decays: after the 8 of the 2-body point and,
 // unless OFFSHELL = 0, the two Breit-Wigner mass draws.
@@ -431,8 +467,8 @@ int point_dim(const grn_process_params &p) {
 
 // Off-shell masses of the two central particles of a cascade (GetOffShellMass, the
 // daughters' mass sum + 1e-5 GeV bounding the Breit-Wigner from below) from u[8], u[9].
-void cascade_masses(const grn_process_params &p, const double *u, double &m3, double &m4) {
-  const double n = offshell_widths(p);
+void cascade_masses(const grn_process_params &p, const real *u, real &m3, real &m4) {
+  const real n = offshell_widths(p);
   m3 = p.m_central[0];
   m4 = p.m_central[1];
   if (n > 0) {
@@ -444,19 +480,19 @@ void cascade_masses(const grn_process_params &p, const double *u, double &m3, do
 // 2-body decay in the mother's rest frame with given (cos theta, phi), boosted to
 // the lab (TwoBodyPhaseSpace + Isotropic + LorentzBoost,
 // include/Graniitti/MKinematics.h:294-298, 384-459). Returns dPhi2 (MKinematics.h:267).
-double two_body(const V4 &mother, double M0, double m3, double m4, double ct, double phi,
+real two_body(const V4 &mother, real M0, real m3, real m4, real ct, real phi,
                 V4 &p3, V4 &p4) {
-  const double x = M0, y = m3, z = m4;
-  const double pn = msqrt((x - y - z) * (x + y + z) * (x + y - z) * (x - y + z)) / (2.0 * x);
-  const double st = msqrt(1.0 - ct * ct);
-  const double k[3] = {pn * st * std::cos(phi), pn * st * std::sin(phi), pn * ct};
+  const real x = M0, y = m3, z = m4;
+  const real pn = msqrt((x - y - z) * (x + y + z) * (x + y - z) * (x - y + z)) / (2.0 * x);
+  const real st = msqrt(1.0 - ct * ct);
+  const real k[3] = {pn * st * std::cos(phi), pn * st * std::sin(phi), pn * ct};
   V4 d[2] = {V4(k[0], k[1], k[2], msqrt(m3 * m3 + pn * pn)),
              V4(-k[0], -k[1], -k[2], msqrt(m4 * m4 + pn * pn))};
-  const double b[3] = {mother.x / mother.e, mother.y / mother.e, mother.z / mother.e};
-  const double gam = mother.e / M0;
+  const real b[3] = {mother.x / mother.e, mother.y / mother.e, mother.z / mother.e};
+  const real gam = mother.e / M0;
   for (V4 &p : d) {
-    const double k1 = b[0] * p.x + b[1] * p.y + b[2] * p.z;
-    const double k2 = gam * (gam * k1 / (1.0 + gam) + p.e);
+    const real k1 = b[0] * p.x + b[1] * p.y + b[2] * p.z;
+    const real k2 = gam * (gam * k1 / (1.0 + gam) + p.e);
     p = V4(p.x + k2 * b[0], p.y + k2 * b[1], p.z + k2 * b[2], gam * (p.e + k1));
   }
   p3 = d[0];
@@ -467,8 +503,8 @@ double two_body(const V4 &mother, double M0, double m3, double m4, double ct, do
 // Isotropic two-body decays of the two central particles of a cascade, (cos theta, phi) from
 // u[dec0..dec0 + 3] (ConstructDecayKinematics, src/MProcess.cc:1231-1283: TwoBodyPhaseSpace
 // with FlatIsotropic draws in the mother's rest frame).
-void cascade_decays(const Setup &S, const double *u, double m3, double m4, Event &ev) {
-  const double *v = u + decay_coord(S.p);
+void cascade_decays(const Setup &S, const real *u, real m3, real m4, Event &ev) {
+  const real *v = u + decay_coord(S.p);
   two_body(ev.pf[3], m3, S.p.m_daughter[0], S.p.m_daughter[1], 2.0 * v[0] - 1.0, 2.0 * PI * v[1],
            ev.leaf[0], ev.leaf[1]);
   two_body(ev.pf[4], m4, S.p.m_daughter[2], S.p.m_daughter[3], 2.0 * v[2] - 1.0, 2.0 * PI * v[3],
@@ -477,11 +513,11 @@ void cascade_decays(const Setup &S, const double *u, double m3, double m4, Event
 
 // LorentzBoost (include/Graniitti/MKinematics.h:384-401), sign +1: p from the rest frame of
 // the system b (mass M0) to the frame where b has its given momentum.
-V4 boost_from_rest(const V4 &b, double M0, const V4 &p) {
-  const double bx = b.x / b.e, by = b.y / b.e, bz = b.z / b.e;
-  const double gam = b.e / M0;
-  const double k1  = bx * p.x + by * p.y + bz * p.z;
-  const double k2  = gam * (gam * k1 / (1.0 + gam) + p.e);
+V4 boost_from_rest(const V4 &b, real M0, const V4 &p) {
+  const real bx = b.x / b.e, by = b.y / b.e, bz = b.z / b.e;
+  const real gam = b.e / M0;
+  const real k1  = bx * p.x + by * p.y + bz * p.z;
+  const real k2  = gam * (gam * k1 / (1.0 + gam) + p.e);
   return V4(p.x + k2 * bx, p.y + k2 * by, p.z + k2 * bz, gam * (p.e + k1));
 }
 
@@ -489,28 +525,28 @@ V4 boost_from_rest(const V4 &b, double M0, const V4 &p) {
 // include/Graniitti/MKinematics.h:523-691) for N = 4, the reference's generator draws taken
 // from r: r[0], r[1] the intermediate masses (sorted), then (cos theta, phi) pairs for
 // particles 3, 2, 1. Returns the weight prod(p*) x volume, or -1.
-double n_body(const V4 &mother, double M0, const double *m, const double *r, V4 *p) {
+real n_body(const V4 &mother, real M0, const real *m, const real *r, V4 *p) {
   const int N = 4;
-  double sum[N];
+  real sum[N];
   for (int i = 0; i < N; ++i) sum[i] = (i ? sum[i - 1] : 0.0) + m[i];
-  const double D = M0 - sum[N - 1];
+  const real D = M0 - sum[N - 1];
   if (!(D > 0)) return -1.0;
-  double rv[2] = {r[0], r[1]};
+  real rv[2] = {r[0], r[1]};
   std::sort(rv, rv + 2);
-  const double Meff[N] = {m[0], sum[1] + rv[0] * D, sum[2] + rv[1] * D, M0};
-  double pn[N] = {0, 0, 0, 0};
-  double w = 1.0;
+  const real Meff[N] = {m[0], sum[1] + rv[0] * D, sum[2] + rv[1] * D, M0};
+  real pn[N] = {0, 0, 0, 0};
+  real w = 1.0;
   for (int i = 1; i < N; ++i) {
-    const double x = Meff[i], y = Meff[i - 1], z = m[i];
+    const real x = Meff[i], y = Meff[i - 1], z = m[i];
     pn[i] = msqrt((x - y - z) * (x + y + z) * (x + y - z) * (x - y + z)) / (2.0 * x);
     w *= pn[i];
   }
-  const double volume = 1.0 / (2.0 * std::pow(2.0 * PI, 2 * N - 3)) * std::pow(D, N - 2) / 2.0 / M0;
+  const real volume = 1.0 / (2.0 * std::pow(2.0 * PI, 2 * N - 3)) * std::pow(D, N - 2) / 2.0 / M0;
   V4 k = mother;
   for (int i = N - 1, j = 2; i >= 1; --i, j += 2) {
-    const double ct = 2.0 * r[j] - 1.0;
-    const double st = msqrt(1.0 - ct * ct);
-    const double ph = 2.0 * PI * r[j + 1];
+    const real ct = 2.0 * r[j] - 1.0;
+    const real st = msqrt(1.0 - ct * ct);
+    const real ph = 2.0 * PI * r[j + 1];
     const V4 q(pn[i] * st * std::cos(ph), pn[i] * st * std::sin(ph), pn[i] * ct,
                msqrt(m[i] * m[i] + pn[i] * pn[i]));
     p[i] = boost_from_rest(k, k.m(), q);
@@ -522,28 +558,28 @@ double n_body(const V4 &mother, double M0, const double *m, const double *r, V4 
 
 // B51RandomKin + B51BuildKin for a 2-body central state, decay angles taken from
 // u[6] (cos theta = 2 u6 - 1) and u[7] (phi = 2 pi u7) (MFactorized.cc:245-412).
-bool build_kinematics_F(const Setup &S, const double *u, Event &ev) {
+bool build_kinematics_F(const Setup &S, const real *u, Event &ev) {
   const grn_gencuts &g = S.p.gcuts;
-  const double lo  = std::log(g.fpt_min + ZERO_EPS);
-  const double hi  = std::log(g.fpt_max);
-  const double pt1 = std::exp(lo + (hi - lo) * u[0]);
-  const double pt2 = std::exp(lo + (hi - lo) * u[1]);
-  const double phi1 = 2.0 * PI * u[2];
-  const double phi2 = 2.0 * PI * u[3];
-  const double yX   = g.Y_min + (g.Y_max - g.Y_min) * u[4];
-  double m3 = S.p.m_central[0], m4 = S.p.m_central[1];
+  const real lo  = std::log(g.fpt_min + ZERO_EPS);
+  const real hi  = std::log(g.fpt_max);
+  const real pt1 = std::exp(lo + (hi - lo) * u[0]);
+  const real pt2 = std::exp(lo + (hi - lo) * u[1]);
+  const real phi1 = 2.0 * PI * u[2];
+  const real phi2 = 2.0 * PI * u[3];
+  const real yX   = g.Y_min + (g.Y_max - g.Y_min) * u[4];
+  real m3 = S.p.m_central[0], m4 = S.p.m_central[1];
   if (S.p.n_central == 4) m4 = S.p.m_central[1] + S.p.m_central[2] + S.p.m_central[3];
   if (S.p.n_decay == 2) cascade_masses(S.p, u, m3, m4);  // off-shell central masses
-  const double Mmin = std::max(m3 + m4 + 1e-4, g.M_min);
-  const double Mmax = std::min(S.sqrt_s - (S.pb1.m() + S.pb2.m()), g.M_max);
+  const real Mmin = std::max<real>(m3 + m4 + 1e-4, g.M_min);
+  const real Mmax = std::min<real>(S.sqrt_s - (S.pb1.m() + S.pb2.m()), g.M_max);
   if (!(Mmin < Mmax)) return false;
-  const double m2X  = Mmin * Mmin + (Mmax * Mmax - Mmin * Mmin) * u[5];
+  const real m2X  = Mmin * Mmin + (Mmax * Mmax - Mmin * Mmin) * u[5];
   ev.m2lo = Mmin * Mmin;
   ev.m2hi = Mmax * Mmax;
   V4 p1(pt1 * std::cos(phi1), pt1 * std::sin(phi1), 0, 0);
   V4 p2(pt2 * std::cos(phi2), pt2 * std::sin(phi2), 0, 0);
   V4 pX(-(p1.x + p2.x), -(p1.y + p2.y), 0, 0);
-  const double mtX = msqrt(m2X + pX.pt2());
+  const real mtX = msqrt(m2X + pX.pt2());
   pX.z = mtX * std::sinh(yX);
   pX.e = mtX * std::cosh(yX);
   if (pX.e > S.sqrt_s - 2.0 * S.p.m_beam) return false;
@@ -553,7 +589,9 @@ bool build_kinematics_F(const Setup &S, const double *u, Event &ev) {
   ev.pf[2] = p2;
   if (!check_emc((S.pb1 + S.pb2) - (p1 + p2 + pX))) return false;
   if (S.p.n_central == 4) {
-    ev.dw = n_body(pX, msqrt(m2X), S.p.m_central, u + 6, ev.pf + 3);
+    real mc[4];
+    for (int i = 0; i < 4; ++i) mc[i] = S.p.m_central[i];
+    ev.dw = n_body(pX, msqrt(m2X), mc, u + 6, ev.pf + 3);
     if (!(ev.dw >= 0)) return false;
     for (int k = 0; k < 4; ++k) ev.leaf[k] = ev.pf[3 + k];
     return lorentz_scalars(S, ev);
@@ -566,16 +604,16 @@ bool build_kinematics_F(const Setup &S, const double *u, Event &ev) {
 // LoopKinematics for Kf = 2 (MContinuum.cc:94-161): new forward transverse momenta,
 // central pair re-solved with the tree-level difference momentum, rapidities and
 // masses of the tree-level central particles.
-bool loop_kinematics(const Setup &S, const Event &born, double p1x, double p1y, double p2x,
-                     double p2y, Event &ev) {
+bool loop_kinematics(const Setup &S, const Event &born, real p1x, real p1y, real p2x,
+                     real p2y, Event &ev) {
   const V4 p1T(p1x, p1y, 0, 0), p2T(p2x, p2y, 0, 0);
   if (S.p.phase_space == GRN_PS_FACTORIZED) {
     // MFactorized::LoopKinematics (src/MFactorized.cc:84-139): the central system keeps
     // its mass and rapidity, its pT balances the new forward legs; the decay products
     // keep their tree-level momenta.
-    const double mX = born.pf[0].m(), yX = born.pf[0].rap();
+    const real mX = born.pf[0].m(), yX = born.pf[0].rap();
     V4 pX(-(p1x + p2x), -(p1y + p2y), 0, 0);
-    const double mtX = msqrt(mX * mX + pX.pt2());
+    const real mtX = msqrt(mX * mX + pX.pt2());
     pX.z = mtX * std::sinh(yX);
     pX.e = mtX * std::cosh(yX);
     if (pX.e > S.sqrt_s - 2.0 * S.p.m_beam) return false;
@@ -591,7 +629,7 @@ bool loop_kinematics(const Setup &S, const Event &born, double p1x, double p1y, 
   if (S.p.n_central == 4) {
     // MContinuum::LoopKinematics: central transverse momenta re-solved with the tree-level
     // difference momenta, rapidities and masses
-    double m4[4], y4[4];
+    real m4[4], y4[4];
     for (int i = 0; i < 4; ++i) {
       m4[i] = born.pf[3 + i].m();
       y4[i] = born.pf[3 + i].rap();
@@ -609,12 +647,12 @@ bool loop_kinematics(const Setup &S, const Event &born, double p1x, double p1y, 
     if (!check_emc((S.pb1 + S.pb2) - (p1 + p2 + sumP))) return false;
     return lorentz_scalars(S, ev);
   }
-  const double m[2] = {born.pf[3].m(), born.pf[4].m()};
-  const double y[2] = {born.pf[3].rap(), born.pf[4].rap()};
+  const real m[2] = {born.pf[3].m(), born.pf[4].m()};
+  const real y[2] = {born.pf[3].rap(), born.pf[4].rap()};
   V4 c[2];
   central_pair(born.q, p1T, p2T, m, y, c);
   const V4 sumP = c[0] + c[1];
-  const double pt1 = p1T.pt(), pt2 = p2T.pt();
+  const real pt1 = p1T.pt(), pt2 = p2T.pt();
   V4 p1, p2;
   if (!forward_legs(S, pt1, p1x, p1y, pt2, p2x, p2y, sumP, p1, p2)) return false;
   ev.q     = born.q;
@@ -631,10 +669,10 @@ bool loop_kinematics(const Setup &S, const Event &born, double p1x, double p1y, 
 // (MRegge::ME4, src/MRegge.cc:394-438; PomPomProtonVertex 637-644).
 cplx regge_me4(const Setup &S, const Event &ev) {
   const grn_regge_params &rp = S.p.regge;
-  const double M2  = sq(S.p.m_central[0]);
-  const double FFA = S.p.soft.gN_P * proton_ff(S.p.soft, ev.t1);
-  const double FFB = S.p.soft.gN_P * proton_ff(S.p.soft, ev.t2);
-  const double g   = rp.c[0] / S.p.soft.gN_P;
+  const real M2  = sq(S.p.m_central[0]);
+  const real FFA = S.p.soft.gN_P * proton_ff(S.p.soft, ev.t1);
+  const real FFB = S.p.soft.gN_P * proton_ff(S.p.soft, ev.t2);
+  const real g   = rp.c[0] / S.p.soft.gN_P;
   const cplx At = regge_prop(rp, ev.ss[1][3], ev.t1) * FFA * meson_ff(rp, ev.that, M2) * g *
                   (1.0 / (ev.that - M2)) * meson_ff(rp, ev.that, M2) * g *
                   regge_prop(rp, ev.ss[2][4], ev.t2) * FFB;
@@ -651,15 +689,15 @@ cplx regge_me4(const Setup &S, const Event &ev) {
 // particle of the decay list.
 cplx regge_me6(const Setup &S, const Event &ev) {
   const grn_regge_params &rp = S.p.regge;
-  const double MA  = sq(S.p.m_central[0]), MB = sq(S.p.m_central[2]);
-  const double FFA = S.p.soft.gN_P * proton_ff(S.p.soft, ev.t1);
-  const double FFB = S.p.soft.gN_P * proton_ff(S.p.soft, ev.t2);
-  const double g   = rp.c[0] / S.p.soft.gN_P;
+  const real MA  = sq(S.p.m_central[0]), MB = sq(S.p.m_central[2]);
+  const real FFA = S.p.soft.gN_P * proton_ff(S.p.soft, ev.t1);
+  const real FFB = S.p.soft.gN_P * proton_ff(S.p.soft, ev.t2);
+  const real g   = rp.c[0] / S.p.soft.gN_P;
   int perm[4] = {3, 4, 5, 6};
   cplx A(0, 0);
   do {
     const int a = perm[0], b = perm[1], c = perm[2], d = perm[3];
-    const double tab = ev.tt1[a], tbc = ev.ttxy[a][b], tcd = ev.tt2[d];
+    const real tab = ev.tt1[a], tbc = ev.ttxy[a][b], tcd = ev.tt2[d];
     A += regge_prop(rp, ev.ss[1][a], ev.t1) * FFA * meson_ff(rp, tab, MA) * g *
          (1.0 / (tab - MA)) * meson_ff(rp, tbc, MA) * g * regge_prop(rp, ev.ss[b][c], tbc) *
          meson_ff(rp, tbc, MB) * g * (1.0 / (tcd - MB)) * meson_ff(rp, tcd, MB) * g *
@@ -672,15 +710,15 @@ cplx regge_me6(const Setup &S, const Event &ev) {
 // Tensor-pomeron continuum of two pseudoscalars (MTensorPomeron::ME4, "2xS",
 // src/MTensorPomeron.cc:572-898), restated with explicit Lorentz-index sums as the
 // reference contracts them (covariant components, metric diag(+,-,-,-)).
-constexpr double MP_PDG = 0.938272081;  // PDG::mp (include/Graniitti/MPDG.h:54)
+constexpr real MP_PDG = 0.938272081;  // PDG::mp (include/Graniitti/MPDG.h:54)
 
 // Sachs form factors and the Dirac form factor F1 (src/MForm.cc:541-645): Kelly
 // (PRC 70, 068202) or dipole parametrisation.
-double F1_em(double Q2, bool kelly) {
+real F1_em(real Q2, bool kelly) {
   Q2 = std::fabs(Q2);
-  const double tau = Q2 / sq(2.0 * MP_PDG);
-  const double mu  = 2.792847337;
-  double GE, GM;
+  const real tau = Q2 / sq(2.0 * MP_PDG);
+  const real mu  = 2.792847337;
+  real GE, GM;
   if (kelly) {
     GE = (1.0 - 0.24 * tau) / (1.0 + 10.98 * tau + 12.82 * tau * tau + 21.97 * tau * tau * tau);
     GM = mu * (1.0 + 0.12 * tau) / (1.0 + 10.97 * tau + 18.86 * tau * tau + 6.55 * tau * tau * tau);
@@ -691,9 +729,9 @@ double F1_em(double Q2, bool kelly) {
   return 1.0 / (tau + 1.0) * GE + tau / (tau + 1.0) * GM;
 }
 
-typedef std::array<double, 4> L4;
+typedef std::array<real, 4> L4;
 L4 lower(const V4 &p) { return {p.e, -p.x, -p.y, -p.z}; }
-const double G_METRIC[4] = {1.0, -1.0, -1.0, -1.0};
+const real G_METRIC[4] = {1.0, -1.0, -1.0, -1.0};
 
 // Rank-2 vertex tensors (covariant).
 struct T2 {
@@ -713,7 +751,7 @@ T2 vertex_ppP(const grn_process_params &p, const V4 &prime, const V4 &q) {
 T2 vertex_Pss(const grn_process_params &p, const V4 &prime, const V4 &q) {
   const V4     ps = prime + q;
   const L4     l  = lower(ps);
-  const double M2 = ps.m2();
+  const real M2 = ps.m2();
   const cplx   f  = cplx(0, -1) * 2.0 * p.tensor.gPps * (1.0 / (1.0 - (prime - q).m2() / 0.5));
   T2 T;
   for (int u = 0; u < 4; ++u)
@@ -723,8 +761,8 @@ T2 vertex_Pss(const grn_process_params &p, const V4 &prime, const V4 &q) {
 }
 // Pomeron propagator factor 1/(4s) (-i s ap)^(alpha(t)-1) (MTensorPomeron.cc:2288-2298);
 // its index structure g_uk g_vl + g_ul g_vk - g_uv g_kl / 2 is applied in contract().
-cplx pomeron_prop(const grn_process_params &p, double s, double t) {
-  const double a = 1.0 + p.tensor.delta_P + p.tensor.ap_P * t;
+cplx pomeron_prop(const grn_process_params &p, real s, real t) {
+  const real a = 1.0 + p.tensor.delta_P + p.tensor.ap_P * t;
   return 1.0 / (4.0 * s) * std::pow(cplx(0, -s * p.tensor.ap_P), a - 1.0);
 }
 // A_{mu nu} D^{mu nu, alpha beta} B_{alpha beta} as plain index sums.
@@ -734,7 +772,7 @@ cplx contract(const T2 &A, cplx c, const T2 &B) {
     for (int v = 0; v < 4; ++v)
       for (int k = 0; k < 4; ++k)
         for (int l = 0; l < 4; ++l) {
-          const double g = (u == k && v == l ? G_METRIC[u] * G_METRIC[v] : 0.0) +
+          const real g = (u == k && v == l ? G_METRIC[u] * G_METRIC[v] : 0.0) +
                            (u == l && v == k ? G_METRIC[u] * G_METRIC[v] : 0.0) -
                            0.5 * (u == v ? G_METRIC[u] : 0.0) * (k == l ? G_METRIC[k] : 0.0);
           if (g != 0.0) sum += A.c[u][v] * g * B.c[k][l];
@@ -746,7 +784,7 @@ cplx tensor_me4_2xs(const Setup &S, const Event &ev) {
   const grn_process_params &p = S.p;
   const V4 &pa = S.pb1, &pb = S.pb2;
   const V4 &p1 = ev.pf[1], &p2 = ev.pf[2], &p3 = ev.pf[3], &p4 = ev.pf[4];
-  const double M2  = sq(p.m_central[0]);
+  const real M2  = sq(p.m_central[0]);
   const V4     pt  = pa - p1 - p3;
   const V4     pu  = p4 - pa + p1;
   const V4     mp3 = V4(-p3.x, -p3.y, -p3.z, -p3.e);
@@ -768,16 +806,16 @@ cplx tensor_me4_2xs(const Setup &S, const Event &ev) {
 // decay vertex, pomeron propagators and proton vertices, contracted as plain sums over
 // index values (the reference's tensors carry the index positions that make these
 // sums Lorentz contractions).
-inline double gm(int u, int v) { return u == v ? G_METRIC[u] : 0.0; }
-inline double up(const V4 &p, int u) { return u == 0 ? p.e : (u == 1 ? p.x : (u == 2 ? p.y : p.z)); }
-inline double dn(const V4 &p, int u) { return u == 0 ? p.e : -up(p, u); }
+inline real gm(int u, int v) { return u == v ? G_METRIC[u] : 0.0; }
+inline real up(const V4 &p, int u) { return u == 0 ? p.e : (u == 1 ? p.x : (u == 2 ? p.y : p.z)); }
+inline real dn(const V4 &p, int u) { return u == 0 ? p.e : -up(p, u); }
 inline int    i6(int u, int v, int k, int l, int r, int s) {
   return ((((u * 4 + v) * 4 + k) * 4 + l) * 4 + r) * 4 + s;
 }
 
 // Auxiliary tensor R_{abcd} = g_ac g_bd / 2 + g_ad g_bc / 2 + g_ab g_cd / 4 with the sign of
 // the last term as MTensorPomeron::CalcRTensor sets it (src/MTensorPomeron.cc:2563-2564).
-double R_dddd(int a, int b, int c, int d) {
+real R_dddd(int a, int b, int c, int d) {
   return 0.5 * gm(a, c) * gm(b, d) + 0.5 * gm(a, d) * gm(b, c) + 0.25 * gm(a, b) * gm(c, d);
 }
 
@@ -809,11 +847,11 @@ const std::vector<cplx> &ppt_structure0() {
 
 // Mixed-position versions of R (MTensorPomeron::CalcRTensor, :2566-2569): raised indices
 // carry the metric factor of their slot.
-double R_dddu(int a, int b, int c, int d) { return R_dddd(a, b, c, d) * G_METRIC[d]; }
-double R_dduu(int a, int b, int c, int d) {
+real R_dddu(int a, int b, int c, int d) { return R_dddd(a, b, c, d) * G_METRIC[d]; }
+real R_dduu(int a, int b, int c, int d) {
   return R_dddd(a, b, c, d) * G_METRIC[c] * G_METRIC[d];
 }
-double R_uudd(int a, int b, int c, int d) {
+real R_uudd(int a, int b, int c, int d) {
   return R_dddd(a, b, c, d) * G_METRIC[a] * G_METRIC[b];
 }
 inline int i8(int u, int v, int k, int l, int r, int s, int a, int b) {
@@ -823,7 +861,7 @@ inline int i8(int u, int v, int k, int l, int r, int s, int a, int b) {
 // Pre-contracted R products of coupling structures #1, #2 (the FIX1/FIX2/FIX3 tensors of
 // MTensorPomeron::CalcRTensor, :2583-2631).
 struct PPTFix {
-  std::vector<double> T1, T2, T3;
+  std::vector<real> T1, T2, T3;
   PPTFix() : T1(4096, 0.0), T2(65536, 0.0), T3(65536, 0.0) {
     for (int u = 0; u < 4; ++u)
       for (int v = 0; v < 4; ++v)
@@ -868,21 +906,21 @@ const PPTFix &ppt_fix() {
 // Kinematics-dependent coupling structures #1..#6 (iG_PPT_12 :1738-1780, iG_PPT_03
 // :1786-1834, iG_PPT_04 :1839-1906, iG_PPT_05 :1911-1983, iG_PPT_06 :1988-2014), each with its
 // coupling g applied, added into T.
-void ppt_structures(const V4 &q1, const V4 &q2, const double *g, std::vector<cplx> &T) {
-  const double q1q2 = q1.e * q2.e - (q1.x * q2.x + q1.y * q2.y + q1.z * q2.z);
+void ppt_structures(const V4 &q1, const V4 &q2, const real *g, std::vector<cplx> &T) {
+  const real q1q2 = q1.e * q2.e - (q1.x * q2.x + q1.y * q2.y + q1.z * q2.z);
   const PPTFix &F   = ppt_fix();
-  const double  EPS = 1e-6;  // structures with |g| <= 1e-6 are skipped (:1659-1670)
+  const real  EPS = 1e-6;  // structures with |g| <= 1e-6 are skipped (:1659-1670)
   for (int mode = 1; mode <= 2; ++mode) {
     if (!(std::fabs(g[mode]) > EPS)) continue;
     const cplx   f    = cplx(0, -2.0) * g[mode];
-    const double sign = mode == 1 ? -1.0 : 1.0;
+    const real sign = mode == 1 ? -1.0 : 1.0;
     for (int u = 0; u < 4; ++u)
       for (int v = 0; v < 4; ++v)
         for (int k = 0; k < 4; ++k)
           for (int l = 0; l < 4; ++l)
             for (int r = 0; r < 4; ++r)
               for (int s = 0; s < 4; ++s) {
-                double t = q1q2 * F.T1[i6(u, v, k, l, r, s)];
+                real t = q1q2 * F.T1[i6(u, v, k, l, r, s)];
                 for (int a = 0; a < 4; ++a)
                   for (int b = 0; b < 4; ++b) {
                     t += sign * up(q2, a) * dn(q1, b) * F.T2[i8(u, v, k, l, r, s, a, b)];
@@ -894,7 +932,7 @@ void ppt_structures(const V4 &q1, const V4 &q2, const double *g, std::vector<cpl
   }
   if (std::fabs(g[3]) > EPS) {
     const cplx f = cplx(0, -1.0) * g[3];
-    double A[4][4][4] = {}, B[4][4][4] = {};
+    real A[4][4][4] = {}, B[4][4][4] = {};
     for (int u = 0; u < 4; ++u)
       for (int v = 0; v < 4; ++v)
         for (int k = 0; k < 4; ++k)
@@ -908,7 +946,7 @@ void ppt_structures(const V4 &q1, const V4 &q2, const double *g, std::vector<cpl
           for (int l = 0; l < 4; ++l)
             for (int r = 0; r < 4; ++r)
               for (int s = 0; s < 4; ++s) {
-                double t = 0;
+                real t = 0;
                 for (int v1 = 0; v1 < 4; ++v1)
                   for (int l1 = 0; l1 < 4; ++l1)
                     t += (A[u][v][v1] * B[k][l][l1] + A[u][v][l1] * B[k][l][v1]) *
@@ -918,7 +956,7 @@ void ppt_structures(const V4 &q1, const V4 &q2, const double *g, std::vector<cpl
   }
   if (std::fabs(g[4]) > EPS) {
     const cplx f = cplx(0, -2.0) * g[4];
-    double A[4][4][4][4] = {}, B[4][4][4][4] = {}, C[4][4] = {};
+    real A[4][4][4][4] = {}, B[4][4][4][4] = {}, C[4][4] = {};
     for (int u = 0; u < 4; ++u)
       for (int v = 0; v < 4; ++v)
         for (int k = 0; k < 4; ++k)
@@ -946,7 +984,7 @@ void ppt_structures(const V4 &q1, const V4 &q2, const double *g, std::vector<cpl
   }
   if (std::fabs(g[5]) > EPS) {
     const cplx f = cplx(0, 1.0) * g[5];
-    double A[4][4][4][4] = {}, C[4][4][4][4] = {}, B[4][4] = {}, D[4][4] = {};
+    real A[4][4][4][4] = {}, C[4][4][4][4] = {}, B[4][4] = {}, D[4][4] = {};
     for (int u = 0; u < 4; ++u)
       for (int v = 0; v < 4; ++v)
         for (int r = 0; r < 4; ++r)
@@ -977,7 +1015,7 @@ void ppt_structures(const V4 &q1, const V4 &q2, const double *g, std::vector<cpl
   }
   if (std::fabs(g[6]) > EPS) {
     const cplx f = cplx(0, -2.0) * g[6];
-    double A[4][4] = {}, B[4][4] = {}, C[4][4] = {};
+    real A[4][4] = {}, B[4][4] = {}, C[4][4] = {};
     for (int a = 0; a < 4; ++a)
       for (int b = 0; b < 4; ++b)
         for (int c = 0; c < 4; ++c)
@@ -998,8 +1036,8 @@ void ppt_structures(const V4 &q1, const V4 &q2, const double *g, std::vector<cpl
 
 // Resonance form factor exp(-(q^2 - M0^2)^2 / Lambda^4) (MTensorPomeron::F, :2489) and the
 // pion-electromagnetic-type FM(q^2) = 1 / (1 - q^2 / Lambda^2) with Lambda^2 = 1 (:2485).
-double ff_res(double q2, double M0) { return std::exp(-sq(q2 - M0 * M0)); }
-double ff_M(double q2) { return 1.0 / (1.0 - q2 / 1.0); }
+real ff_res(real q2, real M0) { return std::exp(-sq(q2 - M0 * M0)); }
+real ff_M(real q2) { return 1.0 / (1.0 - q2 / 1.0); }
 
 cplx tensor_me3(const Setup &S, const Event &ev) {
   const grn_process_params &p = S.p;
@@ -1019,7 +1057,7 @@ cplx tensor_me3(const Setup &S, const Event &ev) {
       cplx s1(0, 0), s2(0, 0);
       for (int u = 0; u < 4; ++u)
         for (int v = 0; v < 4; ++v) {
-          const double g = gm(u, a) * gm(v, b) + gm(u, b) * gm(v, a) - 0.5 * gm(u, v) * gm(a, b);
+          const real g = gm(u, a) * gm(v, b) + gm(u, b) * gm(v, a) - 0.5 * gm(u, v) * gm(a, b);
           if (g == 0.0) continue;
           s1 += G1a.c[u][v] * g;
           s2 += G2b.c[u][v] * g;
@@ -1027,13 +1065,13 @@ cplx tensor_me3(const Setup &S, const Event &ev) {
       X1[a][b] = c1 * s1;
       X2[a][b] = c2 * s2;
     }
-  const double m2   = X.m2();
-  const double Ft   = ff_M(q1.m2()) * ff_M(q2.m2());  // times F((q1+q2)^2, M0) per resonance
+  const real m2   = X.m2();
+  const real Ft   = ff_M(q1.m2()) * ff_M(q2.m2());  // times F((q1+q2)^2, M0) per resonance
   const V4     q12  = q1 + q2;
   cplx         A(0, 0);
   for (int r = 0; r < p.n_res; ++r) {
     const grn_resonance &R = p.res[r];
-    const double F_tilde   = Ft * ff_res(q12.m2(), R.M);
+    const real F_tilde   = Ft * ff_res(q12.m2(), R.M);
     const cplx   Delta     = 1.0 / cplx(m2 - R.M * R.M, R.M * R.W);
     cplx cvtx[4][4][4][4];
     if (R.J == 2) {
@@ -1042,7 +1080,7 @@ cplx tensor_me3(const Setup &S, const Event &ev) {
       auto ghat = [&](int u, int v) { return -gm(u, v) + up(X, u) * up(X, v) / m2; };
       const V4   k   = p3 - p4;
       const cplx fd  = cplx(0, -1) * R.g_decay / 2.0 * ff_res((p3 + p4).m2(), R.M);
-      const double k2 = k.m2();
+      const real k2 = k.m2();
       cplx dec[4][4];
       for (int u = 0; u < 4; ++u)
         for (int v = 0; v < 4; ++v) dec[u][v] = fd * (dn(k, u) * dn(k, v) - 0.25 * gm(u, v) * k2);
@@ -1061,7 +1099,9 @@ cplx tensor_me3(const Setup &S, const Event &ev) {
       const std::vector<cplx> &G0 = ppt_structure0();
       std::vector<cplx>        Gt(4096);
       for (int i = 0; i < 4096; ++i) Gt[i] = G0[i] * R.g_tensor[0];
-      ppt_structures(q1, q2, R.g_tensor, Gt);
+      real gt[7];
+      for (int j = 0; j < 7; ++j) gt[j] = R.g_tensor[j];
+      ppt_structures(q1, q2, gt, Gt);
       for (int u = 0; u < 4; ++u)
         for (int v = 0; v < 4; ++v)
           for (int k_ = 0; k_ < 4; ++k_)
@@ -1074,14 +1114,14 @@ cplx tensor_me3(const Setup &S, const Event &ev) {
     } else {
       // scalar: (g0 iG_PPS_0 + iG_PPS_1) F_tilde (:1492-1571) x iD_MES (:2383-2387) x
       // iG_f0ss (:2028-2038)
-      const double q1q2 = q1.e * q2.e - (q1.x * q2.x + q1.y * q2.y + q1.z * q2.z);
+      const real q1q2 = q1.e * q2.e - (q1.x * q2.x + q1.y * q2.y + q1.z * q2.z);
       const cplx   f1   = cplx(0, 1) * R.g_tensor[1] / 2.0;
       const cplx   tail = cplx(0, 1) * Delta * cplx(0, 1) * R.g_decay * ff_res((p3 + p4).m2(), R.M);
       for (int u = 0; u < 4; ++u)
         for (int v = 0; v < 4; ++v)
           for (int k_ = 0; k_ < 4; ++k_)
             for (int l = 0; l < 4; ++l) {
-              const double gg = gm(u, k_) * gm(v, l) + gm(u, l) * gm(v, k_);
+              const real gg = gm(u, k_) * gm(v, l) + gm(u, l) * gm(v, k_);
               const cplx   t0 = cplx(0, 1) * (gg - 0.5 * gm(u, v) * gm(k_, l));
               const cplx   t1 = f1 * (dn(q1, k_) * dn(q2, u) * gm(v, l) + dn(q1, k_) * dn(q2, v) * gm(u, l) +
                                     dn(q1, l) * dn(q2, u) * gm(v, k_) + dn(q1, l) * dn(q2, v) * gm(u, k_) -
@@ -1105,13 +1145,13 @@ cplx tensor_me3(const Setup &S, const Event &ev) {
 typedef std::array<std::array<std::array<std::array<cplx, 4>, 4>, 4>, 4> T4;
 
 // Gamma^(0) and Gamma^(2) of the pomeron-vector-vector vertex (:2500-2529).
-double vv_gamma0(const V4 &k1, const V4 &k2, int u, int v, int k, int l) {
-  const double k1k2 = k1.e * k2.e - (k1.x * k2.x + k1.y * k2.y + k1.z * k2.z);
+real vv_gamma0(const V4 &k1, const V4 &k2, int u, int v, int k, int l) {
+  const real k1k2 = k1.e * k2.e - (k1.x * k2.x + k1.y * k2.y + k1.z * k2.z);
   return (k1k2 * gm(u, v) - dn(k2, u) * dn(k1, v)) *
          (dn(k1, k) * dn(k2, l) + dn(k2, k) * dn(k1, l) - 0.5 * k1k2 * gm(k, l));
 }
-double vv_gamma2(const V4 &k1, const V4 &k2, int u, int v, int k, int l) {
-  const double k1k2 = k1.e * k2.e - (k1.x * k2.x + k1.y * k2.y + k1.z * k2.z);
+real vv_gamma2(const V4 &k1, const V4 &k2, int u, int v, int k, int l) {
+  const real k1k2 = k1.e * k2.e - (k1.x * k2.x + k1.y * k2.y + k1.z * k2.z);
   return k1k2 * (gm(u, k) * gm(v, l) + gm(u, l) * gm(v, k)) +
          gm(u, v) * (dn(k1, k) * dn(k2, l) + dn(k2, k) * dn(k1, l)) -
          dn(k1, v) * dn(k2, l) * gm(u, k) - dn(k1, v) * dn(k2, k) * gm(u, l) -
@@ -1135,11 +1175,11 @@ T4 vertex_Pvv(const grn_process_params &p, const V4 &prime, const V4 &q) {
 // Reggeized vector propagator factor -1/(m^2 - M0^2) (e^{i phi} s34 / (4 M0^2))^(alpha - 1)
 // with alpha = 0.5 + 0.9 m^2 (iD_V, :2353-2369); its index structure g^{uv} is applied in
 // the contraction.
-cplx vector_prop(const V4 &p, double M0, double s34) {
-  const double m2    = p.m2();
-  const double alpha = 0.5 + 0.9 * m2;
-  const double sth   = 4.0 * M0 * M0;
-  const double phi   = PI / 2.0 * std::exp((sth - s34) / sth) - PI / 2.0;
+cplx vector_prop(const V4 &p, real M0, real s34) {
+  const real m2    = p.m2();
+  const real alpha = 0.5 + 0.9 * m2;
+  const real sth   = 4.0 * M0 * M0;
+  const real phi   = PI / 2.0 * std::exp((sth - s34) / sth) - PI / 2.0;
   const cplx   R     = std::pow(std::exp(cplx(0, phi)) * s34 / sth, alpha - 1.0);
   return -1.0 / (m2 - M0 * M0) * R;
 }
@@ -1148,22 +1188,22 @@ cplx vector_prop(const V4 &p, double M0, double s34) {
 // components): two transverse unit vectors and the longitudinal (|p|/m, E p^/m)
 // (MDirac::EpsMassiveSpin1, src/MDirac.cc:435-456, in a linear instead of the helicity
 // basis; the sum over states of |amplitude|^2 is the same).
-void vector_basis(const V4 &p, double e[3][4]) {
-  const double P = std::sqrt(p.x * p.x + p.y * p.y + p.z * p.z);
-  const double m = msqrt(p.m2());
-  double n[3] = {0, 0, 1};
+void vector_basis(const V4 &p, real e[3][4]) {
+  const real P = std::sqrt(p.x * p.x + p.y * p.y + p.z * p.z);
+  const real m = msqrt(p.m2());
+  real n[3] = {0, 0, 1};
   if (P > 1e-12) {
     n[0] = p.x / P;
     n[1] = p.y / P;
     n[2] = p.z / P;
   }
   // first transverse direction: z x n (or x x n near the z axis), normalised
-  double a[3] = {0, 0, 1};
+  real a[3] = {0, 0, 1};
   if (std::fabs(n[2]) > 0.9) { a[0] = 1; a[2] = 0; }
-  double t1[3] = {a[1] * n[2] - a[2] * n[1], a[2] * n[0] - a[0] * n[2], a[0] * n[1] - a[1] * n[0]};
-  const double nt = std::sqrt(t1[0] * t1[0] + t1[1] * t1[1] + t1[2] * t1[2]);
-  for (double &x : t1) x /= nt;
-  const double t2[3] = {n[1] * t1[2] - n[2] * t1[1], n[2] * t1[0] - n[0] * t1[2],
+  real t1[3] = {a[1] * n[2] - a[2] * n[1], a[2] * n[0] - a[0] * n[2], a[0] * n[1] - a[1] * n[0]};
+  const real nt = std::sqrt(t1[0] * t1[0] + t1[1] * t1[1] + t1[2] * t1[2]);
+  for (real &x : t1) x /= nt;
+  const real t2[3] = {n[1] * t1[2] - n[2] * t1[1], n[2] * t1[0] - n[0] * t1[2],
                         n[0] * t1[1] - n[1] * t1[0]};
   e[0][0] = 0; e[0][1] = t1[0]; e[0][2] = t1[1]; e[0][3] = t1[2];
   e[1][0] = 0; e[1][1] = t2[0]; e[1][2] = t2[1]; e[1][3] = t2[2];
@@ -1175,7 +1215,7 @@ int tensor_me4_2xv(const Setup &S, const Event &ev, cplx *out) {
   const grn_process_params &p = S.p;
   const V4 &pa = S.pb1, &pb = S.pb2;
   const V4 &p1 = ev.pf[1], &p2 = ev.pf[2], &p3 = ev.pf[3], &p4 = ev.pf[4];
-  const double M0 = p.m_central[0], M2 = M0 * M0;
+  const real M0 = p.m_central[0], M2 = M0 * M0;
   const V4     pt  = pa - p1 - p3;
   const V4     pu  = p4 - pa + p1;
   const V4     mp3 = V4(-p3.x, -p3.y, -p3.z, -p3.e);
@@ -1183,14 +1223,14 @@ int tensor_me4_2xv(const Setup &S, const Event &ev, cplx *out) {
   const T2     G1a = vertex_ppP(p, p1, pa);
   const T2     G2b = vertex_ppP(p, p2, pb);
   // X^{ab} = G(mu, nu) iD_P(mu, nu, a, b) for the four pomeron propagators
-  auto legX = [&](const T2 &G, double s, double t, cplx X[4][4]) {
+  auto legX = [&](const T2 &G, real s, real t, cplx X[4][4]) {
     const cplx c = pomeron_prop(p, s, t);
     for (int a = 0; a < 4; ++a)
       for (int b = 0; b < 4; ++b) {
         cplx sum(0, 0);
         for (int u = 0; u < 4; ++u)
           for (int v = 0; v < 4; ++v) {
-            const double g = gm(u, a) * gm(v, b) + gm(u, b) * gm(v, a) - 0.5 * gm(u, v) * gm(a, b);
+            const real g = gm(u, a) * gm(v, b) + gm(u, b) * gm(v, a) - 0.5 * gm(u, v) * gm(a, b);
             if (g != 0.0) sum += G.c[u][v] * g;
           }
         X[a][b] = c * sum;
@@ -1217,7 +1257,7 @@ int tensor_me4_2xv(const Setup &S, const Event &ev, cplx *out) {
   vblock(vertex_Pvv(p, p4, pu), X14, Au);    // Au(rho4, rho1)
   vblock(vertex_Pvv(p, pu, mp3), X23, Bu);   // Bu(rho2, rho3)
   (void)mpt;
-  const double s34 = ev.pf[0].m2();
+  const real s34 = ev.pf[0].m2();
   const cplx   Dt  = vector_prop(pt, M0, s34) * sq(meson_ff(p.regge, pt.m2(), M2));
   const cplx   Du  = vector_prop(pu, M0, s34) * sq(meson_ff(p.regge, pu.m2(), M2));
   cplx M[4][4];
@@ -1231,7 +1271,7 @@ int tensor_me4_2xv(const Setup &S, const Event &ev, cplx *out) {
       }
       M[r3][r4] = cplx(0, -1) * (mt * Dt + mu * Du);
     }
-  double e3[3][4], e4[3][4];
+  real e3[3][4], e4[3][4];
   vector_basis(p3, e3);
   vector_basis(p4, e4);
   for (int i = 0; i < 3; ++i)
@@ -1250,34 +1290,34 @@ int  bare_amps(const Setup &S, const Event &ev, cplx *A);
 
 // Linear interpolation on the kt^2 screening table (IArray1D::Interpolate1D,
 // src/MEikonal.cc:489-512).
-cplx msa_interp(const Setup &S, double a) {
+cplx msa_interp(const Setup &S, real a) {
   const int    N    = S.n_kt2;
-  const double step = (MAX_KT2 - MIN_KT2) / N;
+  const real step = (MAX_KT2 - MIN_KT2) / N;
   if (a < MIN_KT2) a = MIN_KT2;
   int i = static_cast<int>(std::floor((a - MIN_KT2) / step));
   if (i < 0) i = 0;
   if (i >= N) i = N - 1;
   const double *r0 = S.msa + 3 * i, *r1 = S.msa + 3 * (i + 1);
   const cplx    y0(r0[1], r0[2]), y1(r1[1], r1[2]);
-  return y0 + (a - r0[0]) * ((y1 - y0) / (r1[0] - r0[0]));
+  return y0 + (a - real(r0[0])) * ((y1 - y0) / (real(r1[0]) - real(r0[0])));
 }
 
 // Eikonal kt-loop screened |M|^2 (MProcess::S3ScreenedAmp2, src/MProcess.cc:157-288): every
 // helicity amplitude is screened on its own and the |.|^2 are summed.
-double screened_amp2(const Setup &S, const Event &born, const cplx *A0, int nh) {
+real screened_amp2(const Setup &S, const Event &born, const cplx *A0, int nh) {
   const grn_loop_numerics &L = S.p.loop;
-  const double stepKT  = (L.kt_max - L.kt_min) / L.n_kt;
-  const double stepPhi = 2.0 * PI / L.n_phi;
-  const std::vector<double> U = simpson38_weights(L.n_phi);
-  const std::vector<double> V = simpson38_weights(L.n_kt);
+  const real stepKT  = (L.kt_max - L.kt_min) / L.n_kt;
+  const real stepPhi = 2.0 * PI / L.n_phi;
+  const std::vector<real> U = simpson38_weights(L.n_phi);
+  const std::vector<real> V = simpson38_weights(L.n_kt);
   cplx sum[9];
   Event lev;
   for (int i = 0; i <= L.n_phi; ++i) {
-    const double phi = i * stepPhi;
+    const real phi = i * stepPhi;
     for (int j = 0; j <= L.n_kt; ++j) {
-      const double kt   = L.kt_min + j * stepKT;
+      const real kt   = L.kt_min + j * stepKT;
       const cplx   Aeik = msa_interp(S, kt * kt);
-      const double kx = kt * std::cos(phi), ky = kt * std::sin(phi);
+      const real kx = kt * std::cos(phi), ky = kt * std::sin(phi);
       if (!loop_kinematics(S, born, born.pf[1].x - kx, born.pf[1].y - ky, born.pf[2].x + kx,
                            born.pf[2].y + ky, lev))
         continue;
@@ -1287,7 +1327,7 @@ double screened_amp2(const Setup &S, const Event &born, const cplx *A0, int nh) 
     }
   }
   const cplx norm = cplx(0, 1) / (8.0 * PI * PI * S.s);
-  double amp2 = 0;
+  real amp2 = 0;
   for (int h = 0; h < nh; ++h)
     amp2 += std::norm(A0[h] + norm * sum[h] * (9.0 * stepPhi * stepKT / 64.0));
   return amp2;
@@ -1301,10 +1341,10 @@ double screened_amp2(const Setup &S, const Event &born, const cplx *A0, int nh) 
 //         [g_decay NORM sqrt(Re Tr f R f^+)],  R = D^+ rho D,  NORM = sqrt(2J+1),
 // f0 (f) the row D^J_{0M}(theta, phi) of q1 (of the first daughter) boosted to the X rest
 // frame, D_{MM'} = D^J_{MM'}(theta_R, phi_R) of the frame; J = 0: both brackets g, g_decay.
-double fact(int n) { double f = 1; for (int i = 2; i <= n; ++i) f *= i; return f; }
+real fact(int n) { real f = 1; for (int i = 2; i <= n; ++i) f *= i; return f; }
 // Wigner small-d by its closed sum over k (as MSpin.cc:927-961 writes it), integer J.
-double wigner_small_d(double theta, int m, int mp, int J) {
-  double s = 0;
+real wigner_small_d(real theta, int m, int mp, int J) {
+  real s = 0;
   for (int k = 0; k <= 2 * J; ++k) {
     if (J - mp - k < 0 || J + m - k < 0 || k + mp - m < 0) continue;
     s += std::pow(-1.0, mp - m + k) /
@@ -1314,23 +1354,23 @@ double wigner_small_d(double theta, int m, int mp, int J) {
   }
   return std::sqrt(fact(J + m) * fact(J - m) * fact(J + mp) * fact(J - mp)) * s;
 }
-cplx wigner_D(double theta, double phi, int m, int mp, int J) {
-  return wigner_small_d(theta, m, mp, J) * std::exp(cplx(0, 1) * double(mp) * phi);
+cplx wigner_D(real theta, real phi, int m, int mp, int J) {
+  return wigner_small_d(theta, m, mp, J) * std::exp(cplx(0, 1) * real(mp) * phi);
 }
 // p in the rest frame of X (kinematics::LorentzBoost with sign -1, MKinematics.h:384-401).
 V4 to_rest(const V4 &X, const V4 &p) {
-  const double M = X.m(), g = X.e / M;
-  const double bx = -X.x / X.e, by = -X.y / X.e, bz = -X.z / X.e;
-  const double k1 = bx * p.x + by * p.y + bz * p.z;
-  const double k2 = g * (g * k1 / (1.0 + g) + p.e);
+  const real M = X.m(), g = X.e / M;
+  const real bx = -X.x / X.e, by = -X.y / X.e, bz = -X.z / X.e;
+  const real k1 = bx * p.x + by * p.y + bz * p.z;
+  const real k2 = g * (g * k1 / (1.0 + g) + p.e);
   return V4(p.x + k2 * bx, p.y + k2 * by, p.z + k2 * bz, g * (p.e + k1));
 }
-double theta_of(const V4 &v) {
+real theta_of(const V4 &v) {
   return (v.x == 0 && v.y == 0 && v.z == 0) ? 0.0 : std::atan2(v.pt(), v.z);
 }
-double phi_of(const V4 &v) { return (v.x == 0 && v.y == 0) ? 0.0 : std::atan2(v.y, v.x); }
+real phi_of(const V4 &v) { return (v.x == 0 && v.y == 0) ? 0.0 : std::atan2(v.y, v.x); }
 
-double spin_weight(const std::vector<std::vector<cplx>> &R, double theta, double phi, int J) {
+real spin_weight(const std::vector<std::vector<cplx>> &R, real theta, real phi, int J) {
   const int n = 2 * J + 1;
   std::vector<cplx> f(n);
   for (int j = 0; j < n; ++j) f[j] = wigner_D(theta, phi, 0, j - J, J);
@@ -1343,47 +1383,47 @@ double spin_weight(const std::vector<std::vector<cplx>> &R, double theta, double
 cplx regge_res(const Setup &S, const Event &ev) {
   const grn_process_params &p = S.p;
   const V4 &X = ev.pf[0];
-  const double m2 = ev.m2;
+  const real m2 = ev.m2;
   // frame rotation angles (spin::GetRhoRotation, MSpin.cc:544-600)
-  double thR = 0, phR = 0;
+  real thR = 0, phR = 0;
   if (p.spin_frame == GRN_FRAME_HX) {
     thR = theta_of(X);
     phR = phi_of(X);
   } else if (p.spin_frame == GRN_FRAME_CS) {
     const V4 a = to_rest(X, S.pb1), b = to_rest(X, S.pb2);
-    const double na = a.p3(), nb = b.p3();
+    const real na = a.p3(), nb = b.p3();
     V4 z(a.x / na - b.x / nb, a.y / na - b.y / nb, a.z / na - b.z / nb, 0);
-    const double nz = z.p3();
+    const real nz = z.p3();
     z = V4(z.x / nz, z.y / nz, z.z / nz, 0);
     thR = theta_of(z);
     phR = phi_of(z);
   }
   const V4 q1  = to_rest(X, S.pb1 - ev.pf[1]);
   const V4 dau = to_rest(X, ev.pf[3]);
-  const double FFA = p.soft.gN_P * proton_ff(p.soft, ev.t1);
-  const double FFB = p.soft.gN_P * proton_ff(p.soft, ev.t2);
+  const real FFA = p.soft.gN_P * proton_ff(p.soft, ev.t1);
+  const real FFB = p.soft.gN_P * proton_ff(p.soft, ev.t2);
   const cplx   prop = regge_prop(p.regge, ev.ss[1][0], ev.t1) * FFA *
                     regge_prop(p.regge, ev.ss[2][0], ev.t2) * FFB;
   cplx sum = 0;
   for (int r = 0; r < p.n_res; ++r) {
     const grn_resonance &R = p.res[r];
     const int    J = R.J;
-    const double M0 = R.M, W = R.W;
+    const real M0 = R.M, W = R.W;
     cplx den(m2 - M0 * M0, M0 * W), num = 1.0;
     if (R.bw == 2) den = cplx(m2 - M0 * M0, std::sqrt(m2) * W);
     if (R.bw == 3) {
-      const double ma = p.m_central[0], mb = p.m_central[1];
-      const double u = msqrt((m2 - sq(ma + mb)) * (m2 - sq(ma - mb))) / (2 * std::sqrt(m2));
-      const double d = msqrt((M0 * M0 - sq(ma + mb)) * (M0 * M0 - sq(ma - mb))) / (2 * M0);
+      const real ma = p.m_central[0], mb = p.m_central[1];
+      const real u = msqrt((m2 - sq(ma + mb)) * (m2 - sq(ma - mb))) / (2 * std::sqrt(m2));
+      const real d = msqrt((M0 * M0 - sq(ma + mb)) * (M0 * M0 - sq(ma - mb))) / (2 * M0);
       den = cplx(m2 - M0 * M0, W * M0 * M0 / std::sqrt(m2) * std::pow(u / d, 2 * J + 1));
     }
     if (R.bw == 4 && J == 2)
       num = 7.0 / 6.0 - (4.0 / 3.0) * (m2 / (M0 * M0)) + (2.0 / 3.0) * sq(m2) / sq(sq(M0));
     const cplx   cbw = -num / den;
-    const double rff = std::exp(-sq(m2 - M0 * M0) / sq(sq(R.g_ff)));
-    const double V   = std::pow(1.0 / m2, p.omega);
+    const real rff = std::exp(-sq(m2 - M0 * M0) / sq(sq(R.g_ff)));
+    const real V   = std::pow(1.0 / m2, p.omega);
     cplx prod = cplx(R.g_regge[0], R.g_regge[1]);
-    double dec = R.g_decay;
+    real dec = R.g_decay;
     if (J == 2) {
       const int n = 5;
       std::vector<std::vector<cplx>> D(n, std::vector<cplx>(n)), rho = D, Rr = D;
@@ -1412,12 +1452,12 @@ cplx regge_res(const Setup &S, const Event &ev) {
 // src/MUserHistograms.cc:60-125, frames of kinematics::LorentzFrame, MKinematics.h:952-1011):
 // order M, Y, Pt, |dphi_pp|, pT1, m(first central), y3, y4, then (cos theta, phi) of the first
 // central particle in CS, HX, AH, PG (beam 2), CM and the lab.
-void observables(const Setup &S, const Event &ev, double *o) {
+void observables(const Setup &S, const Event &ev, real *o) {
   const V4 &X = ev.pf[0];
   o[0] = X.m();
   o[1] = X.rap();
   o[2] = X.pt();
-  double D = std::atan2(ev.pf[1].y, ev.pf[1].x) - std::atan2(ev.pf[2].y, ev.pf[2].x);
+  real D = std::atan2(ev.pf[1].y, ev.pf[1].x) - std::atan2(ev.pf[2].y, ev.pf[2].x);
   while (D >= PI) D -= 2 * PI;
   while (D < -PI) D += 2 * PI;
   o[3] = std::fabs(D);
@@ -1426,9 +1466,9 @@ void observables(const Setup &S, const Event &ev, double *o) {
   o[6] = ev.pf[3].rap();
   o[7] = ev.pf[4].rap();
   const V4 p = to_rest(X, ev.pf[3]), b1 = to_rest(X, S.pb1), b2 = to_rest(X, S.pb2);
-  using A3 = std::array<double, 3>;
+  using A3 = std::array<real, 3>;
   auto unit = [](A3 v) {
-    const double n = std::sqrt(v[0] * v[0] + v[1] * v[1] + v[2] * v[2]);
+    const real n = std::sqrt(v[0] * v[0] + v[1] * v[1] + v[2] * v[2]);
     return A3{v[0] / n, v[1] / n, v[2] / n};
   };
   auto cross = [](const A3 &u, const A3 &v) {
@@ -1442,9 +1482,9 @@ void observables(const Setup &S, const Event &ev, double *o) {
   for (int f = 0; f < 5; ++f) {
     const A3 y = f == 4 ? A3{0, 1, 0} : unit(cross(u1, u2));
     const A3 x = unit(cross(y, zs[f]));
-    const double qx = x[0] * P3[0] + x[1] * P3[1] + x[2] * P3[2];
-    const double qy = y[0] * P3[0] + y[1] * P3[1] + y[2] * P3[2];
-    const double qz = zs[f][0] * P3[0] + zs[f][1] * P3[1] + zs[f][2] * P3[2];
+    const real qx = x[0] * P3[0] + x[1] * P3[1] + x[2] * P3[2];
+    const real qy = y[0] * P3[0] + y[1] * P3[1] + y[2] * P3[2];
+    const real qz = zs[f][0] * P3[0] + zs[f][1] * P3[1] + zs[f][2] * P3[2];
     o[8 + 2 * f] = std::cos(std::atan2(std::sqrt(qx * qx + qy * qy), qz));
     o[9 + 2 * f] = (qx == 0 && qy == 0) ? 0.0 : std::atan2(qy, qx);
   }
@@ -1477,31 +1517,31 @@ int bare_amps(const Setup &S, const Event &ev, cplx *A) {
 
 // Phase-space weight and integration volume (MContinuum.cc:619-656; ForwardVolume
 // MProcess.cc:1390-1415), elastic forward legs, Kf = 2.
-double ps_factor(const Setup &S, const Event &ev) {
+real ps_factor(const Setup &S, const Event &ev) {
   const grn_gencuts &g = S.p.gcuts;
-  const double J = 1.0 / std::fabs(ev.pf[1].z / ev.pf[1].e - ev.pf[2].z / ev.pf[2].e);
+  const real J = 1.0 / std::fabs(ev.pf[1].z / ev.pf[1].e - ev.pf[2].z / ev.pf[2].e);
   if (S.p.phase_space == GRN_PS_FACTORIZED) {
     // C_space = dPhi2/(2 pi), B51PhaseSpaceWeight x B51IntegralVolume (MFactorized.cc:160-183,
     // 418-450)
-    const double m3 = S.p.m_central[0], m4 = S.p.m_central[1];
+    const real m3 = S.p.m_central[0], m4 = S.p.m_central[1];
     (void)m3;
     (void)m4;
-    const double psw  = 0.5 * (1.0 / std::pow(2.0 * PI, 5)) * (ev.pf[1].pt() / (2.0 * ev.pf[1].e)) *
+    const real psw  = 0.5 * (1.0 / std::pow(2.0 * PI, 5)) * (ev.pf[1].pt() / (2.0 * ev.pf[1].e)) *
                        (ev.pf[2].pt() / (2.0 * ev.pf[2].e)) * J;
-    const double fwd = sq(2.0 * PI) * ev.pf[1].pt() * ev.pf[2].pt() *
+    const real fwd = sq(2.0 * PI) * ev.pf[1].pt() * ev.pf[2].pt() *
                        sq(std::log(g.fpt_max) - std::log(g.fpt_min + ZERO_EPS));
-    const double vol = (ev.m2hi - ev.m2lo) * (g.Y_max - g.Y_min) * fwd;
+    const real vol = (ev.m2hi - ev.m2lo) * (g.Y_max - g.Y_min) * fwd;
     return (ev.dw / (2.0 * PI)) * psw * vol;
   }
   const int Kf = S.p.n_central, Nf = Kf + 2;
-  double prod = ev.q.pt();
+  real prod = ev.q.pt();
   if (Kf == 4) prod = ev.kq[0].pt() * ev.kq[1].pt() * ev.kq[2].pt();
-  const double psw = (1.0 / std::pow(2.0, 2 * (Nf - 2))) * (1.0 / std::pow(2.0 * PI, 3 * Nf - 4)) *
+  const real psw = (1.0 / std::pow(2.0, 2 * (Nf - 2))) * (1.0 / std::pow(2.0 * PI, 3 * Nf - 4)) *
                      (ev.pf[1].pt() / (2.0 * ev.pf[1].e)) * (ev.pf[2].pt() / (2.0 * ev.pf[2].e)) *
                      J * prod;
-  const double fwd = sq(2.0 * PI) * ev.pf[1].pt() * ev.pf[2].pt() *
+  const real fwd = sq(2.0 * PI) * ev.pf[1].pt() * ev.pf[2].pt() *
                      sq(std::log(g.fpt_max) - std::log(g.fpt_min + ZERO_EPS));
-  const double vol = std::pow(g.kt_max - g.kt_min, Kf - 1) * std::pow(2.0 * PI, Kf - 1) *
+  const real vol = std::pow(g.kt_max - g.kt_min, Kf - 1) * std::pow(2.0 * PI, Kf - 1) *
                      std::pow(g.rap_max - g.rap_min, Kf) * fwd;
   return psw * vol;
 }
@@ -1510,9 +1550,9 @@ double ps_factor(const Setup &S, const Event &ev) {
 bool fiducial(const Setup &S, const Event &ev) {
   const grn_fidcuts &f = S.p.fcuts;
   if (!f.active) return true;
-  const double at1 = std::fabs(ev.t1), at2 = std::fabs(ev.t2);
+  const real at1 = std::fabs(ev.t1), at2 = std::fabs(ev.t2);
   if (!(at1 >= f.ft_min && at1 <= f.ft_max && at2 >= f.ft_min && at2 <= f.ft_max)) return false;
-  const double M = msqrt(ev.m2);
+  const real M = msqrt(ev.m2);
   if (!(M >= f.M_min && M <= f.M_max && ev.Y >= f.Y_min && ev.Y <= f.Y_max && ev.Pt >= f.Pt_min &&
         ev.Pt <= f.Pt_max))
     return false;
@@ -1522,7 +1562,7 @@ bool fiducial(const Setup &S, const Event &ev) {
   const int  np   = (casc || S.p.n_central == 4) ? 4 : 2;
   for (int k = 0; k < np; ++k) {
     const V4 &p = casc ? ev.leaf[k] : ev.pf[3 + k];
-    const double pt = p.pt(), et = p.mt(), eta = p.eta(), rap = p.rap();
+    const real pt = p.pt(), et = p.mt(), eta = p.eta(), rap = p.rap();
     if (!(pt >= f.pt_min && pt <= f.pt_max && et >= f.Et_min && et <= f.Et_max &&
           eta >= f.eta_min && eta <= f.eta_max && rap >= f.rap_min && rap <= f.rap_max))
       ok = false;
@@ -1539,7 +1579,7 @@ bool veto_cuts(const Setup &S, const Event &ev) {
   const int  np     = leaves ? 4 : 2;
   for (int k = 0; k < np; ++k) {
     const V4 &p = leaves ? ev.leaf[k] : ev.pf[3 + k];
-    const double pt = p.pt(), eta = p.eta();
+    const real pt = p.pt(), eta = p.eta();
     for (int d = 0; d < S.p.n_veto; ++d)
       if (pt >= S.p.veto_pt_min[d] && pt <= S.p.veto_pt_max[d] && eta >= S.p.veto_eta_min[d] &&
           eta <= S.p.veto_eta_max[d])
@@ -1549,8 +1589,8 @@ bool veto_cuts(const Setup &S, const Event &ev) {
 }
 
 // One event weight (MContinuum::EventWeight, src/MContinuum.cc:164-193).
-double event_weight(const Setup &S, const double *u, uint8_t &flags, Event &ev) {
-  double W = 0.0;
+real event_weight(const Setup &S, const real *u, uint8_t &flags, Event &ev) {
+  real W = 0.0;
   const bool kin = S.p.phase_space == GRN_PS_FACTORIZED ? build_kinematics_F(S, u, ev)
                                                         : build_kinematics(S, u, ev);
   const bool fid = kin && fiducial(S, ev);
@@ -1558,7 +1598,7 @@ double event_weight(const Setup &S, const double *u, uint8_t &flags, Event &ev) 
   if (kin && fid && veto) {
     cplx A0[9];
     const int nh = bare_amps(S, ev, A0);
-    double amp2 = 0;
+    real amp2 = 0;
     if (S.p.screening) {
       amp2 = screened_amp2(S, ev, A0, nh);
     } else {
@@ -1581,8 +1621,8 @@ Setup make_setup(const grn_process_params *p, const double *msa, int n_kt2) {
   S.p      = *p;
   S.sqrt_s = p->sqrt_s;
   S.s      = p->sqrt_s * p->sqrt_s;
-  const double E  = p->sqrt_s / 2.0;
-  const double pz = msqrt(E * E - sq(p->m_beam));
+  const real E  = p->sqrt_s / 2.0;
+  const real pz = msqrt(E * E - sq(p->m_beam));
   S.pb1 = V4(0, 0, pz, E);
   S.pb2 = V4(0, 0, -pz, E);
   S.msa   = msa;
@@ -1610,15 +1650,15 @@ void parallel_for(int64_t n, int nthreads, F &&fn) {
 // Eikonal tables.
 
 // Linear interpolation of the density table (IArray1D::Interpolate1D).
-cplx table_interp(const double *tab, int N, double xmin, double xmax, double a) {
-  const double step = (xmax - xmin) / N;
+cplx table_interp(const double *tab, int N, real xmin, real xmax, real a) {
+  const real step = (xmax - xmin) / N;
   if (a < xmin) a = xmin;
   int i = static_cast<int>(std::floor((a - xmin) / step));
   if (i < 0) i = 0;
   if (i >= N) i = N - 1;
   const double *r0 = tab + 3 * i, *r1 = tab + 3 * (i + 1);
   const cplx y0(r0[1], r0[2]), y1(r1[1], r1[2]);
-  return y0 + (a - r0[0]) * ((y1 - y0) / (r1[0] - r0[0]));
+  return y0 + (a - real(r0[0])) * ((y1 - y0) / (real(r1[0]) - real(r0[0])));
 }
 
 }  // namespace orc
@@ -1643,7 +1683,9 @@ int orc_weights(const grn_process_params *p, const double *u, int64_t n, int32_t
     for (int64_t i = a; i < b; ++i) {
       uint8_t f = 0;
       ev        = orc::Event();
-      w[i]      = orc::event_weight(S, u + i * dim, f, ev);
+      orc::real ur[16];
+      for (int d = 0; d < dim; ++d) ur[d] = u[i * dim + d];
+      w[i]      = double(orc::event_weight(S, ur, f, ev));
       if (flags) flags[i] = f;
       if (rec) {
         double *r = rec + i * 35;
@@ -1677,9 +1719,14 @@ int orc_observables(const grn_process_params *p, const double *u, int64_t n, int
     for (int64_t i = a; i < b; ++i) {
       uint8_t    f  = 0;
       orc::Event ev = orc::Event();
-      orc::event_weight(S, u + i * dim, f, ev);
+      orc::real ur[16], ob[20];
+      for (int d = 0; d < dim; ++d) ur[d] = u[i * dim + d];
+      orc::event_weight(S, ur, f, ev);
       ok[i] = (f & GRN_FLAG_KINEMATICS_OK) ? 1 : 0;
-      if (ok[i]) orc::observables(S, ev, obs + i * 20);
+      if (ok[i]) {
+        orc::observables(S, ev, ob);
+        for (int k = 0; k < 20; ++k) obs[i * 20 + k] = double(ob[k]);
+      }
     }
   });
   return GRN_OK;

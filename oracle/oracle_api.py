@@ -11,19 +11,28 @@ import numpy as np
 
 _HERE = os.path.dirname(os.path.abspath(__file__))
 LIB = os.path.join(_HERE, "_build", "liborc.so")
+LIB_LD = os.path.join(_HERE, "_build", "liborc_ld.so")  # the same restatement in long double
 _lib = None
+_lib_ld = None
 
 
 def build():
     subprocess.check_call(["make", "-s", "-C", _HERE])
 
 
-def lib():
-    global _lib
-    if _lib is None:
-        if not os.path.exists(LIB):
+def lib(long_double=False):
+    """The oracle library; long_double selects the extended-precision build (same code and
+    constants, long double arithmetic: 64-bit significand on x86, 113-bit on aarch64)."""
+    global _lib, _lib_ld
+    if long_double and _lib_ld is not None:
+        return _lib_ld
+    if not long_double and _lib is not None:
+        return _lib
+    path = LIB_LD if long_double else LIB
+    if True:
+        if not os.path.exists(path):
             build()
-        L = ctypes.CDLL(LIB)
+        L = ctypes.CDLL(path)
         vp = ctypes.c_void_p
         L.orc_weights.restype = ctypes.c_int
         L.orc_weights.argtypes = [vp, vp, ctypes.c_int64, ctypes.c_int32, vp, vp, vp, vp,
@@ -41,18 +50,22 @@ def lib():
                                     vp]
         L.orc_uniforms.argtypes = [ctypes.c_uint64, ctypes.c_uint32, ctypes.c_int64,
                                    ctypes.c_int64, ctypes.c_int32, vp]
-        _lib = L
-    return _lib
+        if long_double:
+            _lib_ld = L
+        else:
+            _lib = L
+    return L
 
 
 def _p(a):
     return None if a is None else a.ctypes.data_as(ctypes.c_void_p)
 
 
-def weights(params, u, msa=None, nthreads=1, with_rec=False):
-    """(w, flags[, rec]) for u of shape (n, 8), or (n, 14) for two-body cascades. rec per
-    point: t1, t2, m2, the 4-momenta (px, py, pz, E) of pfinal[1..4] and of the four cascade
-    daughters."""
+def weights(params, u, msa=None, nthreads=1, with_rec=False, long_double=False):
+    """(w, flags[, rec]) for u of shape (n, dim) (8 for 2-body states, 12 or 14 for two-body
+    cascades, 14 for 4-body states). rec per point: t1, t2, m2, the 4-momenta (px, py, pz, E)
+    of pfinal[1..4] and of the four cascade daughters. long_double: evaluate in the extended-
+    precision build (results rounded to double)."""
     u = np.ascontiguousarray(u, dtype=np.float64)
     n, dim = u.shape
     w = np.zeros(n)
@@ -62,8 +75,8 @@ def weights(params, u, msa=None, nthreads=1, with_rec=False):
     if msa is not None:
         msa = np.ascontiguousarray(msa, dtype=np.float64)
         n_kt2 = msa.shape[0] - 1
-    st = lib().orc_weights(ctypes.byref(params), _p(u), n, dim, _p(w), _p(fl), _p(rec), _p(msa),
-                           n_kt2, nthreads)
+    st = lib(long_double).orc_weights(ctypes.byref(params), _p(u), n, dim, _p(w), _p(fl),
+                                      _p(rec), _p(msa), n_kt2, nthreads)
     if st != 0:
         raise RuntimeError("orc_weights status %d" % st)
     return (w, fl, rec) if with_rec else (w, fl)

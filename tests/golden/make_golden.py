@@ -342,15 +342,43 @@ def ccascade_fixtures():
     write_sigma("rrc_vegas_sigma.json", out, proc, os.path.basename(CARD))
 
 
+def ld_fixtures():
+    """The oracle restatement in long double arithmetic (oracle/_build/liborc_ld.so: the same
+    formulas and constants as the reference, 64-bit significands on x86) on the points of every
+    weight fixture: long_double_oracle.npz holds, per fixture, the weights nearer the exact value of the
+    reference's formulas than any FP64 evaluation (the reference's own or the engine's)."""
+    sys.path.insert(0, REPO)
+    sys.path.insert(0, HERE)
+    from oracle import oracle_api as orc
+    from fixture_meta import fixture_params, weight_fixtures
+    subprocess.check_call(["make", "-s", "-C", os.path.join(REPO, "oracle")])
+    out = {}
+    for f in weight_fixtures():
+        g = np.load(os.path.join(HERE, f))
+        P, msa = fixture_params(f, g)
+        w, _ = orc.weights(P, g["u"], msa=msa, nthreads=8, long_double=True)
+        out[f[:-len(".npz")]] = w
+        nz = g["w"] > 0
+        print("%-34s reference vs long double: max rel %.2e" %
+              (f, np.max(np.abs(g["w"][nz] - w[nz]) / w[nz]) if nz.any() else 0.0))
+    np.savez_compressed(os.path.join(HERE, "long_double_oracle.npz"), **out)
+    print("wrote long_double_oracle.npz")
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--ref", default=REF_DEFAULT)
     ap.add_argument("--only", choices=["all", "resonances", "cascades", "rescon", "regge_res",
-                                       "nbody", "nbody_c", "veto", "ccascades"],
+                                       "nbody", "nbody_c", "veto", "ccascades", "ld"],
                     default="all")
     a = ap.parse_args()
+    if a.only == "ld":  # needs only the oracle
+        ld_fixtures()
+        return
     subprocess.check_call(["make", "-s", "-C", os.path.join(REPO, "oracle", "refbuild"), "-j8",
                            "REF=" + a.ref])
+    if a.only == "all":
+        ld_fixtures()
     if a.only in ("all", "ccascades"):
         ccascade_fixtures()
     if a.only == "ccascades":

@@ -317,3 +317,47 @@ def test_veto_cuts(name):
     kin = g["kin"] == 1
     assert np.array_equal(((fl >> 2) & 1)[kin], g["veto"][kin])
     assert (g["veto"][kin] == 0).sum() > 100
+
+
+# The restatement in long double arithmetic (oracle/_build/liborc_ld.so): the same formulas
+# and constants as the reference with 11 more significand bits (x86), i.e. the reference's own
+# value with its FP64 rounding removed. tests/golden/long_double_oracle.npz holds its weights
+# for every weight fixture (make_golden.py --only ld).
+def test_long_double_oracle_reproduces_stored_weights():
+    import sys
+    sys.path.insert(0, GOLDEN)
+    from fixture_meta import fixture_params
+    ld = np.load(os.path.join(GOLDEN, "long_double_oracle.npz"))
+    for name in ("c1_tune0_weights.npz", "rc_tree_weights.npz", "rrc_tree_weights.npz",
+                 "c2_screened_63x33_weights.npz"):
+        g = _load(name)
+        P, msa = fixture_params(name, g)
+        w, _ = orc.weights(P, g["u"], msa=msa, nthreads=8, long_double=True)
+        wl = ld[name[:-4]]
+        nz = wl > 0
+        assert np.array_equal(w > 0, nz)
+        assert np.max(np.abs(w[nz] - wl[nz]) / wl[nz]) < 1e-13
+
+
+def test_fp64_evaluations_vs_long_double():
+    """How far FP64 evaluations of the reference's formulas sit from their long-double value:
+    the reference itself and the FP64 oracle both carry up to ~2.5e-9 relative rounding on
+    fixtures where 13 TeV 4-vector products cancel (tensor resonances in <C>), typically
+    1e-10; the tests of the GPU engine compare it with the long-double weights."""
+    import sys
+    sys.path.insert(0, GOLDEN)
+    from fixture_meta import fixture_params, weight_fixtures
+    ld = np.load(os.path.join(GOLDEN, "long_double_oracle.npz"))
+    worst_ref = worst_orc = 0.0
+    for name in weight_fixtures():
+        g = _load(name)
+        if g["u"].shape[0] > 1024 or "loop_kt" in g or "n_bt" in g:
+            continue  # the large and the screened fixtures: covered by the GPU comparison
+        P, msa = fixture_params(name, g)
+        w, _ = orc.weights(P, g["u"], msa=msa, nthreads=8)
+        wl = ld[name[:-4]]
+        nz = (wl > 0) & (g["w"] > 0)
+        worst_ref = max(worst_ref, np.max(np.abs(g["w"][nz] - wl[nz]) / wl[nz]))
+        worst_orc = max(worst_orc, np.max(np.abs(w[nz] - wl[nz]) / wl[nz]))
+    print("vs long double: reference %.2e, FP64 oracle %.2e" % (worst_ref, worst_orc))
+    assert worst_ref < 3e-9 and worst_orc < 3e-9
