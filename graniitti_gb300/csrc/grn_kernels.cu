@@ -16,7 +16,7 @@
 #include <cstdint>
 
 #include "grn_internal.cuh"
-#include "grn_loop2.cuh"
+#include "grn_loop3.cuh"
 #include "grn_philox.cuh"
 
 // Resident blocks per SM requested for the FP32 loop kernels (register budget
@@ -332,39 +332,61 @@ __device__ __forceinline__ double record_weight(const KArgs &A, const LoopEventF
   return W;
 }
 
-// Loop nodes as duplicated pairs for the two-events-per-thread loop.
-__device__ void stage_nodes2(const KArgs &A, KtNode2 *skt, PhiNode2 *sphi) {
+// Loop nodes of the azimuth-outer paired loop (grn_loop3.cuh).
+__device__ void stage_nodes3(const KArgs &A, KtNode3 *skt, PhiNode3 *sphi) {
   for (int j = threadIdx.x; j < A.n_kt_nodes; j += blockDim.x) {
-    const float kt = float(A.lc_kt[3 * j]);
-    skt[j] = {f2s(kt), f2s(kt * kt), f2s(float(A.lc_kt[3 * j + 1])),
-              f2s(float(A.lc_kt[3 * j + 2]))};
+    const float kt = float(A.lc_kt[3 * j]), ci = float(A.lc_kt[3 * j + 2]);
+    skt[j] = {f2s(kt), f2s(kt * kt), f2s(float(A.lc_kt[3 * j + 1])), f2s(ci), f2s(-ci)};
   }
-  for (int i = threadIdx.x; i < A.n_phi_nodes; i += blockDim.x)
-    sphi[i] = {f2s(float(A.lc_phi[3 * i])), f2s(float(A.lc_phi[3 * i + 1])),
-               f2s(float(A.lc_phi[3 * i + 2]))};
+  for (int i = threadIdx.x; i < A.n_phi_nodes; i += blockDim.x) {
+    const double c = A.lc_phi[3 * i], s = A.lc_phi[3 * i + 1];
+    sphi[i] = {f2s(float(c)), f2s(float(s)), f2s(float(A.lc_phi[3 * i + 2])),
+               f2s(float(atan2(s, c) * (0.5 / kPi)))};
+  }
 }
 
-// Screened weights of records ra and rb (rb may repeat ra; then only wa is meaningful).
-__device__ __forceinline__ void record_weights2(const KArgs &A, const LoopEventF<float> &consts,
+// Screened weights of records ra and rb (rb may repeat ra; then only wa is meaningful) on the
+// azimuth-outer loop; a pair with an event outside the validity bound (loop3_safe) takes the
+// per-point-tested loop instead.
+__device__ __forceinline__ void record_weights3(const KArgs &A, const LoopEventF<float> &consts,
                                                 const float *__restrict__ rf,
                                                 const double *__restrict__ rd, int64_t cap,
-                                                int64_t ra, int64_t rb, const KtNode2 *skt,
-                                                const PhiNode2 *sphi, double &wa, double &wb,
+                                                int64_t ra, int64_t rb, const KtNode3 *skt,
+                                                const PhiNode3 *sphi, double &wa, double &wb,
                                                 uint8_t &fa, uint8_t &fb) {
   LoopEventF<float> ea = consts, eb = consts;
   double            a0r[2], a0i[2], jac[2];
   load_record(ea, a0r[0], a0i[0], jac[0], rf, rd, ra, cap);
   load_record(eb, a0r[1], a0i[1], jac[1], rf, rd, rb, cap);
-  LoopEvent2 e;
-  make_loop_event2(ea, eb, e);
-  float2 sr, si;
-  loop_integral2(e, A.n_kt_nodes, A.n_phi_nodes, skt, sphi, sr, si);
+  const float kt_max = float(A.P.loop.kt_max);
+  double      sr[2], si[2];
+  if (loop3_safe(ea, kt_max) && loop3_safe(eb, kt_max)) {
+    Loop3<float2> e;
+    make_loop3<float2>(ea, eb, [](float x, float y) { return make_float2(x, y); }, e);
+    float2 s_re, s_im;
+    loop_integral3(e, A.n_kt_nodes, A.n_phi_nodes, skt, sphi, s_re, s_im);
+    // the event's prefactor (couplings x ReggeEta^2 x tree-level phase), after the sum
+    const float pr[2] = {ea.pre_re, eb.pre_re}, pi[2] = {ea.pre_im, eb.pre_im};
+    const float xr[2] = {s_re.x, s_re.y}, xi[2] = {s_im.x, s_im.y};
+    for (int k = 0; k < 2; ++k) {
+      sr[k] = double(pr[k]) * xr[k] - double(pi[k]) * xi[k];
+      si[k] = double(pr[k]) * xi[k] + double(pi[k]) * xr[k];
+    }
+  } else {
+    LoopEvent2 e;
+    make_loop_event2(ea, eb, e);
+    float2 s_re, s_im;
+    loop_integral2(e, A.n_kt_nodes, A.n_phi_nodes, skt, sphi, s_re, s_im);
+    sr[0] = s_re.x;
+    sr[1] = s_re.y;
+    si[0] = s_im.x;
+    si[1] = s_im.y;
+  }
   const double esc[2] = {ea.escale, eb.escale};
-  const float  lr[2]  = {sr.x, sr.y}, li[2] = {si.x, si.y};
   double       W[2];
   uint8_t      F[2];
   for (int k = 0; k < 2; ++k) {
-    const double xr = double(lr[k]) * esc[k], xi = double(li[k]) * esc[k];
+    const double xr = sr[k] * esc[k], xi = si[k] * esc[k];
     const double re = a0r[k] + (A.loop_norm_re * xr - A.loop_norm_im * xi);
     const double im = a0i[k] + (A.loop_norm_re * xi + A.loop_norm_im * xr);
     W[k] = jac[k] * (re * re + im * im);
@@ -626,9 +648,9 @@ __global__ void __launch_bounds__(kWeightThreads, MINB)
                         const float *__restrict__ rf, const double *__restrict__ rd, int64_t cap,
                         const unsigned long long *__restrict__ count, double *__restrict__ w,
                         uint8_t *__restrict__ flags) {
-  __shared__ KtNode2  skt[kMaxLoopNodes];
-  __shared__ PhiNode2 sphi[kMaxLoopNodes];
-  stage_nodes2(A, skt, sphi);
+  __shared__ KtNode3  skt[kMaxLoopNodes];
+  __shared__ PhiNode3 sphi[kMaxLoopNodes];
+  stage_nodes3(A, skt, sphi);
   __syncthreads();
   LoopEventF<float> c;
   make_loop_consts_fast<float>(A.P, A.K, c);
@@ -638,7 +660,7 @@ __global__ void __launch_bounds__(kWeightThreads, MINB)
     const int64_t ra = 2 * q, rb = (2 * q + 1 < cnt) ? 2 * q + 1 : 2 * q;
     double  wa, wb;
     uint8_t fa, fb;
-    record_weights2(A, c, rf, rd, cap, ra, rb, skt, sphi, wa, wb, fa, fb);
+    record_weights3(A, c, rf, rd, cap, ra, rb, skt, sphi, wa, wb, fa, fb);
     w[list[ra]] = wa;
     if (flags) flags[list[ra]] = fa;
     if (rb != ra) {
@@ -1305,9 +1327,9 @@ __global__ void __launch_bounds__(kVegasThreads, MINB)
                       unsigned long long *__restrict__ acc,
                       const int64_t *__restrict__ l_idx, const double *__restrict__ l_vw,
                       const float *__restrict__ rf, const double *__restrict__ rd, int64_t cap) {
-  __shared__ KtNode2  skt[kMaxLoopNodes];
-  __shared__ PhiNode2 sphi[kMaxLoopNodes];
-  stage_nodes2(A, skt, sphi);
+  __shared__ KtNode3  skt[kMaxLoopNodes];
+  __shared__ PhiNode3 sphi[kMaxLoopNodes];
+  stage_nodes3(A, skt, sphi);
   __syncthreads();
   LoopEventF<float> c;
   make_loop_consts_fast<float>(A.P, A.K, c);
@@ -1320,7 +1342,7 @@ __global__ void __launch_bounds__(kVegasThreads, MINB)
     const int64_t ra = 2 * q, rb = (2 * q + 1 < n) ? 2 * q + 1 : 2 * q;
     double  W[2];
     uint8_t F[2];
-    record_weights2(A, c, rf, rd, cap, ra, rb, skt, sphi, W[0], W[1], F[0], F[1]);
+    record_weights3(A, c, rf, rd, cap, ra, rb, skt, sphi, W[0], W[1], F[0], F[1]);
     for (int k = 0; k < (rb != ra ? 2 : 1); ++k) {
       const int64_t r = k ? rb : ra;
       const double  f = W[k] * l_vw[r];
@@ -1575,8 +1597,8 @@ constexpr int kBatchChunk = kVegasThreads;  // work units per grab (one per thre
 template <bool REC>
 __global__ void __launch_bounds__(kVegasThreads, 2)
     k_batch_loop(int np, unsigned long long *__restrict__ counter) {
-  using KT = typename std::conditional<REC, KtNode2, KtNode<float>>::type;
-  using PT = typename std::conditional<REC, PhiNode2, PhiNode<float>>::type;
+  using KT = typename std::conditional<REC, KtNode3, KtNode<float>>::type;
+  using PT = typename std::conditional<REC, PhiNode3, PhiNode<float>>::type;
   __shared__ KT                 skt[kMaxLoopNodes];
   __shared__ PT                 sphi[kMaxLoopNodes];
   __shared__ int64_t            s_begin[kMaxBatch + 1];  // unit ranges, padded to whole chunks
@@ -1619,7 +1641,7 @@ __global__ void __launch_bounds__(kVegasThreads, 2)
       const BatchProc &q = c_procs[p];
       __syncthreads();
       if constexpr (REC) {
-        stage_nodes2(q.A, skt, sphi);
+        stage_nodes3(q.A, skt, sphi);
         make_loop_consts_fast<float>(q.A.P, q.A.K, c);
       } else {
         stage_nodes<float>(q.A, skt, sphi);
@@ -1633,7 +1655,7 @@ __global__ void __launch_bounds__(kVegasThreads, 2)
         const int64_t ra = 2 * unit, rb = (2 * unit + 1 < n) ? 2 * unit + 1 : 2 * unit;
         double  W[2];
         uint8_t F[2];
-        record_weights2(q.A, c, q.rf, q.rd, q.ncall, ra, rb, skt, sphi, W[0], W[1], F[0], F[1]);
+        record_weights3(q.A, c, q.rf, q.rd, q.ncall, ra, rb, skt, sphi, W[0], W[1], F[0], F[1]);
         for (int k = 0; k < (rb != ra ? 2 : 1); ++k) {
           const int64_t r = k ? rb : ra;
           const double  f = W[k] * q.l_vw[r];

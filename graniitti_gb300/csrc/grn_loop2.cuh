@@ -5,7 +5,9 @@
 // and lane y = event B; both events run over the same loop grid, so the loop-node values
 // come from shared memory as duplicated pairs {v, v} (one 64-bit load, no broadcast
 // instructions). Transcendentals and the division stay per lane (MUFU). Sums are
-// Kahan-compensated per lane, as in the scalar loop.
+// Kahan-compensated per lane, as in the scalar loop. This form tests every point for
+// kinematic validity; the record-mode kernels run the azimuth-outer loop of grn_loop3.cuh
+// and fall back to this one for events outside its validity bound.
 #pragma once
 
 #include <cuda_runtime.h>
@@ -22,14 +24,6 @@ __device__ __forceinline__ float2 fma2(float2 a, float2 b, float2 c) { return __
 __device__ __forceinline__ float2 sub2(float2 a, float2 b) {
   return __ffma2_rn(b, make_float2(-1.f, -1.f), a);
 }
-
-// Loop nodes as duplicated pairs.
-struct KtNode2 {
-  float2 kt, k2, cre, cim;
-};
-struct PhiNode2 {
-  float2 c, s, u;
-};
 
 // Per-event fields of two events (the record fields) + per-engine constants as pairs.
 struct LoopEvent2 {
@@ -153,16 +147,19 @@ __device__ __forceinline__ void kahan_add2(float2 &sum, float2 &comp, float2 x) 
 }
 
 // Loop integrals of both events (relative to their exp(Emax)): lane x event A, y event B.
+// Every point is tested for kinematic validity. KN, PN: node types with the fields kt, k2,
+// cre, cim and c, s, u.
+template <typename KN, typename PN>
 __device__ __forceinline__ void loop_integral2(const LoopEvent2 &e, int n_kt, int n_phi,
-                                               const KtNode2 *skt, const PhiNode2 *sphi,
+                                               const KN *skt, const PN *sphi,
                                                float2 &out_re, float2 &out_im) {
   const float2 zero = f2s(0.f);
   float2 ar = zero, ai = zero, cr = zero, ci = zero;
   for (int j = 0; j < n_kt; ++j) {
-    const KtNode2 nj = skt[j];
+    const KN nj = skt[j];
     float2 ir = zero, ii = zero, dr = zero, di = zero;
     for (int i = 0; i < n_phi; ++i) {
-      const PhiNode2 ni = sphi[i];
+      const PN ni = sphi[i];
       float2 are, aim;
       const unsigned ok = loop_point_amp2(e, mul2(nj.kt, ni.c), mul2(nj.kt, ni.s), nj.k2, are, aim);
       float2 xr = mul2(ni.u, are), xi = mul2(ni.u, aim);

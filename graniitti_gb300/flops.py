@@ -11,7 +11,7 @@ EXE = os.path.join(HERE, "_build", "flopcount")
 
 def build():
     os.makedirs(os.path.dirname(EXE), exist_ok=True)
-    deps = [SRC, os.path.join(HERE, "csrc", "grn_physics.cuh")]
+    deps = [SRC] + [os.path.join(HERE, "csrc", f) for f in ("grn_physics.cuh", "grn_loop3.cuh")]
     if os.path.exists(EXE) and all(os.path.getmtime(d) <= os.path.getmtime(EXE) for d in deps):
         return EXE
     subprocess.check_call(["g++", "-std=c++17", "-O1", "-I", os.path.join(HERE, "..", "include"),
