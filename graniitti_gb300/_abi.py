@@ -235,6 +235,7 @@ SIGNATURES = {
     "grn_flow_default_params": (None, [c_void_p]),
     "grn_flow_create": (c_int32, [c_void_p, c_void_p, c_void_p]),
     "grn_flow_destroy": (c_int32, [c_void_p]),
+    "grn_flow_set_wait_polls": (c_int32, [c_void_p, c_int32]),
     "grn_flow_num_params": (c_int64, [c_void_p]),
     "grn_flow_get_params": (c_int32, [c_void_p, c_void_p]),
     "grn_flow_set_params": (c_int32, [c_void_p, c_void_p]),

@@ -185,6 +185,7 @@ struct grn_flow {
   DevBuf      d_tu, d_tlq, d_tcoef;          // training set
   DevBuf      d_fu, d_flq;                   // points of the last flow pass
   int         in_batches = 0;                // batches that draw a member's points from it
+  int         first_wait_polls = -1;         // forward kernel: poll limit of the first wait
 };
 
 namespace {
@@ -1887,7 +1888,7 @@ cudaError_t flow_forward(grn_flow *f, int mode, const float *xin, int64_t ld_in,
                                      xout, ld_out, lq, xs_store, f->d_err.as<int>(), f->e->stream);
   return grn::launch_flow_forward(mode, f->d_theta.as<float>(), f->d_w2c.p, f->d_w3c.p,
                                   f->layers, xin, ld_in, n, seed, stream, first, xout, ld_out, lq,
-                                  xs_store, f->d_err.as<int>(), f->e->stream);
+                                  xs_store, f->d_err.as<int>(), f->e->stream, f->first_wait_polls);
 }
 
 // Bounded waits inside the forward kernel report through d_err (read after a sync).
@@ -2059,6 +2060,12 @@ grn_status grn_flow_destroy(grn_flow *f) {
     f->e->have_last = false;
   }
   delete f;
+  return GRN_OK;
+}
+
+grn_status grn_flow_set_wait_polls(grn_flow *f, int32_t polls) {
+  if (!f) return fail(GRN_ERR_INVALID, "null flow");
+  f->first_wait_polls = polls < 0 ? -1 : polls;
   return GRN_OK;
 }
 

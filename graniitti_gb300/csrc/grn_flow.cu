@@ -216,7 +216,7 @@ __global__ void __launch_bounds__(kFwdThreads, 1)
                const bf16 *__restrict__ w3c, int layers, const float *__restrict__ xin,
                int64_t ld_in, int64_t n, uint64_t seed, uint32_t stream, int64_t first,
                float *__restrict__ xout, int64_t ld_out, float *__restrict__ lq_out,
-               float *__restrict__ xs_store, int *__restrict__ err) {
+               float *__restrict__ xs_store, int *__restrict__ err, int first_wait_polls) {
   extern __shared__ __align__(1024) unsigned char fwd_smem[];
   unsigned char *smem = fwd_smem;
   float    *sX  = reinterpret_cast<float *>(smem + kOffX);
@@ -296,7 +296,10 @@ __global__ void __launch_bounds__(kFwdThreads, 1)
           if (base + p < n) xs_store[(static_cast<int64_t>(l) * kDim + j) * n + base + p] = sX[i];
         }
       }
-      const bool okw = mbar_wait(bar_w, (n_w - 1) & 1u);
+      // the first weight-copy wait of the CTA may take a caller-set poll limit (the test of
+      // the timeout path); the drain waits below keep the default limit
+      const bool okw = mbar_wait(bar_w, (n_w - 1) & 1u,
+                                 n_w == 1 && first_wait_polls >= 0 ? first_wait_polls : kSpinLimit);
       if (__syncthreads_or(!okw)) {
         aborted = true;
         break;
@@ -898,7 +901,7 @@ cudaError_t launch_flow_forward(int mode, const float *theta, const void *w2c, c
                                 int layers, const float *xin, int64_t ld_in, int64_t n,
                                 uint64_t seed, uint32_t stream, int64_t first, float *xout,
                                 int64_t ld_out, float *lq, float *xs_store, int *err,
-                                cudaStream_t st) {
+                                cudaStream_t st, int first_wait_polls) {
   if (n <= 0) return cudaSuccess;
   const int64_t sup  = (n + flow::kSuper - 1) / flow::kSuper;
   const int     grid = static_cast<int>(std::min<int64_t>(sup, sm_count()));
@@ -907,11 +910,13 @@ cudaError_t launch_flow_forward(int mode, const float *theta, const void *w2c, c
   if (mode == 0) {
     cudaFuncSetAttribute(flow::k_flow_fwd<0>, cudaFuncAttributeMaxDynamicSharedMemorySize, sm);
     flow::k_flow_fwd<0><<<grid, flow::kFwdThreads, sm, st>>>(
-        theta, a, b, layers, xin, ld_in, n, seed, stream, first, xout, ld_out, lq, xs_store, err);
+        theta, a, b, layers, xin, ld_in, n, seed, stream, first, xout, ld_out, lq, xs_store, err,
+        first_wait_polls);
   } else {
     cudaFuncSetAttribute(flow::k_flow_fwd<1>, cudaFuncAttributeMaxDynamicSharedMemorySize, sm);
     flow::k_flow_fwd<1><<<grid, flow::kFwdThreads, sm, st>>>(
-        theta, a, b, layers, xin, ld_in, n, seed, stream, first, xout, ld_out, lq, xs_store, err);
+        theta, a, b, layers, xin, ld_in, n, seed, stream, first, xout, ld_out, lq, xs_store, err,
+        first_wait_polls);
   }
   return cudaGetLastError();
 }

@@ -33,12 +33,13 @@ cudaError_t launch_flow_pack(const float *theta, int layers, void *w2p, void *w3
 // stream id `stream`; xout = x). Arrays are dimension-major with leading dimension
 // ld_in / ld_out. lq receives log q(x). xs_store (density mode, may be null) receives
 // each layer's input, layers x 8 x n. err: device int set to 1 when a bounded wait of
-// the kernel gave up (its outputs are then invalid).
+// the kernel gave up (its outputs are then invalid). first_wait_polls >= 0: the poll limit
+// of each CTA's first wait (on its first weight copy) instead of the default.
 cudaError_t launch_flow_forward(int mode, const float *theta, const void *w2c, const void *w3c,
                                 int layers, const float *xin, int64_t ld_in, int64_t n,
                                 uint64_t seed, uint32_t stream, int64_t first, float *xout,
                                 int64_t ld_out, float *lq, float *xs_store, int *err,
-                                cudaStream_t st);
+                                cudaStream_t st, int first_wait_polls = -1);
 // Loss over n points and its gradient: grad <- d(sum_i l_i / n)/d theta and loss_sum <-
 // sum_i l_i, both deterministic (each backward block accumulates a private slice of part,
 // flow_backward_slices() x parameters floats, and loss_part, flow_backward_slices()

@@ -256,9 +256,9 @@ __device__ __forceinline__ bool mbar_try(uint32_t bar, uint32_t parity) {
   return ok != 0;
 }
 
-// Bounded wait: false after kSpinLimit polls.
-__device__ __forceinline__ bool mbar_wait(uint32_t bar, uint32_t parity) {
-  for (int i = 0; i < kSpinLimit; ++i)
+// Bounded wait: false after `limit` polls (kSpinLimit by default).
+__device__ __forceinline__ bool mbar_wait(uint32_t bar, uint32_t parity, int limit = kSpinLimit) {
+  for (int i = 0; i < limit; ++i)
     if (mbar_try(bar, parity)) return true;
   return false;
 }

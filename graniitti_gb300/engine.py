@@ -268,6 +268,11 @@ class Flow:
         except Exception:
             pass
 
+    def set_wait_polls(self, polls):
+        """Poll limit of the forward kernel's first bounded wait (< 0: the default); 0 makes
+        the next forward call give up at once and fail with GRN_ERR_CUDA (diagnostic)."""
+        _abi.check(self.lib.grn_flow_set_wait_polls(self.h, int(polls)))
+
     def get_params(self):
         t = np.zeros(self.n_params, dtype=np.float32)
         _abi.check(self.lib.grn_flow_get_params(self.h, _ptr(t)))

@@ -507,6 +507,14 @@ void       grn_flow_default_params(grn_flow_params *p);
 /* The flow lives on the engine's device and stream. */
 grn_status grn_flow_create(grn_engine *e, const grn_flow_params *p, grn_flow **out);
 grn_status grn_flow_destroy(grn_flow *f);
+/* Diagnostic control of the flow's tensor-core forward kernel (no counterpart in the
+ * reference): every wait of the kernel on a copy or a product is bounded, and a wait that
+ * gives up makes the call return GRN_ERR_CUDA (outputs invalid) after the kernel has let
+ * its copies and products in flight complete and released its tensor memory. polls >= 0
+ * sets the poll limit of each CTA's first wait (its first weight copy; 0 gives up at once,
+ * the way to exercise that path); polls < 0 restores the default (2^22 polls). Applies to
+ * the (8, 128) shape. The flow stays usable after such an error. */
+grn_status grn_flow_set_wait_polls(grn_flow *f, int32_t polls);
 int64_t    grn_flow_num_params(const grn_flow *f);
 /* FP32 master weights, layer after layer: W1[4][H], b1[H], W2[H][H], b2[H],
  * W3[H][4(3K+1)], b3[4(3K+1)] (row-major [in][out]). Host or device pointer.

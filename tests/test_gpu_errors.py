@@ -51,3 +51,26 @@ def test_nan_weights_are_zeroed_and_flagged(gpu, params):
     u[0, 0] = np.nan
     w, fl = e.event_weights(u)
     assert np.all(np.isfinite(w)) and w[0] == 0.0
+
+
+def test_flow_wait_timeout_reports_and_recovers(gpu, params):
+    """The bounded waits of the tensor-core flow kernel: with the first wait's poll limit set
+    to 0 it gives up while the weight copy is in flight; the kernel drains the copy, frees its
+    tensor memory and sets its error flag, the call fails with GRN_ERR_CUDA, and the next call
+    (default limit) gives the same result as before."""
+    import graniitti_gb300 as g
+    from graniitti_gb300 import _abi
+    e = g.Engine(params, 0)
+    f = g.Flow(e, seed=3)
+    rng = np.random.default_rng(1)
+    x = rng.random((8, 4096)).astype(np.float32)
+    z0, lq0 = f.density(x)
+    f.set_wait_polls(0)
+    with pytest.raises(_abi.GrnError) as ei:
+        f.density(x)
+    assert ei.value.status == _abi.GRN_ERR_CUDA and "bounded wait" in str(ei.value)
+    f.set_wait_polls(-1)
+    z1, lq1 = f.density(x)
+    assert np.array_equal(z0, z1) and np.array_equal(lq0, lq1)
+    f.close()
+    e.close()
