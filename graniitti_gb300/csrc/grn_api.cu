@@ -1387,8 +1387,11 @@ struct grn_batch {
   int                       max_dim     = 8;  // largest hypercube dimension of the batch
   int                       max_nh      = 0;  // largest bins * dim of the batch
   bool                      has_kind[2] = {false, false};  // generic / record-mode processes
-  cudaStream_t              side = nullptr;     // second branch of the captured graph
-  cudaEvent_t               fork = nullptr, join = nullptr;
+  // per member on the generic loop: its own branch of the captured graph (stage B and the
+  // pass reductions), joined back into the main stream
+  cudaStream_t              side[grn::kMaxBatch] = {};
+  cudaEvent_t               join[grn::kMaxBatch] = {};
+  cudaEvent_t               fork = nullptr;
   cudaGraphExec_t           exec[4] = {};  // by (refine, maximum tracking)
   cudaEvent_t               ev0 = nullptr, ev1 = nullptr;
   double                    last_ms = 0.0;
@@ -1423,41 +1426,48 @@ grn_status batch_capture(grn_batch *b, int refine, int track_max) {
     ce = cudaMemsetAsync(b->d_counter.p, 0, sizeof(unsigned long long), b->stream);
   if (ce == cudaSuccess)
     ce = grn::launch_batch_born(np, b->born_blocks, b->max_dim, b->max_nh, b->stream);
-  // stage B: the record-mode processes in one persistent launch; the processes on the
-  // generic loop in their own launches on a second branch of the graph (concurrent)
-  const bool two = b->has_kind[0] && b->has_kind[1];
-  if (ce == cudaSuccess && two) ce = cudaEventRecord(b->fork, b->stream);
-  if (ce == cudaSuccess && two) ce = cudaStreamWaitEvent(b->side, b->fork, 0);
+  // stage B: the record-mode processes in one persistent launch on the main stream; each
+  // process on the generic loop in its own branch of the graph (its FP32 loop, FP64
+  // refinement and reductions overlap the other processes' work, notably the refinement
+  // passes, which occupy few SMs)
+  auto reduce = [&](int p, cudaStream_t s) {
+    grn_engine *e  = b->eng[p];
+    cudaError_t c = grn::launch_vegas_reduce(e->d_f.as<double>(), e->ncall,
+                                             e->d_acc.as<unsigned long long>(),
+                                             e->d_parts.as<double>(), e->d_sc.as<double>(), s);
+    if (c == cudaSuccess)
+      c = cudaMemcpyAsync(e->h_sc, e->d_sc.p, grn::VS_COUNT * sizeof(double),
+                          cudaMemcpyDeviceToHost, s);
+    if (c == cudaSuccess && refine)
+      c = grn::launch_batch_hist(p, e->bins, e->dim, e->d_hpart.as<double>(),
+                                 e->d_f2mat.as<double>(), s);
+    if (c == cudaSuccess && refine)
+      c = grn::launch_vegas_refine(e->d_xmat.as<double>(), e->d_f2mat.as<double>(), e->bins,
+                                   e->dim, e->lambda, s);
+    return c;
+  };
+  auto generic = [&](int p) { return b->eng[p]->P.screening && !b->h_procs[p].rf; };
+  if (ce == cudaSuccess && b->has_kind[0]) ce = cudaEventRecord(b->fork, b->stream);
+  for (int p = 0; p < np && ce == cudaSuccess; ++p) {
+    if (!generic(p)) continue;
+    grn_engine *e = b->eng[p];
+    ce = cudaStreamWaitEvent(b->side[p], b->fork, 0);
+    if (ce == cudaSuccess)
+      ce = grn::launch_vegas_loop(b->h_procs[p].A, GRN_PREC_MIXED, e->bins, e->dim, e->ncall,
+                                  track_max, e->d_f.as<double>(),
+                                  e->d_acc.as<unsigned long long>(), e->d_lidx.as<int64_t>(),
+                                  e->d_lx.as<double>(), e->d_lvw.as<double>(), nullptr, nullptr,
+                                  e->d_rlist.as<int64_t>(), e->nblocks, b->side[p]);
+    if (ce == cudaSuccess) ce = reduce(p, b->side[p]);
+    if (ce == cudaSuccess) ce = cudaEventRecord(b->join[p], b->side[p]);
+  }
   if (ce == cudaSuccess && b->has_kind[1])
     ce = grn::launch_batch_loop(np, b->d_counter.as<unsigned long long>(), b->loop_blocks,
-                                b->max_nh,
-                                b->stream);
-  for (int p = 0; p < np && ce == cudaSuccess; ++p) {
-    grn_engine *e = b->eng[p];
-    if (!e->P.screening || b->h_procs[p].rf) continue;
-    ce = grn::launch_vegas_loop(b->h_procs[p].A, GRN_PREC_MIXED, e->bins, e->dim, e->ncall,
-                                track_max, e->d_f.as<double>(), e->d_acc.as<unsigned long long>(),
-                                e->d_lidx.as<int64_t>(), e->d_lx.as<double>(),
-                                e->d_lvw.as<double>(), nullptr, nullptr,
-                                e->d_rlist.as<int64_t>(), e->nblocks,
-                                two ? b->side : b->stream);
-  }
-  if (ce == cudaSuccess && two) ce = cudaEventRecord(b->join, b->side);
-  if (ce == cudaSuccess && two) ce = cudaStreamWaitEvent(b->stream, b->join, 0);
-  for (int p = 0; p < np && ce == cudaSuccess; ++p) {
-    grn_engine *e = b->eng[p];
-    ce = grn::launch_vegas_reduce(e->d_f.as<double>(), e->ncall, e->d_acc.as<unsigned long long>(),
-                                  e->d_parts.as<double>(), e->d_sc.as<double>(), b->stream);
-    if (ce == cudaSuccess)
-      ce = cudaMemcpyAsync(e->h_sc, e->d_sc.p, grn::VS_COUNT * sizeof(double),
-                           cudaMemcpyDeviceToHost, b->stream);
-    if (ce == cudaSuccess && refine)
-      ce = grn::launch_batch_hist(p, e->bins, e->dim, e->d_hpart.as<double>(),
-                                  e->d_f2mat.as<double>(), b->stream);
-    if (ce == cudaSuccess && refine)
-      ce = grn::launch_vegas_refine(e->d_xmat.as<double>(), e->d_f2mat.as<double>(), e->bins,
-                                    e->dim, e->lambda, b->stream);
-  }
+                                b->max_nh, b->stream);
+  for (int p = 0; p < np && ce == cudaSuccess; ++p)
+    if (!generic(p)) ce = reduce(p, b->stream);
+  for (int p = 0; p < np && ce == cudaSuccess; ++p)
+    if (generic(p)) ce = cudaStreamWaitEvent(b->stream, b->join[p], 0);
   cudaGraph_t       g  = nullptr;
   const cudaError_t ce2 = cudaStreamEndCapture(b->stream, &g);
   if (ce != cudaSuccess || ce2 != cudaSuccess) {
@@ -1498,14 +1508,17 @@ grn_status grn_batch_create(grn_engine *const *engines, int32_t n, grn_batch **o
   b->device = dev;
   b->eng.assign(engines, engines + n);
   grn_status st = GRN_OK;
-  if (cudaStreamCreateWithFlags(&b->stream, cudaStreamNonBlocking) != cudaSuccess ||
-      cudaStreamCreateWithFlags(&b->side, cudaStreamNonBlocking) != cudaSuccess ||
+  bool sides_ok = true;
+  for (int p = 0; p < n; ++p)
+    sides_ok = sides_ok &&
+               cudaStreamCreateWithFlags(&b->side[p], cudaStreamNonBlocking) == cudaSuccess &&
+               cudaEventCreateWithFlags(&b->join[p], cudaEventDisableTiming) == cudaSuccess;
+  if (!sides_ok || cudaStreamCreateWithFlags(&b->stream, cudaStreamNonBlocking) != cudaSuccess ||
       cudaMallocHost(reinterpret_cast<void **>(&b->h_procs), n * sizeof(grn::BatchProc)) !=
           cudaSuccess ||
       b->d_counter.ensure(2 * sizeof(unsigned long long)) != cudaSuccess ||
       cudaEventCreate(&b->ev0) != cudaSuccess || cudaEventCreate(&b->ev1) != cudaSuccess ||
-      cudaEventCreateWithFlags(&b->fork, cudaEventDisableTiming) != cudaSuccess ||
-      cudaEventCreateWithFlags(&b->join, cudaEventDisableTiming) != cudaSuccess) {
+      cudaEventCreateWithFlags(&b->fork, cudaEventDisableTiming) != cudaSuccess) {
     cudaGetLastError();
     st = fail(GRN_ERR_CUDA, "batch: allocation failed");
   }
@@ -1582,8 +1595,10 @@ grn_status grn_batch_destroy(grn_batch *b) {
   if (b->ev0) cudaEventDestroy(b->ev0);
   if (b->ev1) cudaEventDestroy(b->ev1);
   if (b->fork) cudaEventDestroy(b->fork);
-  if (b->join) cudaEventDestroy(b->join);
-  if (b->side) cudaStreamDestroy(b->side);
+  for (int p = 0; p < grn::kMaxBatch; ++p) {
+    if (b->join[p]) cudaEventDestroy(b->join[p]);
+    if (b->side[p]) cudaStreamDestroy(b->side[p]);
+  }
   if (b->stream) cudaStreamDestroy(b->stream);
   if (b->registered)
     for (grn_engine *e : b->eng) e->in_batches -= 1;

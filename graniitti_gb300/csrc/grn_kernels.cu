@@ -436,10 +436,7 @@ template <typename T, bool CASC>
 __device__ double screened_weight(const KArgs &A, const double *x, uint8_t &flags,
                                   const KtNode<T> *skt, const PhiNode<T> *sphi,
                                   bool *refine = nullptr) {
-  if (CASC && is_nbody(A.P)) {
-    if (refine) *refine = false;
-    return nbody_screened_weight<T>(A, x, flags, skt, sphi);
-  }
+  if (CASC && is_nbody(A.P)) return nbody_screened_weight<T>(A, x, flags, skt, sphi, refine);
   Born b;
   born_kinematics<CASC>(A.P, A.K, x, b);
   double amp2, mag = 0.0;

@@ -397,6 +397,242 @@ __device__ cx<double> nbody_loop(const KArgs &A, const NBEvent &e, const KtNode<
   return {A.loop_norm_re * ar - A.loop_norm_im * ai, A.loop_norm_re * ai + A.loop_norm_im * ar};
 }
 
+// FP32 kt-loop of the N-body amplitude for one Regge trajectory (alpha(t) = a0 + ap t,
+// signature factor eta). In both classes the central particles keep their momenta in the loop
+// (factorized: MFactorized::LoopKinematics; continuum: their transverse momenta depend on the
+// forward legs only through p1T + p2T, which the loop leaves unchanged), so only the forward
+// legs move. With one trajectory each ordering (a b c d) of the ladder is
+//   eta^3 e^{-i pi ap (t1 + t_ab + t2) / 2} e^{x_1a + x_abc + x_2d} f_a f_ab f_d
+// with real exponents x = alpha(t) (ln s - ln s0) of size ~10: their FP32 rounding alone would
+// leave ~1e-6 relative error per propagator. So each exponent is split into its tree-level
+// value (FP64 per event; rho = e^{x_term - X} per ordering, X the largest) and an increment
+//   x - x0 = ap (t - t0) l0 + alpha(t) ln(s / s0)
+// formed from explicit differences of the light-cone components (t - t0, s / s0 - 1 and
+// t_ab - t_ab0 never subtract two large numbers), which is small where the loop integrand is
+// large; the phases e^{-i pi ap t / 2} likewise as tree-level phase times increment. Form
+// factors and vertices run in FP32 on the point's own invariants.
+template <typename T>
+struct LCT {
+  T p, m, x, y;
+};
+template <typename T>
+GRN_HD T lct_dot(const LCT<T> &a, const LCT<T> &b) {
+  return T(0.5) * (a.p * b.m + a.m * b.p) - a.x * b.x - a.y * b.y;
+}
+
+constexpr int kNbPairs = 6;   // unordered pairs {a < b}: (01) (02) (03) (12) (13) (23)
+constexpr int kNbTerms = 24;  // orderings, 4 per pair
+
+struct NBLoopF {
+  LCT<float> c[kNb];                // central particles
+  float      m2[kNb];
+  float      p1x, p1y, p2x, p2y;    // tree-level forward transverse momenta
+  float      a1, a2, ia1, ia2, L, invL, invL2, mp2;
+  float      x1r, x2r;              // tree level x1 - a1 = c2 r2, x2 - a2 = c1 r1
+  float      p1m, p2p, g1m, g2p;    // tree level p1-, p2+, q1-, q2+
+  float      t1, t2;                // tree level t1, t2
+  float      is1[kNb], is2[kNb];    // 1 / s_1a, 1 / s_2a at tree level
+  float      l1[kNb], l2[kNb];      // ln s_1a - ln s0, ln s_2a - ln s0 at tree level
+  float      tab[kNbPairs];         // t_ab at tree level
+  cx<float>  ph[kNbPairs];          // e^{-i pi ap t_ab / 2} at tree level
+  float      ljk[kNb][kNb];         // ln s_jk - ln s0
+  float      rho[kNbTerms];         // e^{x_term - X} at tree level
+  float      a0, ap;
+};
+
+// The ordering o = 0..3 of pair {a < b}: (i, j, k, l) = (a, b, c0, c1), (a, b, c1, c0),
+// (b, a, c0, c1), (b, a, c1, c0) with c0 < c1 the two particles left.
+GRN_HD void nb_order(int a, int b, int o, int &i, int &j, int &k, int &l) {
+  const int c0 = (a == 0) ? (b == 1 ? 2 : 1) : 0;
+  const int c1 = 6 - a - b - c0;
+  i = o < 2 ? a : b;
+  j = o < 2 ? b : a;
+  k = (o & 1) ? c1 : c0;
+  l = (o & 1) ? c0 : c1;
+}
+
+// Tree-level constants of the FP32 loop (FP64 in, FP32 out); *omega = eta^3 e^X
+// e^{-i pi ap (t1 + t2) / 2} at tree level, the factor applied to the loop sum in FP64. The forward legs close with the two-step form of the point.
+GRN_HD void make_nbody_loop_f(const grn_process_params &P, const Consts &K, const NBEvent &e,
+                              int q, NBLoopF &f, cx<double> &omega) {
+  const double a0 = P.regge.a0[q], ap = P.regge.ap[q], l0 = K.lns0;
+  const double L = K.L, iL = 1.0 / L, iL2 = iL * iL, mp2 = K.mp2;
+  const double ia1 = 1.0 / (1.0 - e.a1), ia2 = 1.0 / (1.0 - e.a2);
+  const double mT1sq = mp2 + e.pt1sq, mT2sq = mp2 + e.pt2sq;
+  const double c1 = mT1sq * iL2, c2 = mT2sq * iL2;
+  const double r1 = 1.0 / (1.0 - (e.a1 + c2 * ia2)), r2 = 1.0 / (1.0 - (e.a2 + c1 * ia1));
+  const double x1r = c2 * r2, x2r = c1 * r1, x1 = e.a1 + x1r, x2 = e.a2 + x2r;
+  const LC4 p1{(1.0 - x1) * L, mT1sq * r1 * iL, e.p1x, e.p1y};
+  const LC4 p2{mT2sq * r2 * iL, (1.0 - x2) * L, e.p2x, e.p2y};
+  const LC4 g1{x1 * L, -(e.pt1sq + x1 * mp2) * r1 * iL, -e.p1x, -e.p1y};
+  const LC4 g2{-(e.pt2sq + x2 * mp2) * r2 * iL, x2 * L, -e.p2x, -e.p2y};
+  const double t1 = -(e.pt1sq + x1 * x1 * mp2) * r1, t2 = -(e.pt2sq + x2 * x2 * mp2) * r2;
+  double x1a[kNb], x2a[kNb], d1[kNb], ljk[kNb][kNb], tab[kNbPairs], xt[kNbTerms];
+  for (int a = 0; a < kNb; ++a) {
+    f.c[a]  = {float(e.c[a].p), float(e.c[a].m), float(e.c[a].x), float(e.c[a].y)};
+    f.m2[a] = float(e.m2[a]);
+    const double s1 = mp2 + e.m2[a] + 2.0 * lc_dot(p1, e.c[a]);
+    const double s2 = mp2 + e.m2[a] + 2.0 * lc_dot(p2, e.c[a]);
+    f.is1[a] = float(1.0 / s1);
+    f.is2[a] = float(1.0 / s2);
+    const double l1 = log(s1) - l0, l2 = log(s2) - l0;
+    f.l1[a] = float(l1);
+    f.l2[a] = float(l2);
+    x1a[a]  = (a0 + ap * t1) * l1;
+    x2a[a]  = (a0 + ap * t2) * l2;
+    d1[a]   = lc_dot(g1, e.c[a]);
+    for (int b = 0; b < kNb; ++b) {
+      ljk[a][b]   = b == a ? 0.0 : log(e.sbc[a][b]) - l0;
+      f.ljk[a][b] = float(ljk[a][b]);
+    }
+  }
+  double X = -1e300;
+  for (int a = 0, p = 0; a < kNb; ++a)
+    for (int b = a + 1; b < kNb; ++b, ++p) {
+      tab[p]   = t1 + e.sbc[a][b] - 2.0 * (d1[a] + d1[b]);
+      f.tab[p] = float(tab[p]);
+      double sn, cs;
+      sincos_pi(-0.5 * ap * tab[p], sn, cs);
+      f.ph[p] = {float(cs), float(sn)};
+      for (int o = 0; o < 4; ++o) {
+        int i, j, k, l;
+        nb_order(a, b, o, i, j, k, l);
+        xt[4 * p + o] = x1a[i] + (a0 + ap * tab[p]) * ljk[j][k] + x2a[l];
+        X = fmax(X, xt[4 * p + o]);
+      }
+    }
+  for (int t = 0; t < kNbTerms; ++t) f.rho[t] = float(exp(xt[t] - X));
+  f.p1x = float(e.p1x); f.p1y = float(e.p1y); f.p2x = float(e.p2x); f.p2y = float(e.p2y);
+  f.a1 = float(e.a1); f.a2 = float(e.a2); f.ia1 = float(ia1); f.ia2 = float(ia2);
+  f.L = float(L); f.invL = float(iL); f.invL2 = float(iL2); f.mp2 = float(mp2);
+  f.x1r = float(x1r); f.x2r = float(x2r);
+  f.p1m = float(p1.m); f.p2p = float(p2.p); f.g1m = float(g1.m); f.g2p = float(g2.p);
+  f.t1 = float(t1); f.t2 = float(t2);
+  f.a0 = float(a0); f.ap = float(ap);
+  const cx<double> eta{K.eta0_re[q], K.eta0_im[q]};
+  double sn, cs;
+  sincos_pi(-0.5 * ap * (t1 + t2), sn, cs);
+  omega = cscale(cmul(cmul(cmul(eta, eta), eta), cx<double>{cs, sn}), exp(X));
+}
+
+// ME6 / omega at one loop point (forward legs p1T - k, p2T + k) in FP32; false when the
+// point is kinematically invalid or an invariant check fails (as nbody_amp). *mag = |vertex|
+// sum over pairs of |f_ab| sum of the pair's four (positive) real ladder factors: the scale of
+// the point's FP32 error, with the cancellation among the pairs' phases.
+GRN_HD bool nbody_point_f(const grn_process_params &P, const Consts &K, const NBLoopF &f,
+                          float kx, float ky, cx<float> &A, float &mag) {
+  const grn_regge_params &rp = P.regge;
+  const float q1x = f.p1x - kx, q1y = f.p1y - ky, q2x = f.p2x + kx, q2y = f.p2y + ky;
+  const float pt1sq = q1x * q1x + q1y * q1y, pt2sq = q2x * q2x + q2y * q2y;
+  const float mT1sq = f.mp2 + pt1sq, mT2sq = f.mp2 + pt2sq;
+  const float c1 = mT1sq * f.invL2, c2 = mT2sq * f.invL2;
+  const float r1 = 1.f / (1.f - (f.a1 + c2 * f.ia2)), r2 = 1.f / (1.f - (f.a2 + c1 * f.ia1));
+  const float x1r = c2 * r2, x2r = c1 * r1;
+  const float x1 = f.a1 + x1r, x2 = f.a2 + x2r;
+  if (!(x1 > 0.f && x2 > 0.f && x1 < 1.f && x2 < 1.f)) return false;
+  // t = -(pT^2 + x^2 mp^2) r: its increment from pT'^2 - pT^2 = k^2 -+ 2 pT.k and
+  // x - x0 = x1r - x1r0 (r - r0 = r r0 (x - x0)), exact where k -> 0
+  const float dx1 = x1r - f.x1r, dx2 = x2r - f.x2r;
+  const float k2 = kx * kx + ky * ky;
+  const float dpt1 = k2 - 2.f * (f.p1x * kx + f.p1y * ky);
+  const float dpt2 = k2 + 2.f * (f.p2x * kx + f.p2y * ky);
+  const float dt1 = f.t1 * r1 * dx1 - (dpt1 + dx1 * (2.f * f.a1 + x1r + f.x1r) * f.mp2) * r1;
+  const float dt2 = f.t2 * r2 * dx2 - (dpt2 + dx2 * (2.f * f.a2 + x2r + f.x2r) * f.mp2) * r2;
+  const float t1 = f.t1 + dt1, t2 = f.t2 + dt2;
+  if (t1 > 0.f || t2 > 0.f) return false;
+  // increments of p1 = ((1 - x1) L, p1-, q1T), p2, q1 = (x1 L, q1-, -q1T), q2 over the tree
+  // level; their transverse parts are -k, +k, +k, -k
+  const float dx1L = dx1 * f.L, dx2L = dx2 * f.L;
+  const float dp1m = mT1sq * r1 * f.invL - f.p1m, dp2p = mT2sq * r2 * f.invL - f.p2p;
+  const float dg1m = -(pt1sq + x1 * f.mp2) * r1 * f.invL - f.g1m;
+  const float dg2p = -(pt2sq + x2 * f.mp2) * r2 * f.invL - f.g2p;
+  const float g1p = x1 * f.L, g1m = f.g1m + dg1m, g2m = x2 * f.L, g2p = f.g2p + dg2p;
+  const float al1 = f.a0 + f.ap * t1, al2 = f.a0 + f.ap * t2;
+  const float MA = float(K.m3sq), MB = float(K.M2propB);
+  float e1[kNb], e2[kNb], f1[kNb], f2[kNb], dd1[kNb];
+#pragma unroll
+  for (int a = 0; a < kNb; ++a) {
+    const LCT<float> &c  = f.c[a];
+    const float       kc = kx * c.x + ky * c.y;
+    // s / s0 - 1 = 2 (dp . c) / s0
+    const float y1 = (-dx1L * c.m + dp1m * c.p + 2.f * kc) * f.is1[a];
+    const float y2 = (dp2p * c.m - dx2L * c.p - 2.f * kc) * f.is2[a];
+    if (!(y1 >= -1.f && y2 >= -1.f)) return false;
+    e1[a]  = f.ap * dt1 * f.l1[a] + al1 * log1pf(y1);
+    e2[a]  = f.ap * dt2 * f.l2[a] + al2 * log1pf(y2);
+    dd1[a] = 0.5f * (dx1L * c.m + dg1m * c.p) - kc;
+    const float d1 = 0.5f * (g1p * c.m + g1m * c.p) + q1x * c.x + q1y * c.y;
+    const float d2 = 0.5f * (g2p * c.m + g2m * c.p) + q2x * c.x + q2y * c.y;
+    const float ta = t1 + f.m2[a] - 2.f * d1, td = t2 + f.m2[a] - 2.f * d2;
+    f1[a] = meson_ff<float>(rp, ta, MA) / (ta - MA);
+    f2[a] = meson_ff<float>(rp, td, MB) / (td - MB);
+  }
+  cx<float> S{0.f, 0.f};
+  float     M = 0.f;
+#pragma unroll
+  for (int a = 0, p = 0; a < kNb; ++a)
+#pragma unroll
+    for (int b = a + 1; b < kNb; ++b, ++p) {
+      const float dtab = dt1 - 2.f * (dd1[a] + dd1[b]);
+      const float tab  = f.tab[p] + dtab;
+      const float fab  = meson_ff<float>(rp, tab, MA) * meson_ff<float>(rp, tab, MB);
+      const float apd  = f.ap * dtab;
+      float       Sp   = 0.f;
+#pragma unroll
+      for (int o = 0; o < 4; ++o) {
+        int i, j, k, l;
+        nb_order(a, b, o, i, j, k, l);
+        Sp += f.rho[4 * p + o] * exp(e1[i] + apd * f.ljk[j][k] + e2[l]) * (f1[i] * f2[l]);
+      }
+      float sn, cs;
+      sincos_pi(-0.5f * apd, sn, cs);
+      const cx<float> ph = cmul(f.ph[p], cx<float>{cs, sn});
+      S.re += fab * Sp * ph.re;
+      S.im += fab * Sp * ph.im;
+      M += fabsf(fab * Sp);
+    }
+  float sn, cs;
+  sincos_pi(-0.5f * f.ap * (dt1 + dt2), sn, cs);
+  const float g2c = float(K.g2);
+  const float vtx = float(K.gN2) * proton_ff<float>(float(P.soft.fc1), float(P.soft.fc2), t1) *
+                    proton_ff<float>(float(P.soft.fc1), float(P.soft.fc2), t2) * g2c * g2c;
+  A   = cscale(cmul(S, cx<float>{cs, sn}), vtx);
+  mag = M * fabsf(vtx);
+  return true;
+}
+
+// FP32 loop integral with compensated sums (one trajectory); *mag: sum_ij |U_i c_j| mag_ij in
+// units of the returned amplitude (see loop_integral for the summation part).
+__device__ cx<double> nbody_loop_f(const KArgs &A, const NBEvent &e, const KtNode<float> *skt,
+                                   const PhiNode<float> *sphi, double *mag) {
+  const int q = A.K.active[0] ? 0 : (A.K.active[1] ? 1 : 2);
+  NBLoopF    f;
+  cx<double> omega;
+  make_nbody_loop_f(A.P, A.K, e, q, f, omega);
+  float ar = 0.f, ai = 0.f, cr = 0.f, ci = 0.f, m = 0.f;
+  for (int j = 0; j < A.n_kt_nodes; ++j) {
+    const KtNode<float> nj = skt[j];
+    float ir = 0.f, ii = 0.f, dr = 0.f, di = 0.f, ab = 0.f;
+    for (int i = 0; i < A.n_phi_nodes; ++i) {
+      const PhiNode<float> ni = sphi[i];
+      cx<float> a;
+      float     ma;
+      if (!nbody_point_f(A.P, A.K, f, nj.kt * ni.c, nj.kt * ni.s, a, ma)) continue;
+      kahan_add(ir, dr, ni.u * a.re);
+      kahan_add(ii, di, ni.u * a.im);
+      ab += ni.u * ma;
+    }
+    kahan_add(ar, cr, nj.cre * ir - nj.cim * ii);
+    kahan_add(ai, ci, nj.cre * ii + nj.cim * ir);
+    m += sqrtf(nj.cre * nj.cre + nj.cim * nj.cim) * ab;
+  }
+  const double om = sqrt(omega.re * omega.re + omega.im * omega.im);
+  *mag = double(m) * om;
+  const cx<double> s = cmul(omega, cx<double>{double(ar), double(ai)});
+  return {A.loop_norm_re * s.re - A.loop_norm_im * s.im,
+          A.loop_norm_re * s.im + A.loop_norm_im * s.re};
+}
+
 // Stage A of an N-body point: kinematics, cuts and (unscreened) the weight; true when the
 // point needs the kt-loop. Flags as born_stage.
 __device__ __noinline__ bool nbody_born_stage(const KArgs &A, const double *x, double &W,
@@ -422,18 +658,39 @@ __device__ __noinline__ bool nbody_born_stage(const KArgs &A, const double *x, d
   return false;
 }
 
-// Screened weight of an N-body point that passed stage A (FP64 loop whatever T).
+// Screened weight of an N-body point that passed stage A: T = double the FP64 loop; T = float
+// the FP32 loop for one trajectory (the FP64 loop for several), and with refine non-null
+// *refine tells whether its estimated relative error 2 kRefineKappa u |norm| mag / |A0 + A_loop|
+// exceeds A.refine_tol (or is not finite): the caller then recomputes the point with T = double.
 template <typename T>
 __device__ __noinline__ double nbody_screened_weight(const KArgs &A, const double *x,
                                                      uint8_t &flags, const KtNode<T> *skt,
-                                                     const PhiNode<T> *sphi) {
+                                                     const PhiNode<T> *sphi,
+                                                     bool *refine = nullptr) {
   NBEvent e;
   NBLegs  g;
   cx<double> A0{0.0, 0.0};
   nbody_kinematics(A.P, A.K, x, e);
   nbody_legs(A.K, e, e.p1x, e.p1y, e.p2x, e.p2y, g);
   nbody_amp(A.P, A.K, e, g, A0);
-  const cx<double> Al = nbody_loop<T>(A, e, skt, sphi);
+  cx<double> Al;
+  bool       fp32 = false;
+  if (refine) *refine = false;
+  if constexpr (sizeof(T) == sizeof(float)) {
+    if (A.K.n_active == 1) {
+      fp32        = true;
+      double mag  = 0.0;
+      Al = nbody_loop_f(A, e, skt, sphi, &mag);
+      const double re = A0.re + Al.re, im = A0.im + Al.im;
+      if (refine) {
+        const double norm =
+            sqrt(A.loop_norm_re * A.loop_norm_re + A.loop_norm_im * A.loop_norm_im);
+        const double est = 2.0 * kRefineKappa * 0x1p-24 * norm * mag;
+        *refine = A.refine_tol > 0.0 && !(est <= A.refine_tol * sqrt(re * re + im * im));
+      }
+    }
+  }
+  if (!fp32) Al = nbody_loop<T>(A, e, skt, sphi);
   const double re = A0.re + Al.re, im = A0.im + Al.im;
   double W = nbody_jacobian(A.K, e, g) * (re * re + im * im);
   flags = GRN_FLAG_KINEMATICS_OK | GRN_FLAG_FIDCUTS_OK | GRN_FLAG_VETOCUTS_OK |

@@ -1177,7 +1177,17 @@ GRN_HD_COLD void regge_res_event(const grn_process_params &P, const Consts &K, d
     const double na = sqrt(ax * ax + ay * ay + az * az), nb = sqrt(bx * bx + by * by + bz * bz);
     direction<double>(ax / na - bx / nb, ay / na - by / nb, az / na - bz / nb, ct, st, cp, sp);
   }
-  const double hc = sqrt(fmax(0.0, 0.5 * (1.0 + ct))), hs = sqrt(fmax(0.0, 0.5 * (1.0 - ct)));
+  // half-angle cosine and sine; the smaller one from sin theta_R = 2 hc hs (the form
+  // sqrt((1 - cos) / 2) would keep few digits for theta_R -> 0, the frame of a central
+  // system with vanishing transverse momentum)
+  double hc, hs;
+  if (ct >= 0.0) {
+    hc = sqrt(0.5 * (1.0 + ct));
+    hs = 0.5 * st / hc;
+  } else {
+    hs = sqrt(0.5 * (1.0 - ct));
+    hc = 0.5 * st / hs;
+  }
   // D_{ij} = d^2_{M_i M_j}(theta_R) e^{i M_j phi_R}
   double Dr[5][5], Di[5][5];
   for (int j = 0; j < 5; ++j) {

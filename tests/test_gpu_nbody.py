@@ -68,11 +68,41 @@ def test_four_body_screened_weights_match_reference(gpu, name):
     r = _rel(w, gl["w"])
     print("%s: GPU FP64 vs reference max rel %.2e" % (name, r.max()))
     assert r.max() < 1e-9
-    # the FP32 pass runs the 4-body loop in FP64 from FP32-rounded loop nodes
+    # MIXED: the FP32 4-body loop, events whose error estimate exceeds 1e-5 redone in FP64
     wm, _ = e.event_weights(gl["u"], prec=g.MIXED)
     rm = _rel(wm, gl["w"])
-    print("%s: GPU MIXED vs reference max rel %.2e" % (name, rm.max()))
+    e.set_tuning(fp64_refine=0)
+    w32, _ = e.event_weights(gl["u"], prec=g.MIXED)
+    r32 = _rel(w32, gl["w"])
+    print("%s: GPU MIXED vs reference max rel %.2e (FP32 loop alone %.2e)"
+          % (name, rm.max(), r32.max()))
     assert rm.max() < 1e-5
+    # the FP32 loop ran: its weights are not the FP64 ones
+    assert not np.array_equal(w32, w)
+    e.close()
+
+
+@pytest.mark.parametrize("card_name", ["f4_screened", "c4_screened"])
+def test_four_body_fp32_loop_vs_fp64(gpu, card_name):
+    """The FP32 4-body loop with FP64 refinement against the FP64 loop over 2^14 seeded
+    points: relative weight difference below 1e-5 on every point (the refinement bound)."""
+    import graniitti_gb300 as g
+    import philox_np
+    gl = _load(card_name + "_weights.npz")
+    t = _load("eikonal_nbt1024_nkt10000.npz")
+    P = _params(gl)
+    e = g.Engine(P, 0)
+    e.eikonal_set(t["mbt"], t["msa"])
+    u = philox_np.uniforms(91, 1 << 14, 14)
+    w64, fl = e.event_weights(u, prec=g.FP64)
+    wm, flm = e.event_weights(u, prec=g.MIXED)
+    assert np.array_equal(fl, flm)
+    nz = w64 > 0
+    assert nz.sum() > 500 and np.array_equal(wm > 0, nz)
+    r = np.abs(wm[nz] - w64[nz]) / w64[nz]
+    print("%s: MIXED vs FP64 over %d points with W > 0: max rel %.2e, median %.2e"
+          % (card_name, nz.sum(), r.max(), np.median(r)))
+    assert r.max() < 1e-5
     e.close()
 
 
