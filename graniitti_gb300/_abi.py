@@ -104,7 +104,8 @@ class ProcessParams(ctypes.Structure):
                 ("offshell_user", c_int32), ("omega", c_double), ("offshell", c_double),
                 ("veto_active", c_int32), ("n_veto", c_int32),
                 ("veto_eta_min", c_double * GRN_MAX_VETO), ("veto_eta_max", c_double * GRN_MAX_VETO),
-                ("veto_pt_min", c_double * GRN_MAX_VETO), ("veto_pt_max", c_double * GRN_MAX_VETO)]
+                ("veto_pt_min", c_double * GRN_MAX_VETO), ("veto_pt_max", c_double * GRN_MAX_VETO),
+                ("excitation", c_int32), ("_pad_x", c_int32), ("xi_max", c_double)]
 
 
 class VegasParams(ctypes.Structure):
@@ -139,7 +140,7 @@ class HistSpec(ctypes.Structure):
 
 class Tuning(ctypes.Structure):
     _fields_ = [("loop_pair", c_int32), ("vegas_blocks", c_int32), ("weight_blocks", c_int32),
-                ("fp64_refine", c_int32)]
+                ("fp64_refine", c_int32), ("refine_tol", c_double)]
 
 
 class TuneResult(ctypes.Structure):

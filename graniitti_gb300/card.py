@@ -187,8 +187,12 @@ def build_params(card, process=None, tune=None):
     if channel in ("RES", "RES+CON", "RESTENSOR", "RES+CONTENSOR") and \
             sorted(finals) not in (["pi+", "pi-"], ["K+", "K-"]):
         raise UnsupportedProcess("%s is implemented for pi+ pi- and K+ K- decays" % channel)
-    if int(pp.get("NSTARS", 0)) != 0:
-        raise UnsupportedProcess("forward excitation (NSTARS > 0) is not implemented")
+    nstars = int(pp.get("NSTARS", 0))
+    if nstars not in (0, 1, 2):
+        raise ValueError("NSTARS must be 0, 1 or 2")
+    if nstars and not (channel == "CON" and len(finals) == 2 and not any(casc)):
+        raise UnsupportedProcess("forward excitation (NSTARS > 0) is implemented for the Regge "
+                                 "continuum of two central particles")
     if pp["BEAM"] != ["p+", "p+"]:
         raise UnsupportedProcess("beams other than p+ p+ are not implemented")
     E1, E2 = float(pp["ENERGY"][0]), float(pp["ENERGY"][1])
@@ -235,8 +239,18 @@ def build_params(card, process=None, tune=None):
     P.gcuts.rap_min, P.gcuts.rap_max = rap
     kt = g.get("Kt", [0.0, 10.0 / len(finals)])
     P.gcuts.kt_min, P.gcuts.kt_max = kt
-    pt = g.get("Pt", [0.0, 2.5])
+    # forward pT: the technical boundary of MProcess::SetTechnicalBoundaries (src/MProcess.cc:
+    # 1369-1386) grows with the excitation (2.5, 50, 100 GeV) unless set by the user
+    pt = g.get("Pt", [0.0, (2.5, 50.0, 100.0)[nstars]])
     P.gcuts.fpt_min, P.gcuts.fpt_max = pt
+    # forward excitation (NSTARS; GENCUTS "Xi" of the class: M^2 / s of an excited leg)
+    P.excitation = nstars
+    P.xi_max = 1.0
+    xi = card.get("GENCUTS", {}).get("<%s>" % cls, {}).get("Xi")
+    if xi is not None:
+        if not (0.0 <= xi[0] <= xi[1] <= 1.0):
+            raise ValueError("GENCUTS Xi must satisfy 0 <= min <= max <= 1")
+        P.xi_max = float(xi[1])
     # <F>: system rapidity and mass windows (MGraniitti::ReadGenCuts; GENCUT defaults)
     gf = card.get("GENCUTS", {}).get("<F>", {})
     P.gcuts.Y_min, P.gcuts.Y_max = gf.get("Rap", [-9.0, 9.0])
@@ -244,8 +258,7 @@ def build_params(card, process=None, tune=None):
     if cls == "F":
         if "Rap" not in gf or "M" not in gf:
             raise ValueError('<F> needs "GENCUTS" : { "<F>" : { "Rap" : [..], "M" : [..] } }')
-        if "Pt" in gf:
-            P.gcuts.fpt_min, P.gcuts.fpt_max = gf["Pt"]
+        P.gcuts.fpt_min, P.gcuts.fpt_max = gf.get("Pt", [0.0, (2.5, 50.0, 100.0)[nstars]])
 
     # Fiducial cuts (FIDCUT defaults, MKinematics.h:1579-1611).
     f = card.get("FIDCUTS", {})

@@ -82,7 +82,7 @@ inline CF2 sinpi_turns2(CF2 d) {
   return {CF(std::sin(grn::kPi * d.x.v)), CF(std::sin(grn::kPi * d.y.v))};
 }
 struct KtNodeC {
-  CF2 kt, k2, cre, cim, ncim;
+  CF2 kt, k2, cre, cim, ncim, cabs;
 };
 struct PhiNodeC {
   CF2 c, s, u, t;
@@ -114,7 +114,7 @@ int main() {
   for (int j = 0; j < n_kt; ++j) {
     const float k = float(1e-4 + j * (3.0 - 1e-4) / (n_kt - 1));
     kt[j] = {grn::splat<CF2>(k), grn::splat<CF2>(k * k), grn::splat<CF2>(1.f),
-             grn::splat<CF2>(0.5f), grn::splat<CF2>(-0.5f)};
+             grn::splat<CF2>(0.5f), grn::splat<CF2>(-0.5f), grn::splat<CF2>(1.118f)};
   }
   for (int i = 0; i < n_phi; ++i) {
     const double a = 2 * grn::kPi * i / (n_phi - 1);
@@ -147,8 +147,8 @@ int main() {
     g_cnt = keep;  // record building (stage A) is not loop-stage work
     grn::Loop3<CF2> e;
     grn::make_loop3<CF2>(a, b, [](CF x, CF y) { return CF2{x, y}; }, e);
-    CF2 sr, si;
-    grn::loop_integral3(e, n_kt, n_phi, kt.data(), ph.data(), sr, si);
+    CF2 sr, si, sm;
+    grn::loop_integral3(e, n_kt, n_phi, kt.data(), ph.data(), sr, si, sm);
     g_cnt.mul += 2 * 4;
     g_cnt.add += 2 * 2;
     points += 2.0 * n_kt * n_phi;

@@ -108,7 +108,8 @@ struct grn_engine {
   DevBuf d_u, d_w, d_flags, d_aux, d_wlist, d_wrlist, d_wcount;
   int    loop_blocks = 0;
   int    loop_pair   = 0;  // record-mode loop: events per thread - 1 (set by grn_autotune)
-  int    fp64_refine = 1;  // FP32 generic loop: redo badly conditioned events in FP64
+  int    fp64_refine = 1;  // FP32 loops: redo badly conditioned events in FP64
+  double refine_tol  = grn::kRefineTol;  // estimated relative error that sends them there
 
   // VEGAS
   int         bins = 0;
@@ -160,7 +161,7 @@ struct grn_engine {
     a.loop_norm_re = 0.0;
     a.loop_norm_im = loop_norm_im;
     a.loop_pair    = loop_pair;
-    a.refine_tol   = fp64_refine ? grn::kRefineTol : 0.0;
+    a.refine_tol   = fp64_refine ? refine_tol : 0.0;
     return a;
   }
 };
@@ -327,6 +328,22 @@ grn_status derive_consts(const grn_process_params &P, grn::Consts &K) {
   }
   if ((P.process == GRN_PROC_TENSOR_RES || rescon || rr) && P.central_spin != 0)
     return fail(GRN_ERR_UNSUPPORTED, "the resonances decay to pseudoscalars");
+  // forward excitation (NSTARS): the Regge continuum of two stable central particles
+  if (P.excitation < 0 || P.excitation > 2)
+    return fail(GRN_ERR_INVALID, "excitation must be 0, 1 or 2");
+  if (P.excitation) {
+    if (P.process != GRN_PROC_REGGE_CON || P.n_central != 2 || P.n_decay != 0)
+      return fail(GRN_ERR_UNSUPPORTED,
+                  "forward excitation: the Regge continuum of two central particles");
+    if (!(P.xi_max > 0.0 && P.xi_max <= 1.0))
+      return fail(GRN_ERR_INVALID, "xi_max must be in (0, 1]");
+    if (!(P.xi_max * P.sqrt_s * P.sqrt_s > 1.09 * 1.09))
+      return fail(GRN_ERR_INVALID, "xi_max s below the inelastic threshold 1.09^2 GeV^2");
+    if (!(P.soft.g3P > 0.0)) return fail(GRN_ERR_INVALID, "the triple-pomeron coupling g3P");
+  }
+  K.lnM2f_lo = std::log(1.09 * 1.09);  // neutron + pi+ threshold (MProcess.cc:1324)
+  K.lnM2f_hi = P.excitation ? std::log(P.xi_max * P.sqrt_s * P.sqrt_s) : K.lnM2f_lo;
+  K.gin      = std::sqrt(std::max(0.0, P.soft.g3P * P.soft.gN_P));
   if (!(P.sqrt_s > 2 * P.m_beam)) return fail(GRN_ERR_INVALID, "sqrt_s below threshold");
   if (!(P.gcuts.fpt_max > 0) || !(P.gcuts.kt_max > P.gcuts.kt_min) ||
       !(P.gcuts.rap_max > P.gcuts.rap_min))
@@ -528,6 +545,8 @@ void grn_default_params(grn_process_params *p) {
   p->loop = {15, 12, 1e-4, 1.75, 10000, 10000};
   // TUNE0 PARAM_TENSORPOM, pion coupling; Kelly proton form factors (GENERAL.json:178-219)
   p->tensor = {0.0808, 0.25, 1.87, 1.76, 1, 0, {0.70, 6.20}};
+  p->excitation = 0;
+  p->xi_max     = 1.0;  // GENCUT default (include/Graniitti/MKinematics.h:1575)
 }
 
 double grn_tensor_decay_coupling(int32_t J, double M, double W, double m_daughter, double BR) {
@@ -596,7 +615,7 @@ grn_status grn_create(const grn_process_params *p, int32_t device, grn_engine **
   e->K          = K;
   // hypercube dimension: 8 for a 2-body point; cascades add the decay angles (4) and, unless
   // OFFSHELL = 0, the two masses (2); 4-body central states have 14
-  e->dim = p->n_central == 4 ? 14 : (p->n_decay == 2 ? K.dec0 + 4 : 8);
+  e->dim = p->n_central == 4 ? 14 : (p->n_decay == 2 ? K.dec0 + 4 : (p->excitation ? 10 : 8));
   cudaError_t ce = cudaStreamCreateWithFlags(&e->stream, cudaStreamNonBlocking);
   if (ce == cudaSuccess) ce = cudaMallocHost(&e->h_sc, grn::VS_COUNT * sizeof(double));
   if (ce == cudaSuccess) ce = cudaEventCreate(&e->ev0);
@@ -760,7 +779,7 @@ grn_status grn_event_weights(grn_engine *e, const double *u, int64_t n, int32_t 
     GRN_CUDA(grn::launch_event_weights_rec(a, du, n, dim, dw, df, e->d_wlist.as<int64_t>(),
                                            e->d_recf.as<float>(), e->d_recd.as<double>(),
                                            e->d_wcount.as<unsigned long long>(), e->loop_blocks,
-                                           e->stream));
+                                           e->stream, e->d_wrlist.as<int64_t>()));
   } else {
     GRN_CUDA(grn::launch_event_weights(a, prec, du, n, dim, dw, df, e->d_wlist.as<int64_t>(),
                                        e->d_wrlist.as<int64_t>(),
@@ -941,19 +960,26 @@ static grn_status vegas_pass(grn_engine *e, int prec, int track_max, int refine,
   const bool  rec = grn::record_mode(a, prec);
   float      *rf  = rec ? e->d_recf.as<float>() : nullptr;
   double     *rd  = rec ? e->d_recd.as<double>() : nullptr;
+  // the mapped points of listed events: the generic loop's input; in record mode only the
+  // input of the FP64 refinement
+  double *lx = (rec && a.refine_tol <= 0.0) ? nullptr : e->d_lx.as<double>();
   GRN_CUDA(grn::launch_vegas_born(a, xmat, e->bins, e->dim, e->ncall, e->seed,
                                   stream_id, track_max, e->d_f.as<double>(),
                                   e->d_acc.as<unsigned long long>(), e->d_lidx.as<int64_t>(),
-                                  e->d_lx.as<double>(), e->d_lvw.as<double>(), rf, rd,
-                                  e->stream, fu, flq));
-  // the timed kernel: the kt-loop stage when screening is on
+                                  lx, e->d_lvw.as<double>(), rf, rd, e->stream, fu, flq));
+  // the timed kernel: the kt-loop stage when screening is on (in record mode the FP32 record
+  // loop alone; its FP64 refinement follows)
   GRN_CUDA(cudaEventRecord(e->ev0, e->stream));
   GRN_CUDA(grn::launch_vegas_loop(a, prec, e->bins, e->dim, e->ncall, track_max,
                                   e->d_f.as<double>(), e->d_acc.as<unsigned long long>(),
-                                  e->d_lidx.as<int64_t>(), e->d_lx.as<double>(),
-                                  e->d_lvw.as<double>(), rf, rd, e->d_rlist.as<int64_t>(),
-                                  e->nblocks, e->stream));
+                                  e->d_lidx.as<int64_t>(), lx, e->d_lvw.as<double>(), rf, rd,
+                                  e->d_rlist.as<int64_t>(), e->nblocks, e->stream, !rec));
   GRN_CUDA(cudaEventRecord(e->ev1, e->stream));
+  if (rec && lx)
+    GRN_CUDA(grn::launch_vegas_loop_fp64(a, e->bins, e->dim, e->ncall, track_max,
+                                         e->d_f.as<double>(), e->d_acc.as<unsigned long long>(),
+                                         e->d_lidx.as<int64_t>(), lx, e->d_lvw.as<double>(),
+                                         e->d_rlist.as<int64_t>(), e->stream));
   GRN_CUDA(grn::launch_vegas_reduce(e->d_f.as<double>(), e->ncall,
                                     e->d_acc.as<unsigned long long>(), e->d_parts.as<double>(),
                                     e->d_sc.as<double>(), e->stream));
@@ -1464,8 +1490,17 @@ grn_status batch_capture(grn_batch *b, int refine, int track_max) {
   if (ce == cudaSuccess && b->has_kind[1])
     ce = grn::launch_batch_loop(np, b->d_counter.as<unsigned long long>(), b->loop_blocks,
                                 b->max_nh, b->stream);
-  for (int p = 0; p < np && ce == cudaSuccess; ++p)
-    if (!generic(p)) ce = reduce(p, b->stream);
+  for (int p = 0; p < np && ce == cudaSuccess; ++p) {
+    if (generic(p)) continue;
+    const grn::BatchProc &q = b->h_procs[p];
+    grn_engine           *e = b->eng[p];
+    if (q.r_list)  // the record loop's events for the FP64 loop
+      ce = grn::launch_vegas_loop_fp64(q.A, e->bins, e->dim, e->ncall, track_max,
+                                       e->d_f.as<double>(), e->d_acc.as<unsigned long long>(),
+                                       e->d_lidx.as<int64_t>(), e->d_lx.as<double>(),
+                                       e->d_lvw.as<double>(), q.r_list, b->stream);
+    if (ce == cudaSuccess) ce = reduce(p, b->stream);
+  }
   for (int p = 0; p < np && ce == cudaSuccess; ++p)
     if (generic(p)) ce = cudaStreamWaitEvent(b->stream, b->join[p], 0);
   cudaGraph_t       g  = nullptr;
@@ -1552,6 +1587,7 @@ grn_status grn_batch_create(grn_engine *const *engines, int32_t n, grn_batch **o
     b->max_nh   = std::max(b->max_nh, e->bins * e->dim);
     q.rf        = rec ? e->d_recf.as<float>() : nullptr;
     q.rd        = rec ? e->d_recd.as<double>() : nullptr;
+    q.r_list    = (rec && q.A.refine_tol > 0.0) ? e->d_rlist.as<int64_t>() : nullptr;
     if (e->P.screening) b->has_kind[rec ? 1 : 0] = true;
     const int k = (p == n - 1) ? nb - blk
                                : std::max<int>(1, static_cast<int>(nb * (double(e->ncall) / total)));
@@ -1677,6 +1713,7 @@ grn_status grn_get_tuning(grn_engine *e, grn_tuning *t) {
   t->vegas_blocks  = e->nblocks;
   t->weight_blocks = e->loop_blocks;
   t->fp64_refine   = e->fp64_refine;
+  t->refine_tol    = e->refine_tol;
   return GRN_OK;
 }
 
@@ -1684,10 +1721,12 @@ grn_status grn_set_tuning(grn_engine *e, const grn_tuning *t) {
   if (!e || !t) return fail(GRN_ERR_INVALID, "null argument");
   if (t->loop_pair < 0 || t->loop_pair > 2 || t->vegas_blocks < 1 || t->weight_blocks < 1 ||
       t->vegas_blocks > (1 << 20) || t->weight_blocks > (1 << 20) ||
-      (t->fp64_refine != 0 && t->fp64_refine != 1))
+      (t->fp64_refine != 0 && t->fp64_refine != 1) ||
+      !(t->refine_tol >= 1e-9 && t->refine_tol <= 1.0))
     return fail(GRN_ERR_INVALID, "bad tuning");
   e->loop_pair   = t->loop_pair;
   e->fp64_refine = t->fp64_refine;
+  e->refine_tol  = t->refine_tol;
   e->nblocks     = t->vegas_blocks;
   e->loop_blocks = t->weight_blocks;
   return GRN_OK;
@@ -1725,19 +1764,19 @@ grn_status grn_autotune(grn_engine *e, int64_t sample, grn_tune_result *out) {
         double    tmin   = 1e300;
         for (int rep = 0; rep < 2; ++rep) {
           GRN_CUDA(cudaEventRecord(e->ev0, e->stream));
+          // no refinement list: every candidate reads the same stage-A output
           GRN_CUDA(grn::launch_vegas_loop(a, GRN_PREC_MIXED, e->bins, e->dim, nc0, 0,
                                           e->d_f.as<double>(), e->d_acc.as<unsigned long long>(),
                                           e->d_lidx.as<int64_t>(), e->d_lx.as<double>(),
                                           e->d_lvw.as<double>(), e->d_recf.as<float>(),
-                                          e->d_recd.as<double>(), e->d_rlist.as<int64_t>(),
-                                          blocks, e->stream));
+                                          e->d_recd.as<double>(), nullptr, blocks, e->stream));
           GRN_CUDA(cudaEventRecord(e->ev1, e->stream));
           GRN_CUDA(cudaEventSynchronize(e->ev1));
           float ms = 0.f;
           GRN_CUDA(cudaEventElapsedTime(&ms, e->ev0, e->ev1));
           if (rep > 0) tmin = std::min(tmin, static_cast<double>(ms));
         }
-        out->cand[nc] = {pair, blocks, blocks, e->fp64_refine};
+        out->cand[nc] = {pair, blocks, blocks, e->fp64_refine, e->refine_tol};
         out->ms[nc]   = tmin;
         if (tmin < best) {
           best      = tmin;
@@ -1786,7 +1825,7 @@ grn_status grn_autotune(grn_engine *e, int64_t sample, grn_tune_result *out) {
         GRN_CUDA(cudaEventElapsedTime(&ms, e->ev0, e->ev1));
         if (rep > 0) tmin = std::min(tmin, static_cast<double>(ms));  // first launch warms up
       }
-      out->cand[nc] = {pair, blocks, blocks, e->fp64_refine};
+      out->cand[nc] = {pair, blocks, blocks, e->fp64_refine, e->refine_tol};
       out->ms[nc]   = tmin;
       if (tmin < best) {
         best      = tmin;

@@ -82,7 +82,8 @@ cudaError_t launch_vegas_grid_init(double *xmat, int bins, int dim, cudaStream_t
 // accumulators (see kAccRefine); the list arrays have
 // capacity ncall (l_x: dim x ncall, dimension-major).
 // rf/rd: loop records (record mode, see record_mode()); null for the point mode,
-// in which the mapped points l_x are stored and stage B recomputes the tree level.
+// in which stage B recomputes the tree level from the mapped points l_x. Record mode stores
+// l_x too unless it is null (then its loop hands no events to the FP64 loop).
 cudaError_t launch_vegas_born(const KArgs &a, const double *xmat, int bins, int dim, int64_t ncall,
                               uint64_t seed, uint32_t stream, int track_max, double *f_out,
                               unsigned long long *acc, int64_t *l_idx, double *l_x, double *l_vw,
@@ -90,13 +91,22 @@ cudaError_t launch_vegas_born(const KArgs &a, const double *xmat, int bins, int 
                               const float *flq = nullptr);
 // fu / flq: points drawn from the flow (dimension-major, leading dimension ncall) and
 // their log density; the VEGAS weight of a point is then vw(u) / q(u).
-// r_list (capacity ncall): slots of the FP32 generic loop whose error estimate exceeds
-// a.refine_tol, finished by an FP64 pass over them in the same call.
+// The FP64 loop over the listed events an FP32 loop handed over (sel = r_list, its length
+// acc[kAccRefine] read on the device; l_x the events' mapped points).
+cudaError_t launch_vegas_loop_fp64(const KArgs &a, int bins, int dim, int64_t ncall,
+                                   int track_max, double *f_out, unsigned long long *acc,
+                                   const int64_t *l_idx, const double *l_x, const double *l_vw,
+                                   const int64_t *r_list, cudaStream_t st);
+// Stage B (nblocks: the record loop's grid; the generic loops size theirs from their own
+// occupancy). r_list (capacity ncall): slots of the FP32 loop (generic, or record mode when l_x
+// is stored) whose error estimate exceeds a.refine_tol, finished by an FP64 pass over them in
+// the same call; in record mode fp64_pass = false leaves that pass to the caller
+// (launch_vegas_loop_fp64 with the same arguments).
 cudaError_t launch_vegas_loop(const KArgs &a, int prec, int bins, int dim, int64_t ncall,
                               int track_max, double *f_out, unsigned long long *acc,
                               const int64_t *l_idx, const double *l_x, const double *l_vw,
                               const float *rf, const double *rd, int64_t *r_list, int nblocks,
-                              cudaStream_t st);
+                              cudaStream_t st, bool fp64_pass = true);
 // The f^2 histogram of a finished pass (bins x dim, the input of launch_vegas_refine) from its
 // f array and its points (Philox (seed, stream), or the flow points fu with leading dimension
 // ncall), summed in a fixed order: equal f arrays give equal histograms bit for bit.
@@ -115,15 +125,18 @@ constexpr int kRecordDoubles = 4;
 cudaError_t launch_weights_born_rec(const KArgs &a, const double *u, int64_t n, int dim, double *w,
                                     uint8_t *flags, int64_t *list, float *rf, double *rd,
                                     unsigned long long *count, cudaStream_t st);
+// rlist non-null (capacity n, with u and dim): points whose error estimate exceeds
+// a.refine_tol go to rlist (length count[1]) and get their weights from the FP64 loop.
 cudaError_t launch_weights_loop_rec(const KArgs &a, int64_t n, double *w, uint8_t *flags,
                                     const int64_t *list, const float *rf, const double *rd,
-                                    const unsigned long long *count, int loop_blocks,
-                                    cudaStream_t st);
+                                    unsigned long long *count, int loop_blocks, cudaStream_t st,
+                                    int64_t *rlist = nullptr, const double *u = nullptr,
+                                    int dim = 0);
 int         loop_rec_blocks_per_sm(int pair);
 cudaError_t launch_event_weights_rec(const KArgs &a, const double *u, int64_t n, int dim,
                                      double *w, uint8_t *flags, int64_t *list, float *rf,
                                      double *rd, unsigned long long *count, int loop_blocks,
-                                     cudaStream_t st);
+                                     cudaStream_t st, int64_t *rlist = nullptr);
 constexpr int kVegasSumParts = 256;
 cudaError_t launch_vegas_reduce(const double *f_out, int64_t ncall,
                                 const unsigned long long *acc, double *part, double *sc,
@@ -157,6 +170,7 @@ struct BatchProc {
   double             *l_x, *l_vw;
   float              *rf;
   double             *rd;
+  int64_t            *r_list;      // record mode with refinement: events for the FP64 loop
   const float        *fu, *flq;    // flow points of the pass and their log density (or null)
   int                 blk0, blk1;  // stage-A blocks of this process: [blk0, blk1)
 };

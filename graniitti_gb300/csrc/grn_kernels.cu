@@ -244,13 +244,14 @@ __device__ __noinline__ cx<double> loop_integral_rr(const KArgs &A, const Born &
 }
 
 // *mag: see loop_integral (0 from the single-trajectory Regge loop, whose increment form
-// keeps every FP32 operand O(1) and whose rings do not cancel).
+// keeps every FP32 operand O(1) and whose rings do not cancel). The increment form is written
+// for elastic forward legs; excited ones take the loop with the per-leg masses.
 template <typename T>
 __device__ __forceinline__ cx<double> loop_dispatch(const KArgs &A, const Born &b,
                                                     const KtNode<T> *skt, const PhiNode<T> *sphi,
                                                     double *mag) {
   if constexpr (sizeof(T) == sizeof(float)) {
-    if (A.K.n_active == 1 && A.P.process == GRN_PROC_REGGE_CON) {
+    if (A.K.n_active == 1 && A.P.process == GRN_PROC_REGGE_CON && b.exc == 0) {
       *mag = 0.0;
       return loop_integral_fast(A, b, skt, sphi);
     }
@@ -291,37 +292,58 @@ __device__ __forceinline__ void load_record(LoopEventF<float> &e, double &a0r, d
   jac      = rd[3 * cap + slot];
 }
 
-// Loop integral of a loaded record (constants of e already set).
+// Loop integral of a loaded record (constants of e already set); *mag (in the units of the
+// result without the loop norm): sum_ij |U_i c_j| (|Re A_ij| + |Im A_ij|).
 __device__ __forceinline__ cx<double> loop_integral_rec(const KArgs &A, const LoopEventF<float> &e,
                                                         const KtNode<float> *skt,
-                                                        const PhiNode<float> *sphi) {
-  float ar = 0.f, ai = 0.f, cr = 0.f, ci = 0.f;
+                                                        const PhiNode<float> *sphi,
+                                                        double *mag) {
+  float ar = 0.f, ai = 0.f, cr = 0.f, ci = 0.f, m = 0.f;
   for (int j = 0; j < A.n_kt_nodes; ++j) {
     const KtNode<float> nj = skt[j];
     const float         k2 = nj.kt * nj.kt;
-    float ir = 0.f, ii = 0.f, dr = 0.f, di = 0.f;
+    float ir = 0.f, ii = 0.f, dr = 0.f, di = 0.f, ab = 0.f;
     for (int i = 0; i < A.n_phi_nodes; ++i) {
       const PhiNode<float> ni = sphi[i];
       cx<float> a;
       if (loop_point_amp_fast<float>(e, nj.kt * ni.c, nj.kt * ni.s, k2, a)) {
         kahan_add(ir, dr, ni.u * a.re);
         kahan_add(ii, di, ni.u * a.im);
+        ab += ni.u * (fabsf(a.re) + fabsf(a.im));
       }
     }
     kahan_add(ar, cr, nj.cre * ir - nj.cim * ii);
     kahan_add(ai, ci, nj.cre * ii + nj.cim * ir);
+    m += sqrtf(nj.cre * nj.cre + nj.cim * nj.cim) * ab;
   }
+  *mag = double(m) * e.escale;
   const double sr = double(ar) * e.escale, si = double(ai) * e.escale;
   return {A.loop_norm_re * sr - A.loop_norm_im * si, A.loop_norm_re * si + A.loop_norm_im * sr};
 }
 
-// Screened weight from a record: W = Jacobian x |A0 + A_loop|^2 (NaN/Inf -> 0).
+// Whether the record loop's estimated relative error of |A| exceeds A.refine_tol (or |A| is
+// not finite): 2 kRefineKappaRecord u |norm| mag / |A|, mag the loop's magnitude sum
+// (unnormalised). The record loop's points carry a few u of error (delta formulation), so
+// its kappa is calibrated lower than the generic loop's: the estimate then selects the deep
+// screening dips.
+constexpr double kRefineKappaRecord = 1.0;
+__device__ __forceinline__ bool loop_needs_fp64(const KArgs &A, double mag, double re, double im) {
+  const double norm = sqrt(A.loop_norm_re * A.loop_norm_re + A.loop_norm_im * A.loop_norm_im);
+  const double est  = 2.0 * kRefineKappaRecord * 0x1p-24 * norm * mag;
+  return A.refine_tol > 0.0 && !(est <= A.refine_tol * sqrt(re * re + im * im));
+}
+
+// Screened weight from a record: W = Jacobian x |A0 + A_loop|^2 (NaN/Inf -> 0); with redo
+// non-null, *redo = loop_needs_fp64.
 __device__ __forceinline__ double record_weight(const KArgs &A, const LoopEventF<float> &e,
                                                 double a0r, double a0i, double jac,
                                                 const KtNode<float> *skt,
-                                                const PhiNode<float> *sphi, uint8_t &flags) {
-  const cx<double> Al = loop_integral_rec(A, e, skt, sphi);
+                                                const PhiNode<float> *sphi, uint8_t &flags,
+                                                bool *redo = nullptr) {
+  double           mag;
+  const cx<double> Al = loop_integral_rec(A, e, skt, sphi, &mag);
   const double re = a0r + Al.re, im = a0i + Al.im;
+  if (redo) *redo = loop_needs_fp64(A, mag, re, im);
   double W = jac * (re * re + im * im);
   flags = GRN_FLAG_KINEMATICS_OK | GRN_FLAG_FIDCUTS_OK | GRN_FLAG_VETOCUTS_OK |
           GRN_FLAG_AMPLITUDE_OK;
@@ -336,7 +358,8 @@ __device__ __forceinline__ double record_weight(const KArgs &A, const LoopEventF
 __device__ void stage_nodes3(const KArgs &A, KtNode3 *skt, PhiNode3 *sphi) {
   for (int j = threadIdx.x; j < A.n_kt_nodes; j += blockDim.x) {
     const float kt = float(A.lc_kt[3 * j]), ci = float(A.lc_kt[3 * j + 2]);
-    skt[j] = {f2s(kt), f2s(kt * kt), f2s(float(A.lc_kt[3 * j + 1])), f2s(ci), f2s(-ci)};
+    const float ca = float(hypot(A.lc_kt[3 * j + 1], A.lc_kt[3 * j + 2]));
+    skt[j] = {f2s(kt), f2s(kt * kt), f2s(float(A.lc_kt[3 * j + 1])), f2s(ci), f2s(-ci), f2s(ca)};
   }
   for (int i = threadIdx.x; i < A.n_phi_nodes; i += blockDim.x) {
     const double c = A.lc_phi[3 * i], s = A.lc_phi[3 * i + 1];
@@ -347,40 +370,43 @@ __device__ void stage_nodes3(const KArgs &A, KtNode3 *skt, PhiNode3 *sphi) {
 
 // Screened weights of records ra and rb (rb may repeat ra; then only wa is meaningful) on the
 // azimuth-outer loop; a pair with an event outside the validity bound (loop3_safe) takes the
-// per-point-tested loop instead.
+// per-point-tested loop instead. With redo non-null, redo[k] = loop_needs_fp64 of event k.
 __device__ __forceinline__ void record_weights3(const KArgs &A, const LoopEventF<float> &consts,
                                                 const float *__restrict__ rf,
                                                 const double *__restrict__ rd, int64_t cap,
                                                 int64_t ra, int64_t rb, const KtNode3 *skt,
                                                 const PhiNode3 *sphi, double &wa, double &wb,
-                                                uint8_t &fa, uint8_t &fb) {
+                                                uint8_t &fa, uint8_t &fb, bool *redo = nullptr) {
   LoopEventF<float> ea = consts, eb = consts;
   double            a0r[2], a0i[2], jac[2];
   load_record(ea, a0r[0], a0i[0], jac[0], rf, rd, ra, cap);
   load_record(eb, a0r[1], a0i[1], jac[1], rf, rd, rb, cap);
   const float kt_max = float(A.P.loop.kt_max);
-  double      sr[2], si[2];
+  double      sr[2], si[2], sm[2];
   if (loop3_safe(ea, kt_max) && loop3_safe(eb, kt_max)) {
     Loop3<float2> e;
     make_loop3<float2>(ea, eb, [](float x, float y) { return make_float2(x, y); }, e);
-    float2 s_re, s_im;
-    loop_integral3(e, A.n_kt_nodes, A.n_phi_nodes, skt, sphi, s_re, s_im);
+    float2 s_re, s_im, s_m;
+    loop_integral3(e, A.n_kt_nodes, A.n_phi_nodes, skt, sphi, s_re, s_im, s_m);
     // the event's prefactor (couplings x ReggeEta^2 x tree-level phase), after the sum
     const float pr[2] = {ea.pre_re, eb.pre_re}, pi[2] = {ea.pre_im, eb.pre_im};
-    const float xr[2] = {s_re.x, s_re.y}, xi[2] = {s_im.x, s_im.y};
+    const float xr[2] = {s_re.x, s_re.y}, xi[2] = {s_im.x, s_im.y}, xm[2] = {s_m.x, s_m.y};
     for (int k = 0; k < 2; ++k) {
       sr[k] = double(pr[k]) * xr[k] - double(pi[k]) * xi[k];
       si[k] = double(pr[k]) * xi[k] + double(pi[k]) * xr[k];
+      sm[k] = sqrt(double(pr[k]) * pr[k] + double(pi[k]) * pi[k]) * xm[k];
     }
   } else {
     LoopEvent2 e;
     make_loop_event2(ea, eb, e);
-    float2 s_re, s_im;
-    loop_integral2(e, A.n_kt_nodes, A.n_phi_nodes, skt, sphi, s_re, s_im);
+    float2 s_re, s_im, s_m;
+    loop_integral2(e, A.n_kt_nodes, A.n_phi_nodes, skt, sphi, s_re, s_im, s_m);
     sr[0] = s_re.x;
     sr[1] = s_re.y;
     si[0] = s_im.x;
     si[1] = s_im.y;
+    sm[0] = s_m.x;
+    sm[1] = s_m.y;
   }
   const double esc[2] = {ea.escale, eb.escale};
   double       W[2];
@@ -389,6 +415,7 @@ __device__ __forceinline__ void record_weights3(const KArgs &A, const LoopEventF
     const double xr = sr[k] * esc[k], xi = si[k] * esc[k];
     const double re = a0r[k] + (A.loop_norm_re * xr - A.loop_norm_im * xi);
     const double im = a0i[k] + (A.loop_norm_re * xi + A.loop_norm_im * xr);
+    if (redo) redo[k] = loop_needs_fp64(A, sm[k] * esc[k], re, im);
     W[k] = jac[k] * (re * re + im * im);
     F[k] = GRN_FLAG_KINEMATICS_OK | GRN_FLAG_FIDCUTS_OK | GRN_FLAG_VETOCUTS_OK |
            GRN_FLAG_AMPLITUDE_OK;
@@ -490,6 +517,23 @@ __device__ __forceinline__ int64_t list_append(bool pred, unsigned long long *co
 
 constexpr int kWeightThreads = 128;
 
+// One full wave of a grid-stride kernel: the SM count times the blocks of this kernel that fit
+// on an SM (from its own registers and shared memory, so that each instantiation fills the
+// GPU; a grid sized for another kernel can leave a partial second wave at reduced occupancy).
+template <typename K>
+int resident_grid(K kernel, int threads) {
+  int dev = 0, sms = 0, per = 0;
+  cudaGetDevice(&dev);
+  cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+  cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, kernel, threads, 0);
+  return sms * (per < 1 ? 1 : per);
+}
+// Launch of a grid-stride kernel on one full wave of its own (resident_grid).
+template <typename K, typename... Args>
+void launch_wave(K kernel, int threads, cudaStream_t st, Args... args) {
+  kernel<<<resident_grid(kernel, threads), threads, 0, st>>>(args...);
+}
+
 // Stage A over a user point array: cuts, unscreened weights, screened work list.
 template <int MAXD>
 __global__ void __launch_bounds__(kWeightThreads)
@@ -568,18 +612,18 @@ cudaError_t launch_event_weights(const KArgs &a, int prec, const double *u, int6
   if (a.P.screening) {
     if (dim <= 8) {
       if (prec == GRN_PREC_MIXED)
-        k_weights_loop<float, 8><<<loop_blocks, kWeightThreads, 0, st>>>(
-            a, u, dim, list, count, w, flags, rl, count + 1);
+        launch_wave(k_weights_loop<float, 8>, kWeightThreads, st, a, u, dim, list, count, w, flags,
+                    rl, count + 1);
       if (prec != GRN_PREC_MIXED || rl)
-        k_weights_loop<double, 8><<<loop_blocks, kWeightThreads, 0, st>>>(
-            a, u, dim, rl ? rl : list, rl ? count + 1 : count, w, flags, nullptr, nullptr);
+        launch_wave(k_weights_loop<double, 8>, kWeightThreads, st, a, u, dim, rl ? rl : list,
+                    rl ? count + 1 : count, w, flags, nullptr, nullptr);
     } else {
       if (prec == GRN_PREC_MIXED)
-        k_weights_loop<float, kMaxDim><<<loop_blocks, kWeightThreads, 0, st>>>(
-            a, u, dim, list, count, w, flags, rl, count + 1);
+        launch_wave(k_weights_loop<float, kMaxDim>, kWeightThreads, st, a, u, dim, list, count, w,
+                    flags, rl, count + 1);
       if (prec != GRN_PREC_MIXED || rl)
-        k_weights_loop<double, kMaxDim><<<loop_blocks, kWeightThreads, 0, st>>>(
-            a, u, dim, rl ? rl : list, rl ? count + 1 : count, w, flags, nullptr, nullptr);
+        launch_wave(k_weights_loop<double, kMaxDim>, kWeightThreads, st, a, u, dim, rl ? rl : list,
+                    rl ? count + 1 : count, w, flags, nullptr, nullptr);
     }
   }
   return cudaGetLastError();
@@ -614,11 +658,14 @@ __global__ void __launch_bounds__(kWeightThreads)
   }
 }
 
+// rlist non-null: points whose error estimate exceeds A.refine_tol are appended to rlist
+// (length *rcount) and left to the FP64 loop of k_weights_loop.
 __global__ void __launch_bounds__(kWeightThreads, GRN_LOOP_MIN_BLOCKS)
     k_weights_loop_rec(const KArgs A, const int64_t *__restrict__ list,
                        const float *__restrict__ rf, const double *__restrict__ rd, int64_t cap,
                        const unsigned long long *__restrict__ count, double *__restrict__ w,
-                       uint8_t *__restrict__ flags) {
+                       uint8_t *__restrict__ flags, int64_t *__restrict__ rlist,
+                       unsigned long long *__restrict__ rcount) {
   __shared__ KtNode<float>  skt[kMaxLoopNodes];
   __shared__ PhiNode<float> sphi[kMaxLoopNodes];
   stage_nodes<float>(A, skt, sphi);
@@ -630,9 +677,18 @@ __global__ void __launch_bounds__(kWeightThreads, GRN_LOOP_MIN_BLOCKS)
        r += static_cast<int64_t>(gridDim.x) * blockDim.x) {
     double a0r, a0i, jac;
     load_record(e, a0r, a0i, jac, rf, rd, r, cap);
-    uint8_t f;
-    const int64_t i = list[r];
-    w[i] = record_weight(A, e, a0r, a0i, jac, skt, sphi, f);
+    uint8_t       f;
+    bool          redo = false;
+    const int64_t i    = list[r];
+    const double  W    = record_weight(A, e, a0r, a0i, jac, skt, sphi, f, rlist ? &redo : nullptr);
+    if (rlist) {
+      const int64_t slot = list_append(redo, rcount);
+      if (redo) {
+        rlist[slot] = i;
+        continue;
+      }
+    }
+    w[i] = W;
     if (flags) flags[i] = f;
   }
 }
@@ -644,7 +700,8 @@ __global__ void __launch_bounds__(kWeightThreads, MINB)
     k_weights_loop_rec2(const KArgs A, const int64_t *__restrict__ list,
                         const float *__restrict__ rf, const double *__restrict__ rd, int64_t cap,
                         const unsigned long long *__restrict__ count, double *__restrict__ w,
-                        uint8_t *__restrict__ flags) {
+                        uint8_t *__restrict__ flags, int64_t *__restrict__ rlist,
+                        unsigned long long *__restrict__ rcount) {
   __shared__ KtNode3  skt[kMaxLoopNodes];
   __shared__ PhiNode3 sphi[kMaxLoopNodes];
   stage_nodes3(A, skt, sphi);
@@ -655,28 +712,36 @@ __global__ void __launch_bounds__(kWeightThreads, MINB)
   for (int64_t q = static_cast<int64_t>(blockIdx.x) * blockDim.x + threadIdx.x; q < npair;
        q += static_cast<int64_t>(gridDim.x) * blockDim.x) {
     const int64_t ra = 2 * q, rb = (2 * q + 1 < cnt) ? 2 * q + 1 : 2 * q;
-    double  wa, wb;
-    uint8_t fa, fb;
-    record_weights3(A, c, rf, rd, cap, ra, rb, skt, sphi, wa, wb, fa, fb);
-    w[list[ra]] = wa;
-    if (flags) flags[list[ra]] = fa;
-    if (rb != ra) {
-      w[list[rb]] = wb;
-      if (flags) flags[list[rb]] = fb;
+    double  W[2];
+    uint8_t F[2];
+    bool    redo[2] = {false, false};
+    record_weights3(A, c, rf, rd, cap, ra, rb, skt, sphi, W[0], W[1], F[0], F[1],
+                    rlist ? redo : nullptr);
+    for (int k = 0; k < 2; ++k) {  // both lanes of every pair take both steps (list_append)
+      const bool    real = k == 0 || rb != ra;
+      const int64_t i    = list[k ? rb : ra];
+      if (rlist) {
+        const int64_t slot = list_append(real && redo[k], rcount);
+        if (real && redo[k]) rlist[slot] = i;
+      }
+      if (real && !redo[k]) {
+        w[i] = W[k];
+        if (flags) flags[i] = F[k];
+      }
     }
   }
 }
 
 bool record_mode(const KArgs &a, int prec) {
   return a.P.screening && prec == GRN_PREC_MIXED && a.K.n_active == 1 &&
-         a.P.process == GRN_PROC_REGGE_CON && a.P.n_central == 2;
+         a.P.process == GRN_PROC_REGGE_CON && a.P.n_central == 2 && a.P.excitation == 0;
 }
 
 cudaError_t launch_weights_born_rec(const KArgs &a, const double *u, int64_t n, int dim, double *w,
                                     uint8_t *flags, int64_t *list, float *rf, double *rd,
                                     unsigned long long *count, cudaStream_t st) {
   if (n <= 0) return cudaSuccess;
-  cudaError_t e = cudaMemsetAsync(count, 0, sizeof(unsigned long long), st);
+  cudaError_t e = cudaMemsetAsync(count, 0, 2 * sizeof(unsigned long long), st);
   if (e != cudaSuccess) return e;
   const unsigned blocks = static_cast<unsigned>((n + kWeightThreads - 1) / kWeightThreads);
   if (dim <= 8)
@@ -690,28 +755,42 @@ cudaError_t launch_weights_born_rec(const KArgs &a, const double *u, int64_t n, 
 
 cudaError_t launch_weights_loop_rec(const KArgs &a, int64_t n, double *w, uint8_t *flags,
                                     const int64_t *list, const float *rf, const double *rd,
-                                    const unsigned long long *count, int loop_blocks,
-                                    cudaStream_t st) {
+                                    unsigned long long *count, int loop_blocks, cudaStream_t st,
+                                    int64_t *rlist, const double *u, int dim) {
   if (n <= 0) return cudaSuccess;
+  int64_t *rl = (rlist && u && a.refine_tol > 0.0) ? rlist : nullptr;
+  if (rl) {
+    const cudaError_t e = cudaMemsetAsync(count + 1, 0, sizeof(unsigned long long), st);
+    if (e != cudaSuccess) return e;
+  }
+  unsigned long long *rc = rl ? count + 1 : nullptr;
   if (a.loop_pair == 2)
     k_weights_loop_rec2<3><<<loop_blocks, kWeightThreads, 0, st>>>(a, list, rf, rd, n, count, w,
-                                                                   flags);
+                                                                   flags, rl, rc);
   else if (a.loop_pair)
     k_weights_loop_rec2<2><<<loop_blocks, kWeightThreads, 0, st>>>(a, list, rf, rd, n, count, w,
-                                                                   flags);
+                                                                   flags, rl, rc);
   else
     k_weights_loop_rec<<<loop_blocks, kWeightThreads, 0, st>>>(a, list, rf, rd, n, count, w,
-                                                               flags);
+                                                               flags, rl, rc);
+  if (!rl) return cudaGetLastError();
+  if (dim <= 8)
+    launch_wave(k_weights_loop<double, 8>, kWeightThreads, st, a, u, dim, rl, rc, w, flags, nullptr,
+                nullptr);
+  else
+    launch_wave(k_weights_loop<double, kMaxDim>, kWeightThreads, st, a, u, dim, rl, rc, w, flags,
+                nullptr, nullptr);
   return cudaGetLastError();
 }
 
 cudaError_t launch_event_weights_rec(const KArgs &a, const double *u, int64_t n, int dim,
                                      double *w, uint8_t *flags, int64_t *list, float *rf,
                                      double *rd, unsigned long long *count, int loop_blocks,
-                                     cudaStream_t st) {
+                                     cudaStream_t st, int64_t *rlist) {
   cudaError_t e = launch_weights_born_rec(a, u, n, dim, w, flags, list, rf, rd, count, st);
   if (e != cudaSuccess) return e;
-  return launch_weights_loop_rec(a, n, w, flags, list, rf, rd, count, loop_blocks, st);
+  return launch_weights_loop_rec(a, n, w, flags, list, rf, rd, count, loop_blocks, st, rlist, u,
+                                 dim);
 }
 
 // Kinematics only: pfinal[1..4] as (px, py, pz, E), and t1, t2.
@@ -1212,10 +1291,12 @@ __device__ __forceinline__ void born_pass_body(
         double            a0r, a0i;
         make_loop_event_fast<float>(A.P, A.K, b, le, &a0r, &a0i);
         store_record(le, a0r, a0i, weight_jacobian(A.K, b), rf, rd, slot, cap);
-      } else {
+      }
+      // the mapped point: the generic loop's input, and the record loop's for the events it
+      // hands to the FP64 loop (l_x null: record mode without refinement)
+      if (l_x)
         for (int j = 0; j < MAXD; ++j)
           if (j < dim) l_x[static_cast<int64_t>(j) * cap + slot] = x[j];
-      }
     }
   }
   flush_counters(acc, cnt, maxf, maxW);
@@ -1281,12 +1362,42 @@ __global__ void __launch_bounds__(kVegasThreads)
   flush_counters(acc, cnt, maxf, maxW);
 }
 
+// Results of a pair of listed events (ra, rb; rb == ra for a single one): f and counters, or
+// with r_list the slots of events to redo in FP64 (every lane of the warp takes both steps of
+// the list append).
+__device__ __forceinline__ void finish_pair(int64_t ra, int64_t rb, const double *W,
+                                            const uint8_t *F, const bool *redo, int64_t *r_list,
+                                            unsigned long long *rcount,
+                                            const int64_t *__restrict__ l_idx,
+                                            const double *__restrict__ l_vw,
+                                            double *__restrict__ f_out, int track_max,
+                                            unsigned long long *cnt, double &maxf, double &maxW) {
+  for (int k = 0; k < 2; ++k) {
+    const int64_t r    = k ? rb : ra;
+    const bool    real = k == 0 || rb != ra;
+    if (r_list) {
+      const int64_t slot = list_append(real && redo[k], rcount);
+      if (real && redo[k]) r_list[slot] = r;
+    }
+    if (!real || redo[k]) continue;
+    const double f  = W[k] * l_vw[r];
+    f_out[l_idx[r]] = f;
+    cnt[VS_AMP_OK] += (F[k] & GRN_FLAG_AMPLITUDE_OK) ? 1 : 0;
+    cnt[VS_NAN] += (F[k] & GRN_FLAG_AMPLITUDE_OK) ? 0 : 1;
+    if (track_max) {
+      maxf = fmax(maxf, f);
+      maxW = fmax(maxW, W[k]);
+    }
+  }
+}
+
 // Stage B, record mode: FP32 loop of the listed events from their records.
 __global__ void __launch_bounds__(kVegasThreads, GRN_LOOP_MIN_BLOCKS)
     k_vegas_loop_rec(const KArgs A, int bins, int dim, int track_max, double *__restrict__ f_out,
                      unsigned long long *__restrict__ acc,
                      const int64_t *__restrict__ l_idx, const double *__restrict__ l_vw,
-                     const float *__restrict__ rf, const double *__restrict__ rd, int64_t cap) {
+                     const float *__restrict__ rf, const double *__restrict__ rd, int64_t cap,
+                     int64_t *__restrict__ r_list) {
   __shared__ KtNode<float>  skt[kMaxLoopNodes];
   __shared__ PhiNode<float> sphi[kMaxLoopNodes];
   stage_nodes<float>(A, skt, sphi);
@@ -1302,7 +1413,15 @@ __global__ void __launch_bounds__(kVegasThreads, GRN_LOOP_MIN_BLOCKS)
     double a0r, a0i, jac;
     load_record(e, a0r, a0i, jac, rf, rd, r, cap);
     uint8_t      fl;
-    const double W = record_weight(A, e, a0r, a0i, jac, skt, sphi, fl);
+    bool         redo = false;
+    const double W    = record_weight(A, e, a0r, a0i, jac, skt, sphi, fl, r_list ? &redo : nullptr);
+    if (r_list) {
+      const int64_t slot = list_append(redo, &acc[kAccRefine]);
+      if (redo) {
+        r_list[slot] = r;
+        continue;
+      }
+    }
     const double f = W * l_vw[r];
     f_out[l_idx[r]] = f;
     cnt[VS_AMP_OK] += (fl & GRN_FLAG_AMPLITUDE_OK) ? 1 : 0;
@@ -1323,7 +1442,8 @@ __global__ void __launch_bounds__(kVegasThreads, MINB)
     k_vegas_loop_rec2(const KArgs A, int bins, int dim, int track_max, double *__restrict__ f_out,
                       unsigned long long *__restrict__ acc,
                       const int64_t *__restrict__ l_idx, const double *__restrict__ l_vw,
-                      const float *__restrict__ rf, const double *__restrict__ rd, int64_t cap) {
+                      const float *__restrict__ rf, const double *__restrict__ rd, int64_t cap,
+                      int64_t *__restrict__ r_list) {
   __shared__ KtNode3  skt[kMaxLoopNodes];
   __shared__ PhiNode3 sphi[kMaxLoopNodes];
   stage_nodes3(A, skt, sphi);
@@ -1339,18 +1459,11 @@ __global__ void __launch_bounds__(kVegasThreads, MINB)
     const int64_t ra = 2 * q, rb = (2 * q + 1 < n) ? 2 * q + 1 : 2 * q;
     double  W[2];
     uint8_t F[2];
-    record_weights3(A, c, rf, rd, cap, ra, rb, skt, sphi, W[0], W[1], F[0], F[1]);
-    for (int k = 0; k < (rb != ra ? 2 : 1); ++k) {
-      const int64_t r = k ? rb : ra;
-      const double  f = W[k] * l_vw[r];
-      f_out[l_idx[r]] = f;
-      cnt[VS_AMP_OK] += (F[k] & GRN_FLAG_AMPLITUDE_OK) ? 1 : 0;
-      cnt[VS_NAN] += (F[k] & GRN_FLAG_AMPLITUDE_OK) ? 0 : 1;
-      if (track_max) {
-        maxf = fmax(maxf, f);
-        maxW = fmax(maxW, W[k]);
-      }
-    }
+    bool redo[2] = {false, false};
+    record_weights3(A, c, rf, rd, cap, ra, rb, skt, sphi, W[0], W[1], F[0], F[1],
+                    r_list ? redo : nullptr);
+    finish_pair(ra, rb, W, F, redo, r_list, &acc[kAccRefine], l_idx, l_vw, f_out, track_max,
+                cnt, maxf, maxW);
   }
   __syncwarp();
   flush_counters(acc, cnt, maxf, maxW);
@@ -1399,40 +1512,62 @@ cudaError_t launch_vegas_born(const KArgs &a, const double *xmat, int bins, int 
   return cudaGetLastError();
 }
 
+// The FP64 loop over the events an FP32 loop handed over (sel = r_list, length
+// acc[kAccRefine], read on the device).
+cudaError_t launch_vegas_loop_fp64(const KArgs &a, int bins, int dim, int64_t ncall,
+                                   int track_max, double *f_out, unsigned long long *acc,
+                                   const int64_t *l_idx, const double *l_x, const double *l_vw,
+                                   const int64_t *r_list, cudaStream_t st) {
+  if (dim <= 8)
+    launch_wave(k_vegas_loop<double, 8>, kVegasThreads, st, a, bins, dim, track_max, f_out, acc,
+                l_idx, l_x, l_vw, ncall, nullptr, r_list);
+  else
+    launch_wave(k_vegas_loop<double, kMaxDim>, kVegasThreads, st, a, bins, dim, track_max, f_out,
+                acc, l_idx, l_x, l_vw, ncall, nullptr, r_list);
+  return cudaGetLastError();
+}
+
 cudaError_t launch_vegas_loop(const KArgs &a, int prec, int bins, int dim, int64_t ncall,
                               int track_max, double *f_out, unsigned long long *acc,
                               const int64_t *l_idx, const double *l_x, const double *l_vw,
                               const float *rf, const double *rd, int64_t *r_list, int nblocks,
-                              cudaStream_t st) {
+                              cudaStream_t st, bool fp64_pass) {
   if (!a.P.screening) return cudaSuccess;
+  int64_t *rl = (prec == GRN_PREC_MIXED && a.refine_tol > 0.0 && l_x) ? r_list : nullptr;
   if (rf) {
+    if (rl) {  // the list of this launch starts empty (the loop may be re-run on one stage A)
+      const cudaError_t ce = cudaMemsetAsync(acc + kAccRefine, 0, sizeof(unsigned long long), st);
+      if (ce != cudaSuccess) return ce;
+    }
     if (a.loop_pair == 2)
       k_vegas_loop_rec2<3><<<nblocks, kVegasThreads, 0, st>>>(a, bins, dim, track_max, f_out, acc,
-                                                             l_idx, l_vw, rf, rd, ncall);
+                                                             l_idx, l_vw, rf, rd, ncall, rl);
     else if (a.loop_pair)
       k_vegas_loop_rec2<2><<<nblocks, kVegasThreads, 0, st>>>(a, bins, dim, track_max, f_out, acc,
-                                                             l_idx, l_vw, rf, rd, ncall);
+                                                             l_idx, l_vw, rf, rd, ncall, rl);
     else
       k_vegas_loop_rec<<<nblocks, kVegasThreads, 0, st>>>(a, bins, dim, track_max, f_out, acc,
-                                                         l_idx, l_vw, rf, rd, ncall);
-    return cudaGetLastError();
+                                                         l_idx, l_vw, rf, rd, ncall, rl);
+    const cudaError_t ce = cudaGetLastError();
+    if (ce != cudaSuccess || !rl || !fp64_pass) return ce;
+    return launch_vegas_loop_fp64(a, bins, dim, ncall, track_max, f_out, acc, l_idx, l_x, l_vw,
+                                  rl, st);
   }
-  int64_t *rl = (prec == GRN_PREC_MIXED && a.refine_tol > 0.0) ? r_list : nullptr;
   // MIXED: FP32 pass, then the FP64 pass over the refinement list (when refining)
   if (dim <= 8) {
     if (prec == GRN_PREC_MIXED)
-      k_vegas_loop<float, 8><<<nblocks, kVegasThreads, 0, st>>>(
-          a, bins, dim, track_max, f_out, acc, l_idx, l_x, l_vw, ncall, rl, nullptr);
+      launch_wave(k_vegas_loop<float, 8>, kVegasThreads, st, a, bins, dim, track_max, f_out, acc,
+                  l_idx, l_x, l_vw, ncall, rl, nullptr);
     if (prec != GRN_PREC_MIXED || rl)
-      k_vegas_loop<double, 8><<<nblocks, kVegasThreads, 0, st>>>(
-          a, bins, dim, track_max, f_out, acc, l_idx, l_x, l_vw, ncall, nullptr, rl);
+      launch_wave(k_vegas_loop<double, 8>, kVegasThreads, st, a, bins, dim, track_max, f_out, acc,
+                  l_idx, l_x, l_vw, ncall, nullptr, rl);
   } else {
     if (prec == GRN_PREC_MIXED)
-      k_vegas_loop<float, kMaxDim><<<nblocks, kVegasThreads, 0, st>>>(
-          a, bins, dim, track_max, f_out, acc, l_idx, l_x, l_vw, ncall, rl, nullptr);
+      launch_wave(k_vegas_loop<float, kMaxDim>, kVegasThreads, st, a, bins, dim, track_max, f_out,
+                  acc, l_idx, l_x, l_vw, ncall, rl, nullptr);
     if (prec != GRN_PREC_MIXED || rl)
-      k_vegas_loop<double, kMaxDim><<<nblocks, kVegasThreads, 0, st>>>(
-          a, bins, dim, track_max, f_out, acc, l_idx, l_x, l_vw, ncall, nullptr, rl);
+      launch_wave(k_vegas_loop<double, kMaxDim>, kVegasThreads, st, a, bins, dim, track_max, f_out,
+                  acc, l_idx, l_x, l_vw, ncall, nullptr, rl);
   }
   return cudaGetLastError();
 }
@@ -1652,18 +1787,11 @@ __global__ void __launch_bounds__(kVegasThreads, 2)
         const int64_t ra = 2 * unit, rb = (2 * unit + 1 < n) ? 2 * unit + 1 : 2 * unit;
         double  W[2];
         uint8_t F[2];
-        record_weights3(q.A, c, q.rf, q.rd, q.ncall, ra, rb, skt, sphi, W[0], W[1], F[0], F[1]);
-        for (int k = 0; k < (rb != ra ? 2 : 1); ++k) {
-          const int64_t r = k ? rb : ra;
-          const double  f = W[k] * q.l_vw[r];
-          q.f_out[q.l_idx[r]] = f;
-          cnt[VS_AMP_OK] += (F[k] & GRN_FLAG_AMPLITUDE_OK) ? 1 : 0;
-          cnt[VS_NAN] += (F[k] & GRN_FLAG_AMPLITUDE_OK) ? 0 : 1;
-          if (q.track_max) {
-            maxf = fmax(maxf, f);
-            maxW = fmax(maxW, W[k]);
-          }
-        }
+        bool    redo[2] = {false, false};
+        record_weights3(q.A, c, q.rf, q.rd, q.ncall, ra, rb, skt, sphi, W[0], W[1], F[0], F[1],
+                        q.r_list ? redo : nullptr);
+        finish_pair(ra, rb, W, F, redo, q.r_list, &q.acc[kAccRefine], q.l_idx, q.l_vw, q.f_out,
+                    q.track_max, cnt, maxf, maxW);
       }
     } else if (unit < n) {
       double x[kMaxDim];

@@ -152,12 +152,13 @@ __device__ __forceinline__ void kahan_add2(float2 &sum, float2 &comp, float2 x) 
 template <typename KN, typename PN>
 __device__ __forceinline__ void loop_integral2(const LoopEvent2 &e, int n_kt, int n_phi,
                                                const KN *skt, const PN *sphi,
-                                               float2 &out_re, float2 &out_im) {
+                                               float2 &out_re, float2 &out_im,
+                                               float2 &out_mag) {
   const float2 zero = f2s(0.f);
-  float2 ar = zero, ai = zero, cr = zero, ci = zero;
+  float2 ar = zero, ai = zero, cr = zero, ci = zero, am = zero;
   for (int j = 0; j < n_kt; ++j) {
     const KN nj = skt[j];
-    float2 ir = zero, ii = zero, dr = zero, di = zero;
+    float2 ir = zero, ii = zero, dr = zero, di = zero, im = zero;
     for (int i = 0; i < n_phi; ++i) {
       const PN ni = sphi[i];
       float2 are, aim;
@@ -167,12 +168,16 @@ __device__ __forceinline__ void loop_integral2(const LoopEvent2 &e, int n_kt, in
       if (!(ok & 2u)) xr.y = xi.y = 0.f;
       kahan_add2(ir, dr, xr);
       kahan_add2(ii, di, xi);
+      im = add2(im, add2(make_float2(fabsf(xr.x), fabsf(xr.y)),
+                         make_float2(fabsf(xi.x), fabsf(xi.y))));
     }
     kahan_add2(ar, cr, sub2(mul2(nj.cre, ir), mul2(nj.cim, ii)));
     kahan_add2(ai, ci, fma2(nj.cre, ii, mul2(nj.cim, ir)));
+    am = fma2(nj.cabs, im, am);
   }
-  out_re = ar;
-  out_im = ai;
+  out_re  = ar;
+  out_im  = ai;
+  out_mag = am;
 }
 
 }  // namespace grn

@@ -66,10 +66,10 @@ __device__ __forceinline__ float2 sinpi_turns2(float2 d) {
   return make_float2(sinpif(d.x), sinpif(d.y));
 }
 
-// Loop nodes of the azimuth-outer loop, duplicated pairs: kt nodes (kt, kt^2, c_j, -Im c_j),
-// phi nodes (cos, sin, U, phi in turns).
+// Loop nodes of the azimuth-outer loop, duplicated pairs: kt nodes (kt, kt^2, c_j, -Im c_j,
+// |c_j|), phi nodes (cos, sin, U, phi in turns).
 struct KtNode3 {
-  float2 kt, k2, cre, cim, ncim;
+  float2 kt, k2, cre, cim, ncim, cabs;
 };
 struct PhiNode3 {
   float2 c, s, u, t;
@@ -175,12 +175,13 @@ GRN_L3 void kahan_add3(V &sum, V &comp, V x) {
 }
 
 // Loop integral sum_i U_i sum_j c_j z_ij of both events (relative to their prefactors and
-// exp(Emax)); kt nodes (kt, kt^2, Re c, Im c, -Im c), phi nodes (cos, sin, U, phi / (2 pi)).
+// exp(Emax)); kt nodes (kt, kt^2, Re c, Im c, -Im c, |c|), phi nodes (cos, sin, U, phi / (2 pi)).
+// out_mag = sum_i U_i sum_j |c_j| (|Re z_ij| + |Im z_ij|), the scale of its rounding error.
 template <typename V, typename KN, typename PN>
 GRN_L3 void loop_integral3(const Loop3<V> &e, int n_kt, int n_phi, const KN *skt,
-                           const PN *sphi, V &out_re, V &out_im) {
+                           const PN *sphi, V &out_re, V &out_im, V &out_mag) {
   const V zero = splat<V>(0.f);
-  V ar = zero, ai = zero, cr = zero, ci = zero;
+  V ar = zero, ai = zero, cr = zero, ci = zero, am = zero;
   for (int i = 0; i < n_phi; ++i) {
     const PN ni = sphi[i];
     Phi3<V> f;
@@ -201,6 +202,7 @@ GRN_L3 void loop_integral3(const Loop3<V> &e, int n_kt, int n_phi, const KN *skt
       f.W4 = mul2(mul2(four, e.c4m), mul2(s4, s4));
     }
     V rr = zero, ri = zero, qr = zero, qi = zero;  // the ring over kt, compensated per block
+    V rm = zero;
     for (int j0 = 0; j0 < n_kt; j0 += 8) {
       V br = zero, bi = zero;
       const int j1 = j0 + 8 < n_kt ? j0 + 8 : n_kt;
@@ -210,15 +212,18 @@ GRN_L3 void loop_integral3(const Loop3<V> &e, int n_kt, int n_phi, const KN *skt
         loop_point3(e, f, nj.kt, nj.k2, zr, zi);
         br = fma2(nj.cre, zr, fma2(nj.ncim, zi, br));
         bi = fma2(nj.cre, zi, fma2(nj.cim, zr, bi));
+        rm = fma2(nj.cabs, add2(abs2(zr), abs2(zi)), rm);
       }
       kahan_add3(rr, qr, br);
       kahan_add3(ri, qi, bi);
     }
     kahan_add3(ar, cr, mul2(ni.u, rr));
     kahan_add3(ai, ci, mul2(ni.u, ri));
+    am = fma2(ni.u, rm, am);
   }
-  out_re = ar;
-  out_im = ai;
+  out_re  = ar;
+  out_im  = ai;
+  out_mag = am;
 }
 
 // The per-pair constants from two loaded records (scalar LoopEventF of events a and b) and

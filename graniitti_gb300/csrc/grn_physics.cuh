@@ -73,6 +73,8 @@ struct Consts {
   double w_const;           // every u-independent factor of the weight
   double M2min, M2max;      // <F>: central-system mass^2 window (B51RandomKin)
   double offshell;          // cascades: widths of the Breit-Wigner mass draws (OFFSHELL)
+  double lnM2f_lo, lnM2f_hi;  // excitation: log of the excited masses^2 range [1.09^2, xi s]
+  double gin;               // excitation: sqrt(g3P gN_P), the inelastic vertex coupling
   int    dec0;              // cascades: first decay coordinate (10; 8 with OFFSHELL = 0)
   double M2prop;            // off-shell propagator nominal mass^2 (ME4: first central mass)
   double M2propB;           // ME6: mass^2 of the third central particle (second propagator)
@@ -134,6 +136,21 @@ GRN_HD T meson_ff(const grn_regge_params &rp, T that, T M2) {
     return exp(-T(rp.b_OREAR) * sqrt(fabs(tp) + T(rp.a_OREAR) * T(rp.a_OREAR)) +
                T(rp.a_OREAR) * T(rp.b_OREAR));
   return T(1) / (T(1) - tp / T(rp.b_POW));
+}
+
+// Inelastic proton vertex of an excited forward leg of mass^2 M2 (S3FINEL, src/MForm.cc:
+// 443-449): (|t| / (M2 (|t| + a)))^((1 + Delta_P) / 2), Delta_P = 0.0808, a = 0.5616 GeV^2.
+template <typename T>
+GRN_HD T proton_ff_inel(T t, T M2) {
+  const T at = fabs(t);
+  return exp(T(0.5 * (1.0 + 0.0808)) * log(at / (M2 * (at + T(0.5616)))));
+}
+// Pomeron-proton vertex of forward leg i (MRegge::PomPomProtonVertex, src/MRegge.cc:637-644):
+// gN_P F(t) elastic, sqrt(g3P gN_P) S3FINEL(t, M^2) excited (bit i of exc).
+template <typename T>
+GRN_HD T leg_vertex(const grn_process_params &P, const Consts &K, int exc, int i, T t, T M2) {
+  if (exc & (1 << i)) return T(K.gin) * proton_ff_inel<T>(t, M2);
+  return T(P.soft.gN_P) * proton_ff<T>(T(P.soft.fc1), T(P.soft.fc2), t);
 }
 
 // Regge propagator sum over active trajectories:
@@ -684,26 +701,30 @@ struct Born {
                                // p*/M_X x (M_max^2 - M_min^2) (<F>)
   double m3sq, m4sq;           // central masses^2 (off-shell ones for cascades)
   int    leafok;               // cascades: all four daughters pass the particle cuts
+  // forward legs: masses^2 (mp^2, or an excited N* mass^2), excitation bits (1: leg 1, 2:
+  // leg 2) and the forward-mass volume factor of the weight (1 when elastic)
+  double mf1sq, mf2sq, jf;
+  int    exc;
   // invariants
   double t1, t2, s13, s14, s23, s24, that, uhat, m2;
 };
 
-// Forward-leg light-cone solution given the central pair's P+, P- and the two
-// forward transverse masses^2 (elastic legs): longitudinal conservation
-//   x1 = (P+ - eps)/L + mT2^2/((1-x2) L^2),  x2 = (P- - eps)/L + mT1^2/((1-x1) L^2).
-// Same physical root as kinematics::SolvePz (include/Graniitti/MKinematics.h:220)
-// picks (forward-going legs, MContinuum.cc:375-380).
+// Forward-leg light-cone solution given the central pair's P+, P- and the two forward
+// transverse masses^2: longitudinal conservation
+//   x1 = a1 + c2 / (1 - x2),  x2 = a2 + c1 / (1 - x1),  a = (P+- - eps) / L, c = mT^2 / L^2.
+// Eliminating x2 gives for d = x1 - a1 the quadratic b2 d^2 - (b1 b2 - c1 + c2) d + b1 c2 = 0
+// (b = 1 - a), whose small root d = 2 b1 c2 / (B + sqrt(B^2 - 4 b1 b2 c2)), B = b1 b2 - c1 + c2,
+// is free of cancellation for elastic legs (c ~ 1e-8) and excited ones (c up to M^2 / s).
+// Same physical root as kinematics::SolvePz (include/Graniitti/MKinematics.h:220) picks
+// (forward-going legs, MContinuum.cc:375-380).
 template <typename T>
 GRN_HD bool solve_x(T a1, T a2, T c1, T c2, T &x1, T &x2) {
-  x1 = a1;
-  x2 = a2;
-#pragma unroll
-  for (int it = 0; it < 3; ++it) {
-    const T n1 = a1 + c2 / (T(1) - x2);
-    const T n2 = a2 + c1 / (T(1) - x1);
-    x1         = n1;
-    x2         = n2;
-  }
+  const T b1 = T(1) - a1, b2 = T(1) - a2;
+  const T B  = b1 * b2 - c1 + c2;
+  const T D  = B * B - T(4) * b1 * b2 * c2;
+  if (!(B > T(0) && D >= T(0))) return false;
+  x1 = a1 + T(2) * b1 * c2 / (B + sqrt(D));
+  x2 = a2 + c1 / (T(1) - x1);
   return (x1 > T(0)) && (x2 > T(0)) && (x1 < T(1)) && (x2 < T(1));
 }
 
@@ -716,6 +737,35 @@ GRN_HD void cascade_masses(const grn_process_params &P, const Consts &K, const d
 GRN_HD_COLD int cascade_cuts(const grn_process_params &P, int dec0, double p3x, double p3y,
                              double p3z, double E3, double m3, double p4x, double p4y, double p4z,
                              double E4, double m4, const double *u);
+
+// Forward legs' masses (MProcess::SampleForwardMasses, src/MProcess.cc:1317-1365): elastic,
+// or excited N* masses^2 log-uniform in [1.09^2, xi_max s] from u_m0 (and u_m1 for double
+// excitation); single excitation takes the side from u_side (< 0.5: leg 1). The weight gains
+// M^2 x (log range) per excited leg (ForwardVolume, src/MProcess.cc:1399-1413).
+GRN_HD void forward_masses(const grn_process_params &P, const Consts &K, double u_m0,
+                           double u_m1, double u_side, Born &b) {
+  b.mf1sq = b.mf2sq = K.mp2;
+  b.exc   = 0;
+  b.jf    = 1.0;
+  if (!P.excitation) return;
+  const double range = K.lnM2f_hi - K.lnM2f_lo;
+  if (P.excitation == 1) {
+    const double M2 = exp(K.lnM2f_lo + range * u_m0);
+    if (u_side < 0.5) {
+      b.mf1sq = M2;
+      b.exc   = 1;
+    } else {
+      b.mf2sq = M2;
+      b.exc   = 2;
+    }
+    b.jf = M2 * range;
+  } else {
+    b.mf1sq = exp(K.lnM2f_lo + range * u_m0);
+    b.mf2sq = exp(K.lnM2f_lo + range * u_m1);
+    b.exc   = 3;
+    b.jf    = b.mf1sq * range * b.mf2sq * range;
+  }
+}
 
 // CASC: the instantiation serves two-body cascades of the central particles (their masses
 // from cascade_masses, the daughters from the decay coordinates, particle cuts on them).
@@ -765,6 +815,13 @@ GRN_HD bool born_kinematics_C(const grn_process_params &P, const Consts &K, cons
   b.p4m = b.mt4 / e4;
   const double Pp = b.p3p + b.p4p, Pm = b.p3m + b.p4m;
   if (0.5 * (Pp + Pm) > K.sqrt_s) return false;  // crude energy check (MContinuum.cc:373)
+  // forward masses: u[8] (and u[9] for double excitation; the side draw u[9] for single).
+  // Excited processes have 10 coordinates, so they run the 16-dimensional instantiation;
+  // the 8-dimensional one never reads past u[7].
+  if (CASC)
+    forward_masses(P, K, u[8], u[9], u[9], b);
+  else
+    forward_masses(P, K, 0.0, 0.0, 0.0, b);
   if (CASC && P.n_decay == 2) {
     // isotropic decays of the two central particles (ConstructDecayKinematics); the particle
     // cuts act on the four daughters (FindDecayCuts, src/MProcess.cc:1140-1154)
@@ -780,7 +837,7 @@ GRN_HD bool born_kinematics_C(const grn_process_params &P, const Consts &K, cons
 // MProcess.cc:1499-1584).
 GRN_HD bool born_invariants(const Consts &K, Born &b) {
   const double Pp = b.p3p + b.p4p, Pm = b.p3m + b.p4m;
-  const double mT1sq = K.mp2 + b.pt1sq, mT2sq = K.mp2 + b.pt2sq;
+  const double mT1sq = b.mf1sq + b.pt1sq, mT2sq = b.mf2sq + b.pt2sq;
   const double L2    = K.L * K.L;
   if (!solve_x((Pp - K.eps) / K.L, (Pm - K.eps) / K.L, mT1sq / L2, mT2sq / L2, b.x1, b.x2))
     return false;
@@ -790,12 +847,13 @@ GRN_HD bool born_invariants(const Consts &K, Born &b) {
   b.p2p = mT2sq / b.p2m;
 
   // Invariants: (pa + pb)^2 = ma^2 + mb^2 + pa+ pb- + pa- pb+ - 2 paT.pbT
-  b.t1  = -(b.pt1sq + b.x1 * b.x1 * K.mp2) / (1.0 - b.x1);
-  b.t2  = -(b.pt2sq + b.x2 * b.x2 * K.mp2) / (1.0 - b.x2);
-  b.s13 = K.mp2 + b.m3sq + b.p1p * b.p3m + b.p1m * b.p3p - 2.0 * (b.p1x * b.p3x + b.p1y * b.p3y);
-  b.s14 = K.mp2 + b.m4sq + b.p1p * b.p4m + b.p1m * b.p4p - 2.0 * (b.p1x * b.p4x + b.p1y * b.p4y);
-  b.s23 = K.mp2 + b.m3sq + b.p2p * b.p3m + b.p2m * b.p3p - 2.0 * (b.p2x * b.p3x + b.p2y * b.p3y);
-  b.s24 = K.mp2 + b.m4sq + b.p2p * b.p4m + b.p2m * b.p4p - 2.0 * (b.p2x * b.p4x + b.p2y * b.p4y);
+  // t = (pb - p)^2 = -(pT^2 + x (m_f^2 - mp^2) + x^2 mp^2) / (1 - x): same-sign terms (m_f >= mp)
+  b.t1  = -(b.pt1sq + b.x1 * (b.mf1sq - K.mp2) + b.x1 * b.x1 * K.mp2) / (1.0 - b.x1);
+  b.t2  = -(b.pt2sq + b.x2 * (b.mf2sq - K.mp2) + b.x2 * b.x2 * K.mp2) / (1.0 - b.x2);
+  b.s13 = b.mf1sq + b.m3sq + b.p1p * b.p3m + b.p1m * b.p3p - 2.0 * (b.p1x * b.p3x + b.p1y * b.p3y);
+  b.s14 = b.mf1sq + b.m4sq + b.p1p * b.p4m + b.p1m * b.p4p - 2.0 * (b.p1x * b.p4x + b.p1y * b.p4y);
+  b.s23 = b.mf2sq + b.m3sq + b.p2p * b.p3m + b.p2m * b.p3p - 2.0 * (b.p2x * b.p3x + b.p2y * b.p3y);
+  b.s24 = b.mf2sq + b.m4sq + b.p2p * b.p4m + b.p2m * b.p4p - 2.0 * (b.p2x * b.p4x + b.p2y * b.p4y);
   b.m2  = b.m3sq + b.m4sq + b.p3p * b.p4m + b.p3m * b.p4p - 2.0 * (b.p3x * b.p4x + b.p3y * b.p4y);
   // t_hat = (q1 - p3)^2 with q1 = pb1 - p1: (q1+ - p3+) = p4+ - eps + p2+ by conservation.
   {
@@ -950,15 +1008,19 @@ GRN_HD bool born_kinematics_F(const grn_process_params &P, const Consts &K, cons
   const double eY  = exp(yX);
   const double XP = mTX * eY, XM = mTX / eY;
   const double EX = 0.5 * (XP + XM), ZX = 0.5 * (XP - XM);
-  if (EX > K.sqrt_s - 2.0 * sqrt(K.mp2)) return false;  // energy overflow (MFactorized.cc:323)
+  // forward masses: u[6] (and u[7] for double excitation; the side draw u[7] for single)
+  forward_masses(P, K, u[6], u[7], u[7], b);
+  if (EX > K.sqrt_s - (sqrt(b.mf1sq) + sqrt(b.mf2sq))) return false;  // MFactorized.cc:321
   // isotropic decay in the central-system rest frame, boosted to the lab
   const double MX = sqrt(m2X);
   const double ms = m3 + m4, md = m3 - m4;
   const double ps = sqrt(fmax(0.0, (MX - ms) * (MX + ms) * (MX + md) * (MX - md))) / (2.0 * MX);
-  const double ct = 2.0 * u[6] - 1.0;
+  // decay angles: the draws after the forward masses (u[6], u[7]; u[8], u[9] when excited)
+  const int    da = (CASC && P.excitation) ? 8 : 6;
+  const double ct = 2.0 * u[da] - 1.0;
   const double st = sqrt(fmax(0.0, 1.0 - ct * ct));
   double sp, cp;
-  sincos_pi(2.0 * u[7], sp, cp);
+  sincos_pi(2.0 * u[da + 1], sp, cp);
   const double kx = ps * st * cp, ky = ps * st * sp, kz = ps * ct;
   const double E3s = sqrt(b.m3sq + ps * ps), E4s = sqrt(b.m4sq + ps * ps);
   const double bx = Xx / EX, by = Xy / EX, bz = ZX / EX, gam = EX / MX;
@@ -1003,6 +1065,12 @@ GRN_HD bool fiducial_cuts(const grn_process_params &P, const Consts &K, const Bo
   if (!f.active) return true;
   const double at1 = fabs(b.t1), at2 = fabs(b.t2);
   if (!(at1 >= f.ft_min && at1 <= f.ft_max && at2 >= f.ft_min && at2 <= f.ft_max)) return false;
+  // excited forward systems: their mass window (CommonCuts, src/MProcess.cc:1105-1119)
+  if (b.exc) {
+    const double mf1 = sqrt(b.mf1sq), mf2 = sqrt(b.mf2sq);
+    if ((b.exc & 1) && !(mf1 >= f.fM_min && mf1 <= f.fM_max)) return false;
+    if ((b.exc & 2) && !(mf2 >= f.fM_min && mf2 <= f.fM_max)) return false;
+  }
   const double M  = sqrt(fmax(b.m2, 0.0));
   const double Y  = 0.5 * log((b.p3p + b.p4p) / (b.p3m + b.p4m));
   const double sx = b.p3x + b.p4x, sy = b.p3y + b.p4y;
@@ -1040,15 +1108,18 @@ GRN_HD bool veto_cuts(const grn_process_params &P, const Born &b) {
 // invariants. Used for the FP64 Born amplitude and, with T = float, per loop point.
 template <typename T>
 GRN_HD cx<T> regge_me4(const grn_process_params &P, const Consts &K, T t1, T t2, T lns13, T lns14,
-                       T lns23, T lns24, T that, T uhat) {
+                       T lns23, T lns24, T that, T uhat, int exc = 0, T mf1sq = T(0),
+                       T mf2sq = T(0)) {
   const grn_regge_params &rp = P.regge;
   const T M2  = T(K.M2prop);
   const T ffa = meson_ff<T>(rp, that, M2);
   const T ffb = meson_ff<T>(rp, uhat, M2);
   const T Xt  = ffa * ffa / (that - M2);
   const T Xu  = ffb * ffb / (uhat - M2);
-  const T vtx = T(K.gN2) * proton_ff<T>(T(P.soft.fc1), T(P.soft.fc2), t1) *
-                proton_ff<T>(T(P.soft.fc1), T(P.soft.fc2), t2) * T(K.g2);
+  const T vtx = exc ? leg_vertex<T>(P, K, exc, 0, t1, mf1sq) *
+                          leg_vertex<T>(P, K, exc, 1, t2, mf2sq) * T(K.g2)
+                    : T(K.gN2) * proton_ff<T>(T(P.soft.fc1), T(P.soft.fc2), t1) *
+                          proton_ff<T>(T(P.soft.fc1), T(P.soft.fc2), t2) * T(K.g2);
   if (K.n_active == 1) {
     // One trajectory: both channels share the phase exp(-i pi ap (t1+t2)/2).
     const int k  = K.active[0] ? 0 : (K.active[1] ? 1 : 2);
@@ -1306,6 +1377,8 @@ struct LoopEvent {
   T a1, a2;                 // (P+ - eps)/L, (P- - eps)/L
   T ia1, ia2;               // 1/(1 - a1), 1/(1 - a2)
   T invL, invL2, L, eps, mp2, m3sq, m4sq;
+  T mf1, mf2;               // forward legs' masses^2 (mp2 unless excited)
+  int exc;                  // excited forward legs (bit 0: leg 1, bit 1: leg 2)
   ResSums<T> res;           // PP[RESTENSOR]: resonance sums of the tree-level central mass
 };
 
@@ -1320,11 +1393,16 @@ GRN_HD bool loop_point_kin(const LoopEvent<T> &e, T kx, T ky, LCKin<T> &kk) {
   const T q2x = e.p2x + kx, q2y = e.p2y + ky;
   const T pt1sq = q1x * q1x + q1y * q1y;
   const T pt2sq = q2x * q2x + q2y * q2y;
-  const T mT1sq = e.mp2 + pt1sq, mT2sq = e.mp2 + pt2sq;
+  const T mT1sq = e.mf1 + pt1sq, mT2sq = e.mf2 + pt2sq;
   const T c1 = mT1sq * e.invL2, c2 = mT2sq * e.invL2;
-  const T r1 = T(1) / (T(1) - (e.a1 + c2 * e.ia2));
-  const T r2 = T(1) / (T(1) - (e.a2 + c1 * e.ia1));
-  const T x1 = e.a1 + c2 * r2, x2 = e.a2 + c1 * r1;
+  T r1 = T(1) / (T(1) - (e.a1 + c2 * e.ia2));
+  T r2 = T(1) / (T(1) - (e.a2 + c1 * e.ia1));
+  T x1 = e.a1 + c2 * r2, x2 = e.a2 + c1 * r1;
+  if (e.exc) {  // excited legs: c up to M^2 / s, the closed-form closure (solve_x)
+    if (!solve_x<T>(e.a1, e.a2, c1, c2, x1, x2)) return false;
+    r1 = T(1) / (T(1) - x1);
+    r2 = T(1) / (T(1) - x2);
+  }
   if (!((x1 > T(0)) && (x2 > T(0)) && (x1 < T(1)) && (x2 < T(1)))) return false;
   const T p1p = (T(1) - x1) * e.L;
   const T p1m = mT1sq * r1 * e.invL;
@@ -1335,12 +1413,12 @@ GRN_HD bool loop_point_kin(const LoopEvent<T> &e, T kx, T ky, LCKin<T> &kk) {
   kk.p3p = e.p3p; kk.p3m = e.p3m; kk.p3x = e.p3x; kk.p3y = e.p3y;
   kk.p4p = e.p4p; kk.p4m = e.p4m; kk.p4x = e.p4x; kk.p4y = e.p4y;
   kk.L = e.L; kk.eps = e.eps; kk.mp2 = e.mp2;
-  kk.t1  = -(pt1sq + x1 * x1 * e.mp2) * r1;
-  kk.t2  = -(pt2sq + x2 * x2 * e.mp2) * r2;
-  kk.s13 = e.mp2 + e.m3sq + p1p * e.p3m + p1m * e.p3p - T(2) * (q1x * e.p3x + q1y * e.p3y);
-  kk.s14 = e.mp2 + e.m4sq + p1p * e.p4m + p1m * e.p4p - T(2) * (q1x * e.p4x + q1y * e.p4y);
-  kk.s23 = e.mp2 + e.m3sq + p2p * e.p3m + p2m * e.p3p - T(2) * (q2x * e.p3x + q2y * e.p3y);
-  kk.s24 = e.mp2 + e.m4sq + p2p * e.p4m + p2m * e.p4p - T(2) * (q2x * e.p4x + q2y * e.p4y);
+  kk.t1  = -(pt1sq + x1 * (e.mf1 - e.mp2) + x1 * x1 * e.mp2) * r1;
+  kk.t2  = -(pt2sq + x2 * (e.mf2 - e.mp2) + x2 * x2 * e.mp2) * r2;
+  kk.s13 = e.mf1 + e.m3sq + p1p * e.p3m + p1m * e.p3p - T(2) * (q1x * e.p3x + q1y * e.p3y);
+  kk.s14 = e.mf1 + e.m4sq + p1p * e.p4m + p1m * e.p4p - T(2) * (q1x * e.p4x + q1y * e.p4y);
+  kk.s23 = e.mf2 + e.m3sq + p2p * e.p3m + p2m * e.p3p - T(2) * (q2x * e.p3x + q2y * e.p3y);
+  kk.s24 = e.mf2 + e.m4sq + p2p * e.p4m + p2m * e.p4p - T(2) * (q2x * e.p4x + q2y * e.p4y);
   {
     const T dp = e.p4p - e.eps + p2p;
     const T dm = e.eps - p1m - e.p3m;
@@ -1355,9 +1433,9 @@ GRN_HD bool loop_point_kin(const LoopEvent<T> &e, T kx, T ky, LCKin<T> &kk) {
   }
   // q1 = pa - p1: q1+ = x1 L, q1- = -(pT1^2 + x1 mp^2) / ((1 - x1) L) (q_lightcone)
   kk.q1p = x1 * e.L;
-  kk.q1m = -(pt1sq + x1 * e.mp2) * r1 * e.invL;
+  kk.q1m = -(pt1sq + (e.mf1 - e.mp2) + x1 * e.mp2) * r1 * e.invL;
   kk.q2m = x2 * e.L;
-  kk.q2p = -(pt2sq + x2 * e.mp2) * r2 * e.invL;
+  kk.q2p = -(pt2sq + (e.mf2 - e.mp2) + x2 * e.mp2) * r2 * e.invL;
   return true;
 }
 
@@ -1375,7 +1453,7 @@ GRN_HD bool loop_point_amp(const grn_process_params &P, const Consts &K, const L
     if (K.n_res > 0) A = cadd(A, tensor_me3<T>(P, K, kk, e.res));
   } else {
     A = regge_me4<T>(P, K, kk.t1, kk.t2, log(kk.s13), log(kk.s14), log(kk.s23), log(kk.s24),
-                     kk.that, kk.uhat);
+                     kk.that, kk.uhat, e.exc, e.mf1, e.mf2);
   }
   return true;
 }
@@ -1669,6 +1747,7 @@ GRN_HD void make_loop_event(const Consts &K, const Born &b, LoopEvent<T> &e) {
   e.ia2 = T(1.0 / (1.0 - a2));
   e.L = T(K.L); e.invL2 = T(1.0 / (K.L * K.L)); e.invL = T(1.0 / K.L);
   e.eps = T(K.eps); e.mp2 = T(K.mp2); e.m3sq = T(b.m3sq); e.m4sq = T(b.m4sq);
+  e.mf1 = T(b.mf1sq); e.mf2 = T(b.mf2sq); e.exc = b.exc;
   if (K.n_res > 0) {
     const ResVec<double> v =
         res_vectors<double>(K, b.p3p, b.p3m, b.p3x, b.p3y, b.p4p, b.p4m, b.p4x, b.p4y);
@@ -1795,7 +1874,7 @@ GRN_HD cx<double> born_amp(const grn_process_params &P, const Consts &K, const B
     return cadd(Ac, tensor_me3<double>(P, K, k, resonance_sums(K, b.m2, v)));
   }
   return regge_me4<double>(P, K, b.t1, b.t2, log(b.s13), log(b.s14), log(b.s23), log(b.s24),
-                           b.that, b.uhat);
+                           b.that, b.uhat, b.exc, b.mf1sq, b.mf2sq);
 }
 
 // Processes whose |M|^2 is a sum over several helicity amplitudes (vector pairs, "2xV").
@@ -1842,7 +1921,7 @@ GRN_HD double weight_jacobian(const Consts &K, const Born &b) {
   const double E2 = 0.5 * (b.p2p + b.p2m), pz2 = 0.5 * (b.p2p - b.p2m);
   const double J  = 1.0 / fabs(pz1 / E1 - pz2 / E2);
   const double pt1 = sqrt(b.pt1sq), pt2 = sqrt(b.pt2sq);
-  return K.w_const * (pt1 / (2.0 * E1)) * (pt2 / (2.0 * E2)) * J * b.jx * pt1 * pt2;
+  return K.w_const * (pt1 / (2.0 * E1)) * (pt2 / (2.0 * E2)) * J * b.jx * pt1 * pt2 * b.jf;
 }
 
 }  // namespace grn

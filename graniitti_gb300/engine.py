@@ -150,10 +150,12 @@ class Engine:
         return t
 
     def set_tuning(self, loop_pair=None, vegas_blocks=None, weight_blocks=None,
-                   fp64_refine=None):
+                   fp64_refine=None, refine_tol=None):
         t = self.tuning()
         if fp64_refine is not None:
             t.fp64_refine = int(fp64_refine)
+        if refine_tol is not None:
+            t.refine_tol = float(refine_tol)
         if loop_pair is not None:
             t.loop_pair = loop_pair
         if vegas_blocks is not None:

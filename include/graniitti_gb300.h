@@ -205,6 +205,15 @@ typedef struct grn_process_params {
   int32_t           veto_active, n_veto;
   double            veto_eta_min[GRN_MAX_VETO], veto_eta_max[GRN_MAX_VETO];
   double            veto_pt_min[GRN_MAX_VETO], veto_pt_max[GRN_MAX_VETO];
+  /* Forward excitation (NSTARS, MProcess::SampleForwardMasses, src/MProcess.cc:1317-1365):
+   * 0 elastic forward protons, 1 one of them excited (the side drawn 50-50), 2 both. The
+   * excited masses^2 are drawn log-uniformly in [1.09^2, xi_max s] (GENCUTS "Xi"); the
+   * excited leg's vertex is sqrt(g3P gN_P) S3FINEL(t, M^2) (MRegge::PomPomProtonVertex). The
+   * hypercube gains the mass coordinates and, for 1, the side choice (2-body states: 10
+   * dimensions). Implemented for the Regge continuum of two central particles. */
+  int32_t           excitation;
+  int32_t           _pad_x;
+  double            xi_max;
 } grn_process_params;
 
 /* Fill every field with the reference defaults for "PP[CON]<C> -> pi+ pi-" at
@@ -636,6 +645,8 @@ typedef struct grn_tuning {
   int32_t vegas_blocks;  /* grid of the loop stage of VEGAS and flow passes */
   int32_t weight_blocks; /* grid of the loop stage of grn_event_weights */
   int32_t fp64_refine;   /* 1 recompute badly conditioned FP32-loop events in FP64, 0 never */
+  double  refine_tol;    /* relative weight error above which an FP32-loop event's estimated
+                            rounding sends it to FP64 (default 1e-5; in [1e-9, 1]) */
 } grn_tuning;
 grn_status grn_get_tuning(grn_engine *e, grn_tuning *t);
 grn_status grn_set_tuning(grn_engine *e, const grn_tuning *t);

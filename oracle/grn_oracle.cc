@@ -166,6 +166,12 @@ cplx regge_eta_linear(real t, real a0, real ap, real sigma) {
 real proton_ff(const grn_soft_params &sp, real t) {
   return (1.0 / (1.0 - t / sp.fc1)) * (1.0 / (1.0 - t / sp.fc2));
 }
+// Inelastic proton vertex of an excited forward leg of mass^2 M2 (S3FINEL, src/MForm.cc:
+// 443-449): (|t| / (M2 (|t| + a)))^((1 + Delta_P) / 2), Delta_P = 0.0808, a = 0.5616 GeV^2.
+real proton_ff_inel(real t, real M2) {
+  const real DELTA_P = 0.0808, a = 0.5616;
+  return std::pow(std::fabs(t) / (M2 * (std::fabs(t) + a)), 0.5 * (1.0 + DELTA_P));
+}
 // Pion-loop insert of the non-linear pomeron trajectory (src/MForm.cc:418-427).
 real pion_loop(const grn_soft_params &sp, real tau, real t) {
   const real sqt = std::sqrt(1.0 + tau);
@@ -224,6 +230,9 @@ struct Event {
   V4     leaf[4];          // cascades: final-state daughters (central 1: 0, 1; central 2: 2, 3)
   real t1 = 0, t2 = 0, that = 0, uhat = 0, m2 = 0, Y = 0, Pt = 0;
   real ss[7][7] = {};
+  // forward legs: masses (the beam mass, or the excited N* mass) and the excitation flags
+  real mf1 = 0, mf2 = 0;
+  bool ex1 = false, ex2 = false;
   // 4-body central states: (q1 - p_i)^2, (q2 - p_i)^2, (q1 - p_i - p_j)^2 (MProcess.cc:1556-1561)
   real tt1[7] = {}, tt2[7] = {}, ttxy[7][7] = {};
 };
@@ -235,6 +244,8 @@ struct Setup {
   const double      *msa = nullptr;  // (x, re, im) rows (the table as given, double)
   int                n_kt2 = 0;
 };
+
+void forward_masses(const Setup &S, real u_m0, real u_m1, real u_side, Event &ev);
 
 // Longitudinal momentum of leg 3 in p1 p2 -> p3 {p5} p4 (CM frame): the two
 // forward legs carry transverse masses a = m3^2+pt3^2, b = m4^2+pt4^2 and share the
@@ -302,9 +313,7 @@ void central_pair(const V4 &q, const V4 &p1, const V4 &p2, const real m[2], cons
 // Forward legs from the central system (MContinuum.cc:372-384); false when the
 // event fails the crude energy check or the forward-direction check.
 bool forward_legs(const Setup &S, real pt1, real phi1x, real phi1y, real pt2,
-                  real phi2x, real phi2y, const V4 &sumP, V4 &p1, V4 &p2) {
-  (void)phi1x;
-  const real m1 = S.p.m_beam, m2 = S.p.m_beam;
+                  real phi2x, real phi2y, const V4 &sumP, V4 &p1, V4 &p2, real m1, real m2) {
   const real p1z = solve_pz(m1, m2, pt1, pt2, sumP.z, sumP.e, S.s);
   const real p2z = -(sumP.z + p1z);
   if (p1z < 0 || p2z > 0) return false;
@@ -379,7 +388,9 @@ bool build_kinematics_c4(const Setup &S, const real *u, Event &ev) {
   central_four(ev.kq, p1, p2, mc, y, c);
   const V4 sumP = c[0] + c[1] + c[2] + c[3];
   if (sumP.e > S.sqrt_s) return false;
-  if (!forward_legs(S, pt1, p1.x, p1.y, pt2, p2.x, p2.y, sumP, p1, p2)) return false;
+  forward_masses(S, 0, 0, 0, ev);
+  if (!forward_legs(S, pt1, p1.x, p1.y, pt2, p2.x, p2.y, sumP, p1, p2, ev.mf1, ev.mf2))
+    return false;
   ev.pf[0] = sumP;
   ev.pf[1] = p1;
   ev.pf[2] = p2;
@@ -423,7 +434,10 @@ bool build_kinematics(const Setup &S, const real *u, Event &ev) {
   central_pair(ev.q, p1, p2, m, y, c);
   const V4 sumP = c[0] + c[1];
   if (sumP.e > S.sqrt_s) return false;
-  if (!forward_legs(S, pt1, p1.x, p1.y, pt2, p2.x, p2.y, sumP, p1, p2)) return false;
+  // forward N* masses: u[8] (and u[9] for double excitation; the side draw for single)
+  forward_masses(S, u[8], S.p.excitation == 2 ? u[9] : 0, S.p.excitation == 1 ? u[9] : 0, ev);
+  if (!forward_legs(S, pt1, p1.x, p1.y, pt2, p2.x, p2.y, sumP, p1, p2, ev.mf1, ev.mf2))
+    return false;
 
   ev.pf[0] = sumP;
   ev.pf[1] = p1;
@@ -462,7 +476,33 @@ int decay_coord(const grn_process_params &p) { return offshell_widths(p) > 0 ? 1
 // Hypercube dimension of a process.
 int point_dim(const grn_process_params &p) {
   if (p.n_central == 4) return 14;
+  if (p.excitation) return 10;
   return p.n_decay == 2 ? decay_coord(p) + 4 : 8;
+}
+
+// Forward N* masses (MProcess::SampleForwardMasses, src/MProcess.cc:1317-1365): M^2
+// log-uniform in [1.09^2, xi_max s] from the class's mass coordinates; single excitation
+// takes the side from a further draw (< 0.5: the first leg), lifted to the coordinate after.
+// u_m: the mass coordinate(s); u_side: the side draw (single excitation).
+void forward_masses(const Setup &S, real u_m0, real u_m1, real u_side, Event &ev) {
+  ev.mf1 = ev.mf2 = S.p.m_beam;
+  ev.ex1 = ev.ex2 = false;
+  if (!S.p.excitation) return;
+  const real lo = std::log(sq(1.09)), hi = std::log(S.p.xi_max * S.s);
+  if (S.p.excitation == 1) {
+    const real M = std::sqrt(std::exp(lo + (hi - lo) * u_m0));
+    if (u_side < 0.5) {
+      ev.mf1 = M;
+      ev.ex1 = true;
+    } else {
+      ev.mf2 = M;
+      ev.ex2 = true;
+    }
+  } else {
+    ev.mf1 = std::sqrt(std::exp(lo + (hi - lo) * u_m0));
+    ev.mf2 = std::sqrt(std::exp(lo + (hi - lo) * u_m1));
+    ev.ex1 = ev.ex2 = true;
+  }
 }
 
 // Off-shell masses of the two central particles of a cascade (GetOffShellMass, the
@@ -582,8 +622,11 @@ bool build_kinematics_F(const Setup &S, const real *u, Event &ev) {
   const real mtX = msqrt(m2X + pX.pt2());
   pX.z = mtX * std::sinh(yX);
   pX.e = mtX * std::cosh(yX);
-  if (pX.e > S.sqrt_s - 2.0 * S.p.m_beam) return false;
-  if (!forward_legs(S, pt1, p1.x, p1.y, pt2, p2.x, p2.y, pX, p1, p2)) return false;
+  // forward N* masses: u[6] (and u[7] for double excitation; the side draw u[7] for single)
+  forward_masses(S, u[6], S.p.excitation == 2 ? u[7] : 0, S.p.excitation == 1 ? u[7] : 0, ev);
+  if (pX.e > S.sqrt_s - (ev.mf1 + ev.mf2)) return false;  // MFactorized.cc:321
+  if (!forward_legs(S, pt1, p1.x, p1.y, pt2, p2.x, p2.y, pX, p1, p2, ev.mf1, ev.mf2))
+    return false;
   ev.pf[0] = pX;
   ev.pf[1] = p1;
   ev.pf[2] = p2;
@@ -596,7 +639,10 @@ bool build_kinematics_F(const Setup &S, const real *u, Event &ev) {
     for (int k = 0; k < 4; ++k) ev.leaf[k] = ev.pf[3 + k];
     return lorentz_scalars(S, ev);
   }
-  ev.dw = two_body(pX, msqrt(m2X), m3, m4, 2.0 * u[6] - 1.0, 2.0 * PI * u[7], ev.pf[3], ev.pf[4]);
+  // decay angles: the draws after the forward masses (u[6], u[7]; u[8], u[9] when excited)
+  const int da = S.p.excitation ? 8 : 6;
+  ev.dw = two_body(pX, msqrt(m2X), m3, m4, 2.0 * u[da] - 1.0, 2.0 * PI * u[da + 1], ev.pf[3],
+                   ev.pf[4]);
   if (S.p.n_decay == 2) cascade_decays(S, u, m3, m4, ev);
   return lorentz_scalars(S, ev);
 }
@@ -616,9 +662,10 @@ bool loop_kinematics(const Setup &S, const Event &born, real p1x, real p1y, real
     const real mtX = msqrt(mX * mX + pX.pt2());
     pX.z = mtX * std::sinh(yX);
     pX.e = mtX * std::cosh(yX);
-    if (pX.e > S.sqrt_s - 2.0 * S.p.m_beam) return false;
+    if (pX.e > S.sqrt_s - (born.mf1 + born.mf2)) return false;
     V4 p1, p2;
-    if (!forward_legs(S, p1T.pt(), p1x, p1y, p2T.pt(), p2x, p2y, pX, p1, p2)) return false;
+    if (!forward_legs(S, p1T.pt(), p1x, p1y, p2T.pt(), p2x, p2y, pX, p1, p2, born.mf1, born.mf2))
+      return false;
     ev       = born;
     ev.pf[0] = pX;
     ev.pf[1] = p1;
@@ -638,7 +685,9 @@ bool loop_kinematics(const Setup &S, const Event &born, real p1x, real p1y, real
     central_four(born.kq, p1T, p2T, m4, y4, c);
     const V4 sumP = c[0] + c[1] + c[2] + c[3];
     V4 p1, p2;
-    if (!forward_legs(S, p1T.pt(), p1x, p1y, p2T.pt(), p2x, p2y, sumP, p1, p2)) return false;
+    if (!forward_legs(S, p1T.pt(), p1x, p1y, p2T.pt(), p2x, p2y, sumP, p1, p2, born.mf1,
+                      born.mf2))
+      return false;
     ev       = born;
     ev.pf[0] = sumP;
     ev.pf[1] = p1;
@@ -654,7 +703,12 @@ bool loop_kinematics(const Setup &S, const Event &born, real p1x, real p1y, real
   const V4 sumP = c[0] + c[1];
   const real pt1 = p1T.pt(), pt2 = p2T.pt();
   V4 p1, p2;
-  if (!forward_legs(S, pt1, p1x, p1y, pt2, p2x, p2y, sumP, p1, p2)) return false;
+  if (!forward_legs(S, pt1, p1x, p1y, pt2, p2x, p2y, sumP, p1, p2, born.mf1, born.mf2))
+    return false;
+  ev.mf1   = born.mf1;
+  ev.mf2   = born.mf2;
+  ev.ex1   = born.ex1;
+  ev.ex2   = born.ex2;
   ev.q     = born.q;
   ev.pf[0] = sumP;
   ev.pf[1] = p1;
@@ -670,8 +724,12 @@ bool loop_kinematics(const Setup &S, const Event &born, real p1x, real p1y, real
 cplx regge_me4(const Setup &S, const Event &ev) {
   const grn_regge_params &rp = S.p.regge;
   const real M2  = sq(S.p.m_central[0]);
-  const real FFA = S.p.soft.gN_P * proton_ff(S.p.soft, ev.t1);
-  const real FFB = S.p.soft.gN_P * proton_ff(S.p.soft, ev.t2);
+  // PomPomProtonVertex (src/MRegge.cc:637-644): elastic, or the excited leg's inelastic vertex
+  const real gin = std::sqrt(S.p.soft.g3P * S.p.soft.gN_P);
+  const real FFA = ev.ex1 ? gin * proton_ff_inel(ev.t1, ev.pf[1].m2())
+                          : S.p.soft.gN_P * proton_ff(S.p.soft, ev.t1);
+  const real FFB = ev.ex2 ? gin * proton_ff_inel(ev.t2, ev.pf[2].m2())
+                          : S.p.soft.gN_P * proton_ff(S.p.soft, ev.t2);
   const real g   = rp.c[0] / S.p.soft.gN_P;
   const cplx At = regge_prop(rp, ev.ss[1][3], ev.t1) * FFA * meson_ff(rp, ev.that, M2) * g *
                   (1.0 / (ev.that - M2)) * meson_ff(rp, ev.that, M2) * g *
@@ -690,8 +748,12 @@ cplx regge_me4(const Setup &S, const Event &ev) {
 cplx regge_me6(const Setup &S, const Event &ev) {
   const grn_regge_params &rp = S.p.regge;
   const real MA  = sq(S.p.m_central[0]), MB = sq(S.p.m_central[2]);
-  const real FFA = S.p.soft.gN_P * proton_ff(S.p.soft, ev.t1);
-  const real FFB = S.p.soft.gN_P * proton_ff(S.p.soft, ev.t2);
+  // PomPomProtonVertex (src/MRegge.cc:637-644): elastic, or the excited leg's inelastic vertex
+  const real gin = std::sqrt(S.p.soft.g3P * S.p.soft.gN_P);
+  const real FFA = ev.ex1 ? gin * proton_ff_inel(ev.t1, ev.pf[1].m2())
+                          : S.p.soft.gN_P * proton_ff(S.p.soft, ev.t1);
+  const real FFB = ev.ex2 ? gin * proton_ff_inel(ev.t2, ev.pf[2].m2())
+                          : S.p.soft.gN_P * proton_ff(S.p.soft, ev.t2);
   const real g   = rp.c[0] / S.p.soft.gN_P;
   int perm[4] = {3, 4, 5, 6};
   cplx A(0, 0);
@@ -1515,8 +1577,19 @@ int bare_amps(const Setup &S, const Event &ev, cplx *A) {
   return 1;
 }
 
+// ForwardVolume's excitation factor (src/MProcess.cc:1399-1413): per excited leg the
+// log-change Jacobian M^2 times the log range of M^2.
+real forward_mass_volume(const Setup &S, const Event &ev) {
+  if (!S.p.excitation) return 1.0;
+  const real range = std::log(S.p.xi_max * S.s) - std::log(sq(1.09));
+  real v = 1.0;
+  if (ev.ex1) v *= ev.pf[1].m2() * range;
+  if (ev.ex2) v *= ev.pf[2].m2() * range;
+  return v;
+}
+
 // Phase-space weight and integration volume (MContinuum.cc:619-656; ForwardVolume
-// MProcess.cc:1390-1415), elastic forward legs, Kf = 2.
+// MProcess.cc:1390-1415).
 real ps_factor(const Setup &S, const Event &ev) {
   const grn_gencuts &g = S.p.gcuts;
   const real J = 1.0 / std::fabs(ev.pf[1].z / ev.pf[1].e - ev.pf[2].z / ev.pf[2].e);
@@ -1529,7 +1602,8 @@ real ps_factor(const Setup &S, const Event &ev) {
     const real psw  = 0.5 * (1.0 / std::pow(2.0 * PI, 5)) * (ev.pf[1].pt() / (2.0 * ev.pf[1].e)) *
                        (ev.pf[2].pt() / (2.0 * ev.pf[2].e)) * J;
     const real fwd = sq(2.0 * PI) * ev.pf[1].pt() * ev.pf[2].pt() *
-                       sq(std::log(g.fpt_max) - std::log(g.fpt_min + ZERO_EPS));
+                       sq(std::log(g.fpt_max) - std::log(g.fpt_min + ZERO_EPS)) *
+                       forward_mass_volume(S, ev);
     const real vol = (ev.m2hi - ev.m2lo) * (g.Y_max - g.Y_min) * fwd;
     return (ev.dw / (2.0 * PI)) * psw * vol;
   }
@@ -1540,7 +1614,8 @@ real ps_factor(const Setup &S, const Event &ev) {
                      (ev.pf[1].pt() / (2.0 * ev.pf[1].e)) * (ev.pf[2].pt() / (2.0 * ev.pf[2].e)) *
                      J * prod;
   const real fwd = sq(2.0 * PI) * ev.pf[1].pt() * ev.pf[2].pt() *
-                     sq(std::log(g.fpt_max) - std::log(g.fpt_min + ZERO_EPS));
+                     sq(std::log(g.fpt_max) - std::log(g.fpt_min + ZERO_EPS)) *
+                     forward_mass_volume(S, ev);
   const real vol = std::pow(g.kt_max - g.kt_min, Kf - 1) * std::pow(2.0 * PI, Kf - 1) *
                      std::pow(g.rap_max - g.rap_min, Kf) * fwd;
   return psw * vol;
@@ -1552,6 +1627,9 @@ bool fiducial(const Setup &S, const Event &ev) {
   if (!f.active) return true;
   const real at1 = std::fabs(ev.t1), at2 = std::fabs(ev.t2);
   if (!(at1 >= f.ft_min && at1 <= f.ft_max && at2 >= f.ft_min && at2 <= f.ft_max)) return false;
+  // excited forward systems: their mass window (CommonCuts, src/MProcess.cc:1105-1119)
+  if (ev.ex1 && !(ev.pf[1].m() >= f.fM_min && ev.pf[1].m() <= f.fM_max)) return false;
+  if (ev.ex2 && !(ev.pf[2].m() >= f.fM_min && ev.pf[2].m() <= f.fM_max)) return false;
   const real M = msqrt(ev.m2);
   if (!(M >= f.M_min && M <= f.M_max && ev.Y >= f.Y_min && ev.Y <= f.Y_max && ev.Pt >= f.Pt_min &&
         ev.Pt <= f.Pt_max))

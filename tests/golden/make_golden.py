@@ -9,7 +9,8 @@ reference does not. Steps:
   4. run the reference VEGAS integration for the cross section
 
 Usage: python tests/golden/make_golden.py [--ref <reference source tree>]
-                                          [--only resonances|cascades|rescon|regge_res]
+                                          [--only resonances|cascades|rescon|regge_res|
+                                                  nbody|nbody_c|veto|ccascades|excitation|ld]
 """
 import argparse
 import json
@@ -342,6 +343,32 @@ def ccascade_fixtures():
     write_sigma("rrc_vegas_sigma.json", out, proc, os.path.basename(CARD))
 
 
+def excitation_fixtures():
+    """Forward excitation (NSTARS = 1, 2; MProcess::SampleForwardMasses, PomPomProtonVertex,
+    ForwardVolume) of the Regge pi+ pi- continuum, both classes, M^2 / s <= 0.05, 10-dimensional
+    points: <C> u[8] (u[9]) the excited masses, single excitation's side draw u[9]; <F> u[6]
+    (u[7]) the masses or the side draw, the decay angles u[8], u[9]. The specs below serve the
+    draws the reference takes inside EventWeight, in order (two inert pion mass draws, the side,
+    the decay angles); each was checked to be consumed exactly."""
+    c1 = os.path.join(HERE, "cards", "pp_con_pipi_nstar1.json")
+    c2 = os.path.join(HERE, "cards", "pp_con_pipi_nstar2.json")
+    cs = os.path.join(HERE, "cards", "pp_con_pipi_nstar1_screened.json")
+    PC, PF = "PP[CON]<C> -> pi+ pi-", "PP[CON]<F> -> pi+ pi-"
+    cases = [("nstar1_c_tree_weights.npz", 221, c1, PC, "h,h,9", 9),
+             ("nstar2_c_tree_weights.npz", 222, c2, PC, "h,h", 10),
+             ("nstar1_f_tree_weights.npz", 223, c1, PF, "h,h,7,8,9", 7),
+             ("nstar2_f_tree_weights.npz", 224, c2, PF, "h,h,8,9", 8)]
+    for name, seed, card, proc, spec, dim in cases:
+        u = philox_np.uniforms(seed, 1024, 10)
+        r = run_weights(card, u, ["--replay", spec], proc=proc, dim=dim)
+        save(name, seed=seed, u=u, card=os.path.basename(card), proc=proc, **r)
+    u = philox_np.uniforms(225, 128, 10)
+    r = run_weights(cs, u, ["--replay", "h,h,9", "--nbt", "1024", "--nkt2", "10000"], proc=PC,
+                    dim=9)
+    save("nstar1_c_screened_15x12_weights.npz", seed=225, u=u, card=os.path.basename(cs),
+         proc=PC, n_bt=1024, n_kt2=10000, loop_kt=15, loop_phi=12, loop_ktmax=1.75, **r)
+
+
 def ld_fixtures():
     """The oracle restatement in long double arithmetic (oracle/_build/liborc_ld.so: the same
     formulas and constants as the reference, 64-bit significands on x86) on the points of every
@@ -369,7 +396,8 @@ def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--ref", default=REF_DEFAULT)
     ap.add_argument("--only", choices=["all", "resonances", "cascades", "rescon", "regge_res",
-                                       "nbody", "nbody_c", "veto", "ccascades", "ld"],
+                                       "nbody", "nbody_c", "veto", "ccascades", "ld",
+                                       "excitation"],
                     default="all")
     a = ap.parse_args()
     if a.only == "ld":  # needs only the oracle
@@ -377,6 +405,11 @@ def main():
         return
     subprocess.check_call(["make", "-s", "-C", os.path.join(REPO, "oracle", "refbuild"), "-j8",
                            "REF=" + a.ref])
+    if a.only in ("all", "excitation"):
+        excitation_fixtures()
+    if a.only == "excitation":
+        ld_fixtures()
+        return
     if a.only == "all":
         ld_fixtures()
     if a.only in ("all", "ccascades"):

@@ -305,6 +305,30 @@ def test_histogram_observables_from_reference_kinematics(params):
         assert diff.max() < 1e-8, (k, diff.max())
 
 
+# Forward excitation: the reference's own FP64 weights carry up to 4e-8 of rounding here (its
+# 4-vector forward legs at pT <= 100 GeV and N* masses up to sqrt(0.05 s); both it and the FP64
+# oracle are within that of the long-double oracle, see test_fp64_evaluations_vs_long_double).
+EXC_TOL = 1e-7
+
+
+@pytest.mark.parametrize("name", ["nstar1_c_tree_weights.npz", "nstar2_c_tree_weights.npz",
+                                  "nstar1_f_tree_weights.npz", "nstar2_f_tree_weights.npz",
+                                  "nstar1_c_screened_15x12_weights.npz"])
+def test_forward_excitation_weights(name):
+    """NSTARS = 1, 2 (MProcess::SampleForwardMasses, PomPomProtonVertex with S3FINEL,
+    ForwardVolume): the oracle against the reference's weights of the same 10-dimensional
+    points, both classes, tree level and screened."""
+    import sys
+    sys.path.insert(0, GOLDEN)
+    from fixture_meta import fixture_params
+    g = _load(name)
+    P, msa = fixture_params(name, g)
+    assert P.excitation in (1, 2) and g["u"].shape[1] == 10
+    w, fl = orc.weights(P, g["u"], msa=msa, nthreads=8)
+    rel = _check_weights(w, fl, g, tol=EXC_TOL)
+    print("%s: oracle vs reference max rel %.2e median %.2e" % (name, rel.max(), np.median(rel)))
+
+
 @pytest.mark.parametrize("name", ["veto_c_weights.npz", "veto_rr_weights.npz",
                                   "veto_f4_weights.npz"])
 def test_veto_cuts(name):
@@ -343,12 +367,14 @@ def test_fp64_evaluations_vs_long_double():
     """How far FP64 evaluations of the reference's formulas sit from their long-double value:
     the reference itself and the FP64 oracle both carry up to ~2.5e-9 relative rounding on
     fixtures where 13 TeV 4-vector products cancel (tensor resonances in <C>), typically
-    1e-10; the tests of the GPU engine compare it with the long-double weights."""
+    1e-10, and up to 4e-8 with excited forward legs (N* 4-vectors of mass up to sqrt(0.05 s),
+    forward pT up to 100 GeV); the tests of the GPU engine compare it with the long-double
+    weights."""
     import sys
     sys.path.insert(0, GOLDEN)
     from fixture_meta import fixture_params, weight_fixtures
     ld = np.load(os.path.join(GOLDEN, "long_double_oracle.npz"))
-    worst_ref = worst_orc = 0.0
+    worst_ref = worst_orc = worst_exc = 0.0
     for name in weight_fixtures():
         g = _load(name)
         if g["u"].shape[0] > 1024 or "loop_kt" in g or "n_bt" in g:
@@ -357,7 +383,13 @@ def test_fp64_evaluations_vs_long_double():
         w, _ = orc.weights(P, g["u"], msa=msa, nthreads=8)
         wl = ld[name[:-4]]
         nz = (wl > 0) & (g["w"] > 0)
-        worst_ref = max(worst_ref, np.max(np.abs(g["w"][nz] - wl[nz]) / wl[nz]))
-        worst_orc = max(worst_orc, np.max(np.abs(w[nz] - wl[nz]) / wl[nz]))
-    print("vs long double: reference %.2e, FP64 oracle %.2e" % (worst_ref, worst_orc))
-    assert worst_ref < 3e-9 and worst_orc < 3e-9
+        r_ref = np.max(np.abs(g["w"][nz] - wl[nz]) / wl[nz])
+        r_orc = np.max(np.abs(w[nz] - wl[nz]) / wl[nz])
+        if P.excitation:
+            worst_exc = max(worst_exc, r_ref, r_orc)
+        else:
+            worst_ref = max(worst_ref, r_ref)
+            worst_orc = max(worst_orc, r_orc)
+    print("vs long double: reference %.2e, FP64 oracle %.2e; with excitation %.2e" %
+          (worst_ref, worst_orc, worst_exc))
+    assert worst_ref < 3e-9 and worst_orc < 3e-9 and worst_exc < 1e-7
