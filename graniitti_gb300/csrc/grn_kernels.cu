@@ -91,7 +91,7 @@ __device__ cx<double> loop_integral(const KArgs &A, const Born &b, const KtNode<
                                     const PhiNode<T> *sphi, double *mag = nullptr) {
   constexpr bool kMag = sizeof(T) == sizeof(float);
   LoopEvent<T> e;
-  make_loop_event<T>(A.K, b, e);
+  make_loop_event<T>(A.P, A.K, b, e, kMag);
   T ar = T(0), ai = T(0), cr = T(0), ci = T(0), m = T(0);
   for (int j = 0; j < A.n_kt_nodes; ++j) {
     const KtNode<T> nj = skt[j];
@@ -109,8 +109,8 @@ __device__ cx<double> loop_integral(const KArgs &A, const Born &b, const KtNode<
     kahan_add(ai, ci, nj.cre * ii + nj.cim * ir);
     if constexpr (kMag) m += sqrt(nj.cre * nj.cre + nj.cim * nj.cim) * ab;
   }
-  if (mag) *mag = double(m);
-  const double sr = double(ar), si = double(ai);
+  if (mag) *mag = double(m) * e.escale;
+  const double sr = double(ar) * e.escale, si = double(ai) * e.escale;
   return {A.loop_norm_re * sr - A.loop_norm_im * si, A.loop_norm_re * si + A.loop_norm_im * sr};
 }
 
@@ -155,7 +155,7 @@ __device__ double screened_amp2_vv(const KArgs &A, const Born &b, const KtNode<T
   cx<double> A0[9];
   born_amps_2xv(A.P, A.K, b, A0);
   LoopEvent<T> e;
-  make_loop_event<T>(A.K, b, e);
+  make_loop_event<T>(A.P, A.K, b, e);
   LV<T> e3[3], e4[3];
   vector_basis<T>(T(b.p3p), T(b.p3m), T(b.p3x), T(b.p3y), e3);
   vector_basis<T>(T(b.p4p), T(b.p4m), T(b.p4x), T(b.p4y), e4);
@@ -203,12 +203,24 @@ __device__ __noinline__ cx<double> loop_integral_rr(const KArgs &A, const Born &
                                                     const PhiNode<T> *sphi, double *mag) {
   constexpr bool kMag = sizeof(T) == sizeof(float);
   LoopEvent<T> e;
-  make_loop_event<T>(A.K, b, e);
+  make_loop_event<T>(A.P, A.K, b, e);
   RegRes<double> Rd;
   regge_res_event(A.P, A.K, b.p3p, b.p3m, b.p3x, b.p3y, b.p4p, b.p4m, b.p4x, b.p4y, Rd);
   RegRes<T> R;
+  // resonances alone: factors C (form factor exp(-(m^2 - M0^2)^2 / S0^4) x Breit-Wigner) that
+  // leave the FP32 range are stored scaled by a power of two, undone after the sum in FP64
+  double sc = 1.0;
+  if (kMag && A.P.process == GRN_PROC_REGGE_RES) {
+    double cmax = 0.0;
+    for (int r = 0; r < A.K.rr_n; ++r) cmax = fmax(cmax, fabs(Rd.C[r].re) + fabs(Rd.C[r].im));
+    if (cmax > 0.0 && (cmax < 1e-25 || cmax > 1e25)) {
+      const int k = ilogb(cmax);
+      sc       = ldexp(1.0, -k);
+      e.escale = ldexp(1.0, k);
+    }
+  }
   for (int r = 0; r < A.K.rr_n; ++r) {
-    R.C[r] = {T(Rd.C[r].re), T(Rd.C[r].im)};
+    R.C[r] = {T(Rd.C[r].re * sc), T(Rd.C[r].im * sc)};
     for (int k = 0; k < 25; ++k) R.rho[r][k] = T(Rd.rho[r][k]);
   }
   R.Xe = T(Rd.Xe); R.Xx = T(Rd.Xx); R.Xy = T(Rd.Xy); R.Xz = T(Rd.Xz); R.M = T(Rd.M);
@@ -238,8 +250,8 @@ __device__ __noinline__ cx<double> loop_integral_rr(const KArgs &A, const Born &
     kahan_add(ai, ci, nj.cre * ii + nj.cim * ir);
     if constexpr (kMag) m += sqrt(nj.cre * nj.cre + nj.cim * nj.cim) * ab;
   }
-  *mag = double(m);
-  const double sr = double(ar), si = double(ai);
+  *mag = double(m) * e.escale;
+  const double sr = double(ar) * e.escale, si = double(ai) * e.escale;
   return {A.loop_norm_re * sr - A.loop_norm_im * si, A.loop_norm_re * si + A.loop_norm_im * sr};
 }
 
@@ -466,6 +478,17 @@ __device__ double screened_weight(const KArgs &A, const double *x, uint8_t &flag
   if (CASC && is_nbody(A.P)) return nbody_screened_weight<T>(A, x, flags, skt, sphi, refine);
   Born b;
   born_kinematics<CASC>(A.P, A.K, x, b);
+  if constexpr (sizeof(T) == sizeof(float)) {
+    // excited forward legs: Regge exponents alpha(t) ln s of 10^2 and more, whose FP32
+    // rounding alone is ~1e-5 relative; with a refinement list the event goes straight to
+    // the FP64 loop
+    if (b.exc && refine && A.refine_tol > 0.0) {
+      *refine = true;
+      flags   = GRN_FLAG_KINEMATICS_OK | GRN_FLAG_FIDCUTS_OK | GRN_FLAG_VETOCUTS_OK |
+              GRN_FLAG_AMPLITUDE_OK;
+      return 0.0;
+    }
+  }
   double amp2, mag = 0.0;
   if (CASC && is_vector_pair(A.P)) {
     amp2 = screened_amp2_vv<T>(A, b, skt, sphi, &mag);

@@ -157,12 +157,12 @@ GRN_HD T leg_vertex(const grn_process_params &P, const Consts &K, int exc, int i
 //   sum_k ReggeEta(a0_k,sgn_k) exp(-i pi/2 ap_k t) (s/s0)^(a0_k + ap_k t)
 // (src/MRegge.cc:888-906 with src/MForm.cc:382-396), from ln s.
 template <typename T>
-GRN_HD cx<T> regge_prop(const Consts &K, const grn_regge_params &rp, T lns, T t) {
+GRN_HD cx<T> regge_prop(const Consts &K, const grn_regge_params &rp, T lns, T t, T off = T(0)) {
   cx<T> M{T(0), T(0)};
 #pragma unroll
   for (int k = 0; k < 3; ++k) {
     if (!K.active[k]) continue;
-    const T mag = exp((T(rp.a0[k]) + T(rp.ap[k]) * t) * (lns - T(K.lns0)));
+    const T mag = exp((T(rp.a0[k]) + T(rp.ap[k]) * t) * (lns - T(K.lns0)) - off);
     T sn, cs;
     sincos_pi(-T(0.5) * T(rp.ap[k]) * t, sn, cs);
     const cx<T> ph{cs * mag, sn * mag};
@@ -1109,7 +1109,7 @@ GRN_HD bool veto_cuts(const grn_process_params &P, const Born &b) {
 template <typename T>
 GRN_HD cx<T> regge_me4(const grn_process_params &P, const Consts &K, T t1, T t2, T lns13, T lns14,
                        T lns23, T lns24, T that, T uhat, int exc = 0, T mf1sq = T(0),
-                       T mf2sq = T(0)) {
+                       T mf2sq = T(0), T lnsc = T(0)) {
   const grn_regge_params &rp = P.regge;
   const T M2  = T(K.M2prop);
   const T ffa = meson_ff<T>(rp, that, M2);
@@ -1126,17 +1126,20 @@ GRN_HD cx<T> regge_me4(const grn_process_params &P, const Consts &K, T t1, T t2,
     const T   a1 = T(rp.a0[k]) + T(rp.ap[k]) * t1;
     const T   a2 = T(rp.a0[k]) + T(rp.ap[k]) * t2;
     const T   l0 = T(K.lns0);
-    const T   mt = exp(a1 * (lns13 - l0) + a2 * (lns24 - l0)) * Xt +
-                 exp(a1 * (lns14 - l0) + a2 * (lns23 - l0)) * Xu;
+    const T   mt = exp(a1 * (lns13 - l0) + a2 * (lns24 - l0) - lnsc) * Xt +
+                 exp(a1 * (lns14 - l0) + a2 * (lns23 - l0) - lnsc) * Xu;
     T sn, cs;
     sincos_pi(-T(0.5) * T(rp.ap[k]) * (t1 + t2), sn, cs);
     const cx<T> e0{T(K.eta0_re[k]), T(K.eta0_im[k])};
     const cx<T> e2 = cmul(e0, e0);
     return cscale(cmul(e2, cx<T>{cs, sn}), vtx * mt);
   }
-  const cx<T> At = cscale(cmul(regge_prop<T>(K, rp, lns13, t1), regge_prop<T>(K, rp, lns24, t2)),
+  const T     ho = T(0.5) * lnsc;
+  const cx<T> At = cscale(cmul(regge_prop<T>(K, rp, lns13, t1, ho),
+                               regge_prop<T>(K, rp, lns24, t2, ho)),
                           Xt);
-  const cx<T> Au = cscale(cmul(regge_prop<T>(K, rp, lns14, t1), regge_prop<T>(K, rp, lns23, t2)),
+  const cx<T> Au = cscale(cmul(regge_prop<T>(K, rp, lns14, t1, ho),
+                               regge_prop<T>(K, rp, lns23, t2, ho)),
                           Xu);
   return cscale(cadd(At, Au), vtx);
 }
@@ -1379,6 +1382,11 @@ struct LoopEvent {
   T invL, invL2, L, eps, mp2, m3sq, m4sq;
   T mf1, mf2;               // forward legs' masses^2 (mp2 unless excited)
   int exc;                  // excited forward legs (bit 0: leg 1, bit 1: leg 2)
+  // event scale of the FP32 loop: lnsc is subtracted from the Regge exponents (FP32 exp
+  // covers only |x| < 87), the resonance sums are stored divided by escale, and the loop sum
+  // is multiplied by escale in FP64 (1 and 0 for events inside the FP32 range)
+  T      lnsc;
+  double escale;
   ResSums<T> res;           // PP[RESTENSOR]: resonance sums of the tree-level central mass
 };
 
@@ -1453,7 +1461,7 @@ GRN_HD bool loop_point_amp(const grn_process_params &P, const Consts &K, const L
     if (K.n_res > 0) A = cadd(A, tensor_me3<T>(P, K, kk, e.res));
   } else {
     A = regge_me4<T>(P, K, kk.t1, kk.t2, log(kk.s13), log(kk.s14), log(kk.s23), log(kk.s24),
-                     kk.that, kk.uhat, e.exc, e.mf1, e.mf2);
+                     kk.that, kk.uhat, e.exc, e.mf1, e.mf2, e.lnsc);
   }
   return true;
 }
@@ -1735,8 +1743,12 @@ GRN_HD bool loop_point_amp_fast(const LoopEventF<T> &e, T kx, T ky, T k2, cx<T> 
   return (e.x10 + dx1 < T(1)) && (e.x20 + dx2 < T(1));
 }
 
+// rescale (the FP32 loop): events whose Regge exponent (Regge continuum) or resonance sums
+// (tensor-pomeron resonances alone) fall outside the FP32 range get the event scale of
+// LoopEvent (lnsc, escale); the FP64 loop keeps 0 and 1.
 template <typename T>
-GRN_HD void make_loop_event(const Consts &K, const Born &b, LoopEvent<T> &e) {
+GRN_HD void make_loop_event(const grn_process_params &P, const Consts &K, const Born &b,
+                            LoopEvent<T> &e, bool rescale = false) {
   e.p1x = T(b.p1x); e.p1y = T(b.p1y); e.p2x = T(b.p2x); e.p2y = T(b.p2y);
   e.p3x = T(b.p3x); e.p3y = T(b.p3y); e.p4x = T(b.p4x); e.p4y = T(b.p4y);
   e.p3p = T(b.p3p); e.p3m = T(b.p3m); e.p4p = T(b.p4p); e.p4m = T(b.p4m);
@@ -1748,17 +1760,47 @@ GRN_HD void make_loop_event(const Consts &K, const Born &b, LoopEvent<T> &e) {
   e.L = T(K.L); e.invL2 = T(1.0 / (K.L * K.L)); e.invL = T(1.0 / K.L);
   e.eps = T(K.eps); e.mp2 = T(K.mp2); e.m3sq = T(b.m3sq); e.m4sq = T(b.m4sq);
   e.mf1 = T(b.mf1sq); e.mf2 = T(b.mf2sq); e.exc = b.exc;
+  e.lnsc   = T(0);
+  e.escale = 1.0;
   if (K.n_res > 0) {
     const ResVec<double> v =
         res_vectors<double>(K, b.p3p, b.p3m, b.p3x, b.p3y, b.p4p, b.p4m, b.p4x, b.p4y);
     const ResSums<double> R = resonance_sums(K, b.m2, v);
-    for (int j = 0; j < 7; ++j) e.res.Rs[j] = {T(R.Rs[j].re), T(R.Rs[j].im)};
-    e.res.R0 = {T(R.R0.re), T(R.R0.im)};
-    e.res.R1 = {T(R.R1.re), T(R.R1.im)};
+    double sc = 1.0;
+    if (rescale && P.process == GRN_PROC_TENSOR_RES) {
+      // the resonance factors F^2 / |m^2 - M0^2 + i M0 W|^2 reach exp(-2 (m^2 - M0^2)^2)
+      double rmax = fmax(fabs(R.R0.re) + fabs(R.R0.im), fabs(R.R1.re) + fabs(R.R1.im));
+      for (int j = 0; j < 7; ++j) rmax = fmax(rmax, fabs(R.Rs[j].re) + fabs(R.Rs[j].im));
+      if (rmax > 0.0 && (rmax < 1e-25 || rmax > 1e25)) {
+        const int k = ilogb(rmax);
+        sc       = ldexp(1.0, -k);
+        e.escale = ldexp(1.0, k);
+      }
+    }
+    for (int j = 0; j < 7; ++j) e.res.Rs[j] = {T(R.Rs[j].re * sc), T(R.Rs[j].im * sc)};
+    e.res.R0 = {T(R.R0.re * sc), T(R.R0.im * sc)};
+    e.res.R1 = {T(R.R1.re * sc), T(R.R1.im * sc)};
     e.res.pi = {T(R.pi.pp), T(R.pi.pm), T(R.pi.px), T(R.pi.py), T(R.pi.mm),
                 T(R.pi.mx), T(R.pi.my), T(R.pi.xx), T(R.pi.xy), T(R.pi.yy)};
   } else {
     e.res = ResSums<T>{};
+  }
+  if (rescale && P.process == GRN_PROC_REGGE_CON) {
+    // the tree-level exponent alpha(t1) ln(s1x) + alpha(t2) ln(s2y) of the larger channel and
+    // trajectory; beyond +-40 the loop points (within ~20 of it) would leave the FP32 range
+    const grn_regge_params &rp = P.regge;
+    const double l13 = log(b.s13) - K.lns0, l14 = log(b.s14) - K.lns0;
+    const double l23 = log(b.s23) - K.lns0, l24 = log(b.s24) - K.lns0;
+    double x0 = -1e300;
+    for (int k = 0; k < 3; ++k) {
+      if (!K.active[k]) continue;
+      const double al1 = rp.a0[k] + rp.ap[k] * b.t1, al2 = rp.a0[k] + rp.ap[k] * b.t2;
+      x0 = fmax(x0, fmax(al1 * l13 + al2 * l24, al1 * l14 + al2 * l23));
+    }
+    if (x0 < -40.0 || (x0 > 40.0 && x0 < 700.0)) {
+      e.lnsc   = T(x0);
+      e.escale = exp(double(T(x0)));
+    }
   }
 }
 

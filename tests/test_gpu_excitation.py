@@ -66,8 +66,11 @@ def test_excitation_weights_match_reference(gpu, name):
 
 
 def test_excitation_fp32_loop_vs_fp64(gpu):
-    """Screened single excitation: MIXED (the generic FP32 loop with the per-leg masses and the
-    closed-form light-cone closure, FP64 refinement) against FP64 on 2^14 seeded points."""
+    """Screened single excitation in MIXED precision against FP64 on 2^14 seeded points: with
+    an excited leg the Regge exponents alpha(t) ln s reach 10^2 and more, beyond what the FP32
+    loop resolves to 1e-5, so MIXED hands these events to the FP64 loop; without the
+    refinement the FP32 loop (per-leg masses, closed-form light-cone closure, event scale)
+    still gives their weights to ~1e-4."""
     import graniitti_gb300 as gg
     import philox_np
     g, P, msa = _fixture("nstar1_c_screened_15x12_weights.npz")
@@ -81,6 +84,13 @@ def test_excitation_fp32_loop_vs_fp64(gpu):
     print("screened excitation: MIXED vs FP64 over %d points: max %.2e, median %.2e" %
           (nz.sum(), r.max(), np.median(r)))
     assert nz.sum() > 1000 and r.max() < 1e-5
+    e.set_tuning(fp64_refine=0)
+    w32, _ = e.event_weights(u, prec=gg.MIXED)
+    big = nz & (w64 > 1e-30 * w64.max())  # the weights that the FP32 range holds
+    r32 = np.abs(w32[big] - w64[big]) / w64[big]
+    print("   FP32 loop alone over %d points: median %.2e, p99 %.2e" %
+          (big.sum(), np.median(r32), np.quantile(r32, 0.99)))
+    assert np.median(r32) < 1e-5
     e.close()
 
 
