@@ -438,7 +438,20 @@ struct NBLoopF {
   float      ljk[kNb][kNb];         // ln s_jk - ln s0
   float      rho[kNbTerms];         // e^{x_term - X} at tree level
   float      a0, ap;
+  // process constants in FP32 (converted once per event, not per point): propagator masses^2,
+  // couplings, proton form factor poles, off-shell form factor (form and parameters)
+  float      MA, MB, g2, gN2, fc1, fc2;
+  int        ffform;
+  float      bexp, aore, bore, bpow;
 };
+
+// Off-shell meson form factor (meson_ff) from the FP32 copies of its parameters.
+GRN_HD float meson_ff_f(const NBLoopF &f, float that, float M2) {
+  const float tp = that - M2;
+  if (f.ffform == 0) return expf(-f.bexp * fabsf(tp));
+  if (f.ffform == 1) return expf(-f.bore * sqrtf(fabsf(tp) + f.aore * f.aore) + f.aore * f.bore);
+  return 1.f / (1.f - tp / f.bpow);
+}
 
 // The ordering o = 0..3 of pair {a < b}: (i, j, k, l) = (a, b, c0, c1), (a, b, c1, c0),
 // (b, a, c0, c1), (b, a, c1, c0) with c0 < c1 the two particles left.
@@ -509,6 +522,11 @@ GRN_HD void make_nbody_loop_f(const grn_process_params &P, const Consts &K, cons
   f.p1m = float(p1.m); f.p2p = float(p2.p); f.g1m = float(g1.m); f.g2p = float(g2.p);
   f.t1 = float(t1); f.t2 = float(t2);
   f.a0 = float(a0); f.ap = float(ap);
+  f.MA = float(K.m3sq); f.MB = float(K.M2propB); f.g2 = float(K.g2); f.gN2 = float(K.gN2);
+  f.fc1 = float(P.soft.fc1); f.fc2 = float(P.soft.fc2);
+  f.ffform = P.regge.offshellFF;
+  f.bexp = float(P.regge.b_EXP); f.aore = float(P.regge.a_OREAR);
+  f.bore = float(P.regge.b_OREAR); f.bpow = float(P.regge.b_POW);
   const cx<double> eta{K.eta0_re[q], K.eta0_im[q]};
   double sn, cs;
   sincos_pi(-0.5 * ap * (t1 + t2), sn, cs);
@@ -521,7 +539,8 @@ GRN_HD void make_nbody_loop_f(const grn_process_params &P, const Consts &K, cons
 // the point's FP32 error, with the cancellation among the pairs' phases.
 GRN_HD bool nbody_point_f(const grn_process_params &P, const Consts &K, const NBLoopF &f,
                           float kx, float ky, cx<float> &A, float &mag) {
-  const grn_regge_params &rp = P.regge;
+  (void)P;
+  (void)K;
   const float q1x = f.p1x - kx, q1y = f.p1y - ky, q2x = f.p2x + kx, q2y = f.p2y + ky;
   const float pt1sq = q1x * q1x + q1y * q1y, pt2sq = q2x * q2x + q2y * q2y;
   const float mT1sq = f.mp2 + pt1sq, mT2sq = f.mp2 + pt2sq;
@@ -548,7 +567,7 @@ GRN_HD bool nbody_point_f(const grn_process_params &P, const Consts &K, const NB
   const float dg2p = -(pt2sq + x2 * f.mp2) * r2 * f.invL - f.g2p;
   const float g1p = x1 * f.L, g1m = f.g1m + dg1m, g2m = x2 * f.L, g2p = f.g2p + dg2p;
   const float al1 = f.a0 + f.ap * t1, al2 = f.a0 + f.ap * t2;
-  const float MA = float(K.m3sq), MB = float(K.M2propB);
+  const float MA = f.MA, MB = f.MB;
   float e1[kNb], e2[kNb], f1[kNb], f2[kNb], dd1[kNb];
 #pragma unroll
   for (int a = 0; a < kNb; ++a) {
@@ -564,8 +583,8 @@ GRN_HD bool nbody_point_f(const grn_process_params &P, const Consts &K, const NB
     const float d1 = 0.5f * (g1p * c.m + g1m * c.p) + q1x * c.x + q1y * c.y;
     const float d2 = 0.5f * (g2p * c.m + g2m * c.p) + q2x * c.x + q2y * c.y;
     const float ta = t1 + f.m2[a] - 2.f * d1, td = t2 + f.m2[a] - 2.f * d2;
-    f1[a] = meson_ff<float>(rp, ta, MA) / (ta - MA);
-    f2[a] = meson_ff<float>(rp, td, MB) / (td - MB);
+    f1[a] = meson_ff_f(f, ta, MA) / (ta - MA);
+    f2[a] = meson_ff_f(f, td, MB) / (td - MB);
   }
   cx<float> S{0.f, 0.f};
   float     M = 0.f;
@@ -575,7 +594,7 @@ GRN_HD bool nbody_point_f(const grn_process_params &P, const Consts &K, const NB
     for (int b = a + 1; b < kNb; ++b, ++p) {
       const float dtab = dt1 - 2.f * (dd1[a] + dd1[b]);
       const float tab  = f.tab[p] + dtab;
-      const float fab  = meson_ff<float>(rp, tab, MA) * meson_ff<float>(rp, tab, MB);
+      const float fab  = meson_ff_f(f, tab, MA) * meson_ff_f(f, tab, MB);
       const float apd  = f.ap * dtab;
       float       Sp   = 0.f;
 #pragma unroll
@@ -593,9 +612,8 @@ GRN_HD bool nbody_point_f(const grn_process_params &P, const Consts &K, const NB
     }
   float sn, cs;
   sincos_pi(-0.5f * f.ap * (dt1 + dt2), sn, cs);
-  const float g2c = float(K.g2);
-  const float vtx = float(K.gN2) * proton_ff<float>(float(P.soft.fc1), float(P.soft.fc2), t1) *
-                    proton_ff<float>(float(P.soft.fc1), float(P.soft.fc2), t2) * g2c * g2c;
+  const float vtx = f.gN2 * proton_ff<float>(f.fc1, f.fc2, t1) * proton_ff<float>(f.fc1, f.fc2, t2) *
+                    f.g2 * f.g2;
   A   = cscale(cmul(S, cx<float>{cs, sn}), vtx);
   mag = M * fabsf(vtx);
   return true;
