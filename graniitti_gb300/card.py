@@ -169,15 +169,15 @@ def build_params(card, process=None, tune=None):
     elif any(f in PARTICLES and PARTICLES[f][2] > 1e-6 for f in finals):
         # the reference draws Breit-Wigner masses for them (MProcess::GetOffShellMass)
         raise UnsupportedProcess("unstable central particles need their decays: a > {c d}")
-    four = len(finals) == 4 and channel == "CON" and not any(casc)
+    nbody = len(finals) in (4, 6) and channel == "CON" and not any(casc)
     if not (istate == "PP" and channel in ("CON", "RES", "RES+CON", "CONTENSOR", "RESTENSOR",
                                            "RES+CONTENSOR") and
-            cls in ("C", "F") and (len(finals) == 2 or four)):
+            cls in ("C", "F") and (len(finals) == 2 or nbody)):
         raise UnsupportedProcess(
             "engine implements PP[CON|RES|RES+CON|CONTENSOR|RESTENSOR|RES+CONTENSOR]<C|F> -> "
-            "2-body and PP[CON]<C|F> -> 4-body, got %r" % proc)
-    if four and any(SPIN.get(f, 0) != 0 for f in finals):
-        raise UnsupportedProcess("4-body central states of spin-0 particles")
+            "2-body and PP[CON]<C|F> -> 4- and 6-body, got %r" % proc)
+    if nbody and any(SPIN.get(f, 0) != 0 for f in finals):
+        raise UnsupportedProcess("4- and 6-body central states of spin-0 particles")
     vec = all(SPIN.get(f, 0) == 1 for f in finals)
     if channel == "CONTENSOR" and not (
             all(f in ("pi+", "pi-", "K+", "K-", "pi0") for f in finals) or

@@ -221,20 +221,22 @@ real meson_ff(const grn_regge_params &rp, real that, real M2) {
 // Kinematics state of one event (the part of LORENTZSCALAR the path uses).
 struct Event {
   V4     pb1, pb2;         // beams
-  V4     pf[7];            // pfinal[0..6]: central system, forward 1, forward 2, central a, b
-                           // (c, d for 4-body central states)
+  V4     pf[9];            // pfinal[0..8]: central system, forward 1, forward 2, central a, b
+                           // (c, d, ... for 4- and 6-body central states)
   V4     q;                // intermediate difference momentum (pkt_[0]), <C>
-  V4     kq[3];            // <C> with 4 central particles: the difference momenta pkt_[0..2]
+  V4     kq[5];            // <C> with 4 or 6 central particles: the difference momenta pkt_
   real dw = 0;           // <F>: 2-body phase-space weight dPhi2 (MFactorized.cc:381)
   real m2lo = 0, m2hi = 0;  // <F>: central mass^2 window of this point
-  V4     leaf[4];          // cascades: final-state daughters (central 1: 0, 1; central 2: 2, 3)
+  V4     leaf[6];          // cascades: final-state daughters (central 1: 0, 1; central 2: 2, 3);
+                           // N-body states: the central particles
   real t1 = 0, t2 = 0, that = 0, uhat = 0, m2 = 0, Y = 0, Pt = 0;
-  real ss[7][7] = {};
+  real ss[9][9] = {};
   // forward legs: masses (the beam mass, or the excited N* mass) and the excitation flags
   real mf1 = 0, mf2 = 0;
   bool ex1 = false, ex2 = false;
-  // 4-body central states: (q1 - p_i)^2, (q2 - p_i)^2, (q1 - p_i - p_j)^2 (MProcess.cc:1556-1561)
-  real tt1[7] = {}, tt2[7] = {}, ttxy[7][7] = {};
+  // 4- and 6-body central states: (q1 - p_i)^2, (q2 - p_i)^2, (q1 - p_i - p_j)^2
+  // (MProcess.cc:1556-1561)
+  real tt1[9] = {}, tt2[9] = {}, ttxy[9][9] = {};
 };
 
 struct Setup {
@@ -323,49 +325,55 @@ bool forward_legs(const Setup &S, real pt1, real phi1x, real phi1y, real pt2,
 }
 
 // BNRandomKin + BNBuildKin for Kf = 2 (MContinuum.cc:276-435).
-// Central particles of the <C> class with four central particles: transverse momenta from
-// the linear system of MContinuum::BLinearSystem (MContinuum.cc:438-560),
-//   2 p0 = q0 - w - p2 - p3,  2 p1 = -q0 - w - p2 - p3,  2 p2 = -q1 - w - p0 - p3,
-//   2 p3 = -q2 - w - p0 - p1,  w = p1T + p2T,
-// solved here by Gaussian elimination; (pz, E) from the rapidities and masses.
-void central_four(const V4 *q, const V4 &p1, const V4 &p2, const real *m, const real *y,
-                  V4 *out) {
-  real Mx[4][5], My[4][5];
-  const real coef[4][4] = {{2, 0, 1, 1}, {0, 2, 1, 1}, {1, 0, 2, 1}, {1, 1, 0, 2}};
+// Central particles of the <C> class with N = 4 or 6 central particles: transverse momenta
+// from the linear system of MContinuum::BLinearSystem (MContinuum.cc:438-560),
+//   2 p0 = q0 - w - (p2 + ... + p_{N-1}),  2 p1 = -q0 - w - (p2 + ... + p_{N-1}),
+//   2 p_i = -q_{i-1} - w - (the sum of the p_j with j != i, i - 1),  i >= 2,  w = p1T + p2T,
+// whose matrix the reference tabulates inverted; solved here by Gaussian elimination. (pz, E)
+// from the rapidities and masses.
+void central_n(int N, const V4 *q, const V4 &p1, const V4 &p2, const real *m, const real *y,
+               V4 *out) {
+  real Mx[6][7], My[6][7];
   const real wx = p1.x + p2.x, wy = p1.y + p2.y;
-  const real bx[4] = {q[0].x - wx, -q[0].x - wx, -q[1].x - wx, -q[2].x - wx};
-  const real by[4] = {q[0].y - wy, -q[0].y - wy, -q[1].y - wy, -q[2].y - wy};
-  for (int i = 0; i < 4; ++i) {
-    for (int j = 0; j < 4; ++j) Mx[i][j] = My[i][j] = coef[i][j];
-    Mx[i][4] = bx[i];
-    My[i][4] = by[i];
+  for (int i = 0; i < N; ++i) {
+    for (int j = 0; j < N; ++j) {
+      real c = 1;
+      if (i < 2) c = j == i ? 2 : (j < 2 ? 0 : 1);
+      else c = j == i ? 2 : (j == i - 1 ? 0 : 1);
+      Mx[i][j] = My[i][j] = c;
+    }
+    const V4 &qi = i == 0 ? q[0] : q[i - 1];
+    const real sg = i == 0 ? 1.0 : -1.0;
+    Mx[i][N] = sg * qi.x - wx;
+    My[i][N] = sg * qi.y - wy;
   }
-  real px[4], py[4];
+  real px[6], py[6];
   for (auto *Mp : {&Mx, &My}) {
-    real (&M)[4][5] = *Mp;
-    for (int c = 0; c < 4; ++c) {
+    real (&M)[6][7] = *Mp;
+    for (int c = 0; c < N; ++c) {
       int piv = c;
-      for (int r = c + 1; r < 4; ++r)
+      for (int r = c + 1; r < N; ++r)
         if (std::fabs(M[r][c]) > std::fabs(M[piv][c])) piv = r;
-      for (int k = 0; k < 5; ++k) std::swap(M[c][k], M[piv][k]);
-      for (int r = 0; r < 4; ++r) {
+      for (int k = 0; k <= N; ++k) std::swap(M[c][k], M[piv][k]);
+      for (int r = 0; r < N; ++r) {
         if (r == c) continue;
         const real f = M[r][c] / M[c][c];
-        for (int k = 0; k < 5; ++k) M[r][k] -= f * M[c][k];
+        for (int k = 0; k <= N; ++k) M[r][k] -= f * M[c][k];
       }
     }
     real *dst = Mp == &Mx ? px : py;
-    for (int i = 0; i < 4; ++i) dst[i] = M[i][4] / M[i][i];
+    for (int i = 0; i < N; ++i) dst[i] = M[i][N] / M[i][i];
   }
-  for (int i = 0; i < 4; ++i) {
+  for (int i = 0; i < N; ++i) {
     const real mt = msqrt(m[i] * m[i] + px[i] * px[i] + py[i] * py[i]);
     out[i]          = V4(px[i], py[i], mt * std::sinh(y[i]), mt * std::cosh(y[i]));
   }
 }
 
-// BNRandomKin + BNBuildKin for four central particles (MContinuum.cc:276-435): forward legs
-// u[0..3], kt u[4..6], azimuths u[7..9], rapidities u[10..13].
-bool build_kinematics_c4(const Setup &S, const real *u, Event &ev) {
+// BNRandomKin + BNBuildKin for N = 4 or 6 central particles (MContinuum.cc:276-435): forward
+// legs u[0..3], kt u[4..N+2], azimuths u[N+3..2N+1], rapidities u[2N+2..3N+1].
+bool build_kinematics_cn(const Setup &S, const real *u, Event &ev) {
+  const int N = S.p.n_central;
   const grn_gencuts &g = S.p.gcuts;
   const real lo  = std::log(g.fpt_min + ZERO_EPS);
   const real hi  = std::log(g.fpt_max);
@@ -373,20 +381,21 @@ bool build_kinematics_c4(const Setup &S, const real *u, Event &ev) {
   const real pt2 = std::exp(lo + (hi - lo) * u[1]);
   const real phi1 = 2.0 * PI * u[2];
   const real phi2 = 2.0 * PI * u[3];
-  for (int i = 0; i < 3; ++i) {
+  for (int i = 0; i < N - 1; ++i) {
     const real kt = g.kt_min + (g.kt_max - g.kt_min) * u[4 + i];
-    const real ph = 2.0 * PI * u[7 + i];
+    const real ph = 2.0 * PI * u[N + 3 + i];
     ev.kq[i] = V4(kt * std::cos(ph), kt * std::sin(ph), 0, 0);
   }
-  real y[4];
-  for (int i = 0; i < 4; ++i) y[i] = g.rap_min + (g.rap_max - g.rap_min) * u[10 + i];
+  real y[6];
+  for (int i = 0; i < N; ++i) y[i] = g.rap_min + (g.rap_max - g.rap_min) * u[2 * N + 2 + i];
   V4 p1(pt1 * std::cos(phi1), pt1 * std::sin(phi1), 0, 0);
   V4 p2(pt2 * std::cos(phi2), pt2 * std::sin(phi2), 0, 0);
-  V4 c[4];
-  real mc[4];
-  for (int i = 0; i < 4; ++i) mc[i] = S.p.m_central[i];
-  central_four(ev.kq, p1, p2, mc, y, c);
-  const V4 sumP = c[0] + c[1] + c[2] + c[3];
+  V4 c[6];
+  real mc[6];
+  for (int i = 0; i < N; ++i) mc[i] = S.p.m_central[i];
+  central_n(N, ev.kq, p1, p2, mc, y, c);
+  V4 sumP = c[0];
+  for (int i = 1; i < N; ++i) sumP = sumP + c[i];
   if (sumP.e > S.sqrt_s) return false;
   forward_masses(S, 0, 0, 0, ev);
   if (!forward_legs(S, pt1, p1.x, p1.y, pt2, p2.x, p2.y, sumP, p1, p2, ev.mf1, ev.mf2))
@@ -395,7 +404,7 @@ bool build_kinematics_c4(const Setup &S, const real *u, Event &ev) {
   ev.pf[1] = p1;
   ev.pf[2] = p2;
   real msum = 0;
-  for (int i = 0; i < 4; ++i) {
+  for (int i = 0; i < N; ++i) {
     ev.pf[3 + i] = c[i];
     ev.leaf[i]   = c[i];
     msum += c[i].m();
@@ -409,7 +418,7 @@ void cascade_masses(const grn_process_params &p, const real *u, real &m3, real &
 void cascade_decays(const Setup &S, const real *u, real m3, real m4, Event &ev);
 
 bool build_kinematics(const Setup &S, const real *u, Event &ev) {
-  if (S.p.n_central == 4) return build_kinematics_c4(S, u, ev);
+  if (S.p.n_central >= 4) return build_kinematics_cn(S, u, ev);
   const grn_gencuts &g = S.p.gcuts;
   const real lo  = std::log(g.fpt_min + ZERO_EPS);
   const real hi  = std::log(g.fpt_max);
@@ -475,7 +484,7 @@ int decay_coord(const grn_process_params &p) { return offshell_widths(p) > 0 ? 1
 
 // Hypercube dimension of a process.
 int point_dim(const grn_process_params &p) {
-  if (p.n_central == 4) return 14;
+  if (p.n_central >= 4) return 3 * p.n_central + 2;  // 14 or 20
   if (p.excitation) return 10;
   return p.n_decay == 2 ? decay_coord(p) + 4 : 8;
 }
@@ -562,28 +571,33 @@ V4 boost_from_rest(const V4 &b, real M0, const V4 &p) {
 }
 
 // Flat N-body phase space, weighted (NBodySetup with unweight = false + NBodyPhaseSpace,
-// include/Graniitti/MKinematics.h:523-691) for N = 4, the reference's generator draws taken
-// from r: r[0], r[1] the intermediate masses (sorted), then (cos theta, phi) pairs for
-// particles 3, 2, 1. Returns the weight prod(p*) x volume, or -1.
-real n_body(const V4 &mother, real M0, const real *m, const real *r, V4 *p) {
-  const int N = 4;
-  real sum[N];
+// include/Graniitti/MKinematics.h:523-691) for N = 4 or 6, the reference's generator draws
+// taken from r: r[0..N-3] the intermediate masses (sorted ascending), then (cos theta, phi)
+// pairs for particles N-1, ..., 1. Returns the weight prod(p*) x volume, or -1.
+real n_body(int N, const V4 &mother, real M0, const real *m, const real *r, V4 *p) {
+  real sum[6];
   for (int i = 0; i < N; ++i) sum[i] = (i ? sum[i - 1] : 0.0) + m[i];
   const real D = M0 - sum[N - 1];
   if (!(D > 0)) return -1.0;
-  real rv[2] = {r[0], r[1]};
-  std::sort(rv, rv + 2);
-  const real Meff[N] = {m[0], sum[1] + rv[0] * D, sum[2] + rv[1] * D, M0};
-  real pn[N] = {0, 0, 0, 0};
+  real rv[4];
+  for (int i = 0; i < N - 2; ++i) rv[i] = r[i];
+  std::sort(rv, rv + N - 2);
+  real Meff[6];
+  Meff[0]     = m[0];
+  Meff[N - 1] = M0;
+  for (int i = 1; i < N - 1; ++i) Meff[i] = sum[i] + rv[i - 1] * D;
+  real pn[6] = {0, 0, 0, 0, 0, 0};
   real w = 1.0;
   for (int i = 1; i < N; ++i) {
     const real x = Meff[i], y = Meff[i - 1], z = m[i];
     pn[i] = msqrt((x - y - z) * (x + y + z) * (x + y - z) * (x - y + z)) / (2.0 * x);
     w *= pn[i];
   }
-  const real volume = 1.0 / (2.0 * std::pow(2.0 * PI, 2 * N - 3)) * std::pow(D, N - 2) / 2.0 / M0;
+  real fact = 1.0;
+  for (int i = 2; i <= N - 2; ++i) fact *= i;
+  const real volume = 1.0 / (2.0 * std::pow(2.0 * PI, 2 * N - 3)) * std::pow(D, N - 2) / fact / M0;
   V4 k = mother;
-  for (int i = N - 1, j = 2; i >= 1; --i, j += 2) {
+  for (int i = N - 1, j = N - 2; i >= 1; --i, j += 2) {
     const real ct = 2.0 * r[j] - 1.0;
     const real st = msqrt(1.0 - ct * ct);
     const real ph = 2.0 * PI * r[j + 1];
@@ -608,7 +622,10 @@ bool build_kinematics_F(const Setup &S, const real *u, Event &ev) {
   const real phi2 = 2.0 * PI * u[3];
   const real yX   = g.Y_min + (g.Y_max - g.Y_min) * u[4];
   real m3 = S.p.m_central[0], m4 = S.p.m_central[1];
-  if (S.p.n_central == 4) m4 = S.p.m_central[1] + S.p.m_central[2] + S.p.m_central[3];
+  if (S.p.n_central >= 4) {
+    m4 = 0;
+    for (int i = 1; i < S.p.n_central; ++i) m4 += S.p.m_central[i];
+  }
   if (S.p.n_decay == 2) cascade_masses(S.p, u, m3, m4);  // off-shell central masses
   const real Mmin = std::max<real>(m3 + m4 + 1e-4, g.M_min);
   const real Mmax = std::min<real>(S.sqrt_s - (S.pb1.m() + S.pb2.m()), g.M_max);
@@ -631,12 +648,13 @@ bool build_kinematics_F(const Setup &S, const real *u, Event &ev) {
   ev.pf[1] = p1;
   ev.pf[2] = p2;
   if (!check_emc((S.pb1 + S.pb2) - (p1 + p2 + pX))) return false;
-  if (S.p.n_central == 4) {
-    real mc[4];
-    for (int i = 0; i < 4; ++i) mc[i] = S.p.m_central[i];
-    ev.dw = n_body(pX, msqrt(m2X), mc, u + 6, ev.pf + 3);
+  if (S.p.n_central >= 4) {
+    const int N = S.p.n_central;
+    real mc[6];
+    for (int i = 0; i < N; ++i) mc[i] = S.p.m_central[i];
+    ev.dw = n_body(N, pX, msqrt(m2X), mc, u + 6, ev.pf + 3);
     if (!(ev.dw >= 0)) return false;
-    for (int k = 0; k < 4; ++k) ev.leaf[k] = ev.pf[3 + k];
+    for (int k = 0; k < N; ++k) ev.leaf[k] = ev.pf[3 + k];
     return lorentz_scalars(S, ev);
   }
   // decay angles: the draws after the forward masses (u[6], u[7]; u[8], u[9] when excited)
@@ -673,17 +691,19 @@ bool loop_kinematics(const Setup &S, const Event &born, real p1x, real p1y, real
     if (!check_emc((S.pb1 + S.pb2) - (p1 + p2 + pX))) return false;
     return lorentz_scalars(S, ev);
   }
-  if (S.p.n_central == 4) {
+  if (S.p.n_central >= 4) {
     // MContinuum::LoopKinematics: central transverse momenta re-solved with the tree-level
     // difference momenta, rapidities and masses
-    real m4[4], y4[4];
-    for (int i = 0; i < 4; ++i) {
+    const int N = S.p.n_central;
+    real m4[6], y4[6];
+    for (int i = 0; i < N; ++i) {
       m4[i] = born.pf[3 + i].m();
       y4[i] = born.pf[3 + i].rap();
     }
-    V4 c[4];
-    central_four(born.kq, p1T, p2T, m4, y4, c);
-    const V4 sumP = c[0] + c[1] + c[2] + c[3];
+    V4 c[6];
+    central_n(N, born.kq, p1T, p2T, m4, y4, c);
+    V4 sumP = c[0];
+    for (int i = 1; i < N; ++i) sumP = sumP + c[i];
     V4 p1, p2;
     if (!forward_legs(S, p1T.pt(), p1x, p1y, p2T.pt(), p2x, p2y, sumP, p1, p2, born.mf1,
                       born.mf2))
@@ -692,7 +712,7 @@ bool loop_kinematics(const Setup &S, const Event &born, real p1x, real p1y, real
     ev.pf[0] = sumP;
     ev.pf[1] = p1;
     ev.pf[2] = p2;
-    for (int i = 0; i < 4; ++i) ev.pf[3 + i] = c[i];
+    for (int i = 0; i < N; ++i) ev.pf[3 + i] = c[i];
     if (!check_emc((S.pb1 + S.pb2) - (p1 + p2 + sumP))) return false;
     return lorentz_scalars(S, ev);
   }
@@ -765,6 +785,36 @@ cplx regge_me6(const Setup &S, const Event &ev) {
          meson_ff(rp, tbc, MB) * g * (1.0 / (tcd - MB)) * meson_ff(rp, tcd, MB) * g *
          regge_prop(rp, ev.ss[2][d], ev.t2) * FFB;
   } while (std::next_permutation(perm, perm + 4));
+  return A;
+}
+
+// Regge continuum amplitude for a 6-body central state (MRegge::ME8, src/MRegge.cc:560-627):
+// all 720 orderings (a, b, c, d, e, f) of the central particles along the ladder
+// (GetAmpPerm(6, 1)), with the reference's invariants and form-factor arguments as it writes
+// them: t_ab = (q1 - p_a)^2, t_bc = (q1 - p_a - p_b)^2, t_cd = (q1 - p_b - p_c)^2,
+// t_de = (q1 - p_c - p_d)^2, t_ef = (q2 - p_f)^2; off-shell propagator masses of the first,
+// third and fifth particle of the decay list.
+cplx regge_me8(const Setup &S, const Event &ev) {
+  const grn_regge_params &rp = S.p.regge;
+  const real MA = sq(S.p.m_central[0]), MB = sq(S.p.m_central[2]), MC = sq(S.p.m_central[4]);
+  const real gin = std::sqrt(S.p.soft.g3P * S.p.soft.gN_P);
+  const real FFA = ev.ex1 ? gin * proton_ff_inel(ev.t1, ev.pf[1].m2())
+                          : S.p.soft.gN_P * proton_ff(S.p.soft, ev.t1);
+  const real FFB = ev.ex2 ? gin * proton_ff_inel(ev.t2, ev.pf[2].m2())
+                          : S.p.soft.gN_P * proton_ff(S.p.soft, ev.t2);
+  const real g   = rp.c[0] / S.p.soft.gN_P;
+  int perm[6] = {3, 4, 5, 6, 7, 8};
+  cplx A(0, 0);
+  do {
+    const int a = perm[0], b = perm[1], c = perm[2], d = perm[3], e = perm[4], f = perm[5];
+    const real tab = ev.tt1[a], tbc = ev.ttxy[a][b], tcd = ev.ttxy[b][c];
+    const real tde = ev.ttxy[c][d], tef = ev.tt2[f];
+    A += regge_prop(rp, ev.ss[1][a], ev.t1) * FFA * meson_ff(rp, tab, MA) * g *
+         (1.0 / (tab - MA)) * meson_ff(rp, tbc, MA) * g * regge_prop(rp, ev.ss[b][c], tbc) *
+         meson_ff(rp, tbc, MB) * g * (1.0 / (tcd - MB)) * meson_ff(rp, tde, MB) * g *
+         regge_prop(rp, ev.ss[d][e], tde) * meson_ff(rp, tde, MC) * g * (1.0 / (tef - MC)) *
+         meson_ff(rp, tef, MC) * g * regge_prop(rp, ev.ss[2][f], ev.t2) * FFB;
+  } while (std::next_permutation(perm, perm + 6));
   return A;
 }
 
@@ -1560,6 +1610,7 @@ void observables(const Setup &S, const Event &ev, real *o) {
 // so the sum of one configuration carries |M|^2.
 cplx bare_amp(const Setup &S, const Event &ev) {
   if (S.p.n_central == 4) return regge_me6(S, ev);
+  if (S.p.n_central == 6) return regge_me8(S, ev);
   if (S.p.process == GRN_PROC_TENSOR_RES) return tensor_me3(S, ev);
   if (S.p.process == GRN_PROC_TENSOR_RESCON)
     return tensor_me4_2xs(S, ev) + (S.p.n_res > 0 ? tensor_me3(S, ev) : cplx(0.0));
@@ -1609,7 +1660,10 @@ real ps_factor(const Setup &S, const Event &ev) {
   }
   const int Kf = S.p.n_central, Nf = Kf + 2;
   real prod = ev.q.pt();
-  if (Kf == 4) prod = ev.kq[0].pt() * ev.kq[1].pt() * ev.kq[2].pt();
+  if (Kf >= 4) {
+    prod = 1.0;
+    for (int i = 0; i < Kf - 1; ++i) prod *= ev.kq[i].pt();
+  }
   const real psw = (1.0 / std::pow(2.0, 2 * (Nf - 2))) * (1.0 / std::pow(2.0 * PI, 3 * Nf - 4)) *
                      (ev.pf[1].pt() / (2.0 * ev.pf[1].e)) * (ev.pf[2].pt() / (2.0 * ev.pf[2].e)) *
                      J * prod;
@@ -1637,7 +1691,7 @@ bool fiducial(const Setup &S, const Event &ev) {
   bool ok = true;
   // final-state particles: the central pair, or the leaves of its decays (FindDecayCuts)
   const bool casc = S.p.n_decay == 2;
-  const int  np   = (casc || S.p.n_central == 4) ? 4 : 2;
+  const int  np   = casc ? 4 : S.p.n_central;
   for (int k = 0; k < np; ++k) {
     const V4 &p = casc ? ev.leaf[k] : ev.pf[3 + k];
     const real pt = p.pt(), et = p.mt(), eta = p.eta(), rap = p.rap();
@@ -1653,8 +1707,8 @@ bool fiducial(const Setup &S, const Event &ev) {
 // protons have no fragments to test).
 bool veto_cuts(const Setup &S, const Event &ev) {
   if (!S.p.veto_active) return true;
-  const bool leaves = S.p.n_decay == 2 || S.p.n_central == 4;
-  const int  np     = leaves ? 4 : 2;
+  const bool leaves = S.p.n_decay == 2 || S.p.n_central >= 4;
+  const int  np     = S.p.n_decay == 2 ? 4 : S.p.n_central;
   for (int k = 0; k < np; ++k) {
     const V4 &p = leaves ? ev.leaf[k] : ev.pf[3 + k];
     const real pt = p.pt(), eta = p.eta();
@@ -1751,9 +1805,10 @@ extern "C" {
 int orc_weights(const grn_process_params *p, const double *u, int64_t n, int32_t dim, double *w,
                 uint8_t *flags, double *rec, const double *msa, int32_t n_kt2, int32_t nthreads) {
   const int32_t want = p ? orc::point_dim(*p) : 8;
-  if (!p || !u || !w || dim != want || (p->n_central != 2 && p->n_central != 4))
+  if (!p || !u || !w || dim != want ||
+      (p->n_central != 2 && p->n_central != 4 && p->n_central != 6))
     return GRN_ERR_INVALID;
-  if (p->n_central == 4 && p->process != GRN_PROC_REGGE_CON) return GRN_ERR_INVALID;
+  if (p->n_central >= 4 && p->process != GRN_PROC_REGGE_CON) return GRN_ERR_INVALID;
   if (p->screening && (!msa || n_kt2 < 2)) return GRN_ERR_STATE;
   const orc::Setup S = orc::make_setup(p, msa, n_kt2);
   orc::parallel_for(n, nthreads, [&](int64_t a, int64_t b) {
@@ -1761,7 +1816,7 @@ int orc_weights(const grn_process_params *p, const double *u, int64_t n, int32_t
     for (int64_t i = a; i < b; ++i) {
       uint8_t f = 0;
       ev        = orc::Event();
-      orc::real ur[16];
+      orc::real ur[24];
       for (int d = 0; d < dim; ++d) ur[d] = u[i * dim + d];
       w[i]      = double(orc::event_weight(S, ur, f, ev));
       if (flags) flags[i] = f;
@@ -1788,7 +1843,8 @@ int orc_weights(const grn_process_params *p, const double *u, int64_t n, int32_t
 int orc_observables(const grn_process_params *p, const double *u, int64_t n, int32_t dim,
                     double *obs, uint8_t *ok, int32_t nthreads) {
   const int32_t want = p ? orc::point_dim(*p) : 8;
-  if (!p || !u || !obs || dim != want || (p->n_central != 2 && p->n_central != 4))
+  if (!p || !u || !obs || dim != want ||
+      (p->n_central != 2 && p->n_central != 4 && p->n_central != 6))
     return GRN_ERR_INVALID;
   grn_process_params q = *p;
   q.screening = 0;
@@ -1797,7 +1853,7 @@ int orc_observables(const grn_process_params *p, const double *u, int64_t n, int
     for (int64_t i = a; i < b; ++i) {
       uint8_t    f  = 0;
       orc::Event ev = orc::Event();
-      orc::real ur[16], ob[20];
+      orc::real ur[24], ob[20];
       for (int d = 0; d < dim; ++d) ur[d] = u[i * dim + d];
       orc::event_weight(S, ur, f, ev);
       ok[i] = (f & GRN_FLAG_KINEMATICS_OK) ? 1 : 0;

@@ -10,7 +10,8 @@ reference does not. Steps:
 
 Usage: python tests/golden/make_golden.py [--ref <reference source tree>]
                                           [--only resonances|cascades|rescon|regge_res|
-                                                  nbody|nbody_c|veto|ccascades|excitation|ld]
+                                                  nbody|nbody_c|nbody6|veto|ccascades|
+                                                  excitation|ld]
 """
 import argparse
 import json
@@ -191,6 +192,33 @@ def nbody_fixtures():
                    "flat_sigma_barn": flat[0], "flat_sigma_err_barn": flat[1],
                    "vegas_sigma_barn": vegas[0], "vegas_sigma_err_barn": vegas[1]}, fh, indent=1)
     print("f4: flat", flat, "vegas", vegas)
+
+
+def nbody6_fixtures():
+    """Regge continuum of six central particles (PP[CON] -> pi+ pi- pi+ pi- pi+ pi-,
+    MRegge::ME8) in both classes, tree level and screened. Factorized class: the generator
+    draws inside EventWeight, in order, are six inert off-shell masses (0.5), the four
+    intermediate masses of NBodySetup u[6..9], its acceptance draw (inert, 0.5) and
+    (cos theta, phi) of five decays u[10..19]; continuum class: the six inert masses."""
+    proc_f = "PP[CON]<F> -> pi+ pi- pi+ pi- pi+ pi-"
+    proc_c = "PP[CON]<C> -> pi+ pi- pi+ pi- pi+ pi-"
+    rep_f = ["--replay", "h,h,h,h,h,h,6,7,8,9,h," + ",".join(str(k) for k in range(10, 20))]
+    rep_c = ["--replay", "h,h,h,h,h,h"]
+    scr = ["--nbt", "1024", "--nkt2", "10000"]
+    u = philox_np.uniforms(161, 1024, 20)
+    r = run_weights(CARD, u, rep_f, proc=proc_f, dim=6, leaves=6)
+    save("f6_tree_weights.npz", seed=161, u=u, card=os.path.basename(CARD), proc=proc_f, **r)
+    u = philox_np.uniforms(162, 1024, 20)
+    r = run_weights(CARD, u, rep_c, proc=proc_c, leaves=6)
+    save("c6_tree_weights.npz", seed=162, u=u, card=os.path.basename(CARD), proc=proc_c, **r)
+    u = philox_np.uniforms(163, 384, 20)
+    r = run_weights(CARD_SCR, u, rep_f + scr, proc=proc_f, dim=6, leaves=6)
+    save("f6_screened_weights.npz", seed=163, u=u, card=os.path.basename(CARD_SCR), proc=proc_f,
+         n_bt=1024, n_kt2=10000, **r)
+    u = philox_np.uniforms(164, 64, 20)
+    r = run_weights(CARD_SCR, u, rep_c + scr, proc=proc_c, leaves=6)
+    save("c6_screened_weights.npz", seed=164, u=u, card=os.path.basename(CARD_SCR), proc=proc_c,
+         n_bt=1024, n_kt2=10000, **r)
 
 
 def veto_fixtures():
@@ -396,8 +424,8 @@ def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--ref", default=REF_DEFAULT)
     ap.add_argument("--only", choices=["all", "resonances", "cascades", "rescon", "regge_res",
-                                       "nbody", "nbody_c", "veto", "ccascades", "ld",
-                                       "excitation"],
+                                       "nbody", "nbody_c", "nbody6", "veto", "ccascades",
+                                       "ld", "excitation"],
                     default="all")
     a = ap.parse_args()
     if a.only == "ld":  # needs only the oracle
@@ -405,6 +433,10 @@ def main():
         return
     subprocess.check_call(["make", "-s", "-C", os.path.join(REPO, "oracle", "refbuild"), "-j8",
                            "REF=" + a.ref])
+    if a.only in ("all", "nbody6"):
+        nbody6_fixtures()
+    if a.only == "nbody6":
+        return
     if a.only in ("all", "excitation"):
         excitation_fixtures()
     if a.only == "excitation":

@@ -133,11 +133,23 @@ def test_regge_resonance_params(lib_built):
 
 
 @pytest.mark.parametrize("proc", ["PP[RESHEL]<C> -> pi+ pi-", "PP[CON]<Q> -> pi+ pi-",
-                                  "PP[CON]<C> -> pi+ pi- pi+ pi- pi+ pi-", "yy[CON]<C> -> mu+ mu-",
-                                  "PP[CONTENSOR]<F> -> pi+ pi- pi+ pi-"])
+                                  "PP[CON]<C> -> pi+ pi- pi+ pi- pi+", "yy[CON]<C> -> mu+ mu-",
+                                  "PP[CONTENSOR]<F> -> pi+ pi- pi+ pi-",
+                                  "PP[CON]<C> -> pi+ pi- pi+ pi- pi+ pi- pi+ pi-"])
 def test_unsupported_processes_are_rejected(proc):
     with pytest.raises(card.UnsupportedProcess):
         card.build_params(card.read_card(CARD), proc)
+
+
+def test_six_body_continuum():
+    """PP[CON]<C|F> -> 6 bodies (MRegge::ME8): 20 hypercube dimensions, the continuum class's
+    default kt_max = 10 GeV / 6 (MContinuum.cc:72-77)."""
+    for cls in ("C", "F"):
+        P = card.build_params(card.read_card(CARD), "PP[CON]<%s> -> pi+ pi- pi+ pi- pi+ pi-" % cls)
+        assert P.n_central == 6 and P.process == card._abi.GRN_PROC_REGGE_CON
+        assert P.s_factor == 36.0  # 3! 3!
+        if cls == "C":
+            assert abs(P.gcuts.kt_max - 10.0 / 6) < 1e-15
 
 
 def test_vegas_params():

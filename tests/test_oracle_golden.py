@@ -215,20 +215,23 @@ def test_vector_pair_cascade_weights(name):
 
 @pytest.mark.parametrize("name", ["f4_tree_weights.npz", "f4_kk_tree_weights.npz",
                                   "f4_screened_weights.npz", "c4_tree_weights.npz",
-                                  "c4_screened_weights.npz"])
-def test_four_body_continuum_weights(name):
-    """PP[CON]<F|C> -> 4 bodies (MRegge::ME6 with the weighted N-body phase space, or the
-    continuum class's 14-dimensional phase space)."""
+                                  "c4_screened_weights.npz", "f6_tree_weights.npz",
+                                  "c6_tree_weights.npz", "f6_screened_weights.npz",
+                                  "c6_screened_weights.npz"])
+def test_n_body_continuum_weights(name):
+    """PP[CON]<F|C> -> 4 or 6 bodies (MRegge::ME6 / ME8 with the weighted N-body phase space,
+    or the continuum class's 14- or 20-dimensional phase space)."""
     g = _load(name)
     P = _params_res(g)
-    assert P.n_central == 4
+    assert P.n_central == (6 if name[1] == "6" else 4)
     msa = _load("eikonal_nbt1024_nkt10000.npz")["msa"] if P.screening else None
     w, fl, rec = orc.weights(P, g["u"], msa=msa, nthreads=4, with_rec=True)
     _check_weights(w, fl, g, tol=W_TOL)
     kin = g["kin"] == 1
-    cen = rec[:, 19:35].reshape(-1, 4, 4)
-    scale = np.abs(g["leaves"]).max(axis=2, keepdims=True)
-    assert (np.abs(cen - g["leaves"])[kin] / scale[kin]).max() < 1e-12
+    cen = rec[:, 19:35].reshape(-1, 4, 4)  # the first four central particles
+    ref = g["leaves"][:, :4]
+    scale = np.abs(ref).max(axis=2, keepdims=True)
+    assert (np.abs(cen - ref)[kin] / scale[kin]).max() < 1e-12
 
 
 def _np_rest(X, p):
