@@ -282,16 +282,17 @@ grn_status derive_consts(const grn_process_params &P, grn::Consts &K) {
     }
     K.n_res = P.n_res;
   }
-  const bool nbody = P.n_central == 4;
+  const bool nbody = P.n_central == 4 || P.n_central == 6;
   if (P.n_central != 2 && !nbody)
-    return fail(GRN_ERR_UNSUPPORTED, "central states of 2 or 4 particles");
+    return fail(GRN_ERR_UNSUPPORTED, "central states of 2, 4 or 6 particles");
   if (nbody) {
-    // PP[CON]<F> -> a b c d (MRegge::ME6 with the N-body phase space)
+    // PP[CON]<F|C> -> a b c d (MRegge::ME6) or a b c d e f (MRegge::ME8)
     if (P.process != GRN_PROC_REGGE_CON)
-      return fail(GRN_ERR_UNSUPPORTED, "4-body central states: PP[CON]<F|C> (Regge ME6)");
-    if (P.n_decay != 0 || P.central_spin != 0)
-      return fail(GRN_ERR_UNSUPPORTED, "4-body central states of stable spin-0 particles");
-    for (int k = 0; k < 4; ++k)
+      return fail(GRN_ERR_UNSUPPORTED,
+                  "4- and 6-body central states: PP[CON]<F|C> (Regge ME6, ME8)");
+    if (P.n_decay != 0 || P.central_spin != 0 || P.excitation != 0)
+      return fail(GRN_ERR_UNSUPPORTED, "N-body central states of stable spin-0 particles");
+    for (int k = 0; k < P.n_central; ++k)
       if (!(P.m_central[k] >= 0)) return fail(GRN_ERR_INVALID, "central masses");
   }
   if (P.n_decay != 0 && P.n_decay != 2)
@@ -372,20 +373,23 @@ grn_status derive_consts(const grn_process_params &P, grn::Consts &K) {
   K.w_const = (1.0 / P.s_factor) * (1.0 / std::pow(2.0, 2 * (Nf - 2))) *
               (1.0 / std::pow(2.0 * kPi, 3 * Nf - 4)) * vol * kGeV2barn / (2.0 * K.s);
   if (nbody && P.phase_space == GRN_PS_CONTINUUM) {
-    // BNPhaseSpaceWeight x BNIntegralVolume for Nf = 6 (MContinuum.cc:619-656): kt, phi and
-    // rapidity volumes of 3 difference momenta and 4 central particles
-    const int    N6  = 6;
-    const double v6 = std::pow(P.gcuts.kt_max - P.gcuts.kt_min, 3) * std::pow(2.0 * kPi, 3) *
-                      std::pow(P.gcuts.rap_max - P.gcuts.rap_min, 4) * std::pow(2.0 * kPi, 2) *
-                      fwd_log * fwd_log;
-    K.w_const = (1.0 / P.s_factor) * (1.0 / std::pow(2.0, 2 * (N6 - 2))) *
-                (1.0 / std::pow(2.0 * kPi, 3 * N6 - 4)) * v6 * kGeV2barn / (2.0 * K.s);
+    // BNPhaseSpaceWeight x BNIntegralVolume for Nf = Kf + 2 (MContinuum.cc:619-656): kt, phi
+    // and rapidity volumes of Kf - 1 difference momenta and Kf central particles
+    const int    Kf = P.n_central, Nn = Kf + 2;
+    const double vn = std::pow(P.gcuts.kt_max - P.gcuts.kt_min, Kf - 1) *
+                      std::pow(2.0 * kPi, Kf - 1) * std::pow(P.gcuts.rap_max - P.gcuts.rap_min, Kf) *
+                      std::pow(2.0 * kPi, 2) * fwd_log * fwd_log;
+    K.w_const = (1.0 / P.s_factor) * (1.0 / std::pow(2.0, 2 * (Nn - 2))) *
+                (1.0 / std::pow(2.0 * kPi, 3 * Nn - 4)) * vn * kGeV2barn / (2.0 * K.s);
   }
   if (P.phase_space == GRN_PS_FACTORIZED) {
     // mass window (B51RandomKin, MFactorized.cc:263-291): M_MIN = sum of daughter masses
     // + 1e-4 GeV, M_MAX = sqrt(s) - 2 m_beam, both clipped to the <F> generation cuts.
     double msum = K.m3 + K.m4;
-    if (nbody) msum = P.m_central[0] + P.m_central[1] + P.m_central[2] + P.m_central[3];
+    if (nbody) {  // summed in the decay-list order, as the reference does
+      msum = 0.0;
+      for (int k = 0; k < P.n_central; ++k) msum += P.m_central[k];
+    }
     const double Mmin = std::max(msum + 1e-4, P.gcuts.M_min);
     const double Mmax = std::min(P.sqrt_s - 2.0 * P.m_beam, P.gcuts.M_max);
     if (!(Mmin < Mmax)) return fail(GRN_ERR_INVALID, "<F> mass window is empty (GENCUTS <F> M)");
@@ -615,7 +619,8 @@ grn_status grn_create(const grn_process_params *p, int32_t device, grn_engine **
   e->K          = K;
   // hypercube dimension: 8 for a 2-body point; cascades add the decay angles (4) and, unless
   // OFFSHELL = 0, the two masses (2); 4-body central states have 14
-  e->dim = p->n_central == 4 ? 14 : (p->n_decay == 2 ? K.dec0 + 4 : (p->excitation ? 10 : 8));
+  e->dim = p->n_central >= 4 ? 3 * p->n_central + 2
+                            : (p->n_decay == 2 ? K.dec0 + 4 : (p->excitation ? 10 : 8));
   cudaError_t ce = cudaStreamCreateWithFlags(&e->stream, cudaStreamNonBlocking);
   if (ce == cudaSuccess) ce = cudaMallocHost(&e->h_sc, grn::VS_COUNT * sizeof(double));
   if (ce == cudaSuccess) ce = cudaEventCreate(&e->ev0);
@@ -823,18 +828,19 @@ grn_status grn_event_daughters(grn_engine *e, const double *u, int64_t n, int32_
                                double *pd_out) {
   if (!e || !u || !pd_out || n < 0) return fail(GRN_ERR_INVALID, "null argument");
   if (dim != e->dim) return fail(GRN_ERR_INVALID, "dim must equal grn_dim()");
-  if (e->P.n_decay != 2 && e->P.n_central != 4)
-    return fail(GRN_ERR_STATE, "the process has no decay cascades or 4-body central states");
+  if (e->P.n_decay != 2 && e->P.n_central < 4)
+    return fail(GRN_ERR_STATE, "the process has no decay cascades or N-body central states");
   if (n == 0) return GRN_OK;
+  const int64_t per = e->P.n_central == 6 ? 24 : 16;  // doubles per point
   GRN_CUDA(cudaSetDevice(e->device));
   GRN_CUDA(e->d_u.ensure(n * dim * sizeof(double)));
-  GRN_CUDA(e->d_aux.ensure(n * 16 * sizeof(double)));
+  GRN_CUDA(e->d_aux.ensure(n * per * sizeof(double)));
   GRN_CUDA(cudaMemcpyAsync(e->d_u.p, u, n * dim * sizeof(double),
                            is_device_ptr(u) ? cudaMemcpyDeviceToDevice : cudaMemcpyHostToDevice,
                            e->stream));
   GRN_CUDA(grn::launch_event_daughters(e->args(), e->d_u.as<double>(), n, dim,
                                        e->d_aux.as<double>(), e->stream));
-  GRN_CUDA(cudaMemcpyAsync(pd_out, e->d_aux.p, n * 16 * sizeof(double), cudaMemcpyDefault,
+  GRN_CUDA(cudaMemcpyAsync(pd_out, e->d_aux.p, n * per * sizeof(double), cudaMemcpyDefault,
                            e->stream));
   GRN_CUDA(cudaStreamSynchronize(e->stream));
   return GRN_OK;
@@ -842,7 +848,8 @@ grn_status grn_event_daughters(grn_engine *e, const double *u, int64_t n, int32_
 
 grn_status grn_uniforms(grn_engine *e, uint64_t seed, uint32_t stream, int64_t first, int64_t n,
                         int32_t dim, double *out) {
-  if (!e || !out || n < 0 || dim < 1 || dim > 16) return fail(GRN_ERR_INVALID, "bad argument");
+  if (!e || !out || n < 0 || dim < 1 || dim > grn::kMaxDim)
+    return fail(GRN_ERR_INVALID, "bad argument");
   if (n == 0) return GRN_OK;
   GRN_CUDA(cudaSetDevice(e->device));
   const bool dev = is_device_ptr(out);

@@ -33,7 +33,8 @@ constexpr double kRefineKappa = 8.0;
 constexpr double kRefineTol   = 1e-5;
 
 constexpr int kMaxLoopNodes = 256;  // per axis
-constexpr int kMaxDim       = 16;   // hypercube dimensions: 8 (2-body), 14 (cascades, 4-body)
+constexpr int kMaxDim       = 20;   // hypercube dimensions: 8 (2-body), 10 (excitation), 12, 14
+                                    // (cascades, 4-body), 20 (6-body)
 
 // Scalars accumulated per block by the VEGAS sampling kernel.
 enum VegasScalar {

@@ -874,7 +874,9 @@ __global__ void k_event_kinematics(const KArgs A, const double *__restrict__ u, 
                (veto ? GRN_FLAG_VETOCUTS_OK : 0) | GRN_FLAG_AMPLITUDE_OK;
 }
 
-// Cascade daughters (px, py, pz, E) of the points (zeros where the kinematics fail).
+// Cascade daughters (px, py, pz, E) of the points, or the central particles of an N-body
+// state (4 x 4 doubles per point; 6 x 4 for six central particles); zeros where the
+// kinematics fail.
 __global__ void k_event_daughters(const KArgs A, const double *__restrict__ u, int64_t n, int dim,
                                   double *__restrict__ pd) {
   const int64_t i = static_cast<int64_t>(blockIdx.x) * blockDim.x + threadIdx.x;
@@ -882,16 +884,17 @@ __global__ void k_event_daughters(const KArgs A, const double *__restrict__ u, i
   double x[kMaxDim];
   for (int d = 0; d < kMaxDim; ++d) x[d] = d < dim ? u[i * dim + d] : 0.0;
   double d4[4][4] = {};
-  if (is_nbody(A.P)) {  // the four central particles
-    NBEvent e;
-    if (nbody_kinematics(A.P, A.K, x, e))
-      for (int k = 0; k < 4; ++k) {
-        d4[k][0] = e.c[k].x;
-        d4[k][1] = e.c[k].y;
-        d4[k][2] = 0.5 * (e.c[k].p - e.c[k].m);
-        d4[k][3] = 0.5 * (e.c[k].p + e.c[k].m);
-      }
-    for (int k = 0; k < 16; ++k) pd[i * 16 + k] = d4[k / 4][k % 4];
+  if (is_nbody(A.P)) {  // the central particles
+    const int nc = A.P.n_central;
+    NBEvent   e;
+    const bool kin = nbody_kinematics(A.P, A.K, x, e);
+    for (int k = 0; k < nc; ++k) {
+      double *o = pd + (i * nc + k) * 4;
+      o[0] = kin ? e.c[k].x : 0.0;
+      o[1] = kin ? e.c[k].y : 0.0;
+      o[2] = kin ? 0.5 * (e.c[k].p - e.c[k].m) : 0.0;
+      o[3] = kin ? 0.5 * (e.c[k].p + e.c[k].m) : 0.0;
+    }
     return;
   }
   Born b;
@@ -1626,7 +1629,8 @@ __device__ void vegas_hist_body(int bins, int dim, int64_t ncall, uint64_t seed,
       const double fe = f[e];
       f2              = fe * fe;
     }
-    uint64_t lo = 0ull, hi = 0ull;  // bins of dimensions 0..7 and 8..15, one byte each
+    // bins of dimensions 0..7, 8..15 and 16..23, one byte each
+    uint64_t b0 = 0ull, b1 = 0ull, b2 = 0ull;
     if (f2 != 0.0) {
       double u[kMaxDim];
       if (fu) {
@@ -1637,9 +1641,11 @@ __device__ void vegas_hist_body(int bins, int dim, int64_t ncall, uint64_t seed,
       for (int j = 0; j < dim; ++j) {
         const uint64_t k = static_cast<uint64_t>(vegas_bin(u[j], dbins, bins));
         if (j < 8)
-          lo |= k << (8 * j);
+          b0 |= k << (8 * j);
+        else if (j < 16)
+          b1 |= k << (8 * (j - 8));
         else
-          hi |= k << (8 * (j - 8));
+          b2 |= k << (8 * (j - 16));
       }
     }
     unsigned m = __ballot_sync(0xffffffffu, f2 != 0.0);
@@ -1647,10 +1653,12 @@ __device__ void vegas_hist_body(int bins, int dim, int64_t ncall, uint64_t seed,
       const int src = __ffs(m) - 1;
       m &= m - 1;
       const double   v  = __shfl_sync(0xffffffffu, f2, src);
-      const uint64_t pl = __shfl_sync(0xffffffffu, lo, src);
-      const uint64_t ph = __shfl_sync(0xffffffffu, hi, src);
+      const uint64_t p0 = __shfl_sync(0xffffffffu, b0, src);
+      const uint64_t p1 = __shfl_sync(0xffffffffu, b1, src);
+      const uint64_t p2 = __shfl_sync(0xffffffffu, b2, src);
       if (lane < dim) {
-        const int k = static_cast<int>(((lane < 8 ? pl : ph) >> (8 * (lane & 7))) & 0xFFu);
+        const uint64_t w = lane < 8 ? p0 : (lane < 16 ? p1 : p2);
+        const int      k = static_cast<int>((w >> (8 * (lane & 7))) & 0xFFu);
         hw[k * dim + lane] += v;
       }
     }

@@ -1,15 +1,16 @@
-// Regge continuum of four central particles: PP[CON]<F|C> -> a b c d (MRegge::ME6,
-// src/MRegge.cc:470-534). Factorized class: the central system decayed by the flat N-body
+// Regge continuum of four or six central particles: PP[CON]<F|C> -> a b c d (MRegge::ME6,
+// src/MRegge.cc:470-534) and -> a b c d e f (MRegge::ME8, src/MRegge.cc:560-627).
+// Factorized class: the central system decayed by the flat N-body
 // phase space of MKinematics.h:523-691 (NBodySetup, NBodyPhaseSpace) and the event weight of
 // MFactorized::EventWeight (src/MFactorized.cc:142-184). Continuum class: the 14-dimensional
 // phase space of MContinuum::BNRandomKin / BNBuildKin (src/MContinuum.cc:276-435).
 //
-// Factorized hypercube (14 coordinates): u[0..5] the factorized skeleton (log pT of the forward legs,
-// their azimuths, the system rapidity and mass^2), u[6], u[7] the two intermediate-mass draws
-// of NBodySetup (used in ascending order), u[8 + 2 k], u[9 + 2 k] (cos theta = 2 u - 1,
-// phi = 2 pi u) of the k-th decay of the recursion (particles 3, 2, 1 of the decay list in
-// that order). These are the draws the reference takes from its random-number generator
-// inside EventWeight, in the same order.
+// Factorized hypercube (3 N + 2 coordinates, N central particles): u[0..5] the factorized
+// skeleton (log pT of the forward legs, their azimuths, the system rapidity and mass^2),
+// u[6..N+3] the N - 2 intermediate-mass draws of NBodySetup (used in ascending order),
+// u[N+4+2k], u[N+5+2k] (cos theta = 2 u - 1, phi = 2 pi u) of the k-th decay of the
+// recursion (particles N-1, ..., 1 of the decay list in that order). These are the draws the
+// reference takes from its random-number generator inside EventWeight, in the same order.
 //
 // The amplitude is the sum over the 24 orderings (a, b, c, d) of the four particles along
 // the ladder:
@@ -29,9 +30,10 @@
 
 namespace grn {
 
-constexpr int kNb = 4;  // central particles of the N-body processes
+constexpr int kNb    = 4;  // central particles of the 4-body processes (the FP32 loop's shape)
+constexpr int kNbMax = 6;  // the largest central multiplicity (ME8)
 
-GRN_HD bool is_nbody(const grn_process_params &P) { return P.n_central == kNb; }
+GRN_HD bool is_nbody(const grn_process_params &P) { return P.n_central >= kNb; }
 
 // Light-cone 4-vector (p = E + pz, m = E - pz).
 struct LC4 {
@@ -59,19 +61,20 @@ GRN_HD LC4 lc_from_lab(double px, double py, double pz, double E, double m2) {
 }
 
 struct NBEvent {
+  int    n;                 // central particles (4 or 6)
   LC4    X;                 // central system
-  LC4    c[kNb];            // central particles in decay-list order
-  double m2[kNb];           // their masses^2
+  LC4    c[kNbMax];         // central particles in decay-list order
+  double m2[kNbMax];        // their masses^2
   double p1x, p1y, p2x, p2y, pt1sq, pt2sq;  // tree-level forward transverse momenta
   double a1, a2;            // (X+ - eps)/L, (X- - eps)/L: forward-leg closure constants
   double dw;                // N-body phase-space weight (NBodySetup volume x momenta)
   double m2w;               // mass^2 window of the system (B51IntegralVolume)
-  double sbc[kNb][kNb];     // (p_b + p_c)^2 of central pairs
+  double sbc[kNbMax][kNbMax];  // (p_b + p_c)^2 of central pairs
   bool   cuts;              // the central particles pass the particle cuts
   bool   veto;              // a central particle hits a veto domain
   double jx;                // per-event phase-space factor: F dPhi_N / (2 pi) x mass^2 window,
                             // C the product of the difference momenta kt_i
-  double kx[kNb - 1], ky[kNb - 1], y[kNb];  // C: difference momenta, rapidities
+  double kx[kNbMax - 1], ky[kNbMax - 1], y[kNbMax];  // C: difference momenta, rapidities
 };
 
 // Forward legs at transverse momenta (q1x, q1y), (q2x, q2y): light-cone closure (the
@@ -106,20 +109,20 @@ GRN_HD bool nbody_legs(const Consts &K, const NBEvent &e, double p1x, double p1y
 // Pair invariants and particle cuts of the central particles in e.c (GetLorentzScalars,
 // MProcess.cc:1515-1530; CommonCuts, MProcess.cc:1085-1138); false for a negative pair mass^2.
 GRN_HD bool nbody_finish(const grn_process_params &P, NBEvent &e) {
-  for (int a = 0; a < kNb; ++a)
-    for (int b = a + 1; b < kNb; ++b) {
+  for (int a = 0; a < e.n; ++a)
+    for (int b = a + 1; b < e.n; ++b) {
       e.sbc[a][b] = e.m2[a] + e.m2[b] + 2.0 * lc_dot(e.c[a], e.c[b]);
       e.sbc[b][a] = e.sbc[a][b];
       if (e.sbc[a][b] < 0) return false;
     }
   e.veto = false;
   if (P.veto_active)
-    for (int a = 0; a < kNb; ++a)
+    for (int a = 0; a < e.n; ++a)
       e.veto |= veto_hit(P, e.c[a].x, e.c[a].y, 0.5 * (e.c[a].p - e.c[a].m));
   const grn_fidcuts &f = P.fcuts;
   e.cuts = true;
   if (f.active) {
-    for (int a = 0; a < kNb; ++a) {
+    for (int a = 0; a < e.n; ++a) {
       const double pt  = sqrt(e.c[a].x * e.c[a].x + e.c[a].y * e.c[a].y);
       const double mt  = sqrt(e.m2[a] + pt * pt);
       const double y   = 0.5 * log(e.c[a].p / e.c[a].m);
@@ -133,28 +136,43 @@ GRN_HD bool nbody_finish(const grn_process_params &P, NBEvent &e) {
 }
 
 // Continuum class (MContinuum::BNBuildKin, src/MContinuum.cc:334-435): central transverse
-// momenta from the linear system of MContinuum::BLinearSystem for four particles,
-//   2 p0 = q0 - w - p2 - p3,  2 p1 = -q0 - w - p2 - p3,  2 p2 = -q1 - w - p0 - p3,
-//   2 p3 = -q2 - w - p0 - p1,  w = p1T + p2T,
-// solved with the inverse of its matrix; rapidities and masses fixed, the system X their sum,
-// the forward-leg closure constants from X. Also the loop kinematics of the class
-// (MContinuum::LoopKinematics, src/MContinuum.cc:94-161) at new forward transverse momenta.
+// momenta from the linear system of MContinuum::BLinearSystem for N = 4 or 6 particles,
+//   2 p0 = q0 - w - (p2 + ... + p_{N-1}),  2 p1 = -q0 - w - (p2 + ... + p_{N-1}),
+//   2 p_i = -q_{i-1} - w - (the sum of the p_j with j != i, i - 1),  i >= 2,  w = p1T + p2T,
+// solved with the inverse of its matrix (exact rationals); rapidities and masses fixed, the
+// system X their sum, the forward-leg closure constants from X. Also the loop kinematics of
+// the class (MContinuum::LoopKinematics, src/MContinuum.cc:94-161) at new forward transverse
+// momenta.
 GRN_HD bool nbody_build_C(const Consts &K, NBEvent &e, double p1x, double p1y, double p2x,
                           double p2y) {
-  constexpr double Ai[kNb][kNb] = {{0.875, 0.125, -0.5, -0.25},
-                                   {0.375, 0.625, -0.5, -0.25},
-                                   {-0.125, 0.125, 0.5, -0.25},
-                                   {-0.625, -0.375, 0.5, 0.75}};
+  constexpr double A4[4][4] = {{0.875, 0.125, -0.5, -0.25},
+                               {0.375, 0.625, -0.5, -0.25},
+                               {-0.125, 0.125, 0.5, -0.25},
+                               {-0.625, -0.375, 0.5, 0.75}};
+  constexpr double A6[6][6] = {
+      {4.0 / 3, 1.0 / 2, -2.0 / 3, -1.0 / 2, -1.0 / 3, -1.0 / 6},
+      {5.0 / 6, 1.0, -2.0 / 3, -1.0 / 2, -1.0 / 3, -1.0 / 6},
+      {1.0 / 3, 1.0 / 2, 1.0 / 3, -1.0 / 2, -1.0 / 3, -1.0 / 6},
+      {-1.0 / 6, 0.0, 1.0 / 3, 1.0 / 2, -1.0 / 3, -1.0 / 6},
+      {-2.0 / 3, -1.0 / 2, 1.0 / 3, 1.0 / 2, 2.0 / 3, -1.0 / 6},
+      {-7.0 / 6, -1.0, 1.0 / 3, 1.0 / 2, 2.0 / 3, 5.0 / 6}};
+  const int    N  = e.n;
   const double wx = p1x + p2x, wy = p1y + p2y;
-  const double bx[kNb] = {e.kx[0] - wx, -e.kx[0] - wx, -e.kx[1] - wx, -e.kx[2] - wx};
-  const double by[kNb] = {e.ky[0] - wy, -e.ky[0] - wy, -e.ky[1] - wy, -e.ky[2] - wy};
+  double bx[kNbMax], by[kNbMax];
+  bx[0] = e.kx[0] - wx;
+  by[0] = e.ky[0] - wy;
+  for (int i = 1; i < N; ++i) {
+    bx[i] = -e.kx[i - 1] - wx;
+    by[i] = -e.ky[i - 1] - wy;
+  }
   LC4    X{0.0, 0.0, 0.0, 0.0};
   double msum = 0.0;
-  for (int i = 0; i < kNb; ++i) {
+  for (int i = 0; i < N; ++i) {
     double px = 0.0, py = 0.0;
-    for (int j = 0; j < kNb; ++j) {
-      px += Ai[i][j] * bx[j];
-      py += Ai[i][j] * by[j];
+    for (int j = 0; j < N; ++j) {
+      const double a = N == 4 ? A4[i][j] : A6[i][j];
+      px += a * bx[j];
+      py += a * by[j];
     }
     const double mt = sqrt(e.m2[i] + px * px + py * py);
     const double ey = exp(e.y[i]);
@@ -178,9 +196,11 @@ GRN_HD bool nbody_build_C(const Consts &K, NBEvent &e, double p1x, double p1y, d
 GRN_HD bool nbody_kinematics(const grn_process_params &P, const Consts &K, const double *u,
                              NBEvent &e) {
   const grn_gencuts &g = P.gcuts;
+  const int          N = P.n_central;
+  e.n                  = N;
   if (P.phase_space == GRN_PS_CONTINUUM) {
     // BNRandomKin (src/MContinuum.cc:276-331): forward legs u[0..3], difference momenta kt
-    // u[4..6] and azimuths u[7..9], rapidities u[10..13]
+    // u[4..N+2] and azimuths u[N+3..2N+1], rapidities u[2N+2..3N+1]
     const double pt1 = exp(K.lnpt_lo + (K.lnpt_hi - K.lnpt_lo) * u[0]);
     const double pt2 = exp(K.lnpt_lo + (K.lnpt_hi - K.lnpt_lo) * u[1]);
     double s1, c1, s2, c2;
@@ -193,16 +213,16 @@ GRN_HD bool nbody_kinematics(const grn_process_params &P, const Consts &K, const
     e.pt1sq = e.p1x * e.p1x + e.p1y * e.p1y;
     e.pt2sq = e.p2x * e.p2x + e.p2y * e.p2y;
     e.jx = 1.0;
-    for (int i = 0; i < kNb - 1; ++i) {
+    for (int i = 0; i < N - 1; ++i) {
       const double kt = g.kt_min + (g.kt_max - g.kt_min) * u[4 + i];
       double sk, ck;
-      sincos_pi(2.0 * u[7 + i], sk, ck);
+      sincos_pi(2.0 * u[N + 3 + i], sk, ck);
       e.kx[i] = kt * ck;
       e.ky[i] = kt * sk;
       e.jx *= kt;
     }
-    for (int i = 0; i < kNb; ++i) {
-      e.y[i]  = g.rap_min + (g.rap_max - g.rap_min) * u[10 + i];
+    for (int i = 0; i < N; ++i) {
+      e.y[i]  = g.rap_min + (g.rap_max - g.rap_min) * u[2 * N + 2 + i];
       e.m2[i] = P.m_central[i] * P.m_central[i];
     }
     if (!nbody_build_C(K, e, e.p1x, e.p1y, e.p2x, e.p2y)) return false;
@@ -242,33 +262,47 @@ GRN_HD bool nbody_kinematics(const grn_process_params &P, const Consts &K, const
   // NBodySetup (MKinematics.h:529-605), weighted: intermediate masses from the ordered draws,
   // decay momenta, volume 1 / (2 (2 pi)^(2N-3)) DELTA^(N-2) / (N-2)! / M0
   const double M0 = sqrt(m2X);
-  double m[kNb], sum[kNb];
-  for (int i = 0; i < kNb; ++i) {
+  double m[kNbMax], sum[kNbMax];
+  for (int i = 0; i < N; ++i) {
     m[i]   = P.m_central[i];
     sum[i] = (i ? sum[i - 1] : 0.0) + m[i];
     e.m2[i] = m[i] * m[i];
   }
-  const double D = M0 - sum[kNb - 1];
+  const double D = M0 - sum[N - 1];
   if (!(D > 0)) return false;
-  const double r0 = fmin(u[6], u[7]), r1 = fmax(u[6], u[7]);
-  const double Meff[kNb] = {m[0], sum[1] + r0 * D, sum[2] + r1 * D, M0};
-  double pn[kNb];
+  double r[kNbMax - 2];  // the N - 2 mass draws in ascending order (insertion sort)
+  for (int i = 0; i < N - 2; ++i) {
+    const double v = u[6 + i];
+    int          j = i;
+    for (; j > 0 && r[j - 1] > v; --j) r[j] = r[j - 1];
+    r[j] = v;
+  }
+  double Meff[kNbMax];
+  Meff[0]     = m[0];
+  Meff[N - 1] = M0;
+  for (int i = 1; i < N - 1; ++i) Meff[i] = sum[i] + r[i - 1] * D;
+  double pn[kNbMax];
   double w = 1.0;
-  for (int i = 1; i < kNb; ++i) {
+  for (int i = 1; i < N; ++i) {
     const double x = Meff[i], y = Meff[i - 1], z = m[i];
     pn[i] = sqrt(fmax(0.0, (x - y - z) * (x + y + z) * (x + y - z) * (x - y + z))) / (2.0 * x);
     w *= pn[i];
   }
   const double tp = 2.0 * kPi;
-  e.dw = w / (2.0 * (tp * tp * tp * tp * tp)) * (D * D) / 2.0 / M0;
+  if (N == 4) {
+    e.dw = w / (2.0 * (tp * tp * tp * tp * tp)) * (D * D) / 2.0 / M0;
+  } else {
+    const double tp3 = tp * tp * tp, D2 = D * D;
+    e.dw = w / (2.0 * (tp3 * tp3 * tp3)) * (D2 * D2) / 24.0 / M0;
+  }
   e.jx = e.m2w * e.dw / (2.0 * kPi);
 
   // NBodyPhaseSpace (MKinematics.h:643-691): from the last particle down, an isotropic
   // momentum in the rest frame of what is left, boosted to the lab with that system's
   // lab momentum, then subtracted from it; the first particle takes the remainder.
   double kx = Xx, ky = Xy, kz = ZX, kE = EX;
-  for (int i = kNb - 1; i >= 1; --i) {
-    const int    j  = 8 + 2 * (kNb - 1 - i);
+  for (int i = N - 1; i >= 1; --i) {
+    const int    j  = N + 4 + 2 * (N - 1 - i);
     const double ct = 2.0 * u[j] - 1.0;
     const double st = sqrt(fmax(0.0, 1.0 - ct * ct));
     double sp, cp;
@@ -307,10 +341,14 @@ GRN_HD bool nbody_fiducial(const grn_process_params &P, const NBEvent &e, const 
   return e.cuts;
 }
 
-// ME6 (MRegge.cc:470-534) at forward legs g; false when an invariant check fails
-// (GetLorentzScalars: negative s-type invariants or positive t1, t2).
+GRN_HD_COLD bool nbody_amp6(const grn_process_params &P, const Consts &K, const NBEvent &e,
+                            const NBLegs &g, cx<double> &A);
+
+// ME6 (MRegge.cc:470-534) at forward legs g, or ME8 for six central particles; false when an
+// invariant check fails (GetLorentzScalars: negative s-type invariants or positive t1, t2).
 GRN_HD bool nbody_amp(const grn_process_params &P, const Consts &K, const NBEvent &e,
                       const NBLegs &g, cx<double> &A) {
+  if (e.n == kNbMax) return nbody_amp6(P, K, e, g, A);
   const grn_regge_params &rp = P.regge;
   if (g.t1 > 0 || g.t2 > 0) return false;
   double lns1[kNb], lns2[kNb], d1[kNb], f1[kNb], f2[kNb];
@@ -347,6 +385,77 @@ GRN_HD bool nbody_amp(const grn_process_params &P, const Consts &K, const NBEven
   const double g2 = K.g2;
   const double vtx = K.gN2 * proton_ff<double>(P.soft.fc1, P.soft.fc2, g.t1) *
                      proton_ff<double>(P.soft.fc1, P.soft.fc2, g.t2) * g2 * g2;
+  A = cscale(S, vtx);
+  return true;
+}
+
+// ME8 (MRegge.cc:560-627): the sum over the 720 orderings (a b c d e f) of the six central
+// particles along the ladder of
+//   R(s_1a, t1) FF_A ff(t_ab, MA) g / (t_ab - MA) ff(t_bc, MA) g R(s_bc, t_bc) ff(t_bc, MB) g
+//   / (t_cd - MB) ff(t_de, MB) g R(s_de, t_de) ff(t_de, MC) g / (t_ef - MC) ff(t_ef, MC) g
+//   R(s_2f, t2) FF_B
+// with the reference's invariants t_ab = (q1 - p_a)^2, t_bc = T_ab, t_cd = T_bc, t_de = T_cd,
+// t_ef = (q2 - p_f)^2, where T_xy = (q1 - p_x - p_y)^2 (the scalars it reads from
+// LORENTZSCALAR::tt_xy), and MA, MB, MC the masses^2 of the first, third and fifth particle of
+// the decay list. The 120 Regge factors R(s_yz, T_xy) of distinct (x, y, z) are formed once;
+// each ordering is then a product of five tabulated factors.
+GRN_HD_COLD bool nbody_amp6(const grn_process_params &P, const Consts &K, const NBEvent &e,
+                            const NBLegs &g, cx<double> &A) {
+  constexpr int N = kNbMax;
+  const grn_regge_params &rp = P.regge;
+  if (g.t1 > 0 || g.t2 > 0) return false;
+  const double MA = P.m_central[0] * P.m_central[0], MB = P.m_central[2] * P.m_central[2];
+  const double MC = P.m_central[4] * P.m_central[4];
+  double     d1[N];
+  cx<double> X1[N], X2[N];
+  for (int a = 0; a < N; ++a) {
+    const double s1 = K.mp2 + e.m2[a] + 2.0 * lc_dot(g.p1, e.c[a]);
+    const double s2 = K.mp2 + e.m2[a] + 2.0 * lc_dot(g.p2, e.c[a]);
+    if (s1 < 0 || s2 < 0) return false;
+    d1[a] = lc_dot(g.q1, e.c[a]);
+    const double ta = g.t1 + e.m2[a] - 2.0 * d1[a];
+    const double tf = g.t2 + e.m2[a] - 2.0 * lc_dot(g.q2, e.c[a]);
+    X1[a] = cscale(regge_prop<double>(K, rp, log(s1), g.t1), meson_ff<double>(rp, ta, MA) / (ta - MA));
+    X2[a] = cscale(regge_prop<double>(K, rp, log(s2), g.t2), meson_ff<double>(rp, tf, MC) / (tf - MC));
+  }
+  double     fAB[N][N], fBC[N][N], pB[N][N], lsb[N][N];
+  for (int x = 0; x < N; ++x)
+    for (int y = x + 1; y < N; ++y) {
+      const double T = g.t1 + e.sbc[x][y] - 2.0 * (d1[x] + d1[y]);
+      fAB[x][y] = fAB[y][x] = meson_ff<double>(rp, T, MA) * meson_ff<double>(rp, T, MB);
+      fBC[x][y] = fBC[y][x] = meson_ff<double>(rp, T, MB) * meson_ff<double>(rp, T, MC);
+      pB[x][y] = pB[y][x] = 1.0 / (T - MB);
+      lsb[x][y] = lsb[y][x] = log(e.sbc[x][y]);
+    }
+  cx<double> Rt[N][N][N];  // R(s_yz, T_xy)
+  for (int x = 0; x < N; ++x)
+    for (int y = 0; y < N; ++y) {
+      if (y == x) continue;
+      const int    lo = x < y ? x : y, hi = x < y ? y : x;
+      const double T  = g.t1 + e.sbc[lo][hi] - 2.0 * (d1[x] + d1[y]);
+      for (int z = 0; z < N; ++z)
+        if (z != x && z != y) Rt[x][y][z] = regge_prop<double>(K, rp, lsb[y][z], T);
+    }
+  cx<double> S{0.0, 0.0};
+  for (int a = 0; a < N; ++a)
+    for (int b = 0; b < N; ++b) {
+      if (b == a) continue;
+      for (int c = 0; c < N; ++c) {
+        if (c == a || c == b) continue;
+        const cx<double> Y = cscale(cmul(X1[a], Rt[a][b][c]), fAB[a][b] * pB[b][c]);
+        for (int d = 0; d < N; ++d) {
+          if (d == a || d == b || d == c) continue;
+          for (int k = 0; k < N; ++k) {  // k = e of the ordering, f the one left
+            if (k == a || k == b || k == c || k == d) continue;
+            const int f = 15 - a - b - c - d - k;
+            S = cadd(S, cmul(cscale(cmul(Y, Rt[c][d][k]), fBC[c][d]), X2[f]));
+          }
+        }
+      }
+    }
+  const double g2  = K.g2;
+  const double vtx = K.gN2 * proton_ff<double>(P.soft.fc1, P.soft.fc2, g.t1) *
+                     proton_ff<double>(P.soft.fc1, P.soft.fc2, g.t2) * g2 * g2 * g2;
   A = cscale(S, vtx);
   return true;
 }
@@ -695,7 +804,7 @@ __device__ __noinline__ double nbody_screened_weight(const KArgs &A, const doubl
   bool       fp32 = false;
   if (refine) *refine = false;
   if constexpr (sizeof(T) == sizeof(float)) {
-    if (A.K.n_active == 1) {
+    if (A.K.n_active == 1 && e.n == kNb) {
       fp32        = true;
       double mag  = 0.0;
       Al = nbody_loop_f(A, e, skt, sphi, &mag);

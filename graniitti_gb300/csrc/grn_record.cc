@@ -110,21 +110,25 @@ Tree build_tree(const double *q, const double *d, const int32_t *pdg, const doub
   return t;
 }
 
-// 4-body central states: system (90) -> the four central particles (status 1). q holds the
-// forward legs (8 doubles), c the central particles (16).
-Tree build_tree_4(const double *q, const double *c, const int32_t *pdg, const double *mass,
-                  double sqrt_s) {
+// N-body central states: system (90) -> the nc central particles (status 1). q holds the
+// forward legs (8 doubles), c the central particles (4 nc).
+Tree build_tree_n(const double *q, const double *c, int nc, const int32_t *pdg,
+                  const double *mass, double sqrt_s) {
   double q2[16];
   for (int k = 0; k < 8; ++k) q2[k] = q[k];
   for (int k = 0; k < 8; ++k) q2[8 + k] = c[k];
   const int32_t pdg2[3]  = {pdg[0], pdg[1], pdg[2]};
   const double  mass2[3] = {mass[0], mass[1], mass[2]};
   Tree t = build_tree(q2, nullptr, pdg2, mass2, sqrt_s);
-  // the system is the sum of all four; the last two central particles join the same vertex
+  // the system is the sum of all of them; the others join the same vertex
   const int X = 6;
-  for (int k = 0; k < 4; ++k) t.part[X].p[k] = c[k] + c[4 + k] + c[8 + k] + c[12 + k];
+  for (int k = 0; k < 4; ++k) {
+    double v = 0.0;
+    for (int j = 0; j < nc; ++j) v += c[4 * j + k];
+    t.part[X].p[k] = v;
+  }
   t.part[X].m = mass_of(t.part[X].p);
-  for (int j = 2; j < 4; ++j)
+  for (int j = 2; j < nc; ++j)
     t.add({pdg[1 + j], 1, {c[4 * j], c[4 * j + 1], c[4 * j + 2], c[4 * j + 3]}, mass[1 + j]}, 4);
   return t;
 }
@@ -274,12 +278,14 @@ grn_status grn_write_events(grn_writer *w, grn_engine *e, const double *u, int64
   if (written) *written = 0;
   if (!w || !w->fp || !e || !pdg || n < 0 || (n > 0 && !u)) return GRN_ERR_INVALID;
   const grn_process_params *P = grn_engine_params(e);
-  const bool casc = P->n_decay == 2, four = P->n_central == 4;
-  if (n_pdg != (casc ? 7 : (four ? 5 : 3))) return GRN_ERR_INVALID;
+  const int  nc   = P->n_central;
+  const bool casc = P->n_decay == 2, four = nc >= 4;  // four: an N-body central state
+  if (n_pdg != (casc ? 7 : (four ? 1 + nc : 3))) return GRN_ERR_INVALID;
   if (n == 0) return GRN_OK;
   const int dim = grn_dim(e);
   std::vector<double>  p4(static_cast<size_t>(n) * 16), ts(static_cast<size_t>(n) * 2);
-  std::vector<double>  pd((casc || four) ? static_cast<size_t>(n) * 16 : 0);
+  const size_t per = four ? static_cast<size_t>(4 * nc) : 16;  // daughters' doubles per point
+  std::vector<double>  pd((casc || four) ? static_cast<size_t>(n) * per : 0);
   std::vector<uint8_t> fl(static_cast<size_t>(n));
   grn_status st = grn_event_kinematics(e, u, n, dim, p4.data(), ts.data(), fl.data());
   if (st == GRN_OK && (casc || four)) st = grn_event_daughters(e, u, n, dim, pd.data());
@@ -290,16 +296,16 @@ grn_status grn_write_events(grn_writer *w, grn_engine *e, const double *u, int64
     if (!(fl[i] & GRN_FLAG_KINEMATICS_OK)) continue;
     if (m != i) {
       std::copy(&p4[i * 16], &p4[i * 16] + 16, &p4[m * 16]);
-      if (casc || four) std::copy(&pd[i * 16], &pd[i * 16] + 16, &pd[m * 16]);
+      if (casc || four) std::copy(&pd[i * per], &pd[i * per] + per, &pd[m * per]);
     }
     ++m;
   }
   if (four) {
-    const double mass[5] = {P->m_beam, P->m_central[0], P->m_central[1], P->m_central[2],
-                            P->m_central[3]};
+    double mass[7] = {P->m_beam};
+    for (int k = 0; k < nc; ++k) mass[1 + k] = P->m_central[k];
     if (!(P->sqrt_s > 2 * mass[0])) return GRN_ERR_INVALID;
     for (int64_t i = 0; i < m; ++i)
-      write_tree(w, build_tree_4(&p4[i * 16], &pd[i * 16], pdg, mass, P->sqrt_s), weight,
+      write_tree(w, build_tree_n(&p4[i * 16], &pd[i * per], nc, pdg, mass, P->sqrt_s), weight,
                  sigma_pb, sigma_err_pb);
     std::fflush(w->fp);
   } else if (casc) {

@@ -72,9 +72,10 @@ class Engine:
         return w, flags
 
     def event_daughters(self, u):
-        """Cascade daughters, or the four central particles of a 4-body state (n, 4, 4)."""
+        """Cascade daughters (n, 4, 4), or the central particles of a 4- or 6-body state
+        (n, 4, 4) / (n, 6, 4)."""
         u = np.ascontiguousarray(u, dtype=np.float64)
-        pd = np.zeros((u.shape[0], 4, 4))
+        pd = np.zeros((u.shape[0], 6 if self.params.n_central == 6 else 4, 4))
         _abi.check(self.lib.grn_event_daughters(self.h, _ptr(u), u.shape[0], self.dim, _ptr(pd)))
         return pd
 

@@ -319,9 +319,9 @@ grn_status grn_event_kinematics(grn_engine *e, const double *u, int64_t n, int32
 
 /* Cascade processes (n_decay = 2): the four daughters of the two central particles, per
  * point 16 doubles (px, py, pz, E) in the order central 1 -> 2 daughters, central 2 -> 2
- * daughters (the leaves of lts.decaytree, ConstructDecayKinematics). 4-body central states
- * (n_central = 4): the four central particles (LORENTZSCALAR::pfinal[3..6]). GRN_ERR_STATE
- * for other engines. */
+ * daughters (the leaves of lts.decaytree, ConstructDecayKinematics). N-body central states
+ * (n_central = 4, 6): the central particles (LORENTZSCALAR::pfinal[3..]), 16 or 24 doubles
+ * per point. GRN_ERR_STATE for other engines. */
 grn_status grn_event_daughters(grn_engine *e, const double *u, int64_t n, int32_t dim,
                                double *pd_out);
 
@@ -582,7 +582,7 @@ grn_status grn_writer_close(grn_writer *w);
  * in pdg[n_pdg]: the beams and the two central particles (n_pdg = 3), followed for cascades
  * by the four daughters (n_pdg = 7; the central particles are then written with status 2 and
  * their decay vertices, WriteDecayKinematics, src/MProcess.cc:1289-1315, at the origin), or
- * for 4-body central states the beams and the four central particles (n_pdg = 5),
+ * for N-body central states the beams and the central particles (n_pdg = 1 + n_central),
  * weight written with every event (1 for unweighted events), cross section and error in pb.
  * Event numbers continue from the writer's count. Points whose kinematics fail are skipped
  * (*written says how many were written). */

@@ -622,12 +622,13 @@ bool build_kinematics_F(const Setup &S, const real *u, Event &ev) {
   const real phi2 = 2.0 * PI * u[3];
   const real yX   = g.Y_min + (g.Y_max - g.Y_min) * u[4];
   real m3 = S.p.m_central[0], m4 = S.p.m_central[1];
-  if (S.p.n_central >= 4) {
-    m4 = 0;
-    for (int i = 1; i < S.p.n_central; ++i) m4 += S.p.m_central[i];
-  }
   if (S.p.n_decay == 2) cascade_masses(S.p, u, m3, m4);  // off-shell central masses
-  const real Mmin = std::max<real>(m3 + m4 + 1e-4, g.M_min);
+  real msum = m3 + m4;
+  if (S.p.n_central >= 4) {  // M_sum in the decay-list order (MFactorized.cc:265-270)
+    msum = 0;
+    for (int i = 0; i < S.p.n_central; ++i) msum += S.p.m_central[i];
+  }
+  const real Mmin = std::max<real>(msum + 1e-4, g.M_min);
   const real Mmax = std::min<real>(S.sqrt_s - (S.pb1.m() + S.pb2.m()), g.M_max);
   if (!(Mmin < Mmax)) return false;
   const real m2X  = Mmin * Mmin + (Mmax * Mmax - Mmin * Mmin) * u[5];
