@@ -109,14 +109,34 @@ GRN_HD void sincos_pi(double x, double &s, double &c) {
   c = std::cos(kPi * x);
 #endif
 }
-GRN_HD void sincos_pi(float x, float &s, float &c) {
-#ifdef __CUDA_ARCH__
-  sincospif(x, &s, &c);
-#else
-  s = std::sin(float(kPi) * x);
-  c = std::cos(float(kPi) * x);
-#endif
+// sin(pi x), cos(pi x) in FP32 arithmetic only: x = n + r with n = rint(x), |r| <= 1/2 (r
+// exact), then the Taylor series of sin(pi r) / r and cos(pi r) in r^2 through the r^14 term,
+// evaluated by Horner's rule (truncation below 1e-9 at |r| = 1/2), and the sign (-1)^n. About
+// 2 ulp; relative accuracy kept for small r (the leading term is pi r).
+GRN_HD void sincos_pi_poly(float x, float &s, float &c) {
+  const float n  = rintf(x);
+  const float r  = x - n;
+  const float r2 = r * r;
+  float ps = 4.6630280576761255e-4f;  // pi^13 / 13!
+  ps = fmaf(ps, r2, -7.3704309457143508e-3f);
+  ps = fmaf(ps, r2, 8.2145886611128228e-2f);
+  ps = fmaf(ps, r2, -5.9926452932079208e-1f);
+  ps = fmaf(ps, r2, 2.5501640398773455f);
+  ps = fmaf(ps, r2, -5.1677127800499703f);
+  ps = fmaf(ps, r2, 3.1415926535897932f);
+  float pc = -1.0463810492484570e-4f;  // -pi^14 / 14!
+  pc = fmaf(pc, r2, 1.9295743094039231e-3f);
+  pc = fmaf(pc, r2, -2.5806891390014061e-2f);
+  pc = fmaf(pc, r2, 2.3533063035889320e-1f);
+  pc = fmaf(pc, r2, -1.3352627688545894f);
+  pc = fmaf(pc, r2, 4.0587121264167683f);
+  pc = fmaf(pc, r2, -4.9348022005446793f);
+  pc = fmaf(pc, r2, 1.0f);
+  const bool odd = (static_cast<int>(n) & 1) != 0;
+  s = odd ? -(r * ps) : r * ps;
+  c = odd ? -pc : pc;
 }
+GRN_HD void sincos_pi(float x, float &s, float &c) { sincos_pi_poly(x, s, c); }
 
 // ---------------------------------------------------------------------------
 // Model functions, arithmetic type T.
@@ -1506,7 +1526,9 @@ GRN_HD float fast_log2(float x) {
 }
 GRN_HD float fast_exp2(float x) {
 #ifdef __CUDA_ARCH__
-  return exp2f(x);
+  float y;
+  asm("ex2.approx.ftz.f32 %0, %1;" : "=f"(y) : "f"(x));  // the SFU's 2^x (~2 ulp)
+  return y;
 #else
   return std::exp2(x);
 #endif
