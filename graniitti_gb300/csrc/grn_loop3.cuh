@@ -58,8 +58,8 @@ __device__ __forceinline__ float2 sqrt2(float2 a) { return make_float2(sqrtf(a.x
 // (absolute error ~5e-7 on |2 pi h| <= pi).
 __device__ __forceinline__ void sincos_turns2(float2 h, float2 &s, float2 &c) {
   const float rx = h.x - rintf(h.x), ry = h.y - rintf(h.y);
-  __sincosf(float(2.0 * kPi) * rx, &s.x, &c.x);
-  __sincosf(float(2.0 * kPi) * ry, &s.y, &c.y);
+  sfu_sincos(float(2.0 * kPi) * rx, s.x, c.x);
+  sfu_sincos(float(2.0 * kPi) * ry, s.y, c.y);
 }
 // sin(pi d) for |d| < 1 (accurate: the once-per-phi-node projections).
 __device__ __forceinline__ float2 sinpi_turns2(float2 d) {

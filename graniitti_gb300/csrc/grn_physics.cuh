@@ -1519,7 +1519,9 @@ GRN_HD float fast_exp(float x) {
 // logarithms and exponents in log2 units, so no ln 2 scalings are executed.
 GRN_HD float fast_log2(float x) {
 #ifdef __CUDA_ARCH__
-  return __log2f(x);
+  float y;
+  asm("lg2.approx.ftz.f32 %0, %1;" : "=f"(y) : "f"(x));  // the SFU's log2 (normal x)
+  return y;
 #else
   return std::log2(x);
 #endif
@@ -1536,9 +1538,21 @@ GRN_HD float fast_exp2(float x) {
 // a / b through the reciprocal unit (about 2 ulp); b in the normal range.
 GRN_HD float fast_div(float a, float b) {
 #ifdef __CUDA_ARCH__
-  return __fdividef(a, b);
+  float r;
+  asm("rcp.approx.ftz.f32 %0, %1;" : "=f"(r) : "f"(b));  // the SFU's 1/b (normal b)
+  return a * r;
 #else
   return a / b;
+#endif
+}
+// The SFU's sine and cosine of an argument in [-pi, pi] (absolute error ~5e-7).
+GRN_HD void sfu_sincos(float a, float &s, float &c) {
+#ifdef __CUDA_ARCH__
+  asm("sin.approx.ftz.f32 %0, %1;" : "=f"(s) : "f"(a));
+  asm("cos.approx.ftz.f32 %0, %1;" : "=f"(c) : "f"(a));
+#else
+  s = std::sin(a);
+  c = std::cos(a);
 #endif
 }
 // sin(pi x), cos(pi x) for the loop phase: x reduced by its period 2 to [-1, 1], then
@@ -1546,7 +1560,7 @@ GRN_HD float fast_div(float a, float b) {
 GRN_HD void fast_sincos_pi(float x, float &s, float &c) {
 #ifdef __CUDA_ARCH__
   const float r = fmaf(-2.f, rintf(0.5f * x), x);
-  __sincosf(float(kPi) * r, &s, &c);
+  sfu_sincos(float(kPi) * r, s, c);
 #else
   s = std::sin(float(kPi) * x);
   c = std::cos(float(kPi) * x);
