@@ -56,8 +56,16 @@ __device__ __forceinline__ float2 abs2(float2 a) { return make_float2(fabsf(a.x)
 __device__ __forceinline__ float2 sqrt2(float2 a) { return make_float2(sqrtf(a.x), sqrtf(a.y)); }
 // (sin 2 pi h, cos 2 pi h): h reduced to [-1/2, 1/2] turns, then the hardware sine / cosine
 // (absolute error ~5e-7 on |2 pi h| <= pi).
+__device__ __forceinline__ float near_int(float x) {
+  // the nearest integer to x (|x| < 2^22): x + 1.5 2^23 has no fraction bits left, and
+  // subtracting 1.5 2^23 back is exact; two FP32 additions
+  float t, r;
+  asm("add.rn.f32 %0, %1, 0f4B400000;" : "=f"(t) : "f"(x));
+  asm("sub.rn.f32 %0, %1, 0f4B400000;" : "=f"(r) : "f"(t));
+  return r;
+}
 __device__ __forceinline__ void sincos_turns2(float2 h, float2 &s, float2 &c) {
-  const float rx = h.x - rintf(h.x), ry = h.y - rintf(h.y);
+  const float rx = h.x - near_int(h.x), ry = h.y - near_int(h.y);
   sfu_sincos(float(2.0 * kPi) * rx, s.x, c.x);
   sfu_sincos(float(2.0 * kPi) * ry, s.y, c.y);
 }
