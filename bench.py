@@ -495,11 +495,18 @@ def main():
     # full pass over the adapted grid (untimed set-up)
     tune = eng.autotune()
     variant = {0: "1 event/thread", 1: "2 events/thread", 2: "2 events/thread, 3 blocks/SM"}
+
+    def _label(k):
+        c = tune.cand[k]
+        if tune.stage[k] == 0:
+            return "stage A x %d blocks" % c.born_blocks
+        if tune.stage[k] == 2:
+            return "generic loop x %d blocks" % c.generic_blocks
+        return "%s x %d blocks" % (variant[c.loop_pair], c.vegas_blocks)
     tuned = {"loop_variant": variant[tune.best.loop_pair],
              "loop_blocks": tune.best.vegas_blocks,
-             "candidates_ms": {"%s x %d blocks" % (variant[tune.cand[k].loop_pair],
-                                                  tune.cand[k].vegas_blocks):
-                               round(tune.ms[k], 4) for k in range(tune.n_candidates)},
+             "stage_a_blocks": tune.best.born_blocks,
+             "candidates_ms": {_label(k): round(tune.ms[k], 4) for k in range(tune.n_candidates)},
              "listed_events": tune.sample_events}
     eng.vegas_clear()
     ms_plain, res_plain = _timed_passes(

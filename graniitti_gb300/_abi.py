@@ -140,12 +140,17 @@ class HistSpec(ctypes.Structure):
 
 class Tuning(ctypes.Structure):
     _fields_ = [("loop_pair", c_int32), ("vegas_blocks", c_int32), ("weight_blocks", c_int32),
-                ("fp64_refine", c_int32), ("refine_tol", c_double)]
+                ("fp64_refine", c_int32), ("refine_tol", c_double), ("born_blocks", c_int32),
+                ("generic_blocks", c_int32)]
+
+
+GRN_TUNE_MAX = 16
 
 
 class TuneResult(ctypes.Structure):
     _fields_ = [("best", Tuning), ("n_candidates", c_int32), ("_pad", c_int32),
-                ("ms", c_double * 8), ("cand", Tuning * 8), ("sample_events", c_int64)]
+                ("ms", c_double * GRN_TUNE_MAX), ("cand", Tuning * GRN_TUNE_MAX),
+                ("stage", c_int32 * GRN_TUNE_MAX), ("sample_events", c_int64)]
 
 
 GRN_FORMAT_HEPMC3 = 0

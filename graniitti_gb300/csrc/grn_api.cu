@@ -110,6 +110,8 @@ struct grn_engine {
   int    loop_pair   = 0;  // record-mode loop: events per thread - 1 (set by grn_autotune)
   int    fp64_refine = 1;  // FP32 loops: redo badly conditioned events in FP64
   double refine_tol  = grn::kRefineTol;  // estimated relative error that sends them there
+  int    born_blocks = 0;  // VEGAS stage-A grid (0: default), set by grn_autotune
+  int    gen_blocks  = 0;  // FP32 generic loop grid (0: one resident wave), set by grn_autotune
 
   // VEGAS
   int         bins = 0;
@@ -162,6 +164,8 @@ struct grn_engine {
     a.loop_norm_im = loop_norm_im;
     a.loop_pair    = loop_pair;
     a.refine_tol   = fp64_refine ? refine_tol : 0.0;
+    a.born_blocks  = born_blocks;
+    a.gen_blocks   = gen_blocks;
     return a;
   }
 };
@@ -1721,6 +1725,8 @@ grn_status grn_get_tuning(grn_engine *e, grn_tuning *t) {
   t->weight_blocks = e->loop_blocks;
   t->fp64_refine   = e->fp64_refine;
   t->refine_tol    = e->refine_tol;
+  t->born_blocks   = e->born_blocks;
+  t->generic_blocks = e->gen_blocks;
   return GRN_OK;
 }
 
@@ -1729,13 +1735,16 @@ grn_status grn_set_tuning(grn_engine *e, const grn_tuning *t) {
   if (t->loop_pair < 0 || t->loop_pair > 2 || t->vegas_blocks < 1 || t->weight_blocks < 1 ||
       t->vegas_blocks > (1 << 20) || t->weight_blocks > (1 << 20) ||
       (t->fp64_refine != 0 && t->fp64_refine != 1) ||
-      !(t->refine_tol >= 1e-9 && t->refine_tol <= 1.0))
+      !(t->refine_tol >= 1e-9 && t->refine_tol <= 1.0) || t->born_blocks < 0 ||
+      t->born_blocks > (1 << 20) || t->generic_blocks < 0 || t->generic_blocks > (1 << 20))
     return fail(GRN_ERR_INVALID, "bad tuning");
   e->loop_pair   = t->loop_pair;
   e->fp64_refine = t->fp64_refine;
   e->refine_tol  = t->refine_tol;
   e->nblocks     = t->vegas_blocks;
   e->loop_blocks = t->weight_blocks;
+  e->born_blocks = t->born_blocks;
+  e->gen_blocks  = t->generic_blocks;
   return GRN_OK;
 }
 
@@ -1748,57 +1757,128 @@ grn_status grn_autotune(grn_engine *e, int64_t sample, grn_tune_result *out) {
   st = grn_get_tuning(e, &out->best);
   if (st != GRN_OK) return st;
   KArgs a = e->args();
-  if (!grn::record_mode(a, GRN_PREC_MIXED)) return GRN_OK;  // nothing to choose
+  const bool rec = grn::record_mode(a, GRN_PREC_MIXED);
   int sms = 0;
   GRN_CUDA(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, e->device));
   // candidates: kernel variant x grid (multiples of the resident blocks)
   const int mults[3][3] = {{1, 4, 0}, {2, 4, 8}, {2, 4, 8}};
   if (e->vegas_ready) {
-    // the loop stage of a full VEGAS pass on the engine's grid: stage A once (records), then
-    // every candidate's stage B on the same list (its outputs are rewritten by the next pass)
     const int64_t nc0 = e->ncall;
-    GRN_CUDA(grn::launch_vegas_born(a, e->d_xmat.as<double>(), e->bins, e->dim, nc0, e->seed,
+    int           nc  = 0;
+    // time one launch sequence twice on the engine stream, keep the second
+    auto timed = [&](auto &&launch, double &ms_out) -> grn_status {
+      double tmin = 1e300;
+      for (int rep = 0; rep < 2; ++rep) {
+        GRN_CUDA(cudaEventRecord(e->ev0, e->stream));
+        GRN_CUDA(launch());
+        GRN_CUDA(cudaEventRecord(e->ev1, e->stream));
+        GRN_CUDA(cudaEventSynchronize(e->ev1));
+        float ms = 0.f;
+        GRN_CUDA(cudaEventElapsedTime(&ms, e->ev0, e->ev1));
+        if (rep > 0) tmin = std::min(tmin, static_cast<double>(ms));
+      }
+      ms_out = tmin;
+      return GRN_OK;
+    };
+    auto born = [&]() {
+      return grn::launch_vegas_born(a, e->d_xmat.as<double>(), e->bins, e->dim, nc0, e->seed,
                                     0xA7A7A7u, 0, e->d_f.as<double>(),
                                     e->d_acc.as<unsigned long long>(), e->d_lidx.as<int64_t>(),
                                     e->d_lx.as<double>(), e->d_lvw.as<double>(),
-                                    e->d_recf.as<float>(), e->d_recd.as<double>(), e->stream));
-    double best = 1e300;
-    int    nc   = 0;
-    for (int pair = 0; pair < 3; ++pair)
-      for (int m = 0; m < 3 && mults[pair][m]; ++m) {
-        a.loop_pair      = pair;
-        const int blocks = sms * grn::loop_rec_blocks_per_sm(pair) * mults[pair][m];
-        double    tmin   = 1e300;
-        for (int rep = 0; rep < 2; ++rep) {
-          GRN_CUDA(cudaEventRecord(e->ev0, e->stream));
-          // no refinement list: every candidate reads the same stage-A output
-          GRN_CUDA(grn::launch_vegas_loop(a, GRN_PREC_MIXED, e->bins, e->dim, nc0, 0,
-                                          e->d_f.as<double>(), e->d_acc.as<unsigned long long>(),
-                                          e->d_lidx.as<int64_t>(), e->d_lx.as<double>(),
-                                          e->d_lvw.as<double>(), e->d_recf.as<float>(),
-                                          e->d_recd.as<double>(), nullptr, blocks, e->stream));
-          GRN_CUDA(cudaEventRecord(e->ev1, e->stream));
-          GRN_CUDA(cudaEventSynchronize(e->ev1));
-          float ms = 0.f;
-          GRN_CUDA(cudaEventElapsedTime(&ms, e->ev0, e->ev1));
-          if (rep > 0) tmin = std::min(tmin, static_cast<double>(ms));
-        }
-        out->cand[nc] = {pair, blocks, blocks, e->fp64_refine, e->refine_tol};
-        out->ms[nc]   = tmin;
-        if (tmin < best) {
-          best      = tmin;
-          out->best = out->cand[nc];
+                                    rec ? e->d_recf.as<float>() : nullptr,
+                                    rec ? e->d_recd.as<double>() : nullptr, e->stream);
+    };
+    // 1. stage A: grids of 1, 2, 4, 8 times its resident blocks (the same points each time)
+    {
+      const int per  = grn::vegas_born_blocks_per_sm(e->dim, e->bins);
+      double    best = 1e300;
+      for (int m : {1, 2, 4, 8}) {
+        a.born_blocks = sms * per * m;
+        double ms = 0.0;
+        st        = timed(born, ms);
+        if (st != GRN_OK) return st;
+        grn_tuning c = out->best;
+        c.born_blocks = a.born_blocks;
+        out->cand[nc] = c;
+        out->ms[nc]   = ms;
+        out->stage[nc] = 0;
+        if (ms < best) {
+          best                  = ms;
+          out->best.born_blocks = a.born_blocks;
         }
         ++nc;
       }
+      a.born_blocks = out->best.born_blocks;
+    }
+    // 2. the loop stage on one stage-A output (its outputs are rewritten by the next pass)
+    if (e->P.screening) {
+      GRN_CUDA(born());
+      double best = 1e300;
+      if (rec) {
+        for (int pair = 0; pair < 3; ++pair)
+          for (int m = 0; m < 3 && mults[pair][m]; ++m) {
+            a.loop_pair      = pair;
+            const int blocks = sms * grn::loop_rec_blocks_per_sm(pair) * mults[pair][m];
+            double    ms     = 0.0;
+            // no refinement list: every candidate reads the same stage-A output
+            st = timed([&]() {
+              return grn::launch_vegas_loop(a, GRN_PREC_MIXED, e->bins, e->dim, nc0, 0,
+                                            e->d_f.as<double>(), e->d_acc.as<unsigned long long>(),
+                                            e->d_lidx.as<int64_t>(), e->d_lx.as<double>(),
+                                            e->d_lvw.as<double>(), e->d_recf.as<float>(),
+                                            e->d_recd.as<double>(), nullptr, blocks, e->stream);
+            }, ms);
+            if (st != GRN_OK) return st;
+            grn_tuning c   = out->best;
+            c.loop_pair    = pair;
+            c.vegas_blocks = blocks;
+            c.weight_blocks = blocks;
+            out->cand[nc]  = c;
+            out->ms[nc]    = ms;
+            out->stage[nc] = 1;
+            if (ms < best) {
+              best                   = ms;
+              out->best.loop_pair    = pair;
+              out->best.vegas_blocks = blocks;
+              out->best.weight_blocks = blocks;
+            }
+            ++nc;
+          }
+      } else {
+        const int per = grn::generic_loop_blocks_per_sm(e->dim);
+        for (int m : {1, 2, 4}) {
+          a.gen_blocks = sms * per * m;
+          double ms    = 0.0;
+          st = timed([&]() {
+            return grn::launch_vegas_loop(a, GRN_PREC_MIXED, e->bins, e->dim, nc0, 0,
+                                          e->d_f.as<double>(), e->d_acc.as<unsigned long long>(),
+                                          e->d_lidx.as<int64_t>(), e->d_lx.as<double>(),
+                                          e->d_lvw.as<double>(), nullptr, nullptr, nullptr,
+                                          e->nblocks, e->stream);
+          }, ms);
+          if (st != GRN_OK) return st;
+          grn_tuning c     = out->best;
+          c.generic_blocks = a.gen_blocks;
+          out->cand[nc]    = c;
+          out->ms[nc]      = ms;
+          out->stage[nc]   = 2;
+          if (ms < best) {
+            best                     = ms;
+            out->best.generic_blocks = a.gen_blocks;
+          }
+          ++nc;
+        }
+      }
+      unsigned long long listed = 0;
+      GRN_CUDA(cudaMemcpy(&listed, e->d_acc.as<unsigned long long>() + grn::VS_COUNT,
+                          sizeof(listed), cudaMemcpyDeviceToHost));
+      out->sample_events = static_cast<int64_t>(listed);
+    }
     out->n_candidates = nc;
-    unsigned long long listed = 0;
-    GRN_CUDA(cudaMemcpy(&listed, e->d_acc.as<unsigned long long>() + grn::VS_COUNT,
-                        sizeof(listed), cudaMemcpyDeviceToHost));
-    out->sample_events = static_cast<int64_t>(listed);
-    e->have_last = false;  // the tuning pass is not an integration pass
+    e->have_last = false;  // the tuning passes are not integration passes
     return grn_set_tuning(e, &out->best);
   }
+  if (!rec) return GRN_OK;  // without VEGAS only the record loop has candidates
   const int64_t n = sample;
   GRN_CUDA(e->d_u.ensure(static_cast<size_t>(n) * e->dim * sizeof(double)));
   GRN_CUDA(e->d_w.ensure(static_cast<size_t>(n) * sizeof(double)));
@@ -1832,11 +1912,18 @@ grn_status grn_autotune(grn_engine *e, int64_t sample, grn_tune_result *out) {
         GRN_CUDA(cudaEventElapsedTime(&ms, e->ev0, e->ev1));
         if (rep > 0) tmin = std::min(tmin, static_cast<double>(ms));  // first launch warms up
       }
-      out->cand[nc] = {pair, blocks, blocks, e->fp64_refine, e->refine_tol};
-      out->ms[nc]   = tmin;
+      grn_tuning c    = out->best;
+      c.loop_pair     = pair;
+      c.vegas_blocks  = blocks;
+      c.weight_blocks = blocks;
+      out->cand[nc]   = c;
+      out->ms[nc]     = tmin;
+      out->stage[nc]  = 1;
       if (tmin < best) {
-        best      = tmin;
-        out->best = out->cand[nc];
+        best = tmin;
+        out->best.loop_pair     = pair;
+        out->best.vegas_blocks  = blocks;
+        out->best.weight_blocks = blocks;
       }
       ++nc;
     }

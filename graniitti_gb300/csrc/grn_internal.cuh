@@ -24,6 +24,8 @@ struct KArgs {
   // FP32 generic loop: an event whose estimated relative weight error exceeds refine_tol is
   // listed for the FP64 loop (0: never)
   double        refine_tol;
+  int           born_blocks;  // grid of the VEGAS stage A (0: the default)
+  int           gen_blocks;   // grid of the FP32 generic loop stage (0: one resident wave)
 };
 
 // Error estimate of the FP32 generic loop: |error of the loop sum| ~ kRefineKappa u
@@ -188,6 +190,10 @@ cudaError_t launch_batch_loop(int np, unsigned long long *counter, int nblocks, 
 // The f^2 histogram of member p of the uploaded table into f2mat (part: its q.hpart).
 cudaError_t launch_batch_hist(int p, int bins, int dim, const double *part, double *f2mat,
                               cudaStream_t st);
+// Resident blocks per SM of the VEGAS stage-A kernel and of the FP32 generic loop kernel for
+// a hypercube dimension (bins x dim doubles of shared memory for stage A).
+int vegas_born_blocks_per_sm(int dim, int bins);
+int generic_loop_blocks_per_sm(int dim);
 int         batch_loop_blocks(int device, int max_nh);
 
 // On-the-fly histograms: every point e < ncall of the last pass with f[e] > 0 (its point from

@@ -1507,6 +1507,26 @@ int loop_rec_blocks_per_sm(int pair) {
   return per < 1 ? 1 : per;
 }
 
+int vegas_born_blocks_per_sm(int dim, int bins) {
+  int          per = 0;
+  const size_t sm  = static_cast<size_t>(bins) * dim * sizeof(double);
+  if (dim <= 8)
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, k_vegas_born<8>, kVegasThreads, sm);
+  else
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, k_vegas_born<kMaxDim>, kVegasThreads, sm);
+  return per < 1 ? 1 : per;
+}
+
+int generic_loop_blocks_per_sm(int dim) {
+  int per = 0;
+  if (dim <= 8)
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, k_vegas_loop<float, 8>, kVegasThreads, 0);
+  else
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, k_vegas_loop<float, kMaxDim>,
+                                                  kVegasThreads, 0);
+  return per < 1 ? 1 : per;
+}
+
 int vegas_grid_blocks(int device) {
   int sms = 0, per = 0;
   cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, device);
@@ -1526,7 +1546,9 @@ cudaError_t launch_vegas_born(const KArgs &a, const double *xmat, int bins, int 
   cudaGetDevice(&dev);
   cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
   const int64_t want = (ncall + kVegasThreads - 1) / kVegasThreads;
-  const int     ba   = static_cast<int>(std::min<int64_t>(want, static_cast<int64_t>(sms) * 16));
+  const int     ba   = a.born_blocks > 0
+                           ? a.born_blocks
+                           : static_cast<int>(std::min<int64_t>(want, static_cast<int64_t>(sms) * 16));
   if (dim <= 8)
     k_vegas_born<8><<<ba, kVegasThreads, nh * sizeof(double), st>>>(
         a, xmat, bins, dim, ncall, seed, stream, track_max, f_out, acc, l_idx, l_x, l_vw, ncall,
@@ -1579,16 +1601,23 @@ cudaError_t launch_vegas_loop(const KArgs &a, int prec, int bins, int dim, int64
     return launch_vegas_loop_fp64(a, bins, dim, ncall, track_max, f_out, acc, l_idx, l_x, l_vw,
                                   rl, st);
   }
-  // MIXED: FP32 pass, then the FP64 pass over the refinement list (when refining)
+  // MIXED: FP32 pass (one resident wave, or the tuned grid), then the FP64 pass over the
+  // refinement list (when refining)
   if (dim <= 8) {
-    if (prec == GRN_PREC_MIXED)
+    if (prec == GRN_PREC_MIXED && a.gen_blocks > 0)
+      k_vegas_loop<float, 8><<<a.gen_blocks, kVegasThreads, 0, st>>>(
+          a, bins, dim, track_max, f_out, acc, l_idx, l_x, l_vw, ncall, rl, nullptr);
+    else if (prec == GRN_PREC_MIXED)
       launch_wave(k_vegas_loop<float, 8>, kVegasThreads, st, a, bins, dim, track_max, f_out, acc,
                   l_idx, l_x, l_vw, ncall, rl, nullptr);
     if (prec != GRN_PREC_MIXED || rl)
       launch_wave(k_vegas_loop<double, 8>, kVegasThreads, st, a, bins, dim, track_max, f_out, acc,
                   l_idx, l_x, l_vw, ncall, nullptr, rl);
   } else {
-    if (prec == GRN_PREC_MIXED)
+    if (prec == GRN_PREC_MIXED && a.gen_blocks > 0)
+      k_vegas_loop<float, kMaxDim><<<a.gen_blocks, kVegasThreads, 0, st>>>(
+          a, bins, dim, track_max, f_out, acc, l_idx, l_x, l_vw, ncall, rl, nullptr);
+    else if (prec == GRN_PREC_MIXED)
       launch_wave(k_vegas_loop<float, kMaxDim>, kVegasThreads, st, a, bins, dim, track_max, f_out,
                   acc, l_idx, l_x, l_vw, ncall, rl, nullptr);
     if (prec != GRN_PREC_MIXED || rl)

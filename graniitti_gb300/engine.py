@@ -151,8 +151,12 @@ class Engine:
         return t
 
     def set_tuning(self, loop_pair=None, vegas_blocks=None, weight_blocks=None,
-                   fp64_refine=None, refine_tol=None):
+                   fp64_refine=None, refine_tol=None, born_blocks=None, generic_blocks=None):
         t = self.tuning()
+        if born_blocks is not None:
+            t.born_blocks = int(born_blocks)
+        if generic_blocks is not None:
+            t.generic_blocks = int(generic_blocks)
         if fp64_refine is not None:
             t.fp64_refine = int(fp64_refine)
         if refine_tol is not None:

@@ -647,23 +647,31 @@ typedef struct grn_tuning {
   int32_t fp64_refine;   /* 1 recompute badly conditioned FP32-loop events in FP64, 0 never */
   double  refine_tol;    /* relative weight error above which an FP32-loop event's estimated
                             rounding sends it to FP64 (default 1e-5; in [1e-9, 1]) */
+  int32_t born_blocks;   /* grid of the VEGAS stage A (kinematics, cuts, records); 0 default */
+  int32_t generic_blocks;/* grid of the FP32 generic loop stage of VEGAS passes (processes
+                            outside record mode); 0 one resident wave */
 } grn_tuning;
 grn_status grn_get_tuning(grn_engine *e, grn_tuning *t);
 grn_status grn_set_tuning(grn_engine *e, const grn_tuning *t);
 
+#define GRN_TUNE_MAX 16
 typedef struct grn_tune_result {
   grn_tuning best;           /* the configuration kept */
   int32_t    n_candidates;
   int32_t    _pad;
-  double     ms[8];          /* loop-stage time of each candidate (best of 2 after a warm-up) */
-  grn_tuning cand[8];
-  int64_t    sample_events;  /* listed (screened) events the candidates were timed on */
+  double     ms[GRN_TUNE_MAX];   /* stage time of each candidate (best of 2 after a warm-up) */
+  grn_tuning cand[GRN_TUNE_MAX];
+  int32_t    stage[GRN_TUNE_MAX];/* what candidate k varies: 0 the stage-A grid, 1 the record
+                                    loop's variant and grid, 2 the generic FP32 loop's grid */
+  int64_t    sample_events;  /* listed (screened) events the loop candidates were timed on */
 } grn_tune_result;
-/* Times every candidate (kernel variant x grid of 1 to 8 times the resident blocks): once
- * grn_vegas_init has run, on the loop stage of a full VEGAS pass of the engine (ncall points,
- * its grid; sample is then unused), otherwise on the loop records of `sample` Philox points
- * through grn_event_weights' kernels; CUDA events on the engine stream, the fastest is kept.
- * Needs the eikonal tables; a no-op outside record mode. */
+/* Times the candidates with CUDA events on the engine stream and keeps the fastest of each
+ * stage. Once grn_vegas_init has run, on a full VEGAS pass of the engine (ncall points, its
+ * grid; sample is then unused): the stage-A grid (1, 2, 4, 8 times its resident blocks), then
+ * on one stage-A output the loop stage: in record mode the kernel variant x grid (1 to 8 times
+ * the resident blocks), otherwise the FP32 generic loop's grid (1, 2, 4 resident waves; MIXED
+ * passes). Without VEGAS, the record loop on the loop records of `sample` Philox points
+ * through grn_event_weights' kernels. Needs the eikonal tables of screened processes. */
 grn_status grn_autotune(grn_engine *e, int64_t sample, grn_tune_result *out);
 
 /* ------------------------------------------------------------------------ */

@@ -342,11 +342,21 @@ def test_autotune_on_the_vegas_loop_stage(gpu, params_screened):
         e.vegas_iteration(mode=0, refine=True, iter_id=1 + it)
     grid = e.vegas_grid()
     r = e.autotune()
-    ms = list(r.ms)[:r.n_candidates]
-    print("VEGAS-stage autotune: %d candidates on %d listed events, ms %s, best %d x %d" %
-          (r.n_candidates, r.sample_events, np.round(ms, 3), r.best.loop_pair,
-           r.best.vegas_blocks))
-    assert r.n_candidates == 8 and 0 < r.sample_events <= vp.ncall
+    ms = np.array(list(r.ms)[:r.n_candidates])
+    stage = np.array(list(r.stage)[:r.n_candidates])
+    print("VEGAS-stage autotune: %d candidates on %d listed events, ms %s, best stage A %d "
+          "blocks, loop %d x %d" % (r.n_candidates, r.sample_events, np.round(ms, 3),
+                                    r.best.born_blocks, r.best.loop_pair, r.best.vegas_blocks))
+    # stage A: 4 grids; the record loop: 8 variant x grid candidates
+    assert r.n_candidates == 12 and list(stage) == [0] * 4 + [1] * 8
+    assert 0 < r.sample_events <= vp.ncall
+    ka = int(np.argmin(ms[:4]))
+    kl = 4 + int(np.argmin(ms[4:]))
+    assert r.best.born_blocks == r.cand[ka].born_blocks
+    assert (r.best.loop_pair, r.best.vegas_blocks) == (r.cand[kl].loop_pair, r.cand[kl].vegas_blocks)
+    t = e.tuning()
+    assert (t.born_blocks, t.loop_pair, t.vegas_blocks) == (r.best.born_blocks, r.best.loop_pair,
+                                                            r.best.vegas_blocks)
     assert np.array_equal(e.vegas_grid(), grid)  # tuning does not refine
     res = [e.vegas_iteration(mode=1, refine=True, iter_id=10 + it) for it in range(2)]
     e.set_tuning(loop_pair=0)
@@ -400,3 +410,39 @@ def test_fp64_engine_vs_long_double_oracle(gpu, name):
           (name, r_eng.max(), np.median(r_eng), r_ref.max(), beyond.sum(), LD_TOL))
     assert np.all(ok | (r_eng <= r_ref_all)), r_eng.max()
     e.close()
+
+
+def test_autotune_generic_loop_keeps_results(gpu):
+    """A process outside record mode (tensor-pomeron f2(1270), screened): the tuner times the
+    stage-A grid and the FP32 generic loop's grid; a VEGAS pass on the tuned grids gives the
+    same integral bit for bit as on the default ones (every event is computed on its own and
+    every sum has a fixed order)."""
+    import graniitti_gb300 as g
+    from graniitti_gb300 import _abi, card
+    from conftest import CARD_SCR
+    c = card.read_card(CARD_SCR)
+    c["PROCESSPARAM"]["RES"] = ["f2_1270"]
+    P = card.build_params(c, "PP[RESTENSOR]<C> -> pi+ pi- @RES{f2_1270:1}")
+    res = []
+    for tune in (False, True):
+        e = _engine(P)
+        e.eikonal_build(512, 2000)
+        vp = _abi.VegasParams()
+        vp.bins, vp.iter, vp.ncall, vp.lambda_ = 128, 5, 1 << 17, 1.5
+        vp.chi2max, vp.precision, vp.burnin_iter, vp.prec, vp.seed = 10.0, 1e-3, 3, g.MIXED, 3
+        e.vegas_init(vp)
+        for it in range(2):
+            e.vegas_iteration(mode=0, refine=True, iter_id=1 + it)
+        if tune:
+            r = e.autotune()
+            ms = np.array(list(r.ms)[:r.n_candidates])
+            stage = list(r.stage)[:r.n_candidates]
+            print("generic-loop autotune: ms %s, best stage A %d, generic loop %d blocks"
+                  % (np.round(ms, 3), r.best.born_blocks, r.best.generic_blocks))
+            assert stage == [0] * 4 + [2] * 3 and r.sample_events > 0
+            kg = 4 + int(np.argmin(ms[4:]))
+            assert r.best.generic_blocks == r.cand[kg].generic_blocks > 0
+            assert e.tuning().generic_blocks == r.best.generic_blocks
+        res.append(e.vegas_iteration(mode=1, refine=True, iter_id=10))
+        e.close()
+    assert res[0].I_this == res[1].I_this and res[0].refined == res[1].refined
