@@ -5,6 +5,7 @@
 
 #include <algorithm>
 #include <cmath>
+#include <limits>
 #include <complex>
 #include <cstdio>
 #include <cstring>
@@ -367,6 +368,20 @@ grn_status derive_consts(const grn_process_params &P, grn::Consts &K) {
   K.m4      = P.m_central[1];
   K.m3sq    = K.m3 * K.m3;
   K.m4sq    = K.m4 * K.m4;
+  {
+    // monotone images of the fiducial windows (fiducial_cuts): M^2, pT^2 (a lower edge <= 0
+    // is no cut), exp(2 Y), sinh(eta)
+    const grn_fidcuts &f = P.fcuts;
+    const double ninf = -std::numeric_limits<double>::infinity();
+    K.cut_m2lo    = f.M_min > 0 ? f.M_min * f.M_min : ninf;
+    K.cut_m2hi    = f.M_max >= 0 ? f.M_max * f.M_max : ninf;
+    K.cut_pt2lo   = f.Pt_min > 0 ? f.Pt_min * f.Pt_min : ninf;
+    K.cut_pt2hi   = f.Pt_max >= 0 ? f.Pt_max * f.Pt_max : ninf;
+    K.cut_e2ylo   = std::exp(2.0 * f.Y_min);
+    K.cut_e2yhi   = std::exp(2.0 * f.Y_max);
+    K.cut_sheta_lo = std::sinh(f.eta_min);
+    K.cut_sheta_hi = std::sinh(f.eta_max);
+  }
   K.lnpt_lo = std::log(P.gcuts.fpt_min + kZeroEps);
   K.lnpt_hi = std::log(P.gcuts.fpt_max);
   const int    Nf = 4;

@@ -65,6 +65,10 @@ GRN_HD cx<T> cadd(cx<T> a, cx<T> b) {
 
 // Per-engine constants derived once on the host from grn_process_params.
 struct Consts {
+  // fiducial windows as monotone images (comparisons without transcendentals): the system
+  // mass^2 and pT^2, exp(2 Y) of the system rapidity, sinh(eta) of the particles' eta
+  double cut_m2lo, cut_m2hi, cut_pt2lo, cut_pt2hi, cut_e2ylo, cut_e2yhi, cut_sheta_lo,
+      cut_sheta_hi;
   double s, sqrt_s;
   double L, eps;            // beam light-cone: pb1+ = pb2- = L, pb1- = pb2+ = eps = m^2/L
   double mp2;               // forward-leg mass^2 (elastic)
@@ -1091,24 +1095,26 @@ GRN_HD bool fiducial_cuts(const grn_process_params &P, const Consts &K, const Bo
     if ((b.exc & 1) && !(mf1 >= f.fM_min && mf1 <= f.fM_max)) return false;
     if ((b.exc & 2) && !(mf2 >= f.fM_min && mf2 <= f.fM_max)) return false;
   }
-  const double M  = sqrt(fmax(b.m2, 0.0));
-  const double Y  = 0.5 * log((b.p3p + b.p4p) / (b.p3m + b.p4m));
+  // M = sqrt(m2), Y = log(P+ / P-) / 2, Pt and each particle's eta = asinh(pz / pT) are
+  // compared through monotone images of the windows (Consts::cut_*), without transcendentals
+  const double m2 = fmax(b.m2, 0.0);
+  const double Pp = b.p3p + b.p4p, Pm = b.p3m + b.p4m;
   const double sx = b.p3x + b.p4x, sy = b.p3y + b.p4y;
-  const double Pt = sqrt(sx * sx + sy * sy);
-  if (!(M >= f.M_min && M <= f.M_max && Y >= f.Y_min && Y <= f.Y_max && Pt >= f.Pt_min &&
-        Pt <= f.Pt_max))
+  const double pt2 = sx * sx + sy * sy;
+  if (!(m2 >= K.cut_m2lo && m2 <= K.cut_m2hi && Pp >= Pm * K.cut_e2ylo &&
+        Pp <= Pm * K.cut_e2yhi && pt2 >= K.cut_pt2lo && pt2 <= K.cut_pt2hi))
     return false;
   if (P.n_decay == 2) return (b.leafok & 1) != 0;
   bool ok = true;
   const double px[2] = {b.p3x, b.p4x}, py[2] = {b.p3y, b.p4y};
   const double mt[2] = {b.mt3, b.mt4}, y[2] = {b.y3, b.y4};
+  const double pz[2] = {0.5 * (b.p3p - b.p3m), 0.5 * (b.p4p - b.p4m)};
 #pragma unroll
   for (int k = 0; k < 2; ++k) {
-    const double pt  = sqrt(px[k] * px[k] + py[k] * py[k]);
-    const double pz  = mt[k] * sinh(y[k]);
-    const double eta = asinh(pz / pt);
+    const double pt = sqrt(px[k] * px[k] + py[k] * py[k]);
     if (!(pt >= f.pt_min && pt <= f.pt_max && mt[k] >= f.Et_min && mt[k] <= f.Et_max &&
-          eta >= f.eta_min && eta <= f.eta_max && y[k] >= f.rap_min && y[k] <= f.rap_max))
+          pz[k] >= pt * K.cut_sheta_lo && pz[k] <= pt * K.cut_sheta_hi &&
+          y[k] >= f.rap_min && y[k] <= f.rap_max))
       ok = false;
   }
   return ok;
@@ -1651,7 +1657,13 @@ GRN_HD void make_loop_event_fast(const grn_process_params &P, const Consts &K, c
   const double s14 = sinv(p1p, p1m, mp2, b.p4p, b.p4m, b.m4sq, b.p1x * b.p4x + b.p1y * b.p4y);
   const double s23 = sinv(p2p, p2m, mp2, b.p3p, b.p3m, b.m3sq, b.p2x * b.p3x + b.p2y * b.p3y);
   const double s24 = sinv(p2p, p2m, mp2, b.p4p, b.p4m, b.m4sq, b.p2x * b.p4x + b.p2y * b.p4y);
-  e.is13 = T(1.0 / s13); e.is14 = T(1.0 / s14); e.is23 = T(1.0 / s23); e.is24 = T(1.0 / s24);
+  if constexpr (sizeof(T) == sizeof(float)) {
+    // FP32 fields: the reciprocal of the rounded value (within 1 ulp of the rounded FP64 one)
+    e.is13 = 1.0f / float(s13); e.is14 = 1.0f / float(s14);
+    e.is23 = 1.0f / float(s23); e.is24 = 1.0f / float(s24);
+  } else {
+    e.is13 = T(1.0 / s13); e.is14 = T(1.0 / s14); e.is23 = T(1.0 / s23); e.is24 = T(1.0 / s24);
+  }
   const double l0 = log(P.regge.s0);
   const double L13 = log(s13) - l0, L14 = log(s14) - l0, L23 = log(s23) - l0, L24 = log(s24) - l0;
   e.L13 = T(L13 * kLog2e); e.L14 = T(L14 * kLog2e); e.L23 = T(L23 * kLog2e);
@@ -1687,7 +1699,10 @@ GRN_HD void make_loop_event_fast(const grn_process_params &P, const Consts &K, c
   Et += fa;
   Eu += fb;
   const double Em = Et > Eu ? Et : Eu;
-  e.rho_t = T(exp(Et - Em)); e.rho_u = T(exp(Eu - Em));
+  // exp(Et - Em), exp(Eu - Em): the larger channel's is exactly 1
+  const double rx = exp(Et > Eu ? Eu - Et : Et - Eu);
+  const double rt = Et > Eu ? 1.0 : rx, ru = Et > Eu ? rx : 1.0;
+  e.rho_t = T(rt); e.rho_u = T(ru);
   e.escale = exp(Em);
   // couplings x ReggeEta(a0)^2 x exp(-i pi ap (t1 + t2)/2) at k = 0
   const double er = K.eta0_re[k], ei = K.eta0_im[k];
@@ -1699,9 +1714,8 @@ GRN_HD void make_loop_event_fast(const grn_process_params &P, const Consts &K, c
   e.pre_im = T(pi);
   if (A0re) {
     // tree-level amplitude from the same factors (FP64)
-    const double Pd = (1.0 - t1 / P.soft.fc1) * (1.0 - t1 / P.soft.fc2) *
-                      (1.0 - t2 / P.soft.fc1) * (1.0 - t2 / P.soft.fc2);
-    const double rt = exp(Et - Em), ru = exp(Eu - Em);
+    const double i1 = 1.0 / P.soft.fc1, i2 = 1.0 / P.soft.fc2;
+    const double Pd = (1.0 - t1 * i1) * (1.0 - t1 * i2) * (1.0 - t2 * i1) * (1.0 - t2 * i2);
     double m;
     if (e.ffmode == 2) {
       const double Da = P.regge.b_POW - ta, Db = P.regge.b_POW - tb;
