@@ -2011,9 +2011,11 @@ GRN_HD double born_amp2(const grn_process_params &P, const Consts &K, const Born
 GRN_HD double weight_jacobian(const Consts &K, const Born &b) {
   const double E1 = 0.5 * (b.p1p + b.p1m), pz1 = 0.5 * (b.p1p - b.p1m);
   const double E2 = 0.5 * (b.p2p + b.p2m), pz2 = 0.5 * (b.p2p - b.p2m);
-  const double J  = 1.0 / fabs(pz1 / E1 - pz2 / E2);
-  const double pt1 = sqrt(b.pt1sq), pt2 = sqrt(b.pt2sq);
-  return K.w_const * (pt1 / (2.0 * E1)) * (pt2 / (2.0 * E2)) * J * b.jx * pt1 * pt2 * b.jf;
+  // (pT1 / 2E1) (pT2 / 2E2) J pT1 pT2 with J = 1 / |pz1/E1 - pz2/E2|
+  //   = pT1^2 pT2^2 / (4 |pz1 E2 - pz2 E1|): one division, no square root (pz1 E2 and
+  // -pz2 E1 have the same sign for the two forward legs, so nothing cancels)
+  const double den = 4.0 * fabs(pz1 * E2 - pz2 * E1);
+  return K.w_const * (b.pt1sq * b.pt2sq / den) * b.jx * b.jf;
 }
 
 }  // namespace grn
