@@ -49,25 +49,26 @@ __device__ __forceinline__ float2 log2_2(float2 a) {
 __device__ __forceinline__ float2 exp2_2(float2 a) {
   return make_float2(fast_exp2(a.x), fast_exp2(a.y));
 }
+// a / b per lane: the SFU's reciprocal of each lane, then one packed multiplication
 __device__ __forceinline__ float2 div2(float2 a, float2 b) {
-  return make_float2(fast_div(a.x, b.x), fast_div(a.y, b.y));
+  float rx, ry;
+  asm("rcp.approx.ftz.f32 %0, %1;" : "=f"(rx) : "f"(b.x));
+  asm("rcp.approx.ftz.f32 %0, %1;" : "=f"(ry) : "f"(b.y));
+  return __fmul2_rn(a, make_float2(rx, ry));
 }
 __device__ __forceinline__ float2 abs2(float2 a) { return make_float2(fabsf(a.x), fabsf(a.y)); }
 __device__ __forceinline__ float2 sqrt2(float2 a) { return make_float2(sqrtf(a.x), sqrtf(a.y)); }
 // (sin 2 pi h, cos 2 pi h): h reduced to [-1/2, 1/2] turns, then the hardware sine / cosine
 // (absolute error ~5e-7 on |2 pi h| <= pi).
-__device__ __forceinline__ float near_int(float x) {
-  // the nearest integer to x (|x| < 2^22): x + 1.5 2^23 has no fraction bits left, and
-  // subtracting 1.5 2^23 back is exact; two FP32 additions
-  float t, r;
-  asm("add.rn.f32 %0, %1, 0f4B400000;" : "=f"(t) : "f"(x));
-  asm("sub.rn.f32 %0, %1, 0f4B400000;" : "=f"(r) : "f"(t));
-  return r;
-}
 __device__ __forceinline__ void sincos_turns2(float2 h, float2 &s, float2 &c) {
-  const float rx = h.x - near_int(h.x), ry = h.y - near_int(h.y);
-  sfu_sincos(float(2.0 * kPi) * rx, s.x, c.x);
-  sfu_sincos(float(2.0 * kPi) * ry, s.y, c.y);
+  // the nearest integers to h (|h| < 2^22): h + 1.5 2^23 has no fraction bits left, and
+  // subtracting 1.5 2^23 back is exact (packed round-to-nearest additions)
+  const float2 big = make_float2(12582912.f, 12582912.f);
+  const float2 n   = __fadd2_rn(__fadd2_rn(h, big), make_float2(-12582912.f, -12582912.f));
+  const float2 a   = __fmul2_rn(make_float2(float(2.0 * kPi), float(2.0 * kPi)),
+                                __ffma2_rn(n, make_float2(-1.f, -1.f), h));
+  sfu_sincos(a.x, s.x, c.x);
+  sfu_sincos(a.y, s.y, c.y);
 }
 // sin(pi d) for |d| < 1 (accurate: the once-per-phi-node projections).
 __device__ __forceinline__ float2 sinpi_turns2(float2 d) {
