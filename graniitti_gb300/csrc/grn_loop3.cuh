@@ -215,6 +215,7 @@ GRN_L3 void loop_integral3(const Loop3<V> &e, int n_kt, int n_phi, const KN *skt
     for (int j0 = 0; j0 < n_kt; j0 += 8) {
       V br = zero, bi = zero;
       const int j1 = j0 + 8 < n_kt ? j0 + 8 : n_kt;
+#pragma unroll 2
       for (int j = j0; j < j1; ++j) {
         const KN nj = skt[j];
         V zr, zi;
