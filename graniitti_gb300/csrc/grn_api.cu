@@ -362,6 +362,8 @@ grn_status derive_consts(const grn_process_params &P, grn::Consts &K) {
   const double E  = 0.5 * P.sqrt_s;
   const double pz = std::sqrt(std::max(0.0, E * E - P.m_beam * P.m_beam));
   K.L       = E + pz;
+  K.invL    = 1.0 / K.L;
+  K.invL2   = 1.0 / (K.L * K.L);
   K.eps     = P.m_beam * P.m_beam / K.L;
   K.mp2     = P.m_beam * P.m_beam;
   K.m3      = P.m_central[0];

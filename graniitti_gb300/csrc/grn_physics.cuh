@@ -71,6 +71,7 @@ struct Consts {
       cut_sheta_hi;
   double s, sqrt_s;
   double L, eps;            // beam light-cone: pb1+ = pb2- = L, pb1- = pb2+ = eps = m^2/L
+  double invL, invL2;       // 1 / L, 1 / L^2
   double mp2;               // forward-leg mass^2 (elastic)
   double m3, m4, m3sq, m4sq;
   double lnpt_lo, lnpt_hi;  // log(fpt_min + ZERO_EPS), log(fpt_max)
@@ -862,8 +863,8 @@ GRN_HD bool born_kinematics_C(const grn_process_params &P, const Consts &K, cons
 GRN_HD bool born_invariants(const Consts &K, Born &b) {
   const double Pp = b.p3p + b.p4p, Pm = b.p3m + b.p4m;
   const double mT1sq = b.mf1sq + b.pt1sq, mT2sq = b.mf2sq + b.pt2sq;
-  const double L2    = K.L * K.L;
-  if (!solve_x((Pp - K.eps) / K.L, (Pm - K.eps) / K.L, mT1sq / L2, mT2sq / L2, b.x1, b.x2))
+  if (!solve_x((Pp - K.eps) * K.invL, (Pm - K.eps) * K.invL, mT1sq * K.invL2, mT2sq * K.invL2,
+               b.x1, b.x2))
     return false;
   b.p1p = (1.0 - b.x1) * K.L;
   b.p1m = mT1sq / b.p1p;
@@ -1613,7 +1614,7 @@ template <typename T>
 GRN_HD void make_loop_consts_fast(const grn_process_params &P, const Consts &K,
                                   LoopEventF<T> &e) {
   const int k = K.active[0] ? 0 : (K.active[1] ? 1 : 2);
-  e.L = T(K.L); e.invL = T(1.0 / K.L); e.invL2 = T(1.0 / (K.L * K.L));
+  e.L = T(K.L); e.invL = T(K.invL); e.invL2 = T(K.invL2);
   e.mp2 = T(K.mp2); e.M2 = T(K.M2prop);
   e.ap = T(P.regge.ap[k]);
   e.ifc1 = T(1.0 / P.soft.fc1); e.ifc2 = T(1.0 / P.soft.fc2);
@@ -1634,10 +1635,10 @@ GRN_HD void make_loop_event_fast(const grn_process_params &P, const Consts &K, c
   e.p1x = T(b.p1x); e.p1y = T(b.p1y); e.p2x = T(b.p2x); e.p2y = T(b.p2y);
   e.p3x = T(b.p3x); e.p3y = T(b.p3y); e.p4x = T(b.p4x); e.p4y = T(b.p4y);
   e.p3p = T(b.p3p); e.p3m = T(b.p3m); e.p4p = T(b.p4p); e.p4m = T(b.p4m);
-  const double a1 = (b.p3p + b.p4p - K.eps) / K.L, a2 = (b.p3m + b.p4m - K.eps) / K.L;
+  const double a1 = (b.p3p + b.p4p - K.eps) * K.invL, a2 = (b.p3m + b.p4m - K.eps) * K.invL;
   const double ia1 = 1.0 / (1.0 - a1), ia2 = 1.0 / (1.0 - a2);
   e.ia1 = T(ia1); e.ia2 = T(ia2); e.q1c = T(ia1 * ia1 * ia2); e.q2c = T(ia2 * ia2 * ia1);
-  const double L = K.L, invL = 1.0 / K.L, invL2 = invL * invL, mp2 = K.mp2;
+  const double L = K.L, invL = K.invL, invL2 = K.invL2, mp2 = K.mp2;
   // k = 0 values of the linear closure (same formulas as the loop point, in FP64)
   const double mT1s = mp2 + b.pt1sq, mT2s = mp2 + b.pt2sq;
   const double c1 = mT1s * invL2, c2 = mT2s * invL2;
@@ -1802,12 +1803,12 @@ GRN_HD void make_loop_event(const grn_process_params &P, const Consts &K, const 
   e.p1x = T(b.p1x); e.p1y = T(b.p1y); e.p2x = T(b.p2x); e.p2y = T(b.p2y);
   e.p3x = T(b.p3x); e.p3y = T(b.p3y); e.p4x = T(b.p4x); e.p4y = T(b.p4y);
   e.p3p = T(b.p3p); e.p3m = T(b.p3m); e.p4p = T(b.p4p); e.p4m = T(b.p4m);
-  const double a1 = (b.p3p + b.p4p - K.eps) / K.L, a2 = (b.p3m + b.p4m - K.eps) / K.L;
+  const double a1 = (b.p3p + b.p4p - K.eps) * K.invL, a2 = (b.p3m + b.p4m - K.eps) * K.invL;
   e.a1 = T(a1);
   e.a2 = T(a2);
   e.ia1 = T(1.0 / (1.0 - a1));
   e.ia2 = T(1.0 / (1.0 - a2));
-  e.L = T(K.L); e.invL2 = T(1.0 / (K.L * K.L)); e.invL = T(1.0 / K.L);
+  e.L = T(K.L); e.invL2 = T(K.invL2); e.invL = T(K.invL);
   e.eps = T(K.eps); e.mp2 = T(K.mp2); e.m3sq = T(b.m3sq); e.m4sq = T(b.m4sq);
   e.mf1 = T(b.mf1sq); e.mf2 = T(b.mf2sq); e.exc = b.exc;
   e.lnsc   = T(0);
