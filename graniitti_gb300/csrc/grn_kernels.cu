@@ -214,7 +214,8 @@ __device__ __noinline__ cx<double> loop_integral_rr(const KArgs &A, const Born &
     double cmax = 0.0;
     for (int r = 0; r < A.K.rr_n; ++r) cmax = fmax(cmax, fabs(Rd.C[r].re) + fabs(Rd.C[r].im));
     if (cmax > 0.0 && (cmax < 1e-25 || cmax > 1e25)) {
-      const int k = ilogb(cmax);
+      // clamped so that 2^-k stays finite for subnormal factors (their weights are ~0)
+      const int k = max(-1020, min(1020, ilogb(cmax)));
       sc       = ldexp(1.0, -k);
       e.escale = ldexp(1.0, k);
     }

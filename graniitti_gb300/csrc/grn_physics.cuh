@@ -1823,7 +1823,8 @@ GRN_HD void make_loop_event(const grn_process_params &P, const Consts &K, const 
       double rmax = fmax(fabs(R.R0.re) + fabs(R.R0.im), fabs(R.R1.re) + fabs(R.R1.im));
       for (int j = 0; j < 7; ++j) rmax = fmax(rmax, fabs(R.Rs[j].re) + fabs(R.Rs[j].im));
       if (rmax > 0.0 && (rmax < 1e-25 || rmax > 1e25)) {
-        const int k = ilogb(rmax);
+        // clamped so that 2^-k stays finite for subnormal factors (their weights are ~0)
+        const int k = ilogb(rmax) < -1020 ? -1020 : (ilogb(rmax) > 1020 ? 1020 : ilogb(rmax));
         sc       = ldexp(1.0, -k);
         e.escale = ldexp(1.0, k);
       }
