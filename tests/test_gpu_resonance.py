@@ -255,3 +255,31 @@ def test_fp32_loop_refinement_vegas_pass(gpu):
     assert rm.I_this == pytest.approx(r64.I_this, rel=1e-5)
     assert rm.maxf == pytest.approx(r64.maxf, rel=1e-5)
     assert rm.nan_count == r64.nan_count
+
+
+def test_far_off_shell_events_without_refinement():
+    """f2(1270) alone on the 63 x 33 grid with the FP64 refinement off: events ~3 GeV off the
+    pole, whose resonance factors are FP64-subnormal, keep a finite FP32 loop (the event scale
+    stays finite), so a VEGAS pass meets no NaN weight and gives the refined pass's integral."""
+    import graniitti_gb300 as g
+    from graniitti_gb300 import _abi, card
+    from conftest import CARD_SCR
+    c = card.read_card(CARD_SCR)
+    c["PROCESSPARAM"]["RES"] = ["f2_1270"]
+    res = []
+    for ref in (1, 0):
+        P = card.build_params(c, "PP[RESTENSOR]<C> -> pi+ pi- @RES{f2_1270:1}")
+        P.loop.n_kt, P.loop.n_phi, P.loop.kt_max = 63, 33, 3.0
+        e = _engine(P)
+        e.eikonal_build(1024, 10000)
+        e.set_tuning(fp64_refine=ref)
+        vp = _abi.VegasParams()
+        vp.bins, vp.iter, vp.ncall, vp.lambda_ = 128, 5, 1 << 18, 1.5
+        vp.chi2max, vp.precision, vp.burnin_iter, vp.prec, vp.seed = 10.0, 1e-3, 3, g.MIXED, 7
+        e.vegas_init(vp)
+        res.append(e.vegas_iteration(mode=0, refine=False, iter_id=1))  # the uniform grid
+        e.close()
+    print("f2 uniform-grid pass: refined %d, I %.10e (refined) vs %.10e (FP32 only), NaN %d"
+          % (res[0].refined, res[0].I_this, res[1].I_this, res[1].nan_count))
+    assert res[1].nan_count == 0 and res[1].refined == 0
+    assert res[1].I_this == pytest.approx(res[0].I_this, rel=1e-5)
