@@ -103,6 +103,7 @@ int main() {
   const double E = 6500.0, pz = std::sqrt(E * E - P.m_beam * P.m_beam);
   K.s = 13000.0 * 13000.0; K.sqrt_s = 13000.0; K.L = E + pz; K.eps = P.m_beam * P.m_beam / K.L;
   K.invL = 1.0 / K.L; K.invL2 = 1.0 / (K.L * K.L);
+  K.ifc1 = 1.0 / P.soft.fc1; K.ifc2 = 1.0 / P.soft.fc2;
   K.mp2 = P.m_beam * P.m_beam; K.m3 = K.m4 = P.m_central[0]; K.m3sq = K.m4sq = K.m3 * K.m3;
   K.lnpt_lo = std::log(1e-12); K.lnpt_hi = std::log(2.5); K.M2prop = K.m3sq;
   K.g2 = 1.0; K.gN2 = 1.0; K.n_active = 1; K.active[0] = 1; K.eta0_re[0] = 1.0;

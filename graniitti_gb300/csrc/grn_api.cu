@@ -364,6 +364,8 @@ grn_status derive_consts(const grn_process_params &P, grn::Consts &K) {
   K.L       = E + pz;
   K.invL    = 1.0 / K.L;
   K.invL2   = 1.0 / (K.L * K.L);
+  K.ifc1    = 1.0 / P.soft.fc1;
+  K.ifc2    = 1.0 / P.soft.fc2;
   K.eps     = P.m_beam * P.m_beam / K.L;
   K.mp2     = P.m_beam * P.m_beam;
   K.m3      = P.m_central[0];

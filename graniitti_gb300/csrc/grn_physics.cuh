@@ -72,6 +72,7 @@ struct Consts {
   double s, sqrt_s;
   double L, eps;            // beam light-cone: pb1+ = pb2- = L, pb1- = pb2+ = eps = m^2/L
   double invL, invL2;       // 1 / L, 1 / L^2
+  double ifc1, ifc2;        // 1 / fc1, 1 / fc2 of the proton form factor
   double mp2;               // forward-leg mass^2 (elastic)
   double m3, m4, m3sq, m4sq;
   double lnpt_lo, lnpt_hi;  // log(fpt_min + ZERO_EPS), log(fpt_max)
@@ -866,15 +867,17 @@ GRN_HD bool born_invariants(const Consts &K, Born &b) {
   if (!solve_x((Pp - K.eps) * K.invL, (Pm - K.eps) * K.invL, mT1sq * K.invL2, mT2sq * K.invL2,
                b.x1, b.x2))
     return false;
+  // 1 / (1 - x) of each leg, shared by its minus (plus) component and its t
+  const double r1 = 1.0 / (1.0 - b.x1), r2 = 1.0 / (1.0 - b.x2);
   b.p1p = (1.0 - b.x1) * K.L;
-  b.p1m = mT1sq / b.p1p;
+  b.p1m = mT1sq * r1 * K.invL;
   b.p2m = (1.0 - b.x2) * K.L;
-  b.p2p = mT2sq / b.p2m;
+  b.p2p = mT2sq * r2 * K.invL;
 
   // Invariants: (pa + pb)^2 = ma^2 + mb^2 + pa+ pb- + pa- pb+ - 2 paT.pbT
   // t = (pb - p)^2 = -(pT^2 + x (m_f^2 - mp^2) + x^2 mp^2) / (1 - x): same-sign terms (m_f >= mp)
-  b.t1  = -(b.pt1sq + b.x1 * (b.mf1sq - K.mp2) + b.x1 * b.x1 * K.mp2) / (1.0 - b.x1);
-  b.t2  = -(b.pt2sq + b.x2 * (b.mf2sq - K.mp2) + b.x2 * b.x2 * K.mp2) / (1.0 - b.x2);
+  b.t1  = -(b.pt1sq + b.x1 * (b.mf1sq - K.mp2) + b.x1 * b.x1 * K.mp2) * r1;
+  b.t2  = -(b.pt2sq + b.x2 * (b.mf2sq - K.mp2) + b.x2 * b.x2 * K.mp2) * r2;
   b.s13 = b.mf1sq + b.m3sq + b.p1p * b.p3m + b.p1m * b.p3p - 2.0 * (b.p1x * b.p3x + b.p1y * b.p3y);
   b.s14 = b.mf1sq + b.m4sq + b.p1p * b.p4m + b.p1m * b.p4p - 2.0 * (b.p1x * b.p4x + b.p1y * b.p4y);
   b.s23 = b.mf2sq + b.m3sq + b.p2p * b.p3m + b.p2m * b.p3p - 2.0 * (b.p2x * b.p3x + b.p2y * b.p3y);
@@ -1715,7 +1718,7 @@ GRN_HD void make_loop_event_fast(const grn_process_params &P, const Consts &K, c
   e.pre_im = T(pi);
   if (A0re) {
     // tree-level amplitude from the same factors (FP64)
-    const double i1 = 1.0 / P.soft.fc1, i2 = 1.0 / P.soft.fc2;
+    const double i1 = K.ifc1, i2 = K.ifc2;
     const double Pd = (1.0 - t1 * i1) * (1.0 - t1 * i2) * (1.0 - t2 * i1) * (1.0 - t2 * i2);
     double m;
     if (e.ffmode == 2) {
