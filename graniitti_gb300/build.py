@@ -13,8 +13,9 @@ REPO = os.path.dirname(HERE)
 CSRC = os.path.join(HERE, "csrc")
 OUT = os.path.join(HERE, "_build")
 LIB = os.path.join(OUT, "libgrn.so")
-SOURCES = ["grn_kernels.cu", "grn_api.cu", "grn_noalloc.cu", "grn_flow.cu", "grn_flow_wide.cu",
-           "grn_record.cc"]
+SOURCES = ["grn_kernels.cu", "grn_kernels_wide.cu", "grn_kernels_wide_f32.cu",
+           "grn_kernels_wide_f64.cu", "grn_api.cu", "grn_noalloc.cu", "grn_flow.cu",
+           "grn_flow_wide.cu", "grn_record.cc"]
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 
 
@@ -43,7 +44,13 @@ def build_library(verbose=False, extra=(), force=False):
 
     def compile_one(pair):
         src, obj = pair
-        cmd = [nvcc()] + _flags(extra) + ["-c", src, "-o", obj]
+        # grn_kernels.cu launches the >8-dimensional instantiations of its kernel templates that
+        # the grn_kernels_wide*.cu units define (explicit instantiation declarations and
+        # definitions, each instantiation in exactly one unit): their host stubs need external
+        # linkage across those units
+        own = ["-static-global-template-stub=false"] if os.path.basename(src).startswith(
+            "grn_kernels") else []
+        cmd = [nvcc()] + _flags(extra) + own + ["-c", src, "-o", obj]
         if verbose:
             print(" ".join(cmd))
         r = subprocess.run(cmd, capture_output=True, text=True)

@@ -30,7 +30,7 @@ namespace grn {
 // ---------------------------------------------------------------------------
 // Bessel J0: Abramowitz & Stegun 9.4 rational / asymptotic approximation, the
 // same published coefficients as the reference's BESSJ0 (libs/extmath.hpp:12).
-__device__ double bessel_j0(double x) {
+static __device__ double bessel_j0(double x) {
   if (x == 0.0) return 1.0;
   const double ax = fabs(x);
   if (ax < 8.0) {
@@ -115,8 +115,9 @@ __device__ cx<double> loop_integral(const KArgs &A, const Born &b, const KtNode<
 }
 
 // FP32 loop with the one-division point evaluation (single active trajectory).
-__device__ cx<double> loop_integral_fast(const KArgs &A, const Born &b, const KtNode<float> *skt,
-                                         const PhiNode<float> *sphi) {
+static __device__ cx<double> loop_integral_fast(const KArgs &A, const Born &b,
+                                                const KtNode<float> *skt,
+                                                const PhiNode<float> *sphi) {
   LoopEventF<float> e;
   make_loop_event_fast<float>(A.P, A.K, b, e);
   float ar = 0.f, ai = 0.f, cr = 0.f, ci = 0.f;
@@ -368,7 +369,7 @@ __device__ __forceinline__ double record_weight(const KArgs &A, const LoopEventF
 }
 
 // Loop nodes of the azimuth-outer paired loop (grn_loop3.cuh).
-__device__ void stage_nodes3(const KArgs &A, KtNode3 *skt, PhiNode3 *sphi) {
+static __device__ void stage_nodes3(const KArgs &A, KtNode3 *skt, PhiNode3 *sphi) {
   for (int j = threadIdx.x; j < A.n_kt_nodes; j += blockDim.x) {
     const float kt = float(A.lc_kt[3 * j]), ci = float(A.lc_kt[3 * j + 2]);
     const float ca = float(hypot(A.lc_kt[3 * j + 1], A.lc_kt[3 * j + 2]));
@@ -613,6 +614,20 @@ __global__ void __launch_bounds__(kWeightThreads)
   }
 }
 
+#ifndef GRN_KERNELS_WIDE
+// the instantiations for more than 8 dimensions live in grn_kernels_wide.cu
+extern template __global__ void k_weights_born<kMaxDim>(
+    const KArgs, const double *__restrict__, int64_t, int, double *__restrict__,
+    uint8_t *__restrict__, int64_t *__restrict__, unsigned long long *__restrict__);
+extern template __global__ void k_weights_loop<float, kMaxDim>(
+    const KArgs, const double *__restrict__, int, const int64_t *__restrict__,
+    const unsigned long long *__restrict__, double *__restrict__, uint8_t *__restrict__,
+    int64_t *__restrict__, unsigned long long *__restrict__);
+extern template __global__ void k_weights_loop<double, kMaxDim>(
+    const KArgs, const double *__restrict__, int, const int64_t *__restrict__,
+    const unsigned long long *__restrict__, double *__restrict__, uint8_t *__restrict__,
+    int64_t *__restrict__, unsigned long long *__restrict__);
+
 int loop_grid_blocks(int device) {
   int sms = 0, per = 0;
   cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, device);
@@ -654,6 +669,8 @@ cudaError_t launch_event_weights(const KArgs &a, int prec, const double *u, int6
 }
 
 // Record-mode user-array stages (FP32 loop, single active trajectory).
+#endif  // GRN_KERNELS_WIDE
+
 template <int MAXD>
 __global__ void __launch_bounds__(kWeightThreads)
     k_weights_born_rec(const KArgs A, const double *__restrict__ u, int64_t n, int dim,
@@ -681,6 +698,12 @@ __global__ void __launch_bounds__(kWeightThreads)
     if (flags) flags[i] = f;
   }
 }
+
+#ifndef GRN_KERNELS_WIDE
+extern template __global__ void k_weights_born_rec<kMaxDim>(
+    const KArgs, const double *__restrict__, int64_t, int, double *__restrict__,
+    uint8_t *__restrict__, int64_t *__restrict__, float *__restrict__, double *__restrict__,
+    unsigned long long *__restrict__);
 
 // rlist non-null: points whose error estimate exceeds A.refine_tol are appended to rlist
 // (length *rcount) and left to the FP64 loop of k_weights_loop.
@@ -716,6 +739,8 @@ __global__ void __launch_bounds__(kWeightThreads, GRN_LOOP_MIN_BLOCKS)
     if (flags) flags[i] = f;
   }
 }
+
+#endif  // GRN_KERNELS_WIDE
 
 // Record mode, two events per thread on the packed FP32x2 loop; MINB resident blocks per SM
 // (2: 226 registers; 3: capped at 168, a few spills for 50% more warps).
@@ -756,6 +781,7 @@ __global__ void __launch_bounds__(kWeightThreads, MINB)
   }
 }
 
+#ifndef GRN_KERNELS_WIDE
 bool record_mode(const KArgs &a, int prec) {
   return a.P.screening && prec == GRN_PREC_MIXED && a.K.n_active == 1 &&
          a.P.process == GRN_PROC_REGGE_CON && a.P.n_central == 2 && a.P.excitation == 0;
@@ -1116,6 +1142,8 @@ cudaError_t launch_eikonal_xs(const double *mbt, int n_bt, double *xs, cudaStrea
   return cudaGetLastError();
 }
 
+#endif  // GRN_KERNELS_WIDE
+
 // ---------------------------------------------------------------------------
 // VEGAS (MGraniitti::VEGASMultiThread, src/MGraniitti.cc:1341-1443;
 // VEGASData, include/Graniitti/MVEGAS.h).
@@ -1157,8 +1185,9 @@ __device__ __forceinline__ double vegas_map(const double *sx, int bins, int dim,
 // atomic per warp and counter (exact, so order-free); maxima of non-negative doubles as
 // atomicMax on their bit patterns. The f^2 histogram of the grid refinement is built
 // after the pass from the f array (k_vegas_hist), in a fixed order.
-__device__ void flush_counters(unsigned long long *acc, const unsigned long long cnt[VS_COUNT],
-                               double maxf, double maxW) {
+static __device__ void flush_counters(unsigned long long *acc,
+                                      const unsigned long long cnt[VS_COUNT], double maxf,
+                                      double maxW) {
   for (int c = 0; c < VS_COUNT; ++c) {
     if (c == VS_FSUM || c == VS_F2SUM || c == VS_MAXF || c == VS_MAXW) continue;
     unsigned long long v = cnt[c];
@@ -1237,6 +1266,13 @@ __global__ void __launch_bounds__(128)
   }
 }
 
+#ifndef GRN_KERNELS_WIDE
+extern template __global__ void k_hist_fill<kMaxDim>(
+    const KArgs, const double *__restrict__, int, int, int64_t, uint64_t, uint32_t,
+    const float *__restrict__, const double *__restrict__, const grn_hist_spec *__restrict__,
+    const int *__restrict__, int, double *__restrict__, double *__restrict__,
+    unsigned long long *__restrict__, unsigned long long *__restrict__);
+
 cudaError_t launch_hist_fill(const KArgs &a, const double *xmat, int bins, int dim, int64_t ncall,
                              uint64_t seed, uint32_t stream, const float *fu, const double *f,
                              const grn_hist_spec *specs, const int *off, int nh, double *w,
@@ -1261,6 +1297,8 @@ cudaError_t launch_hist_fill(const KArgs &a, const double *xmat, int bins, int d
 // cuts. Rejected and unscreened events are finished here; screened events that pass the
 // cuts go to the work list (index, VEGAS weight, and the loop record or the mapped
 // point). Block `bid` of `nbid` blocks serving this pass; dsm: bins * dim doubles (the grid).
+#endif  // GRN_KERNELS_WIDE
+
 template <int MAXD>
 __device__ __forceinline__ void born_pass_body(
     const KArgs &A, const double *__restrict__ xmat, int bins, int dim, int64_t ncall,
@@ -1418,6 +1456,21 @@ __device__ __forceinline__ void finish_pair(int64_t ra, int64_t rb, const double
   }
 }
 
+#ifndef GRN_KERNELS_WIDE
+extern template __global__ void k_vegas_born<kMaxDim>(
+    const KArgs, const double *__restrict__, int, int, int64_t, uint64_t, uint32_t, int,
+    double *__restrict__, unsigned long long *__restrict__, int64_t *__restrict__,
+    double *__restrict__, double *__restrict__, int64_t, float *__restrict__,
+    double *__restrict__, const float *__restrict__, const float *__restrict__);
+extern template __global__ void k_vegas_loop<float, kMaxDim>(
+    const KArgs, int, int, int, double *__restrict__, unsigned long long *__restrict__,
+    const int64_t *__restrict__, const double *__restrict__, const double *__restrict__, int64_t,
+    int64_t *__restrict__, const int64_t *__restrict__);
+extern template __global__ void k_vegas_loop<double, kMaxDim>(
+    const KArgs, int, int, int, double *__restrict__, unsigned long long *__restrict__,
+    const int64_t *__restrict__, const double *__restrict__, const double *__restrict__, int64_t,
+    int64_t *__restrict__, const int64_t *__restrict__);
+
 // Stage B, record mode: FP32 loop of the listed events from their records.
 __global__ void __launch_bounds__(kVegasThreads, GRN_LOOP_MIN_BLOCKS)
     k_vegas_loop_rec(const KArgs A, int bins, int dim, int track_max, double *__restrict__ f_out,
@@ -1462,6 +1515,8 @@ __global__ void __launch_bounds__(kVegasThreads, GRN_LOOP_MIN_BLOCKS)
   flush_counters(acc, cnt, maxf, maxW);
 }
 
+#endif  // GRN_KERNELS_WIDE
+
 // Stage B, record mode, two events per thread on the packed FP32x2 loop (MINB as for
 // k_weights_loop_rec2).
 template <int MINB>
@@ -1496,6 +1551,7 @@ __global__ void __launch_bounds__(kVegasThreads, MINB)
   flush_counters(acc, cnt, maxf, maxW);
 }
 
+#ifndef GRN_KERNELS_WIDE
 // Resident blocks per SM of the record-mode loop kernels (one or two events per thread).
 int loop_rec_blocks_per_sm(int pair) {
   int per = 0;
@@ -2236,5 +2292,7 @@ cudaError_t launch_fma_probe(int blocks, int threads, int iters, float *sink, cu
   k_fma_probe<<<blocks, threads, 0, st>>>(iters, sink);
   return cudaGetLastError();
 }
+
+#endif  // GRN_KERNELS_WIDE
 
 }  // namespace grn

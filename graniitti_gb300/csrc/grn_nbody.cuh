@@ -730,8 +730,9 @@ GRN_HD bool nbody_point_f(const grn_process_params &P, const Consts &K, const NB
 
 // FP32 loop integral with compensated sums (one trajectory); *mag: sum_ij |U_i c_j| mag_ij in
 // units of the returned amplitude (see loop_integral for the summation part).
-__device__ cx<double> nbody_loop_f(const KArgs &A, const NBEvent &e, const KtNode<float> *skt,
-                                   const PhiNode<float> *sphi, double *mag) {
+static __device__ cx<double> nbody_loop_f(const KArgs &A, const NBEvent &e,
+                                          const KtNode<float> *skt, const PhiNode<float> *sphi,
+                                          double *mag) {
   const int q = A.K.active[0] ? 0 : (A.K.active[1] ? 1 : 2);
   NBLoopF    f;
   cx<double> omega;
@@ -762,7 +763,7 @@ __device__ cx<double> nbody_loop_f(const KArgs &A, const NBEvent &e, const KtNod
 
 // Stage A of an N-body point: kinematics, cuts and (unscreened) the weight; true when the
 // point needs the kt-loop. Flags as born_stage.
-__device__ __noinline__ bool nbody_born_stage(const KArgs &A, const double *x, double &W,
+static __device__ __noinline__ bool nbody_born_stage(const KArgs &A, const double *x, double &W,
                                               uint8_t &flags) {
   NBEvent e;
   NBLegs  g;
