@@ -1,10 +1,9 @@
 // grn_kernels_wide_f32.cu — the FP32 loop-stage kernels for hypercubes of more than 8
-// dimensions (cascades,
-// 4- and 6-body central states, forward excitation), instantiated in a translation unit of
-// their own so that they compile in parallel with the rest of grn_kernels.cu. The same source
-// is included with its launchers and the other kernels left out (GRN_KERNELS_WIDE); the
-// launchers in grn_kernels.cu reach these instantiations through explicit instantiation
-// declarations.
+// dimensions (cascades, 4- and 6-body central states, forward excitation), instantiated in a
+// translation unit of their own so that they compile in parallel with grn_kernels.cu. The
+// same source is included with its launchers and its other kernels left out
+// (GRN_KERNELS_WIDE); the launchers in grn_kernels.cu reach these instantiations through
+// explicit instantiation declarations.
 #define GRN_KERNELS_WIDE
 #include "grn_kernels.cu"
 
