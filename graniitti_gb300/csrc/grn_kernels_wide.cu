@@ -1,5 +1,5 @@
-// grn_kernels_wide.cu — the stage-A, record-build and histogram kernels for hypercubes of more than 8
-// dimensions (cascades, 4- and 6-body central states, forward excitation), instantiated in a
+// grn_kernels_wide.cu — the stage-A, record-build and histogram kernels for hypercubes of more
+// than 8 dimensions (cascades, 4- and 6-body central states, forward excitation), instantiated in a
 // translation unit of their own so that they compile in parallel with grn_kernels.cu. The
 // same source is included with its launchers and its other kernels left out
 // (GRN_KERNELS_WIDE); the launchers in grn_kernels.cu reach these instantiations through
